@@ -1,0 +1,348 @@
+"""Seeded synthetic ``ldbd_data`` generator.
+
+Writes exactly the binary/text files that DMD's readers consume, so the same directory can be
+fed to the reference program and to this package:
+
+* ``ldbd_size.dat`` -- text header read by ``electron::read_ldbd_size`` (electron.cpp:100-133),
+  ``electronphonon::get_brange/get_nkpair`` (ElectronPhonon.cpp:132-177), ``phonon::read_jdftx``
+  (phonon.h:49-79) and ``parameters::read_jdftx`` (parameters.cpp:7-23).
+* ``ldbd_R.dat`` -- dimension + lattice vectors (lattice.h:48-56).
+* ``ldbd_kvec.bin`` double[nk][3], ``ldbd_ek.bin`` double[nk][nb], ``ldbd_smat.bin``
+  complex128[nk][3][nb*nb] (electron.cpp:134-314).
+* ``ldbd_kpair_k1st.bin`` / ``ldbd_kpair_k2nd.bin`` uint64[npair] with k1st <= k2nd
+  (ElectronPhonon.cpp:182-204).
+* ``ldbd_P1_lindblad.bin`` / ``ldbd_P2_lindblad.bin`` complex128[npair][nb^4], row-major
+  ``[(i1*nb+i2)*nb*nb + i3*nb + i4]`` (ElectronPhonon.cpp:209-253).
+* optionally ``ldbd_P1_lindblad_D1.bin`` / ``ldbd_P2_lindblad_D1.bin`` -- the ab-initio
+  ("ab_neutral") electron-impurity operators that DMD scales by |n_i V_cell| and adds into P
+  (ElectronImpurity.cpp:3-49).
+
+The P operators follow the Lindblad initializer's construction
+(lindbladInit_for-DMD-4.5.6/ElectronPhonon.h:432-572): per phonon mode and for emission /
+absorption, G = g * sqrt(prefac_delta * exp(-(dE +- w)^2 / (2 sigma^2))) inside the energy cutoff,
+A = G*sqrt(n_q+1) or G*sqrt(n_q), and
+
+    P1[(i1 i2),(i3 i4)] += App[i1,i3] conj(App[i2,i4]) + Amm[i1,i3] conj(Amm[i2,i4])
+    P2[(i1 i2),(i3 i4)] += Amp[i3,i1] conj(Amp[i4,i2]) + Apm[i3,i1] conj(Apm[i4,i2])
+
+The electron-impurity operator is the elastic analogue with a single A (ElecImp_Model.h:185-214).
+Random numbers come from ``numpy.random.default_rng([seed, stream, chunk])`` so any chunk can be
+regenerated on its own.
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field, asdict
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import units
+
+
+@dataclass
+class SynthConfig:
+    nk: int = 500                    # k-points kept
+    nb: int = 2                      # bands (2: spin-split pair, 4: two spin-split pairs)
+    seed: int = 0
+    meff: float = 0.3                # parabolic-band effective mass (electron masses)
+    ewindow_ev: float = 0.2          # energy window above the band bottom
+    split_mev: float = 2.0           # spin splitting Delta ~ U(0, split)
+    pair_offset_mev: float = 50.0    # nb=4: offset of the second spin pair
+    de_pair_mev: float = 60.0        # k-pairs kept when |E_k - E_k'| < de_pair
+    nmodes: int = 6
+    omega_mev: Sequence[float] = (5.0, 60.0)
+    g_sigma_mev: float = 20.0
+    degauss_mev: float = 10.0
+    ndegauss: float = 5.0
+    temperature_K: float = 300.0
+    mu_below_cbm_ev: float = 0.1     # chemical potential below the band bottom
+    spin_mix: float = 0.1            # spin-mixing angle scale of the band eigenvectors
+    lattice_a_bohr: float = 10.68    # fcc lattice constant
+    eimp_sigma_mev: Optional[float] = None   # write D1 e-imp files when set
+    ecbm_ha: float = 0.05            # absolute energy of the band bottom (Ha)
+    extra_bands: int = 0             # bands of the density matrix below the e-ph window
+    chunk_pairs: int = 1 << 18
+
+    def to_dict(self):
+        return asdict(self)
+
+
+@dataclass
+class SynthInfo:
+    nk: int
+    nb: int
+    npair: int
+    nk_full: float
+    kmesh: tuple
+    cell_volume: float
+    temperature: float
+    mu: float
+    mode_omega: list = field(default_factory=list)
+
+
+def _fcc(a):
+    return 0.5 * a * np.array([[0.0, 1.0, 1.0], [1.0, 0.0, 1.0], [1.0, 1.0, 0.0]])
+
+
+def _kset(cfg: SynthConfig, rng):
+    """Grid k-points (fractional) inside the energy window, randomly subsampled to nk."""
+    R = _fcc(cfg.lattice_a_bohr)
+    V = abs(np.linalg.det(R))
+    B = 2.0 * np.pi * np.linalg.inv(R).T          # k_cart = B @ k_frac
+    emax = cfg.ewindow_ev * units.eV
+    kmax = math.sqrt(2.0 * cfg.meff * emax)
+    vbz = (2.0 * np.pi) ** 3 / V
+    sphere = 4.0 / 3.0 * np.pi * kmax ** 3
+    n = int(math.ceil((1.4 * cfg.nk * vbz / sphere) ** (1.0 / 3.0)))
+    n = max(n, 4)
+    binv = np.linalg.norm(np.linalg.inv(B), 2)
+    while True:
+        M = int(math.ceil(n * binv * kmax)) + 1
+        r = np.arange(-M, M + 1)
+        g = np.stack(np.meshgrid(r, r, r, indexing="ij"), -1).reshape(-1, 3)
+        kf = g / float(n)
+        kc = kf @ B.T
+        e = (kc ** 2).sum(1) / (2.0 * cfg.meff)
+        keep = np.nonzero(e < emax)[0]
+        if keep.size >= int(1.2 * cfg.nk) + 1:
+            break
+        n += 1
+    sel = np.sort(rng.choice(keep, size=cfg.nk, replace=False))
+    rng.shuffle(sel)                       # a random k order, as a k-point selection would give
+    return R, V, n, kf[sel], e[sel]
+
+
+def _bands(cfg: SynthConfig, e0, rng):
+    nk = e0.size
+    d1 = rng.uniform(0.0, cfg.split_mev * 1e-3 * units.eV, nk)
+    if cfg.nb == 2:
+        e = np.stack([e0 - 0.5 * d1, e0 + 0.5 * d1], 1)
+    elif cfg.nb == 4:
+        d2 = rng.uniform(0.0, cfg.split_mev * 1e-3 * units.eV, nk)
+        off = cfg.pair_offset_mev * 1e-3 * units.eV
+        e = np.stack([e0 - 0.5 * d1, e0 + 0.5 * d1, e0 + off - 0.5 * d2, e0 + off + 0.5 * d2], 1)
+    else:
+        raise ValueError("nb must be 2 or 4")
+    if cfg.extra_bands:
+        lo = np.stack([e[:, 0] - (cfg.extra_bands - i) * 0.02 * units.eV for i in range(cfg.extra_bands)], 1)
+        e = np.concatenate([lo, e], 1)
+    return e + cfg.ecbm_ha
+
+
+def _spin(cfg: SynthConfig, nk, rng):
+    """S_d(k) = 1/2 U_k^dag Sigma_d U_k with U_k = exp(i * mix * H_k), H_k random Hermitian."""
+    nb = cfg.nb + cfg.extra_bands
+    sig = np.array([[[0, 1], [1, 0]], [[0, -1j], [1j, 0]], [[1, 0], [0, -1]]], dtype=np.complex128)
+    if nb % 2 == 0 and nb > 2:
+        sig = np.stack([np.kron(np.eye(nb // 2), s) for s in sig])
+    a = rng.standard_normal((nk, nb, nb)) + 1j * rng.standard_normal((nk, nb, nb))
+    h = 0.5 * (a + np.conj(np.swapaxes(a, 1, 2))) / math.sqrt(2.0 * nb)
+    w, v = np.linalg.eigh(h)
+    u = np.einsum("kij,kj,klj->kil", v, np.exp(1j * cfg.spin_mix * w), np.conj(v))
+    ud = np.conj(np.swapaxes(u, 1, 2))
+    s = 0.5 * np.einsum("kij,djl,klm->kdim", ud, sig, u)
+    s = 0.5 * (s + np.conj(np.swapaxes(s, 2, 3)))   # exactly Hermitian
+    return s.reshape(nk, 3, nb * nb)
+
+
+def _pairs(cfg: SynthConfig, e):
+    """All (k, k') with k <= k' and |Ebar_k - Ebar_k'| < de_pair, in k-major order."""
+    ebar = e.mean(1)
+    order = np.argsort(ebar, kind="stable")
+    es = ebar[order]
+    w = cfg.de_pair_mev * 1e-3 * units.eV
+    lo = np.searchsorted(es, ebar - w, side="right")
+    hi = np.searchsorted(es, ebar + w, side="left")
+    k1, k2 = [], []
+    for ik in range(e.shape[0]):
+        cand = order[lo[ik]:hi[ik]]
+        cand = np.sort(cand[cand >= ik])
+        cand = cand[np.abs(ebar[cand] - ebar[ik]) < w]
+        k1.append(np.full(cand.size, ik, dtype=np.uint64))
+        k2.append(cand.astype(np.uint64))
+    return np.concatenate(k1), np.concatenate(k2)
+
+
+def _cgauss(rng, shape, sigma):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) * (sigma / math.sqrt(2.0))
+
+
+def _outer_p1(a):
+    # P[(i1 i2),(i3 i4)] = A[i1,i3] conj(A[i2,i4])
+    n = a.shape[0]
+    nb = a.shape[1]
+    return np.einsum("nik,njl->nijkl", a, np.conj(a)).reshape(n, nb ** 4)
+
+
+def _outer_p2(a):
+    # P[(i1 i2),(i3 i4)] = A[i3,i1] conj(A[i4,i2])
+    n = a.shape[0]
+    nb = a.shape[1]
+    return np.einsum("nki,nlj->nijkl", a, np.conj(a)).reshape(n, nb ** 4)
+
+
+def eph_chunk(cfg: SynthConfig, ek, ekp, omegas, chunk_index):
+    """P1, P2 (complex128 [n][nb^4]) of the e-ph term for one chunk of pairs."""
+    rng = np.random.default_rng([cfg.seed, 1, chunk_index])
+    n, nb = ek.shape
+    T = cfg.temperature_K * units.Kelvin
+    sigma = cfg.degauss_mev * 1e-3 * units.eV
+    ethr = sigma * cfg.ndegauss
+    gsig = cfg.g_sigma_mev * 1e-3 * units.eV
+    sq_delta = math.sqrt(1.0 / (sigma * math.sqrt(2.0 * math.pi)))
+    dE = ek[:, :, None] - ekp[:, None, :]
+    P1 = np.zeros((n, nb ** 4), np.complex128)
+    P2 = np.zeros((n, nb ** 4), np.complex128)
+    for w in omegas:
+        nq = 1.0 / math.expm1(max(1e-3, w / T))
+        gp = _cgauss(rng, (n, nb, nb), gsig)
+        gm = _cgauss(rng, (n, nb, nb), gsig)
+        xp = dE + w
+        xm = dE - w
+        G2p = np.where(np.abs(xp) < ethr, sq_delta * gp * np.exp(-xp * xp / (4.0 * sigma * sigma)), 0)
+        G2m = np.where(np.abs(xm) < ethr, sq_delta * gm * np.exp(-xm * xm / (4.0 * sigma * sigma)), 0)
+        App = G2p * math.sqrt(nq + 1.0)
+        Apm = G2p * math.sqrt(nq)
+        Amp = G2m * math.sqrt(nq + 1.0)
+        Amm = G2m * math.sqrt(nq)
+        P1 += _outer_p1(App) + _outer_p1(Amm)
+        P2 += _outer_p2(Amp) + _outer_p2(Apm)
+    return P1, P2
+
+
+def eimp_chunk(cfg: SynthConfig, ek, ekp, chunk_index):
+    """Elastic e-imp P1, P2 (unscaled) for one chunk of pairs."""
+    rng = np.random.default_rng([cfg.seed, 2, chunk_index])
+    n, nb = ek.shape
+    sigma = cfg.degauss_mev * 1e-3 * units.eV
+    ethr = sigma * cfg.ndegauss
+    gsig = cfg.eimp_sigma_mev * 1e-3 * units.eV
+    sq_delta = math.sqrt(1.0 / (sigma * math.sqrt(2.0 * math.pi)))
+    dE = ek[:, :, None] - ekp[:, None, :]
+    g = _cgauss(rng, (n, nb, nb), gsig)
+    A = np.where(np.abs(dE) < ethr, sq_delta * g * np.exp(-dE * dE / (4.0 * sigma * sigma)), 0)
+    return _outer_p1(A), _outer_p2(A)
+
+
+def mode_energies(cfg: SynthConfig):
+    rng = np.random.default_rng([cfg.seed, 3])
+    lo, hi = cfg.omega_mev
+    return list(rng.uniform(lo, hi, cfg.nmodes) * 1e-3 * units.eV)
+
+
+def make_ldbd(outdir: str, cfg: SynthConfig, write_param: bool = True, **param_kw) -> SynthInfo:
+    """Write ``outdir/ldbd_data/*`` (and ``outdir/param.in``) for ``cfg``."""
+    d = os.path.join(outdir, "ldbd_data")
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng([cfg.seed, 0])
+    R, V, n, kf, e0 = _kset(cfg, rng)
+    e = _bands(cfg, e0, rng)
+    s = _spin(cfg, cfg.nk, rng)
+    nx = cfg.extra_bands
+    ew = e[:, nx:]                    # energies of the e-ph window
+    k1, k2 = _pairs(cfg, ew)
+    npair = int(k1.size)
+    omegas = mode_energies(cfg)
+    T = cfg.temperature_K * units.Kelvin
+    mu = ew.min() - cfg.mu_below_cbm_ev * units.eV
+    nb = cfg.nb
+    ndm = nb + nx
+
+    with open(os.path.join(d, "ldbd_size.dat"), "w") as f:
+        f.write("There are scatterings only for conduction electrons\n")
+        f.write("%d 0 0 %d %d %d %d 0 0 # nb nv bBot_dm bTop_dm bBot_eph_elec bTop_eph_elec nb_wannier bBot_probe band_dft_skipped\n"
+                % (ndm, ndm, nx, ndm, ndm))
+        f.write("%21.14le %d %d %d %d # nk_full nk kmesh\n" % (float(n) ** 3, cfg.nk, n, n, n))
+        f.write("%d # nkpair_elec\n" % npair)
+        f.write("0 %d 0 0# modeStart modeStp modeSkipStart modeSkipStop\n" % cfg.nmodes)
+        f.write("%21.14le # T\n" % T)
+        f.write("%21.14le %21.14le %21.14le # muMin, muMax mu (given carrier density)\n" % (mu, mu, mu))
+        f.write("%.17g %.17g # degauss\n" % (cfg.degauss_mev * 1e-3 * units.eV, cfg.ndegauss))
+        f.write("%14.7le %14.7le %14.7le %14.7le %14.7le %14.7le # EBot_probe, ETop_probe, EBot_dm, ETop_dm, EBot_eph, ETop_eph\n"
+                % (e.min(), e.max(), e.min(), e.max(), e.min(), e.max()))
+        f.write("%14.7le # omegaMax" % max(omegas))
+    with open(os.path.join(d, "ldbd_R.dat"), "w") as f:
+        f.write("3\n")
+        for i in range(3):
+            f.write("%.17g %.17g %.17g\n" % tuple(R[i]))
+    kf.astype(np.float64).tofile(os.path.join(d, "ldbd_kvec.bin"))
+    e.astype(np.float64).tofile(os.path.join(d, "ldbd_ek.bin"))
+    s.astype(np.complex128).tofile(os.path.join(d, "ldbd_smat.bin"))
+    k1.tofile(os.path.join(d, "ldbd_kpair_k1st.bin"))
+    k2.tofile(os.path.join(d, "ldbd_kpair_k2nd.bin"))
+
+    names = [("ldbd_P1_lindblad.bin", "ldbd_P2_lindblad.bin")]
+    if cfg.eimp_sigma_mev is not None:
+        names.append(("ldbd_P1_lindblad_D1.bin", "ldbd_P2_lindblad_D1.bin"))
+    files = [(open(os.path.join(d, a), "wb"), open(os.path.join(d, b), "wb")) for a, b in names]
+    try:
+        C = cfg.chunk_pairs if nb == 2 else max(1, cfg.chunk_pairs // 8)
+        for ic, p0 in enumerate(range(0, npair, C)):
+            p1 = min(npair, p0 + C)
+            ek = ew[k1[p0:p1].astype(np.int64)]
+            ekp = ew[k2[p0:p1].astype(np.int64)]
+            P1, P2 = eph_chunk(cfg, ek, ekp, omegas, ic)
+            files[0][0].write(P1.tobytes())
+            files[0][1].write(P2.tobytes())
+            if len(files) > 1:
+                Q1, Q2 = eimp_chunk(cfg, ek, ekp, ic)
+                files[1][0].write(Q1.tobytes())
+                files[1][1].write(Q2.tobytes())
+    finally:
+        for a, b in files:
+            a.close()
+            b.close()
+
+    info = SynthInfo(nk=cfg.nk, nb=nb, npair=npair, nk_full=float(n) ** 3, kmesh=(n, n, n),
+                     cell_volume=V, temperature=T, mu=mu, mode_omega=omegas)
+    if write_param:
+        write_param_in(outdir, cfg, info, **param_kw)
+    return info
+
+
+def write_param_in(outdir: str, cfg: SynthConfig, info: SynthInfo, *, tstep_fs=1.0, tend_fs=10.0,
+                   Bpert_T=(0.0, 0.0, 0.1), B_T=(0.0, 0.0, 0.0), eimp_fraction=1e-4,
+                   ode_method="rkf45", extra: Optional[dict] = None):
+    """param.in with the keys DMD's ``parameters::read_param`` (parameters.cpp:48-529) reads."""
+    lines = [
+        "restart = 0",
+        "code = jdftx",
+        "alg_eph_sepr_eh = 1",
+        "alg_eph_need_elec = 1",
+        "alg_eph_need_hole = 0",
+        "alg_scatt = lindblad",
+        "need_imsig = 0",
+        "Bxpert = %.17g" % Bpert_T[0],
+        "Bypert = %.17g" % Bpert_T[1],
+        "Bzpert = %.17g" % Bpert_T[2],
+        "t0 = 0",
+        "tend = %.17g" % tend_fs,
+        "tstep = %.17g" % tstep_fs,
+        "freq_measure_ene = 1000000000",
+        "freq_compute_tau = 1000000000",
+        "alg_ode_method = %s" % ode_method,
+    ]
+    if any(abs(b) > 0 for b in B_T):
+        lines += ["Bx = %.17g" % B_T[0], "By = %.17g" % B_T[1], "Bz = %.17g" % B_T[2]]
+    if cfg.eimp_sigma_mev is not None:
+        # DMD scales the D1 operators by fraction = |n_i * V_cell| (ElectronImpurity.h:18);
+        # impurity_density is read in cm^-3 and converted with bohr2cm^3 (parameters.cpp:221).
+        ni_au = eimp_fraction / info.cell_volume
+        lines += ["impurity_density = %.17g" % (ni_au / units.bohr2cm ** 3), "impMode = ab_neutral"]
+    for k, v in (extra or {}).items():
+        lines.append("%s = %s" % (k, v))
+    with open(os.path.join(outdir, "param.in"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+# Workloads named by what they are, with their sizes.
+WORKLOADS = {
+    # Si-like plain FP64 case: nb=2, nk=500, ~50k pairs.
+    "si_nk500": SynthConfig(nk=500, nb=2, de_pair_mev=60.0),
+    # GaAs-like at scale: nb=2, nk=20k, ~10M pairs, e-ph + e-imp.
+    "gaas_nk20k": SynthConfig(nk=20000, nb=2, de_pair_mev=5.6, eimp_sigma_mev=5.0),
+    # MoS2-like precision case: nb=4, nk=30k, ~4M pairs.
+    "mos2_nk30k": SynthConfig(nk=30000, nb=4, de_pair_mev=3.9),
+}

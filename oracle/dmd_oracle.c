@@ -1,0 +1,459 @@
+/* ORACLE -- CPU restatement of DMD's Lindblad density-matrix right-hand side and steppers.
+ *
+ * TEST INFRASTRUCTURE ONLY. Imported solely by tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg, always as the checker; never part of the product path.
+ *
+ * Pinned against the reference: tests/golden/ holds vectors produced by the reference's own
+ * sources (src_v4.5.7, compiled unmodified against oracle/ref_shim by oracle/Makefile.ref) and the
+ * CPU tests check this file against them. The complex BLAS calls go through the same
+ * cblas_zgemm/cblas_zhemm definitions (oracle/ref_shim/cblas_shim.c) as that build.
+ *
+ * Every function follows the reference statement by statement; file:line citations are relative
+ * to the reference tree. complex128 arrays are interleaved (re, im) doubles, k-major, then
+ * row-major nb x nb.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include "gsl/gsl_cblas.h"
+#include "gsl/gsl_errno.h"
+#include "gsl/gsl_odeiv2.h"
+
+typedef struct { double x, y; } zc;
+
+static inline zc zmk(double x, double y) { zc r = {x, y}; return r; }
+static inline zc zmul(zc a, zc b) { return zmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+static inline zc zadd(zc a, zc b) { return zmk(a.x + b.x, a.y + b.y); }
+static inline zc zsub(zc a, zc b) { return zmk(a.x - b.x, a.y - b.y); }
+static inline zc zconj(zc a) { return zmk(a.x, -a.y); }
+static inline zc zscale(double s, zc a) { return zmk(a.x * s, a.y * s); } /* complex*double (scalar.h:96) */
+static inline zc zcis(double x) { return zmk(cos(x), sin(x)); }          /* cis (scalar.h:122-125) */
+
+/* ---------------------------------------------------------------------------------------------
+ * System description (what DMD holds in electronphonon / singdenmat_k after setup).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct {
+  int nk;            /* elec->nk */
+  int nb_dm;         /* elec->nb_dm: bands of the density matrix */
+  int bstart, bend;  /* electronphonon::bStart/bEnd relative to bStart_dm (ElectronPhonon.cpp:143) */
+  int64_t npair;     /* nkpair_glob (single rank: nkpair_proc) */
+  const uint64_t* k1st;
+  const uint64_t* k2nd;
+  const zc* P1;      /* [npair][nb^4], already scaled and with e-imp folded (ElectronPhonon.cpp:209-253, 44-113) */
+  const zc* P2;
+  const double* e_dm;  /* [nk][nb_dm] */
+  double prefac_eph;   /* 2*pi/nk_full (ElectronPhonon.h:61) */
+  const zc* Hcoh;      /* [nk][nb_dm^2] or NULL (DenMat.cpp:7-28) */
+  int picture_schrodinger; /* alg.picture == "schrodinger" */
+  int expt;            /* alg.expt */
+  const zc* ddmdt_eq;  /* [nk][nb^2] window, NULL unless alg.ddmdteq */
+  int scatt_enable;    /* alg.scatt_enable */
+} orc_sys;
+
+/* workspace for one RHS evaluation */
+typedef struct {
+  zc *dm, *dm1, *ddmdt_eph, *Pdm, *dm1P, *P1t, *P2t, *P1n, *P2n, *coh, *dmx, *dm1x, *ddmx, *ddmdt;
+} orc_ws;
+
+static void* xmalloc(size_t n) { void* p = calloc(n ? n : 1, 1); if (!p) abort(); return p; }
+
+orc_ws* orc_ws_new(const orc_sys* s) {
+  orc_ws* w = (orc_ws*)xmalloc(sizeof(orc_ws));
+  const int nb = s->bend - s->bstart, nb2 = nb * nb, nb4 = nb2 * nb2, nd2 = s->nb_dm * s->nb_dm;
+  w->dm = (zc*)xmalloc(sizeof(zc) * s->nk * nb2);
+  w->dm1 = (zc*)xmalloc(sizeof(zc) * s->nk * nb2);
+  w->ddmdt_eph = (zc*)xmalloc(sizeof(zc) * s->nk * nb2);
+  w->Pdm = (zc*)xmalloc(sizeof(zc) * s->nk * nb2);
+  w->dm1P = (zc*)xmalloc(sizeof(zc) * s->nk * nb2);
+  w->P1t = (zc*)xmalloc(sizeof(zc) * nb4);
+  w->P2t = (zc*)xmalloc(sizeof(zc) * nb4);
+  w->P1n = (zc*)xmalloc(sizeof(zc) * nb4);
+  w->P2n = (zc*)xmalloc(sizeof(zc) * nb4);
+  w->coh = (zc*)xmalloc(sizeof(zc) * s->nk * nd2);
+  w->dmx = (zc*)xmalloc(sizeof(zc) * s->nk * nd2);
+  w->dm1x = (zc*)xmalloc(sizeof(zc) * s->nk * nd2);
+  w->ddmx = (zc*)xmalloc(sizeof(zc) * s->nk * nd2);
+  w->ddmdt = (zc*)xmalloc(sizeof(zc) * s->nk * nd2);
+  return w;
+}
+
+void orc_ws_free(orc_ws* w) {
+  if (!w) return;
+  zc* p[] = {w->dm, w->dm1, w->ddmdt_eph, w->Pdm, w->dm1P, w->P1t, w->P2t, w->P1n, w->P2n, w->coh, w->dmx, w->dm1x, w->ddmx, w->ddmdt};
+  for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); ++i) free(p[i]);
+  free(w);
+}
+
+/* zgemm_interface(C, A, B, m, n, k, alpha, beta) -- comm/mymatrix.cpp:82-86 (row-major, no trans) */
+static void zgemm_mnk(zc* C, const zc* A, const zc* B, int m, int n, int k, zc alpha, zc beta) {
+  cblas_zgemm(CblasRowMajor, CblasNoTrans, CblasNoTrans, m, n, k, &alpha, A, k, B, n, &beta, C, n);
+}
+/* zhemm_interface(C, left, A, B, n, alpha, beta) -- comm/mymatrix.cpp:73-76 (upper triangle) */
+static void zhemm_n(zc* C, int left, const zc* A, const zc* B, int n, zc alpha, zc beta) {
+  cblas_zhemm(CblasRowMajor, left ? CblasLeft : CblasRight, CblasUpper, n, n, &alpha, A, n, B, n, &beta, C, n);
+}
+
+/* compute_Pt -- evolve_eph.cpp:169-187 */
+static void compute_Pt(int nb, double t, const double* ek, const double* ekp, const zc* P, zc* Pt, int minus) {
+  for (int i1 = 0; i1 < nb; i1++) {
+    int n1 = i1 * nb;
+    for (int i2 = 0; i2 < nb; i2++) {
+      int n12 = (n1 + i2) * nb;
+      for (int i3 = 0; i3 < nb; i3++) {
+        int n123 = (n12 + i3) * nb;
+        for (int i4 = 0; i4 < nb; i4++) {
+          if (!minus) Pt[n123 + i4] = zmul(P[n123 + i4], zcis((ek[i1] - ekp[i3] - ek[i2] + ekp[i4]) * t));
+          else Pt[n123 + i4] = zmul(P[n123 + i4], zcis((ek[i3] - ekp[i1] - ek[i4] + ekp[i2]) * t));
+        }
+      }
+    }
+  }
+}
+
+/* electronphonon::evolve -- evolve_eph.cpp:34-166 (summode, dense P, expt or not, optional ddmdteq;
+ * no valley filtering: the default alg.only_intra/intervalley = false and fewer than two valleys
+ * keep every pair, evolve_eph.cpp:52-58). e is the window energy array [nk][nb]. */
+void orc_evolve(const orc_sys* s, orc_ws* w, const double* e, double t, const zc* dm, const zc* dm1, zc* ddmdt_eph, int compute_eq) {
+  const int nk = s->nk, nb = s->bend - s->bstart, nb2 = nb * nb, nb4 = nb2 * nb2;
+  const zc c1 = zmk(1, 0), cm1 = zmk(-1, 0), c0 = zmk(0, 0);
+  memset(ddmdt_eph, 0, sizeof(zc) * nk * nb2);
+  memset(w->Pdm, 0, sizeof(zc) * nk * nb2);
+  memset(w->dm1P, 0, sizeof(zc) * nk * nb2);
+  for (int64_t ip = 0; ip < s->npair; ip++) {
+    const int ik = (int)s->k1st[ip], ikp = (int)s->k2nd[ip];
+    const zc* P1 = s->P1 + (size_t)ip * nb4;
+    const zc* P2 = s->P2 + (size_t)ip * nb4;
+    if (!s->expt) {
+      /* axbyc(P1t, P1, nb^4): y = x */
+      memcpy(w->P1t, P1, sizeof(zc) * nb4);
+      memcpy(w->P2t, P2, sizeof(zc) * nb4);
+    } else {
+      compute_Pt(nb, t, e + (size_t)ik * nb, e + (size_t)ikp * nb, P1, w->P1t, 0);
+      compute_Pt(nb, t, e + (size_t)ik * nb, e + (size_t)ikp * nb, P2, w->P2t, 1);
+    }
+    zgemm_mnk(w->Pdm + (size_t)ik * nb2, w->P1t, dm + (size_t)ikp * nb2, nb2, 1, nb2, c1, c1);
+    zgemm_mnk(w->dm1P + (size_t)ik * nb2, dm1 + (size_t)ikp * nb2, w->P2t, 1, nb2, nb2, c1, c1);
+    if (ik < ikp) {
+      for (int i = 0; i < nb4; i++) { w->P2n[i] = zconj(w->P1t[i]); w->P1n[i] = zconj(w->P2t[i]); }
+      zgemm_mnk(w->Pdm + (size_t)ikp * nb2, w->P1n, dm + (size_t)ik * nb2, nb2, 1, nb2, c1, c1);
+      zgemm_mnk(w->dm1P + (size_t)ikp * nb2, dm1 + (size_t)ik * nb2, w->P2n, 1, nb2, nb2, c1, c1);
+    }
+  }
+  /* the rank-local sums are complete on a single rank (mymp allreduce, evolve_eph.cpp:137) */
+  zc* contrib = w->P1t; /* reuse as ddmdt_contrib (nb2 <= nb4) */
+  for (int ik = 0; ik < nk; ik++) {
+    memset(contrib, 0, sizeof(zc) * nb2);
+    zhemm_n(contrib, 1, dm1 + (size_t)ik * nb2, w->Pdm + (size_t)ik * nb2, nb, c1, c0);
+    zhemm_n(contrib, 0, dm + (size_t)ik * nb2, w->dm1P + (size_t)ik * nb2, nb, cm1, c1);
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < nb; j++)
+        ddmdt_eph[(size_t)ik * nb2 + i * nb + j] = zscale(s->prefac_eph * 0.5, zadd(contrib[i * nb + j], zconj(contrib[j * nb + i])));
+  }
+  if (!compute_eq && s->ddmdt_eq) {
+    for (int ik = 0; ik < nk; ik++)
+      for (int i = 0; i < nb; i++)
+        for (int j = 0; j < nb; j++) {
+          zc* o = &ddmdt_eph[(size_t)ik * nb2 + i * nb + j];
+          const zc q = s->ddmdt_eq[(size_t)ik * nb2 + i * nb + j];
+          if (i == j || s->picture_schrodinger) *o = zsub(*o, q);
+          else *o = zsub(*o, zmul(q, zcis((e[(size_t)ik * nb + i] - e[(size_t)ik * nb + j]) * t)));
+        }
+  }
+}
+
+/* trunc_copy_arraymat -- comm/mymatrix.cpp:134-144 */
+static void trunc_copy(zc* A, const zc* B, int n1, int n2, int bs, int be) {
+  const int nb = be - bs;
+  for (int i1 = 0; i1 < n1; i1++)
+    for (int b1 = 0; b1 < nb; b1++)
+      for (int b2 = 0; b2 < nb; b2++) A[(size_t)i1 * nb * nb + b1 * nb + b2] = B[(size_t)i1 * n2 * n2 + (b1 + bs) * n2 + b2 + bs];
+}
+
+/* electronphonon::evolve_driver -- evolve_eph.cpp:21-32 (window copy, evolve, set_mat back;
+ * set_mat's column loop starts at i0 = bStart, comm/mymatrix.cpp:114-119, and i0 = j0 here) */
+void orc_evolve_driver(const orc_sys* s, orc_ws* w, double t, const zc* dm_x, const zc* dm1_x, zc* ddmdt_x) {
+  const int nk = s->nk, nd = s->nb_dm, bs = s->bstart, be = s->bend, nb = be - bs;
+  double* e = (double*)xmalloc(sizeof(double) * nk * nb);
+  for (int ik = 0; ik < nk; ik++)
+    for (int b = 0; b < nb; b++) e[ik * nb + b] = s->e_dm[(size_t)ik * nd + bs + b]; /* trunc_alloccopy_array (ElectronPhonon.h:79) */
+  trunc_copy(w->dm, dm_x, nk, nd, bs, be);
+  trunc_copy(w->dm1, dm1_x, nk, nd, bs, be);
+  orc_evolve(s, w, e, t, w->dm, w->dm1, w->ddmdt_eph, 0);
+  memset(ddmdt_x, 0, sizeof(zc) * nk * nd * nd);
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = bs; i < be; i++)
+      for (int j = bs; j < be; j++) ddmdt_x[(size_t)ik * nd * nd + i * nd + j] = w->ddmdt_eph[(size_t)ik * nb * nb + (i - bs) * nb + j - bs];
+  free(e);
+}
+
+/* singdenmat_k::evolve_coh -- DenMat.cpp:29-55 (single rank: nk_proc = nk, ik0 = 0) */
+void orc_evolve_coh(const orc_sys* s, orc_ws* w, double t, const zc* dm, zc* out) {
+  const int nk = s->nk, nb = s->nb_dm, nb2 = nb * nb;
+  const zc c1 = zmk(1, 0), cm1 = zmk(-1, 0), c0 = zmk(0, 0), cmi = zmk(0, -1);
+  zc* Hbuf = (zc*)xmalloc(sizeof(zc) * nb2);
+  zc* Ht = Hbuf;
+  memset(out, 0, sizeof(zc) * nk * nb2);
+  for (int ik = 0; ik < nk; ik++) {
+    const zc* dmk = dm + (size_t)ik * nb2;
+    zc* o = out + (size_t)ik * nb2;
+    const double* ek = s->e_dm + (size_t)ik * nb;
+    if (s->Hcoh) {
+      const zc* Hk = s->Hcoh + (size_t)ik * nb2;
+      if (!s->picture_schrodinger) {
+        for (int i = 0; i < nb; i++)
+          for (int j = 0; j < nb; j++) Ht[i * nb + j] = (i == j) ? Hk[i * nb + j] : zmul(Hk[i * nb + j], zcis((ek[i] - ek[j]) * t));
+      } else {
+        memcpy(Ht, Hk, sizeof(zc) * nb2); /* Hcoh already holds H + diag(e) (DenMat.cpp:20-24) */
+      }
+      zhemm_n(o, 0, Ht, dmk, nb, c1, c0);   /* dm * H   (Right) */
+      zhemm_n(o, 1, Ht, dmk, nb, c1, cm1);  /* H * dm - dm * H */
+      for (int i = 0; i < nb2; i++) o[i] = zmul(o[i], cmi);
+    } else if (s->picture_schrodinger) {
+      /* commutator_mat_diag(C, e, dm, nb, cmi) (comm/mymatrix.cpp:230-235 with mat_diag_mult
+       * :173-199): C = dm_ij e_j; C = -C + e_i dm_ij; C *= -i */
+      for (int i = 0; i < nb; i++)
+        for (int j = 0; j < nb; j++) {
+          const zc d = dmk[i * nb + j];
+          const zc a = zmk(-(d.x * ek[j]), -(d.y * ek[j]));
+          o[i * nb + j] = zmul(zadd(a, zmul(zmk(ek[i], 0), d)), cmi);
+        }
+    }
+  }
+  free(Hbuf);
+}
+
+/* dm_dynamics::compute -- DensityMatrix_Dynamics.h:243-278 (no laser, no phenomenological term,
+ * not semiclassical): ddmdt = coherent + scattering on the state dm; 1 - dm per set_oneminusdm
+ * (DenMat.cpp:249-261). */
+void orc_compute(const orc_sys* s, orc_ws* w, double t, const zc* dm, zc* ddmdt) {
+  const int nk = s->nk, nb = s->nb_dm, nb2 = nb * nb;
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < nb; j++) {
+        const zc v = dm[(size_t)ik * nb2 + i * nb + j];
+        w->dm1x[(size_t)ik * nb2 + i * nb + j] = (i == j) ? zsub(zmk(1, 0), v) : zmk(-v.x, -v.y);
+      }
+  memset(ddmdt, 0, sizeof(zc) * nk * nb2);
+  if (s->picture_schrodinger || s->Hcoh) {
+    orc_evolve_coh(s, w, t, dm, w->coh);
+    for (size_t i = 0; i < (size_t)nk * nb2; i++) ddmdt[i] = zadd(ddmdt[i], w->coh[i]);
+  }
+  if (s->scatt_enable) {
+    orc_evolve_driver(s, w, t, dm, w->dm1x, w->ddmx);
+    for (size_t i = 0; i < (size_t)nk * nb2; i++) ddmdt[i] = zadd(ddmdt[i], w->ddmx[i]);
+  }
+}
+
+/* func -- DensityMatrix_Dynamics.h:358-369 with copy_complex_from_real / copy_real_from_complex
+ * (comm/ODE.h:6-15): y and dydt are interleaved (re, im). */
+typedef struct { const orc_sys* s; orc_ws* w; unsigned long ncalls; } orc_ctx;
+
+int orc_func(double t, const double y[], double dydt[], void* params) {
+  orc_ctx* c = (orc_ctx*)params;
+  c->ncalls++;
+  orc_compute(c->s, c->w, t, (const zc*)y, (zc*)dydt);
+  return GSL_SUCCESS;
+}
+
+/* observable "sx/sy/sz" for bands [bs, be) -- observable.h:356-366 (general branch) and
+ * 412-429 (totals): tot = prefac * sum_k sum_{i in [bs,be)} sum_b Re[o_ib(t) (dm_bi - f_i delta_ib)]
+ * with o_ib(t) = o_ib * cis((e_i - e_b) t) off the diagonal in the interaction picture, and
+ * tot_amp the same without the phase. prefac = 1/(nk_full * cell_size_cmd) (observable.h:54). */
+void orc_measure(int nk, int nb, int bs, int be, const zc* obs /*[nk][nb^2] one direction*/, size_t obs_kstride,
+                 const double* f, const double* e, double t, int picture_schrodinger, const zc* dm, double prefac,
+                 double* tot_out, double* amp_out) {
+  double tot = 0, tot_amp = 0;
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = bs; i < be; i++) {
+      double ob = 0, ob_amp = 0;
+      for (int b = 0; b < nb; b++) {
+        const zc ob_kib = obs[(size_t)ik * obs_kstride + i * nb + b];
+        const zc ob_kib_t = (i == b || picture_schrodinger) ? ob_kib : zmul(ob_kib, zcis((e[(size_t)ik * nb + i] - e[(size_t)ik * nb + b]) * t));
+        zc dm_kbi = dm[(size_t)ik * nb * nb + b * nb + i];
+        if (i == b) dm_kbi = zsub(dm_kbi, zmk(f[(size_t)ik * nb + i], 0));
+        ob += zmul(ob_kib_t, dm_kbi).x;
+        ob_amp += zmul(ob_kib, dm_kbi).x;
+      }
+      tot += ob;
+      tot_amp += ob_amp;
+    }
+  *tot_out = tot * prefac;
+  *amp_out = tot_amp * prefac;
+}
+
+/* electron::compute_dm_Bpert_1st -- electron.cpp:62-98 (needL = false): dm = f + dfde * (Bpert . S)
+ * with the interaction-picture phase at t0 off the diagonal. */
+void orc_dm_bpert(int nk, int nb, const zc* s /*[nk][3][nb^2]*/, const double* e, const double* f, double temperature,
+                  const double* Bpert, double t0, int picture_schrodinger, zc* dm_out) {
+  const double degthr = 1e-8;
+  for (int ik = 0; ik < nk; ik++) {
+    zc* d = dm_out + (size_t)ik * nb * nb;
+    const zc* sk = s + (size_t)ik * 3 * nb * nb;
+    for (int i = 0; i < nb; i++)
+      for (int j = i; j < nb; j++) {
+        zc H1 = zadd(zadd(zscale(Bpert[0], sk[i * nb + j]), zscale(Bpert[1], sk[nb * nb + i * nb + j])), zscale(Bpert[2], sk[2 * nb * nb + i * nb + j]));
+        double dfde;
+        const double *ek = e + (size_t)ik * nb, *fk = f + (size_t)ik * nb;
+        if (fabs(ek[i] - ek[j]) < degthr) {
+          double favg = 0.5 * (fk[i] + fk[j]);
+          dfde = favg * (favg - 1.) / temperature;
+        } else {
+          dfde = (fk[i] - fk[j]) / (ek[i] - ek[j]);
+        }
+        d[i * nb + j] = zscale(dfde, H1);
+        if (i != j && !picture_schrodinger) d[i * nb + j] = zmul(d[i * nb + j], zcis((ek[i] - ek[j]) * t0));
+        if (i < j) d[j * nb + i] = zconj(d[i * nb + j]);
+      }
+    for (int i = 0; i < nb; i++) d[i * nb + i] = zadd(d[i * nb + i], zmk(f[(size_t)ik * nb + i], 0));
+  }
+}
+
+/* singdenmat_k::init_dm(complex**) -- DenMat.cpp:65-81: Hermitian part of dm0 */
+void orc_init_dm(int nk, int nb, const zc* dm0, zc* dm) {
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < nb; j++)
+        dm[(size_t)ik * nb * nb + i * nb + j] = zscale(0.5, zadd(dm0[(size_t)ik * nb * nb + i * nb + j], zconj(dm0[(size_t)ik * nb * nb + j * nb + i])));
+}
+
+/* electron::set_H_BS -- electron.cpp:19-42 (no g-factor distribution, no Bso, needL = false):
+ * H = B . S; then singdenmat_k::init_Hcoh (DenMat.cpp:7-28) adds diag(e) in the Schrodinger picture. */
+void orc_H_BS(int nk, int nb, const zc* s, const double* B, const double* e, int picture_schrodinger, zc* H) {
+  for (int ik = 0; ik < nk; ik++)
+    for (int ij = 0; ij < nb * nb; ij++) {
+      const zc* sk = s + (size_t)ik * 3 * nb * nb;
+      /* vec3_dot_vec3array(vm, v, m, n): vm = v[0]*m[0] + v[1]*m[1] + v[2]*m[2] */
+      H[(size_t)ik * nb * nb + ij] = zadd(zadd(zscale(B[0], sk[ij]), zscale(B[1], sk[nb * nb + ij])), zscale(B[2], sk[2 * nb * nb + ij]));
+    }
+  if (picture_schrodinger)
+    for (int ik = 0; ik < nk; ik++)
+      for (int i = 0; i < nb; i++) H[(size_t)ik * nb * nb + i * nb + i].x += e[(size_t)ik * nb + i];
+}
+
+/* ---------------------------------------------------------------------------------------------
+ * Steppers.
+ * ------------------------------------------------------------------------------------------- */
+
+/* Classic fixed-step RK4 calling func (the oracle driver's mode; DMD itself offers RKF45 and
+ * Euler). y_{n+1} = y_n + h/6 (k1 + 2 k2 + 2 k3 + k4), stages at t, t+h/2, t+h/2, t+h.
+ * After every `every` steps the S observable of direction idir is recorded (if obs != NULL). */
+typedef struct {
+  const zc* obs; size_t obs_kstride; const double* f; double prefac; int bs, be;
+} orc_meas;
+
+int orc_rk4(const orc_sys* s, double t0, double h, long nsteps, double* y, long every, const orc_meas* m, double* rec /* [nsteps/every][3] t,tot,amp */) {
+  const size_t n2 = (size_t)2 * s->nk * s->nb_dm * s->nb_dm;
+  orc_ws* w = orc_ws_new(s);
+  orc_ctx c = {s, w, 0};
+  double *k1 = (double*)xmalloc(n2 * 8), *k2 = (double*)xmalloc(n2 * 8), *k3 = (double*)xmalloc(n2 * 8), *k4 = (double*)xmalloc(n2 * 8), *yt = (double*)xmalloc(n2 * 8);
+  const double hh = 0.5 * h, h6 = h / 6.0;
+  long irec = 0;
+  for (long st = 0; st < nsteps; ++st) {
+    const double t = t0 + (double)st * h;
+    orc_func(t, y, k1, &c);
+    for (size_t i = 0; i < n2; ++i) yt[i] = y[i] + hh * k1[i];
+    orc_func(t + hh, yt, k2, &c);
+    for (size_t i = 0; i < n2; ++i) yt[i] = y[i] + hh * k2[i];
+    orc_func(t + hh, yt, k3, &c);
+    for (size_t i = 0; i < n2; ++i) yt[i] = y[i] + h * k3[i];
+    orc_func(t + h, yt, k4, &c);
+    for (size_t i = 0; i < n2; ++i) y[i] = y[i] + h6 * (k1[i] + 2.0 * k2[i] + 2.0 * k3[i] + k4[i]);
+    if (m && rec && every > 0 && (st + 1) % every == 0) {
+      const double t1 = t0 + (double)(st + 1) * h;
+      double tot, amp;
+      orc_measure(s->nk, s->nb_dm, m->bs, m->be, m->obs, m->obs_kstride, m->f, s->e_dm, t1, s->picture_schrodinger, (const zc*)y, m->prefac, &tot, &amp);
+      rec[3 * irec + 0] = t1; rec[3 * irec + 1] = tot; rec[3 * irec + 2] = amp;
+      ++irec;
+    }
+  }
+  free(k1); free(k2); free(k3); free(k4); free(yt);
+  orc_ws_free(w);
+  return 0;
+}
+
+/* DMD's evolve_gsl loop (DensityMatrix_Dynamics.h:189-225) without laser / scattering updates:
+ * the GSL driver (oracle/gsl_rkf45.c) advances to ti = t0 + it*tstep for it = 1..nout and S is
+ * recorded after each output interval. Returns the GSL status; ncalls_out[it-1] holds the RHS
+ * evaluations of each interval (ode.ncalls). */
+int orc_rkf45(const orc_sys* s, double t0, double tend, double tstep, double hstart, double hmin, double hmax, double epsabs,
+              double* y, const orc_meas* m, double* rec, long* ncalls_out, long max_out) {
+  const size_t n2 = (size_t)2 * s->nk * s->nb_dm * s->nb_dm;
+  orc_ws* w = orc_ws_new(s);
+  orc_ctx c = {s, w, 0};
+  gsl_odeiv2_system sys = {orc_func, 0, n2, &c};
+  gsl_odeiv2_driver* d = gsl_odeiv2_driver_alloc_y_new(&sys, gsl_odeiv2_step_rkf45, hstart, epsabs, 0.0);
+  gsl_odeiv2_driver_set_hmin(d, hmin);
+  gsl_odeiv2_driver_set_hmax(d, hmax);
+  double t = t0, ti = t0;
+  int status = GSL_SUCCESS;
+  long it = 1;
+  for (; t < tend && it <= max_out; it += 1) {
+    ti += tstep;
+    c.ncalls = 0;
+    status = gsl_odeiv2_driver_apply(d, &t, ti, y);
+    if (status != GSL_SUCCESS) break;
+    if (ncalls_out) ncalls_out[it - 1] = (long)c.ncalls;
+    if (m && rec) {
+      double tot, amp;
+      orc_measure(s->nk, s->nb_dm, m->bs, m->be, m->obs, m->obs_kstride, m->f, s->e_dm, t, s->picture_schrodinger, (const zc*)y, m->prefac, &tot, &amp);
+      rec[3 * (it - 1) + 0] = t; rec[3 * (it - 1) + 1] = tot; rec[3 * (it - 1) + 2] = amp;
+    }
+  }
+  gsl_odeiv2_driver_free(d);
+  orc_ws_free(w);
+  return status;
+}
+
+/* Euler step -- singdenmat_k::update_dm_euler (DenMat.cpp:236-248) after compute(t). */
+int orc_euler(const orc_sys* s, double t0, double h, long nsteps, double* y) {
+  const int nk = s->nk, nb = s->nb_dm, nb2 = nb * nb;
+  orc_ws* w = orc_ws_new(s);
+  for (long st = 0; st < nsteps; ++st) {
+    const double t = t0 + (double)st * h; /* sdmk->t += dt: accumulated in DMD, identical for these h */
+    orc_compute(s, w, t, (const zc*)y, w->ddmdt);
+    zc* dm = (zc*)y;
+    for (int ik = 0; ik < nk; ik++)
+      for (int i = 0; i < nb; i++)
+        for (int j = 0; j < nb; j++)
+          dm[(size_t)ik * nb2 + i * nb + j] = zadd(dm[(size_t)ik * nb2 + i * nb + j],
+              zscale(0.5 * h, zadd(w->ddmdt[(size_t)ik * nb2 + i * nb + j], zconj(w->ddmdt[(size_t)ik * nb2 + j * nb + i]))));
+  }
+  orc_ws_free(w);
+  return 0;
+}
+
+/* one-call wrappers used through ctypes */
+void orc_rhs(const orc_sys* s, double t, const double* y, double* dydt) {
+  orc_ws* w = orc_ws_new(s);
+  orc_compute(s, w, t, (const zc*)y, (zc*)dydt);
+  orc_ws_free(w);
+}
+
+void orc_rhs_parts(const orc_sys* s, double t, const double* y, double* ddmdt_eph, double* ddmdt_coh) {
+  orc_ws* w = orc_ws_new(s);
+  const int nk = s->nk, nb = s->nb_dm, nb2 = nb * nb;
+  const zc* dm = (const zc*)y;
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < nb; j++) {
+        const zc v = dm[(size_t)ik * nb2 + i * nb + j];
+        w->dm1x[(size_t)ik * nb2 + i * nb + j] = (i == j) ? zsub(zmk(1, 0), v) : zmk(-v.x, -v.y);
+      }
+  orc_evolve_driver(s, w, t, dm, w->dm1x, (zc*)ddmdt_eph);
+  if (s->Hcoh || s->picture_schrodinger) orc_evolve_coh(s, w, t, dm, (zc*)ddmdt_coh);
+  else memset(ddmdt_coh, 0, sizeof(zc) * nk * nb2);
+  orc_ws_free(w);
+}
+
+size_t orc_sys_size(void) { return sizeof(orc_sys); }
+
+/* electron::fermi (electron.h:119-124) over an array, with the C library's exp */
+void orc_fermi(double T, double mu, const double* e, double* f, size_t n) {
+  for (size_t i = 0; i < n; i++) {
+    const double ebyt = (e[i] - mu) / T;
+    if (ebyt < -46) f[i] = 1;
+    else if (ebyt > 46) f[i] = 0;
+    else f[i] = 1. / (exp(ebyt) + 1);
+  }
+}

@@ -1,0 +1,374 @@
+"""ORACLE (test infrastructure only): Python side of the CPU restatement in dmd_oracle.c.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module, always as
+the checker. It reads a DMD input directory (param.in + ldbd_data/) the way the reference's
+constructors do and calls the C restatement through ctypes.
+
+Setup statements restated here (reference file:line):
+  * param.in parsing -- parameters::map_input (parameters.cpp:591-623) and get() (:530-548),
+    including the key = trim(substr(0, '=' position - 1)) convention;
+  * ldbd_size.dat / ldbd_R.dat / ldbd_ek.bin / ldbd_smat.bin / kpair / P readers --
+    electron.cpp:100-314, lattice.h:48-56, ElectronPhonon.cpp:132-253, parameters.cpp:7-23;
+  * Fermi occupations -- electron::fermi (electron.h:119-124) with mu = (mu_file/eV)*eV as get()
+    returns it;
+  * e-imp fold P += |n_i V_cell| * P_D1 -- ElectronImpurity.cpp:3-49 and ElectronPhonon.cpp:44-113;
+  * initial state -- electron::compute_dm_Bpert_1st (electron.cpp:62-98) then
+    singdenmat_k::init_dm (DenMat.cpp:65-81);
+  * coherent Hamiltonian -- electron::set_H_BS (electron.cpp:19-42), singdenmat_k::init_Hcoh
+    (DenMat.cpp:7-28);
+  * observable prefactor 1/(nk_full * cell_size_cmd) -- observable.h:54, lattice.h:27-36.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import subprocess
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+SRCS = [os.path.join(HERE, "dmd_oracle.c"), os.path.join(HERE, "gsl_rkf45.c"),
+        os.path.join(HERE, "ref_shim", "cblas_shim.c")]
+
+# comm/Units.h
+eV = 1.0 / 27.21138505
+Joule = 1.0 / 4.35974434e-18
+Angstrom = 1.0 / 0.5291772
+meter = 1e10 * Angstrom
+kg = 1.0 / 9.10938291e-31
+Newton = Joule / meter
+sec = math.sqrt((kg * meter) / Newton)
+fs = sec * 1.0e-15
+Tesla2au = 1.0 / 2.3505175675871e5
+bohr2cm = 5.291772109038e-9
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so (gcc, -ffp-contract=off so rounding is host independent)."""
+    newest = max(os.path.getmtime(s) for s in SRCS)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", os.path.join(HERE, "ref_shim", "include"),
+               "-o", LIB + ".tmp"] + SRCS + ["-lm"]
+        subprocess.run(cmd, check=True)
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        _lib.orc_rhs.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]
+        _lib.orc_rhs_parts.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_rk4.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_long, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p]
+        _lib.orc_rkf45.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                   C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long]
+        _lib.orc_rkf45.restype = C.c_int
+        _lib.orc_euler.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_long, C.c_void_p]
+        _lib.orc_measure.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
+                                     C.c_double, C.c_int, C.c_void_p, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib.orc_sys_size.restype = C.c_size_t
+    return _lib
+
+
+class _Sys(C.Structure):
+    _fields_ = [("nk", C.c_int), ("nb_dm", C.c_int), ("bstart", C.c_int), ("bend", C.c_int), ("npair", C.c_int64),
+                ("k1st", C.c_void_p), ("k2nd", C.c_void_p), ("P1", C.c_void_p), ("P2", C.c_void_p),
+                ("e_dm", C.c_void_p), ("prefac_eph", C.c_double), ("Hcoh", C.c_void_p),
+                ("picture_schrodinger", C.c_int), ("expt", C.c_int), ("ddmdt_eq", C.c_void_p), ("scatt_enable", C.c_int)]
+
+
+class _Meas(C.Structure):
+    _fields_ = [("obs", C.c_void_p), ("obs_kstride", C.c_size_t), ("f", C.c_void_p), ("prefac", C.c_double),
+                ("bs", C.c_int), ("be", C.c_int)]
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+# ------------------------------------------------------------------------------------------------
+# param.in
+# ------------------------------------------------------------------------------------------------
+def parse_param_in(path: str) -> dict:
+    """parameters::map_input (parameters.cpp:591-623)."""
+    def trim(s):
+        s = s.lstrip(" ")
+        return s.rstrip(" \n\r\t")
+    out, last_key, b_join = {}, "", False
+    with open(path) as f:
+        for line in f.read().split("\n"):
+            b_will_join = False
+            b_joined = False
+            line2 = trim(line)
+            if line[:1] == "#":
+                continue
+            if line2 and line2[-1] == "\\":
+                b_will_join = True
+                line2 = line2[:-1] + " "
+            if b_join:
+                out[last_key] += " " + line2
+                b_joined = True
+            b_join = b_will_join
+            if not b_joined:
+                eq = line2.find("=")
+                if eq < 0:
+                    continue
+                last_key = trim(line2[:max(eq - 1, 0)])
+                out[last_key] = trim(line2[eq + 1:])
+    return out
+
+
+def _atof(s: str) -> float:
+    """C atof: longest numeric prefix, 0 when none."""
+    s = s.strip()
+    best = 0.0
+    for i in range(len(s), 0, -1):
+        try:
+            best = float(s[:i])
+            return best
+        except ValueError:
+            continue
+    return best
+
+
+def pget(m: dict, key: str, default: float, unit: float = 1.0) -> float:
+    """parameters::get (parameters.cpp:530-548)."""
+    if key in m:
+        return _atof(m[key]) * unit
+    return default * unit
+
+
+# ------------------------------------------------------------------------------------------------
+# ldbd_data
+# ------------------------------------------------------------------------------------------------
+def read_size(d: str) -> dict:
+    with open(os.path.join(d, "ldbd_data", "ldbd_size.dat")) as f:
+        lines = f.read().split("\n")
+    l2 = [int(x) for x in lines[1].split("#")[0].split()]
+    l3 = lines[2].split("#")[0].split()
+    info = dict(nb=l2[0], nv=l2[1], bStart_dm=l2[2], bEnd_dm=l2[3], bStart_eph=l2[4], bEnd_eph=l2[5],
+                nk_full=float(l3[0]), nk=int(l3[1]), kmesh=tuple(int(x) for x in l3[2:5]),
+                nkpair=int(lines[3].split("#")[0].split()[0]),
+                temperature=float(lines[5].split("#")[0].split()[0]),
+                mu=float(lines[6].split("#")[0].split()[2]))
+    return info
+
+
+def read_R(d: str) -> np.ndarray:
+    with open(os.path.join(d, "ldbd_data", "ldbd_R.dat")) as f:
+        tok = f.read().split()
+    dim = int(tok[0])
+    R = np.array([float(x) for x in tok[1:10]]).reshape(3, 3)
+    return dim, R
+
+
+def det3(R):
+    """matrix3 determinant by cofactor expansion along the first row."""
+    return (R[0, 0] * (R[1, 1] * R[2, 2] - R[1, 2] * R[2, 1]) - R[0, 1] * (R[1, 0] * R[2, 2] - R[1, 2] * R[2, 0])
+            + R[0, 2] * (R[1, 0] * R[2, 1] - R[1, 1] * R[2, 0]))
+
+
+def fermi(T, mu, e):
+    """electron::fermi (electron.h:119-124), elementwise, evaluated in C with libm's exp."""
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    out = np.empty_like(e)
+    lib().orc_fermi(C.c_double(T), C.c_double(mu), C.c_void_p(e.ctypes.data), C.c_void_p(out.ctypes.data),
+                    C.c_size_t(e.size))
+    return out
+
+
+@dataclass
+class OracleSystem:
+    nk: int
+    nb_dm: int
+    bstart: int
+    bend: int
+    npair: int
+    e_dm: np.ndarray
+    f_dm: np.ndarray
+    k1st: np.ndarray
+    k2nd: np.ndarray
+    P1: np.ndarray
+    P2: np.ndarray
+    prefac_eph: float
+    Hcoh: Optional[np.ndarray]
+    smat: np.ndarray
+    dm0: np.ndarray
+    picture_schrodinger: int
+    expt: int
+    t0: float
+    tstep: float
+    tend: float
+    temperature: float
+    mu: float
+    nk_full: float
+    ob_prefac: float
+    ode: dict
+    params: dict
+
+    def cstruct(self):
+        s = _Sys(nk=self.nk, nb_dm=self.nb_dm, bstart=self.bstart, bend=self.bend, npair=self.npair,
+                 k1st=_ptr(self.k1st), k2nd=_ptr(self.k2nd), P1=_ptr(self.P1), P2=_ptr(self.P2), e_dm=_ptr(self.e_dm),
+                 prefac_eph=self.prefac_eph, Hcoh=_ptr(self.Hcoh), picture_schrodinger=self.picture_schrodinger,
+                 expt=self.expt, ddmdt_eq=None, scatt_enable=1)
+        return s
+
+    @property
+    def ny(self):
+        return 2 * self.nk * self.nb_dm * self.nb_dm
+
+
+def load(d: str) -> OracleSystem:
+    """Read param.in + ldbd_data/ in directory d and build the state DMD has after set-up."""
+    pm = parse_param_in(os.path.join(d, "param.in"))
+    sz = read_size(d)
+    nk, nbt = sz["nk"], sz["nb"]
+    nb_dm = sz["bEnd_dm"] - sz["bStart_dm"]
+    bstart, bend = sz["bStart_eph"] - sz["bStart_dm"], sz["bEnd_eph"] - sz["bStart_dm"]
+    nb = bend - bstart
+    T = sz["temperature"]
+    mu = pget(pm, "mu", sz["mu"] / eV, eV)
+    dd = os.path.join(d, "ldbd_data")
+    e = np.fromfile(os.path.join(dd, "ldbd_ek.bin"), dtype=np.float64).reshape(nk, nbt)
+    scissor = pget(pm, "scissor", 0.0, eV)
+    if scissor != 0:
+        e[:, sz["nv"]:] += scissor
+    f = fermi(T, mu, e)
+    e_dm = np.ascontiguousarray(e[:, sz["bStart_dm"]:sz["bEnd_dm"]])
+    f_dm = np.ascontiguousarray(f[:, sz["bStart_dm"]:sz["bEnd_dm"]])
+    smat = np.fromfile(os.path.join(dd, "ldbd_smat.bin"), dtype=np.complex128).reshape(nk, 3, nb_dm * nb_dm)
+    npair = sz["nkpair"]
+    k1 = np.fromfile(os.path.join(dd, "ldbd_kpair_k1st.bin"), dtype=np.uint64)
+    k2 = np.fromfile(os.path.join(dd, "ldbd_kpair_k2nd.bin"), dtype=np.uint64)
+    assert k1.size == npair and k2.size == npair, "ldbd_kpair size does not match nkpair"
+    nb4 = nb ** 4
+    P1 = np.fromfile(os.path.join(dd, "ldbd_P1_lindblad.bin"), dtype=np.complex128)
+    P2 = np.fromfile(os.path.join(dd, "ldbd_P2_lindblad.bin"), dtype=np.complex128)
+    assert P1.size == npair * nb4 and P2.size == npair * nb4, "ldbd_P size does not match"
+    scale_scatt = pget(pm, "scale_scatt", 1.0)
+    scale_eph = pget(pm, "scale_eph", scale_scatt)
+    if scale_eph != 1.0:
+        P1 = P1 * complex(scale_eph, 0)
+        P2 = P2 * complex(scale_eph, 0)
+    dim, R = read_R(d)
+    vol = abs(det3(R))
+    cell_size = vol if dim == 3 else (vol / R[2, 2] if dim == 2 else (R[2, 2] if dim == 1 else 1.0))
+    ni = pget(pm, "impurity_density", 0.0, bohr2cm ** dim)
+    if ni != 0:
+        fraction = abs(ni * cell_size)
+        Q1 = np.fromfile(os.path.join(dd, "ldbd_P1_lindblad_D1.bin"), dtype=np.complex128)
+        Q2 = np.fromfile(os.path.join(dd, "ldbd_P2_lindblad_D1.bin"), dtype=np.complex128)
+        P1 = P1 + Q1 * fraction
+        P2 = P2 + Q2 * fraction
+    picture = pm.get("alg_picture", "interaction")
+    schrod = 1 if picture in ("schrodinger", "non-interaction") else 0
+    expt = int(pget(pm, "alg_expt", 1.0))
+    t0 = pget(pm, "t0", 0.0, fs)
+    Bpert = np.array([pget(pm, "Bxpert", 0.0, Tesla2au), pget(pm, "Bypert", 0.0, Tesla2au), pget(pm, "Bzpert", 0.0, Tesla2au)])
+    B = np.array([pget(pm, "Bx", 0.0, Tesla2au), pget(pm, "By", 0.0, Tesla2au), pget(pm, "Bz", 0.0, Tesla2au)])
+    L = lib()
+    dmB = np.zeros((nk, nb_dm * nb_dm), np.complex128)
+    L.orc_dm_bpert(C.c_int(nk), C.c_int(nb_dm), C.c_void_p(smat.ctypes.data), C.c_void_p(e_dm.ctypes.data),
+                   C.c_void_p(f_dm.ctypes.data), C.c_double(T), C.c_void_p(Bpert.ctypes.data), C.c_double(t0),
+                   C.c_int(schrod), C.c_void_p(dmB.ctypes.data))
+    dm0 = np.zeros_like(dmB)
+    L.orc_init_dm(C.c_int(nk), C.c_int(nb_dm), C.c_void_p(dmB.ctypes.data), C.c_void_p(dm0.ctypes.data))
+    Hcoh = None
+    if math.sqrt(float((B * B).sum())) > 1e-10:
+        Hcoh = np.zeros((nk, nb_dm * nb_dm), np.complex128)
+        L.orc_H_BS(C.c_int(nk), C.c_int(nb_dm), C.c_void_p(smat.ctypes.data), C.c_void_p(B.ctypes.data),
+                   C.c_void_p(e_dm.ctypes.data), C.c_int(schrod), C.c_void_p(Hcoh.ctypes.data))
+    tstep = pget(pm, "tstep", 1.0, fs)
+    ode = dict(hstart=pget(pm, "ode_hstart", 1e-3, fs), hmin=pget(pm, "ode_hmin", 0.0, fs),
+               hmax=pget(pm, "ode_hmax", tstep / fs, fs), epsabs=pget(pm, "ode_epsabs", 1e-8))
+    cell_size_cmd = cell_size * bohr2cm ** dim
+    return OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
+                        k1st=k1, k2nd=k2, P1=np.ascontiguousarray(P1), P2=np.ascontiguousarray(P2),
+                        prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=Hcoh, smat=smat, dm0=dm0,
+                        picture_schrodinger=schrod, expt=expt, t0=t0, tstep=tstep, tend=pget(pm, "tend", 0.0, fs),
+                        temperature=T, mu=mu, nk_full=sz["nk_full"], ob_prefac=(1.0 / sz["nk_full"]) / cell_size_cmd,
+                        ode=ode, params=pm)
+
+
+def _setup_prototypes():
+    L = lib()
+    L.orc_dm_bpert.restype = None
+    L.orc_init_dm.restype = None
+    L.orc_H_BS.restype = None
+
+
+def y_of(dm: np.ndarray) -> np.ndarray:
+    """complex [nk][nb^2] -> interleaved double y (copy_real_from_complex, comm/ODE.h:10-15)."""
+    return np.ascontiguousarray(dm).view(np.float64).reshape(-1).copy()
+
+
+def rhs(s: OracleSystem, t: float, y: np.ndarray) -> np.ndarray:
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    out = np.zeros_like(y)
+    cs = s.cstruct()
+    lib().orc_rhs(C.addressof(cs), t, y.ctypes.data, out.ctypes.data)
+    return out
+
+
+def rhs_parts(s: OracleSystem, t: float, y: np.ndarray):
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    a = np.zeros_like(y)
+    b = np.zeros_like(y)
+    cs = s.cstruct()
+    lib().orc_rhs_parts(C.addressof(cs), t, y.ctypes.data, a.ctypes.data, b.ctypes.data)
+    return a, b
+
+
+def _meas(s: OracleSystem, idir: int):
+    obs = np.ascontiguousarray(s.smat[:, idir, :])
+    m = _Meas(obs=obs.ctypes.data, obs_kstride=s.nb_dm * s.nb_dm, f=s.f_dm.ctypes.data, prefac=s.ob_prefac,
+              bs=0, be=s.nb_dm)
+    return m, obs
+
+
+def measure(s: OracleSystem, y: np.ndarray, t: float, idir: int = 2):
+    m, obs = _meas(s, idir)
+    tot, amp = C.c_double(), C.c_double()
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    lib().orc_measure(s.nk, s.nb_dm, 0, s.nb_dm, obs.ctypes.data, s.nb_dm * s.nb_dm, s.f_dm.ctypes.data,
+                      s.e_dm.ctypes.data, t, s.picture_schrodinger, y.ctypes.data, s.ob_prefac, C.byref(tot), C.byref(amp))
+    return tot.value, amp.value
+
+
+def rk4(s: OracleSystem, t0: float, h: float, nsteps: int, y: np.ndarray, every: int = 0, idir: int = 2):
+    y = np.ascontiguousarray(y, dtype=np.float64).copy()
+    nrec = nsteps // every if every > 0 else 0
+    rec = np.zeros((max(nrec, 1), 3))
+    m, obs = _meas(s, idir)
+    cs = s.cstruct()
+    lib().orc_rk4(C.addressof(cs), t0, h, nsteps, y.ctypes.data, every, C.addressof(m), rec.ctypes.data)
+    return y, rec[:nrec]
+
+
+def rkf45(s: OracleSystem, y: np.ndarray, t0: float, tend: float, tstep: float, hstart: float, hmin: float,
+          hmax: float, epsabs: float, idir: int = 2):
+    y = np.ascontiguousarray(y, dtype=np.float64).copy()
+    nout = int(math.ceil((tend - t0) / tstep - 1e-9)) + 1
+    rec = np.zeros((nout, 3))
+    ncalls = np.zeros(nout, dtype=np.int64)
+    m, obs = _meas(s, idir)
+    cs = s.cstruct()
+    st = lib().orc_rkf45(C.addressof(cs), t0, tend, tstep, hstart, hmin, hmax, epsabs, y.ctypes.data, C.addressof(m),
+                         rec.ctypes.data, ncalls.ctypes.data, nout)
+    n = int(np.count_nonzero(rec[:, 0]))
+    return st, y, rec[:n], ncalls[:n]
+
+
+def euler(s: OracleSystem, t0: float, h: float, nsteps: int, y: np.ndarray):
+    y = np.ascontiguousarray(y, dtype=np.float64).copy()
+    cs = s.cstruct()
+    lib().orc_euler(C.addressof(cs), t0, h, nsteps, y.ctypes.data)
+    return y

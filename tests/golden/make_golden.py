@@ -1,0 +1,152 @@
+"""Generate the golden fixtures under tests/golden/<case>/ from the reference's own code.
+
+Run in a container that has the reference sources (it builds oracle/_ref/dmd_ref with
+oracle/Makefile.ref first):
+
+    python tests/golden/make_golden.py [--ref /root/reference/src_v4.5.7]
+
+For every case it writes a small synthetic DMD input (param.in + ldbd_data/ from the package's
+seeded generator) and runs the shim-built reference program on it:
+  * dump  -- setup arrays (initial density matrix, H_BS, occupations);
+  * rhs   -- func / evolve_driver / evolve_coh on three states;
+  * rk4   -- 40 classic RK4 steps through DMD's func, S_z every 5 steps;
+  * gsl   -- DMD's own evolve_gsl (RKF45) for 20 output intervals (S_z file + restart state).
+The outputs are stored in golden.npz next to the inputs. Nothing here runs at test time.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, make_ldbd  # noqa: E402
+
+FS = None
+
+CASES = {
+    # e-ph only, nb=2, S_z perturbation, interaction picture
+    "nb2_eph": dict(cfg=SynthConfig(nk=40, nb=2, seed=11, de_pair_mev=60.0), param=dict(Bpert_T=(0, 0, 0.1))),
+    # e-ph + e-imp (D1 files), B field along x -> coherent precession term
+    "nb2_eimp_B": dict(cfg=SynthConfig(nk=40, nb=2, seed=12, de_pair_mev=60.0, eimp_sigma_mev=5.0),
+                       param=dict(Bpert_T=(0, 0, 0.1), B_T=(2.0, 0, 0), eimp_fraction=0.05)),
+    # nb=4 (two spin pairs), e-imp, B field
+    "nb4_eimp_B": dict(cfg=SynthConfig(nk=16, nb=4, seed=13, de_pair_mev=60.0, eimp_sigma_mev=5.0),
+                       param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0.5, 0.3, 0), eimp_fraction=0.05)),
+    # Schrodinger picture without P(t) phases
+    "nb2_schrod": dict(cfg=SynthConfig(nk=30, nb=2, seed=14, de_pair_mev=60.0),
+                       param=dict(Bpert_T=(0, 0, 0.1), B_T=(0, 1.0, 0),
+                                  extra={"alg_picture": "schrodinger", "alg_expt": 0})),
+    # density matrix with 4 bands, e-ph window on the upper 2 (trunc_copy / set_mat path)
+    "nb2_window": dict(cfg=SynthConfig(nk=24, nb=2, seed=15, de_pair_mev=60.0, extra_bands=2),
+                       param=dict(Bpert_T=(0.1, 0, 0.05), B_T=(0, 0, 1.0))),
+}
+
+
+def run(ref_bin, d, *args):
+    shutil.rmtree(os.path.join(d, "restart"), ignore_errors=True)
+    for f in os.listdir(d):
+        if f.endswith(".out") and f != "ref.out":
+            os.remove(os.path.join(d, f))
+    p = subprocess.run([ref_bin] + list(args), cwd=d, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("reference run failed: %s\n%s" % (args, p.stdout[-3000:] + p.stderr[-3000:]))
+    return p.stdout
+
+
+def read_s_file(path):
+    rows = []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("#"):
+                continue
+            v = line.split()
+            if len(v) >= 3:
+                rows.append([float(v[0]), float(v[1]), float(v[2])])
+    return np.array(rows)
+
+
+def make_case(name, spec, ref_bin, outroot):
+    d = os.path.join(outroot, name)
+    shutil.rmtree(d, ignore_errors=True)
+    os.makedirs(d)
+    cfg = spec["cfg"]
+    info = make_ldbd(d, cfg, tstep_fs=1.0, tend_fs=20.0, **spec["param"])
+    tmp = os.path.join(d, "_run")
+    os.makedirs(tmp)
+    shutil.copytree(os.path.join(d, "ldbd_data"), os.path.join(tmp, "ldbd_data"))
+    shutil.copy(os.path.join(d, "param.in"), tmp)
+    out = {}
+    # dump
+    os.makedirs(os.path.join(tmp, "o"), exist_ok=True)
+    run(ref_bin, tmp, "dump", "o")
+    meta = {}
+    with open(os.path.join(tmp, "o", "meta.txt")) as f:
+        for line in f:
+            k, v = line.split()
+            meta[k] = float(v)
+    nk, nbdm = int(meta["nk"]), int(meta["nb_dm"])
+    out["meta_keys"] = np.array(list(meta.keys()))
+    out["meta_vals"] = np.array(list(meta.values()))
+    out["dm0"] = np.fromfile(os.path.join(tmp, "o", "dm0.bin"), dtype=np.complex128).reshape(nk, nbdm * nbdm)
+    out["e_dm"] = np.fromfile(os.path.join(tmp, "o", "e_dm.bin")).reshape(nk, nbdm)
+    out["f_dm"] = np.fromfile(os.path.join(tmp, "o", "f_dm.bin")).reshape(nk, nbdm)
+    if meta["has_H"]:
+        out["Hcoh"] = np.fromfile(os.path.join(tmp, "o", "Hcoh.bin"), dtype=np.complex128).reshape(nk, nbdm * nbdm)
+    # rhs on three Hermitian states
+    rng = np.random.default_rng([cfg.seed, 99])
+    fs = 1e-15 * float(np.sqrt((1.0 / 9.10938291e-31) * (1e10 / 0.5291772) ** 2 / (1.0 / 4.35974434e-18)))
+    ts = [0.0, 7.3 * fs, 123.4 * fs]
+    ys = []
+    for t in ts:
+        pert = (rng.standard_normal(out["dm0"].shape) + 1j * rng.standard_normal(out["dm0"].shape)) * 1e-3
+        dm = (out["dm0"] + pert).reshape(nk, nbdm, nbdm)
+        dm = 0.5 * (dm + np.conj(np.swapaxes(dm, 1, 2)))
+        ys.append(np.ascontiguousarray(dm.reshape(nk, -1)).view(np.float64).reshape(-1).copy())
+    with open(os.path.join(tmp, "rhs_in.bin"), "wb") as f:
+        for t, y in zip(ts, ys):
+            f.write(np.float64(t).tobytes())
+            f.write(y.tobytes())
+    run(ref_bin, tmp, "rhs", "rhs_in.bin", "o")
+    out["rhs_t"] = np.array(ts)
+    out["rhs_y"] = np.stack(ys)
+    out["rhs_dydt"] = np.fromfile(os.path.join(tmp, "o", "dydt.bin")).reshape(len(ts), -1)
+    out["rhs_eph"] = np.fromfile(os.path.join(tmp, "o", "ddmdt_eph.bin")).reshape(len(ts), -1)
+    out["rhs_coh"] = np.fromfile(os.path.join(tmp, "o", "ddmdt_coh.bin")).reshape(len(ts), -1)
+    # rk4: 40 steps of 1 fs, S_z every 5 steps
+    run(ref_bin, tmp, "rk4", "1.0", "40", "5", "o")
+    out["rk4_y"] = np.fromfile(os.path.join(tmp, "o", "y_final.bin"))
+    out["rk4_sz"] = read_s_file(os.path.join(tmp, "sz_elec_tot.out"))
+    # gsl: DMD's evolve_gsl to tend = 20 fs, output every tstep = 1 fs
+    log = run(ref_bin, tmp, "gsl")
+    out["gsl_sz"] = read_s_file(os.path.join(tmp, "sz_elec_tot.out"))
+    out["gsl_ncalls"] = np.array([int(m) for m in re.findall(r"ncalls= (\d+) at ti=", log)])
+    out["gsl_y"] = np.fromfile(os.path.join(tmp, "restart", "denmat_restart.bin"))
+    np.savez_compressed(os.path.join(d, "golden.npz"), **out)
+    shutil.rmtree(tmp)
+    return info
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference/src_v4.5.7")
+    ap.add_argument("--cases", nargs="*", default=list(CASES))
+    a = ap.parse_args()
+    subprocess.run(["make", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), "-j8", "REF=" + a.ref], check=True,
+                   cwd=ROOT, stdout=subprocess.DEVNULL)
+    ref_bin = os.path.join(ROOT, "oracle", "_ref", "dmd_ref")
+    outroot = os.path.dirname(os.path.abspath(__file__))
+    for name in a.cases:
+        info = make_case(name, CASES[name], ref_bin, outroot)
+        print(name, "nk=%d nb=%d npair=%d" % (info.nk, info.nb, info.npair))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,83 @@
+"""Pin the oracle: the CPU restatement against vectors produced by the reference's own sources.
+
+tests/golden/<case>/golden.npz was written by tests/golden/make_golden.py from the shim-built
+reference program (DMD src_v4.5.7 compiled unmodified). The restatement shares the reference
+build's BLAS definitions and C library, so set-up and right-hand side must agree bit for bit;
+the steppers must agree to rounding of the printed S(t) files.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, GOLDEN_CASES
+
+
+def _load(case, oracle):
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = oracle.load(d)
+    return d, g, s
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_setup_bitwise(case, oracle):
+    d, g, s = _load(case, oracle)
+    meta = dict(zip(g["meta_keys"], g["meta_vals"]))
+    assert s.nk == int(meta["nk"]) and s.nb_dm == int(meta["nb_dm"])
+    assert s.bstart == int(meta["bstart"]) and s.bend == int(meta["bend"])
+    assert s.npair == int(meta["nkpair"])
+    assert s.prefac_eph == meta["prefac_eph"]
+    np.testing.assert_array_equal(s.e_dm, g["e_dm"])
+    np.testing.assert_array_equal(s.f_dm, g["f_dm"])
+    np.testing.assert_array_equal(s.dm0, g["dm0"])
+    if "Hcoh" in g:
+        np.testing.assert_array_equal(s.Hcoh, g["Hcoh"])
+    else:
+        assert s.Hcoh is None
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_rhs_bitwise(case, oracle):
+    d, g, s = _load(case, oracle)
+    for i, t in enumerate(g["rhs_t"]):
+        y = g["rhs_y"][i]
+        np.testing.assert_array_equal(oracle.rhs(s, t, y), g["rhs_dydt"][i])
+        eph, coh = oracle.rhs_parts(s, t, y)
+        np.testing.assert_array_equal(eph, g["rhs_eph"][i])
+        np.testing.assert_array_equal(coh, g["rhs_coh"][i])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_rk4_trajectory(case, oracle):
+    d, g, s = _load(case, oracle)
+    y, rec = oracle.rk4(s, s.t0, 1.0 * oracle.fs, 40, oracle.y_of(s.dm0), every=5, idir=2)
+    np.testing.assert_array_equal(y, g["rk4_y"])
+    ref = g["rk4_sz"][1:]  # first row is report(0) at t0
+    assert rec.shape[0] == ref.shape[0]
+    # the S file is printed with %21.14le (15 significant digits)
+    np.testing.assert_allclose(rec[:, 0], ref[:, 0], rtol=2e-14)
+    np.testing.assert_allclose(rec[:, 1], ref[:, 1], rtol=2e-14, atol=1e-300)
+    np.testing.assert_allclose(rec[:, 2], ref[:, 2], rtol=2e-14, atol=1e-300)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_rkf45_gsl_driver(case, oracle):
+    d, g, s = _load(case, oracle)
+    st, y, rec, ncalls = oracle.rkf45(s, oracle.y_of(s.dm0), s.t0, s.tend, s.tstep, s.ode["hstart"], s.ode["hmin"],
+                                      s.ode["hmax"], s.ode["epsabs"])
+    assert st == 0
+    np.testing.assert_array_equal(y, g["gsl_y"])
+    ref = g["gsl_sz"][1:]
+    assert rec.shape[0] == ref.shape[0]
+    np.testing.assert_allclose(rec[:, 1], ref[:, 1], rtol=2e-14, atol=1e-300)
+    # the reference resets ncalls after its first compute() (report_tau at it = 1)
+    np.testing.assert_array_equal(ncalls, g["gsl_ncalls"])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_hermiticity_of_rhs(case, oracle):
+    """dρ/dt is exactly Hermitian: (c + c†)/2 in the finish (evolve_eph.cpp:149-151)."""
+    d, g, s = _load(case, oracle)
+    eph = g["rhs_eph"][0].view(np.complex128).reshape(s.nk, s.nb_dm, s.nb_dm)
+    np.testing.assert_array_equal(eph, np.conj(np.swapaxes(eph, 1, 2)))
