@@ -1,0 +1,686 @@
+// C ABI of the GB300 Lindblad RHS (see include/dmd_gpu.h): handle, device layout, steppers.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dmd_gpu.h"
+#include "dmd_kernels.cuh"
+#include "dmd_pairs.cuh"
+
+using namespace dmd;
+
+struct dmd_handle {
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  int nk = 0, nbdm = 0, bs = 0, be = 0, nb = 0, nb2 = 0, nb4 = 0;
+  long long npair = 0;
+  double prefac = 0;
+  int picture = 0, expt = 1, prec = 0;
+  size_t nstate = 0;  // complex elements of the state (nk * nbdm^2)
+  // device arrays
+  double* d_ew = nullptr;      // [nk][nb]
+  double* d_edm = nullptr;     // [nk][nbdm]
+  int2* d_kk = nullptr;        // [npair]
+  double2* d_P = nullptr;      // [npair][2][nb4]
+  double2* d_H = nullptr;      // [nk][nbdm^2]
+  double2* d_eq = nullptr;     // [nk][nb2]
+  double2* d_rs = nullptr;     // [nk][2][nb2]
+  double2* d_acc = nullptr;    // [nk][2][nb2]
+  double2* d_y = nullptr;      // state
+  double2* d_ytmp = nullptr;
+  double2* d_y0 = nullptr;     // RKF45 retry copy
+  double2* d_in = nullptr;     // host-call staging
+  double2* d_in1 = nullptr;
+  double2* d_out = nullptr;
+  double2* d_K = nullptr;      // [6][nstate]
+  double* d_tref = nullptr;    // [t0, h]
+  long long* d_step = nullptr;
+  double* d_red = nullptr;     // reduction partials
+  int* d_coef_i = nullptr;     // RKF45 coefficient tables
+  double* d_coef = nullptr;
+  int* d_flag = nullptr;
+  double2* d_obs[8] = {nullptr};
+  double* d_f[8] = {nullptr};
+  double obs_prefac[8] = {0};
+  double t = 0;                // time of the device state
+  long long launches = 0;
+  cudaGraphExec_t g_rk4 = nullptr;
+  std::string err;
+};
+
+namespace {
+
+const char* kStatus[] = {"ok", "invalid argument", "out of memory", "file error", "CUDA error", "device wait timed out",
+                         "non-finite state", "wrong call order", "no CUDA device", "ODE step failure"};
+
+int fail(dmd_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return fail(h, e_ == cudaErrorMemoryAllocation ? DMD_E_NOMEM : DMD_E_CUDA,                   \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                             \
+  } while (0)
+
+#define CKL()                                                                                      \
+  do {                                                                                             \
+    cudaError_t e_ = cudaGetLastError();                                                           \
+    if (e_ != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+int dalloc(dmd_handle* h, T** p, size_t n) {
+  CK(cudaMalloc((void**)p, (n ? n : 1) * sizeof(T)));
+  return DMD_OK;
+}
+
+inline unsigned blocks_for(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
+
+// ---------------------------------------------------------------------------------------------
+// one RHS evaluation on device buffers: prep -> pairs -> finish
+// ---------------------------------------------------------------------------------------------
+template <int NB>
+int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
+  const int n = h->nk * NB * NB;
+  k_prep<NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->expt, h->d_rs, h->d_acc);
+  h->launches++;
+  CKL();
+  return DMD_OK;
+}
+
+template <int NB>
+int launch_pairs(dmd_handle* h) {
+  if (h->npair == 0) return DMD_OK;
+  const long long nthr = h->npair * 4LL * NB * NB;
+  k_pairs_f64_atomic<NB><<<blocks_for(nthr, 256), 256, 0, h->st>>>(h->npair, h->d_kk, h->d_P, h->d_rs, h->d_acc);
+  h->launches++;
+  CKL();
+  return DMD_OK;
+}
+
+template <int NB>
+int launch_finish(dmd_handle* h, FinishArgs a) {
+  k_finish<NB><<<blocks_for(h->nk, 128), 128, 0, h->st>>>(a);
+  h->launches++;
+  CKL();
+  return DMD_OK;
+}
+
+FinishArgs base_finish(dmd_handle* h, const double2* y) {
+  FinishArgs a;
+  memset(&a, 0, sizeof(a));
+  a.nk = h->nk;
+  a.nbdm = h->nbdm;
+  a.bs = h->bs;
+  a.prefac = h->prefac;
+  a.picture = h->picture;
+  a.phase = h->expt;
+  a.ew = h->d_ew;
+  a.edm = h->d_edm;
+  a.H = h->d_H;
+  a.eq = h->d_eq;
+  a.y = y;
+  a.acc = h->d_acc;
+  a.want_eph = 1;
+  a.want_coh = (h->picture == DMD_PICTURE_SCHRODINGER || h->d_H) ? 1 : 0;
+  return a;
+}
+
+template <int NB>
+int rhs_impl(dmd_handle* h, const double2* y, const TimeArg& ta, FinishArgs fa) {
+  int s;
+  if (fa.want_eph) {
+    if ((s = launch_prep<NB>(h, y, ta))) return s;
+    if ((s = launch_pairs<NB>(h))) return s;
+  }
+  fa.ta = ta;
+  return launch_finish<NB>(h, fa);
+}
+
+int rhs(dmd_handle* h, const double2* y, const TimeArg& ta, FinishArgs fa) {
+  switch (h->nb) {
+    case 1: return rhs_impl<1>(h, y, ta, fa);
+    case 2: return rhs_impl<2>(h, y, ta, fa);
+    case 3: return rhs_impl<3>(h, y, ta, fa);
+    case 4: return rhs_impl<4>(h, y, ta, fa);
+  }
+  return fail(h, DMD_E_ARG, "nb out of range");
+}
+
+TimeArg time_value(double t) {
+  TimeArg ta;
+  ta.t = t;
+  ta.tref = nullptr;
+  ta.step = nullptr;
+  ta.stage = 0;
+  return ta;
+}
+
+// plain RHS f(t, in) -> out on device buffers
+int rhs_plain(dmd_handle* h, double t, const double2* in, double2* out) {
+  FinishArgs fa = base_finish(h, in);
+  fa.mode = 0;
+  fa.out = out;
+  return rhs(h, in, time_value(t), fa);
+}
+
+int upload_pairs(dmd_handle* h, const dmd_desc* d) {
+  const size_t nb4 = (size_t)h->nb4;
+  const size_t chunk = (size_t)1 << 16;  // pairs per staging chunk
+  double2* stage = nullptr;
+  CK(cudaMallocHost((void**)&stage, chunk * 2 * nb4 * sizeof(double2)));
+  int2* kst = nullptr;
+  cudaError_t e = cudaMallocHost((void**)&kst, chunk * sizeof(int2));
+  if (e != cudaSuccess) { cudaFreeHost(stage); return fail(h, DMD_E_NOMEM, "pinned staging"); }
+  int rc = DMD_OK;
+  for (long long p0 = 0; p0 < h->npair && rc == DMD_OK; p0 += (long long)chunk) {
+    const size_t n = (size_t)std::min<long long>((long long)chunk, h->npair - p0);
+    for (size_t q = 0; q < n; ++q) {
+      const uint64_t k1 = d->k1st[p0 + q], k2 = d->k2nd[p0 + q];
+      if (k1 >= (uint64_t)h->nk || k2 >= (uint64_t)h->nk) { rc = fail(h, DMD_E_ARG, "k-pair index out of range"); break; }
+      kst[q] = make_int2((int)k1, (int)k2);
+      const double* s1 = d->P1 + 2 * (p0 + q) * nb4;
+      const double* s2 = d->P2 + 2 * (p0 + q) * nb4;
+      double2* o = stage + q * 2 * nb4;
+      for (size_t j = 0; j < nb4; ++j) {
+        double2 v1 = make_double2(s1[2 * j], s1[2 * j + 1]);
+        double2 v2 = make_double2(s2[2 * j], s2[2 * j + 1]);
+        if (d->P1_add) {  // P += P_add * scale (ElectronImpurity.cpp:38-39, ElectronPhonon.cpp:96-97)
+          const double* a1 = d->P1_add + 2 * (p0 + q) * nb4;
+          const double* a2 = d->P2_add + 2 * (p0 + q) * nb4;
+          v1.x = v1.x + a1[2 * j] * d->add_scale;
+          v1.y = v1.y + a1[2 * j + 1] * d->add_scale;
+          v2.x = v2.x + a2[2 * j] * d->add_scale;
+          v2.y = v2.y + a2[2 * j + 1] * d->add_scale;
+        }
+        o[j] = v1;
+        o[nb4 + j] = v2;
+      }
+    }
+    if (rc) break;
+    e = cudaMemcpy(h->d_P + (size_t)p0 * 2 * nb4, stage, n * 2 * nb4 * sizeof(double2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_kk + p0, kst, n * sizeof(int2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = fail(h, DMD_E_CUDA, std::string("P upload: ") + cudaGetErrorString(e));
+  }
+  cudaFreeHost(stage);
+  cudaFreeHost(kst);
+  return rc;
+}
+
+void release(dmd_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->dev);
+  if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
+  void* ptrs[] = {h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
+                  h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
+                  h->d_coef, h->d_flag};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (int i = 0; i < 8; ++i) {
+    if (h->d_obs[i]) cudaFree(h->d_obs[i]);
+    if (h->d_f[i]) cudaFree(h->d_f[i]);
+  }
+  if (h->st) cudaStreamDestroy(h->st);
+}
+
+int check_state(dmd_handle* h) {
+  const size_t n = 2 * h->nstate;
+  CK(cudaMemsetAsync(h->d_flag, 0, sizeof(int), h->st));
+  k_nan_scan<<<blocks_for((long long)n, 256), 256, 0, h->st>>>(n, (const double*)h->d_y, h->d_flag);
+  h->launches++;
+  CKL();
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (flag) return fail(h, DMD_E_NAN, "non-finite value in the density matrix");
+  return DMD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dmd_strerror(int s) {
+  if (s < 0 || s > 9) return "unknown status";
+  return kStatus[s];
+}
+
+const char* dmd_last_error(const dmd_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int dmd_create(const dmd_desc* d, dmd_handle** out) {
+  if (!out) return DMD_E_ARG;
+  *out = nullptr;
+  if (!d) return DMD_E_ARG;
+  if (d->nk <= 0 || d->nb_dm <= 0 || d->nb_dm > DMD_MAX_NBDM || d->bstart < 0 || d->bend > d->nb_dm ||
+      d->bend - d->bstart < 1 || d->bend - d->bstart > 4 || d->nkpair < 0 || !d->e_dm)
+    return DMD_E_ARG;
+  if (d->nkpair > 0 && (!d->k1st || !d->k2nd || !d->P1 || !d->P2)) return DMD_E_ARG;
+  if ((d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
+  if (d->precision != DMD_PREC_F64) return DMD_E_ARG;
+  if (d->picture != DMD_PICTURE_INTERACTION && d->picture != DMD_PICTURE_SCHRODINGER) return DMD_E_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DMD_E_NODEV;
+  if (d->device < 0 || d->device >= ndev) return DMD_E_ARG;
+  dmd_handle* h = new dmd_handle();
+  h->dev = d->device;
+  h->nk = d->nk;
+  h->nbdm = d->nb_dm;
+  h->bs = d->bstart;
+  h->be = d->bend;
+  h->nb = d->bend - d->bstart;
+  h->nb2 = h->nb * h->nb;
+  h->nb4 = h->nb2 * h->nb2;
+  h->npair = d->nkpair;
+  h->prefac = d->prefac_eph;
+  h->picture = d->picture;
+  h->expt = d->expt ? 1 : 0;
+  h->prec = d->precision;
+  h->nstate = (size_t)h->nk * h->nbdm * h->nbdm;
+  int rc = DMD_OK;
+  auto bail = [&](int code) {
+    std::string m = h->err;
+    release(h);
+    delete h;
+    fprintf(stderr, "dmd_create: %s\n", m.c_str());
+    return code;
+  };
+  if (cudaSetDevice(h->dev) != cudaSuccess) return bail(DMD_E_CUDA);
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return bail(DMD_E_CUDA);
+  const size_t nk = h->nk, nbdm = h->nbdm;
+  if ((rc = dalloc(h, &h->d_ew, nk * h->nb)) || (rc = dalloc(h, &h->d_edm, nk * nbdm)) ||
+      (rc = dalloc(h, &h->d_kk, (size_t)h->npair)) || (rc = dalloc(h, &h->d_P, (size_t)h->npair * 2 * h->nb4)) ||
+      (rc = dalloc(h, &h->d_rs, nk * 2 * h->nb2)) || (rc = dalloc(h, &h->d_acc, nk * 2 * h->nb2)) ||
+      (rc = dalloc(h, &h->d_y, h->nstate)) || (rc = dalloc(h, &h->d_ytmp, h->nstate)) ||
+      (rc = dalloc(h, &h->d_y0, h->nstate)) || (rc = dalloc(h, &h->d_in, h->nstate)) ||
+      (rc = dalloc(h, &h->d_in1, h->nstate)) || (rc = dalloc(h, &h->d_out, h->nstate)) ||
+      (rc = dalloc(h, &h->d_K, 6 * h->nstate)) || (rc = dalloc(h, &h->d_tref, 2)) ||
+      (rc = dalloc(h, &h->d_step, 1)) || (rc = dalloc(h, &h->d_red, 4096)) || (rc = dalloc(h, &h->d_coef_i, 64)) ||
+      (rc = dalloc(h, &h->d_coef, 64)) || (rc = dalloc(h, &h->d_flag, 1)))
+    return bail(rc);
+  std::vector<double> ew(nk * h->nb);
+  for (size_t k = 0; k < nk; ++k)
+    for (int b = 0; b < h->nb; ++b) ew[k * h->nb + b] = d->e_dm[k * nbdm + h->bs + b];
+  if (cudaMemcpy(h->d_ew, ew.data(), ew.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(h->d_edm, d->e_dm, nk * nbdm * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(h, DMD_E_CUDA, "upload energies"));
+  if (d->Hcoh) {
+    if ((rc = dalloc(h, &h->d_H, h->nstate))) return bail(rc);
+    if (cudaMemcpy(h->d_H, d->Hcoh, h->nstate * 16, cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(fail(h, DMD_E_CUDA, "upload H"));
+  }
+  if ((rc = upload_pairs(h, d))) return bail(rc);
+  if (cudaMemset(h->d_y, 0, h->nstate * 16) != cudaSuccess || cudaMemset(h->d_step, 0, 8) != cudaSuccess)
+    return bail(fail(h, DMD_E_CUDA, "init"));
+  *out = h;
+  return DMD_OK;
+}
+
+int dmd_destroy(dmd_handle* h) {
+  if (!h) return DMD_E_ARG;
+  release(h);
+  delete h;
+  return DMD_OK;
+}
+
+int dmd_set_ddmdt_eq(dmd_handle* h, const double* eq) {
+  if (!h) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  if (!eq) {
+    if (h->d_eq) cudaFree(h->d_eq);
+    h->d_eq = nullptr;
+    return DMD_OK;
+  }
+  if (!h->d_eq) {
+    int rc = dalloc(h, &h->d_eq, (size_t)h->nk * h->nb2);
+    if (rc) return rc;
+  }
+  CK(cudaMemcpy(h->d_eq, eq, (size_t)h->nk * h->nb2 * 16, cudaMemcpyHostToDevice));
+  return DMD_OK;
+}
+
+int dmd_func(dmd_handle* h, double t, const double* y, double* dydt) {
+  if (!h || !y || !dydt) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaMemcpyAsync(h->d_in, y, h->nstate * 16, cudaMemcpyHostToDevice, h->st));
+  int rc = rhs_plain(h, t, h->d_in, h->d_out);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(dydt, h->d_out, h->nstate * 16, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return DMD_OK;
+}
+
+int dmd_evolve_driver(dmd_handle* h, double t, const double* dm, const double* dm1, double* ddmdt) {
+  if (!h || !dm || !ddmdt) return DMD_E_ARG;
+  (void)dm1;  // the kernels form 1 - dm themselves (set_oneminusdm, DenMat.cpp:249-261)
+  CK(cudaSetDevice(h->dev));
+  CK(cudaMemcpyAsync(h->d_in, dm, h->nstate * 16, cudaMemcpyHostToDevice, h->st));
+  FinishArgs fa = base_finish(h, h->d_in);
+  fa.want_coh = 0;
+  fa.mode = 0;
+  fa.out = h->d_out;
+  int rc = rhs(h, h->d_in, time_value(t), fa);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(ddmdt, h->d_out, h->nstate * 16, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return DMD_OK;
+}
+
+int dmd_evolve_coh(dmd_handle* h, double t, const double* dm, double* out) {
+  if (!h || !dm || !out) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaMemcpyAsync(h->d_in, dm, h->nstate * 16, cudaMemcpyHostToDevice, h->st));
+  FinishArgs fa = base_finish(h, h->d_in);
+  fa.want_eph = 0;
+  fa.want_coh = 1;
+  fa.mode = 0;
+  fa.out = h->d_out;
+  int rc = rhs(h, h->d_in, time_value(t), fa);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out, h->d_out, h->nstate * 16, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return DMD_OK;
+}
+
+int dmd_set_state(dmd_handle* h, double t, const double* y) {
+  if (!h || !y) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaMemcpyAsync(h->d_y, y, h->nstate * 16, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->t = t;
+  return DMD_OK;
+}
+
+int dmd_get_state(dmd_handle* h, double* t, double* y) {
+  if (!h) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  if (y) CK(cudaMemcpyAsync(y, h->d_y, h->nstate * 16, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (t) *t = h->t;
+  return DMD_OK;
+}
+
+static int rk4_step_launches(dmd_handle* h) {
+  for (int s = 0; s < 4; ++s) {
+    TimeArg ta;
+    ta.t = 0;
+    ta.tref = h->d_tref;
+    ta.step = h->d_step;
+    ta.stage = s;
+    const double2* in = (s == 0) ? h->d_y : h->d_ytmp;
+    FinishArgs fa = base_finish(h, in);
+    fa.mode = 1;
+    fa.stage = s;
+    fa.tref = h->d_tref;
+    fa.step = h->d_step;
+    fa.K = h->d_K;
+    fa.ybase = h->d_y;
+    fa.ytmp = h->d_ytmp;
+    int rc = rhs(h, in, ta, fa);
+    if (rc) return rc;
+  }
+  k_step_inc<<<1, 32, 0, h->st>>>(h->d_step);
+  h->launches++;
+  CKL();
+  return DMD_OK;
+}
+
+int dmd_rk4(dmd_handle* h, double dt, int64_t nsteps) {
+  if (!h || nsteps < 0 || !(dt == dt)) return DMD_E_ARG;
+  if (nsteps == 0) return DMD_OK;
+  CK(cudaSetDevice(h->dev));
+  const double tref[2] = {h->t, dt};
+  const long long zero = 0;
+  CK(cudaMemcpyAsync(h->d_tref, tref, 16, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->d_step, &zero, 8, cudaMemcpyHostToDevice, h->st));
+  // pageable sources: wait so the host values stay valid
+  CK(cudaStreamSynchronize(h->st));
+  if (!h->g_rk4) {
+    cudaGraph_t g;
+    const long long l0 = h->launches;
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    int rc = rk4_step_launches(h);
+    cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->g_rk4, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    h->launches = l0;  // captured launches are counted when the graph runs
+  }
+  const long long per_step = (h->npair ? 13 : 9);
+  for (int64_t s = 0; s < nsteps; ++s) {
+    CK(cudaGraphLaunch(h->g_rk4, h->st));
+    h->launches += per_step;
+  }
+  h->t = h->t + (double)nsteps * dt;  // = t0 + n*h as the stage times see it
+  CK(cudaStreamSynchronize(h->st));
+  return check_state(h);
+}
+
+int dmd_euler(dmd_handle* h, double dt, int64_t nsteps) {
+  if (!h || nsteps < 0) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  for (int64_t s = 0; s < nsteps; ++s) {
+    const double tref[2] = {h->t, dt};
+    CK(cudaMemcpyAsync(h->d_tref, tref, 16, cudaMemcpyHostToDevice, h->st));
+    FinishArgs fa = base_finish(h, h->d_y);
+    fa.mode = 2;
+    fa.tref = h->d_tref;
+    fa.ybase = h->d_y;
+    int rc = rhs(h, h->d_y, time_value(h->t), fa);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->st));
+    h->t += dt;  // sdmk->t += dt_current() (DensityMatrix_Dynamics.h:232)
+  }
+  return check_state(h);
+}
+
+// ---------------------------------------------------------------------------------------------
+// RKF45: gsl_odeiv2_driver_apply restated over device-resident state (see oracle/gsl_rkf45.c for
+// the CPU statement of the same algorithm)
+// ---------------------------------------------------------------------------------------------
+namespace {
+const double kAh[] = {1.0 / 4.0, 3.0 / 8.0, 12.0 / 13.0, 1.0, 1.0 / 2.0};
+const double kB3[] = {3.0 / 32.0, 9.0 / 32.0};
+const double kB4[] = {1932.0 / 2197.0, -7200.0 / 2197.0, 7296.0 / 2197.0};
+const double kB5[] = {8341.0 / 4104.0, -32832.0 / 4104.0, 29440.0 / 4104.0, -845.0 / 4104.0};
+const double kB6[] = {-6080.0 / 20520.0, 41040.0 / 20520.0, -28352.0 / 20520.0, 9295.0 / 20520.0, -5643.0 / 20520.0};
+const double kC[] = {902880.0 / 7618050.0, 3953664.0 / 7618050.0, 3855735.0 / 7618050.0, -1371249.0 / 7618050.0,
+                     277020.0 / 7618050.0};
+const double kE[] = {1.0 / 360.0, -128.0 / 4275.0, -2197.0 / 75240.0, 1.0 / 50.0, 2.0 / 55.0};
+
+struct Rkf {
+  dmd_handle* h;
+  int64_t nfev = 0;
+  double* K(int j) { return (double*)(h->d_K + (size_t)j * h->nstate); }
+};
+
+int comb(dmd_handle* h, const double* base, int nterms, const int* kidx, const double* coef, double hs, int premul,
+         double* out) {
+  // coefficients by value through a small device table (copied from pageable host memory)
+  int ibuf[8];
+  double cbuf[8];
+  for (int i = 0; i < nterms; ++i) {
+    ibuf[i] = kidx[i];
+    cbuf[i] = coef[i];
+  }
+  CK(cudaMemcpyAsync(h->d_coef_i, ibuf, sizeof(int) * nterms, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->d_coef, cbuf, sizeof(double) * nterms, cudaMemcpyHostToDevice, h->st));
+  const size_t n = 2 * h->nstate;
+  k_rk_comb<<<blocks_for((long long)n, 256), 256, 0, h->st>>>(n, base, (const double*)h->d_K, 2 * h->nstate, nterms,
+                                                              h->d_coef_i, h->d_coef, hs, premul, out);
+  h->launches++;
+  CKL();
+  CK(cudaStreamSynchronize(h->st));  // the small tables are reused by the next call
+  return DMD_OK;
+}
+
+int feval(Rkf& r, double t, const double* y, double* out) {
+  r.nfev++;
+  return rhs_plain(r.h, t, (const double2*)y, (double2*)out);
+}
+
+int rkf45_step(Rkf& r, double t, double hs, double* y, double* rmax, double eps_abs, double eps_rel) {
+  dmd_handle* h = r.h;
+  double* yt = (double*)h->d_ytmp;
+  int rc;
+  const int i1[] = {0};
+  if ((rc = comb(h, y, 1, i1, &kAh[0], hs, 1, yt))) return rc;
+  if ((rc = feval(r, t + kAh[0] * hs, yt, r.K(1)))) return rc;
+  const int i2[] = {0, 1};
+  if ((rc = comb(h, y, 2, i2, kB3, hs, 0, yt))) return rc;
+  if ((rc = feval(r, t + kAh[1] * hs, yt, r.K(2)))) return rc;
+  const int i3[] = {0, 1, 2};
+  if ((rc = comb(h, y, 3, i3, kB4, hs, 0, yt))) return rc;
+  if ((rc = feval(r, t + kAh[2] * hs, yt, r.K(3)))) return rc;
+  const int i4[] = {0, 1, 2, 3};
+  if ((rc = comb(h, y, 4, i4, kB5, hs, 0, yt))) return rc;
+  if ((rc = feval(r, t + kAh[3] * hs, yt, r.K(4)))) return rc;
+  const int i5[] = {0, 1, 2, 3, 4};
+  if ((rc = comb(h, y, 5, i5, kB6, hs, 0, yt))) return rc;
+  if ((rc = feval(r, t + kAh[4] * hs, yt, r.K(5)))) return rc;
+  const int i6[] = {0, 2, 3, 4, 5};
+  if ((rc = comb(h, y, 5, i6, kC, hs, 0, y))) return rc;
+  // error estimate and control ratio on the updated y
+  int ebuf[5] = {0, 2, 3, 4, 5};
+  CK(cudaMemcpyAsync(h->d_coef_i, ebuf, sizeof(ebuf), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->d_coef, kE, sizeof(kE), cudaMemcpyHostToDevice, h->st));
+  const size_t n = 2 * h->nstate;
+  const unsigned nbk = blocks_for((long long)n, 256);
+  if (nbk > 4096) return fail(h, DMD_E_ARG, "state too large for the error reduction");
+  k_rk_err<<<nbk, 256, 0, h->st>>>(n, y, (const double*)h->d_K, 2 * h->nstate, 5, h->d_coef_i, h->d_coef, hs, eps_abs,
+                                   eps_rel, h->d_red);
+  h->launches++;
+  CKL();
+  std::vector<double> bm(nbk);
+  CK(cudaMemcpyAsync(bm.data(), h->d_red, nbk * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  double m = 2.2250738585072014e-308;
+  for (double v : bm) m = v > m ? v : m;
+  *rmax = m;
+  return DMD_OK;
+}
+
+}  // namespace
+
+int dmd_rkf45_apply(dmd_handle* h, double t1, double* hstep, double hmin, double hmax, double epsabs, double epsrel,
+                    int64_t* nfev) {
+  if (!h || !hstep) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  Rkf r;
+  r.h = h;
+  double* y = (double*)h->d_y;
+  double* y0 = (double*)h->d_y0;
+  const size_t bytes = h->nstate * 16;
+  const int sign = (*hstep > 0.0) ? 1 : -1;
+  if (sign * (t1 - h->t) < 0.0) return fail(h, DMD_E_ODE, "integration limits and step direction disagree");
+  int rc;
+  while (sign * (t1 - h->t) > 0.0) {
+    // gsl_odeiv2_evolve_apply
+    const double t0 = h->t;
+    double h0 = *hstep;
+    const double dt = t1 - t0;
+    if ((dt < 0.0 && h0 > 0.0) || (dt > 0.0 && h0 < 0.0)) return fail(h, DMD_E_ODE, "step direction");
+    CK(cudaMemcpyAsync(y0, y, bytes, cudaMemcpyDeviceToDevice, h->st));
+    if ((rc = feval(r, t0, y, r.K(0)))) return rc;  // dydt_in
+    for (;;) {
+      int final_step = 0;
+      if ((dt >= 0.0 && h0 > dt) || (dt < 0.0 && h0 < dt)) {
+        h0 = dt;
+        final_step = 1;
+      }
+      double rmax;
+      if ((rc = rkf45_step(r, t0, h0, y, &rmax, epsabs, epsrel))) return rc;
+      h->t = final_step ? t1 : t0 + h0;
+      const double h_old = h0;
+      // standard control, order 5
+      int dec = 0;
+      if (rmax > 1.1) {
+        double q = 0.9 / pow(rmax, 1.0 / 5.0);
+        if (q < 0.2) q = 0.2;
+        h0 = q * h_old;
+        dec = 1;
+      } else if (rmax < 0.5) {
+        double q = 0.9 / pow(rmax, 1.0 / 6.0);
+        if (q > 5.0) q = 5.0;
+        if (q < 1.0) q = 1.0;
+        h0 = q * h_old;
+      }
+      if (dec) {
+        volatile double t_curr = h->t, t_next = h->t + h0;
+        if (fabs(h0) < fabs(h_old) && t_next != t_curr) {
+          CK(cudaMemcpyAsync(y, y0, bytes, cudaMemcpyDeviceToDevice, h->st));
+          h->t = t0;
+          continue;  // retry with the smaller step (dydt_in reused)
+        }
+        h0 = h_old;
+      }
+      break;
+    }
+    *hstep = h0;
+    if (fabs(*hstep) > hmax) *hstep = sign * hmax;
+    if (fabs(*hstep) < hmin) {
+      if (nfev) *nfev = r.nfev;
+      return fail(h, DMD_E_ODE, "step size below hmin (GSL_ENOPROG)");
+    }
+  }
+  if (nfev) *nfev = r.nfev;
+  return check_state(h);
+}
+
+int dmd_set_observable(dmd_handle* h, int slot, const double* obs, const double* f, double prefac) {
+  if (!h || slot < 0 || slot >= 8 || !obs || !f) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  int rc;
+  if (!h->d_obs[slot] && (rc = dalloc(h, &h->d_obs[slot], h->nstate))) return rc;
+  if (!h->d_f[slot] && (rc = dalloc(h, &h->d_f[slot], (size_t)h->nk * h->nbdm))) return rc;
+  CK(cudaMemcpy(h->d_obs[slot], obs, h->nstate * 16, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_f[slot], f, (size_t)h->nk * h->nbdm * 8, cudaMemcpyHostToDevice));
+  h->obs_prefac[slot] = prefac;
+  return DMD_OK;
+}
+
+int dmd_measure(dmd_handle* h, int slot, int bstart, int bend, double* tot, double* tot_amp) {
+  if (!h || slot < 0 || slot >= 8 || !h->d_obs[slot] || bstart < 0 || bend > h->nbdm || bstart > bend) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  const unsigned nbk = blocks_for(h->nk, 256);
+  if (2 * nbk > 4096) return fail(h, DMD_E_ARG, "nk too large for the observable reduction");
+  k_measure<<<nbk, 256, 0, h->st>>>(h->nk, h->nbdm, bstart, bend, h->d_obs[slot], h->d_f[slot], h->d_edm, h->t,
+                                    h->picture, h->d_y, h->d_red);
+  h->launches++;
+  CKL();
+  std::vector<double> part(2 * nbk);
+  CK(cudaMemcpyAsync(part.data(), h->d_red, 2 * nbk * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  double s1 = 0, s2 = 0;
+  for (unsigned b = 0; b < nbk; ++b) {
+    s1 += part[2 * b];
+    s2 += part[2 * b + 1];
+  }
+  if (tot) *tot = s1 * h->obs_prefac[slot];
+  if (tot_amp) *tot_amp = s2 * h->obs_prefac[slot];
+  return DMD_OK;
+}
+
+int dmd_launch_count(const dmd_handle* h, int64_t* n) {
+  if (!h || !n) return DMD_E_ARG;
+  *n = h->launches;
+  return DMD_OK;
+}
+
+int dmd_sync(dmd_handle* h) {
+  if (!h) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaStreamSynchronize(h->st));
+  return DMD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,304 @@
+// Per-evaluation kernels of the Lindblad right-hand side: phase/prep, finish (+coherent term and
+// stepper fusion), observables and stepper combinations. The k-pair contraction kernels live in
+// dmd_pairs.cuh.
+//
+// Algebra (exact rewrite of evolve_eph.cpp:34-166). With D_k[(i,j)] = exp(i t (e_k,i - e_k,j)) the
+// reference's P(t) phase factorises: P1(t)[a][b] = P1[a][b] D_k[a] conj(D_k'[b]) and
+// P2(t)[a][b] = P2[a][b] D_k[b] conj(D_k'[a]). Hence, with rt_k = conj(D_k) o rho_k and
+// st_k = conj(D_k) o (1 - rho_k),
+//   Pdm_k  = D_k o X_k,  X_k  = sum_pairs P1 rt_k'        + [k' side] conj(P2) rt_k
+//   dm1P_k = D_k o Y_k,  Y_k  = sum_pairs st_k'^T P2      + [k' side] st_k^T conj(P1)
+// and the pair loop needs no trigonometry. The finish applies D_k, forms
+// c = (1-rho_k) Pdm_k - dm1P_k rho_k with Hermitian operands read from their upper triangles
+// (zhemm, comm/mymatrix.cpp:73-76) and returns (prefac/2) (c + c^dagger) (evolve_eph.cpp:140-152).
+#pragma once
+#include "dmd_common.cuh"
+
+namespace dmd {
+
+// time of an evaluation: either a plain value or derived on the device from a step counter so that
+// captured graphs need no parameter updates. stage: 0 -> t, 1/2 -> t + h/2, 3 -> t + h.
+struct TimeArg {
+  double t;               // used when tref == nullptr
+  const double* tref;     // [t0, h]
+  const long long* step;  // completed steps since t0
+  int stage;
+};
+
+__device__ __forceinline__ double eval_time(const TimeArg& ta) {
+  if (!ta.tref) return ta.t;
+  const double t0 = ta.tref[0], h = ta.tref[1];
+  const double t = t0 + (double)(*ta.step) * h;
+  if (ta.stage == 0) return t;
+  if (ta.stage == 3) return t + h;
+  return t + 0.5 * h;
+}
+
+// rt_k, st_k (window, phase removed) and zeroed X/Y accumulators. One thread per (k, element).
+template <int NB>
+__global__ void k_prep(int nk, int nbdm, int bs, const double2* __restrict__ y, const double* __restrict__ ew,
+                       TimeArg ta, int phase, double2* __restrict__ rs, double2* __restrict__ acc) {
+  constexpr int NB2 = NB * NB;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nk * NB2) return;
+  const int k = idx / NB2, ab = idx - k * NB2, i = ab / NB, j = ab - i * NB;
+  const double2 r = y[(size_t)k * nbdm * nbdm + (bs + i) * nbdm + bs + j];
+  // set_oneminusdm (DenMat.cpp:249-261): 1 - dm on the diagonal, -dm elsewhere
+  const double2 s = (i == j) ? mk2(1.0 - r.x, 0.0 - r.y) : mk2(-r.x, -r.y);
+  double2 rt = r, st = s;
+  if (phase) {
+    const double t = eval_time(ta);
+    const double2 d = ccis((ew[k * NB + i] - ew[k * NB + j]) * t);
+    rt = cmul_rn(cconj(d), r);
+    st = cmul_rn(cconj(d), s);
+  }
+  rs[(size_t)k * 2 * NB2 + ab] = rt;
+  rs[(size_t)k * 2 * NB2 + NB2 + ab] = st;
+  acc[(size_t)k * 2 * NB2 + ab] = mk2(0.0, 0.0);
+  acc[(size_t)k * 2 * NB2 + NB2 + ab] = mk2(0.0, 0.0);
+}
+
+// Hermitian operand read from the upper triangle with a real diagonal (BLAS zhemm semantics)
+__device__ __forceinline__ double2 herm_up(const double2* A, int n, int i, int l) {
+  if (i == l) return mk2(A[i * n + i].x, 0.0);
+  return (i < l) ? A[i * n + l] : cconj(A[l * n + i]);
+}
+
+struct FinishArgs {
+  int nk, nbdm, bs;
+  double prefac;       // prefac_eph
+  int picture;         // 0 interaction, 1 schrodinger
+  int phase;           // alg.expt in the interaction picture
+  const double* ew;    // [nk][NB]
+  const double* edm;   // [nk][nbdm]
+  const double2* H;    // [nk][nbdm^2] or null
+  const double2* eq;   // [nk][NB2] or null
+  const double2* y;    // state the RHS is evaluated on
+  const double2* acc;  // [nk][2][NB2]
+  int want_eph, want_coh;
+  // output: plain RHS
+  double2* out;
+  // RK4 stage fusion (mode 1)
+  int mode;            // 0: out = f; 1: RK4 stage; 2: Euler
+  int stage;
+  const double* tref;  // [t0, h] for RK4/Euler
+  long long* step;
+  double2* K;          // [4][nk*nbdm^2]
+  double2* ybase;      // y_n
+  double2* ytmp;       // next stage input
+  TimeArg ta;
+};
+
+// One thread per k: scattering finish + coherent term, then the stepper's update for this k.
+template <int NB>
+__global__ void k_finish(FinishArgs a) {
+  constexpr int NB2 = NB * NB;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.nk) return;
+  const int nd = a.nbdm, nd2 = nd * nd;
+  const double t = eval_time(a.ta);
+  const double2* yk = a.y + (size_t)k * nd2;
+  double2 f[DMD_MAX_NBDM * DMD_MAX_NBDM];
+  for (int i = 0; i < nd2; ++i) f[i] = mk2(0.0, 0.0);
+
+  // coherent term: -i [H(t), rho] (DenMat.cpp:29-55)
+  if (a.want_coh) {
+    const double* ek = a.edm + (size_t)k * nd;
+    if (a.H) {
+      double2 Ht[DMD_MAX_NBDM * DMD_MAX_NBDM];
+      const double2* Hk = a.H + (size_t)k * nd2;
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j)
+          Ht[i * nd + j] = (a.picture == 0 && i != j) ? cmul_rn(Hk[i * nd + j], ccis((ek[i] - ek[j]) * t)) : Hk[i * nd + j];
+      double2 c1[DMD_MAX_NBDM * DMD_MAX_NBDM];
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j) {  // dm * H (zhemm Right, beta = 0)
+          double2 s = mk2(0.0, 0.0);
+          for (int l = 0; l < nd; ++l) s = cadd_rn(s, cmul_rn(yk[i * nd + l], herm_up(Ht, nd, l, j)));
+          c1[i * nd + j] = cmul_rn(mk2(1.0, 0.0), s);
+        }
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j) {  // H * dm - (dm * H)   (zhemm Left, beta = -1)
+          double2 s = mk2(0.0, 0.0);
+          for (int l = 0; l < nd; ++l) s = cadd_rn(s, cmul_rn(herm_up(Ht, nd, i, l), yk[l * nd + j]));
+          const double2 o = cadd_rn(cmul_rn(mk2(1.0, 0.0), s), cmul_rn(mk2(-1.0, 0.0), c1[i * nd + j]));
+          f[i * nd + j] = cadd_rn(mk2(0.0, 0.0), cmul_rn(o, mk2(0.0, -1.0)));
+        }
+    } else if (a.picture == 1) {  // commutator_mat_diag(C, e, dm, nb, -i)
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j) {
+          const double2 d = yk[i * nd + j];
+          const double2 c = mk2(-__dmul_rn(d.x, ek[j]), -__dmul_rn(d.y, ek[j]));
+          f[i * nd + j] = cadd_rn(mk2(0.0, 0.0), cmul_rn(cadd_rn(c, cmul_rn(mk2(ek[i], 0.0), d)), mk2(0.0, -1.0)));
+        }
+    }
+  }
+
+  // scattering finish on the window (evolve_eph.cpp:140-162, evolve_driver :21-32)
+  if (a.want_eph) {
+    const double* ew = a.ew + (size_t)k * NB;
+    const double2* X = a.acc + (size_t)k * 2 * NB2;
+    const double2* Y = X + NB2;
+    double2 rw[NB2], sw[NB2], Pdm[NB2], dmP[NB2];
+    for (int i = 0; i < NB; ++i)
+      for (int j = 0; j < NB; ++j) {
+        const double2 r = yk[(a.bs + i) * nd + a.bs + j];
+        rw[i * NB + j] = r;
+        sw[i * NB + j] = (i == j) ? mk2(1.0 - r.x, 0.0 - r.y) : mk2(-r.x, -r.y);
+        double2 d = mk2(1.0, 0.0);
+        if (a.phase) d = ccis((ew[i] - ew[j]) * t);
+        Pdm[i * NB + j] = a.phase ? cmul_rn(d, X[i * NB + j]) : X[i * NB + j];
+        dmP[i * NB + j] = a.phase ? cmul_rn(d, Y[i * NB + j]) : Y[i * NB + j];
+      }
+    double2 c[NB2];
+    for (int i = 0; i < NB; ++i)
+      for (int j = 0; j < NB; ++j) {  // (1 - dm) * Pdm   (zhemm Left, alpha 1, beta 0)
+        double2 s = mk2(0.0, 0.0);
+        for (int l = 0; l < NB; ++l) s = cadd_rn(s, cmul_rn(herm_up(sw, NB, i, l), Pdm[l * NB + j]));
+        c[i * NB + j] = cmul_rn(mk2(1.0, 0.0), s);
+      }
+    for (int i = 0; i < NB; ++i)
+      for (int j = 0; j < NB; ++j) {  // - dm1P * dm + c   (zhemm Right, alpha -1, beta 1)
+        double2 s = mk2(0.0, 0.0);
+        for (int l = 0; l < NB; ++l) s = cadd_rn(s, cmul_rn(dmP[i * NB + l], herm_up(rw, NB, l, j)));
+        c[i * NB + j] = cadd_rn(cmul_rn(mk2(-1.0, 0.0), s), cmul_rn(mk2(1.0, 0.0), c[i * NB + j]));
+      }
+    const double pf = a.prefac * 0.5;
+    for (int i = 0; i < NB; ++i)
+      for (int j = 0; j < NB; ++j) {
+        double2 v = cscale_rn(pf, cadd_rn(c[i * NB + j], cconj(c[j * NB + i])));
+        if (a.eq) {
+          const double2 q = a.eq[(size_t)k * NB2 + i * NB + j];
+          if (i == j || a.picture == 1) v = csub_rn(v, q);
+          else v = csub_rn(v, cmul_rn(q, ccis((ew[i] - ew[j]) * t)));
+        }
+        double2& o = f[(a.bs + i) * nd + a.bs + j];
+        o = cadd_rn(o, v);
+      }
+  }
+
+  const size_t base = (size_t)k * nd2;
+  if (a.mode == 0) {
+    for (int i = 0; i < nd2; ++i) a.out[base + i] = f[i];
+    return;
+  }
+  const size_t n = (size_t)a.nk * nd2;
+  if (a.mode == 1) {
+    const double h = a.tref[1], hh = 0.5 * h, h6 = h / 6.0;
+    double2* Ks = a.K + (size_t)a.stage * n;
+    for (int i = 0; i < nd2; ++i) {
+      const double2 yb = a.ybase[base + i];
+      Ks[base + i] = f[i];
+      if (a.stage == 0) a.ytmp[base + i] = cadd_rn(yb, cscale_rn(hh, f[i]));
+      else if (a.stage == 1) a.ytmp[base + i] = cadd_rn(yb, cscale_rn(hh, f[i]));
+      else if (a.stage == 2) a.ytmp[base + i] = cadd_rn(yb, cscale_rn(h, f[i]));
+      else {
+        const double2 k1 = a.K[base + i], k2 = a.K[n + base + i], k3 = a.K[2 * n + base + i];
+        // y + h/6 * (k1 + 2 k2 + 2 k3 + k4), evaluated left to right
+        const double sx = __dadd_rn(__dadd_rn(__dadd_rn(k1.x, __dmul_rn(2.0, k2.x)), __dmul_rn(2.0, k3.x)), f[i].x);
+        const double sy = __dadd_rn(__dadd_rn(__dadd_rn(k1.y, __dmul_rn(2.0, k2.y)), __dmul_rn(2.0, k3.y)), f[i].y);
+        a.ybase[base + i] = mk2(__dadd_rn(yb.x, __dmul_rn(h6, sx)), __dadd_rn(yb.y, __dmul_rn(h6, sy)));
+      }
+    }
+    return;
+  }
+  if (a.mode == 2) {  // update_dm_euler: dm += 0.5*dt*(ddmdt + ddmdt^dagger)
+    const double h = a.tref[1];
+    const double hf = 0.5 * h;
+    for (int i = 0; i < nd; ++i)
+      for (int j = 0; j < nd; ++j) {
+        const double2 v = cscale_rn(hf, cadd_rn(f[i * nd + j], cconj(f[j * nd + i])));
+        a.ybase[base + i * nd + j] = cadd_rn(a.ybase[base + i * nd + j], v);
+      }
+  }
+}
+
+// advance the device step counter after the last kernel of a step
+__global__ void k_step_inc(long long* step) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1;
+}
+
+// out = base + h * (c0 K0 + c1 K1 + ...), left to right; premul: (c0*h)*K0 form of the first stage
+__global__ void k_rk_comb(size_t n, const double* __restrict__ base, const double* __restrict__ K, size_t kstride,
+                          int nk_terms, const int* __restrict__ kidx, const double* __restrict__ coef, double h,
+                          int premul, double* __restrict__ out) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (premul) {  // y + c*h*k
+    out[i] = __dadd_rn(base[i], __dmul_rn(__dmul_rn(coef[0], h), K[kidx[0] * kstride + i]));
+    return;
+  }
+  double s = __dmul_rn(coef[0], K[kidx[0] * kstride + i]);
+  for (int j = 1; j < nk_terms; ++j) s = __dadd_rn(s, __dmul_rn(coef[j], K[kidx[j] * kstride + i]));
+  out[i] = __dadd_rn(base[i], __dmul_rn(h, s));
+}
+
+// yerr = h * (e1 K1 + e3 K3 + ...) and per-block max of |yerr| / (eps_rel * |y| + eps_abs)
+__global__ void k_rk_err(size_t n, const double* __restrict__ y, const double* __restrict__ K, size_t kstride,
+                         int nk_terms, const int* __restrict__ kidx, const double* __restrict__ coef, double h,
+                         double eps_abs, double eps_rel, double* __restrict__ blockmax) {
+  __shared__ double sm[256];
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  double r = 2.2250738585072014e-308;
+  if (i < n) {
+    double s = __dmul_rn(coef[0], K[kidx[0] * kstride + i]);
+    for (int j = 1; j < nk_terms; ++j) s = __dadd_rn(s, __dmul_rn(coef[j], K[kidx[j] * kstride + i]));
+    const double yerr = __dmul_rn(h, s);
+    const double D0 = __dadd_rn(__dmul_rn(eps_rel, __dadd_rn(fabs(y[i]), 0.0)), eps_abs);
+    r = fabs(yerr) / fabs(D0);
+  }
+  sm[threadIdx.x] = r;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) blockmax[blockIdx.x] = sm[0];
+}
+
+// observable totals (observable.h:356-366), per-block partial sums; block b covers k in a stripe
+__global__ void k_measure(int nk, int nbdm, int bs, int be, const double2* __restrict__ obs, const double* __restrict__ f,
+                          const double* __restrict__ edm, double t, int picture, const double2* __restrict__ y,
+                          double* __restrict__ part) {
+  __shared__ double s1[256], s2[256];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double ob = 0.0, oba = 0.0;
+  if (k < nk) {
+    const int nd = nbdm;
+    for (int i = bs; i < be; ++i) {
+      double o1 = 0.0, o2 = 0.0;
+      for (int b = 0; b < nd; ++b) {
+        const double2 okib = obs[(size_t)k * nd * nd + i * nd + b];
+        const double2 okt = (i == b || picture == 1) ? okib : cmul_rn(okib, ccis((edm[k * nd + i] - edm[k * nd + b]) * t));
+        double2 dkbi = y[(size_t)k * nd * nd + b * nd + i];
+        if (i == b) dkbi = mk2(__dsub_rn(dkbi.x, f[k * nd + i]), dkbi.y);
+        o1 = __dadd_rn(o1, cmul_rn(okt, dkbi).x);
+        o2 = __dadd_rn(o2, cmul_rn(okib, dkbi).x);
+      }
+      ob = __dadd_rn(ob, o1);
+      oba = __dadd_rn(oba, o2);
+    }
+  }
+  s1[threadIdx.x] = ob;
+  s2[threadIdx.x] = oba;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      s1[threadIdx.x] += s1[threadIdx.x + s];
+      s2[threadIdx.x] += s2[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s1[0];
+    part[2 * blockIdx.x + 1] = s2[0];
+  }
+}
+
+// non-finite scan of the state
+__global__ void k_nan_scan(size_t n, const double* __restrict__ y, int* __restrict__ flag) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n && !isfinite(y[i])) atomicOr(flag, 1);
+}
+
+}  // namespace dmd

@@ -1,0 +1,200 @@
+"""Python binding of the GPU C ABI (include/dmd_gpu.h) through ctypes.
+
+``LindbladGPU`` mirrors the reference's call surface for this path: ``func`` is the GSL callback
+of DensityMatrix_Dynamics.h:358-369, ``evolve_driver`` is electronphonon::evolve_driver
+(evolve_eph.cpp:21-32), ``evolve_coh`` is singdenmat_k::evolve_coh (DenMat.cpp:29-55); the
+steppers run with the density matrix resident on the GPU. There is no CPU fallback: without the
+compiled library or a CUDA device every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from .build import GPU_LIB
+
+PREC = {"f64": 0, "f64x": 1, "f32": 2, "bf16x2": 3}
+PICTURE = {"interaction": 0, "schrodinger": 1}
+
+
+class DMDError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("dmd status %d (%s): %s" % (status, _lib().dmd_strerror(status).decode(), msg))
+        self.status = status
+
+
+class _Desc(C.Structure):
+    _fields_ = [("nk", C.c_int32), ("nb_dm", C.c_int32), ("bstart", C.c_int32), ("bend", C.c_int32),
+                ("nkpair", C.c_int64), ("prefac_eph", C.c_double), ("e_dm", C.c_void_p), ("k1st", C.c_void_p),
+                ("k2nd", C.c_void_p), ("P1", C.c_void_p), ("P2", C.c_void_p), ("P1_add", C.c_void_p),
+                ("P2_add", C.c_void_p), ("add_scale", C.c_double), ("Hcoh", C.c_void_p), ("picture", C.c_int32),
+                ("expt", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32)]
+
+
+_L = None
+
+EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_set_ddmdt_eq", "dmd_func",
+           "dmd_evolve_driver", "dmd_evolve_coh", "dmd_set_state", "dmd_get_state", "dmd_rk4", "dmd_euler",
+           "dmd_rkf45_apply", "dmd_set_observable", "dmd_measure", "dmd_launch_count", "dmd_sync"]
+
+
+def _lib():
+    global _L
+    if _L is None:
+        if not os.path.exists(GPU_LIB):
+            raise RuntimeError("libdmdgpu.so is not built (call __graft_entry__.build() or "
+                               "denmat_dynm_development_gb300.build.build_all())")
+        L = C.CDLL(GPU_LIB)
+        vp, d, i64 = C.c_void_p, C.c_double, C.c_int64
+        L.dmd_create.argtypes = [C.POINTER(_Desc), C.POINTER(vp)]
+        L.dmd_destroy.argtypes = [vp]
+        L.dmd_last_error.argtypes = [vp]
+        L.dmd_last_error.restype = C.c_char_p
+        L.dmd_strerror.argtypes = [C.c_int]
+        L.dmd_strerror.restype = C.c_char_p
+        L.dmd_set_ddmdt_eq.argtypes = [vp, vp]
+        L.dmd_func.argtypes = [vp, d, vp, vp]
+        L.dmd_evolve_driver.argtypes = [vp, d, vp, vp, vp]
+        L.dmd_evolve_coh.argtypes = [vp, d, vp, vp]
+        L.dmd_set_state.argtypes = [vp, d, vp]
+        L.dmd_get_state.argtypes = [vp, C.POINTER(d), vp]
+        L.dmd_rk4.argtypes = [vp, d, i64]
+        L.dmd_euler.argtypes = [vp, d, i64]
+        L.dmd_rkf45_apply.argtypes = [vp, d, C.POINTER(d), d, d, d, d, C.POINTER(i64)]
+        L.dmd_set_observable.argtypes = [vp, C.c_int, vp, vp, d]
+        L.dmd_measure.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(d), C.POINTER(d)]
+        L.dmd_launch_count.argtypes = [vp, C.POINTER(i64)]
+        L.dmd_sync.argtypes = [vp]
+        _L = L
+    return _L
+
+
+def _c(a, dtype):
+    return None if a is None else np.ascontiguousarray(a, dtype=dtype)
+
+
+class LindbladGPU:
+    """Device-resident Lindblad RHS for one set of k-pair operators."""
+
+    def __init__(self, *, nk, nb_dm, bstart, bend, e_dm, k1st, k2nd, P1, P2, prefac_eph, Hcoh=None,
+                 picture="interaction", expt=1, precision="f64", P1_add=None, P2_add=None, add_scale=0.0, device=0):
+        L = _lib()
+        self._keep = dict(e=_c(e_dm, np.float64), k1=_c(k1st, np.uint64), k2=_c(k2nd, np.uint64),
+                          P1=_c(P1, np.complex128), P2=_c(P2, np.complex128), H=_c(Hcoh, np.complex128),
+                          A1=_c(P1_add, np.complex128), A2=_c(P2_add, np.complex128))
+        k = self._keep
+        ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+        desc = _Desc(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, nkpair=int(k["k1"].size), prefac_eph=prefac_eph,
+                     e_dm=ptr(k["e"]), k1st=ptr(k["k1"]), k2nd=ptr(k["k2"]), P1=ptr(k["P1"]), P2=ptr(k["P2"]),
+                     P1_add=ptr(k["A1"]), P2_add=ptr(k["A2"]), add_scale=add_scale, Hcoh=ptr(k["H"]),
+                     picture=PICTURE[picture] if isinstance(picture, str) else int(picture), expt=int(expt),
+                     precision=PREC[precision] if isinstance(precision, str) else int(precision), device=device,
+                     flags=0)
+        h = C.c_void_p()
+        st = L.dmd_create(C.byref(desc), C.byref(h))
+        if st != 0:
+            raise DMDError(st, "dmd_create failed")
+        self._h = h
+        self._keep = None  # the library copied everything it needs
+        self.nk, self.nb_dm = nk, nb_dm
+        self.ny = 2 * nk * nb_dm * nb_dm
+
+    # ------------------------------------------------------------------ plumbing
+    def _ck(self, st):
+        if st != 0:
+            raise DMDError(st, _lib().dmd_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib().dmd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _y(self, y):
+        y = np.ascontiguousarray(y)
+        if y.dtype == np.complex128:
+            y = y.view(np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64).reshape(-1)
+        if y.size != self.ny:
+            raise ValueError("state has %d doubles, expected %d" % (y.size, self.ny))
+        return y
+
+    # ------------------------------------------------------------------ reference-facing calls
+    def func(self, t, y, dydt=None):
+        y = self._y(y)
+        out = np.empty_like(y) if dydt is None else dydt
+        self._ck(_lib().dmd_func(self._h, float(t), y.ctypes.data, out.ctypes.data))
+        return out
+
+    def evolve_driver(self, t, dm, dm1=None):
+        y = self._y(dm)
+        out = np.empty_like(y)
+        self._ck(_lib().dmd_evolve_driver(self._h, float(t), y.ctypes.data, None, out.ctypes.data))
+        return out
+
+    def evolve_coh(self, t, dm):
+        y = self._y(dm)
+        out = np.empty_like(y)
+        self._ck(_lib().dmd_evolve_coh(self._h, float(t), y.ctypes.data, out.ctypes.data))
+        return out
+
+    def set_ddmdt_eq(self, eq: Optional[np.ndarray]):
+        a = None if eq is None else np.ascontiguousarray(eq, dtype=np.complex128)
+        self._ck(_lib().dmd_set_ddmdt_eq(self._h, None if a is None else a.ctypes.data))
+
+    # ------------------------------------------------------------------ device-resident stepping
+    def set_state(self, t, y):
+        y = self._y(y)
+        self._ck(_lib().dmd_set_state(self._h, float(t), y.ctypes.data))
+
+    def get_state(self):
+        y = np.empty(self.ny, np.float64)
+        t = C.c_double()
+        self._ck(_lib().dmd_get_state(self._h, C.byref(t), y.ctypes.data))
+        return t.value, y
+
+    def rk4(self, dt, nsteps):
+        self._ck(_lib().dmd_rk4(self._h, float(dt), int(nsteps)))
+
+    def euler(self, dt, nsteps):
+        self._ck(_lib().dmd_euler(self._h, float(dt), int(nsteps)))
+
+    def rkf45_apply(self, t1, hstep, hmin=0.0, hmax=1e300, epsabs=1e-8, epsrel=0.0):
+        hs = C.c_double(hstep)
+        nf = C.c_int64()
+        self._ck(_lib().dmd_rkf45_apply(self._h, float(t1), C.byref(hs), hmin, hmax, epsabs, epsrel, C.byref(nf)))
+        return hs.value, nf.value
+
+    def set_observable(self, slot, obs, f, prefac):
+        o = np.ascontiguousarray(obs, dtype=np.complex128)
+        ff = np.ascontiguousarray(f, dtype=np.float64)
+        self._ck(_lib().dmd_set_observable(self._h, slot, o.ctypes.data, ff.ctypes.data, float(prefac)))
+
+    def measure(self, slot=0, bstart=0, bend=None):
+        bend = self.nb_dm if bend is None else bend
+        a, b = C.c_double(), C.c_double()
+        self._ck(_lib().dmd_measure(self._h, slot, bstart, bend, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    @property
+    def launches(self):
+        n = C.c_int64()
+        self._ck(_lib().dmd_launch_count(self._h, C.byref(n)))
+        return n.value
+
+    def sync(self):
+        self._ck(_lib().dmd_sync(self._h))

@@ -1,0 +1,120 @@
+/* dmd_gpu.h -- C ABI of the GB300 (sm_103a) Lindblad density-matrix right-hand side and steppers.
+ *
+ * Drop-in boundary for DMD's scattering/coherent RHS and its ODE stepping. Every entry point takes
+ * plain pointers and sizes and returns an int status (DMD_OK = 0); nothing throws across the ABI.
+ * complex128 arrays are interleaved (re, im) doubles; density matrices are k-major, then row-major
+ * nb_dm x nb_dm; P operators are [nkpair][nb^4] with row (i1*nb+i2), column (i3*nb+i4).
+ *
+ * A handle owns one CUDA stream on one device and is not thread-safe.
+ *
+ * Reference interfaces replaced (file:line in the reference tree):
+ *   dmd_create          electronphonon::set_eph / alloc_ephmat / read_ldbd_eph + add_scatt_contrib
+ *                       (ElectronPhonon.cpp:3-14, 44-113, 209-304), singdenmat_k::init_Hcoh
+ *                       (DenMat.cpp:7-28)
+ *   dmd_func            GSL callback func(t, y, dydt, params) (DensityMatrix_Dynamics.h:358-369)
+ *                       = dm_dynamics::compute (DensityMatrix_Dynamics.h:243-278)
+ *   dmd_evolve_driver   electronphonon::evolve_driver (evolve_eph.cpp:21-32) -> evolve (:34-166)
+ *   dmd_evolve_coh      singdenmat_k::evolve_coh (DenMat.cpp:29-55)
+ *   dmd_set_ddmdt_eq    electronphonon::ddmdt_eq subtraction (evolve_eph.cpp:154-162)
+ *   dmd_rk4             fixed-step RK4 over func (device resident; DMD's stepper loop
+ *                       DensityMatrix_Dynamics.h:189-225 with the state kept on the GPU)
+ *   dmd_rkf45_apply     gsl_odeiv2_driver_apply with gsl_odeiv2_step_rkf45 and the y_new control
+ *                       (DensityMatrix_Dynamics.h:197-224)
+ *   dmd_euler           evolve_euler_one_step + singdenmat_k::update_dm_euler
+ *                       (DensityMatrix_Dynamics.h:227-234, DenMat.cpp:236-248)
+ *   dmd_measure         ob_1dmk::measure("sx"/"sy"/"sz"...) totals (observable.h:301-366)
+ *   dmd_set_state / dmd_get_state   copy_complex_from_real / copy_real_from_complex (comm/ODE.h:6-15)
+ */
+#ifndef DMD_GPU_H
+#define DMD_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define DMD_OK 0
+#define DMD_E_ARG 1        /* invalid argument or size */
+#define DMD_E_NOMEM 2      /* device or host allocation failed */
+#define DMD_E_FILE 3       /* input file missing or of the wrong size */
+#define DMD_E_CUDA 4       /* CUDA runtime error */
+#define DMD_E_TIMEOUT 5    /* a bounded device wait gave up */
+#define DMD_E_NAN 6        /* non-finite value in the state */
+#define DMD_E_STATE 7      /* call made in the wrong state */
+#define DMD_E_NODEV 8      /* no CUDA device */
+#define DMD_E_ODE 9        /* step size underflow (GSL_ENOPROG) or bad step direction */
+
+/* arithmetic of the k-pair contraction */
+#define DMD_PREC_F64 0     /* P complex128, native FP64 multiply-adds */
+#define DMD_PREC_F64X 1    /* P and rho as (hi, lo) FP32 pairs: ~2^-46 products, double-FP32 sums */
+#define DMD_PREC_F32 2     /* P stored complex64, FP32 products, FP64 per-k sums */
+#define DMD_PREC_BF16X2 3  /* P stored as bf16 hi + bf16 lo per component, FP32 products */
+
+/* pictures (alg.picture) */
+#define DMD_PICTURE_INTERACTION 0
+#define DMD_PICTURE_SCHRODINGER 1
+
+typedef struct dmd_handle dmd_handle;
+
+typedef struct dmd_desc {
+  int32_t nk;            /* k-points (elec->nk) */
+  int32_t nb_dm;         /* bands of the density matrix (elec->nb_dm), <= 8 */
+  int32_t bstart, bend;  /* e-ph band window relative to bStart_dm; nb = bend - bstart in 1..4 */
+  int64_t nkpair;        /* stored k-pairs */
+  double prefac_eph;     /* 2*pi / nk_full (ElectronPhonon.h:61) */
+  const double* e_dm;    /* [nk][nb_dm] band energies (Hartree) */
+  const uint64_t* k1st;  /* [nkpair] first k of each pair (k1st <= k2nd) */
+  const uint64_t* k2nd;  /* [nkpair] */
+  const double* P1;      /* complex128 [nkpair][nb^4], scaled by scale_eph */
+  const double* P2;      /* complex128 [nkpair][nb^4] */
+  const double* P1_add;  /* optional complex128 [nkpair][nb^4] added as P1 += add_scale * P1_add */
+  const double* P2_add;  /*   (ab-initio e-imp "D1" operators, ElectronImpurity.cpp:3-49) */
+  double add_scale;      /* |n_i * V_cell| */
+  const double* Hcoh;    /* optional complex128 [nk][nb_dm^2] coherent Hamiltonian (H_BS [+ H_Ez]) */
+  int32_t picture;       /* DMD_PICTURE_* */
+  int32_t expt;          /* 1: time-dependent P phases (alg.expt) */
+  int32_t precision;     /* DMD_PREC_* */
+  int32_t device;        /* CUDA device ordinal */
+  uint32_t flags;        /* reserved, 0 */
+} dmd_desc;
+
+int dmd_create(const dmd_desc* desc, dmd_handle** out);
+int dmd_destroy(dmd_handle* h);
+const char* dmd_last_error(const dmd_handle* h);
+const char* dmd_strerror(int status);
+
+/* optional equilibrium drift subtracted from the scattering term, complex128 [nk][nb^2] */
+int dmd_set_ddmdt_eq(dmd_handle* h, const double* ddmdt_eq);
+
+/* RHS on host buffers (each call copies y in and the result out) */
+int dmd_func(dmd_handle* h, double t, const double* y, double* dydt);
+int dmd_evolve_driver(dmd_handle* h, double t, const double* dm, const double* dm1, double* ddmdt_eph);
+int dmd_evolve_coh(dmd_handle* h, double t, const double* dm, double* ddmdt_coh);
+
+/* device-resident state */
+int dmd_set_state(dmd_handle* h, double t, const double* y);
+int dmd_get_state(dmd_handle* h, double* t, double* y);
+int dmd_rk4(dmd_handle* h, double dt, int64_t nsteps);
+int dmd_euler(dmd_handle* h, double dt, int64_t nsteps);
+/* One gsl_odeiv2_driver_apply call from the current time to t1. *hstep carries the driver's step
+ * size between calls (initialise it with hstart). nfev (optional) receives the RHS evaluations. */
+int dmd_rkf45_apply(dmd_handle* h, double t1, double* hstep, double hmin, double hmax, double epsabs,
+                    double epsrel, int64_t* nfev);
+
+/* observables: slot 0..7 holds complex128 [nk][nb_dm^2] matrix elements (e.g. s_z), the occupations
+ * f [nk][nb_dm] and the prefactor 1/(nk_full*cell_size_cmd); measure returns (tot, tot_amp) over
+ * bands [bstart, bend) of the density matrix. */
+int dmd_set_observable(dmd_handle* h, int slot, const double* obs, const double* f, double prefac);
+int dmd_measure(dmd_handle* h, int slot, int bstart, int bend, double* tot, double* tot_amp);
+
+/* counters: kernel launches issued by this handle since creation */
+int dmd_launch_count(const dmd_handle* h, int64_t* launches);
+/* wait for the handle's stream */
+int dmd_sync(dmd_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

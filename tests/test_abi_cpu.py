@@ -1,0 +1,44 @@
+"""CPU-only checks of the native boundary: the libraries build, load, and export every symbol the
+public headers declare; argument validation answers without touching a GPU."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def declared(header):
+    src = open(os.path.join(ROOT, "include", header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(dmd_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def gpu_lib():
+    from denmat_dynm_development_gb300 import build as B
+    path = B.build_gpu()
+    return C.CDLL(path)
+
+
+def test_gpu_lib_exports_header(gpu_lib):
+    names = declared("dmd_gpu.h")
+    assert "dmd_create" in names and "dmd_func" in names
+    missing = [n for n in names if not hasattr(gpu_lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_lists_all_exports():
+    from denmat_dynm_development_gb300 import dmd
+    assert sorted(dmd.EXPORTS) == declared("dmd_gpu.h")
+
+
+def test_strerror_and_null_arguments(gpu_lib):
+    gpu_lib.dmd_strerror.restype = C.c_char_p
+    assert gpu_lib.dmd_strerror(0) == b"ok"
+    assert gpu_lib.dmd_strerror(1) == b"invalid argument"
+    # a null descriptor is rejected before any device call
+    h = C.c_void_p()
+    assert gpu_lib.dmd_create(None, C.byref(h)) == 1
+    assert gpu_lib.dmd_destroy(None) == 1

@@ -1,0 +1,143 @@
+"""GPU parity: the CUDA path through the C ABI against the golden fixtures and the oracle.
+
+Tolerances (normwise relative, max|gpu - ref| / max|ref|):
+  * RHS (func, evolve_driver, evolve_coh) in FP64: 1e-12 -- the reference forms each P(t)
+    element's phase cis(t(e1-e3-e2+e4)) while the GPU factorises it per k, and the pair sums
+    run in a different order;
+  * trajectories (40 RK4 steps, RKF45 to 20 fs): 1e-10 (the benchmark spec's bound for rho(t), S(t)).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, GOLDEN_CASES
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300))
+
+
+def make_gpu(s, precision="f64"):
+    from denmat_dynm_development_gb300.dmd import LindbladGPU
+    return LindbladGPU(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
+                       P1=s.P1, P2=s.P2, prefac_eph=s.prefac_eph, Hcoh=s.Hcoh, picture=s.picture_schrodinger,
+                       expt=s.expt, precision=precision)
+
+
+@pytest.fixture(scope="module")
+def built():
+    import __graft_entry__ as G
+    G.build()
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_rhs_vs_golden(case, oracle, built):
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = oracle.load(d)
+    with make_gpu(s) as gpu:
+        for i, t in enumerate(g["rhs_t"]):
+            y = g["rhs_y"][i]
+            assert rel(gpu.func(t, y), g["rhs_dydt"][i]) < 1e-12
+            assert rel(gpu.evolve_driver(t, y), g["rhs_eph"][i]) < 1e-12
+            if np.abs(g["rhs_coh"][i]).max() > 0:
+                assert rel(gpu.evolve_coh(t, y), g["rhs_coh"][i]) < 1e-12
+            # exact Hermiticity of the scattering term (c + c^dagger, evolve_eph.cpp:151)
+            e = gpu.evolve_driver(t, y).view(np.complex128).reshape(s.nk, s.nb_dm, s.nb_dm)
+            np.testing.assert_array_equal(e, np.conj(np.swapaxes(e, 1, 2)))
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_rk4_vs_golden(case, oracle, built):
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = oracle.load(d)
+    with make_gpu(s) as gpu:
+        gpu.set_state(s.t0, oracle.y_of(s.dm0))
+        gpu.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+        rec = []
+        for _ in range(8):
+            gpu.rk4(1.0 * oracle.fs, 5)
+            t, _ = gpu.get_state()
+            tot, amp = gpu.measure(0)
+            rec.append((t, tot, amp))
+        t, y = gpu.get_state()
+        assert rel(y, g["rk4_y"]) < 1e-10
+        rec = np.array(rec)
+        ref = g["rk4_sz"][1:]
+        assert rel(rec[:, 0], ref[:, 0]) < 1e-14
+        assert rel(rec[:, 1], ref[:, 1]) < 1e-10
+        assert rel(rec[:, 2], ref[:, 2]) < 1e-10
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_rkf45_vs_golden(case, oracle, built):
+    """DMD's evolve_gsl loop: one driver_apply per output interval (DensityMatrix_Dynamics.h:210-223)."""
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = oracle.load(d)
+    with make_gpu(s) as gpu:
+        gpu.set_state(s.t0, oracle.y_of(s.dm0))
+        gpu.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+        hs = s.ode["hstart"]
+        ti = s.t0
+        tcur = s.t0
+        sz, nf = [], []
+        while tcur < s.tend:
+            ti += s.tstep
+            hs, n = gpu.rkf45_apply(ti, hs, s.ode["hmin"], s.ode["hmax"], s.ode["epsabs"], 0.0)
+            tcur, _ = gpu.get_state()
+            sz.append(gpu.measure(0)[0])
+            nf.append(n)
+        _, y = gpu.get_state()
+        assert rel(y, g["gsl_y"]) < 1e-10
+        assert rel(np.array(sz), g["gsl_sz"][1:, 1]) < 1e-10
+        np.testing.assert_array_equal(np.array(nf), g["gsl_ncalls"])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_euler_vs_oracle(case, oracle, built):
+    d = os.path.join(GOLDEN, case)
+    s = oracle.load(d)
+    y0 = oracle.y_of(s.dm0)
+    with make_gpu(s) as gpu:
+        gpu.set_state(s.t0, y0)
+        gpu.euler(0.5 * oracle.fs, 6)
+        _, y = gpu.get_state()
+    yr = oracle.euler(s, s.t0, 0.5 * oracle.fs, 6, y0)
+    assert rel(y, yr) < 1e-12
+
+
+def test_larger_random_case_vs_oracle(oracle, built, tmp_path):
+    """nk=500 Si-like workload (about 70k pairs) with e-imp and a B field."""
+    from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, make_ldbd
+    cfg = SynthConfig(nk=500, nb=2, seed=3, eimp_sigma_mev=5.0)
+    make_ldbd(str(tmp_path), cfg, B_T=(1.0, 0.0, 0.0), eimp_fraction=1e-2)
+    s = oracle.load(str(tmp_path))
+    rng = np.random.default_rng(5)
+    with make_gpu(s) as gpu:
+        for t in (0.0, 11.0 * oracle.fs, 4000.0 * oracle.fs):
+            dm = s.dm0 + 1e-3 * (rng.standard_normal(s.dm0.shape) + 1j * rng.standard_normal(s.dm0.shape))
+            dm = dm.reshape(s.nk, s.nb_dm, s.nb_dm)
+            dm = 0.5 * (dm + np.conj(np.swapaxes(dm, 1, 2)))
+            y = oracle.y_of(dm.reshape(s.nk, -1))
+            assert rel(gpu.func(t, y), oracle.rhs(s, t, y)) < 1e-12
+
+
+def test_nb4_larger_vs_oracle(oracle, built, tmp_path):
+    from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, make_ldbd
+    cfg = SynthConfig(nk=120, nb=4, seed=4, eimp_sigma_mev=5.0)
+    make_ldbd(str(tmp_path), cfg, B_T=(0.0, 0.7, 0.0), eimp_fraction=1e-2)
+    s = oracle.load(str(tmp_path))
+    y = oracle.y_of(s.dm0)
+    with make_gpu(s) as gpu:
+        t = 250.0 * oracle.fs
+        assert rel(gpu.func(t, y), oracle.rhs(s, t, y)) < 1e-12
+        gpu.set_state(s.t0, y)
+        gpu.rk4(2.0 * oracle.fs, 10)
+        _, yg = gpu.get_state()
+    yr, _ = oracle.rk4(s, s.t0, 2.0 * oracle.fs, 10, y)
+    assert rel(yg, yr) < 1e-10
