@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Benchmark: RK4 steps/s of DMD's Lindblad density-matrix dynamics on the GaAs-like workload.
+
+Workload (gaas_nk20k): nb = 2 spin-split conduction bands, nk = 20000 k-points, ~9.7M k-pairs
+(P1 + P2 = 5.0 GB complex128), e-ph plus an ab-initio-style e-imp term folded into P
+(|n_i V_cell| = 1e-4), spin perturbation Bz = 0.1 T, RK4 with dt = 1 fs. Seeded synthetic data
+from the package generator (the reference publishes no dataset for this path).
+
+One step = one RK4 step = four RHS evaluations, each streaming all of P once (inputs are larger
+than the 129 MB L2, so no flush is needed between steps).
+
+  value       RK4 steps/s with the density matrix resident on the GPU (dmd_rk4, CUDA graph)
+  e2e         the same metric through the reference-facing GSL callback dmd_func: the host runs
+              the RK4 combination and every RHS call copies y in and dydt out (pinned buffers)
+  roofline    k-pair contraction kernel: algorithmic bytes per launch / its mean event-timed
+              duration, against the measured HBM copy bandwidth
+  cpu_baseline the oracle port of the reference's RHS on this host (test infrastructure)
+
+--impl reference runs the CPU restatement of the reference's code path (DMD's MPI pair
+decomposition as forked processes over all host cores) on the same workload and metric.
+N > 1 GPUs run independent replicas (the path's only exchange is a per-RHS allreduce that this
+build does not distribute); value is the sum over ranks of steps/s.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from denmat_dynm_development_gb300 import ldbd_synth as S  # noqa: E402
+from denmat_dynm_development_gb300 import units as U  # noqa: E402
+
+METRIC = "RK4 steps/s (plain FP64 Lindblad RHS, k-pair P streamed from HBM)"
+UNIT = "RK4 steps/s"
+
+
+def env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+# ------------------------------------------------------------------------------------------------
+# workload
+# ------------------------------------------------------------------------------------------------
+def build_workload(name, procs):
+    cfg = S.WORKLOADS[name]
+    frac = 1e-4 if cfg.eimp_sigma_mev is not None else None
+    t0 = time.time()
+    st, P1, P2, _, _ = S.generate_arrays(cfg, fold_fraction=frac, procs=procs)
+    gen_s = time.time() - t0
+    from denmat_dynm_development_gb300 import host as H
+    T = st.T
+    mu = (st.mu / U.eV) * U.eV          # parameters::get round trip
+    e = np.ascontiguousarray(st.e)
+    f = H.fermi(T, mu, e)
+    Bpert = np.array([0.0, 0.0, 0.1 * U.Tesla2au])
+    dm0 = H.dm_bpert(st.s, e, f, T, Bpert, 0.0, 0)
+    nk_full = float(st.n) ** 3
+    V = st.V
+    ob_prefac = (1.0 / nk_full) / (V * U.bohr2cm ** 3)
+    w = dict(name=name, cfg=cfg, st=st, P1=P1, P2=P2, e=e, f=f, dm0=dm0, T=T, mu=mu, nk_full=nk_full,
+             prefac=2 * math.pi / nk_full, ob_prefac=ob_prefac, gen_s=gen_s, frac=frac)
+    return w
+
+
+def algorithmic_bytes(nb, npair, nk, prec_bytes=16):
+    """Per RHS evaluation of the pair contraction: P1+P2 once, two int32 indices per pair, the
+    per-k vectors read and the per-k sums written."""
+    return npair * (2 * nb ** 4 * prec_bytes + 8) + nk * nb * nb * 16 * 2 + nk * nb * 8
+
+
+def config_of(w, extra=None):
+    st = w["st"]
+    nb = st.cfg.nb
+    c = {"workload": "%s: nb=%d, nk=%d, %d k-pairs (P1+P2 %.2f GB complex128), e-ph%s, Bz_pert 0.1 T, RK4 dt=1 fs"
+                     % (w["name"], nb, st.cfg.nk, st.npair, 2 * st.npair * nb ** 4 * 16 / 1e9,
+                        " + e-imp (|n_i V|=1e-4)" if w["frac"] else ""),
+         "nk": st.cfg.nk, "nb": nb, "npair": st.npair, "dt_fs": 1.0,
+         "l2": "inputs larger than L2 (P streamed once per RHS: %.2f GB > 129 MB); no flush" %
+               (2 * st.npair * nb ** 4 * 16 / 1e9),
+         "parallelism": "replicas"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ------------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ------------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            v = [x.strip() for x in ln.split(",")]
+            if len(v) < 9:
+                continue
+            try:
+                sm.append(float(v[1]))
+                smax.append(float(v[2]))
+            except ValueError:
+                continue
+            for n, x in zip(names, v[5:9]):
+                if x.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per pair-kernel launch from the committed ncu summary, scaled to this workload."""
+    p = os.path.join(ROOT, "profiles", "pairs_kernel_gaas_traffic.json")
+    try:
+        with open(p) as f:
+            j = json.load(f)
+        return j
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU baseline (oracle port) and reference arm
+# ------------------------------------------------------------------------------------------------
+def oracle_system(w):
+    from oracle import oracle as O
+    O.build()
+    O._setup_prototypes()
+    st = w["st"]
+    return O, O.from_arrays(nk=st.cfg.nk, nb_dm=st.cfg.nb, bstart=0, bend=st.cfg.nb, e_dm=w["e"], f_dm=w["f"],
+                            k1st=st.k1, k2nd=st.k2, P1=w["P1"], P2=w["P2"], prefac_eph=w["prefac"], dm0=w["dm0"],
+                            temperature=w["T"], mu=w["mu"], nk_full=w["nk_full"], ob_prefac=w["ob_prefac"])
+
+
+def rk4_host_step(f, t, y, h):
+    """y_{n+1} = y + h/6 (k1 + 2 k2 + 2 k3 + k4) with f(t, y) a host-buffer RHS."""
+    k1 = f(t, y)
+    k2 = f(t + 0.5 * h, y + (0.5 * h) * k1)
+    k3 = f(t + 0.5 * h, y + (0.5 * h) * k2)
+    k4 = f(t + h, y + h * k3)
+    return y + (h / 6.0) * (((k1 + 2.0 * k2) + 2.0 * k3) + k4)
+
+
+def cpu_baseline_single(w):
+    """One oracle func() evaluation of the full workload on one core (the reference is serial per
+    MPI rank): steps/s = 1 / (4 t_eval)."""
+    O, s = oracle_system(w)
+    y = O.y_of(w["dm0"])
+    t0 = time.perf_counter()
+    O.rhs(s, 3.0 * U.fs, y)
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / (4.0 * dt), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "one func() evaluation of the full workload (%d pairs) in %.1f s on one core; "
+                      "RK4 step = 4 evaluations" % (s.npair, dt)}
+
+
+def run_reference(args, w):
+    O, s = oracle_system(w)
+    cores = os.cpu_count() or 1
+    par = O.ParallelRHS(s, cores)
+    try:
+        h = 1.0 * U.fs
+        y = O.y_of(w["dm0"])
+        t = 0.0
+        for _ in range(args.warmup):
+            y = rk4_host_step(par, t, y, h)
+            t += h
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            y = rk4_host_step(par, t, y, h)
+            t += h
+        el = time.perf_counter() - t0
+    finally:
+        par.close()
+    v = args.steps / el
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_of(w, {"parallelism": "%d forked CPU ranks (DMD's MPI pair split)" % cores}),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d RK4 steps of the full workload, pairs split over %d processes as DMD's "
+                                       "MPI ranks split them, allreduce by summation" % (args.steps, cores)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------------
+def run_gpu(args, w, rank, world, dist):
+    from denmat_dynm_development_gb300.dmd import LindbladGPU, PinnedArray
+    st = w["st"]
+    nb = st.cfg.nb
+    dev = env_int("LOCAL_RANK", 0)
+    g = LindbladGPU(nk=st.cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=w["e"], k1st=st.k1, k2nd=st.k2, P1=w["P1"],
+                    P2=w["P2"], prefac_eph=w["prefac"], picture=0, expt=1, precision=args.precision, device=dev)
+    h = 1.0 * U.fs
+    y0 = np.ascontiguousarray(w["dm0"]).view(np.float64).reshape(-1).copy()
+    g.set_state(0.0, y0)
+    g.rk4(h, args.warmup)                      # warm-up (also captures the step graph)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+    # ---- timed region: device-resident RK4 --------------------------------------------------
+    clk = ClockSampler(dev)
+    clk.start()
+    barrier()
+    g.sync()
+    l0 = g.launches
+    g.timer_start()
+    g.rk4(h, args.steps)
+    ms = g.timer_stop()
+    g.sync()
+    barrier()
+    clocks = clk.stop()
+    launches = g.launches - l0
+    if dist is not None:
+        import torch
+        tt = torch.tensor([ms], dtype=torch.float64, device="cuda:%d" % dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    ms_per_step = ms / args.steps
+    value = world * 1e3 / ms_per_step
+    # ---- per-kernel event timing (profiled pass, same steps) ----------------------------------
+    g.set_profiling(True)
+    g.rk4(h, max(2, min(args.steps, 10)))
+    pair_ms, pair_n = g.profile(1)
+    prep_ms, prep_n = g.profile(0)
+    fin_ms, fin_n = g.profile(2)
+    g.set_profiling(False)
+    # ---- end to end through the GSL-callback ABI with host buffers ---------------------------
+    e2e = None
+    if not args.no_e2e:
+        n = y0.size
+        ybuf = PinnedArray(n)
+        dbuf = PinnedArray(n)
+        yin = PinnedArray(n)
+        try:
+            def f(t, y):
+                yin.array[:] = y
+                g.func(t, yin.array, dbuf.array)
+                return dbuf.array.copy()
+            _, ycur = g.get_state()
+            ybuf.array[:] = ycur
+            y = ybuf.array.copy()
+            t = 0.0
+            y = rk4_host_step(f, t, y, h)       # warm-up
+            ne = max(2, min(args.steps, 10))
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(ne):
+                y = rk4_host_step(f, t, y, h)
+                t += h
+            el = time.perf_counter() - t0
+            e2e = {"value": world * ne / el, "unit": UNIT, "h2d_bytes_per_step": 4 * n * 8,
+                   "d2h_bytes_per_step": 4 * n * 8,
+                   "path": "host RK4 loop calling dmd_func (GSL callback semantics) 4x per step from pinned "
+                           "buffers; %d steps" % ne}
+        finally:
+            ybuf.free()
+            dbuf.free()
+            yin.free()
+    g.close()
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    bpl = algorithmic_bytes(nb, st.npair, st.cfg.nk, 16)
+    pair_avg_ms = pair_ms / max(pair_n, 1)
+    achieved = bpl / (pair_avg_ms * 1e-3) / 1e9
+    tr = profile_traffic()
+    traffic = None
+    if tr and tr.get("npair"):
+        traffic = tr["dram_bytes_per_launch"] * st.npair / tr["npair"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": {"f64": "f64", "f64x": "f64 (fp32-pair emulated)", "f32": "f32",
+                                           "bf16x2": "bf16x2"}[args.precision],
+            "data": "synthetic", "config": config_of(w, {"precision": args.precision}),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k-pair contraction", "bytes_per_launch": bpl, "avg_launch_ms": pair_avg_ms,
+                         "launches_profiled": pair_n},
+            "kernel_ms_per_step": {"pairs": pair_ms / max(pair_n, 1) * 4, "prep": prep_ms / max(prep_n, 1) * 4,
+                                   "finish": fin_ms / max(fin_n, 1) * 4},
+            "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+            "gen_seconds": w["gen_s"]}
+    if args.cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline_single(w)
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="gaas_nk20k")
+    ap.add_argument("--precision", default="f64", choices=["f64", "f64x", "f32", "bf16x2"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        w = build_workload(args.workload, min(16, os.cpu_count() or 1))
+        run_reference(args, w)
+        return
+    # the generator's worker processes start before any CUDA call
+    w = build_workload(args.workload, max(1, min(16, (os.cpu_count() or 1) // max(world, 1))))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as D
+        torch.cuda.set_device(env_int("LOCAL_RANK", 0))
+        D.init_process_group("nccl")
+        dist = D
+    try:
+        run_gpu(args, w, rank, world, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

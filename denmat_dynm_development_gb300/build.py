@@ -66,21 +66,20 @@ def build_gpu(force=False, verbose=False):
 def build_host(force=False):
     if not HOST_SRCS:
         return None
-    deps = HOST_SRCS + [os.path.join(CSRC, "dmd_host.h"), os.path.join(INC, "dmd_host.h"), os.path.join(INC, "dmd_gpu.h")]
+    deps = HOST_SRCS + [os.path.join(INC, "dmd_host.h"), os.path.join(INC, "dmd_gpu.h"), GPU_LIB]
     if not force and not _stale(HOST_LIB, deps):
         return HOST_LIB
     tmp = HOST_LIB + ".tmp"
+    build_gpu()
     _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", INC, "-o", tmp] + HOST_SRCS +
-         ["-lm"])
+         ["-L", PKG, "-l:libdmdgpu.so", "-Wl,-rpath,$ORIGIN", "-lm"])
     os.replace(tmp, HOST_LIB)
     return HOST_LIB
 
 
 def build_all(force=False, verbose=False):
-    with ThreadPoolExecutor(max_workers=2) as ex:
-        fg = ex.submit(build_gpu, force, verbose)
-        fh = ex.submit(build_host, force)
-        return fg.result(), fh.result()
+    g = build_gpu(force, verbose)
+    return g, build_host(force)
 
 
 if __name__ == "__main__":

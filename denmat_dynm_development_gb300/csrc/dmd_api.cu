@@ -50,6 +50,17 @@ struct dmd_handle {
   long long launches = 0;
   cudaGraphExec_t g_rk4 = nullptr;
   std::string err;
+  // timing / profiling
+  cudaEvent_t tev[2] = {nullptr, nullptr};
+  int prof_on = 0;
+  struct Rec {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> prof_pending;
+  std::vector<cudaEvent_t> ev_pool;
+  double prof_ms[4] = {0, 0, 0, 0};
+  long long prof_n[4] = {0, 0, 0, 0};
 };
 
 namespace {
@@ -84,12 +95,58 @@ int dalloc(dmd_handle* h, T** p, size_t n) {
 
 inline unsigned blocks_for(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
 
+cudaEvent_t pool_event(dmd_handle* h) {
+  if (!h->ev_pool.empty()) {
+    cudaEvent_t e = h->ev_pool.back();
+    h->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// brackets one kernel launch with events when profiling is on
+struct ProfScope {
+  dmd_handle* h;
+  int cls;
+  cudaEvent_t a = nullptr;
+  ProfScope(dmd_handle* h_, int c) : h(h_), cls(c) {
+    if (h->prof_on) {
+      a = pool_event(h);
+      cudaEventRecord(a, h->st);
+    }
+  }
+  ~ProfScope() {
+    if (h->prof_on && a) {
+      cudaEvent_t b = pool_event(h);
+      cudaEventRecord(b, h->st);
+      h->prof_pending.push_back({cls, a, b});
+    }
+  }
+};
+
+// accumulate finished profiling records (call after the stream is synchronised)
+void prof_harvest(dmd_handle* h) {
+  for (auto& r : h->prof_pending) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      h->prof_ms[r.cls] += ms;
+      h->prof_n[r.cls] += 1;
+    }
+    h->ev_pool.push_back(r.a);
+    h->ev_pool.push_back(r.b);
+  }
+  h->prof_pending.clear();
+}
+
 // ---------------------------------------------------------------------------------------------
 // one RHS evaluation on device buffers: prep -> pairs -> finish
 // ---------------------------------------------------------------------------------------------
 template <int NB>
 int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
   const int n = h->nk * NB * NB;
+  ProfScope ps(h, 0);
   k_prep<NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->expt, h->d_rs, h->d_acc);
   h->launches++;
   CKL();
@@ -100,6 +157,7 @@ template <int NB>
 int launch_pairs(dmd_handle* h) {
   if (h->npair == 0) return DMD_OK;
   const long long nthr = h->npair * 4LL * NB * NB;
+  ProfScope ps(h, 1);
   k_pairs_f64_atomic<NB><<<blocks_for(nthr, 256), 256, 0, h->st>>>(h->npair, h->d_kk, h->d_P, h->d_rs, h->d_acc);
   h->launches++;
   CKL();
@@ -108,6 +166,7 @@ int launch_pairs(dmd_handle* h) {
 
 template <int NB>
 int launch_finish(dmd_handle* h, FinishArgs a) {
+  ProfScope ps(h, 2);
   k_finish<NB><<<blocks_for(h->nk, 128), 128, 0, h->st>>>(a);
   h->launches++;
   CKL();
@@ -228,6 +287,13 @@ void release(dmd_handle* h) {
     if (h->d_obs[i]) cudaFree(h->d_obs[i]);
     if (h->d_f[i]) cudaFree(h->d_f[i]);
   }
+  for (auto& r : h->prof_pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (auto e : h->ev_pool) cudaEventDestroy(e);
+  for (auto e : h->tev)
+    if (e) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
 }
 
@@ -426,7 +492,10 @@ static int rk4_step_launches(dmd_handle* h) {
     int rc = rhs(h, in, ta, fa);
     if (rc) return rc;
   }
-  k_step_inc<<<1, 32, 0, h->st>>>(h->d_step);
+  {
+    ProfScope ps(h, 3);
+    k_step_inc<<<1, 32, 0, h->st>>>(h->d_step);
+  }
   h->launches++;
   CKL();
   return DMD_OK;
@@ -442,6 +511,16 @@ int dmd_rk4(dmd_handle* h, double dt, int64_t nsteps) {
   CK(cudaMemcpyAsync(h->d_step, &zero, 8, cudaMemcpyHostToDevice, h->st));
   // pageable sources: wait so the host values stay valid
   CK(cudaStreamSynchronize(h->st));
+  if (h->prof_on) {  // one step at a time, events around every kernel
+    for (int64_t s = 0; s < nsteps; ++s) {
+      int rc = rk4_step_launches(h);
+      if (rc) return rc;
+      CK(cudaStreamSynchronize(h->st));
+      prof_harvest(h);
+    }
+    h->t = h->t + (double)nsteps * dt;
+    return check_state(h);
+  }
   if (!h->g_rk4) {
     cudaGraph_t g;
     const long long l0 = h->launches;
@@ -680,6 +759,58 @@ int dmd_sync(dmd_handle* h) {
   if (!h) return DMD_E_ARG;
   CK(cudaSetDevice(h->dev));
   CK(cudaStreamSynchronize(h->st));
+  prof_harvest(h);
+  return DMD_OK;
+}
+
+int dmd_pinned_alloc(size_t bytes, void** out) {
+  if (!out) return DMD_E_ARG;
+  *out = nullptr;
+  cudaError_t e = cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault);
+  if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? DMD_E_NOMEM : DMD_E_CUDA;
+  return DMD_OK;
+}
+
+int dmd_pinned_free(void* p) {
+  if (!p) return DMD_E_ARG;
+  return cudaFreeHost(p) == cudaSuccess ? DMD_OK : DMD_E_CUDA;
+}
+
+int dmd_timer(dmd_handle* h, int op, double* ms) {
+  if (!h || (op != 0 && op != 1)) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  for (auto& e : h->tev)
+    if (!e) CK(cudaEventCreate(&e));
+  if (op == 0) {
+    CK(cudaEventRecord(h->tev[0], h->st));
+    return DMD_OK;
+  }
+  CK(cudaEventRecord(h->tev[1], h->st));
+  CK(cudaEventSynchronize(h->tev[1]));
+  float f = 0;
+  CK(cudaEventElapsedTime(&f, h->tev[0], h->tev[1]));
+  if (ms) *ms = f;
+  return DMD_OK;
+}
+
+int dmd_set_profiling(dmd_handle* h, int on) {
+  if (!h) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaStreamSynchronize(h->st));
+  prof_harvest(h);
+  h->prof_on = on ? 1 : 0;
+  if (on)
+    for (int i = 0; i < 4; ++i) {
+      h->prof_ms[i] = 0;
+      h->prof_n[i] = 0;
+    }
+  return DMD_OK;
+}
+
+int dmd_profile_get(const dmd_handle* h, int cls, double* total_ms, int64_t* n) {
+  if (!h || cls < 0 || cls > 3) return DMD_E_ARG;
+  if (total_ms) *total_ms = h->prof_ms[cls];
+  if (n) *n = h->prof_n[cls];
   return DMD_OK;
 }
 

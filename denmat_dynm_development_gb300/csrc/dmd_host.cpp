@@ -1,0 +1,581 @@
+// Host side of the GB300 DMD path (see include/dmd_host.h): DMD's input readers and set-up restated
+// in C++, and DMD's time loop driving the GPU ABI. Compiled with -ffp-contract=off so that every
+// set-up value rounds as the reference's scalar code does.
+#include "dmd_host.h"
+
+#include <sys/stat.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace {
+
+// comm/Units.h
+const double kEV = 1 / 27.21138505;
+const double kJoule = 1 / 4.35974434e-18;
+const double kAngstrom = 1 / 0.5291772;
+const double kMeter = 1e10 * kAngstrom;
+const double kKg = 1. / 9.10938291e-31;
+const double kNewton = kJoule / kMeter;
+const double kSec = sqrt((kKg * kMeter) / kNewton);
+const double kFs = kSec * 1.0e-15;
+const double kTesla2au = 1. / 2.3505175675871e5;
+const double kBohr2cm = 5.291772109038e-9;
+
+thread_local std::string g_err;
+
+int err(int code, const std::string& m) {
+  g_err = m;
+  return code;
+}
+
+bool exists(const std::string& name) {
+  struct stat b;
+  return stat(name.c_str(), &b) == 0;
+}
+
+std::string trim(std::string s) {
+  s.erase(0, s.find_first_not_of(" "));
+  size_t p = s.find_last_not_of(" \n\r\t");
+  return p == std::string::npos ? std::string() : s.erase(p + 1);
+}
+
+// parameters::map_input (parameters.cpp:591-623), including its key = substr(0, '=' - 1) convention
+std::map<std::string, std::string> map_input(std::istream& fin) {
+  std::map<std::string, std::string> param;
+  bool b_join = false, b_joined = false, b_will_join = false;
+  std::string last_key;
+  for (std::string line; std::getline(fin, line);) {
+    b_will_join = false;
+    b_joined = false;
+    std::string line2 = trim(line);
+    if (!line.empty() && line[0] == '#') continue;
+    if (!line2.empty() && line2[line2.length() - 1] == '\\') {
+      b_will_join = true;
+      line2[line2.length() - 1] = ' ';
+    }
+    if (b_join) {
+      param[last_key] += " " + line2;
+      b_joined = true;
+    }
+    b_join = b_will_join;
+    if (!b_joined) {
+      size_t eq = line2.find('=');
+      if (eq == std::string::npos) continue;
+      last_key = trim(line2.substr(0, eq == 0 ? 0 : eq - 1));
+      param[last_key] = trim(line2.substr(eq + 1, line2.length() - eq - 1));
+    }
+  }
+  return param;
+}
+
+double pget(const std::map<std::string, std::string>& m, const std::string& key, double def, double unit = 1) {
+  auto it = m.find(key);
+  if (it == m.end()) return def * unit;
+  return atof(it->second.c_str()) * unit;
+}
+std::string sget(const std::map<std::string, std::string>& m, const std::string& key, const std::string& def) {
+  auto it = m.find(key);
+  return it == m.end() ? def : it->second;
+}
+
+// electron::fermi (electron.h:119-124)
+double fermi(double t, double mu, double e) {
+  double ebyt = (e - mu) / t;
+  if (ebyt < -46) return 1;
+  else if (ebyt > 46) return 0;
+  else return 1. / (exp(ebyt) + 1);
+}
+
+struct zc {
+  double x, y;
+};
+inline zc zmul(zc a, zc b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+inline zc zadd(zc a, zc b) { return {a.x + b.x, a.y + b.y}; }
+inline zc zscale(double s, zc a) { return {a.x * s, a.y * s}; }
+inline zc zconj(zc a) { return {a.x, -a.y}; }
+inline zc zcis(double x) {
+  return {cos(x), sin(x)};
+}
+
+bool read_file(const std::string& path, size_t expect, void* dst, std::string& why) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) {
+    why = path + " does not exist";
+    return false;
+  }
+  fseek(f, 0L, SEEK_END);
+  size_t sz = (size_t)ftell(f);
+  rewind(f);
+  if (sz != expect) {
+    fclose(f);
+    why = path + " size does not match expected size (" + std::to_string(sz) + " vs " + std::to_string(expect) + ")";
+    return false;
+  }
+  size_t got = expect ? fread(dst, 1, expect, f) : 0;
+  fclose(f);
+  if (got != expect) {
+    why = path + " short read";
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+struct dmdh_system {
+  std::map<std::string, std::string> pm;
+  dmdh_info info;
+  std::vector<double> e_dm, f_dm;
+  std::vector<double> smat;         // complex [nk][3][nb_dm^2]
+  std::vector<uint64_t> k1, k2;
+  std::vector<double> P1, P2;       // complex [nkpair][nb^4], folded
+  std::vector<double> dm0;          // complex [nk][nb_dm^2]
+  std::vector<double> H;            // complex [nk][nb_dm^2] or empty
+};
+
+extern "C" {
+
+const char* dmdh_error(void) { return g_err.c_str(); }
+
+int dmdh_fermi(double T, double mu, const double* e, double* f, size_t n) {
+  if ((!e || !f) && n) return DMD_E_ARG;
+  for (size_t i = 0; i < n; ++i) f[i] = fermi(T, mu, e[i]);
+  return DMD_OK;
+}
+
+int dmdh_dm_bpert(int32_t nk, int32_t nb, const double* smat, const double* e, const double* f, double T,
+                  const double Bpert[3], double t0, int32_t picture, double* dm) {
+  if (nk <= 0 || nb <= 0 || !smat || !e || !f || !Bpert || !dm) return DMD_E_ARG;
+  const double degthr = 1e-8;
+  std::vector<zc> tmp((size_t)nb * nb);
+  for (int ik = 0; ik < nk; ik++) {
+    const zc* sk = (const zc*)smat + (size_t)ik * 3 * nb * nb;
+    const double *ek = e + (size_t)ik * nb, *fk = f + (size_t)ik * nb;
+    for (auto& v : tmp) v = {0, 0};
+    for (int i = 0; i < nb; i++)
+      for (int j = i; j < nb; j++) {
+        zc H1 = zadd(zadd(zscale(Bpert[0], sk[i * nb + j]), zscale(Bpert[1], sk[nb * nb + i * nb + j])),
+                     zscale(Bpert[2], sk[2 * nb * nb + i * nb + j]));
+        double dfde;
+        if (fabs(ek[i] - ek[j]) < degthr) {
+          double favg = 0.5 * (fk[i] + fk[j]);
+          dfde = favg * (favg - 1.) / T;
+        } else {
+          dfde = (fk[i] - fk[j]) / (ek[i] - ek[j]);
+        }
+        tmp[i * nb + j] = zscale(dfde, H1);
+        if (i != j && picture == DMD_PICTURE_INTERACTION) tmp[i * nb + j] = zmul(tmp[i * nb + j], zcis((ek[i] - ek[j]) * t0));
+        if (i < j) tmp[j * nb + i] = zconj(tmp[i * nb + j]);
+      }
+    for (int i = 0; i < nb; i++) tmp[i * nb + i] = zadd(tmp[i * nb + i], zc{fk[i], 0});
+    // init_dm: Hermitian part (DenMat.cpp:74-78)
+    zc* o = (zc*)dm + (size_t)ik * nb * nb;
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < nb; j++) o[i * nb + j] = zscale(0.5, zadd(tmp[i * nb + j], zconj(tmp[j * nb + i])));
+  }
+  return DMD_OK;
+}
+
+int dmdh_H_BS(int32_t nk, int32_t nb, const double* smat, const double B[3], const double* e, int32_t picture,
+              double* H) {
+  if (nk <= 0 || nb <= 0 || !smat || !B || !H) return DMD_E_ARG;
+  for (int ik = 0; ik < nk; ik++) {
+    const zc* sk = (const zc*)smat + (size_t)ik * 3 * nb * nb;
+    zc* h = (zc*)H + (size_t)ik * nb * nb;
+    for (int ij = 0; ij < nb * nb; ij++)
+      h[ij] = zadd(zadd(zscale(B[0], sk[ij]), zscale(B[1], sk[nb * nb + ij])), zscale(B[2], sk[2 * nb * nb + ij]));
+    if (picture == DMD_PICTURE_SCHRODINGER)
+      for (int i = 0; i < nb; i++) h[i * nb + i].x += e[(size_t)ik * nb + i];
+  }
+  return DMD_OK;
+}
+
+int dmdh_load(const char* dir_c, dmdh_system** out) {
+  if (!dir_c || !out) return err(DMD_E_ARG, "null argument");
+  *out = nullptr;
+  std::string dir(dir_c);
+  std::unique_ptr<dmdh_system> s(new dmdh_system());
+  dmdh_info& in = s->info;
+  memset(&in, 0, sizeof(in));
+  {
+    std::ifstream fin(dir + "/param.in");
+    if (!fin) return err(DMD_E_FILE, "input file param.in does not exist");
+    s->pm = map_input(fin);
+  }
+  auto& pm = s->pm;
+  // features outside this path are rejected explicitly
+  const char* unsupported[] = {"alg_linearize", "alg_linearize_dPee", "alg_phenom_relax", "alg_semiclassical",
+                               "alg_sparseP", "alg_Pin_is_sparse", "alg_only_eimp", "alg_only_ee", "needL",
+                               "alg_read_Bso", "gfac_normal_dist", "alg_ddmdteq"};
+  for (const char* k : unsupported)
+    if (pget(pm, k, 0) != 0) return err(DMD_E_ARG, std::string(k) + " is not supported by the GB300 path");
+  if (sget(pm, "code", "jdftx") != "jdftx" || sget(pm, "material_model", "none") != "none")
+    return err(DMD_E_ARG, "only code = jdftx, material_model = none");
+  if (pget(pm, "laserA", pget(pm, "pumpA0", 0)) > 0) return err(DMD_E_ARG, "laser is not supported");
+  if (sget(pm, "eeMode", "none") != "none" || sget(pm, "scrMode", "none") != "none")
+    return err(DMD_E_ARG, "model e-e / screening is not supported");
+  if (sget(pm, "alg_scatt", "lindblad") != "lindblad") return err(DMD_E_ARG, "alg_scatt must be lindblad");
+  if (pget(pm, "alg_eph_sepr_eh", 1) != 0 && pget(pm, "alg_eph_need_elec", 1) == 0)
+    return err(DMD_E_ARG, "hole-only e-ph data is not supported");
+  // ldbd_size.dat (electron.cpp:100-133, ElectronPhonon.cpp:132-177, parameters.cpp:7-23)
+  FILE* fp = fopen((dir + "/ldbd_data/ldbd_size.dat").c_str(), "r");
+  if (!fp) return err(DMD_E_FILE, "ldbd_data/ldbd_size.dat does not exist");
+  char line[512];
+  std::vector<std::string> lines;
+  while (fgets(line, sizeof line, fp)) lines.push_back(line);
+  fclose(fp);
+  if (lines.size() < 8) return err(DMD_E_FILE, "ldbd_size.dat is too short");
+  int nb, nv, bStart_dm, bEnd_dm, bStart_eph, bEnd_eph, i7, i8, i9;
+  if (sscanf(lines[1].c_str(), "%d %d %d %d %d %d %d %d %d", &nb, &nv, &bStart_dm, &bEnd_dm, &bStart_eph, &bEnd_eph, &i7,
+             &i8, &i9) < 6)
+    return err(DMD_E_FILE, "ldbd_size.dat line 2");
+  double nk_full;
+  int nk, km0, km1, km2;
+  if (sscanf(lines[2].c_str(), "%le %d %d %d %d", &nk_full, &nk, &km0, &km1, &km2) < 2)
+    return err(DMD_E_FILE, "ldbd_size.dat line 3");
+  int nkpair;
+  if (sscanf(lines[3].c_str(), "%d", &nkpair) != 1) return err(DMD_E_FILE, "ldbd_size.dat line 4");
+  double T, mu_min, mu_max, mu_file;
+  if (sscanf(lines[5].c_str(), "%le", &T) != 1) return err(DMD_E_FILE, "ldbd_size.dat line 6");
+  if (sscanf(lines[6].c_str(), "%lg %lg %lg", &mu_min, &mu_max, &mu_file) != 3) return err(DMD_E_FILE, "line 7");
+  if (nv < 0 || nv > nb || bStart_dm < 0 || bStart_dm > bEnd_dm || bEnd_dm > nb || bStart_eph < bStart_dm ||
+      bStart_eph > bEnd_eph || bEnd_eph > bEnd_dm || nk <= 0 || nkpair < 0)
+    return err(DMD_E_FILE, "inconsistent band ranges in ldbd_size.dat");
+  const int nb_dm = bEnd_dm - bStart_dm;
+  const int bs = bStart_eph - bStart_dm, be = bEnd_eph - bStart_dm, nbw = be - bs;
+  if (nb_dm > 8 || nbw < 1 || nbw > 4) return err(DMD_E_ARG, "band counts out of the supported range");
+  in.nk = nk;
+  in.nb_dm = nb_dm;
+  in.bstart = bs;
+  in.bend = be;
+  in.nb_total = nb;
+  in.nv_dm = std::max(nv - bStart_dm, 0);  // electron.cpp:114
+  in.nkpair = nkpair;
+  in.nk_full = nk_full;
+  in.temperature = T;
+  in.mu = pget(pm, "mu", mu_file / kEV, kEV);
+  in.prefac_eph = 2 * M_PI / nk_full;
+  // lattice (lattice.h:15-56)
+  int dim = 3;
+  double R[3][3] = {{0}};
+  if (FILE* fr = fopen((dir + "/ldbd_data/ldbd_R.dat").c_str(), "r")) {
+    if (fscanf(fr, "%d", &dim) != 1) dim = 3;
+    for (int i = 0; i < 3; i++)
+      if (fscanf(fr, "%lf %lf %lf", &R[i][0], &R[i][1], &R[i][2]) != 3) { fclose(fr); return err(DMD_E_FILE, "ldbd_R.dat"); }
+    fclose(fr);
+  } else {
+    return err(DMD_E_FILE, "ldbd_data/ldbd_R.dat does not exist");
+  }
+  dim = (int)pget(pm, "dim", dim);
+  // det(R) = box(row0, row1, row2) = dot(row0, cross(row1, row2)) (comm/matrix3.h:276, vector3.h:117-126)
+  const double cx = R[1][1] * R[2][2] - R[1][2] * R[2][1], cy = R[1][2] * R[2][0] - R[1][0] * R[2][2],
+               cz = R[1][0] * R[2][1] - R[1][1] * R[2][0];
+  const double volume = fabs(R[0][0] * cx + R[0][1] * cy + R[0][2] * cz);
+  double cell = volume;
+  if (dim == 2) cell = volume / R[2][2];
+  if (dim == 1) cell = R[2][2];
+  if (dim == 0) cell = 1;
+  if (dim == 2 && pget(pm, "thickness", 0) > 1e-6) {
+    // thickness only affects 2D volume-normalised analysis, not the cell size of observables
+  }
+  in.cell_size = cell;
+  in.cell_size_cmd = cell * std::pow(kBohr2cm, dim);
+  in.ob_prefac = (1. / nk_full) / in.cell_size_cmd;
+  // energies and occupations (electron.cpp:171-207)
+  std::string why;
+  std::vector<double> e((size_t)nk * nb);
+  if (!read_file(dir + "/ldbd_data/ldbd_ek.bin", e.size() * 8, e.data(), why)) return err(DMD_E_FILE, why);
+  const double scissor = pget(pm, "scissor", 0, kEV);
+  if (scissor != 0)
+    for (int ik = 0; ik < nk; ik++)
+      for (int i = nv; i < nb; i++) e[(size_t)ik * nb + i] = 1 * e[(size_t)ik * nb + i] + scissor;
+  s->e_dm.resize((size_t)nk * nb_dm);
+  s->f_dm.resize((size_t)nk * nb_dm);
+  for (int ik = 0; ik < nk; ik++)
+    for (int b = 0; b < nb_dm; b++) {
+      s->e_dm[(size_t)ik * nb_dm + b] = e[(size_t)ik * nb + bStart_dm + b];
+      s->f_dm[(size_t)ik * nb_dm + b] = fermi(T, in.mu, e[(size_t)ik * nb + bStart_dm + b]);
+    }
+  // spin matrices (electron.cpp:284-314)
+  s->smat.resize((size_t)nk * 3 * nb_dm * nb_dm * 2);
+  if (!read_file(dir + "/ldbd_data/ldbd_smat.bin", s->smat.size() * 8, s->smat.data(), why)) return err(DMD_E_FILE, why);
+  if (pget(pm, "alg_set_scv_zero", 0) != 0) {
+    const int nvd = std::max(nv - bStart_dm, 0);
+    zc* sm = (zc*)s->smat.data();
+    for (size_t k = 0; k < (size_t)nk * 3; k++)
+      for (int i = 0; i < nvd; i++)
+        for (int j = nvd; j < nb_dm; j++) {
+          sm[k * nb_dm * nb_dm + i * nb_dm + j] = {0, 0};
+          sm[k * nb_dm * nb_dm + j * nb_dm + i] = {0, 0};
+        }
+  }
+  // k-pairs and P (ElectronPhonon.cpp:182-253)
+  s->k1.resize(nkpair);
+  s->k2.resize(nkpair);
+  if (!read_file(dir + "/ldbd_data/ldbd_kpair_k1st.bin", (size_t)nkpair * 8, s->k1.data(), why) ||
+      !read_file(dir + "/ldbd_data/ldbd_kpair_k2nd.bin", (size_t)nkpair * 8, s->k2.data(), why))
+    return err(DMD_E_FILE, why);
+  for (int p = 0; p < nkpair; p++)
+    if (s->k1[p] >= (uint64_t)nk || s->k2[p] >= (uint64_t)nk) return err(DMD_E_FILE, "k-pair index out of range");
+  const size_t np4 = (size_t)nkpair * nbw * nbw * nbw * nbw;
+  s->P1.assign(2 * np4, 0.0);
+  s->P2.assign(2 * np4, 0.0);
+  const double scale_scatt = pget(pm, "scale_scatt", 1.);
+  if (pget(pm, "alg_eph_enable", 1) != 0) {
+    if (!read_file(dir + "/ldbd_data/ldbd_P1_lindblad.bin", np4 * 16, s->P1.data(), why) ||
+        !read_file(dir + "/ldbd_data/ldbd_P2_lindblad.bin", np4 * 16, s->P2.data(), why))
+      return err(DMD_E_FILE, why);
+    const double scale_eph = pget(pm, "scale_eph", scale_scatt);
+    if (scale_eph != 1.)
+      for (size_t i = 0; i < 2 * np4; i++) {
+        s->P1[i] = s->P1[i] * scale_eph;
+        s->P2[i] = s->P2[i] * scale_eph;
+      }
+  }
+  // ab-initio e-imp operators, one per impurity_density{,2,3,...} (parameters.cpp:213-228)
+  const double scale_ei = pget(pm, "scale_ei", scale_scatt);
+  std::vector<double> A1, A2;
+  in.eimp_fraction = 0;
+  for (int iD = 0;; iD++) {
+    const std::string nm = iD == 0 ? "" : std::to_string(iD + 1);
+    const double ni = pget(pm, "impurity_density" + nm, 0, std::pow(kBohr2cm, dim));
+    if (ni == 0) break;
+    if (sget(pm, "impMode" + nm, "model_ionized") != "ab_neutral")
+      return err(DMD_E_ARG, "only impMode = ab_neutral is supported");
+    const double fraction = fabs(ni * cell);  // electronimpurity ctor (ElectronImpurity.h:18)
+    if (iD == 0) in.eimp_fraction = fraction;
+    A1.assign(2 * np4, 0.0);
+    A2.assign(2 * np4, 0.0);
+    const std::string sfx = "_D" + std::to_string(iD + 1);
+    if (!read_file(dir + "/ldbd_data/ldbd_P1_lindblad" + sfx + ".bin", np4 * 16, A1.data(), why) ||
+        !read_file(dir + "/ldbd_data/ldbd_P2_lindblad" + sfx + ".bin", np4 * 16, A2.data(), why))
+      return err(DMD_E_FILE, why);
+    for (size_t i = 0; i < 2 * np4; i++) {
+      double a1 = A1[i] * fraction, a2 = A2[i] * fraction;
+      if (scale_ei != 1.) {
+        a1 = a1 * scale_ei;
+        a2 = a2 * scale_ei;
+      }
+      s->P1[i] = s->P1[i] + a1;
+      s->P2[i] = s->P2[i] + a2;
+    }
+  }
+  // time and picture parameters (parameters.cpp:99-106, 283-336, 359-367)
+  const std::string pic = sget(pm, "alg_picture", "interaction");
+  in.picture = (pic == "schrodinger" || pic == "non-interaction") ? DMD_PICTURE_SCHRODINGER : DMD_PICTURE_INTERACTION;
+  in.expt = (int)pget(pm, "alg_expt", 1);
+  if (in.picture == DMD_PICTURE_SCHRODINGER && in.expt) return err(DMD_E_ARG, "in schrodinger picture, alg_expt must be false");
+  const bool restart = pget(pm, "restart", 0) != 0;
+  in.t0 = pget(pm, "t0", 0., kFs);
+  if (restart) {
+    FILE* ft = fopen((dir + "/restart/time_restart.dat").c_str(), "r");
+    if (!ft) return err(DMD_E_FILE, "restart needs restart/time_restart.dat");
+    if (fscanf(ft, "%le", &in.t0) != 1) { fclose(ft); return err(DMD_E_FILE, "time_restart.dat"); }
+    fclose(ft);
+  }
+  in.tend = pget(pm, "tend", 0., kFs);
+  in.tstep = pget(pm, "tstep", 1., kFs);
+  in.ode_hstart = pget(pm, "ode_hstart", 1e-3, kFs);
+  in.ode_hmin = pget(pm, "ode_hmin", 0, kFs);
+  in.ode_hmax = pget(pm, "ode_hmax", in.tstep / kFs, kFs);
+  in.ode_epsabs = pget(pm, "ode_epsabs", 1e-8);
+  const std::string om = sget(pm, "alg_ode_method", "rkf45");
+  in.ode_method = om == "rkf45" ? 0 : om == "euler" ? 1 : om == "rk4" ? 2 : -1;
+  if (in.ode_method < 0) return err(DMD_E_ARG, "alg_ode_method must be rkf45, euler or rk4");
+  in.Bpert[0] = pget(pm, "Bxpert", 0., kTesla2au);
+  in.Bpert[1] = pget(pm, "Bypert", 0., kTesla2au);
+  in.Bpert[2] = pget(pm, "Bzpert", 0., kTesla2au);
+  in.B[0] = pget(pm, "Bx", 0., kTesla2au);
+  in.B[1] = pget(pm, "By", 0., kTesla2au);
+  in.B[2] = pget(pm, "Bz", 0., kTesla2au);
+  // initial density matrix (electron.cpp:62-98, DenMat.cpp:65-81, 301-317)
+  s->dm0.resize((size_t)nk * nb_dm * nb_dm * 2);
+  if (restart) {
+    if (!read_file(dir + "/restart/denmat_restart.bin", s->dm0.size() * 8, s->dm0.data(), why)) return err(DMD_E_FILE, why);
+  } else {
+    int rc = dmdh_dm_bpert(nk, nb_dm, s->smat.data(), s->e_dm.data(), s->f_dm.data(), T, in.Bpert, in.t0, in.picture,
+                           s->dm0.data());
+    if (rc) return err(rc, "dm_Bpert");
+  }
+  // coherent Hamiltonian (main.cpp:51)
+  const double Blen = sqrt(in.B[0] * in.B[0] + in.B[1] * in.B[1] + in.B[2] * in.B[2]);
+  if (Blen > 1e-10) {
+    s->H.resize((size_t)nk * nb_dm * nb_dm * 2);
+    dmdh_H_BS(nk, nb_dm, s->smat.data(), in.B, s->e_dm.data(), in.picture, s->H.data());
+    in.has_H = 1;
+  }
+  *out = s.release();
+  return DMD_OK;
+}
+
+void dmdh_free(dmdh_system* s) { delete s; }
+
+int dmdh_info_get(const dmdh_system* s, dmdh_info* info) {
+  if (!s || !info) return DMD_E_ARG;
+  *info = s->info;
+  return DMD_OK;
+}
+
+int dmdh_desc(const dmdh_system* s, int32_t precision, int32_t device, dmd_desc* d) {
+  if (!s || !d) return DMD_E_ARG;
+  memset(d, 0, sizeof(*d));
+  d->nk = s->info.nk;
+  d->nb_dm = s->info.nb_dm;
+  d->bstart = s->info.bstart;
+  d->bend = s->info.bend;
+  d->nkpair = s->info.nkpair;
+  d->prefac_eph = s->info.prefac_eph;
+  d->e_dm = s->e_dm.data();
+  d->k1st = s->k1.data();
+  d->k2nd = s->k2.data();
+  d->P1 = s->P1.data();
+  d->P2 = s->P2.data();
+  d->Hcoh = s->H.empty() ? nullptr : s->H.data();
+  d->picture = s->info.picture;
+  d->expt = s->info.expt;
+  d->precision = precision;
+  d->device = device;
+  return DMD_OK;
+}
+
+int dmdh_get_dm0(const dmdh_system* s, double* dm0) {
+  if (!s || !dm0) return DMD_E_ARG;
+  memcpy(dm0, s->dm0.data(), s->dm0.size() * 8);
+  return DMD_OK;
+}
+int dmdh_get_f(const dmdh_system* s, double* f) {
+  if (!s || !f) return DMD_E_ARG;
+  memcpy(f, s->f_dm.data(), s->f_dm.size() * 8);
+  return DMD_OK;
+}
+int dmdh_get_smat(const dmdh_system* s, double* smat) {
+  if (!s || !smat) return DMD_E_ARG;
+  memcpy(smat, s->smat.data(), s->smat.size() * 8);
+  return DMD_OK;
+}
+
+int dmdh_param(const dmdh_system* s, const char* key, double unit, double* value, int* found) {
+  if (!s || !key || !value || !found) return DMD_E_ARG;
+  auto it = s->pm.find(key);
+  *found = it != s->pm.end();
+  *value = *found ? atof(it->second.c_str()) * unit : 0;
+  return DMD_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// DMD's time loop on the GPU (main.cpp:38-84, DensityMatrix_Dynamics.h:177-225, 322-345)
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+struct Reporter {
+  std::string dir;
+  int nv_dm, nb_dm;
+  dmd_handle* h;
+  // observable.h:169-183 (header) and 368-383 (one line per output step)
+  int write_line(const std::string& what, const std::string& scarr, double t, double tot, double amp) {
+    const std::string fname = dir + "/" + what + scarr + "_tot.out";
+    const bool fresh = !exists(fname);
+    FILE* f = fopen(fname.c_str(), "a");
+    if (!f) return err(DMD_E_FILE, "cannot write " + fname);
+    if (fresh) fprintf(f, "#time(au), s(t), s(t) without exp(iwt)\n");
+    if (fabs(t) < 1e-30) fprintf(f, " 0.00000000000000e+01 %21.14le", tot);
+    else fprintf(f, "%21.14le %21.14le", t, tot);
+    fprintf(f, " %21.14le\n", amp);
+    fclose(f);
+    return DMD_OK;
+  }
+  int report(int it, double t, std::vector<double>& ybuf) {
+    int rc;
+    if (it > 0) {  // singdenmat_k::write_dm_tofile (DenMat.cpp:318-334), written to a temp name then renamed
+      double tt;
+      if ((rc = dmd_get_state(h, &tt, ybuf.data()))) return err(rc, dmd_last_error(h));
+      const std::string rb = dir + "/restart/denmat_restart.bin", rt = dir + "/restart/time_restart.dat";
+      FILE* fb = fopen((rb + ".tmp").c_str(), "wb");
+      FILE* ft = fopen((rt + ".tmp").c_str(), "w");
+      if (!fb || !ft) {
+        if (fb) fclose(fb);
+        if (ft) fclose(ft);
+        return err(DMD_E_FILE, "cannot write restart files");
+      }
+      fwrite(ybuf.data(), 8, ybuf.size(), fb);
+      fprintf(ft, "%14.7le", t);
+      fclose(fb);
+      fclose(ft);
+      rename((rb + ".tmp").c_str(), rb.c_str());
+      rename((rt + ".tmp").c_str(), rt.c_str());
+    }
+    const char* names[3] = {"sx", "sy", "sz"};
+    for (int d = 0; d < 3; ++d) {
+      double tot, amp;
+      if (nb_dm > nv_dm) {
+        if ((rc = dmd_measure(h, d, nv_dm, nb_dm, &tot, &amp))) return err(rc, dmd_last_error(h));
+        if ((rc = write_line(names[d], "_elec", t, tot, amp))) return rc;
+      }
+      if (nv_dm > 0) {
+        if ((rc = dmd_measure(h, d, 0, nv_dm, &tot, &amp))) return err(rc, dmd_last_error(h));
+        if ((rc = write_line(names[d], "_hole", t, tot, amp))) return rc;
+      }
+    }
+    return DMD_OK;
+  }
+};
+
+}  // namespace
+
+extern "C" int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max) {
+  dmdh_system* s = nullptr;
+  int rc = dmdh_load(dir, &s);
+  if (rc) return rc;
+  std::unique_ptr<dmdh_system> guard(s);
+  const dmdh_info& in = s->info;
+  dmd_desc d;
+  dmdh_desc(s, precision, 0, &d);
+  dmd_handle* h = nullptr;
+  if ((rc = dmd_create(&d, &h))) return err(rc, "dmd_create failed");
+  struct Closer {
+    dmd_handle* h;
+    ~Closer() { dmd_destroy(h); }
+  } closer{h};
+  const size_t ny = (size_t)in.nk * in.nb_dm * in.nb_dm * 2;
+  std::vector<double> ybuf(ny);
+  if ((rc = dmd_set_state(h, in.t0, s->dm0.data()))) return err(rc, dmd_last_error(h));
+  std::vector<double> obs((size_t)in.nk * in.nb_dm * in.nb_dm * 2);
+  const size_t nd2 = (size_t)in.nb_dm * in.nb_dm;
+  for (int dirn = 0; dirn < 3; ++dirn) {
+    for (int ik = 0; ik < in.nk; ++ik)
+      memcpy(&obs[(size_t)ik * nd2 * 2], &s->smat[((size_t)ik * 3 + dirn) * nd2 * 2], nd2 * 16);
+    if ((rc = dmd_set_observable(h, dirn, obs.data(), s->f_dm.data(), in.ob_prefac))) return err(rc, dmd_last_error(h));
+  }
+  mkdir((std::string(dir) + "/restart").c_str(), 0755);
+  Reporter rep{dir, in.nv_dm, in.nb_dm, h};
+  if ((rc = rep.report(0, in.t0, ybuf))) return rc;
+  double t = in.t0, ti = in.t0, hs = in.ode_hstart;
+  const std::string stopfile = std::string(dir) + "/EXIT_DMD";
+  for (int64_t it = 1; t < in.tend && (nsteps_max < 0 || it <= nsteps_max); ++it) {
+    if (exists(stopfile)) {  // "touch EXIT_DMD" clean exit (DensityMatrix_Dynamics.h:244)
+      remove(stopfile.c_str());
+      break;
+    }
+    ti += in.tstep;
+    int64_t nfev = 0;
+    if (in.ode_method == 0) rc = dmd_rkf45_apply(h, ti, &hs, in.ode_hmin, in.ode_hmax, in.ode_epsabs, 0.0, &nfev);
+    else if (in.ode_method == 1) rc = dmd_euler(h, in.tstep, 1), nfev = 1;
+    else rc = dmd_rk4(h, in.tstep, 1), nfev = 4;
+    if (rc) return err(rc, dmd_last_error(h));
+    if ((rc = dmd_get_state(h, &t, nullptr))) return err(rc, dmd_last_error(h));
+    if ((rc = rep.report((int)it, t, ybuf))) return rc;
+    printf("ncalls= %lld at ti= %lg fs\n", (long long)nfev, ti / kFs);
+    fflush(stdout);
+  }
+  return DMD_OK;
+}

@@ -38,7 +38,8 @@ _L = None
 
 EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_set_ddmdt_eq", "dmd_func",
            "dmd_evolve_driver", "dmd_evolve_coh", "dmd_set_state", "dmd_get_state", "dmd_rk4", "dmd_euler",
-           "dmd_rkf45_apply", "dmd_set_observable", "dmd_measure", "dmd_launch_count", "dmd_sync"]
+           "dmd_rkf45_apply", "dmd_set_observable", "dmd_measure", "dmd_launch_count", "dmd_sync",
+           "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get"]
 
 
 def _lib():
@@ -68,6 +69,11 @@ def _lib():
         L.dmd_measure.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(d), C.POINTER(d)]
         L.dmd_launch_count.argtypes = [vp, C.POINTER(i64)]
         L.dmd_sync.argtypes = [vp]
+        L.dmd_pinned_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
+        L.dmd_pinned_free.argtypes = [vp]
+        L.dmd_timer.argtypes = [vp, C.c_int, C.POINTER(d)]
+        L.dmd_set_profiling.argtypes = [vp, C.c_int]
+        L.dmd_profile_get.argtypes = [vp, C.c_int, C.POINTER(d), C.POINTER(i64)]
         _L = L
     return _L
 
@@ -198,3 +204,38 @@ class LindbladGPU:
 
     def sync(self):
         self._ck(_lib().dmd_sync(self._h))
+
+    def timer_start(self):
+        self._ck(_lib().dmd_timer(self._h, 0, None))
+
+    def timer_stop(self):
+        ms = C.c_double()
+        self._ck(_lib().dmd_timer(self._h, 1, C.byref(ms)))
+        return ms.value
+
+    def set_profiling(self, on):
+        self._ck(_lib().dmd_set_profiling(self._h, 1 if on else 0))
+
+    def profile(self, cls):
+        ms, n = C.c_double(), C.c_int64()
+        self._ck(_lib().dmd_profile_get(self._h, cls, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+
+class PinnedArray:
+    """Page-locked host float64 buffer (cudaHostAlloc) exposed as a numpy array."""
+
+    def __init__(self, n):
+        p = C.c_void_p()
+        st = _lib().dmd_pinned_alloc(int(n) * 8, C.byref(p))
+        if st != 0:
+            raise DMDError(st, "dmd_pinned_alloc")
+        self._p = p
+        buf = (C.c_double * int(n)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=np.float64, count=int(n))
+
+    def free(self):
+        if self._p:
+            self.array = None
+            _lib().dmd_pinned_free(self._p)
+            self._p = None

@@ -1,0 +1,159 @@
+"""Python binding of the host library (include/dmd_host.h): DMD's input readers, set-up and run
+driver in C++, feeding the GPU ABI."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import HOST_LIB
+from . import dmd as _dmd
+
+_L = None
+
+EXPORTS = ["dmdh_load", "dmdh_free", "dmdh_error", "dmdh_info_get", "dmdh_desc", "dmdh_get_dm0", "dmdh_get_f",
+           "dmdh_get_smat", "dmdh_param", "dmdh_fermi", "dmdh_dm_bpert", "dmdh_H_BS", "dmdh_run"]
+
+
+class Info(C.Structure):
+    _fields_ = [("nk", C.c_int32), ("nb_dm", C.c_int32), ("bstart", C.c_int32), ("bend", C.c_int32),
+                ("nb_total", C.c_int32), ("nv_dm", C.c_int32), ("nkpair", C.c_int64), ("nk_full", C.c_double),
+                ("temperature", C.c_double), ("mu", C.c_double), ("prefac_eph", C.c_double), ("cell_size", C.c_double),
+                ("cell_size_cmd", C.c_double), ("ob_prefac", C.c_double), ("t0", C.c_double), ("tend", C.c_double),
+                ("tstep", C.c_double), ("ode_hstart", C.c_double), ("ode_hmin", C.c_double), ("ode_hmax", C.c_double),
+                ("ode_epsabs", C.c_double), ("Bpert", C.c_double * 3), ("B", C.c_double * 3), ("picture", C.c_int32),
+                ("expt", C.c_int32), ("has_H", C.c_int32), ("ode_method", C.c_int32), ("eimp_fraction", C.c_double)]
+
+
+def _lib():
+    global _L
+    if _L is None:
+        if not os.path.exists(HOST_LIB):
+            raise RuntimeError("libdmdhost.so is not built (call __graft_entry__.build())")
+        L = C.CDLL(HOST_LIB)
+        vp, d = C.c_void_p, C.c_double
+        L.dmdh_load.argtypes = [C.c_char_p, C.POINTER(vp)]
+        L.dmdh_free.argtypes = [vp]
+        L.dmdh_free.restype = None
+        L.dmdh_error.restype = C.c_char_p
+        L.dmdh_info_get.argtypes = [vp, C.POINTER(Info)]
+        L.dmdh_desc.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(_dmd._Desc)]
+        L.dmdh_get_dm0.argtypes = [vp, vp]
+        L.dmdh_get_f.argtypes = [vp, vp]
+        L.dmdh_get_smat.argtypes = [vp, vp]
+        L.dmdh_param.argtypes = [vp, C.c_char_p, d, C.POINTER(d), C.POINTER(C.c_int)]
+        L.dmdh_fermi.argtypes = [d, d, vp, vp, C.c_size_t]
+        L.dmdh_dm_bpert.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, d, vp, d, C.c_int32, vp]
+        L.dmdh_H_BS.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, C.c_int32, vp]
+        L.dmdh_run.argtypes = [C.c_char_p, C.c_int32, C.c_int64]
+        _L = L
+    return _L
+
+
+def _ck(st):
+    if st != 0:
+        raise RuntimeError("dmd host status %d: %s" % (st, _lib().dmdh_error().decode()))
+
+
+def _arr(ptr, n, dtype):
+    if not ptr or n == 0:
+        return np.zeros(0, dtype)
+    buf = (C.c_char * (n * np.dtype(dtype).itemsize)).from_address(ptr)
+    return np.frombuffer(buf, dtype=dtype, count=n)
+
+
+class System:
+    """A DMD input directory loaded and set up by the C++ host library."""
+
+    def __init__(self, directory: str):
+        h = C.c_void_p()
+        _ck(_lib().dmdh_load(directory.encode(), C.byref(h)))
+        self._h = h
+        self.info = Info()
+        _ck(_lib().dmdh_info_get(h, C.byref(self.info)))
+        i = self.info
+        self.nk, self.nb_dm = i.nk, i.nb_dm
+        nd2 = i.nb_dm * i.nb_dm
+        self.dm0 = np.zeros((i.nk, nd2), np.complex128)
+        _ck(_lib().dmdh_get_dm0(h, self.dm0.ctypes.data))
+        self.f_dm = np.zeros((i.nk, i.nb_dm), np.float64)
+        _ck(_lib().dmdh_get_f(h, self.f_dm.ctypes.data))
+        self.smat = np.zeros((i.nk, 3, nd2), np.complex128)
+        _ck(_lib().dmdh_get_smat(h, self.smat.ctypes.data))
+        desc = self.desc()
+        nb = i.bend - i.bstart
+        n4 = int(i.nkpair) * nb ** 4
+        self.e_dm = _arr(desc.e_dm, i.nk * i.nb_dm, np.float64).reshape(i.nk, i.nb_dm)
+        self.k1st = _arr(desc.k1st, int(i.nkpair), np.uint64)
+        self.k2nd = _arr(desc.k2nd, int(i.nkpair), np.uint64)
+        self.P1 = _arr(desc.P1, n4, np.complex128)
+        self.P2 = _arr(desc.P2, n4, np.complex128)
+        self.Hcoh = _arr(desc.Hcoh, i.nk * nd2, np.complex128).reshape(i.nk, nd2) if desc.Hcoh else None
+
+    def desc(self, precision="f64", device=0):
+        d = _dmd._Desc()
+        p = _dmd.PREC[precision] if isinstance(precision, str) else int(precision)
+        _ck(_lib().dmdh_desc(self._h, p, device, C.byref(d)))
+        return d
+
+    def y0(self):
+        return np.ascontiguousarray(self.dm0).view(np.float64).reshape(-1).copy()
+
+    def param(self, key, unit=1.0):
+        v, f = C.c_double(), C.c_int()
+        _ck(_lib().dmdh_param(self._h, key.encode(), unit, C.byref(v), C.byref(f)))
+        return v.value if f.value else None
+
+    def gpu(self, precision="f64", device=0):
+        """A LindbladGPU built from this system (dmd_create on the loaded arrays)."""
+        i = self.info
+        return _dmd.LindbladGPU(nk=i.nk, nb_dm=i.nb_dm, bstart=i.bstart, bend=i.bend, e_dm=self.e_dm,
+                                k1st=self.k1st, k2nd=self.k2nd, P1=self.P1, P2=self.P2, prefac_eph=i.prefac_eph,
+                                Hcoh=self.Hcoh, picture=i.picture, expt=i.expt, precision=precision, device=device)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib().dmdh_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fermi(T, mu, e):
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    f = np.empty_like(e)
+    _ck(_lib().dmdh_fermi(T, mu, e.ctypes.data, f.ctypes.data, e.size))
+    return f
+
+
+def dm_bpert(smat, e, f, T, Bpert, t0=0.0, picture=0):
+    smat = np.ascontiguousarray(smat, dtype=np.complex128)
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    nk, nb = e.shape
+    B = np.ascontiguousarray(Bpert, dtype=np.float64)
+    dm = np.zeros((nk, nb * nb), np.complex128)
+    _ck(_lib().dmdh_dm_bpert(nk, nb, smat.ctypes.data, e.ctypes.data, f.ctypes.data, T, B.ctypes.data, t0, picture,
+                             dm.ctypes.data))
+    return dm
+
+
+def H_BS(smat, B, e, picture=0):
+    smat = np.ascontiguousarray(smat, dtype=np.complex128)
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    nk, nb = e.shape
+    Bv = np.ascontiguousarray(B, dtype=np.float64)
+    H = np.zeros((nk, nb * nb), np.complex128)
+    _ck(_lib().dmdh_H_BS(nk, nb, smat.ctypes.data, Bv.ctypes.data, e.ctypes.data, picture, H.ctypes.data))
+    return H
+
+
+def run(directory: str, precision="f64", nsteps_max=-1):
+    """DMD's time loop (evolve_gsl / evolve_euler / RK4) on the GPU, writing the S files into directory."""
+    p = _dmd.PREC[precision] if isinstance(precision, str) else int(precision)
+    _ck(_lib().dmdh_run(directory.encode(), p, int(nsteps_max)))

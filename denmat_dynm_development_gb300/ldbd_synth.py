@@ -169,18 +169,15 @@ def _cgauss(rng, shape, sigma):
     return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) * (sigma / math.sqrt(2.0))
 
 
-def _outer_p1(a):
-    # P[(i1 i2),(i3 i4)] = A[i1,i3] conj(A[i2,i4])
-    n = a.shape[0]
-    nb = a.shape[1]
-    return np.einsum("nik,njl->nijkl", a, np.conj(a)).reshape(n, nb ** 4)
-
-
-def _outer_p2(a):
-    # P[(i1 i2),(i3 i4)] = A[i3,i1] conj(A[i4,i2])
-    n = a.shape[0]
-    nb = a.shape[1]
-    return np.einsum("nki,nlj->nijkl", a, np.conj(a)).reshape(n, nb ** 4)
+def _sum_outer(A, transpose):
+    """sum_m A_m[i1,i3] conj(A_m[i2,i4]) (P1 form) or sum_m A_m[i3,i1] conj(A_m[i4,i2]) (P2 form),
+    returned as [n][(i1*nb+i2)*nb*nb + i3*nb + i4]. A has shape (n, m, nb, nb)."""
+    n, m, nb, _ = A.shape
+    if transpose:
+        A = np.swapaxes(A, 2, 3)
+    X = A.reshape(n, m, nb * nb)                       # [n][m][(i1 i3)]
+    M = np.matmul(np.swapaxes(X, 1, 2), np.conj(X))    # [n][(i1 i3)][(i2 i4)]
+    return np.ascontiguousarray(M.reshape(n, nb, nb, nb, nb).transpose(0, 1, 3, 2, 4)).reshape(n, nb ** 4)
 
 
 def eph_chunk(cfg: SynthConfig, ek, ekp, omegas, chunk_index):
@@ -193,9 +190,10 @@ def eph_chunk(cfg: SynthConfig, ek, ekp, omegas, chunk_index):
     gsig = cfg.g_sigma_mev * 1e-3 * units.eV
     sq_delta = math.sqrt(1.0 / (sigma * math.sqrt(2.0 * math.pi)))
     dE = ek[:, :, None] - ekp[:, None, :]
-    P1 = np.zeros((n, nb ** 4), np.complex128)
-    P2 = np.zeros((n, nb ** 4), np.complex128)
-    for w in omegas:
+    nm = len(omegas)
+    A1 = np.empty((n, 2 * nm, nb, nb), np.complex128)   # App, Amm per mode (P1 terms)
+    A2 = np.empty((n, 2 * nm, nb, nb), np.complex128)   # Amp, Apm per mode (P2 terms)
+    for im, w in enumerate(omegas):
         nq = 1.0 / math.expm1(max(1e-3, w / T))
         gp = _cgauss(rng, (n, nb, nb), gsig)
         gm = _cgauss(rng, (n, nb, nb), gsig)
@@ -203,13 +201,11 @@ def eph_chunk(cfg: SynthConfig, ek, ekp, omegas, chunk_index):
         xm = dE - w
         G2p = np.where(np.abs(xp) < ethr, sq_delta * gp * np.exp(-xp * xp / (4.0 * sigma * sigma)), 0)
         G2m = np.where(np.abs(xm) < ethr, sq_delta * gm * np.exp(-xm * xm / (4.0 * sigma * sigma)), 0)
-        App = G2p * math.sqrt(nq + 1.0)
-        Apm = G2p * math.sqrt(nq)
-        Amp = G2m * math.sqrt(nq + 1.0)
-        Amm = G2m * math.sqrt(nq)
-        P1 += _outer_p1(App) + _outer_p1(Amm)
-        P2 += _outer_p2(Amp) + _outer_p2(Apm)
-    return P1, P2
+        A1[:, 2 * im] = G2p * math.sqrt(nq + 1.0)       # App
+        A1[:, 2 * im + 1] = G2m * math.sqrt(nq)         # Amm
+        A2[:, 2 * im] = G2m * math.sqrt(nq + 1.0)       # Amp
+        A2[:, 2 * im + 1] = G2p * math.sqrt(nq)         # Apm
+    return _sum_outer(A1, False), _sum_outer(A2, True)
 
 
 def eimp_chunk(cfg: SynthConfig, ek, ekp, chunk_index):
@@ -222,8 +218,8 @@ def eimp_chunk(cfg: SynthConfig, ek, ekp, chunk_index):
     sq_delta = math.sqrt(1.0 / (sigma * math.sqrt(2.0 * math.pi)))
     dE = ek[:, :, None] - ekp[:, None, :]
     g = _cgauss(rng, (n, nb, nb), gsig)
-    A = np.where(np.abs(dE) < ethr, sq_delta * g * np.exp(-dE * dE / (4.0 * sigma * sigma)), 0)
-    return _outer_p1(A), _outer_p2(A)
+    A = np.where(np.abs(dE) < ethr, sq_delta * g * np.exp(-dE * dE / (4.0 * sigma * sigma)), 0)[:, None]
+    return _sum_outer(A, False), _sum_outer(A, True)
 
 
 def mode_energies(cfg: SynthConfig):
@@ -232,71 +228,196 @@ def mode_energies(cfg: SynthConfig):
     return list(rng.uniform(lo, hi, cfg.nmodes) * 1e-3 * units.eV)
 
 
-def make_ldbd(outdir: str, cfg: SynthConfig, write_param: bool = True, **param_kw) -> SynthInfo:
-    """Write ``outdir/ldbd_data/*`` (and ``outdir/param.in``) for ``cfg``."""
-    d = os.path.join(outdir, "ldbd_data")
-    os.makedirs(d, exist_ok=True)
+@dataclass
+class SynthSetup:
+    cfg: SynthConfig
+    R: np.ndarray
+    V: float
+    n: int
+    kf: np.ndarray
+    e: np.ndarray          # [nk][nb_dm] all density-matrix bands
+    ew: np.ndarray         # [nk][nb] e-ph window
+    s: np.ndarray          # [nk][3][nb_dm^2]
+    k1: np.ndarray
+    k2: np.ndarray
+    omegas: list
+    T: float
+    mu: float
+
+    @property
+    def npair(self):
+        return int(self.k1.size)
+
+    def info(self):
+        return SynthInfo(nk=self.cfg.nk, nb=self.cfg.nb, npair=self.npair, nk_full=float(self.n) ** 3,
+                         kmesh=(self.n, self.n, self.n), cell_volume=self.V, temperature=self.T, mu=self.mu,
+                         mode_omega=self.omegas)
+
+    def chunk_size(self):
+        return self.cfg.chunk_pairs if self.cfg.nb == 2 else max(1, self.cfg.chunk_pairs // 8)
+
+
+def setup(cfg: SynthConfig) -> SynthSetup:
+    """k-points, bands, spin matrices, k-pairs and mode energies of a synthetic system."""
     rng = np.random.default_rng([cfg.seed, 0])
     R, V, n, kf, e0 = _kset(cfg, rng)
     e = _bands(cfg, e0, rng)
     s = _spin(cfg, cfg.nk, rng)
-    nx = cfg.extra_bands
-    ew = e[:, nx:]                    # energies of the e-ph window
+    ew = np.ascontiguousarray(e[:, cfg.extra_bands:])
     k1, k2 = _pairs(cfg, ew)
-    npair = int(k1.size)
-    omegas = mode_energies(cfg)
-    T = cfg.temperature_K * units.Kelvin
-    mu = ew.min() - cfg.mu_below_cbm_ev * units.eV
-    nb = cfg.nb
-    ndm = nb + nx
+    return SynthSetup(cfg=cfg, R=R, V=V, n=n, kf=kf, e=e, ew=ew, s=s, k1=k1, k2=k2, omegas=mode_energies(cfg),
+                      T=cfg.temperature_K * units.Kelvin, mu=ew.min() - cfg.mu_below_cbm_ev * units.eV)
 
+
+def _chunk(st: SynthSetup, ic: int):
+    C = st.chunk_size()
+    p0 = ic * C
+    p1 = min(st.npair, p0 + C)
+    ek = st.ew[st.k1[p0:p1].astype(np.int64)]
+    ekp = st.ew[st.k2[p0:p1].astype(np.int64)]
+    P1, P2 = eph_chunk(st.cfg, ek, ekp, st.omegas, ic)
+    Q = eimp_chunk(st.cfg, ek, ekp, ic) if st.cfg.eimp_sigma_mev is not None else None
+    return p0, p1, P1, P2, Q
+
+
+def pair_chunks(st: SynthSetup, threads: int = 1):
+    """Yield (p0, p1, P1, P2, (Q1, Q2) or None) in pair order, computed by a thread pool."""
+    nch = (st.npair + st.chunk_size() - 1) // st.chunk_size()
+    if threads <= 1:
+        for ic in range(nch):
+            yield _chunk(st, ic)
+        return
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        futs = {}
+        nxt = 0
+        for ic in range(nch):
+            while nxt < nch and nxt < ic + 2 * threads:
+                futs[nxt] = ex.submit(_chunk, st, nxt)
+                nxt += 1
+            yield futs.pop(ic).result()
+
+
+def _proc_chunk(args):
+    """Worker: one chunk of pairs written into shared memory (spawned process, numpy only)."""
+    from multiprocessing import shared_memory
+    cfg_d, ew, k1, k2, omegas, ic, p0, names, nb4, npair, fold = args
+    cfg = SynthConfig(**cfg_d)
+    ek = ew[k1.astype(np.int64)]
+    ekp = ew[k2.astype(np.int64)]
+    P1, P2 = eph_chunk(cfg, ek, ekp, omegas, ic)
+    Q = eimp_chunk(cfg, ek, ekp, ic) if cfg.eimp_sigma_mev is not None else None
+    if Q is not None and fold is not None:
+        P1 = P1 + Q[0] * fold
+        P2 = P2 + Q[1] * fold
+    outs = [P1, P2] + ([Q[0], Q[1]] if (Q is not None and fold is None) else [])
+    p1 = p0 + P1.shape[0]
+    for name, arr in zip(names, outs):
+        shm = shared_memory.SharedMemory(name=name)
+        try:
+            view = np.ndarray((npair, nb4), np.complex128, buffer=shm.buf)
+            view[p0:p1] = arr
+            del view
+        finally:
+            shm.close()
+    return ic
+
+
+def generate_arrays(cfg: SynthConfig, fold_fraction: Optional[float] = None, procs: Optional[int] = None):
+    """All arrays of a synthetic system in memory. With fold_fraction the e-imp operators are folded
+    into P as DMD does at set-up (P += fraction * P_D1); otherwise they are returned separately.
+    Chunks are computed by `procs` spawned worker processes into shared memory; the result does not
+    depend on the number of processes."""
+    st = setup(cfg)
+    procs = procs or min(16, os.cpu_count() or 1)
+    nb4 = cfg.nb ** 4
+    npair = st.npair
+    want_q = cfg.eimp_sigma_mev is not None and fold_fraction is None
+    if procs <= 1 or npair <= st.chunk_size():
+        P1 = np.empty((npair, nb4), np.complex128)
+        P2 = np.empty((npair, nb4), np.complex128)
+        Q1 = np.empty((npair, nb4), np.complex128) if want_q else None
+        Q2 = np.empty((npair, nb4), np.complex128) if want_q else None
+        for p0, p1, a1, a2, Q in pair_chunks(st, 1):
+            if Q is not None and fold_fraction is not None:
+                a1 = a1 + Q[0] * fold_fraction
+                a2 = a2 + Q[1] * fold_fraction
+            P1[p0:p1] = a1
+            P2[p0:p1] = a2
+            if want_q:
+                Q1[p0:p1] = Q[0]
+                Q2[p0:p1] = Q[1]
+        return st, P1, P2, Q1, Q2
+    import multiprocessing as mp
+    from multiprocessing import shared_memory
+    nbytes = npair * nb4 * 16
+    shms = [shared_memory.SharedMemory(create=True, size=max(nbytes, 1)) for _ in range(4 if want_q else 2)]
+    try:
+        C = st.chunk_size()
+        jobs = []
+        for ic, p0 in enumerate(range(0, npair, C)):
+            p1 = min(npair, p0 + C)
+            jobs.append((cfg.to_dict(), st.ew, st.k1[p0:p1], st.k2[p0:p1], st.omegas, ic, p0,
+                         [m.name for m in shms], nb4, npair, fold_fraction))
+        with mp.get_context("spawn").Pool(processes=procs) as pool:
+            for _ in pool.imap_unordered(_proc_chunk, jobs):
+                pass
+        outs = []
+        for m in shms:
+            outs.append(np.ndarray((npair, nb4), np.complex128, buffer=m.buf).copy())
+    finally:
+        for m in shms:
+            m.close()
+            m.unlink()
+    return (st, outs[0], outs[1], outs[2] if want_q else None, outs[3] if want_q else None)
+
+
+def make_ldbd(outdir: str, cfg: SynthConfig, write_param: bool = True, threads: int = 1, **param_kw) -> SynthInfo:
+    """Write ``outdir/ldbd_data/*`` (and ``outdir/param.in``) for ``cfg``."""
+    d = os.path.join(outdir, "ldbd_data")
+    os.makedirs(d, exist_ok=True)
+    st = setup(cfg)
+    e, R, n, nb, nx = st.e, st.R, st.n, cfg.nb, cfg.extra_bands
+    ndm = nb + nx
+    mu, T = st.mu, st.T
     with open(os.path.join(d, "ldbd_size.dat"), "w") as f:
         f.write("There are scatterings only for conduction electrons\n")
         f.write("%d 0 0 %d %d %d %d 0 0 # nb nv bBot_dm bTop_dm bBot_eph_elec bTop_eph_elec nb_wannier bBot_probe band_dft_skipped\n"
                 % (ndm, ndm, nx, ndm, ndm))
         f.write("%21.14le %d %d %d %d # nk_full nk kmesh\n" % (float(n) ** 3, cfg.nk, n, n, n))
-        f.write("%d # nkpair_elec\n" % npair)
+        f.write("%d # nkpair_elec\n" % st.npair)
         f.write("0 %d 0 0# modeStart modeStp modeSkipStart modeSkipStop\n" % cfg.nmodes)
         f.write("%21.14le # T\n" % T)
         f.write("%21.14le %21.14le %21.14le # muMin, muMax mu (given carrier density)\n" % (mu, mu, mu))
         f.write("%.17g %.17g # degauss\n" % (cfg.degauss_mev * 1e-3 * units.eV, cfg.ndegauss))
         f.write("%14.7le %14.7le %14.7le %14.7le %14.7le %14.7le # EBot_probe, ETop_probe, EBot_dm, ETop_dm, EBot_eph, ETop_eph\n"
                 % (e.min(), e.max(), e.min(), e.max(), e.min(), e.max()))
-        f.write("%14.7le # omegaMax" % max(omegas))
+        f.write("%14.7le # omegaMax" % max(st.omegas))
     with open(os.path.join(d, "ldbd_R.dat"), "w") as f:
         f.write("3\n")
         for i in range(3):
             f.write("%.17g %.17g %.17g\n" % tuple(R[i]))
-    kf.astype(np.float64).tofile(os.path.join(d, "ldbd_kvec.bin"))
+    st.kf.astype(np.float64).tofile(os.path.join(d, "ldbd_kvec.bin"))
     e.astype(np.float64).tofile(os.path.join(d, "ldbd_ek.bin"))
-    s.astype(np.complex128).tofile(os.path.join(d, "ldbd_smat.bin"))
-    k1.tofile(os.path.join(d, "ldbd_kpair_k1st.bin"))
-    k2.tofile(os.path.join(d, "ldbd_kpair_k2nd.bin"))
-
+    st.s.astype(np.complex128).tofile(os.path.join(d, "ldbd_smat.bin"))
+    st.k1.tofile(os.path.join(d, "ldbd_kpair_k1st.bin"))
+    st.k2.tofile(os.path.join(d, "ldbd_kpair_k2nd.bin"))
     names = [("ldbd_P1_lindblad.bin", "ldbd_P2_lindblad.bin")]
     if cfg.eimp_sigma_mev is not None:
         names.append(("ldbd_P1_lindblad_D1.bin", "ldbd_P2_lindblad_D1.bin"))
     files = [(open(os.path.join(d, a), "wb"), open(os.path.join(d, b), "wb")) for a, b in names]
     try:
-        C = cfg.chunk_pairs if nb == 2 else max(1, cfg.chunk_pairs // 8)
-        for ic, p0 in enumerate(range(0, npair, C)):
-            p1 = min(npair, p0 + C)
-            ek = ew[k1[p0:p1].astype(np.int64)]
-            ekp = ew[k2[p0:p1].astype(np.int64)]
-            P1, P2 = eph_chunk(cfg, ek, ekp, omegas, ic)
+        for p0, p1, P1, P2, Q in pair_chunks(st, threads):
             files[0][0].write(P1.tobytes())
             files[0][1].write(P2.tobytes())
-            if len(files) > 1:
-                Q1, Q2 = eimp_chunk(cfg, ek, ekp, ic)
-                files[1][0].write(Q1.tobytes())
-                files[1][1].write(Q2.tobytes())
+            if Q is not None:
+                files[1][0].write(Q[0].tobytes())
+                files[1][1].write(Q[1].tobytes())
     finally:
         for a, b in files:
             a.close()
             b.close()
-
-    info = SynthInfo(nk=cfg.nk, nb=nb, npair=npair, nk_full=float(n) ** 3, kmesh=(n, n, n),
-                     cell_volume=V, temperature=T, mu=mu, mode_omega=omegas)
+    info = st.info()
     if write_param:
         write_param_in(outdir, cfg, info, **param_kw)
     return info
@@ -342,7 +463,9 @@ WORKLOADS = {
     # Si-like plain FP64 case: nb=2, nk=500, ~50k pairs.
     "si_nk500": SynthConfig(nk=500, nb=2, de_pair_mev=60.0),
     # GaAs-like at scale: nb=2, nk=20k, ~10M pairs, e-ph + e-imp.
-    "gaas_nk20k": SynthConfig(nk=20000, nb=2, de_pair_mev=5.6, eimp_sigma_mev=5.0),
+    "gaas_nk20k": SynthConfig(nk=20000, nb=2, de_pair_mev=4.45, eimp_sigma_mev=5.0),
+    # the same generator at nk=8k (~1.6M pairs, P 0.8 GB): profiling-sized GaAs-like case
+    "gaas_nk8k": SynthConfig(nk=8000, nb=2, de_pair_mev=4.45, eimp_sigma_mev=5.0),
     # MoS2-like precision case: nb=4, nk=30k, ~4M pairs.
     "mos2_nk30k": SynthConfig(nk=30000, nb=4, de_pair_mev=3.9),
 }

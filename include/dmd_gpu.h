@@ -114,6 +114,20 @@ int dmd_launch_count(const dmd_handle* h, int64_t* launches);
 /* wait for the handle's stream */
 int dmd_sync(dmd_handle* h);
 
+/* page-locked host buffers for the host-buffer calls (cudaHostAlloc / cudaFreeHost) */
+int dmd_pinned_alloc(size_t bytes, void** out);
+int dmd_pinned_free(void* p);
+
+/* CUDA-event timing on the handle's stream: op 0 records the start event, op 1 records the stop
+ * event, waits for it and returns the elapsed milliseconds in *ms */
+int dmd_timer(dmd_handle* h, int op, double* ms);
+
+/* per-kernel profiling: while on, steppers launch kernels one by one (no graph) with CUDA events
+ * around each launch; dmd_profile_get returns the accumulated device time and launch count of
+ * kernel class 0 (prep), 1 (k-pair contraction), 2 (finish/stepper update), 3 (other) */
+int dmd_set_profiling(dmd_handle* h, int on);
+int dmd_profile_get(const dmd_handle* h, int kernel_class, double* total_ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,77 @@
+/* dmd_host.h -- host side of the GB300 DMD path: the reference's set-up and driver code restated in
+ * C++ on top of the GPU ABI (dmd_gpu.h). All arrays are caller-owned; complex128 is interleaved.
+ *
+ * Reference interfaces mirrored (file:line in the reference tree):
+ *   dmdh_parse_param     parameters::map_input / get (parameters.cpp:530-623)
+ *   dmdh_load            electron::read_ldbd_size/kvec/ek/smat (electron.cpp:100-314),
+ *                        electronphonon::get_brange/get_nkpair/read_ldbd_kpair/read_ldbd_eph
+ *                        (ElectronPhonon.cpp:132-253), electronimpurity::read_ldbd_imp_P
+ *                        (ElectronImpurity.cpp:3-49), lattice::read_ldbd_R (lattice.h:48-56),
+ *                        parameters::read_jdftx (parameters.cpp:7-23); file sizes are checked as
+ *                        check_file_size does (comm/myio.cpp:126-132) but reported as DMD_E_FILE
+ *   dmdh_fermi           electron::fermi (electron.h:119-124)
+ *   dmdh_dm_bpert        electron::compute_dm_Bpert_1st (electron.cpp:62-98) + singdenmat_k::init_dm
+ *                        (DenMat.cpp:65-81)
+ *   dmdh_H_BS            electron::set_H_BS (electron.cpp:19-42) + singdenmat_k::init_Hcoh (DenMat.cpp:7-28)
+ *   dmdh_run             dm_dynamics_jdftx + dm_dynamics::evolve_gsl / evolve_euler
+ *                        (main.cpp:38-84, DensityMatrix_Dynamics.h:177-225), S files as
+ *                        ob_1dmk::measure writes them (observable.h:145-193, 368-404)
+ */
+#ifndef DMD_HOST_H
+#define DMD_HOST_H
+#include <stddef.h>
+#include <stdint.h>
+
+#include "dmd_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dmdh_system dmdh_system;
+
+/* scalar set-up values of a loaded system */
+typedef struct dmdh_info {
+  int32_t nk, nb_dm, bstart, bend, nb_total, nv_dm; /* nv_dm = max(nv - bStart_dm, 0) */
+  int64_t nkpair;
+  double nk_full, temperature, mu, prefac_eph, cell_size, cell_size_cmd, ob_prefac;
+  double t0, tend, tstep;
+  double ode_hstart, ode_hmin, ode_hmax, ode_epsabs;
+  double Bpert[3], B[3];
+  int32_t picture, expt, has_H, ode_method; /* ode_method: 0 rkf45, 1 euler, 2 rk4 */
+  double eimp_fraction;
+} dmdh_info;
+
+/* Read param.in + ldbd_data/ from directory dir (the reference's working directory layout) and
+ * perform DMD's set-up: band windows, occupations, folded P (scale_eph and |n_i V| * D1), initial
+ * density matrix and coherent Hamiltonian. */
+int dmdh_load(const char* dir, dmdh_system** out);
+void dmdh_free(dmdh_system* s);
+const char* dmdh_error(void);
+int dmdh_info_get(const dmdh_system* s, dmdh_info* info);
+/* descriptor for dmd_create pointing into the loaded arrays (valid while s lives) */
+int dmdh_desc(const dmdh_system* s, int32_t precision, int32_t device, dmd_desc* d);
+/* copies of set-up arrays: dm0 (complex [nk][nb_dm^2]), f (double [nk][nb_dm]),
+ * spin matrices (complex [nk][3][nb_dm^2]) */
+int dmdh_get_dm0(const dmdh_system* s, double* dm0);
+int dmdh_get_f(const dmdh_system* s, double* f);
+int dmdh_get_smat(const dmdh_system* s, double* smat);
+
+/* value of a param.in key after get()'s unit conversion; returns 0 and *found = 1 if present */
+int dmdh_param(const dmdh_system* s, const char* key, double unit, double* value, int* found);
+
+/* stand-alone set-up pieces */
+int dmdh_fermi(double T, double mu, const double* e, double* f, size_t n);
+int dmdh_dm_bpert(int32_t nk, int32_t nb, const double* smat, const double* e, const double* f, double T,
+                  const double Bpert[3], double t0, int32_t picture, double* dm);
+int dmdh_H_BS(int32_t nk, int32_t nb, const double* smat, const double B[3], const double* e, int32_t picture,
+              double* H);
+
+/* DMD's time loop on the GPU: evolve_gsl (rkf45), evolve_euler, or fixed-step RK4, writing
+ * sx/sy/sz_elec_tot.out into dir after every output step. nsteps_max < 0 runs to tend. */
+int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -111,45 +111,54 @@ static void compute_Pt(int nb, double t, const double* ek, const double* ekp, co
   }
 }
 
-/* electronphonon::evolve -- evolve_eph.cpp:34-166 (summode, dense P, expt or not, optional ddmdteq;
- * no valley filtering: the default alg.only_intra/intervalley = false and fewer than two valleys
- * keep every pair, evolve_eph.cpp:52-58). e is the window energy array [nk][nb]. */
-void orc_evolve(const orc_sys* s, orc_ws* w, const double* e, double t, const zc* dm, const zc* dm1, zc* ddmdt_eph, int compute_eq) {
-  const int nk = s->nk, nb = s->bend - s->bstart, nb2 = nb * nb, nb4 = nb2 * nb2;
-  const zc c1 = zmk(1, 0), cm1 = zmk(-1, 0), c0 = zmk(0, 0);
-  memset(ddmdt_eph, 0, sizeof(zc) * nk * nb2);
-  memset(w->Pdm, 0, sizeof(zc) * nk * nb2);
-  memset(w->dm1P, 0, sizeof(zc) * nk * nb2);
-  for (int64_t ip = 0; ip < s->npair; ip++) {
+/* The rank-local pair loop of electronphonon::evolve (evolve_eph.cpp:49-135) over pairs [p0, p1)
+ * (one MPI rank's contiguous slice, mymp::distribute_var mymp.cpp:8-36), accumulating into Pdm and
+ * dm1P (summode, dense P, expt or not; no valley filtering: the default alg.only_intra/intervalley =
+ * false and fewer than two valleys keep every pair, evolve_eph.cpp:52-58). e is [nk][nb]. */
+void orc_pairs_partial(const orc_sys* s, const double* e, double t, const zc* dm, const zc* dm1, int64_t p0, int64_t p1,
+                       zc* Pdm, zc* dm1P) {
+  const int nb = s->bend - s->bstart, nb2 = nb * nb, nb4 = nb2 * nb2;
+  const zc c1 = zmk(1, 0);
+  zc *P1t = (zc*)xmalloc(sizeof(zc) * nb4), *P2t = (zc*)xmalloc(sizeof(zc) * nb4);
+  zc *P1n = (zc*)xmalloc(sizeof(zc) * nb4), *P2n = (zc*)xmalloc(sizeof(zc) * nb4);
+  for (int64_t ip = p0; ip < p1; ip++) {
     const int ik = (int)s->k1st[ip], ikp = (int)s->k2nd[ip];
     const zc* P1 = s->P1 + (size_t)ip * nb4;
     const zc* P2 = s->P2 + (size_t)ip * nb4;
     if (!s->expt) {
       /* axbyc(P1t, P1, nb^4): y = x */
-      memcpy(w->P1t, P1, sizeof(zc) * nb4);
-      memcpy(w->P2t, P2, sizeof(zc) * nb4);
+      memcpy(P1t, P1, sizeof(zc) * nb4);
+      memcpy(P2t, P2, sizeof(zc) * nb4);
     } else {
-      compute_Pt(nb, t, e + (size_t)ik * nb, e + (size_t)ikp * nb, P1, w->P1t, 0);
-      compute_Pt(nb, t, e + (size_t)ik * nb, e + (size_t)ikp * nb, P2, w->P2t, 1);
+      compute_Pt(nb, t, e + (size_t)ik * nb, e + (size_t)ikp * nb, P1, P1t, 0);
+      compute_Pt(nb, t, e + (size_t)ik * nb, e + (size_t)ikp * nb, P2, P2t, 1);
     }
-    zgemm_mnk(w->Pdm + (size_t)ik * nb2, w->P1t, dm + (size_t)ikp * nb2, nb2, 1, nb2, c1, c1);
-    zgemm_mnk(w->dm1P + (size_t)ik * nb2, dm1 + (size_t)ikp * nb2, w->P2t, 1, nb2, nb2, c1, c1);
+    zgemm_mnk(Pdm + (size_t)ik * nb2, P1t, dm + (size_t)ikp * nb2, nb2, 1, nb2, c1, c1);
+    zgemm_mnk(dm1P + (size_t)ik * nb2, dm1 + (size_t)ikp * nb2, P2t, 1, nb2, nb2, c1, c1);
     if (ik < ikp) {
-      for (int i = 0; i < nb4; i++) { w->P2n[i] = zconj(w->P1t[i]); w->P1n[i] = zconj(w->P2t[i]); }
-      zgemm_mnk(w->Pdm + (size_t)ikp * nb2, w->P1n, dm + (size_t)ik * nb2, nb2, 1, nb2, c1, c1);
-      zgemm_mnk(w->dm1P + (size_t)ikp * nb2, dm1 + (size_t)ik * nb2, w->P2n, 1, nb2, nb2, c1, c1);
+      for (int i = 0; i < nb4; i++) { P2n[i] = zconj(P1t[i]); P1n[i] = zconj(P2t[i]); }
+      zgemm_mnk(Pdm + (size_t)ikp * nb2, P1n, dm + (size_t)ik * nb2, nb2, 1, nb2, c1, c1);
+      zgemm_mnk(dm1P + (size_t)ikp * nb2, dm1 + (size_t)ik * nb2, P2n, 1, nb2, nb2, c1, c1);
     }
   }
-  /* the rank-local sums are complete on a single rank (mymp allreduce, evolve_eph.cpp:137) */
-  zc* contrib = w->P1t; /* reuse as ddmdt_contrib (nb2 <= nb4) */
+  free(P1t); free(P2t); free(P1n); free(P2n);
+}
+
+/* The per-k finish of electronphonon::evolve after the allreduce (evolve_eph.cpp:140-162). */
+void orc_evolve_finish(const orc_sys* s, const double* e, double t, const zc* dm, const zc* dm1, const zc* Pdm,
+                       const zc* dm1P, zc* ddmdt_eph, int compute_eq) {
+  const int nk = s->nk, nb = s->bend - s->bstart, nb2 = nb * nb;
+  const zc c1 = zmk(1, 0), cm1 = zmk(-1, 0), c0 = zmk(0, 0);
+  zc* contrib = (zc*)xmalloc(sizeof(zc) * nb2);
   for (int ik = 0; ik < nk; ik++) {
     memset(contrib, 0, sizeof(zc) * nb2);
-    zhemm_n(contrib, 1, dm1 + (size_t)ik * nb2, w->Pdm + (size_t)ik * nb2, nb, c1, c0);
-    zhemm_n(contrib, 0, dm + (size_t)ik * nb2, w->dm1P + (size_t)ik * nb2, nb, cm1, c1);
+    zhemm_n(contrib, 1, dm1 + (size_t)ik * nb2, Pdm + (size_t)ik * nb2, nb, c1, c0);
+    zhemm_n(contrib, 0, dm + (size_t)ik * nb2, dm1P + (size_t)ik * nb2, nb, cm1, c1);
     for (int i = 0; i < nb; i++)
       for (int j = 0; j < nb; j++)
         ddmdt_eph[(size_t)ik * nb2 + i * nb + j] = zscale(s->prefac_eph * 0.5, zadd(contrib[i * nb + j], zconj(contrib[j * nb + i])));
   }
+  free(contrib);
   if (!compute_eq && s->ddmdt_eq) {
     for (int ik = 0; ik < nk; ik++)
       for (int i = 0; i < nb; i++)
@@ -160,6 +169,17 @@ void orc_evolve(const orc_sys* s, orc_ws* w, const double* e, double t, const zc
           else *o = zsub(*o, zmul(q, zcis((e[(size_t)ik * nb + i] - e[(size_t)ik * nb + j]) * t)));
         }
   }
+}
+
+/* electronphonon::evolve -- evolve_eph.cpp:34-166 on a single rank */
+void orc_evolve(const orc_sys* s, orc_ws* w, const double* e, double t, const zc* dm, const zc* dm1, zc* ddmdt_eph, int compute_eq) {
+  const int nk = s->nk, nb = s->bend - s->bstart, nb2 = nb * nb;
+  memset(ddmdt_eph, 0, sizeof(zc) * nk * nb2);
+  memset(w->Pdm, 0, sizeof(zc) * nk * nb2);
+  memset(w->dm1P, 0, sizeof(zc) * nk * nb2);
+  orc_pairs_partial(s, e, t, dm, dm1, 0, s->npair, w->Pdm, w->dm1P);
+  /* the rank-local sums are complete on a single rank (mymp allreduce, evolve_eph.cpp:137) */
+  orc_evolve_finish(s, e, t, dm, dm1, w->Pdm, w->dm1P, ddmdt_eph, compute_eq);
 }
 
 /* trunc_copy_arraymat -- comm/mymatrix.cpp:134-144 */
@@ -409,8 +429,8 @@ int orc_rkf45(const orc_sys* s, double t0, double tend, double tstep, double hst
 int orc_euler(const orc_sys* s, double t0, double h, long nsteps, double* y) {
   const int nk = s->nk, nb = s->nb_dm, nb2 = nb * nb;
   orc_ws* w = orc_ws_new(s);
-  for (long st = 0; st < nsteps; ++st) {
-    const double t = t0 + (double)st * h; /* sdmk->t += dt: accumulated in DMD, identical for these h */
+  double t = t0;
+  for (long st = 0; st < nsteps; ++st, t += h) { /* sdmk->t += dt_current() (DensityMatrix_Dynamics.h:232) */
     orc_compute(s, w, t, (const zc*)y, w->ddmdt);
     zc* dm = (zc*)y;
     for (int ik = 0; ik < nk; ik++)
@@ -456,4 +476,43 @@ void orc_fermi(double T, double mu, const double* e, double* f, size_t n) {
     else if (ebyt > 46) f[i] = 0;
     else f[i] = 1. / (exp(ebyt) + 1);
   }
+}
+
+/* Multi-rank form of func (the reference's MPI decomposition, main.cpp:66 + evolve_eph.cpp:137):
+ * orc_window_in builds the window dm / 1-dm (evolve_driver's trunc_copy) and e; each rank runs
+ * orc_pairs_partial on its slice; the sums are added (the allreduce) and orc_rhs_from_partials
+ * finishes, adds the coherent term and writes dydt. */
+void orc_window_in(const orc_sys* s, const double* y, double* e_w, double* dm_w, double* dm1_w) {
+  const int nk = s->nk, nd = s->nb_dm, bs = s->bstart, be = s->bend, nb = be - bs, nd2 = nd * nd;
+  const zc* dm = (const zc*)y;
+  zc* dm1x = (zc*)xmalloc(sizeof(zc) * (size_t)nk * nd2);
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = 0; i < nd; i++)
+      for (int j = 0; j < nd; j++) {
+        const zc v = dm[(size_t)ik * nd2 + i * nd + j];
+        dm1x[(size_t)ik * nd2 + i * nd + j] = (i == j) ? zsub(zmk(1, 0), v) : zmk(-v.x, -v.y);
+      }
+  for (int ik = 0; ik < nk; ik++)
+    for (int b = 0; b < nb; b++) e_w[ik * nb + b] = s->e_dm[(size_t)ik * nd + bs + b];
+  trunc_copy((zc*)dm_w, dm, nk, nd, bs, be);
+  trunc_copy((zc*)dm1_w, dm1x, nk, nd, bs, be);
+  free(dm1x);
+}
+
+void orc_rhs_from_partials(const orc_sys* s, double t, const double* y, const double* e_w, const double* dm_w,
+                           const double* dm1_w, const double* Pdm, const double* dm1P, double* dydt) {
+  const int nk = s->nk, nd = s->nb_dm, bs = s->bstart, be = s->bend, nb = be - bs, nd2 = nd * nd, nb2 = nb * nb;
+  orc_ws* w = orc_ws_new(s);
+  zc* out = (zc*)dydt;
+  memset(out, 0, sizeof(zc) * (size_t)nk * nd2);
+  if (s->picture_schrodinger || s->Hcoh) {
+    orc_evolve_coh(s, w, t, (const zc*)y, w->coh);
+    for (size_t i = 0; i < (size_t)nk * nd2; i++) out[i] = zadd(out[i], w->coh[i]);
+  }
+  orc_evolve_finish(s, e_w, t, (const zc*)dm_w, (const zc*)dm1_w, (const zc*)Pdm, (const zc*)dm1P, w->ddmdt_eph, 0);
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = bs; i < be; i++)
+      for (int j = bs; j < be; j++)
+        out[(size_t)ik * nd2 + i * nd + j] = zadd(out[(size_t)ik * nd2 + i * nd + j], w->ddmdt_eph[(size_t)ik * nb2 + (i - bs) * nb + j - bs]);
+  orc_ws_free(w);
 }

@@ -75,6 +75,12 @@ def lib():
         _lib.orc_measure.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
                                      C.c_double, C.c_int, C.c_void_p, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib.orc_sys_size.restype = C.c_size_t
+        _lib.orc_window_in.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_pairs_partial.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_int64,
+                                           C.c_int64, C.c_void_p, C.c_void_p]
+        _lib.orc_rhs_from_partials.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_fermi.argtypes = [C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_size_t]
     return _lib
 
 
@@ -372,3 +378,102 @@ def euler(s: OracleSystem, t0: float, h: float, nsteps: int, y: np.ndarray):
     cs = s.cstruct()
     lib().orc_euler(C.addressof(cs), t0, h, nsteps, y.ctypes.data)
     return y
+
+
+# ------------------------------------------------------------------------------------------------
+# In-memory systems and the multi-process (rank-sliced) RHS used as the CPU baseline
+# ------------------------------------------------------------------------------------------------
+def from_arrays(*, nk, nb_dm, bstart, bend, e_dm, f_dm, k1st, k2nd, P1, P2, prefac_eph, dm0, smat=None, Hcoh=None,
+                picture_schrodinger=0, expt=1, t0=0.0, temperature=0.0, mu=0.0, nk_full=1.0, ob_prefac=1.0):
+    """An OracleSystem over arrays already in memory (no copies of P)."""
+    return OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=int(np.asarray(k1st).size),
+                        e_dm=np.ascontiguousarray(e_dm, np.float64), f_dm=np.ascontiguousarray(f_dm, np.float64),
+                        k1st=np.ascontiguousarray(k1st, np.uint64), k2nd=np.ascontiguousarray(k2nd, np.uint64),
+                        P1=np.ascontiguousarray(P1, np.complex128), P2=np.ascontiguousarray(P2, np.complex128),
+                        prefac_eph=prefac_eph, Hcoh=None if Hcoh is None else np.ascontiguousarray(Hcoh, np.complex128),
+                        smat=smat, dm0=np.ascontiguousarray(dm0, np.complex128), picture_schrodinger=picture_schrodinger,
+                        expt=expt, t0=t0, tstep=0.0, tend=0.0, temperature=temperature, mu=mu, nk_full=nk_full,
+                        ob_prefac=ob_prefac, ode={}, params={})
+
+
+_PAR = {}
+
+
+def _par_worker(args):
+    """One rank's pair slice; the system lives in module state inherited through fork."""
+    from multiprocessing import shared_memory
+    rank, p0, p1, t, names, shapes = args
+    s = _PAR["sys"]
+    bufs = [shared_memory.SharedMemory(name=n) for n in names]
+    try:
+        e_w = np.ndarray(shapes[0], np.float64, buffer=bufs[0].buf)
+        dm_w = np.ndarray(shapes[1], np.complex128, buffer=bufs[1].buf)
+        dm1_w = np.ndarray(shapes[1], np.complex128, buffer=bufs[2].buf)
+        part = np.ndarray((shapes[2][0],) + shapes[1], np.complex128, buffer=bufs[3].buf)
+        Pdm = np.zeros(shapes[1], np.complex128)
+        dm1P = np.zeros(shapes[1], np.complex128)
+        cs = s.cstruct()
+        lib().orc_pairs_partial(C.addressof(cs), e_w.ctypes.data, t, dm_w.ctypes.data, dm1_w.ctypes.data, p0, p1,
+                                Pdm.ctypes.data, dm1P.ctypes.data)
+        part[2 * rank] = Pdm
+        part[2 * rank + 1] = dm1P
+        del e_w, dm_w, dm1_w, part
+    finally:
+        for b in bufs:
+            b.close()
+    return rank
+
+
+class ParallelRHS:
+    """func(t, y) evaluated as DMD does with nproc MPI ranks: contiguous pair slices
+    (mymp::distribute_var, mymp.cpp:8-36), per-rank partial Pdm/dm1P, summed (the allreduce of
+    evolve_eph.cpp:137), then the finish. Worker processes are forked before any GPU use and read P
+    from the parent's memory."""
+
+    def __init__(self, s: OracleSystem, nproc: int):
+        import multiprocessing as mp
+        from multiprocessing import shared_memory
+        self.s = s
+        self.nproc = max(1, int(nproc))
+        nb = s.bend - s.bstart
+        self.shapes = ((s.nk, nb), (s.nk, nb * nb), (2 * self.nproc,))
+        sz = [s.nk * nb * 8, s.nk * nb * nb * 16, s.nk * nb * nb * 16, 2 * self.nproc * s.nk * nb * nb * 16]
+        self.shm = [shared_memory.SharedMemory(create=True, size=max(z, 16)) for z in sz]
+        self.e_w = np.ndarray(self.shapes[0], np.float64, buffer=self.shm[0].buf)
+        self.dm_w = np.ndarray(self.shapes[1], np.complex128, buffer=self.shm[1].buf)
+        self.dm1_w = np.ndarray(self.shapes[1], np.complex128, buffer=self.shm[2].buf)
+        self.part = np.ndarray((2 * self.nproc,) + self.shapes[1], np.complex128, buffer=self.shm[3].buf)
+        n = s.npair
+        self.ranges = [((n * r) // self.nproc, (n * (r + 1)) // self.nproc) for r in range(self.nproc)]
+        _PAR["sys"] = s
+        self.pool = mp.get_context("fork").Pool(self.nproc) if self.nproc > 1 else None
+
+    def __call__(self, t, y):
+        s = self.s
+        y = np.ascontiguousarray(y, np.float64)
+        cs = s.cstruct()
+        L = lib()
+        L.orc_window_in(C.addressof(cs), y.ctypes.data, self.e_w.ctypes.data, self.dm_w.ctypes.data,
+                        self.dm1_w.ctypes.data)
+        jobs = [(r, p0, p1, float(t), [m.name for m in self.shm], self.shapes) for r, (p0, p1) in enumerate(self.ranges)]
+        if self.pool is not None:
+            list(self.pool.map(_par_worker, jobs))
+        else:
+            _par_worker(jobs[0])
+        Pdm = self.part[0::2].sum(axis=0)
+        dm1P = self.part[1::2].sum(axis=0)
+        out = np.zeros_like(y)
+        L.orc_rhs_from_partials(C.addressof(cs), float(t), y.ctypes.data, self.e_w.ctypes.data, self.dm_w.ctypes.data,
+                                self.dm1_w.ctypes.data, Pdm.ctypes.data, dm1P.ctypes.data, out.ctypes.data)
+        return out
+
+    def close(self):
+        if self.pool is not None:
+            self.pool.terminate()
+            self.pool = None
+        for a in ("e_w", "dm_w", "dm1_w", "part"):
+            setattr(self, a, None)
+        for m in self.shm:
+            m.close()
+            m.unlink()
+        self.shm = []

@@ -1,0 +1,101 @@
+"""CPU tests of the C++ host library: DMD's readers and set-up against the reference's own outputs
+(golden fixtures) and the oracle; file errors and unsupported options fail loudly."""
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, GOLDEN_CASES, ROOT
+
+
+@pytest.fixture(scope="module")
+def host():
+    from denmat_dynm_development_gb300 import build as B
+    B.build_all()
+    from denmat_dynm_development_gb300 import host as H
+    return H
+
+
+def test_host_exports_header(host):
+    import ctypes as C
+    import re
+    src = open(os.path.join(ROOT, "include", "dmd_host.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = sorted(set(re.findall(r"\b(dmdh_[a-z0-9_A-Z]+)\s*\(", src)))
+    L = C.CDLL(host.HOST_LIB)
+    assert not [n for n in names if not hasattr(L, n)]
+    assert sorted(host.EXPORTS) == names
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_load_matches_reference_setup(case, host, oracle):
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = host.System(d)
+    meta = dict(zip(g["meta_keys"], g["meta_vals"]))
+    assert s.info.nk == int(meta["nk"]) and s.info.nb_dm == int(meta["nb_dm"])
+    assert s.info.bstart == int(meta["bstart"]) and s.info.bend == int(meta["bend"])
+    assert s.info.nkpair == int(meta["nkpair"])
+    assert s.info.prefac_eph == meta["prefac_eph"]
+    assert s.info.mu == meta["mu"] and s.info.temperature == meta["temperature"]
+    assert s.info.cell_size == meta["cell_size"] and s.info.cell_size_cmd == meta["cell_size_cmd"]
+    np.testing.assert_array_equal(s.e_dm, g["e_dm"])
+    np.testing.assert_array_equal(s.f_dm, g["f_dm"])
+    np.testing.assert_array_equal(s.dm0, g["dm0"])
+    if "Hcoh" in g:
+        np.testing.assert_array_equal(s.Hcoh, g["Hcoh"])
+    else:
+        assert s.Hcoh is None
+    o = oracle.load(d)
+    np.testing.assert_array_equal(s.P1, o.P1)
+    np.testing.assert_array_equal(s.P2, o.P2)
+    np.testing.assert_array_equal(s.k1st, o.k1st)
+    assert s.info.ob_prefac == o.ob_prefac
+    assert s.info.tstep == o.tstep and s.info.tend == o.tend
+    assert s.info.ode_hstart == o.ode["hstart"] and s.info.ode_hmax == o.ode["hmax"]
+
+
+def test_truncated_P_file_is_a_file_error(host, tmp_path):
+    src = os.path.join(GOLDEN, "nb2_eph")
+    dst = str(tmp_path / "case")
+    shutil.copytree(src, dst)
+    p = os.path.join(dst, "ldbd_data", "ldbd_P1_lindblad.bin")
+    with open(p, "r+b") as f:
+        f.truncate(os.path.getsize(p) - 16)
+    with pytest.raises(RuntimeError, match="size does not match"):
+        host.System(dst)
+
+
+def test_missing_param_and_unsupported_options(host, tmp_path):
+    with pytest.raises(RuntimeError, match="param.in does not exist"):
+        host.System(str(tmp_path))
+    dst = str(tmp_path / "case")
+    shutil.copytree(os.path.join(GOLDEN, "nb2_eph"), dst)
+    with open(os.path.join(dst, "param.in"), "a") as f:
+        f.write("alg_linearize = 1\n")
+    with pytest.raises(RuntimeError, match="alg_linearize"):
+        host.System(dst)
+
+
+def test_param_parser_quirks(host, tmp_path):
+    """map_input drops the character before '=' (parameters.cpp:617): 'key=value' names 'ke'."""
+    dst = str(tmp_path / "case")
+    shutil.copytree(os.path.join(GOLDEN, "nb2_eph"), dst)
+    with open(os.path.join(dst, "param.in"), "a") as f:
+        f.write("# comment = 5\nfoo_bar=3\nspam = 1.5 \\\n  2.5\n")
+    s = host.System(dst)
+    assert s.param("foo_ba") == 3.0
+    assert s.param("foo_bar") is None
+    assert s.param("spam") == 1.5
+    assert s.param("comment") is None
+
+
+def test_setup_pieces_match_oracle(host, oracle):
+    d = os.path.join(GOLDEN, "nb4_eimp_B")
+    o = oracle.load(d)
+    f = host.fermi(o.temperature, o.mu, o.e_dm)
+    np.testing.assert_array_equal(f, o.f_dm)
+    Bp = np.array([0.05, 0.0, 0.1]) * oracle.Tesla2au
+    dm = host.dm_bpert(o.smat, o.e_dm, o.f_dm, o.temperature, Bp, 0.0, 0)
+    np.testing.assert_array_equal(dm, o.dm0)

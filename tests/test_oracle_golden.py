@@ -81,3 +81,22 @@ def test_hermiticity_of_rhs(case, oracle):
     d, g, s = _load(case, oracle)
     eph = g["rhs_eph"][0].view(np.complex128).reshape(s.nk, s.nb_dm, s.nb_dm)
     np.testing.assert_array_equal(eph, np.conj(np.swapaxes(eph, 1, 2)))
+
+
+@pytest.mark.parametrize("nproc", [1, 3])
+def test_rank_sliced_rhs_matches(nproc, oracle):
+    """The multi-process CPU baseline (DMD's MPI decomposition) equals the single-rank RHS up to the
+    order of the allreduce sum."""
+    d = os.path.join(GOLDEN, "nb2_eimp_B")
+    s = oracle.load(d)
+    y = oracle.y_of(s.dm0)
+    t = 17.0 * oracle.fs
+    ref = oracle.rhs(s, t, y)
+    par = oracle.ParallelRHS(s, nproc)
+    try:
+        out = par(t, y)
+    finally:
+        par.close()
+    assert np.abs(out - ref).max() <= 1e-14 * np.abs(ref).max()
+    if nproc == 1:
+        np.testing.assert_array_equal(out, ref)
