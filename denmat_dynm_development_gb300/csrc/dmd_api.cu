@@ -9,7 +9,9 @@
 
 #include "dmd_gpu.h"
 #include "dmd_kernels.cuh"
+#include "dmd_layout.h"
 #include "dmd_pairs.cuh"
+#include "dmd_pairs_cb.cuh"
 
 using namespace dmd;
 
@@ -24,8 +26,17 @@ struct dmd_handle {
   // device arrays
   double* d_ew = nullptr;      // [nk][nb]
   double* d_edm = nullptr;     // [nk][nbdm]
-  int2* d_kk = nullptr;        // [npair]
-  double2* d_P = nullptr;      // [npair][2][nb4]
+  int2* d_kk = nullptr;        // [npair] (per-thread form)
+  double2* d_P = nullptr;      // [npair][2][nb4] (per-thread form) or the column-block element store
+  // column-block layout (nb = 2)
+  int use_cb = 0;
+  int* d_pos = nullptr;        // k -> energy rank
+  dmd::RowBlock* d_rb = nullptr;
+  dmd::WorkItem* d_items = nullptr;
+  int nitems = 0;
+  long long nrb = 0;
+  int cb_variant = 1;          // 0: direct loads, 1: bulk-copy staging through shared memory
+  unsigned int* d_err = nullptr;  // device error flags (bounded waits)
   double2* d_H = nullptr;      // [nk][nbdm^2]
   double2* d_eq = nullptr;     // [nk][nb2]
   double2* d_rs = nullptr;     // [nk][2][nb2]
@@ -147,7 +158,15 @@ template <int NB>
 int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
   const int n = h->nk * NB * NB;
   ProfScope ps(h, 0);
-  k_prep<NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->expt, h->d_rs, h->d_acc);
+  if (!h->use_cb) {
+    k_prep<NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->expt, h->d_rs, h->d_acc);
+  } else if (h->prec == DMD_PREC_F64X) {
+    k_prep_cb<ArithDF, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta,
+                                                                    h->expt, (float4*)h->d_rs, h->d_acc);
+  } else {
+    k_prep_cb<ArithF64, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta,
+                                                                     h->expt, h->d_rs, h->d_acc);
+  }
   h->launches++;
   CKL();
   return DMD_OK;
@@ -156,9 +175,30 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
 template <int NB>
 int launch_pairs(dmd_handle* h) {
   if (h->npair == 0) return DMD_OK;
-  const long long nthr = h->npair * 4LL * NB * NB;
   ProfScope ps(h, 1);
-  k_pairs_f64_atomic<NB><<<blocks_for(nthr, 256), 256, 0, h->st>>>(h->npair, h->d_kk, h->d_P, h->d_rs, h->d_acc);
+  if (!h->use_cb) {
+    const long long nthr = h->npair * 4LL * NB * NB;
+    k_pairs_f64_atomic<NB><<<blocks_for(nthr, 256), 256, 0, h->st>>>(h->npair, h->d_kk, h->d_P, h->d_rs, h->d_acc);
+  } else {
+    if constexpr (NB <= 2) {
+      const unsigned g = blocks_for(h->nitems, 4);
+      if (h->cb_variant == 1) {
+        if (h->prec == DMD_PREC_F64X)
+          k_pairs_cb_tma<ArithDF, NB><<<g, 128, CbTmaSmem<ArithDF, NB>::cta_bytes, h->st>>>(
+              h->d_items, h->nitems, h->d_rb, (const float4*)h->d_P, (const float4*)h->d_rs, (double*)h->d_acc, h->nk,
+              h->d_err);
+        else
+          k_pairs_cb_tma<ArithF64, NB><<<g, 128, CbTmaSmem<ArithF64, NB>::cta_bytes, h->st>>>(
+              h->d_items, h->nitems, h->d_rb, h->d_P, h->d_rs, (double*)h->d_acc, h->nk, h->d_err);
+      } else if (h->prec == DMD_PREC_F64X) {
+        k_pairs_cb<ArithDF, NB><<<g, 128, 0, h->st>>>(h->d_items, h->nitems, h->d_rb, (const float4*)h->d_P,
+                                                      (const float4*)h->d_rs, (double*)h->d_acc, h->nk);
+      } else {
+        k_pairs_cb<ArithF64, NB><<<g, 128, 0, h->st>>>(h->d_items, h->nitems, h->d_rb, h->d_P, h->d_rs,
+                                                       (double*)h->d_acc, h->nk);
+      }
+    }
+  }
   h->launches++;
   CKL();
   return DMD_OK;
@@ -188,6 +228,7 @@ FinishArgs base_finish(dmd_handle* h, const double2* y) {
   a.eq = h->d_eq;
   a.y = y;
   a.acc = h->d_acc;
+  a.pos = h->use_cb ? h->d_pos : nullptr;
   a.want_eph = 1;
   a.want_coh = (h->picture == DMD_PICTURE_SCHRODINGER || h->d_H) ? 1 : 0;
   return a;
@@ -274,11 +315,86 @@ int upload_pairs(dmd_handle* h, const dmd_desc* d) {
   return rc;
 }
 
+// column-block layout upload: pairs permuted into row blocks, element-major inside each block,
+// folded with the optional additive operators and converted to the arithmetic's element format
+int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
+  const int nb = h->nb, nb4 = h->nb4, ne = 2 * nb4;
+  std::vector<double> ew((size_t)h->nk * nb);
+  for (int k = 0; k < h->nk; ++k)
+    for (int b = 0; b < nb; ++b) ew[(size_t)k * nb + b] = d->e_dm[(size_t)k * h->nbdm + h->bs + b];
+  dmd::PairLayout L;
+  if (!dmd::build_pair_layout(h->nk, nb, ew.data(), h->npair, d->k1st, d->k2nd, 512, L))
+    return fail(h, DMD_E_ARG, "k-pair index out of range");
+  h->nitems = (int)L.items.size();
+  h->nrb = (long long)L.rb.size();
+  if (const char* v = getenv("DMD_PAIR_KERNEL")) h->cb_variant = (strcmp(v, "ldg") == 0) ? 0 : 1;
+  CK(cudaFuncSetAttribute(k_pairs_cb_tma<ArithDF, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)CbTmaSmem<ArithDF, 2>::cta_bytes));
+  CK(cudaFuncSetAttribute(k_pairs_cb_tma<ArithF64, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)CbTmaSmem<ArithF64, 2>::cta_bytes));
+  int rc;
+  if ((rc = dalloc(h, &h->d_pos, (size_t)h->nk)) || (rc = dalloc(h, &h->d_rb, L.rb.size())) ||
+      (rc = dalloc(h, &h->d_items, L.items.size())))
+    return rc;
+  CK(cudaMemcpy(h->d_pos, L.pos.data(), L.pos.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_rb, L.rb.data(), L.rb.size() * sizeof(dmd::RowBlock), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_items, L.items.data(), L.items.size() * sizeof(dmd::WorkItem), cudaMemcpyHostToDevice));
+  const bool df = h->prec == DMD_PREC_F64X;
+  const size_t chunk_rb = 1 << 14;  // row blocks per staging chunk
+  double2* stage = nullptr;
+  CK(cudaMallocHost((void**)&stage, chunk_rb * 32 * ne * sizeof(double2)));
+  int out = DMD_OK;
+  for (size_t r0 = 0; r0 < L.rb.size() && out == DMD_OK; r0 += chunk_rb) {
+    const size_t r1 = std::min(L.rb.size(), r0 + chunk_rb);
+    const size_t q0 = L.rb[r0].pair0;
+    const size_t q1 = (r1 < L.rb.size()) ? L.rb[r1].pair0 : (size_t)h->npair;
+    for (size_t r = r0; r < r1; ++r) {
+      const size_t b0 = L.rb[r].pair0;
+      const size_t n = (size_t)__builtin_popcount(L.rb[r].mask);
+      for (size_t i = 0; i < n; ++i) {
+        const size_t src = L.src[b0 + i];
+        const bool tr = L.transposed[b0 + i] != 0;
+        const double* s1 = d->P1 + 2 * src * nb4;
+        const double* s2 = d->P2 + 2 * src * nb4;
+        const double* a1 = d->P1_add ? d->P1_add + 2 * src * nb4 : nullptr;
+        const double* a2 = d->P2_add ? d->P2_add + 2 * src * nb4 : nullptr;
+        if (tr) {  // stored as the pair (k2, k1): P1' = conj(P2), P2' = conj(P1) (evolve_eph.cpp:102-103)
+          std::swap(s1, s2);
+          std::swap(a1, a2);
+        }
+        for (int e = 0; e < ne; ++e) {
+          const double* sp = e < nb4 ? s1 + 2 * e : s2 + 2 * (e - nb4);
+          const double* ap = a1 ? (e < nb4 ? a1 + 2 * e : a2 + 2 * (e - nb4)) : nullptr;
+          double x = sp[0], yv = sp[1];
+          if (ap) {  // P += P_add * scale (ElectronImpurity.cpp:38-39, ElectronPhonon.cpp:96-97)
+            x = x + ap[0] * d->add_scale;
+            yv = yv + ap[1] * d->add_scale;
+          }
+          if (tr) yv = -yv;
+          double2 v;
+          if (df) {
+            const float xh = (float)x, yh = (float)yv;
+            float4 f = make_float4(xh, (float)(x - (double)xh), yh, (float)(yv - (double)yh));
+            memcpy(&v, &f, 16);
+          } else {
+            v = make_double2(x, yv);
+          }
+          stage[(b0 - q0) * ne + (size_t)e * n + i] = v;
+        }
+      }
+    }
+    cudaError_t e = cudaMemcpy(h->d_P + q0 * ne, stage, (q1 - q0) * ne * sizeof(double2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) out = fail(h, DMD_E_CUDA, std::string("P upload: ") + cudaGetErrorString(e));
+  }
+  cudaFreeHost(stage);
+  return out;
+}
+
 void release(dmd_handle* h) {
   if (!h) return;
   cudaSetDevice(h->dev);
   if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
-  void* ptrs[] = {h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
+  void* ptrs[] = {h->d_err, h->d_pos, h->d_rb, h->d_items, h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
                   h->d_coef, h->d_flag};
   for (void* p : ptrs)
@@ -298,6 +414,13 @@ void release(dmd_handle* h) {
 }
 
 int check_state(dmd_handle* h) {
+  unsigned int derr = 0;
+  CK(cudaMemcpyAsync(&derr, h->d_err, sizeof(derr), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (derr) {
+    cudaMemsetAsync(h->d_err, 0, sizeof(derr), h->st);
+    return fail(h, DMD_E_TIMEOUT, "a bounded device wait gave up (bulk copy did not complete)");
+  }
   const size_t n = 2 * h->nstate;
   CK(cudaMemsetAsync(h->d_flag, 0, sizeof(int), h->st));
   k_nan_scan<<<blocks_for((long long)n, 256), 256, 0, h->st>>>(n, (const double*)h->d_y, h->d_flag);
@@ -330,7 +453,8 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
     return DMD_E_ARG;
   if (d->nkpair > 0 && (!d->k1st || !d->k2nd || !d->P1 || !d->P2)) return DMD_E_ARG;
   if ((d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
-  if (d->precision != DMD_PREC_F64) return DMD_E_ARG;
+  if (d->precision != DMD_PREC_F64 && d->precision != DMD_PREC_F64X) return DMD_E_ARG;
+  if (d->precision == DMD_PREC_F64X && d->bend - d->bstart != 2) return DMD_E_ARG;
   if (d->picture != DMD_PICTURE_INTERACTION && d->picture != DMD_PICTURE_SCHRODINGER) return DMD_E_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DMD_E_NODEV;
@@ -362,14 +486,15 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return bail(DMD_E_CUDA);
   const size_t nk = h->nk, nbdm = h->nbdm;
   if ((rc = dalloc(h, &h->d_ew, nk * h->nb)) || (rc = dalloc(h, &h->d_edm, nk * nbdm)) ||
-      (rc = dalloc(h, &h->d_kk, (size_t)h->npair)) || (rc = dalloc(h, &h->d_P, (size_t)h->npair * 2 * h->nb4)) ||
+      (rc = dalloc(h, &h->d_kk, (h->nb == 2) ? 1 : (size_t)h->npair)) ||
+      (rc = dalloc(h, &h->d_P, (size_t)h->npair * 2 * h->nb4)) ||
       (rc = dalloc(h, &h->d_rs, nk * 2 * h->nb2)) || (rc = dalloc(h, &h->d_acc, nk * 2 * h->nb2)) ||
       (rc = dalloc(h, &h->d_y, h->nstate)) || (rc = dalloc(h, &h->d_ytmp, h->nstate)) ||
       (rc = dalloc(h, &h->d_y0, h->nstate)) || (rc = dalloc(h, &h->d_in, h->nstate)) ||
       (rc = dalloc(h, &h->d_in1, h->nstate)) || (rc = dalloc(h, &h->d_out, h->nstate)) ||
       (rc = dalloc(h, &h->d_K, 6 * h->nstate)) || (rc = dalloc(h, &h->d_tref, 2)) ||
       (rc = dalloc(h, &h->d_step, 1)) || (rc = dalloc(h, &h->d_red, 4096)) || (rc = dalloc(h, &h->d_coef_i, 64)) ||
-      (rc = dalloc(h, &h->d_coef, 64)) || (rc = dalloc(h, &h->d_flag, 1)))
+      (rc = dalloc(h, &h->d_coef, 64)) || (rc = dalloc(h, &h->d_flag, 1)) || (rc = dalloc(h, &h->d_err, 1)))
     return bail(rc);
   std::vector<double> ew(nk * h->nb);
   for (size_t k = 0; k < nk; ++k)
@@ -382,8 +507,10 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
     if (cudaMemcpy(h->d_H, d->Hcoh, h->nstate * 16, cudaMemcpyHostToDevice) != cudaSuccess)
       return bail(fail(h, DMD_E_CUDA, "upload H"));
   }
-  if ((rc = upload_pairs(h, d))) return bail(rc);
-  if (cudaMemset(h->d_y, 0, h->nstate * 16) != cudaSuccess || cudaMemset(h->d_step, 0, 8) != cudaSuccess)
+  h->use_cb = (h->nb == 2 && h->npair > 0) ? 1 : 0;
+  if ((rc = h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d))) return bail(rc);
+  if (cudaMemset(h->d_y, 0, h->nstate * 16) != cudaSuccess || cudaMemset(h->d_step, 0, 8) != cudaSuccess ||
+      cudaMemset(h->d_err, 0, sizeof(unsigned int)) != cudaSuccess)
     return bail(fail(h, DMD_E_CUDA, "init"));
   *out = h;
   return DMD_OK;

@@ -74,7 +74,8 @@ struct FinishArgs {
   const double2* H;    // [nk][nbdm^2] or null
   const double2* eq;   // [nk][NB2] or null
   const double2* y;    // state the RHS is evaluated on
-  const double2* acc;  // [nk][2][NB2]
+  const double2* acc;  // [nk][2][NB2], indexed by pos[k] when pos is set
+  const int* pos;      // k -> accumulator row (column-block layout) or null
   int want_eph, want_coh;
   // output: plain RHS
   double2* out;
@@ -137,7 +138,7 @@ __global__ void k_finish(FinishArgs a) {
   // scattering finish on the window (evolve_eph.cpp:140-162, evolve_driver :21-32)
   if (a.want_eph) {
     const double* ew = a.ew + (size_t)k * NB;
-    const double2* X = a.acc + (size_t)k * 2 * NB2;
+    const double2* X = a.acc + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
     const double2* Y = X + NB2;
     double2 rw[NB2], sw[NB2], Pdm[NB2], dmP[NB2];
     for (int i = 0; i < NB; ++i)

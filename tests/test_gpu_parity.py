@@ -4,6 +4,8 @@ Tolerances (normwise relative, max|gpu - ref| / max|ref|):
   * RHS (func, evolve_driver, evolve_coh) in FP64: 1e-12 -- the reference forms each P(t)
     element's phase cis(t(e1-e3-e2+e4)) while the GPU factorises it per k, and the pair sums
     run in a different order;
+  * RHS in the FP32-pair ("f64x") arithmetic: 1e-11 -- products carry ~2^-47 relative error and
+    the scattering-in and scattering-out terms of the finish partly cancel;
   * trajectories (40 RK4 steps, RKF45 to 20 fs): 1e-10 (the benchmark spec's bound for rho(t), S(t)).
 """
 import os
@@ -33,16 +35,35 @@ def built():
     G.build()
 
 
-@pytest.mark.parametrize("case", GOLDEN_CASES)
-def test_rhs_vs_golden(case, oracle, built):
+RHS_TOL = {"f64": 1e-12, "f64x": 1e-11}
+
+
+def cases_for(prec):
+    out = []
+    for c in GOLDEN_CASES:
+        nb = 4 if c.startswith("nb4") else 2
+        if prec == "f64x" and nb != 2:
+            continue
+        out.append((c, prec))
+    return out
+
+
+ALL = cases_for("f64") + cases_for("f64x")
+
+
+@pytest.mark.parametrize("case,prec", ALL)
+def test_rhs_vs_golden(case, prec, oracle, built):
     d = os.path.join(GOLDEN, case)
     g = dict(np.load(os.path.join(d, "golden.npz")))
     s = oracle.load(d)
-    with make_gpu(s) as gpu:
+    tol = RHS_TOL[prec]
+    with make_gpu(s, prec) as gpu:
         for i, t in enumerate(g["rhs_t"]):
             y = g["rhs_y"][i]
-            assert rel(gpu.func(t, y), g["rhs_dydt"][i]) < 1e-12
-            assert rel(gpu.evolve_driver(t, y), g["rhs_eph"][i]) < 1e-12
+            e1 = rel(gpu.func(t, y), g["rhs_dydt"][i])
+            e2 = rel(gpu.evolve_driver(t, y), g["rhs_eph"][i])
+            print("%s %s t=%g func %.3g eph %.3g" % (case, prec, t, e1, e2))
+            assert e1 < tol and e2 < tol
             if np.abs(g["rhs_coh"][i]).max() > 0:
                 assert rel(gpu.evolve_coh(t, y), g["rhs_coh"][i]) < 1e-12
             # exact Hermiticity of the scattering term (c + c^dagger, evolve_eph.cpp:151)
@@ -50,12 +71,12 @@ def test_rhs_vs_golden(case, oracle, built):
             np.testing.assert_array_equal(e, np.conj(np.swapaxes(e, 1, 2)))
 
 
-@pytest.mark.parametrize("case", GOLDEN_CASES)
-def test_rk4_vs_golden(case, oracle, built):
+@pytest.mark.parametrize("case,prec", ALL)
+def test_rk4_vs_golden(case, prec, oracle, built):
     d = os.path.join(GOLDEN, case)
     g = dict(np.load(os.path.join(d, "golden.npz")))
     s = oracle.load(d)
-    with make_gpu(s) as gpu:
+    with make_gpu(s, prec) as gpu:
         gpu.set_state(s.t0, oracle.y_of(s.dm0))
         gpu.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
         rec = []
@@ -73,13 +94,13 @@ def test_rk4_vs_golden(case, oracle, built):
         assert rel(rec[:, 2], ref[:, 2]) < 1e-10
 
 
-@pytest.mark.parametrize("case", GOLDEN_CASES)
-def test_rkf45_vs_golden(case, oracle, built):
+@pytest.mark.parametrize("case,prec", ALL)
+def test_rkf45_vs_golden(case, prec, oracle, built):
     """DMD's evolve_gsl loop: one driver_apply per output interval (DensityMatrix_Dynamics.h:210-223)."""
     d = os.path.join(GOLDEN, case)
     g = dict(np.load(os.path.join(d, "golden.npz")))
     s = oracle.load(d)
-    with make_gpu(s) as gpu:
+    with make_gpu(s, prec) as gpu:
         gpu.set_state(s.t0, oracle.y_of(s.dm0))
         gpu.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
         hs = s.ode["hstart"]
@@ -111,20 +132,50 @@ def test_euler_vs_oracle(case, oracle, built):
     assert rel(y, yr) < 1e-12
 
 
-def test_larger_random_case_vs_oracle(oracle, built, tmp_path):
+@pytest.mark.parametrize("prec", ["f64", "f64x"])
+def test_larger_random_case_vs_oracle(prec, oracle, built, tmp_path):
     """nk=500 Si-like workload (about 70k pairs) with e-imp and a B field."""
     from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, make_ldbd
     cfg = SynthConfig(nk=500, nb=2, seed=3, eimp_sigma_mev=5.0)
     make_ldbd(str(tmp_path), cfg, B_T=(1.0, 0.0, 0.0), eimp_fraction=1e-2)
     s = oracle.load(str(tmp_path))
     rng = np.random.default_rng(5)
-    with make_gpu(s) as gpu:
+    with make_gpu(s, prec) as gpu:
         for t in (0.0, 11.0 * oracle.fs, 4000.0 * oracle.fs):
             dm = s.dm0 + 1e-3 * (rng.standard_normal(s.dm0.shape) + 1j * rng.standard_normal(s.dm0.shape))
             dm = dm.reshape(s.nk, s.nb_dm, s.nb_dm)
             dm = 0.5 * (dm + np.conj(np.swapaxes(dm, 1, 2)))
             y = oracle.y_of(dm.reshape(s.nk, -1))
-            assert rel(gpu.func(t, y), oracle.rhs(s, t, y)) < 1e-12
+            err = rel(gpu.func(t, y), oracle.rhs(s, t, y))
+            print("nk500 %s t=%g rel err %.3g" % (prec, t, err))
+            assert err < RHS_TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["f64", "f64x"])
+def test_irregular_pairs_vs_oracle(prec, oracle, built):
+    """Duplicated pairs, pairs stored with k1 > k2 (no reverse term) and diagonal pairs, as the
+    reference's loop accepts them (evolve_eph.cpp:49-106)."""
+    d = os.path.join(GOLDEN, "nb2_eimp_B")
+    s0 = oracle.load(d)
+    rng = np.random.default_rng(9)
+    n = s0.npair
+    nb4 = 16
+    P1 = s0.P1.reshape(n, nb4)
+    P2 = s0.P2.reshape(n, nb4)
+    dup = rng.choice(n, 40, replace=False)
+    swp = rng.choice(n, 60, replace=False)
+    k1 = np.concatenate([s0.k1st, s0.k1st[dup], s0.k2nd[swp], np.arange(5, dtype=np.uint64)])
+    k2 = np.concatenate([s0.k2nd, s0.k2nd[dup], s0.k1st[swp], np.arange(5, dtype=np.uint64)])
+    Q1 = np.concatenate([P1, 0.5 * P1[dup], 0.3 * P2[swp], P1[:5]])
+    Q2 = np.concatenate([P2, 0.7 * P2[dup], 0.2 * P1[swp], P2[:5]])
+    s = oracle.from_arrays(nk=s0.nk, nb_dm=s0.nb_dm, bstart=s0.bstart, bend=s0.bend, e_dm=s0.e_dm, f_dm=s0.f_dm,
+                           k1st=k1, k2nd=k2, P1=Q1.reshape(-1), P2=Q2.reshape(-1), prefac_eph=s0.prefac_eph,
+                           dm0=s0.dm0, Hcoh=s0.Hcoh)
+    y = oracle.y_of(s.dm0)
+    t = 9.0 * oracle.fs
+    with make_gpu(s, prec) as gpu:
+        err = rel(gpu.func(t, y), oracle.rhs(s, t, y))
+    assert err < RHS_TOL[prec]
 
 
 def test_nb4_larger_vs_oracle(oracle, built, tmp_path):
@@ -133,7 +184,7 @@ def test_nb4_larger_vs_oracle(oracle, built, tmp_path):
     make_ldbd(str(tmp_path), cfg, B_T=(0.0, 0.7, 0.0), eimp_fraction=1e-2)
     s = oracle.load(str(tmp_path))
     y = oracle.y_of(s.dm0)
-    with make_gpu(s) as gpu:
+    with make_gpu(s, "f64") as gpu:
         t = 250.0 * oracle.fs
         assert rel(gpu.func(t, y), oracle.rhs(s, t, y)) < 1e-12
         gpu.set_state(s.t0, y)
