@@ -183,12 +183,13 @@ int launch_pairs(dmd_handle* h) {
     if constexpr (NB <= 2) {
       const unsigned g = blocks_for(h->nitems, 4);
       if (h->cb_variant == 1) {
+        constexpr int RW = NB * NB >= 2 ? 2 : 1;
         if (h->prec == DMD_PREC_F64X)
-          k_pairs_cb_tma<ArithDF, NB><<<g, 128, CbTmaSmem<ArithDF, NB>::cta_bytes, h->st>>>(
+          k_pairs_cb_tma<ArithDF, NB, RW, 4><<<g, 128, CbTmaSmem<ArithDF, NB, RW>::cta_bytes, h->st>>>(
               h->d_items, h->nitems, h->d_rb, (const float4*)h->d_P, (const float4*)h->d_rs, (double*)h->d_acc, h->nk,
               h->d_err);
         else
-          k_pairs_cb_tma<ArithF64, NB><<<g, 128, CbTmaSmem<ArithF64, NB>::cta_bytes, h->st>>>(
+          k_pairs_cb_tma<ArithF64, NB, RW, 4><<<g, 128, CbTmaSmem<ArithF64, NB, RW>::cta_bytes, h->st>>>(
               h->d_items, h->nitems, h->d_rb, h->d_P, h->d_rs, (double*)h->d_acc, h->nk, h->d_err);
       } else if (h->prec == DMD_PREC_F64X) {
         k_pairs_cb<ArithDF, NB><<<g, 128, 0, h->st>>>(h->d_items, h->nitems, h->d_rb, (const float4*)h->d_P,
@@ -328,10 +329,10 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
   h->nitems = (int)L.items.size();
   h->nrb = (long long)L.rb.size();
   if (const char* v = getenv("DMD_PAIR_KERNEL")) h->cb_variant = (strcmp(v, "ldg") == 0) ? 0 : 1;
-  CK(cudaFuncSetAttribute(k_pairs_cb_tma<ArithDF, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)CbTmaSmem<ArithDF, 2>::cta_bytes));
-  CK(cudaFuncSetAttribute(k_pairs_cb_tma<ArithF64, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)CbTmaSmem<ArithF64, 2>::cta_bytes));
+  CK(cudaFuncSetAttribute(k_pairs_cb_tma<ArithDF, 2, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)CbTmaSmem<ArithDF, 2, 2>::cta_bytes));
+  CK(cudaFuncSetAttribute(k_pairs_cb_tma<ArithF64, 2, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)CbTmaSmem<ArithF64, 2, 2>::cta_bytes));
   int rc;
   if ((rc = dalloc(h, &h->d_pos, (size_t)h->nk)) || (rc = dalloc(h, &h->d_rb, L.rb.size())) ||
       (rc = dalloc(h, &h->d_items, L.items.size())))
@@ -363,8 +364,15 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
           std::swap(a1, a2);
         }
         for (int e = 0; e < ne; ++e) {
-          const double* sp = e < nb4 ? s1 + 2 * e : s2 + 2 * (e - nb4);
-          const double* ap = a1 ? (e < nb4 ? a1 + 2 * e : a2 + 2 * (e - nb4)) : nullptr;
+          // stored element e: P1 row-major for e < nb^4; P2 column-major after it
+          // (e = nb^4 + cc * nb^2 + a holds P2[a][cc])
+          int se = e;
+          if (e >= nb4) {
+            const int q = e - nb4, cc = q / h->nb2, a = q % h->nb2;
+            se = nb4 + a * h->nb2 + cc;
+          }
+          const double* sp = se < nb4 ? s1 + 2 * se : s2 + 2 * (se - nb4);
+          const double* ap = a1 ? (se < nb4 ? a1 + 2 * se : a2 + 2 * (se - nb4)) : nullptr;
           double x = sp[0], yv = sp[1];
           if (ap) {  // P += P_add * scale (ElectronImpurity.cpp:38-39, ElectronPhonon.cpp:96-97)
             x = x + ap[0] * d->add_scale;

@@ -90,6 +90,10 @@ struct ArithDF {
     df_renorm(a.rh, a.rl);
     df_renorm(a.ih, a.il);
   }
+  static __device__ __forceinline__ void acc_add(acc& a, const acc& b) {
+    df_add(a.rh, a.rl, b.rh, b.rl);
+    df_add(a.ih, a.il, b.ih, b.il);
+  }
   // reduction scratch entry: one real (hi, lo)
   typedef float2 red_t;
   static __device__ __forceinline__ float2 red_re(const acc& a) { return make_float2(a.rh, a.rl); }
@@ -120,6 +124,10 @@ struct ArithF64 {
     a.y = fma(x.x, y.y, fma(-x.y, y.x, a.y));
   }
   static __device__ __forceinline__ void renorm(acc&) {}
+  static __device__ __forceinline__ void acc_add(acc& a, const acc& b) {
+    a.x += b.x;
+    a.y += b.y;
+  }
   typedef double red_t;
   static __device__ __forceinline__ double red_re(const acc& a) { return a.x; }
   static __device__ __forceinline__ double red_im(const acc& a) { return a.y; }
@@ -214,7 +222,7 @@ __global__ void __launch_bounds__(128) k_pairs_cb(const WorkItem* __restrict__ i
         for (int a = 0; a < NB2; ++a)
 #pragma unroll
           for (int c = 0; c < NB2; ++c) {
-            const E p2 = ld_stream(base + (size_t)(NB4 + a * NB2 + c) * n);
+            const E p2 = ld_stream(base + (size_t)(NB4 + c * NB2 + a) * n);  // P2 stored column-major
             A::mac(f[c], p2, sc[a]);
             if (rev) A::mac_cx(rX[a], p2, rr[c]);
           }
@@ -290,29 +298,38 @@ __global__ void k_prep_cb(int nk, int nbdm, int bs, const double2* __restrict__ 
 
 
 // ---------------------------------------------------------------------------------------------
-// The same contraction with the P elements staged through shared memory by bulk copies: each warp
-// double-buffers half row blocks (its P1 half, then its P2 half), issuing the copy of chunk i + 2
-// while it computes chunk i, so HBM latency is off the critical path and the warp's loads are
-// served from shared memory. Waits are bounded (dmd_tma.cuh); a timeout sets *errflag.
+// The same contraction with the P elements staged through shared memory by bulk copies.
+//
+// In this layout each pair stores P1 row-major and P2 column-major, so both halves are consumed
+// "line by line": a P1 row a completes the forward output X_k[a] and a P2 column c completes
+// Y_k[c], while the lane's reverse sums Y_col (indexed by P1's column) and X_col (indexed by P2's
+// row) stay in registers with compile-time indices. A row block is consumed in chunks of LINES
+// lines; each warp double-buffers its chunks, issuing the copy of chunk i + 2 while it computes
+// chunk i. The row's vectors rt_k, st_k are staged in shared memory once per row block. Waits are
+// bounded (dmd_tma.cuh); a timeout sets *errflag.
 // ---------------------------------------------------------------------------------------------
-template <typename A, int NB>
+template <typename A, int NB, int LINES>
 struct CbTmaSmem {
   static constexpr int NB2 = NB * NB, NB4 = NB2 * NB2, NV = 4 * NB2;
-  static constexpr size_t stage_bytes = (size_t)NB4 * 32 * sizeof(typename A::elem);
+  static constexpr int CPM = NB2 / LINES;  // chunks per matrix
+  static constexpr int CPR = 2 * CPM;      // chunks per row block
+  static constexpr size_t stage_bytes = (size_t)LINES * NB2 * 32 * sizeof(typename A::elem);
   static constexpr size_t red_bytes = (size_t)NV * 32 * sizeof(typename A::red_t);
-  static constexpr size_t warp_bytes = ((2 * stage_bytes + red_bytes + 16) + 127) / 128 * 128;
+  static constexpr size_t row_bytes = (size_t)2 * NB2 * sizeof(typename A::elem);
+  static constexpr size_t warp_bytes = ((2 * stage_bytes + red_bytes + row_bytes + 16) + 127) / 128 * 128;
   static constexpr size_t cta_bytes = 4 * warp_bytes;
 };
 
-template <typename A, int NB>
-__global__ void __launch_bounds__(128, 2) k_pairs_cb_tma(const WorkItem* __restrict__ items, int nitems,
-                                                         const RowBlock* __restrict__ rbs,
-                                                         const typename A::elem* __restrict__ P,
-                                                         const typename A::elem* __restrict__ rs,
-                                                         double* __restrict__ acc, int nk,
-                                                         unsigned int* __restrict__ errflag) {
-  typedef CbTmaSmem<A, NB> S;
-  constexpr int NB2 = S::NB2, NB4 = S::NB4, NV = S::NV;
+template <typename A, int NB, int LINES, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_pairs_cb_tma(const WorkItem* __restrict__ items, int nitems,
+                                                            const RowBlock* __restrict__ rbs,
+                                                            const typename A::elem* __restrict__ P,
+                                                            const typename A::elem* __restrict__ rs,
+                                                            double* __restrict__ acc, int nk,
+                                                            unsigned int* __restrict__ errflag) {
+  typedef CbTmaSmem<A, NB, LINES> S;
+  constexpr int NB2 = S::NB2, NB4 = S::NB4, NV = S::NV, CPM = S::CPM, CPR = S::CPR;
+  constexpr size_t SE = S::stage_bytes / sizeof(typename A::elem);  // elements per stage
   typedef typename A::elem E;
   typedef typename A::acc Acc;
   typedef typename A::red_t R;
@@ -322,11 +339,12 @@ __global__ void __launch_bounds__(128, 2) k_pairs_cb_tma(const WorkItem* __restr
   const int item = blockIdx.x * 4 + wib;
   if (item >= nitems) return;
   unsigned char* wbase = smem_raw + (size_t)wib * S::warp_bytes;
-  E* const stage0 = (E*)wbase;  // stage c & 1 starts at stage0 + (c & 1) * (stage_bytes / sizeof(E))
-  R* red = (R*)(wbase + 2 * S::stage_bytes);  // [NV][32]
-  uint64_t* bar = (uint64_t*)(wbase + 2 * S::stage_bytes + S::red_bytes);
+  E* const stage0 = (E*)wbase;
+  R* const red = (R*)(wbase + 2 * S::stage_bytes);                             // [NV][32]
+  E* const rowv = (E*)(wbase + 2 * S::stage_bytes + S::red_bytes);             // rt_k[NB2], st_k[NB2]
+  uint64_t* const bar = (uint64_t*)(wbase + 2 * S::stage_bytes + S::red_bytes + S::row_bytes);
   const WorkItem w = items[item];
-  const int nch = 2 * (w.rb1 - w.rb0);
+  const int nch = CPR * (w.rb1 - w.rb0);
   if (lane == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -334,13 +352,14 @@ __global__ void __launch_bounds__(128, 2) k_pairs_cb_tma(const WorkItem* __restr
   }
   __syncwarp();
   const uint64_t pol = policy_evict_first();
-  auto issue = [&](int c) {  // lane 0 only
-    const RowBlock b = rbs[w.rb0 + (c >> 1)];
+  auto issue = [&](int c) {  // lane 0 only: chunk c of the item into stage c & 1
+    const RowBlock b = rbs[w.rb0 + c / CPR];
+    const int q = c % CPR;
     const int n = __popc(b.mask);
-    const E* src = P + (size_t)b.pair0 * 2 * NB4 + (size_t)(c & 1) * NB4 * n;
-    const uint32_t bytes = (uint32_t)(NB4 * n * sizeof(E));
+    const size_t off = (size_t)b.pair0 * 2 * NB4 + ((size_t)(q / CPM) * NB4 + (size_t)(q % CPM) * LINES * NB2) * n;
+    const uint32_t bytes = (uint32_t)(LINES * NB2 * n * sizeof(E));
     mbar_arrive_expect_tx(&bar[c & 1], bytes);
-    bulk_g2s(stage0 + (size_t)(c & 1) * (S::stage_bytes / sizeof(E)), src, bytes, &bar[c & 1], pol);
+    bulk_g2s(stage0 + (size_t)(c & 1) * SE, P + off, bytes, &bar[c & 1], pol);
   };
   if (lane == 0) {
     issue(0);
@@ -363,95 +382,97 @@ __global__ void __launch_bounds__(128, 2) k_pairs_cb_tma(const WorkItem* __restr
   bool any_rev = false;
   bool failed = false;
   const unsigned lt = (1u << lane) - 1u;
-  for (int c = 0; c < nch; ++c) {
-    const RowBlock b = rbs[w.rb0 + (c >> 1)];
+#pragma unroll 1
+  for (int rbi = 0; rbi < w.rb1 - w.rb0; ++rbi) {
+    const RowBlock b = rbs[w.rb0 + rbi];
     const bool active = (b.mask >> lane) & 1u;
     const bool rev = (b.revmask >> lane) & 1u;
     any_rev |= rev;
     const int n = __popc(b.mask);
     const int slot = __popc(b.mask & lt);
-    if (!mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1), errflag)) {
-      failed = true;
-      break;
-    }
-    const E* st = stage0 + (size_t)(c & 1) * (S::stage_bytes / sizeof(E)) + slot;
-    const E* rrow = rs + (size_t)b.row * 2 * NB2;
-    if ((c & 1) == 0) {  // P1 half: X_k[a] += P1[a][c] rt_col[c];  Y_col[c] += st_k[a] conj(P1[a][c])
-      if (active) {
-        E sr[NB2];
-        Acc f[NB2];
-#pragma unroll
-        for (int i = 0; i < NB2; ++i) {
-          sr[i] = rrow[NB2 + i];
-          A::zero(f[i]);
-        }
-#pragma unroll
-        for (int a = 0; a < NB2; ++a)
-#pragma unroll
-          for (int cc = 0; cc < NB2; ++cc) {
-            const E p1 = st[(a * NB2 + cc) * n];
-            A::mac(f[a], p1, rc[cc]);
-            if (rev) A::mac_cx(rY[cc], p1, sr[a]);
-          }
-#pragma unroll
-        for (int i = 0; i < NB2; ++i) {
-          red[(2 * i) * 32 + lane] = A::red_re(f[i]);
-          red[(2 * i + 1) * 32 + lane] = A::red_im(f[i]);
-        }
-      }
-    } else {  // P2 half: Y_k[c] += st_col[a] P2[a][c];  X_col[a] += conj(P2[a][c]) rt_k[c]
-      if (active) {
-        E rr[NB2];
-        Acc f[NB2];
-#pragma unroll
-        for (int i = 0; i < NB2; ++i) {
-          rr[i] = rrow[i];
-          A::zero(f[i]);
-        }
-#pragma unroll
-        for (int a = 0; a < NB2; ++a)
-#pragma unroll
-          for (int cc = 0; cc < NB2; ++cc) {
-            const E p2 = st[(a * NB2 + cc) * n];
-            A::mac(f[cc], p2, sc[a]);
-            if (rev) A::mac_cx(rX[a], p2, rr[cc]);
-          }
-#pragma unroll
-        for (int i = 0; i < NB2; ++i) {
-          red[(2 * NB2 + 2 * i) * 32 + lane] = A::red_re(f[i]);
-          red[(2 * NB2 + 2 * i + 1) * 32 + lane] = A::red_im(f[i]);
-        }
-        if (rev) {
-#pragma unroll
-          for (int i = 0; i < NB2; ++i) {
-            A::renorm(rX[i]);
-            A::renorm(rY[i]);
-          }
-        }
-      }
-    }
-    // the stage buffer is free once every lane has read it: order those reads before the next
-    // bulk copy into it (generic -> async proxy), then refill it
-    fence_proxy_async();
+    if (lane < 2 * NB2) rowv[lane] = rs[(size_t)b.row * 2 * NB2 + lane];
     __syncwarp();
-    if (lane == 0 && c + 2 < nch) issue(c + 2);
-    if (c & 1) {  // both halves of the row block are in the scratch: forward reduction
-      constexpr int LPV = 32 / NV > 0 ? 32 / NV : 1;
-      for (int v0 = 0; v0 < NV; v0 += 32 / LPV) {
-        const int v = v0 + lane / LPV;
-        const int part = lane % LPV;
-        R s = A::red_zero();
-        if (v < NV) {
-          const int span = 32 / LPV;
-          for (int j = part * span; j < (part + 1) * span; ++j)
-            if ((b.mask >> j) & 1u) A::red_add(s, red[v * 32 + j]);
-        }
-#pragma unroll
-        for (int m = 1; m < LPV; m <<= 1) A::red_add(s, A::red_shfl_xor(s, m));
-        if (v < NV && part == 0) atomicAdd(acc + (size_t)b.row * 2 * NB2 * 2 + v, A::red_to_double(s));
+#pragma unroll 1
+    for (int q = 0; q < CPR; ++q) {
+      const int c = rbi * CPR + q;
+      if (!mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1), errflag)) {
+        failed = true;
+        break;
       }
+      const E* st = stage0 + (size_t)(c & 1) * SE + slot;
+      const int l0 = (q % CPM) * LINES;
+      if (active) {
+        if (q < CPM) {
+          // P1 rows a = l0..: X_k[a] = sum_cc P1[a][cc] rt_col[cc];  Y_col[cc] += st_k[a] conj(P1[a][cc])
+#pragma unroll
+          for (int r = 0; r < LINES; ++r) {
+            const int a = l0 + r;
+            const E sra = rowv[NB2 + a];
+            Acc f;
+            A::zero(f);
+#pragma unroll
+            for (int cc = 0; cc < NB2; ++cc) {
+              const E p1 = st[(r * NB2 + cc) * n];
+              A::mac(f, p1, rc[cc]);
+              if (rev) A::mac_cx(rY[cc], p1, sra);
+            }
+            red[(2 * a) * 32 + lane] = A::red_re(f);
+            red[(2 * a + 1) * 32 + lane] = A::red_im(f);
+          }
+        } else {
+          // P2 columns cc = l0..: Y_k[cc] = sum_a st_col[a] P2[a][cc];  X_col[a] += conj(P2[a][cc]) rt_k[cc]
+#pragma unroll
+          for (int r = 0; r < LINES; ++r) {
+            const int cc = l0 + r;
+            const E rrc = rowv[cc];
+            Acc f;
+            A::zero(f);
+#pragma unroll
+            for (int a = 0; a < NB2; ++a) {
+              const E p2 = st[(r * NB2 + a) * n];
+              A::mac(f, p2, sc[a]);
+              if (rev) A::mac_cx(rX[a], p2, rrc);
+            }
+            red[(2 * NB2 + 2 * cc) * 32 + lane] = A::red_re(f);
+            red[(2 * NB2 + 2 * cc + 1) * 32 + lane] = A::red_im(f);
+          }
+        }
+      }
+      // the stage buffer is free once every lane has read it: order those reads before the next
+      // bulk copy into it (generic -> async proxy), then refill it
+      fence_proxy_async();
       __syncwarp();
+      if (lane == 0 && c + 2 < nch) issue(c + 2);
     }
+    if (failed) break;
+    if (active && rev) {
+#pragma unroll
+      for (int i = 0; i < NB2; ++i) {
+        A::renorm(rX[i]);
+        A::renorm(rY[i]);
+      }
+    }
+    // the row block is complete: forward reduction over the active lanes
+    constexpr int LPV = 32 / NV > 0 ? 32 / NV : 1;
+#pragma unroll 1
+    for (int v0 = 0; v0 < NV; v0 += 32 / LPV) {
+      const int v = v0 + lane / LPV;
+      const int part = lane % LPV;
+      R s = A::red_zero();
+      if (v < NV) {
+        const int span = 32 / LPV;
+        unsigned m = (b.mask >> (part * span)) & (span == 32 ? 0xffffffffu : ((1u << span) - 1u));
+        while (m) {
+          const int j = __ffs(m) - 1;
+          m &= m - 1;
+          A::red_add(s, red[v * 32 + part * span + j]);
+        }
+      }
+#pragma unroll
+      for (int mm = 1; mm < LPV; mm <<= 1) A::red_add(s, A::red_shfl_xor(s, mm));
+      if (v < NV && part == 0) atomicAdd(acc + (size_t)b.row * 2 * NB2 * 2 + v, A::red_to_double(s));
+    }
+    __syncwarp();
   }
   if (failed) {  // drain whatever copies are still pending (bounded), then leave
     if (lane == 0) {
