@@ -161,13 +161,17 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """dram bytes per pair-kernel launch from the committed ncu summary, scaled to this workload."""
-    p = os.path.join(ROOT, "profiles", "pairs_kernel_gaas_traffic.json")
+def profile_traffic(precision):
+    """DRAM bytes per pair-kernel launch from the committed ncu summary of this arithmetic, as
+    (bytes, npair of the captured workload); scaled by the caller to the benchmarked workload."""
+    p = os.path.join(ROOT, "profiles", "pairs_cb_tma_%s_gaas_nk8k.md" % precision)
     try:
+        vals = {}
         with open(p) as f:
-            j = json.load(f)
-        return j
+            for line in f:
+                if ":" in line and line.split(":")[0].strip() in ("traffic_bytes_per_launch", "traffic_npair"):
+                    vals[line.split(":")[0].strip()] = float(line.split(":")[1])
+        return vals["traffic_bytes_per_launch"], vals["traffic_npair"]
     except Exception:
         return None
 
@@ -321,10 +325,10 @@ def run_gpu(args, w, rank, world, dist):
     bpl = algorithmic_bytes(nb, st.npair, st.cfg.nk, 16)
     pair_avg_ms = pair_ms / max(pair_n, 1)
     achieved = bpl / (pair_avg_ms * 1e-3) / 1e9
-    tr = profile_traffic()
+    tr = profile_traffic(args.precision)
     traffic = None
-    if tr and tr.get("npair"):
-        traffic = tr["dram_bytes_per_launch"] * st.npair / tr["npair"]
+    if tr:
+        traffic = tr[0] * st.npair / tr[1]   # the capture's bytes per pair times this workload's pairs
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": {"f64": "f64", "f64x": "f64 (fp32-pair emulated)", "f32": "f32",
@@ -350,7 +354,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="gaas_nk20k")
-    ap.add_argument("--precision", default="f64", choices=["f64", "f64x", "f32", "bf16x2"])
+    ap.add_argument("--precision", default="f64x", choices=["f64", "f64x", "f32", "bf16x2"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()

@@ -534,6 +534,11 @@ int dmd_destroy(dmd_handle* h) {
 int dmd_set_ddmdt_eq(dmd_handle* h, const double* eq) {
   if (!h) return DMD_E_ARG;
   CK(cudaSetDevice(h->dev));
+  CK(cudaStreamSynchronize(h->st));
+  if (h->g_rk4) {  // the captured step holds the drift pointer: capture again at the next dmd_rk4
+    cudaGraphExecDestroy(h->g_rk4);
+    h->g_rk4 = nullptr;
+  }
   if (!eq) {
     if (h->d_eq) cudaFree(h->d_eq);
     h->d_eq = nullptr;

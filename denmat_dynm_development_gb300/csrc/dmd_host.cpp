@@ -5,6 +5,7 @@
 
 #include <sys/stat.h>
 
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -130,15 +131,94 @@ bool read_file(const std::string& path, size_t expect, void* dst, std::string& w
 
 }  // namespace
 
+// Carrier counting and chemical potentials. The impurity-level carriers of partially ionised
+// impurities (Scatt_Param.h:82-94) are zero for the impurities accepted here.
+namespace {
+
+int isgn(double v) { return (0. < v) - (v < 0.); }  // sgn (electron.cpp:3-5)
+
+// electron::compute_nfree (electron.cpp:578-596): e is [nk][nb], valence bands [0, nv)
+double compute_nfree(bool isHole, double T, double mu, const double* e, int nk, int nb, int nv) {
+  const int b0 = isHole ? 0 : nv, b1 = isHole ? nv : nb;
+  double r = 0.;
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = b0; i < b1; i++) {
+      const double f = fermi(T, mu, e[(size_t)ik * nb + i]);
+      if (!isHole) r += f;
+      else r += (f - 1.);
+    }
+  return r;
+}
+
+// electron::find_mu by bisection in [emin, emax] (electron.cpp:537-572)
+double find_mu_bisect(double carrier_bvk, bool is_excess, double T, double emin, double emax, const double* e, int nk,
+                      int nb, int nv) {
+  const bool isHole = carrier_bvk < 0;
+  double lo = emin, hi = emax, result = 0, cnew;
+  for (int niter = 1; niter <= 200; niter++) {
+    result = 0.5 * (lo + hi);
+    if (is_excess)
+      cnew = compute_nfree(true, T, result, e, nk, nb, nv) + 0. + compute_nfree(false, T, result, e, nk, nb, nv) + 0.;
+    else
+      cnew = compute_nfree(isHole, T, result, e, nk, nb, nv) + 0.;
+    if (fabs(cnew - carrier_bvk) < 1e-12) return result;
+    if (cnew > carrier_bvk) hi = result;
+    else lo = result;
+  }
+  return result;
+}
+
+// singdenmat_k::compute_nfree_eq (DenMat.cpp:198-225) over bands [b0, b1) of e_dm [nk][nb]
+double nfree_eq(bool isHole, double T, double mu, const double* e, int nk, int nb, int b0, int b1) {
+  double r = 0.;
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = b0; i < b1; i++) {
+      const double f = fermi(T, mu, e[(size_t)ik * nb + i]);
+      if (!isHole) r += f;
+      else r += (f - 1.);
+    }
+  return r;
+}
+
+// singdenmat_k::find_mu: damped search from mu0 (DenMat.cpp:150-197)
+double find_mu_eq(bool isHole, double carrier_bvk, double T, double mu0, const double* e, int nk, int nb, int b0,
+                  int b1) {
+  double result = mu0, damp = 0.7, dmu = 5e-6, eoo = 1., eo = 1.;
+  for (int step = 0;;) {
+    const double cnew = nfree_eq(isHole, T, result, e, nk, nb, b0, b1) + 0.;
+    const double excess = cnew - carrier_bvk;
+    if (!(fabs(excess) > 1e-14)) break;
+    if (fabs(excess) > fabs(eo) || fabs(excess) > fabs(eoo)) dmu *= damp;
+    result -= isgn(excess) * dmu;
+    if (step > 0 && isgn(excess) == isgn(eo)) {
+      const double ratio = cnew / carrier_bvk;
+      if (ratio < 1e-9) result -= (double)(isgn(excess) * 10) * T;
+      else if (ratio < 1e-4) result -= (double)(isgn(excess) * 3) * T;
+      else if (ratio < 0.1) result -= isgn(excess) * 0.7 * T;
+    }
+    if (dmu < 1e-16) break;
+    eoo = eo;
+    eo = excess;
+    step++;
+    if (step > 1e4) break;
+  }
+  return result;
+}
+
+}  // namespace
+
 struct dmdh_system {
   std::map<std::string, std::string> pm;
   dmdh_info info;
   std::vector<double> e_dm, f_dm;
+  std::vector<double> f_eq;         // [nk][nb_dm] with alg_ddmdteq
   std::vector<double> smat;         // complex [nk][3][nb_dm^2]
   std::vector<uint64_t> k1, k2;
   std::vector<double> P1, P2;       // complex [nkpair][nb^4], folded
   std::vector<double> dm0;          // complex [nk][nb_dm^2]
   std::vector<double> H;            // complex [nk][nb_dm^2] or empty
+  double carrier_gs[3] = {0, 0, 0};  // eip.carrier_bvk_gs, ne_bvk_gs, nh_bvk_gs (electron.h:155-157)
+  int nimp = 0;                      // number of impurity densities (eip.ni.size())
 };
 
 extern "C" {
@@ -214,7 +294,7 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
   // features outside this path are rejected explicitly
   const char* unsupported[] = {"alg_linearize", "alg_linearize_dPee", "alg_phenom_relax", "alg_semiclassical",
                                "alg_sparseP", "alg_Pin_is_sparse", "alg_only_eimp", "alg_only_ee", "needL",
-                               "alg_read_Bso", "gfac_normal_dist", "alg_ddmdteq"};
+                               "alg_read_Bso", "gfac_normal_dist", "partial_ionized"};
   for (const char* k : unsupported)
     if (pget(pm, k, 0) != 0) return err(DMD_E_ARG, std::string(k) + " is not supported by the GB300 path");
   if (sget(pm, "code", "jdftx") != "jdftx" || sget(pm, "material_model", "none") != "none")
@@ -300,10 +380,40 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
   s->e_dm.resize((size_t)nk * nb_dm);
   s->f_dm.resize((size_t)nk * nb_dm);
   for (int ik = 0; ik < nk; ik++)
-    for (int b = 0; b < nb_dm; b++) {
-      s->e_dm[(size_t)ik * nb_dm + b] = e[(size_t)ik * nb + bStart_dm + b];
-      s->f_dm[(size_t)ik * nb_dm + b] = fermi(T, in.mu, e[(size_t)ik * nb + bStart_dm + b]);
+    for (int b = 0; b < nb_dm; b++) s->e_dm[(size_t)ik * nb_dm + b] = e[(size_t)ik * nb + bStart_dm + b];
+  // electron constructor energy range (electron.h:94-105) and set_mu_and_n (electron.h:141-160)
+  {
+    const int nvd = in.nv_dm;
+    double emax = -DBL_MAX, ecmin = DBL_MAX, evmax = -DBL_MAX, emin = DBL_MAX;
+    for (int ik = 0; ik < nk; ik++) {
+      for (int b = nvd; b < nb_dm; b++) {
+        const double v = s->e_dm[(size_t)ik * nb_dm + b];
+        if (v > emax) emax = v;
+        if (v < ecmin) ecmin = v;
+      }
+      for (int b = 0; b < nvd; b++) {
+        const double v = s->e_dm[(size_t)ik * nb_dm + b];
+        if (v > evmax) evmax = v;
+        if (v < emin) emin = v;
+      }
     }
+    if (nb_dm == nvd) emax = evmax + 1;
+    if (nvd == 0) emin = ecmin - 1;
+    const double cd = pget(pm, "carrier_density", 0, std::pow(kBohr2cm, dim));
+    const bool excess = pget(pm, "carrier_density_means_excess_density", 0) != 0;
+    if (cd != 0 && !excess) in.mu = find_mu_bisect(cd * nk_full * cell, false, T, emin, emax, e.data(), nk, nb, nv);
+    if (excess) in.mu = find_mu_bisect(cd * nk_full * cell, true, T, emin, emax, e.data(), nk, nb, nv);
+    const double ne = compute_nfree(false, T, in.mu, e.data(), nk, nb, nv) / nk_full / cell;
+    const double nh = compute_nfree(true, T, in.mu, e.data(), nk, nb, nv) / nk_full / cell;
+    const double nei = 0. / nk_full / cell, nhi = 0. / nk_full / cell;
+    double gs = fabs(ne + nei) > fabs(nh + nhi) ? ne + nei : nh + nhi;
+    s->carrier_gs[0] = gs * nk_full * cell;
+    s->carrier_gs[1] = ne * nk_full * cell;
+    s->carrier_gs[2] = nh * nk_full * cell;
+  }
+  for (int ik = 0; ik < nk; ik++)
+    for (int b = 0; b < nb_dm; b++)
+      s->f_dm[(size_t)ik * nb_dm + b] = fermi(T, in.mu, e[(size_t)ik * nb + bStart_dm + b]);
   // spin matrices (electron.cpp:284-314)
   s->smat.resize((size_t)nk * 3 * nb_dm * nb_dm * 2);
   if (!read_file(dir + "/ldbd_data/ldbd_smat.bin", s->smat.size() * 8, s->smat.data(), why)) return err(DMD_E_FILE, why);
@@ -350,6 +460,7 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
     if (ni == 0) break;
     if (sget(pm, "impMode" + nm, "model_ionized") != "ab_neutral")
       return err(DMD_E_ARG, "only impMode = ab_neutral is supported");
+    s->nimp = iD + 1;
     const double fraction = fabs(ni * cell);  // electronimpurity ctor (ElectronImpurity.h:18)
     if (iD == 0) in.eimp_fraction = fraction;
     A1.assign(2 * np4, 0.0);
@@ -405,6 +516,43 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
                            s->dm0.data());
     if (rc) return err(rc, "dm_Bpert");
   }
+  // equilibrium occupations for the drift subtraction (DensityMatrix_Dynamics.h:58-63 ->
+  // singdenmat_k::set_dm_eq, DenMat.cpp:97-148, on the initial or restart state)
+  in.mue = in.muh = in.mu;
+  if (pget(pm, "alg_ddmdteq", 0) != 0) {
+    in.ddmdteq = 1;
+    const int nvd = in.nv_dm;
+    const zc* dm = (const zc*)s->dm0.data();
+    double mus[2] = {in.mu, in.mu};
+    for (int pass = 0; pass < 2; pass++) {
+      const bool isHole = pass == 1;
+      if (!isHole && !(nb_dm > nvd)) continue;
+      if (isHole && !(nvd > 0)) continue;
+      const int b0 = isHole ? 0 : nvd, b1 = isHole ? nvd : nb_dm;
+      double nfree = 0.;
+      for (int ik = 0; ik < nk; ik++)
+        for (int i = b0; i < b1; i++) {
+          if (!isHole) nfree += dm[(size_t)ik * nb_dm * nb_dm + i * nb_dm + i].x;
+          else nfree += (dm[(size_t)ik * nb_dm * nb_dm + i * nb_dm + i].x - 1.);
+        }
+      // elecimpParam::carrier_bvk_ex (Scatt_Param.h:63-68)
+      const double* gs = s->carrier_gs;
+      double target;
+      if (s->nimp == 0 || (gs[0] > 0 && isHole) || (gs[0] < 0 && !isHole)) target = nfree;
+      else if (gs[0] < 0 && isHole) target = gs[0] + (nfree - gs[2]);
+      else if (gs[0] > 0 && !isHole) target = gs[0] + (nfree - gs[1]);
+      else return err(DMD_E_ARG, "alg_ddmdteq with impurities needs a non-zero ground-state carrier density");
+      double m = find_mu_eq(isHole, target, T, mus[pass], s->e_dm.data(), nk, nb_dm, b0, b1);
+      if (pget(pm, "DEBUG", 0) != 0) m = mus[pass];
+      mus[pass] = m;
+    }
+    in.mue = mus[0];
+    in.muh = mus[1];
+    s->f_eq.resize((size_t)nk * nb_dm);
+    for (int ik = 0; ik < nk; ik++)
+      for (int i = 0; i < nb_dm; i++)
+        s->f_eq[(size_t)ik * nb_dm + i] = fermi(T, i < nvd ? in.muh : in.mue, s->e_dm[(size_t)ik * nb_dm + i]);
+  }
   // coherent Hamiltonian (main.cpp:51)
   const double Blen = sqrt(in.B[0] * in.B[0] + in.B[1] * in.B[1] + in.B[2] * in.B[2]);
   if (Blen > 1e-10) {
@@ -456,6 +604,43 @@ int dmdh_get_f(const dmdh_system* s, double* f) {
   memcpy(f, s->f_dm.data(), s->f_dm.size() * 8);
   return DMD_OK;
 }
+int dmdh_get_f_eq(const dmdh_system* s, double* f_eq) {
+  if (!s || !f_eq) return DMD_E_ARG;
+  if (s->f_eq.empty()) return err(DMD_E_ARG, "alg_ddmdteq is off: no equilibrium occupations");
+  memcpy(f_eq, s->f_eq.data(), s->f_eq.size() * 8);
+  return DMD_OK;
+}
+
+int dmdh_prepare(const dmdh_system* s, dmd_handle* h) {
+  if (!s || !h) return DMD_E_ARG;
+  if (!s->info.ddmdteq) return dmd_set_ddmdt_eq(h, nullptr);
+  // electronphonon::compute_ddmdt_eq (evolve_eph.cpp:3-19): the scattering term of diag(f_eq) at t = 0,
+  // cut to the e-ph window; the stored drift is cleared first so that nothing is subtracted from it
+  const dmdh_info& in = s->info;
+  const int nd = in.nb_dm, nb = in.bend - in.bstart;
+  const size_t nd2 = (size_t)nd * nd;
+  int rc = dmd_set_ddmdt_eq(h, nullptr);
+  if (rc) return err(rc, dmd_last_error(h));
+  std::vector<double> y((size_t)in.nk * nd2 * 2, 0.0), y1(y.size(), 0.0), out(y.size()),
+      eq((size_t)in.nk * nb * nb * 2);
+  for (int ik = 0; ik < in.nk; ik++)
+    for (int i = 0; i < nd; i++) {
+      y[((size_t)ik * nd2 + (size_t)i * nd + i) * 2] = s->f_eq[(size_t)ik * nd + i];
+      y1[((size_t)ik * nd2 + (size_t)i * nd + i) * 2] = 1 - s->f_eq[(size_t)ik * nd + i];
+    }
+  if ((rc = dmd_evolve_driver(h, 0.0, y.data(), y1.data(), out.data()))) return err(rc, dmd_last_error(h));
+  for (int ik = 0; ik < in.nk; ik++)
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < nb; j++) {
+        const size_t src = ((size_t)ik * nd2 + (size_t)(i + in.bstart) * nd + j + in.bstart) * 2;
+        const size_t dst = ((size_t)ik * nb * nb + (size_t)i * nb + j) * 2;
+        eq[dst] = out[src];
+        eq[dst + 1] = out[src + 1];
+      }
+  if ((rc = dmd_set_ddmdt_eq(h, eq.data()))) return err(rc, dmd_last_error(h));
+  return DMD_OK;
+}
+
 int dmdh_get_smat(const dmdh_system* s, double* smat) {
   if (!s || !smat) return DMD_E_ARG;
   memcpy(smat, s->smat.data(), s->smat.size() * 8);
@@ -548,6 +733,7 @@ extern "C" int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max) 
   } closer{h};
   const size_t ny = (size_t)in.nk * in.nb_dm * in.nb_dm * 2;
   std::vector<double> ybuf(ny);
+  if ((rc = dmdh_prepare(s, h))) return rc;
   if ((rc = dmd_set_state(h, in.t0, s->dm0.data()))) return err(rc, dmd_last_error(h));
   std::vector<double> obs((size_t)in.nk * in.nb_dm * in.nb_dm * 2);
   const size_t nd2 = (size_t)in.nb_dm * in.nb_dm;

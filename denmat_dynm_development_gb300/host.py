@@ -13,7 +13,8 @@ from . import dmd as _dmd
 _L = None
 
 EXPORTS = ["dmdh_load", "dmdh_free", "dmdh_error", "dmdh_info_get", "dmdh_desc", "dmdh_get_dm0", "dmdh_get_f",
-           "dmdh_get_smat", "dmdh_param", "dmdh_fermi", "dmdh_dm_bpert", "dmdh_H_BS", "dmdh_run"]
+           "dmdh_get_smat", "dmdh_get_f_eq", "dmdh_prepare", "dmdh_param", "dmdh_fermi", "dmdh_dm_bpert",
+           "dmdh_H_BS", "dmdh_run"]
 
 
 class Info(C.Structure):
@@ -23,7 +24,8 @@ class Info(C.Structure):
                 ("cell_size_cmd", C.c_double), ("ob_prefac", C.c_double), ("t0", C.c_double), ("tend", C.c_double),
                 ("tstep", C.c_double), ("ode_hstart", C.c_double), ("ode_hmin", C.c_double), ("ode_hmax", C.c_double),
                 ("ode_epsabs", C.c_double), ("Bpert", C.c_double * 3), ("B", C.c_double * 3), ("picture", C.c_int32),
-                ("expt", C.c_int32), ("has_H", C.c_int32), ("ode_method", C.c_int32), ("eimp_fraction", C.c_double)]
+                ("expt", C.c_int32), ("has_H", C.c_int32), ("ode_method", C.c_int32), ("eimp_fraction", C.c_double),
+                ("mue", C.c_double), ("muh", C.c_double), ("ddmdteq", C.c_int32), ("reserved", C.c_int32)]
 
 
 def _lib():
@@ -42,6 +44,8 @@ def _lib():
         L.dmdh_get_dm0.argtypes = [vp, vp]
         L.dmdh_get_f.argtypes = [vp, vp]
         L.dmdh_get_smat.argtypes = [vp, vp]
+        L.dmdh_get_f_eq.argtypes = [vp, vp]
+        L.dmdh_prepare.argtypes = [vp, vp]
         L.dmdh_param.argtypes = [vp, C.c_char_p, d, C.POINTER(d), C.POINTER(C.c_int)]
         L.dmdh_fermi.argtypes = [d, d, vp, vp, C.c_size_t]
         L.dmdh_dm_bpert.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, d, vp, d, C.c_int32, vp]
@@ -81,6 +85,10 @@ class System:
         _ck(_lib().dmdh_get_f(h, self.f_dm.ctypes.data))
         self.smat = np.zeros((i.nk, 3, nd2), np.complex128)
         _ck(_lib().dmdh_get_smat(h, self.smat.ctypes.data))
+        self.f_eq = None
+        if i.ddmdteq:
+            self.f_eq = np.zeros((i.nk, i.nb_dm), np.float64)
+            _ck(_lib().dmdh_get_f_eq(h, self.f_eq.ctypes.data))
         desc = self.desc()
         nb = i.bend - i.bstart
         n4 = int(i.nkpair) * nb ** 4
@@ -106,11 +114,18 @@ class System:
         return v.value if f.value else None
 
     def gpu(self, precision="f64", device=0):
-        """A LindbladGPU built from this system (dmd_create on the loaded arrays)."""
+        """A LindbladGPU built from this system (dmd_create on the loaded arrays), with the
+        equilibrium drift installed when alg_ddmdteq is on (dmdh_prepare)."""
         i = self.info
-        return _dmd.LindbladGPU(nk=i.nk, nb_dm=i.nb_dm, bstart=i.bstart, bend=i.bend, e_dm=self.e_dm,
-                                k1st=self.k1st, k2nd=self.k2nd, P1=self.P1, P2=self.P2, prefac_eph=i.prefac_eph,
-                                Hcoh=self.Hcoh, picture=i.picture, expt=i.expt, precision=precision, device=device)
+        g = _dmd.LindbladGPU(nk=i.nk, nb_dm=i.nb_dm, bstart=i.bstart, bend=i.bend, e_dm=self.e_dm,
+                             k1st=self.k1st, k2nd=self.k2nd, P1=self.P1, P2=self.P2, prefac_eph=i.prefac_eph,
+                             Hcoh=self.Hcoh, picture=i.picture, expt=i.expt, precision=precision, device=device)
+        try:
+            _ck(_lib().dmdh_prepare(self._h, g._h))
+        except Exception:
+            g.close()
+            raise
+        return g
 
     def close(self):
         if getattr(self, "_h", None):

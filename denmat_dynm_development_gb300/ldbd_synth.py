@@ -63,6 +63,7 @@ class SynthConfig:
     eimp_sigma_mev: Optional[float] = None   # write D1 e-imp files when set
     ecbm_ha: float = 0.05            # absolute energy of the band bottom (Ha)
     extra_bands: int = 0             # bands of the density matrix below the e-ph window
+    nv: int = 0                      # lowest bands declared valence in ldbd_size.dat (holes)
     chunk_pairs: int = 1 << 18
 
     def to_dict(self):
@@ -382,8 +383,8 @@ def make_ldbd(outdir: str, cfg: SynthConfig, write_param: bool = True, threads: 
     mu, T = st.mu, st.T
     with open(os.path.join(d, "ldbd_size.dat"), "w") as f:
         f.write("There are scatterings only for conduction electrons\n")
-        f.write("%d 0 0 %d %d %d %d 0 0 # nb nv bBot_dm bTop_dm bBot_eph_elec bTop_eph_elec nb_wannier bBot_probe band_dft_skipped\n"
-                % (ndm, ndm, nx, ndm, ndm))
+        f.write("%d %d 0 %d %d %d %d 0 0 # nb nv bBot_dm bTop_dm bBot_eph_elec bTop_eph_elec nb_wannier bBot_probe band_dft_skipped\n"
+                % (ndm, cfg.nv, ndm, nx, ndm, ndm))
         f.write("%21.14le %d %d %d %d # nk_full nk kmesh\n" % (float(n) ** 3, cfg.nk, n, n, n))
         f.write("%d # nkpair_elec\n" % st.npair)
         f.write("0 %d 0 0# modeStart modeStp modeSkipStart modeSkipStop\n" % cfg.nmodes)

@@ -40,11 +40,15 @@ typedef struct dmdh_info {
   double Bpert[3], B[3];
   int32_t picture, expt, has_H, ode_method; /* ode_method: 0 rkf45, 1 euler, 2 rk4 */
   double eimp_fraction;
+  double mue, muh;  /* chemical potentials of the equilibrium occupations (set_dm_eq), = mu otherwise */
+  int32_t ddmdteq;  /* alg_ddmdteq: the equilibrium drift is subtracted from the scattering term */
+  int32_t reserved;
 } dmdh_info;
 
 /* Read param.in + ldbd_data/ from directory dir (the reference's working directory layout) and
- * perform DMD's set-up: band windows, occupations, folded P (scale_eph and |n_i V| * D1), initial
- * density matrix and coherent Hamiltonian. */
+ * perform DMD's set-up: band windows, chemical potential (carrier_density, electron.h:141-160),
+ * occupations, folded P (scale_eph and |n_i V| * D1), initial density matrix, coherent Hamiltonian
+ * and, with alg_ddmdteq, the equilibrium occupations of singdenmat_k::set_dm_eq (DenMat.cpp:97-225). */
 int dmdh_load(const char* dir, dmdh_system** out);
 void dmdh_free(dmdh_system* s);
 const char* dmdh_error(void);
@@ -56,6 +60,12 @@ int dmdh_desc(const dmdh_system* s, int32_t precision, int32_t device, dmd_desc*
 int dmdh_get_dm0(const dmdh_system* s, double* dm0);
 int dmdh_get_f(const dmdh_system* s, double* f);
 int dmdh_get_smat(const dmdh_system* s, double* smat);
+/* equilibrium occupations f_eq (double [nk][nb_dm]); DMD_E_ARG unless alg_ddmdteq */
+int dmdh_get_f_eq(const dmdh_system* s, double* f_eq);
+/* Per-handle set-up after dmd_create: with alg_ddmdteq, computes the equilibrium drift on the GPU
+ * (electronphonon::compute_ddmdt_eq, evolve_eph.cpp:3-19, via dmd_evolve_driver at t = 0) and
+ * installs it with dmd_set_ddmdt_eq; otherwise clears it. */
+int dmdh_prepare(const dmdh_system* s, dmd_handle* h);
 
 /* value of a param.in key after get()'s unit conversion; returns 0 and *found = 1 if present */
 int dmdh_param(const dmdh_system* s, const char* key, double unit, double* value, int* found);

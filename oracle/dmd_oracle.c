@@ -516,3 +516,153 @@ void orc_rhs_from_partials(const orc_sys* s, double t, const double* y, const do
         out[(size_t)ik * nd2 + i * nd + j] = zadd(out[(size_t)ik * nd2 + i * nd + j], w->ddmdt_eph[(size_t)ik * nb2 + (i - bs) * nb + j - bs]);
   orc_ws_free(w);
 }
+
+/* ------------------------------------------------------------------------------------------------
+ * Chemical potential and the equilibrium drift (set-up, once per run)
+ * ---------------------------------------------------------------------------------------------- */
+static double fermi1(double T, double mu, double e) { /* electron::fermi, electron.h:119-124 */
+  const double ebyt = (e - mu) / T;
+  if (ebyt < -46) return 1;
+  else if (ebyt > 46) return 0;
+  else return 1. / (exp(ebyt) + 1);
+}
+static int isgn(double v) { return (0. < v) - (v < 0.); } /* sgn, electron.cpp:3-5 / DenMat.cpp:3-5 */
+
+/* electron::compute_nfree -- electron.cpp:578-596 (one rank; e is [nk][nb], valence bands [0, nv)) */
+double orc_compute_nfree(int isHole, double T, double mu, const double* e, int nk, int nb, int nv) {
+  const int b0 = isHole ? 0 : nv, b1 = isHole ? nv : nb;
+  double r = 0.;
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = b0; i < b1; i++) {
+      const double f = fermi1(T, mu, e[(size_t)ik * nb + i]);
+      if (!isHole) r += f;
+      else r += (f - 1.);
+    }
+  return r;
+}
+
+/* electron::find_mu by bisection -- electron.cpp:537-572. The impurity-level carriers
+ * (Scatt_Param.h:82-94) are zero without partially ionised impurities, the only case accepted. */
+double orc_find_mu_bisect(double carrier_bvk, int is_excess, double T, double emin, double emax, const double* e,
+                          int nk, int nb, int nv) {
+  const int isHole = carrier_bvk < 0;
+  double lo = emin, hi = emax, result = 0, cnew;
+  int niter = 0;
+  while (niter < 200) {
+    niter++;
+    result = 0.5 * (lo + hi);
+    if (is_excess)
+      cnew = orc_compute_nfree(1, T, result, e, nk, nb, nv) + 0. + orc_compute_nfree(0, T, result, e, nk, nb, nv) + 0.;
+    else
+      cnew = orc_compute_nfree(isHole, T, result, e, nk, nb, nv) + 0.;
+    const double error = cnew - carrier_bvk;
+    if (fabs(error) < 1e-12) return result;
+    if (cnew > carrier_bvk) hi = result;
+    else lo = result;
+  }
+  return result;
+}
+
+/* singdenmat_k::compute_nfree_eq -- DenMat.cpp:198-225 (e = e_dm [nk][nb], bands [b0, b1)) */
+static double nfree_eq(int isHole, double T, double mu, const double* e, int nk, int nb, int b0, int b1) {
+  double r = 0.;
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = b0; i < b1; i++) {
+      const double f = fermi1(T, mu, e[(size_t)ik * nb + i]);
+      if (!isHole) r += f;
+      else r += (f - 1.);
+    }
+  return r;
+}
+
+/* singdenmat_k::find_mu -- DenMat.cpp:150-197 (damped search from mu0) */
+double orc_find_mu_eq(int isHole, double carrier_bvk, double T, double mu0, const double* e, int nk, int nb, int b0,
+                      int b1) {
+  double result = mu0, damp = 0.7, dmu = 5e-6;
+  double eoo = 1., eo = 1., excess, cnew;
+  int step = 0;
+  while (1) {
+    cnew = nfree_eq(isHole, T, result, e, nk, nb, b0, b1) + 0.;
+    excess = cnew - carrier_bvk;
+    if (fabs(excess) > 1e-14) {
+      if (fabs(excess) > fabs(eo) || fabs(excess) > fabs(eoo)) dmu *= damp;
+      result -= isgn(excess) * dmu;
+      if (step > 0 && isgn(excess) == isgn(eo)) {
+        const double ratio = cnew / carrier_bvk;
+        if (ratio < 1e-9) result -= (double)(isgn(excess) * 10) * T;
+        else if (ratio < 1e-4) result -= (double)(isgn(excess) * 3) * T;
+        else if (ratio < 0.1) result -= isgn(excess) * 0.7 * T;
+      }
+      if (dmu < 1e-16) break;
+      eoo = eo;
+      eo = excess;
+      step++;
+      if (step > 1e4) break;
+    } else
+      break;
+  }
+  return result;
+}
+
+/* elecimpParam::carrier_bvk_ex -- Scatt_Param.h:63-68. gs[0..2] = carrier_bvk_gs, ne_bvk_gs, nh_bvk_gs
+ * (electron.h:155-157); nimp = number of impurity densities. Returns 0 in *ok for the combination the
+ * reference leaves undefined (carrier_bvk_gs == 0 with impurities). */
+double orc_carrier_bvk_ex(int isHole, double n_bvk_ex, int nimp, const double* gs, int* ok) {
+  *ok = 1;
+  if (nimp == 0 || (gs[0] > 0 && isHole) || (gs[0] < 0 && !isHole)) return n_bvk_ex;
+  if (gs[0] < 0 && isHole) return gs[0] + (n_bvk_ex - gs[2]);
+  if (gs[0] > 0 && !isHole) return gs[0] + (n_bvk_ex - gs[1]);
+  *ok = 0;
+  return n_bvk_ex;
+}
+
+/* singdenmat_k::set_dm_eq -- DenMat.cpp:97-148 with compute_f (DenMat.h:74-83): the chemical
+ * potentials that keep the carrier numbers of dm, and the occupations f_eq [nk][nb_dm].
+ * mu[0..1] in: mue, muh start values; out: the found ones. Returns 0, or -1 for the undefined case. */
+int orc_set_dm_eq(int nk, int nb, int nv, const zc* dm, double T, const double* e, int nimp, const double* gs,
+                  int debug, double* mu, double* f_eq) {
+  for (int pass = 0; pass < 2; pass++) {
+    const int isHole = pass == 1;
+    if (!isHole && !(nb > nv)) continue;
+    if (isHole && !(nv > 0)) continue;
+    const int b0 = isHole ? 0 : nv, b1 = isHole ? nv : nb;
+    double nfree_bvk = 0.;
+    for (int ik = 0; ik < nk; ik++)
+      for (int i = b0; i < b1; i++) {
+        if (!isHole) nfree_bvk += dm[(size_t)ik * nb * nb + i * nb + i].x;
+        else nfree_bvk += (dm[(size_t)ik * nb * nb + i * nb + i].x - 1.);
+      }
+    int ok;
+    const double target = orc_carrier_bvk_ex(isHole, nfree_bvk, nimp, gs, &ok);
+    if (!ok) return -1;
+    double m = orc_find_mu_eq(isHole, target, T, mu[pass], e, nk, nb, b0, b1);
+    if (debug) m = mu[pass];
+    mu[pass] = m;
+  }
+  for (int ik = 0; ik < nk; ik++) {
+    for (int i = 0; i < nv; i++) f_eq[(size_t)ik * nb + i] = fermi1(T, mu[1], e[(size_t)ik * nb + i]);
+    for (int i = nv; i < nb; i++) f_eq[(size_t)ik * nb + i] = fermi1(T, mu[0], e[(size_t)ik * nb + i]);
+  }
+  return 0;
+}
+
+/* electronphonon::compute_ddmdt_eq -- evolve_eph.cpp:3-19: the scattering term at t = 0 of the
+ * diagonal state f_eq (1 - f_eq on the diagonal of dm1, zeros elsewhere), window [bstart, bend).
+ * s->ddmdt_eq must be NULL (it is still all zeros in the reference when this runs). */
+void orc_compute_ddmdt_eq(const orc_sys* s, const double* f_eq, double* ddmdt_eq) {
+  const int nk = s->nk, nd = s->nb_dm, nd2 = nd * nd, bs = s->bstart, be = s->bend, nb = be - bs;
+  orc_ws* w = orc_ws_new(s);
+  zc* dm = (zc*)xmalloc(sizeof(zc) * (size_t)nk * nd2);
+  zc* dm1 = (zc*)xmalloc(sizeof(zc) * (size_t)nk * nd2);
+  zc* out = (zc*)xmalloc(sizeof(zc) * (size_t)nk * nd2);
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = 0; i < nd; i++) {
+      dm[(size_t)ik * nd2 + i * nd + i] = zmk(f_eq[(size_t)ik * nd + i], 0);
+      dm1[(size_t)ik * nd2 + i * nd + i] = zmk(1 - f_eq[(size_t)ik * nd + i], 0);
+    }
+  orc_evolve_driver(s, w, 0., dm, dm1, out);
+  trunc_copy((zc*)ddmdt_eq, out, nk, nd, bs, be);
+  (void)nb;
+  free(dm); free(dm1); free(out);
+  orc_ws_free(w);
+}

@@ -81,6 +81,16 @@ def lib():
         _lib.orc_rhs_from_partials.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_fermi.argtypes = [C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_size_t]
+        _lib.orc_compute_nfree.argtypes = [C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_int, C.c_int, C.c_int]
+        _lib.orc_compute_nfree.restype = C.c_double
+        _lib.orc_find_mu_bisect.argtypes = [C.c_double, C.c_int, C.c_double, C.c_double, C.c_double, C.c_void_p,
+                                            C.c_int, C.c_int, C.c_int]
+        _lib.orc_find_mu_bisect.restype = C.c_double
+        _lib.orc_set_dm_eq.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_int,
+                                       C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        _lib.orc_set_dm_eq.restype = C.c_int
+        _lib.orc_compute_ddmdt_eq.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_compute_ddmdt_eq.restype = None
     return _lib
 
 
@@ -219,12 +229,17 @@ class OracleSystem:
     ob_prefac: float
     ode: dict
     params: dict
+    nv_dm: int = 0
+    mue: float = 0.0
+    muh: float = 0.0
+    f_eq: Optional[np.ndarray] = None        # [nk][nb_dm] with alg_ddmdteq
+    ddmdt_eq: Optional[np.ndarray] = None    # [nk][nb^2] window, subtracted from the scattering term
 
     def cstruct(self):
         s = _Sys(nk=self.nk, nb_dm=self.nb_dm, bstart=self.bstart, bend=self.bend, npair=self.npair,
                  k1st=_ptr(self.k1st), k2nd=_ptr(self.k2nd), P1=_ptr(self.P1), P2=_ptr(self.P2), e_dm=_ptr(self.e_dm),
                  prefac_eph=self.prefac_eph, Hcoh=_ptr(self.Hcoh), picture_schrodinger=self.picture_schrodinger,
-                 expt=self.expt, ddmdt_eq=None, scatt_enable=1)
+                 expt=self.expt, ddmdt_eq=_ptr(self.ddmdt_eq), scatt_enable=1)
         return s
 
     @property
@@ -247,8 +262,17 @@ def load(d: str) -> OracleSystem:
     scissor = pget(pm, "scissor", 0.0, eV)
     if scissor != 0:
         e[:, sz["nv"]:] += scissor
-    f = fermi(T, mu, e)
     e_dm = np.ascontiguousarray(e[:, sz["bStart_dm"]:sz["bEnd_dm"]])
+    nv_dm = max(sz["nv"] - sz["bStart_dm"], 0)  # electron.cpp:114
+    dim, R = read_R(d)
+    dim = int(pget(pm, "dim", dim))
+    vol = abs(det3(R))
+    cell_size = vol if dim == 3 else (vol / R[2, 2] if dim == 2 else (R[2, 2] if dim == 1 else 1.0))
+    nimp = 0
+    while pget(pm, "impurity_density" + ("" if nimp == 0 else str(nimp + 1)), 0.0) != 0:
+        nimp += 1
+    mu, gs = set_mu_and_n(pm, e, e_dm, sz, nv_dm, T, mu, cell_size, dim)
+    f = fermi(T, mu, e)
     f_dm = np.ascontiguousarray(f[:, sz["bStart_dm"]:sz["bEnd_dm"]])
     smat = np.fromfile(os.path.join(dd, "ldbd_smat.bin"), dtype=np.complex128).reshape(nk, 3, nb_dm * nb_dm)
     npair = sz["nkpair"]
@@ -264,9 +288,6 @@ def load(d: str) -> OracleSystem:
     if scale_eph != 1.0:
         P1 = P1 * complex(scale_eph, 0)
         P2 = P2 * complex(scale_eph, 0)
-    dim, R = read_R(d)
-    vol = abs(det3(R))
-    cell_size = vol if dim == 3 else (vol / R[2, 2] if dim == 2 else (R[2, 2] if dim == 1 else 1.0))
     ni = pget(pm, "impurity_density", 0.0, bohr2cm ** dim)
     if ni != 0:
         fraction = abs(ni * cell_size)
@@ -296,12 +317,65 @@ def load(d: str) -> OracleSystem:
     ode = dict(hstart=pget(pm, "ode_hstart", 1e-3, fs), hmin=pget(pm, "ode_hmin", 0.0, fs),
                hmax=pget(pm, "ode_hmax", tstep / fs, fs), epsabs=pget(pm, "ode_epsabs", 1e-8))
     cell_size_cmd = cell_size * bohr2cm ** dim
+    f_eq = ddmdt_eq = None
+    mue = muh = mu
+    if int(pget(pm, "alg_ddmdteq", 0)):
+        # DensityMatrix_Dynamics.h:58-63: set_dm_eq on the initial state, then compute_ddmdt_eq
+        f_eq = np.zeros((nk, nb_dm))
+        mus = np.array([mu, mu])
+        g = np.array(gs)
+        rc = L.orc_set_dm_eq(nk, nb_dm, nv_dm, dm0.ctypes.data, T, e_dm.ctypes.data, nimp, g.ctypes.data,
+                             int(pget(pm, "DEBUG", 0)), mus.ctypes.data, f_eq.ctypes.data)
+        assert rc == 0, "carrier_bvk_ex is undefined for this input (impurities with zero ground-state carriers)"
+        mue, muh = float(mus[0]), float(mus[1])
+        tmp = OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
+                           k1st=k1, k2nd=k2, P1=np.ascontiguousarray(P1), P2=np.ascontiguousarray(P2),
+                           prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=None, smat=smat, dm0=dm0,
+                           picture_schrodinger=schrod, expt=expt, t0=t0, tstep=0.0, tend=0.0, temperature=T, mu=mu,
+                           nk_full=sz["nk_full"], ob_prefac=1.0, ode={}, params={})
+        ddmdt_eq = np.zeros((nk, nb * nb), np.complex128)
+        cs = tmp.cstruct()
+        L.orc_compute_ddmdt_eq(C.addressof(cs), f_eq.ctypes.data, ddmdt_eq.ctypes.data)
     return OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
                         k1st=k1, k2nd=k2, P1=np.ascontiguousarray(P1), P2=np.ascontiguousarray(P2),
                         prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=Hcoh, smat=smat, dm0=dm0,
                         picture_schrodinger=schrod, expt=expt, t0=t0, tstep=tstep, tend=pget(pm, "tend", 0.0, fs),
                         temperature=T, mu=mu, nk_full=sz["nk_full"], ob_prefac=(1.0 / sz["nk_full"]) / cell_size_cmd,
-                        ode=ode, params=pm)
+                        ode=ode, params=pm, nv_dm=nv_dm, mue=mue, muh=muh, f_eq=f_eq, ddmdt_eq=ddmdt_eq)
+
+
+def set_mu_and_n(pm, e, e_dm, sz, nv_dm, T, mu, cell_size, dim):
+    """electron::set_mu_and_n (electron.h:141-160) with the energy range of the electron constructor
+    (electron.h:94-105). Returns mu and (carrier_bvk_gs, ne_bvk_gs, nh_bvk_gs)."""
+    L = lib()
+    nk, nb, nv = e.shape[0], e.shape[1], sz["nv"]
+    nb_dm = e_dm.shape[1]
+    big = np.finfo(np.float64).max
+    sub_c = e_dm[:, nv_dm:nb_dm]
+    sub_v = e_dm[:, 0:nv_dm]
+    emax = float(sub_c.max()) if sub_c.size else -big
+    ecmin = float(sub_c.min()) if sub_c.size else big
+    evmax = float(sub_v.max()) if sub_v.size else -big
+    emin = float(sub_v.min()) if sub_v.size else big
+    if nb_dm == nv_dm:
+        emax = evmax + 1
+    if nv_dm == 0:
+        emin = ecmin - 1
+    cd = pget(pm, "carrier_density", 0.0, bohr2cm ** dim)
+    excess = int(pget(pm, "carrier_density_means_excess_density", 0))
+    nk_full = sz["nk_full"]
+    ec = np.ascontiguousarray(e)
+    if cd != 0 and not excess:
+        mu = L.orc_find_mu_bisect(cd * nk_full * cell_size, 0, T, emin, emax, ec.ctypes.data, nk, nb, nv)
+    if excess:
+        mu = L.orc_find_mu_bisect(cd * nk_full * cell_size, 1, T, emin, emax, ec.ctypes.data, nk, nb, nv)
+    ne = L.orc_compute_nfree(0, T, mu, ec.ctypes.data, nk, nb, nv) / nk_full / cell_size
+    nh = L.orc_compute_nfree(1, T, mu, ec.ctypes.data, nk, nb, nv) / nk_full / cell_size
+    nei = 0.0 / nk_full / cell_size
+    nhi = 0.0 / nk_full / cell_size
+    gs = (ne + nei) if abs(ne + nei) > abs(nh + nhi) else (nh + nhi)
+    gs = gs * nk_full * cell_size
+    return mu, (gs, ne * nk_full * cell_size, nh * nk_full * cell_size)
 
 
 def _setup_prototypes():
@@ -336,7 +410,7 @@ def rhs_parts(s: OracleSystem, t: float, y: np.ndarray):
 def _meas(s: OracleSystem, idir: int):
     obs = np.ascontiguousarray(s.smat[:, idir, :])
     m = _Meas(obs=obs.ctypes.data, obs_kstride=s.nb_dm * s.nb_dm, f=s.f_dm.ctypes.data, prefac=s.ob_prefac,
-              bs=0, be=s.nb_dm)
+              bs=s.nv_dm, be=s.nb_dm)
     return m, obs
 
 
@@ -344,7 +418,7 @@ def measure(s: OracleSystem, y: np.ndarray, t: float, idir: int = 2):
     m, obs = _meas(s, idir)
     tot, amp = C.c_double(), C.c_double()
     y = np.ascontiguousarray(y, dtype=np.float64)
-    lib().orc_measure(s.nk, s.nb_dm, 0, s.nb_dm, obs.ctypes.data, s.nb_dm * s.nb_dm, s.f_dm.ctypes.data,
+    lib().orc_measure(s.nk, s.nb_dm, s.nv_dm, s.nb_dm, obs.ctypes.data, s.nb_dm * s.nb_dm, s.f_dm.ctypes.data,
                       s.e_dm.ctypes.data, t, s.picture_schrodinger, y.ctypes.data, s.ob_prefac, C.byref(tot), C.byref(amp))
     return tot.value, amp.value
 

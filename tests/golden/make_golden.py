@@ -27,6 +27,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 
+from denmat_dynm_development_gb300 import units  # noqa: E402
 from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, make_ldbd  # noqa: E402
 
 FS = None
@@ -47,6 +48,15 @@ CASES = {
     # density matrix with 4 bands, e-ph window on the upper 2 (trunc_copy / set_mat path)
     "nb2_window": dict(cfg=SynthConfig(nk=24, nb=2, seed=15, de_pair_mev=60.0, extra_bands=2),
                        param=dict(Bpert_T=(0.1, 0, 0.05), B_T=(0, 0, 1.0))),
+    # carrier density given (mu by bisection, electron.h:141-160) and the equilibrium drift
+    # subtracted (alg_ddmdteq: set_dm_eq + compute_ddmdt_eq), e-imp, B field
+    "nb2_carrier_eq": dict(cfg=SynthConfig(nk=40, nb=2, seed=16, de_pair_mev=60.0, eimp_sigma_mev=5.0),
+                           param=dict(Bpert_T=(0, 0, 0.1), B_T=(0.7, 0, 0), eimp_fraction=0.05,
+                                      extra={"alg_ddmdteq": 1}),
+                           carrier_scale=1.7),
+    # two valence bands below the e-ph window (holes: nv_dm = 2), equilibrium drift subtracted
+    "nb2_holes_eq": dict(cfg=SynthConfig(nk=24, nb=2, seed=17, de_pair_mev=60.0, extra_bands=2, nv=2),
+                         param=dict(Bpert_T=(0.1, 0, 0.05), B_T=(0, 0, 1.0), extra={"alg_ddmdteq": 1})),
 }
 
 
@@ -79,6 +89,13 @@ def make_case(name, spec, ref_bin, outroot):
     os.makedirs(d)
     cfg = spec["cfg"]
     info = make_ldbd(d, cfg, tstep_fs=1.0, tend_fs=20.0, **spec["param"])
+    if spec.get("carrier_scale"):
+        # an electron density carrier_scale times the one at the generator's mu, in cm^-3
+        e = np.fromfile(os.path.join(d, "ldbd_data", "ldbd_ek.bin")).reshape(cfg.nk, -1)[:, cfg.nv:]
+        n_bvk = float((1.0 / (np.exp((e - info.mu) / info.temperature) + 1.0)).sum()) * spec["carrier_scale"]
+        cd = n_bvk / (info.nk_full * info.cell_volume) / units.bohr2cm ** 3
+        with open(os.path.join(d, "param.in"), "a") as f:
+            f.write("carrier_density = %.17g\n" % cd)
     tmp = os.path.join(d, "_run")
     os.makedirs(tmp)
     shutil.copytree(os.path.join(d, "ldbd_data"), os.path.join(tmp, "ldbd_data"))
@@ -98,6 +115,10 @@ def make_case(name, spec, ref_bin, outroot):
     out["dm0"] = np.fromfile(os.path.join(tmp, "o", "dm0.bin"), dtype=np.complex128).reshape(nk, nbdm * nbdm)
     out["e_dm"] = np.fromfile(os.path.join(tmp, "o", "e_dm.bin")).reshape(nk, nbdm)
     out["f_dm"] = np.fromfile(os.path.join(tmp, "o", "f_dm.bin")).reshape(nk, nbdm)
+    if meta["ddmdteq"]:
+        nbw = int(meta["bend"] - meta["bstart"])
+        out["f_eq"] = np.fromfile(os.path.join(tmp, "o", "f_eq.bin")).reshape(nk, nbdm)
+        out["ddmdt_eq"] = np.fromfile(os.path.join(tmp, "o", "ddmdt_eq.bin"), dtype=np.complex128).reshape(nk, nbw * nbw)
     if meta["has_H"]:
         out["Hcoh"] = np.fromfile(os.path.join(tmp, "o", "Hcoh.bin"), dtype=np.complex128).reshape(nk, nbdm * nbdm)
     # rhs on three Hermitian states

@@ -24,9 +24,12 @@ def rel(a, b):
 
 def make_gpu(s, precision="f64"):
     from denmat_dynm_development_gb300.dmd import LindbladGPU
-    return LindbladGPU(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
-                       P1=s.P1, P2=s.P2, prefac_eph=s.prefac_eph, Hcoh=s.Hcoh, picture=s.picture_schrodinger,
-                       expt=s.expt, precision=precision)
+    g = LindbladGPU(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
+                    P1=s.P1, P2=s.P2, prefac_eph=s.prefac_eph, Hcoh=s.Hcoh, picture=s.picture_schrodinger,
+                    expt=s.expt, precision=precision)
+    if getattr(s, "ddmdt_eq", None) is not None:
+        g.set_ddmdt_eq(s.ddmdt_eq)
+    return g
 
 
 @pytest.fixture(scope="module")
@@ -83,7 +86,7 @@ def test_rk4_vs_golden(case, prec, oracle, built):
         for _ in range(8):
             gpu.rk4(1.0 * oracle.fs, 5)
             t, _ = gpu.get_state()
-            tot, amp = gpu.measure(0)
+            tot, amp = gpu.measure(0, s.nv_dm)
             rec.append((t, tot, amp))
         t, y = gpu.get_state()
         assert rel(y, g["rk4_y"]) < 1e-10
@@ -111,7 +114,7 @@ def test_rkf45_vs_golden(case, prec, oracle, built):
             ti += s.tstep
             hs, n = gpu.rkf45_apply(ti, hs, s.ode["hmin"], s.ode["hmax"], s.ode["epsabs"], 0.0)
             tcur, _ = gpu.get_state()
-            sz.append(gpu.measure(0)[0])
+            sz.append(gpu.measure(0, s.nv_dm)[0])
             nf.append(n)
         _, y = gpu.get_state()
         assert rel(y, g["gsl_y"]) < 1e-10
@@ -192,3 +195,53 @@ def test_nb4_larger_vs_oracle(oracle, built, tmp_path):
         _, yg = gpu.get_state()
     yr, _ = oracle.rk4(s, s.t0, 2.0 * oracle.fs, 10, y)
     assert rel(yg, yr) < 1e-10
+
+
+@pytest.mark.parametrize("case", ["nb2_carrier_eq", "nb2_holes_eq"])
+def test_equilibrium_drift_on_gpu(case, built):
+    """dmdh_prepare computes compute_ddmdt_eq's drift with the GPU RHS (evolve_eph.cpp:3-19) and
+    installs it; the result matches the reference's drift and the RHS with it subtracted."""
+    from denmat_dynm_development_gb300.host import System
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = System(d)
+    with s.gpu("f64") as gpu:
+        i = s.info
+        y = np.zeros((s.nk, s.nb_dm, s.nb_dm), np.complex128)
+        idx = np.arange(s.nb_dm)
+        y[:, idx, idx] = s.f_eq
+        # with the drift installed, diag(f_eq) is stationary under the scattering term at t = 0
+        eph = gpu.evolve_driver(0.0, y.reshape(s.nk, -1).view(np.float64).reshape(-1).copy())
+        scale = np.abs(g["ddmdt_eq"]).max()
+        assert np.abs(eph).max() < 1e-12 * scale
+        for k, t in enumerate(g["rhs_t"]):
+            assert rel(gpu.func(t, g["rhs_y"][k]), g["rhs_dydt"][k]) < 1e-12
+        assert i.ddmdteq == 1
+
+
+def test_t1_from_gpu_trajectory(oracle, built):
+    """T1 (the fit.py restatement) from the GPU RK4 trajectory against the oracle's: S(t) within the
+    trajectory bound 1e-10, fitted lifetimes within 1e-8 (leastsq's convergence tolerance on beta)."""
+    from denmat_dynm_development_gb300.t1fit import fit_t1
+    s = oracle.load(os.path.join(GOLDEN, "nb2_carrier_eq"))
+    h, nsteps, every = 2.0 * oracle.fs, 1500, 50
+    y0 = oracle.y_of(s.dm0)
+    _, rec_o = oracle.rk4(s, s.t0, h, nsteps, y0, every=every)
+    with make_gpu(s, "f64") as gpu:
+        gpu.set_state(s.t0, y0)
+        gpu.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+        rec = []
+        for _ in range(nsteps // every):
+            gpu.rk4(h, every)
+            t, _ = gpu.get_state()
+            rec.append((t,) + gpu.measure(0, s.nv_dm))
+    rec = np.array(rec)
+    assert rel(rec[:, 1], rec_o[:, 1]) < 1e-10
+    fo = fit_t1(rec_o[:, 0], rec_o[:, 1])
+    fg = fit_t1(rec[:, 0], rec[:, 1])
+    print("T1 oracle %.12g ps gpu %.12g ps" % (fo.tau_lsq, fg.tau_lsq))
+    # the synthetic P follows the initializer's smeared-delta construction without detailed balance,
+    # so |S| need not decay; the fit is still a well-defined function of the trajectory
+    assert np.isfinite(fo.tau_lsq) and np.isfinite(fg.tau_lsq)
+    assert abs(fg.tau_lsq - fo.tau_lsq) / fo.tau_lsq < 1e-8
+    assert abs(fg.tau_cf - fo.tau_cf) / fo.tau_cf < 1e-8

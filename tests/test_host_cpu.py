@@ -47,6 +47,13 @@ def test_load_matches_reference_setup(case, host, oracle):
         np.testing.assert_array_equal(s.Hcoh, g["Hcoh"])
     else:
         assert s.Hcoh is None
+    assert s.info.nv_dm == int(meta["nv_dm"])
+    if meta["ddmdteq"]:
+        assert s.info.ddmdteq == 1
+        assert s.info.mue == meta["mue"] and s.info.muh == meta["muh"]
+        np.testing.assert_array_equal(s.f_eq, g["f_eq"])
+    else:
+        assert s.info.ddmdteq == 0 and s.f_eq is None
     o = oracle.load(d)
     np.testing.assert_array_equal(s.P1, o.P1)
     np.testing.assert_array_equal(s.P2, o.P2)

@@ -35,6 +35,15 @@ def test_setup_bitwise(case, oracle):
         np.testing.assert_array_equal(s.Hcoh, g["Hcoh"])
     else:
         assert s.Hcoh is None
+    assert s.mu == meta["mu"]
+    assert s.nv_dm == int(meta["nv_dm"])
+    if meta["ddmdteq"]:
+        # set_dm_eq (chemical potentials keeping the carrier numbers) and compute_ddmdt_eq
+        assert s.mue == meta["mue"] and s.muh == meta["muh"]
+        np.testing.assert_array_equal(s.f_eq, g["f_eq"])
+        np.testing.assert_array_equal(s.ddmdt_eq, g["ddmdt_eq"])
+    else:
+        assert s.ddmdt_eq is None
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
