@@ -22,7 +22,7 @@ HOST_LIB = os.path.join(PKG, "libdmdhost.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-GPU_SRCS = [os.path.join(CSRC, "dmd_api.cu"), os.path.join(CSRC, "dmd_layout.cpp")]
+GPU_SRCS = [os.path.join(CSRC, "dmd_api.cu"), os.path.join(CSRC, "dmd_layout.cpp"), os.path.join(CSRC, "dmd_noalloc.cu")]
 GPU_DEPS = GPU_SRCS + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))] + \
     [os.path.join(INC, "dmd_gpu.h")]
 HOST_SRCS = [os.path.join(CSRC, f) for f in ("dmd_host.cpp",) if os.path.exists(os.path.join(CSRC, f))]

@@ -39,7 +39,8 @@ _L = None
 EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_set_ddmdt_eq", "dmd_func",
            "dmd_evolve_driver", "dmd_evolve_coh", "dmd_set_state", "dmd_get_state", "dmd_rk4", "dmd_euler",
            "dmd_rkf45_apply", "dmd_set_observable", "dmd_measure", "dmd_launch_count", "dmd_sync",
-           "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get"]
+           "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
+           "dmd_evolve_driver_noalloc"]
 
 
 def _lib():
@@ -74,6 +75,8 @@ def _lib():
         L.dmd_timer.argtypes = [vp, C.c_int, C.POINTER(d)]
         L.dmd_set_profiling.argtypes = [vp, C.c_int]
         L.dmd_profile_get.argtypes = [vp, C.c_int, C.POINTER(d), C.POINTER(i64)]
+        L.dmd_evolve_driver_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, i64, vp, vp, vp, vp, vp, d,
+                                                C.c_int32, d, vp, vp, vp]
         _L = L
     return _L
 

@@ -128,6 +128,22 @@ int dmd_timer(dmd_handle* h, int op, double* ms);
 int dmd_set_profiling(dmd_handle* h, int on);
 int dmd_profile_get(const dmd_handle* h, int kernel_class, double* total_ms, int64_t* launches);
 
+/* No counterpart in the reference. The scattering right-hand side of dmd_evolve_driver for callers
+ * that cannot allocate device memory (code running inside a CUDA graph capture, host frameworks
+ * whose memory pools own the device, plug-ins handed device pointers but no allocator). Every
+ * pointer is a caller-owned DEVICE buffer: k1st/k2nd uint64 [nkpair], P1/P2 complex128
+ * [nkpair][nb^4] in DMD's layout, e_dm [nk][nb_dm], dm and ddmdt_eph complex128 [nk][nb_dm^2];
+ * stream is a cudaStream_t (NULL for the default stream). Nothing is allocated: the scratch lives in
+ * a static device array of 16 MiB that every GPU loading this library keeps until exit, which
+ * limits nk * (bend - bstart)^2 to 262144 (DMD_E_ARG above that). The first call on a device looks
+ * up the array's device address and should come before any stream capture. All calls share the
+ * array: calls that overlap on the GPU race and must be serialised by the caller. Pairs whose
+ * indices fall outside [0, nk) are skipped. The call is asynchronous on `stream`. */
+int dmd_evolve_driver_noalloc(int32_t nk, int32_t nb_dm, int32_t bstart, int32_t bend, int64_t nkpair,
+                              const uint64_t* k1st, const uint64_t* k2nd, const double* P1, const double* P2,
+                              const double* e_dm, double prefac_eph, int32_t expt, double t, const double* dm,
+                              double* ddmdt_eph, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
