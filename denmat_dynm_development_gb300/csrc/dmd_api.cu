@@ -35,11 +35,11 @@ struct dmd_handle {
   dmd::WorkItem* d_items = nullptr;
   int nitems = 0;
   long long nrb = 0;
-  int cb_variant = 1;          // 0: direct loads, 1: bulk-copy staging through shared memory
   unsigned int* d_err = nullptr;  // device error flags (bounded waits)
+  unsigned int* d_hflag = nullptr;  // set by the prep kernel when a state is not exactly Hermitian
   double2* d_H = nullptr;      // [nk][nbdm^2]
   double2* d_eq = nullptr;     // [nk][nb2]
-  double2* d_rs = nullptr;     // [nk][2][nb2]
+  double2* d_rs = nullptr;     // [nk][2][nb2] (per-thread form); Hermitian + anti-Hermitian coordinates (column-block form)
   double2* d_acc = nullptr;    // [nk][2][nb2]
   double2* d_y = nullptr;      // state
   double2* d_ytmp = nullptr;
@@ -161,11 +161,11 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
   if (!h->use_cb) {
     k_prep<NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->expt, h->d_rs, h->d_acc);
   } else if (h->prec == DMD_PREC_F64X) {
-    k_prep_cb<ArithDF, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta,
-                                                                    h->expt, (float4*)h->d_rs, h->d_acc);
+    k_prep_herm<ArithDF, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta,
+                                                                      h->expt, (float2*)h->d_rs, h->d_acc, h->d_hflag);
   } else {
-    k_prep_cb<ArithF64, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta,
-                                                                     h->expt, h->d_rs, h->d_acc);
+    k_prep_herm<ArithF64, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta,
+                                                                       h->expt, (double*)h->d_rs, h->d_acc, h->d_hflag);
   }
   h->launches++;
   CKL();
@@ -180,23 +180,24 @@ int launch_pairs(dmd_handle* h) {
     const long long nthr = h->npair * 4LL * NB * NB;
     k_pairs_f64_atomic<NB><<<blocks_for(nthr, 256), 256, 0, h->st>>>(h->npair, h->d_kk, h->d_P, h->d_rs, h->d_acc);
   } else {
-    if constexpr (NB <= 2) {
+    if constexpr (NB == 2) {
+      // Hermitian coordinates; the second launch carries the anti-Hermitian part of a state that is
+      // not exactly Hermitian and returns at once unless the prep kernel raised d_hflag
       const unsigned g = blocks_for(h->nitems, 4);
-      if (h->cb_variant == 1) {
-        constexpr int RW = NB * NB >= 2 ? 2 : 1;
-        if (h->prec == DMD_PREC_F64X)
-          k_pairs_cb_tma<ArithDF, NB, RW, 4><<<g, 128, CbTmaSmem<ArithDF, NB, RW>::cta_bytes, h->st>>>(
-              h->d_items, h->nitems, h->d_rb, (const float4*)h->d_P, (const float4*)h->d_rs, (double*)h->d_acc, h->nk,
+      const size_t half = (size_t)h->nk * 2 * h->nb2;  // coordinates per part
+      for (int pass = 0; pass < 2; ++pass) {
+        const unsigned int* gate = pass ? h->d_hflag : nullptr;
+        if (h->prec == DMD_PREC_F64X) {
+          const float2* rs = (const float2*)h->d_rs + pass * half;
+          k_pairs_herm<ArithDF, NB, 2, 4><<<g, 128, CbTmaSmem<ArithDF, NB, 2>::cta_bytes, h->st>>>(
+              h->d_items, h->nitems, h->d_rb, (const float4*)h->d_P, rs, (double*)h->d_acc, h->nk, pass, gate,
               h->d_err);
-        else
-          k_pairs_cb_tma<ArithF64, NB, RW, 4><<<g, 128, CbTmaSmem<ArithF64, NB, RW>::cta_bytes, h->st>>>(
-              h->d_items, h->nitems, h->d_rb, h->d_P, h->d_rs, (double*)h->d_acc, h->nk, h->d_err);
-      } else if (h->prec == DMD_PREC_F64X) {
-        k_pairs_cb<ArithDF, NB><<<g, 128, 0, h->st>>>(h->d_items, h->nitems, h->d_rb, (const float4*)h->d_P,
-                                                      (const float4*)h->d_rs, (double*)h->d_acc, h->nk);
-      } else {
-        k_pairs_cb<ArithF64, NB><<<g, 128, 0, h->st>>>(h->d_items, h->nitems, h->d_rb, h->d_P, h->d_rs,
-                                                       (double*)h->d_acc, h->nk);
+        } else {
+          const double* rs = (const double*)h->d_rs + pass * half;
+          k_pairs_herm<ArithF64, NB, 2, 4><<<g, 128, CbTmaSmem<ArithF64, NB, 2>::cta_bytes, h->st>>>(
+              h->d_items, h->nitems, h->d_rb, h->d_P, rs, (double*)h->d_acc, h->nk, pass, gate, h->d_err);
+        }
+        if (pass == 0) h->launches++;
       }
     }
   }
@@ -230,6 +231,8 @@ FinishArgs base_finish(dmd_handle* h, const double2* y) {
   a.y = y;
   a.acc = h->d_acc;
   a.pos = h->use_cb ? h->d_pos : nullptr;
+  a.herm = h->use_cb;
+  a.hflag = h->use_cb ? h->d_hflag : nullptr;
   a.want_eph = 1;
   a.want_coh = (h->picture == DMD_PICTURE_SCHRODINGER || h->d_H) ? 1 : 0;
   return a;
@@ -316,6 +319,61 @@ int upload_pairs(dmd_handle* h, const dmd_desc* d) {
   return rc;
 }
 
+struct cd {
+  double re, im;
+};
+
+// Hermitian coordinates v = M q of an nb x nb Hermitian matrix, column j = (p1, p2) of M:
+// p1 == p2: v_(p1p1) = q_j;  p1 < p2: v_(p1p2) += q_j, v_(p2p1) += q_j;  p1 > p2: v_(p2p1) += i q_j,
+// v_(p1p2) += -i q_j. Returns the entries (index into v, coefficient as (re, im) in {0, +-1}).
+int herm_col(int nb, int j, int* idx, int* cre, int* cim) {
+  const int p1 = j / nb, p2 = j % nb;
+  if (p1 == p2) {
+    idx[0] = j; cre[0] = 1; cim[0] = 0;
+    return 1;
+  }
+  if (p1 < p2) {
+    idx[0] = j; cre[0] = 1; cim[0] = 0;
+    idx[1] = p2 * nb + p1; cre[1] = 1; cim[1] = 0;
+    return 2;
+  }
+  idx[0] = p2 * nb + p1; cre[0] = 0; cim[0] = 1;
+  idx[1] = j; cre[1] = 0; cim[1] = -1;
+  return 2;
+}
+
+// z * (cr + i ci) for cr, ci in {0, +-1}: exact
+inline cd cmul_unit(cd z, int cr, int ci) {
+  if (ci == 0) return cr > 0 ? z : cd{-z.re, -z.im};
+  return ci > 0 ? cd{-z.im, z.re} : cd{z.im, -z.re};
+}
+
+// Q1 = M^H P1 M and Q2 = M^T P2 conj(M) (both nb^2 x nb^2 row-major), the operators of the
+// Hermitian-coordinate contraction (dmd_pairs_cb.cuh)
+void herm_transform(int nb, const cd* P1, const cd* P2, cd* Q1, cd* Q2) {
+  const int n2 = nb * nb;
+  int ia[2], ra[2], ja[2], ib[2], rb[2], jb[2];
+  for (int a = 0; a < n2; ++a) {
+    const int na = herm_col(nb, a, ia, ra, ja);
+    for (int b = 0; b < n2; ++b) {
+      const int nbb = herm_col(nb, b, ib, rb, jb);
+      cd q1 = {0, 0}, q2 = {0, 0};
+      for (int u = 0; u < na; ++u)
+        for (int v = 0; v < nbb; ++v) {
+          const cd p1 = P1[ia[u] * n2 + ib[v]], p2 = P2[ia[u] * n2 + ib[v]];
+          const cd t1 = cmul_unit(cmul_unit(p1, ra[u], -ja[u]), rb[v], jb[v]);  // conj(ca) P1 cb
+          const cd t2 = cmul_unit(cmul_unit(p2, ra[u], ja[u]), rb[v], -jb[v]);  // ca P2 conj(cb)
+          q1.re += t1.re;
+          q1.im += t1.im;
+          q2.re += t2.re;
+          q2.im += t2.im;
+        }
+      Q1[a * n2 + b] = q1;
+      Q2[a * n2 + b] = q2;
+    }
+  }
+}
+
 // column-block layout upload: pairs permuted into row blocks, element-major inside each block,
 // folded with the optional additive operators and converted to the arithmetic's element format
 int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
@@ -328,10 +386,9 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
     return fail(h, DMD_E_ARG, "k-pair index out of range");
   h->nitems = (int)L.items.size();
   h->nrb = (long long)L.rb.size();
-  if (const char* v = getenv("DMD_PAIR_KERNEL")) h->cb_variant = (strcmp(v, "ldg") == 0) ? 0 : 1;
-  CK(cudaFuncSetAttribute(k_pairs_cb_tma<ArithDF, 2, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  CK(cudaFuncSetAttribute(k_pairs_herm<ArithDF, 2, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           (int)CbTmaSmem<ArithDF, 2, 2>::cta_bytes));
-  CK(cudaFuncSetAttribute(k_pairs_cb_tma<ArithF64, 2, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  CK(cudaFuncSetAttribute(k_pairs_herm<ArithF64, 2, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                           (int)CbTmaSmem<ArithF64, 2, 2>::cta_bytes));
   int rc;
   if ((rc = dalloc(h, &h->d_pos, (size_t)h->nk)) || (rc = dalloc(h, &h->d_rb, L.rb.size())) ||
@@ -341,6 +398,8 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
   CK(cudaMemcpy(h->d_rb, L.rb.data(), L.rb.size() * sizeof(dmd::RowBlock), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_items, L.items.data(), L.items.size() * sizeof(dmd::WorkItem), cudaMemcpyHostToDevice));
   const bool df = h->prec == DMD_PREC_F64X;
+  std::vector<cd> Peff[2] = {std::vector<cd>(nb4), std::vector<cd>(nb4)};
+  std::vector<cd> Q[2] = {std::vector<cd>(nb4), std::vector<cd>(nb4)};
   const size_t chunk_rb = 1 << 14;  // row blocks per staging chunk
   double2* stage = nullptr;
   CK(cudaMallocHost((void**)&stage, chunk_rb * 32 * ne * sizeof(double2)));
@@ -363,29 +422,37 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
           std::swap(s1, s2);
           std::swap(a1, a2);
         }
+        // effective P1, P2 of the stored orientation, folded with the additive operators
+        for (int m = 0; m < 2; ++m)
+          for (int e = 0; e < nb4; ++e) {
+            const double* sp = (m == 0 ? s1 : s2) + 2 * e;
+            const double* ap = (m == 0 ? a1 : a2);
+            double x = sp[0], yv = sp[1];
+            if (ap) {  // P += P_add * scale (ElectronImpurity.cpp:38-39, ElectronPhonon.cpp:96-97)
+              x = x + ap[2 * e] * d->add_scale;
+              yv = yv + ap[2 * e + 1] * d->add_scale;
+            }
+            if (tr) yv = -yv;
+            Peff[m][e] = {x, yv};
+          }
+        herm_transform(h->nb, Peff[0].data(), Peff[1].data(), Q[0].data(), Q[1].data());
         for (int e = 0; e < ne; ++e) {
-          // stored element e: P1 row-major for e < nb^4; P2 column-major after it
-          // (e = nb^4 + cc * nb^2 + a holds P2[a][cc])
-          int se = e;
-          if (e >= nb4) {
+          // stored element e: Q1 row-major for e < nb^4; Q2 column-major after it
+          // (e = nb^4 + cc * nb^2 + a holds Q2[a][cc])
+          cd qv;
+          if (e < nb4) {
+            qv = Q[0][e];
+          } else {
             const int q = e - nb4, cc = q / h->nb2, a = q % h->nb2;
-            se = nb4 + a * h->nb2 + cc;
+            qv = Q[1][a * h->nb2 + cc];
           }
-          const double* sp = se < nb4 ? s1 + 2 * se : s2 + 2 * (se - nb4);
-          const double* ap = a1 ? (se < nb4 ? a1 + 2 * se : a2 + 2 * (se - nb4)) : nullptr;
-          double x = sp[0], yv = sp[1];
-          if (ap) {  // P += P_add * scale (ElectronImpurity.cpp:38-39, ElectronPhonon.cpp:96-97)
-            x = x + ap[0] * d->add_scale;
-            yv = yv + ap[1] * d->add_scale;
-          }
-          if (tr) yv = -yv;
           double2 v;
           if (df) {
-            const float xh = (float)x, yh = (float)yv;
-            float4 f = make_float4(xh, (float)(x - (double)xh), yh, (float)(yv - (double)yh));
+            const float xh = (float)qv.re, yh = (float)qv.im;
+            float4 f = make_float4(xh, (float)(qv.re - (double)xh), yh, (float)(qv.im - (double)yh));
             memcpy(&v, &f, 16);
           } else {
-            v = make_double2(x, yv);
+            v = make_double2(qv.re, qv.im);
           }
           stage[(b0 - q0) * ne + (size_t)e * n + i] = v;
         }
@@ -404,7 +471,7 @@ void release(dmd_handle* h) {
   if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
   void* ptrs[] = {h->d_err, h->d_pos, h->d_rb, h->d_items, h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
-                  h->d_coef, h->d_flag};
+                  h->d_coef, h->d_flag, h->d_hflag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -502,7 +569,8 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
       (rc = dalloc(h, &h->d_in1, h->nstate)) || (rc = dalloc(h, &h->d_out, h->nstate)) ||
       (rc = dalloc(h, &h->d_K, 6 * h->nstate)) || (rc = dalloc(h, &h->d_tref, 2)) ||
       (rc = dalloc(h, &h->d_step, 1)) || (rc = dalloc(h, &h->d_red, 4096)) || (rc = dalloc(h, &h->d_coef_i, 64)) ||
-      (rc = dalloc(h, &h->d_coef, 64)) || (rc = dalloc(h, &h->d_flag, 1)) || (rc = dalloc(h, &h->d_err, 1)))
+      (rc = dalloc(h, &h->d_coef, 64)) || (rc = dalloc(h, &h->d_flag, 1)) || (rc = dalloc(h, &h->d_err, 1)) ||
+      (rc = dalloc(h, &h->d_hflag, 1)))
     return bail(rc);
   std::vector<double> ew(nk * h->nb);
   for (size_t k = 0; k < nk; ++k)
@@ -518,7 +586,8 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   h->use_cb = (h->nb == 2 && h->npair > 0) ? 1 : 0;
   if ((rc = h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d))) return bail(rc);
   if (cudaMemset(h->d_y, 0, h->nstate * 16) != cudaSuccess || cudaMemset(h->d_step, 0, 8) != cudaSuccess ||
-      cudaMemset(h->d_err, 0, sizeof(unsigned int)) != cudaSuccess)
+      cudaMemset(h->d_err, 0, sizeof(unsigned int)) != cudaSuccess ||
+      cudaMemset(h->d_hflag, 0, sizeof(unsigned int)) != cudaSuccess)
     return bail(fail(h, DMD_E_CUDA, "init"));
   *out = h;
   return DMD_OK;
@@ -674,7 +743,7 @@ int dmd_rk4(dmd_handle* h, double dt, int64_t nsteps) {
     if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     h->launches = l0;  // captured launches are counted when the graph runs
   }
-  const long long per_step = (h->npair ? 13 : 9);
+  const long long per_step = h->npair ? (h->use_cb ? 17 : 13) : 9;
   for (int64_t s = 0; s < nsteps; ++s) {
     CK(cudaGraphLaunch(h->g_rk4, h->st));
     h->launches += per_step;

@@ -76,6 +76,8 @@ struct FinishArgs {
   const double2* y;    // state the RHS is evaluated on
   const double2* acc;  // [nk][2][NB2], indexed by pos[k] when pos is set
   const int* pos;      // k -> accumulator row (column-block layout) or null
+  int herm;            // accumulators hold X' = M^H X, Y' = M^H Y (Hermitian coordinates)
+  unsigned int* hflag; // non-Hermitian-state flag of the prep kernel, cleared here (or null)
   int want_eph, want_coh;
   // output: plain RHS
   double2* out;
@@ -95,6 +97,7 @@ template <int NB>
 __global__ void k_finish(FinishArgs a) {
   constexpr int NB2 = NB * NB;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a.hflag && k == 0) *a.hflag = 0u;  // every pair launch of this evaluation has completed
   if (k >= a.nk) return;
   const int nd = a.nbdm, nd2 = nd * nd;
   const double t = eval_time(a.ta);
@@ -138,8 +141,22 @@ __global__ void k_finish(FinishArgs a) {
   // scattering finish on the window (evolve_eph.cpp:140-162, evolve_driver :21-32)
   if (a.want_eph) {
     const double* ew = a.ew + (size_t)k * NB;
-    const double2* X = a.acc + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
-    const double2* Y = X + NB2;
+    const double2* Xs = a.acc + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
+    double2 X[NB2], Y[NB2];
+    for (int i = 0; i < NB2; ++i) {
+      X[i] = Xs[i];
+      Y[i] = Xs[NB2 + i];
+    }
+    if (a.herm) {  // X = (M^H)^-1 X': X_ij = (X'_ij + i X'_ji) / 2, X_ji = (X'_ij - i X'_ji) / 2 for i < j
+      for (int i = 0; i < NB; ++i)
+        for (int j = i + 1; j < NB; ++j) {
+          const double2 xu = X[i * NB + j], xl = X[j * NB + i], yu = Y[i * NB + j], yl = Y[j * NB + i];
+          X[i * NB + j] = mk2(0.5 * (xu.x - xl.y), 0.5 * (xu.y + xl.x));
+          X[j * NB + i] = mk2(0.5 * (xu.x + xl.y), 0.5 * (xu.y - xl.x));
+          Y[i * NB + j] = mk2(0.5 * (yu.x - yl.y), 0.5 * (yu.y + yl.x));
+          Y[j * NB + i] = mk2(0.5 * (yu.x + yl.y), 0.5 * (yu.y - yl.x));
+        }
+    }
     double2 rw[NB2], sw[NB2], Pdm[NB2], dmP[NB2];
     for (int i = 0; i < NB; ++i)
       for (int j = 0; j < NB; ++j) {

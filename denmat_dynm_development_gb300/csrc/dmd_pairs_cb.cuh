@@ -1,17 +1,31 @@
-// Column-block k-pair contraction (layout in dmd_layout.h).
+// Column-block k-pair contraction in Hermitian coordinates (layout in dmd_layout.h).
 //
-// One warp per work item: a run of row blocks of one column block J. Lane s owns column
-// c = 32 J + s: it keeps rt_c and st_c in registers and accumulates the reverse (k' side) sums
-//   X_c[a] += sum_b conj(P2[a][b]) rt_k[b],   Y_c[b] += sum_a st_k[a] conj(P1[a][b])
-// across all row blocks of the item without any cross-lane traffic. For each row block the
-// forward sums of the active lanes
-//   X_k[a] = sum_b P1[a][b] rt_c[b],           Y_k[b] = sum_a st_c[a] P2[a][b]
-// are reduced across the warp through shared memory and added to the row's accumulator with
-// FP64 atomics (a few per row block); the reverse sums are flushed once per work item.
+// Coordinates. rt_k = conj(D_k) o rho_k and st_k = conj(D_k) o (1 - rho_k) are Hermitian nb x nb
+// matrices when rho_k is (D_k[(i,j)] = exp(i t (e_i - e_j))). A Hermitian matrix v has nb^2 real
+// coordinates q: q[(i,i)] = v_ii, and for i < j q[(i,j)] = Re v_ij, q[(j,i)] = Im v_ij, so v = M q
+// with M[(ij),(ij)] = 1, M[(ij),(ji)] = i, M[(ji),(ij)] = 1, M[(ji),(ji)] = -i. The host stores
+//   Q1 = M^H P1 M      (row-major, like P1)        Q2 = M^T P2 conj(M)   (column-major, like P2)
+// and the kernel accumulates the transformed sums X' = M^H X, Y' = M^H Y:
+//   X'_k   += Q1 r_c                      Y'_c[j] += sum_a s_k[a] conj(Q1[a][j])
+//   Y'_k[j] += sum_a Q2[a][j] s_c[a]      X'_c[a] += sum_j conj(Q2[a][j]) r_k[j]
+// (r, s: coordinates of rt, st). Every product is complex x real -- half the multiply-adds of the
+// complex form -- and the finish maps X = (M^H)^-1 X' back (k_finish, herm = 1).
+// A state that is not exactly Hermitian is split rho = H + i A with H, A Hermitian; the A part's
+// coordinates go through a second launch of the same kernel, gated on a device flag that the prep
+// kernel raises, whose sums are multiplied by i. The arithmetic is linear in the vectors, so the
+// two launches together equal the general complex contraction.
+//
+// Work decomposition. One warp per work item: a run of row blocks of one column block J. Lane s
+// owns column c = 32 J + s: it keeps r_c, s_c in registers and accumulates the reverse (column
+// side) sums across all row blocks of the item without cross-lane traffic. For each row block the
+// forward sums of the active lanes are reduced through shared memory and added to the row's
+// accumulator with FP64 atomics; the reverse sums are flushed once per work item. The P elements
+// of a row block are staged through shared memory by bulk copies (TMA unit), double-buffered per
+// warp, with bounded waits.
 //
 // Arithmetic policies:
-//   ArithF64 -- complex128 elements, FP64 fused multiply-adds (exact FP64 path).
-//   ArithDF  -- (hi, lo) FP32 pairs for P and the vectors; products are error-free transformed
+//   ArithF64 -- complex128 P, FP64 fused multiply-adds (exact FP64 path).
+//   ArithDF  -- (hi, lo) FP32 pairs for P and the coordinates; products are error-free transformed
 //               (p = xh*yh, e = fma(xh,yh,-p) + xh*yl + xl*yh) and sums use TwoSum on the high
 //               parts, so each product carries ~2^-47 relative error and the FP32 pipes (64x the
 //               FP64 rate on this part) do the work.
@@ -25,10 +39,6 @@ namespace dmd {
 // ---------------------------------------------------------------------------------------------
 // double-float helpers (no contraction: every operation is an explicit round-to-nearest op)
 // ---------------------------------------------------------------------------------------------
-struct dfc {  // complex (re_hi, re_lo, im_hi, im_lo)
-  float rh, rl, ih, il;
-};
-
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = __fadd_rn(a, b);
   const float bb = __fsub_rn(s, a);
@@ -61,43 +71,37 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float bh, float bl)
   lo = __fadd_rn(lo, __fadd_rn(t, bl));
 }
 
-__device__ __forceinline__ float4 split_df(double2 v) {
-  const float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);
-  return make_float4(rh, __double2float_rn(v.x - (double)rh), ih, __double2float_rn(v.y - (double)ih));
+__device__ __forceinline__ float2 split_df1(double v) {
+  const float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(v - (double)h));
 }
 
 struct ArithDF {
-  typedef float4 elem;  // P and vector element: (re_h, re_l, im_h, im_l)
+  typedef float4 elem;  // P element: (re_h, re_l, im_h, im_l)
+  typedef float2 relem;  // real coordinate: (h, l)
   struct acc {
     float rh, rl, ih, il;
   };
   static __device__ __forceinline__ void zero(acc& a) { a.rh = a.rl = a.ih = a.il = 0.f; }
-  // a += x * y
-  static __device__ __forceinline__ void mac(acc& a, const elem& x, const elem& y) {
-    df_mac(a.rh, a.rl, x.x, x.y, y.x, y.y);
-    df_mac(a.rh, a.rl, -x.z, -x.w, y.z, y.w);
-    df_mac(a.ih, a.il, x.x, x.y, y.z, y.w);
-    df_mac(a.ih, a.il, x.z, x.w, y.x, y.y);
+  // a += x * v (complex x real)
+  static __device__ __forceinline__ void mac(acc& a, const elem& x, const relem& v) {
+    df_mac(a.rh, a.rl, x.x, x.y, v.x, v.y);
+    df_mac(a.ih, a.il, x.z, x.w, v.x, v.y);
   }
-  // a += conj(x) * y
-  static __device__ __forceinline__ void mac_cx(acc& a, const elem& x, const elem& y) {
-    df_mac(a.rh, a.rl, x.x, x.y, y.x, y.y);
-    df_mac(a.rh, a.rl, x.z, x.w, y.z, y.w);
-    df_mac(a.ih, a.il, x.x, x.y, y.z, y.w);
-    df_mac(a.ih, a.il, -x.z, -x.w, y.x, y.y);
+  // a += conj(x) * v
+  static __device__ __forceinline__ void mac_cx(acc& a, const elem& x, const relem& v) {
+    df_mac(a.rh, a.rl, x.x, x.y, v.x, v.y);
+    df_mac(a.ih, a.il, -x.z, -x.w, v.x, v.y);
   }
   static __device__ __forceinline__ void renorm(acc& a) {
     df_renorm(a.rh, a.rl);
     df_renorm(a.ih, a.il);
   }
-  static __device__ __forceinline__ void acc_add(acc& a, const acc& b) {
-    df_add(a.rh, a.rl, b.rh, b.rl);
-    df_add(a.ih, a.il, b.ih, b.il);
-  }
   // reduction scratch entry: one real (hi, lo)
   typedef float2 red_t;
   static __device__ __forceinline__ float2 red_re(const acc& a) { return make_float2(a.rh, a.rl); }
   static __device__ __forceinline__ float2 red_im(const acc& a) { return make_float2(a.ih, a.il); }
+  static __device__ __forceinline__ float2 red_neg(float2 v) { return make_float2(-v.x, -v.y); }
   static __device__ __forceinline__ float2 red_zero() { return make_float2(0.f, 0.f); }
   static __device__ __forceinline__ void red_add(float2& s, float2 b) { df_add(s.x, s.y, b.x, b.y); }
   static __device__ __forceinline__ float2 red_shfl_xor(float2 v, int m) {
@@ -106,207 +110,100 @@ struct ArithDF {
   static __device__ __forceinline__ double red_to_double(float2 v) { return (double)v.x + (double)v.y; }
   static __device__ __forceinline__ double re_d(const acc& a) { return (double)a.rh + (double)a.rl; }
   static __device__ __forceinline__ double im_d(const acc& a) { return (double)a.ih + (double)a.il; }
-  static __device__ __forceinline__ elem from_double2(double2 v) { return split_df(v); }
+  static __device__ __forceinline__ relem from_double(double v) { return split_df1(v); }
 };
 
 struct ArithF64 {
   typedef double2 elem;
+  typedef double relem;
   struct acc {
     double x, y;
   };
   static __device__ __forceinline__ void zero(acc& a) { a.x = a.y = 0.0; }
-  static __device__ __forceinline__ void mac(acc& a, const elem& x, const elem& y) {
-    a.x = fma(x.x, y.x, fma(-x.y, y.y, a.x));
-    a.y = fma(x.x, y.y, fma(x.y, y.x, a.y));
+  static __device__ __forceinline__ void mac(acc& a, const elem& x, const relem& v) {
+    a.x = fma(x.x, v, a.x);
+    a.y = fma(x.y, v, a.y);
   }
-  static __device__ __forceinline__ void mac_cx(acc& a, const elem& x, const elem& y) {
-    a.x = fma(x.x, y.x, fma(x.y, y.y, a.x));
-    a.y = fma(x.x, y.y, fma(-x.y, y.x, a.y));
+  static __device__ __forceinline__ void mac_cx(acc& a, const elem& x, const relem& v) {
+    a.x = fma(x.x, v, a.x);
+    a.y = fma(-x.y, v, a.y);
   }
   static __device__ __forceinline__ void renorm(acc&) {}
-  static __device__ __forceinline__ void acc_add(acc& a, const acc& b) {
-    a.x += b.x;
-    a.y += b.y;
-  }
   typedef double red_t;
   static __device__ __forceinline__ double red_re(const acc& a) { return a.x; }
   static __device__ __forceinline__ double red_im(const acc& a) { return a.y; }
+  static __device__ __forceinline__ double red_neg(double v) { return -v; }
   static __device__ __forceinline__ double red_zero() { return 0.0; }
   static __device__ __forceinline__ void red_add(double& s, double b) { s += b; }
   static __device__ __forceinline__ double red_shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
   static __device__ __forceinline__ double red_to_double(double v) { return v; }
   static __device__ __forceinline__ double re_d(const acc& a) { return a.x; }
   static __device__ __forceinline__ double im_d(const acc& a) { return a.y; }
-  static __device__ __forceinline__ elem from_double2(double2 v) { return v; }
+  static __device__ __forceinline__ relem from_double(double v) { return v; }
 };
 
-template <typename E>
-__device__ __forceinline__ E ld_stream(const E* p) {
-  return __ldcs(p);
-}
-
-// rs: [nk][2][NB2] vectors in position (energy-rank) order; acc: [nk][2][NB2] double2
+// ---------------------------------------------------------------------------------------------
+// Prep: Hermitian and anti-Hermitian coordinates of rt, st per k (written at pos[k]), zeroed
+// accumulators. One thread per (k, element (i, j)); the thread of (i, j) with i < j writes the
+// coordinates at (i, j) and (j, i). Raises *hflag when some rho_k is not exactly Hermitian.
+// rs layout: [nk][2][NB2] Hermitian part (r, s), then [nk][2][NB2] anti-Hermitian part.
+// ---------------------------------------------------------------------------------------------
 template <typename A, int NB>
-__global__ void __launch_bounds__(128) k_pairs_cb(const WorkItem* __restrict__ items, int nitems,
-                                                  const RowBlock* __restrict__ rbs,
-                                                  const typename A::elem* __restrict__ P,
-                                                  const typename A::elem* __restrict__ rs, double* __restrict__ acc,
-                                                  int nk) {
-  constexpr int NB2 = NB * NB, NB4 = NB2 * NB2, NV = 4 * NB2;  // NV reals per forward block (X, Y)
-  typedef typename A::elem E;
-  typedef typename A::acc Acc;
-  typedef typename A::red_t R;
-  __shared__ R red[4][NV][32];
-  const int wib = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  const int item = blockIdx.x * 4 + wib;
-  if (item >= nitems) return;
-  const WorkItem w = items[item];
-  const int col = w.J * 32 + lane;
-  const bool colok = col < nk;
-  E rc[NB2], sc[NB2];
-#pragma unroll
-  for (int i = 0; i < NB2; ++i) {
-    rc[i] = colok ? rs[(size_t)col * 2 * NB2 + i] : E();
-    sc[i] = colok ? rs[(size_t)col * 2 * NB2 + NB2 + i] : E();
-  }
-  Acc rX[NB2], rY[NB2];
-#pragma unroll
-  for (int i = 0; i < NB2; ++i) {
-    A::zero(rX[i]);
-    A::zero(rY[i]);
-  }
-  bool any_rev = false;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int r = w.rb0; r < w.rb1; ++r) {
-    const RowBlock b = rbs[r];
-    const bool active = (b.mask >> lane) & 1u;
-    const bool rev = (b.revmask >> lane) & 1u;
-    any_rev |= rev;
-    const int n = __popc(b.mask);
-    const int slot = __popc(b.mask & lt);
-    if (active) {
-      const E* rrow = rs + (size_t)b.row * 2 * NB2;
-      const E* base = P + (size_t)b.pair0 * 2 * NB4 + slot;
-      {  // P1 block: X_k[a] += P1[a][c] rt_col[c];  Y_col[c] += st_k[a] conj(P1[a][c])
-        E sr[NB2];
-        Acc f[NB2];
-#pragma unroll
-        for (int i = 0; i < NB2; ++i) {
-          sr[i] = rrow[NB2 + i];
-          A::zero(f[i]);
-        }
-#pragma unroll
-        for (int a = 0; a < NB2; ++a)
-#pragma unroll
-          for (int c = 0; c < NB2; ++c) {
-            const E p1 = ld_stream(base + (size_t)(a * NB2 + c) * n);
-            A::mac(f[a], p1, rc[c]);
-            if (rev) A::mac_cx(rY[c], p1, sr[a]);
-          }
-#pragma unroll
-        for (int i = 0; i < NB2; ++i) {
-          red[wib][2 * i][lane] = A::red_re(f[i]);
-          red[wib][2 * i + 1][lane] = A::red_im(f[i]);
-        }
-      }
-      {  // P2 block: Y_k[c] += st_col[a] P2[a][c];  X_col[a] += conj(P2[a][c]) rt_k[c]
-        E rr[NB2];
-        Acc f[NB2];
-#pragma unroll
-        for (int i = 0; i < NB2; ++i) {
-          rr[i] = rrow[i];
-          A::zero(f[i]);
-        }
-#pragma unroll
-        for (int a = 0; a < NB2; ++a)
-#pragma unroll
-          for (int c = 0; c < NB2; ++c) {
-            const E p2 = ld_stream(base + (size_t)(NB4 + c * NB2 + a) * n);  // P2 stored column-major
-            A::mac(f[c], p2, sc[a]);
-            if (rev) A::mac_cx(rX[a], p2, rr[c]);
-          }
-#pragma unroll
-        for (int i = 0; i < NB2; ++i) {
-          red[wib][2 * NB2 + 2 * i][lane] = A::red_re(f[i]);
-          red[wib][2 * NB2 + 2 * i + 1][lane] = A::red_im(f[i]);
-        }
-      }
-      if (rev) {
-#pragma unroll
-        for (int i = 0; i < NB2; ++i) {
-          A::renorm(rX[i]);
-          A::renorm(rY[i]);
-        }
-      }
-    }
-    __syncwarp();
-    constexpr int LPV = 32 / NV > 0 ? 32 / NV : 1;  // lanes per value
-    for (int v0 = 0; v0 < NV; v0 += 32 / LPV) {
-      const int v = v0 + lane / LPV;
-      const int part = lane % LPV;
-      R s = A::red_zero();
-      if (v < NV) {
-        const int span = 32 / LPV;
-        for (int j = part * span; j < (part + 1) * span; ++j)
-          if ((b.mask >> j) & 1u) A::red_add(s, red[wib][v][j]);
-      }
-#pragma unroll
-      for (int m = 1; m < LPV; m <<= 1) A::red_add(s, A::red_shfl_xor(s, m));
-      if (v < NV && part == 0) atomicAdd(acc + (size_t)b.row * 2 * NB2 * 2 + v, A::red_to_double(s));
-    }
-    __syncwarp();
-  }
-  // reverse sums of this item's column
-  if (colok && any_rev) {
-    double* dst = acc + (size_t)col * 2 * NB2 * 2;
-#pragma unroll
-    for (int i = 0; i < NB2; ++i) {
-      atomicAdd(dst + 2 * i, A::re_d(rX[i]));
-      atomicAdd(dst + 2 * i + 1, A::im_d(rX[i]));
-      atomicAdd(dst + 2 * NB2 + 2 * i, A::re_d(rY[i]));
-      atomicAdd(dst + 2 * NB2 + 2 * i + 1, A::im_d(rY[i]));
-    }
-  }
-}
-
-// prep for the column-block kernels: rt, st per k written at pos[k] in the arithmetic's element
-// format, accumulators zeroed. One thread per (k, element).
-template <typename A, int NB>
-__global__ void k_prep_cb(int nk, int nbdm, int bs, const double2* __restrict__ y, const double* __restrict__ ew,
-                          const int* __restrict__ pos, TimeArg ta, int phase, typename A::elem* __restrict__ rs,
-                          double2* __restrict__ acc) {
+__global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict__ y, const double* __restrict__ ew,
+                            const int* __restrict__ pos, TimeArg ta, int phase, typename A::relem* __restrict__ rs,
+                            double2* __restrict__ acc, unsigned int* __restrict__ hflag) {
   constexpr int NB2 = NB * NB;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nk * NB2) return;
   const int k = idx / NB2, ab = idx - k * NB2, i = ab / NB, j = ab - i * NB;
-  const double2 r = y[(size_t)k * nbdm * nbdm + (bs + i) * nbdm + bs + j];
-  const double2 s = (i == j) ? mk2(1.0 - r.x, 0.0 - r.y) : mk2(-r.x, -r.y);
-  double2 rt = r, st = s;
-  if (phase) {
-    const double t = eval_time(ta);
-    const double2 d = ccis((ew[k * NB + i] - ew[k * NB + j]) * t);
-    rt = cmul_rn(cconj(d), r);
-    st = cmul_rn(cconj(d), s);
-  }
   const int p = pos[k];
-  rs[(size_t)p * 2 * NB2 + ab] = A::from_double2(rt);
-  rs[(size_t)p * 2 * NB2 + NB2 + ab] = A::from_double2(st);
   acc[(size_t)p * 2 * NB2 + ab] = mk2(0.0, 0.0);
   acc[(size_t)p * 2 * NB2 + NB2 + ab] = mk2(0.0, 0.0);
+  if (i > j) return;
+  typename A::relem* rh = rs + (size_t)p * 2 * NB2;
+  typename A::relem* ra = rs + (size_t)nk * 2 * NB2 + (size_t)p * 2 * NB2;
+  const double2* yk = y + (size_t)k * nbdm * nbdm;
+  const double2 vij = yk[(bs + i) * nbdm + bs + j];
+  if (i == j) {
+    // H_ii = Re rho_ii, A_ii = Im rho_ii; 1 - rho: (1 - Re rho_ii, -Im rho_ii) (set_oneminusdm)
+    rh[ab] = A::from_double(vij.x);
+    rh[NB2 + ab] = A::from_double(1.0 - vij.x);
+    ra[ab] = A::from_double(vij.y);
+    ra[NB2 + ab] = A::from_double(0.0 - vij.y);
+    if (vij.y != 0.0) atomicOr(hflag, 1u);
+    return;
+  }
+  const double2 vji = yk[(bs + j) * nbdm + bs + i];
+  // H_ij = (rho_ij + conj(rho_ji)) / 2, A_ij = (rho_ij - conj(rho_ji)) / (2i); exact for Hermitian rho
+  const double2 hij = mk2(__dmul_rn(__dadd_rn(vij.x, vji.x), 0.5), __dmul_rn(__dsub_rn(vij.y, vji.y), 0.5));
+  const double2 dif = mk2(__dsub_rn(vij.x, vji.x), __dadd_rn(vij.y, vji.y));  // rho_ij - conj(rho_ji)
+  const double2 aij = mk2(__dmul_rn(dif.y, 0.5), __dmul_rn(-dif.x, 0.5));
+  if (dif.x != 0.0 || dif.y != 0.0) atomicOr(hflag, 1u);
+  double2 d = mk2(1.0, 0.0);
+  if (phase) d = cconj(ccis((ew[k * NB + i] - ew[k * NB + j]) * eval_time(ta)));
+  const double2 r1 = cmul_rn(d, hij);                       // conj(D) o H
+  const double2 s1 = cmul_rn(d, mk2(-hij.x, -hij.y));       // conj(D) o (1 - H) off the diagonal
+  const double2 r2 = cmul_rn(d, aij);                       // conj(D) o A
+  const double2 s2 = cmul_rn(d, mk2(-aij.x, -aij.y));       // conj(D) o (-A)
+  const int ji = j * NB + i;
+  rh[ab] = A::from_double(r1.x);
+  rh[ji] = A::from_double(r1.y);
+  rh[NB2 + ab] = A::from_double(s1.x);
+  rh[NB2 + ji] = A::from_double(s1.y);
+  ra[ab] = A::from_double(r2.x);
+  ra[ji] = A::from_double(r2.y);
+  ra[NB2 + ab] = A::from_double(s2.x);
+  ra[NB2 + ji] = A::from_double(s2.y);
 }
 
-
 // ---------------------------------------------------------------------------------------------
-// The same contraction with the P elements staged through shared memory by bulk copies.
-//
-// In this layout each pair stores P1 row-major and P2 column-major, so both halves are consumed
-// "line by line": a P1 row a completes the forward output X_k[a] and a P2 column c completes
-// Y_k[c], while the lane's reverse sums Y_col (indexed by P1's column) and X_col (indexed by P2's
-// row) stay in registers with compile-time indices. A row block is consumed in chunks of LINES
-// lines; each warp double-buffers its chunks, issuing the copy of chunk i + 2 while it computes
-// chunk i. The row's vectors rt_k, st_k are staged in shared memory once per row block. Waits are
-// bounded (dmd_tma.cuh); a timeout sets *errflag.
+// The contraction. P2 is stored column-major, so both halves of a pair are consumed "line by
+// line": a Q1 row a completes X'_k[a] and a Q2 column j completes Y'_k[j], while the lane's reverse
+// sums Y'_c (indexed by Q1's column) and X'_c (indexed by Q2's row) stay in registers with
+// compile-time indices. A row block is consumed in chunks of LINES lines; each warp double-buffers
+// its chunks, issuing the copy of chunk i + 2 while it computes chunk i. The row's coordinates
+// r_k, s_k are staged in shared memory once per row block. Waits are bounded (dmd_tma.cuh); a
+// timeout sets *errflag.
 // ---------------------------------------------------------------------------------------------
 template <typename A, int NB, int LINES>
 struct CbTmaSmem {
@@ -315,33 +212,36 @@ struct CbTmaSmem {
   static constexpr int CPR = 2 * CPM;      // chunks per row block
   static constexpr size_t stage_bytes = (size_t)LINES * NB2 * 32 * sizeof(typename A::elem);
   static constexpr size_t red_bytes = (size_t)NV * 32 * sizeof(typename A::red_t);
-  static constexpr size_t row_bytes = (size_t)2 * NB2 * sizeof(typename A::elem);
+  static constexpr size_t row_bytes = (size_t)2 * NB2 * sizeof(typename A::relem);
   static constexpr size_t warp_bytes = ((2 * stage_bytes + red_bytes + row_bytes + 16) + 127) / 128 * 128;
   static constexpr size_t cta_bytes = 4 * warp_bytes;
 };
 
 template <typename A, int NB, int LINES, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_pairs_cb_tma(const WorkItem* __restrict__ items, int nitems,
-                                                            const RowBlock* __restrict__ rbs,
-                                                            const typename A::elem* __restrict__ P,
-                                                            const typename A::elem* __restrict__ rs,
-                                                            double* __restrict__ acc, int nk,
-                                                            unsigned int* __restrict__ errflag) {
+__global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __restrict__ items, int nitems,
+                                                          const RowBlock* __restrict__ rbs,
+                                                          const typename A::elem* __restrict__ P,
+                                                          const typename A::relem* __restrict__ rs,
+                                                          double* __restrict__ acc, int nk, int imag,
+                                                          const unsigned int* __restrict__ gate,
+                                                          unsigned int* __restrict__ errflag) {
   typedef CbTmaSmem<A, NB, LINES> S;
   constexpr int NB2 = S::NB2, NB4 = S::NB4, NV = S::NV, CPM = S::CPM, CPR = S::CPR;
   constexpr size_t SE = S::stage_bytes / sizeof(typename A::elem);  // elements per stage
   typedef typename A::elem E;
+  typedef typename A::relem V;
   typedef typename A::acc Acc;
   typedef typename A::red_t R;
   extern __shared__ __align__(128) unsigned char smem_raw[];
+  if (gate && *gate == 0u) return;  // anti-Hermitian pass with nothing to do
   const int wib = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int item = blockIdx.x * 4 + wib;
   if (item >= nitems) return;
   unsigned char* wbase = smem_raw + (size_t)wib * S::warp_bytes;
   E* const stage0 = (E*)wbase;
-  R* const red = (R*)(wbase + 2 * S::stage_bytes);                             // [NV][32]
-  E* const rowv = (E*)(wbase + 2 * S::stage_bytes + S::red_bytes);             // rt_k[NB2], st_k[NB2]
+  R* const red = (R*)(wbase + 2 * S::stage_bytes);                 // [NV][32]
+  V* const rowv = (V*)(wbase + 2 * S::stage_bytes + S::red_bytes);  // r_k[NB2], s_k[NB2]
   uint64_t* const bar = (uint64_t*)(wbase + 2 * S::stage_bytes + S::red_bytes + S::row_bytes);
   const WorkItem w = items[item];
   const int nch = CPR * (w.rb1 - w.rb0);
@@ -367,11 +267,11 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_cb_tma(const WorkItem* __re
   }
   const int col = w.J * 32 + lane;
   const bool colok = col < nk;
-  E rc[NB2], sc[NB2];
+  V rc[NB2], sc[NB2];
 #pragma unroll
   for (int i = 0; i < NB2; ++i) {
-    rc[i] = colok ? rs[(size_t)col * 2 * NB2 + i] : E();
-    sc[i] = colok ? rs[(size_t)col * 2 * NB2 + NB2 + i] : E();
+    rc[i] = colok ? rs[(size_t)col * 2 * NB2 + i] : V();
+    sc[i] = colok ? rs[(size_t)col * 2 * NB2 + NB2 + i] : V();
   }
   Acc rX[NB2], rY[NB2];
 #pragma unroll
@@ -403,38 +303,38 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_cb_tma(const WorkItem* __re
       const int l0 = (q % CPM) * LINES;
       if (active) {
         if (q < CPM) {
-          // P1 rows a = l0..: X_k[a] = sum_cc P1[a][cc] rt_col[cc];  Y_col[cc] += st_k[a] conj(P1[a][cc])
+          // Q1 rows a: X'_k[a] = sum_j Q1[a][j] r_c[j];  Y'_c[j] += s_k[a] conj(Q1[a][j])
 #pragma unroll
           for (int r = 0; r < LINES; ++r) {
             const int a = l0 + r;
-            const E sra = rowv[NB2 + a];
+            const V ska = rowv[NB2 + a];
             Acc f;
             A::zero(f);
 #pragma unroll
-            for (int cc = 0; cc < NB2; ++cc) {
-              const E p1 = st[(r * NB2 + cc) * n];
-              A::mac(f, p1, rc[cc]);
-              if (rev) A::mac_cx(rY[cc], p1, sra);
+            for (int j = 0; j < NB2; ++j) {
+              const E p1 = st[(r * NB2 + j) * n];
+              A::mac(f, p1, rc[j]);
+              if (rev) A::mac_cx(rY[j], p1, ska);
             }
-            red[(2 * a) * 32 + lane] = A::red_re(f);
-            red[(2 * a + 1) * 32 + lane] = A::red_im(f);
+            red[(2 * a) * 32 + lane] = imag ? A::red_neg(A::red_im(f)) : A::red_re(f);
+            red[(2 * a + 1) * 32 + lane] = imag ? A::red_re(f) : A::red_im(f);
           }
         } else {
-          // P2 columns cc = l0..: Y_k[cc] = sum_a st_col[a] P2[a][cc];  X_col[a] += conj(P2[a][cc]) rt_k[cc]
+          // Q2 columns j: Y'_k[j] = sum_a Q2[a][j] s_c[a];  X'_c[a] += conj(Q2[a][j]) r_k[j]
 #pragma unroll
           for (int r = 0; r < LINES; ++r) {
-            const int cc = l0 + r;
-            const E rrc = rowv[cc];
+            const int j = l0 + r;
+            const V rkj = rowv[j];
             Acc f;
             A::zero(f);
 #pragma unroll
             for (int a = 0; a < NB2; ++a) {
               const E p2 = st[(r * NB2 + a) * n];
               A::mac(f, p2, sc[a]);
-              if (rev) A::mac_cx(rX[a], p2, rrc);
+              if (rev) A::mac_cx(rX[a], p2, rkj);
             }
-            red[(2 * NB2 + 2 * cc) * 32 + lane] = A::red_re(f);
-            red[(2 * NB2 + 2 * cc + 1) * 32 + lane] = A::red_im(f);
+            red[(2 * NB2 + 2 * j) * 32 + lane] = imag ? A::red_neg(A::red_im(f)) : A::red_re(f);
+            red[(2 * NB2 + 2 * j + 1) * 32 + lane] = imag ? A::red_re(f) : A::red_im(f);
           }
         }
       }
@@ -463,9 +363,9 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_cb_tma(const WorkItem* __re
         const int span = 32 / LPV;
         unsigned m = (b.mask >> (part * span)) & (span == 32 ? 0xffffffffu : ((1u << span) - 1u));
         while (m) {
-          const int j = __ffs(m) - 1;
+          const int jj = __ffs(m) - 1;
           m &= m - 1;
-          A::red_add(s, red[v * 32 + part * span + j]);
+          A::red_add(s, red[v * 32 + part * span + jj]);
         }
       }
 #pragma unroll
@@ -488,10 +388,11 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_cb_tma(const WorkItem* __re
     double* dst = acc + (size_t)col * 2 * NB2 * 2;
 #pragma unroll
     for (int i = 0; i < NB2; ++i) {
-      atomicAdd(dst + 2 * i, A::re_d(rX[i]));
-      atomicAdd(dst + 2 * i + 1, A::im_d(rX[i]));
-      atomicAdd(dst + 2 * NB2 + 2 * i, A::re_d(rY[i]));
-      atomicAdd(dst + 2 * NB2 + 2 * i + 1, A::im_d(rY[i]));
+      const double xr = A::re_d(rX[i]), xi = A::im_d(rX[i]), yr = A::re_d(rY[i]), yi = A::im_d(rY[i]);
+      atomicAdd(dst + 2 * i, imag ? -xi : xr);
+      atomicAdd(dst + 2 * i + 1, imag ? xr : xi);
+      atomicAdd(dst + 2 * NB2 + 2 * i, imag ? -yi : yr);
+      atomicAdd(dst + 2 * NB2 + 2 * i + 1, imag ? yr : yi);
     }
   }
 }

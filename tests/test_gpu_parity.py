@@ -245,3 +245,20 @@ def test_t1_from_gpu_trajectory(oracle, built):
     assert np.isfinite(fo.tau_lsq) and np.isfinite(fg.tau_lsq)
     assert abs(fg.tau_lsq - fo.tau_lsq) / fo.tau_lsq < 1e-8
     assert abs(fg.tau_cf - fo.tau_cf) / fo.tau_cf < 1e-8
+
+
+@pytest.mark.parametrize("prec", ["f64", "f64x"])
+def test_non_hermitian_state_vs_oracle(prec, oracle, built):
+    """func on a state that is not Hermitian (the GSL callback accepts any y): the contraction runs
+    its anti-Hermitian pass, and a Hermitian state right after must not see a stale flag."""
+    s = oracle.load(os.path.join(GOLDEN, "nb2_eimp_B"))
+    rng = np.random.default_rng(21)
+    t = 13.0 * oracle.fs
+    dm = s.dm0 + 1e-3 * (rng.standard_normal(s.dm0.shape) + 1j * rng.standard_normal(s.dm0.shape))
+    y_nh = oracle.y_of(dm)
+    d = dm.reshape(s.nk, s.nb_dm, s.nb_dm)
+    y_h = oracle.y_of((0.5 * (d + np.conj(np.swapaxes(d, 1, 2)))).reshape(s.nk, -1))
+    with make_gpu(s, prec) as gpu:
+        for y in (y_nh, y_h, y_nh):
+            err = rel(gpu.func(t, y), oracle.rhs(s, t, y))
+            assert err < RHS_TOL[prec], err
