@@ -30,6 +30,7 @@ struct dmd_handle {
   double2* d_P = nullptr;      // [npair][2][nb4] (per-thread form) or the column-block element store
   // column-block layout (nb = 2)
   int use_cb = 0;
+  int pcfg = 0;                // pair-kernel shape variant (DMD_PAIR_CFG)
   int* d_pos = nullptr;        // k -> energy rank
   dmd::RowBlock* d_rb = nullptr;
   dmd::WorkItem* d_items = nullptr;
@@ -172,6 +173,28 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
   return DMD_OK;
 }
 
+// the Hermitian pass and the gated anti-Hermitian pass of the nb = 2 contraction
+template <typename A, int L, int NST, int MB>
+void herm_pair_launches(dmd_handle* h, const typename A::relem* rs, size_t half) {
+  typedef CbTmaSmem<A, 2, L, NST> S;
+  const unsigned g = blocks_for(h->nitems, 4);
+  k_pairs_herm<A, 2, L, NST, MB, false><<<g, 128, S::cta_bytes, h->st>>>(
+      h->d_items, h->nitems, h->d_rb, (const typename A::elem*)h->d_P, rs, (double*)h->d_acc, h->nk, nullptr, h->d_err);
+  k_pairs_herm<A, 2, L, NST, MB, true><<<g, 128, S::cta_bytes, h->st>>>(
+      h->d_items, h->nitems, h->d_rb, (const typename A::elem*)h->d_P, rs + half, (double*)h->d_acc, h->nk,
+      h->d_hflag, h->d_err);
+}
+
+template <typename A, int L, int NST, int MB>
+cudaError_t herm_pair_attrs() {
+  const int bytes = (int)CbTmaSmem<A, 2, L, NST>::cta_bytes;
+  cudaError_t e =
+      cudaFuncSetAttribute(k_pairs_herm<A, 2, L, NST, MB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_pairs_herm<A, 2, L, NST, MB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return e;
+}
+
 template <int NB>
 int launch_pairs(dmd_handle* h) {
   if (h->npair == 0) return DMD_OK;
@@ -183,22 +206,20 @@ int launch_pairs(dmd_handle* h) {
     if constexpr (NB == 2) {
       // Hermitian coordinates; the second launch carries the anti-Hermitian part of a state that is
       // not exactly Hermitian and returns at once unless the prep kernel raised d_hflag
-      const unsigned g = blocks_for(h->nitems, 4);
       const size_t half = (size_t)h->nk * 2 * h->nb2;  // coordinates per part
-      for (int pass = 0; pass < 2; ++pass) {
-        const unsigned int* gate = pass ? h->d_hflag : nullptr;
-        if (h->prec == DMD_PREC_F64X) {
-          const float2* rs = (const float2*)h->d_rs + pass * half;
-          k_pairs_herm<ArithDF, NB, 2, 4><<<g, 128, CbTmaSmem<ArithDF, NB, 2>::cta_bytes, h->st>>>(
-              h->d_items, h->nitems, h->d_rb, (const float4*)h->d_P, rs, (double*)h->d_acc, h->nk, pass, gate,
-              h->d_err);
-        } else {
-          const double* rs = (const double*)h->d_rs + pass * half;
-          k_pairs_herm<ArithF64, NB, 2, 4><<<g, 128, CbTmaSmem<ArithF64, NB, 2>::cta_bytes, h->st>>>(
-              h->d_items, h->nitems, h->d_rb, h->d_P, rs, (double*)h->d_acc, h->nk, pass, gate, h->d_err);
+      if (h->prec == DMD_PREC_F64X) {
+        const float2* rs = (const float2*)h->d_rs;
+        switch (h->pcfg) {
+          case 1: herm_pair_launches<ArithDF, 2, 3, 3>(h, rs, half); break;
+          case 2: herm_pair_launches<ArithDF, 1, 4, 4>(h, rs, half); break;
+          case 3: herm_pair_launches<ArithDF, 1, 3, 4>(h, rs, half); break;
+          case 4: herm_pair_launches<ArithDF, 1, 6, 3>(h, rs, half); break;
+          default: herm_pair_launches<ArithDF, 2, 2, 4>(h, rs, half); break;
         }
-        if (pass == 0) h->launches++;
+      } else {
+        herm_pair_launches<ArithF64, 2, 2, 4>(h, (const double*)h->d_rs, half);
       }
+      h->launches++;
     }
   }
   h->launches++;
@@ -386,10 +407,12 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
     return fail(h, DMD_E_ARG, "k-pair index out of range");
   h->nitems = (int)L.items.size();
   h->nrb = (long long)L.rb.size();
-  CK(cudaFuncSetAttribute(k_pairs_herm<ArithDF, 2, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)CbTmaSmem<ArithDF, 2, 2>::cta_bytes));
-  CK(cudaFuncSetAttribute(k_pairs_herm<ArithF64, 2, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)CbTmaSmem<ArithF64, 2, 2>::cta_bytes));
+  // pair-kernel shape (stage lines, resident CTAs per SM); 0 is the default, the others serve tuning
+  if (const char* v = getenv("DMD_PAIR_CFG")) h->pcfg = atoi(v);
+  cudaError_t (*const attrs[])() = {herm_pair_attrs<ArithDF, 2, 2, 4>, herm_pair_attrs<ArithDF, 2, 3, 3>,
+                                    herm_pair_attrs<ArithDF, 1, 4, 4>, herm_pair_attrs<ArithDF, 1, 3, 4>,
+                                    herm_pair_attrs<ArithDF, 1, 6, 3>, herm_pair_attrs<ArithF64, 2, 2, 4>};
+  for (auto fn : attrs) CK(fn());
   int rc;
   if ((rc = dalloc(h, &h->d_pos, (size_t)h->nk)) || (rc = dalloc(h, &h->d_rb, L.rb.size())) ||
       (rc = dalloc(h, &h->d_items, L.items.size())))

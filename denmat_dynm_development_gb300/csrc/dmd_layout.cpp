@@ -82,7 +82,8 @@ bool build_pair_layout(int nk, int nb, const double* e_w, long long npair, const
     w.J = J;
     w.rb0 = (int32_t)i;
     long long np = 0;
-    while (i < L.rb.size() && (pcol[L.src[L.rb[i].pair0]] >> 5) == J && np < pairs_per_item) {
+    while (i < L.rb.size() && (pcol[L.src[L.rb[i].pair0]] >> 5) == J && np < pairs_per_item &&
+           (int)(i - w.rb0) < kMaxRowBlocksPerItem) {
       np += __builtin_popcount(L.rb[i].mask);
       ++i;
     }

@@ -27,6 +27,9 @@ struct RowBlock {
   uint32_t pair0;    // index of the block's first pair in the permuted pair order
 };
 
+// row blocks per work item at most: the contraction kernel keeps one descriptor per lane
+constexpr int kMaxRowBlocksPerItem = 32;
+
 struct WorkItem {
   int32_t J;         // column block
   int32_t rb0, rb1;  // row blocks [rb0, rb1)

@@ -200,34 +200,37 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
 // The contraction. P2 is stored column-major, so both halves of a pair are consumed "line by
 // line": a Q1 row a completes X'_k[a] and a Q2 column j completes Y'_k[j], while the lane's reverse
 // sums Y'_c (indexed by Q1's column) and X'_c (indexed by Q2's row) stay in registers with
-// compile-time indices. A row block is consumed in chunks of LINES lines; each warp double-buffers
-// its chunks, issuing the copy of chunk i + 2 while it computes chunk i. The row's coordinates
-// r_k, s_k are staged in shared memory once per row block. Waits are bounded (dmd_tma.cuh); a
-// timeout sets *errflag.
+// compile-time indices. A row block is consumed in chunks of LINES lines that stream through a
+// per-warp ring of NST stages: the copy of chunk i + NST is issued as soon as chunk i has been
+// read. Lane r holds the descriptor of the item's row block r (items have at most 32), so issuing
+// a copy needs no memory access; the next row's coordinates are fetched one row block ahead.
+// Waits are bounded (dmd_tma.cuh); a timeout sets *errflag.
 // ---------------------------------------------------------------------------------------------
-template <typename A, int NB, int LINES>
+template <typename A, int NB, int LINES, int NST>
 struct CbTmaSmem {
   static constexpr int NB2 = NB * NB, NB4 = NB2 * NB2, NV = 4 * NB2;
   static constexpr int CPM = NB2 / LINES;  // chunks per matrix
   static constexpr int CPR = 2 * CPM;      // chunks per row block
   static constexpr size_t stage_bytes = (size_t)LINES * NB2 * 32 * sizeof(typename A::elem);
   static constexpr size_t red_bytes = (size_t)NV * 32 * sizeof(typename A::red_t);
-  static constexpr size_t row_bytes = (size_t)2 * NB2 * sizeof(typename A::relem);
-  static constexpr size_t warp_bytes = ((2 * stage_bytes + red_bytes + row_bytes + 16) + 127) / 128 * 128;
+  static constexpr size_t row_bytes = (size_t)4 * NB2 * sizeof(typename A::relem);  // r_k, s_k, zeros
+  static constexpr size_t warp_bytes = ((NST * stage_bytes + red_bytes + row_bytes + 8 * NST) + 127) / 128 * 128;
   static constexpr size_t cta_bytes = 4 * warp_bytes;
 };
 
-template <typename A, int NB, int LINES, int MINB>
+// IMAG: the sums are multiplied by i before they are added (anti-Hermitian pass)
+template <typename A, int NB, int LINES, int NST, int MINB, bool IMAG>
 __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __restrict__ items, int nitems,
                                                           const RowBlock* __restrict__ rbs,
                                                           const typename A::elem* __restrict__ P,
                                                           const typename A::relem* __restrict__ rs,
-                                                          double* __restrict__ acc, int nk, int imag,
+                                                          double* __restrict__ acc, int nk,
                                                           const unsigned int* __restrict__ gate,
                                                           unsigned int* __restrict__ errflag) {
-  typedef CbTmaSmem<A, NB, LINES> S;
+  typedef CbTmaSmem<A, NB, LINES, NST> S;
   constexpr int NB2 = S::NB2, NB4 = S::NB4, NV = S::NV, CPM = S::CPM, CPR = S::CPR;
   constexpr size_t SE = S::stage_bytes / sizeof(typename A::elem);  // elements per stage
+  constexpr unsigned FULL = 0xffffffffu;
   typedef typename A::elem E;
   typedef typename A::relem V;
   typedef typename A::acc Acc;
@@ -240,31 +243,44 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
   if (item >= nitems) return;
   unsigned char* wbase = smem_raw + (size_t)wib * S::warp_bytes;
   E* const stage0 = (E*)wbase;
-  R* const red = (R*)(wbase + 2 * S::stage_bytes);                 // [NV][32]
-  V* const rowv = (V*)(wbase + 2 * S::stage_bytes + S::red_bytes);  // r_k[NB2], s_k[NB2]
-  uint64_t* const bar = (uint64_t*)(wbase + 2 * S::stage_bytes + S::red_bytes + S::row_bytes);
+  R* const red = (R*)(wbase + NST * S::stage_bytes);                  // [NV][32]
+  V* const rowv = (V*)(wbase + NST * S::stage_bytes + S::red_bytes);  // r_k[NB2], s_k[NB2], zeros[2 NB2]
+  uint64_t* const bar = (uint64_t*)(wbase + NST * S::stage_bytes + S::red_bytes + S::row_bytes);
   const WorkItem w = items[item];
-  const int nch = CPR * (w.rb1 - w.rb0);
+  const int nrb = w.rb1 - w.rb0;  // <= kMaxRowBlocksPerItem = 32
+  RowBlock mine;                  // lane r: the item's row block r
+  mine.row = 0;
+  mine.mask = 0;
+  mine.revmask = 0;
+  mine.pair0 = 0;
+  if (lane < nrb) mine = rbs[w.rb0 + lane];
+  const int nch = CPR * nrb;
   if (lane == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+#pragma unroll
+    for (int s = 0; s < NST; ++s) mbar_init(&bar[s], 1);
     fence_mbar_init();
   }
   __syncwarp();
   const uint64_t pol = policy_evict_first();
-  auto issue = [&](int c) {  // lane 0 only: chunk c of the item into stage c & 1
-    const RowBlock b = rbs[w.rb0 + c / CPR];
-    const int q = c % CPR;
-    const int n = __popc(b.mask);
-    const size_t off = (size_t)b.pair0 * 2 * NB4 + ((size_t)(q / CPM) * NB4 + (size_t)(q % CPM) * LINES * NB2) * n;
-    const uint32_t bytes = (uint32_t)(LINES * NB2 * n * sizeof(E));
-    mbar_arrive_expect_tx(&bar[c & 1], bytes);
-    bulk_g2s(stage0 + (size_t)(c & 1) * SE, P + off, bytes, &bar[c & 1], pol);
+  // chunk c of the item into stage c % NST; called by the whole warp, lane 0 issues
+  auto issue = [&](int c) {
+    const int rbi = c / CPR;
+    const uint32_t p0 = __shfl_sync(FULL, mine.pair0, rbi);
+    const uint32_t m = __shfl_sync(FULL, mine.mask, rbi);
+    if (lane == 0) {
+      const int q = c % CPR;
+      const int n = __popc(m);
+      const size_t off = (size_t)p0 * 2 * NB4 + ((size_t)(q / CPM) * NB4 + (size_t)(q % CPM) * LINES * NB2) * n;
+      const uint32_t bytes = (uint32_t)(LINES * NB2 * n * sizeof(E));
+      const int s = c % NST;
+      mbar_arrive_expect_tx(&bar[s], bytes);
+      bulk_g2s(stage0 + (size_t)s * SE, P + off, bytes, &bar[s], pol);
+    }
   };
-  if (lane == 0) {
-    issue(0);
-    if (nch > 1) issue(1);
-  }
+#pragma unroll
+  for (int c = 0; c < NST; ++c)
+    if (c < nch) issue(c);
+  if (lane < 2 * NB2) rowv[2 * NB2 + lane] = V();
   const int col = w.J * 32 + lane;
   const bool colok = col < nk;
   V rc[NB2], sc[NB2];
@@ -279,27 +295,43 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
     A::zero(rX[i]);
     A::zero(rY[i]);
   }
+  // coordinates of the first row
+  V rnext = V();
+  {
+    const int r0 = __shfl_sync(FULL, mine.row, 0);
+    if (lane < 2 * NB2 && nrb > 0) rnext = rs[(size_t)r0 * 2 * NB2 + lane];
+  }
   bool any_rev = false;
-  bool failed = false;
+  int cfail = -1;
   const unsigned lt = (1u << lane) - 1u;
 #pragma unroll 1
-  for (int rbi = 0; rbi < w.rb1 - w.rb0; ++rbi) {
-    const RowBlock b = rbs[w.rb0 + rbi];
-    const bool active = (b.mask >> lane) & 1u;
-    const bool rev = (b.revmask >> lane) & 1u;
+  for (int rbi = 0; rbi < nrb; ++rbi) {
+    const int brow = __shfl_sync(FULL, mine.row, rbi);
+    const unsigned bmask = __shfl_sync(FULL, mine.mask, rbi);
+    const unsigned brev = __shfl_sync(FULL, mine.revmask, rbi);
+    const int nrow = __shfl_sync(FULL, mine.row, rbi + 1 < nrb ? rbi + 1 : rbi);
+    const bool active = (bmask >> lane) & 1u;
+    // a lane whose pair has no reverse term reads zero row coordinates: its reverse sums receive
+    // exact zeros and the inner loops carry no branch
+    const bool rev = (brev >> lane) & 1u;
     any_rev |= rev;
-    const int n = __popc(b.mask);
-    const int slot = __popc(b.mask & lt);
-    if (lane < 2 * NB2) rowv[lane] = rs[(size_t)b.row * 2 * NB2 + lane];
+    const int n = __popc(bmask);
+    const int slot = __popc(bmask & lt);
+    if (lane < 2 * NB2) {
+      rowv[lane] = rnext;
+      if (rbi + 1 < nrb) rnext = rs[(size_t)nrow * 2 * NB2 + lane];
+    }
     __syncwarp();
+    const V* rv = rowv + (rev ? 0 : 2 * NB2);
 #pragma unroll 1
     for (int q = 0; q < CPR; ++q) {
       const int c = rbi * CPR + q;
-      if (!mbar_wait_bounded(&bar[c & 1], (uint32_t)((c >> 1) & 1), errflag)) {
-        failed = true;
+      const int s = c % NST;
+      if (!__all_sync(FULL, mbar_wait_bounded(&bar[s], (uint32_t)((c / NST) & 1), errflag))) {
+        cfail = c;
         break;
       }
-      const E* st = stage0 + (size_t)(c & 1) * SE + slot;
+      const E* st = stage0 + (size_t)s * SE + slot;
       const int l0 = (q % CPM) * LINES;
       if (active) {
         if (q < CPM) {
@@ -307,45 +339,45 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
 #pragma unroll
           for (int r = 0; r < LINES; ++r) {
             const int a = l0 + r;
-            const V ska = rowv[NB2 + a];
+            const V ska = rv[NB2 + a];
             Acc f;
             A::zero(f);
 #pragma unroll
             for (int j = 0; j < NB2; ++j) {
               const E p1 = st[(r * NB2 + j) * n];
               A::mac(f, p1, rc[j]);
-              if (rev) A::mac_cx(rY[j], p1, ska);
+              A::mac_cx(rY[j], p1, ska);
             }
-            red[(2 * a) * 32 + lane] = imag ? A::red_neg(A::red_im(f)) : A::red_re(f);
-            red[(2 * a + 1) * 32 + lane] = imag ? A::red_re(f) : A::red_im(f);
+            red[(2 * a) * 32 + lane] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
+            red[(2 * a + 1) * 32 + lane] = IMAG ? A::red_re(f) : A::red_im(f);
           }
         } else {
           // Q2 columns j: Y'_k[j] = sum_a Q2[a][j] s_c[a];  X'_c[a] += conj(Q2[a][j]) r_k[j]
 #pragma unroll
           for (int r = 0; r < LINES; ++r) {
             const int j = l0 + r;
-            const V rkj = rowv[j];
+            const V rkj = rv[j];
             Acc f;
             A::zero(f);
 #pragma unroll
             for (int a = 0; a < NB2; ++a) {
               const E p2 = st[(r * NB2 + a) * n];
               A::mac(f, p2, sc[a]);
-              if (rev) A::mac_cx(rX[a], p2, rkj);
+              A::mac_cx(rX[a], p2, rkj);
             }
-            red[(2 * NB2 + 2 * j) * 32 + lane] = imag ? A::red_neg(A::red_im(f)) : A::red_re(f);
-            red[(2 * NB2 + 2 * j + 1) * 32 + lane] = imag ? A::red_re(f) : A::red_im(f);
+            red[(2 * NB2 + 2 * j) * 32 + lane] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
+            red[(2 * NB2 + 2 * j + 1) * 32 + lane] = IMAG ? A::red_re(f) : A::red_im(f);
           }
         }
       }
-      // the stage buffer is free once every lane has read it: order those reads before the next
-      // bulk copy into it (generic -> async proxy), then refill it
+      // the stage is free once every lane has read it: order those reads before the next bulk copy
+      // into it (generic -> async proxy), then refill it
       fence_proxy_async();
       __syncwarp();
-      if (lane == 0 && c + 2 < nch) issue(c + 2);
+      if (c + NST < nch) issue(c + NST);
     }
-    if (failed) break;
-    if (active && rev) {
+    if (cfail >= 0) break;
+    if (active) {
 #pragma unroll
       for (int i = 0; i < NB2; ++i) {
         A::renorm(rX[i]);
@@ -358,28 +390,26 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
     for (int v0 = 0; v0 < NV; v0 += 32 / LPV) {
       const int v = v0 + lane / LPV;
       const int part = lane % LPV;
-      R s = A::red_zero();
+      R sum = A::red_zero();
       if (v < NV) {
         const int span = 32 / LPV;
-        unsigned m = (b.mask >> (part * span)) & (span == 32 ? 0xffffffffu : ((1u << span) - 1u));
+        unsigned m = (bmask >> (part * span)) & (span == 32 ? 0xffffffffu : ((1u << span) - 1u));
         while (m) {
           const int jj = __ffs(m) - 1;
           m &= m - 1;
-          A::red_add(s, red[v * 32 + part * span + jj]);
+          A::red_add(sum, red[v * 32 + part * span + jj]);
         }
       }
 #pragma unroll
-      for (int mm = 1; mm < LPV; mm <<= 1) A::red_add(s, A::red_shfl_xor(s, mm));
-      if (v < NV && part == 0) atomicAdd(acc + (size_t)b.row * 2 * NB2 * 2 + v, A::red_to_double(s));
+      for (int mm = 1; mm < LPV; mm <<= 1) A::red_add(sum, A::red_shfl_xor(sum, mm));
+      if (v < NV && part == 0) atomicAdd(acc + (size_t)brow * 2 * NB2 * 2 + v, A::red_to_double(sum));
     }
     __syncwarp();
   }
-  if (failed) {  // drain whatever copies are still pending (bounded), then leave
+  if (cfail >= 0) {  // drain the copies still in flight (bounded), then leave
     if (lane == 0) {
-      mbar_wait_bounded(&bar[0], 0, nullptr, 1u << 16);
-      mbar_wait_bounded(&bar[1], 0, nullptr, 1u << 16);
-      mbar_wait_bounded(&bar[0], 1, nullptr, 1u << 16);
-      mbar_wait_bounded(&bar[1], 1, nullptr, 1u << 16);
+      const int clast = (cfail + NST < nch ? cfail + NST : nch) - 1;
+      for (int c = cfail; c <= clast; ++c) mbar_wait_bounded(&bar[c % NST], (uint32_t)((c / NST) & 1), nullptr, 1u << 16);
     }
     __syncwarp();
     return;
@@ -389,10 +419,10 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
 #pragma unroll
     for (int i = 0; i < NB2; ++i) {
       const double xr = A::re_d(rX[i]), xi = A::im_d(rX[i]), yr = A::re_d(rY[i]), yi = A::im_d(rY[i]);
-      atomicAdd(dst + 2 * i, imag ? -xi : xr);
-      atomicAdd(dst + 2 * i + 1, imag ? xr : xi);
-      atomicAdd(dst + 2 * NB2 + 2 * i, imag ? -yi : yr);
-      atomicAdd(dst + 2 * NB2 + 2 * i + 1, imag ? yr : yi);
+      atomicAdd(dst + 2 * i, IMAG ? -xi : xr);
+      atomicAdd(dst + 2 * i + 1, IMAG ? xr : xi);
+      atomicAdd(dst + 2 * NB2 + 2 * i, IMAG ? -yi : yr);
+      atomicAdd(dst + 2 * NB2 + 2 * i + 1, IMAG ? yr : yi);
     }
   }
 }
