@@ -57,6 +57,15 @@ __device__ __forceinline__ void df_mac(float& hi, float& lo, float xh, float xl,
   lo = __fadd_rn(lo, __fadd_rn(t, e));
 }
 
+// (hi, lo) = x * y
+__device__ __forceinline__ void df_mul(float& hi, float& lo, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  float e = __fmaf_rn(xh, yh, -p);
+  e = __fmaf_rn(xh, yl, e);
+  lo = __fmaf_rn(xl, yh, e);
+  hi = p;
+}
+
 __device__ __forceinline__ void df_renorm(float& hi, float& lo) {
   const float s = __fadd_rn(hi, lo);
   lo = __fsub_rn(lo, __fsub_rn(s, hi));
@@ -87,6 +96,11 @@ struct ArithDF {
   static __device__ __forceinline__ void mac(acc& a, const elem& x, const relem& v) {
     df_mac(a.rh, a.rl, x.x, x.y, v.x, v.y);
     df_mac(a.ih, a.il, x.z, x.w, v.x, v.y);
+  }
+  // a = x * v
+  static __device__ __forceinline__ void mul(acc& a, const elem& x, const relem& v) {
+    df_mul(a.rh, a.rl, x.x, x.y, v.x, v.y);
+    df_mul(a.ih, a.il, x.z, x.w, v.x, v.y);
   }
   // a += conj(x) * v
   static __device__ __forceinline__ void mac_cx(acc& a, const elem& x, const relem& v) {
@@ -127,6 +141,10 @@ struct ArithF64 {
   static __device__ __forceinline__ void mac_cx(acc& a, const elem& x, const relem& v) {
     a.x = fma(x.x, v, a.x);
     a.y = fma(-x.y, v, a.y);
+  }
+  static __device__ __forceinline__ void mul(acc& a, const elem& x, const relem& v) {
+    a.x = x.x * v;
+    a.y = x.y * v;
   }
   static __device__ __forceinline__ void renorm(acc&) {}
   typedef double red_t;
@@ -217,6 +235,10 @@ struct CbTmaSmem {
   static constexpr size_t warp_bytes = ((NST * stage_bytes + red_bytes + row_bytes + 8 * NST) + 127) / 128 * 128;
   static constexpr size_t cta_bytes = 4 * warp_bytes;
 };
+
+// slot of (value v, lane j) in the per-warp reduction buffer: rows rotated by v so that the
+// reducing lanes (one value each, all reading entry j of their row) hit distinct banks
+__device__ __forceinline__ int rsw(int v, int j) { return v * 32 + ((j + v) & 31); }
 
 // IMAG: the sums are multiplied by i before they are added (anti-Hermitian pass)
 template <typename A, int NB, int LINES, int NST, int MINB, bool IMAG>
@@ -341,15 +363,15 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
             const int a = l0 + r;
             const V ska = rv[NB2 + a];
             Acc f;
-            A::zero(f);
 #pragma unroll
             for (int j = 0; j < NB2; ++j) {
               const E p1 = st[(r * NB2 + j) * n];
-              A::mac(f, p1, rc[j]);
+              if (j == 0) A::mul(f, p1, rc[j]);
+              else A::mac(f, p1, rc[j]);
               A::mac_cx(rY[j], p1, ska);
             }
-            red[(2 * a) * 32 + lane] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
-            red[(2 * a + 1) * 32 + lane] = IMAG ? A::red_re(f) : A::red_im(f);
+            red[rsw(2 * a, lane)] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
+            red[rsw(2 * a + 1, lane)] = IMAG ? A::red_re(f) : A::red_im(f);
           }
         } else {
           // Q2 columns j: Y'_k[j] = sum_a Q2[a][j] s_c[a];  X'_c[a] += conj(Q2[a][j]) r_k[j]
@@ -358,15 +380,15 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
             const int j = l0 + r;
             const V rkj = rv[j];
             Acc f;
-            A::zero(f);
 #pragma unroll
             for (int a = 0; a < NB2; ++a) {
               const E p2 = st[(r * NB2 + a) * n];
-              A::mac(f, p2, sc[a]);
+              if (a == 0) A::mul(f, p2, sc[a]);
+              else A::mac(f, p2, sc[a]);
               A::mac_cx(rX[a], p2, rkj);
             }
-            red[(2 * NB2 + 2 * j) * 32 + lane] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
-            red[(2 * NB2 + 2 * j + 1) * 32 + lane] = IMAG ? A::red_re(f) : A::red_im(f);
+            red[rsw(2 * NB2 + 2 * j, lane)] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
+            red[rsw(2 * NB2 + 2 * j + 1, lane)] = IMAG ? A::red_re(f) : A::red_im(f);
           }
         }
       }
@@ -377,12 +399,11 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
       if (c + NST < nch) issue(c + NST);
     }
     if (cfail >= 0) break;
-    if (active) {
+    // keep the low parts of the reverse sums small (each took NB2 products in this row block)
 #pragma unroll
-      for (int i = 0; i < NB2; ++i) {
-        A::renorm(rX[i]);
-        A::renorm(rY[i]);
-      }
+    for (int i = 0; i < NB2; ++i) {
+      A::renorm(rX[i]);
+      A::renorm(rY[i]);
     }
     // the row block is complete: forward reduction over the active lanes
     constexpr int LPV = 32 / NV > 0 ? 32 / NV : 1;
@@ -397,7 +418,7 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
         while (m) {
           const int jj = __ffs(m) - 1;
           m &= m - 1;
-          A::red_add(sum, red[v * 32 + part * span + jj]);
+          A::red_add(sum, red[rsw(v, part * span + jj)]);
         }
       }
 #pragma unroll
