@@ -250,7 +250,8 @@ def run_gpu(args, w, rank, world, dist):
     nb = st.cfg.nb
     dev = env_int("LOCAL_RANK", 0)
     g = LindbladGPU(nk=st.cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=w["e"], k1st=st.k1, k2nd=st.k2, P1=w["P1"],
-                    P2=w["P2"], prefac_eph=w["prefac"], picture=0, expt=1, precision=args.precision, device=dev)
+                    P2=w["P2"], prefac_eph=w["prefac"], picture=0, expt=1, precision=args.precision, device=dev,
+                    f_ref=w["f"])
     h = 1.0 * U.fs
     y0 = np.ascontiguousarray(w["dm0"]).view(np.float64).reshape(-1).copy()
     g.set_state(0.0, y0)
@@ -322,7 +323,7 @@ def run_gpu(args, w, rank, world, dist):
     if rank != 0:
         return
     peak, peak_kind = measured_peak()
-    bpl = algorithmic_bytes(nb, st.npair, st.cfg.nk, 16)
+    bpl = algorithmic_bytes(nb, st.npair, st.cfg.nk, ELEM_BYTES[args.precision])
     pair_avg_ms = pair_ms / max(pair_n, 1)
     achieved = bpl / (pair_avg_ms * 1e-3) / 1e9
     tr = profile_traffic(args.precision)
@@ -331,8 +332,10 @@ def run_gpu(args, w, rank, world, dist):
         traffic = tr[0] * st.npair / tr[1]   # the capture's bytes per pair times this workload's pairs
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": {"f64": "f64", "f64x": "f64 (fp32-pair emulated)", "f32": "f32",
-                                           "bf16x2": "bf16x2"}[args.precision],
+            "vs_baseline": None, "dtype": {"f64": "f64", "f64x": "f64 (fp32-pair emulated)",
+                                           "f32": "f32 (P complex64, rho as deviation from f)",
+                                           "bf16x2": "bf16 hi+lo (P 8 B/complex, rho as deviation from f)"
+                                           }[args.precision],
             "data": "synthetic", "config": config_of(w, {"precision": args.precision}),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
@@ -342,9 +345,60 @@ def run_gpu(args, w, rank, world, dist):
                                    "finish": fin_ms / max(fin_n, 1) * 4},
             "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
             "gen_seconds": w["gen_s"]}
+    if args.t1 and args.precision != "f64":
+        line["t1"] = t1_compare(args.precision, args.t1_steps, dev)
     if args.cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline_single(w)
     print(json.dumps(line))
+
+
+ELEM_BYTES = {"f64": 16, "f64x": 16, "f32": 8, "bf16x2": 8}
+
+
+def t1_compare(precision, nsteps, dev):
+    """T1 of the Si-like nk=500 case (RK4 dt = 1 fs, S_z every 100 steps, exponential fit) from this
+    precision and from the plain FP64 GPU path on the same input; the FP64 path itself matches the
+    FP64 reference to 1e-10 (tests). The equilibrium drift of f is subtracted (alg_ddmdteq with
+    f_eq = f) so that f is stationary."""
+    from denmat_dynm_development_gb300.dmd import LindbladGPU
+    from denmat_dynm_development_gb300.t1fit import fit_t1
+    w = build_workload("si_nk500", 1)
+    st = w["st"]
+    nb = st.cfg.nb
+    y0 = np.ascontiguousarray(w["dm0"]).view(np.float64).reshape(-1).copy()
+    idx = np.arange(nb)
+    feq = np.zeros((st.cfg.nk, nb, nb), np.complex128)
+    feq[:, idx, idx] = w["f"]
+    yf = np.ascontiguousarray(feq.reshape(st.cfg.nk, -1)).view(np.float64).reshape(-1).copy()
+    out = {}
+    eq = None
+    t0 = time.perf_counter()
+    for prec in ("f64", precision):
+        g = LindbladGPU(nk=st.cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=w["e"], k1st=st.k1, k2nd=st.k2,
+                        P1=w["P1"], P2=w["P2"], prefac_eph=w["prefac"], picture=0, expt=1, precision=prec, device=dev,
+                        f_ref=w["f"])
+        try:
+            if eq is None:
+                eq = g.evolve_driver(0.0, yf).view(np.complex128).reshape(st.cfg.nk, nb * nb).copy()
+            g.set_ddmdt_eq(eq)
+            g.set_state(0.0, y0)
+            sz = np.ascontiguousarray(st.s[:, 2, :])
+            g.set_observable(0, sz, w["f"], w["ob_prefac"])
+            rec = []
+            for _ in range(nsteps // 100):
+                g.rk4(1.0 * U.fs, 100)
+                t, _ = g.get_state()
+                rec.append((t,) + g.measure(0))
+            out[prec] = np.array(rec)
+        finally:
+            g.close()
+    a, b = out["f64"], out[precision]
+    fa, fb = fit_t1(a[:, 0], a[:, 1]), fit_t1(b[:, 0], b[:, 1])
+    return {"workload": "si_nk500: nb=2, nk=500, %d k-pairs, RK4 dt=1 fs, %d steps, S_z every 100 steps, "
+                        "drift of f subtracted" % (st.npair, nsteps),
+            "tau_ps_f64": fa.tau_lsq, "tau_ps": fb.tau_lsq, "rel_err": abs(fb.tau_lsq - fa.tau_lsq) / abs(fa.tau_lsq),
+            "s_rel_err": float(np.abs(b[:, 1] - a[:, 1]).max() / np.abs(a[:, 1]).max()),
+            "s_ratio_end": float(a[-1, 1] / a[0, 1]), "seconds": time.perf_counter() - t0}
 
 
 def main():
@@ -357,6 +411,8 @@ def main():
     ap.add_argument("--precision", default="f64x", choices=["f64", "f64x", "f32", "bf16x2"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-t1", dest="t1", action="store_false")
+    ap.add_argument("--t1-steps", type=int, default=10000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)

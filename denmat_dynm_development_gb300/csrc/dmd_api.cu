@@ -38,6 +38,8 @@ struct dmd_handle {
   long long nrb = 0;
   unsigned int* d_err = nullptr;  // device error flags (bounded waits)
   unsigned int* d_hflag = nullptr;  // set by the prep kernel when a state is not exactly Hermitian
+  double2* d_acc0 = nullptr;   // deviation form: contraction of diag(f_ref), position order [nk][2][nb2]
+  double* d_fref = nullptr;    // deviation form: window occupations [nk][nb]
   double2* d_H = nullptr;      // [nk][nbdm^2]
   double2* d_eq = nullptr;     // [nk][nb2]
   double2* d_rs = nullptr;     // [nk][2][nb2] (per-thread form); Hermitian + anti-Hermitian coordinates (column-block form)
@@ -107,6 +109,11 @@ int dalloc(dmd_handle* h, T** p, size_t n) {
 
 inline unsigned blocks_for(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
 
+// bytes of one stored Q element per arithmetic
+int elem_bytes(int prec) { return (prec == DMD_PREC_F32 || prec == DMD_PREC_BF16X2) ? 8 : 16; }
+// the reduced-precision forms contract rho - diag(f_ref) only
+bool deviation_form(int prec) { return prec == DMD_PREC_F32 || prec == DMD_PREC_BF16X2; }
+
 cudaEvent_t pool_event(dmd_handle* h) {
   if (!h->ev_pool.empty()) {
     cudaEvent_t e = h->ev_pool.back();
@@ -162,11 +169,15 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
   if (!h->use_cb) {
     k_prep<NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->expt, h->d_rs, h->d_acc);
   } else if (h->prec == DMD_PREC_F64X) {
-    k_prep_herm<ArithDF, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta,
-                                                                      h->expt, (float2*)h->d_rs, h->d_acc, h->d_hflag);
+    k_prep_herm<ArithDF, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(
+        h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt, (float2*)h->d_rs, h->d_acc, h->d_hflag, nullptr, nullptr);
+  } else if (deviation_form(h->prec)) {
+    k_prep_herm<ArithF32, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(
+        h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt, (float*)h->d_rs, h->d_acc, h->d_hflag, h->d_fref,
+        h->d_acc0);
   } else {
-    k_prep_herm<ArithF64, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta,
-                                                                       h->expt, (double*)h->d_rs, h->d_acc, h->d_hflag);
+    k_prep_herm<ArithF64, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(
+        h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt, (double*)h->d_rs, h->d_acc, h->d_hflag, nullptr, nullptr);
   }
   h->launches++;
   CKL();
@@ -216,6 +227,10 @@ int launch_pairs(dmd_handle* h) {
           case 4: herm_pair_launches<ArithDF, 1, 6, 3>(h, rs, half); break;
           default: herm_pair_launches<ArithDF, 2, 2, 4>(h, rs, half); break;
         }
+      } else if (h->prec == DMD_PREC_F32) {
+        herm_pair_launches<ArithF32, 4, 2, 5>(h, (const float*)h->d_rs, half);
+      } else if (h->prec == DMD_PREC_BF16X2) {
+        herm_pair_launches<ArithBF2, 4, 2, 5>(h, (const float*)h->d_rs, half);
       } else {
         herm_pair_launches<ArithF64, 2, 2, 4>(h, (const double*)h->d_rs, half);
       }
@@ -395,6 +410,68 @@ void herm_transform(int nb, const cd* P1, const cd* P2, cd* Q1, cd* Q2) {
   }
 }
 
+uint32_t bf16_bits(float x) {  // round to nearest even (finite values)
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return u >> 16;
+}
+float bf16_value(uint32_t b) {
+  const uint32_t u = b << 16;
+  float x;
+  memcpy(&x, &u, 4);
+  return x;
+}
+// one 32-bit word: bf16(x) in the upper half, bf16(x - that) in the lower half
+uint32_t pack_bf2(double x) {
+  const float xf = (float)x;
+  const uint32_t hi = bf16_bits(xf);
+  const uint32_t lo = bf16_bits((float)(x - (double)bf16_value(hi)));
+  return (hi << 16) | lo;
+}
+
+void pack_elem(int prec, cd v, unsigned char* out) {
+  if (prec == DMD_PREC_F64X) {
+    const float xh = (float)v.re, yh = (float)v.im;
+    const float f[4] = {xh, (float)(v.re - (double)xh), yh, (float)(v.im - (double)yh)};
+    memcpy(out, f, 16);
+  } else if (prec == DMD_PREC_F32) {
+    const float f[2] = {(float)v.re, (float)v.im};
+    memcpy(out, f, 8);
+  } else if (prec == DMD_PREC_BF16X2) {
+    const uint32_t w[2] = {pack_bf2(v.re), pack_bf2(v.im)};
+    memcpy(out, w, 8);
+  } else {
+    const double f[2] = {v.re, v.im};
+    memcpy(out, f, 16);
+  }
+}
+
+// Contribution of r_f = coords(diag f), s_f = coords(diag(1 - f)) through one stored pair to the
+// transformed sums (the kernel's four products, dmd_pairs_cb.cuh): X'_row += Q1 r_f(col),
+// Y'_row += Q2^T s_f(col) and, with the reverse term, Y'_col += Q1^H s_f(row), X'_col += conj(Q2) r_f(row).
+// a_row, a_col: [2][nb2] (X' then Y') of the row and column k-points.
+void fold_reference(int nb, const cd* Q1, const cd* Q2, const double* f_row, const double* f_col, bool rev,
+                    cd* a_row, cd* a_col) {
+  const int n2 = nb * nb;
+  for (int a = 0; a < n2; ++a)
+    for (int i = 0; i < nb; ++i) {
+      const int ii = i * nb + i;
+      const cd q1 = Q1[a * n2 + ii], q2 = Q2[ii * n2 + a];
+      a_row[a].re += q1.re * f_col[i];
+      a_row[a].im += q1.im * f_col[i];
+      a_row[n2 + a].re += q2.re * (1 - f_col[i]);
+      a_row[n2 + a].im += q2.im * (1 - f_col[i]);
+      if (rev) {
+        const cd q1c = Q1[ii * n2 + a], q2c = Q2[a * n2 + ii];
+        a_col[n2 + a].re += q1c.re * (1 - f_row[i]);
+        a_col[n2 + a].im -= q1c.im * (1 - f_row[i]);
+        a_col[a].re += q2c.re * f_row[i];
+        a_col[a].im -= q2c.im * f_row[i];
+      }
+    }
+}
+
 // column-block layout upload: pairs permuted into row blocks, element-major inside each block,
 // folded with the optional additive operators and converted to the arithmetic's element format
 int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
@@ -411,7 +488,8 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
   if (const char* v = getenv("DMD_PAIR_CFG")) h->pcfg = atoi(v);
   cudaError_t (*const attrs[])() = {herm_pair_attrs<ArithDF, 2, 2, 4>, herm_pair_attrs<ArithDF, 2, 3, 3>,
                                     herm_pair_attrs<ArithDF, 1, 4, 4>, herm_pair_attrs<ArithDF, 1, 3, 4>,
-                                    herm_pair_attrs<ArithDF, 1, 6, 3>, herm_pair_attrs<ArithF64, 2, 2, 4>};
+                                    herm_pair_attrs<ArithDF, 1, 6, 3>, herm_pair_attrs<ArithF64, 2, 2, 4>,
+                                    herm_pair_attrs<ArithF32, 4, 2, 5>, herm_pair_attrs<ArithBF2, 4, 2, 5>};
   for (auto fn : attrs) CK(fn());
   int rc;
   if ((rc = dalloc(h, &h->d_pos, (size_t)h->nk)) || (rc = dalloc(h, &h->d_rb, L.rb.size())) ||
@@ -420,12 +498,23 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
   CK(cudaMemcpy(h->d_pos, L.pos.data(), L.pos.size() * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_rb, L.rb.data(), L.rb.size() * sizeof(dmd::RowBlock), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_items, L.items.data(), L.items.size() * sizeof(dmd::WorkItem), cudaMemcpyHostToDevice));
-  const bool df = h->prec == DMD_PREC_F64X;
+  const int esz = elem_bytes(h->prec);
   std::vector<cd> Peff[2] = {std::vector<cd>(nb4), std::vector<cd>(nb4)};
   std::vector<cd> Q[2] = {std::vector<cd>(nb4), std::vector<cd>(nb4)};
+  // deviation form: the constant contraction of diag(f_ref), position order [nk][2][nb2]
+  const bool dev = deviation_form(h->prec);
+  std::vector<cd> acc0;
+  std::vector<double> fw;
+  if (dev) {
+    acc0.assign((size_t)h->nk * 2 * h->nb2, cd{0, 0});
+    fw.assign((size_t)h->nk * nb, 0.0);
+    if (d->f_ref)
+      for (int k = 0; k < h->nk; ++k)
+        for (int b = 0; b < nb; ++b) fw[(size_t)k * nb + b] = d->f_ref[(size_t)k * h->nbdm + h->bs + b];
+  }
   const size_t chunk_rb = 1 << 14;  // row blocks per staging chunk
-  double2* stage = nullptr;
-  CK(cudaMallocHost((void**)&stage, chunk_rb * 32 * ne * sizeof(double2)));
+  unsigned char* stage = nullptr;
+  CK(cudaMallocHost((void**)&stage, chunk_rb * 32 * ne * (size_t)esz));
   int out = DMD_OK;
   for (size_t r0 = 0; r0 < L.rb.size() && out == DMD_OK; r0 += chunk_rb) {
     const size_t r1 = std::min(L.rb.size(), r0 + chunk_rb);
@@ -459,6 +548,12 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
             Peff[m][e] = {x, yv};
           }
         herm_transform(h->nb, Peff[0].data(), Peff[1].data(), Q[0].data(), Q[1].data());
+        if (dev) {  // what the kernel would add for diag(f_ref), in FP64 (see k_prep_herm)
+          const uint64_t kr = tr ? d->k2nd[src] : d->k1st[src], kc = tr ? d->k1st[src] : d->k2nd[src];
+          const bool rev = d->k1st[src] < d->k2nd[src];
+          fold_reference(h->nb, Q[0].data(), Q[1].data(), &fw[kr * nb], &fw[kc * nb], rev,
+                         &acc0[(size_t)L.pos[kr] * 2 * h->nb2], &acc0[(size_t)L.pos[kc] * 2 * h->nb2]);
+        }
         for (int e = 0; e < ne; ++e) {
           // stored element e: Q1 row-major for e < nb^4; Q2 column-major after it
           // (e = nb^4 + cc * nb^2 + a holds Q2[a][cc])
@@ -469,22 +564,20 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
             const int q = e - nb4, cc = q / h->nb2, a = q % h->nb2;
             qv = Q[1][a * h->nb2 + cc];
           }
-          double2 v;
-          if (df) {
-            const float xh = (float)qv.re, yh = (float)qv.im;
-            float4 f = make_float4(xh, (float)(qv.re - (double)xh), yh, (float)(qv.im - (double)yh));
-            memcpy(&v, &f, 16);
-          } else {
-            v = make_double2(qv.re, qv.im);
-          }
-          stage[(b0 - q0) * ne + (size_t)e * n + i] = v;
+          pack_elem(h->prec, qv, stage + ((b0 - q0) * ne + (size_t)e * n + i) * esz);
         }
       }
     }
-    cudaError_t e = cudaMemcpy(h->d_P + q0 * ne, stage, (q1 - q0) * ne * sizeof(double2), cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpy((unsigned char*)h->d_P + q0 * ne * esz, stage, (q1 - q0) * ne * esz,
+                               cudaMemcpyHostToDevice);
     if (e != cudaSuccess) out = fail(h, DMD_E_CUDA, std::string("P upload: ") + cudaGetErrorString(e));
   }
   cudaFreeHost(stage);
+  if (out == DMD_OK && dev) {
+    if ((out = dalloc(h, &h->d_acc0, acc0.size())) || (out = dalloc(h, &h->d_fref, fw.size()))) return out;
+    CK(cudaMemcpy(h->d_acc0, acc0.data(), acc0.size() * 16, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_fref, fw.data(), fw.size() * 8, cudaMemcpyHostToDevice));
+  }
   return out;
 }
 
@@ -494,7 +587,7 @@ void release(dmd_handle* h) {
   if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
   void* ptrs[] = {h->d_err, h->d_pos, h->d_rb, h->d_items, h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
-                  h->d_coef, h->d_flag, h->d_hflag};
+                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -551,8 +644,9 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
     return DMD_E_ARG;
   if (d->nkpair > 0 && (!d->k1st || !d->k2nd || !d->P1 || !d->P2)) return DMD_E_ARG;
   if ((d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
-  if (d->precision != DMD_PREC_F64 && d->precision != DMD_PREC_F64X) return DMD_E_ARG;
-  if (d->precision == DMD_PREC_F64X && d->bend - d->bstart != 2) return DMD_E_ARG;
+  if (d->precision < DMD_PREC_F64 || d->precision > DMD_PREC_BF16X2) return DMD_E_ARG;
+  // the FP32-pair and reduced-precision forms exist for the nb = 2 column-block contraction
+  if (d->precision != DMD_PREC_F64 && (d->bend - d->bstart != 2 || d->nkpair == 0)) return DMD_E_ARG;
   if (d->picture != DMD_PICTURE_INTERACTION && d->picture != DMD_PICTURE_SCHRODINGER) return DMD_E_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DMD_E_NODEV;
@@ -585,7 +679,7 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   const size_t nk = h->nk, nbdm = h->nbdm;
   if ((rc = dalloc(h, &h->d_ew, nk * h->nb)) || (rc = dalloc(h, &h->d_edm, nk * nbdm)) ||
       (rc = dalloc(h, &h->d_kk, (h->nb == 2) ? 1 : (size_t)h->npair)) ||
-      (rc = dalloc(h, &h->d_P, (size_t)h->npair * 2 * h->nb4)) ||
+      (rc = dalloc(h, &h->d_P, ((size_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) + 15) / 16)) ||
       (rc = dalloc(h, &h->d_rs, nk * 2 * h->nb2)) || (rc = dalloc(h, &h->d_acc, nk * 2 * h->nb2)) ||
       (rc = dalloc(h, &h->d_y, h->nstate)) || (rc = dalloc(h, &h->d_ytmp, h->nstate)) ||
       (rc = dalloc(h, &h->d_y0, h->nstate)) || (rc = dalloc(h, &h->d_in, h->nstate)) ||

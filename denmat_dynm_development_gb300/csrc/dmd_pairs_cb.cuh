@@ -160,23 +160,75 @@ struct ArithF64 {
   static __device__ __forceinline__ relem from_double(double v) { return v; }
 };
 
+// Reduced-precision forms: Q stored complex64 (ArithF32) or as bf16 hi + bf16 lo per component
+// (ArithBF2, one 32-bit word per component: hi in the upper half, lo in the lower), FP32 products
+// and sums, FP64 atomics. They contract only rho - diag(f_ref) (see k_prep_herm).
+struct ArithF32 {
+  typedef float2 elem;
+  typedef float relem;
+  typedef float2 acc;
+  static __device__ __forceinline__ float2 val(const elem& x) { return x; }
+  static __device__ __forceinline__ void zero(acc& a) { a.x = a.y = 0.f; }
+  static __device__ __forceinline__ void mac(acc& a, const elem& x, const relem& v) {
+    a.x = __fmaf_rn(x.x, v, a.x);
+    a.y = __fmaf_rn(x.y, v, a.y);
+  }
+  static __device__ __forceinline__ void mac_cx(acc& a, const elem& x, const relem& v) {
+    a.x = __fmaf_rn(x.x, v, a.x);
+    a.y = __fmaf_rn(-x.y, v, a.y);
+  }
+  static __device__ __forceinline__ void mul(acc& a, const elem& x, const relem& v) {
+    a.x = __fmul_rn(x.x, v);
+    a.y = __fmul_rn(x.y, v);
+  }
+  static __device__ __forceinline__ void renorm(acc&) {}
+  typedef float red_t;
+  static __device__ __forceinline__ float red_re(const acc& a) { return a.x; }
+  static __device__ __forceinline__ float red_im(const acc& a) { return a.y; }
+  static __device__ __forceinline__ float red_neg(float v) { return -v; }
+  static __device__ __forceinline__ float red_zero() { return 0.f; }
+  static __device__ __forceinline__ void red_add(float& s, float b) { s = __fadd_rn(s, b); }
+  static __device__ __forceinline__ float red_shfl_xor(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+  static __device__ __forceinline__ double red_to_double(float v) { return (double)v; }
+  static __device__ __forceinline__ double re_d(const acc& a) { return (double)a.x; }
+  static __device__ __forceinline__ double im_d(const acc& a) { return (double)a.y; }
+  static __device__ __forceinline__ relem from_double(double v) { return __double2float_rn(v); }
+};
+
+__device__ __forceinline__ float bf2_to_float(uint32_t w) {
+  return __fadd_rn(__uint_as_float(w & 0xffff0000u), __uint_as_float(w << 16));
+}
+
+struct ArithBF2 : ArithF32 {
+  typedef uint2 elem;
+  static __device__ __forceinline__ float2 val(const elem& x) { return make_float2(bf2_to_float(x.x), bf2_to_float(x.y)); }
+  static __device__ __forceinline__ void mac(acc& a, const elem& x, const relem& v) { ArithF32::mac(a, val(x), v); }
+  static __device__ __forceinline__ void mac_cx(acc& a, const elem& x, const relem& v) { ArithF32::mac_cx(a, val(x), v); }
+  static __device__ __forceinline__ void mul(acc& a, const elem& x, const relem& v) { ArithF32::mul(a, val(x), v); }
+};
+
 // ---------------------------------------------------------------------------------------------
-// Prep: Hermitian and anti-Hermitian coordinates of rt, st per k (written at pos[k]), zeroed
-// accumulators. One thread per (k, element (i, j)); the thread of (i, j) with i < j writes the
-// coordinates at (i, j) and (j, i). Raises *hflag when some rho_k is not exactly Hermitian.
-// rs layout: [nk][2][NB2] Hermitian part (r, s), then [nk][2][NB2] anti-Hermitian part.
+// Prep: Hermitian and anti-Hermitian coordinates of rt, st per k (written at pos[k]) and the
+// accumulators' start values (zero, or acc0). One thread per (k, element (i, j)); the thread of
+// (i, j) with i < j writes the coordinates at (i, j) and (j, i). Raises *hflag when some rho_k is
+// not exactly Hermitian. rs layout: [nk][2][NB2] Hermitian part (r, s), then the anti-Hermitian part.
+// Deviation form (fref != null, window occupations [nk][NB]): the coordinates are those of
+// rho - diag(f) and of (1 - rho) - diag(1 - f) = -(rho - diag(f)); the contraction of diag(f) is
+// the constant acc0 (position order), formed once in FP64.
 // ---------------------------------------------------------------------------------------------
 template <typename A, int NB>
 __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict__ y, const double* __restrict__ ew,
                             const int* __restrict__ pos, TimeArg ta, int phase, typename A::relem* __restrict__ rs,
-                            double2* __restrict__ acc, unsigned int* __restrict__ hflag) {
+                            double2* __restrict__ acc, unsigned int* __restrict__ hflag,
+                            const double* __restrict__ fref, const double2* __restrict__ acc0) {
   constexpr int NB2 = NB * NB;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nk * NB2) return;
   const int k = idx / NB2, ab = idx - k * NB2, i = ab / NB, j = ab - i * NB;
   const int p = pos[k];
-  acc[(size_t)p * 2 * NB2 + ab] = mk2(0.0, 0.0);
-  acc[(size_t)p * 2 * NB2 + NB2 + ab] = mk2(0.0, 0.0);
+  const size_t ax = (size_t)p * 2 * NB2 + ab;
+  acc[ax] = acc0 ? acc0[ax] : mk2(0.0, 0.0);
+  acc[ax + NB2] = acc0 ? acc0[ax + NB2] : mk2(0.0, 0.0);
   if (i > j) return;
   typename A::relem* rh = rs + (size_t)p * 2 * NB2;
   typename A::relem* ra = rs + (size_t)nk * 2 * NB2 + (size_t)p * 2 * NB2;
@@ -184,8 +236,14 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
   const double2 vij = yk[(bs + i) * nbdm + bs + j];
   if (i == j) {
     // H_ii = Re rho_ii, A_ii = Im rho_ii; 1 - rho: (1 - Re rho_ii, -Im rho_ii) (set_oneminusdm)
-    rh[ab] = A::from_double(vij.x);
-    rh[NB2 + ab] = A::from_double(1.0 - vij.x);
+    if (fref) {
+      const double dv = __dsub_rn(vij.x, fref[(size_t)k * NB + i]);
+      rh[ab] = A::from_double(dv);
+      rh[NB2 + ab] = A::from_double(-dv);
+    } else {
+      rh[ab] = A::from_double(vij.x);
+      rh[NB2 + ab] = A::from_double(1.0 - vij.x);
+    }
     ra[ab] = A::from_double(vij.y);
     ra[NB2 + ab] = A::from_double(0.0 - vij.y);
     if (vij.y != 0.0) atomicOr(hflag, 1u);

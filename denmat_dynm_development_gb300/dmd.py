@@ -31,7 +31,8 @@ class _Desc(C.Structure):
                 ("nkpair", C.c_int64), ("prefac_eph", C.c_double), ("e_dm", C.c_void_p), ("k1st", C.c_void_p),
                 ("k2nd", C.c_void_p), ("P1", C.c_void_p), ("P2", C.c_void_p), ("P1_add", C.c_void_p),
                 ("P2_add", C.c_void_p), ("add_scale", C.c_double), ("Hcoh", C.c_void_p), ("picture", C.c_int32),
-                ("expt", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32)]
+                ("expt", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32),
+                ("f_ref", C.c_void_p)]
 
 
 _L = None
@@ -89,11 +90,12 @@ class LindbladGPU:
     """Device-resident Lindblad RHS for one set of k-pair operators."""
 
     def __init__(self, *, nk, nb_dm, bstart, bend, e_dm, k1st, k2nd, P1, P2, prefac_eph, Hcoh=None,
-                 picture="interaction", expt=1, precision="f64", P1_add=None, P2_add=None, add_scale=0.0, device=0):
+                 picture="interaction", expt=1, precision="f64", P1_add=None, P2_add=None, add_scale=0.0, device=0,
+                 f_ref=None):
         L = _lib()
         self._keep = dict(e=_c(e_dm, np.float64), k1=_c(k1st, np.uint64), k2=_c(k2nd, np.uint64),
                           P1=_c(P1, np.complex128), P2=_c(P2, np.complex128), H=_c(Hcoh, np.complex128),
-                          A1=_c(P1_add, np.complex128), A2=_c(P2_add, np.complex128))
+                          A1=_c(P1_add, np.complex128), A2=_c(P2_add, np.complex128), f=_c(f_ref, np.float64))
         k = self._keep
         ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
         desc = _Desc(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, nkpair=int(k["k1"].size), prefac_eph=prefac_eph,
@@ -101,7 +103,7 @@ class LindbladGPU:
                      P1_add=ptr(k["A1"]), P2_add=ptr(k["A2"]), add_scale=add_scale, Hcoh=ptr(k["H"]),
                      picture=PICTURE[picture] if isinstance(picture, str) else int(picture), expt=int(expt),
                      precision=PREC[precision] if isinstance(precision, str) else int(precision), device=device,
-                     flags=0)
+                     flags=0, f_ref=ptr(k["f"]))
         h = C.c_void_p()
         st = L.dmd_create(C.byref(desc), C.byref(h))
         if st != 0:

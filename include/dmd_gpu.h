@@ -49,8 +49,9 @@ extern "C" {
 /* arithmetic of the k-pair contraction */
 #define DMD_PREC_F64 0     /* P complex128, native FP64 multiply-adds */
 #define DMD_PREC_F64X 1    /* P and rho as (hi, lo) FP32 pairs: ~2^-46 products, double-FP32 sums */
-#define DMD_PREC_F32 2     /* P stored complex64, FP32 products, FP64 per-k sums */
-#define DMD_PREC_BF16X2 3  /* P stored as bf16 hi + bf16 lo per component, FP32 products */
+#define DMD_PREC_F32 2     /* P stored complex64, FP32 products; rho enters as its deviation from f_ref */
+#define DMD_PREC_BF16X2 3  /* P stored as bf16 hi + bf16 lo per component (8 bytes per complex), FP32
+                              products; rho enters as its deviation from f_ref */
 
 /* pictures (alg.picture) */
 #define DMD_PICTURE_INTERACTION 0
@@ -78,6 +79,9 @@ typedef struct dmd_desc {
   int32_t precision;     /* DMD_PREC_* */
   int32_t device;        /* CUDA device ordinal */
   uint32_t flags;        /* reserved, 0 */
+  const double* f_ref;   /* optional [nk][nb_dm] reference occupations (e.g. f_dm) of the reduced-
+                            precision forms: the contraction of diag(f_ref) is formed once in FP64 at
+                            dmd_create and each evaluation contracts only rho - diag(f_ref) in FP32 */
 } dmd_desc;
 
 int dmd_create(const dmd_desc* desc, dmd_handle** out);

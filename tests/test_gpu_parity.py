@@ -262,3 +262,67 @@ def test_non_hermitian_state_vs_oracle(prec, oracle, built):
         for y in (y_nh, y_h, y_nh):
             err = rel(gpu.func(t, y), oracle.rhs(s, t, y))
             assert err < RHS_TOL[prec], err
+
+
+# Reduced-precision forms (P stored FP32 or bf16 hi+lo, FP32 products): rho enters as its deviation
+# from f_ref = f_dm, the contraction of diag(f_ref) is formed once in FP64. Tolerances, normwise
+# relative to the oracle's RHS: FP32 storage 1e-6, bf16 hi+lo (16 significant bits) 1e-5; the fitted
+# T1 within 1e-4 relative of the FP64 oracle (the target of the reduced-precision forms).
+LOWP_TOL = {"f32": 1e-6, "bf16x2": 1e-5}
+
+
+def make_gpu_lowp(s, prec, with_ref=True):
+    from denmat_dynm_development_gb300.dmd import LindbladGPU
+    g = LindbladGPU(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
+                    P1=s.P1, P2=s.P2, prefac_eph=s.prefac_eph, Hcoh=s.Hcoh, picture=s.picture_schrodinger,
+                    expt=s.expt, precision=prec, f_ref=s.f_dm if with_ref else None)
+    if getattr(s, "ddmdt_eq", None) is not None:
+        g.set_ddmdt_eq(s.ddmdt_eq)
+    return g
+
+
+@pytest.mark.parametrize("prec", ["f32", "bf16x2"])
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_window", "nb2_carrier_eq"])
+def test_lowp_rhs_vs_golden(case, prec, oracle, built):
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = oracle.load(d)
+    with make_gpu_lowp(s, prec) as gpu:
+        for i, t in enumerate(g["rhs_t"]):
+            e = rel(gpu.func(t, g["rhs_y"][i]), g["rhs_dydt"][i])
+            print("%s %s t=%g rel err %.3g" % (case, prec, t, e))
+            assert e < LOWP_TOL[prec]
+
+
+def test_lowp_without_reference_occupations(oracle, built):
+    """f_ref omitted: the deviation is taken from zero occupations (still correct, less accurate)."""
+    d = os.path.join(GOLDEN, "nb2_eimp_B")
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = oracle.load(d)
+    with make_gpu_lowp(s, "f32", with_ref=False) as gpu:
+        e = rel(gpu.func(g["rhs_t"][1], g["rhs_y"][1]), g["rhs_dydt"][1])
+        print("f32 without f_ref: rel err %.3g" % e)
+        assert e < 1e-3
+
+
+@pytest.mark.parametrize("prec", ["f32", "bf16x2"])
+def test_lowp_t1_vs_oracle(prec, oracle, built):
+    from denmat_dynm_development_gb300.t1fit import fit_t1
+    s = oracle.load(os.path.join(GOLDEN, "nb2_carrier_eq"))
+    h, nsteps, every = 2.0 * oracle.fs, 1500, 50
+    y0 = oracle.y_of(s.dm0)
+    _, rec_o = oracle.rk4(s, s.t0, h, nsteps, y0, every=every)
+    with make_gpu_lowp(s, prec) as gpu:
+        gpu.set_state(s.t0, y0)
+        gpu.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+        rec = []
+        for _ in range(nsteps // every):
+            gpu.rk4(h, every)
+            t, _ = gpu.get_state()
+            rec.append((t,) + gpu.measure(0, s.nv_dm))
+    rec = np.array(rec)
+    es = rel(rec[:, 1], rec_o[:, 1])
+    fo, fg = fit_t1(rec_o[:, 0], rec_o[:, 1]), fit_t1(rec[:, 0], rec[:, 1])
+    et = abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq)
+    print("%s: S(t) rel err %.3g, T1 %.10g vs %.10g ps, rel err %.3g" % (prec, es, fg.tau_lsq, fo.tau_lsq, et))
+    assert et < 1e-4
