@@ -185,24 +185,25 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
 }
 
 // the Hermitian pass and the gated anti-Hermitian pass of the nb = 2 contraction
-template <typename A, int L, int NST, int MB>
+template <typename A, int NB, int L, int NST, int MB>
 void herm_pair_launches(dmd_handle* h, const typename A::relem* rs, size_t half) {
-  typedef CbTmaSmem<A, 2, L, NST> S;
+  typedef CbTmaSmem<A, NB, L, NST> S;
   const unsigned g = blocks_for(h->nitems, 4);
-  k_pairs_herm<A, 2, L, NST, MB, false><<<g, 128, S::cta_bytes, h->st>>>(
+  k_pairs_herm<A, NB, L, NST, MB, false><<<g, 128, S::cta_bytes, h->st>>>(
       h->d_items, h->nitems, h->d_rb, (const typename A::elem*)h->d_P, rs, (double*)h->d_acc, h->nk, nullptr, h->d_err);
-  k_pairs_herm<A, 2, L, NST, MB, true><<<g, 128, S::cta_bytes, h->st>>>(
+  k_pairs_herm<A, NB, L, NST, MB, true><<<g, 128, S::cta_bytes, h->st>>>(
       h->d_items, h->nitems, h->d_rb, (const typename A::elem*)h->d_P, rs + half, (double*)h->d_acc, h->nk,
       h->d_hflag, h->d_err);
 }
 
-template <typename A, int L, int NST, int MB>
+template <typename A, int NB, int L, int NST, int MB>
 cudaError_t herm_pair_attrs() {
-  const int bytes = (int)CbTmaSmem<A, 2, L, NST>::cta_bytes;
+  const int bytes = (int)CbTmaSmem<A, NB, L, NST>::cta_bytes;
   cudaError_t e =
-      cudaFuncSetAttribute(k_pairs_herm<A, 2, L, NST, MB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      cudaFuncSetAttribute(k_pairs_herm<A, NB, L, NST, MB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_pairs_herm<A, 2, L, NST, MB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    e = cudaFuncSetAttribute(k_pairs_herm<A, NB, L, NST, MB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             bytes);
   return e;
 }
 
@@ -214,25 +215,29 @@ int launch_pairs(dmd_handle* h) {
     const long long nthr = h->npair * 4LL * NB * NB;
     k_pairs_f64_atomic<NB><<<blocks_for(nthr, 256), 256, 0, h->st>>>(h->npair, h->d_kk, h->d_P, h->d_rs, h->d_acc);
   } else {
-    if constexpr (NB == 2) {
+    if constexpr (NB == 2 || NB == 4) {
       // Hermitian coordinates; the second launch carries the anti-Hermitian part of a state that is
       // not exactly Hermitian and returns at once unless the prep kernel raised d_hflag
       const size_t half = (size_t)h->nk * 2 * h->nb2;  // coordinates per part
       if (h->prec == DMD_PREC_F64X) {
         const float2* rs = (const float2*)h->d_rs;
-        switch (h->pcfg) {
-          case 1: herm_pair_launches<ArithDF, 2, 3, 3>(h, rs, half); break;
-          case 2: herm_pair_launches<ArithDF, 1, 4, 4>(h, rs, half); break;
-          case 3: herm_pair_launches<ArithDF, 1, 3, 4>(h, rs, half); break;
-          case 4: herm_pair_launches<ArithDF, 1, 6, 3>(h, rs, half); break;
-          default: herm_pair_launches<ArithDF, 2, 2, 4>(h, rs, half); break;
+        if constexpr (NB == 4) {
+          herm_pair_launches<ArithDF, NB, 2, 2, 4>(h, rs, half);
+        } else {
+          switch (h->pcfg) {
+            case 1: herm_pair_launches<ArithDF, NB, 2, 3, 3>(h, rs, half); break;
+            case 2: herm_pair_launches<ArithDF, NB, 1, 4, 4>(h, rs, half); break;
+            case 3: herm_pair_launches<ArithDF, NB, 1, 3, 4>(h, rs, half); break;
+            case 4: herm_pair_launches<ArithDF, NB, 1, 6, 3>(h, rs, half); break;
+            default: herm_pair_launches<ArithDF, NB, 2, 2, 4>(h, rs, half); break;
+          }
         }
       } else if (h->prec == DMD_PREC_F32) {
-        herm_pair_launches<ArithF32, 4, 2, 5>(h, (const float*)h->d_rs, half);
+        herm_pair_launches<ArithF32, NB, 4, 2, 5>(h, (const float*)h->d_rs, half);
       } else if (h->prec == DMD_PREC_BF16X2) {
-        herm_pair_launches<ArithBF2, 4, 2, 5>(h, (const float*)h->d_rs, half);
+        herm_pair_launches<ArithBF2, NB, 4, 2, 5>(h, (const float*)h->d_rs, half);
       } else {
-        herm_pair_launches<ArithF64, 2, 2, 4>(h, (const double*)h->d_rs, half);
+        herm_pair_launches<ArithF64, NB, 2, 2, 4>(h, (const double*)h->d_rs, half);
       }
       h->launches++;
     }
@@ -480,17 +485,24 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
   for (int k = 0; k < h->nk; ++k)
     for (int b = 0; b < nb; ++b) ew[(size_t)k * nb + b] = d->e_dm[(size_t)k * h->nbdm + h->bs + b];
   dmd::PairLayout L;
-  if (!dmd::build_pair_layout(h->nk, nb, ew.data(), h->npair, d->k1st, d->k2nd, 512, L))
+  const int G = h->nb2 / 4, W = 32 / G;  // lanes per pair, columns per column block
+  if (!dmd::build_pair_layout(h->nk, nb, ew.data(), h->npair, d->k1st, d->k2nd, 512 / G, W, L))
     return fail(h, DMD_E_ARG, "k-pair index out of range");
   h->nitems = (int)L.items.size();
   h->nrb = (long long)L.rb.size();
   // pair-kernel shape (stage lines, resident CTAs per SM); 0 is the default, the others serve tuning
   if (const char* v = getenv("DMD_PAIR_CFG")) h->pcfg = atoi(v);
-  cudaError_t (*const attrs[])() = {herm_pair_attrs<ArithDF, 2, 2, 4>, herm_pair_attrs<ArithDF, 2, 3, 3>,
-                                    herm_pair_attrs<ArithDF, 1, 4, 4>, herm_pair_attrs<ArithDF, 1, 3, 4>,
-                                    herm_pair_attrs<ArithDF, 1, 6, 3>, herm_pair_attrs<ArithF64, 2, 2, 4>,
-                                    herm_pair_attrs<ArithF32, 4, 2, 5>, herm_pair_attrs<ArithBF2, 4, 2, 5>};
-  for (auto fn : attrs) CK(fn());
+  if (nb == 2) {
+    cudaError_t (*const attrs[])() = {
+        herm_pair_attrs<ArithDF, 2, 2, 2, 4>, herm_pair_attrs<ArithDF, 2, 2, 3, 3>, herm_pair_attrs<ArithDF, 2, 1, 4, 4>,
+        herm_pair_attrs<ArithDF, 2, 1, 3, 4>, herm_pair_attrs<ArithDF, 2, 1, 6, 3>, herm_pair_attrs<ArithF64, 2, 2, 2, 4>,
+        herm_pair_attrs<ArithF32, 2, 4, 2, 5>, herm_pair_attrs<ArithBF2, 2, 4, 2, 5>};
+    for (auto fn : attrs) CK(fn());
+  } else {
+    cudaError_t (*const attrs[])() = {herm_pair_attrs<ArithDF, 4, 2, 2, 4>, herm_pair_attrs<ArithF64, 4, 2, 2, 4>,
+                                      herm_pair_attrs<ArithF32, 4, 4, 2, 5>, herm_pair_attrs<ArithBF2, 4, 4, 2, 5>};
+    for (auto fn : attrs) CK(fn());
+  }
   int rc;
   if ((rc = dalloc(h, &h->d_pos, (size_t)h->nk)) || (rc = dalloc(h, &h->d_rb, L.rb.size())) ||
       (rc = dalloc(h, &h->d_items, L.items.size())))
@@ -645,8 +657,9 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   if (d->nkpair > 0 && (!d->k1st || !d->k2nd || !d->P1 || !d->P2)) return DMD_E_ARG;
   if ((d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
   if (d->precision < DMD_PREC_F64 || d->precision > DMD_PREC_BF16X2) return DMD_E_ARG;
-  // the FP32-pair and reduced-precision forms exist for the nb = 2 column-block contraction
-  if (d->precision != DMD_PREC_F64 && (d->bend - d->bstart != 2 || d->nkpair == 0)) return DMD_E_ARG;
+  // the FP32-pair and reduced-precision forms exist for the column-block contraction (nb = 2, 4)
+  const int nbw = d->bend - d->bstart;
+  if (d->precision != DMD_PREC_F64 && ((nbw != 2 && nbw != 4) || d->nkpair == 0)) return DMD_E_ARG;
   if (d->picture != DMD_PICTURE_INTERACTION && d->picture != DMD_PICTURE_SCHRODINGER) return DMD_E_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DMD_E_NODEV;
@@ -678,7 +691,7 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return bail(DMD_E_CUDA);
   const size_t nk = h->nk, nbdm = h->nbdm;
   if ((rc = dalloc(h, &h->d_ew, nk * h->nb)) || (rc = dalloc(h, &h->d_edm, nk * nbdm)) ||
-      (rc = dalloc(h, &h->d_kk, (h->nb == 2) ? 1 : (size_t)h->npair)) ||
+      (rc = dalloc(h, &h->d_kk, (h->nb == 2 || h->nb == 4) ? 1 : (size_t)h->npair)) ||
       (rc = dalloc(h, &h->d_P, ((size_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) + 15) / 16)) ||
       (rc = dalloc(h, &h->d_rs, nk * 2 * h->nb2)) || (rc = dalloc(h, &h->d_acc, nk * 2 * h->nb2)) ||
       (rc = dalloc(h, &h->d_y, h->nstate)) || (rc = dalloc(h, &h->d_ytmp, h->nstate)) ||
@@ -700,7 +713,7 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
     if (cudaMemcpy(h->d_H, d->Hcoh, h->nstate * 16, cudaMemcpyHostToDevice) != cudaSuccess)
       return bail(fail(h, DMD_E_CUDA, "upload H"));
   }
-  h->use_cb = (h->nb == 2 && h->npair > 0) ? 1 : 0;
+  h->use_cb = ((h->nb == 2 || h->nb == 4) && h->npair > 0) ? 1 : 0;
   if ((rc = h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d))) return bail(rc);
   if (cudaMemset(h->d_y, 0, h->nstate * 16) != cudaSuccess || cudaMemset(h->d_step, 0, 8) != cudaSuccess ||
       cudaMemset(h->d_err, 0, sizeof(unsigned int)) != cudaSuccess ||

@@ -7,7 +7,7 @@
 namespace dmd {
 
 bool build_pair_layout(int nk, int nb, const double* e_w, long long npair, const uint64_t* k1, const uint64_t* k2,
-                       int pairs_per_item, PairLayout& L) {
+                       int pairs_per_item, int width, PairLayout& L) {
   // energy ranks
   std::vector<double> eb(nk);
   for (int k = 0; k < nk; ++k) {
@@ -33,7 +33,7 @@ bool build_pair_layout(int nk, int nb, const double* e_w, long long npair, const
     }
     prow[p] = r;
     pcol[p] = c;
-    key[p] = ((uint64_t)(c >> 5) << 37) | ((uint64_t)r << 5) | (uint64_t)(c & 31);  // nk < 2^31
+    key[p] = ((uint64_t)(c / width) << 37) | ((uint64_t)r << 5) | (uint64_t)(c % width);  // nk < 2^31
   }
   std::vector<uint32_t> ord(npair);
   std::iota(ord.begin(), ord.end(), 0u);
@@ -48,7 +48,7 @@ bool build_pair_layout(int nk, int nb, const double* e_w, long long npair, const
   while (q < npair) {
     const uint32_t p = ord[q];
     const int row = prow[p];
-    const int J = pcol[p] >> 5;
+    const int J = pcol[p] / width;
     RowBlock b;
     b.row = row;
     b.mask = 0;
@@ -58,8 +58,8 @@ bool build_pair_layout(int nk, int nb, const double* e_w, long long npair, const
     while (e < npair) {
       const uint32_t pe = ord[e];
       const int c = pcol[pe];
-      if (prow[pe] != row || (c >> 5) != J) break;
-      const uint32_t bit = 1u << (c & 31);
+      if (prow[pe] != row || c / width != J) break;
+      const uint32_t bit = 1u << (c % width);
       if (b.mask & bit) break;  // duplicate pair: next block
       b.mask |= bit;
       if (k1[pe] < k2[pe]) b.revmask |= bit;
@@ -77,12 +77,12 @@ bool build_pair_layout(int nk, int nb, const double* e_w, long long npair, const
   // work items: runs of row blocks of one column block, about pairs_per_item pairs each
   size_t i = 0;
   while (i < L.rb.size()) {
-    const int J = pcol[L.src[L.rb[i].pair0]] >> 5;
+    const int J = pcol[L.src[L.rb[i].pair0]] / width;
     WorkItem w;
     w.J = J;
     w.rb0 = (int32_t)i;
     long long np = 0;
-    while (i < L.rb.size() && (pcol[L.src[L.rb[i].pair0]] >> 5) == J && np < pairs_per_item &&
+    while (i < L.rb.size() && pcol[L.src[L.rb[i].pair0]] / width == J && np < pairs_per_item &&
            (int)(i - w.rb0) < kMaxRowBlocksPerItem) {
       np += __builtin_popcount(L.rb[i].mask);
       ++i;

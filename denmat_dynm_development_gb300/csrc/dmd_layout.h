@@ -2,9 +2,10 @@
 //
 // k-points are ranked by their mean band energy (pos[k]); with the energy-window pair selection of
 // the Lindblad initializer this turns the set of stored pairs into a band around the diagonal of
-// the (pos[k1], pos[k2]) plane. Pairs are grouped by column block J = pos[k2] / 32 and, inside a
-// block, by row pos[k1]: a "row block" holds the pairs of one row whose columns fall in one column
-// block, one per lane slot (lane s <-> column 32 J + s). A row block stores its P1 and P2 elements
+// the (pos[k1], pos[k2]) plane. Pairs are grouped by column block J = pos[k2] / W (W = 32 for nb = 2,
+// 8 for nb = 4, where four lanes share a pair) and, inside a block, by row pos[k1]: a "row block"
+// holds the pairs of one row whose columns fall in one column block, one per slot (slot s <-> column
+// W J + s). A row block stores its P1 and P2 elements
 // element-major ([element][slot]) so that a warp reads each element of all its pairs with one
 // coalesced access. Work items are runs of row blocks of the same column block.
 //
@@ -22,8 +23,8 @@ namespace dmd {
 
 struct RowBlock {
   int32_t row;       // pos of the forward target k1
-  uint32_t mask;     // lanes holding a pair
-  uint32_t revmask;  // lanes whose pair also has the reverse (k' side) term: k1 < k2 as stored
+  uint32_t mask;     // slots holding a pair
+  uint32_t revmask;  // slots whose pair also has the reverse (k' side) term: k1 < k2 as stored
   uint32_t pair0;    // index of the block's first pair in the permuted pair order
 };
 
@@ -45,9 +46,9 @@ struct PairLayout {
   std::vector<uint8_t> transposed;  // permuted pair slot stored as (k2, k1) with (conj P2, conj P1)
 };
 
-// Builds the layout from the stored pairs. e_w is [nk][nb] (window energies). Returns false on an
-// out-of-range pair index.
+// Builds the layout from the stored pairs. e_w is [nk][nb] (window energies), width the columns per
+// column block (<= 32). Returns false on an out-of-range pair index.
 bool build_pair_layout(int nk, int nb, const double* e_w, long long npair, const uint64_t* k1, const uint64_t* k2,
-                       int pairs_per_item, PairLayout& L);
+                       int pairs_per_item, int width, PairLayout& L);
 
 }  // namespace dmd

@@ -274,24 +274,31 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
 
 // ---------------------------------------------------------------------------------------------
 // The contraction. P2 is stored column-major, so both halves of a pair are consumed "line by
-// line": a Q1 row a completes X'_k[a] and a Q2 column j completes Y'_k[j], while the lane's reverse
-// sums Y'_c (indexed by Q1's column) and X'_c (indexed by Q2's row) stay in registers with
-// compile-time indices. A row block is consumed in chunks of LINES lines that stream through a
-// per-warp ring of NST stages: the copy of chunk i + NST is issued as soon as chunk i has been
-// read. Lane r holds the descriptor of the item's row block r (items have at most 32), so issuing
-// a copy needs no memory access; the next row's coordinates are fetched one row block ahead.
-// Waits are bounded (dmd_tma.cuh); a timeout sets *errflag.
+// line": a Q1 row a gives X'_k[a] and a Q2 column j gives Y'_k[j], while the reverse sums Y'_c
+// (indexed by Q1's column) and X'_c (indexed by Q2's row) stay in registers with compile-time
+// indices. G = nb^2 / 4 lanes share a pair (1 for nb = 2, 4 for nb = 4): lane (g, s) owns slot s of
+// the row block (column W J + s, W = 32 / G) and the quarter [4g, 4g + 4) of every line, so each lane
+// handles 4 elements per line and holds 4 coordinates and 8 reverse sums whatever nb is. A row
+// block is consumed in chunks of LINES lines that stream through a per-warp ring of NST stages: the
+// copy of chunk i + NST is issued as soon as chunk i has been read. Lane r holds the descriptor of
+// the item's row block r (items have at most 32), so issuing a copy needs no memory access; the next
+// row's coordinates are fetched one row block ahead. The forward partials of every 8 lines are
+// reduced over the warp through a shared buffer and added with 16 FP64 atomics. Waits are bounded
+// (dmd_tma.cuh); a timeout sets *errflag.
 // ---------------------------------------------------------------------------------------------
 template <typename A, int NB, int LINES, int NST>
 struct CbTmaSmem {
-  static constexpr int NB2 = NB * NB, NB4 = NB2 * NB2, NV = 4 * NB2;
-  static constexpr int CPM = NB2 / LINES;  // chunks per matrix
-  static constexpr int CPR = 2 * CPM;      // chunks per row block
-  static constexpr size_t stage_bytes = (size_t)LINES * NB2 * 32 * sizeof(typename A::elem);
+  static constexpr int NB2 = NB * NB, NB4 = NB2 * NB2;
+  static constexpr int G = NB2 / 4, W = 32 / G;  // lanes per pair, slots (columns) per row block
+  static constexpr int FL = 8, NV = 2 * FL;      // lines per forward flush, reals per flush
+  static constexpr int CPM = NB2 / LINES;        // chunks per matrix
+  static constexpr int CPR = 2 * CPM;            // chunks per row block
+  static constexpr size_t stage_bytes = (size_t)LINES * NB2 * W * sizeof(typename A::elem);
   static constexpr size_t red_bytes = (size_t)NV * 32 * sizeof(typename A::red_t);
   static constexpr size_t row_bytes = (size_t)4 * NB2 * sizeof(typename A::relem);  // r_k, s_k, zeros
   static constexpr size_t warp_bytes = ((NST * stage_bytes + red_bytes + row_bytes + 8 * NST) + 127) / 128 * 128;
   static constexpr size_t cta_bytes = 4 * warp_bytes;
+  static_assert(NB2 % 4 == 0 && (2 * NB2) % FL == 0 && FL % LINES == 0, "shape");
 };
 
 // slot of (value v, lane j) in the per-warp reduction buffer: rows rotated by v so that the
@@ -308,7 +315,8 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
                                                           const unsigned int* __restrict__ gate,
                                                           unsigned int* __restrict__ errflag) {
   typedef CbTmaSmem<A, NB, LINES, NST> S;
-  constexpr int NB2 = S::NB2, NB4 = S::NB4, NV = S::NV, CPM = S::CPM, CPR = S::CPR;
+  constexpr int NB2 = S::NB2, NB4 = S::NB4, G = S::G, W = S::W, FL = S::FL, NV = S::NV;
+  constexpr int CPM = S::CPM, CPR = S::CPR;
   constexpr size_t SE = S::stage_bytes / sizeof(typename A::elem);  // elements per stage
   constexpr unsigned FULL = 0xffffffffu;
   typedef typename A::elem E;
@@ -321,6 +329,8 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
   const int lane = threadIdx.x & 31;
   const int item = blockIdx.x * 4 + wib;
   if (item >= nitems) return;
+  const int qg = lane / W, sl = lane % W;  // quarter, slot
+  const int q4 = 4 * qg;
   unsigned char* wbase = smem_raw + (size_t)wib * S::warp_bytes;
   E* const stage0 = (E*)wbase;
   R* const red = (R*)(wbase + NST * S::stage_bytes);                  // [NV][32]
@@ -361,17 +371,17 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
   for (int c = 0; c < NST; ++c)
     if (c < nch) issue(c);
   if (lane < 2 * NB2) rowv[2 * NB2 + lane] = V();
-  const int col = w.J * 32 + lane;
+  const int col = w.J * W + sl;
   const bool colok = col < nk;
-  V rc[NB2], sc[NB2];
+  V rc[4], sc[4];  // r_col, s_col on this lane's quarter
 #pragma unroll
-  for (int i = 0; i < NB2; ++i) {
-    rc[i] = colok ? rs[(size_t)col * 2 * NB2 + i] : V();
-    sc[i] = colok ? rs[(size_t)col * 2 * NB2 + NB2 + i] : V();
+  for (int i = 0; i < 4; ++i) {
+    rc[i] = colok ? rs[(size_t)col * 2 * NB2 + q4 + i] : V();
+    sc[i] = colok ? rs[(size_t)col * 2 * NB2 + NB2 + q4 + i] : V();
   }
-  Acc rX[NB2], rY[NB2];
+  Acc rX[4], rY[4];
 #pragma unroll
-  for (int i = 0; i < NB2; ++i) {
+  for (int i = 0; i < 4; ++i) {
     A::zero(rX[i]);
     A::zero(rY[i]);
   }
@@ -383,20 +393,23 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
   }
   bool any_rev = false;
   int cfail = -1;
-  const unsigned lt = (1u << lane) - 1u;
+  const unsigned lt = (1u << sl) - 1u;
 #pragma unroll 1
   for (int rbi = 0; rbi < nrb; ++rbi) {
     const int brow = __shfl_sync(FULL, mine.row, rbi);
     const unsigned bmask = __shfl_sync(FULL, mine.mask, rbi);
     const unsigned brev = __shfl_sync(FULL, mine.revmask, rbi);
     const int nrow = __shfl_sync(FULL, mine.row, rbi + 1 < nrb ? rbi + 1 : rbi);
-    const bool active = (bmask >> lane) & 1u;
+    const bool active = (bmask >> sl) & 1u;
     // a lane whose pair has no reverse term reads zero row coordinates: its reverse sums receive
     // exact zeros and the inner loops carry no branch
-    const bool rev = (brev >> lane) & 1u;
+    const bool rev = (brev >> sl) & 1u;
     any_rev |= rev;
     const int n = __popc(bmask);
     const int slot = __popc(bmask & lt);
+    unsigned lm = 0;  // active lanes of the warp
+#pragma unroll
+    for (int gg = 0; gg < G; ++gg) lm |= bmask << (gg * W);
     if (lane < 2 * NB2) {
       rowv[lane] = rnext;
       if (rbi + 1 < nrb) rnext = rs[(size_t)nrow * 2 * NB2 + lane];
@@ -422,14 +435,15 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
             const V ska = rv[NB2 + a];
             Acc f;
 #pragma unroll
-            for (int j = 0; j < NB2; ++j) {
-              const E p1 = st[(r * NB2 + j) * n];
-              if (j == 0) A::mul(f, p1, rc[j]);
-              else A::mac(f, p1, rc[j]);
-              A::mac_cx(rY[j], p1, ska);
+            for (int i = 0; i < 4; ++i) {
+              const E p1 = st[(r * NB2 + q4 + i) * n];
+              if (i == 0) A::mul(f, p1, rc[i]);
+              else A::mac(f, p1, rc[i]);
+              A::mac_cx(rY[i], p1, ska);
             }
-            red[rsw(2 * a, lane)] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
-            red[rsw(2 * a + 1, lane)] = IMAG ? A::red_re(f) : A::red_im(f);
+            const int v = 2 * ((q * LINES + r) % FL);
+            red[rsw(v, lane)] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
+            red[rsw(v + 1, lane)] = IMAG ? A::red_re(f) : A::red_im(f);
           }
         } else {
           // Q2 columns j: Y'_k[j] = sum_a Q2[a][j] s_c[a];  X'_c[a] += conj(Q2[a][j]) r_k[j]
@@ -439,14 +453,15 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
             const V rkj = rv[j];
             Acc f;
 #pragma unroll
-            for (int a = 0; a < NB2; ++a) {
-              const E p2 = st[(r * NB2 + a) * n];
-              if (a == 0) A::mul(f, p2, sc[a]);
-              else A::mac(f, p2, sc[a]);
-              A::mac_cx(rX[a], p2, rkj);
+            for (int i = 0; i < 4; ++i) {
+              const E p2 = st[(r * NB2 + q4 + i) * n];
+              if (i == 0) A::mul(f, p2, sc[i]);
+              else A::mac(f, p2, sc[i]);
+              A::mac_cx(rX[i], p2, rkj);
             }
-            red[rsw(2 * NB2 + 2 * j, lane)] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
-            red[rsw(2 * NB2 + 2 * j + 1, lane)] = IMAG ? A::red_re(f) : A::red_im(f);
+            const int v = 2 * ((q * LINES + r) % FL);
+            red[rsw(v, lane)] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
+            red[rsw(v + 1, lane)] = IMAG ? A::red_re(f) : A::red_im(f);
           }
         }
       }
@@ -455,35 +470,39 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
       fence_proxy_async();
       __syncwarp();
       if (c + NST < nch) issue(c + NST);
+      if (((q + 1) * LINES) % FL == 0) {
+        // lines [L0, L0 + FL) of this row block are complete: reduce over the active lanes and add
+        // to the row's sums (line L is real pair 2L, 2L + 1 of [X'(NB2) | Y'(NB2)])
+        const int L0 = (q + 1) * LINES - FL;
+        constexpr int LPV = 32 / NV > 0 ? 32 / NV : 1;
+#pragma unroll 1
+        for (int v0 = 0; v0 < NV; v0 += 32 / LPV) {
+          const int v = v0 + lane / LPV;
+          const int part = lane % LPV;
+          R sum = A::red_zero();
+          if (v < NV) {
+            const int span = 32 / LPV;
+            unsigned m = (lm >> (part * span)) & (span == 32 ? 0xffffffffu : ((1u << span) - 1u));
+            while (m) {
+              const int jj = __ffs(m) - 1;
+              m &= m - 1;
+              A::red_add(sum, red[rsw(v, part * span + jj)]);
+            }
+          }
+#pragma unroll
+          for (int mm = 1; mm < LPV; mm <<= 1) A::red_add(sum, A::red_shfl_xor(sum, mm));
+          if (v < NV && part == 0) atomicAdd(acc + (size_t)brow * 4 * NB2 + 2 * L0 + v, A::red_to_double(sum));
+        }
+        __syncwarp();
+      }
     }
     if (cfail >= 0) break;
     // keep the low parts of the reverse sums small (each took NB2 products in this row block)
 #pragma unroll
-    for (int i = 0; i < NB2; ++i) {
+    for (int i = 0; i < 4; ++i) {
       A::renorm(rX[i]);
       A::renorm(rY[i]);
     }
-    // the row block is complete: forward reduction over the active lanes
-    constexpr int LPV = 32 / NV > 0 ? 32 / NV : 1;
-#pragma unroll 1
-    for (int v0 = 0; v0 < NV; v0 += 32 / LPV) {
-      const int v = v0 + lane / LPV;
-      const int part = lane % LPV;
-      R sum = A::red_zero();
-      if (v < NV) {
-        const int span = 32 / LPV;
-        unsigned m = (bmask >> (part * span)) & (span == 32 ? 0xffffffffu : ((1u << span) - 1u));
-        while (m) {
-          const int jj = __ffs(m) - 1;
-          m &= m - 1;
-          A::red_add(sum, red[rsw(v, part * span + jj)]);
-        }
-      }
-#pragma unroll
-      for (int mm = 1; mm < LPV; mm <<= 1) A::red_add(sum, A::red_shfl_xor(sum, mm));
-      if (v < NV && part == 0) atomicAdd(acc + (size_t)brow * 2 * NB2 * 2 + v, A::red_to_double(sum));
-    }
-    __syncwarp();
   }
   if (cfail >= 0) {  // drain the copies still in flight (bounded), then leave
     if (lane == 0) {
@@ -494,14 +513,14 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
     return;
   }
   if (colok && any_rev) {
-    double* dst = acc + (size_t)col * 2 * NB2 * 2;
+    double* dst = acc + (size_t)col * 4 * NB2;
 #pragma unroll
-    for (int i = 0; i < NB2; ++i) {
+    for (int i = 0; i < 4; ++i) {
       const double xr = A::re_d(rX[i]), xi = A::im_d(rX[i]), yr = A::re_d(rY[i]), yi = A::im_d(rY[i]);
-      atomicAdd(dst + 2 * i, IMAG ? -xi : xr);
-      atomicAdd(dst + 2 * i + 1, IMAG ? xr : xi);
-      atomicAdd(dst + 2 * NB2 + 2 * i, IMAG ? -yi : yr);
-      atomicAdd(dst + 2 * NB2 + 2 * i + 1, IMAG ? yr : yi);
+      atomicAdd(dst + 2 * (q4 + i), IMAG ? -xi : xr);
+      atomicAdd(dst + 2 * (q4 + i) + 1, IMAG ? xr : xi);
+      atomicAdd(dst + 2 * NB2 + 2 * (q4 + i), IMAG ? -yi : yr);
+      atomicAdd(dst + 2 * NB2 + 2 * (q4 + i) + 1, IMAG ? yr : yi);
     }
   }
 }
