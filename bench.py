@@ -346,7 +346,7 @@ def run_gpu(args, w, rank, world, dist):
             "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
             "gen_seconds": w["gen_s"]}
     if args.t1 and args.precision != "f64":
-        line["t1"] = t1_compare(args.precision, args.t1_steps, dev)
+        line["t1"] = t1_compare(args.precision, args.t1_steps, dev, "si_nk500" if nb == 2 else "mos2_nk2k")
     if args.cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline_single(w)
     print(json.dumps(line))
@@ -355,14 +355,14 @@ def run_gpu(args, w, rank, world, dist):
 ELEM_BYTES = {"f64": 16, "f64x": 16, "f32": 8, "bf16x2": 8}
 
 
-def t1_compare(precision, nsteps, dev):
-    """T1 of the Si-like nk=500 case (RK4 dt = 1 fs, S_z every 100 steps, exponential fit) from this
-    precision and from the plain FP64 GPU path on the same input; the FP64 path itself matches the
-    FP64 reference to 1e-10 (tests). The equilibrium drift of f is subtracted (alg_ddmdteq with
-    f_eq = f) so that f is stationary."""
+def t1_compare(precision, nsteps, dev, workload):
+    """T1 of a small case of the same band count (Si-like nk=500 for nb=2, MoS2-like nk=2000 for
+    nb=4; RK4 dt = 1 fs, S_z every 100 steps, exponential fit) from this precision and from the plain
+    FP64 GPU path on the same input; the FP64 path itself matches the FP64 reference to 1e-10 (tests).
+    The equilibrium drift of f is subtracted (alg_ddmdteq with f_eq = f) so that f is stationary."""
     from denmat_dynm_development_gb300.dmd import LindbladGPU
     from denmat_dynm_development_gb300.t1fit import fit_t1
-    w = build_workload("si_nk500", 1)
+    w = build_workload(workload, 4)
     st = w["st"]
     nb = st.cfg.nb
     y0 = np.ascontiguousarray(w["dm0"]).view(np.float64).reshape(-1).copy()
@@ -394,8 +394,8 @@ def t1_compare(precision, nsteps, dev):
             g.close()
     a, b = out["f64"], out[precision]
     fa, fb = fit_t1(a[:, 0], a[:, 1]), fit_t1(b[:, 0], b[:, 1])
-    return {"workload": "si_nk500: nb=2, nk=500, %d k-pairs, RK4 dt=1 fs, %d steps, S_z every 100 steps, "
-                        "drift of f subtracted" % (st.npair, nsteps),
+    return {"workload": "%s: nb=%d, nk=%d, %d k-pairs, RK4 dt=1 fs, %d steps, S_z every 100 steps, "
+                        "drift of f subtracted" % (workload, nb, st.cfg.nk, st.npair, nsteps),
             "tau_ps_f64": fa.tau_lsq, "tau_ps": fb.tau_lsq, "rel_err": abs(fb.tau_lsq - fa.tau_lsq) / abs(fa.tau_lsq),
             "s_rel_err": float(np.abs(b[:, 1] - a[:, 1]).max() / np.abs(a[:, 1]).max()),
             "s_ratio_end": float(a[-1, 1] / a[0, 1]), "seconds": time.perf_counter() - t0}

@@ -467,6 +467,8 @@ WORKLOADS = {
     "gaas_nk20k": SynthConfig(nk=20000, nb=2, de_pair_mev=4.45, eimp_sigma_mev=5.0),
     # the same generator at nk=8k (~1.6M pairs, P 0.8 GB): profiling-sized GaAs-like case
     "gaas_nk8k": SynthConfig(nk=8000, nb=2, de_pair_mev=4.45, eimp_sigma_mev=5.0),
-    # MoS2-like precision case: nb=4, nk=30k, ~4M pairs.
-    "mos2_nk30k": SynthConfig(nk=30000, nb=4, de_pair_mev=3.9),
+    # MoS2-like precision case: nb=4 (two spin-split pairs), nk=30k, 4.19M pairs (P 34 GB complex128).
+    "mos2_nk30k": SynthConfig(nk=30000, nb=4, de_pair_mev=0.8),
+    # the same nb=4 generator at nk=2000 (~46k pairs): T1 comparisons of the nb=4 forms
+    "mos2_nk2k": SynthConfig(nk=2000, nb=4, de_pair_mev=0.8),
 }
