@@ -30,6 +30,7 @@ struct dmd_handle {
   double2* d_P = nullptr;      // [npair][2][nb4] (per-thread form) or the column-block element store
   // column-block layout (nb = 2)
   int use_cb = 0;
+  int lin = 0;                 // linearized master equation (DMD_FLAG_LINEAR)
   int pcfg = 0;                // pair-kernel shape variant (DMD_PAIR_CFG)
   int* d_pos = nullptr;        // k -> energy rank
   dmd::RowBlock* d_rb = nullptr;
@@ -168,16 +169,19 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
   ProfScope ps(h, 0);
   if (!h->use_cb) {
     k_prep<NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->expt, h->d_rs, h->d_acc);
-  } else if (h->prec == DMD_PREC_F64X) {
-    k_prep_herm<ArithDF, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(
-        h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt, (float2*)h->d_rs, h->d_acc, h->d_hflag, nullptr, nullptr);
-  } else if (deviation_form(h->prec)) {
-    k_prep_herm<ArithF32, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(
-        h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt, (float*)h->d_rs, h->d_acc, h->d_hflag, h->d_fref,
-        h->d_acc0);
   } else {
-    k_prep_herm<ArithF64, NB><<<blocks_for(n, 256), 256, 0, h->st>>>(
-        h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt, (double*)h->d_rs, h->d_acc, h->d_hflag, nullptr, nullptr);
+    // deviation coordinates for the reduced-precision and the linearized forms
+    const double* fref = (deviation_form(h->prec) || h->lin) ? h->d_fref : nullptr;
+    const unsigned g = blocks_for(n, 256);
+    if (h->prec == DMD_PREC_F64X)
+      k_prep_herm<ArithDF, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
+                                                      (float2*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin);
+    else if (deviation_form(h->prec))
+      k_prep_herm<ArithF32, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
+                                                       (float*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin);
+    else
+      k_prep_herm<ArithF64, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
+                                                       (double*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin);
   }
   h->launches++;
   CKL();
@@ -273,6 +277,7 @@ FinishArgs base_finish(dmd_handle* h, const double2* y) {
   a.acc = h->d_acc;
   a.pos = h->use_cb ? h->d_pos : nullptr;
   a.herm = h->use_cb;
+  a.lin = h->lin;
   a.hflag = h->use_cb ? h->d_hflag : nullptr;
   a.want_eph = 1;
   a.want_coh = (h->picture == DMD_PICTURE_SCHRODINGER || h->d_H) ? 1 : 0;
@@ -514,11 +519,11 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
   std::vector<cd> Peff[2] = {std::vector<cd>(nb4), std::vector<cd>(nb4)};
   std::vector<cd> Q[2] = {std::vector<cd>(nb4), std::vector<cd>(nb4)};
   // deviation form: the constant contraction of diag(f_ref), position order [nk][2][nb2]
-  const bool dev = deviation_form(h->prec);
+  const bool dev = deviation_form(h->prec) && !h->lin;
   std::vector<cd> acc0;
   std::vector<double> fw;
-  if (dev) {
-    acc0.assign((size_t)h->nk * 2 * h->nb2, cd{0, 0});
+  if (dev || h->lin) {
+    if (dev) acc0.assign((size_t)h->nk * 2 * h->nb2, cd{0, 0});
     fw.assign((size_t)h->nk * nb, 0.0);
     if (d->f_ref)
       for (int k = 0; k < h->nk; ++k)
@@ -556,7 +561,9 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
               x = x + ap[2 * e] * d->add_scale;
               yv = yv + ap[2 * e + 1] * d->add_scale;
             }
-            if (tr) yv = -yv;
+            // P: the transposed pair carries (conj P2, conj P1); linear: (Lji, Lij) with the reverse
+            // operator conjugated, so that conj(Q2) = M^H L_rev M (see the header comment of dmd_pairs_cb.cuh)
+            if (h->lin ? (m == 1) : tr) yv = -yv;
             Peff[m][e] = {x, yv};
           }
         herm_transform(h->nb, Peff[0].data(), Peff[1].data(), Q[0].data(), Q[1].data());
@@ -585,10 +592,13 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
     if (e != cudaSuccess) out = fail(h, DMD_E_CUDA, std::string("P upload: ") + cudaGetErrorString(e));
   }
   cudaFreeHost(stage);
-  if (out == DMD_OK && dev) {
-    if ((out = dalloc(h, &h->d_acc0, acc0.size())) || (out = dalloc(h, &h->d_fref, fw.size()))) return out;
-    CK(cudaMemcpy(h->d_acc0, acc0.data(), acc0.size() * 16, cudaMemcpyHostToDevice));
+  if (out == DMD_OK && (dev || h->lin)) {
+    if ((out = dalloc(h, &h->d_fref, fw.size()))) return out;
     CK(cudaMemcpy(h->d_fref, fw.data(), fw.size() * 8, cudaMemcpyHostToDevice));
+  }
+  if (out == DMD_OK && dev) {
+    if ((out = dalloc(h, &h->d_acc0, acc0.size()))) return out;
+    CK(cudaMemcpy(h->d_acc0, acc0.data(), acc0.size() * 16, cudaMemcpyHostToDevice));
   }
   return out;
 }
@@ -656,6 +666,10 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
     return DMD_E_ARG;
   if (d->nkpair > 0 && (!d->k1st || !d->k2nd || !d->P1 || !d->P2)) return DMD_E_ARG;
   if ((d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
+  if (d->flags & ~DMD_FLAG_LINEAR) return DMD_E_ARG;
+  if ((d->flags & DMD_FLAG_LINEAR) &&
+      (!d->f_ref || d->P1_add || (d->bend - d->bstart != 2 && d->bend - d->bstart != 4) || d->nkpair == 0))
+    return DMD_E_ARG;
   if (d->precision < DMD_PREC_F64 || d->precision > DMD_PREC_BF16X2) return DMD_E_ARG;
   // the FP32-pair and reduced-precision forms exist for the column-block contraction (nb = 2, 4)
   const int nbw = d->bend - d->bstart;
@@ -678,6 +692,7 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   h->picture = d->picture;
   h->expt = d->expt ? 1 : 0;
   h->prec = d->precision;
+  h->lin = (d->flags & DMD_FLAG_LINEAR) ? 1 : 0;
   h->nstate = (size_t)h->nk * h->nbdm * h->nbdm;
   int rc = DMD_OK;
   auto bail = [&](int code) {

@@ -218,6 +218,7 @@ struct dmdh_system {
   std::vector<double> dm0;          // complex [nk][nb_dm^2]
   std::vector<double> H;            // complex [nk][nb_dm^2] or empty
   double carrier_gs[3] = {0, 0, 0};  // eip.carrier_bvk_gs, ne_bvk_gs, nh_bvk_gs (electron.h:155-157)
+  std::vector<std::pair<std::vector<double>, std::vector<double>>> imp;  // impurity P x |n_i V| (linear mode)
   int nimp = 0;                      // number of impurity densities (eip.ni.size())
 };
 
@@ -278,6 +279,56 @@ int dmdh_H_BS(int32_t nk, int32_t nb, const double* smat, const double B[3], con
   return DMD_OK;
 }
 
+// Linear operators from one source of P (electronphonon::add_Lscii_from_P1_P2 and
+// add_Lscij_from_P1_P2 with fac2 = false, ElectronPhonon_linear.cpp:147-225), every pair in order.
+// f is the window f_eq [nk][nb].
+void lsc_add(int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, const zc* P1, const zc* P2, const double* f,
+             zc* Lscii, zc* Lij, zc* Lji) {
+  const int nb2 = nb * nb, nb4 = nb2 * nb2;
+  auto sub = [](zc a, zc b) { return zc{a.x - b.x, a.y - b.y}; };
+  auto add = [](zc a, zc b) { return zc{a.x + b.x, a.y + b.y}; };
+  auto scl = [](double r, zc a) { return zc{a.x * r, a.y * r}; };  // complex * double
+  auto cj = [](zc a) { return zc{a.x, -a.y}; };
+  for (int64_t p = 0; p < npair; p++) {
+    const int ik = (int)k1[p], jk = (int)k2[p];
+    const zc* P1p = P1 + (size_t)p * nb4;
+    const zc* P2p = P2 + (size_t)p * nb4;
+    zc* Li = Lscii + (size_t)ik * nb4;
+    zc* Lj = Lscii + (size_t)jk * nb4;
+    for (int i1 = 0; i1 < nb; i1++)
+      for (int i2 = 0; i2 < nb; i2++) {
+        const int n12 = (i1 * nb + i2) * nb2;
+        for (int ib = 0; ib < nb; ib++) {
+          const int nbv = (ib * nb + i2) * nb2, i12ab = n12 + i1 * nb + ib;
+          for (int i3 = 0; i3 < nb; i3++) {
+            const int ib233 = nbv + i3 * nb + i3;
+            Li[i12ab] = sub(Li[i12ab], scl(f[(size_t)jk * nb + i3], P1p[ib233]));
+            if (jk > ik) Lj[i12ab] = sub(Lj[i12ab], scl(f[(size_t)ik * nb + i3], cj(P2p[ib233])));
+          }
+        }
+        for (int ia = 0; ia < nb; ia++) {
+          const int i1a = i1 * nb + ia, i12ab = n12 + ia * nb + i2;
+          for (int i3 = 0; i3 < nb; i3++) {
+            const int i331a = (i3 * nb + i3) * nb2 + i1a;
+            Li[i12ab] = sub(Li[i12ab], scl(1 - f[(size_t)jk * nb + i3], P2p[i331a]));
+            if (jk > ik) Lj[i12ab] = sub(Lj[i12ab], scl(1 - f[(size_t)ik * nb + i3], cj(P1p[i331a])));
+          }
+        }
+      }
+    zc* a = Lij + (size_t)p * nb4;
+    zc* b = Lji + (size_t)p * nb4;
+    for (int i1 = 0; i1 < nb; i1++)
+      for (int i2 = 0; i2 < nb; i2++) {
+        const int i12 = i1 * nb + i2, n12 = i12 * nb2;
+        for (int iab = 0; iab < nb2; iab++) {
+          const int i12ab = n12 + iab, iab12 = iab * nb2 + i12;
+          a[i12ab] = add(a[i12ab], add(scl(1 - f[(size_t)ik * nb + i1], P1p[i12ab]), scl(f[(size_t)ik * nb + i2], P2p[iab12])));
+          b[i12ab] = add(b[i12ab], add(scl(1 - f[(size_t)jk * nb + i1], cj(P2p[i12ab])), scl(f[(size_t)jk * nb + i2], cj(P1p[iab12]))));
+        }
+      }
+  }
+}
+
 int dmdh_load(const char* dir_c, dmdh_system** out) {
   if (!dir_c || !out) return err(DMD_E_ARG, "null argument");
   *out = nullptr;
@@ -292,11 +343,14 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
   }
   auto& pm = s->pm;
   // features outside this path are rejected explicitly
-  const char* unsupported[] = {"alg_linearize", "alg_linearize_dPee", "alg_phenom_relax", "alg_semiclassical",
+  const char* unsupported[] = {"alg_linearize_dPee", "alg_phenom_relax", "alg_semiclassical",
                                "alg_sparseP", "alg_Pin_is_sparse", "alg_only_eimp", "alg_only_ee", "needL",
                                "alg_read_Bso", "gfac_normal_dist", "partial_ionized"};
   for (const char* k : unsupported)
     if (pget(pm, k, 0) != 0) return err(DMD_E_ARG, std::string(k) + " is not supported by the GB300 path");
+  const bool linear = pget(pm, "alg_linearize", 0) != 0;
+  if (linear && pget(pm, "alg_ddmdteq", 0) != 0)  // parameters.cpp:428-429
+    return err(DMD_E_ARG, "if master equation is linearized, ddmdt_eq is not needed");
   if (sget(pm, "code", "jdftx") != "jdftx" || sget(pm, "material_model", "none") != "none")
     return err(DMD_E_ARG, "only code = jdftx, material_model = none");
   if (pget(pm, "laserA", pget(pm, "pumpA0", 0)) > 0) return err(DMD_E_ARG, "laser is not supported");
@@ -475,9 +529,15 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
         a1 = a1 * scale_ei;
         a2 = a2 * scale_ei;
       }
-      s->P1[i] = s->P1[i] + a1;
-      s->P2[i] = s->P2[i] + a2;
+      if (linear) {  // kept apart: each source adds its own linear operators (ElectronPhonon_linear.cpp:57-79)
+        A1[i] = a1;
+        A2[i] = a2;
+      } else {
+        s->P1[i] = s->P1[i] + a1;
+        s->P2[i] = s->P2[i] + a2;
+      }
     }
+    if (linear) s->imp.push_back({A1, A2});
   }
   // time and picture parameters (parameters.cpp:99-106, 283-336, 359-367)
   const std::string pic = sget(pm, "alg_picture", "interaction");
@@ -519,8 +579,9 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
   // equilibrium occupations for the drift subtraction (DensityMatrix_Dynamics.h:58-63 ->
   // singdenmat_k::set_dm_eq, DenMat.cpp:97-148, on the initial or restart state)
   in.mue = in.muh = in.mu;
-  if (pget(pm, "alg_ddmdteq", 0) != 0) {
-    in.ddmdteq = 1;
+  if (pget(pm, "alg_ddmdteq", 0) != 0 || linear) {
+    in.ddmdteq = linear ? 0 : 1;
+    in.linear = linear ? 1 : 0;
     const int nvd = in.nv_dm;
     const zc* dm = (const zc*)s->dm0.data();
     double mus[2] = {in.mu, in.mu};
@@ -552,6 +613,34 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
     for (int ik = 0; ik < nk; ik++)
       for (int i = 0; i < nb_dm; i++)
         s->f_eq[(size_t)ik * nb_dm + i] = fermi(T, i < nvd ? in.muh : in.mue, s->e_dm[(size_t)ik * nb_dm + i]);
+  }
+  if (linear) {
+    // electronphonon::set_Lsc (ElectronPhonon_linear.cpp:3-31): the e-ph operators, each impurity's,
+    // then Lscii onto the diagonal pairs; the linear operators replace P1, P2
+    std::vector<double> fw((size_t)nk * nbw);
+    for (int ik = 0; ik < nk; ik++)
+      for (int b = 0; b < nbw; b++) fw[(size_t)ik * nbw + b] = s->f_eq[(size_t)ik * nb_dm + bs + b];
+    const size_t nb4 = (size_t)nbw * nbw * nbw * nbw;
+    std::vector<double> Lii(2 * (size_t)nk * nb4, 0.0), Lij(2 * np4, 0.0), Lji(2 * np4, 0.0);
+    lsc_add(nbw, nkpair, s->k1.data(), s->k2.data(), (const zc*)s->P1.data(), (const zc*)s->P2.data(), fw.data(),
+            (zc*)Lii.data(), (zc*)Lij.data(), (zc*)Lji.data());
+    for (auto& a : s->imp)
+      lsc_add(nbw, nkpair, s->k1.data(), s->k2.data(), (const zc*)a.first.data(), (const zc*)a.second.data(), fw.data(),
+              (zc*)Lii.data(), (zc*)Lij.data(), (zc*)Lji.data());
+    for (int p = 0; p < nkpair; p++) {
+      if (s->k1[p] != s->k2[p]) continue;
+      const zc* x = (const zc*)Lii.data() + s->k1[p] * nb4;
+      zc* a = (zc*)Lij.data() + (size_t)p * nb4;
+      zc* b = (zc*)Lji.data() + (size_t)p * nb4;
+      for (size_t e = 0; e < nb4; e++) {  // axbyc(L, Lscii, n, c1, c1): L += Lscii + 0
+        const zc t = {x[e].x + 0.0, x[e].y + 0.0};
+        a[e] = {a[e].x + t.x, a[e].y + t.y};
+        b[e] = {b[e].x + t.x, b[e].y + t.y};
+      }
+    }
+    s->P1.swap(Lij);
+    s->P2.swap(Lji);
+    s->imp.clear();
   }
   // coherent Hamiltonian (main.cpp:51)
   const double Blen = sqrt(in.B[0] * in.B[0] + in.B[1] * in.B[1] + in.B[2] * in.B[2]);
@@ -591,6 +680,8 @@ int dmdh_desc(const dmdh_system* s, int32_t precision, int32_t device, dmd_desc*
   d->expt = s->info.expt;
   d->precision = precision;
   d->device = device;
+  d->flags = s->info.linear ? DMD_FLAG_LINEAR : 0u;
+  d->f_ref = s->f_eq.empty() ? s->f_dm.data() : s->f_eq.data();
   return DMD_OK;
 }
 
@@ -606,7 +697,7 @@ int dmdh_get_f(const dmdh_system* s, double* f) {
 }
 int dmdh_get_f_eq(const dmdh_system* s, double* f_eq) {
   if (!s || !f_eq) return DMD_E_ARG;
-  if (s->f_eq.empty()) return err(DMD_E_ARG, "alg_ddmdteq is off: no equilibrium occupations");
+  if (s->f_eq.empty()) return err(DMD_E_ARG, "alg_ddmdteq and alg_linearize are off: no equilibrium occupations");
   memcpy(f_eq, s->f_eq.data(), s->f_eq.size() * 8);
   return DMD_OK;
 }

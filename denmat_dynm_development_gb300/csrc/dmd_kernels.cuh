@@ -77,6 +77,7 @@ struct FinishArgs {
   const double2* acc;  // [nk][2][NB2], indexed by pos[k] when pos is set
   const int* pos;      // k -> accumulator row (column-block layout) or null
   int herm;            // accumulators hold X' = M^H X, Y' = M^H Y (Hermitian coordinates)
+  int lin;             // linearized: the scattering term is (prefac/2)(D o X + h.c.) (evolve_eph_linear.cpp:44-51)
   unsigned int* hflag; // non-Hermitian-state flag of the prep kernel, cleared here (or null)
   int want_eph, want_coh;
   // output: plain RHS
@@ -169,6 +170,9 @@ __global__ void k_finish(FinishArgs a) {
         dmP[i * NB + j] = a.phase ? cmul_rn(d, Y[i * NB + j]) : Y[i * NB + j];
       }
     double2 c[NB2];
+    if (a.lin) {
+      for (int i = 0; i < NB2; ++i) c[i] = Pdm[i];
+    } else {
     for (int i = 0; i < NB; ++i)
       for (int j = 0; j < NB; ++j) {  // (1 - dm) * Pdm   (zhemm Left, alpha 1, beta 0)
         double2 s = mk2(0.0, 0.0);
@@ -181,6 +185,7 @@ __global__ void k_finish(FinishArgs a) {
         for (int l = 0; l < NB; ++l) s = cadd_rn(s, cmul_rn(dmP[i * NB + l], herm_up(rw, NB, l, j)));
         c[i * NB + j] = cadd_rn(cmul_rn(mk2(-1.0, 0.0), s), cmul_rn(mk2(1.0, 0.0), c[i * NB + j]));
       }
+    }
     const double pf = a.prefac * 0.5;
     for (int i = 0; i < NB; ++i)
       for (int j = 0; j < NB; ++j) {

@@ -214,13 +214,14 @@ struct ArithBF2 : ArithF32 {
 // not exactly Hermitian. rs layout: [nk][2][NB2] Hermitian part (r, s), then the anti-Hermitian part.
 // Deviation form (fref != null, window occupations [nk][NB]): the coordinates are those of
 // rho - diag(f) and of (1 - rho) - diag(1 - f) = -(rho - diag(f)); the contraction of diag(f) is
-// the constant acc0 (position order), formed once in FP64.
+// the constant acc0 (position order), formed once in FP64. Linearized form (lin): the coordinates of
+// rho - diag(f_eq) only, with zero st coordinates (the Q2 slot then carries the reverse operator).
 // ---------------------------------------------------------------------------------------------
 template <typename A, int NB>
 __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict__ y, const double* __restrict__ ew,
                             const int* __restrict__ pos, TimeArg ta, int phase, typename A::relem* __restrict__ rs,
                             double2* __restrict__ acc, unsigned int* __restrict__ hflag,
-                            const double* __restrict__ fref, const double2* __restrict__ acc0) {
+                            const double* __restrict__ fref, const double2* __restrict__ acc0, int lin) {
   constexpr int NB2 = NB * NB;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nk * NB2) return;
@@ -239,13 +240,13 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
     if (fref) {
       const double dv = __dsub_rn(vij.x, fref[(size_t)k * NB + i]);
       rh[ab] = A::from_double(dv);
-      rh[NB2 + ab] = A::from_double(-dv);
+      rh[NB2 + ab] = A::from_double(lin ? 0.0 : -dv);
     } else {
       rh[ab] = A::from_double(vij.x);
       rh[NB2 + ab] = A::from_double(1.0 - vij.x);
     }
     ra[ab] = A::from_double(vij.y);
-    ra[NB2 + ab] = A::from_double(0.0 - vij.y);
+    ra[NB2 + ab] = A::from_double(lin ? 0.0 : 0.0 - vij.y);
     if (vij.y != 0.0) atomicOr(hflag, 1u);
     return;
   }
@@ -264,12 +265,12 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
   const int ji = j * NB + i;
   rh[ab] = A::from_double(r1.x);
   rh[ji] = A::from_double(r1.y);
-  rh[NB2 + ab] = A::from_double(s1.x);
-  rh[NB2 + ji] = A::from_double(s1.y);
+  rh[NB2 + ab] = A::from_double(lin ? 0.0 : s1.x);
+  rh[NB2 + ji] = A::from_double(lin ? 0.0 : s1.y);
   ra[ab] = A::from_double(r2.x);
   ra[ji] = A::from_double(r2.y);
-  ra[NB2 + ab] = A::from_double(s2.x);
-  ra[NB2 + ji] = A::from_double(s2.y);
+  ra[NB2 + ab] = A::from_double(lin ? 0.0 : s2.x);
+  ra[NB2 + ji] = A::from_double(lin ? 0.0 : s2.y);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -25,7 +25,7 @@ class Info(C.Structure):
                 ("tstep", C.c_double), ("ode_hstart", C.c_double), ("ode_hmin", C.c_double), ("ode_hmax", C.c_double),
                 ("ode_epsabs", C.c_double), ("Bpert", C.c_double * 3), ("B", C.c_double * 3), ("picture", C.c_int32),
                 ("expt", C.c_int32), ("has_H", C.c_int32), ("ode_method", C.c_int32), ("eimp_fraction", C.c_double),
-                ("mue", C.c_double), ("muh", C.c_double), ("ddmdteq", C.c_int32), ("reserved", C.c_int32)]
+                ("mue", C.c_double), ("muh", C.c_double), ("ddmdteq", C.c_int32), ("linear", C.c_int32)]
 
 
 def _lib():
@@ -86,7 +86,7 @@ class System:
         self.smat = np.zeros((i.nk, 3, nd2), np.complex128)
         _ck(_lib().dmdh_get_smat(h, self.smat.ctypes.data))
         self.f_eq = None
-        if i.ddmdteq:
+        if i.ddmdteq or i.linear:
             self.f_eq = np.zeros((i.nk, i.nb_dm), np.float64)
             _ck(_lib().dmdh_get_f_eq(h, self.f_eq.ctypes.data))
         desc = self.desc()
@@ -119,7 +119,8 @@ class System:
         i = self.info
         g = _dmd.LindbladGPU(nk=i.nk, nb_dm=i.nb_dm, bstart=i.bstart, bend=i.bend, e_dm=self.e_dm,
                              k1st=self.k1st, k2nd=self.k2nd, P1=self.P1, P2=self.P2, prefac_eph=i.prefac_eph,
-                             Hcoh=self.Hcoh, picture=i.picture, expt=i.expt, precision=precision, device=device)
+                             Hcoh=self.Hcoh, picture=i.picture, expt=i.expt, precision=precision, device=device,
+                             f_ref=self.f_eq if self.f_eq is not None else self.f_dm, linear=bool(i.linear))
         try:
             _ck(_lib().dmdh_prepare(self._h, g._h))
         except Exception:

@@ -53,6 +53,11 @@ extern "C" {
 #define DMD_PREC_BF16X2 3  /* P stored as bf16 hi + bf16 lo per component (8 bytes per complex), FP32
                               products; rho enters as its deviation from f_ref */
 
+/* dmd_desc.flags */
+#define DMD_FLAG_LINEAR 1u /* alg_linearize: P1, P2 hold Lscij, Lscji (ElectronPhonon_linear.cpp) and the
+                              RHS is sum herm(L(t) (rho_k' - diag f_ref)) (evolve_eph_linear.cpp:3-51);
+                              f_ref (the f_eq of the linearization) is required */
+
 /* pictures (alg.picture) */
 #define DMD_PICTURE_INTERACTION 0
 #define DMD_PICTURE_SCHRODINGER 1

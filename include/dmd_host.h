@@ -42,7 +42,7 @@ typedef struct dmdh_info {
   double eimp_fraction;
   double mue, muh;  /* chemical potentials of the equilibrium occupations (set_dm_eq), = mu otherwise */
   int32_t ddmdteq;  /* alg_ddmdteq: the equilibrium drift is subtracted from the scattering term */
-  int32_t reserved;
+  int32_t linear;   /* alg_linearize: P1, P2 of the system hold the linear operators Lscij, Lscji */
 } dmdh_info;
 
 /* Read param.in + ldbd_data/ from directory dir (the reference's working directory layout) and

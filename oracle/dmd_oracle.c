@@ -49,6 +49,8 @@ typedef struct {
   int expt;            /* alg.expt */
   const zc* ddmdt_eq;  /* [nk][nb^2] window, NULL unless alg.ddmdteq */
   int scatt_enable;    /* alg.scatt_enable */
+  int linear;          /* alg.linearize: P1, P2 hold Lscij, Lscji (ElectronPhonon_linear.cpp) */
+  const double* f_lin; /* [nk][nb] window f_eq of the linearization */
 } orc_sys;
 
 /* workspace for one RHS evaluation */
@@ -190,6 +192,106 @@ static void trunc_copy(zc* A, const zc* B, int n1, int n2, int bs, int be) {
       for (int b2 = 0; b2 < nb; b2++) A[(size_t)i1 * nb * nb + b1 * nb + b2] = B[(size_t)i1 * n2 * n2 + (b1 + bs) * n2 + b2 + bs];
 }
 
+/* electronphonon::compute_ddmdt -- evolve_eph_linear.cpp:44-51 */
+static void lin_compute_ddmdt(const orc_sys* s, int nb, const zc* dmkp, const zc* lsc, zc* ddmdtk) {
+  const int nb2 = nb * nb;
+  zc contrib[16];
+  memset(contrib, 0, sizeof(contrib));
+  zgemm_mnk(contrib, lsc, dmkp, nb2, 1, nb2, zmk(1, 0), zmk(0, 0));
+  for (int i = 0; i < nb; i++)
+    for (int j = 0; j < nb; j++)
+      ddmdtk[i * nb + j] = zadd(ddmdtk[i * nb + j], zscale(s->prefac_eph * 0.5, zadd(contrib[i * nb + j], zconj(contrib[j * nb + i]))));
+}
+
+/* electronphonon::evolve_linear -- evolve_eph_linear.cpp:3-42 on a single rank; dm is the window
+ * copy, modified in place (dm_ii -= f_eq) as the reference does */
+static void orc_evolve_linear(const orc_sys* s, const double* e, double t, zc* dm, zc* ddmdt_eph) {
+  const int nk = s->nk, nb = s->bend - s->bstart, nb2 = nb * nb, nb4 = nb2 * nb2;
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = 0; i < nb; i++) dm[(size_t)ik * nb2 + i * nb + i].x -= s->f_lin[(size_t)ik * nb + i];
+  memset(ddmdt_eph, 0, sizeof(zc) * (size_t)nk * nb2);
+  zc* Lsct = (zc*)xmalloc(sizeof(zc) * nb4);
+  for (int64_t ip = 0; ip < s->npair; ip++) {
+    const int ik = (int)s->k1st[ip], ikp = (int)s->k2nd[ip];
+    const zc* Lij = s->P1 + (size_t)ip * nb4;
+    const zc* Lji = s->P2 + (size_t)ip * nb4;
+    if (!s->expt) {
+      lin_compute_ddmdt(s, nb, dm + (size_t)ikp * nb2, Lij, ddmdt_eph + (size_t)ik * nb2);
+      if (ik < ikp) lin_compute_ddmdt(s, nb, dm + (size_t)ik * nb2, Lji, ddmdt_eph + (size_t)ikp * nb2);
+    } else {
+      compute_Pt(nb, t, e + (size_t)ik * nb, e + (size_t)ikp * nb, Lij, Lsct, 0);
+      lin_compute_ddmdt(s, nb, dm + (size_t)ikp * nb2, Lsct, ddmdt_eph + (size_t)ik * nb2);
+      if (ik < ikp) {
+        compute_Pt(nb, t, e + (size_t)ikp * nb, e + (size_t)ik * nb, Lji, Lsct, 0);
+        lin_compute_ddmdt(s, nb, dm + (size_t)ik * nb2, Lsct, ddmdt_eph + (size_t)ikp * nb2);
+      }
+    }
+  }
+  free(Lsct);
+}
+
+/* Linear operators from one source of P (ElectronPhonon_linear.cpp:147-225): for every pair,
+ * add_Lscii_from_P1_P2 then add_Lscij_from_P1_P2 (fac2 = false). f is the window f_eq [nk][nb]. */
+void orc_lsc_add(int nk, int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, const zc* P1, const zc* P2,
+                 const double* f, zc* Lscii, zc* Lij, zc* Lji) {
+  const int nb2 = nb * nb, nb4 = nb2 * nb2;
+  (void)nk;
+  for (int64_t p = 0; p < npair; p++) {
+    const int ik = (int)k1[p], jk = (int)k2[p];
+    const zc* P1p = P1 + (size_t)p * nb4;
+    const zc* P2p = P2 + (size_t)p * nb4;
+    zc* Li = Lscii + (size_t)ik * nb4;
+    zc* Lj = Lscii + (size_t)jk * nb4;
+    for (int i1 = 0; i1 < nb; i1++)
+      for (int i2 = 0; i2 < nb; i2++) {
+        const int i12 = i1 * nb + i2, n12 = i12 * nb2;
+        for (int ib = 0; ib < nb; ib++) {
+          const int nbv = (ib * nb + i2) * nb2, iab = i1 * nb + ib, i12ab = n12 + iab;
+          for (int i3 = 0; i3 < nb; i3++) {
+            const int ib233 = nbv + i3 * nb + i3;
+            Li[i12ab] = zsub(Li[i12ab], zscale(f[(size_t)jk * nb + i3], P1p[ib233]));
+            if (jk > ik) Lj[i12ab] = zsub(Lj[i12ab], zscale(f[(size_t)ik * nb + i3], zconj(P2p[ib233])));
+          }
+        }
+        for (int ia = 0; ia < nb; ia++) {
+          const int i1a = i1 * nb + ia, iab = ia * nb + i2, i12ab = n12 + iab;
+          for (int i3 = 0; i3 < nb; i3++) {
+            const int i331a = (i3 * nb + i3) * nb2 + i1a;
+            Li[i12ab] = zsub(Li[i12ab], zscale(1 - f[(size_t)jk * nb + i3], P2p[i331a]));
+            if (jk > ik) Lj[i12ab] = zsub(Lj[i12ab], zscale(1 - f[(size_t)ik * nb + i3], zconj(P1p[i331a])));
+          }
+        }
+      }
+    zc* Lijp = Lij + (size_t)p * nb4;
+    zc* Ljip = Lji + (size_t)p * nb4;
+    for (int i1 = 0; i1 < nb; i1++)
+      for (int i2 = 0; i2 < nb; i2++) {
+        const int i12 = i1 * nb + i2, n12 = i12 * nb2;
+        for (int ia = 0; ia < nb; ia++)
+          for (int ib = 0; ib < nb; ib++) {
+            const int iab = ia * nb + ib, i12ab = n12 + iab, iab12 = iab * nb2 + i12;
+            zc c = zadd(zscale(1 - f[(size_t)ik * nb + i1], P1p[i12ab]), zscale(f[(size_t)ik * nb + i2], P2p[iab12]));
+            Lijp[i12ab] = zadd(Lijp[i12ab], c);
+            c = zadd(zscale(1 - f[(size_t)jk * nb + i1], zconj(P2p[i12ab])), zscale(f[(size_t)jk * nb + i2], zconj(P1p[iab12])));
+            Ljip[i12ab] = zadd(Ljip[i12ab], c);
+          }
+      }
+  }
+}
+
+/* set_Lsc's last step (ElectronPhonon_linear.cpp:23-30): Lscii joins the diagonal pairs */
+void orc_lsc_diag(int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, const zc* Lscii, zc* Lij, zc* Lji) {
+  const int nb4 = nb * nb * nb * nb;
+  for (int64_t p = 0; p < npair; p++) {
+    if (k1[p] != k2[p]) continue;
+    const zc* x = Lscii + (size_t)k1[p] * nb4;
+    for (int e = 0; e < nb4; e++) {
+      Lij[(size_t)p * nb4 + e] = zadd(Lij[(size_t)p * nb4 + e], zadd(x[e], zmk(0, 0)));
+      Lji[(size_t)p * nb4 + e] = zadd(Lji[(size_t)p * nb4 + e], zadd(x[e], zmk(0, 0)));
+    }
+  }
+}
+
 /* electronphonon::evolve_driver -- evolve_eph.cpp:21-32 (window copy, evolve, set_mat back;
  * set_mat's column loop starts at i0 = bStart, comm/mymatrix.cpp:114-119, and i0 = j0 here) */
 void orc_evolve_driver(const orc_sys* s, orc_ws* w, double t, const zc* dm_x, const zc* dm1_x, zc* ddmdt_x) {
@@ -199,7 +301,8 @@ void orc_evolve_driver(const orc_sys* s, orc_ws* w, double t, const zc* dm_x, co
     for (int b = 0; b < nb; b++) e[ik * nb + b] = s->e_dm[(size_t)ik * nd + bs + b]; /* trunc_alloccopy_array (ElectronPhonon.h:79) */
   trunc_copy(w->dm, dm_x, nk, nd, bs, be);
   trunc_copy(w->dm1, dm1_x, nk, nd, bs, be);
-  orc_evolve(s, w, e, t, w->dm, w->dm1, w->ddmdt_eph, 0);
+  if (s->linear) orc_evolve_linear(s, e, t, w->dm, w->ddmdt_eph);
+  else orc_evolve(s, w, e, t, w->dm, w->dm1, w->ddmdt_eph, 0);
   memset(ddmdt_x, 0, sizeof(zc) * nk * nd * nd);
   for (int ik = 0; ik < nk; ik++)
     for (int i = bs; i < be; i++)

@@ -91,6 +91,11 @@ def lib():
         _lib.orc_set_dm_eq.restype = C.c_int
         _lib.orc_compute_ddmdt_eq.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_compute_ddmdt_eq.restype = None
+        _lib.orc_lsc_add.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_lsc_add.restype = None
+        _lib.orc_lsc_diag.argtypes = [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_lsc_diag.restype = None
     return _lib
 
 
@@ -98,7 +103,8 @@ class _Sys(C.Structure):
     _fields_ = [("nk", C.c_int), ("nb_dm", C.c_int), ("bstart", C.c_int), ("bend", C.c_int), ("npair", C.c_int64),
                 ("k1st", C.c_void_p), ("k2nd", C.c_void_p), ("P1", C.c_void_p), ("P2", C.c_void_p),
                 ("e_dm", C.c_void_p), ("prefac_eph", C.c_double), ("Hcoh", C.c_void_p),
-                ("picture_schrodinger", C.c_int), ("expt", C.c_int), ("ddmdt_eq", C.c_void_p), ("scatt_enable", C.c_int)]
+                ("picture_schrodinger", C.c_int), ("expt", C.c_int), ("ddmdt_eq", C.c_void_p), ("scatt_enable", C.c_int),
+                ("linear", C.c_int), ("f_lin", C.c_void_p)]
 
 
 class _Meas(C.Structure):
@@ -232,14 +238,17 @@ class OracleSystem:
     nv_dm: int = 0
     mue: float = 0.0
     muh: float = 0.0
-    f_eq: Optional[np.ndarray] = None        # [nk][nb_dm] with alg_ddmdteq
+    f_eq: Optional[np.ndarray] = None        # [nk][nb_dm] with alg_ddmdteq or alg_linearize
     ddmdt_eq: Optional[np.ndarray] = None    # [nk][nb^2] window, subtracted from the scattering term
+    linear: bool = False                     # alg_linearize: P1, P2 hold Lscij, Lscji
+    f_lin: Optional[np.ndarray] = None       # [nk][nb] window f_eq of the linearization
 
     def cstruct(self):
         s = _Sys(nk=self.nk, nb_dm=self.nb_dm, bstart=self.bstart, bend=self.bend, npair=self.npair,
                  k1st=_ptr(self.k1st), k2nd=_ptr(self.k2nd), P1=_ptr(self.P1), P2=_ptr(self.P2), e_dm=_ptr(self.e_dm),
                  prefac_eph=self.prefac_eph, Hcoh=_ptr(self.Hcoh), picture_schrodinger=self.picture_schrodinger,
-                 expt=self.expt, ddmdt_eq=_ptr(self.ddmdt_eq), scatt_enable=1)
+                 expt=self.expt, ddmdt_eq=_ptr(self.ddmdt_eq), scatt_enable=1, linear=1 if self.linear else 0,
+                 f_lin=_ptr(self.f_lin))
         return s
 
     @property
@@ -288,13 +297,18 @@ def load(d: str) -> OracleSystem:
     if scale_eph != 1.0:
         P1 = P1 * complex(scale_eph, 0)
         P2 = P2 * complex(scale_eph, 0)
+    linear = int(pget(pm, "alg_linearize", 0)) != 0
+    imps = []  # impurity operators times |n_i V| (electronimpurity::read_ldbd_imp_P, ElectronImpurity.cpp:38-39)
     ni = pget(pm, "impurity_density", 0.0, bohr2cm ** dim)
     if ni != 0:
         fraction = abs(ni * cell_size)
         Q1 = np.fromfile(os.path.join(dd, "ldbd_P1_lindblad_D1.bin"), dtype=np.complex128)
         Q2 = np.fromfile(os.path.join(dd, "ldbd_P2_lindblad_D1.bin"), dtype=np.complex128)
-        P1 = P1 + Q1 * fraction
-        P2 = P2 + Q2 * fraction
+        if linear:
+            imps.append((Q1 * fraction, Q2 * fraction))
+        else:
+            P1 = P1 + Q1 * fraction
+            P2 = P2 + Q2 * fraction
     picture = pm.get("alg_picture", "interaction")
     schrod = 1 if picture in ("schrodinger", "non-interaction") else 0
     expt = int(pget(pm, "alg_expt", 1.0))
@@ -319,8 +333,9 @@ def load(d: str) -> OracleSystem:
     cell_size_cmd = cell_size * bohr2cm ** dim
     f_eq = ddmdt_eq = None
     mue = muh = mu
-    if int(pget(pm, "alg_ddmdteq", 0)):
-        # DensityMatrix_Dynamics.h:58-63: set_dm_eq on the initial state, then compute_ddmdt_eq
+    f_lin = None
+    if int(pget(pm, "alg_ddmdteq", 0)) or linear:
+        # DensityMatrix_Dynamics.h:58-63: set_dm_eq on the initial state, then compute_ddmdt_eq or set_Lsc
         f_eq = np.zeros((nk, nb_dm))
         mus = np.array([mu, mu])
         g = np.array(gs)
@@ -328,6 +343,22 @@ def load(d: str) -> OracleSystem:
                              int(pget(pm, "DEBUG", 0)), mus.ctypes.data, f_eq.ctypes.data)
         assert rc == 0, "carrier_bvk_ex is undefined for this input (impurities with zero ground-state carriers)"
         mue, muh = float(mus[0]), float(mus[1])
+    if linear:
+        # electronphonon::set_Lsc (ElectronPhonon_linear.cpp:3-31): e-ph operators, then each impurity's,
+        # then Lscii onto the diagonal pairs
+        f_lin = np.ascontiguousarray(f_eq[:, bstart:bend])
+        nb4 = nb ** 4
+        Lii = np.zeros(nk * nb4, np.complex128)
+        Lij = np.zeros(npair * nb4, np.complex128)
+        Lji = np.zeros(npair * nb4, np.complex128)
+        srcs = [(np.ascontiguousarray(P1), np.ascontiguousarray(P2))] + [
+            (np.ascontiguousarray(a), np.ascontiguousarray(b)) for a, b in imps]
+        for a, b in srcs:
+            L.orc_lsc_add(nk, nb, npair, k1.ctypes.data, k2.ctypes.data, a.ctypes.data, b.ctypes.data, f_lin.ctypes.data,
+                          Lii.ctypes.data, Lij.ctypes.data, Lji.ctypes.data)
+        L.orc_lsc_diag(nb, npair, k1.ctypes.data, k2.ctypes.data, Lii.ctypes.data, Lij.ctypes.data, Lji.ctypes.data)
+        P1, P2 = Lij, Lji
+    if int(pget(pm, "alg_ddmdteq", 0)):
         tmp = OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
                            k1st=k1, k2nd=k2, P1=np.ascontiguousarray(P1), P2=np.ascontiguousarray(P2),
                            prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=None, smat=smat, dm0=dm0,
@@ -341,7 +372,8 @@ def load(d: str) -> OracleSystem:
                         prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=Hcoh, smat=smat, dm0=dm0,
                         picture_schrodinger=schrod, expt=expt, t0=t0, tstep=tstep, tend=pget(pm, "tend", 0.0, fs),
                         temperature=T, mu=mu, nk_full=sz["nk_full"], ob_prefac=(1.0 / sz["nk_full"]) / cell_size_cmd,
-                        ode=ode, params=pm, nv_dm=nv_dm, mue=mue, muh=muh, f_eq=f_eq, ddmdt_eq=ddmdt_eq)
+                        ode=ode, params=pm, nv_dm=nv_dm, mue=mue, muh=muh, f_eq=f_eq, ddmdt_eq=ddmdt_eq, linear=linear,
+                        f_lin=f_lin)
 
 
 def set_mu_and_n(pm, e, e_dm, sz, nv_dm, T, mu, cell_size, dim):

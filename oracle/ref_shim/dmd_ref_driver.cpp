@@ -77,20 +77,23 @@ int main(int argc, char** argv) {
                "temperature %.17g\nmu %.17g\ncell_size %.17g\ncell_size_cmd %.17g\nhas_H %d\n",
             nk, nbdm, eph->bStart, eph->bEnd, eph->nkpair_glob, eph->prefac_eph, elec->nk_full, param->t0,
             param->temperature, param->mu, latt->cell_size, latt->cell_size_cmd, dmdyn->sdmk->Hcoh ? 1 : 0);
-    fprintf(m, "nv_dm %d\nmue %.17g\nmuh %.17g\nddmdteq %d\n", elec->nv_dm, dmdyn->sdmk->mue, dmdyn->sdmk->muh,
-            alg.ddmdteq ? 1 : 0);
+    fprintf(m, "nv_dm %d\nmue %.17g\nmuh %.17g\nddmdteq %d\nlinearize %d\n", elec->nv_dm, dmdyn->sdmk->mue,
+            dmdyn->sdmk->muh, alg.ddmdteq ? 1 : 0, alg.linearize ? 1 : 0);
     fclose(m);
-    if (alg.ddmdteq) {
-      write_bin(out + "/f_eq.bin", dmdyn->sdmk->f_eq[0], sizeof(double) * nk * nbdm);
-      write_bin(out + "/ddmdt_eq.bin", eph->ddmdt_eq[0], sizeof(complex) * nk * eph->nb * eph->nb);
-    }
+    if (alg.ddmdteq || alg.linearize) write_bin(out + "/f_eq.bin", dmdyn->sdmk->f_eq[0], sizeof(double) * nk * nbdm);
+    if (alg.ddmdteq) write_bin(out + "/ddmdt_eq.bin", eph->ddmdt_eq[0], sizeof(complex) * nk * eph->nb * eph->nb);
     write_bin(out + "/e_dm.bin", elec->e_dm[0], sizeof(double) * nk * nbdm);
     write_bin(out + "/f_dm.bin", elec->f_dm[0], sizeof(double) * nk * nbdm);
     write_bin(out + "/dm0.bin", dmdyn->sdmk->dm[0], sizeof(complex) * n);
     if (dmdyn->sdmk->Hcoh) write_bin(out + "/Hcoh.bin", dmdyn->sdmk->Hcoh[0], sizeof(complex) * n);
     size_t np4 = (size_t)eph->nkpair_proc * (size_t)std::pow(eph->nb, 4);
-    write_bin(out + "/P1.bin", eph->P1[0], sizeof(complex) * np4);
-    write_bin(out + "/P2.bin", eph->P2[0], sizeof(complex) * np4);
+    if (alg.linearize) {  // the linear operators replace P1, P2 (ElectronPhonon_linear.cpp:3-31)
+      write_bin(out + "/Lscij.bin", eph->Lscij[0], sizeof(complex) * np4);
+      write_bin(out + "/Lscji.bin", eph->Lscji[0], sizeof(complex) * np4);
+    } else {
+      write_bin(out + "/P1.bin", eph->P1[0], sizeof(complex) * np4);
+      write_bin(out + "/P2.bin", eph->P2[0], sizeof(complex) * np4);
+    }
     return 0;
   }
   if (mode == "rhs") {

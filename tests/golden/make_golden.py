@@ -54,6 +54,15 @@ CASES = {
                            param=dict(Bpert_T=(0, 0, 0.1), B_T=(0.7, 0, 0), eimp_fraction=0.05,
                                       extra={"alg_ddmdteq": 1}),
                            carrier_scale=1.7),
+    # linearized master equation (alg_linearize: L_sc operators built from P and f_eq), e-imp, B field
+    "nb2_linear": dict(cfg=SynthConfig(nk=40, nb=2, seed=18, de_pair_mev=60.0, eimp_sigma_mev=5.0),
+                       param=dict(Bpert_T=(0, 0, 0.1), B_T=(0.5, 0, 0), eimp_fraction=0.05,
+                                  extra={"alg_linearize": 1}),
+                       carrier_scale=1.3),
+    # nb = 4 linearized, Schrodinger picture without phases
+    "nb4_linear": dict(cfg=SynthConfig(nk=16, nb=4, seed=19, de_pair_mev=60.0),
+                       param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0, 0.4, 0),
+                                  extra={"alg_linearize": 1, "alg_picture": "schrodinger", "alg_expt": 0})),
     # two valence bands below the e-ph window (holes: nv_dm = 2), equilibrium drift subtracted
     "nb2_holes_eq": dict(cfg=SynthConfig(nk=24, nb=2, seed=17, de_pair_mev=60.0, extra_bands=2, nv=2),
                          param=dict(Bpert_T=(0.1, 0, 0.05), B_T=(0, 0, 1.0), extra={"alg_ddmdteq": 1})),
@@ -115,10 +124,14 @@ def make_case(name, spec, ref_bin, outroot):
     out["dm0"] = np.fromfile(os.path.join(tmp, "o", "dm0.bin"), dtype=np.complex128).reshape(nk, nbdm * nbdm)
     out["e_dm"] = np.fromfile(os.path.join(tmp, "o", "e_dm.bin")).reshape(nk, nbdm)
     out["f_dm"] = np.fromfile(os.path.join(tmp, "o", "f_dm.bin")).reshape(nk, nbdm)
-    if meta["ddmdteq"]:
-        nbw = int(meta["bend"] - meta["bstart"])
+    nbw = int(meta["bend"] - meta["bstart"])
+    if meta["ddmdteq"] or meta["linearize"]:
         out["f_eq"] = np.fromfile(os.path.join(tmp, "o", "f_eq.bin")).reshape(nk, nbdm)
+    if meta["ddmdteq"]:
         out["ddmdt_eq"] = np.fromfile(os.path.join(tmp, "o", "ddmdt_eq.bin"), dtype=np.complex128).reshape(nk, nbw * nbw)
+    if meta["linearize"]:
+        out["Lscij"] = np.fromfile(os.path.join(tmp, "o", "Lscij.bin"), dtype=np.complex128).reshape(-1, nbw ** 4)
+        out["Lscji"] = np.fromfile(os.path.join(tmp, "o", "Lscji.bin"), dtype=np.complex128).reshape(-1, nbw ** 4)
     if meta["has_H"]:
         out["Hcoh"] = np.fromfile(os.path.join(tmp, "o", "Hcoh.bin"), dtype=np.complex128).reshape(nk, nbdm * nbdm)
     # rhs on three Hermitian states

@@ -24,9 +24,10 @@ def rel(a, b):
 
 def make_gpu(s, precision="f64"):
     from denmat_dynm_development_gb300.dmd import LindbladGPU
+    lin = bool(getattr(s, "linear", False))
     g = LindbladGPU(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
                     P1=s.P1, P2=s.P2, prefac_eph=s.prefac_eph, Hcoh=s.Hcoh, picture=s.picture_schrodinger,
-                    expt=s.expt, precision=precision)
+                    expt=s.expt, precision=precision, linear=lin, f_ref=s.f_eq if lin else None)
     if getattr(s, "ddmdt_eq", None) is not None:
         g.set_ddmdt_eq(s.ddmdt_eq)
     return g
@@ -271,16 +272,18 @@ LOWP_TOL = {"f32": 1e-6, "bf16x2": 1e-5}
 
 def make_gpu_lowp(s, prec, with_ref=True):
     from denmat_dynm_development_gb300.dmd import LindbladGPU
+    lin = bool(getattr(s, "linear", False))
     g = LindbladGPU(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
                     P1=s.P1, P2=s.P2, prefac_eph=s.prefac_eph, Hcoh=s.Hcoh, picture=s.picture_schrodinger,
-                    expt=s.expt, precision=prec, f_ref=s.f_dm if with_ref else None)
+                    expt=s.expt, precision=prec, linear=lin,
+                    f_ref=s.f_eq if lin else (s.f_dm if with_ref else None))
     if getattr(s, "ddmdt_eq", None) is not None:
         g.set_ddmdt_eq(s.ddmdt_eq)
     return g
 
 
 @pytest.mark.parametrize("prec", ["f32", "bf16x2"])
-@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_window", "nb2_carrier_eq", "nb4_eimp_B"])
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_window", "nb2_carrier_eq", "nb4_eimp_B", "nb2_linear", "nb4_linear"])
 def test_lowp_rhs_vs_golden(case, prec, oracle, built):
     d = os.path.join(GOLDEN, case)
     g = dict(np.load(os.path.join(d, "golden.npz")))

@@ -48,12 +48,15 @@ def test_load_matches_reference_setup(case, host, oracle):
     else:
         assert s.Hcoh is None
     assert s.info.nv_dm == int(meta["nv_dm"])
-    if meta["ddmdteq"]:
-        assert s.info.ddmdteq == 1
+    assert s.info.ddmdteq == int(meta["ddmdteq"]) and s.info.linear == int(meta["linearize"])
+    if meta["ddmdteq"] or meta["linearize"]:
         assert s.info.mue == meta["mue"] and s.info.muh == meta["muh"]
         np.testing.assert_array_equal(s.f_eq, g["f_eq"])
     else:
-        assert s.info.ddmdteq == 0 and s.f_eq is None
+        assert s.f_eq is None
+    if meta["linearize"]:  # the linear operators replace P1, P2
+        np.testing.assert_array_equal(s.P1.reshape(g["Lscij"].shape), g["Lscij"])
+        np.testing.assert_array_equal(s.P2.reshape(g["Lscji"].shape), g["Lscji"])
     o = oracle.load(d)
     np.testing.assert_array_equal(s.P1, o.P1)
     np.testing.assert_array_equal(s.P2, o.P2)
@@ -80,9 +83,15 @@ def test_missing_param_and_unsupported_options(host, tmp_path):
     dst = str(tmp_path / "case")
     shutil.copytree(os.path.join(GOLDEN, "nb2_eph"), dst)
     with open(os.path.join(dst, "param.in"), "a") as f:
-        f.write("alg_linearize = 1\n")
-    with pytest.raises(RuntimeError, match="alg_linearize"):
+        f.write("alg_phenom_relax = 1\n")
+    with pytest.raises(RuntimeError, match="alg_phenom_relax"):
         host.System(dst)
+    dst2 = str(tmp_path / "case2")
+    shutil.copytree(os.path.join(GOLDEN, "nb2_eph"), dst2)
+    with open(os.path.join(dst2, "param.in"), "a") as f:
+        f.write("alg_linearize = 1\nalg_ddmdteq = 1\n")
+    with pytest.raises(RuntimeError, match="linearized"):  # parameters.cpp:428-429
+        host.System(dst2)
 
 
 def test_param_parser_quirks(host, tmp_path):

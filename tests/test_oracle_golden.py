@@ -44,6 +44,12 @@ def test_setup_bitwise(case, oracle):
         np.testing.assert_array_equal(s.ddmdt_eq, g["ddmdt_eq"])
     else:
         assert s.ddmdt_eq is None
+    if meta["linearize"]:
+        # set_dm_eq and set_Lsc (the linear operators replace P1, P2)
+        assert s.mue == meta["mue"] and s.muh == meta["muh"]
+        np.testing.assert_array_equal(s.f_eq, g["f_eq"])
+        np.testing.assert_array_equal(s.P1.reshape(g["Lscij"].shape), g["Lscij"])
+        np.testing.assert_array_equal(s.P2.reshape(g["Lscji"].shape), g["Lscji"])
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
