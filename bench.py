@@ -244,6 +244,70 @@ def run_reference(args, w):
 # ------------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------------
+def batch_states(w, nrhs, seed=7):
+    """nrhs initial states sharing the workload's P: first-order spin polarisations along x, y, z
+    (0.1 T, electron.cpp:62-98) in turn, each with its own random Hermitian 1e-4 deviation standing
+    in for a pump with a random Jones vector."""
+    from denmat_dynm_development_gb300 import host as H
+    st = w["st"]
+    rng = np.random.default_rng(seed)
+    out = []
+    for q in range(nrhs):
+        B = np.zeros(3)
+        B[q % 3] = 0.1 * U.Tesla2au
+        d = H.dm_bpert(st.s, w["e"], w["f"], w["T"], B, 0.0, 0).reshape(st.cfg.nk, st.cfg.nb, st.cfg.nb)
+        x = 1e-4 * (rng.standard_normal(d.shape) + 1j * rng.standard_normal(d.shape)) * w["f"][:, :, None]
+        d = d + 0.5 * (x + np.conj(np.swapaxes(x, 1, 2)))
+        out.append(np.ascontiguousarray(d.reshape(st.cfg.nk, -1)).view(np.float64).reshape(-1))
+    return np.concatenate(out)
+
+
+def run_gpu_batched(args, w):
+    """Batched form: args.nrhs states share P; value = states x RK4 steps per second."""
+    from denmat_dynm_development_gb300.dmd import LindbladGPU
+    st = w["st"]
+    nb = st.cfg.nb
+    R = args.nrhs
+    prec = args.precision if args.precision in ("f32", "bf16x2") else "f32"
+    g = LindbladGPU(nk=st.cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=w["e"], k1st=st.k1, k2nd=st.k2, P1=w["P1"],
+                    P2=w["P2"], prefac_eph=w["prefac"], picture=0, expt=1, precision=prec, f_ref=w["f"], nrhs=R)
+    h = 1.0 * U.fs
+    g.set_state(0.0, batch_states(w, R))
+    g.rk4(h, args.warmup)
+    clk = ClockSampler(0)
+    clk.start()
+    g.sync()
+    l0 = g.launches
+    g.timer_start()
+    g.rk4(h, args.steps)
+    ms = g.timer_stop()
+    g.sync()
+    clocks = clk.stop()
+    launches = g.launches - l0
+    g.set_profiling(True)
+    g.rk4(h, 2)
+    pair_ms, pair_n = g.profile(1)
+    g.set_profiling(False)
+    g.close()
+    ms_per_step = ms / args.steps
+    peak, peak_kind = measured_peak()
+    bpl = algorithmic_bytes(nb, st.npair, st.cfg.nk, ELEM_BYTES[prec]) + (R - 1) * st.cfg.nk * nb * nb * 16 * 2
+    pair_avg = pair_ms / max(pair_n, 1)
+    flops = 2.0 * 4 * nb ** 4 * 2 * st.npair * R  # complex x real products of the four sums, per RHS evaluation
+    line = {"metric": "ensemble RK4 steps/s (%d states sharing P, batched form)" % R, "value": R * 1e3 / ms_per_step,
+            "unit": "state-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": prec + " (rho as deviation from f)", "data": "synthetic",
+            "config": config_of(w, {"precision": prec, "nrhs": R,
+                                    "states": "spin polarisation along x/y/z in turn + random 1e-4 deviation"}),
+            "roofline": {"bound": "fp32-issue", "achieved": bpl / (pair_avg * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": bpl / (pair_avg * 1e-3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "batched k-pair contraction", "avg_launch_ms": pair_avg,
+                         "tflops": flops / (pair_avg * 1e-3) / 1e12},
+            "clocks": clocks, "gpu_launches": launches}
+    print(json.dumps(line))
+
+
 def run_gpu(args, w, rank, world, dist):
     from denmat_dynm_development_gb300.dmd import LindbladGPU, PinnedArray
     st = w["st"]
@@ -413,6 +477,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-t1", dest="t1", action="store_false")
     ap.add_argument("--t1-steps", type=int, default=10000)
+    ap.add_argument("--nrhs", type=int, default=1, help="batched form: states sharing P (f32 / bf16x2)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
@@ -424,6 +489,10 @@ def main():
         return
     # the generator's worker processes start before any CUDA call
     w = build_workload(args.workload, max(1, min(16, (os.cpu_count() or 1) // max(world, 1))))
+    if args.nrhs > 1:
+        if rank == 0:
+            run_gpu_batched(args, w)
+        return
     dist = None
     if world > 1:
         import torch

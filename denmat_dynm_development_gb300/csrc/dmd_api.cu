@@ -22,7 +22,10 @@ struct dmd_handle {
   long long npair = 0;
   double prefac = 0;
   int picture = 0, expt = 1, prec = 0;
-  size_t nstate = 0;  // complex elements of the state (nk * nbdm^2)
+  size_t nstate = 0;  // complex elements of the state (nrhs * nk * nbdm^2)
+  size_t nstate1 = 0; // complex elements of one state (nk * nbdm^2)
+  int nrhs = 1;       // batched form: states sharing P
+  int brw = 4;        // batched form: states per warp in the contraction
   // device arrays
   double* d_ew = nullptr;      // [nk][nb]
   double* d_edm = nullptr;     // [nk][nbdm]
@@ -110,6 +113,12 @@ int dalloc(dmd_handle* h, T** p, size_t n) {
 
 inline unsigned blocks_for(long long n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
 
+// doubles of the reduction scratch: RKF45 error blocks of the whole state, observable partials
+size_t red_elems(const dmd_handle* h) {
+  const size_t a = 4096, b = (2 * h->nstate + 255) / 256 + 64, c = 2 * ((size_t)h->nk / 256 + 1) * h->nrhs;
+  return a > b ? (a > c ? a : c) : (b > c ? b : c);
+}
+
 // bytes of one stored Q element per arithmetic
 int elem_bytes(int prec) { return (prec == DMD_PREC_F32 || prec == DMD_PREC_BF16X2) ? 8 : 16; }
 // the reduced-precision forms contract rho - diag(f_ref) only
@@ -172,16 +181,19 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
   } else {
     // deviation coordinates for the reduced-precision and the linearized forms
     const double* fref = (deviation_form(h->prec) || h->lin) ? h->d_fref : nullptr;
-    const unsigned g = blocks_for(n, 256);
+    const dim3 g(blocks_for(n, 256), h->nrhs);
     if (h->prec == DMD_PREC_F64X)
       k_prep_herm<ArithDF, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
-                                                      (float2*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin);
+                                                      (float2*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin,
+                                                      h->nrhs);
     else if (deviation_form(h->prec))
       k_prep_herm<ArithF32, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
-                                                       (float*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin);
+                                                       (float*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin,
+                                                       h->nrhs);
     else
       k_prep_herm<ArithF64, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
-                                                       (double*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin);
+                                                       (double*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin,
+                                                       h->nrhs);
   }
   h->launches++;
   CKL();
@@ -189,24 +201,27 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
 }
 
 // the Hermitian pass and the gated anti-Hermitian pass of the nb = 2 contraction
-template <typename A, int NB, int L, int NST, int MB>
+template <typename A, int NB, int L, int NST, int MB, int RW = 1>
 void herm_pair_launches(dmd_handle* h, const typename A::relem* rs, size_t half) {
-  typedef CbTmaSmem<A, NB, L, NST> S;
-  const unsigned g = blocks_for(h->nitems, 4);
-  k_pairs_herm<A, NB, L, NST, MB, false><<<g, 128, S::cta_bytes, h->st>>>(
-      h->d_items, h->nitems, h->d_rb, (const typename A::elem*)h->d_P, rs, (double*)h->d_acc, h->nk, nullptr, h->d_err);
-  k_pairs_herm<A, NB, L, NST, MB, true><<<g, 128, S::cta_bytes, h->st>>>(
+  typedef CbTmaSmem<A, NB, L, NST, RW> S;
+  const size_t cstride = (size_t)h->nk * 2 * h->nb2;  // coordinates and sums per state
+  const long long warps = (long long)h->nitems * ((h->nrhs + RW - 1) / RW);
+  const unsigned g = blocks_for(warps, 4);
+  k_pairs_herm<A, NB, L, NST, MB, false, RW><<<g, 128, S::cta_bytes, h->st>>>(
+      h->d_items, h->nitems, h->d_rb, (const typename A::elem*)h->d_P, rs, (double*)h->d_acc, h->nk, nullptr, h->d_err,
+      h->nrhs, cstride, 2 * cstride);
+  k_pairs_herm<A, NB, L, NST, MB, true, RW><<<g, 128, S::cta_bytes, h->st>>>(
       h->d_items, h->nitems, h->d_rb, (const typename A::elem*)h->d_P, rs + half, (double*)h->d_acc, h->nk,
-      h->d_hflag, h->d_err);
+      h->d_hflag, h->d_err, h->nrhs, cstride, 2 * cstride);
 }
 
-template <typename A, int NB, int L, int NST, int MB>
+template <typename A, int NB, int L, int NST, int MB, int RW = 1>
 cudaError_t herm_pair_attrs() {
-  const int bytes = (int)CbTmaSmem<A, NB, L, NST>::cta_bytes;
-  cudaError_t e =
-      cudaFuncSetAttribute(k_pairs_herm<A, NB, L, NST, MB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  const int bytes = (int)CbTmaSmem<A, NB, L, NST, RW>::cta_bytes;
+  cudaError_t e = cudaFuncSetAttribute(k_pairs_herm<A, NB, L, NST, MB, false, RW>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_pairs_herm<A, NB, L, NST, MB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(k_pairs_herm<A, NB, L, NST, MB, true, RW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              bytes);
   return e;
 }
@@ -222,8 +237,13 @@ int launch_pairs(dmd_handle* h) {
     if constexpr (NB == 2 || NB == 4) {
       // Hermitian coordinates; the second launch carries the anti-Hermitian part of a state that is
       // not exactly Hermitian and returns at once unless the prep kernel raised d_hflag
-      const size_t half = (size_t)h->nk * 2 * h->nb2;  // coordinates per part
-      if (h->prec == DMD_PREC_F64X) {
+      const size_t half = (size_t)h->nk * 2 * h->nb2 * h->nrhs;  // coordinates per part
+      if (h->nrhs > 1) {  // batched form: reduced-precision arithmetics only (dmd_create)
+        const float* rs = (const float*)h->d_rs;
+        if (h->prec == DMD_PREC_BF16X2) herm_pair_launches<ArithBF2, NB, 4, 2, 2, 4>(h, rs, half);
+        else if (h->brw == 8) herm_pair_launches<ArithF32, NB, 4, 2, 2, 8>(h, rs, half);
+        else herm_pair_launches<ArithF32, NB, 4, 2, 2, 4>(h, rs, half);
+      } else if (h->prec == DMD_PREC_F64X) {
         const float2* rs = (const float2*)h->d_rs;
         if constexpr (NB == 4) {
           herm_pair_launches<ArithDF, NB, 2, 2, 4>(h, rs, half);
@@ -254,7 +274,7 @@ int launch_pairs(dmd_handle* h) {
 template <int NB>
 int launch_finish(dmd_handle* h, FinishArgs a) {
   ProfScope ps(h, 2);
-  k_finish<NB><<<blocks_for(h->nk, 128), 128, 0, h->st>>>(a);
+  k_finish<NB><<<dim3(blocks_for(h->nk, 128), h->nrhs), 128, 0, h->st>>>(a);
   h->launches++;
   CKL();
   return DMD_OK;
@@ -279,6 +299,9 @@ FinishArgs base_finish(dmd_handle* h, const double2* y) {
   a.herm = h->use_cb;
   a.lin = h->lin;
   a.hflag = h->use_cb ? h->d_hflag : nullptr;
+  a.nrhs = h->nrhs;
+  a.sstride = h->nstate1;
+  a.astride = (size_t)h->nk * 2 * h->nb2;
   a.want_eph = 1;
   a.want_coh = (h->picture == DMD_PICTURE_SCHRODINGER || h->d_H) ? 1 : 0;
   return a;
@@ -501,11 +524,15 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
     cudaError_t (*const attrs[])() = {
         herm_pair_attrs<ArithDF, 2, 2, 2, 4>, herm_pair_attrs<ArithDF, 2, 2, 3, 3>, herm_pair_attrs<ArithDF, 2, 1, 4, 4>,
         herm_pair_attrs<ArithDF, 2, 1, 3, 4>, herm_pair_attrs<ArithDF, 2, 1, 6, 3>, herm_pair_attrs<ArithF64, 2, 2, 2, 4>,
-        herm_pair_attrs<ArithF32, 2, 4, 2, 5>, herm_pair_attrs<ArithBF2, 2, 4, 2, 5>};
+        herm_pair_attrs<ArithF32, 2, 4, 2, 5>, herm_pair_attrs<ArithBF2, 2, 4, 2, 5>,
+        herm_pair_attrs<ArithF32, 2, 4, 2, 2, 4>, herm_pair_attrs<ArithF32, 2, 4, 2, 2, 8>,
+        herm_pair_attrs<ArithBF2, 2, 4, 2, 2, 4>};
     for (auto fn : attrs) CK(fn());
   } else {
     cudaError_t (*const attrs[])() = {herm_pair_attrs<ArithDF, 4, 2, 2, 4>, herm_pair_attrs<ArithF64, 4, 2, 2, 4>,
-                                      herm_pair_attrs<ArithF32, 4, 4, 2, 5>, herm_pair_attrs<ArithBF2, 4, 4, 2, 5>};
+                                      herm_pair_attrs<ArithF32, 4, 4, 2, 5>, herm_pair_attrs<ArithBF2, 4, 4, 2, 5>,
+                                      herm_pair_attrs<ArithF32, 4, 4, 2, 2, 4>, herm_pair_attrs<ArithF32, 4, 4, 2, 2, 8>,
+                                      herm_pair_attrs<ArithBF2, 4, 4, 2, 2, 4>};
     for (auto fn : attrs) CK(fn());
   }
   int rc;
@@ -667,6 +694,9 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   if (d->nkpair > 0 && (!d->k1st || !d->k2nd || !d->P1 || !d->P2)) return DMD_E_ARG;
   if ((d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
   if (d->flags & ~DMD_FLAG_LINEAR) return DMD_E_ARG;
+  const int nrhs = d->nrhs > 1 ? d->nrhs : 1;
+  // batched form: FP32 or bf16 hi+lo storage on the column-block contraction
+  if (nrhs > 1 && (d->precision != DMD_PREC_F32 && d->precision != DMD_PREC_BF16X2)) return DMD_E_ARG;
   if ((d->flags & DMD_FLAG_LINEAR) &&
       (!d->f_ref || d->P1_add || (d->bend - d->bstart != 2 && d->bend - d->bstart != 4) || d->nkpair == 0))
     return DMD_E_ARG;
@@ -693,7 +723,10 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   h->expt = d->expt ? 1 : 0;
   h->prec = d->precision;
   h->lin = (d->flags & DMD_FLAG_LINEAR) ? 1 : 0;
-  h->nstate = (size_t)h->nk * h->nbdm * h->nbdm;
+  h->nrhs = nrhs;
+  h->nstate1 = (size_t)h->nk * h->nbdm * h->nbdm;
+  h->nstate = h->nstate1 * nrhs;
+  if (const char* v = getenv("DMD_BATCH_RW")) h->brw = atoi(v) == 8 ? 8 : 4;
   int rc = DMD_OK;
   auto bail = [&](int code) {
     std::string m = h->err;
@@ -708,12 +741,12 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   if ((rc = dalloc(h, &h->d_ew, nk * h->nb)) || (rc = dalloc(h, &h->d_edm, nk * nbdm)) ||
       (rc = dalloc(h, &h->d_kk, (h->nb == 2 || h->nb == 4) ? 1 : (size_t)h->npair)) ||
       (rc = dalloc(h, &h->d_P, ((size_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) + 15) / 16)) ||
-      (rc = dalloc(h, &h->d_rs, nk * 2 * h->nb2)) || (rc = dalloc(h, &h->d_acc, nk * 2 * h->nb2)) ||
+      (rc = dalloc(h, &h->d_rs, nk * 2 * h->nb2 * nrhs)) || (rc = dalloc(h, &h->d_acc, nk * 2 * h->nb2 * nrhs)) ||
       (rc = dalloc(h, &h->d_y, h->nstate)) || (rc = dalloc(h, &h->d_ytmp, h->nstate)) ||
       (rc = dalloc(h, &h->d_y0, h->nstate)) || (rc = dalloc(h, &h->d_in, h->nstate)) ||
       (rc = dalloc(h, &h->d_in1, h->nstate)) || (rc = dalloc(h, &h->d_out, h->nstate)) ||
       (rc = dalloc(h, &h->d_K, 6 * h->nstate)) || (rc = dalloc(h, &h->d_tref, 2)) ||
-      (rc = dalloc(h, &h->d_step, 1)) || (rc = dalloc(h, &h->d_red, 4096)) || (rc = dalloc(h, &h->d_coef_i, 64)) ||
+      (rc = dalloc(h, &h->d_step, 1)) || (rc = dalloc(h, &h->d_red, red_elems(h))) || (rc = dalloc(h, &h->d_coef_i, 64)) ||
       (rc = dalloc(h, &h->d_coef, 64)) || (rc = dalloc(h, &h->d_flag, 1)) || (rc = dalloc(h, &h->d_err, 1)) ||
       (rc = dalloc(h, &h->d_hflag, 1)))
     return bail(rc);
@@ -724,8 +757,8 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
       cudaMemcpy(h->d_edm, d->e_dm, nk * nbdm * 8, cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(h, DMD_E_CUDA, "upload energies"));
   if (d->Hcoh) {
-    if ((rc = dalloc(h, &h->d_H, h->nstate))) return bail(rc);
-    if (cudaMemcpy(h->d_H, d->Hcoh, h->nstate * 16, cudaMemcpyHostToDevice) != cudaSuccess)
+    if ((rc = dalloc(h, &h->d_H, h->nstate1))) return bail(rc);
+    if (cudaMemcpy(h->d_H, d->Hcoh, h->nstate1 * 16, cudaMemcpyHostToDevice) != cudaSuccess)
       return bail(fail(h, DMD_E_CUDA, "upload H"));
   }
   h->use_cb = ((h->nb == 2 || h->nb == 4) && h->npair > 0) ? 1 : 0;
@@ -988,7 +1021,7 @@ int rkf45_step(Rkf& r, double t, double hs, double* y, double* rmax, double eps_
   CK(cudaMemcpyAsync(h->d_coef, kE, sizeof(kE), cudaMemcpyHostToDevice, h->st));
   const size_t n = 2 * h->nstate;
   const unsigned nbk = blocks_for((long long)n, 256);
-  if (nbk > 4096) return fail(h, DMD_E_ARG, "state too large for the error reduction");
+  if (nbk > red_elems(h)) return fail(h, DMD_E_ARG, "state too large for the error reduction");
   k_rk_err<<<nbk, 256, 0, h->st>>>(n, y, (const double*)h->d_K, 2 * h->nstate, 5, h->d_coef_i, h->d_coef, hs, eps_abs,
                                    eps_rel, h->d_red);
   h->launches++;
@@ -1073,9 +1106,9 @@ int dmd_set_observable(dmd_handle* h, int slot, const double* obs, const double*
   if (!h || slot < 0 || slot >= 8 || !obs || !f) return DMD_E_ARG;
   CK(cudaSetDevice(h->dev));
   int rc;
-  if (!h->d_obs[slot] && (rc = dalloc(h, &h->d_obs[slot], h->nstate))) return rc;
+  if (!h->d_obs[slot] && (rc = dalloc(h, &h->d_obs[slot], h->nstate1))) return rc;
   if (!h->d_f[slot] && (rc = dalloc(h, &h->d_f[slot], (size_t)h->nk * h->nbdm))) return rc;
-  CK(cudaMemcpy(h->d_obs[slot], obs, h->nstate * 16, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_obs[slot], obs, h->nstate1 * 16, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_f[slot], f, (size_t)h->nk * h->nbdm * 8, cudaMemcpyHostToDevice));
   h->obs_prefac[slot] = prefac;
   return DMD_OK;
@@ -1100,6 +1133,29 @@ int dmd_measure(dmd_handle* h, int slot, int bstart, int bend, double* tot, doub
   }
   if (tot) *tot = s1 * h->obs_prefac[slot];
   if (tot_amp) *tot_amp = s2 * h->obs_prefac[slot];
+  return DMD_OK;
+}
+
+int dmd_measure_batch(dmd_handle* h, int slot, int bstart, int bend, double* tot, double* tot_amp) {
+  if (!h || slot < 0 || slot >= 8 || !h->d_obs[slot] || bstart < 0 || bend > h->nbdm || bstart > bend) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  const unsigned nbk = blocks_for(h->nk, 256);
+  k_measure<<<dim3(nbk, h->nrhs), 256, 0, h->st>>>(h->nk, h->nbdm, bstart, bend, h->d_obs[slot], h->d_f[slot],
+                                                   h->d_edm, h->t, h->picture, h->d_y, h->d_red, h->nstate1);
+  h->launches++;
+  CKL();
+  std::vector<double> part(2 * (size_t)nbk * h->nrhs);
+  CK(cudaMemcpyAsync(part.data(), h->d_red, part.size() * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int q = 0; q < h->nrhs; ++q) {
+    double s1 = 0, s2 = 0;
+    for (unsigned b = 0; b < nbk; ++b) {
+      s1 += part[2 * ((size_t)q * nbk + b)];
+      s2 += part[2 * ((size_t)q * nbk + b) + 1];
+    }
+    if (tot) tot[q] = s1 * h->obs_prefac[slot];
+    if (tot_amp) tot_amp[q] = s2 * h->obs_prefac[slot];
+  }
   return DMD_OK;
 }
 

@@ -77,6 +77,9 @@ struct FinishArgs {
   const double2* acc;  // [nk][2][NB2], indexed by pos[k] when pos is set
   const int* pos;      // k -> accumulator row (column-block layout) or null
   int herm;            // accumulators hold X' = M^H X, Y' = M^H Y (Hermitian coordinates)
+  int nrhs;            // batched form: states evaluated together (blockIdx.y), 1 otherwise
+  size_t sstride;      // state elements per state (nk * nbdm^2)
+  size_t astride;      // accumulator elements (double2) per state
   int lin;             // linearized: the scattering term is (prefac/2)(D o X + h.c.) (evolve_eph_linear.cpp:44-51)
   unsigned int* hflag; // non-Hermitian-state flag of the prep kernel, cleared here (or null)
   int want_eph, want_coh;
@@ -98,11 +101,13 @@ template <int NB>
 __global__ void k_finish(FinishArgs a) {
   constexpr int NB2 = NB * NB;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a.hflag && k == 0) *a.hflag = 0u;  // every pair launch of this evaluation has completed
+  const int q = blockIdx.y;  // state of the batch
+  if (a.hflag && k == 0 && q == 0) *a.hflag = 0u;  // every pair launch of this evaluation has completed
   if (k >= a.nk) return;
   const int nd = a.nbdm, nd2 = nd * nd;
   const double t = eval_time(a.ta);
-  const double2* yk = a.y + (size_t)k * nd2;
+  const size_t qs = (size_t)q * a.sstride;
+  const double2* yk = a.y + qs + (size_t)k * nd2;
   double2 f[DMD_MAX_NBDM * DMD_MAX_NBDM];
   for (int i = 0; i < nd2; ++i) f[i] = mk2(0.0, 0.0);
 
@@ -142,7 +147,7 @@ __global__ void k_finish(FinishArgs a) {
   // scattering finish on the window (evolve_eph.cpp:140-162, evolve_driver :21-32)
   if (a.want_eph) {
     const double* ew = a.ew + (size_t)k * NB;
-    const double2* Xs = a.acc + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
+    const double2* Xs = a.acc + (size_t)q * a.astride + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
     double2 X[NB2], Y[NB2];
     for (int i = 0; i < NB2; ++i) {
       X[i] = Xs[i];
@@ -200,12 +205,12 @@ __global__ void k_finish(FinishArgs a) {
       }
   }
 
-  const size_t base = (size_t)k * nd2;
+  const size_t base = qs + (size_t)k * nd2;
   if (a.mode == 0) {
     for (int i = 0; i < nd2; ++i) a.out[base + i] = f[i];
     return;
   }
-  const size_t n = (size_t)a.nk * nd2;
+  const size_t n = a.sstride * a.nrhs;  // stage stride: the whole batch
   if (a.mode == 1) {
     const double h = a.tref[1], hh = 0.5 * h, h6 = h / 6.0;
     double2* Ks = a.K + (size_t)a.stage * n;
@@ -282,9 +287,11 @@ __global__ void k_rk_err(size_t n, const double* __restrict__ y, const double* _
 // observable totals (observable.h:356-366), per-block partial sums; block b covers k in a stripe
 __global__ void k_measure(int nk, int nbdm, int bs, int be, const double2* __restrict__ obs, const double* __restrict__ f,
                           const double* __restrict__ edm, double t, int picture, const double2* __restrict__ y,
-                          double* __restrict__ part) {
+                          double* __restrict__ part, size_t ystride = 0) {
   __shared__ double s1[256], s2[256];
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  y += (size_t)blockIdx.y * ystride;        // state of the batch
+  part += (size_t)blockIdx.y * gridDim.x * 2;
   double ob = 0.0, oba = 0.0;
   if (k < nk) {
     const int nd = nbdm;

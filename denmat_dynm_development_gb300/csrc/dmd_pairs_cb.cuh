@@ -211,7 +211,8 @@ struct ArithBF2 : ArithF32 {
 // Prep: Hermitian and anti-Hermitian coordinates of rt, st per k (written at pos[k]) and the
 // accumulators' start values (zero, or acc0). One thread per (k, element (i, j)); the thread of
 // (i, j) with i < j writes the coordinates at (i, j) and (j, i). Raises *hflag when some rho_k is
-// not exactly Hermitian. rs layout: [nk][2][NB2] Hermitian part (r, s), then the anti-Hermitian part.
+// not exactly Hermitian. rs layout: [nrhs][nk][2][NB2] Hermitian part (r, s), then the anti-Hermitian
+// part; the batched form runs one grid row (blockIdx.y) per state.
 // Deviation form (fref != null, window occupations [nk][NB]): the coordinates are those of
 // rho - diag(f) and of (1 - rho) - diag(1 - f) = -(rho - diag(f)); the contraction of diag(f) is
 // the constant acc0 (position order), formed once in FP64. Linearized form (lin): the coordinates of
@@ -221,10 +222,17 @@ template <typename A, int NB>
 __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict__ y, const double* __restrict__ ew,
                             const int* __restrict__ pos, TimeArg ta, int phase, typename A::relem* __restrict__ rs,
                             double2* __restrict__ acc, unsigned int* __restrict__ hflag,
-                            const double* __restrict__ fref, const double2* __restrict__ acc0, int lin) {
+                            const double* __restrict__ fref, const double2* __restrict__ acc0, int lin,
+                            int nrhs = 1) {
   constexpr int NB2 = NB * NB;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nk * NB2) return;
+  // batched form: state q = blockIdx.y; its state, coordinates and sums follow those of q - 1
+  const int q = blockIdx.y;
+  const size_t cstride = (size_t)nk * 2 * NB2;  // coordinates (and sums) per state
+  y += (size_t)q * nk * nbdm * nbdm;
+  acc += (size_t)q * cstride;
+  rs += (size_t)q * cstride;
   const int k = idx / NB2, ab = idx - k * NB2, i = ab / NB, j = ab - i * NB;
   const int p = pos[k];
   const size_t ax = (size_t)p * 2 * NB2 + ab;
@@ -232,7 +240,7 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
   acc[ax + NB2] = acc0 ? acc0[ax + NB2] : mk2(0.0, 0.0);
   if (i > j) return;
   typename A::relem* rh = rs + (size_t)p * 2 * NB2;
-  typename A::relem* ra = rs + (size_t)nk * 2 * NB2 + (size_t)p * 2 * NB2;
+  typename A::relem* ra = rs + (size_t)nrhs * cstride + (size_t)p * 2 * NB2;
   const double2* yk = y + (size_t)k * nbdm * nbdm;
   const double2 vij = yk[(bs + i) * nbdm + bs + j];
   if (i == j) {
@@ -287,16 +295,16 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
 // reduced over the warp through a shared buffer and added with 16 FP64 atomics. Waits are bounded
 // (dmd_tma.cuh); a timeout sets *errflag.
 // ---------------------------------------------------------------------------------------------
-template <typename A, int NB, int LINES, int NST>
+template <typename A, int NB, int LINES, int NST, int RW = 1>
 struct CbTmaSmem {
   static constexpr int NB2 = NB * NB, NB4 = NB2 * NB2;
   static constexpr int G = NB2 / 4, W = 32 / G;  // lanes per pair, slots (columns) per row block
-  static constexpr int FL = 8, NV = 2 * FL;      // lines per forward flush, reals per flush
+  static constexpr int FL = 8, NV = 2 * FL * RW; // lines per forward flush, reals per flush (all RHS)
   static constexpr int CPM = NB2 / LINES;        // chunks per matrix
   static constexpr int CPR = 2 * CPM;            // chunks per row block
   static constexpr size_t stage_bytes = (size_t)LINES * NB2 * W * sizeof(typename A::elem);
   static constexpr size_t red_bytes = (size_t)NV * 32 * sizeof(typename A::red_t);
-  static constexpr size_t row_bytes = (size_t)4 * NB2 * sizeof(typename A::relem);  // r_k, s_k, zeros
+  static constexpr size_t row_bytes = (size_t)4 * NB2 * RW * sizeof(typename A::relem);  // r_k, s_k, zeros
   static constexpr size_t warp_bytes = ((NST * stage_bytes + red_bytes + row_bytes + 8 * NST) + 127) / 128 * 128;
   static constexpr size_t cta_bytes = 4 * warp_bytes;
   static_assert(NB2 % 4 == 0 && (2 * NB2) % FL == 0 && FL % LINES == 0, "shape");
@@ -306,16 +314,21 @@ struct CbTmaSmem {
 // reducing lanes (one value each, all reading entry j of their row) hit distinct banks
 __device__ __forceinline__ int rsw(int v, int j) { return v * 32 + ((j + v) & 31); }
 
-// IMAG: the sums are multiplied by i before they are added (anti-Hermitian pass)
-template <typename A, int NB, int LINES, int NST, int MINB, bool IMAG>
+// IMAG: the sums are multiplied by i before they are added (anti-Hermitian pass).
+// Batched form (RW > 1 or nrhs > 1): nrhs states share P; a warp carries RW of them, so each
+// staged element feeds RW products. Warp w of the grid takes RHS group w % ngroups of work item
+// w / ngroups (the warps of a block share an item, so its P chunks come from HBM once and from L2
+// for the others). Coordinates of state q start at rs + q * rstride, its sums at acc + q * astride.
+template <typename A, int NB, int LINES, int NST, int MINB, bool IMAG, int RW = 1>
 __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __restrict__ items, int nitems,
                                                           const RowBlock* __restrict__ rbs,
                                                           const typename A::elem* __restrict__ P,
                                                           const typename A::relem* __restrict__ rs,
                                                           double* __restrict__ acc, int nk,
                                                           const unsigned int* __restrict__ gate,
-                                                          unsigned int* __restrict__ errflag) {
-  typedef CbTmaSmem<A, NB, LINES, NST> S;
+                                                          unsigned int* __restrict__ errflag, int nrhs = 1,
+                                                          size_t rstride = 0, size_t astride = 0) {
+  typedef CbTmaSmem<A, NB, LINES, NST, RW> S;
   constexpr int NB2 = S::NB2, NB4 = S::NB4, G = S::G, W = S::W, FL = S::FL, NV = S::NV;
   constexpr int CPM = S::CPM, CPR = S::CPR;
   constexpr size_t SE = S::stage_bytes / sizeof(typename A::elem);  // elements per stage
@@ -328,14 +341,18 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
   if (gate && *gate == 0u) return;  // anti-Hermitian pass with nothing to do
   const int wib = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  const int item = blockIdx.x * 4 + wib;
+  const int ngroups = (nrhs + RW - 1) / RW;
+  const int wg = blockIdx.x * 4 + wib;
+  const int item = wg / ngroups;
+  const int q0 = (wg % ngroups) * RW;  // first state of this warp
   if (item >= nitems) return;
-  const int qg = lane / W, sl = lane % W;  // quarter, slot
+  const int nq = nrhs - q0 < RW ? nrhs - q0 : RW;  // states carried (the last group may be short)
+  const int qg = lane / W, sl = lane % W;          // quarter, slot
   const int q4 = 4 * qg;
   unsigned char* wbase = smem_raw + (size_t)wib * S::warp_bytes;
   E* const stage0 = (E*)wbase;
   R* const red = (R*)(wbase + NST * S::stage_bytes);                  // [NV][32]
-  V* const rowv = (V*)(wbase + NST * S::stage_bytes + S::red_bytes);  // r_k[NB2], s_k[NB2], zeros[2 NB2]
+  V* const rowv = (V*)(wbase + NST * S::stage_bytes + S::red_bytes);  // [RW][r_k, s_k], then zeros
   uint64_t* const bar = (uint64_t*)(wbase + NST * S::stage_bytes + S::red_bytes + S::row_bytes);
   const WorkItem w = items[item];
   const int nrb = w.rb1 - w.rb0;  // <= kMaxRowBlocksPerItem = 32
@@ -371,26 +388,42 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
 #pragma unroll
   for (int c = 0; c < NST; ++c)
     if (c < nch) issue(c);
-  if (lane < 2 * NB2) rowv[2 * NB2 + lane] = V();
+  constexpr int RV = 2 * NB2 * RW;  // row coordinates of all carried states
+  for (int i = lane; i < RV; i += 32) rowv[RV + i] = V();
   const int col = w.J * W + sl;
   const bool colok = col < nk;
-  V rc[4], sc[4];  // r_col, s_col on this lane's quarter
+  V rc[4][RW], sc[4][RW];  // r_col, s_col on this lane's quarter, per state
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    rc[i] = colok ? rs[(size_t)col * 2 * NB2 + q4 + i] : V();
-    sc[i] = colok ? rs[(size_t)col * 2 * NB2 + NB2 + q4 + i] : V();
-  }
-  Acc rX[4], rY[4];
+  for (int u = 0; u < RW; ++u)
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    A::zero(rX[i]);
-    A::zero(rY[i]);
-  }
-  // coordinates of the first row
-  V rnext = V();
+    for (int i = 0; i < 4; ++i) {
+      const bool ok = colok && u < nq;
+      const V* rq = rs + (size_t)(q0 + u) * rstride + (size_t)col * 2 * NB2;
+      rc[i][u] = ok ? rq[q4 + i] : V();
+      sc[i][u] = ok ? rq[NB2 + q4 + i] : V();
+    }
+  Acc rX[4][RW], rY[4][RW];
+#pragma unroll
+  for (int u = 0; u < RW; ++u)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      A::zero(rX[i][u]);
+      A::zero(rY[i][u]);
+    }
+  // coordinates of the first row: element i of state u at rowv[u * 2 NB2 + i]
+  auto row_coord = [&](int row, int i) -> V {
+    const int u = i / (2 * NB2), e = i % (2 * NB2);
+    return u < nq ? rs[(size_t)(q0 + u) * rstride + (size_t)row * 2 * NB2 + e] : V();
+  };
+  constexpr int RPL = (RV + 31) / 32;  // row coordinates per lane
+  V rnext[RPL];
   {
     const int r0 = __shfl_sync(FULL, mine.row, 0);
-    if (lane < 2 * NB2 && nrb > 0) rnext = rs[(size_t)r0 * 2 * NB2 + lane];
+#pragma unroll
+    for (int t = 0; t < RPL; ++t) {
+      const int i = lane + 32 * t;
+      rnext[t] = (i < RV && nrb > 0) ? row_coord(r0, i) : V();
+    }
   }
   bool any_rev = false;
   int cfail = -1;
@@ -411,12 +444,16 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
     unsigned lm = 0;  // active lanes of the warp
 #pragma unroll
     for (int gg = 0; gg < G; ++gg) lm |= bmask << (gg * W);
-    if (lane < 2 * NB2) {
-      rowv[lane] = rnext;
-      if (rbi + 1 < nrb) rnext = rs[(size_t)nrow * 2 * NB2 + lane];
+#pragma unroll
+    for (int t = 0; t < RPL; ++t) {
+      const int i = lane + 32 * t;
+      if (i < RV) {
+        rowv[i] = rnext[t];
+        if (rbi + 1 < nrb) rnext[t] = row_coord(nrow, i);
+      }
     }
     __syncwarp();
-    const V* rv = rowv + (rev ? 0 : 2 * NB2);
+    const V* rv = rowv + (rev ? 0 : RV);
 #pragma unroll 1
     for (int q = 0; q < CPR; ++q) {
       const int c = rbi * CPR + q;
@@ -433,36 +470,46 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
 #pragma unroll
           for (int r = 0; r < LINES; ++r) {
             const int a = l0 + r;
-            const V ska = rv[NB2 + a];
-            Acc f;
+            Acc f[RW];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
               const E p1 = st[(r * NB2 + q4 + i) * n];
-              if (i == 0) A::mul(f, p1, rc[i]);
-              else A::mac(f, p1, rc[i]);
-              A::mac_cx(rY[i], p1, ska);
+#pragma unroll
+              for (int u = 0; u < RW; ++u) {
+                if (i == 0) A::mul(f[u], p1, rc[i][u]);
+                else A::mac(f[u], p1, rc[i][u]);
+                A::mac_cx(rY[i][u], p1, rv[u * 2 * NB2 + NB2 + a]);
+              }
             }
             const int v = 2 * ((q * LINES + r) % FL);
-            red[rsw(v, lane)] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
-            red[rsw(v + 1, lane)] = IMAG ? A::red_re(f) : A::red_im(f);
+#pragma unroll
+            for (int u = 0; u < RW; ++u) {
+              red[rsw(v * RW + 2 * u, lane)] = IMAG ? A::red_neg(A::red_im(f[u])) : A::red_re(f[u]);
+              red[rsw(v * RW + 2 * u + 1, lane)] = IMAG ? A::red_re(f[u]) : A::red_im(f[u]);
+            }
           }
         } else {
           // Q2 columns j: Y'_k[j] = sum_a Q2[a][j] s_c[a];  X'_c[a] += conj(Q2[a][j]) r_k[j]
 #pragma unroll
           for (int r = 0; r < LINES; ++r) {
             const int j = l0 + r;
-            const V rkj = rv[j];
-            Acc f;
+            Acc f[RW];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
               const E p2 = st[(r * NB2 + q4 + i) * n];
-              if (i == 0) A::mul(f, p2, sc[i]);
-              else A::mac(f, p2, sc[i]);
-              A::mac_cx(rX[i], p2, rkj);
+#pragma unroll
+              for (int u = 0; u < RW; ++u) {
+                if (i == 0) A::mul(f[u], p2, sc[i][u]);
+                else A::mac(f[u], p2, sc[i][u]);
+                A::mac_cx(rX[i][u], p2, rv[u * 2 * NB2 + j]);
+              }
             }
             const int v = 2 * ((q * LINES + r) % FL);
-            red[rsw(v, lane)] = IMAG ? A::red_neg(A::red_im(f)) : A::red_re(f);
-            red[rsw(v + 1, lane)] = IMAG ? A::red_re(f) : A::red_im(f);
+#pragma unroll
+            for (int u = 0; u < RW; ++u) {
+              red[rsw(v * RW + 2 * u, lane)] = IMAG ? A::red_neg(A::red_im(f[u])) : A::red_re(f[u]);
+              red[rsw(v * RW + 2 * u + 1, lane)] = IMAG ? A::red_re(f[u]) : A::red_im(f[u]);
+            }
           }
         }
       }
@@ -473,7 +520,8 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
       if (c + NST < nch) issue(c + NST);
       if (((q + 1) * LINES) % FL == 0) {
         // lines [L0, L0 + FL) of this row block are complete: reduce over the active lanes and add
-        // to the row's sums (line L is real pair 2L, 2L + 1 of [X'(NB2) | Y'(NB2)])
+        // to the row's sums (line L is real pair 2L, 2L + 1 of [X'(NB2) | Y'(NB2)]); buffer value
+        // v * RW + 2u + ri holds line v / 2 (of the flush), part ri, state u
         const int L0 = (q + 1) * LINES - FL;
         constexpr int LPV = 32 / NV > 0 ? 32 / NV : 1;
 #pragma unroll 1
@@ -492,7 +540,12 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
           }
 #pragma unroll
           for (int mm = 1; mm < LPV; mm <<= 1) A::red_add(sum, A::red_shfl_xor(sum, mm));
-          if (v < NV && part == 0) atomicAdd(acc + (size_t)brow * 4 * NB2 + 2 * L0 + v, A::red_to_double(sum));
+          if (v < NV && part == 0) {
+            const int line2 = v / (2 * RW), u = (v / 2) % RW, ri = v & 1;
+            if (u < nq)
+              atomicAdd(acc + (size_t)(q0 + u) * astride + (size_t)brow * 4 * NB2 + 2 * L0 + 2 * line2 + ri,
+                        A::red_to_double(sum));
+          }
         }
         __syncwarp();
       }
@@ -500,10 +553,12 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
     if (cfail >= 0) break;
     // keep the low parts of the reverse sums small (each took NB2 products in this row block)
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      A::renorm(rX[i]);
-      A::renorm(rY[i]);
-    }
+    for (int u = 0; u < RW; ++u)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        A::renorm(rX[i][u]);
+        A::renorm(rY[i][u]);
+      }
   }
   if (cfail >= 0) {  // drain the copies still in flight (bounded), then leave
     if (lane == 0) {
@@ -514,14 +569,18 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
     return;
   }
   if (colok && any_rev) {
-    double* dst = acc + (size_t)col * 4 * NB2;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const double xr = A::re_d(rX[i]), xi = A::im_d(rX[i]), yr = A::re_d(rY[i]), yi = A::im_d(rY[i]);
-      atomicAdd(dst + 2 * (q4 + i), IMAG ? -xi : xr);
-      atomicAdd(dst + 2 * (q4 + i) + 1, IMAG ? xr : xi);
-      atomicAdd(dst + 2 * NB2 + 2 * (q4 + i), IMAG ? -yi : yr);
-      atomicAdd(dst + 2 * NB2 + 2 * (q4 + i) + 1, IMAG ? yr : yi);
+    for (int u = 0; u < RW; ++u) {
+      if (u >= nq) break;
+      double* dst = acc + (size_t)(q0 + u) * astride + (size_t)col * 4 * NB2;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const double xr = A::re_d(rX[i][u]), xi = A::im_d(rX[i][u]), yr = A::re_d(rY[i][u]), yi = A::im_d(rY[i][u]);
+        atomicAdd(dst + 2 * (q4 + i), IMAG ? -xi : xr);
+        atomicAdd(dst + 2 * (q4 + i) + 1, IMAG ? xr : xi);
+        atomicAdd(dst + 2 * NB2 + 2 * (q4 + i), IMAG ? -yi : yr);
+        atomicAdd(dst + 2 * NB2 + 2 * (q4 + i) + 1, IMAG ? yr : yi);
+      }
     }
   }
 }

@@ -33,7 +33,7 @@ class _Desc(C.Structure):
                 ("k2nd", C.c_void_p), ("P1", C.c_void_p), ("P2", C.c_void_p), ("P1_add", C.c_void_p),
                 ("P2_add", C.c_void_p), ("add_scale", C.c_double), ("Hcoh", C.c_void_p), ("picture", C.c_int32),
                 ("expt", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32),
-                ("f_ref", C.c_void_p)]
+                ("f_ref", C.c_void_p), ("nrhs", C.c_int32), ("reserved", C.c_int32)]
 
 
 _L = None
@@ -42,7 +42,7 @@ EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_s
            "dmd_evolve_driver", "dmd_evolve_coh", "dmd_set_state", "dmd_get_state", "dmd_rk4", "dmd_euler",
            "dmd_rkf45_apply", "dmd_set_observable", "dmd_measure", "dmd_launch_count", "dmd_sync",
            "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
-           "dmd_evolve_driver_noalloc"]
+           "dmd_evolve_driver_noalloc", "dmd_measure_batch"]
 
 
 def _lib():
@@ -69,6 +69,7 @@ def _lib():
         L.dmd_euler.argtypes = [vp, d, i64]
         L.dmd_rkf45_apply.argtypes = [vp, d, C.POINTER(d), d, d, d, d, C.POINTER(i64)]
         L.dmd_set_observable.argtypes = [vp, C.c_int, vp, vp, d]
+        L.dmd_measure_batch.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp]
         L.dmd_measure.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(d), C.POINTER(d)]
         L.dmd_launch_count.argtypes = [vp, C.POINTER(i64)]
         L.dmd_sync.argtypes = [vp]
@@ -92,7 +93,7 @@ class LindbladGPU:
 
     def __init__(self, *, nk, nb_dm, bstart, bend, e_dm, k1st, k2nd, P1, P2, prefac_eph, Hcoh=None,
                  picture="interaction", expt=1, precision="f64", P1_add=None, P2_add=None, add_scale=0.0, device=0,
-                 f_ref=None, linear=False):
+                 f_ref=None, linear=False, nrhs=1):
         L = _lib()
         self._keep = dict(e=_c(e_dm, np.float64), k1=_c(k1st, np.uint64), k2=_c(k2nd, np.uint64),
                           P1=_c(P1, np.complex128), P2=_c(P2, np.complex128), H=_c(Hcoh, np.complex128),
@@ -104,15 +105,15 @@ class LindbladGPU:
                      P1_add=ptr(k["A1"]), P2_add=ptr(k["A2"]), add_scale=add_scale, Hcoh=ptr(k["H"]),
                      picture=PICTURE[picture] if isinstance(picture, str) else int(picture), expt=int(expt),
                      precision=PREC[precision] if isinstance(precision, str) else int(precision), device=device,
-                     flags=FLAG_LINEAR if linear else 0, f_ref=ptr(k["f"]))
+                     flags=FLAG_LINEAR if linear else 0, f_ref=ptr(k["f"]), nrhs=int(nrhs))
         h = C.c_void_p()
         st = L.dmd_create(C.byref(desc), C.byref(h))
         if st != 0:
             raise DMDError(st, "dmd_create failed")
         self._h = h
         self._keep = None  # the library copied everything it needs
-        self.nk, self.nb_dm = nk, nb_dm
-        self.ny = 2 * nk * nb_dm * nb_dm
+        self.nk, self.nb_dm, self.nrhs = nk, nb_dm, max(1, int(nrhs))
+        self.ny = 2 * nk * nb_dm * nb_dm * self.nrhs
 
     # ------------------------------------------------------------------ plumbing
     def _ck(self, st):
@@ -195,6 +196,13 @@ class LindbladGPU:
         o = np.ascontiguousarray(obs, dtype=np.complex128)
         ff = np.ascontiguousarray(f, dtype=np.float64)
         self._ck(_lib().dmd_set_observable(self._h, slot, o.ctypes.data, ff.ctypes.data, float(prefac)))
+
+    def measure_batch(self, slot=0, bstart=0, bend=None):
+        """Totals of every state of a batched handle: arrays (tot, tot_amp) of nrhs values."""
+        bend = self.nb_dm if bend is None else bend
+        a, b = np.zeros(self.nrhs), np.zeros(self.nrhs)
+        self._ck(_lib().dmd_measure_batch(self._h, slot, bstart, bend, a.ctypes.data, b.ctypes.data))
+        return a, b
 
     def measure(self, slot=0, bstart=0, bend=None):
         bend = self.nb_dm if bend is None else bend

@@ -87,6 +87,10 @@ typedef struct dmd_desc {
   const double* f_ref;   /* optional [nk][nb_dm] reference occupations (e.g. f_dm) of the reduced-
                             precision forms: the contraction of diag(f_ref) is formed once in FP64 at
                             dmd_create and each evaluation contracts only rho - diag(f_ref) in FP32 */
+  int32_t nrhs;          /* batched form: states that share P (0 or 1: a single state). With nrhs > 1 the
+                            state of every call is nrhs consecutive [nk][nb_dm^2] states, stepped
+                            together; precision DMD_PREC_F32 or DMD_PREC_BF16X2, nb = 2 or 4 */
+  int32_t reserved;
 } dmd_desc;
 
 int dmd_create(const dmd_desc* desc, dmd_handle** out);
@@ -117,6 +121,8 @@ int dmd_rkf45_apply(dmd_handle* h, double t1, double* hstep, double hmin, double
  * bands [bstart, bend) of the density matrix. */
 int dmd_set_observable(dmd_handle* h, int slot, const double* obs, const double* f, double prefac);
 int dmd_measure(dmd_handle* h, int slot, int bstart, int bend, double* tot, double* tot_amp);
+/* batched form: the totals of every state (tot, tot_amp: nrhs doubles each) */
+int dmd_measure_batch(dmd_handle* h, int slot, int bstart, int bend, double* tot, double* tot_amp);
 
 /* counters: kernel launches issued by this handle since creation */
 int dmd_launch_count(const dmd_handle* h, int64_t* launches);

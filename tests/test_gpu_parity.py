@@ -270,13 +270,13 @@ def test_non_hermitian_state_vs_oracle(prec, oracle, built):
 LOWP_TOL = {"f32": 1e-6, "bf16x2": 1e-5}
 
 
-def make_gpu_lowp(s, prec, with_ref=True):
+def make_gpu_lowp(s, prec, with_ref=True, nrhs=1):
     from denmat_dynm_development_gb300.dmd import LindbladGPU
     lin = bool(getattr(s, "linear", False))
     g = LindbladGPU(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
                     P1=s.P1, P2=s.P2, prefac_eph=s.prefac_eph, Hcoh=s.Hcoh, picture=s.picture_schrodinger,
                     expt=s.expt, precision=prec, linear=lin,
-                    f_ref=s.f_eq if lin else (s.f_dm if with_ref else None))
+                    f_ref=s.f_eq if lin else (s.f_dm if with_ref else None), nrhs=nrhs)
     if getattr(s, "ddmdt_eq", None) is not None:
         g.set_ddmdt_eq(s.ddmdt_eq)
     return g
@@ -327,3 +327,49 @@ def test_lowp_t1_vs_oracle(prec, oracle, built):
     et = abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq)
     print("%s: S(t) rel err %.3g, T1 %.10g vs %.10g ps, rel err %.3g" % (prec, es, fg.tau_lsq, fo.tau_lsq, et))
     assert et < 1e-4
+
+
+def _herm_states(s, n, seed, scale=1e-3):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        d = s.dm0 + scale * (rng.standard_normal(s.dm0.shape) + 1j * rng.standard_normal(s.dm0.shape))
+        d = d.reshape(s.nk, s.nb_dm, s.nb_dm)
+        d = 0.5 * (d + np.conj(np.swapaxes(d, 1, 2)))
+        out.append(np.ascontiguousarray(d.reshape(s.nk, -1)).view(np.float64).reshape(-1))
+    return out
+
+
+@pytest.mark.parametrize("prec", ["f32", "bf16x2"])
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb4_eimp_B", "nb2_linear", "nb2_carrier_eq"])
+def test_batched_states_vs_oracle(case, prec, oracle, built):
+    """Batched form: 7 states share P (RW states per warp, the last group short); every state's
+    RHS matches the oracle at the reduced-precision tolerance, and 20 RK4 steps of the batch match
+    the same steps of each state alone."""
+    s = oracle.load(os.path.join(GOLDEN, case))
+    R = 7
+    ys = _herm_states(s, R, 31)
+    t = 41.0 * oracle.fs
+    with make_gpu_lowp(s, prec, nrhs=R) as gb:
+        out = gb.func(t, np.concatenate(ys)).reshape(R, -1)
+        for q in range(R):
+            e = rel(out[q], oracle.rhs(s, t, ys[q]))
+            assert e < LOWP_TOL[prec], (q, e)
+        gb.set_state(s.t0, np.concatenate(ys))
+        gb.rk4(2.0 * oracle.fs, 20)
+        _, yb = gb.get_state()
+        yb = yb.reshape(R, -1)
+        if s.nb_dm * s.nb_dm * s.nk > 0:
+            gb.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+            tot, _ = gb.measure_batch(0, s.nv_dm)
+    for q in (0, 3, R - 1):
+        with make_gpu_lowp(s, prec) as g1:
+            g1.set_state(s.t0, ys[q])
+            g1.rk4(2.0 * oracle.fs, 20)
+            _, y1 = g1.get_state()
+            g1.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+            t1, _ = g1.measure(0, s.nv_dm)
+        # the batch and the single state sum in different atomic orders: FP32-level differences of
+        # the RHS, integrated over 20 steps
+        assert rel(yb[q], y1) < 1e-10
+        assert abs(tot[q] - t1) <= 1e-5 * abs(t1)
