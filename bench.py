@@ -268,7 +268,8 @@ def run_gpu_batched(args, w):
     st = w["st"]
     nb = st.cfg.nb
     R = args.nrhs
-    prec = args.precision if args.precision in ("f32", "bf16x2") else "f32"
+    prec = args.precision if args.precision in ("f32", "bf16x2") else "bf16x2"
+    tc = prec == "bf16x2" and nb == 2 and os.environ.get("DMD_BATCH_TC", "1") != "0"
     g = LindbladGPU(nk=st.cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=w["e"], k1st=st.k1, k2nd=st.k2, P1=w["P1"],
                     P2=w["P2"], prefac_eph=w["prefac"], picture=0, expt=1, precision=prec, f_ref=w["f"], nrhs=R)
     h = 1.0 * U.fs
@@ -288,21 +289,33 @@ def run_gpu_batched(args, w):
     g.rk4(h, 2)
     pair_ms, pair_n = g.profile(1)
     g.set_profiling(False)
+    pbytes = g.pair_bytes
     g.close()
     ms_per_step = ms / args.steps
     peak, peak_kind = measured_peak()
-    bpl = algorithmic_bytes(nb, st.npair, st.cfg.nk, ELEM_BYTES[prec]) + (R - 1) * st.cfg.nk * nb * nb * 16 * 2
     pair_avg = pair_ms / max(pair_n, 1)
-    flops = 2.0 * 4 * nb ** 4 * 2 * st.npair * R  # complex x real products of the four sums, per RHS evaluation
+    nk = st.cfg.nk
+    if tc:
+        # per contraction (packing + Hermitian pass): operator blocks once from HBM, coordinates in
+        # (FP32) and as bf16 hi + lo blocks out and back in, the sums out
+        nmb = (R + 127) // 128
+        ngroups = (nk + 7) // 8
+        bpl = pbytes + R * nk * 8 * 4 + 2 * ngroups * nmb * 32768 + R * nk * 8 * 16
+        flops = (pbytes / 32768) * nmb * 12 * 2.0 * 128 * 128 * 16  # issued MMA flops (padding included)
+        kernel, bound = "tensor-core batched k-pair contraction (tcgen05, bf16 hi+lo)", "hbm"
+    else:
+        bpl = algorithmic_bytes(nb, st.npair, nk, ELEM_BYTES[prec]) + (R - 1) * nk * nb * nb * 16 * 2
+        flops = 2.0 * 4 * nb ** 4 * 2 * st.npair * R  # complex x real products of the four sums, per RHS evaluation
+        kernel, bound = "batched k-pair contraction (CUDA cores)", "fp32-issue"
     line = {"metric": "ensemble RK4 steps/s (%d states sharing P, batched form)" % R, "value": R * 1e3 / ms_per_step,
             "unit": "state-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": prec + " (rho as deviation from f)", "data": "synthetic",
-            "config": config_of(w, {"precision": prec, "nrhs": R,
+            "config": config_of(w, {"precision": prec, "nrhs": R, "tensor_cores": tc,
                                     "states": "spin polarisation along x/y/z in turn + random 1e-4 deviation"}),
-            "roofline": {"bound": "fp32-issue", "achieved": bpl / (pair_avg * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+            "roofline": {"bound": bound, "achieved": bpl / (pair_avg * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": bpl / (pair_avg * 1e-3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
-                         "kernel": "batched k-pair contraction", "avg_launch_ms": pair_avg,
+                         "kernel": kernel, "avg_launch_ms": pair_avg, "pair_bytes": pbytes,
                          "tflops": flops / (pair_avg * 1e-3) / 1e12},
             "clocks": clocks, "gpu_launches": launches}
     print(json.dumps(line))

@@ -58,7 +58,7 @@ def build_gpu(force=False, verbose=False):
             if verbose:
                 sys.stderr.write(p.stderr)
     tmp = GPU_LIB + ".tmp"
-    _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs)
+    _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
     os.replace(tmp, GPU_LIB)
     return GPU_LIB
 

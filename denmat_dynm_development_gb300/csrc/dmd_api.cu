@@ -4,9 +4,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
+#include "dmd_batched_tc.cuh"
 #include "dmd_gpu.h"
 #include "dmd_kernels.cuh"
 #include "dmd_layout.h"
@@ -44,6 +48,13 @@ struct dmd_handle {
   unsigned int* d_hflag = nullptr;  // set by the prep kernel when a state is not exactly Hermitian
   double2* d_acc0 = nullptr;   // deviation form: contraction of diag(f_ref), position order [nk][2][nb2]
   double* d_fref = nullptr;    // deviation form: window occupations [nk][nb]
+  // batched form on the tensor cores (nb = 2, bf16 hi + lo): operator and coordinate blocks
+  int use_tc = 0;
+  uint16_t* d_tcB = nullptr;   // [blocks][4 planes][128 x 32] bf16, per tile its column groups
+  uint16_t* d_tcA = nullptr;   // [part][group][state block][4 planes][128 x 32] bf16
+  dmd::TcTile* d_tiles = nullptr;
+  int ntiles = 0, ngroups = 0, nmb = 0;
+  int64_t pair_bytes = 0;      // stored operator bytes (dmd_pair_bytes)
   double2* d_H = nullptr;      // [nk][nbdm^2]
   double2* d_eq = nullptr;     // [nk][nb2]
   double2* d_rs = nullptr;     // [nk][2][nb2] (per-thread form); Hermitian + anti-Hermitian coordinates (column-block form)
@@ -226,6 +237,24 @@ cudaError_t herm_pair_attrs() {
   return e;
 }
 
+// tensor-core batched form: pack the coordinates, then the Hermitian pass and the gated
+// anti-Hermitian pass (dmd_batched_tc.cuh)
+void tc_launches(dmd_handle* h, size_t half) {
+  const size_t per = (size_t)h->nrhs * h->nk * 8;
+  k_pack_tc<<<dim3(blocks_for((long long)per, 256), 2), 256, 0, h->st>>>(h->nk, h->nrhs, h->ngroups, h->nmb,
+                                                                         (const float*)h->d_rs, h->d_tcA, h->d_hflag);
+  const size_t smem = (size_t)TC_NST * 2 * TC_BLOCK_BYTES + 128;
+  const size_t apart = (size_t)h->ngroups * h->nmb * TC_BLOCK;
+  const size_t astride = (size_t)h->nk * 2 * h->nb2;
+  const unsigned g = (unsigned)((size_t)h->ntiles * h->nmb);
+  k_pairs_tc<false><<<g, 128, smem, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA, h->nmb, h->nrhs, h->nk,
+                                             h->d_acc0, h->d_acc, astride, nullptr, h->d_err);
+  k_pairs_tc<true><<<g, 128, smem, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA + apart, h->nmb, h->nrhs, h->nk,
+                                            nullptr, h->d_acc, astride, h->d_hflag, h->d_err);
+  (void)half;
+  h->launches += 1;  // the packing launch; the two passes are counted with the other forms
+}
+
 template <int NB>
 int launch_pairs(dmd_handle* h) {
   if (h->npair == 0) return DMD_OK;
@@ -238,7 +267,9 @@ int launch_pairs(dmd_handle* h) {
       // Hermitian coordinates; the second launch carries the anti-Hermitian part of a state that is
       // not exactly Hermitian and returns at once unless the prep kernel raised d_hflag
       const size_t half = (size_t)h->nk * 2 * h->nb2 * h->nrhs;  // coordinates per part
-      if (h->nrhs > 1) {  // batched form: reduced-precision arithmetics only (dmd_create)
+      if (h->use_tc) {
+        tc_launches(h, half);
+      } else if (h->nrhs > 1) {  // batched form: reduced-precision arithmetics only (dmd_create)
         const float* rs = (const float*)h->d_rs;
         if (h->prec == DMD_PREC_BF16X2) herm_pair_launches<ArithBF2, NB, 4, 2, 2, 4>(h, rs, half);
         else if (h->brw == 8) herm_pair_launches<ArithF32, NB, 4, 2, 2, 8>(h, rs, half);
@@ -630,13 +661,210 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
   return out;
 }
 
+// Effective P1, P2 of stored pair src in its given orientation (k1 <- k2): folded with the additive
+// operators (ElectronImpurity.cpp:38-39, ElectronPhonon.cpp:96-97); the linearized form carries
+// conj(Lji) in the P2 slot (the reverse operator, see dmd_pairs_cb.cuh)
+void pair_operators(const dmd_handle* h, const dmd_desc* d, size_t src, cd* P1, cd* P2) {
+  const int nb4 = h->nb4;
+  for (int m = 0; m < 2; ++m) {
+    const double* sp = (m == 0 ? d->P1 : d->P2) + 2 * src * nb4;
+    const double* ap = (m == 0 ? d->P1_add : d->P2_add);
+    cd* out = m == 0 ? P1 : P2;
+    for (int e = 0; e < nb4; ++e) {
+      double x = sp[2 * e], yv = sp[2 * e + 1];
+      if (ap) {
+        x = x + ap[2 * src * nb4 + 2 * e] * d->add_scale;
+        yv = yv + ap[2 * src * nb4 + 2 * e + 1] * d->add_scale;
+      }
+      if (h->lin && m == 1) yv = -yv;
+      out[e] = {x, yv};
+    }
+  }
+}
+
+// Tensor-core batched form (nb = 2, dmd_batched_tc.cuh): every stored pair becomes the directed
+// operators (k1 <- k2): A = Q1, B = Q2 and, with the reverse term (k1 < k2, evolve_eph.cpp:101),
+// (k2 <- k1): A = conj(Q2), B = conj(Q1). They are bucketed by the row tile of their target
+// (16 energy ranks); a tile's column groups (8 ranks) between the first and the last it touches form
+// dense blocks laid out as the MMA reads them, split into bf16 hi + lo. Tiles are built on host threads.
+int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
+  const int nb = h->nb, nk = h->nk;
+  std::vector<double> ew((size_t)nk * nb);
+  for (int k = 0; k < nk; ++k)
+    for (int b = 0; b < nb; ++b) ew[(size_t)k * nb + b] = d->e_dm[(size_t)k * h->nbdm + h->bs + b];
+  dmd::PairLayout L;  // only the energy ranks are used
+  if (!dmd::build_pair_layout(nk, nb, ew.data(), h->npair, d->k1st, d->k2nd, 512, 32, L))
+    return fail(h, DMD_E_ARG, "k-pair index out of range");
+  L.rb.clear();
+  L.items.clear();
+  L.src.clear();
+  const size_t smem = (size_t)TC_NST * 2 * TC_BLOCK_BYTES + 128;
+  CK(cudaFuncSetAttribute(k_pairs_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  CK(cudaFuncSetAttribute(k_pairs_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  h->ntiles = (nk + TC_TR - 1) / TC_TR;
+  h->ngroups = (nk + TC_CG - 1) / TC_CG;
+  h->nmb = (h->nrhs + TC_M - 1) / TC_M;
+  int rc;
+  if ((rc = dalloc(h, &h->d_pos, (size_t)nk))) return rc;
+  CK(cudaMemcpy(h->d_pos, L.pos.data(), (size_t)nk * 4, cudaMemcpyHostToDevice));
+  // directed entries (src << 1 | reverse) bucketed by row tile
+  const size_t np = (size_t)h->npair;
+  std::vector<size_t> start((size_t)h->ntiles + 1, 0);
+  auto row_of = [&](size_t src, int dir) { return L.pos[dir ? d->k2nd[src] : d->k1st[src]]; };
+  auto col_of = [&](size_t src, int dir) { return L.pos[dir ? d->k1st[src] : d->k2nd[src]]; };
+  for (size_t p = 0; p < np; ++p) {
+    start[row_of(p, 0) / TC_TR + 1]++;
+    if (d->k1st[p] < d->k2nd[p]) start[row_of(p, 1) / TC_TR + 1]++;
+  }
+  for (int t = 0; t < h->ntiles; ++t) start[t + 1] += start[t];
+  std::vector<uint64_t> ent(start[h->ntiles]);
+  {
+    std::vector<size_t> fill(start.begin(), start.end() - 1);
+    for (size_t p = 0; p < np; ++p) {
+      ent[fill[row_of(p, 0) / TC_TR]++] = (uint64_t)p << 1;
+      if (d->k1st[p] < d->k2nd[p]) ent[fill[row_of(p, 1) / TC_TR]++] = ((uint64_t)p << 1) | 1u;
+    }
+  }
+  std::vector<TcTile> tiles(h->ntiles);
+  int64_t nblocks = 0;
+  for (int t = 0; t < h->ntiles; ++t) {
+    int gmin = INT32_MAX, gmax = -1;
+    for (size_t e = start[t]; e < start[t + 1]; ++e) {
+      const int g = col_of(ent[e] >> 1, (int)(ent[e] & 1)) / TC_CG;
+      gmin = std::min(gmin, g);
+      gmax = std::max(gmax, g);
+    }
+    tiles[t].boff = nblocks;
+    if (gmax < 0) {
+      tiles[t].g0 = tiles[t].g1 = 0;
+    } else {
+      tiles[t].g0 = gmin;
+      tiles[t].g1 = gmax + 1;
+      nblocks += gmax + 1 - gmin;
+    }
+  }
+  if ((rc = dalloc(h, &h->d_tiles, tiles.size())) || (rc = dalloc(h, &h->d_tcB, (size_t)nblocks * TC_BLOCK)) ||
+      (rc = dalloc(h, &h->d_tcA, (size_t)2 * h->ngroups * h->nmb * TC_BLOCK)))
+    return rc;
+  CK(cudaMemcpy(h->d_tiles, tiles.data(), tiles.size() * sizeof(TcTile), cudaMemcpyHostToDevice));
+  h->pair_bytes = nblocks * (int64_t)TC_BLOCK_BYTES;
+  CK(cudaMemset(h->d_tcA, 0, (size_t)2 * h->ngroups * h->nmb * TC_BLOCK * 2));
+  // deviation form: acc0 = contraction of diag(f_ref) in FP64, position order [nk][2][nb2]
+  const bool dev = deviation_form(h->prec) && !h->lin;
+  std::vector<double> fw;
+  std::vector<cd> acc0;
+  if (dev || h->lin) {
+    fw.assign((size_t)nk * nb, 0.0);
+    if (d->f_ref)
+      for (int k = 0; k < nk; ++k)
+        for (int b = 0; b < nb; ++b) fw[(size_t)k * nb + b] = d->f_ref[(size_t)k * h->nbdm + h->bs + b];
+    if (dev) acc0.assign((size_t)nk * 2 * h->nb2, cd{0, 0});
+  }
+  // tiles in chunks of at most kChunk blocks (one tile at least), one pinned staging buffer
+  const int64_t kChunk = 1024;
+  int64_t maxb = kChunk;
+  for (const TcTile& tl : tiles) maxb = std::max<int64_t>(maxb, tl.g1 - tl.g0);
+  uint16_t* stage = nullptr;
+  CK(cudaMallocHost((void**)&stage, (size_t)maxb * TC_BLOCK * 2));
+  unsigned nthr = std::thread::hardware_concurrency();
+  nthr = nthr < 1 ? 1 : (nthr > 32 ? 32 : nthr);
+  int out = DMD_OK;
+  const int n2 = h->nb2;
+  for (int t0 = 0; t0 < h->ntiles && out == DMD_OK;) {
+    int t1 = t0;
+    int64_t nb_chunk = 0;
+    while (t1 < h->ntiles && (t1 == t0 || nb_chunk + (tiles[t1].g1 - tiles[t1].g0) <= maxb)) {
+      nb_chunk += tiles[t1].g1 - tiles[t1].g0;
+      ++t1;
+    }
+    const int64_t b0 = tiles[t0].boff;
+    std::atomic<int> next(t0);
+    auto work = [&]() {
+      std::vector<double> f64;
+      cd P1[16], P2[16], Q1[16], Q2[16], A[16], Bm[16];
+      for (int t; (t = next.fetch_add(1)) < t1;) {
+        const TcTile& tl = tiles[t];
+        const int nblk = tl.g1 - tl.g0;
+        if (nblk == 0) continue;
+        f64.assign((size_t)nblk * 2 * TC_N * TC_K, 0.0);  // [block][X|Y][n][kk]
+        for (size_t e = start[t]; e < start[t + 1]; ++e) {
+          const size_t src = ent[e] >> 1;
+          const int dir = (int)(ent[e] & 1);
+          pair_operators(h, d, src, P1, P2);
+          herm_transform(nb, P1, P2, Q1, Q2);
+          for (int i = 0; i < 16; ++i) {
+            A[i] = dir ? cd{Q2[i].re, -Q2[i].im} : Q1[i];
+            Bm[i] = dir ? cd{Q1[i].re, -Q1[i].im} : Q2[i];
+          }
+          const int rp = row_of(src, dir), cp = col_of(src, dir);
+          const int r = rp - t * TC_TR, blk = cp / TC_CG - tl.g0, c = cp % TC_CG;
+          double* fx = &f64[(size_t)blk * 2 * TC_N * TC_K];
+          double* fy = fx + TC_N * TC_K;
+          for (int a = 0; a < n2; ++a)
+            for (int j = 0; j < n2; ++j) {
+              // X'_row[a] += A[a][j] r_col[j]: n = (r, a, re|im), kk = (c, j)
+              const cd x = A[a * n2 + j];
+              fx[((r * n2 + a) * 2) * TC_K + c * n2 + j] += x.re;
+              fx[((r * n2 + a) * 2 + 1) * TC_K + c * n2 + j] += x.im;
+              // Y'_row[j] += B[a][j] s_col[a]: n = (r, j, re|im), kk = (c, a)
+              const cd y = Bm[a * n2 + j];
+              fy[((r * n2 + j) * 2) * TC_K + c * n2 + a] += y.re;
+              fy[((r * n2 + j) * 2 + 1) * TC_K + c * n2 + a] += y.im;
+            }
+          if (dev) {  // what the contraction adds for diag(f_ref) of the column (see k_prep_herm)
+            const uint64_t kc = dir ? d->k1st[src] : d->k2nd[src];
+            cd* ar = &acc0[(size_t)rp * 2 * n2];
+            for (int a = 0; a < n2; ++a)
+              for (int i = 0; i < nb; ++i) {
+                const int ii = i * nb + i;
+                const double fc = fw[kc * nb + i];
+                ar[a].re += A[a * n2 + ii].re * fc;
+                ar[a].im += A[a * n2 + ii].im * fc;
+                ar[n2 + a].re += Bm[ii * n2 + a].re * (1 - fc);
+                ar[n2 + a].im += Bm[ii * n2 + a].im * (1 - fc);
+              }
+          }
+        }
+        uint16_t* dst0 = stage + (size_t)(tl.boff - b0) * TC_BLOCK;
+        for (int blk = 0; blk < nblk; ++blk)
+          for (int m = 0; m < 2; ++m)
+            for (int n = 0; n < TC_N; ++n)
+              for (int kk = 0; kk < TC_K; ++kk) {
+                const uint32_t w = pack_bf2(f64[(((size_t)blk * 2 + m) * TC_N + n) * TC_K + kk]);
+                uint16_t* pl = dst0 + (size_t)blk * TC_BLOCK + (size_t)m * 2 * TC_PLANE;
+                pl[tc_ci(n, kk)] = (uint16_t)(w >> 16);
+                pl[TC_PLANE + tc_ci(n, kk)] = (uint16_t)(w & 0xffffu);
+              }
+      }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned i = 1; i < nthr; ++i) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    cudaError_t e = cudaMemcpy(h->d_tcB + (size_t)b0 * TC_BLOCK, stage, (size_t)nb_chunk * TC_BLOCK * 2,
+                               cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) out = fail(h, DMD_E_CUDA, std::string("operator upload: ") + cudaGetErrorString(e));
+    t0 = t1;
+  }
+  cudaFreeHost(stage);
+  if (out == DMD_OK && (dev || h->lin)) {
+    if ((out = dalloc(h, &h->d_fref, fw.size()))) return out;
+    CK(cudaMemcpy(h->d_fref, fw.data(), fw.size() * 8, cudaMemcpyHostToDevice));
+  }
+  if (out == DMD_OK && dev) {
+    if ((out = dalloc(h, &h->d_acc0, acc0.size()))) return out;
+    CK(cudaMemcpy(h->d_acc0, acc0.data(), acc0.size() * 16, cudaMemcpyHostToDevice));
+  }
+  return out;
+}
+
 void release(dmd_handle* h) {
   if (!h) return;
   cudaSetDevice(h->dev);
   if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
   void* ptrs[] = {h->d_err, h->d_pos, h->d_rb, h->d_items, h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
-                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref};
+                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -727,6 +955,12 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   h->nstate1 = (size_t)h->nk * h->nbdm * h->nbdm;
   h->nstate = h->nstate1 * nrhs;
   if (const char* v = getenv("DMD_BATCH_RW")) h->brw = atoi(v) == 8 ? 8 : 4;
+  // batched bf16 hi + lo form with nb = 2: the tensor-core contraction (DMD_BATCH_TC=0 keeps the
+  // CUDA-core column-block form)
+  {
+    const char* v = getenv("DMD_BATCH_TC");
+    h->use_tc = (nrhs > 1 && h->nb == 2 && h->npair > 0 && h->prec == DMD_PREC_BF16X2 && !(v && atoi(v) == 0)) ? 1 : 0;
+  }
   int rc = DMD_OK;
   auto bail = [&](int code) {
     std::string m = h->err;
@@ -740,7 +974,7 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   const size_t nk = h->nk, nbdm = h->nbdm;
   if ((rc = dalloc(h, &h->d_ew, nk * h->nb)) || (rc = dalloc(h, &h->d_edm, nk * nbdm)) ||
       (rc = dalloc(h, &h->d_kk, (h->nb == 2 || h->nb == 4) ? 1 : (size_t)h->npair)) ||
-      (rc = dalloc(h, &h->d_P, ((size_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) + 15) / 16)) ||
+      (rc = dalloc(h, &h->d_P, h->use_tc ? 1 : ((size_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) + 15) / 16)) ||
       (rc = dalloc(h, &h->d_rs, nk * 2 * h->nb2 * nrhs)) || (rc = dalloc(h, &h->d_acc, nk * 2 * h->nb2 * nrhs)) ||
       (rc = dalloc(h, &h->d_y, h->nstate)) || (rc = dalloc(h, &h->d_ytmp, h->nstate)) ||
       (rc = dalloc(h, &h->d_y0, h->nstate)) || (rc = dalloc(h, &h->d_in, h->nstate)) ||
@@ -762,7 +996,10 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
       return bail(fail(h, DMD_E_CUDA, "upload H"));
   }
   h->use_cb = ((h->nb == 2 || h->nb == 4) && h->npair > 0) ? 1 : 0;
-  if ((rc = h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d))) return bail(rc);
+  if (!h->use_tc)
+    h->pair_bytes = h->use_cb ? (int64_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) : (int64_t)h->npair * 2 * h->nb4 * 16;
+  if ((rc = h->use_tc ? upload_pairs_tc(h, d) : h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d)))
+    return bail(rc);
   if (cudaMemset(h->d_y, 0, h->nstate * 16) != cudaSuccess || cudaMemset(h->d_step, 0, 8) != cudaSuccess ||
       cudaMemset(h->d_err, 0, sizeof(unsigned int)) != cudaSuccess ||
       cudaMemset(h->d_hflag, 0, sizeof(unsigned int)) != cudaSuccess)
@@ -921,7 +1158,7 @@ int dmd_rk4(dmd_handle* h, double dt, int64_t nsteps) {
     if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     h->launches = l0;  // captured launches are counted when the graph runs
   }
-  const long long per_step = h->npair ? (h->use_cb ? 17 : 13) : 9;
+  const long long per_step = h->npair ? (h->use_tc ? 21 : h->use_cb ? 17 : 13) : 9;
   for (int64_t s = 0; s < nsteps; ++s) {
     CK(cudaGraphLaunch(h->g_rk4, h->st));
     h->launches += per_step;
@@ -1156,6 +1393,12 @@ int dmd_measure_batch(dmd_handle* h, int slot, int bstart, int bend, double* tot
     if (tot) tot[q] = s1 * h->obs_prefac[slot];
     if (tot_amp) tot_amp[q] = s2 * h->obs_prefac[slot];
   }
+  return DMD_OK;
+}
+
+int dmd_pair_bytes(const dmd_handle* h, int64_t* n) {
+  if (!h || !n) return DMD_E_ARG;
+  *n = h->pair_bytes;
   return DMD_OK;
 }
 

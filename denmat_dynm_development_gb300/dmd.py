@@ -42,7 +42,7 @@ EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_s
            "dmd_evolve_driver", "dmd_evolve_coh", "dmd_set_state", "dmd_get_state", "dmd_rk4", "dmd_euler",
            "dmd_rkf45_apply", "dmd_set_observable", "dmd_measure", "dmd_launch_count", "dmd_sync",
            "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
-           "dmd_evolve_driver_noalloc", "dmd_measure_batch"]
+           "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes"]
 
 
 def _lib():
@@ -72,6 +72,7 @@ def _lib():
         L.dmd_measure_batch.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp]
         L.dmd_measure.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(d), C.POINTER(d)]
         L.dmd_launch_count.argtypes = [vp, C.POINTER(i64)]
+        L.dmd_pair_bytes.argtypes = [vp, C.POINTER(i64)]
         L.dmd_sync.argtypes = [vp]
         L.dmd_pinned_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
         L.dmd_pinned_free.argtypes = [vp]
@@ -214,6 +215,13 @@ class LindbladGPU:
     def launches(self):
         n = C.c_int64()
         self._ck(_lib().dmd_launch_count(self._h, C.byref(n)))
+        return n.value
+
+    @property
+    def pair_bytes(self):
+        """device bytes of the stored k-pair operators"""
+        n = C.c_int64()
+        self._ck(_lib().dmd_pair_bytes(self._h, C.byref(n)))
         return n.value
 
     def sync(self):

@@ -126,6 +126,9 @@ int dmd_measure_batch(dmd_handle* h, int slot, int bstart, int bend, double* tot
 
 /* counters: kernel launches issued by this handle since creation */
 int dmd_launch_count(const dmd_handle* h, int64_t* launches);
+/* No counterpart in the reference: device bytes of the stored k-pair operators in the handle's
+ * layout (what one contraction pass streams from HBM) */
+int dmd_pair_bytes(const dmd_handle* h, int64_t* bytes);
 /* wait for the handle's stream */
 int dmd_sync(dmd_handle* h);
 

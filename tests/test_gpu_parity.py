@@ -268,6 +268,9 @@ def test_non_hermitian_state_vs_oracle(prec, oracle, built):
 # relative to the oracle's RHS: FP32 storage 1e-6, bf16 hi+lo (16 significant bits) 1e-5; the fitted
 # T1 within 1e-4 relative of the FP64 oracle (the target of the reduced-precision forms).
 LOWP_TOL = {"f32": 1e-6, "bf16x2": 1e-5}
+# the tensor-core batched form rounds the coordinates of rho to bf16 hi + lo as well (16 significant
+# bits on both operands of every product)
+TC_TOL = 2e-5
 
 
 def make_gpu_lowp(s, prec, with_ref=True, nrhs=1):
@@ -340,36 +343,135 @@ def _herm_states(s, n, seed, scale=1e-3):
     return out
 
 
+def _tensor_core_form(s, prec):
+    """the batched form runs on the tensor cores for nb = 2 with bf16 hi + lo storage"""
+    return prec == "bf16x2" and s.bend - s.bstart == 2 and os.environ.get("DMD_BATCH_TC", "1") != "0"
+
+
 @pytest.mark.parametrize("prec", ["f32", "bf16x2"])
 @pytest.mark.parametrize("case", ["nb2_eimp_B", "nb4_eimp_B", "nb2_linear", "nb2_carrier_eq"])
 def test_batched_states_vs_oracle(case, prec, oracle, built):
-    """Batched form: 7 states share P (RW states per warp, the last group short); every state's
-    RHS matches the oracle at the reduced-precision tolerance, and 20 RK4 steps of the batch match
-    the same steps of each state alone."""
+    """Batched form: 7 states share P (nb = 2 with bf16 hi + lo: the tensor-core contraction; else
+    RW states per warp on the CUDA cores, the last group short). Every state's RHS matches the oracle
+    at the reduced-precision tolerance; 20 RK4 steps of the batch change every state as 20 oracle
+    steps do, to that tolerance; the CUDA-core batch also matches each state stepped alone."""
     s = oracle.load(os.path.join(GOLDEN, case))
     R = 7
     ys = _herm_states(s, R, 31)
     t = 41.0 * oracle.fs
+    h = 2.0 * oracle.fs
+    tc = _tensor_core_form(s, prec)
+    tol = TC_TOL if tc else LOWP_TOL[prec]
     with make_gpu_lowp(s, prec, nrhs=R) as gb:
         out = gb.func(t, np.concatenate(ys)).reshape(R, -1)
         for q in range(R):
             e = rel(out[q], oracle.rhs(s, t, ys[q]))
-            assert e < LOWP_TOL[prec], (q, e)
+            assert e < tol, (q, e)
         gb.set_state(s.t0, np.concatenate(ys))
-        gb.rk4(2.0 * oracle.fs, 20)
+        gb.rk4(h, 20)
         _, yb = gb.get_state()
         yb = yb.reshape(R, -1)
-        if s.nb_dm * s.nb_dm * s.nk > 0:
-            gb.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
-            tot, _ = gb.measure_batch(0, s.nv_dm)
+        gb.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+        tot, _ = gb.measure_batch(0, s.nv_dm)
     for q in (0, 3, R - 1):
+        yo, _ = oracle.rk4(s, s.t0, h, 20, ys[q])
+        e = rel(yb[q] - ys[q], yo - ys[q])
+        print("%s %s state %d: 20-step change rel err %.3g" % (case, prec, q, e))
+        assert e < 3 * tol
         with make_gpu_lowp(s, prec) as g1:
             g1.set_state(s.t0, ys[q])
-            g1.rk4(2.0 * oracle.fs, 20)
+            g1.rk4(h, 20)
             _, y1 = g1.get_state()
             g1.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
             t1, _ = g1.measure(0, s.nv_dm)
-        # the batch and the single state sum in different atomic orders: FP32-level differences of
-        # the RHS, integrated over 20 steps
-        assert rel(yb[q], y1) < 1e-10
+        if not tc:
+            # the batch and the single state sum in different atomic orders: FP32-level differences
+            # of the RHS, integrated over 20 steps
+            assert rel(yb[q], y1) < 1e-10
         assert abs(tot[q] - t1) <= 1e-5 * abs(t1)
+
+
+def test_batched_tensor_core_many_states(oracle, built, tmp_path, monkeypatch):
+    """Tensor-core batched form on a larger random case (nk = 500, about 70k pairs, tiles spanning
+    many column groups) with 130 states: two state blocks of 128, the second nearly empty. Every
+    checked state matches the oracle; the whole batch matches the CUDA-core batched form
+    (DMD_BATCH_TC=0); a batch holding non-Hermitian states runs the anti-Hermitian pass."""
+    from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, make_ldbd
+    cfg = SynthConfig(nk=500, nb=2, seed=3, eimp_sigma_mev=5.0)
+    make_ldbd(str(tmp_path), cfg, B_T=(1.0, 0.0, 0.0), eimp_fraction=1e-2)
+    s = oracle.load(str(tmp_path))
+    R = 130
+    ys = _herm_states(s, R, 12)
+    t = 11.0 * oracle.fs
+    with make_gpu_lowp(s, "bf16x2", nrhs=R) as gb:
+        out_tc = gb.func(t, np.concatenate(ys)).reshape(R, -1)
+    monkeypatch.setenv("DMD_BATCH_TC", "0")
+    with make_gpu_lowp(s, "bf16x2", nrhs=R) as gc:
+        out_cc = gc.func(t, np.concatenate(ys)).reshape(R, -1)
+    monkeypatch.delenv("DMD_BATCH_TC")
+    for q in (0, 1, 64, 127, 128, 129):
+        e = rel(out_tc[q], oracle.rhs(s, t, ys[q]))
+        print("nk500 state %d: tensor-core rel err %.3g" % (q, e))
+        assert e < TC_TOL
+    for q in range(R):
+        assert rel(out_tc[q], out_cc[q]) < TC_TOL + LOWP_TOL["bf16x2"], q
+    # non-Hermitian states in the batch (the GSL callback accepts any y)
+    rng = np.random.default_rng(4)
+    nh = [y + 1e-3 * rng.standard_normal(y.shape) for y in ys[:3]]
+    with make_gpu_lowp(s, "bf16x2", nrhs=3) as gb:
+        for batch in (nh, ys[:3], nh):
+            out = gb.func(t, np.concatenate(batch)).reshape(3, -1)
+            for q in range(3):
+                assert rel(out[q], oracle.rhs(s, t, batch[q])) < TC_TOL, q
+
+
+def test_batched_tensor_core_irregular_pairs(oracle, built):
+    """Duplicated pairs (two operators in one block entry), pairs stored with k1 > k2 (no reverse
+    term) and diagonal pairs through the tensor-core batched form."""
+    d = os.path.join(GOLDEN, "nb2_eimp_B")
+    s0 = oracle.load(d)
+    rng = np.random.default_rng(9)
+    n = s0.npair
+    P1 = s0.P1.reshape(n, 16)
+    P2 = s0.P2.reshape(n, 16)
+    dup = rng.choice(n, 40, replace=False)
+    swp = rng.choice(n, 60, replace=False)
+    k1 = np.concatenate([s0.k1st, s0.k1st[dup], s0.k2nd[swp], np.arange(5, dtype=np.uint64)])
+    k2 = np.concatenate([s0.k2nd, s0.k2nd[dup], s0.k1st[swp], np.arange(5, dtype=np.uint64)])
+    Q1 = np.concatenate([P1, 0.5 * P1[dup], 0.3 * P2[swp], P1[:5]])
+    Q2 = np.concatenate([P2, 0.7 * P2[dup], 0.2 * P1[swp], P2[:5]])
+    s = oracle.from_arrays(nk=s0.nk, nb_dm=s0.nb_dm, bstart=s0.bstart, bend=s0.bend, e_dm=s0.e_dm, f_dm=s0.f_dm,
+                           k1st=k1, k2nd=k2, P1=Q1.reshape(-1), P2=Q2.reshape(-1), prefac_eph=s0.prefac_eph,
+                           dm0=s0.dm0, Hcoh=s0.Hcoh)
+    ys = _herm_states(s, 4, 8)
+    t = 9.0 * oracle.fs
+    with make_gpu_lowp(s, "bf16x2", nrhs=4) as gb:
+        out = gb.func(t, np.concatenate(ys)).reshape(4, -1)
+    for q in range(4):
+        assert rel(out[q], oracle.rhs(s, t, ys[q])) < TC_TOL, q
+
+
+def test_batched_tensor_core_t1_vs_oracle(oracle, built):
+    """T1 fitted from a state of a tensor-core batch (3 states, 1500 RK4 steps) within 1e-4 of the
+    FP64 oracle's, the target of the reduced-precision forms."""
+    from denmat_dynm_development_gb300.t1fit import fit_t1
+    s = oracle.load(os.path.join(GOLDEN, "nb2_carrier_eq"))
+    h, nsteps, every = 2.0 * oracle.fs, 1500, 50
+    y0 = oracle.y_of(s.dm0)
+    _, rec_o = oracle.rk4(s, s.t0, h, nsteps, y0, every=every)
+    ys = [y0] + _herm_states(s, 2, 17)
+    with make_gpu_lowp(s, "bf16x2", nrhs=3) as gb:
+        gb.set_state(s.t0, np.concatenate(ys))
+        gb.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+        rec = []
+        for _ in range(nsteps // every):
+            gb.rk4(h, every)
+            t, _ = gb.get_state()
+            tot, _ = gb.measure_batch(0, s.nv_dm)
+            rec.append((t, tot[0]))
+    rec = np.array(rec)
+    fo, fg = fit_t1(rec_o[:, 0], rec_o[:, 1]), fit_t1(rec[:, 0], rec[:, 1])
+    et = abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq)
+    print("tensor-core batch: S(t) rel err %.3g, T1 %.10g vs %.10g ps, rel err %.3g"
+          % (rel(rec[:, 1], rec_o[:, 1]), fg.tau_lsq, fo.tau_lsq, et))
+    assert et < 1e-4
