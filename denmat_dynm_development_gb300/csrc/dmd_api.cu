@@ -48,6 +48,7 @@ struct dmd_handle {
   unsigned int* d_hflag = nullptr;  // set by the prep kernel when a state is not exactly Hermitian
   double2* d_acc0 = nullptr;   // deviation form: contraction of diag(f_ref), position order [nk][2][nb2]
   double* d_fref = nullptr;    // deviation form: window occupations [nk][nb]
+  double2* d_ph = nullptr;     // phases D_k(i, j) of the current evaluation [nk][nb2]
   // batched form on the tensor cores (nb = 2, bf16 hi + lo): operator and coordinate blocks
   int use_tc = 0;
   uint16_t* d_tcB = nullptr;   // [blocks][4 planes][128 x 32] bf16, per tile its column groups
@@ -188,23 +189,26 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
   const int n = h->nk * NB * NB;
   ProfScope ps(h, 0);
   if (!h->use_cb) {
-    k_prep<NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->expt, h->d_rs, h->d_acc);
+    k_prep<NB><<<blocks_for(n, 256), 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->expt, h->d_rs, h->d_acc,
+                                                       h->d_ph);
   } else {
     // deviation coordinates for the reduced-precision and the linearized forms
     const double* fref = (deviation_form(h->prec) || h->lin) ? h->d_fref : nullptr;
-    const dim3 g(blocks_for(n, 256), h->nrhs);
+    // batched form: a thread serves up to 8 states of its (k, element), so the phase is computed once
+    const int qc = h->nrhs < 8 ? h->nrhs : 8;
+    const dim3 g(blocks_for(n, 256), (h->nrhs + qc - 1) / qc);
     if (h->prec == DMD_PREC_F64X)
       k_prep_herm<ArithDF, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
                                                       (float2*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin,
-                                                      h->nrhs);
+                                                      h->nrhs, qc, h->d_ph);
     else if (deviation_form(h->prec))
       k_prep_herm<ArithF32, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
                                                        (float*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin,
-                                                       h->nrhs);
+                                                       h->nrhs, qc, h->d_ph);
     else
       k_prep_herm<ArithF64, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
                                                        (double*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin,
-                                                       h->nrhs);
+                                                       h->nrhs, qc, h->d_ph);
   }
   h->launches++;
   CKL();
@@ -305,7 +309,9 @@ int launch_pairs(dmd_handle* h) {
 template <int NB>
 int launch_finish(dmd_handle* h, FinishArgs a) {
   ProfScope ps(h, 2);
-  k_finish<NB><<<dim3(blocks_for(h->nk, 128), h->nrhs), 128, 0, h->st>>>(a);
+  const dim3 g(blocks_for(h->nk, 128), h->nrhs);
+  if (h->nbdm == NB) k_finish<NB, NB><<<g, 128, 0, h->st>>>(a);
+  else k_finish<NB><<<g, 128, 0, h->st>>>(a);
   h->launches++;
   CKL();
   return DMD_OK;
@@ -326,6 +332,7 @@ FinishArgs base_finish(dmd_handle* h, const double2* y) {
   a.eq = h->d_eq;
   a.y = y;
   a.acc = h->d_acc;
+  a.ph = h->expt ? h->d_ph : nullptr;  // written by the prep kernels when the phase is on
   a.pos = h->use_cb ? h->d_pos : nullptr;
   a.herm = h->use_cb;
   a.lin = h->lin;
@@ -864,7 +871,7 @@ void release(dmd_handle* h) {
   if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
   void* ptrs[] = {h->d_err, h->d_pos, h->d_rb, h->d_items, h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
-                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles};
+                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -982,7 +989,7 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
       (rc = dalloc(h, &h->d_K, 6 * h->nstate)) || (rc = dalloc(h, &h->d_tref, 2)) ||
       (rc = dalloc(h, &h->d_step, 1)) || (rc = dalloc(h, &h->d_red, red_elems(h))) || (rc = dalloc(h, &h->d_coef_i, 64)) ||
       (rc = dalloc(h, &h->d_coef, 64)) || (rc = dalloc(h, &h->d_flag, 1)) || (rc = dalloc(h, &h->d_err, 1)) ||
-      (rc = dalloc(h, &h->d_hflag, 1)))
+      (rc = dalloc(h, &h->d_hflag, 1)) || (rc = dalloc(h, &h->d_ph, nk * h->nb2)))
     return bail(rc);
   std::vector<double> ew(nk * h->nb);
   for (size_t k = 0; k < nk; ++k)

@@ -34,10 +34,12 @@ __device__ __forceinline__ double eval_time(const TimeArg& ta) {
   return t + 0.5 * h;
 }
 
-// rt_k, st_k (window, phase removed) and zeroed X/Y accumulators. One thread per (k, element).
+// rt_k, st_k (window, phase removed) and zeroed X/Y accumulators. One thread per (k, element); the
+// phase D_k(i, j) is stored in ph ([nk][NB2]) for the finish kernel.
 template <int NB>
 __global__ void k_prep(int nk, int nbdm, int bs, const double2* __restrict__ y, const double* __restrict__ ew,
-                       TimeArg ta, int phase, double2* __restrict__ rs, double2* __restrict__ acc) {
+                       TimeArg ta, int phase, double2* __restrict__ rs, double2* __restrict__ acc,
+                       double2* __restrict__ ph) {
   constexpr int NB2 = NB * NB;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nk * NB2) return;
@@ -49,6 +51,7 @@ __global__ void k_prep(int nk, int nbdm, int bs, const double2* __restrict__ y, 
   if (phase) {
     const double t = eval_time(ta);
     const double2 d = ccis((ew[k * NB + i] - ew[k * NB + j]) * t);
+    ph[(size_t)k * NB2 + ab] = d;
     rt = cmul_rn(cconj(d), r);
     st = cmul_rn(cconj(d), s);
   }
@@ -75,6 +78,7 @@ struct FinishArgs {
   const double2* eq;   // [nk][NB2] or null
   const double2* y;    // state the RHS is evaluated on
   const double2* acc;  // [nk][2][NB2], indexed by pos[k] when pos is set
+  const double2* ph;   // D_k(i, j) = exp(i t (e_i - e_j)) of this evaluation [nk][NB2] (prep kernels)
   const int* pos;      // k -> accumulator row (column-block layout) or null
   int herm;            // accumulators hold X' = M^H X, Y' = M^H Y (Hermitian coordinates)
   int nrhs;            // batched form: states evaluated together (blockIdx.y), 1 otherwise
@@ -97,45 +101,60 @@ struct FinishArgs {
 };
 
 // One thread per k: scattering finish + coherent term, then the stepper's update for this k.
-template <int NB>
+// ND > 0: the density matrix has ND = nbdm = NB bands (compile time, arrays in registers); ND = 0:
+// nbdm is read at run time.
+template <int NB, int ND = 0>
 __global__ void k_finish(FinishArgs a) {
   constexpr int NB2 = NB * NB;
+  constexpr int NDA = ND > 0 ? ND : DMD_MAX_NBDM;  // array extent
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int q = blockIdx.y;  // state of the batch
   if (a.hflag && k == 0 && q == 0) *a.hflag = 0u;  // every pair launch of this evaluation has completed
   if (k >= a.nk) return;
-  const int nd = a.nbdm, nd2 = nd * nd;
+  const int nd = ND > 0 ? ND : a.nbdm, nd2 = nd * nd;
+  const int bs = (ND == NB) ? 0 : a.bs;  // the window is the whole density matrix
   const double t = eval_time(a.ta);
   const size_t qs = (size_t)q * a.sstride;
   const double2* yk = a.y + qs + (size_t)k * nd2;
-  double2 f[DMD_MAX_NBDM * DMD_MAX_NBDM];
+  double2 f[NDA * NDA];
+#pragma unroll
   for (int i = 0; i < nd2; ++i) f[i] = mk2(0.0, 0.0);
 
   // coherent term: -i [H(t), rho] (DenMat.cpp:29-55)
   if (a.want_coh) {
     const double* ek = a.edm + (size_t)k * nd;
     if (a.H) {
-      double2 Ht[DMD_MAX_NBDM * DMD_MAX_NBDM];
+      double2 Ht[NDA * NDA];
       const double2* Hk = a.H + (size_t)k * nd2;
+#pragma unroll
       for (int i = 0; i < nd; ++i)
+#pragma unroll
         for (int j = 0; j < nd; ++j)
           Ht[i * nd + j] = (a.picture == 0 && i != j) ? cmul_rn(Hk[i * nd + j], ccis((ek[i] - ek[j]) * t)) : Hk[i * nd + j];
-      double2 c1[DMD_MAX_NBDM * DMD_MAX_NBDM];
+      double2 c1[NDA * NDA];
+#pragma unroll
       for (int i = 0; i < nd; ++i)
+#pragma unroll
         for (int j = 0; j < nd; ++j) {  // dm * H (zhemm Right, beta = 0)
           double2 s = mk2(0.0, 0.0);
+#pragma unroll
           for (int l = 0; l < nd; ++l) s = cadd_rn(s, cmul_rn(yk[i * nd + l], herm_up(Ht, nd, l, j)));
           c1[i * nd + j] = cmul_rn(mk2(1.0, 0.0), s);
         }
+#pragma unroll
       for (int i = 0; i < nd; ++i)
+#pragma unroll
         for (int j = 0; j < nd; ++j) {  // H * dm - (dm * H)   (zhemm Left, beta = -1)
           double2 s = mk2(0.0, 0.0);
+#pragma unroll
           for (int l = 0; l < nd; ++l) s = cadd_rn(s, cmul_rn(herm_up(Ht, nd, i, l), yk[l * nd + j]));
           const double2 o = cadd_rn(cmul_rn(mk2(1.0, 0.0), s), cmul_rn(mk2(-1.0, 0.0), c1[i * nd + j]));
           f[i * nd + j] = cadd_rn(mk2(0.0, 0.0), cmul_rn(o, mk2(0.0, -1.0)));
         }
     } else if (a.picture == 1) {  // commutator_mat_diag(C, e, dm, nb, -i)
+#pragma unroll
       for (int i = 0; i < nd; ++i)
+#pragma unroll
         for (int j = 0; j < nd; ++j) {
           const double2 d = yk[i * nd + j];
           const double2 c = mk2(-__dmul_rn(d.x, ek[j]), -__dmul_rn(d.y, ek[j]));
@@ -149,12 +168,15 @@ __global__ void k_finish(FinishArgs a) {
     const double* ew = a.ew + (size_t)k * NB;
     const double2* Xs = a.acc + (size_t)q * a.astride + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
     double2 X[NB2], Y[NB2];
+#pragma unroll
     for (int i = 0; i < NB2; ++i) {
       X[i] = Xs[i];
       Y[i] = Xs[NB2 + i];
     }
     if (a.herm) {  // X = (M^H)^-1 X': X_ij = (X'_ij + i X'_ji) / 2, X_ji = (X'_ij - i X'_ji) / 2 for i < j
+#pragma unroll
       for (int i = 0; i < NB; ++i)
+#pragma unroll
         for (int j = i + 1; j < NB; ++j) {
           const double2 xu = X[i * NB + j], xl = X[j * NB + i], yu = Y[i * NB + j], yl = Y[j * NB + i];
           X[i * NB + j] = mk2(0.5 * (xu.x - xl.y), 0.5 * (xu.y + xl.x));
@@ -164,49 +186,70 @@ __global__ void k_finish(FinishArgs a) {
         }
     }
     double2 rw[NB2], sw[NB2], Pdm[NB2], dmP[NB2];
+#pragma unroll
     for (int i = 0; i < NB; ++i)
+#pragma unroll
       for (int j = 0; j < NB; ++j) {
-        const double2 r = yk[(a.bs + i) * nd + a.bs + j];
+        const double2 r = yk[(bs + i) * nd + bs + j];
         rw[i * NB + j] = r;
         sw[i * NB + j] = (i == j) ? mk2(1.0 - r.x, 0.0 - r.y) : mk2(-r.x, -r.y);
-        double2 d = mk2(1.0, 0.0);
-        if (a.phase) d = ccis((ew[i] - ew[j]) * t);
-        Pdm[i * NB + j] = a.phase ? cmul_rn(d, X[i * NB + j]) : X[i * NB + j];
-        dmP[i * NB + j] = a.phase ? cmul_rn(d, Y[i * NB + j]) : Y[i * NB + j];
+        if (a.phase && i != j) {  // D_k(i, i) = 1
+          const double2 d = a.ph ? a.ph[(size_t)k * NB2 + i * NB + j] : ccis((ew[i] - ew[j]) * t);
+          Pdm[i * NB + j] = cmul_rn(d, X[i * NB + j]);
+          dmP[i * NB + j] = cmul_rn(d, Y[i * NB + j]);
+        } else {
+          Pdm[i * NB + j] = X[i * NB + j];
+          dmP[i * NB + j] = Y[i * NB + j];
+        }
       }
     double2 c[NB2];
     if (a.lin) {
+#pragma unroll
       for (int i = 0; i < NB2; ++i) c[i] = Pdm[i];
     } else {
-    for (int i = 0; i < NB; ++i)
-      for (int j = 0; j < NB; ++j) {  // (1 - dm) * Pdm   (zhemm Left, alpha 1, beta 0)
-        double2 s = mk2(0.0, 0.0);
-        for (int l = 0; l < NB; ++l) s = cadd_rn(s, cmul_rn(herm_up(sw, NB, i, l), Pdm[l * NB + j]));
-        c[i * NB + j] = cmul_rn(mk2(1.0, 0.0), s);
-      }
-    for (int i = 0; i < NB; ++i)
-      for (int j = 0; j < NB; ++j) {  // - dm1P * dm + c   (zhemm Right, alpha -1, beta 1)
-        double2 s = mk2(0.0, 0.0);
-        for (int l = 0; l < NB; ++l) s = cadd_rn(s, cmul_rn(dmP[i * NB + l], herm_up(rw, NB, l, j)));
-        c[i * NB + j] = cadd_rn(cmul_rn(mk2(-1.0, 0.0), s), cmul_rn(mk2(1.0, 0.0), c[i * NB + j]));
-      }
+      // c = (1 - dm) Pdm - dm1P dm (zhemm Left alpha 1 beta 0, then zhemm Right alpha -1 beta 1):
+      // the Hermitian operands are read from their upper triangles; complex multiply-adds on the FMA
+      // pipe (the unit scalings alpha = 1, -1 are exact and not multiplied out)
+#pragma unroll
+      for (int i = 0; i < NB; ++i)
+#pragma unroll
+        for (int j = 0; j < NB; ++j) {
+          double2 s = mk2(0.0, 0.0);
+#pragma unroll
+          for (int l = 0; l < NB; ++l) s = cfma(herm_up(sw, NB, i, l), Pdm[l * NB + j], s);
+#pragma unroll
+          for (int l = 0; l < NB; ++l) {
+            const double2 m = dmP[i * NB + l];
+            s = cfma(mk2(-m.x, -m.y), herm_up(rw, NB, l, j), s);
+          }
+          c[i * NB + j] = s;
+        }
     }
     const double pf = a.prefac * 0.5;
+#pragma unroll
     for (int i = 0; i < NB; ++i)
-      for (int j = 0; j < NB; ++j) {
-        double2 v = cscale_rn(pf, cadd_rn(c[i * NB + j], cconj(c[j * NB + i])));
-        if (a.eq) {
-          const double2 q = a.eq[(size_t)k * NB2 + i * NB + j];
-          if (i == j || a.picture == 1) v = csub_rn(v, q);
-          else v = csub_rn(v, cmul_rn(q, ccis((ew[i] - ew[j]) * t)));
+#pragma unroll
+      for (int j = i; j < NB; ++j) {
+        // (prefac/2)(c + c^dagger); the (j, i) element is the exact conjugate of the (i, j) one
+        const double2 v = cscale_rn(pf, cadd_rn(c[i * NB + j], cconj(c[j * NB + i])));
+#pragma unroll
+        for (int w = 0; w < (i == j ? 1 : 2); ++w) {
+          const int ii = w ? j : i, jj = w ? i : j;
+          double2 u = w ? cconj(v) : v;
+          if (a.eq) {
+            const double2 q = a.eq[(size_t)k * NB2 + ii * NB + jj];
+            if (ii == jj || a.picture == 1) u = csub_rn(u, q);
+            else u = csub_rn(u, cmul_rn(q, a.ph ? a.ph[(size_t)k * NB2 + ii * NB + jj] : ccis((ew[ii] - ew[jj]) * t)));
+          }
+          double2& o = f[(bs + ii) * nd + bs + jj];
+          o = cadd_rn(o, u);
         }
-        double2& o = f[(a.bs + i) * nd + a.bs + j];
-        o = cadd_rn(o, v);
       }
   }
 
   const size_t base = qs + (size_t)k * nd2;
   if (a.mode == 0) {
+#pragma unroll
     for (int i = 0; i < nd2; ++i) a.out[base + i] = f[i];
     return;
   }
@@ -214,6 +257,7 @@ __global__ void k_finish(FinishArgs a) {
   if (a.mode == 1) {
     const double h = a.tref[1], hh = 0.5 * h, h6 = h / 6.0;
     double2* Ks = a.K + (size_t)a.stage * n;
+#pragma unroll
     for (int i = 0; i < nd2; ++i) {
       const double2 yb = a.ybase[base + i];
       Ks[base + i] = f[i];
@@ -233,7 +277,9 @@ __global__ void k_finish(FinishArgs a) {
   if (a.mode == 2) {  // update_dm_euler: dm += 0.5*dt*(ddmdt + ddmdt^dagger)
     const double h = a.tref[1];
     const double hf = 0.5 * h;
+#pragma unroll
     for (int i = 0; i < nd; ++i)
+#pragma unroll
       for (int j = 0; j < nd; ++j) {
         const double2 v = cscale_rn(hf, cadd_rn(f[i * nd + j], cconj(f[j * nd + i])));
         a.ybase[base + i * nd + j] = cadd_rn(a.ybase[base + i * nd + j], v);

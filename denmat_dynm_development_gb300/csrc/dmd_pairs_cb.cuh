@@ -209,10 +209,12 @@ struct ArithBF2 : ArithF32 {
 
 // ---------------------------------------------------------------------------------------------
 // Prep: Hermitian and anti-Hermitian coordinates of rt, st per k (written at pos[k]) and the
-// accumulators' start values (zero, or acc0). One thread per (k, element (i, j)); the thread of
-// (i, j) with i < j writes the coordinates at (i, j) and (j, i). Raises *hflag when some rho_k is
-// not exactly Hermitian. rs layout: [nrhs][nk][2][NB2] Hermitian part (r, s), then the anti-Hermitian
-// part; the batched form runs one grid row (blockIdx.y) per state.
+// accumulators' start values (zero, or acc0). One thread per (k, element (i, j)) and chunk of qc
+// states; the thread of (i, j) with i < j writes the coordinates at (i, j) and (j, i). Raises *hflag
+// when some rho_k is not exactly Hermitian. rs layout: [nrhs][nk][2][NB2] Hermitian part (r, s), then
+// the anti-Hermitian part; the batched form runs one grid row (blockIdx.y) per chunk of states, and
+// the phase D_k(i, j) = exp(i t (e_i - e_j)) is computed once per thread for all states of its chunk.
+// The first chunk stores D_k in ph ([nk][NB2], read by the finish kernel).
 // Deviation form (fref != null, window occupations [nk][NB]): the coordinates are those of
 // rho - diag(f) and of (1 - rho) - diag(1 - f) = -(rho - diag(f)); the contraction of diag(f) is
 // the constant acc0 (position order), formed once in FP64. Linearized form (lin): the coordinates of
@@ -223,62 +225,80 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
                             const int* __restrict__ pos, TimeArg ta, int phase, typename A::relem* __restrict__ rs,
                             double2* __restrict__ acc, unsigned int* __restrict__ hflag,
                             const double* __restrict__ fref, const double2* __restrict__ acc0, int lin,
-                            int nrhs = 1) {
+                            int nrhs, int qc, double2* __restrict__ ph) {
   constexpr int NB2 = NB * NB;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nk * NB2) return;
-  // batched form: state q = blockIdx.y; its state, coordinates and sums follow those of q - 1
-  const int q = blockIdx.y;
+  const int q0 = blockIdx.y * qc, q1 = min(nrhs, q0 + qc);
   const size_t cstride = (size_t)nk * 2 * NB2;  // coordinates (and sums) per state
-  y += (size_t)q * nk * nbdm * nbdm;
-  acc += (size_t)q * cstride;
-  rs += (size_t)q * cstride;
+  const size_t sstride = (size_t)nk * nbdm * nbdm;
   const int k = idx / NB2, ab = idx - k * NB2, i = ab / NB, j = ab - i * NB;
   const int p = pos[k];
   const size_t ax = (size_t)p * 2 * NB2 + ab;
-  acc[ax] = acc0 ? acc0[ax] : mk2(0.0, 0.0);
-  acc[ax + NB2] = acc0 ? acc0[ax + NB2] : mk2(0.0, 0.0);
+  const double2 a0 = acc0 ? acc0[ax] : mk2(0.0, 0.0), a1 = acc0 ? acc0[ax + NB2] : mk2(0.0, 0.0);
+  for (int q = q0; q < q1; ++q) {
+    acc[(size_t)q * cstride + ax] = a0;
+    acc[(size_t)q * cstride + ax + NB2] = a1;
+  }
   if (i > j) return;
-  typename A::relem* rh = rs + (size_t)p * 2 * NB2;
-  typename A::relem* ra = rs + (size_t)nrhs * cstride + (size_t)p * 2 * NB2;
   const double2* yk = y + (size_t)k * nbdm * nbdm;
-  const double2 vij = yk[(bs + i) * nbdm + bs + j];
   if (i == j) {
-    // H_ii = Re rho_ii, A_ii = Im rho_ii; 1 - rho: (1 - Re rho_ii, -Im rho_ii) (set_oneminusdm)
-    if (fref) {
-      const double dv = __dsub_rn(vij.x, fref[(size_t)k * NB + i]);
-      rh[ab] = A::from_double(dv);
-      rh[NB2 + ab] = A::from_double(lin ? 0.0 : -dv);
-    } else {
-      rh[ab] = A::from_double(vij.x);
-      rh[NB2 + ab] = A::from_double(1.0 - vij.x);
+    if (ph && blockIdx.y == 0) ph[(size_t)k * NB2 + ab] = mk2(1.0, 0.0);
+    const double fi = fref ? fref[(size_t)k * NB + i] : 0.0;
+    for (int q = q0; q < q1; ++q) {
+      typename A::relem* rh = rs + (size_t)q * cstride + (size_t)p * 2 * NB2;
+      typename A::relem* ra = rs + (size_t)(nrhs + q) * cstride + (size_t)p * 2 * NB2;
+      const double2 vij = yk[(size_t)q * sstride + (bs + i) * nbdm + bs + j];
+      // H_ii = Re rho_ii, A_ii = Im rho_ii; 1 - rho: (1 - Re rho_ii, -Im rho_ii) (set_oneminusdm)
+      if (fref) {
+        const double dv = __dsub_rn(vij.x, fi);
+        rh[ab] = A::from_double(dv);
+        rh[NB2 + ab] = A::from_double(lin ? 0.0 : -dv);
+      } else {
+        rh[ab] = A::from_double(vij.x);
+        rh[NB2 + ab] = A::from_double(1.0 - vij.x);
+      }
+      ra[ab] = A::from_double(vij.y);
+      ra[NB2 + ab] = A::from_double(lin ? 0.0 : 0.0 - vij.y);
+      if (vij.y != 0.0) atomicOr(hflag, 1u);
     }
-    ra[ab] = A::from_double(vij.y);
-    ra[NB2 + ab] = A::from_double(lin ? 0.0 : 0.0 - vij.y);
-    if (vij.y != 0.0) atomicOr(hflag, 1u);
     return;
   }
-  const double2 vji = yk[(bs + j) * nbdm + bs + i];
-  // H_ij = (rho_ij + conj(rho_ji)) / 2, A_ij = (rho_ij - conj(rho_ji)) / (2i); exact for Hermitian rho
-  const double2 hij = mk2(__dmul_rn(__dadd_rn(vij.x, vji.x), 0.5), __dmul_rn(__dsub_rn(vij.y, vji.y), 0.5));
-  const double2 dif = mk2(__dsub_rn(vij.x, vji.x), __dadd_rn(vij.y, vji.y));  // rho_ij - conj(rho_ji)
-  const double2 aij = mk2(__dmul_rn(dif.y, 0.5), __dmul_rn(-dif.x, 0.5));
-  if (dif.x != 0.0 || dif.y != 0.0) atomicOr(hflag, 1u);
-  double2 d = mk2(1.0, 0.0);
-  if (phase) d = cconj(ccis((ew[k * NB + i] - ew[k * NB + j]) * eval_time(ta)));
-  const double2 r1 = cmul_rn(d, hij);                       // conj(D) o H
-  const double2 s1 = cmul_rn(d, mk2(-hij.x, -hij.y));       // conj(D) o (1 - H) off the diagonal
-  const double2 r2 = cmul_rn(d, aij);                       // conj(D) o A
-  const double2 s2 = cmul_rn(d, mk2(-aij.x, -aij.y));       // conj(D) o (-A)
   const int ji = j * NB + i;
-  rh[ab] = A::from_double(r1.x);
-  rh[ji] = A::from_double(r1.y);
-  rh[NB2 + ab] = A::from_double(lin ? 0.0 : s1.x);
-  rh[NB2 + ji] = A::from_double(lin ? 0.0 : s1.y);
-  ra[ab] = A::from_double(r2.x);
-  ra[ji] = A::from_double(r2.y);
-  ra[NB2 + ab] = A::from_double(lin ? 0.0 : s2.x);
-  ra[NB2 + ji] = A::from_double(lin ? 0.0 : s2.y);
+  double2 d = mk2(1.0, 0.0);
+  if (phase) {
+    const double2 dk = ccis((ew[k * NB + i] - ew[k * NB + j]) * eval_time(ta));
+    if (ph && blockIdx.y == 0) {
+      ph[(size_t)k * NB2 + ab] = dk;
+      ph[(size_t)k * NB2 + ji] = cconj(dk);
+    }
+    d = cconj(dk);
+  }
+  for (int q = q0; q < q1; ++q) {
+    typename A::relem* rh = rs + (size_t)q * cstride + (size_t)p * 2 * NB2;
+    typename A::relem* ra = rs + (size_t)(nrhs + q) * cstride + (size_t)p * 2 * NB2;
+    const double2 vij = yk[(size_t)q * sstride + (bs + i) * nbdm + bs + j];
+    const double2 vji = yk[(size_t)q * sstride + (bs + j) * nbdm + bs + i];
+    // H_ij = (rho_ij + conj(rho_ji)) / 2, A_ij = (rho_ij - conj(rho_ji)) / (2i); exact for Hermitian rho
+    const double2 hij = mk2(__dmul_rn(__dadd_rn(vij.x, vji.x), 0.5), __dmul_rn(__dsub_rn(vij.y, vji.y), 0.5));
+    const double2 dif = mk2(__dsub_rn(vij.x, vji.x), __dadd_rn(vij.y, vji.y));  // rho_ij - conj(rho_ji)
+    const double2 r1 = cmul_rn(d, hij);                       // conj(D) o H
+    rh[ab] = A::from_double(r1.x);
+    rh[ji] = A::from_double(r1.y);
+    rh[NB2 + ab] = A::from_double(lin ? 0.0 : -r1.x);      // conj(D) o (1 - H) off the diagonal
+    rh[NB2 + ji] = A::from_double(lin ? 0.0 : -r1.y);
+    if (dif.x != 0.0 || dif.y != 0.0) {  // the anti-Hermitian part is read only when hflag is raised
+      atomicOr(hflag, 1u);
+      const double2 aij = mk2(__dmul_rn(dif.y, 0.5), __dmul_rn(-dif.x, 0.5));
+      const double2 r2 = cmul_rn(d, aij);                     // conj(D) o A
+      ra[ab] = A::from_double(r2.x);
+      ra[ji] = A::from_double(r2.y);
+      ra[NB2 + ab] = A::from_double(lin ? 0.0 : -r2.x);    // conj(D) o (-A)
+      ra[NB2 + ji] = A::from_double(lin ? 0.0 : -r2.y);
+    } else {
+      ra[ab] = ra[ji] = ra[NB2 + ab] = ra[NB2 + ji] = A::from_double(0.0);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------------------------
