@@ -288,6 +288,8 @@ def run_gpu_batched(args, w):
     g.set_profiling(True)
     g.rk4(h, 2)
     pair_ms, pair_n = g.profile(1)
+    prep_ms, prep_n = g.profile(0)
+    fin_ms, fin_n = g.profile(2)
     g.set_profiling(False)
     pbytes = g.pair_bytes
     g.close()
@@ -296,12 +298,12 @@ def run_gpu_batched(args, w):
     pair_avg = pair_ms / max(pair_n, 1)
     nk = st.cfg.nk
     if tc:
-        # per contraction (packing + Hermitian pass): operator blocks once from HBM, coordinates in
-        # (FP32) and as bf16 hi + lo blocks out and back in, the sums out
+        # per contraction (packing + Hermitian pass): operator blocks once from HBM, the r coordinates
+        # in (FP32) and as bf16 hi + lo blocks out and back in, the sums out
         nmb = (R + 127) // 128
         ngroups = (nk + 7) // 8
-        bpl = pbytes + R * nk * 8 * 4 + 2 * ngroups * nmb * 32768 + R * nk * 8 * 16
-        flops = (pbytes / 32768) * nmb * 12 * 2.0 * 128 * 128 * 16  # issued MMA flops (padding included)
+        bpl = pbytes + R * nk * 4 * 4 + 2 * ngroups * nmb * 16384 + R * nk * 8 * 16
+        flops = (pbytes / 32768) * nmb * 6 * 2.0 * 128 * 256 * 16  # issued MMA flops (padding included)
         kernel, bound = "tensor-core batched k-pair contraction (tcgen05, bf16 hi+lo)", "hbm"
     else:
         bpl = algorithmic_bytes(nb, st.npair, nk, ELEM_BYTES[prec]) + (R - 1) * nk * nb * nb * 16 * 2
@@ -316,7 +318,9 @@ def run_gpu_batched(args, w):
             "roofline": {"bound": bound, "achieved": bpl / (pair_avg * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": bpl / (pair_avg * 1e-3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
                          "kernel": kernel, "avg_launch_ms": pair_avg, "pair_bytes": pbytes,
-                         "tflops": flops / (pair_avg * 1e-3) / 1e12},
+                         "tflops": flops / (pair_avg * 1e-3) / 1e12,
+                         "per_rhs_ms": {"prep": prep_ms / max(prep_n, 1), "contraction": pair_avg,
+                                        "finish": fin_ms / max(fin_n, 1)}},
             "clocks": clocks, "gpu_launches": launches}
     print(json.dumps(line))
 

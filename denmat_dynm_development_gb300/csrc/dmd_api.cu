@@ -51,8 +51,8 @@ struct dmd_handle {
   double2* d_ph = nullptr;     // phases D_k(i, j) of the current evaluation [nk][nb2]
   // batched form on the tensor cores (nb = 2, bf16 hi + lo): operator and coordinate blocks
   int use_tc = 0;
-  uint16_t* d_tcB = nullptr;   // [blocks][4 planes][128 x 32] bf16, per tile its column groups
-  uint16_t* d_tcA = nullptr;   // [part][group][state block][4 planes][128 x 32] bf16
+  uint16_t* d_tcB = nullptr;   // [blocks][256 x (hi 32 | lo 32)] bf16, per tile its column groups
+  uint16_t* d_tcA = nullptr;   // [part][group][state block][128 x (hi 32 | lo 32)] bf16
   dmd::TcTile* d_tiles = nullptr;
   int ntiles = 0, ngroups = 0, nmb = 0;
   int64_t pair_bytes = 0;      // stored operator bytes (dmd_pair_bytes)
@@ -244,17 +244,18 @@ cudaError_t herm_pair_attrs() {
 // tensor-core batched form: pack the coordinates, then the Hermitian pass and the gated
 // anti-Hermitian pass (dmd_batched_tc.cuh)
 void tc_launches(dmd_handle* h, size_t half) {
-  const size_t per = (size_t)h->nrhs * h->nk * 8;
+  const size_t per = (size_t)h->nrhs * h->nk * 4;
   k_pack_tc<<<dim3(blocks_for((long long)per, 256), 2), 256, 0, h->st>>>(h->nk, h->nrhs, h->ngroups, h->nmb,
                                                                          (const float*)h->d_rs, h->d_tcA, h->d_hflag);
-  const size_t smem = (size_t)TC_NST * 2 * TC_BLOCK_BYTES + 128;
-  const size_t apart = (size_t)h->ngroups * h->nmb * TC_BLOCK;
+  const size_t apart = (size_t)h->ngroups * h->nmb * TC_ABLOCK;
   const size_t astride = (size_t)h->nk * 2 * h->nb2;
   const unsigned g = (unsigned)((size_t)h->ntiles * h->nmb);
-  k_pairs_tc<false><<<g, 128, smem, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA, h->nmb, h->nrhs, h->nk,
-                                             h->d_acc0, h->d_acc, astride, nullptr, h->d_err);
-  k_pairs_tc<true><<<g, 128, smem, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA + apart, h->nmb, h->nrhs, h->nk,
-                                            nullptr, h->d_acc, astride, h->d_hflag, h->d_err);
+  const double ysign = h->lin ? 0.0 : -1.0;  // s = -r (deviation form) or 0 (linearized form)
+  k_pairs_tc<false><<<g, 128, TC_SMEM_BYTES, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA, h->nmb, h->nrhs,
+                                                      h->nk, h->d_acc0, h->d_acc, astride, ysign, nullptr, h->d_err);
+  k_pairs_tc<true><<<g, 128, TC_SMEM_BYTES, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA + apart, h->nmb,
+                                                     h->nrhs, h->nk, nullptr, h->d_acc, astride, ysign, h->d_hflag,
+                                                     h->d_err);
   (void)half;
   h->launches += 1;  // the packing launch; the two passes are counted with the other forms
 }
@@ -705,9 +706,8 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
   L.rb.clear();
   L.items.clear();
   L.src.clear();
-  const size_t smem = (size_t)TC_NST * 2 * TC_BLOCK_BYTES + 128;
-  CK(cudaFuncSetAttribute(k_pairs_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  CK(cudaFuncSetAttribute(k_pairs_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  CK(cudaFuncSetAttribute(k_pairs_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_BYTES));
+  CK(cudaFuncSetAttribute(k_pairs_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_BYTES));
   h->ntiles = (nk + TC_TR - 1) / TC_TR;
   h->ngroups = (nk + TC_CG - 1) / TC_CG;
   h->nmb = (h->nrhs + TC_M - 1) / TC_M;
@@ -751,11 +751,11 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
     }
   }
   if ((rc = dalloc(h, &h->d_tiles, tiles.size())) || (rc = dalloc(h, &h->d_tcB, (size_t)nblocks * TC_BLOCK)) ||
-      (rc = dalloc(h, &h->d_tcA, (size_t)2 * h->ngroups * h->nmb * TC_BLOCK)))
+      (rc = dalloc(h, &h->d_tcA, (size_t)2 * h->ngroups * h->nmb * TC_ABLOCK)))
     return rc;
   CK(cudaMemcpy(h->d_tiles, tiles.data(), tiles.size() * sizeof(TcTile), cudaMemcpyHostToDevice));
   h->pair_bytes = nblocks * (int64_t)TC_BLOCK_BYTES;
-  CK(cudaMemset(h->d_tcA, 0, (size_t)2 * h->ngroups * h->nmb * TC_BLOCK * 2));
+  CK(cudaMemset(h->d_tcA, 0, (size_t)2 * h->ngroups * h->nmb * TC_ABLOCK * 2));
   // deviation form: acc0 = contraction of diag(f_ref) in FP64, position order [nk][2][nb2]
   const bool dev = deviation_form(h->prec) && !h->lin;
   std::vector<double> fw;
@@ -838,9 +838,9 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
             for (int n = 0; n < TC_N; ++n)
               for (int kk = 0; kk < TC_K; ++kk) {
                 const uint32_t w = pack_bf2(f64[(((size_t)blk * 2 + m) * TC_N + n) * TC_K + kk]);
-                uint16_t* pl = dst0 + (size_t)blk * TC_BLOCK + (size_t)m * 2 * TC_PLANE;
+                uint16_t* pl = dst0 + (size_t)blk * TC_BLOCK + (size_t)m * TC_PLANE;
                 pl[tc_ci(n, kk)] = (uint16_t)(w >> 16);
-                pl[TC_PLANE + tc_ci(n, kk)] = (uint16_t)(w & 0xffffu);
+                pl[tc_ci(n, kk + 32)] = (uint16_t)(w & 0xffffu);
               }
       }
     };

@@ -5,18 +5,23 @@
 // reverse term, (k2 <- k1) with A = conj(Q2), B = conj(Q1) (Q1, Q2: the Hermitian-coordinate
 // operators of dmd_pairs_cb.cuh). Then for every row k
 //   X'_k[a] = sum_c sum_j A_kc[a][j] r_c[j],      Y'_k[j] = sum_c sum_a B_kc[a][j] s_c[a]
-// and no reverse sums remain. Rows (energy-rank positions) are grouped in tiles of TR = 16, columns
-// in groups of CG = 8; a tile's operators over one column group form a dense block (zeros where a
-// row and a column have no pair; rows of an energy window pair with nearly the same columns, so the
-// blocks are nearly full). For a tile and up to 128 states one CTA computes
-//   D_X[q][(r, a, re|im)] = sum_(c, j) R[q][(c, j)] * BX[(c, j)][(r, a, re|im)]
-//   D_Y[q][(r, j, re|im)] = sum_(c, a) S[q][(c, a)] * BY[(c, a)][(r, j, re|im)]
-// (M = 128 states, N = 16 rows x 4 x 2 = 128, K = 8 columns x 4 = 32 per group) as tcgen05 MMAs
-// accumulating in tensor memory over all of the tile's column groups, then writes each row's sums
-// once: no atomics. Operands are bf16 hi + lo splits (x = hi + lo, 16 significant bits); the
-// product keeps hi*hi + hi*lo + lo*hi. Operand blocks are laid out in HBM exactly as the MMA reads
-// them (K-major, no swizzle: core matrices of 8 rows x 16 B), so one bulk copy per block fills a
-// pipeline stage: thread 0 produces, thread 32 issues MMAs, all four warps read TMEM at the end.
+// and no reverse sums remain. The batched form runs in the deviation form, where s = -r (or s = 0 in
+// the linearized form), so both sums contract the same coordinates: Y'_k[j] = -sum B_kc[a][j] r_c[a].
+// Rows (energy-rank positions) are grouped in tiles of TR = 16, columns in groups of CG = 8; a tile's
+// operators over one column group form a dense block (zeros where a row and a column have no pair;
+// rows of an energy window pair with nearly the same columns, so the blocks are nearly full). For a
+// tile and up to 128 states one CTA computes
+//   D[q][n] = sum_(c, j) R[q][(c, j)] * B[(c, j)][n],  n < 128: (r, a, re|im) of X', n >= 128: (r, j, re|im) of -Y'
+// (M = 128 states, N = 256, K = 8 columns x 4 = 32 per group) as tcgen05 MMAs accumulating in tensor
+// memory over all of the tile's column groups, then writes each row's sums once: no atomics.
+// Operands are bf16 hi + lo splits (x = hi + lo, 16 significant bits); the product keeps
+// hi*hi + hi*lo + lo*hi. Every operand row holds [hi (32) | lo (32)] = 128 bytes, so a tile is a
+// 128-byte-swizzled K-major tile and the three products are MMAs over K slices paired through
+// descriptor offsets (hi: +0, +32 B; lo: +64, +96 B). Operand blocks are laid out in HBM exactly as
+// the MMA reads them (swizzle included), so two bulk copies fill a pipeline stage. Warp 0 (one lane)
+// produces, warp 1 (one lane) issues MMAs, the other lanes of both warps park at __syncwarp (a lane
+// polling an mbarrier would hold up the working lane of its warp), and all four warps write the sums
+// through shared memory in 512-byte rows.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -32,52 +37,57 @@ struct TcTile {
 };
 
 constexpr int TC_TR = 16, TC_CG = 8, TC_K = 32, TC_N = 128, TC_M = 128;
-constexpr int TC_PLANE = 4096;                     // bf16 per plane (128 x 32)
-constexpr int TC_BLOCK = 4 * TC_PLANE;             // bf16 per block: 4 planes
+constexpr int TC_PLANE = 8192;                     // bf16 per 128-row tile (128 rows x [hi 32 | lo 32])
+constexpr int TC_BLOCK = 2 * TC_PLANE;             // bf16 per operator block: X rows, then Y rows (256)
+constexpr int TC_ABLOCK = TC_PLANE;                // bf16 per coordinate block: R (128 states)
 constexpr uint32_t TC_BLOCK_BYTES = 2 * TC_BLOCK;  // 32 KB
-constexpr int TC_NST = 3;                          // pipeline stages of (coordinate block, operator block)
+constexpr uint32_t TC_ABLOCK_BYTES = 2 * TC_ABLOCK;  // 16 KB
+constexpr uint32_t TC_STAGE_BYTES = TC_ABLOCK_BYTES + TC_BLOCK_BYTES;
+constexpr int TC_NST = 4;                          // pipeline stages of (coordinate block, operator block)
+constexpr size_t TC_SMEM_BYTES = (size_t)TC_NST * TC_STAGE_BYTES + 1024 + 128;
 
-// element (row, kk) of a 128 x 32 K-major plane: core matrices [row / 8][kk / 8] of 8 x 8
-__host__ __device__ __forceinline__ int tc_ci(int row, int kk) {
-  return (((row >> 3) * 4 + (kk >> 3)) << 6) + ((row & 7) << 3) + (kk & 7);
-}
+// element (row, kk) of a tile: kk < 32 the hi part, kk + 32 the lo part of K index kk
+__host__ __device__ __forceinline__ int tc_ci(int row, int kk) { return tc_sw128(row, kk); }
 
-// coordinates (FP32, [part][q][pos][2 NB2] as written by k_prep_herm) -> coordinate blocks
-// [part][group][mblock][r_hi, r_lo, s_hi, s_lo][128 x 32]; entries of padding states stay zero.
-// Part 1 (anti-Hermitian) is packed only when *gate is set.
+// r coordinates (FP32, [part][q][pos][2 NB2] as written by k_prep_herm, the first NB2 of each 2 NB2)
+// -> coordinate blocks [part][group][mblock][128 x (hi 32 | lo 32)]; entries of padding states stay
+// zero. Part 1 (anti-Hermitian) is packed only when *gate is set.
 __global__ void k_pack_tc(int nk, int nrhs, int ngroups, int nmb, const float* __restrict__ rs,
                           uint16_t* __restrict__ A, const unsigned int* __restrict__ gate) {
   const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const int part = blockIdx.y;
   if (part == 1 && *gate == 0u) return;
-  const size_t per = (size_t)nrhs * nk * 8;
+  const size_t per = (size_t)nrhs * nk * 4;
   if (idx >= per) return;
-  const int e = (int)(idx % 8), p = (int)((idx / 8) % nk), q = (int)(idx / ((size_t)8 * nk));
-  const float v = rs[(size_t)part * per + idx];
+  const int e = (int)(idx % 4), p = (int)((idx / 4) % nk), q = (int)(idx / ((size_t)4 * nk));
+  const float v = rs[(size_t)part * 2 * per + ((size_t)q * nk + p) * 8 + e];
   const __nv_bfloat16 hi = __float2bfloat16_rn(v);
   const __nv_bfloat16 lo = __float2bfloat16_rn(__fsub_rn(v, __bfloat162float(hi)));
-  const int g = p / TC_CG, kk = (p % TC_CG) * 4 + (e & 3), mb = q / TC_M, m = q % TC_M;
-  uint16_t* blk = A + (((size_t)part * ngroups + g) * nmb + mb) * TC_BLOCK + (e < 4 ? 0 : 2 * TC_PLANE);
+  const int g = p / TC_CG, kk = (p % TC_CG) * 4 + e, mb = q / TC_M, m = q % TC_M;
+  uint16_t* blk = A + (((size_t)part * ngroups + g) * nmb + mb) * TC_ABLOCK;
   blk[tc_ci(m, kk)] = __bfloat16_as_ushort(hi);
-  blk[TC_PLANE + tc_ci(m, kk)] = __bfloat16_as_ushort(lo);
+  blk[tc_ci(m, kk + 32)] = __bfloat16_as_ushort(lo);
 }
 
-// IMAG: the anti-Hermitian pass (sums times i, added); otherwise acc = acc0 + sums (stored)
+// IMAG: the anti-Hermitian pass (sums times i, added); otherwise acc = acc0 + sums (stored).
+// ysign: -1 (Y' = -D_Y, s = -r) or 0 (linearized form, s = 0).
 template <bool IMAG>
 __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ tiles, int ntiles,
                                                      const uint16_t* __restrict__ B, const uint16_t* __restrict__ A,
                                                      int nmb, int nrhs, int nk, const double2* __restrict__ acc0,
-                                                     double2* __restrict__ acc, size_t astride,
+                                                     double2* __restrict__ acc, size_t astride, double ysign,
                                                      const unsigned int* __restrict__ gate,
                                                      unsigned int* __restrict__ errflag) {
-  extern __shared__ __align__(1024) unsigned char smem[];
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
   if (gate && *gate == 0u) return;
+  // swizzled operand tiles start on 1024-byte boundaries (1 KB of slack is allocated)
+  unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   // the CTAs of one tile (all state blocks) are adjacent, so its operator blocks are read from HBM once
   const int t = blockIdx.x / nmb, mb = blockIdx.x % nmb;
   if (t >= ntiles) return;
   const TcTile tile = tiles[t];
   const int nch = tile.g1 - tile.g0;
-  uint64_t* full = (uint64_t*)(smem + TC_NST * 2 * TC_BLOCK_BYTES);
+  uint64_t* full = (uint64_t*)(smem + TC_NST * TC_STAGE_BYTES);
   uint64_t* empty = full + TC_NST;
   uint64_t* done = empty + TC_NST;
   uint32_t* tslot = (uint32_t*)(done + 1);
@@ -91,7 +101,7 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
     fence_mbar_init();
   }
   if (warp == 0) {
-    tc_alloc(tslot, 256);  // D_X in columns [0, 128), D_Y in [128, 256)
+    tc_alloc(tslot, 256);  // D: X' in columns [0, 128), -Y' in [128, 256)
     tc_relinquish();
   }
   tc_fence_before();
@@ -99,82 +109,92 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
   tc_fence_after();
   const uint32_t tmem = *tslot;
   if (nch > 0) {
-    int issued = 0;
-    if (threadIdx.x == 0) {  // producer: coordinate block + operator block per column group
-      const uint64_t pol_a = policy_evict_last(), pol_b = policy_evict_first();
-      for (int i = 0; i < nch; ++i) {
-        const int s = i % TC_NST;
-        if (i >= TC_NST && !mbar_wait_bounded(&empty[s], (uint32_t)((i / TC_NST - 1) & 1), errflag)) break;
-        unsigned char* st = smem + (size_t)s * 2 * TC_BLOCK_BYTES;
-        mbar_arrive_expect_tx(&full[s], 2 * TC_BLOCK_BYTES);
-        bulk_g2s(st, A + ((size_t)(tile.g0 + i) * nmb + mb) * TC_BLOCK, TC_BLOCK_BYTES, &full[s], pol_a);
-        bulk_g2s(st + TC_BLOCK_BYTES, B + (size_t)(tile.boff + i) * TC_BLOCK, TC_BLOCK_BYTES, &full[s], pol_b);
-        ++issued;
-      }
-    } else if (threadIdx.x == 32) {  // MMA issuer
-      constexpr uint32_t idesc = tc_idesc_bf16(TC_M, TC_N);
-      constexpr uint32_t LBO = 128, SBO = 512, PL = 2 * TC_PLANE;  // bytes: K-adjacent, M/N-adjacent core matrices; plane
-      for (int i = 0; i < nch; ++i) {
-        const int s = i % TC_NST;
-        if (!mbar_wait_bounded(&full[s], (uint32_t)((i / TC_NST) & 1), errflag)) break;
-        tc_fence_after();
-        const uint32_t a0 = smem_u32(smem + (size_t)s * 2 * TC_BLOCK_BYTES), b0 = a0 + TC_BLOCK_BYTES;
-#pragma unroll
-        for (int ks = 0; ks < 2; ++ks) {  // K = 32 as two MMAs of K = 16 (two core matrices apart)
-          const uint32_t ko = ks * 2 * LBO;
-          const uint32_t accum = (i | ks) != 0;  // the tile's first MMA overwrites the accumulator
-          // X: R x BX (planes r_hi, r_lo / x_hi, x_lo)
-          tc_mma(tmem, tc_desc(a0 + ko, LBO, SBO), tc_desc(b0 + ko, LBO, SBO), idesc, accum);
-          tc_mma(tmem, tc_desc(a0 + ko, LBO, SBO), tc_desc(b0 + PL + ko, LBO, SBO), idesc, 1);
-          tc_mma(tmem, tc_desc(a0 + PL + ko, LBO, SBO), tc_desc(b0 + ko, LBO, SBO), idesc, 1);
-          // Y: S x BY (planes s_hi, s_lo / y_hi, y_lo)
-          tc_mma(tmem + 128, tc_desc(a0 + 2 * PL + ko, LBO, SBO), tc_desc(b0 + 2 * PL + ko, LBO, SBO), idesc, accum);
-          tc_mma(tmem + 128, tc_desc(a0 + 2 * PL + ko, LBO, SBO), tc_desc(b0 + 3 * PL + ko, LBO, SBO), idesc, 1);
-          tc_mma(tmem + 128, tc_desc(a0 + 3 * PL + ko, LBO, SBO), tc_desc(b0 + 2 * PL + ko, LBO, SBO), idesc, 1);
+    if (warp == 0) {
+      if (lane == 0) {  // producer: coordinate block + operator block per column group
+        const uint64_t pol_a = policy_evict_last(), pol_b = policy_evict_first();
+        int issued = 0;
+        for (int i = 0; i < nch; ++i) {
+          const int s = i % TC_NST;
+          if (i >= TC_NST && !mbar_wait_bounded(&empty[s], (uint32_t)((i / TC_NST - 1) & 1), errflag)) break;
+          unsigned char* st = smem + (size_t)s * TC_STAGE_BYTES;
+          mbar_arrive_expect_tx(&full[s], TC_STAGE_BYTES);
+          bulk_g2s(st, A + ((size_t)(tile.g0 + i) * nmb + mb) * TC_ABLOCK, TC_ABLOCK_BYTES, &full[s], pol_a);
+          bulk_g2s(st + TC_ABLOCK_BYTES, B + (size_t)(tile.boff + i) * TC_BLOCK, TC_BLOCK_BYTES, &full[s], pol_b);
+          ++issued;
         }
-        tc_commit(&empty[s]);  // the stage is free once these MMAs have read it
+        mbar_wait_bounded(done, 0, errflag);
+        // no bulk copy into this CTA's shared memory outlives it (all landed unless a wait gave up)
+        for (int j = issued > TC_NST ? issued - TC_NST : 0; j < issued; ++j)
+          mbar_wait_bounded(&full[j % TC_NST], (uint32_t)((j / TC_NST) & 1), errflag);
       }
-      tc_commit(done);  // arrives when every MMA issued above has completed (also after a failure)
+      __syncwarp();
+    } else if (warp == 1) {
+      if (lane == 0) {  // MMA issuer
+        constexpr uint32_t idesc = tc_idesc_bf16(TC_M, 2 * TC_N);
+        constexpr uint32_t SBO = 1024, LO = 64;  // bytes: 8-row atoms; hi -> lo slice of a row
+        for (int i = 0; i < nch; ++i) {
+          const int s = i % TC_NST;
+          if (!mbar_wait_bounded(&full[s], (uint32_t)((i / TC_NST) & 1), errflag)) break;
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(smem + (size_t)s * TC_STAGE_BYTES), b0 = a0 + TC_ABLOCK_BYTES;
+#pragma unroll
+          for (int ks = 0; ks < 2; ++ks) {  // K = 32 as two MMAs of K = 16 (32 bytes of the row apart)
+            const uint32_t ko = ks * 32;
+            const uint32_t accum = (i | ks) != 0;  // the tile's first MMA overwrites the accumulator
+            tc_mma(tmem, tc_desc_sw128(a0 + ko, SBO), tc_desc_sw128(b0 + ko, SBO), idesc, accum);  // hi x hi
+            tc_mma(tmem, tc_desc_sw128(a0 + LO + ko, SBO), tc_desc_sw128(b0 + ko, SBO), idesc, 1);  // lo x hi
+            tc_mma(tmem, tc_desc_sw128(a0 + ko, SBO), tc_desc_sw128(b0 + LO + ko, SBO), idesc, 1);  // hi x lo
+          }
+          tc_commit(&empty[s]);  // the stage is free once these MMAs have read it
+        }
+        tc_commit(done);  // arrives when every MMA issued above has completed (also after a failure)
+      }
+      __syncwarp();
     }
     // all MMAs complete before TMEM is read (bounded; a timeout sets the flag)
     mbar_wait_bounded(done, 0, errflag);
-    if (threadIdx.x == 0)  // no bulk copy into this CTA's shared memory outlives it (all done unless a wait gave up)
-      for (int j = issued > TC_NST ? issued - TC_NST : 0; j < issued; ++j)
-        mbar_wait_bounded(&full[j % TC_NST], (uint32_t)((j / TC_NST) & 1), errflag);
   }
-  __syncwarp();  // the producer and issuer lanes rejoin their warps before the warp-wide TMEM loads
   tc_fence_after();
-  // epilogue: thread (warp w, lane l) owns state q = 128 mb + 32 w + l = TMEM lane 32 w + l
-  const int q = mb * TC_M + warp * 32 + lane;
+  // epilogue: TMEM lane 32 w + l holds state q = 128 mb + 32 w + l. Per group of 4 rows a thread
+  // writes its state's 4 x 8 sums into shared memory (a row of 33 double2 per state), then the warp
+  // stores each state's 512 contiguous bytes with one coalesced instruction.
+  double2* wsm = (double2*)smem + (size_t)warp * 32 * 33;
+  const int qb = mb * TC_M + warp * 32;
   const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-  for (int cb = 0; cb < 8; ++cb) {  // 8 x 32 columns: D_X then D_Y
-    float v[32];
+  for (int rq = 0; rq < 4; ++rq) {
+    float vx[32], vy[32];
     if (nch > 0) {
-      tc_ld32(lane_addr + cb * 32, v);
+      tc_ld32(lane_addr + rq * 32, vx);
+      tc_ld32(lane_addr + 128 + rq * 32, vy);
     } else {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = 0.f;
+      for (int i = 0; i < 32; ++i) vx[i] = vy[i] = 0.f;
     }
-    if (q >= nrhs) continue;
-    // columns cb*32 .. cb*32+31 = 4 rows x (4 elements x re|im) of X' (cb < 4) or Y' (cb >= 4)
-    const int half = cb >> 2;  // 0: X', 1: Y'
+    double2* my = wsm + lane * 33;
 #pragma unroll
-    for (int rr = 0; rr < 4; ++rr) {
-      const int r = (cb & 3) * 4 + rr, p = t * TC_TR + r;
-      if (p >= nk) continue;
-      double2* dst = acc + (size_t)q * astride + (size_t)p * 8 + half * 4;
+    for (int rr = 0; rr < 4; ++rr)
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
-        const double re = v[rr * 8 + 2 * a], im = v[rr * 8 + 2 * a + 1];
+        my[rr * 8 + a] = mk2((double)vx[rr * 8 + 2 * a], (double)vx[rr * 8 + 2 * a + 1]);
+        my[rr * 8 + 4 + a] = mk2(ysign * (double)vy[rr * 8 + 2 * a], ysign * (double)vy[rr * 8 + 2 * a + 1]);
+      }
+    __syncwarp();
+    // lane l covers row p0 + l / 8, element l % 8 of every state of the warp
+    const int p = t * TC_TR + rq * 4 + (lane >> 3);
+    if (p < nk) {
+      const double2 c = (!IMAG && acc0) ? acc0[(size_t)p * 8 + (lane & 7)] : mk2(0.0, 0.0);
+      for (int j = 0; j < 32 && qb + j < nrhs; ++j) {
+        const double2 v = wsm[j * 33 + lane];
+        double2* dst = acc + (size_t)(qb + j) * astride + (size_t)p * 8 + (lane & 7);
         if (IMAG) {
-          const double2 o = dst[a];
-          dst[a] = mk2(o.x - im, o.y + re);
+          const double2 o = *dst;
+          *dst = mk2(o.x - v.y, o.y + v.x);
         } else {
-          const double2 c = acc0 ? acc0[(size_t)p * 8 + half * 4 + a] : mk2(0.0, 0.0);
-          dst[a] = mk2(c.x + re, c.y + im);
+          *dst = mk2(c.x + v.x, c.y + v.y);
         }
       }
     }
+    __syncwarp();
   }
   tc_fence_before();
   __syncthreads();

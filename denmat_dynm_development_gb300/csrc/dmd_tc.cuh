@@ -21,6 +21,25 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32
   return d;
 }
 
+// Shared-memory matrix descriptor, 128-byte swizzle, K-major: rows of 128 bytes (64 bf16 along K),
+// 8-row atoms of 1024 bytes in which the 16-byte chunk index is XORed with the row index (mod 8);
+// atoms are sbo bytes apart along M (or N). The atom must start on a 1024-byte boundary; a K offset
+// inside the row is added to the start address. Bits as tc_desc, with [16,30) lbo = 1 (unused for
+// swizzled K-major layouts) and [61,64) layout 2 (128-byte swizzle).
+__device__ __forceinline__ uint64_t tc_desc_sw128(uint32_t saddr, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Element index of (row, kk) in a 128-byte-swizzled K-major tile of 16-bit elements (64 per row)
+__host__ __device__ __forceinline__ int tc_sw128(int row, int kk) {
+  return ((row >> 3) << 9) + ((row & 7) << 6) + ((((kk >> 3) ^ row) & 7) << 3) + (kk & 7);
+}
+
 // Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, shape M x N.
 // Bits: [4,6) D format (1 = F32), [7,10) A format (1 = BF16), [10,13) B format (1 = BF16),
 // [15] A major (0 = K), [16] B major (0 = K), [17,23) N >> 3, [24,29) M >> 4.
