@@ -40,6 +40,7 @@ struct dmd_handle {
   int lin = 0;                 // linearized master equation (DMD_FLAG_LINEAR)
   int pcfg = 0;                // pair-kernel shape variant (DMD_PAIR_CFG)
   int* d_pos = nullptr;        // k -> energy rank
+  int* d_inv = nullptr;        // energy rank -> k
   dmd::RowBlock* d_rb = nullptr;
   dmd::WorkItem* d_items = nullptr;
   int nitems = 0;
@@ -56,6 +57,8 @@ struct dmd_handle {
   dmd::TcTile* d_tiles = nullptr;
   int ntiles = 0, ngroups = 0, nmb = 0;
   int64_t pair_bytes = 0;      // stored operator bytes (dmd_pair_bytes)
+  float2* d_x0y0 = nullptr;    // tensor-core form: contraction of diag(f_ref), back-transformed, by k
+  double2* d_v0 = nullptr;     // tensor-core form: (prefac/2)(C0 + C0^dagger) by k
   double2* d_H = nullptr;      // [nk][nbdm^2]
   double2* d_eq = nullptr;     // [nk][nb2]
   double2* d_rs = nullptr;     // [nk][2][nb2] (per-thread form); Hermitian + anti-Hermitian coordinates (column-block form)
@@ -198,17 +201,17 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
     const int qc = h->nrhs < 8 ? h->nrhs : 8;
     const dim3 g(blocks_for(n, 256), (h->nrhs + qc - 1) / qc);
     if (h->prec == DMD_PREC_F64X)
-      k_prep_herm<ArithDF, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
+      k_prep_herm<ArithDF, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_inv, ta, h->expt,
                                                       (float2*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin,
-                                                      h->nrhs, qc, h->d_ph);
+                                                      h->nrhs, qc, h->d_ph, 1);
     else if (deviation_form(h->prec))
-      k_prep_herm<ArithF32, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
-                                                       (float*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin,
-                                                       h->nrhs, qc, h->d_ph);
+      k_prep_herm<ArithF32, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_inv, ta, h->expt,
+                                                       (float*)h->d_rs, h->use_tc ? nullptr : h->d_acc, h->d_hflag,
+                                                       fref, h->d_acc0, h->lin, h->nrhs, qc, h->d_ph, h->use_tc ? 0 : 1);
     else
-      k_prep_herm<ArithF64, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_pos, ta, h->expt,
+      k_prep_herm<ArithF64, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_inv, ta, h->expt,
                                                        (double*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin,
-                                                       h->nrhs, qc, h->d_ph);
+                                                       h->nrhs, qc, h->d_ph, 1);
   }
   h->launches++;
   CKL();
@@ -311,6 +314,15 @@ template <int NB>
 int launch_finish(dmd_handle* h, FinishArgs a) {
   ProfScope ps(h, 2);
   const dim3 g(blocks_for(h->nk, 128), h->nrhs);
+  if constexpr (NB == 2) {
+    if (h->use_tc) {  // split FP64 / FP32 finish of the tensor-core form
+      if (h->nbdm == NB) k_finish<NB, NB, true><<<g, 128, 0, h->st>>>(a);
+      else k_finish<NB, 0, true><<<g, 128, 0, h->st>>>(a);
+      h->launches++;
+      CKL();
+      return DMD_OK;
+    }
+  }
   if (h->nbdm == NB) k_finish<NB, NB><<<g, 128, 0, h->st>>>(a);
   else k_finish<NB><<<g, 128, 0, h->st>>>(a);
   h->launches++;
@@ -334,6 +346,9 @@ FinishArgs base_finish(dmd_handle* h, const double2* y) {
   a.y = y;
   a.acc = h->d_acc;
   a.ph = h->expt ? h->d_ph : nullptr;  // written by the prep kernels when the phase is on
+  a.fref = h->d_fref;
+  a.x0y0 = h->d_x0y0;
+  a.v0 = h->d_v0;
   a.pos = h->use_cb ? h->d_pos : nullptr;
   a.herm = h->use_cb;
   a.lin = h->lin;
@@ -579,6 +594,8 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
       (rc = dalloc(h, &h->d_items, L.items.size())))
     return rc;
   CK(cudaMemcpy(h->d_pos, L.pos.data(), L.pos.size() * 4, cudaMemcpyHostToDevice));
+  if ((rc = dalloc(h, &h->d_inv, (size_t)h->nk))) return rc;
+  CK(cudaMemcpy(h->d_inv, L.inv.data(), L.inv.size() * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_rb, L.rb.data(), L.rb.size() * sizeof(dmd::RowBlock), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_items, L.items.data(), L.items.size() * sizeof(dmd::WorkItem), cudaMemcpyHostToDevice));
   const int esz = elem_bytes(h->prec);
@@ -712,8 +729,9 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
   h->ngroups = (nk + TC_CG - 1) / TC_CG;
   h->nmb = (h->nrhs + TC_M - 1) / TC_M;
   int rc;
-  if ((rc = dalloc(h, &h->d_pos, (size_t)nk))) return rc;
+  if ((rc = dalloc(h, &h->d_pos, (size_t)nk)) || (rc = dalloc(h, &h->d_inv, (size_t)nk))) return rc;
   CK(cudaMemcpy(h->d_pos, L.pos.data(), (size_t)nk * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_inv, L.inv.data(), (size_t)nk * 4, cudaMemcpyHostToDevice));
   // directed entries (src << 1 | reverse) bucketed by row tile
   const size_t np = (size_t)h->npair;
   std::vector<size_t> start((size_t)h->ntiles + 1, 0);
@@ -859,8 +877,44 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
     CK(cudaMemcpy(h->d_fref, fw.data(), fw.size() * 8, cudaMemcpyHostToDevice));
   }
   if (out == DMD_OK && dev) {
-    if ((out = dalloc(h, &h->d_acc0, acc0.size()))) return out;
-    CK(cudaMemcpy(h->d_acc0, acc0.data(), acc0.size() * 16, cudaMemcpyHostToDevice));
+    // the split finish (k_finish<2, ., true>): X0, Y0 back-transformed by k and the constant
+    // V0 = (prefac/2)(C0 + C0^dagger), C0 = (1 - F) X0 - Y0 F (Hermitian reads of diagonal F)
+    const int n2 = h->nb2;
+    std::vector<float2> x0y0((size_t)nk * 2 * n2);
+    std::vector<cd> v0((size_t)nk * n2);
+    const double pf = 0.5 * h->prefac;
+    for (int k = 0; k < nk; ++k) {
+      const cd* a = &acc0[(size_t)L.pos[k] * 2 * n2];
+      cd X[16], Y[16];
+      for (int e = 0; e < n2; ++e) {
+        X[e] = a[e];
+        Y[e] = a[n2 + e];
+      }
+      for (int i = 0; i < nb; ++i)
+        for (int j = i + 1; j < nb; ++j) {  // X = (M^H)^-1 X' (dmd_kernels.cuh, k_finish)
+          const cd xu = X[i * nb + j], xl = X[j * nb + i], yu = Y[i * nb + j], yl = Y[j * nb + i];
+          X[i * nb + j] = {0.5 * (xu.re - xl.im), 0.5 * (xu.im + xl.re)};
+          X[j * nb + i] = {0.5 * (xu.re + xl.im), 0.5 * (xu.im - xl.re)};
+          Y[i * nb + j] = {0.5 * (yu.re - yl.im), 0.5 * (yu.im + yl.re)};
+          Y[j * nb + i] = {0.5 * (yu.re + yl.im), 0.5 * (yu.im - yl.re)};
+        }
+      const double* f = &fw[(size_t)k * nb];
+      cd C[16];
+      for (int i = 0; i < nb; ++i)
+        for (int j = 0; j < nb; ++j)
+          C[i * nb + j] = {(1 - f[i]) * X[i * nb + j].re - Y[i * nb + j].re * f[j],
+                           (1 - f[i]) * X[i * nb + j].im - Y[i * nb + j].im * f[j]};
+      for (int i = 0; i < nb; ++i)
+        for (int j = 0; j < nb; ++j) {
+          const cd c1 = C[i * nb + j], c2 = C[j * nb + i];
+          v0[(size_t)k * n2 + i * nb + j] = {pf * (c1.re + c2.re), pf * (c1.im - c2.im)};
+          x0y0[(size_t)k * 2 * n2 + i * nb + j] = make_float2((float)X[i * nb + j].re, (float)X[i * nb + j].im);
+          x0y0[(size_t)k * 2 * n2 + n2 + i * nb + j] = make_float2((float)Y[i * nb + j].re, (float)Y[i * nb + j].im);
+        }
+    }
+    if ((out = dalloc(h, &h->d_x0y0, x0y0.size())) || (out = dalloc(h, &h->d_v0, v0.size()))) return out;
+    CK(cudaMemcpy(h->d_x0y0, x0y0.data(), x0y0.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_v0, v0.data(), v0.size() * 16, cudaMemcpyHostToDevice));
   }
   return out;
 }
@@ -871,7 +925,7 @@ void release(dmd_handle* h) {
   if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
   void* ptrs[] = {h->d_err, h->d_pos, h->d_rb, h->d_items, h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
-                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph};
+                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {

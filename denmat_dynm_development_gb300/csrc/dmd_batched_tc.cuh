@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
                                                      double2* __restrict__ acc, size_t astride, double ysign,
                                                      const unsigned int* __restrict__ gate,
                                                      unsigned int* __restrict__ errflag) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   if (gate && *gate == 0u) return;
   // swizzled operand tiles start on 1024-byte boundaries (1 KB of slack is allocated)
   unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);

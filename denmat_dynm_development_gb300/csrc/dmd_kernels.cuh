@@ -79,6 +79,10 @@ struct FinishArgs {
   const double2* y;    // state the RHS is evaluated on
   const double2* acc;  // [nk][2][NB2], indexed by pos[k] when pos is set
   const double2* ph;   // D_k(i, j) = exp(i t (e_i - e_j)) of this evaluation [nk][NB2] (prep kernels)
+  // split finish (k_finish<.., DEV = true): acc holds the contraction of rho - F only, F = diag(fref)
+  const double* fref;  // [nk][NB]
+  const float2* x0y0;  // X0, Y0 = contraction of F, back-transformed [nk][2][NB2] (null: zero)
+  const double2* v0;   // (prefac/2)(C0 + C0^dagger), C0 = (1 - F) X0 - Y0 F, [nk][NB2] (null: zero)
   const int* pos;      // k -> accumulator row (column-block layout) or null
   int herm;            // accumulators hold X' = M^H X, Y' = M^H Y (Hermitian coordinates)
   int nrhs;            // batched form: states evaluated together (blockIdx.y), 1 otherwise
@@ -100,10 +104,23 @@ struct FinishArgs {
   TimeArg ta;
 };
 
+__device__ __forceinline__ float2 f2(double2 v) { return make_float2((float)v.x, (float)v.y); }
+__device__ __forceinline__ float2 fmul(float2 a, float2 b) {
+  return make_float2(__fmaf_rn(a.x, b.x, -a.y * b.y), __fmaf_rn(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 ffma(float2 a, float2 b, float2 c) {  // c + a*b
+  return make_float2(__fmaf_rn(a.x, b.x, __fmaf_rn(-a.y, b.y, c.x)), __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, c.y)));
+}
+
 // One thread per k: scattering finish + coherent term, then the stepper's update for this k.
 // ND > 0: the density matrix has ND = nbdm = NB bands (compile time, arrays in registers); ND = 0:
 // nbdm is read at run time.
-template <int NB, int ND = 0>
+// DEV (batched reduced-precision form): with rho = F + delta, F = diag(f_ref),
+//   c = D o C0 + (1 - F)(D o Xd) - (D o Yd) F - delta (D o (X0 + Xd)) - (D o (Y0 + Yd)) delta
+// (Hermitian operands from their upper triangles, F diagonal, C0 = (1 - F) X0 - Y0 F), so
+// (prefac/2)(c + c^dagger) = D o V0 + (prefac/2)(c1 + c1^dagger) with the per-k constant V0 in FP64
+// and the terms of first and second order in delta (c1) in FP32; the state update stays FP64.
+template <int NB, int ND = 0, bool DEV = false>
 __global__ void k_finish(FinishArgs a) {
   constexpr int NB2 = NB * NB;
   constexpr int NDA = ND > 0 ? ND : DMD_MAX_NBDM;  // array extent
@@ -164,7 +181,99 @@ __global__ void k_finish(FinishArgs a) {
   }
 
   // scattering finish on the window (evolve_eph.cpp:140-162, evolve_driver :21-32)
-  if (a.want_eph) {
+  if (DEV && a.want_eph) {
+    const double* ew = a.ew + (size_t)k * NB;
+    const double2* Xs = a.acc + (size_t)q * a.astride + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
+    float2 X[NB2], Y[NB2];
+#pragma unroll
+    for (int i = 0; i < NB2; ++i) {
+      X[i] = f2(Xs[i]);
+      Y[i] = f2(Xs[NB2 + i]);
+    }
+    if (a.herm) {  // X = (M^H)^-1 X'
+#pragma unroll
+      for (int i = 0; i < NB; ++i)
+#pragma unroll
+        for (int j = i + 1; j < NB; ++j) {
+          const float2 xu = X[i * NB + j], xl = X[j * NB + i], yu = Y[i * NB + j], yl = Y[j * NB + i];
+          X[i * NB + j] = make_float2(0.5f * (xu.x - xl.y), 0.5f * (xu.y + xl.x));
+          X[j * NB + i] = make_float2(0.5f * (xu.x + xl.y), 0.5f * (xu.y - xl.x));
+          Y[i * NB + j] = make_float2(0.5f * (yu.x - yl.y), 0.5f * (yu.y + yl.x));
+          Y[j * NB + i] = make_float2(0.5f * (yu.x + yl.y), 0.5f * (yu.y - yl.x));
+        }
+    }
+    const double* fk = a.fref + (size_t)k * NB;
+    float ff[NB];
+    float2 dh[NB2], D[NB2], PXd[NB2], PXt[NB2], PYd[NB2], PYt[NB2];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) ff[i] = (float)fk[i];
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        const int e = i * NB + j;
+        // herm_up(rho - F): upper triangle, real diagonal
+        if (i == j) dh[e] = make_float2((float)__dsub_rn(yk[(bs + i) * nd + bs + i].x, fk[i]), 0.f);
+        else if (i < j) dh[e] = f2(yk[(bs + i) * nd + bs + j]);
+        else {
+          const double2 u = yk[(bs + j) * nd + bs + i];
+          dh[e] = make_float2((float)u.x, -(float)u.y);
+        }
+        D[e] = make_float2(1.f, 0.f);
+        if (a.phase && i != j) D[e] = f2(a.ph ? a.ph[(size_t)k * NB2 + e] : ccis((ew[i] - ew[j]) * t));
+        const float2 x0 = a.x0y0 ? a.x0y0[(size_t)k * 2 * NB2 + e] : make_float2(0.f, 0.f);
+        const float2 y0 = a.x0y0 ? a.x0y0[(size_t)k * 2 * NB2 + NB2 + e] : make_float2(0.f, 0.f);
+        PXd[e] = fmul(D[e], X[e]);
+        PYd[e] = fmul(D[e], Y[e]);
+        PXt[e] = ffma(D[e], x0, PXd[e]);
+        PYt[e] = ffma(D[e], y0, PYd[e]);
+      }
+    float2 c[NB2];
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        const int e = i * NB + j;
+        if (a.lin) {
+          c[e] = PXd[e];
+        } else {
+          float2 s = make_float2((1.f - ff[i]) * PXd[e].x - ff[j] * PYd[e].x, (1.f - ff[i]) * PXd[e].y - ff[j] * PYd[e].y);
+#pragma unroll
+          for (int l = 0; l < NB; ++l) {
+            const float2 d1 = dh[i * NB + l], d2 = dh[l * NB + j];
+            s = ffma(make_float2(-d1.x, -d1.y), PXt[l * NB + j], s);
+            s = ffma(make_float2(-PYt[i * NB + l].x, -PYt[i * NB + l].y), d2, s);
+          }
+          c[e] = s;
+        }
+      }
+    const float pf = (float)(a.prefac * 0.5);
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int j = i; j < NB; ++j) {
+        const float2 c1 = c[i * NB + j], c2 = c[j * NB + i];
+        double2 v = mk2((double)(pf * (c1.x + c2.x)), (double)(pf * (c1.y - c2.y)));
+        if (a.v0) {  // D o V0 in FP64
+          const double2 w = a.v0[(size_t)k * NB2 + i * NB + j];
+          const double2 d = (i != j && a.phase) ? (a.ph ? a.ph[(size_t)k * NB2 + i * NB + j] : ccis((ew[i] - ew[j]) * t))
+                                                : mk2(1.0, 0.0);
+          v = cadd_rn(v, (i == j) ? w : cmul_rn(d, w));
+        }
+#pragma unroll
+        for (int w = 0; w < (i == j ? 1 : 2); ++w) {
+          const int ii = w ? j : i, jj = w ? i : j;
+          double2 u = w ? cconj(v) : v;
+          if (a.eq) {
+            const double2 qv = a.eq[(size_t)k * NB2 + ii * NB + jj];
+            if (ii == jj || a.picture == 1) u = csub_rn(u, qv);
+            else u = csub_rn(u, cmul_rn(qv, a.ph ? a.ph[(size_t)k * NB2 + ii * NB + jj] : ccis((ew[ii] - ew[jj]) * t)));
+          }
+          double2& o = f[(bs + ii) * nd + bs + jj];
+          o = cadd_rn(o, u);
+        }
+      }
+  } else if (a.want_eph) {
     const double* ew = a.ew + (size_t)k * NB;
     const double2* Xs = a.acc + (size_t)q * a.astride + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
     double2 X[NB2], Y[NB2];

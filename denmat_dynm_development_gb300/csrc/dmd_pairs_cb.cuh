@@ -209,8 +209,10 @@ struct ArithBF2 : ArithF32 {
 
 // ---------------------------------------------------------------------------------------------
 // Prep: Hermitian and anti-Hermitian coordinates of rt, st per k (written at pos[k]) and the
-// accumulators' start values (zero, or acc0). One thread per (k, element (i, j)) and chunk of qc
-// states; the thread of (i, j) with i < j writes the coordinates at (i, j) and (j, i). Raises *hflag
+// accumulators' start values (zero, or acc0; skipped when acc is null). One thread per (energy rank
+// p, element (i, j)) and chunk of qc states, k = inv[p], so that the stores run in position order;
+// the thread of (i, j) with i < j writes the coordinates at (i, j) and (j, i). ws = 0 skips the st
+// coordinates (the tensor-core form contracts rt only, s = -r there). Raises *hflag
 // when some rho_k is not exactly Hermitian. rs layout: [nrhs][nk][2][NB2] Hermitian part (r, s), then
 // the anti-Hermitian part; the batched form runs one grid row (blockIdx.y) per chunk of states, and
 // the phase D_k(i, j) = exp(i t (e_i - e_j)) is computed once per thread for all states of its chunk.
@@ -222,23 +224,25 @@ struct ArithBF2 : ArithF32 {
 // ---------------------------------------------------------------------------------------------
 template <typename A, int NB>
 __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict__ y, const double* __restrict__ ew,
-                            const int* __restrict__ pos, TimeArg ta, int phase, typename A::relem* __restrict__ rs,
+                            const int* __restrict__ inv, TimeArg ta, int phase, typename A::relem* __restrict__ rs,
                             double2* __restrict__ acc, unsigned int* __restrict__ hflag,
                             const double* __restrict__ fref, const double2* __restrict__ acc0, int lin,
-                            int nrhs, int qc, double2* __restrict__ ph) {
+                            int nrhs, int qc, double2* __restrict__ ph, int ws) {
   constexpr int NB2 = NB * NB;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nk * NB2) return;
   const int q0 = blockIdx.y * qc, q1 = min(nrhs, q0 + qc);
   const size_t cstride = (size_t)nk * 2 * NB2;  // coordinates (and sums) per state
   const size_t sstride = (size_t)nk * nbdm * nbdm;
-  const int k = idx / NB2, ab = idx - k * NB2, i = ab / NB, j = ab - i * NB;
-  const int p = pos[k];
+  const int p = idx / NB2, ab = idx - p * NB2, i = ab / NB, j = ab - i * NB;
+  const int k = inv[p];
   const size_t ax = (size_t)p * 2 * NB2 + ab;
-  const double2 a0 = acc0 ? acc0[ax] : mk2(0.0, 0.0), a1 = acc0 ? acc0[ax + NB2] : mk2(0.0, 0.0);
-  for (int q = q0; q < q1; ++q) {
-    acc[(size_t)q * cstride + ax] = a0;
-    acc[(size_t)q * cstride + ax + NB2] = a1;
+  if (acc) {
+    const double2 a0 = acc0 ? acc0[ax] : mk2(0.0, 0.0), a1 = acc0 ? acc0[ax + NB2] : mk2(0.0, 0.0);
+    for (int q = q0; q < q1; ++q) {
+      acc[(size_t)q * cstride + ax] = a0;
+      acc[(size_t)q * cstride + ax + NB2] = a1;
+    }
   }
   if (i > j) return;
   const double2* yk = y + (size_t)k * nbdm * nbdm;
@@ -253,13 +257,13 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
       if (fref) {
         const double dv = __dsub_rn(vij.x, fi);
         rh[ab] = A::from_double(dv);
-        rh[NB2 + ab] = A::from_double(lin ? 0.0 : -dv);
+        if (ws) rh[NB2 + ab] = A::from_double(lin ? 0.0 : -dv);
       } else {
         rh[ab] = A::from_double(vij.x);
-        rh[NB2 + ab] = A::from_double(1.0 - vij.x);
+        if (ws) rh[NB2 + ab] = A::from_double(1.0 - vij.x);
       }
       ra[ab] = A::from_double(vij.y);
-      ra[NB2 + ab] = A::from_double(lin ? 0.0 : 0.0 - vij.y);
+      if (ws) ra[NB2 + ab] = A::from_double(lin ? 0.0 : 0.0 - vij.y);
       if (vij.y != 0.0) atomicOr(hflag, 1u);
     }
     return;
@@ -285,18 +289,23 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
     const double2 r1 = cmul_rn(d, hij);                       // conj(D) o H
     rh[ab] = A::from_double(r1.x);
     rh[ji] = A::from_double(r1.y);
-    rh[NB2 + ab] = A::from_double(lin ? 0.0 : -r1.x);      // conj(D) o (1 - H) off the diagonal
-    rh[NB2 + ji] = A::from_double(lin ? 0.0 : -r1.y);
+    if (ws) {
+      rh[NB2 + ab] = A::from_double(lin ? 0.0 : -r1.x);      // conj(D) o (1 - H) off the diagonal
+      rh[NB2 + ji] = A::from_double(lin ? 0.0 : -r1.y);
+    }
     if (dif.x != 0.0 || dif.y != 0.0) {  // the anti-Hermitian part is read only when hflag is raised
       atomicOr(hflag, 1u);
       const double2 aij = mk2(__dmul_rn(dif.y, 0.5), __dmul_rn(-dif.x, 0.5));
       const double2 r2 = cmul_rn(d, aij);                     // conj(D) o A
       ra[ab] = A::from_double(r2.x);
       ra[ji] = A::from_double(r2.y);
-      ra[NB2 + ab] = A::from_double(lin ? 0.0 : -r2.x);    // conj(D) o (-A)
-      ra[NB2 + ji] = A::from_double(lin ? 0.0 : -r2.y);
+      if (ws) {
+        ra[NB2 + ab] = A::from_double(lin ? 0.0 : -r2.x);    // conj(D) o (-A)
+        ra[NB2 + ji] = A::from_double(lin ? 0.0 : -r2.y);
+      }
     } else {
-      ra[ab] = ra[ji] = ra[NB2 + ab] = ra[NB2 + ji] = A::from_double(0.0);
+      ra[ab] = ra[ji] = A::from_double(0.0);
+      if (ws) ra[NB2 + ab] = ra[NB2 + ji] = A::from_double(0.0);
     }
   }
 }
