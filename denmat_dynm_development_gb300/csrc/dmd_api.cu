@@ -58,7 +58,7 @@ struct dmd_handle {
   int ntiles = 0, ngroups = 0, nmb = 0;
   int64_t pair_bytes = 0;      // stored operator bytes (dmd_pair_bytes)
   float2* d_x0y0 = nullptr;    // tensor-core form: contraction of diag(f_ref), back-transformed, by k
-  double2* d_v0 = nullptr;     // tensor-core form: (prefac/2)(C0 + C0^dagger) by k
+  float2* d_v0 = nullptr;      // tensor-core form: (prefac/2)(C0 + C0^dagger) by k
   double2* d_H = nullptr;      // [nk][nbdm^2]
   double2* d_eq = nullptr;     // [nk][nb2]
   double2* d_rs = nullptr;     // [nk][2][nb2] (per-thread form); Hermitian + anti-Hermitian coordinates (column-block form)
@@ -253,12 +253,12 @@ void tc_launches(dmd_handle* h, size_t half) {
   const size_t apart = (size_t)h->ngroups * h->nmb * TC_ABLOCK;
   const size_t astride = (size_t)h->nk * 2 * h->nb2;
   const unsigned g = (unsigned)((size_t)h->ntiles * h->nmb);
-  const double ysign = h->lin ? 0.0 : -1.0;  // s = -r (deviation form) or 0 (linearized form)
+  const float ysign = h->lin ? 0.f : -1.f;  // s = -r (deviation form) or 0 (linearized form)
+  float2* accf = (float2*)h->d_acc;          // FP32 sums in the tensor-core form
   k_pairs_tc<false><<<g, 128, TC_SMEM_BYTES, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA, h->nmb, h->nrhs,
-                                                      h->nk, h->d_acc0, h->d_acc, astride, ysign, nullptr, h->d_err);
+                                                      h->nk, accf, astride, ysign, nullptr, h->d_err);
   k_pairs_tc<true><<<g, 128, TC_SMEM_BYTES, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA + apart, h->nmb,
-                                                     h->nrhs, h->nk, nullptr, h->d_acc, astride, ysign, h->d_hflag,
-                                                     h->d_err);
+                                                     h->nrhs, h->nk, accf, astride, ysign, h->d_hflag, h->d_err);
   (void)half;
   h->launches += 1;  // the packing launch; the two passes are counted with the other forms
 }
@@ -349,6 +349,7 @@ FinishArgs base_finish(dmd_handle* h, const double2* y) {
   a.fref = h->d_fref;
   a.x0y0 = h->d_x0y0;
   a.v0 = h->d_v0;
+  a.ph32 = h->use_tc ? (const float2*)h->d_ph : nullptr;  // the tensor-core prep stores FP32 phases
   a.pos = h->use_cb ? h->d_pos : nullptr;
   a.herm = h->use_cb;
   a.lin = h->lin;
@@ -881,7 +882,7 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
     // V0 = (prefac/2)(C0 + C0^dagger), C0 = (1 - F) X0 - Y0 F (Hermitian reads of diagonal F)
     const int n2 = h->nb2;
     std::vector<float2> x0y0((size_t)nk * 2 * n2);
-    std::vector<cd> v0((size_t)nk * n2);
+    std::vector<float2> v0((size_t)nk * n2);
     const double pf = 0.5 * h->prefac;
     for (int k = 0; k < nk; ++k) {
       const cd* a = &acc0[(size_t)L.pos[k] * 2 * n2];
@@ -907,14 +908,14 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
       for (int i = 0; i < nb; ++i)
         for (int j = 0; j < nb; ++j) {
           const cd c1 = C[i * nb + j], c2 = C[j * nb + i];
-          v0[(size_t)k * n2 + i * nb + j] = {pf * (c1.re + c2.re), pf * (c1.im - c2.im)};
+          v0[(size_t)k * n2 + i * nb + j] = make_float2((float)(pf * (c1.re + c2.re)), (float)(pf * (c1.im - c2.im)));
           x0y0[(size_t)k * 2 * n2 + i * nb + j] = make_float2((float)X[i * nb + j].re, (float)X[i * nb + j].im);
           x0y0[(size_t)k * 2 * n2 + n2 + i * nb + j] = make_float2((float)Y[i * nb + j].re, (float)Y[i * nb + j].im);
         }
     }
     if ((out = dalloc(h, &h->d_x0y0, x0y0.size())) || (out = dalloc(h, &h->d_v0, v0.size()))) return out;
     CK(cudaMemcpy(h->d_x0y0, x0y0.data(), x0y0.size() * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->d_v0, v0.data(), v0.size() * 16, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_v0, v0.data(), v0.size() * 8, cudaMemcpyHostToDevice));
   }
   return out;
 }

@@ -13,7 +13,8 @@
 // tile and up to 128 states one CTA computes
 //   D[q][n] = sum_(c, j) R[q][(c, j)] * B[(c, j)][n],  n < 128: (r, a, re|im) of X', n >= 128: (r, j, re|im) of -Y'
 // (M = 128 states, N = 256, K = 8 columns x 4 = 32 per group) as tcgen05 MMAs accumulating in tensor
-// memory over all of the tile's column groups, then writes each row's sums once: no atomics.
+// memory over all of the tile's column groups, then writes each row's sums once (FP32, as the
+// tensor memory holds them): no atomics.
 // Operands are bf16 hi + lo splits (x = hi + lo, 16 significant bits); the product keeps
 // hi*hi + hi*lo + lo*hi. Every operand row holds [hi (32) | lo (32)] = 128 bytes, so a tile is a
 // 128-byte-swizzled K-major tile and the three products are MMAs over K slices paired through
@@ -69,13 +70,14 @@ __global__ void k_pack_tc(int nk, int nrhs, int ngroups, int nmb, const float* _
   blk[tc_ci(m, kk + 32)] = __bfloat16_as_ushort(lo);
 }
 
-// IMAG: the anti-Hermitian pass (sums times i, added); otherwise acc = acc0 + sums (stored).
-// ysign: -1 (Y' = -D_Y, s = -r) or 0 (linearized form, s = 0).
+// IMAG: the anti-Hermitian pass (sums times i, added); otherwise acc = sums (stored). acc is FP32,
+// [state][position][X' (4) | Y' (4)], astride float2 per state. ysign: -1 (Y' = -D_Y, s = -r) or 0
+// (linearized form, s = 0).
 template <bool IMAG>
 __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ tiles, int ntiles,
                                                      const uint16_t* __restrict__ B, const uint16_t* __restrict__ A,
-                                                     int nmb, int nrhs, int nk, const double2* __restrict__ acc0,
-                                                     double2* __restrict__ acc, size_t astride, double ysign,
+                                                     int nmb, int nrhs, int nk, float2* __restrict__ acc,
+                                                     size_t astride, float ysign,
                                                      const unsigned int* __restrict__ gate,
                                                      unsigned int* __restrict__ errflag) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -156,9 +158,9 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
   }
   tc_fence_after();
   // epilogue: TMEM lane 32 w + l holds state q = 128 mb + 32 w + l. Per group of 4 rows a thread
-  // writes its state's 4 x 8 sums into shared memory (a row of 33 double2 per state), then the warp
-  // stores each state's 512 contiguous bytes with one coalesced instruction.
-  double2* wsm = (double2*)smem + (size_t)warp * 32 * 33;
+  // writes its state's 4 x 8 sums into shared memory (a row of 33 float2 per state), then the warp
+  // stores each state's 256 contiguous bytes with one coalesced instruction.
+  float2* wsm = (float2*)smem + (size_t)warp * 32 * 33;
   const int qb = mb * TC_M + warp * 32;
   const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
   for (int rq = 0; rq < 4; ++rq) {
@@ -170,27 +172,26 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
 #pragma unroll
       for (int i = 0; i < 32; ++i) vx[i] = vy[i] = 0.f;
     }
-    double2* my = wsm + lane * 33;
+    float2* my = wsm + lane * 33;
 #pragma unroll
     for (int rr = 0; rr < 4; ++rr)
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
-        my[rr * 8 + a] = mk2((double)vx[rr * 8 + 2 * a], (double)vx[rr * 8 + 2 * a + 1]);
-        my[rr * 8 + 4 + a] = mk2(ysign * (double)vy[rr * 8 + 2 * a], ysign * (double)vy[rr * 8 + 2 * a + 1]);
+        my[rr * 8 + a] = make_float2(vx[rr * 8 + 2 * a], vx[rr * 8 + 2 * a + 1]);
+        my[rr * 8 + 4 + a] = make_float2(ysign * vy[rr * 8 + 2 * a], ysign * vy[rr * 8 + 2 * a + 1]);
       }
     __syncwarp();
     // lane l covers row p0 + l / 8, element l % 8 of every state of the warp
     const int p = t * TC_TR + rq * 4 + (lane >> 3);
     if (p < nk) {
-      const double2 c = (!IMAG && acc0) ? acc0[(size_t)p * 8 + (lane & 7)] : mk2(0.0, 0.0);
       for (int j = 0; j < 32 && qb + j < nrhs; ++j) {
-        const double2 v = wsm[j * 33 + lane];
-        double2* dst = acc + (size_t)(qb + j) * astride + (size_t)p * 8 + (lane & 7);
+        const float2 v = wsm[j * 33 + lane];
+        float2* dst = acc + (size_t)(qb + j) * astride + (size_t)p * 8 + (lane & 7);
         if (IMAG) {
-          const double2 o = *dst;
-          *dst = mk2(o.x - v.y, o.y + v.x);
+          const float2 o = *dst;
+          *dst = make_float2(o.x - v.y, o.y + v.x);
         } else {
-          *dst = mk2(c.x + v.x, c.y + v.y);
+          *dst = v;
         }
       }
     }

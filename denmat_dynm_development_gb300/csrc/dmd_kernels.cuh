@@ -79,10 +79,12 @@ struct FinishArgs {
   const double2* y;    // state the RHS is evaluated on
   const double2* acc;  // [nk][2][NB2], indexed by pos[k] when pos is set
   const double2* ph;   // D_k(i, j) = exp(i t (e_i - e_j)) of this evaluation [nk][NB2] (prep kernels)
-  // split finish (k_finish<.., DEV = true): acc holds the contraction of rho - F only, F = diag(fref)
+  // split finish (k_finish<.., DEV = true): acc holds the FP32 contraction of rho - F only,
+  // F = diag(fref), and the phases are FP32 (ph32)
   const double* fref;  // [nk][NB]
   const float2* x0y0;  // X0, Y0 = contraction of F, back-transformed [nk][2][NB2] (null: zero)
-  const double2* v0;   // (prefac/2)(C0 + C0^dagger), C0 = (1 - F) X0 - Y0 F, [nk][NB2] (null: zero)
+  const float2* v0;    // (prefac/2)(C0 + C0^dagger), C0 = (1 - F) X0 - Y0 F, [nk][NB2] (null: zero)
+  const float2* ph32;  // D_k(i, j) in FP32 [nk][NB2]
   const int* pos;      // k -> accumulator row (column-block layout) or null
   int herm;            // accumulators hold X' = M^H X, Y' = M^H Y (Hermitian coordinates)
   int nrhs;            // batched form: states evaluated together (blockIdx.y), 1 otherwise
@@ -118,8 +120,9 @@ __device__ __forceinline__ float2 ffma(float2 a, float2 b, float2 c) {  // c + a
 // DEV (batched reduced-precision form): with rho = F + delta, F = diag(f_ref),
 //   c = D o C0 + (1 - F)(D o Xd) - (D o Yd) F - delta (D o (X0 + Xd)) - (D o (Y0 + Yd)) delta
 // (Hermitian operands from their upper triangles, F diagonal, C0 = (1 - F) X0 - Y0 F), so
-// (prefac/2)(c + c^dagger) = D o V0 + (prefac/2)(c1 + c1^dagger) with the per-k constant V0 in FP64
-// and the terms of first and second order in delta (c1) in FP32; the state update stays FP64.
+// (prefac/2)(c + c^dagger) = D o V0 + (prefac/2)(c1 + c1^dagger). The per-k constant V0 is formed
+// in FP64 on the host (where (1 - F) X0 and Y0 F cancel) and stored rounded to FP32; the terms of
+// first and second order in delta (c1) are FP32; the state update stays FP64.
 template <int NB, int ND = 0, bool DEV = false>
 __global__ void k_finish(FinishArgs a) {
   constexpr int NB2 = NB * NB;
@@ -182,13 +185,12 @@ __global__ void k_finish(FinishArgs a) {
 
   // scattering finish on the window (evolve_eph.cpp:140-162, evolve_driver :21-32)
   if (DEV && a.want_eph) {
-    const double* ew = a.ew + (size_t)k * NB;
-    const double2* Xs = a.acc + (size_t)q * a.astride + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
+    const float2* Xs = (const float2*)a.acc + (size_t)q * a.astride + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
     float2 X[NB2], Y[NB2];
 #pragma unroll
     for (int i = 0; i < NB2; ++i) {
-      X[i] = f2(Xs[i]);
-      Y[i] = f2(Xs[NB2 + i]);
+      X[i] = Xs[i];
+      Y[i] = Xs[NB2 + i];
     }
     if (a.herm) {  // X = (M^H)^-1 X'
 #pragma unroll
@@ -212,15 +214,11 @@ __global__ void k_finish(FinishArgs a) {
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
         const int e = i * NB + j;
-        // herm_up(rho - F): upper triangle, real diagonal
+        // herm_up(rho - F): upper triangle, real diagonal (the diagonal difference in FP64)
         if (i == j) dh[e] = make_float2((float)__dsub_rn(yk[(bs + i) * nd + bs + i].x, fk[i]), 0.f);
         else if (i < j) dh[e] = f2(yk[(bs + i) * nd + bs + j]);
-        else {
-          const double2 u = yk[(bs + j) * nd + bs + i];
-          dh[e] = make_float2((float)u.x, -(float)u.y);
-        }
-        D[e] = make_float2(1.f, 0.f);
-        if (a.phase && i != j) D[e] = f2(a.ph ? a.ph[(size_t)k * NB2 + e] : ccis((ew[i] - ew[j]) * t));
+        else dh[e] = make_float2(dh[j * NB + i].x, -dh[j * NB + i].y);
+        D[e] = (a.phase && i != j) ? a.ph32[(size_t)k * NB2 + e] : make_float2(1.f, 0.f);
         const float2 x0 = a.x0y0 ? a.x0y0[(size_t)k * 2 * NB2 + e] : make_float2(0.f, 0.f);
         const float2 y0 = a.x0y0 ? a.x0y0[(size_t)k * 2 * NB2 + NB2 + e] : make_float2(0.f, 0.f);
         PXd[e] = fmul(D[e], X[e]);
@@ -253,13 +251,9 @@ __global__ void k_finish(FinishArgs a) {
 #pragma unroll
       for (int j = i; j < NB; ++j) {
         const float2 c1 = c[i * NB + j], c2 = c[j * NB + i];
-        double2 v = mk2((double)(pf * (c1.x + c2.x)), (double)(pf * (c1.y - c2.y)));
-        if (a.v0) {  // D o V0 in FP64
-          const double2 w = a.v0[(size_t)k * NB2 + i * NB + j];
-          const double2 d = (i != j && a.phase) ? (a.ph ? a.ph[(size_t)k * NB2 + i * NB + j] : ccis((ew[i] - ew[j]) * t))
-                                                : mk2(1.0, 0.0);
-          v = cadd_rn(v, (i == j) ? w : cmul_rn(d, w));
-        }
+        float2 vf = make_float2(pf * (c1.x + c2.x), pf * (c1.y - c2.y));
+        if (a.v0) vf = ffma(D[i * NB + j], a.v0[(size_t)k * NB2 + i * NB + j], vf);  // + D o V0
+        const double2 v = mk2((double)vf.x, (double)vf.y);
 #pragma unroll
         for (int w = 0; w < (i == j ? 1 : 2); ++w) {
           const int ii = w ? j : i, jj = w ? i : j;
@@ -267,10 +261,13 @@ __global__ void k_finish(FinishArgs a) {
           if (a.eq) {
             const double2 qv = a.eq[(size_t)k * NB2 + ii * NB + jj];
             if (ii == jj || a.picture == 1) u = csub_rn(u, qv);
-            else u = csub_rn(u, cmul_rn(qv, a.ph ? a.ph[(size_t)k * NB2 + ii * NB + jj] : ccis((ew[ii] - ew[jj]) * t)));
+            else {
+              const float2 d = a.phase ? a.ph32[(size_t)k * NB2 + ii * NB + jj] : make_float2(1.f, 0.f);
+              u = csub_rn(u, cmul_rn(qv, mk2((double)d.x, (double)d.y)));
+            }
           }
           double2& o = f[(bs + ii) * nd + bs + jj];
-          o = cadd_rn(o, u);
+          o = a.want_coh ? cadd_rn(o, u) : u;
         }
       }
   } else if (a.want_eph) {

@@ -212,7 +212,9 @@ struct ArithBF2 : ArithF32 {
 // accumulators' start values (zero, or acc0; skipped when acc is null). One thread per (energy rank
 // p, element (i, j)) and chunk of qc states, k = inv[p], so that the stores run in position order;
 // the thread of (i, j) with i < j writes the coordinates at (i, j) and (j, i). ws = 0 skips the st
-// coordinates (the tensor-core form contracts rt only, s = -r there). Raises *hflag
+// coordinates (the tensor-core form contracts rt only, s = -r there); the tensor-core form (ws = 0,
+// FP32 coordinates) also takes its phases and its off-diagonal products in FP32 (the phase argument
+// is reduced modulo 2 pi in FP64) and stores FP32 phases in ph. Raises *hflag
 // when some rho_k is not exactly Hermitian. rs layout: [nrhs][nk][2][NB2] Hermitian part (r, s), then
 // the anti-Hermitian part; the batched form runs one grid row (blockIdx.y) per chunk of states, and
 // the phase D_k(i, j) = exp(i t (e_i - e_j)) is computed once per thread for all states of its chunk.
@@ -246,8 +248,13 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
   }
   if (i > j) return;
   const double2* yk = y + (size_t)k * nbdm * nbdm;
+  constexpr bool F32C = sizeof(typename A::relem) == 4;  // FP32 coordinates
+  const bool fast = F32C && ws == 0;
   if (i == j) {
-    if (ph && blockIdx.y == 0) ph[(size_t)k * NB2 + ab] = mk2(1.0, 0.0);
+    if (ph && blockIdx.y == 0) {
+      if (fast) ((float2*)ph)[(size_t)k * NB2 + ab] = make_float2(1.f, 0.f);
+      else ph[(size_t)k * NB2 + ab] = mk2(1.0, 0.0);
+    }
     const double fi = fref ? fref[(size_t)k * NB + i] : 0.0;
     for (int q = q0; q < q1; ++q) {
       typename A::relem* rh = rs + (size_t)q * cstride + (size_t)p * 2 * NB2;
@@ -269,6 +276,44 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
     return;
   }
   const int ji = j * NB + i;
+  if constexpr (F32C) {
+    if (fast) {
+      float2 dc = make_float2(1.f, 0.f);  // conj(D)
+      if (phase) {
+        const double x = (ew[k * NB + i] - ew[k * NB + j]) * eval_time(ta);
+        const double xr = fma(-6.283185307179586, rint(x * 0.15915494309189535), x);
+        float sn, cs;
+        sincosf((float)xr, &sn, &cs);
+        if (ph && blockIdx.y == 0) {
+          ((float2*)ph)[(size_t)k * NB2 + ab] = make_float2(cs, sn);
+          ((float2*)ph)[(size_t)k * NB2 + ji] = make_float2(cs, -sn);
+        }
+        dc = make_float2(cs, -sn);
+      }
+      for (int q = q0; q < q1; ++q) {
+        typename A::relem* rh = rs + (size_t)q * cstride + (size_t)p * 2 * NB2;
+        typename A::relem* ra = rs + (size_t)(nrhs + q) * cstride + (size_t)p * 2 * NB2;
+        const double2 vij = yk[(size_t)q * sstride + (bs + i) * nbdm + bs + j];
+        const double2 vji = yk[(size_t)q * sstride + (bs + j) * nbdm + bs + i];
+        float2 hf = make_float2(0.5f * ((float)vij.x + (float)vji.x), 0.5f * ((float)vij.y - (float)vji.y));
+        float2 af = make_float2(0.f, 0.f);
+        if (vij.x != vji.x || vij.y != -vji.y) {  // not exactly Hermitian: the anti-Hermitian pass runs
+          atomicOr(hflag, 1u);
+          const double2 hij = mk2(__dmul_rn(__dadd_rn(vij.x, vji.x), 0.5), __dmul_rn(__dsub_rn(vij.y, vji.y), 0.5));
+          const double2 dif = mk2(__dsub_rn(vij.x, vji.x), __dadd_rn(vij.y, vji.y));
+          hf = make_float2((float)hij.x, (float)hij.y);
+          af = make_float2((float)__dmul_rn(dif.y, 0.5), (float)__dmul_rn(-dif.x, 0.5));
+        }
+        const float2 r1 = make_float2(__fmaf_rn(dc.x, hf.x, -dc.y * hf.y), __fmaf_rn(dc.x, hf.y, dc.y * hf.x));
+        const float2 r2 = make_float2(__fmaf_rn(dc.x, af.x, -dc.y * af.y), __fmaf_rn(dc.x, af.y, dc.y * af.x));
+        rh[ab] = r1.x;
+        rh[ji] = r1.y;
+        ra[ab] = r2.x;
+        ra[ji] = r2.y;
+      }
+      return;
+    }
+  }
   double2 d = mk2(1.0, 0.0);
   if (phase) {
     const double2 dk = ccis((ew[k * NB + i] - ew[k * NB + j]) * eval_time(ta));
