@@ -1,0 +1,274 @@
+// Adjoint (reverse-mode) kernels of the Lindblad right-hand side, FP64.
+//
+// With the real inner product <A, B> = Re sum conj(A) B over all entries, the vector-Jacobian
+// product of f at a state u for a cotangent v (same layout as the state) is formed in three steps,
+// all written for complex n x n blocks (n = nb^2 for the pair operators):
+//
+//   local (per k):  cbar = (prefac/2)(v + v^H) on the e-ph window;
+//                   c = (1 - rho) Pdm - dm1P rho, Pdm = D o X, dm1P = D o Y  (forward sums at u)
+//                   Xbar = conj(D) o ((1 - rho)^H cbar),  Ybar = conj(D) o (-cbar rho^H)
+//                   rho_bar = -cbar Pdm^H - dm1P^H cbar   (+ the coherent term's adjoint)
+//   pairs:          the transposed contraction of the forward pair loop (evolve_eph.cpp:49-106):
+//                   rt_bar[k'] += P1^H Xbar[k],  st_bar[k'] += conj(P2) Ybar[k]  and, for k < k',
+//                   rt_bar[k] += P2^T Xbar[k'],  st_bar[k] += P1 Ybar[k'];
+//                   and the gradient with respect to the stored operators,
+//                   G1 += conj(Xbar[k]) rt[k']^T + conj(st[k]) Ybar[k']^T,
+//                   G2 += st[k'] conj(Ybar[k])^T + Xbar[k'] conj(rt[k])^T   (dJ = Re sum(dP o G))
+//   combine:        rho_bar += D o rt_bar - D o st_bar   (rt = conj(D) o rho, st = conj(D) o (1 - rho))
+//
+// The forward finish reads rho and 1 - rho through their upper triangles (zhemm); on Hermitian
+// states, where the trajectory lives, that map equals the plain-product map used here, so the
+// gradients with respect to the operators (and the initial state's Hermitian part) are exact.
+#pragma once
+#include "dmd_common.cuh"
+#include "dmd_kernels.cuh"
+
+namespace dmd {
+
+struct AdjLocalArgs {
+  int nk, nbdm, bs, picture, phase, herm, lin, want_coh;
+  double prefac, t;
+  const double2* u;     // state the RHS was evaluated on [k][nbdm^2]
+  const double2* vbar;  // cotangent of the RHS [k][nbdm^2]
+  const double2* acc;   // forward sums X', Y' at u ([.][2][NB2], by pos[k] when pos is set)
+  const int* pos;
+  const double2* ph;    // phases D_k of this evaluation (or null)
+  const double* ew;     // [nk][NB]
+  const double* edm;    // [nk][nbdm]
+  const double2* H;     // coherent H_k (or null)
+  double2* Xb;          // [k][NB2]
+  double2* Yb;
+  double2* rt;          // forward coordinates conj(D) o rho, conj(D) o (1 - rho) [k][NB2]
+  double2* st;
+  double2* ubar;        // [k][nbdm^2]: coherent adjoint + local e-ph adjoint
+};
+
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {  // conj(a) * b
+  return mk2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return mk2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return mk2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return mk2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+
+template <int NB>
+__global__ void k_adj_local(AdjLocalArgs a) {
+  constexpr int NB2 = NB * NB;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.nk) return;
+  const int nd = a.nbdm, nd2 = nd * nd;
+  const double2* yk = a.u + (size_t)k * nd2;
+  const double2* vk = a.vbar + (size_t)k * nd2;
+  double2* ub = a.ubar + (size_t)k * nd2;
+  for (int e = 0; e < nd2; ++e) ub[e] = mk2(0.0, 0.0);
+  // coherent term -i[H(t), rho]: adjoint i(H v - v H) (H Hermitian, read from its upper triangle)
+  if (a.want_coh) {
+    const double* ek = a.edm + (size_t)k * nd;
+    if (a.H) {
+      const double2* Hk = a.H + (size_t)k * nd2;
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j) {
+          double2 s = mk2(0.0, 0.0);
+          for (int l = 0; l < nd; ++l) {
+            // Ht(i, l) and Ht(l, j) of the forward: upper triangle, interaction-picture phase
+            double2 hil, hlj;
+            {
+              const int r = i < l ? i : l, c = i < l ? l : i;
+              double2 hv = (r == c) ? mk2(Hk[r * nd + r].x, 0.0) : Hk[r * nd + c];
+              if (a.picture == 0 && r != c) hv = cmul(hv, ccis((ek[r] - ek[c]) * a.t));
+              hil = (i <= l) ? hv : cconj(hv);
+            }
+            {
+              const int r = l < j ? l : j, c = l < j ? j : l;
+              double2 hv = (r == c) ? mk2(Hk[r * nd + r].x, 0.0) : Hk[r * nd + c];
+              if (a.picture == 0 && r != c) hv = cmul(hv, ccis((ek[r] - ek[c]) * a.t));
+              hlj = (l <= j) ? hv : cconj(hv);
+            }
+            s = cadd(s, csub(cmul(hil, vk[l * nd + j]), cmul(vk[i * nd + l], hlj)));
+          }
+          ub[i * nd + j] = mk2(-s.y, s.x);  // i * s
+        }
+    } else if (a.picture == 1) {  // -i[E, rho]: adjoint i (e_i - e_j) v_ij
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j) {
+          const double w = ek[i] - ek[j];
+          const double2 v = vk[i * nd + j];
+          ub[i * nd + j] = mk2(-w * v.y, w * v.x);
+        }
+    }
+  }
+  // e-ph window
+  const double2* Xs = a.acc + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
+  double2 X[NB2], Y[NB2];
+  for (int e = 0; e < NB2; ++e) {
+    X[e] = Xs[e];
+    Y[e] = Xs[NB2 + e];
+  }
+  if (a.herm) {  // X = (M^H)^-1 X'
+    for (int i = 0; i < NB; ++i)
+      for (int j = i + 1; j < NB; ++j) {
+        const double2 xu = X[i * NB + j], xl = X[j * NB + i], yu = Y[i * NB + j], yl = Y[j * NB + i];
+        X[i * NB + j] = mk2(0.5 * (xu.x - xl.y), 0.5 * (xu.y + xl.x));
+        X[j * NB + i] = mk2(0.5 * (xu.x + xl.y), 0.5 * (xu.y - xl.x));
+        Y[i * NB + j] = mk2(0.5 * (yu.x - yl.y), 0.5 * (yu.y + yl.x));
+        Y[j * NB + i] = mk2(0.5 * (yu.x + yl.y), 0.5 * (yu.y - yl.x));
+      }
+  }
+  const double* ew = a.ew + (size_t)k * NB;
+  const double pf = 0.5 * a.prefac;
+  double2 D[NB2], r[NB2], om[NB2], cb[NB2], Pdm[NB2], dmP[NB2];
+  for (int i = 0; i < NB; ++i)
+    for (int j = 0; j < NB; ++j) {
+      const int e = i * NB + j;
+      D[e] = mk2(1.0, 0.0);
+      if (a.phase && i != j) D[e] = a.ph ? a.ph[(size_t)k * NB2 + e] : ccis((ew[i] - ew[j]) * a.t);
+      r[e] = yk[(a.bs + i) * nd + a.bs + j];
+      om[e] = (i == j) ? mk2(1.0 - r[e].x, -r[e].y) : mk2(-r[e].x, -r[e].y);
+      const double2 v1 = vk[(a.bs + i) * nd + a.bs + j], v2 = vk[(a.bs + j) * nd + a.bs + i];
+      cb[e] = mk2(pf * (v1.x + v2.x), pf * (v1.y - v2.y));
+      Pdm[e] = cmul(D[e], X[e]);
+      dmP[e] = cmul(D[e], Y[e]);
+    }
+  double2* Xbk = a.Xb + (size_t)k * NB2;
+  double2* Ybk = a.Yb + (size_t)k * NB2;
+  for (int i = 0; i < NB; ++i)
+    for (int j = 0; j < NB; ++j) {
+      const int e = i * NB + j;
+      double2 pb = mk2(0.0, 0.0), db = mk2(0.0, 0.0), rb = mk2(0.0, 0.0);
+      if (a.lin) {
+        pb = cb[e];
+      } else {
+        for (int l = 0; l < NB; ++l) {
+          pb = cadd(pb, cmulc(om[l * NB + i], cb[l * NB + j]));               // (1 - rho)^H cbar
+          db = csub(db, cmul(cb[i * NB + l], cconj(r[j * NB + l])));          // -cbar rho^H
+          rb = csub(rb, cmul(cb[i * NB + l], cconj(Pdm[j * NB + l])));        // -cbar Pdm^H
+          rb = csub(rb, cmulc(dmP[l * NB + i], cb[l * NB + j]));              // -dm1P^H cbar
+        }
+      }
+      Xbk[e] = cmulc(D[e], pb);
+      Ybk[e] = cmulc(D[e], db);
+      a.rt[(size_t)k * NB2 + e] = cmulc(D[e], r[e]);
+      a.st[(size_t)k * NB2 + e] = cmulc(D[e], om[e]);
+      double2& o = ub[(a.bs + i) * nd + a.bs + j];
+      o = cadd(o, rb);
+    }
+}
+
+// Transposed pair contraction and the operator gradient. One thread per (pair, index b).
+template <int NB>
+__global__ void k_adj_pairs(long long npair, const int2* __restrict__ kk, const double2* __restrict__ P,
+                            const double2* __restrict__ Xb, const double2* __restrict__ Yb,
+                            const double2* __restrict__ rt, const double2* __restrict__ st, double* __restrict__ rtb,
+                            double* __restrict__ stb, double2* __restrict__ G) {
+  constexpr int NB2 = NB * NB, NB4 = NB2 * NB2;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= npair * NB2) return;
+  const long long p = idx / NB2;
+  const int b = (int)(idx - p * NB2);
+  const int2 kp2 = kk[p];
+  const int k = kp2.x, kq = kp2.y;
+  const double2* P1 = P + (size_t)p * 2 * NB4;
+  const double2* P2 = P1 + NB4;
+  double2* G1 = G + (size_t)p * 2 * NB4;
+  double2* G2 = G1 + NB4;
+  const double2* Xk = Xb + (size_t)k * NB2;
+  const double2* Yk = Yb + (size_t)k * NB2;
+  const double2* rtq = rt + (size_t)kq * NB2;
+  const double2* stq = st + (size_t)kq * NB2;
+  double2 a1 = mk2(0.0, 0.0), a2 = mk2(0.0, 0.0);
+  for (int a = 0; a < NB2; ++a) {
+    a1 = cadd(a1, cmulc(P1[a * NB2 + b], Xk[a]));  // P1^H Xbar[k]
+    a2 = cadd(a2, cmulc(P2[b * NB2 + a], Yk[a]));  // conj(P2) Ybar[k]
+  }
+  atomicAdd(&rtb[((size_t)kq * NB2 + b) * 2], a1.x);
+  atomicAdd(&rtb[((size_t)kq * NB2 + b) * 2 + 1], a1.y);
+  atomicAdd(&stb[((size_t)kq * NB2 + b) * 2], a2.x);
+  atomicAdd(&stb[((size_t)kq * NB2 + b) * 2 + 1], a2.y);
+  const bool rev = k < kq;
+  const double2* Xq = Xb + (size_t)kq * NB2;
+  const double2* Yq = Yb + (size_t)kq * NB2;
+  const double2* rtk = rt + (size_t)k * NB2;
+  const double2* stk = st + (size_t)k * NB2;
+  for (int a = 0; a < NB2; ++a) {
+    double2 g1 = cmulc(Xk[a], rtq[b]);                      // conj(Xbar[k][a]) rt[k'][b]
+    double2 g2 = cmulc(Yk[b], stq[a]);                      // st[k'][a] conj(Ybar[k][b])
+    if (rev) {
+      g1 = cadd(g1, cmulc(stk[a], Yq[b]));                  // conj(st[k][a]) Ybar[k'][b]
+      g2 = cadd(g2, cmulc(rtk[b], Xq[a]));                  // Xbar[k'][a] conj(rt[k][b])
+    }
+    G1[a * NB2 + b] = cadd(G1[a * NB2 + b], g1);
+    G2[a * NB2 + b] = cadd(G2[a * NB2 + b], g2);
+  }
+  if (rev) {
+    double2 a3 = mk2(0.0, 0.0), a4 = mk2(0.0, 0.0);
+    for (int a = 0; a < NB2; ++a) {
+      a3 = cadd(a3, cmul(P2[a * NB2 + b], Xq[a]));          // P2^T Xbar[k']
+      a4 = cadd(a4, cmul(P1[b * NB2 + a], Yq[a]));          // P1 Ybar[k']
+    }
+    atomicAdd(&rtb[((size_t)k * NB2 + b) * 2], a3.x);
+    atomicAdd(&rtb[((size_t)k * NB2 + b) * 2 + 1], a3.y);
+    atomicAdd(&stb[((size_t)k * NB2 + b) * 2], a4.x);
+    atomicAdd(&stb[((size_t)k * NB2 + b) * 2 + 1], a4.y);
+  }
+}
+
+// ubar (window) += D o rt_bar - D o st_bar; then ybar += ubar and, when kprev is set,
+// kprev += c * ubar. One thread per state element.
+template <int NB>
+__global__ void k_adj_combine(int nk, int nbdm, int bs, int phase, double t, const double* __restrict__ ew,
+                              const double2* __restrict__ ph, const double2* __restrict__ rtb,
+                              const double2* __restrict__ stb, const double2* __restrict__ ubar,
+                              double2* __restrict__ ybar, double2* __restrict__ kprev, double c) {
+  constexpr int NB2 = NB * NB;
+  const int nd2 = nbdm * nbdm;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)nk * nd2) return;
+  const int k = (int)(idx / nd2), e = (int)(idx - (long long)k * nd2), ii = e / nbdm, jj = e - ii * nbdm;
+  double2 u = ubar[idx];
+  const int i = ii - bs, j = jj - bs;
+  if (i >= 0 && i < NB && j >= 0 && j < NB) {
+    const int w = i * NB + j;
+    double2 D = mk2(1.0, 0.0);
+    if (phase && i != j) D = ph ? ph[(size_t)k * NB2 + w] : ccis((ew[(size_t)k * NB + i] - ew[(size_t)k * NB + j]) * t);
+    u = cadd(u, cmul(D, csub(rtb[(size_t)k * NB2 + w], stb[(size_t)k * NB2 + w])));
+  }
+  ybar[idx] = cadd(ybar[idx], u);
+  if (kprev) kprev[idx] = cadd(kprev[idx], mk2(c * u.x, c * u.y));
+}
+
+// cotangent of an observable total (observable.h:356-366) with weight w:
+// ybar[k][b][i] += w * prefac * conj(o_t(i, b)) for i in [bs, be)
+__global__ void k_adj_obs(int nk, int nbdm, int bs, int be, const double2* __restrict__ obs,
+                          const double* __restrict__ edm, double t, int picture, double w, double2* __restrict__ ybar) {
+  const int nd2 = nbdm * nbdm;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)nk * nd2) return;
+  const int k = (int)(idx / nd2), e = (int)(idx - (long long)k * nd2), b = e / nbdm, i = e - b * nbdm;
+  if (i < bs || i >= be) return;
+  const double2 oib = obs[(size_t)k * nd2 + i * nbdm + b];
+  const double2 ot = (i == b || picture == 1) ? oib : cmul(oib, ccis((edm[(size_t)k * nbdm + i] - edm[(size_t)k * nbdm + b]) * t));
+  ybar[idx] = cadd(ybar[idx], mk2(w * ot.x, -w * ot.y));
+}
+
+// out = y + c k; out = c x
+__global__ void k_axpy(size_t n, double2* __restrict__ out, const double2* __restrict__ y, double c,
+                       const double2* __restrict__ k) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = mk2(fma(c, k[i].x, y[i].x), fma(c, k[i].y, y[i].y));
+}
+__global__ void k_scale(size_t n, double2* __restrict__ out, double c, const double2* __restrict__ x) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = mk2(c * x[i].x, c * x[i].y);
+}
+// y_next = y + h/6 (k1 + 2 k2 + 2 k3 + k4)
+__global__ void k_rk4_final(size_t n, double2* __restrict__ out, const double2* __restrict__ y,
+                            const double2* __restrict__ K, size_t ks, double h) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 k1 = K[i], k2 = K[ks + i], k3 = K[2 * ks + i], k4 = K[3 * ks + i];
+  const double sx = k1.x + 2.0 * k2.x + 2.0 * k3.x + k4.x, sy = k1.y + 2.0 * k2.y + 2.0 * k3.y + k4.y;
+  out[i] = mk2(y[i].x + h / 6.0 * sx, y[i].y + h / 6.0 * sy);
+}
+
+}  // namespace dmd

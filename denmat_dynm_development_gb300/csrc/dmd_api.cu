@@ -10,6 +10,7 @@
 #include <thread>
 #include <vector>
 
+#include "dmd_adjoint.cuh"
 #include "dmd_batched_tc.cuh"
 #include "dmd_gpu.h"
 #include "dmd_kernels.cuh"
@@ -57,6 +58,9 @@ struct dmd_handle {
   dmd::TcTile* d_tiles = nullptr;
   int ntiles = 0, ngroups = 0, nmb = 0;
   int64_t pair_bytes = 0;      // stored operator bytes (dmd_pair_bytes)
+  int adj = 0;                 // DMD_FLAG_ADJOINT: pair operators also in stored order (d_Praw, d_kkraw)
+  double2* d_Praw = nullptr;   // [npair][2][nb4] folded P1, P2
+  int2* d_kkraw = nullptr;
   float2* d_x0y0 = nullptr;    // tensor-core form: contraction of diag(f_ref), back-transformed, by k
   float2* d_v0 = nullptr;      // tensor-core form: (prefac/2)(C0 + C0^dagger) by k
   double2* d_H = nullptr;      // [nk][nbdm^2]
@@ -400,7 +404,12 @@ int rhs_plain(dmd_handle* h, double t, const double2* in, double2* out) {
   return rhs(h, in, time_value(t), fa);
 }
 
-int upload_pairs(dmd_handle* h, const dmd_desc* d) {
+// pair operators in stored order, folded with the additive operators: dP [npair][2][nb4], dkk [npair]
+int upload_raw(dmd_handle* h, const dmd_desc* d, double2* dP, int2* dkk);
+
+int upload_pairs(dmd_handle* h, const dmd_desc* d) { return upload_raw(h, d, h->d_P, h->d_kk); }
+
+int upload_raw(dmd_handle* h, const dmd_desc* d, double2* dP, int2* dkk) {
   const size_t nb4 = (size_t)h->nb4;
   const size_t chunk = (size_t)1 << 16;  // pairs per staging chunk
   double2* stage = nullptr;
@@ -434,8 +443,8 @@ int upload_pairs(dmd_handle* h, const dmd_desc* d) {
       }
     }
     if (rc) break;
-    e = cudaMemcpy(h->d_P + (size_t)p0 * 2 * nb4, stage, n * 2 * nb4 * sizeof(double2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(h->d_kk + p0, kst, n * sizeof(int2), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(dP + (size_t)p0 * 2 * nb4, stage, n * 2 * nb4 * sizeof(double2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dkk + p0, kst, n * sizeof(int2), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) rc = fail(h, DMD_E_CUDA, std::string("P upload: ") + cudaGetErrorString(e));
   }
   cudaFreeHost(stage);
@@ -926,7 +935,7 @@ void release(dmd_handle* h) {
   if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
   void* ptrs[] = {h->d_err, h->d_pos, h->d_rb, h->d_items, h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
-                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0};
+                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0, h->d_Praw, h->d_kkraw};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -941,6 +950,123 @@ void release(dmd_handle* h) {
   for (auto e : h->tev)
     if (e) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
+}
+
+// ---------------------------------------------------------------------------------------------
+// adjoint (dmd_adjoint_rk4): work buffers, forward RK4 with stored stage inputs, one VJP
+// ---------------------------------------------------------------------------------------------
+struct AdjWork {
+  dmd_handle* h = nullptr;
+  std::vector<void*> owned;
+  double2 *ck = nullptr, *U = nullptr, *yb = nullptr, *ub = nullptr, *kb = nullptr, *tmp = nullptr;
+  double2 *Xb = nullptr, *Yb = nullptr, *rt = nullptr, *st = nullptr, *rtb = nullptr, *stb = nullptr, *G = nullptr;
+  ~AdjWork() {
+    for (void* p : owned) cudaFree(p);
+  }
+  template <typename T>
+  int get(T** p, size_t n) {
+    int rc = dalloc(h, p, n);
+    if (rc == DMD_OK) owned.push_back((void*)*p);
+    return rc;
+  }
+};
+
+// y_out = one RK4 step of y; the stage inputs u1..u4 go to U[0..3] (stride n) when U is set
+int adj_rk4_step(dmd_handle* h, const double2* y, double t, double dt, double2* U, double2* y_out, double2* tmp) {
+  const size_t n = h->nstate;
+  const unsigned g = blocks_for((long long)n, 256);
+  double2* K = h->d_K;
+  int rc;
+  if (U) CK(cudaMemcpyAsync(U, y, n * 16, cudaMemcpyDeviceToDevice, h->st));
+  if ((rc = rhs_plain(h, t, y, K))) return rc;
+  double2* u = U ? U + n : tmp;
+  k_axpy<<<g, 256, 0, h->st>>>(n, u, y, 0.5 * dt, K);
+  if ((rc = rhs_plain(h, t + 0.5 * dt, u, K + n))) return rc;
+  u = U ? U + 2 * n : tmp;
+  k_axpy<<<g, 256, 0, h->st>>>(n, u, y, 0.5 * dt, K + n);
+  if ((rc = rhs_plain(h, t + 0.5 * dt, u, K + 2 * n))) return rc;
+  u = U ? U + 3 * n : tmp;
+  k_axpy<<<g, 256, 0, h->st>>>(n, u, y, dt, K + 2 * n);
+  if ((rc = rhs_plain(h, t + dt, u, K + 3 * n))) return rc;
+  k_rk4_final<<<g, 256, 0, h->st>>>(n, y_out, y, K, n, dt);
+  h->launches += 5;
+  CKL();
+  return DMD_OK;
+}
+
+// ybar += VJP_f(u, t)(vbar); kprev += c * VJP_f(u, t)(vbar) when kprev is set
+template <int NB>
+int adj_vjp_nb(dmd_handle* h, AdjWork& w, const double2* u, double t, const double2* vbar, double2* kprev, double c) {
+  int rc;
+  const TimeArg ta = time_value(t);
+  if ((rc = launch_prep<NB>(h, u, ta)) || (rc = launch_pairs<NB>(h))) return rc;  // forward sums at u
+  CK(cudaMemsetAsync(h->d_hflag, 0, sizeof(unsigned int), h->st));
+  const size_t nk2 = (size_t)h->nk * NB * NB;
+  CK(cudaMemsetAsync(w.rtb, 0, nk2 * 16, h->st));
+  CK(cudaMemsetAsync(w.stb, 0, nk2 * 16, h->st));
+  AdjLocalArgs a;
+  a.nk = h->nk;
+  a.nbdm = h->nbdm;
+  a.bs = h->bs;
+  a.picture = h->picture;
+  a.phase = h->expt;
+  a.herm = h->use_cb;
+  a.lin = h->lin;
+  a.want_coh = (h->picture == DMD_PICTURE_SCHRODINGER || h->d_H) ? 1 : 0;
+  a.prefac = h->prefac;
+  a.t = t;
+  a.u = u;
+  a.vbar = vbar;
+  a.acc = h->d_acc;
+  a.pos = h->use_cb ? h->d_pos : nullptr;
+  a.ph = h->expt ? h->d_ph : nullptr;
+  a.ew = h->d_ew;
+  a.edm = h->d_edm;
+  a.H = h->d_H;
+  a.Xb = w.Xb;
+  a.Yb = w.Yb;
+  a.rt = w.rt;
+  a.st = w.st;
+  a.ubar = w.ub;
+  k_adj_local<NB><<<blocks_for(h->nk, 128), 128, 0, h->st>>>(a);
+  if (h->npair > 0) {
+    const double2* P = h->use_cb ? h->d_Praw : h->d_P;
+    const int2* kk = h->use_cb ? h->d_kkraw : h->d_kk;
+    k_adj_pairs<NB><<<blocks_for(h->npair * NB * NB, 128), 128, 0, h->st>>>(h->npair, kk, P, w.Xb, w.Yb, w.rt, w.st,
+                                                                           (double*)w.rtb, (double*)w.stb, w.G);
+  }
+  k_adj_combine<NB><<<blocks_for((long long)h->nstate, 256), 256, 0, h->st>>>(
+      h->nk, h->nbdm, h->bs, h->expt, t, h->d_ew, h->expt ? h->d_ph : nullptr, w.rtb, w.stb, w.ub, w.yb, kprev, c);
+  h->launches += 3;
+  CKL();
+  return DMD_OK;
+}
+
+int adj_vjp(dmd_handle* h, AdjWork& w, const double2* u, double t, const double2* vbar, double2* kprev, double c) {
+  switch (h->nb) {
+    case 1: return adj_vjp_nb<1>(h, w, u, t, vbar, kprev, c);
+    case 2: return adj_vjp_nb<2>(h, w, u, t, vbar, kprev, c);
+    case 3: return adj_vjp_nb<3>(h, w, u, t, vbar, kprev, c);
+    case 4: return adj_vjp_nb<4>(h, w, u, t, vbar, kprev, c);
+  }
+  return fail(h, DMD_E_ARG, "nb out of range");
+}
+
+// total of observable `slot` on the device state y at time t (dmd_measure's reduction)
+int measure_on(dmd_handle* h, int slot, int bstart, int bend, const double2* y, double t, double* tot) {
+  const unsigned nbk = blocks_for(h->nk, 256);
+  if (2 * nbk > red_elems(h)) return fail(h, DMD_E_ARG, "nk too large for the observable reduction");
+  k_measure<<<nbk, 256, 0, h->st>>>(h->nk, h->nbdm, bstart, bend, h->d_obs[slot], h->d_f[slot], h->d_edm, t,
+                                    h->picture, y, h->d_red);
+  h->launches++;
+  CKL();
+  std::vector<double> part(2 * nbk);
+  CK(cudaMemcpyAsync(part.data(), h->d_red, 2 * nbk * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  double s1 = 0;
+  for (unsigned b = 0; b < nbk; ++b) s1 += part[2 * b];
+  *tot = s1 * h->obs_prefac[slot];
+  return DMD_OK;
 }
 
 int check_state(dmd_handle* h) {
@@ -983,7 +1109,8 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
     return DMD_E_ARG;
   if (d->nkpair > 0 && (!d->k1st || !d->k2nd || !d->P1 || !d->P2)) return DMD_E_ARG;
   if ((d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
-  if (d->flags & ~DMD_FLAG_LINEAR) return DMD_E_ARG;
+  if (d->flags & ~(DMD_FLAG_LINEAR | DMD_FLAG_ADJOINT)) return DMD_E_ARG;
+  if ((d->flags & DMD_FLAG_ADJOINT) && d->nrhs > 1) return DMD_E_ARG;
   const int nrhs = d->nrhs > 1 ? d->nrhs : 1;
   // batched form: FP32 or bf16 hi+lo storage on the column-block contraction
   if (nrhs > 1 && (d->precision != DMD_PREC_F32 && d->precision != DMD_PREC_BF16X2)) return DMD_E_ARG;
@@ -1013,6 +1140,7 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   h->expt = d->expt ? 1 : 0;
   h->prec = d->precision;
   h->lin = (d->flags & DMD_FLAG_LINEAR) ? 1 : 0;
+  h->adj = (d->flags & DMD_FLAG_ADJOINT) ? 1 : 0;
   h->nrhs = nrhs;
   h->nstate1 = (size_t)h->nk * h->nbdm * h->nbdm;
   h->nstate = h->nstate1 * nrhs;
@@ -1062,6 +1190,11 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
     h->pair_bytes = h->use_cb ? (int64_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) : (int64_t)h->npair * 2 * h->nb4 * 16;
   if ((rc = h->use_tc ? upload_pairs_tc(h, d) : h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d)))
     return bail(rc);
+  if (h->adj && h->use_cb && h->npair > 0) {  // the adjoint's transposed contraction reads stored-order P
+    if ((rc = dalloc(h, &h->d_Praw, (size_t)h->npair * 2 * h->nb4)) || (rc = dalloc(h, &h->d_kkraw, (size_t)h->npair)) ||
+        (rc = upload_raw(h, d, h->d_Praw, h->d_kkraw)))
+      return bail(rc);
+  }
   if (cudaMemset(h->d_y, 0, h->nstate * 16) != cudaSuccess || cudaMemset(h->d_step, 0, 8) != cudaSuccess ||
       cudaMemset(h->d_err, 0, sizeof(unsigned int)) != cudaSuccess ||
       cudaMemset(h->d_hflag, 0, sizeof(unsigned int)) != cudaSuccess)
@@ -1454,6 +1587,116 @@ int dmd_measure_batch(dmd_handle* h, int slot, int bstart, int bend, double* tot
     }
     if (tot) tot[q] = s1 * h->obs_prefac[slot];
     if (tot_amp) tot_amp[q] = s2 * h->obs_prefac[slot];
+  }
+  return DMD_OK;
+}
+
+int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64_t nsteps, int64_t checkpoint,
+                    int slot, int bstart, int bend, int64_t nobs, const int64_t* obs_step,
+                    const double* obs_weight, double* s_obs, double* dJdP, double* dJdy0) {
+  if (!h || !y0 || nsteps < 1 || checkpoint < 1 || nobs < 0 || (nobs > 0 && (!obs_step || !obs_weight)))
+    return DMD_E_ARG;
+  if (slot < 0 || slot >= 8 || !h->d_obs[slot] || bstart < 0 || bend > h->nbdm || bstart > bend) return DMD_E_ARG;
+  if (!h->adj) return fail(h, DMD_E_ARG, "dmd_adjoint_rk4 needs a handle created with DMD_FLAG_ADJOINT");
+  if (h->lin || h->d_eq || h->nrhs != 1)
+    return fail(h, DMD_E_ARG, "dmd_adjoint_rk4: linearized form, equilibrium drift and batches are not supported");
+  for (int64_t i = 0; i < nobs; ++i)
+    if (obs_step[i] < 0 || obs_step[i] > nsteps || (i > 0 && obs_step[i] < obs_step[i - 1]))
+      return fail(h, DMD_E_ARG, "obs_step must be ascending in [0, nsteps]");
+  CK(cudaSetDevice(h->dev));
+  const size_t n = h->nstate;
+  const int64_t nseg = (nsteps + checkpoint - 1) / checkpoint, seglen = checkpoint < nsteps ? checkpoint : nsteps;
+  const size_t nk2 = (size_t)h->nk * h->nb2;
+  const size_t np = (size_t)h->npair * 2 * h->nb4;
+  AdjWork w;
+  w.h = h;
+  int rc;
+  if ((rc = w.get(&w.ck, (size_t)nseg * n)) || (rc = w.get(&w.U, (size_t)seglen * 4 * n)) || (rc = w.get(&w.yb, n)) ||
+      (rc = w.get(&w.ub, n)) || (rc = w.get(&w.kb, 4 * n)) || (rc = w.get(&w.tmp, 3 * n)) || (rc = w.get(&w.Xb, nk2)) ||
+      (rc = w.get(&w.Yb, nk2)) || (rc = w.get(&w.rt, nk2)) || (rc = w.get(&w.st, nk2)) || (rc = w.get(&w.rtb, nk2)) ||
+      (rc = w.get(&w.stb, nk2)) || (rc = w.get(&w.G, np)))
+    return rc;
+  CK(cudaMemsetAsync(w.G, 0, (np ? np : 1) * 16, h->st));
+  CK(cudaMemsetAsync(w.yb, 0, n * 16, h->st));
+  CK(cudaMemcpyAsync(w.ck, y0, n * 16, cudaMemcpyHostToDevice, h->st));
+  // forward: checkpoints at multiples of `checkpoint`, observed totals
+  int64_t j = 0;
+  double2* cur = w.ck;
+  double2* spare[2] = {w.tmp + n, w.tmp + 2 * n};
+  int sp = 0;
+  for (; j < nobs && obs_step[j] == 0; ++j) {
+    double v;
+    if ((rc = measure_on(h, slot, bstart, bend, cur, t0, &v))) return rc;
+    if (s_obs) s_obs[j] = v;
+  }
+  for (int64_t s = 0; s < nsteps; ++s) {
+    double2* next = ((s + 1) % checkpoint == 0 && (s + 1) < nsteps) ? w.ck + (size_t)((s + 1) / checkpoint) * n
+                                                                      : spare[sp];
+    if ((rc = adj_rk4_step(h, cur, t0 + (double)s * dt, dt, nullptr, next, w.tmp))) return rc;
+    for (; j < nobs && obs_step[j] == s + 1; ++j) {
+      double v;
+      if ((rc = measure_on(h, slot, bstart, bend, next, t0 + (double)(s + 1) * dt, &v))) return rc;
+      if (s_obs) s_obs[j] = v;
+    }
+    if (next == spare[sp]) sp ^= 1;
+    cur = next;
+  }
+  // backward
+  const unsigned gn = blocks_for((long long)n, 256);
+  j = nobs - 1;
+  for (int64_t sg = nseg - 1; sg >= 0; --sg) {
+    const int64_t n0 = sg * checkpoint, n1 = std::min<int64_t>(n0 + checkpoint, nsteps);
+    const double2* y = w.ck + (size_t)sg * n;
+    for (int64_t s = n0; s < n1; ++s) {  // stage inputs of the stretch
+      double2* out = spare[sp];
+      if ((rc = adj_rk4_step(h, y, t0 + (double)s * dt, dt, w.U + (size_t)(s - n0) * 4 * n, out, w.tmp))) return rc;
+      y = out;
+      sp ^= 1;
+    }
+    for (int64_t s = n1 - 1; s >= n0; --s) {
+      const double t = t0 + (double)s * dt;
+      for (; j >= 0 && obs_step[j] == s + 1; --j) {
+        k_adj_obs<<<gn, 256, 0, h->st>>>(h->nk, h->nbdm, bstart, bend, h->d_obs[slot], h->d_edm, t + dt, h->picture,
+                                         obs_weight[j] * h->obs_prefac[slot], w.yb);
+        h->launches++;
+      }
+      const double cst[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};
+      for (int q = 0; q < 4; ++q) k_scale<<<gn, 256, 0, h->st>>>(n, w.kb + q * n, cst[q], w.yb);
+      h->launches += 4;
+      CKL();
+      const double2* U = w.U + (size_t)(s - n0) * 4 * n;
+      if ((rc = adj_vjp(h, w, U + 3 * n, t + dt, w.kb + 3 * n, w.kb + 2 * n, dt)) ||
+          (rc = adj_vjp(h, w, U + 2 * n, t + 0.5 * dt, w.kb + 2 * n, w.kb + n, 0.5 * dt)) ||
+          (rc = adj_vjp(h, w, U + n, t + 0.5 * dt, w.kb + n, w.kb, 0.5 * dt)) ||
+          (rc = adj_vjp(h, w, U, t, w.kb, nullptr, 0.0)))
+        return rc;
+    }
+  }
+  for (; j >= 0 && obs_step[j] == 0; --j) {
+    k_adj_obs<<<gn, 256, 0, h->st>>>(h->nk, h->nbdm, bstart, bend, h->d_obs[slot], h->d_edm, t0, h->picture,
+                                     obs_weight[j] * h->obs_prefac[slot], w.yb);
+    h->launches++;
+  }
+  CKL();
+  if (dJdy0) CK(cudaMemcpyAsync(dJdy0, w.yb, n * 16, cudaMemcpyDeviceToHost, h->st));
+  std::vector<double> g(dJdP ? 2 * np : 0);
+  if (dJdP && np) CK(cudaMemcpyAsync(g.data(), w.G, np * 16, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (dJdP) {  // device G is [pair][P1 | P2][nb4] with dJ = Re sum(dP o G); out: dJ/dRe P = Re G, dJ/dIm P = -Im G
+    const size_t nb4 = h->nb4, npair = (size_t)h->npair;
+    for (size_t p = 0; p < npair; ++p)
+      for (size_t m = 0; m < 2; ++m)
+        for (size_t e = 0; e < nb4; ++e) {
+          const size_t src = (p * 2 + m) * nb4 + e, dst = (m * npair + p) * nb4 + e;
+          dJdP[2 * dst] = g[2 * src];
+          dJdP[2 * dst + 1] = -g[2 * src + 1];
+        }
+  }
+  unsigned int derr = 0;
+  CK(cudaMemcpy(&derr, h->d_err, sizeof(derr), cudaMemcpyDeviceToHost));
+  if (derr) {
+    cudaMemset(h->d_err, 0, sizeof(derr));
+    return fail(h, DMD_E_TIMEOUT, "a bounded device wait gave up (bulk copy did not complete)");
   }
   return DMD_OK;
 }

@@ -18,6 +18,7 @@ from .build import GPU_LIB
 
 PREC = {"f64": 0, "f64x": 1, "f32": 2, "bf16x2": 3}
 FLAG_LINEAR = 1  # DMD_FLAG_LINEAR: P1, P2 are the linear operators Lscij, Lscji
+FLAG_ADJOINT = 2  # DMD_FLAG_ADJOINT: keep the operators in stored order for adjoint_rk4
 PICTURE = {"interaction": 0, "schrodinger": 1}
 
 
@@ -42,7 +43,7 @@ EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_s
            "dmd_evolve_driver", "dmd_evolve_coh", "dmd_set_state", "dmd_get_state", "dmd_rk4", "dmd_euler",
            "dmd_rkf45_apply", "dmd_set_observable", "dmd_measure", "dmd_launch_count", "dmd_sync",
            "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
-           "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes"]
+           "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes", "dmd_adjoint_rk4"]
 
 
 def _lib():
@@ -73,6 +74,7 @@ def _lib():
         L.dmd_measure.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(d), C.POINTER(d)]
         L.dmd_launch_count.argtypes = [vp, C.POINTER(i64)]
         L.dmd_pair_bytes.argtypes = [vp, C.POINTER(i64)]
+        L.dmd_adjoint_rk4.argtypes = [vp, d, vp, d, i64, i64, C.c_int, C.c_int, C.c_int, i64, vp, vp, vp, vp, vp]
         L.dmd_sync.argtypes = [vp]
         L.dmd_pinned_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
         L.dmd_pinned_free.argtypes = [vp]
@@ -94,7 +96,7 @@ class LindbladGPU:
 
     def __init__(self, *, nk, nb_dm, bstart, bend, e_dm, k1st, k2nd, P1, P2, prefac_eph, Hcoh=None,
                  picture="interaction", expt=1, precision="f64", P1_add=None, P2_add=None, add_scale=0.0, device=0,
-                 f_ref=None, linear=False, nrhs=1):
+                 f_ref=None, linear=False, nrhs=1, adjoint=False):
         L = _lib()
         self._keep = dict(e=_c(e_dm, np.float64), k1=_c(k1st, np.uint64), k2=_c(k2nd, np.uint64),
                           P1=_c(P1, np.complex128), P2=_c(P2, np.complex128), H=_c(Hcoh, np.complex128),
@@ -106,7 +108,8 @@ class LindbladGPU:
                      P1_add=ptr(k["A1"]), P2_add=ptr(k["A2"]), add_scale=add_scale, Hcoh=ptr(k["H"]),
                      picture=PICTURE[picture] if isinstance(picture, str) else int(picture), expt=int(expt),
                      precision=PREC[precision] if isinstance(precision, str) else int(precision), device=device,
-                     flags=FLAG_LINEAR if linear else 0, f_ref=ptr(k["f"]), nrhs=int(nrhs))
+                     flags=(FLAG_LINEAR if linear else 0) | (FLAG_ADJOINT if adjoint else 0), f_ref=ptr(k["f"]),
+                     nrhs=int(nrhs))
         h = C.c_void_p()
         st = L.dmd_create(C.byref(desc), C.byref(h))
         if st != 0:
@@ -114,6 +117,7 @@ class LindbladGPU:
         self._h = h
         self._keep = None  # the library copied everything it needs
         self.nk, self.nb_dm, self.nrhs = nk, nb_dm, max(1, int(nrhs))
+        self.npair, self.nb4 = int(np.asarray(k1st).size), (bend - bstart) ** 4
         self.ny = 2 * nk * nb_dm * nb_dm * self.nrhs
 
     # ------------------------------------------------------------------ plumbing
@@ -216,6 +220,26 @@ class LindbladGPU:
         n = C.c_int64()
         self._ck(_lib().dmd_launch_count(self._h, C.byref(n)))
         return n.value
+
+    def adjoint_rk4(self, t0, y0, dt, nsteps, obs_step, obs_weight, slot=0, bstart=0, bend=None, checkpoint=200,
+                    want_dP=True, want_dy0=False):
+        """Reverse mode of `nsteps` RK4 steps from (t0, y0) for J = sum_i w_i S(t0 + obs_step[i] dt) (S: the
+        total of observable `slot`). Returns (S at the observed steps, dJ/dP as complex [2][nkpair][nb^4]
+        with dJ = Re sum(conj(dJ/dP) dP) or None, dJ/dy0 as y0's layout or None)."""
+        bend = self.nb_dm if bend is None else bend
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        st = np.ascontiguousarray(obs_step, dtype=np.int64)
+        w = np.ascontiguousarray(obs_weight, dtype=np.float64)
+        s = np.zeros(st.size)
+        dP = np.zeros(2 * self.npair * self.nb4 * 2) if want_dP else None
+        dy = np.zeros(self.ny) if want_dy0 else None
+        ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+        self._ck(_lib().dmd_adjoint_rk4(self._h, float(t0), y0.ctypes.data, float(dt), int(nsteps), int(checkpoint),
+                                        int(slot), int(bstart), int(bend), int(st.size), ptr(st), ptr(w), s.ctypes.data,
+                                        ptr(dP), ptr(dy)))
+        if dP is not None:
+            dP = dP.view(np.complex128).reshape(2, self.npair, self.nb4)
+        return s, dP, dy
 
     @property
     def pair_bytes(self):

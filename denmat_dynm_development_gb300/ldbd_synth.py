@@ -183,6 +183,21 @@ def _sum_outer(A, transpose):
 
 def eph_chunk(cfg: SynthConfig, ek, ekp, omegas, chunk_index):
     """P1, P2 (complex128 [n][nb^4]) of the e-ph term for one chunk of pairs."""
+    A1, A2 = eph_amplitudes(cfg, ek, ekp, omegas, chunk_index)
+    return _sum_outer(A1, False), _sum_outer(A2, True)
+
+
+def eph_chunk_modes(cfg: SynthConfig, ek, ekp, omegas, chunk_index):
+    """The e-ph P1, P2 of one chunk split by phonon mode: [nmodes][n][nb^4] each (their sum over modes
+    is eph_chunk's, up to rounding). A scale on mode m's coupling |g|^2 scales its operators."""
+    A1, A2 = eph_amplitudes(cfg, ek, ekp, omegas, chunk_index)
+    nm = len(omegas)
+    return (np.stack([_sum_outer(A1[:, 2 * m:2 * m + 2], False) for m in range(nm)]),
+            np.stack([_sum_outer(A2[:, 2 * m:2 * m + 2], True) for m in range(nm)]))
+
+
+def eph_amplitudes(cfg: SynthConfig, ek, ekp, omegas, chunk_index):
+    """Emission/absorption amplitudes per mode: A1 = (App, Amm), A2 = (Amp, Apm) per mode, [n][2 nmodes][nb][nb]."""
     rng = np.random.default_rng([cfg.seed, 1, chunk_index])
     n, nb = ek.shape
     T = cfg.temperature_K * units.Kelvin
@@ -206,7 +221,7 @@ def eph_chunk(cfg: SynthConfig, ek, ekp, omegas, chunk_index):
         A1[:, 2 * im + 1] = G2m * math.sqrt(nq)         # Amm
         A2[:, 2 * im] = G2m * math.sqrt(nq + 1.0)       # Amp
         A2[:, 2 * im + 1] = G2p * math.sqrt(nq)         # Apm
-    return _sum_outer(A1, False), _sum_outer(A2, True)
+    return A1, A2
 
 
 def eimp_chunk(cfg: SynthConfig, ek, ekp, chunk_index):
@@ -371,6 +386,29 @@ def generate_arrays(cfg: SynthConfig, fold_fraction: Optional[float] = None, pro
             m.close()
             m.unlink()
     return (st, outs[0], outs[1], outs[2] if want_q else None, outs[3] if want_q else None)
+
+
+def mode_operators(cfg: SynthConfig):
+    """Per-mode e-ph operators and the unscaled e-imp operators of a (small) synthetic system:
+    (setup, P1m [nmodes][npair][nb^4], P2m, Q1 or None, Q2 or None), chunk by chunk in one process."""
+    st = setup(cfg)
+    nb4, nm = cfg.nb ** 4, cfg.nmodes
+    P1m = np.empty((nm, st.npair, nb4), np.complex128)
+    P2m = np.empty((nm, st.npair, nb4), np.complex128)
+    want_q = cfg.eimp_sigma_mev is not None
+    Q1 = np.empty((st.npair, nb4), np.complex128) if want_q else None
+    Q2 = np.empty((st.npair, nb4), np.complex128) if want_q else None
+    C = st.chunk_size()
+    for ic, p0 in enumerate(range(0, st.npair, C)):
+        p1 = min(st.npair, p0 + C)
+        ek = st.ew[st.k1[p0:p1].astype(np.int64)]
+        ekp = st.ew[st.k2[p0:p1].astype(np.int64)]
+        a1, a2 = eph_chunk_modes(cfg, ek, ekp, st.omegas, ic)
+        P1m[:, p0:p1] = a1
+        P2m[:, p0:p1] = a2
+        if want_q:
+            Q1[p0:p1], Q2[p0:p1] = eimp_chunk(cfg, ek, ekp, ic)
+    return st, P1m, P2m, Q1, Q2
 
 
 def make_ldbd(outdir: str, cfg: SynthConfig, write_param: bool = True, threads: int = 1, **param_kw) -> SynthInfo:

@@ -57,6 +57,8 @@ extern "C" {
 #define DMD_FLAG_LINEAR 1u /* alg_linearize: P1, P2 hold Lscij, Lscji (ElectronPhonon_linear.cpp) and the
                               RHS is sum herm(L(t) (rho_k' - diag f_ref)) (evolve_eph_linear.cpp:3-51);
                               f_ref (the f_eq of the linearization) is required */
+#define DMD_FLAG_ADJOINT 2u /* keep the pair operators in their stored order as well, for dmd_adjoint_rk4
+                               (one extra copy of P on the device; single state only) */
 
 /* pictures (alg.picture) */
 #define DMD_PICTURE_INTERACTION 0
@@ -129,6 +131,21 @@ int dmd_launch_count(const dmd_handle* h, int64_t* launches);
 /* No counterpart in the reference: device bytes of the stored k-pair operators in the handle's
  * layout (what one contraction pass streams from HBM) */
 int dmd_pair_bytes(const dmd_handle* h, int64_t* bytes);
+
+/* No counterpart in the reference (DMD computes no gradients). Reverse mode of nsteps fixed-step RK4
+ * steps of size dt from (t0, y0) (y0: 2 nk nb_dm^2 doubles, as dmd_func's y), for the objective
+ * J = sum_i obs_weight[i] * S(t0 + obs_step[i] dt), S = the total of observable `slot` over bands
+ * [bstart, bend) as dmd_measure returns it. The forward pass keeps the state every `checkpoint`
+ * steps; the backward pass recomputes each stretch of steps from its checkpoint and integrates the
+ * adjoint through the exact discrete RK4 map with the transposed k-pair contraction. Outputs (any
+ * may be null): s_obs [nobs] the observed totals, dJdP [2][nkpair][nb^4] complex (dJ/dRe P, dJ/dIm P
+ * interleaved, P1 then P2, of the folded operators P = P + add_scale P_add), dJdy0 [2 nk nb_dm^2]
+ * (the gradient with respect to y0's real and imaginary parts). Requires DMD_FLAG_ADJOINT, a single
+ * state, no linearized form and no equilibrium drift; obs_step ascending in [0, nsteps]. The
+ * handle's own state and time are left unchanged. */
+int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64_t nsteps, int64_t checkpoint,
+                    int slot, int bstart, int bend, int64_t nobs, const int64_t* obs_step,
+                    const double* obs_weight, double* s_obs, double* dJdP, double* dJdy0);
 /* wait for the handle's stream */
 int dmd_sync(dmd_handle* h);
 

@@ -1,0 +1,179 @@
+"""Reverse-mode gradients (dmd_adjoint_rk4) against central finite differences.
+
+The objective is J = sum_i w_i S_z(t_i) over fixed RK4 steps. The adjoint's dJ/dP (the gradient with
+respect to the stored pair operators) and dJ/dy0 are checked along random directions against
+central differences (h = 1e-4) of the GPU forward; the per-mode gradient dJ/dtheta of a synthetic
+system with P = sum_m theta_m P^(m) (6 phonon modes + the impurity term) against central
+differences of the GPU forward and of the FP64 oracle; and the torch.autograd wrapper through a
+fitted lifetime. Tolerance: 1e-5 relative (the target for the adjoint), cases without the
+equilibrium-drift subtraction.
+"""
+import dataclasses
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+FD_H = 1e-4
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def built():
+    import __graft_entry__ as G
+    G.build()
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+def _gpu(s, P1=None, P2=None, adjoint=False, precision="f64"):
+    from denmat_dynm_development_gb300.dmd import LindbladGPU
+    g = LindbladGPU(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
+                    P1=s.P1 if P1 is None else P1, P2=s.P2 if P2 is None else P2, prefac_eph=s.prefac_eph,
+                    Hcoh=s.Hcoh, picture=s.picture_schrodinger, expt=s.expt, precision=precision, adjoint=adjoint)
+    g.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+    return g
+
+
+def _objective(s, y0, dt, steps, w, P1=None, P2=None):
+    with _gpu(s, P1, P2) as g:
+        g.set_state(s.t0, y0)
+        out, cur = [], 0
+        for st in steps:
+            if st > cur:
+                g.rk4(dt, int(st - cur))
+                cur = int(st)
+            out.append(g.measure(0, s.nv_dm)[0])
+    return float(np.dot(w, out)), np.array(out)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_schrod", "nb4_eimp_B"])
+def test_adjoint_directional_derivatives_vs_fd(case, oracle, built):
+    s = oracle.load(os.path.join(GOLDEN, case))
+    rng = np.random.default_rng(3)
+    dt = 2.0 * oracle.fs
+    steps = np.array([0, 9, 20, 33])
+    w = rng.standard_normal(steps.size)
+    y0 = oracle.y_of(s.dm0)
+    with _gpu(s, adjoint=True) as g:
+        sv, dP, dy0 = g.adjoint_rk4(s.t0, y0, dt, int(steps[-1]), steps, w, slot=0, bstart=s.nv_dm, checkpoint=7,
+                                    want_dy0=True)
+    J0, s_fwd = _objective(s, y0, dt, steps, w)
+    assert rel(sv, s_fwd) < 1e-12
+    # dJ/dP along a random complex direction of both operators
+    n = s.P1.size
+    d1 = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * np.abs(s.P1).max()
+    d2 = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * np.abs(s.P2).max()
+    jp, _ = _objective(s, y0, dt, steps, w, s.P1 + FD_H * d1, s.P2 + FD_H * d2)
+    jm, _ = _objective(s, y0, dt, steps, w, s.P1 - FD_H * d1, s.P2 - FD_H * d2)
+    fd = (jp - jm) / (2 * FD_H)
+    ad = np.vdot(dP[0].reshape(-1), d1).real + np.vdot(dP[1].reshape(-1), d2).real
+    print("%s dJ/dP: adjoint %.12g fd %.12g rel %.3g" % (case, ad, fd, abs(ad - fd) / abs(fd)))
+    assert abs(ad - fd) <= TOL * abs(fd)
+    # dJ/dy0 along a random Hermitian direction (the state stays Hermitian)
+    dm = rng.standard_normal(s.dm0.shape) + 1j * rng.standard_normal(s.dm0.shape)
+    dm = dm.reshape(s.nk, s.nb_dm, s.nb_dm)
+    dm = 0.5 * (dm + np.conj(np.swapaxes(dm, 1, 2)))
+    dy = oracle.y_of(dm.reshape(s.nk, -1)) * 1e-3
+    jp, _ = _objective(s, y0 + FD_H * dy, dt, steps, w)
+    jm, _ = _objective(s, y0 - FD_H * dy, dt, steps, w)
+    fd = (jp - jm) / (2 * FD_H)
+    ad = float(np.dot(dy0, dy))
+    print("%s dJ/dy0: adjoint %.12g fd %.12g rel %.3g" % (case, ad, fd, abs(ad - fd) / abs(fd)))
+    assert abs(ad - fd) <= TOL * abs(fd)
+
+
+def _mode_model(oracle, tmp_path, nb=2, nk=60, nsteps=60):
+    """a synthetic system whose operators are sum_m theta_m P^(m): 6 phonon modes + impurities"""
+    from denmat_dynm_development_gb300.adjoint import ModeScaledRK4
+    from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, make_ldbd, mode_operators
+    cfg = SynthConfig(nk=nk, nb=nb, seed=11, eimp_sigma_mev=5.0)
+    make_ldbd(str(tmp_path), cfg, B_T=(0.3, 0.0, 0.0))
+    s = oracle.load(str(tmp_path))
+    _, P1m, P2m, Q1, Q2 = mode_operators(cfg)
+    P1m = np.concatenate([P1m, Q1[None]])
+    P2m = np.concatenate([P2m, Q2[None]])
+    # impurity scale 0.2: at the loader's 1e-2 the impurities move S_z by ~1e-6 of itself over this
+    # horizon, below what a central difference with h = 1e-4 resolves in FP64
+    theta = np.array([1.0, 0.8, 1.3, 1.0, 0.6, 1.1, 0.2])
+    steps = np.arange(0, nsteps + 1, 10)
+    model = ModeScaledRK4(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st,
+                          k2nd=s.k2nd, P1_modes=P1m, P2_modes=P2m, prefac_eph=s.prefac_eph, y0=oracle.y_of(s.dm0),
+                          dt=2.0 * oracle.fs, nsteps=nsteps, obs_steps=steps, obs=s.smat[:, 2, :], f_obs=s.f_dm,
+                          ob_prefac=s.ob_prefac, obs_bstart=s.nv_dm, t0=s.t0, Hcoh=s.Hcoh,
+                          picture=s.picture_schrodinger, expt=s.expt, precision="f64", checkpoint=16)
+    return s, model, theta, steps
+
+
+@pytest.mark.gpu
+def test_mode_scale_gradient_vs_fd_gpu_and_oracle(oracle, built, tmp_path):
+    s, model, theta, steps = _mode_model(oracle, tmp_path)
+    w = np.zeros(steps.size)
+    w[-1] = 1.0  # J = S_z(t_f)
+    sv, grad = model.gradient(theta, w)
+    fd = np.zeros(theta.size)
+    for m in range(theta.size):
+        e = np.zeros(theta.size)
+        e[m] = FD_H * theta[m]
+        fd[m] = (model.forward(theta + e)[-1] - model.forward(theta - e)[-1]) / (2 * FD_H * theta[m])
+    print("dS_z(t_f)/dtheta adjoint", grad, "\n fd", fd)
+    assert rel(grad, fd) < TOL
+    # the FP64 oracle's forward (the reference's algorithm) for two of the scales
+    y0 = oracle.y_of(s.dm0)
+    for m in (1, theta.size - 1):
+        vals = []
+        for sg in (1, -1):
+            th = theta.copy()
+            th[m] += sg * FD_H * theta[m]
+            P1, P2 = model.operators(th)
+            so = dataclasses.replace(s, P1=np.ascontiguousarray(P1.reshape(-1)), P2=np.ascontiguousarray(P2.reshape(-1)))
+            y, _ = oracle.rk4(so, s.t0, model.dt, model.nsteps, y0)
+            vals.append(oracle.measure(so, y, s.t0 + model.nsteps * model.dt)[0])
+        fo = (vals[0] - vals[1]) / (2 * FD_H * theta[m])
+        print("mode %d: adjoint %.12g oracle fd %.12g" % (m, grad[m], fo))
+        assert abs(grad[m] - fo) <= TOL * abs(fo)
+
+
+@pytest.mark.gpu
+def test_autograd_through_fitted_lifetime(oracle, built, tmp_path):
+    torch = pytest.importorskip("torch")
+    from denmat_dynm_development_gb300.adjoint import sz_trajectory, t1_loglinear
+    s, model, theta, steps = _mode_model(oracle, tmp_path, nsteps=80)
+    t = steps * model.dt
+    th = torch.tensor(theta, dtype=torch.float64, requires_grad=True)
+    tau = t1_loglinear(t, sz_trajectory(th, model))
+    tau.backward()
+    g = th.grad.numpy()
+    for m in (0, 3, theta.size - 1):
+        e = np.zeros(theta.size)
+        e[m] = FD_H * theta[m]
+        tp = float(t1_loglinear(t, torch.as_tensor(model.forward(theta + e))))
+        tm = float(t1_loglinear(t, torch.as_tensor(model.forward(theta - e))))
+        fd = (tp - tm) / (2 * FD_H * theta[m])
+        print("dT1/dtheta_%d: autograd %.12g fd %.12g" % (m, g[m], fd))
+        assert abs(g[m] - fd) <= TOL * abs(fd)
+
+
+def test_mode_operators_sum_to_the_combined_operators():
+    from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, generate_arrays, mode_operators
+    cfg = SynthConfig(nk=40, nb=2, seed=5, eimp_sigma_mev=5.0)
+    _, P1, P2, Q1, Q2 = generate_arrays(cfg, fold_fraction=None, procs=1)
+    _, P1m, P2m, R1, R2 = mode_operators(cfg)
+    assert P1m.shape == (cfg.nmodes,) + P1.shape
+    assert rel(P1m.sum(0), P1) < 1e-14 and rel(P2m.sum(0), P2) < 1e-14
+    np.testing.assert_array_equal(R1, Q1)
+    np.testing.assert_array_equal(R2, Q2)
+
+
+def test_t1_loglinear_recovers_an_exponential():
+    torch = pytest.importorskip("torch")
+    from denmat_dynm_development_gb300.adjoint import t1_loglinear
+    t = np.linspace(0, 10, 21)
+    s = torch.tensor(3e-4 * np.exp(-t / 4.5), dtype=torch.float64)
+    assert abs(float(t1_loglinear(t, s)) - 4.5) < 1e-12
