@@ -482,6 +482,58 @@ def t1_compare(precision, nsteps, dev, workload):
             "s_ratio_end": float(a[-1, 1] / a[0, 1]), "seconds": time.perf_counter() - t0}
 
 
+def run_adjoint(args):
+    """Adjoint configuration: dS_z(t_f)/d(6 per-mode coupling scales, impurity scale) on the Si-like
+    nk = 500 system (e-ph + e-imp operators kept per mode), RK4 dt = 1 fs, checkpoints every 200
+    steps; timed against the forward alone and checked against central differences (h = 1e-4)."""
+    import dataclasses
+    from denmat_dynm_development_gb300 import host as H
+    from denmat_dynm_development_gb300.adjoint import ModeScaledRK4
+    name = args.workload if args.workload in ("si_nk500", "mos2_nk2k") else "si_nk500"
+    cfg = dataclasses.replace(S.WORKLOADS[name], eimp_sigma_mev=5.0)
+    st, P1m, P2m, Q1, Q2 = S.mode_operators(cfg)
+    P1m = np.concatenate([P1m, Q1[None]])
+    P2m = np.concatenate([P2m, Q2[None]])
+    e = np.ascontiguousarray(st.e)
+    f = H.fermi(st.T, st.mu, e)
+    dm0 = H.dm_bpert(st.s, e, f, st.T, np.array([0.0, 0.0, 0.1 * U.Tesla2au]), 0.0, 0)
+    nk_full = float(st.n) ** 3
+    ob_prefac = (1.0 / nk_full) / (st.V * U.bohr2cm ** 3)
+    nb = cfg.nb
+    dt = 1.0 * U.fs
+    nsteps = int(round(args.adj_tf_ps * 1000.0))
+    theta = np.array([1.0] * cfg.nmodes + [0.2])
+    model = ModeScaledRK4(nk=cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=e, k1st=st.k1, k2nd=st.k2, P1_modes=P1m,
+                          P2_modes=P2m, prefac_eph=2 * math.pi / nk_full,
+                          y0=np.ascontiguousarray(dm0).view(np.float64).reshape(-1), dt=dt, nsteps=nsteps,
+                          obs_steps=[nsteps], obs=np.ascontiguousarray(st.s[:, 2, :]), f_obs=f, ob_prefac=ob_prefac,
+                          obs_bstart=0, picture=0, expt=1, precision="f64x", checkpoint=200)
+    model.forward(theta)  # warm-up (library load, first launches)
+    t0 = time.perf_counter()
+    s_f = model.forward(theta)[-1]
+    fwd_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    s_a, grad = model.gradient(theta, [1.0])
+    adj_s = time.perf_counter() - t0
+    fd = []
+    for m in range(theta.size):
+        ep = np.zeros(theta.size)
+        ep[m] = 1e-4 * theta[m]
+        fd.append((model.forward(theta + ep)[-1] - model.forward(theta - ep)[-1]) / (2e-4 * theta[m]))
+    fd = np.array(fd)
+    err = np.abs(grad - fd) / np.abs(fd)
+    line = {"metric": "adjoint: dS_z(t_f)/d(6 mode scales, n_imp scale), t_f = %g ps" % args.adj_tf_ps,
+            "value": adj_s, "unit": "s (forward with checkpoints + backward, 7 gradients)", "n_gpus": 1,
+            "higher_is_better": False, "vs_baseline": None, "dtype": "f64 (fp32-pair emulated forward sums)",
+            "data": "synthetic", "forward_s": fwd_s, "adjoint_over_forward": adj_s / fwd_s,
+            "rk4_steps": nsteps, "s_z_tf": s_f, "s_z_tf_adjoint_pass": s_a[-1], "grad": grad.tolist(),
+            "fd_central_h1e-4": fd.tolist(), "rel_err_vs_fd": err.tolist(), "max_rel_err_vs_fd": float(err.max()),
+            "config": {"workload": "%s + e-imp (sigma 5 meV): nb=%d, nk=%d, %d k-pairs, %d modes kept apart + "
+                                   "impurity operator, theta = (1,..,1, 0.2), Bz_pert 0.1 T, RK4 dt=1 fs, "
+                                   "checkpoint every 200 steps" % (name, nb, cfg.nk, st.npair, cfg.nmodes)}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -495,6 +547,8 @@ def main():
     ap.add_argument("--no-t1", dest="t1", action="store_false")
     ap.add_argument("--t1-steps", type=int, default=10000)
     ap.add_argument("--nrhs", type=int, default=1, help="batched form: states sharing P (f32 / bf16x2)")
+    ap.add_argument("--adjoint", action="store_true", help="adjoint configuration (gradients of S_z(t_f))")
+    ap.add_argument("--adj-tf-ps", type=float, default=50.0, help="adjoint: t_f in ps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
@@ -503,6 +557,10 @@ def main():
             return
         w = build_workload(args.workload, min(16, os.cpu_count() or 1))
         run_reference(args, w)
+        return
+    if args.adjoint:
+        if rank == 0:
+            run_adjoint(args)
         return
     # the generator's worker processes start before any CUDA call
     w = build_workload(args.workload, max(1, min(16, (os.cpu_count() or 1) // max(world, 1))))

@@ -578,7 +578,16 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
     for (int b = 0; b < nb; ++b) ew[(size_t)k * nb + b] = d->e_dm[(size_t)k * h->nbdm + h->bs + b];
   dmd::PairLayout L;
   const int G = h->nb2 / 4, W = 32 / G;  // lanes per pair, columns per column block
-  if (!dmd::build_pair_layout(h->nk, nb, ew.data(), h->npair, d->k1st, d->k2nd, 512 / G, W, L))
+  // pairs per work item: 512 (a warp's share on large workloads), fewer when the workload would
+  // not give every SM its 16 resident warps
+  int ppi = 512 / G;
+  {
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev) != cudaSuccess || nsm <= 0) nsm = 1;
+    const long long want = (long long)nsm * 16;
+    if (h->npair / ppi < want) ppi = (int)std::max<long long>(1, h->npair / want);
+  }
+  if (!dmd::build_pair_layout(h->nk, nb, ew.data(), h->npair, d->k1st, d->k2nd, ppi, W, L))
     return fail(h, DMD_E_ARG, "k-pair index out of range");
   h->nitems = (int)L.items.size();
   h->nrb = (long long)L.rb.size();
