@@ -55,8 +55,8 @@ def env_int(k, d):
 # ------------------------------------------------------------------------------------------------
 # workload
 # ------------------------------------------------------------------------------------------------
-def build_workload(name, procs):
-    cfg = S.WORKLOADS[name]
+def build_workload(name, procs, cfg=None):
+    cfg = S.WORKLOADS[name] if cfg is None else cfg
     frac = 1e-4 if cfg.eimp_sigma_mev is not None else None
     t0 = time.time()
     st, P1, P2, _, _ = S.generate_arrays(cfg, fold_fraction=frac, procs=procs)
@@ -274,6 +274,7 @@ def run_gpu_batched(args, w):
                     P2=w["P2"], prefac_eph=w["prefac"], picture=0, expt=1, precision=prec, f_ref=w["f"], nrhs=R)
     h = 1.0 * U.fs
     g.set_state(0.0, batch_states(w, R))
+    shape = g.autotune(3)
     g.rk4(h, args.warmup)
     clk = ClockSampler(0)
     clk.start()
@@ -313,7 +314,7 @@ def run_gpu_batched(args, w):
             "unit": "state-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": prec + " (rho as deviation from f)", "data": "synthetic",
-            "config": config_of(w, {"precision": prec, "nrhs": R, "tensor_cores": tc,
+            "config": config_of(w, {"precision": prec, "nrhs": R, "tensor_cores": tc, "autotuned_shape": shape,
                                     "states": "spin polarisation along x/y/z in turn + random 1e-4 deviation"}),
             "roofline": {"bound": bound, "achieved": bpl / (pair_avg * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": bpl / (pair_avg * 1e-3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
@@ -336,6 +337,7 @@ def run_gpu(args, w, rank, world, dist):
     h = 1.0 * U.fs
     y0 = np.ascontiguousarray(w["dm0"]).view(np.float64).reshape(-1).copy()
     g.set_state(0.0, y0)
+    shape = g.autotune(3)                      # compiled contraction shapes timed, fastest kept
     g.rk4(h, args.warmup)                      # warm-up (also captures the step graph)
 
     def barrier():
@@ -417,7 +419,7 @@ def run_gpu(args, w, rank, world, dist):
                                            "f32": "f32 (P complex64, rho as deviation from f)",
                                            "bf16x2": "bf16 hi+lo (P 8 B/complex, rho as deviation from f)"
                                            }[args.precision],
-            "data": "synthetic", "config": config_of(w, {"precision": args.precision}),
+            "data": "synthetic", "config": config_of(w, {"precision": args.precision, "autotuned_shape": shape}),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k-pair contraction", "bytes_per_launch": bpl, "avg_launch_ms": pair_avg_ms,
@@ -534,6 +536,62 @@ def run_adjoint(args):
     print(json.dumps(line))
 
 
+def run_temperatures(args):
+    """Batched form over separate P sets: 8 temperatures 50-400 K on GaAs-like systems of uneven nk
+    (5k-20k), each a tensor-core batch of states (bf16 hi+lo), advanced together by dmd_group_rk4
+    (one CUDA graph launch per RK4 step, one parallel branch per temperature)."""
+    import dataclasses
+    from denmat_dynm_development_gb300.dmd import Group, LindbladGPU
+    temps = np.linspace(50.0, 400.0, 8)
+    nks = np.linspace(5000, 20000, 8).astype(int)
+    R = args.nrhs if args.nrhs > 1 else 12
+    h = 1.0 * U.fs
+    hs, pairs, desc = [], 0, []
+    t0 = time.time()
+    for i, (T, nk) in enumerate(zip(temps, nks)):
+        cfg = dataclasses.replace(S.WORKLOADS["gaas_nk20k"], nk=int(nk), temperature_K=float(T), seed=100 + i)
+        w = build_workload("gaas_nk20k", max(1, min(16, os.cpu_count() or 1)), cfg)
+        st = w["st"]
+        g = LindbladGPU(nk=st.cfg.nk, nb_dm=st.cfg.nb, bstart=0, bend=st.cfg.nb, e_dm=w["e"], k1st=st.k1, k2nd=st.k2,
+                        P1=w["P1"], P2=w["P2"], prefac_eph=w["prefac"], picture=0, expt=1, precision="bf16x2",
+                        f_ref=w["f"], nrhs=R)
+        g.set_state(0.0, batch_states(w, R, seed=7 + i))
+        hs.append(g)
+        pairs += st.npair
+        desc.append("%gK/nk%d/%dpairs" % (T, nk, st.npair))
+        del w
+    setup_s = time.time() - t0
+    # each system alone, one after another
+    for g in hs:
+        g.rk4(h, args.warmup)
+    t0 = time.perf_counter()
+    for g in hs:
+        g.rk4(h, args.steps)
+    alone_s = time.perf_counter() - t0
+    with Group(hs) as grp:
+        grp.rk4(h, args.warmup)
+        clk = ClockSampler(0)
+        clk.start()
+        t0 = time.perf_counter()
+        grp.rk4(h, args.steps)
+        grp_s = time.perf_counter() - t0
+        clocks = clk.stop()
+    launches = sum(g.launches for g in hs)
+    for g in hs:
+        g.close()
+    nstates = R * len(hs)
+    line = {"metric": "ensemble RK4 steps/s over 8 temperatures (separate P sets, %d states each), one graph per step"
+                      % R, "value": nstates * args.steps / grp_s, "unit": "state-steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": grp_s * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2 (rho as deviation from f)",
+            "data": "synthetic", "sequential_state_steps_per_s": nstates * args.steps / alone_s,
+            "group_speedup_over_sequential": alone_s / grp_s,
+            "config": {"workload": "8 GaAs-like P sets: " + ", ".join(desc), "total_pairs": pairs, "states": nstates,
+                       "setup_s": setup_s, "timing": "host wall clock around the synchronised group launches"},
+            "clocks": clocks, "gpu_launches_total": launches}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -548,6 +606,7 @@ def main():
     ap.add_argument("--t1-steps", type=int, default=10000)
     ap.add_argument("--nrhs", type=int, default=1, help="batched form: states sharing P (f32 / bf16x2)")
     ap.add_argument("--adjoint", action="store_true", help="adjoint configuration (gradients of S_z(t_f))")
+    ap.add_argument("--temperatures", action="store_true", help="batched form over 8 temperature P sets")
     ap.add_argument("--adj-tf-ps", type=float, default=50.0, help="adjoint: t_f in ps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -561,6 +620,10 @@ def main():
     if args.adjoint:
         if rank == 0:
             run_adjoint(args)
+        return
+    if args.temperatures:
+        if rank == 0:
+            run_temperatures(args)
         return
     # the generator's worker processes start before any CUDA call
     w = build_workload(args.workload, max(1, min(16, (os.cpu_count() or 1) // max(world, 1))))

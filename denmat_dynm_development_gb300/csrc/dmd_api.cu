@@ -1710,6 +1710,160 @@ int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64
   return DMD_OK;
 }
 
+}  // extern "C"
+
+struct dmd_group {
+  std::vector<dmd_handle*> m;
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<cudaEvent_t> ev;  // [0] fork, [1..n] joins
+};
+
+extern "C" {
+
+int dmd_group_create(dmd_handle* const* members, int n, dmd_group** out) {
+  if (!members || n < 1 || !out) return DMD_E_ARG;
+  *out = nullptr;
+  for (int i = 0; i < n; ++i)
+    if (!members[i] || members[i]->dev != members[0]->dev) return DMD_E_ARG;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < i; ++j)
+      if (members[i] == members[j]) return DMD_E_ARG;
+  if (cudaSetDevice(members[0]->dev) != cudaSuccess) return DMD_E_CUDA;
+  dmd_group* g = new dmd_group();
+  g->m.assign(members, members + n);
+  g->dev = members[0]->dev;
+  bool ok = cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) == cudaSuccess;
+  g->ev.assign(n + 1, nullptr);
+  for (auto& e : g->ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    dmd_group_destroy(g);
+    return DMD_E_CUDA;
+  }
+  *out = g;
+  return DMD_OK;
+}
+
+int dmd_group_destroy(dmd_group* g) {
+  if (!g) return DMD_E_ARG;
+  cudaSetDevice(g->dev);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  for (auto e : g->ev)
+    if (e) cudaEventDestroy(e);
+  if (g->st) cudaStreamDestroy(g->st);
+  delete g;
+  return DMD_OK;
+}
+
+int dmd_group_rk4(dmd_group* g, double dt, int64_t nsteps) {
+  if (!g || nsteps < 0 || !(dt == dt)) return DMD_E_ARG;
+  if (nsteps == 0) return DMD_OK;
+  dmd_handle* h0 = g->m[0];
+  dmd_handle* h = h0;  // error messages go to the first member
+  CK(cudaSetDevice(g->dev));
+  for (dmd_handle* hm : g->m) {  // every member's stage times start from its own time
+    const double tref[2] = {hm->t, dt};
+    const long long zero = 0;
+    if (cudaMemcpyAsync(hm->d_tref, tref, 16, cudaMemcpyHostToDevice, hm->st) != cudaSuccess ||
+        cudaMemcpyAsync(hm->d_step, &zero, 8, cudaMemcpyHostToDevice, hm->st) != cudaSuccess ||
+        cudaStreamSynchronize(hm->st) != cudaSuccess)
+      return fail(hm, DMD_E_CUDA, "group: time reference upload");
+  }
+  if (!g->exec) {  // one step of every member as parallel branches of one graph
+    std::vector<long long> l0;
+    for (dmd_handle* hm : g->m) l0.push_back(hm->launches);
+    CK(cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal));
+    int rc = DMD_OK;
+    cudaError_t e = cudaEventRecord(g->ev[0], g->st);
+    for (size_t i = 0; i < g->m.size() && rc == DMD_OK && e == cudaSuccess; ++i) {
+      dmd_handle* hm = g->m[i];
+      e = cudaStreamWaitEvent(hm->st, g->ev[0], 0);
+      if (e == cudaSuccess) rc = rk4_step_launches(hm);
+      if (rc == DMD_OK && e == cudaSuccess) e = cudaEventRecord(g->ev[i + 1], hm->st);
+      if (rc == DMD_OK && e == cudaSuccess) e = cudaStreamWaitEvent(g->st, g->ev[i + 1], 0);
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(g->st, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return fail(h, DMD_E_CUDA, std::string("group graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    e = cudaGraphInstantiate(&g->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("group graph instantiate: ") + cudaGetErrorString(e));
+    for (size_t i = 0; i < g->m.size(); ++i) g->m[i]->launches = l0[i];  // counted when the graph runs
+  }
+  for (int64_t s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(g->exec, g->st));
+  CK(cudaStreamSynchronize(g->st));
+  int rc = DMD_OK;
+  for (dmd_handle* hm : g->m) {
+    const long long per_step = hm->npair ? (hm->use_tc ? 21 : hm->use_cb ? 17 : 13) : 9;
+    hm->launches += per_step * nsteps;
+    hm->t = hm->t + (double)nsteps * dt;
+    const int r = check_state(hm);
+    if (r && !rc) rc = r;
+  }
+  return rc;
+}
+
+int dmd_autotune(dmd_handle* h, int evals, int* chosen) {
+  if (!h || evals < 1) return DMD_E_ARG;
+  CK(cudaSetDevice(h->dev));
+  // candidate shapes of this handle's contraction
+  std::vector<int> cand;
+  int* knob = nullptr;
+  if (h->use_cb && !h->use_tc && h->nrhs == 1 && h->prec == DMD_PREC_F64X && h->nb == 2) {
+    cand = {0, 1, 2, 3, 4};
+    knob = &h->pcfg;
+  } else if (h->use_cb && !h->use_tc && h->nrhs > 1 && h->prec == DMD_PREC_F32) {
+    cand = {4, 8};
+    knob = &h->brw;
+  }
+  if (!knob) {
+    if (chosen) *chosen = 0;
+    return DMD_OK;
+  }
+  cudaEvent_t a = nullptr, b = nullptr;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  const int keep = *knob;
+  int best = keep, rc = DMD_OK;
+  float best_ms = 1e30f;
+  for (int c : cand) {
+    *knob = c;
+    if ((rc = rhs_plain(h, h->t, h->d_y, h->d_out))) break;  // warm-up
+    cudaEventRecord(a, h->st);
+    for (int i = 0; i < evals && rc == DMD_OK; ++i) rc = rhs_plain(h, h->t, h->d_y, h->d_out);
+    cudaEventRecord(b, h->st);
+    if (rc) break;
+    if (cudaEventSynchronize(b) != cudaSuccess) {
+      rc = fail(h, DMD_E_CUDA, "autotune timing");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *knob = rc ? keep : best;
+  if (h->g_rk4) {  // the captured step holds the old kernels
+    cudaGraphExecDestroy(h->g_rk4);
+    h->g_rk4 = nullptr;
+  }
+  if (rc) return rc;
+  if (chosen) *chosen = best;
+  return check_state(h);
+}
+
 int dmd_pair_bytes(const dmd_handle* h, int64_t* n) {
   if (!h || !n) return DMD_E_ARG;
   *n = h->pair_bytes;

@@ -43,7 +43,8 @@ EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_s
            "dmd_evolve_driver", "dmd_evolve_coh", "dmd_set_state", "dmd_get_state", "dmd_rk4", "dmd_euler",
            "dmd_rkf45_apply", "dmd_set_observable", "dmd_measure", "dmd_launch_count", "dmd_sync",
            "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
-           "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes", "dmd_adjoint_rk4"]
+           "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes", "dmd_adjoint_rk4", "dmd_autotune",
+           "dmd_group_create", "dmd_group_rk4", "dmd_group_destroy"]
 
 
 def _lib():
@@ -74,6 +75,10 @@ def _lib():
         L.dmd_measure.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(d), C.POINTER(d)]
         L.dmd_launch_count.argtypes = [vp, C.POINTER(i64)]
         L.dmd_pair_bytes.argtypes = [vp, C.POINTER(i64)]
+        L.dmd_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
+        L.dmd_group_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(vp)]
+        L.dmd_group_rk4.argtypes = [vp, d, i64]
+        L.dmd_group_destroy.argtypes = [vp]
         L.dmd_adjoint_rk4.argtypes = [vp, d, vp, d, i64, i64, C.c_int, C.c_int, C.c_int, i64, vp, vp, vp, vp, vp]
         L.dmd_sync.argtypes = [vp]
         L.dmd_pinned_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
@@ -241,6 +246,12 @@ class LindbladGPU:
             dP = dP.view(np.complex128).reshape(2, self.npair, self.nb4)
         return s, dP, dy
 
+    def autotune(self, evals=3):
+        """time the compiled contraction shapes on the current state, keep the fastest; returns its index"""
+        c = C.c_int()
+        self._ck(_lib().dmd_autotune(self._h, int(evals), C.byref(c)))
+        return c.value
+
     @property
     def pair_bytes(self):
         """device bytes of the stored k-pair operators"""
@@ -266,6 +277,43 @@ class LindbladGPU:
         ms, n = C.c_double(), C.c_int64()
         self._ck(_lib().dmd_profile_get(self._h, cls, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+
+class Group:
+    """Several LindbladGPU handles of one device stepped together: one CUDA graph launch per RK4 step
+    runs every member's step as a parallel branch (separate P sets, e.g. temperatures)."""
+
+    def __init__(self, members):
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m._h for m in self.members])
+        g = C.c_void_p()
+        st = _lib().dmd_group_create(arr, len(self.members), C.byref(g))
+        if st != 0:
+            raise DMDError(st, "dmd_group_create failed")
+        self._g = g
+
+    def rk4(self, dt, nsteps):
+        st = _lib().dmd_group_rk4(self._g, float(dt), int(nsteps))
+        if st != 0:
+            msg = "; ".join(_lib().dmd_last_error(m._h).decode() for m in self.members)
+            raise DMDError(st, msg)
+
+    def close(self):
+        if self._g is not None:
+            _lib().dmd_group_destroy(self._g)
+            self._g = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PinnedArray:

@@ -161,6 +161,23 @@ int dmd_timer(dmd_handle* h, int op, double* ms);
  * around each launch; dmd_profile_get returns the accumulated device time and launch count of
  * kernel class 0 (prep), 1 (k-pair contraction), 2 (finish/stepper update), 3 (other) */
 int dmd_set_profiling(dmd_handle* h, int on);
+
+/* No counterpart in the reference. A group steps several handles of one device together (separate
+ * P sets: temperatures, materials, uneven nk), each possibly batched: dmd_group_rk4 advances every
+ * member by nsteps RK4 steps of size dt from its own time, one CUDA graph launch per step in which
+ * each member's kernels form a parallel branch. Members keep their own state, observables and
+ * errors; a member must not be stepped on its own while the group steps it. */
+typedef struct dmd_group dmd_group;
+int dmd_group_create(dmd_handle* const* members, int n, dmd_group** out);
+int dmd_group_rk4(dmd_group* g, double dt, int64_t nsteps);
+int dmd_group_destroy(dmd_group* g);
+
+/* No counterpart in the reference. Shape autotuner: times every compiled shape variant of the
+ * handle's contraction (f64x, nb = 2: lines per stage, ring depth, CTAs per SM; CUDA-core batches:
+ * states per warp) on `evals` right-hand-side evaluations of the current device state (CUDA events,
+ * after one warm-up evaluation each), keeps the fastest and returns its index in *chosen (0 when
+ * the handle's form has a single shape). The state is not modified. */
+int dmd_autotune(dmd_handle* h, int evals, int* chosen);
 int dmd_profile_get(const dmd_handle* h, int kernel_class, double* total_ms, int64_t* launches);
 
 /* No counterpart in the reference. The scattering right-hand side of dmd_evolve_driver for callers

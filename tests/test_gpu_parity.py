@@ -475,3 +475,63 @@ def test_batched_tensor_core_t1_vs_oracle(oracle, built):
     print("tensor-core batch: S(t) rel err %.3g, T1 %.10g vs %.10g ps, rel err %.3g"
           % (rel(rec[:, 1], rec_o[:, 1]), fg.tau_lsq, fo.tau_lsq, et))
     assert et < 1e-4
+
+
+@pytest.mark.parametrize("prec,nrhs", [("f64x", 1), ("f32", 5)])
+def test_autotune_keeps_the_results(prec, nrhs, oracle, built):
+    """dmd_autotune times the compiled contraction shapes and keeps the fastest: the RHS stays the
+    oracle's (the shapes differ only in summation order), the state is untouched, and stepping
+    afterwards (a new captured graph) works."""
+    s = oracle.load(os.path.join(GOLDEN, "nb2_eimp_B"))
+    ys = _herm_states(s, nrhs, 5)
+    t = 17.0 * oracle.fs
+    mk = (lambda: make_gpu(s, prec)) if nrhs == 1 else (lambda: make_gpu_lowp(s, prec, nrhs=nrhs))
+    tol = RHS_TOL[prec] if nrhs == 1 else LOWP_TOL[prec]
+    with mk() as g:
+        y = np.concatenate(ys)
+        g.set_state(s.t0, y)
+        g.rk4(1.0 * oracle.fs, 2)
+        _, ya = g.get_state()
+        c = g.autotune(2)
+        assert c in ((0, 1, 2, 3, 4) if nrhs == 1 else (4, 8))
+        _, yb = g.get_state()
+        np.testing.assert_array_equal(ya, yb)
+        out = g.func(t, y).reshape(nrhs, -1)
+        for q in range(nrhs):
+            assert rel(out[q], oracle.rhs(s, t, ys[q])) < tol
+        g.rk4(1.0 * oracle.fs, 2)
+
+
+def test_group_steps_members_as_when_alone(oracle, built):
+    """dmd_group_rk4: three handles with different P sets and forms (f64x nb = 2, f64x nb = 4, a
+    tensor-core batch of 3) advanced by one graph per step match the same handles stepped alone."""
+    from denmat_dynm_development_gb300.dmd import Group
+    sa = oracle.load(os.path.join(GOLDEN, "nb2_eimp_B"))
+    sb = oracle.load(os.path.join(GOLDEN, "nb4_eimp_B"))
+    ya, yb = oracle.y_of(sa.dm0), oracle.y_of(sb.dm0)
+    yc = np.concatenate(_herm_states(sa, 3, 9))
+    h = 2.0 * oracle.fs
+
+    def handles():
+        return [make_gpu(sa, "f64x"), make_gpu(sb, "f64x"), make_gpu_lowp(sa, "bf16x2", nrhs=3)]
+
+    alone = []
+    for g, y in zip(handles(), (ya, yb, yc)):
+        with g:
+            g.set_state(sa.t0, y)
+            g.rk4(h, 12)
+            alone.append(g.get_state())
+    hs = handles()
+    try:
+        for g, y in zip(hs, (ya, yb, yc)):
+            g.set_state(sa.t0, y)
+        with Group(hs) as grp:
+            grp.rk4(h, 5)
+            grp.rk4(h, 7)
+        for g, (t1, y1) in zip(hs, alone):
+            t2, y2 = g.get_state()
+            assert abs(t2 - t1) <= 1e-12 * abs(t1)
+            assert rel(y2, y1) < 1e-12
+    finally:
+        for g in hs:
+            g.close()
