@@ -331,9 +331,11 @@ def run_gpu(args, w, rank, world, dist):
     st = w["st"]
     nb = st.cfg.nb
     dev = env_int("LOCAL_RANK", 0)
+    t_create = time.perf_counter()
     g = LindbladGPU(nk=st.cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=w["e"], k1st=st.k1, k2nd=st.k2, P1=w["P1"],
                     P2=w["P2"], prefac_eph=w["prefac"], picture=0, expt=1, precision=args.precision, device=dev,
                     f_ref=w["f"])
+    t_create = time.perf_counter() - t_create  # layout, device conversion and upload of P
     h = 1.0 * U.fs
     y0 = np.ascontiguousarray(w["dm0"]).view(np.float64).reshape(-1).copy()
     g.set_state(0.0, y0)
@@ -419,7 +421,8 @@ def run_gpu(args, w, rank, world, dist):
                                            "f32": "f32 (P complex64, rho as deviation from f)",
                                            "bf16x2": "bf16 hi+lo (P 8 B/complex, rho as deviation from f)"
                                            }[args.precision],
-            "data": "synthetic", "config": config_of(w, {"precision": args.precision, "autotuned_shape": shape}),
+            "data": "synthetic", "config": config_of(w, {"precision": args.precision, "autotuned_shape": shape,
+                                                         "create_s": t_create}),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k-pair contraction", "bytes_per_launch": bpl, "avg_launch_ms": pair_avg_ms,

@@ -20,12 +20,18 @@
 
 using namespace dmd;
 
+namespace {
+struct PairSource;
+}
+
 struct dmd_handle {
   int dev = 0;
   cudaStream_t st = nullptr;
   int nk = 0, nbdm = 0, bs = 0, be = 0, nb = 0, nb2 = 0, nb4 = 0;
   long long npair = 0;
   double prefac = 0;
+  double add_scale = 0;        // scale of the additive operators (P += add_scale P_add)
+  PairSource* src = nullptr;   // set while creating from files: where the raw operators come from
   int picture = 0, expt = 1, prec = 0;
   size_t nstate = 0;  // complex elements of the state (nrhs * nk * nbdm^2)
   size_t nstate1 = 0; // complex elements of one state (nk * nbdm^2)
@@ -459,7 +465,7 @@ struct cd {
 // Hermitian coordinates v = M q of an nb x nb Hermitian matrix, column j = (p1, p2) of M:
 // p1 == p2: v_(p1p1) = q_j;  p1 < p2: v_(p1p2) += q_j, v_(p2p1) += q_j;  p1 > p2: v_(p2p1) += i q_j,
 // v_(p1p2) += -i q_j. Returns the entries (index into v, coefficient as (re, im) in {0, +-1}).
-int herm_col(int nb, int j, int* idx, int* cre, int* cim) {
+__host__ __device__ int herm_col(int nb, int j, int* idx, int* cre, int* cim) {
   const int p1 = j / nb, p2 = j % nb;
   if (p1 == p2) {
     idx[0] = j; cre[0] = 1; cim[0] = 0;
@@ -476,14 +482,14 @@ int herm_col(int nb, int j, int* idx, int* cre, int* cim) {
 }
 
 // z * (cr + i ci) for cr, ci in {0, +-1}: exact
-inline cd cmul_unit(cd z, int cr, int ci) {
+__host__ __device__ inline cd cmul_unit(cd z, int cr, int ci) {
   if (ci == 0) return cr > 0 ? z : cd{-z.re, -z.im};
   return ci > 0 ? cd{-z.im, z.re} : cd{z.im, -z.re};
 }
 
 // Q1 = M^H P1 M and Q2 = M^T P2 conj(M) (both nb^2 x nb^2 row-major), the operators of the
 // Hermitian-coordinate contraction (dmd_pairs_cb.cuh)
-void herm_transform(int nb, const cd* P1, const cd* P2, cd* Q1, cd* Q2) {
+__host__ __device__ void herm_transform(int nb, const cd* P1, const cd* P2, cd* Q1, cd* Q2) {
   const int n2 = nb * nb;
   int ia[2], ra[2], ja[2], ib[2], rb[2], jb[2];
   for (int a = 0; a < n2; ++a) {
@@ -507,27 +513,27 @@ void herm_transform(int nb, const cd* P1, const cd* P2, cd* Q1, cd* Q2) {
   }
 }
 
-uint32_t bf16_bits(float x) {  // round to nearest even (finite values)
+__host__ __device__ uint32_t bf16_bits(float x) {  // round to nearest even (finite values)
   uint32_t u;
   memcpy(&u, &x, 4);
   u += 0x7fffu + ((u >> 16) & 1u);
   return u >> 16;
 }
-float bf16_value(uint32_t b) {
+__host__ __device__ float bf16_value(uint32_t b) {
   const uint32_t u = b << 16;
   float x;
   memcpy(&x, &u, 4);
   return x;
 }
 // one 32-bit word: bf16(x) in the upper half, bf16(x - that) in the lower half
-uint32_t pack_bf2(double x) {
+__host__ __device__ uint32_t pack_bf2(double x) {
   const float xf = (float)x;
   const uint32_t hi = bf16_bits(xf);
   const uint32_t lo = bf16_bits((float)(x - (double)bf16_value(hi)));
   return (hi << 16) | lo;
 }
 
-void pack_elem(int prec, cd v, unsigned char* out) {
+__host__ __device__ void pack_elem(int prec, cd v, unsigned char* out) {
   if (prec == DMD_PREC_F64X) {
     const float xh = (float)v.re, yh = (float)v.im;
     const float f[4] = {xh, (float)(v.re - (double)xh), yh, (float)(v.im - (double)yh)};
@@ -544,35 +550,125 @@ void pack_elem(int prec, cd v, unsigned char* out) {
   }
 }
 
-// Contribution of r_f = coords(diag f), s_f = coords(diag(1 - f)) through one stored pair to the
-// transformed sums (the kernel's four products, dmd_pairs_cb.cuh): X'_row += Q1 r_f(col),
-// Y'_row += Q2^T s_f(col) and, with the reverse term, Y'_col += Q1^H s_f(row), X'_col += conj(Q2) r_f(row).
-// a_row, a_col: [2][nb2] (X' then Y') of the row and column k-points.
-void fold_reference(int nb, const cd* Q1, const cd* Q2, const double* f_row, const double* f_col, bool rev,
-                    cd* a_row, cd* a_col) {
-  const int n2 = nb * nb;
-  for (int a = 0; a < n2; ++a)
-    for (int i = 0; i < nb; ++i) {
-      const int ii = i * nb + i;
-      const cd q1 = Q1[a * n2 + ii], q2 = Q2[ii * n2 + a];
-      a_row[a].re += q1.re * f_col[i];
-      a_row[a].im += q1.im * f_col[i];
-      a_row[n2 + a].re += q2.re * (1 - f_col[i]);
-      a_row[n2 + a].im += q2.im * (1 - f_col[i]);
+
+// Raw pair operators in stored order, read in chunks: P1 [cnt][nb4], P2 [cnt][nb4] and, when
+// present, P1_add, P2_add after them (complex128), into one host buffer.
+struct PairSource {
+  virtual ~PairSource() {}
+  virtual bool has_add() const = 0;
+  virtual int read(long long p0, long long cnt, double2* dst) = 0;  // DMD_OK or an error code
+  std::string err;
+};
+
+struct ArraySource : PairSource {
+  const dmd_desc* d;
+  size_t nb4;
+  ArraySource(const dmd_desc* d_, int nb4_) : d(d_), nb4((size_t)nb4_) {}
+  bool has_add() const override { return d->P1_add != nullptr; }
+  int read(long long p0, long long cnt, double2* dst) override {
+    const size_t n = (size_t)cnt * nb4;
+    const double* src[4] = {d->P1, d->P2, d->P1_add, d->P2_add};
+    for (int m = 0; m < (has_add() ? 4 : 2); ++m) memcpy(dst + m * n, src[m] + 2 * (size_t)p0 * nb4, n * 16);
+    return DMD_OK;
+  }
+};
+
+// where stored pair src goes in the column-block element store, and what the deviation fold needs
+struct CbDst {
+  int32_t b0;           // first slot of its row block
+  int16_t n, i;         // pairs in the row block, slot
+  int32_t pr, pc;       // energy ranks of its row and column k-points (stored orientation)
+  int32_t kr, kc;       // the k-points themselves
+  int32_t flags;        // bit 0: stored transposed, bit 1: reverse term (k1 < k2)
+  int32_t pad;
+};
+
+// One thread per pair of a chunk: fold the additive operators, orient, transform to Hermitian
+// coordinates (Q1 = M^H P1 M, Q2 = M^T P2 conj(M)), pack in the arithmetic's format and store at
+// the pair's slot (element-major inside its row block: Q1 row-major, then Q2 column-major). In the
+// deviation form the contraction of diag(f_ref) through the pair is added to acc0 (FP64 atomics).
+template <int NB>
+__global__ void k_cb_fill(long long p0, long long cnt, const double2* __restrict__ raw, int has_add, double add_scale,
+                          const CbDst* __restrict__ dst, int lin, int prec, int esz, unsigned char* __restrict__ store,
+                          const double* __restrict__ fw, double* __restrict__ acc0) {
+  constexpr int NB2 = NB * NB, NB4 = NB2 * NB2, NE = 2 * NB4;
+  const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (j >= cnt) return;
+  const CbDst dd = dst[p0 + j];
+  const bool tr = dd.flags & 1, rev = (dd.flags >> 1) & 1;
+  const size_t nn = (size_t)cnt * NB4;
+  cd Pe[2][NB4];
+  for (int m = 0; m < 2; ++m) {
+    const int sm = tr ? 1 - m : m;  // the transposed pair carries (conj P2, conj P1)
+    const double2* sp = raw + sm * nn + (size_t)j * NB4;
+    const double2* ap = has_add ? raw + (2 + sm) * nn + (size_t)j * NB4 : nullptr;
+    for (int e = 0; e < NB4; ++e) {
+      double x = sp[e].x, yv = sp[e].y;
+      if (ap) {  // P += P_add * scale (ElectronImpurity.cpp:38-39, ElectronPhonon.cpp:96-97)
+        x = __dadd_rn(x, __dmul_rn(ap[e].x, add_scale));
+        yv = __dadd_rn(yv, __dmul_rn(ap[e].y, add_scale));
+      }
+      if (lin ? (m == 1) : tr) yv = -yv;
+      Pe[m][e] = cd{x, yv};
+    }
+  }
+  cd Q[2][NB4];
+  herm_transform(NB, Pe[0], Pe[1], Q[0], Q[1]);
+  if (acc0) {  // what the contraction adds for diag(f_ref), in FP64 (see k_prep_herm)
+    const double* fr = fw + (size_t)dd.kr * NB;
+    const double* fc = fw + (size_t)dd.kc * NB;
+    double* ar = acc0 + (size_t)dd.pr * 2 * NB2 * 2;
+    double* ac = acc0 + (size_t)dd.pc * 2 * NB2 * 2;
+    for (int a = 0; a < NB2; ++a) {
+      double x0 = 0, x1 = 0, y0 = 0, y1 = 0, u0 = 0, u1 = 0, v0 = 0, v1 = 0;
+      for (int i = 0; i < NB; ++i) {
+        const int ii = i * NB + i;
+        const cd q1 = Q[0][a * NB2 + ii], q2 = Q[1][ii * NB2 + a];
+        x0 = __dadd_rn(x0, __dmul_rn(q1.re, fc[i]));
+        x1 = __dadd_rn(x1, __dmul_rn(q1.im, fc[i]));
+        y0 = __dadd_rn(y0, __dmul_rn(q2.re, __dsub_rn(1.0, fc[i])));
+        y1 = __dadd_rn(y1, __dmul_rn(q2.im, __dsub_rn(1.0, fc[i])));
+        if (rev) {
+          const cd q1c = Q[0][ii * NB2 + a], q2c = Q[1][a * NB2 + ii];
+          u0 = __dadd_rn(u0, __dmul_rn(q1c.re, __dsub_rn(1.0, fr[i])));
+          u1 = __dsub_rn(u1, __dmul_rn(q1c.im, __dsub_rn(1.0, fr[i])));
+          v0 = __dadd_rn(v0, __dmul_rn(q2c.re, fr[i]));
+          v1 = __dsub_rn(v1, __dmul_rn(q2c.im, fr[i]));
+        }
+      }
+      atomicAdd(&ar[2 * a], x0);
+      atomicAdd(&ar[2 * a + 1], x1);
+      atomicAdd(&ar[2 * (NB2 + a)], y0);
+      atomicAdd(&ar[2 * (NB2 + a) + 1], y1);
       if (rev) {
-        const cd q1c = Q1[ii * n2 + a], q2c = Q2[a * n2 + ii];
-        a_col[n2 + a].re += q1c.re * (1 - f_row[i]);
-        a_col[n2 + a].im -= q1c.im * (1 - f_row[i]);
-        a_col[a].re += q2c.re * f_row[i];
-        a_col[a].im -= q2c.im * f_row[i];
+        atomicAdd(&ac[2 * (NB2 + a)], u0);
+        atomicAdd(&ac[2 * (NB2 + a) + 1], u1);
+        atomicAdd(&ac[2 * a], v0);
+        atomicAdd(&ac[2 * a + 1], v1);
       }
     }
+  }
+  for (int e = 0; e < NE; ++e) {
+    // stored element e: Q1 row-major for e < nb^4; Q2 column-major after it (e = nb^4 + cc nb^2 + a
+    // holds Q2[a][cc])
+    cd qv;
+    if (e < NB4) {
+      qv = Q[0][e];
+    } else {
+      const int q = e - NB4, cc = q / NB2, a = q % NB2;
+      qv = Q[1][a * NB2 + cc];
+    }
+    pack_elem(prec, qv, store + ((size_t)dd.b0 * NE + (size_t)e * dd.n + dd.i) * esz);
+  }
 }
+
+struct CbDst;
+int fill_pairs_cb(dmd_handle* h, PairSource& src, const std::vector<CbDst>& dst, bool dev);
 
 // column-block layout upload: pairs permuted into row blocks, element-major inside each block,
 // folded with the optional additive operators and converted to the arithmetic's element format
 int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
-  const int nb = h->nb, nb4 = h->nb4, ne = 2 * nb4;
+  const int nb = h->nb, nb4 = h->nb4;
   std::vector<double> ew((size_t)h->nk * nb);
   for (int k = 0; k < h->nk; ++k)
     for (int b = 0; b < nb; ++b) ew[(size_t)k * nb + b] = d->e_dm[(size_t)k * h->nbdm + h->bs + b];
@@ -618,91 +714,109 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
   CK(cudaMemcpy(h->d_rb, L.rb.data(), L.rb.size() * sizeof(dmd::RowBlock), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_items, L.items.data(), L.items.size() * sizeof(dmd::WorkItem), cudaMemcpyHostToDevice));
   const int esz = elem_bytes(h->prec);
-  std::vector<cd> Peff[2] = {std::vector<cd>(nb4), std::vector<cd>(nb4)};
-  std::vector<cd> Q[2] = {std::vector<cd>(nb4), std::vector<cd>(nb4)};
   // deviation form: the constant contraction of diag(f_ref), position order [nk][2][nb2]
   const bool dev = deviation_form(h->prec) && !h->lin;
-  std::vector<cd> acc0;
   std::vector<double> fw;
   if (dev || h->lin) {
-    if (dev) acc0.assign((size_t)h->nk * 2 * h->nb2, cd{0, 0});
     fw.assign((size_t)h->nk * nb, 0.0);
     if (d->f_ref)
       for (int k = 0; k < h->nk; ++k)
         for (int b = 0; b < nb; ++b) fw[(size_t)k * nb + b] = d->f_ref[(size_t)k * h->nbdm + h->bs + b];
-  }
-  const size_t chunk_rb = 1 << 14;  // row blocks per staging chunk
-  unsigned char* stage = nullptr;
-  CK(cudaMallocHost((void**)&stage, chunk_rb * 32 * ne * (size_t)esz));
-  int out = DMD_OK;
-  for (size_t r0 = 0; r0 < L.rb.size() && out == DMD_OK; r0 += chunk_rb) {
-    const size_t r1 = std::min(L.rb.size(), r0 + chunk_rb);
-    const size_t q0 = L.rb[r0].pair0;
-    const size_t q1 = (r1 < L.rb.size()) ? L.rb[r1].pair0 : (size_t)h->npair;
-    for (size_t r = r0; r < r1; ++r) {
-      const size_t b0 = L.rb[r].pair0;
-      const size_t n = (size_t)__builtin_popcount(L.rb[r].mask);
-      for (size_t i = 0; i < n; ++i) {
-        const size_t src = L.src[b0 + i];
-        const bool tr = L.transposed[b0 + i] != 0;
-        const double* s1 = d->P1 + 2 * src * nb4;
-        const double* s2 = d->P2 + 2 * src * nb4;
-        const double* a1 = d->P1_add ? d->P1_add + 2 * src * nb4 : nullptr;
-        const double* a2 = d->P2_add ? d->P2_add + 2 * src * nb4 : nullptr;
-        if (tr) {  // stored as the pair (k2, k1): P1' = conj(P2), P2' = conj(P1) (evolve_eph.cpp:102-103)
-          std::swap(s1, s2);
-          std::swap(a1, a2);
-        }
-        // effective P1, P2 of the stored orientation, folded with the additive operators
-        for (int m = 0; m < 2; ++m)
-          for (int e = 0; e < nb4; ++e) {
-            const double* sp = (m == 0 ? s1 : s2) + 2 * e;
-            const double* ap = (m == 0 ? a1 : a2);
-            double x = sp[0], yv = sp[1];
-            if (ap) {  // P += P_add * scale (ElectronImpurity.cpp:38-39, ElectronPhonon.cpp:96-97)
-              x = x + ap[2 * e] * d->add_scale;
-              yv = yv + ap[2 * e + 1] * d->add_scale;
-            }
-            // P: the transposed pair carries (conj P2, conj P1); linear: (Lji, Lij) with the reverse
-            // operator conjugated, so that conj(Q2) = M^H L_rev M (see the header comment of dmd_pairs_cb.cuh)
-            if (h->lin ? (m == 1) : tr) yv = -yv;
-            Peff[m][e] = {x, yv};
-          }
-        herm_transform(h->nb, Peff[0].data(), Peff[1].data(), Q[0].data(), Q[1].data());
-        if (dev) {  // what the kernel would add for diag(f_ref), in FP64 (see k_prep_herm)
-          const uint64_t kr = tr ? d->k2nd[src] : d->k1st[src], kc = tr ? d->k1st[src] : d->k2nd[src];
-          const bool rev = d->k1st[src] < d->k2nd[src];
-          fold_reference(h->nb, Q[0].data(), Q[1].data(), &fw[kr * nb], &fw[kc * nb], rev,
-                         &acc0[(size_t)L.pos[kr] * 2 * h->nb2], &acc0[(size_t)L.pos[kc] * 2 * h->nb2]);
-        }
-        for (int e = 0; e < ne; ++e) {
-          // stored element e: Q1 row-major for e < nb^4; Q2 column-major after it
-          // (e = nb^4 + cc * nb^2 + a holds Q2[a][cc])
-          cd qv;
-          if (e < nb4) {
-            qv = Q[0][e];
-          } else {
-            const int q = e - nb4, cc = q / h->nb2, a = q % h->nb2;
-            qv = Q[1][a * h->nb2 + cc];
-          }
-          pack_elem(h->prec, qv, stage + ((b0 - q0) * ne + (size_t)e * n + i) * esz);
-        }
-      }
-    }
-    cudaError_t e = cudaMemcpy((unsigned char*)h->d_P + q0 * ne * esz, stage, (q1 - q0) * ne * esz,
-                               cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) out = fail(h, DMD_E_CUDA, std::string("P upload: ") + cudaGetErrorString(e));
-  }
-  cudaFreeHost(stage);
-  if (out == DMD_OK && (dev || h->lin)) {
-    if ((out = dalloc(h, &h->d_fref, fw.size()))) return out;
+    if ((rc = dalloc(h, &h->d_fref, fw.size()))) return rc;
     CK(cudaMemcpy(h->d_fref, fw.data(), fw.size() * 8, cudaMemcpyHostToDevice));
   }
-  if (out == DMD_OK && dev) {
-    if ((out = dalloc(h, &h->d_acc0, acc0.size()))) return out;
-    CK(cudaMemcpy(h->d_acc0, acc0.data(), acc0.size() * 16, cudaMemcpyHostToDevice));
+  if (dev) {
+    if ((rc = dalloc(h, &h->d_acc0, (size_t)h->nk * 2 * h->nb2))) return rc;
+    CK(cudaMemset(h->d_acc0, 0, (size_t)h->nk * 2 * h->nb2 * 16));
   }
-  return out;
+  // destination of every stored pair
+  std::vector<CbDst> dst((size_t)h->npair);
+  for (size_t r = 0; r < L.rb.size(); ++r) {
+    const size_t b0 = L.rb[r].pair0;
+    const int n = __builtin_popcount(L.rb[r].mask);
+    for (int i = 0; i < n; ++i) {
+      const size_t src = L.src[b0 + i];
+      const bool tr = L.transposed[b0 + i] != 0;
+      const uint64_t kr = tr ? d->k2nd[src] : d->k1st[src], kc = tr ? d->k1st[src] : d->k2nd[src];
+      CbDst& o = dst[src];
+      o.b0 = (int32_t)b0;
+      o.n = (int16_t)n;
+      o.i = (int16_t)i;
+      o.kr = (int32_t)kr;
+      o.kc = (int32_t)kc;
+      o.pr = L.pos[kr];
+      o.pc = L.pos[kc];
+      o.flags = (tr ? 1 : 0) | (d->k1st[src] < d->k2nd[src] ? 2 : 0);
+      o.pad = 0;
+    }
+  }
+  PairSource* srcp = h->src ? h->src : nullptr;
+  ArraySource arrays(d, nb4);
+  if (!srcp) srcp = &arrays;
+  return fill_pairs_cb(h, *srcp, dst, dev);
+}
+
+// Streams the raw operators through two pinned chunks and the fill kernel: the host reads chunk
+// c + 1 while the device converts chunk c.
+int fill_pairs_cb(dmd_handle* h, PairSource& src, const std::vector<CbDst>& dst, bool dev) {
+  const int nb4 = h->nb4, esz = elem_bytes(h->prec);
+  const int nseg = src.has_add() ? 4 : 2;
+  const size_t per_pair = (size_t)nseg * nb4 * 16;
+  long long chunk = std::max<long long>(1, std::min<long long>(h->npair, (256LL << 20) / (long long)per_pair));
+  if (const char* v = getenv("DMD_FILL_CHUNK")) chunk = std::max(1LL, std::min<long long>(chunk, atoll(v)));  // tests
+  CbDst* d_dst = nullptr;
+  int rc;
+  if ((rc = dalloc(h, &d_dst, dst.size()))) return rc;
+  double2* pin[2] = {nullptr, nullptr};
+  double2* dev_raw[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(h->st);
+    for (int b = 0; b < 2; ++b) {
+      if (pin[b]) cudaFreeHost(pin[b]);
+      if (dev_raw[b]) cudaFree(dev_raw[b]);
+      if (done[b]) cudaEventDestroy(done[b]);
+    }
+    cudaFree(d_dst);
+  };
+  cudaError_t e = cudaMemcpy(d_dst, dst.data(), dst.size() * sizeof(CbDst), cudaMemcpyHostToDevice);
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    e = cudaMallocHost((void**)&pin[b], (size_t)chunk * per_pair);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dev_raw[b], (size_t)chunk * per_pair);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    cleanup();
+    return fail(h, e == cudaErrorMemoryAllocation ? DMD_E_NOMEM : DMD_E_CUDA,
+                std::string("pair staging: ") + cudaGetErrorString(e));
+  }
+  int b = 0;
+  for (long long p0 = 0; p0 < h->npair; p0 += chunk, b ^= 1) {
+    const long long cnt = std::min<long long>(chunk, h->npair - p0);
+    if (cudaEventSynchronize(done[b]) != cudaSuccess) break;  // the copy out of this buffer has finished
+    if ((rc = src.read(p0, cnt, pin[b]))) {
+      cleanup();
+      return fail(h, rc, src.err.empty() ? "reading the pair operators" : src.err);
+    }
+    // the chunk is contiguous in pin[b] with segment stride cnt * nb4
+    e = cudaMemcpyAsync(dev_raw[b], pin[b], (size_t)cnt * per_pair, cudaMemcpyHostToDevice, h->st);
+    if (e != cudaSuccess) break;
+    cudaEventRecord(done[b], h->st);
+    const unsigned g = blocks_for(cnt, 128);
+    double* a0 = dev ? (double*)h->d_acc0 : nullptr;
+    if (h->nb == 2)
+      k_cb_fill<2><<<g, 128, 0, h->st>>>(p0, cnt, dev_raw[b], src.has_add(), h->add_scale, d_dst, h->lin, h->prec,
+                                         esz, (unsigned char*)h->d_P, h->d_fref, a0);
+    else
+      k_cb_fill<4><<<g, 128, 0, h->st>>>(p0, cnt, dev_raw[b], src.has_add(), h->add_scale, d_dst, h->lin, h->prec,
+                                         esz, (unsigned char*)h->d_P, h->d_fref, a0);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) break;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  cleanup();
+  if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("pair fill: ") + cudaGetErrorString(e));
+  return DMD_OK;
 }
 
 // Effective P1, P2 of stored pair src in its given orientation (k1 <- k2): folded with the additive
@@ -1109,15 +1223,15 @@ const char* dmd_strerror(int s) {
 
 const char* dmd_last_error(const dmd_handle* h) { return h ? h->err.c_str() : "null handle"; }
 
-int dmd_create(const dmd_desc* d, dmd_handle** out) {
+static int create_impl(const dmd_desc* d, dmd_handle** out, PairSource* src) {
   if (!out) return DMD_E_ARG;
   *out = nullptr;
   if (!d) return DMD_E_ARG;
   if (d->nk <= 0 || d->nb_dm <= 0 || d->nb_dm > DMD_MAX_NBDM || d->bstart < 0 || d->bend > d->nb_dm ||
       d->bend - d->bstart < 1 || d->bend - d->bstart > 4 || d->nkpair < 0 || !d->e_dm)
     return DMD_E_ARG;
-  if (d->nkpair > 0 && (!d->k1st || !d->k2nd || !d->P1 || !d->P2)) return DMD_E_ARG;
-  if ((d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
+  if (d->nkpair > 0 && (!d->k1st || !d->k2nd || (!src && (!d->P1 || !d->P2)))) return DMD_E_ARG;
+  if (!src && (d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
   if (d->flags & ~(DMD_FLAG_LINEAR | DMD_FLAG_ADJOINT)) return DMD_E_ARG;
   if ((d->flags & DMD_FLAG_ADJOINT) && d->nrhs > 1) return DMD_E_ARG;
   const int nrhs = d->nrhs > 1 ? d->nrhs : 1;
@@ -1145,6 +1259,7 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   h->nb4 = h->nb2 * h->nb2;
   h->npair = d->nkpair;
   h->prefac = d->prefac_eph;
+  h->add_scale = d->add_scale;
   h->picture = d->picture;
   h->expt = d->expt ? 1 : 0;
   h->prec = d->precision;
@@ -1197,8 +1312,11 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
   h->use_cb = ((h->nb == 2 || h->nb == 4) && h->npair > 0) ? 1 : 0;
   if (!h->use_tc)
     h->pair_bytes = h->use_cb ? (int64_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) : (int64_t)h->npair * 2 * h->nb4 * 16;
-  if ((rc = h->use_tc ? upload_pairs_tc(h, d) : h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d)))
-    return bail(rc);
+  if (src && (!h->use_cb || h->use_tc || h->adj)) return bail(fail(h, DMD_E_ARG, "streamed operators need the column-block form"));
+  h->src = src;
+  rc = h->use_tc ? upload_pairs_tc(h, d) : h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d);
+  h->src = nullptr;
+  if (rc) return bail(rc);
   if (h->adj && h->use_cb && h->npair > 0) {  // the adjoint's transposed contraction reads stored-order P
     if ((rc = dalloc(h, &h->d_Praw, (size_t)h->npair * 2 * h->nb4)) || (rc = dalloc(h, &h->d_kkraw, (size_t)h->npair)) ||
         (rc = upload_raw(h, d, h->d_Praw, h->d_kkraw)))
@@ -1210,6 +1328,87 @@ int dmd_create(const dmd_desc* d, dmd_handle** out) {
     return bail(fail(h, DMD_E_CUDA, "init"));
   *out = h;
   return DMD_OK;
+}
+
+int dmd_create(const dmd_desc* d, dmd_handle** out) { return create_impl(d, out, nullptr); }
+
+}  // extern "C"
+
+namespace {
+// DMD's operator files (complex128 [nkpair][nb^4], ldbd_P1_lindblad.bin etc.), read chunk by chunk
+struct FileSource : PairSource {
+  FILE* f[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t nb4 = 0;
+  bool add = false;
+  ~FileSource() override {
+    for (FILE* x : f)
+      if (x) fclose(x);
+  }
+  bool has_add() const override { return add; }
+  int open(int m, const char* path, long long npair) {
+    f[m] = fopen(path, "rb");
+    if (!f[m]) {
+      err = std::string("cannot open ") + path;
+      return DMD_E_FILE;
+    }
+    if (fseeko(f[m], 0, SEEK_END) != 0 || ftello(f[m]) != (off_t)(npair * (long long)nb4 * 16)) {
+      err = std::string("size of ") + path + " does not match nkpair * nb^4 complex128";
+      return DMD_E_FILE;
+    }
+    fseeko(f[m], 0, SEEK_SET);
+    return DMD_OK;
+  }
+  int read(long long p0, long long cnt, double2* dst) override {
+    const size_t n = (size_t)cnt * nb4;
+    for (int m = 0; m < (add ? 4 : 2); ++m) {
+      if (fseeko(f[m], (off_t)(p0 * (long long)nb4 * 16), SEEK_SET) != 0 || fread(dst + m * n, 16, n, f[m]) != n) {
+        err = "short read of a pair-operator file";
+        return DMD_E_FILE;
+      }
+    }
+    return DMD_OK;
+  }
+};
+}  // namespace
+
+extern "C" {
+
+int dmd_create_from_files(const dmd_desc* d, const char* p1_path, const char* p2_path, const char* p1_add_path,
+                          const char* p2_add_path, dmd_handle** out) {
+  if (!d || !out || !p1_path || !p2_path || (p1_add_path == nullptr) != (p2_add_path == nullptr)) return DMD_E_ARG;
+  if (d->bend - d->bstart < 1 || d->bend - d->bstart > 4 || d->nkpair < 0) return DMD_E_ARG;
+  const int nb = d->bend - d->bstart;
+  FileSource fs;
+  fs.nb4 = (size_t)nb * nb * nb * nb;
+  fs.add = p1_add_path != nullptr;
+  const char* paths[4] = {p1_path, p2_path, p1_add_path, p2_add_path};
+  for (int m = 0; m < (fs.add ? 4 : 2); ++m)
+    if (fs.open(m, paths[m], d->nkpair) != DMD_OK) {
+      fprintf(stderr, "dmd_create_from_files: %s\n", fs.err.c_str());
+      return DMD_E_FILE;
+    }
+  dmd_desc dc = *d;
+  dc.P1 = dc.P2 = dc.P1_add = dc.P2_add = nullptr;
+  const char* tc = getenv("DMD_BATCH_TC");
+  const bool tc_form = d->nrhs > 1 && nb == 2 && d->precision == DMD_PREC_BF16X2 && !(tc && atoi(tc) == 0);
+  if ((nb == 2 || nb == 4) && d->nkpair > 0 && !tc_form && !(d->flags & DMD_FLAG_ADJOINT))
+    return create_impl(&dc, out, &fs);  // streamed: two chunks of the files in host memory at a time
+  // the other forms take the operators from host memory
+  std::vector<double> buf[4];
+  const size_t n = (size_t)d->nkpair * fs.nb4;
+  for (int m = 0; m < (fs.add ? 4 : 2); ++m) buf[m].resize(2 * (n ? n : 1));
+  if (n) {
+    for (int m = 0; m < (fs.add ? 4 : 2); ++m) {
+      if (fseeko(fs.f[m], 0, SEEK_SET) != 0 || fread(buf[m].data(), 16, n, fs.f[m]) != n) return DMD_E_FILE;
+    }
+  }
+  dc.P1 = buf[0].data();
+  dc.P2 = buf[1].data();
+  if (fs.add) {
+    dc.P1_add = buf[2].data();
+    dc.P2_add = buf[3].data();
+  }
+  return create_impl(&dc, out, nullptr);
 }
 
 int dmd_destroy(dmd_handle* h) {

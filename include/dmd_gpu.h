@@ -96,6 +96,14 @@ typedef struct dmd_desc {
 } dmd_desc;
 
 int dmd_create(const dmd_desc* desc, dmd_handle** out);
+/* dmd_create with the pair operators read from DMD's files (ldbd_P1_lindblad.bin, ldbd_P2_lindblad.bin
+ * and, optionally, the _D1 impurity files scaled by desc->add_scale; complex128 [nkpair][nb^4],
+ * ElectronPhonon.cpp:209-253); desc->P1/P2/P1_add/P2_add are ignored. The column-block forms stream
+ * the files in chunks through pinned buffers and convert them on the device (two chunks of 256 MB in
+ * host memory at a time); the other forms read the files into host memory first. A file whose size
+ * is not nkpair * nb^4 * 16 bytes gives DMD_E_FILE (check_file_size). */
+int dmd_create_from_files(const dmd_desc* desc, const char* p1_path, const char* p2_path, const char* p1_add_path,
+                          const char* p2_add_path, dmd_handle** out);
 int dmd_destroy(dmd_handle* h);
 const char* dmd_last_error(const dmd_handle* h);
 const char* dmd_strerror(int status);

@@ -4,6 +4,7 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
 import pytest
 
 from conftest import ROOT
@@ -42,3 +43,21 @@ def test_strerror_and_null_arguments(gpu_lib):
     h = C.c_void_p()
     assert gpu_lib.dmd_create(None, C.byref(h)) == 1
     assert gpu_lib.dmd_destroy(None) == 1
+
+
+def test_create_from_files_rejects_wrong_sizes(tmp_path):
+    """a file whose size is not nkpair * nb^4 * 16 bytes gives DMD_E_FILE before any device work"""
+    import ctypes as C
+    from denmat_dynm_development_gb300 import dmd
+    L = dmd._lib()
+    good = tmp_path / "P1.bin"
+    bad = tmp_path / "P2.bin"
+    np.zeros(5 * 16, np.complex128).tofile(str(good))
+    np.zeros(5 * 16 - 1, np.complex128).tofile(str(bad))
+    d = dmd._Desc(nk=10, nb_dm=2, bstart=0, bend=2, nkpair=5)
+    h = C.c_void_p()
+    st = L.dmd_create_from_files(C.byref(d), str(good).encode(), str(bad).encode(), None, None, C.byref(h))
+    assert st == 3  # DMD_E_FILE
+    st = L.dmd_create_from_files(C.byref(d), str(good).encode(), str(tmp_path / "missing").encode(), None, None,
+                                 C.byref(h))
+    assert st == 3

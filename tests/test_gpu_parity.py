@@ -535,3 +535,47 @@ def test_group_steps_members_as_when_alone(oracle, built):
     finally:
         for g in hs:
             g.close()
+
+
+def _write_c128(path, a):
+    np.ascontiguousarray(a, dtype=np.complex128).tofile(str(path))
+    return str(path)
+
+
+@pytest.mark.parametrize("case,prec,nrhs", [("nb2_eimp_B", "f64x", 1), ("nb2_eimp_B", "bf16x2", 1),
+                                            ("nb4_eimp_B", "f64x", 1), ("nb2_linear", "f32", 1),
+                                            ("nb2_eimp_B", "f32", 3)])
+@pytest.mark.parametrize("chunk", [None, "7"])
+def test_create_from_files_matches_arrays(case, prec, nrhs, chunk, oracle, built, tmp_path, monkeypatch):
+    """dmd_create_from_files streams DMD's operator files (here with additive operators scaled by
+    add_scale) through pinned chunks into the device conversion; the handle equals one created from
+    the same arrays (the deviation forms fold diag(f_ref) with atomics: rounding-level differences),
+    also when the files go through in chunks of 7 pairs."""
+    from denmat_dynm_development_gb300.dmd import LindbladGPU
+    s = oracle.load(os.path.join(GOLDEN, case))
+    if chunk:
+        monkeypatch.setenv("DMD_FILL_CHUNK", chunk)
+    rng = np.random.default_rng(2)
+    A1 = (rng.standard_normal(s.P1.size) + 1j * rng.standard_normal(s.P1.size)) * np.abs(s.P1).max()
+    A2 = (rng.standard_normal(s.P2.size) + 1j * rng.standard_normal(s.P2.size)) * np.abs(s.P2).max()
+    files = [_write_c128(tmp_path / n, a) for n, a in (("P1.bin", s.P1), ("P2.bin", s.P2), ("A1.bin", A1),
+                                                      ("A2.bin", A2))]
+    lin = bool(getattr(s, "linear", False))
+    kw = dict(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
+              prefac_eph=s.prefac_eph, Hcoh=s.Hcoh, picture=s.picture_schrodinger, expt=s.expt, precision=prec,
+              linear=lin, nrhs=nrhs, f_ref=(s.f_eq if lin else s.f_dm) if prec in ("f32", "bf16x2") else None)
+    if lin:  # the linearized form takes no additive operators
+        files = files[:2]
+        arrays = dict(P1=s.P1, P2=s.P2)
+    else:
+        arrays = dict(P1=s.P1, P2=s.P2, P1_add=A1, P2_add=A2, add_scale=0.3)
+        kw["add_scale"] = 0.3
+    ys = np.concatenate(_herm_states(s, nrhs, 4))
+    t = 23.0 * oracle.fs
+    with LindbladGPU(**kw, **{k: v for k, v in arrays.items() if k != "add_scale"}) as ga:
+        ra = ga.func(t, ys)
+    with LindbladGPU(P1=None, P2=None, P_files=files, **kw) as gf:
+        rf = gf.func(t, ys)
+    tol = 1e-15 if prec in ("f64", "f64x") else 1e-12
+    assert rel(rf, ra) <= tol
+
