@@ -1369,9 +1369,129 @@ struct FileSource : PairSource {
     return DMD_OK;
   }
 };
+// DMD's sparse operator files (alg.Pin_is_sparse: sparse2D / sparse_mat, comm/sparse2D.h:115-128,
+// comm/sparse_matrix.h:30-36): per pair a count ns (int32, <prefix>_ns.bin), then ns values
+// (complex128, _s.bin) with their row and column indices (int32, _i.bin, _j.bin), read in pair order
+// and written densely into the chunk (optional dense additive files as in FileSource)
+struct SparseFileSource : PairSource {
+  FILE* f[2][4] = {{nullptr, nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr, nullptr}};
+  FileSource add;  // the dense additive operators in its slots 0 and 1
+  size_t nb4 = 0, nb2 = 0;
+  long long next = 0;  // the next pair the streams are positioned at
+  std::vector<double2> sv;
+  std::vector<int32_t> si, sj;
+  ~SparseFileSource() override {
+    for (auto& g : f)
+      for (FILE* x : g)
+        if (x) fclose(x);
+  }
+  bool has_add() const override { return add.add; }
+  int open(int m, const std::string& prefix, long long npair) {
+    const char* sfx[4] = {"_ns.bin", "_s.bin", "_i.bin", "_j.bin"};
+    for (int q = 0; q < 4; ++q) {
+      const std::string path = prefix + sfx[q];
+      f[m][q] = fopen(path.c_str(), "rb");
+      if (!f[m][q]) {
+        err = "cannot open " + path;
+        return DMD_E_FILE;
+      }
+    }
+    if (fseeko(f[m][0], 0, SEEK_END) != 0 || ftello(f[m][0]) != (off_t)(npair * 4)) {
+      err = prefix + "_ns.bin does not hold one int32 count per k-pair";
+      return DMD_E_FILE;
+    }
+    fseeko(f[m][0], 0, SEEK_SET);
+    return DMD_OK;
+  }
+  int read(long long p0, long long cnt, double2* dst) override {
+    if (p0 != next) {
+      err = "sparse operator files are read in pair order";
+      return DMD_E_FILE;
+    }
+    const size_t n = (size_t)cnt * nb4;
+    std::vector<int32_t> ns((size_t)cnt);
+    for (int m = 0; m < 2; ++m) {
+      double2* out = dst + m * n;
+      memset(out, 0, n * 16);
+      if (fread(ns.data(), 4, (size_t)cnt, f[m][0]) != (size_t)cnt) {
+        err = "short read of an _ns.bin file";
+        return DMD_E_FILE;
+      }
+      long long tot = 0;
+      for (int32_t c : ns) {
+        if (c < 0 || (size_t)c > nb4) {
+          err = "invalid element count in an _ns.bin file";
+          return DMD_E_FILE;
+        }
+        tot += c;
+      }
+      sv.resize((size_t)tot);
+      si.resize((size_t)tot);
+      sj.resize((size_t)tot);
+      if (fread(sv.data(), 16, (size_t)tot, f[m][1]) != (size_t)tot || fread(si.data(), 4, (size_t)tot, f[m][2]) != (size_t)tot ||
+          fread(sj.data(), 4, (size_t)tot, f[m][3]) != (size_t)tot) {
+        err = "short read of a sparse operator file";
+        return DMD_E_FILE;
+      }
+      size_t q = 0;
+      for (long long p = 0; p < cnt; ++p)
+        for (int32_t c = 0; c < ns[(size_t)p]; ++c, ++q) {
+          const int32_t a = si[q], b = sj[q];
+          if (a < 0 || b < 0 || (size_t)a >= nb2 || (size_t)b >= nb2) {
+            err = "element index out of range in a sparse operator file";
+            return DMD_E_FILE;
+          }
+          double2& o = out[(size_t)p * nb4 + (size_t)a * nb2 + b];  // repeated (i, j) add up
+          o.x += sv[q].x;
+          o.y += sv[q].y;
+        }
+    }
+    if (add.add) {  // dense additive operators: segments 2 and 3
+      add.add = false;  // FileSource reads its two slots
+      const int rc = add.read(p0, cnt, dst + 2 * n);
+      add.add = true;
+      if (rc != DMD_OK) {
+        err = add.err;
+        return DMD_E_FILE;
+      }
+    }
+    next = p0 + cnt;
+    return DMD_OK;
+  }
+};
 }  // namespace
 
 extern "C" {
+
+int dmd_create_from_sparse_files(const dmd_desc* d, const char* sp1_prefix, const char* sp2_prefix,
+                                 const char* p1_add_path, const char* p2_add_path, dmd_handle** out) {
+  if (!d || !out || !sp1_prefix || !sp2_prefix || (p1_add_path == nullptr) != (p2_add_path == nullptr))
+    return DMD_E_ARG;
+  if (d->bend - d->bstart < 1 || d->bend - d->bstart > 4 || d->nkpair < 0) return DMD_E_ARG;
+  const int nb = d->bend - d->bstart;
+  SparseFileSource ss;
+  ss.nb2 = (size_t)nb * nb;
+  ss.nb4 = ss.nb2 * ss.nb2;
+  if (ss.open(0, sp1_prefix, d->nkpair) != DMD_OK || ss.open(1, sp2_prefix, d->nkpair) != DMD_OK) {
+    fprintf(stderr, "dmd_create_from_sparse_files: %s\n", ss.err.c_str());
+    return DMD_E_FILE;
+  }
+  if (p1_add_path) {
+    ss.add.nb4 = ss.nb4;
+    ss.add.add = true;
+    if (ss.add.open(0, p1_add_path, d->nkpair) != DMD_OK || ss.add.open(1, p2_add_path, d->nkpair) != DMD_OK) {
+      fprintf(stderr, "dmd_create_from_sparse_files: %s\n", ss.add.err.c_str());
+      return DMD_E_FILE;
+    }
+  }
+  dmd_desc dc = *d;
+  dc.P1 = dc.P2 = dc.P1_add = dc.P2_add = nullptr;
+  const char* tc = getenv("DMD_BATCH_TC");
+  const bool tc_form = d->nrhs > 1 && nb == 2 && d->precision == DMD_PREC_BF16X2 && !(tc && atoi(tc) == 0);
+  if (!((nb == 2 || nb == 4) && d->nkpair > 0 && !tc_form && !(d->flags & DMD_FLAG_ADJOINT)))
+    return DMD_E_ARG;  // the other forms take dense operators (dmd_create, dmd_create_from_files)
+  return create_impl(&dc, out, &ss);
+}
 
 int dmd_create_from_files(const dmd_desc* d, const char* p1_path, const char* p2_path, const char* p1_add_path,
                           const char* p2_add_path, dmd_handle** out) {

@@ -45,7 +45,7 @@ EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_s
            "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
            "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes", "dmd_adjoint_rk4", "dmd_autotune",
            "dmd_group_create", "dmd_group_rk4", "dmd_group_destroy",
-           "dmd_create_from_files"]
+           "dmd_create_from_files", "dmd_create_from_sparse_files"]
 
 
 def _lib():
@@ -82,6 +82,8 @@ def _lib():
         L.dmd_group_destroy.argtypes = [vp]
         L.dmd_create_from_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                             C.POINTER(vp)]
+        L.dmd_create_from_sparse_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p,
+                                                   C.c_char_p, C.POINTER(vp)]
         L.dmd_adjoint_rk4.argtypes = [vp, d, vp, d, i64, i64, C.c_int, C.c_int, C.c_int, i64, vp, vp, vp, vp, vp]
         L.dmd_sync.argtypes = [vp]
         L.dmd_pinned_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
@@ -104,7 +106,7 @@ class LindbladGPU:
 
     def __init__(self, *, nk, nb_dm, bstart, bend, e_dm, k1st, k2nd, P1, P2, prefac_eph, Hcoh=None,
                  picture="interaction", expt=1, precision="f64", P1_add=None, P2_add=None, add_scale=0.0, device=0,
-                 f_ref=None, linear=False, nrhs=1, adjoint=False, P_files=None):
+                 f_ref=None, linear=False, nrhs=1, adjoint=False, P_files=None, P_sparse=None):
         L = _lib()
         self._keep = dict(e=_c(e_dm, np.float64), k1=_c(k1st, np.uint64), k2=_c(k2nd, np.uint64),
                           P1=_c(P1, np.complex128), P2=_c(P2, np.complex128), H=_c(Hcoh, np.complex128),
@@ -122,6 +124,9 @@ class LindbladGPU:
         if P_files is not None:  # DMD's operator files, streamed by the library
             fp = [None if f is None else os.fsencode(f) for f in (list(P_files) + [None, None])[:4]]
             st = L.dmd_create_from_files(C.byref(desc), fp[0], fp[1], fp[2], fp[3], C.byref(h))
+        elif P_sparse is not None:  # DMD's sparse operator files (prefixes), plus optional dense additive files
+            fp = [None if f is None else os.fsencode(f) for f in (list(P_sparse) + [None, None])[:4]]
+            st = L.dmd_create_from_sparse_files(C.byref(desc), fp[0], fp[1], fp[2], fp[3], C.byref(h))
         else:
             st = L.dmd_create(C.byref(desc), C.byref(h))
         if st != 0:

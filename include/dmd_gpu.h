@@ -104,6 +104,13 @@ int dmd_create(const dmd_desc* desc, dmd_handle** out);
  * is not nkpair * nb^4 * 16 bytes gives DMD_E_FILE (check_file_size). */
 int dmd_create_from_files(const dmd_desc* desc, const char* p1_path, const char* p2_path, const char* p1_add_path,
                           const char* p2_add_path, dmd_handle** out);
+/* dmd_create_from_files for DMD's sparse operator input (alg.Pin_is_sparse, ElectronPhonon.cpp:240-247):
+ * <prefix>_ns.bin (int32 count per pair), _s.bin (complex128 values), _i.bin and _j.bin (int32 row
+ * and column in the nb^2 x nb^2 operator) for P1 and P2, plus optional dense additive files. The
+ * operators are densified chunk by chunk on the host and converted on the device; the column-block
+ * forms only (DMD_E_ARG otherwise). */
+int dmd_create_from_sparse_files(const dmd_desc* desc, const char* sp1_prefix, const char* sp2_prefix,
+                                 const char* p1_add_path, const char* p2_add_path, dmd_handle** out);
 int dmd_destroy(dmd_handle* h);
 const char* dmd_last_error(const dmd_handle* h);
 const char* dmd_strerror(int status);

@@ -61,3 +61,19 @@ def test_create_from_files_rejects_wrong_sizes(tmp_path):
     st = L.dmd_create_from_files(C.byref(d), str(good).encode(), str(tmp_path / "missing").encode(), None, None,
                                  C.byref(h))
     assert st == 3
+
+
+def test_create_from_sparse_files_checks_the_counts_file(tmp_path):
+    """the per-pair count file must hold one int32 per k-pair (DMD_E_FILE before any device work)"""
+    import ctypes as C
+    from denmat_dynm_development_gb300 import dmd
+    L = dmd._lib()
+    for m in ("sP1", "sP2"):
+        np.zeros(4, np.int32).tofile(str(tmp_path / (m + "_ns.bin")))  # 4 counts for 5 pairs
+        for sfx in ("_s.bin", "_i.bin", "_j.bin"):
+            open(str(tmp_path / (m + sfx)), "wb").close()
+    d = dmd._Desc(nk=10, nb_dm=2, bstart=0, bend=2, nkpair=5)
+    h = C.c_void_p()
+    st = L.dmd_create_from_sparse_files(C.byref(d), str(tmp_path / "sP1").encode(), str(tmp_path / "sP2").encode(),
+                                        None, None, C.byref(h))
+    assert st == 3  # DMD_E_FILE

@@ -579,3 +579,49 @@ def test_create_from_files_matches_arrays(case, prec, nrhs, chunk, oracle, built
     tol = 1e-15 if prec in ("f64", "f64x") else 1e-12
     assert rel(rf, ra) <= tol
 
+
+
+def write_sparse(prefix, P, nb4, rng):
+    """DMD's sparse operator files: nonzeros of each pair in a random order"""
+    n2 = int(round(nb4 ** 0.5))
+    P = np.asarray(P, np.complex128).reshape(-1, nb4)
+    ns, sv, si, sj = [], [], [], []
+    for row in P:
+        nz = np.nonzero(row)[0]
+        nz = nz[rng.permutation(nz.size)]
+        ns.append(nz.size)
+        sv.append(row[nz])
+        si.append(nz // n2)
+        sj.append(nz % n2)
+    np.array(ns, np.int32).tofile(prefix + "_ns.bin")
+    np.concatenate(sv).astype(np.complex128).tofile(prefix + "_s.bin")
+    np.concatenate(si).astype(np.int32).tofile(prefix + "_i.bin")
+    np.concatenate(sj).astype(np.int32).tofile(prefix + "_j.bin")
+    return prefix
+
+
+@pytest.mark.parametrize("prec", ["f64x", "bf16x2"])
+def test_create_from_sparse_files_matches_dense(prec, oracle, built, tmp_path, monkeypatch):
+    """DMD's sparse operator input (alg.Pin_is_sparse): operators with structural zeros written as
+    per-pair (count, values, row, column) files in a random element order, streamed in chunks of 5
+    pairs, equal the dense operators."""
+    from denmat_dynm_development_gb300.dmd import LindbladGPU
+    s = oracle.load(os.path.join(GOLDEN, "nb2_eimp_B"))
+    rng = np.random.default_rng(8)
+    P1 = s.P1.copy().reshape(-1, 16)
+    P2 = s.P2.copy().reshape(-1, 16)
+    P1[rng.random(P1.shape) < 0.4] = 0  # structural zeros
+    P2[rng.random(P2.shape) < 0.4] = 0
+    P1[3] = 0  # an empty operator
+    monkeypatch.setenv("DMD_FILL_CHUNK", "5")
+    sp = [write_sparse(str(tmp_path / n), P, 16, rng) for n, P in (("sP1", P1), ("sP2", P2))]
+    kw = dict(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
+              prefac_eph=s.prefac_eph, Hcoh=s.Hcoh, picture=s.picture_schrodinger, expt=s.expt, precision=prec,
+              f_ref=s.f_dm if prec == "bf16x2" else None)
+    y = oracle.y_of(s.dm0)
+    t = 31.0 * oracle.fs
+    with LindbladGPU(P1=P1.reshape(-1), P2=P2.reshape(-1), **kw) as gd:
+        rd = gd.func(t, y)
+    with LindbladGPU(P1=None, P2=None, P_sparse=sp, **kw) as gs:
+        rs = gs.func(t, y)
+    assert rel(rs, rd) <= (1e-15 if prec == "f64x" else 1e-12)
