@@ -625,3 +625,29 @@ def test_create_from_sparse_files_matches_dense(prec, oracle, built, tmp_path, m
     with LindbladGPU(P1=None, P2=None, P_sparse=sp, **kw) as gs:
         rs = gs.func(t, y)
     assert rel(rs, rd) <= (1e-15 if prec == "f64x" else 1e-12)
+
+
+def test_t2_in_transverse_field_from_gpu_trajectory(oracle, built):
+    """T2: S_z precessing about the 2 T in-plane field of nb2_eimp_B (initial spin along z), fitted
+    with the decaying-cosine model of fit.py (the field sets omega); the GPU trajectory's fitted
+    lifetime within 1e-8 of the oracle's (the fits' convergence tolerance), S(t) within 1e-10."""
+    from denmat_dynm_development_gb300.t1fit import fit_t1
+    s = oracle.load(os.path.join(GOLDEN, "nb2_eimp_B"))
+    h, nsteps, every = 10.0 * oracle.fs, 3000, 50
+    y0 = oracle.y_of(s.dm0)
+    _, rec_o = oracle.rk4(s, s.t0, h, nsteps, y0, every=every)
+    with make_gpu(s, "f64") as gpu:
+        gpu.set_state(s.t0, y0)
+        gpu.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+        rec = []
+        for _ in range(nsteps // every):
+            gpu.rk4(h, every)
+            t, _ = gpu.get_state()
+            rec.append((t,) + gpu.measure(0, s.nv_dm))
+    rec = np.array(rec)
+    assert rel(rec[:, 1], rec_o[:, 1]) < 1e-10
+    fo = fit_t1(rec_o[:, 0], rec_o[:, 1], bfield_tesla=2.0)
+    fg = fit_t1(rec[:, 0], rec[:, 1], bfield_tesla=2.0)
+    print("T2 oracle %.12g ps gpu %.12g ps" % (fo.tau_lsq, fg.tau_lsq))
+    assert np.isfinite(fo.tau_lsq) and np.isfinite(fg.tau_lsq)
+    assert abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq) < 1e-8
