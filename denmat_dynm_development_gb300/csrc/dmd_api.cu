@@ -2130,6 +2130,48 @@ int dmd_group_rk4(dmd_group* g, double dt, int64_t nsteps) {
   return rc;
 }
 
+}  // extern "C"
+
+namespace {
+// waits on a phase that nothing completes: the bounded wait gives up and raises the flag
+__global__ void k_wait_never(unsigned int* errflag, uint32_t polls) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_wait_bounded(&bar, 0u, errflag, polls);
+}
+__global__ void k_set_one(unsigned int* p) { *p = 1u; }
+}  // namespace
+
+extern "C" {
+
+int dmd_selftest_wait_timeout(int device, uint32_t polls, int* status) {
+  if (!status || polls < 1 || polls > (1u << 20)) return DMD_E_ARG;
+  *status = DMD_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return DMD_E_NODEV;
+  unsigned int* d = nullptr;
+  if (cudaMalloc((void**)&d, 2 * sizeof(unsigned int)) != cudaSuccess) return DMD_E_NOMEM;
+  int rc = DMD_OK;
+  unsigned int hv[2] = {0, 0};
+  if (cudaMemset(d, 0, 2 * sizeof(unsigned int)) != cudaSuccess) rc = DMD_E_CUDA;
+  if (rc == DMD_OK) {
+    k_wait_never<<<1, 32>>>(d, polls);
+    if (cudaDeviceSynchronize() != cudaSuccess) rc = DMD_E_CUDA;
+  }
+  if (rc == DMD_OK) {  // the context still works: a second kernel runs and writes
+    k_set_one<<<1, 1>>>(d + 1);
+    if (cudaMemcpy(hv, d, sizeof(hv), cudaMemcpyDeviceToHost) != cudaSuccess) rc = DMD_E_CUDA;
+  }
+  cudaFree(d);
+  if (rc != DMD_OK) return rc;
+  if (hv[1] != 1u) return DMD_E_CUDA;
+  *status = (hv[0] & DMD_DEVERR_TIMEOUT) ? DMD_E_TIMEOUT : DMD_OK;
+  return DMD_OK;
+}
+
 int dmd_autotune(dmd_handle* h, int evals, int* chosen) {
   if (!h || evals < 1) return DMD_E_ARG;
   CK(cudaSetDevice(h->dev));

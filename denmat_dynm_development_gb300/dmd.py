@@ -45,7 +45,7 @@ EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_s
            "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
            "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes", "dmd_adjoint_rk4", "dmd_autotune",
            "dmd_group_create", "dmd_group_rk4", "dmd_group_destroy",
-           "dmd_create_from_files", "dmd_create_from_sparse_files"]
+           "dmd_create_from_files", "dmd_create_from_sparse_files", "dmd_selftest_wait_timeout"]
 
 
 def _lib():
@@ -80,6 +80,7 @@ def _lib():
         L.dmd_group_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(vp)]
         L.dmd_group_rk4.argtypes = [vp, d, i64]
         L.dmd_group_destroy.argtypes = [vp]
+        L.dmd_selftest_wait_timeout.argtypes = [C.c_int, C.c_uint32, C.POINTER(C.c_int)]
         L.dmd_create_from_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                             C.POINTER(vp)]
         L.dmd_create_from_sparse_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p,

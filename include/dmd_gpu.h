@@ -187,6 +187,12 @@ int dmd_group_create(dmd_handle* const* members, int n, dmd_group** out);
 int dmd_group_rk4(dmd_group* g, double dt, int64_t nsteps);
 int dmd_group_destroy(dmd_group* g);
 
+/* No counterpart in the reference. Self-test of the bounded waits that every bulk-copy pipeline
+ * uses: a kernel waits on an mbarrier phase that nothing completes, gives up after `polls` polls and
+ * raises the device error flag; *status receives what the steppers would return then
+ * (DMD_E_TIMEOUT) and the call checks that the context still runs a kernel afterwards. */
+int dmd_selftest_wait_timeout(int device, uint32_t polls, int* status);
+
 /* No counterpart in the reference. Shape autotuner: times every compiled shape variant of the
  * handle's contraction (f64x, nb = 2: lines per stage, ring depth, CTAs per SM; CUDA-core batches:
  * states per warp) on `evals` right-hand-side evaluations of the current device state (CUDA events,

@@ -651,3 +651,21 @@ def test_t2_in_transverse_field_from_gpu_trajectory(oracle, built):
     print("T2 oracle %.12g ps gpu %.12g ps" % (fo.tau_lsq, fg.tau_lsq))
     assert np.isfinite(fo.tau_lsq) and np.isfinite(fg.tau_lsq)
     assert abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq) < 1e-8
+
+
+def test_bounded_wait_gives_up_and_reports_a_timeout(oracle, built):
+    """A bulk-copy wait that cannot complete (an mbarrier phase nothing completes) gives up after its
+    poll limit and raises the device flag: the host reads DMD_E_TIMEOUT, the context stays usable
+    (the self-test runs a kernel afterwards, and a handle steps normally after it)."""
+    import ctypes as C
+    from denmat_dynm_development_gb300 import dmd
+    L = dmd._lib()
+    st = C.c_int(-1)
+    assert L.dmd_selftest_wait_timeout(0, 256, C.byref(st)) == 0
+    assert st.value == 5  # DMD_E_TIMEOUT
+    s = oracle.load(os.path.join(GOLDEN, "nb2_eimp_B"))
+    with make_gpu(s, "f64x") as gpu:
+        gpu.set_state(s.t0, oracle.y_of(s.dm0))
+        gpu.rk4(1.0 * oracle.fs, 3)
+        _, y = gpu.get_state()
+        assert np.all(np.isfinite(y))
