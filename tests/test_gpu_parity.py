@@ -349,7 +349,7 @@ def _tensor_core_form(s, prec):
 
 
 @pytest.mark.parametrize("prec", ["f32", "bf16x2"])
-@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb4_eimp_B", "nb2_linear", "nb2_carrier_eq"])
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb4_eimp_B", "nb2_linear", "nb2_carrier_eq", "nb2_window"])
 def test_batched_states_vs_oracle(case, prec, oracle, built):
     """Batched form: 7 states share P (nb = 2 with bf16 hi + lo: the tensor-core contraction; else
     RW states per warp on the CUDA cores, the last group short). Every state's RHS matches the oracle
