@@ -63,6 +63,7 @@ struct dmd_handle {
   uint16_t* d_tcA = nullptr;   // [part][group][state block][128 x (hi 32 | lo 32)] bf16
   dmd::TcTile* d_tiles = nullptr;
   int ntiles = 0, ngroups = 0, nmb = 0;
+  int tcst = 4;                // pipeline stages of the tensor-core contraction (autotuned: 4, 3, 2)
   int64_t pair_bytes = 0;      // stored operator bytes (dmd_pair_bytes)
   int adj = 0;                 // DMD_FLAG_ADJOINT: pair operators also in stored order (d_Praw, d_kkraw)
   double2* d_Praw = nullptr;   // [npair][2][nb4] folded P1, P2
@@ -265,10 +266,16 @@ void tc_launches(dmd_handle* h, size_t half) {
   const unsigned g = (unsigned)((size_t)h->ntiles * h->nmb);
   const float ysign = h->lin ? 0.f : -1.f;  // s = -r (deviation form) or 0 (linearized form)
   float2* accf = (float2*)h->d_acc;          // FP32 sums in the tensor-core form
-  k_pairs_tc<false><<<g, 128, TC_SMEM_BYTES, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA, h->nmb, h->nrhs,
-                                                      h->nk, accf, astride, ysign, nullptr, h->d_err);
-  k_pairs_tc<true><<<g, 128, TC_SMEM_BYTES, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA + apart, h->nmb,
-                                                     h->nrhs, h->nk, accf, astride, ysign, h->d_hflag, h->d_err);
+  auto pass = [&](auto kfwd, auto kimag, size_t smem) {
+    kfwd<<<g, 128, smem, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA, h->nmb, h->nrhs, h->nk, accf, astride,
+                                  ysign, nullptr, h->d_err);
+    kimag<<<g, 128, smem, h->st>>>(h->d_tiles, h->ntiles, h->d_tcB, h->d_tcA + apart, h->nmb, h->nrhs, h->nk, accf,
+                                   astride, ysign, h->d_hflag, h->d_err);
+  };
+  // pipeline depth (the shape the autotuner chooses): 4, 3 or 2 stages of 48 KB
+  if (h->tcst == 3) pass(k_pairs_tc<false, 3>, k_pairs_tc<true, 3>, tc_smem_bytes(3));
+  else if (h->tcst == 2) pass(k_pairs_tc<false, 2>, k_pairs_tc<true, 2>, tc_smem_bytes(2));
+  else pass(k_pairs_tc<false, 4>, k_pairs_tc<true, 4>, tc_smem_bytes(4));
   (void)half;
   h->launches += 1;  // the packing launch; the two passes are counted with the other forms
 }
@@ -856,8 +863,12 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
   L.rb.clear();
   L.items.clear();
   L.src.clear();
-  CK(cudaFuncSetAttribute(k_pairs_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_BYTES));
-  CK(cudaFuncSetAttribute(k_pairs_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_BYTES));
+  CK(cudaFuncSetAttribute(k_pairs_tc<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(4)));
+  CK(cudaFuncSetAttribute(k_pairs_tc<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(4)));
+  CK(cudaFuncSetAttribute(k_pairs_tc<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(3)));
+  CK(cudaFuncSetAttribute(k_pairs_tc<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(3)));
+  CK(cudaFuncSetAttribute(k_pairs_tc<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(2)));
+  CK(cudaFuncSetAttribute(k_pairs_tc<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(2)));
   h->ntiles = (nk + TC_TR - 1) / TC_TR;
   h->ngroups = (nk + TC_CG - 1) / TC_CG;
   h->nmb = (h->nrhs + TC_M - 1) / TC_M;
@@ -2184,6 +2195,9 @@ int dmd_autotune(dmd_handle* h, int evals, int* chosen) {
   } else if (h->use_cb && !h->use_tc && h->nrhs > 1 && h->prec == DMD_PREC_F32) {
     cand = {4, 8};
     knob = &h->brw;
+  } else if (h->use_tc) {
+    cand = {4, 3, 2};
+    knob = &h->tcst;
   }
   if (!knob) {
     if (chosen) *chosen = 0;

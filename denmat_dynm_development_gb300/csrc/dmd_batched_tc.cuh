@@ -45,7 +45,9 @@ constexpr uint32_t TC_BLOCK_BYTES = 2 * TC_BLOCK;  // 32 KB
 constexpr uint32_t TC_ABLOCK_BYTES = 2 * TC_ABLOCK;  // 16 KB
 constexpr uint32_t TC_STAGE_BYTES = TC_ABLOCK_BYTES + TC_BLOCK_BYTES;
 constexpr int TC_NST = 4;                          // pipeline stages of (coordinate block, operator block)
-constexpr size_t TC_SMEM_BYTES = (size_t)TC_NST * TC_STAGE_BYTES + 1024 + 128;
+// dynamic shared memory of a CTA with nst stages (2 stages leave room for 2 CTAs per SM)
+__host__ __device__ constexpr size_t tc_smem_bytes(int nst) { return (size_t)nst * TC_STAGE_BYTES + 1024 + 128; }
+constexpr size_t TC_SMEM_BYTES = tc_smem_bytes(TC_NST);
 
 // element (row, kk) of a tile: kk < 32 the hi part, kk + 32 the lo part of K index kk
 __host__ __device__ __forceinline__ int tc_ci(int row, int kk) { return tc_sw128(row, kk); }
@@ -73,7 +75,7 @@ __global__ void k_pack_tc(int nk, int nrhs, int ngroups, int nmb, const float* _
 // IMAG: the anti-Hermitian pass (sums times i, added); otherwise acc = sums (stored). acc is FP32,
 // [state][position][X' (4) | Y' (4)], astride float2 per state. ysign: -1 (Y' = -D_Y, s = -r) or 0
 // (linearized form, s = 0).
-template <bool IMAG>
+template <bool IMAG, int NST = TC_NST>
 __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ tiles, int ntiles,
                                                      const uint16_t* __restrict__ B, const uint16_t* __restrict__ A,
                                                      int nmb, int nrhs, int nk, float2* __restrict__ acc,
@@ -89,13 +91,13 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
   if (t >= ntiles) return;
   const TcTile tile = tiles[t];
   const int nch = tile.g1 - tile.g0;
-  uint64_t* full = (uint64_t*)(smem + TC_NST * TC_STAGE_BYTES);
-  uint64_t* empty = full + TC_NST;
-  uint64_t* done = empty + TC_NST;
+  uint64_t* full = (uint64_t*)(smem + NST * TC_STAGE_BYTES);
+  uint64_t* empty = full + NST;
+  uint64_t* done = empty + NST;
   uint32_t* tslot = (uint32_t*)(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < TC_NST; ++s) {
+    for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -116,8 +118,8 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
         const uint64_t pol_a = policy_evict_last(), pol_b = policy_evict_first();
         int issued = 0;
         for (int i = 0; i < nch; ++i) {
-          const int s = i % TC_NST;
-          if (i >= TC_NST && !mbar_wait_bounded(&empty[s], (uint32_t)((i / TC_NST - 1) & 1), errflag)) break;
+          const int s = i % NST;
+          if (i >= NST && !mbar_wait_bounded(&empty[s], (uint32_t)((i / NST - 1) & 1), errflag)) break;
           unsigned char* st = smem + (size_t)s * TC_STAGE_BYTES;
           mbar_arrive_expect_tx(&full[s], TC_STAGE_BYTES);
           bulk_g2s(st, A + ((size_t)(tile.g0 + i) * nmb + mb) * TC_ABLOCK, TC_ABLOCK_BYTES, &full[s], pol_a);
@@ -126,8 +128,8 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
         }
         mbar_wait_bounded(done, 0, errflag);
         // no bulk copy into this CTA's shared memory outlives it (all landed unless a wait gave up)
-        for (int j = issued > TC_NST ? issued - TC_NST : 0; j < issued; ++j)
-          mbar_wait_bounded(&full[j % TC_NST], (uint32_t)((j / TC_NST) & 1), errflag);
+        for (int j = issued > NST ? issued - NST : 0; j < issued; ++j)
+          mbar_wait_bounded(&full[j % NST], (uint32_t)((j / NST) & 1), errflag);
       }
       __syncwarp();
     } else if (warp == 1) {
@@ -135,8 +137,8 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
         constexpr uint32_t idesc = tc_idesc_bf16(TC_M, 2 * TC_N);
         constexpr uint32_t SBO = 1024, LO = 64;  // bytes: 8-row atoms; hi -> lo slice of a row
         for (int i = 0; i < nch; ++i) {
-          const int s = i % TC_NST;
-          if (!mbar_wait_bounded(&full[s], (uint32_t)((i / TC_NST) & 1), errflag)) break;
+          const int s = i % NST;
+          if (!mbar_wait_bounded(&full[s], (uint32_t)((i / NST) & 1), errflag)) break;
           tc_fence_after();
           const uint32_t a0 = smem_u32(smem + (size_t)s * TC_STAGE_BYTES), b0 = a0 + TC_ABLOCK_BYTES;
 #pragma unroll

@@ -195,7 +195,8 @@ int dmd_selftest_wait_timeout(int device, uint32_t polls, int* status);
 
 /* No counterpart in the reference. Shape autotuner: times every compiled shape variant of the
  * handle's contraction (f64x, nb = 2: lines per stage, ring depth, CTAs per SM; CUDA-core batches:
- * states per warp) on `evals` right-hand-side evaluations of the current device state (CUDA events,
+ * states per warp; tensor-core batches: pipeline stages, 2 of which leave room for 2 CTAs per SM) on
+ * `evals` right-hand-side evaluations of the current device state (CUDA events,
  * after one warm-up evaluation each), keeps the fastest and returns its index in *chosen (0 when
  * the handle's form has a single shape). The state is not modified. */
 int dmd_autotune(dmd_handle* h, int evals, int* chosen);
