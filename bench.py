@@ -269,7 +269,7 @@ def run_gpu_batched(args, w):
     nb = st.cfg.nb
     R = args.nrhs
     prec = args.precision if args.precision in ("f32", "bf16x2") else "bf16x2"
-    tc = prec == "bf16x2" and nb == 2 and os.environ.get("DMD_BATCH_TC", "1") != "0"
+    tc = prec == "bf16x2" and nb in (2, 4) and os.environ.get("DMD_BATCH_TC", "1") != "0"
     g = LindbladGPU(nk=st.cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=w["e"], k1st=st.k1, k2nd=st.k2, P1=w["P1"],
                     P2=w["P2"], prefac_eph=w["prefac"], picture=0, expt=1, precision=prec, f_ref=w["f"], nrhs=R)
     h = 1.0 * U.fs
@@ -301,9 +301,10 @@ def run_gpu_batched(args, w):
     if tc:
         # per contraction (packing + Hermitian pass): operator blocks once from HBM, the r coordinates
         # in (FP32) and as bf16 hi + lo blocks out and back in, the sums out
+        nb2 = nb * nb
         nmb = (R + 127) // 128
-        ngroups = (nk + 7) // 8
-        bpl = pbytes + R * nk * 4 * 4 + 2 * ngroups * nmb * 16384 + R * nk * 8 * 16
+        ngroups = (nk + 32 // nb2 - 1) // (32 // nb2)  # column groups of 32 / nb^2 k-points
+        bpl = pbytes + R * nk * nb2 * 4 + 2 * ngroups * nmb * 16384 + R * nk * 2 * nb2 * 16
         flops = (pbytes / 32768) * nmb * 6 * 2.0 * 128 * 256 * 16  # issued MMA flops (padding included)
         kernel, bound = "tensor-core batched k-pair contraction (tcgen05, bf16 hi+lo)", "hbm"
     else:

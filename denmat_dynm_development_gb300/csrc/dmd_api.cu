@@ -257,9 +257,10 @@ cudaError_t herm_pair_attrs() {
 
 // tensor-core batched form: pack the coordinates, then the Hermitian pass and the gated
 // anti-Hermitian pass (dmd_batched_tc.cuh)
+template <int NB>
 void tc_launches(dmd_handle* h, size_t half) {
-  const size_t per = (size_t)h->nrhs * h->nk * 4;
-  k_pack_tc<<<dim3(blocks_for((long long)per, 256), 2), 256, 0, h->st>>>(h->nk, h->nrhs, h->ngroups, h->nmb,
+  const size_t per = (size_t)h->nrhs * h->nk * NB * NB;
+  k_pack_tc<NB><<<dim3(blocks_for((long long)per, 256), 2), 256, 0, h->st>>>(h->nk, h->nrhs, h->ngroups, h->nmb,
                                                                          (const float*)h->d_rs, h->d_tcA, h->d_hflag);
   const size_t apart = (size_t)h->ngroups * h->nmb * TC_ABLOCK;
   const size_t astride = (size_t)h->nk * 2 * h->nb2;
@@ -273,9 +274,9 @@ void tc_launches(dmd_handle* h, size_t half) {
                                    astride, ysign, h->d_hflag, h->d_err);
   };
   // pipeline depth (the shape the autotuner chooses): 4, 3 or 2 stages of 48 KB
-  if (h->tcst == 3) pass(k_pairs_tc<false, 3>, k_pairs_tc<true, 3>, tc_smem_bytes(3));
-  else if (h->tcst == 2) pass(k_pairs_tc<false, 2>, k_pairs_tc<true, 2>, tc_smem_bytes(2));
-  else pass(k_pairs_tc<false, 4>, k_pairs_tc<true, 4>, tc_smem_bytes(4));
+  if (h->tcst == 3) pass(k_pairs_tc<false, 3, NB>, k_pairs_tc<true, 3, NB>, tc_smem_bytes(3));
+  else if (h->tcst == 2) pass(k_pairs_tc<false, 2, NB>, k_pairs_tc<true, 2, NB>, tc_smem_bytes(2));
+  else pass(k_pairs_tc<false, 4, NB>, k_pairs_tc<true, 4, NB>, tc_smem_bytes(4));
   (void)half;
   h->launches += 1;  // the packing launch; the two passes are counted with the other forms
 }
@@ -293,7 +294,7 @@ int launch_pairs(dmd_handle* h) {
       // not exactly Hermitian and returns at once unless the prep kernel raised d_hflag
       const size_t half = (size_t)h->nk * 2 * h->nb2 * h->nrhs;  // coordinates per part
       if (h->use_tc) {
-        tc_launches(h, half);
+        tc_launches<NB>(h, half);
       } else if (h->nrhs > 1) {  // batched form: reduced-precision arithmetics only (dmd_create)
         const float* rs = (const float*)h->d_rs;
         if (h->prec == DMD_PREC_BF16X2) herm_pair_launches<ArithBF2, NB, 4, 2, 2, 4>(h, rs, half);
@@ -331,7 +332,7 @@ template <int NB>
 int launch_finish(dmd_handle* h, FinishArgs a) {
   ProfScope ps(h, 2);
   const dim3 g(blocks_for(h->nk, 128), h->nrhs);
-  if constexpr (NB == 2) {
+  if constexpr (NB == 2 || NB == 4) {
     if (h->use_tc) {  // split FP64 / FP32 finish of the tensor-core form
       if (h->nbdm == NB) k_finish<NB, NB, true><<<g, 128, 0, h->st>>>(a);
       else k_finish<NB, 0, true><<<g, 128, 0, h->st>>>(a);
@@ -852,6 +853,21 @@ void pair_operators(const dmd_handle* h, const dmd_desc* d, size_t src, cd* P1, 
 // (k2 <- k1): A = conj(Q2), B = conj(Q1). They are bucketed by the row tile of their target
 // (16 energy ranks); a tile's column groups (8 ranks) between the first and the last it touches form
 // dense blocks laid out as the MMA reads them, split into bf16 hi + lo. Tiles are built on host threads.
+template <int NB>
+cudaError_t tc_attrs() {
+  cudaError_t e = cudaSuccess;
+  auto set = [&](auto k, int nst) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(nst));
+  };
+  set(k_pairs_tc<false, 4, NB>, 4);
+  set(k_pairs_tc<true, 4, NB>, 4);
+  set(k_pairs_tc<false, 3, NB>, 3);
+  set(k_pairs_tc<true, 3, NB>, 3);
+  set(k_pairs_tc<false, 2, NB>, 2);
+  set(k_pairs_tc<true, 2, NB>, 2);
+  return e;
+}
+
 int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
   const int nb = h->nb, nk = h->nk;
   std::vector<double> ew((size_t)nk * nb);
@@ -863,14 +879,13 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
   L.rb.clear();
   L.items.clear();
   L.src.clear();
-  CK(cudaFuncSetAttribute(k_pairs_tc<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(4)));
-  CK(cudaFuncSetAttribute(k_pairs_tc<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(4)));
-  CK(cudaFuncSetAttribute(k_pairs_tc<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(3)));
-  CK(cudaFuncSetAttribute(k_pairs_tc<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(3)));
-  CK(cudaFuncSetAttribute(k_pairs_tc<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(2)));
-  CK(cudaFuncSetAttribute(k_pairs_tc<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes(2)));
-  h->ntiles = (nk + TC_TR - 1) / TC_TR;
-  h->ngroups = (nk + TC_CG - 1) / TC_CG;
+  if (nb == 4) CK(tc_attrs<4>());
+  else CK(tc_attrs<2>());
+  // rows per tile and columns per group: a block is 128 X rows (TR rows x nb^2 x re|im) by K = 32
+  // (CG columns x nb^2)
+  const int TR = tc_tr(h->nb2), CG = tc_cg(h->nb2);
+  h->ntiles = (nk + TR - 1) / TR;
+  h->ngroups = (nk + CG - 1) / CG;
   h->nmb = (h->nrhs + TC_M - 1) / TC_M;
   int rc;
   if ((rc = dalloc(h, &h->d_pos, (size_t)nk)) || (rc = dalloc(h, &h->d_inv, (size_t)nk))) return rc;
@@ -882,16 +897,16 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
   auto row_of = [&](size_t src, int dir) { return L.pos[dir ? d->k2nd[src] : d->k1st[src]]; };
   auto col_of = [&](size_t src, int dir) { return L.pos[dir ? d->k1st[src] : d->k2nd[src]]; };
   for (size_t p = 0; p < np; ++p) {
-    start[row_of(p, 0) / TC_TR + 1]++;
-    if (d->k1st[p] < d->k2nd[p]) start[row_of(p, 1) / TC_TR + 1]++;
+    start[row_of(p, 0) / TR + 1]++;
+    if (d->k1st[p] < d->k2nd[p]) start[row_of(p, 1) / TR + 1]++;
   }
   for (int t = 0; t < h->ntiles; ++t) start[t + 1] += start[t];
   std::vector<uint64_t> ent(start[h->ntiles]);
   {
     std::vector<size_t> fill(start.begin(), start.end() - 1);
     for (size_t p = 0; p < np; ++p) {
-      ent[fill[row_of(p, 0) / TC_TR]++] = (uint64_t)p << 1;
-      if (d->k1st[p] < d->k2nd[p]) ent[fill[row_of(p, 1) / TC_TR]++] = ((uint64_t)p << 1) | 1u;
+      ent[fill[row_of(p, 0) / TR]++] = (uint64_t)p << 1;
+      if (d->k1st[p] < d->k2nd[p]) ent[fill[row_of(p, 1) / TR]++] = ((uint64_t)p << 1) | 1u;
     }
   }
   std::vector<TcTile> tiles(h->ntiles);
@@ -899,7 +914,7 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
   for (int t = 0; t < h->ntiles; ++t) {
     int gmin = INT32_MAX, gmax = -1;
     for (size_t e = start[t]; e < start[t + 1]; ++e) {
-      const int g = col_of(ent[e] >> 1, (int)(ent[e] & 1)) / TC_CG;
+      const int g = col_of(ent[e] >> 1, (int)(ent[e] & 1)) / CG;
       gmin = std::min(gmin, g);
       gmax = std::max(gmax, g);
     }
@@ -950,7 +965,7 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
     std::atomic<int> next(t0);
     auto work = [&]() {
       std::vector<double> f64;
-      cd P1[16], P2[16], Q1[16], Q2[16], A[16], Bm[16];
+      cd P1[256], P2[256], Q1[256], Q2[256], A[256], Bm[256];
       for (int t; (t = next.fetch_add(1)) < t1;) {
         const TcTile& tl = tiles[t];
         const int nblk = tl.g1 - tl.g0;
@@ -961,12 +976,12 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
           const int dir = (int)(ent[e] & 1);
           pair_operators(h, d, src, P1, P2);
           herm_transform(nb, P1, P2, Q1, Q2);
-          for (int i = 0; i < 16; ++i) {
+          for (int i = 0; i < n2 * n2; ++i) {
             A[i] = dir ? cd{Q2[i].re, -Q2[i].im} : Q1[i];
             Bm[i] = dir ? cd{Q1[i].re, -Q1[i].im} : Q2[i];
           }
           const int rp = row_of(src, dir), cp = col_of(src, dir);
-          const int r = rp - t * TC_TR, blk = cp / TC_CG - tl.g0, c = cp % TC_CG;
+          const int r = rp - t * TR, blk = cp / CG - tl.g0, c = cp % CG;
           double* fx = &f64[(size_t)blk * 2 * TC_N * TC_K];
           double* fy = fx + TC_N * TC_K;
           for (int a = 0; a < n2; ++a)
@@ -1021,7 +1036,7 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
     CK(cudaMemcpy(h->d_fref, fw.data(), fw.size() * 8, cudaMemcpyHostToDevice));
   }
   if (out == DMD_OK && dev) {
-    // the split finish (k_finish<2, ., true>): X0, Y0 back-transformed by k and the constant
+    // the split finish (k_finish<nb, ., true>): X0, Y0 back-transformed by k and the constant
     // V0 = (prefac/2)(C0 + C0^dagger), C0 = (1 - F) X0 - Y0 F (Hermitian reads of diagonal F)
     const int n2 = h->nb2;
     std::vector<float2> x0y0((size_t)nk * 2 * n2);
@@ -1029,7 +1044,7 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
     const double pf = 0.5 * h->prefac;
     for (int k = 0; k < nk; ++k) {
       const cd* a = &acc0[(size_t)L.pos[k] * 2 * n2];
-      cd X[16], Y[16];
+      cd X[16], Y[16];  // nb^2 <= 16
       for (int e = 0; e < n2; ++e) {
         X[e] = a[e];
         Y[e] = a[n2 + e];
@@ -1284,7 +1299,7 @@ static int create_impl(const dmd_desc* d, dmd_handle** out, PairSource* src) {
   // CUDA-core column-block form)
   {
     const char* v = getenv("DMD_BATCH_TC");
-    h->use_tc = (nrhs > 1 && h->nb == 2 && h->npair > 0 && h->prec == DMD_PREC_BF16X2 && !(v && atoi(v) == 0)) ? 1 : 0;
+    h->use_tc = (nrhs > 1 && (h->nb == 2 || h->nb == 4) && h->npair > 0 && h->prec == DMD_PREC_BF16X2 && !(v && atoi(v) == 0)) ? 1 : 0;
   }
   int rc = DMD_OK;
   auto bail = [&](int code) {

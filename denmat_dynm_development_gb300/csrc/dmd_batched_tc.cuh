@@ -1,4 +1,4 @@
-// Batched form of the k-pair contraction on the tensor cores (tcgen05), nb = 2.
+// Batched form of the k-pair contraction on the tensor cores (tcgen05), nb = 2 and nb = 4.
 //
 // With many states sharing P the contraction is a GEMM. Every stored pair (k1, k2) is kept twice, as
 // directed operators (row <- column): (k1 <- k2) with A = Q1, B = Q2 and, when the pair carries the
@@ -7,12 +7,12 @@
 //   X'_k[a] = sum_c sum_j A_kc[a][j] r_c[j],      Y'_k[j] = sum_c sum_a B_kc[a][j] s_c[a]
 // and no reverse sums remain. The batched form runs in the deviation form, where s = -r (or s = 0 in
 // the linearized form), so both sums contract the same coordinates: Y'_k[j] = -sum B_kc[a][j] r_c[a].
-// Rows (energy-rank positions) are grouped in tiles of TR = 16, columns in groups of CG = 8; a tile's
-// operators over one column group form a dense block (zeros where a row and a column have no pair;
-// rows of an energy window pair with nearly the same columns, so the blocks are nearly full). For a
-// tile and up to 128 states one CTA computes
+// Rows (energy-rank positions) are grouped in tiles of TR = 64 / nb^2 (16 for nb = 2, 4 for nb = 4),
+// columns in groups of CG = 32 / nb^2 (8, 2); a tile's operators over one column group form a dense
+// block (zeros where a row and a column have no pair; rows of an energy window pair with nearly the
+// same columns, so the blocks are nearly full). For a tile and up to 128 states one CTA computes
 //   D[q][n] = sum_(c, j) R[q][(c, j)] * B[(c, j)][n],  n < 128: (r, a, re|im) of X', n >= 128: (r, j, re|im) of -Y'
-// (M = 128 states, N = 256, K = 8 columns x 4 = 32 per group) as tcgen05 MMAs accumulating in tensor
+// (M = 128 states, N = 256, K = CG columns x nb^2 = 32 per group) as tcgen05 MMAs accumulating in tensor
 // memory over all of the tile's column groups, then writes each row's sums once (FP32, as the
 // tensor memory holds them): no atomics.
 // Operands are bf16 hi + lo splits (x = hi + lo, 16 significant bits); the product keeps
@@ -37,7 +37,10 @@ struct TcTile {
   int64_t boff;    // index of the tile's first operator block
 };
 
-constexpr int TC_TR = 16, TC_CG = 8, TC_K = 32, TC_N = 128, TC_M = 128;
+constexpr int TC_K = 32, TC_N = 128, TC_M = 128;
+// rows per tile and columns per group for nb2 = nb^2 coordinates per k-point
+__host__ __device__ constexpr int tc_tr(int nb2) { return 64 / nb2; }
+__host__ __device__ constexpr int tc_cg(int nb2) { return 32 / nb2; }
 constexpr int TC_PLANE = 8192;                     // bf16 per 128-row tile (128 rows x [hi 32 | lo 32])
 constexpr int TC_BLOCK = 2 * TC_PLANE;             // bf16 per operator block: X rows, then Y rows (256)
 constexpr int TC_ABLOCK = TC_PLANE;                // bf16 per coordinate block: R (128 states)
@@ -55,27 +58,29 @@ __host__ __device__ __forceinline__ int tc_ci(int row, int kk) { return tc_sw128
 // r coordinates (FP32, [part][q][pos][2 NB2] as written by k_prep_herm, the first NB2 of each 2 NB2)
 // -> coordinate blocks [part][group][mblock][128 x (hi 32 | lo 32)]; entries of padding states stay
 // zero. Part 1 (anti-Hermitian) is packed only when *gate is set.
+template <int NB>
 __global__ void k_pack_tc(int nk, int nrhs, int ngroups, int nmb, const float* __restrict__ rs,
                           uint16_t* __restrict__ A, const unsigned int* __restrict__ gate) {
+  constexpr int NB2 = NB * NB, CG = tc_cg(NB2);
   const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const int part = blockIdx.y;
   if (part == 1 && *gate == 0u) return;
-  const size_t per = (size_t)nrhs * nk * 4;
+  const size_t per = (size_t)nrhs * nk * NB2;
   if (idx >= per) return;
-  const int e = (int)(idx % 4), p = (int)((idx / 4) % nk), q = (int)(idx / ((size_t)4 * nk));
-  const float v = rs[(size_t)part * 2 * per + ((size_t)q * nk + p) * 8 + e];
+  const int e = (int)(idx % NB2), p = (int)((idx / NB2) % nk), q = (int)(idx / ((size_t)NB2 * nk));
+  const float v = rs[(size_t)part * 2 * per + ((size_t)q * nk + p) * 2 * NB2 + e];
   const __nv_bfloat16 hi = __float2bfloat16_rn(v);
   const __nv_bfloat16 lo = __float2bfloat16_rn(__fsub_rn(v, __bfloat162float(hi)));
-  const int g = p / TC_CG, kk = (p % TC_CG) * 4 + e, mb = q / TC_M, m = q % TC_M;
+  const int g = p / CG, kk = (p % CG) * NB2 + e, mb = q / TC_M, m = q % TC_M;
   uint16_t* blk = A + (((size_t)part * ngroups + g) * nmb + mb) * TC_ABLOCK;
   blk[tc_ci(m, kk)] = __bfloat16_as_ushort(hi);
   blk[tc_ci(m, kk + 32)] = __bfloat16_as_ushort(lo);
 }
 
 // IMAG: the anti-Hermitian pass (sums times i, added); otherwise acc = sums (stored). acc is FP32,
-// [state][position][X' (4) | Y' (4)], astride float2 per state. ysign: -1 (Y' = -D_Y, s = -r) or 0
+// [state][position][X' (NB2) | Y' (NB2)], astride float2 per state. ysign: -1 (Y' = -D_Y, s = -r) or 0
 // (linearized form, s = 0).
-template <bool IMAG, int NST = TC_NST>
+template <bool IMAG, int NST = TC_NST, int NB = 2>
 __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ tiles, int ntiles,
                                                      const uint16_t* __restrict__ B, const uint16_t* __restrict__ A,
                                                      int nmb, int nrhs, int nk, float2* __restrict__ acc,
@@ -159,9 +164,11 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
     mbar_wait_bounded(done, 0, errflag);
   }
   tc_fence_after();
-  // epilogue: TMEM lane 32 w + l holds state q = 128 mb + 32 w + l. Per group of 4 rows a thread
-  // writes its state's 4 x 8 sums into shared memory (a row of 33 float2 per state), then the warp
-  // stores each state's 256 contiguous bytes with one coalesced instruction.
+  // epilogue: TMEM lane 32 w + l holds state q = 128 mb + 32 w + l. 32 TMEM columns hold RPC rows of
+  // the tile (4 for nb = 2, 1 for nb = 4) x NB2 elements x (re, im); per such chunk a thread writes its
+  // state's RPC x 2 NB2 sums into shared memory (a row of 33 float2 per state), then the warp stores
+  // each state's 256 contiguous bytes with one coalesced instruction.
+  constexpr int NB2 = NB * NB, RPC = 16 / NB2, TR = tc_tr(NB2);
   float2* wsm = (float2*)smem + (size_t)warp * 32 * 33;
   const int qb = mb * TC_M + warp * 32;
   const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
@@ -176,19 +183,20 @@ __global__ void __launch_bounds__(128, 1) k_pairs_tc(const TcTile* __restrict__ 
     }
     float2* my = wsm + lane * 33;
 #pragma unroll
-    for (int rr = 0; rr < 4; ++rr)
+    for (int rr = 0; rr < RPC; ++rr)
 #pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        my[rr * 8 + a] = make_float2(vx[rr * 8 + 2 * a], vx[rr * 8 + 2 * a + 1]);
-        my[rr * 8 + 4 + a] = make_float2(ysign * vy[rr * 8 + 2 * a], ysign * vy[rr * 8 + 2 * a + 1]);
+      for (int a = 0; a < NB2; ++a) {
+        my[rr * 2 * NB2 + a] = make_float2(vx[rr * 2 * NB2 + 2 * a], vx[rr * 2 * NB2 + 2 * a + 1]);
+        my[rr * 2 * NB2 + NB2 + a] =
+            make_float2(ysign * vy[rr * 2 * NB2 + 2 * a], ysign * vy[rr * 2 * NB2 + 2 * a + 1]);
       }
     __syncwarp();
-    // lane l covers row p0 + l / 8, element l % 8 of every state of the warp
-    const int p = t * TC_TR + rq * 4 + (lane >> 3);
+    // lane l covers row p0 + l / (2 NB2), element l % (2 NB2) of every state of the warp
+    const int p = t * TR + rq * RPC + lane / (2 * NB2);
     if (p < nk) {
       for (int j = 0; j < 32 && qb + j < nrhs; ++j) {
         const float2 v = wsm[j * 33 + lane];
-        float2* dst = acc + (size_t)(qb + j) * astride + (size_t)p * 8 + (lane & 7);
+        float2* dst = acc + (size_t)(qb + j) * astride + (size_t)p * 2 * NB2 + lane % (2 * NB2);
         if (IMAG) {
           const float2 o = *dst;
           *dst = make_float2(o.x - v.y, o.y + v.x);

@@ -344,14 +344,15 @@ def _herm_states(s, n, seed, scale=1e-3):
 
 
 def _tensor_core_form(s, prec):
-    """the batched form runs on the tensor cores for nb = 2 with bf16 hi + lo storage"""
-    return prec == "bf16x2" and s.bend - s.bstart == 2 and os.environ.get("DMD_BATCH_TC", "1") != "0"
+    """the batched form runs on the tensor cores for nb = 2 and nb = 4 with bf16 hi + lo storage"""
+    return prec == "bf16x2" and s.bend - s.bstart in (2, 4) and os.environ.get("DMD_BATCH_TC", "1") != "0"
 
 
 @pytest.mark.parametrize("prec", ["f32", "bf16x2"])
-@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb4_eimp_B", "nb2_linear", "nb2_carrier_eq", "nb2_window"])
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb4_eimp_B", "nb2_linear", "nb4_linear", "nb2_carrier_eq",
+                                  "nb2_window"])
 def test_batched_states_vs_oracle(case, prec, oracle, built):
-    """Batched form: 7 states share P (nb = 2 with bf16 hi + lo: the tensor-core contraction; else
+    """Batched form: 7 states share P (bf16 hi + lo: the tensor-core contraction; else
     RW states per warp on the CUDA cores, the last group short). Every state's RHS matches the oracle
     at the reduced-precision tolerance; 20 RK4 steps of the batch change every state as 20 oracle
     steps do, to that tolerance; the CUDA-core batch also matches each state stepped alone."""
@@ -423,6 +424,42 @@ def test_batched_tensor_core_many_states(oracle, built, tmp_path, monkeypatch):
             out = gb.func(t, np.concatenate(batch)).reshape(3, -1)
             for q in range(3):
                 assert rel(out[q], oracle.rhs(s, t, batch[q])) < TC_TOL, q
+
+
+def test_batched_tensor_core_nb4_many_states(oracle, built, tmp_path, monkeypatch):
+    """Tensor-core batched form for nb = 4 (tiles of 4 rows, column groups of 2) on a random case
+    (nk = 240, spin-split pairs of bands) with 129 states: every checked state matches the oracle and
+    the whole batch matches the CUDA-core batched form (DMD_BATCH_TC=0); 10 RK4 steps of the batch
+    change the states as the oracle's steps do."""
+    from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, make_ldbd
+    cfg = SynthConfig(nk=240, nb=4, seed=8, eimp_sigma_mev=5.0)
+    make_ldbd(str(tmp_path), cfg, B_T=(0.0, 0.0, 0.5), eimp_fraction=1e-2)
+    s = oracle.load(str(tmp_path))
+    R = 129
+    ys = _herm_states(s, R, 21)
+    t = 7.0 * oracle.fs
+    with make_gpu_lowp(s, "bf16x2", nrhs=R) as gb:
+        out_tc = gb.func(t, np.concatenate(ys)).reshape(R, -1)
+        h = 2.0 * oracle.fs
+        gb.set_state(s.t0, np.concatenate(ys))
+        gb.rk4(h, 10)
+        _, yb = gb.get_state()
+        yb = yb.reshape(R, -1)
+    monkeypatch.setenv("DMD_BATCH_TC", "0")
+    with make_gpu_lowp(s, "bf16x2", nrhs=R) as gc:
+        out_cc = gc.func(t, np.concatenate(ys)).reshape(R, -1)
+    monkeypatch.delenv("DMD_BATCH_TC")
+    for q in (0, 77, 127, 128):
+        e = rel(out_tc[q], oracle.rhs(s, t, ys[q]))
+        print("nb4 nk240 state %d: tensor-core rel err %.3g" % (q, e))
+        assert e < TC_TOL
+    for q in range(R):
+        assert rel(out_tc[q], out_cc[q]) < TC_TOL + LOWP_TOL["bf16x2"], q
+    for q in (0, 128):
+        yo, _ = oracle.rk4(s, s.t0, h, 10, ys[q])
+        e = rel(yb[q] - ys[q], yo - ys[q])
+        print("nb4 nk240 state %d: 10-step change rel err %.3g" % (q, e))
+        assert e < 3 * TC_TOL
 
 
 def test_batched_tensor_core_irregular_pairs(oracle, built):
