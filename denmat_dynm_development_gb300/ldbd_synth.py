@@ -9,6 +9,10 @@ fed to the reference program and to this package:
 * ``ldbd_R.dat`` -- dimension + lattice vectors (lattice.h:48-56).
 * ``ldbd_kvec.bin`` double[nk][3], ``ldbd_ek.bin`` double[nk][nb], ``ldbd_smat.bin``
   complex128[nk][3][nb*nb] (electron.cpp:134-314).
+* optionally ``ldbd_Umat.bin`` complex128[nk][nb_wannier][nb_eph] (electron.cpp:388-410): the
+  e-ph window's columns of the Wannier rotations, whose overlaps U_k^dag U_k' enter the e-e model
+  (ElecElec_Model.h:72-79). The reader's full-matrix branch depends on a size check that returns
+  no value when the sizes match (comm/myio.cpp:133-137), so only this partial layout loads reliably.
 * ``ldbd_kpair_k1st.bin`` / ``ldbd_kpair_k2nd.bin`` uint64[npair] with k1st <= k2nd
   (ElectronPhonon.cpp:182-204).
 * ``ldbd_P1_lindblad.bin`` / ``ldbd_P2_lindblad.bin`` complex128[npair][nb^4], row-major
@@ -64,6 +68,8 @@ class SynthConfig:
     ecbm_ha: float = 0.05            # absolute energy of the band bottom (Ha)
     extra_bands: int = 0             # bands of the density matrix below the e-ph window
     nv: int = 0                      # lowest bands declared valence in ldbd_size.dat (holes)
+    nwannier: Optional[int] = None   # write ldbd_Umat.bin with this many Wannier functions (>= nb_dm)
+    kball: bool = False              # keep the nk lowest-energy grid points (a ball: k1 + k3 - k2 mostly inside)
     chunk_pairs: int = 1 << 18
 
     def to_dict(self):
@@ -110,7 +116,10 @@ def _kset(cfg: SynthConfig, rng):
         if keep.size >= int(1.2 * cfg.nk) + 1:
             break
         n += 1
-    sel = np.sort(rng.choice(keep, size=cfg.nk, replace=False))
+    if cfg.kball:
+        sel = np.sort(keep[np.argsort(e[keep], kind="stable")[:cfg.nk]])
+    else:
+        sel = np.sort(rng.choice(keep, size=cfg.nk, replace=False))
     rng.shuffle(sel)                       # a random k order, as a k-point selection would give
     return R, V, n, kf[sel], e[sel]
 
@@ -236,6 +245,23 @@ def eimp_chunk(cfg: SynthConfig, ek, ekp, chunk_index):
     g = _cgauss(rng, (n, nb, nb), gsig)
     A = np.where(np.abs(dE) < ethr, sq_delta * g * np.exp(-dE * dE / (4.0 * sigma * sigma)), 0)[:, None]
     return _sum_outer(A, False), _sum_outer(A, True)
+
+
+def umat(cfg: SynthConfig, kf):
+    """Wannier rotations U_k = exp(i (H0 + sum_d k_d A_d)), [nk][nbw][nbw] unitary and smooth in the
+    fractional k (H0, A_d fixed random Hermitian), so that overlaps of nearby k are near identity."""
+    nbw = cfg.nwannier
+    rng = np.random.default_rng([cfg.seed, 4])
+
+    def herm():
+        a = rng.standard_normal((nbw, nbw)) + 1j * rng.standard_normal((nbw, nbw))
+        return 0.5 * (a + a.conj().T) / math.sqrt(2.0 * nbw)
+
+    H0 = herm()
+    A = np.stack([herm() for _ in range(3)])
+    h = H0[None] + 4.0 * np.einsum("kd,dij->kij", kf, A)
+    w, v = np.linalg.eigh(h)
+    return np.einsum("kij,kj,klj->kil", v, np.exp(1j * w), np.conj(v))
 
 
 def mode_energies(cfg: SynthConfig):
@@ -418,11 +444,14 @@ def make_ldbd(outdir: str, cfg: SynthConfig, write_param: bool = True, threads: 
     st = setup(cfg)
     e, R, n, nb, nx = st.e, st.R, st.n, cfg.nb, cfg.extra_bands
     ndm = nb + nx
+    nbw = cfg.nwannier or ndm
+    if nbw < ndm:
+        raise ValueError("nwannier must be >= the density-matrix bands")
     mu, T = st.mu, st.T
     with open(os.path.join(d, "ldbd_size.dat"), "w") as f:
         f.write("There are scatterings only for conduction electrons\n")
         f.write("%d %d 0 %d %d %d %d 0 0 # nb nv bBot_dm bTop_dm bBot_eph_elec bTop_eph_elec nb_wannier bBot_probe band_dft_skipped\n"
-                % (ndm, cfg.nv, ndm, nx, ndm, ndm))
+                % (ndm, cfg.nv, ndm, nx, ndm, nbw))
         f.write("%21.14le %d %d %d %d # nk_full nk kmesh\n" % (float(n) ** 3, cfg.nk, n, n, n))
         f.write("%d # nkpair_elec\n" % st.npair)
         f.write("0 %d 0 0# modeStart modeStp modeSkipStart modeSkipStop\n" % cfg.nmodes)
@@ -437,6 +466,9 @@ def make_ldbd(outdir: str, cfg: SynthConfig, write_param: bool = True, threads: 
         for i in range(3):
             f.write("%.17g %.17g %.17g\n" % tuple(R[i]))
     st.kf.astype(np.float64).tofile(os.path.join(d, "ldbd_kvec.bin"))
+    if cfg.nwannier:
+        U = umat(cfg, st.kf)[:, :, nx:nx + nb]
+        np.ascontiguousarray(U, np.complex128).tofile(os.path.join(d, "ldbd_Umat.bin"))
     e.astype(np.float64).tofile(os.path.join(d, "ldbd_ek.bin"))
     st.s.astype(np.complex128).tofile(os.path.join(d, "ldbd_smat.bin"))
     st.k1.tofile(os.path.join(d, "ldbd_kpair_k1st.bin"))

@@ -51,7 +51,35 @@ typedef struct {
   int scatt_enable;    /* alg.scatt_enable */
   int linear;          /* alg.linearize: P1, P2 hold Lscij, Lscji (ElectronPhonon_linear.cpp) */
   const double* f_lin; /* [nk][nb] window f_eq of the linearization */
+  struct orc_ee* ee;   /* e-e model rebuilt from rho on every RHS (eeMode Pee_update, freq < 0), or NULL */
 } orc_sys;
+
+/* e-e scattering model (ElecElec_Model.h) with static screening (Coulomb_Model.h:394-688):
+ * what electronphonon holds for eeMode = Pee_update. P1, P2 of the system point at P1eff, P2eff. */
+typedef struct orc_ee {
+  int nb, nbw;             /* window bands; Wannier functions (elec->nb_wannier) */
+  const double* kvec;      /* [nk][3] fractional (electron.cpp:134-146) */
+  int kmesh[3];
+  const zc* U;             /* [nk][nbw][nb] (electron.cpp:388-410) */
+  double GGT[9];           /* lattice.h:41-42 */
+  double cell_size, nk_full, T, eps, meff;
+  int formula;             /* 0 unscreened, 1 debye, 2 Bechstedt (clp.scrFormula) */
+  double nfree;            /* clp.nfreetot: the screening density */
+  int update_screening;    /* clp.update: nfree from rho at each rebuild (Coulomb_Model.h:533-553) */
+  int nv;                  /* coul_model->nv: window bands below it count holes */
+  double degauss, ethr;    /* eep.degauss; param->degauss * ndegauss */
+  int antisym;             /* eep.antisymmetry */
+  double scale;            /* scale_ee */
+  int inside;              /* rebuild before every RHS evaluation */
+  const zc* P1base;        /* [npair][nb^4]: P_eph (+ P_eimp) */
+  const zc* P2base;
+  zc* P1eff;               /* P_base + scale P_ee: the operators the RHS uses */
+  zc* P2eff;
+  zc* P1ee;                /* the last P_ee (prefactor included, scale not) */
+  zc* P2ee;
+} orc_ee;
+
+void orc_ee_rebuild(struct orc_ee* ee, const orc_sys* s, double t, const double* y);
 
 /* workspace for one RHS evaluation */
 typedef struct {
@@ -346,6 +374,255 @@ void orc_evolve_coh(const orc_sys* s, orc_ws* w, double t, const zc* dm, zc* out
   free(Hbuf);
 }
 
+/* ---------------------------------------------------------------------------------------------
+ * e-e model (eeMode = Pee_update)
+ * ------------------------------------------------------------------------------------------- */
+
+/* wrap to [-0.5, 0.5) -- comm/kmap.h:6-15 */
+static void ee_wrap(const double* x, double* r) {
+  for (int d = 0; d < 3; d++) {
+    r[d] = x[d];
+    r[d] -= floor(0.5 + r[d]);
+    if (fabs(r[d] - 0.5) < 1e-6) r[d] = -0.5;
+  }
+}
+
+/* GGT.metric_length_squared(wrap(q)) -- comm/matrix3.h:119-121 */
+static double ee_q2(const orc_ee* ee, const double* q) {
+  double v[3];
+  ee_wrap(q, v);
+  const double* m = ee->GGT;
+  return v[0] * v[0] * m[0] + v[1] * v[1] * m[4] + v[2] * v[2] * m[8] +
+         2 * (v[0] * v[1] * m[1] + v[0] * v[2] * m[2] + v[1] * v[2] * m[5]);
+}
+
+/* screening constants of coulomb_model::init_model (Coulomb_Model.h:555-569) for density n */
+typedef struct { double prefac_vq, prefac_vq_bare, qscr2_debye, fac0, fac2, fac4; } ee_scr;
+
+static ee_scr ee_screen(const orc_ee* ee, double n) {
+  ee_scr c;
+  c.prefac_vq = 4 * M_PI / ee->eps / ee->cell_size;  /* Coulomb_Model.h:423-424 */
+  c.prefac_vq_bare = 4 * M_PI / ee->cell_size;
+  const double kF = pow(3 * M_PI * M_PI * n, 1. / 3.);
+  const double kF2 = kF * kF;
+  const double EF = kF2 / 2. / ee->meff;
+  const double qTF2 = 6 * M_PI * n / ee->eps / EF;
+  c.fac0 = 1. / (ee->eps - 1);
+  c.fac2 = 1. / qTF2;
+  c.fac4 = 3. / 4. / kF2 / qTF2;
+  c.qscr2_debye = 4 * M_PI * n / ee->eps / ee->T;
+  return c;
+}
+
+/* coulomb_model::vq, static branches (Coulomb_Model.h:632-660) */
+static double ee_vq(const orc_ee* ee, const ee_scr* c, const double* q) {
+  const double q2 = ee_q2(ee, q);
+  if (ee->formula == 0) return q2 < 1e-20 ? 0.0 : c->prefac_vq / q2;
+  if (ee->formula == 1) return c->prefac_vq / (c->qscr2_debye + q2);
+  if (q2 < 1e-20) return 0.0;
+  const double epsq = 1 + 1. / (c->fac0 + c->fac2 * q2 + c->fac4 * q2 * q2);
+  return c->prefac_vq_bare / epsq / q2;
+}
+
+/* kIndexMap::ikvec3 -- comm/kmap.cpp:15-23 */
+static void ee_ikvec3(const orc_ee* ee, const double* k, int* v) {
+  for (int d = 0; d < 3; d++) {
+    const double ki = k[d] - floor(k[d]);
+    v[d] = (int)round(ee->kmesh[d] * ki);
+    if (v[d] == ee->kmesh[d]) v[d] = 0;
+  }
+}
+
+/* kIndexMap::findk (comm/kmap.cpp:3-10) over the k-points' mesh indices */
+static int ee_findk(const orc_ee* ee, int nk, const int* kidx, const double* k) {
+  int v[3];
+  ee_ikvec3(ee, k, v);
+  for (int i = 0; i < nk; i++)
+    if (kidx[3 * i] == v[0] && kidx[3 * i + 1] == v[1] && kidx[3 * i + 2] == v[2]) return i;
+  return -1;
+}
+
+/* elecelec_model::calc_ovlp -- ElecElec_Model.h:72-80: ovlp = U_ik^dagger U_jk (nb x nb), times
+ * vq(k_ik - k_jk) when asked */
+static void ee_ovlp(const orc_ee* ee, const ee_scr* c, zc* ovlp, zc* Uih, int ik, int jk, int with_vq) {
+  const int nb = ee->nb, nbw = ee->nbw;
+  const zc* Ui = ee->U + (size_t)ik * nbw * nb;
+  for (int i = 0; i < nb; i++) /* hermite(a, h, m = nbw, n = nb): h[i*m + j] = conj(a[j*n + i]) */
+    for (int j = 0; j < nbw; j++) Uih[i * nbw + j] = zconj(Ui[j * nb + i]);
+  zgemm_mnk(ovlp, Uih, ee->U + (size_t)jk * nbw * nb, nb, nb, nbw, zmk(1, 0), zmk(0, 0));
+  if (!with_vq) return;
+  double q[3];
+  for (int d = 0; d < 3; d++) q[d] = ee->kvec[3 * ik + d] - ee->kvec[3 * jk + d];
+  const zc vq = zmk(ee_vq(ee, c, q), 0);
+  for (int i = 0; i < nb * nb; i++) ovlp[i] = zmul(vq, ovlp[i]); /* axbyc(ovlp, nullptr, n, c0, vq) */
+}
+
+/* elecelec_model::calc_P for every stored pair (ElecElec_Model.h:186-262, static screening,
+ * Lindblad, not linearized). dm, dm1: window [nk][nb^2] in the Schrodinger picture, or NULL for the
+ * equilibrium occupations f ([nk][nb] window). Out: P1ee, P2ee [npair][nb^4] (prefactor included). */
+void orc_ee_P(const orc_ee* ee, const orc_sys* s, const zc* dm, const zc* dm1, const double* f, double nfree,
+              zc* P1out, zc* P2out) {
+  const int nk = s->nk, nb = ee->nb, nb2 = nb * nb, nb4 = nb2 * nb2, nd = s->nb_dm, bs = s->bstart;
+  const ee_scr c = ee_screen(ee, nfree);
+  double* e = (double*)xmalloc(sizeof(double) * nk * nb);
+  for (int ik = 0; ik < nk; ik++)
+    for (int b = 0; b < nb; b++) e[ik * nb + b] = s->e_dm[(size_t)ik * nd + bs + b];
+  int* kidx = (int*)xmalloc(sizeof(int) * 3 * nk);
+  for (int ik = 0; ik < nk; ik++) ee_ikvec3(ee, ee->kvec + 3 * ik, kidx + 3 * ik);
+  zc *Uih = (zc*)xmalloc(sizeof(zc) * nb * ee->nbw), *o12 = (zc*)xmalloc(sizeof(zc) * nb2),
+     *o34 = (zc*)xmalloc(sizeof(zc) * nb2), *o14 = (zc*)xmalloc(sizeof(zc) * nb2), *o32 = (zc*)xmalloc(sizeof(zc) * nb2),
+     *mee = (zc*)xmalloc(sizeof(zc) * nb4), *mex = (zc*)xmalloc(sizeof(zc) * nb4), *A = (zc*)xmalloc(sizeof(zc) * nb4),
+     *A1rho = (zc*)xmalloc(sizeof(zc) * nb2), *A1rhobar = (zc*)xmalloc(sizeof(zc) * nb2),
+     *mtmp = (zc*)xmalloc(sizeof(zc) * nb2), *P1 = (zc*)xmalloc(sizeof(zc) * nb4), *P2 = (zc*)xmalloc(sizeof(zc) * nb4);
+  double* delta = (double*)xmalloc(sizeof(double) * nb4);
+  const double prefac_gauss = 1. / (ee->degauss * sqrt(2. * M_PI));
+  const double prefac_exp = -0.25 / pow(ee->degauss, 2); /* Lindblad: prefac_exp_ld */
+  for (int64_t ip = 0; ip < s->npair; ip++) {
+    const int ik1 = (int)s->k1st[ip], ik2 = (int)s->k2nd[ip];
+    zc* P1o = P1out + (size_t)ip * nb4;
+    zc* P2o = P2out + (size_t)ip * nb4;
+    if (ik1 == ik2 && !ee->antisym) {
+      memset(P1o, 0, sizeof(zc) * nb4);
+      memset(P2o, 0, sizeof(zc) * nb4);
+      continue;
+    }
+    memset(P1, 0, sizeof(zc) * nb4);
+    memset(P2, 0, sizeof(zc) * nb4);
+    ee_ovlp(ee, &c, o12, Uih, ik1, ik2, 1);
+    for (int ik3 = 0; ik3 < nk; ik3++) {
+      if (ee->antisym && ik1 == ik2 && ik2 == ik3) continue;
+      double k4v[3];
+      for (int d = 0; d < 3; d++) k4v[d] = ee->kvec[3 * ik1 + d] + ee->kvec[3 * ik3 + d] - ee->kvec[3 * ik2 + d];
+      const int ik4 = ee_findk(ee, nk, kidx, k4v);
+      if (ik4 < 0) continue;
+      /* calc_delta (ElecElec_Model.h:164-184) */
+      int conserved = 0;
+      const double *e1 = e + ik1 * nb, *e2 = e + ik2 * nb, *e3 = e + ik3 * nb, *e4 = e + ik4 * nb;
+      for (int i1 = 0; i1 < nb; i1++)
+        for (int i2 = 0; i2 < nb; i2++)
+          for (int i3 = 0; i3 < nb; i3++)
+            for (int i4 = 0; i4 < nb; i4++) {
+              const int i1234 = ((i1 * nb + i2) * nb + i3) * nb + i4;
+              const double de = e1[i1] - e2[i2] + e3[i3] - e4[i4];
+              if (fabs(de) < ee->ethr) {
+                delta[i1234] = exp(prefac_exp * pow(de, 2));
+                conserved = 1;
+              } else {
+                delta[i1234] = 0;
+              }
+            }
+      if (!conserved) continue;
+      /* calc_ovlps (ElecElec_Model.h:64-71; ovlp12 kept from above) and calc_mee / calc_mee_ex */
+      ee_ovlp(ee, &c, o34, Uih, ik3, ik4, 0);
+      if (ee->antisym) {
+        ee_ovlp(ee, &c, o14, Uih, ik1, ik4, 1);
+        ee_ovlp(ee, &c, o32, Uih, ik3, ik2, 0);
+      }
+      for (int i1 = 0; i1 < nb; i1++)
+        for (int i2 = 0; i2 < nb; i2++)
+          for (int i3 = 0; i3 < nb; i3++)
+            for (int i4 = 0; i4 < nb; i4++) {
+              const int i1234 = ((i1 * nb + i2) * nb + i3) * nb + i4;
+              mee[i1234] = zmul(o12[i1 * nb + i2], o34[i3 * nb + i4]);
+              if (ee->antisym) mex[i1234] = zmul(o14[i1 * nb + i4], o32[i3 * nb + i2]);
+            }
+      if (ee->antisym) /* axbyc(mee, mee_ex, n, -0.5, 0.5): mee = -0.5 mee_ex + 0.5 mee */
+        for (int i = 0; i < nb4; i++) mee[i] = zadd(zmul(zmk(-0.5, 0), mex[i]), zmul(zmk(0.5, 0), mee[i]));
+      for (int i = 0; i < nb4; i++) A[i] = zscale(delta[i], mee[i]); /* A2 = delta mee; A1 = A2 (Lindblad) */
+      /* P1ee, P2ee accumulation (ElecElec_Model.h:199-240) */
+      for (int i1 = 0; i1 < nb; i1++)
+        for (int i3 = 0; i3 < nb; i3++) {
+          const zc* Ab = A + (size_t)(i1 * nb + i3) * nb2;
+          const zc* Abar = A + (size_t)(i3 * nb + i1) * nb2;
+          if (!dm) { /* calc_A1f, calc_A1fbar */
+            const double *f3 = f + (size_t)ik3 * nb, *f4 = f + (size_t)ik4 * nb;
+            for (int i = 0; i < nb; i++)
+              for (int j = 0; j < nb; j++) {
+                A1rho[i * nb + j] = zscale(f4[j], zscale(1 - f3[i], Ab[i * nb + j]));
+                A1rhobar[i * nb + j] = zscale(1 - f4[j], zscale(f3[i], Abar[i * nb + j]));
+              }
+          } else { /* calc_A1rho: dmleft * A1 * dmright (two zhemm) */
+            zhemm_n(mtmp, 0, dm + (size_t)ik4 * nb2, Ab, nb, zmk(1, 0), zmk(0, 0));
+            zhemm_n(A1rho, 1, dm1 + (size_t)ik3 * nb2, mtmp, nb, zmk(1, 0), zmk(0, 0));
+            zhemm_n(mtmp, 0, dm1 + (size_t)ik4 * nb2, Abar, nb, zmk(1, 0), zmk(0, 0));
+            zhemm_n(A1rhobar, 1, dm + (size_t)ik3 * nb2, mtmp, nb, zmk(1, 0), zmk(0, 0));
+          }
+          for (int i2 = 0; i2 < nb; i2++)
+            for (int i4 = 0; i4 < nb; i4++) {
+              const int i1234 = ((i1 * nb + i2) * nb + i3) * nb + i4;
+              const int n24 = (i2 * nb + i4) * nb2, n42 = (i4 * nb + i2) * nb2;
+              for (int i6 = 0; i6 < nb; i6++)
+                for (int i8 = 0; i8 < nb; i8++) {
+                  const int i68 = i6 * nb + i8;
+                  P1[i1234] = zadd(P1[i1234], zmul(A1rho[i68], zconj(A[n24 + i68])));
+                  P2[i1234] = zadd(P2[i1234], zmul(A1rhobar[i68], zconj(A[n42 + i68])));
+                }
+            }
+        }
+    }
+    zc prefac = zmk(prefac_gauss / ee->nk_full, 0);
+    if (ee->antisym) prefac = zmk(prefac.x * 2, prefac.y * 2);
+    for (int i = 0; i < nb4; i++) {
+      P1o[i] = zmul(prefac, P1[i]);
+      P2o[i] = zmul(prefac, P2[i]);
+    }
+  }
+  free(e); free(kidx); free(Uih); free(o12); free(o34); free(o14); free(o32); free(mee); free(mex); free(A);
+  free(A1rho); free(A1rhobar); free(mtmp); free(P1); free(P2); free(delta);
+}
+
+/* electronphonon::reset_scatt (ElectronPhonon.cpp:15-42) for the e-e update on state y (the
+ * density matrix of all nb_dm bands, in the system's picture) at time t: the window copy, the
+ * screening density from its diagonal (coulomb_model::init, Coulomb_Model.h:533-553), the
+ * Schrodinger-picture conversion of add_scatt_contrib (ElectronPhonon.cpp:56-66), P_ee, and
+ * P = P_base + scale_ee P_ee (ElectronPhonon.cpp:87-100). */
+void orc_ee_rebuild(orc_ee* ee, const orc_sys* s, double t, const double* y) {
+  const int nk = s->nk, nb = ee->nb, nb2 = nb * nb, nb4 = nb2 * nb2, nd = s->nb_dm, bs = s->bstart;
+  const zc* dmx = (const zc*)y;
+  zc* dm = (zc*)xmalloc(sizeof(zc) * nk * nb2);
+  zc* dm1 = (zc*)xmalloc(sizeof(zc) * nk * nb2);
+  for (int ik = 0; ik < nk; ik++)
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < nb; j++) {
+        const zc v = dmx[(size_t)ik * nd * nd + (bs + i) * nd + bs + j];
+        dm[(size_t)ik * nb2 + i * nb + j] = v;
+        dm1[(size_t)ik * nb2 + i * nb + j] = (i == j) ? zsub(zmk(1, 0), v) : zmk(-v.x, -v.y);
+      }
+  if (ee->update_screening) {
+    double n = 0;
+    for (int ik = 0; ik < nk; ik++)
+      for (int b = 0; b < nb; b++) {
+        const double ft = dm[(size_t)ik * nb2 + b * nb + b].x;
+        if (b < ee->nv) n += (1 - ft);
+        else n += ft;
+      }
+    ee->nfree = n / (ee->nk_full * ee->cell_size);
+  }
+  if (!s->picture_schrodinger)
+    for (int ik = 0; ik < nk; ik++) {
+      const double* e = s->e_dm + (size_t)ik * nd + bs;
+      zc* d = dm + (size_t)ik * nb2;
+      zc* d1 = dm1 + (size_t)ik * nb2;
+      for (int i = 0; i < nb; i++)
+        for (int j = i + 1; j < nb; j++) {
+          d[i * nb + j] = zmul(d[i * nb + j], zcis((e[j] - e[i]) * t));
+          d1[i * nb + j] = zmk(-d[i * nb + j].x, -d[i * nb + j].y);
+          d[j * nb + i] = zconj(d[i * nb + j]);
+          d1[j * nb + i] = zconj(d1[i * nb + j]);
+        }
+    }
+  orc_ee_P(ee, s, dm, dm1, NULL, ee->nfree, ee->P1ee, ee->P2ee);
+  const zc sc = zmk(ee->scale, 0);
+  for (size_t i = 0; i < (size_t)s->npair * nb4; i++) {
+    const zc a1 = ee->scale != 1. ? zmul(ee->P1ee[i], sc) : ee->P1ee[i];
+    const zc a2 = ee->scale != 1. ? zmul(ee->P2ee[i], sc) : ee->P2ee[i];
+    ee->P1eff[i] = zadd(a1, ee->P1base[i]);
+    ee->P2eff[i] = zadd(a2, ee->P2base[i]);
+  }
+  free(dm);
+  free(dm1);
+}
+
 /* dm_dynamics::compute -- DensityMatrix_Dynamics.h:243-278 (no laser, no phenomenological term,
  * not semiclassical): ddmdt = coherent + scattering on the state dm; 1 - dm per set_oneminusdm
  * (DenMat.cpp:249-261). */
@@ -363,6 +640,7 @@ void orc_compute(const orc_sys* s, orc_ws* w, double t, const zc* dm, zc* ddmdt)
     for (size_t i = 0; i < (size_t)nk * nb2; i++) ddmdt[i] = zadd(ddmdt[i], w->coh[i]);
   }
   if (s->scatt_enable) {
+    if (s->ee && s->ee->inside) orc_ee_rebuild(s->ee, s, t, (const double*)dm);  /* update_scatt_inside */
     orc_evolve_driver(s, w, t, dm, w->dm1x, w->ddmx);
     for (size_t i = 0; i < (size_t)nk * nb2; i++) ddmdt[i] = zadd(ddmdt[i], w->ddmx[i]);
   }

@@ -66,6 +66,11 @@ def lib():
     if _lib is None:
         _lib = C.CDLL(build())
         _lib.orc_rhs.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]
+        _lib.orc_ee_P.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                  C.c_void_p, C.c_void_p]
+        _lib.orc_ee_P.restype = None
+        _lib.orc_ee_rebuild.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
+        _lib.orc_ee_rebuild.restype = None
         _lib.orc_rhs_parts.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_rk4.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_long, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p]
         _lib.orc_rkf45.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -104,7 +109,86 @@ class _Sys(C.Structure):
                 ("k1st", C.c_void_p), ("k2nd", C.c_void_p), ("P1", C.c_void_p), ("P2", C.c_void_p),
                 ("e_dm", C.c_void_p), ("prefac_eph", C.c_double), ("Hcoh", C.c_void_p),
                 ("picture_schrodinger", C.c_int), ("expt", C.c_int), ("ddmdt_eq", C.c_void_p), ("scatt_enable", C.c_int),
-                ("linear", C.c_int), ("f_lin", C.c_void_p)]
+                ("linear", C.c_int), ("f_lin", C.c_void_p), ("ee", C.c_void_p)]
+
+
+class _EE(C.Structure):
+    """orc_ee (dmd_oracle.c): the e-e model of eeMode = Pee_update with static screening"""
+    _fields_ = [("nb", C.c_int), ("nbw", C.c_int), ("kvec", C.c_void_p), ("kmesh", C.c_int * 3), ("U", C.c_void_p),
+                ("GGT", C.c_double * 9), ("cell_size", C.c_double), ("nk_full", C.c_double), ("T", C.c_double),
+                ("eps", C.c_double), ("meff", C.c_double), ("formula", C.c_int), ("nfree", C.c_double),
+                ("update_screening", C.c_int), ("nv", C.c_int), ("degauss", C.c_double), ("ethr", C.c_double),
+                ("antisym", C.c_int), ("scale", C.c_double), ("inside", C.c_int), ("P1base", C.c_void_p),
+                ("P2base", C.c_void_p), ("P1eff", C.c_void_p), ("P2eff", C.c_void_p), ("P1ee", C.c_void_p),
+                ("P2ee", C.c_void_p)]
+
+
+EE_FORMULAS = {"unscreened": 0, "debye": 1, "Bechstedt": 2}
+
+
+def ggt_of(R):
+    """lattice::GGT = Gvec Gvec^T with Gvec = 2 pi inv(R) (lattice.h:41-42), in the operation order of
+    comm/matrix3.h (inv = adjugate / det with det = box of the rows, products summed from k = 0) and
+    comm/vector3.h (cross, dot)."""
+    r = [[float(R[i][j]) for j in range(3)] for i in range(3)]
+
+    def cross(a, b):
+        return [a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]]
+
+    def dot(a, b):
+        return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]
+
+    det = dot(r[0], cross(r[1], r[2]))
+    cols = [cross(r[1], r[2]), cross(r[2], r[0]), cross(r[0], r[1])]
+    s = 1. / det
+    inv = [[cols[j][i] * s for j in range(3)] for i in range(3)]
+    G = [[inv[i][j] * (2. * math.pi) for j in range(3)] for i in range(3)]
+    out = np.zeros((3, 3))
+    for i in range(3):
+        for j in range(3):
+            acc = 0.0
+            for k in range(3):
+                acc += G[i][k] * G[j][k]
+            out[i, j] = acc
+    return out
+
+
+class EEModel:
+    """The e-e model's inputs (what elecelec_model / coulomb_model hold) and its operator buffers.
+    P1eff, P2eff are the system's P1, P2: P_base + scale P_ee, rebuilt in place from rho."""
+
+    def __init__(self, *, nb, kvec, kmesh, U, GGT, cell_size, nk_full, T, eps, meff, formula, nfree, update_screening,
+                 nv, degauss, ethr, antisym, scale, inside, P1base, P2base):
+        self.kvec = np.ascontiguousarray(kvec, np.float64)
+        self.U = np.ascontiguousarray(U, np.complex128)
+        self.P1base = np.ascontiguousarray(P1base, np.complex128)
+        self.P2base = np.ascontiguousarray(P2base, np.complex128)
+        self.P1eff = self.P1base.copy()
+        self.P2eff = self.P2base.copy()
+        self.P1ee = np.zeros_like(self.P1base)
+        self.P2ee = np.zeros_like(self.P2base)
+        self.nb, self.nbw = int(nb), int(self.U.shape[1])
+        self.kmesh = tuple(int(x) for x in kmesh)
+        self.GGT = np.ascontiguousarray(GGT, np.float64).reshape(9)
+        self.cell_size, self.nk_full, self.T, self.eps, self.meff = cell_size, nk_full, T, eps, meff
+        self.formula = EE_FORMULAS[formula] if isinstance(formula, str) else int(formula)
+        self.update_screening, self.nv = int(update_screening), int(nv)
+        self.degauss, self.ethr, self.antisym, self.scale = degauss, ethr, int(antisym), scale
+        self.inside = int(inside)
+        self.c = _EE(nb=self.nb, nbw=self.nbw, kvec=self.kvec.ctypes.data, kmesh=(C.c_int * 3)(*self.kmesh),
+                     U=self.U.ctypes.data, GGT=(C.c_double * 9)(*self.GGT), cell_size=cell_size, nk_full=nk_full, T=T,
+                     eps=eps, meff=meff, formula=self.formula, nfree=nfree, update_screening=self.update_screening,
+                     nv=self.nv, degauss=degauss, ethr=ethr, antisym=self.antisym, scale=scale, inside=self.inside,
+                     P1base=self.P1base.ctypes.data, P2base=self.P2base.ctypes.data, P1eff=self.P1eff.ctypes.data,
+                     P2eff=self.P2eff.ctypes.data, P1ee=self.P1ee.ctypes.data, P2ee=self.P2ee.ctypes.data)
+
+    @property
+    def nfree(self):
+        return self.c.nfree
+
+    @nfree.setter
+    def nfree(self, v):
+        self.c.nfree = v
 
 
 class _Meas(C.Structure):
@@ -180,7 +264,11 @@ def read_size(d: str) -> dict:
                 nk_full=float(l3[0]), nk=int(l3[1]), kmesh=tuple(int(x) for x in l3[2:5]),
                 nkpair=int(lines[3].split("#")[0].split()[0]),
                 temperature=float(lines[5].split("#")[0].split()[0]),
-                mu=float(lines[6].split("#")[0].split()[2]))
+                mu=float(lines[6].split("#")[0].split()[2]),
+                nb_wannier=l2[6] if len(l2) > 6 else l2[0])
+    dg = lines[7].split("#")[0].split() if len(lines) > 7 else []
+    info["degauss"] = float(dg[0]) if dg else 0.0
+    info["ndegauss"] = float(dg[1]) if len(dg) > 1 else 0.0
     return info
 
 
@@ -242,13 +330,14 @@ class OracleSystem:
     ddmdt_eq: Optional[np.ndarray] = None    # [nk][nb^2] window, subtracted from the scattering term
     linear: bool = False                     # alg_linearize: P1, P2 hold Lscij, Lscji
     f_lin: Optional[np.ndarray] = None       # [nk][nb] window f_eq of the linearization
+    ee: Optional[EEModel] = None             # eeMode = Pee_update: P1, P2 are ee.P1eff, ee.P2eff
 
     def cstruct(self):
         s = _Sys(nk=self.nk, nb_dm=self.nb_dm, bstart=self.bstart, bend=self.bend, npair=self.npair,
                  k1st=_ptr(self.k1st), k2nd=_ptr(self.k2nd), P1=_ptr(self.P1), P2=_ptr(self.P2), e_dm=_ptr(self.e_dm),
                  prefac_eph=self.prefac_eph, Hcoh=_ptr(self.Hcoh), picture_schrodinger=self.picture_schrodinger,
                  expt=self.expt, ddmdt_eq=_ptr(self.ddmdt_eq), scatt_enable=1, linear=1 if self.linear else 0,
-                 f_lin=_ptr(self.f_lin))
+                 f_lin=_ptr(self.f_lin), ee=C.addressof(self.ee.c) if self.ee is not None else None)
         return s
 
     @property
@@ -280,7 +369,7 @@ def load(d: str) -> OracleSystem:
     nimp = 0
     while pget(pm, "impurity_density" + ("" if nimp == 0 else str(nimp + 1)), 0.0) != 0:
         nimp += 1
-    mu, gs = set_mu_and_n(pm, e, e_dm, sz, nv_dm, T, mu, cell_size, dim)
+    mu, gs, nfree = set_mu_and_n(pm, e, e_dm, sz, nv_dm, T, mu, cell_size, dim)
     f = fermi(T, mu, e)
     f_dm = np.ascontiguousarray(f[:, sz["bStart_dm"]:sz["bEnd_dm"]])
     smat = np.fromfile(os.path.join(dd, "ldbd_smat.bin"), dtype=np.complex128).reshape(nk, 3, nb_dm * nb_dm)
@@ -367,13 +456,76 @@ def load(d: str) -> OracleSystem:
         ddmdt_eq = np.zeros((nk, nb * nb), np.complex128)
         cs = tmp.cstruct()
         L.orc_compute_ddmdt_eq(C.addressof(cs), f_eq.ctypes.data, ddmdt_eq.ctypes.data)
+    ee = None
+    ee_mode = pm.get("eeMode", "none")
+    if ee_mode != "none":
+        if ee_mode != "Pee_update" or linear or int(pget(pm, "alg_linearize_dPee", 0)):
+            raise ValueError("the oracle restates eeMode = Pee_update without linearization")
+        if pm.get("dynamic_screening", "static") != "static":
+            raise ValueError("the oracle restates static screening only")
+        nbw = sz["nb_wannier"]
+        nb_eph = sz["bEnd_eph"] - sz["bStart_eph"]
+        U = np.fromfile(os.path.join(dd, "ldbd_Umat.bin"), dtype=np.complex128).reshape(nk, nbw, nb_eph)
+        kvec = np.fromfile(os.path.join(dd, "ldbd_kvec.bin"), dtype=np.float64).reshape(nk, 3)
+        degauss, ndegauss = sz["degauss"], sz["ndegauss"]
+        degauss = pget(pm, "degauss", degauss / eV, eV)
+        ndegauss = pget(pm, "ndegauss", ndegauss)
+        scale_scatt = pget(pm, "scale_scatt", 1.0)
+        ee = EEModel(nb=nb, kvec=kvec, kmesh=sz["kmesh"], U=U, GGT=ggt_of(R), cell_size=cell_size,
+                     nk_full=sz["nk_full"], T=T, eps=pget(pm, "epsilon_background", 1.0),
+                     meff=pget(pm, "meff_screening", 1.0), formula=pm.get("scrFormula", "RPA"), nfree=nfree,
+                     update_screening=int(pget(pm, "update_screening", 1)), nv=nv_dm - bstart,
+                     degauss=pget(pm, "degauss_ee", degauss / eV, eV), ethr=degauss * ndegauss,
+                     antisym=int(pget(pm, "ee_antisymmetry", 0)), scale=pget(pm, "scale_ee", scale_scatt),
+                     inside=pget(pm, "freq_update_ee_model", 0) < 0, P1base=P1, P2base=P2)
+        # set-up (ElectronPhonon.cpp:3-14): P_ee at the equilibrium occupations with the set-up density
+        tmp = OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
+                           k1st=k1, k2nd=k2, P1=ee.P1eff, P2=ee.P2eff, prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=None,
+                           smat=smat, dm0=dm0, picture_schrodinger=schrod, expt=expt, t0=t0, tstep=0.0, tend=0.0,
+                           temperature=T, mu=mu, nk_full=sz["nk_full"], ob_prefac=1.0, ode={}, params={})
+        ee_operators(tmp, ee, None, np.ascontiguousarray(f_dm[:, bstart:bend]), nfree)
+        P1, P2 = ee.P1eff, ee.P2eff
     return OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
-                        k1st=k1, k2nd=k2, P1=np.ascontiguousarray(P1), P2=np.ascontiguousarray(P2),
+                        k1st=k1, k2nd=k2, P1=P1 if ee is not None else np.ascontiguousarray(P1),
+                        P2=P2 if ee is not None else np.ascontiguousarray(P2),
                         prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=Hcoh, smat=smat, dm0=dm0,
                         picture_schrodinger=schrod, expt=expt, t0=t0, tstep=tstep, tend=pget(pm, "tend", 0.0, fs),
                         temperature=T, mu=mu, nk_full=sz["nk_full"], ob_prefac=(1.0 / sz["nk_full"]) / cell_size_cmd,
                         ode=ode, params=pm, nv_dm=nv_dm, mue=mue, muh=muh, f_eq=f_eq, ddmdt_eq=ddmdt_eq, linear=linear,
-                        f_lin=f_lin)
+                        f_lin=f_lin, ee=ee)
+
+
+def ee_operators(s: OracleSystem, ee: EEModel, dm_window, f_window, nfree):
+    """P_ee of every pair (orc_ee_P) for window density matrices dm_window [nk][nb^2] (Schrodinger
+    picture; dm1 = 1 - dm) or, with dm_window None, the occupations f_window [nk][nb]; then the
+    system's operators P_base + scale P_ee. Returns (P1ee, P2ee)."""
+    L = lib()
+    cs = s.cstruct()
+    if dm_window is None:
+        L.orc_ee_P(C.addressof(ee.c), C.addressof(cs), None, None, f_window.ctypes.data, C.c_double(nfree),
+                   ee.P1ee.ctypes.data, ee.P2ee.ctypes.data)
+    else:
+        dm = np.ascontiguousarray(dm_window, np.complex128)
+        nb = ee.nb
+        dm1 = -dm.reshape(-1, nb, nb)
+        dm1[:, range(nb), range(nb)] += 1.0
+        dm1 = np.ascontiguousarray(dm1.reshape(dm.shape))
+        L.orc_ee_P(C.addressof(ee.c), C.addressof(cs), dm.ctypes.data, dm1.ctypes.data, None, C.c_double(nfree),
+                   ee.P1ee.ctypes.data, ee.P2ee.ctypes.data)
+    a1 = ee.P1ee * complex(ee.scale, 0) if ee.scale != 1.0 else ee.P1ee
+    a2 = ee.P2ee * complex(ee.scale, 0) if ee.scale != 1.0 else ee.P2ee
+    ee.P1eff[:] = a1 + ee.P1base
+    ee.P2eff[:] = a2 + ee.P2base
+    return ee.P1ee.copy(), ee.P2ee.copy()
+
+
+def ee_rebuild(s: OracleSystem, t: float, y: np.ndarray):
+    """reset_scatt's e-e update on state y at time t (orc_ee_rebuild): the screening density from y
+    (with update_screening), P_ee(rho), P = P_base + scale P_ee. Returns (P1, P2) copies."""
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    cs = s.cstruct()
+    lib().orc_ee_rebuild(C.addressof(s.ee.c), C.addressof(cs), C.c_double(t), y.ctypes.data)
+    return s.ee.P1eff.copy(), s.ee.P2eff.copy()
 
 
 def set_mu_and_n(pm, e, e_dm, sz, nv_dm, T, mu, cell_size, dim):
@@ -407,7 +559,7 @@ def set_mu_and_n(pm, e, e_dm, sz, nv_dm, T, mu, cell_size, dim):
     nhi = 0.0 / nk_full / cell_size
     gs = (ne + nei) if abs(ne + nei) > abs(nh + nhi) else (nh + nhi)
     gs = gs * nk_full * cell_size
-    return mu, (gs, ne * nk_full * cell_size, nh * nk_full * cell_size)
+    return mu, (gs, ne * nk_full * cell_size, nh * nk_full * cell_size), abs(ne) + abs(nh)
 
 
 def _setup_prototypes():

@@ -13,6 +13,10 @@
 //   gsl                  DMD's native evolve_gsl (RKF45 through the GSL restatement)
 //   euler                DMD's native evolve_euler
 //   tau                  compute(t0) + report_tau(0) (DensityMatrix_Dynamics.h:75)
+//   pee   IN OUT         e-e model: for each (t, y) record of IN, electronphonon::reset_scatt
+//                        (ElectronPhonon.cpp:15-42) on that density matrix -- the screening update
+//                        and P = P_eph (+ P_eimp) + scale_ee P_ee(rho) (ElecElec_Model.h:186-262) --
+//                        then the folded P1, P2 and the screening density
 #include "DensityMatrix_Dynamics.h"
 #include <vector>
 
@@ -79,6 +83,15 @@ int main(int argc, char** argv) {
             param->temperature, param->mu, latt->cell_size, latt->cell_size_cmd, dmdyn->sdmk->Hcoh ? 1 : 0);
     fprintf(m, "nv_dm %d\nmue %.17g\nmuh %.17g\nddmdteq %d\nlinearize %d\n", elec->nv_dm, dmdyn->sdmk->mue,
             dmdyn->sdmk->muh, alg.ddmdteq ? 1 : 0, alg.linearize ? 1 : 0);
+    if (eph->ee_model) {  // e-e model constants (ElecElec_Model.h:22-37, Coulomb_Model.h:415-423, 555-569)
+      coulomb_model* cm = eph->coul_model;
+      fprintf(m, "ee 1\nee_nfree %.17g\nee_scale %.17g\nee_degauss %.17g\nee_ethr %.17g\nee_eps %.17g\n"
+                 "ee_meff %.17g\nee_T %.17g\nee_nv %d\nee_antisym %d\nee_qscr2_debye %.17g\nee_nbw %d\n",
+              clp.nfreetot, eph->scale_ee, eph->ee_model->degauss, eph->ee_model->ethr, clp.eps, clp.meff, cm->T,
+              cm->nv, eep.antisymmetry ? 1 : 0, cm->qscr2_debye, elec->nb_wannier);
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) fprintf(m, "ee_ggt%d%d %.17g\n", i, j, latt->GGT(i, j));
+    }
     fclose(m);
     if (alg.ddmdteq || alg.linearize) write_bin(out + "/f_eq.bin", dmdyn->sdmk->f_eq[0], sizeof(double) * nk * nbdm);
     if (alg.ddmdteq) write_bin(out + "/ddmdt_eq.bin", eph->ddmdt_eq[0], sizeof(complex) * nk * eph->nb * eph->nb);
@@ -151,6 +164,30 @@ int main(int argc, char** argv) {
       }
     }
     write_bin(out + "/y_final.bin", y.data(), y.size() * sizeof(double));
+    return 0;
+  }
+  if (mode == "pee") {
+    FILE* in = fopen(argv[2], "rb");
+    std::string out = argv[3];
+    if (!in || !eph->ee_model) { fprintf(stderr, "pee needs %s and an e-e model\n", argv[2]); return 2; }
+    std::vector<double> y(2 * n);
+    std::vector<complex> all1, all2;
+    std::vector<double> nfree;
+    const size_t np4 = (size_t)eph->nkpair_proc * (size_t)std::pow(eph->nb, 4);
+    double t;
+    while (fread(&t, sizeof(double), 1, in) == 1) {
+      if (fread(y.data(), sizeof(double), 2 * n, in) != 2 * n) { fprintf(stderr, "short record\n"); return 2; }
+      copy_complex_from_real(dmdyn->sdmk->dm, y.data(), n);
+      dmdyn->sdmk->set_oneminusdm();
+      eph->reset_scatt(false, true, dmdyn->sdmk->dm, dmdyn->sdmk->oneminusdm, t, dmdyn->sdmk->f_eq);
+      all1.insert(all1.end(), eph->P1[0], eph->P1[0] + np4);
+      all2.insert(all2.end(), eph->P2[0], eph->P2[0] + np4);
+      nfree.push_back(clp.nfreetot);
+    }
+    fclose(in);
+    write_bin(out + "/pee_P1.bin", all1.data(), all1.size() * sizeof(complex));
+    write_bin(out + "/pee_P2.bin", all2.data(), all2.size() * sizeof(complex));
+    write_bin(out + "/pee_nfree.bin", nfree.data(), nfree.size() * sizeof(double));
     return 0;
   }
   if (mode == "gsl") { dmdyn->evolve_gsl(); return 0; }

@@ -9,6 +9,9 @@ if ROOT not in sys.path:
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 GOLDEN_CASES = sorted(d for d in os.listdir(GOLDEN) if os.path.isfile(os.path.join(GOLDEN, d, "golden.npz")))
+# cases whose operators are rebuilt from rho by the e-e model (eeMode = Pee_update), and the others
+EE_CASES = [c for c in GOLDEN_CASES if c.startswith("ee_")]
+FIXED_P_CASES = [c for c in GOLDEN_CASES if not c.startswith("ee_")]
 
 
 def pytest_configure(config):

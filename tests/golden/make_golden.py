@@ -10,7 +10,11 @@ seeded generator) and runs the shim-built reference program on it:
   * dump  -- setup arrays (initial density matrix, H_BS, occupations);
   * rhs   -- func / evolve_driver / evolve_coh on three states;
   * rk4   -- 40 classic RK4 steps through DMD's func, S_z every 5 steps;
-  * gsl   -- DMD's own evolve_gsl (RKF45) for 20 output intervals (S_z file + restart state).
+  * gsl   -- DMD's own evolve_gsl (RKF45) for 20 output intervals (S_z file + restart state);
+  * pee   -- (e-e cases) the operators rebuilt on the three states by reset_scatt: screening density
+             from the state, P = P_eph (+ P_eimp) + scale_ee P_ee(rho).
+The e-e cases rebuild P_ee on every RHS evaluation (eeMode = Pee_update, freq_update_ee_model < 0),
+so their rhs / rk4 / gsl records include the rebuild.
 The outputs are stored in golden.npz next to the inputs. Nothing here runs at test time.
 """
 from __future__ import annotations
@@ -31,6 +35,10 @@ from denmat_dynm_development_gb300 import units  # noqa: E402
 from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, make_ldbd  # noqa: E402
 
 FS = None
+
+# e-e model keys of param.in (parameters.cpp:192-231): rebuilt from rho on every RHS evaluation
+EE_COMMON = {"eeMode": "Pee_update", "scrMode": "medium", "freq_update_ee_model": -1,
+             "freq_update_eimp_model": -1, "epsilon_background": 12.9}
 
 CASES = {
     # e-ph only, nb=2, S_z perturbation, interaction picture
@@ -63,6 +71,22 @@ CASES = {
     "nb4_linear": dict(cfg=SynthConfig(nk=16, nb=4, seed=19, de_pair_mev=60.0),
                        param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0, 0.4, 0),
                                   extra={"alg_linearize": 1, "alg_picture": "schrodinger", "alg_expt": 0})),
+    # e-e scattering rebuilt from rho on every RHS (Pee_update), Debye screening updated from rho,
+    # e-imp folded in, B field; a ball of k-points on the mesh so that k1 + k3 - k2 is mostly present
+    "ee_nb2_debye": dict(cfg=SynthConfig(nk=40, nb=2, seed=31, de_pair_mev=60.0, eimp_sigma_mev=5.0, nwannier=4,
+                                         kball=True),
+                         param=dict(Bpert_T=(0, 0, 0.1), B_T=(0.8, 0, 0), eimp_fraction=0.05,
+                                    extra=dict(EE_COMMON, scrFormula="debye", update_screening=1))),
+    # exchange term (ee_antisymmetry), Bechstedt screening, Schrodinger picture without phases
+    "ee_nb2_bechstedt_anti": dict(cfg=SynthConfig(nk=32, nb=2, seed=32, de_pair_mev=60.0, nwannier=3, kball=True),
+                                  param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0, 0.6, 0),
+                                             extra=dict(EE_COMMON, scrFormula="Bechstedt", update_screening=1,
+                                                        ee_antisymmetry=1, meff_screening=0.3,
+                                                        alg_picture="schrodinger", alg_expt=0))),
+    # nb = 4, unscreened Coulomb (Gamma skipped), screening not updated
+    "ee_nb4_unscreened": dict(cfg=SynthConfig(nk=16, nb=4, seed=33, de_pair_mev=60.0, nwannier=6, kball=True),
+                              param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0.5, 0.3, 0),
+                                         extra=dict(EE_COMMON, scrFormula="unscreened", update_screening=0))),
     # two valence bands below the e-ph window (holes: nv_dm = 2), equilibrium drift subtracted
     "nb2_holes_eq": dict(cfg=SynthConfig(nk=24, nb=2, seed=17, de_pair_mev=60.0, extra_bands=2, nv=2),
                          param=dict(Bpert_T=(0.1, 0, 0.05), B_T=(0, 0, 1.0), extra={"alg_ddmdteq": 1})),
@@ -134,6 +158,10 @@ def make_case(name, spec, ref_bin, outroot):
         out["Lscji"] = np.fromfile(os.path.join(tmp, "o", "Lscji.bin"), dtype=np.complex128).reshape(-1, nbw ** 4)
     if meta["has_H"]:
         out["Hcoh"] = np.fromfile(os.path.join(tmp, "o", "Hcoh.bin"), dtype=np.complex128).reshape(nk, nbdm * nbdm)
+    ee = bool(meta.get("ee", 0))
+    if ee:  # P after set-up: P_eph (+ P_eimp) + scale_ee P_ee at the equilibrium occupations
+        out["ee_P1_eq"] = np.fromfile(os.path.join(tmp, "o", "P1.bin"), dtype=np.complex128).reshape(-1, nbw ** 4)
+        out["ee_P2_eq"] = np.fromfile(os.path.join(tmp, "o", "P2.bin"), dtype=np.complex128).reshape(-1, nbw ** 4)
     # rhs on three Hermitian states
     rng = np.random.default_rng([cfg.seed, 99])
     fs = 1e-15 * float(np.sqrt((1.0 / 9.10938291e-31) * (1e10 / 0.5291772) ** 2 / (1.0 / 4.35974434e-18)))
@@ -148,6 +176,11 @@ def make_case(name, spec, ref_bin, outroot):
         for t, y in zip(ts, ys):
             f.write(np.float64(t).tobytes())
             f.write(y.tobytes())
+    if ee:
+        run(ref_bin, tmp, "pee", "rhs_in.bin", "o")
+        out["pee_P1"] = np.fromfile(os.path.join(tmp, "o", "pee_P1.bin"), dtype=np.complex128).reshape(len(ts), -1, nbw ** 4)
+        out["pee_P2"] = np.fromfile(os.path.join(tmp, "o", "pee_P2.bin"), dtype=np.complex128).reshape(len(ts), -1, nbw ** 4)
+        out["pee_nfree"] = np.fromfile(os.path.join(tmp, "o", "pee_nfree.bin"))
     run(ref_bin, tmp, "rhs", "rhs_in.bin", "o")
     out["rhs_t"] = np.array(ts)
     out["rhs_y"] = np.stack(ys)

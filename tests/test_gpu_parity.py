@@ -13,7 +13,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, GOLDEN_CASES
+from conftest import GOLDEN, FIXED_P_CASES
 
 pytestmark = pytest.mark.gpu
 
@@ -43,7 +43,7 @@ RHS_TOL = {"f64": 1e-12, "f64x": 1e-11}
 
 
 def cases_for(prec):
-    return [(c, prec) for c in GOLDEN_CASES]
+    return [(c, prec) for c in FIXED_P_CASES]
 
 
 ALL = cases_for("f64") + cases_for("f64x")
@@ -117,7 +117,7 @@ def test_rkf45_vs_golden(case, prec, oracle, built):
         np.testing.assert_array_equal(np.array(nf), g["gsl_ncalls"])
 
 
-@pytest.mark.parametrize("case", GOLDEN_CASES)
+@pytest.mark.parametrize("case", FIXED_P_CASES)
 def test_euler_vs_oracle(case, oracle, built):
     d = os.path.join(GOLDEN, case)
     s = oracle.load(d)

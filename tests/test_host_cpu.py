@@ -6,7 +6,7 @@ import shutil
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, GOLDEN_CASES, ROOT
+from conftest import GOLDEN, FIXED_P_CASES, ROOT
 
 
 @pytest.fixture(scope="module")
@@ -28,7 +28,7 @@ def test_host_exports_header(host):
     assert sorted(host.EXPORTS) == names
 
 
-@pytest.mark.parametrize("case", GOLDEN_CASES)
+@pytest.mark.parametrize("case", FIXED_P_CASES)
 def test_load_matches_reference_setup(case, host, oracle):
     d = os.path.join(GOLDEN, case)
     g = dict(np.load(os.path.join(d, "golden.npz")))

@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, GOLDEN_CASES
+from conftest import EE_CASES, GOLDEN, GOLDEN_CASES
 
 
 def _load(case, oracle):
@@ -115,3 +115,33 @@ def test_rank_sliced_rhs_matches(nproc, oracle):
     assert np.abs(out - ref).max() <= 1e-14 * np.abs(ref).max()
     if nproc == 1:
         np.testing.assert_array_equal(out, ref)
+
+
+@pytest.mark.parametrize("case", EE_CASES)
+def test_ee_operators_bitwise(case, oracle):
+    """e-e model (eeMode = Pee_update): the operators after set-up (P_ee at the equilibrium
+    occupations) and after reset_scatt on three states (screening density from each state, P_ee(rho))
+    equal the reference's bit for bit."""
+    d = os.path.join(GOLDEN, case)
+    g = np.load(os.path.join(d, "golden.npz"))
+    s = oracle.load(d)
+    nb4 = (s.bend - s.bstart) ** 4
+    np.testing.assert_array_equal(s.P1.reshape(-1, nb4), g["ee_P1_eq"])
+    np.testing.assert_array_equal(s.P2.reshape(-1, nb4), g["ee_P2_eq"])
+    for i, (t, y) in enumerate(zip(g["rhs_t"], g["rhs_y"])):
+        P1, P2 = oracle.ee_rebuild(s, t, y)
+        np.testing.assert_array_equal(P1.reshape(-1, nb4), g["pee_P1"][i])
+        np.testing.assert_array_equal(P2.reshape(-1, nb4), g["pee_P2"][i])
+        assert s.ee.nfree == g["pee_nfree"][i]
+
+
+def test_ee_cases_cover_the_model():
+    """the e-e golden cases span the screening formulas, the exchange term, both pictures and nb = 2, 4"""
+    seen = set()
+    for case in EE_CASES:
+        from oracle.oracle import parse_param_in
+        pm = parse_param_in(os.path.join(GOLDEN, case, "param.in"))
+        seen.add(pm["scrFormula"])
+        seen.add("anti" if pm.get("ee_antisymmetry", "0") == "1" else "direct")
+        seen.add(pm.get("alg_picture", "interaction"))
+    assert {"debye", "Bechstedt", "unscreened", "anti", "direct", "schrodinger", "interaction"} <= seen
