@@ -12,6 +12,7 @@
 
 #include "dmd_adjoint.cuh"
 #include "dmd_batched_tc.cuh"
+#include "dmd_ee.cuh"
 #include "dmd_gpu.h"
 #include "dmd_kernels.cuh"
 #include "dmd_layout.h"
@@ -68,6 +69,22 @@ struct dmd_handle {
   int adj = 0;                 // DMD_FLAG_ADJOINT: pair operators also in stored order (d_Praw, d_kkraw)
   double2* d_Praw = nullptr;   // [npair][2][nb4] folded P1, P2
   int2* d_kkraw = nullptr;
+  int eek = 0;                 // DMD_FLAG_EE: d_Praw, d_kkraw and d_dst kept for the e-e model
+  void* d_dst = nullptr;       // column-block destination of every stored pair (CbDst)
+  // e-e model (dmd_ee_attach): P = P_base (d_Praw) + ee_scale P_ee, rebuilt from rho
+  int ee_on = 0, ee_every = 0, ee_update = 0, ee_nv = 0;
+  double ee_scale = 1, ee_nfree0 = 0, ee_nkfull = 1, ee_cell = 1, ee_eps = 1, ee_T = 1, ee_meff = 1;
+  dmd::EeArgs ee_args;
+  double* d_ee_kvec = nullptr;
+  int4* d_ee_kidx = nullptr;
+  int* d_ee_kmap = nullptr;
+  double2* d_ee_U = nullptr;
+  double2* d_ee_erng = nullptr;
+  double* d_ee_f = nullptr;
+  double2* d_ee_dm = nullptr;
+  double2* d_ee_dm1 = nullptr;
+  dmd::EeScreen* d_ee_scr = nullptr;
+  double2* d_ee_Pee = nullptr;
   float2* d_x0y0 = nullptr;    // tensor-core form: contraction of diag(f_ref), back-transformed, by k
   float2* d_v0 = nullptr;      // tensor-core form: (prefac/2)(C0 + C0^dagger) by k
   double2* d_H = nullptr;      // [nk][nbdm^2]
@@ -103,8 +120,8 @@ struct dmd_handle {
   };
   std::vector<Rec> prof_pending;
   std::vector<cudaEvent_t> ev_pool;
-  double prof_ms[4] = {0, 0, 0, 0};
-  long long prof_n[4] = {0, 0, 0, 0};
+  double prof_ms[5] = {0, 0, 0, 0, 0};  // prep, contraction, finish, step counter, e-e rebuild
+  long long prof_n[5] = {0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -381,8 +398,15 @@ FinishArgs base_finish(dmd_handle* h, const double2* y) {
 }
 
 template <int NB>
+int ee_rebuild(dmd_handle* h, const double2* y, const TimeArg& ta, bool eq);
+
+template <int NB>
 int rhs_impl(dmd_handle* h, const double2* y, const TimeArg& ta, FinishArgs fa) {
   int s;
+  if constexpr (NB == 2 || NB == 4) {
+    // e-e operators rebuilt from this state first (update_scatt_inside, DensityMatrix_Dynamics.h:263)
+    if (h->ee_on && h->ee_every && fa.want_eph && (s = ee_rebuild<NB>(h, y, ta, false))) return s;
+  }
   if (fa.want_eph) {
     if ((s = launch_prep<NB>(h, y, ta))) return s;
     if ((s = launch_pairs<NB>(h))) return s;
@@ -595,24 +619,32 @@ struct CbDst {
 // coordinates (Q1 = M^H P1 M, Q2 = M^T P2 conj(M)), pack in the arithmetic's format and store at
 // the pair's slot (element-major inside its row block: Q1 row-major, then Q2 column-major). In the
 // deviation form the contraction of diag(f_ref) through the pair is added to acc0 (FP64 atomics).
+// Operators of the chunk's pair j, operator m (P1, P2): element e at raw[m sseg + j spair + e], the
+// additive ones (or null) at add[m aseg + j apair + e].
+struct FillSrc {
+  const double2* raw;
+  size_t sseg, spair;
+  const double2* add;
+  size_t aseg, apair;
+};
+
 template <int NB>
-__global__ void k_cb_fill(long long p0, long long cnt, const double2* __restrict__ raw, int has_add, double add_scale,
-                          const CbDst* __restrict__ dst, int lin, int prec, int esz, unsigned char* __restrict__ store,
-                          const double* __restrict__ fw, double* __restrict__ acc0) {
+__global__ void k_cb_fill(long long p0, long long cnt, FillSrc src, double add_scale, const CbDst* __restrict__ dst,
+                          int lin, int prec, int esz, unsigned char* __restrict__ store, const double* __restrict__ fw,
+                          double* __restrict__ acc0) {
   constexpr int NB2 = NB * NB, NB4 = NB2 * NB2, NE = 2 * NB4;
   const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (j >= cnt) return;
   const CbDst dd = dst[p0 + j];
   const bool tr = dd.flags & 1, rev = (dd.flags >> 1) & 1;
-  const size_t nn = (size_t)cnt * NB4;
   cd Pe[2][NB4];
   for (int m = 0; m < 2; ++m) {
     const int sm = tr ? 1 - m : m;  // the transposed pair carries (conj P2, conj P1)
-    const double2* sp = raw + sm * nn + (size_t)j * NB4;
-    const double2* ap = has_add ? raw + (2 + sm) * nn + (size_t)j * NB4 : nullptr;
+    const double2* sp = src.raw + sm * src.sseg + (size_t)j * src.spair;
+    const double2* ap = src.add ? src.add + sm * src.aseg + (size_t)j * src.apair : nullptr;
     for (int e = 0; e < NB4; ++e) {
       double x = sp[e].x, yv = sp[e].y;
-      if (ap) {  // P += P_add * scale (ElectronImpurity.cpp:38-39, ElectronPhonon.cpp:96-97)
+      if (ap) {  // P += P_add * scale (ElectronImpurity.cpp:38-39, ElectronPhonon.cpp:87-100)
         x = __dadd_rn(x, __dmul_rn(ap[e].x, add_scale));
         yv = __dadd_rn(yv, __dmul_rn(ap[e].y, add_scale));
       }
@@ -812,16 +844,22 @@ int fill_pairs_cb(dmd_handle* h, PairSource& src, const std::vector<CbDst>& dst,
     cudaEventRecord(done[b], h->st);
     const unsigned g = blocks_for(cnt, 128);
     double* a0 = dev ? (double*)h->d_acc0 : nullptr;
+    const size_t nn = (size_t)cnt * nb4;
+    const FillSrc fs = {dev_raw[b], nn, (size_t)nb4, src.has_add() ? dev_raw[b] + 2 * nn : nullptr, nn, (size_t)nb4};
     if (h->nb == 2)
-      k_cb_fill<2><<<g, 128, 0, h->st>>>(p0, cnt, dev_raw[b], src.has_add(), h->add_scale, d_dst, h->lin, h->prec,
-                                         esz, (unsigned char*)h->d_P, h->d_fref, a0);
+      k_cb_fill<2><<<g, 128, 0, h->st>>>(p0, cnt, fs, h->add_scale, d_dst, h->lin, h->prec, esz,
+                                         (unsigned char*)h->d_P, h->d_fref, a0);
     else
-      k_cb_fill<4><<<g, 128, 0, h->st>>>(p0, cnt, dev_raw[b], src.has_add(), h->add_scale, d_dst, h->lin, h->prec,
-                                         esz, (unsigned char*)h->d_P, h->d_fref, a0);
+      k_cb_fill<4><<<g, 128, 0, h->st>>>(p0, cnt, fs, h->add_scale, d_dst, h->lin, h->prec, esz,
+                                         (unsigned char*)h->d_P, h->d_fref, a0);
     e = cudaGetLastError();
     if (e != cudaSuccess) break;
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  if (e == cudaSuccess && h->eek) {  // kept for the e-e model's refills
+    h->d_dst = d_dst;
+    d_dst = nullptr;
+  }
   cleanup();
   if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("pair fill: ") + cudaGetErrorString(e));
   return DMD_OK;
@@ -1084,7 +1122,9 @@ void release(dmd_handle* h) {
   if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
   void* ptrs[] = {h->d_err, h->d_pos, h->d_rb, h->d_items, h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
-                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0, h->d_Praw, h->d_kkraw};
+                  h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0, h->d_Praw, h->d_kkraw,
+                  h->d_dst, h->d_ee_kvec, h->d_ee_kidx, h->d_ee_kmap, h->d_ee_U, h->d_ee_erng, h->d_ee_f,
+                  h->d_ee_dm, h->d_ee_dm1, h->d_ee_scr, h->d_ee_Pee};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -1099,6 +1139,44 @@ void release(dmd_handle* h) {
   for (auto e : h->tev)
     if (e) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
+}
+
+// ---------------------------------------------------------------------------------------------
+// e-e model: P = P_base + scale P_ee(rho) (dmd_ee.cuh), refilled into the column-block store
+// ---------------------------------------------------------------------------------------------
+template <int NB>
+int ee_rebuild(dmd_handle* h, const double2* y, const TimeArg& ta, bool eq) {
+  constexpr int NB2 = NB * NB, NB4 = NB2 * NB2;
+  ProfScope ps(h, 4);
+  EeArgs a = h->ee_args;
+  if (!eq) {  // the window density matrix of y in the Schrodinger picture
+    k_ee_dm<NB><<<blocks_for((long long)h->nk * NB2, 256), 256, 0, h->st>>>(
+        h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->picture == DMD_PICTURE_INTERACTION ? 1 : 0, h->d_ee_dm, h->d_ee_dm1);
+    a.dm = h->d_ee_dm;
+    a.dm1 = h->d_ee_dm1;
+    a.f = nullptr;
+  } else {  // the set-up: occupations instead of rho (calc_A1f, calc_A1fbar)
+    a.dm = a.dm1 = nullptr;
+    a.f = h->d_ee_f;
+  }
+  k_ee_screen<<<1, 256, 0, h->st>>>(h->nk, NB, h->ee_nv, h->d_ee_dm, (!eq && h->ee_update) ? 1 : 0, h->ee_nfree0,
+                                    h->ee_nkfull, h->ee_cell, h->ee_eps, h->ee_T, h->ee_meff, h->d_ee_scr);
+  k_ee_pairs<NB><<<(unsigned)((h->npair + 3) / 4), 128, 0, h->st>>>(a);
+  const bool dev = deviation_form(h->prec) && !h->lin;
+  if (dev && cudaMemsetAsync(h->d_acc0, 0, (size_t)h->nk * 2 * NB2 * sizeof(double2), h->st) != cudaSuccess)
+    return fail(h, DMD_E_CUDA, "e-e refill");
+  const FillSrc fs = {h->d_Praw, (size_t)NB4, (size_t)2 * NB4, h->d_ee_Pee, (size_t)NB4, (size_t)2 * NB4};
+  k_cb_fill<NB><<<blocks_for(h->npair, 128), 128, 0, h->st>>>(0, h->npair, fs, h->ee_scale, (const CbDst*)h->d_dst,
+                                                              h->lin, h->prec, elem_bytes(h->prec),
+                                                              (unsigned char*)h->d_P, h->d_fref,
+                                                              dev ? (double*)h->d_acc0 : nullptr);
+  h->launches += eq ? 3 : 4;
+  CKL();
+  return DMD_OK;
+}
+
+int ee_rebuild_nb(dmd_handle* h, const double2* y, const TimeArg& ta, bool eq) {
+  return h->nb == 2 ? ee_rebuild<2>(h, y, ta, eq) : ee_rebuild<4>(h, y, ta, eq);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1258,7 +1336,7 @@ static int create_impl(const dmd_desc* d, dmd_handle** out, PairSource* src) {
     return DMD_E_ARG;
   if (d->nkpair > 0 && (!d->k1st || !d->k2nd || (!src && (!d->P1 || !d->P2)))) return DMD_E_ARG;
   if (!src && (d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
-  if (d->flags & ~(DMD_FLAG_LINEAR | DMD_FLAG_ADJOINT)) return DMD_E_ARG;
+  if (d->flags & ~(DMD_FLAG_LINEAR | DMD_FLAG_ADJOINT | DMD_FLAG_EE)) return DMD_E_ARG;
   if ((d->flags & DMD_FLAG_ADJOINT) && d->nrhs > 1) return DMD_E_ARG;
   const int nrhs = d->nrhs > 1 ? d->nrhs : 1;
   // batched form: FP32 or bf16 hi+lo storage on the column-block contraction
@@ -1291,6 +1369,7 @@ static int create_impl(const dmd_desc* d, dmd_handle** out, PairSource* src) {
   h->prec = d->precision;
   h->lin = (d->flags & DMD_FLAG_LINEAR) ? 1 : 0;
   h->adj = (d->flags & DMD_FLAG_ADJOINT) ? 1 : 0;
+  h->eek = (d->flags & DMD_FLAG_EE) ? 1 : 0;
   h->nrhs = nrhs;
   h->nstate1 = (size_t)h->nk * h->nbdm * h->nbdm;
   h->nstate = h->nstate1 * nrhs;
@@ -1339,11 +1418,14 @@ static int create_impl(const dmd_desc* d, dmd_handle** out, PairSource* src) {
   if (!h->use_tc)
     h->pair_bytes = h->use_cb ? (int64_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) : (int64_t)h->npair * 2 * h->nb4 * 16;
   if (src && (!h->use_cb || h->use_tc || h->adj)) return bail(fail(h, DMD_E_ARG, "streamed operators need the column-block form"));
+  if (h->eek && (!h->use_cb || h->use_tc || h->nrhs != 1 || h->lin || src))
+    return bail(fail(h, DMD_E_ARG, "DMD_FLAG_EE needs nb = 2 or 4, a single state, no linearization and the "
+                                   "operators as arrays"));
   h->src = src;
   rc = h->use_tc ? upload_pairs_tc(h, d) : h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d);
   h->src = nullptr;
   if (rc) return bail(rc);
-  if (h->adj && h->use_cb && h->npair > 0) {  // the adjoint's transposed contraction reads stored-order P
+  if ((h->adj || h->eek) && h->use_cb && h->npair > 0) {  // stored-order P: the adjoint, the e-e refill
     if ((rc = dalloc(h, &h->d_Praw, (size_t)h->npair * 2 * h->nb4)) || (rc = dalloc(h, &h->d_kkraw, (size_t)h->npair)) ||
         (rc = upload_raw(h, d, h->d_Praw, h->d_kkraw)))
       return bail(rc);
@@ -2311,15 +2393,146 @@ int dmd_set_profiling(dmd_handle* h, int on) {
   prof_harvest(h);
   h->prof_on = on ? 1 : 0;
   if (on)
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < 5; ++i) {
       h->prof_ms[i] = 0;
       h->prof_n[i] = 0;
     }
   return DMD_OK;
 }
 
+int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
+  if (!h || !ee) return DMD_E_ARG;
+  if (!h->eek || !h->d_dst || !h->d_Praw) return fail(h, DMD_E_STATE, "the handle was not made with DMD_FLAG_EE");
+  if (h->ee_on) return fail(h, DMD_E_STATE, "an e-e model is already attached");
+  if (ee->nbw < h->nb || !ee->kvec || !ee->U || !ee->f || ee->kmesh[0] < 1 || ee->kmesh[1] < 1 || ee->kmesh[2] < 1 ||
+      ee->formula < DMD_SCREEN_UNSCREENED || ee->formula > DMD_SCREEN_BECHSTEDT || !(ee->degauss > 0) ||
+      !(ee->ethr >= 0) || !(ee->cell_size > 0) || !(ee->nk_full > 0) || !(ee->temperature > 0) ||
+      !(ee->eps_background >= 1) || !(ee->meff > 0))
+    return fail(h, DMD_E_ARG, "e-e model description");
+  CK(cudaSetDevice(h->dev));
+  const int nk = h->nk, nb = h->nb;
+  const size_t nmesh = (size_t)ee->kmesh[0] * ee->kmesh[1] * ee->kmesh[2];
+  if (nmesh > ((size_t)1 << 31)) return fail(h, DMD_E_ARG, "k mesh too large for the mesh table");
+  // mesh indices (kIndexMap::ikvec3, comm/kmap.cpp:15-23) and the mesh table; the first k-point of
+  // an index wins, as std::map::insert keeps it (comm/kmap.h:22-28)
+  std::vector<int4> kidx(nk);
+  std::vector<int> kmap(nmesh, -1);
+  for (int k = 0; k < nk; ++k) {
+    int v[3];
+    for (int d = 0; d < 3; ++d) {
+      const double x = ee->kvec[3 * k + d];
+      const double ki = x - std::floor(x);
+      v[d] = (int)std::round(ee->kmesh[d] * ki);
+      if (v[d] == ee->kmesh[d]) v[d] = 0;
+      if (!(v[d] >= 0 && v[d] < ee->kmesh[d])) return fail(h, DMD_E_ARG, "k-point off the mesh table");
+    }
+    kidx[k] = make_int4(v[0], v[1], v[2], 0);
+    int& slot = kmap[((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2]];
+    if (slot < 0) slot = k;
+  }
+  std::vector<double> ew((size_t)nk * nb);
+  CK(cudaMemcpy(ew.data(), h->d_ew, ew.size() * 8, cudaMemcpyDeviceToHost));
+  std::vector<double2> erng(nk);
+  for (int k = 0; k < nk; ++k) {
+    double lo = ew[(size_t)k * nb], hi = lo;
+    for (int b = 1; b < nb; ++b) {
+      lo = std::min(lo, ew[(size_t)k * nb + b]);
+      hi = std::max(hi, ew[(size_t)k * nb + b]);
+    }
+    erng[k] = make_double2(lo, hi);
+  }
+  int rc;
+  if ((rc = dalloc(h, &h->d_ee_kvec, (size_t)nk * 3)) || (rc = dalloc(h, &h->d_ee_kidx, (size_t)nk)) ||
+      (rc = dalloc(h, &h->d_ee_kmap, nmesh)) || (rc = dalloc(h, &h->d_ee_U, (size_t)nk * ee->nbw * nb)) ||
+      (rc = dalloc(h, &h->d_ee_erng, (size_t)nk)) || (rc = dalloc(h, &h->d_ee_f, (size_t)nk * nb)) ||
+      (rc = dalloc(h, &h->d_ee_dm, (size_t)nk * h->nb2)) || (rc = dalloc(h, &h->d_ee_dm1, (size_t)nk * h->nb2)) ||
+      (rc = dalloc(h, &h->d_ee_scr, 1)) || (rc = dalloc(h, &h->d_ee_Pee, (size_t)h->npair * 2 * h->nb4)))
+    return rc;
+  CK(cudaMemcpy(h->d_ee_kvec, ee->kvec, (size_t)nk * 3 * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_ee_kidx, kidx.data(), (size_t)nk * sizeof(int4), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_ee_kmap, kmap.data(), nmesh * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_ee_U, ee->U, (size_t)nk * ee->nbw * nb * 16, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_ee_erng, erng.data(), (size_t)nk * sizeof(double2), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_ee_f, ee->f, (size_t)nk * nb * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemset(h->d_ee_dm, 0, (size_t)nk * h->nb2 * 16));
+  EeArgs& a = h->ee_args;
+  memset(&a, 0, sizeof(a));
+  a.nk = nk;
+  a.npair = (int)h->npair;
+  a.nbw = ee->nbw;
+  for (int d = 0; d < 3; ++d) a.kmesh[d] = ee->kmesh[d];
+  for (int i = 0; i < 9; ++i) a.GGT[i] = ee->GGT[i];
+  a.ethr = ee->ethr;
+  a.prefac_exp = -0.25 / std::pow(ee->degauss, 2);  // Lindblad (ElecElec_Model.h:33-34)
+  a.prefac = 1. / (ee->degauss * std::sqrt(2. * M_PI)) / ee->nk_full;
+  if (ee->antisymmetry) a.prefac *= 2;
+  a.formula = ee->formula;
+  a.antisym = ee->antisymmetry ? 1 : 0;
+  a.kk = h->d_kkraw;
+  a.kvec = h->d_ee_kvec;
+  a.kidx = h->d_ee_kidx;
+  a.kmap = h->d_ee_kmap;
+  a.U = h->d_ee_U;
+  a.ew = h->d_ew;
+  a.erng = h->d_ee_erng;
+  a.scr = h->d_ee_scr;
+  a.Pee = h->d_ee_Pee;
+  h->ee_every = ee->every_rhs ? 1 : 0;
+  h->ee_update = ee->update_screening ? 1 : 0;
+  h->ee_nv = ee->nv;
+  h->ee_scale = ee->scale;
+  h->ee_nfree0 = ee->nfree;
+  h->ee_nkfull = ee->nk_full;
+  h->ee_cell = ee->cell_size;
+  h->ee_eps = ee->eps_background;
+  h->ee_T = ee->temperature;
+  h->ee_meff = ee->meff;
+  h->ee_on = 1;
+  if ((rc = ee_rebuild_nb(h, nullptr, time_value(h->t), true))) return rc;
+  CK(cudaStreamSynchronize(h->st));
+  if (h->g_rk4) {  // the captured step must include the update
+    cudaGraphExecDestroy(h->g_rk4);
+    h->g_rk4 = nullptr;
+  }
+  return DMD_OK;
+}
+
+int dmd_ee_update(dmd_handle* h) {
+  if (!h) return DMD_E_ARG;
+  if (!h->ee_on) return fail(h, DMD_E_STATE, "no e-e model attached");
+  CK(cudaSetDevice(h->dev));
+  int rc = ee_rebuild_nb(h, h->d_y, time_value(h->t), false);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->st));
+  return DMD_OK;
+}
+
+int dmd_ee_read(dmd_handle* h, double* P1ee, double* P2ee, double* nfree) {
+  if (!h) return DMD_E_ARG;
+  if (!h->ee_on) return fail(h, DMD_E_STATE, "no e-e model attached");
+  CK(cudaSetDevice(h->dev));
+  CK(cudaStreamSynchronize(h->st));
+  const size_t nb4 = (size_t)h->nb4, np = (size_t)h->npair;
+  if (P1ee || P2ee) {
+    std::vector<double2> buf(np * 2 * nb4);
+    CK(cudaMemcpy(buf.data(), h->d_ee_Pee, buf.size() * 16, cudaMemcpyDeviceToHost));
+    for (size_t p = 0; p < np; ++p)
+      for (int m = 0; m < 2; ++m) {
+        double* o = m == 0 ? P1ee : P2ee;
+        if (!o) continue;
+        memcpy(o + 2 * p * nb4, &buf[(p * 2 + m) * nb4], nb4 * 16);
+      }
+  }
+  if (nfree) {
+    EeScreen c;
+    CK(cudaMemcpy(&c, h->d_ee_scr, sizeof(c), cudaMemcpyDeviceToHost));
+    *nfree = c.nfree;
+  }
+  return DMD_OK;
+}
+
 int dmd_profile_get(const dmd_handle* h, int cls, double* total_ms, int64_t* n) {
-  if (!h || cls < 0 || cls > 3) return DMD_E_ARG;
+  if (!h || cls < 0 || cls > 4) return DMD_E_ARG;
   if (total_ms) *total_ms = h->prof_ms[cls];
   if (n) *n = h->prof_n[cls];
   return DMD_OK;

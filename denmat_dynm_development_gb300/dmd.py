@@ -19,6 +19,7 @@ from .build import GPU_LIB
 PREC = {"f64": 0, "f64x": 1, "f32": 2, "bf16x2": 3}
 FLAG_LINEAR = 1  # DMD_FLAG_LINEAR: P1, P2 are the linear operators Lscij, Lscji
 FLAG_ADJOINT = 2  # DMD_FLAG_ADJOINT: keep the operators in stored order for adjoint_rk4
+FLAG_EE = 4  # DMD_FLAG_EE: keep P_eph (+ P_eimp) in stored order and the column-block map for the e-e model
 PICTURE = {"interaction": 0, "schrodinger": 1}
 
 
@@ -37,6 +38,18 @@ class _Desc(C.Structure):
                 ("f_ref", C.c_void_p), ("nrhs", C.c_int32), ("reserved", C.c_int32)]
 
 
+class _EEDesc(C.Structure):
+    """dmd_ee_desc (include/dmd_gpu.h)"""
+    _fields_ = [("nbw", C.c_int32), ("kvec", C.c_void_p), ("kmesh", C.c_int32 * 3), ("U", C.c_void_p),
+                ("f", C.c_void_p), ("GGT", C.c_double * 9), ("cell_size", C.c_double), ("nk_full", C.c_double),
+                ("temperature", C.c_double), ("eps_background", C.c_double), ("meff", C.c_double),
+                ("formula", C.c_int32), ("nfree", C.c_double), ("update_screening", C.c_int32), ("nv", C.c_int32),
+                ("degauss", C.c_double), ("ethr", C.c_double), ("antisymmetry", C.c_int32), ("scale", C.c_double),
+                ("every_rhs", C.c_int32)]
+
+
+SCREEN = {"unscreened": 0, "debye": 1, "Bechstedt": 2}
+
 _L = None
 
 EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_set_ddmdt_eq", "dmd_func",
@@ -45,7 +58,8 @@ EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_s
            "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
            "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes", "dmd_adjoint_rk4", "dmd_autotune",
            "dmd_group_create", "dmd_group_rk4", "dmd_group_destroy",
-           "dmd_create_from_files", "dmd_create_from_sparse_files", "dmd_selftest_wait_timeout"]
+           "dmd_create_from_files", "dmd_create_from_sparse_files", "dmd_selftest_wait_timeout",
+           "dmd_ee_attach", "dmd_ee_update", "dmd_ee_read"]
 
 
 def _lib():
@@ -86,6 +100,9 @@ def _lib():
         L.dmd_create_from_sparse_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p,
                                                    C.c_char_p, C.POINTER(vp)]
         L.dmd_adjoint_rk4.argtypes = [vp, d, vp, d, i64, i64, C.c_int, C.c_int, C.c_int, i64, vp, vp, vp, vp, vp]
+        L.dmd_ee_attach.argtypes = [vp, C.POINTER(_EEDesc)]
+        L.dmd_ee_update.argtypes = [vp]
+        L.dmd_ee_read.argtypes = [vp, vp, vp, C.POINTER(d)]
         L.dmd_sync.argtypes = [vp]
         L.dmd_pinned_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
         L.dmd_pinned_free.argtypes = [vp]
@@ -107,7 +124,7 @@ class LindbladGPU:
 
     def __init__(self, *, nk, nb_dm, bstart, bend, e_dm, k1st, k2nd, P1, P2, prefac_eph, Hcoh=None,
                  picture="interaction", expt=1, precision="f64", P1_add=None, P2_add=None, add_scale=0.0, device=0,
-                 f_ref=None, linear=False, nrhs=1, adjoint=False, P_files=None, P_sparse=None):
+                 f_ref=None, linear=False, nrhs=1, adjoint=False, P_files=None, P_sparse=None, ee=None):
         L = _lib()
         self._keep = dict(e=_c(e_dm, np.float64), k1=_c(k1st, np.uint64), k2=_c(k2nd, np.uint64),
                           P1=_c(P1, np.complex128), P2=_c(P2, np.complex128), H=_c(Hcoh, np.complex128),
@@ -119,7 +136,8 @@ class LindbladGPU:
                      P1_add=ptr(k["A1"]), P2_add=ptr(k["A2"]), add_scale=add_scale, Hcoh=ptr(k["H"]),
                      picture=PICTURE[picture] if isinstance(picture, str) else int(picture), expt=int(expt),
                      precision=PREC[precision] if isinstance(precision, str) else int(precision), device=device,
-                     flags=(FLAG_LINEAR if linear else 0) | (FLAG_ADJOINT if adjoint else 0), f_ref=ptr(k["f"]),
+                     flags=(FLAG_LINEAR if linear else 0) | (FLAG_ADJOINT if adjoint else 0) | (FLAG_EE if ee else 0),
+                     f_ref=ptr(k["f"]),
                      nrhs=int(nrhs))
         h = C.c_void_p()
         if P_files is not None:  # DMD's operator files, streamed by the library
@@ -137,6 +155,40 @@ class LindbladGPU:
         self.nk, self.nb_dm, self.nrhs = nk, nb_dm, max(1, int(nrhs))
         self.npair, self.nb4 = int(np.asarray(k1st).size), (bend - bstart) ** 4
         self.ny = 2 * nk * nb_dm * nb_dm * self.nrhs
+        if ee:
+            try:
+                self.ee_attach(**ee)
+            except Exception:
+                self.close()
+                raise
+
+    # ------------------------------------------------------------------ e-e model (eeMode = Pee_update)
+    def ee_attach(self, *, kvec, kmesh, U, f, GGT, cell_size, nk_full, temperature, eps_background, meff, formula,
+                  nfree, update_screening, nv, degauss, ethr, antisymmetry, scale, every_rhs):
+        """Attach the e-e model (dmd_ee_attach): U complex [nk][nbw][nb], kvec [nk][3] fractional,
+        f [nk][nb] window occupations of the set-up, formula "unscreened" / "debye" / "Bechstedt"."""
+        U = np.ascontiguousarray(U, np.complex128)
+        keep = dict(kvec=np.ascontiguousarray(kvec, np.float64), U=U, f=np.ascontiguousarray(f, np.float64))
+        d = _EEDesc(nbw=int(U.shape[1]), kvec=keep["kvec"].ctypes.data, kmesh=(C.c_int32 * 3)(*[int(x) for x in kmesh]),
+                    U=U.ctypes.data, f=keep["f"].ctypes.data,
+                    GGT=(C.c_double * 9)(*np.asarray(GGT, np.float64).reshape(9)), cell_size=cell_size,
+                    nk_full=nk_full, temperature=temperature, eps_background=eps_background, meff=meff,
+                    formula=SCREEN[formula] if isinstance(formula, str) else int(formula), nfree=nfree,
+                    update_screening=int(update_screening), nv=int(nv), degauss=degauss, ethr=ethr,
+                    antisymmetry=int(antisymmetry), scale=scale, every_rhs=int(every_rhs))
+        self._ck(_lib().dmd_ee_attach(self._h, C.byref(d)))
+
+    def ee_update(self):
+        """Rebuild P_ee from the handle's state at its time (dmd_ee_update)."""
+        self._ck(_lib().dmd_ee_update(self._h))
+
+    def ee_read(self):
+        """(P1ee, P2ee complex [npair][nb^4], screening density) of the last rebuild."""
+        P1 = np.empty((self.npair, self.nb4), np.complex128)
+        P2 = np.empty((self.npair, self.nb4), np.complex128)
+        n = C.c_double()
+        self._ck(_lib().dmd_ee_read(self._h, P1.ctypes.data, P2.ctypes.data, C.byref(n)))
+        return P1, P2, n.value
 
     # ------------------------------------------------------------------ plumbing
     def _ck(self, st):

@@ -59,6 +59,9 @@ extern "C" {
                               f_ref (the f_eq of the linearization) is required */
 #define DMD_FLAG_ADJOINT 2u /* keep the pair operators in their stored order as well, for dmd_adjoint_rk4
                                (one extra copy of P on the device; single state only) */
+#define DMD_FLAG_EE 4u      /* keep the operators P_eph (+ P_eimp) in their stored order and the
+                               column-block map, for the e-e model (dmd_ee_attach); single state,
+                               not linearized, operators given as arrays */
 
 /* pictures (alg.picture) */
 #define DMD_PICTURE_INTERACTION 0
@@ -192,6 +195,50 @@ int dmd_group_destroy(dmd_group* g);
  * raises the device error flag; *status receives what the steppers would return then
  * (DMD_E_TIMEOUT) and the call checks that the context still runs a kernel afterwards. */
 int dmd_selftest_wait_timeout(int device, uint32_t polls, int* status);
+
+/* ---- e-e scattering rebuilt from the density matrix (eeMode = Pee_update) ------------------------
+ * The e-e operators P_ee(rho) of elecelec_model::calc_P (ElecElec_Model.h:186-262) for every stored
+ * k-pair, with the static screened Coulomb interaction of coulomb_model::vq (Coulomb_Model.h:632-660),
+ * are added to the handle's operators: P = P_eph (+ P_eimp) + scale P_ee (ElectronPhonon.cpp:44-113).
+ * dmd_ee_attach replaces electronphonon::set_eph's e-e contribution (ElectronPhonon.cpp:12: P_ee at the
+ * equilibrium occupations with the set-up screening density); dmd_ee_update replaces reset_scatt's
+ * e-e update (ElectronPhonon.cpp:15-42, called by update_scatt_outside, DensityMatrix_Dynamics.h:290-
+ * 299) on the handle's state; with every_rhs the update runs on the device before every RHS
+ * evaluation, inside the captured RK4 step as well (update_scatt_inside, DensityMatrix_Dynamics.h:
+ * 280-289). Requires a handle made with DMD_FLAG_EE and nb = 2 or 4. */
+#define DMD_SCREEN_UNSCREENED 0 /* clp.scrFormula = "unscreened" */
+#define DMD_SCREEN_DEBYE 1      /* "debye" */
+#define DMD_SCREEN_BECHSTEDT 2  /* "Bechstedt" */
+
+typedef struct dmd_ee_desc {
+  int32_t nbw;              /* Wannier functions (elec->nb_wannier) */
+  const double* kvec;       /* [nk][3] fractional k-points (ldbd_kvec.bin) */
+  int32_t kmesh[3];         /* elec->kmesh */
+  const double* U;          /* complex128 [nk][nbw][nb]: the window's columns of U (ldbd_Umat.bin) */
+  const double* f;          /* [nk][nb] window occupations of the set-up (coul_model->f) */
+  double GGT[9];            /* reciprocal metric, row-major (lattice.h:41-42) */
+  double cell_size;         /* latt->cell_size */
+  double nk_full;           /* elec->nk_full */
+  double temperature;       /* Hartree */
+  double eps_background;    /* clp.eps (epsilon_background) */
+  double meff;              /* clp.meff (meff_screening) */
+  int32_t formula;          /* DMD_SCREEN_* */
+  double nfree;             /* screening density of the set-up (clp.nfreetot), bohr^-dim */
+  int32_t update_screening; /* clp.update: the density from rho's diagonal at each update */
+  int32_t nv;               /* window bands below nv are valence (holes) in that density */
+  double degauss;           /* eep.degauss (degauss_ee) */
+  double ethr;              /* energy-conservation window: degauss * ndegauss (param) */
+  int32_t antisymmetry;     /* eep.antisymmetry: the exchange term */
+  double scale;             /* scale_ee */
+  int32_t every_rhs;        /* freq_update_ee_model < 0: update before every RHS evaluation */
+} dmd_ee_desc;
+
+int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee);
+/* Update from the handle's state at its time (set_state / after stepping). */
+int dmd_ee_update(dmd_handle* h);
+/* The last P_ee (complex128 [npair][nb^4] each, prefactor included, scale not; either may be NULL)
+ * and the screening density it used (may be NULL). */
+int dmd_ee_read(dmd_handle* h, double* P1ee, double* P2ee, double* nfree);
 
 /* No counterpart in the reference. Shape autotuner: times every compiled shape variant of the
  * handle's contraction (f64x, nb = 2: lines per stage, ring depth, CTAs per SM; CUDA-core batches:

