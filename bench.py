@@ -607,6 +607,142 @@ def run_temperatures(args):
     print(json.dumps(line))
 
 
+def ee_survivors(st, kidx, table, n, ethr, pairs):
+    """(k1, k2, k3) with k4 = k1 + k3 - k2 on the k-point set and some band combination inside the
+    energy window (the reference's calc_P work items), counted for the given pairs"""
+    ew = st.ew
+    nk = ew.shape[0]
+    cnt = 0
+    for p in pairs:
+        k1, k2 = int(st.k1[p]), int(st.k2[p])
+        m = (kidx[k1][None, :] + kidx - kidx[k2][None, :]) % n
+        k4 = table[m[:, 0], m[:, 1], m[:, 2]]
+        ok = k4 >= 0
+        k3 = np.nonzero(ok)[0]
+        k4 = k4[ok]
+        de = (ew[k1][:, None, None, None] - ew[k2][None, :, None, None])[None] + \
+             (ew[k3][:, None, :, None] - ew[k4][:, None, None, :])[:, None]
+        cnt += int(np.any(np.abs(de.reshape(k3.size, -1)) < ethr, axis=1).sum())
+    return cnt
+
+
+def run_ee(args):
+    """e-e operators rebuilt from rho (eeMode = Pee_update, Debye screening updated from rho): the
+    rebuild alone (P_ee of every pair from the state, refill of the stored operators) and RK4 with the
+    rebuild before every RHS evaluation, on a ball of k-points of a GaAs-like mesh."""
+    from denmat_dynm_development_gb300 import host as H
+    from denmat_dynm_development_gb300.dmd import LindbladGPU
+    nb, nbw = 2, 4
+    cfg = S.SynthConfig(nk=args.ee_nk, nb=nb, seed=51, de_pair_mev=args.ee_de_mev, nwannier=nbw, kball=True)
+    t0 = time.time()
+    st, P1, P2, _, _ = S.generate_arrays(cfg, procs=max(1, min(16, os.cpu_count() or 1)))
+    gen_s = time.time() - t0
+    T, mu = st.T, st.mu
+    e = np.ascontiguousarray(st.e)
+    f = H.fermi(T, mu, e)
+    dm0 = H.dm_bpert(st.s, e, f, T, np.array([0.0, 0.0, 0.1 * U.Tesla2au]), 0.0, 0)
+    nk_full, V, n = float(st.n) ** 3, st.V, st.n
+    G = 2.0 * math.pi * np.linalg.inv(st.R)
+    degauss = cfg.degauss_mev * 1e-3 * U.eV
+    ee = dict(kvec=st.kf, kmesh=(n, n, n), U=S.umat(cfg, st.kf)[:, :, :nb], f=f, GGT=G @ G.T, cell_size=V,
+              nk_full=nk_full, temperature=T, eps_background=12.9, meff=0.3, formula="debye",
+              nfree=float(f.sum()) / (nk_full * V), update_screening=1, nv=0, degauss=degauss,
+              ethr=degauss * cfg.ndegauss, antisymmetry=0, scale=1.0, every_rhs=1)
+    prec = args.precision
+    g = LindbladGPU(nk=cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=e, k1st=st.k1, k2nd=st.k2, P1=P1, P2=P2,
+                    prefac_eph=2 * math.pi / nk_full, picture=0, expt=1, precision=prec, ee=ee)
+    y0 = np.ascontiguousarray(dm0).view(np.float64).reshape(-1)
+    g.set_state(0.0, y0)
+    for _ in range(args.warmup):
+        g.ee_update()
+    clk = ClockSampler(0)
+    clk.start()
+    g.sync()
+    l0 = g.launches
+    g.timer_start()
+    for _ in range(args.steps):
+        g.ee_update()
+    ms = g.timer_stop() / args.steps
+    clocks = clk.stop()
+    launches = g.launches - l0
+    g.set_profiling(True)
+    g.ee_update()
+    g.set_profiling(False)  # harvests the recorded events
+    reb_ms, reb_n = g.profile(4)
+    # RK4 with the rebuild before every stage (freq_update_ee_model < 0)
+    h = 1.0 * U.fs
+    nst = max(3, args.steps // 4)
+    g.rk4(h, args.warmup)
+    g.sync()
+    g.timer_start()
+    g.rk4(h, nst)
+    rk_ms = g.timer_stop() / nst
+    g.close()
+    # work items of the reference's loop (exact count on a pair sample, scaled), flops per item
+    kidx = np.rint(n * (st.kf - np.floor(st.kf))).astype(np.int64) % n
+    table = -np.ones((n, n, n), np.int64)
+    for k in range(cfg.nk - 1, -1, -1):
+        table[tuple(kidx[k])] = k
+    rng = np.random.default_rng(3)
+    sample = rng.choice(st.npair, size=min(st.npair, 400), replace=False)
+    surv = ee_survivors(st, kidx, table, n, ee["ethr"], sample) * st.npair / sample.size
+    flops_item = 8 * (nb * nb * nbw + 4 * nb ** 5 + 2 * nb ** 6) + 8 * nb ** 4
+    flops = surv * flops_item
+    peak = 1250.0
+    line = {"metric": "e-e operator rebuilds/s (P_ee of every k-pair from rho, Pee_update)", "value": 1e3 / ms,
+            "unit": "rebuilds/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "ee_ball_nk%d: nb=2, nk=%d (ball of a %d^3 mesh), %d k-pairs, %d Wannier functions, "
+                                   "Debye screening from rho, Lindblad e-e (ElecElec_Model.h:186-262)"
+                                   % (cfg.nk, cfg.nk, n, st.npair, nbw),
+                       "npair": st.npair, "nk": cfg.nk, "k3_candidates": st.npair * cfg.nk,
+                       "work_items_estimated": surv, "work_item_sample_pairs": int(sample.size),
+                       "l2": "per rebuild the operators (%.2f GB) are read and written; no flush" %
+                             (2 * st.npair * nb ** 4 * 16 * 2 / 1e9),
+                       "gen_s": gen_s},
+            "rk4_with_every_rhs_rebuild": {"steps_per_s": 1e3 / rk_ms, "ms_per_step": rk_ms, "precision": prec},
+            "roofline": {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GFLOP/s",
+                         "frac": flops / (ms * 1e-3) / 1e9 / peak, "traffic": None, "peak_kind": "nominal FP64",
+                         "kernel": "e-e rebuild (k_ee_pairs + refill)", "flops_per_work_item": flops_item,
+                         "profiled_rebuild_ms": reb_ms / max(reb_n, 1)},
+            "clocks": clocks, "gpu_launches": launches}
+    if args.cpu_baseline:
+        line["cpu_baseline"] = ee_cpu_baseline(st, P1, P2, e, f, ee, nb)
+    print(json.dumps(line))
+
+
+def ee_cpu_baseline(st, P1, P2, e, f, ee, nb):
+    """the oracle's calc_P restatement (one core) on a bounded sample of the pairs"""
+    from oracle import oracle as O
+    O.build()
+
+    order = np.random.default_rng(7).permutation(st.npair)
+
+    def timed(m):
+        idx = np.sort(order[:m])  # a random sample: the pairs' work varies along the stored order
+        s = O.from_arrays(nk=st.cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=e, f_dm=f, k1st=st.k1[idx], k2nd=st.k2[idx],
+                          P1=P1[idx], P2=P2[idx], prefac_eph=1.0, dm0=np.zeros((st.cfg.nk, nb * nb), np.complex128))
+        m_ = O.EEModel(nb=nb, kvec=ee["kvec"], kmesh=ee["kmesh"], U=ee["U"], GGT=ee["GGT"], cell_size=ee["cell_size"],
+                       nk_full=ee["nk_full"], T=ee["temperature"], eps=ee["eps_background"], meff=ee["meff"],
+                       formula=ee["formula"], nfree=ee["nfree"], update_screening=1, nv=0, degauss=ee["degauss"],
+                       ethr=ee["ethr"], antisym=0, scale=1.0, inside=0, P1base=P1[idx].reshape(-1),
+                       P2base=P2[idx].reshape(-1))
+        dmw = np.zeros((st.cfg.nk, nb * nb), np.complex128)
+        dmw[:, 0], dmw[:, 3] = f[:, 0], f[:, 1]
+        t0 = time.perf_counter()
+        O.ee_operators(s, m_, dmw, None, ee["nfree"])
+        return time.perf_counter() - t0
+
+    m = 50
+    dt = timed(m)
+    m2 = int(min(st.npair, max(m, m * 15.0 / max(dt, 1e-3))))
+    dt2 = timed(m2) if m2 > m else dt
+    pairs_s = m2 / dt2
+    return {"value": pairs_s / st.npair, "unit": "rebuilds/s", "cores": 1, "kind": "port",
+            "sample": "oracle calc_P restatement over %d random pairs of %d (all k3), %.1f s; scaled to a full "
+                      "rebuild" % (m2, st.npair, dt2)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -623,6 +759,9 @@ def main():
     ap.add_argument("--adjoint", action="store_true", help="adjoint configuration (gradients of S_z(t_f))")
     ap.add_argument("--temperatures", action="store_true", help="batched form over 8 temperature P sets")
     ap.add_argument("--adj-tf-ps", type=float, default=50.0, help="adjoint: t_f in ps")
+    ap.add_argument("--ee", action="store_true", help="e-e operators rebuilt from rho (Pee_update)")
+    ap.add_argument("--ee-nk", type=int, default=2000, help="e-e: k-points of the ball")
+    ap.add_argument("--ee-de-mev", type=float, default=20.0, help="e-e: pair energy window (meV)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)
@@ -639,6 +778,10 @@ def main():
     if args.temperatures:
         if rank == 0:
             run_temperatures(args)
+        return
+    if args.ee:
+        if rank == 0:
+            run_ee(args)
         return
     # the generator's worker processes start before any CUDA call
     w = build_workload(args.workload, max(1, min(16, (os.cpu_count() or 1) // max(world, 1))))

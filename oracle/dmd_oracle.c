@@ -433,13 +433,12 @@ static void ee_ikvec3(const orc_ee* ee, const double* k, int* v) {
   }
 }
 
-/* kIndexMap::findk (comm/kmap.cpp:3-10) over the k-points' mesh indices */
-static int ee_findk(const orc_ee* ee, int nk, const int* kidx, const double* k) {
+/* kIndexMap::findk (comm/kmap.cpp:3-10): the map from mesh indices to k as a dense table over the
+ * mesh, the first k-point of an index kept as std::map::insert keeps it (comm/kmap.h:22-28) */
+static int ee_findk(const orc_ee* ee, const int* table, const double* k) {
   int v[3];
   ee_ikvec3(ee, k, v);
-  for (int i = 0; i < nk; i++)
-    if (kidx[3 * i] == v[0] && kidx[3 * i + 1] == v[1] && kidx[3 * i + 2] == v[2]) return i;
-  return -1;
+  return table[((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2]];
 }
 
 /* elecelec_model::calc_ovlp -- ElecElec_Model.h:72-80: ovlp = U_ik^dagger U_jk (nb x nb), times
@@ -467,8 +466,15 @@ void orc_ee_P(const orc_ee* ee, const orc_sys* s, const zc* dm, const zc* dm1, c
   double* e = (double*)xmalloc(sizeof(double) * nk * nb);
   for (int ik = 0; ik < nk; ik++)
     for (int b = 0; b < nb; b++) e[ik * nb + b] = s->e_dm[(size_t)ik * nd + bs + b];
-  int* kidx = (int*)xmalloc(sizeof(int) * 3 * nk);
-  for (int ik = 0; ik < nk; ik++) ee_ikvec3(ee, ee->kvec + 3 * ik, kidx + 3 * ik);
+  const size_t nmesh = (size_t)ee->kmesh[0] * ee->kmesh[1] * ee->kmesh[2];
+  int* table = (int*)xmalloc(sizeof(int) * nmesh);
+  for (size_t i = 0; i < nmesh; i++) table[i] = -1;
+  for (int ik = 0; ik < nk; ik++) {
+    int v[3];
+    ee_ikvec3(ee, ee->kvec + 3 * ik, v);
+    int* slot = &table[((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2]];
+    if (*slot < 0) *slot = ik;
+  }
   zc *Uih = (zc*)xmalloc(sizeof(zc) * nb * ee->nbw), *o12 = (zc*)xmalloc(sizeof(zc) * nb2),
      *o34 = (zc*)xmalloc(sizeof(zc) * nb2), *o14 = (zc*)xmalloc(sizeof(zc) * nb2), *o32 = (zc*)xmalloc(sizeof(zc) * nb2),
      *mee = (zc*)xmalloc(sizeof(zc) * nb4), *mex = (zc*)xmalloc(sizeof(zc) * nb4), *A = (zc*)xmalloc(sizeof(zc) * nb4),
@@ -493,7 +499,7 @@ void orc_ee_P(const orc_ee* ee, const orc_sys* s, const zc* dm, const zc* dm1, c
       if (ee->antisym && ik1 == ik2 && ik2 == ik3) continue;
       double k4v[3];
       for (int d = 0; d < 3; d++) k4v[d] = ee->kvec[3 * ik1 + d] + ee->kvec[3 * ik3 + d] - ee->kvec[3 * ik2 + d];
-      const int ik4 = ee_findk(ee, nk, kidx, k4v);
+      const int ik4 = ee_findk(ee, table, k4v);
       if (ik4 < 0) continue;
       /* calc_delta (ElecElec_Model.h:164-184) */
       int conserved = 0;
@@ -567,7 +573,7 @@ void orc_ee_P(const orc_ee* ee, const orc_sys* s, const zc* dm, const zc* dm1, c
       P2o[i] = zmul(prefac, P2[i]);
     }
   }
-  free(e); free(kidx); free(Uih); free(o12); free(o34); free(o14); free(o32); free(mee); free(mex); free(A);
+  free(e); free(table); free(Uih); free(o12); free(o34); free(o14); free(o32); free(mee); free(mex); free(A);
   free(A1rho); free(A1rhobar); free(mtmp); free(P1); free(P2); free(delta);
 }
 
