@@ -220,6 +220,12 @@ struct dmdh_system {
   double carrier_gs[3] = {0, 0, 0};  // eip.carrier_bvk_gs, ne_bvk_gs, nh_bvk_gs (electron.h:155-157)
   std::vector<std::pair<std::vector<double>, std::vector<double>>> imp;  // impurity P x |n_i V| (linear mode)
   int nimp = 0;                      // number of impurity densities (eip.ni.size())
+  double nfree = 0;                  // clp.nfreetot = |ne| + |nh| of set_mu_and_n (electron.h:157)
+  // e-e model (eeMode): the descriptor for dmd_ee_attach and the arrays it points into
+  int ee = 0;                        // 1: Pee_update, 2: Pee_fixed_at_eq
+  int ee_freq = 0;                   // freq_update_ee_model (> 0: update between output steps)
+  std::vector<double> kvec, U, f_win;
+  dmd_ee_desc eed;
 };
 
 extern "C" {
@@ -354,8 +360,27 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
   if (sget(pm, "code", "jdftx") != "jdftx" || sget(pm, "material_model", "none") != "none")
     return err(DMD_E_ARG, "only code = jdftx, material_model = none");
   if (pget(pm, "laserA", pget(pm, "pumpA0", 0)) > 0) return err(DMD_E_ARG, "laser is not supported");
-  if (sget(pm, "eeMode", "none") != "none" || sget(pm, "scrMode", "none") != "none")
-    return err(DMD_E_ARG, "model e-e / screening is not supported");
+  const std::string ee_mode = sget(pm, "eeMode", "none"), scr_mode = sget(pm, "scrMode", "none");
+  if (ee_mode == "none" && scr_mode != "none") return err(DMD_E_ARG, "screening without the e-e model is not supported");
+  if (ee_mode != "none") {  // the e-e model (parameters.cpp:479-500, Scatt_Param.h:21-47)
+    if (ee_mode != "Pee_update" && ee_mode != "Pee_fixed_at_eq")
+      return err(DMD_E_ARG, "eeMode must be none, Pee_fixed_at_eq or Pee_update");
+    if (scr_mode != "medium") return err(DMD_E_ARG, "the e-e model needs scrMode = medium");
+    const std::string f = sget(pm, "scrFormula", "RPA");
+    if (f != "unscreened" && f != "debye" && f != "Bechstedt")
+      return err(DMD_E_ARG, "scrFormula " + f + " is not supported (unscreened, debye, Bechstedt are)");
+    if (sget(pm, "dynamic_screening", "static") != "static") return err(DMD_E_ARG, "only static screening is supported");
+    if (linear) return err(DMD_E_ARG, "the e-e model is not supported with alg_linearize");
+    if (pget(pm, "alg_ddmdteq", 0) != 0) return err(DMD_E_ARG, "the e-e model is not supported with alg_ddmdteq");
+    if (pget(pm, "alg_summode", 1) == 0) return err(DMD_E_ARG, "the e-e model needs alg_summode");
+    const double fe = pget(pm, "freq_update_ee_model", 0), fi = pget(pm, "freq_update_eimp_model", 0);
+    if (ee_mode == "Pee_update" && fe == 0)  // parameters.cpp:483-484
+      return err(DMD_E_ARG, "want to update Pee but set freq_update_ee_model as 0");
+    if (fi != fe)  // parameters.cpp:499-500
+      return err(DMD_E_ARG, "freq_update_eimp_model is the same as freq_update_ee_model in current version");
+    s->ee = ee_mode == "Pee_update" ? 1 : 2;
+    s->ee_freq = ee_mode == "Pee_update" && fe > 0 ? (int)fe : 0;
+  }
   if (sget(pm, "alg_scatt", "lindblad") != "lindblad") return err(DMD_E_ARG, "alg_scatt must be lindblad");
   if (pget(pm, "alg_eph_sepr_eh", 1) != 0 && pget(pm, "alg_eph_need_elec", 1) == 0)
     return err(DMD_E_ARG, "hole-only e-ph data is not supported");
@@ -460,6 +485,7 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
     const double ne = compute_nfree(false, T, in.mu, e.data(), nk, nb, nv) / nk_full / cell;
     const double nh = compute_nfree(true, T, in.mu, e.data(), nk, nb, nv) / nk_full / cell;
     const double nei = 0. / nk_full / cell, nhi = 0. / nk_full / cell;
+    s->nfree = fabs(ne) + fabs(nh);
     double gs = fabs(ne + nei) > fabs(nh + nhi) ? ne + nei : nh + nhi;
     s->carrier_gs[0] = gs * nk_full * cell;
     s->carrier_gs[1] = ne * nk_full * cell;
@@ -642,6 +668,73 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
     s->P2.swap(Lji);
     s->imp.clear();
   }
+  if (s->ee) {
+    // elecelec_model / coulomb_model inputs (ElecElec_Model.h:22-37, Coulomb_Model.h:415-424): the
+    // k-points and U (electron.cpp:134-146, 388-410; U's partial layout [nk][nb_wannier][nb_eph] is
+    // the one the reference reads, see its size check), the reciprocal metric (lattice.h:41-42)
+    int nbwan = 0;
+    if (sscanf(lines[1].c_str(), "%*d %*d %*d %*d %*d %*d %d", &nbwan) != 1 || nbwan < nbw)
+      return err(DMD_E_FILE, "ldbd_size.dat: nb_wannier");
+    s->kvec.resize((size_t)nk * 3);
+    s->U.resize((size_t)nk * nbwan * nbw * 2);
+    if (!read_file(dir + "/ldbd_data/ldbd_kvec.bin", s->kvec.size() * 8, s->kvec.data(), why) ||
+        !read_file(dir + "/ldbd_data/ldbd_Umat.bin", s->U.size() * 8, s->U.data(), why))
+      return err(DMD_E_FILE, why);
+    s->f_win.resize((size_t)nk * nbw);
+    for (int ik = 0; ik < nk; ik++)
+      for (int b = 0; b < nbw; b++) s->f_win[(size_t)ik * nbw + b] = s->f_dm[(size_t)ik * nb_dm + bs + b];
+    // GGT = Gvec Gvec^T, Gvec = 2 pi inv(R), inv = adjugate / det (comm/matrix3.h:248-284)
+    double adj[3][3], G[3][3];
+    const double c0[3] = {R[1][1] * R[2][2] - R[1][2] * R[2][1], R[1][2] * R[2][0] - R[1][0] * R[2][2],
+                          R[1][0] * R[2][1] - R[1][1] * R[2][0]};
+    const double c1[3] = {R[2][1] * R[0][2] - R[2][2] * R[0][1], R[2][2] * R[0][0] - R[2][0] * R[0][2],
+                          R[2][0] * R[0][1] - R[2][1] * R[0][0]};
+    const double c2[3] = {R[0][1] * R[1][2] - R[0][2] * R[1][1], R[0][2] * R[1][0] - R[0][0] * R[1][2],
+                          R[0][0] * R[1][1] - R[0][1] * R[1][0]};
+    const double det = R[0][0] * c0[0] + R[0][1] * c0[1] + R[0][2] * c0[2];
+    for (int i = 0; i < 3; i++) {
+      adj[i][0] = c0[i];
+      adj[i][1] = c1[i];
+      adj[i][2] = c2[i];
+    }
+    const double sdet = 1. / det;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) G[i][j] = (adj[i][j] * sdet) * (2. * M_PI);
+    dmd_ee_desc& ee = s->eed;
+    memset(&ee, 0, sizeof(ee));
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        double acc = 0;
+        for (int k = 0; k < 3; k++) acc += G[i][k] * G[j][k];
+        ee.GGT[i * 3 + j] = acc;
+      }
+    double degauss = 0, ndegauss = 0;
+    if (sscanf(lines[7].c_str(), "%lg %lg", &degauss, &ndegauss) != 2) return err(DMD_E_FILE, "ldbd_size.dat line 8");
+    degauss = pget(pm, "degauss", degauss / kEV, kEV);  // parameters.cpp:131-140
+    ndegauss = pget(pm, "ndegauss", ndegauss);
+    const std::string f = sget(pm, "scrFormula", "RPA");
+    ee.nbw = nbwan;
+    ee.kvec = s->kvec.data();
+    ee.kmesh[0] = km0;
+    ee.kmesh[1] = km1;
+    ee.kmesh[2] = km2;
+    ee.U = s->U.data();
+    ee.f = s->f_win.data();
+    ee.cell_size = cell;
+    ee.nk_full = nk_full;
+    ee.temperature = T;
+    ee.eps_background = pget(pm, "epsilon_background", 1);
+    ee.meff = pget(pm, "meff_screening", 1);
+    ee.formula = f == "unscreened" ? DMD_SCREEN_UNSCREENED : f == "debye" ? DMD_SCREEN_DEBYE : DMD_SCREEN_BECHSTEDT;
+    ee.nfree = s->nfree;
+    ee.update_screening = pget(pm, "update_screening", 1) != 0;
+    ee.nv = in.nv_dm - bs;  // coul_model->nv (Coulomb_Model.h:418)
+    ee.degauss = pget(pm, "degauss_ee", degauss / kEV, kEV);
+    ee.ethr = degauss * ndegauss;
+    ee.antisymmetry = pget(pm, "ee_antisymmetry", 0) != 0;
+    ee.scale = pget(pm, "scale_ee", scale_scatt);
+    ee.every_rhs = s->ee == 1 && pget(pm, "freq_update_ee_model", 0) < 0;
+  }
   // coherent Hamiltonian (main.cpp:51)
   const double Blen = sqrt(in.B[0] * in.B[0] + in.B[1] * in.B[1] + in.B[2] * in.B[2]);
   if (Blen > 1e-10) {
@@ -680,7 +773,7 @@ int dmdh_desc(const dmdh_system* s, int32_t precision, int32_t device, dmd_desc*
   d->expt = s->info.expt;
   d->precision = precision;
   d->device = device;
-  d->flags = s->info.linear ? DMD_FLAG_LINEAR : 0u;
+  d->flags = (s->info.linear ? DMD_FLAG_LINEAR : 0u) | (s->ee ? DMD_FLAG_EE : 0u);
   d->f_ref = s->f_eq.empty() ? s->f_dm.data() : s->f_eq.data();
   return DMD_OK;
 }
@@ -702,8 +795,19 @@ int dmdh_get_f_eq(const dmdh_system* s, double* f_eq) {
   return DMD_OK;
 }
 
+int dmdh_ee_desc(const dmdh_system* s, dmd_ee_desc* ee, int32_t* on) {
+  if (!s || !ee || !on) return DMD_E_ARG;
+  *on = s->ee ? 1 : 0;
+  if (s->ee) *ee = s->eed;
+  return DMD_OK;
+}
+
 int dmdh_prepare(const dmdh_system* s, dmd_handle* h) {
   if (!s || !h) return DMD_E_ARG;
+  if (s->ee) {  // electronphonon::set_eph's e-e term (ElectronPhonon.cpp:12)
+    const int rc = dmd_ee_attach(h, &s->eed);
+    if (rc) return err(rc, dmd_last_error(h));
+  }
   if (!s->info.ddmdteq) return dmd_set_ddmdt_eq(h, nullptr);
   // electronphonon::compute_ddmdt_eq (evolve_eph.cpp:3-19): the scattering term of diag(f_eq) at t = 0,
   // cut to the e-ph window; the stored drift is cleared first so that nothing is subtracted from it
@@ -844,6 +948,9 @@ extern "C" int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max) 
       break;
     }
     ti += in.tstep;
+    // update_scatt_outside (DensityMatrix_Dynamics.h:216-217, 290-299): the e-e operators from the
+    // state before every freq_update_ee_model-th step
+    if (s->ee_freq > 0 && (it - 1) % s->ee_freq == 0 && (rc = dmd_ee_update(h))) return err(rc, dmd_last_error(h));
     int64_t nfev = 0;
     if (in.ode_method == 0) rc = dmd_rkf45_apply(h, ti, &hs, in.ode_hmin, in.ode_hmax, in.ode_epsabs, 0.0, &nfev);
     else if (in.ode_method == 1) rc = dmd_euler(h, in.tstep, 1), nfev = 1;

@@ -124,7 +124,8 @@ class LindbladGPU:
 
     def __init__(self, *, nk, nb_dm, bstart, bend, e_dm, k1st, k2nd, P1, P2, prefac_eph, Hcoh=None,
                  picture="interaction", expt=1, precision="f64", P1_add=None, P2_add=None, add_scale=0.0, device=0,
-                 f_ref=None, linear=False, nrhs=1, adjoint=False, P_files=None, P_sparse=None, ee=None):
+                 f_ref=None, linear=False, nrhs=1, adjoint=False, P_files=None, P_sparse=None, ee=None,
+                 ee_flag=False):
         L = _lib()
         self._keep = dict(e=_c(e_dm, np.float64), k1=_c(k1st, np.uint64), k2=_c(k2nd, np.uint64),
                           P1=_c(P1, np.complex128), P2=_c(P2, np.complex128), H=_c(Hcoh, np.complex128),
@@ -136,7 +137,7 @@ class LindbladGPU:
                      P1_add=ptr(k["A1"]), P2_add=ptr(k["A2"]), add_scale=add_scale, Hcoh=ptr(k["H"]),
                      picture=PICTURE[picture] if isinstance(picture, str) else int(picture), expt=int(expt),
                      precision=PREC[precision] if isinstance(precision, str) else int(precision), device=device,
-                     flags=(FLAG_LINEAR if linear else 0) | (FLAG_ADJOINT if adjoint else 0) | (FLAG_EE if ee else 0),
+                     flags=(FLAG_LINEAR if linear else 0) | (FLAG_ADJOINT if adjoint else 0) | (FLAG_EE if (ee or ee_flag) else 0),
                      f_ref=ptr(k["f"]),
                      nrhs=int(nrhs))
         h = C.c_void_p()

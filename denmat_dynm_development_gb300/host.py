@@ -14,7 +14,7 @@ _L = None
 
 EXPORTS = ["dmdh_load", "dmdh_free", "dmdh_error", "dmdh_info_get", "dmdh_desc", "dmdh_get_dm0", "dmdh_get_f",
            "dmdh_get_smat", "dmdh_get_f_eq", "dmdh_prepare", "dmdh_param", "dmdh_fermi", "dmdh_dm_bpert",
-           "dmdh_H_BS", "dmdh_run"]
+           "dmdh_H_BS", "dmdh_run", "dmdh_ee_desc"]
 
 
 class Info(C.Structure):
@@ -46,6 +46,7 @@ def _lib():
         L.dmdh_get_smat.argtypes = [vp, vp]
         L.dmdh_get_f_eq.argtypes = [vp, vp]
         L.dmdh_prepare.argtypes = [vp, vp]
+        L.dmdh_ee_desc.argtypes = [vp, C.POINTER(_dmd._EEDesc), C.POINTER(C.c_int32)]
         L.dmdh_param.argtypes = [vp, C.c_char_p, d, C.POINTER(d), C.POINTER(C.c_int)]
         L.dmdh_fermi.argtypes = [d, d, vp, vp, C.c_size_t]
         L.dmdh_dm_bpert.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, d, vp, d, C.c_int32, vp]
@@ -98,6 +99,18 @@ class System:
         self.P1 = _arr(desc.P1, n4, np.complex128)
         self.P2 = _arr(desc.P2, n4, np.complex128)
         self.Hcoh = _arr(desc.Hcoh, i.nk * nd2, np.complex128).reshape(i.nk, nd2) if desc.Hcoh else None
+        # the e-e model (eeMode), as dmdh_prepare will attach it
+        ed, on = _dmd._EEDesc(), C.c_int32()
+        _ck(_lib().dmdh_ee_desc(h, C.byref(ed), C.byref(on)))
+        self.ee = None
+        if on.value:
+            self.ee = dict(kvec=_arr(ed.kvec, i.nk * 3, np.float64).reshape(i.nk, 3), kmesh=tuple(ed.kmesh),
+                           U=_arr(ed.U, i.nk * ed.nbw * nb, np.complex128).reshape(i.nk, ed.nbw, nb),
+                           f=_arr(ed.f, i.nk * nb, np.float64).reshape(i.nk, nb), GGT=np.array(ed.GGT[:]),
+                           cell_size=ed.cell_size, nk_full=ed.nk_full, temperature=ed.temperature,
+                           eps_background=ed.eps_background, meff=ed.meff, formula=ed.formula, nfree=ed.nfree,
+                           update_screening=ed.update_screening, nv=ed.nv, degauss=ed.degauss, ethr=ed.ethr,
+                           antisymmetry=ed.antisymmetry, scale=ed.scale, every_rhs=ed.every_rhs)
 
     def desc(self, precision="f64", device=0):
         d = _dmd._Desc()
@@ -114,13 +127,14 @@ class System:
         return v.value if f.value else None
 
     def gpu(self, precision="f64", device=0):
-        """A LindbladGPU built from this system (dmd_create on the loaded arrays), with the
-        equilibrium drift installed when alg_ddmdteq is on (dmdh_prepare)."""
+        """A LindbladGPU built from this system (dmd_create on the loaded arrays), with the e-e model
+        attached and the equilibrium drift installed when param.in asks for them (dmdh_prepare)."""
         i = self.info
         g = _dmd.LindbladGPU(nk=i.nk, nb_dm=i.nb_dm, bstart=i.bstart, bend=i.bend, e_dm=self.e_dm,
                              k1st=self.k1st, k2nd=self.k2nd, P1=self.P1, P2=self.P2, prefac_eph=i.prefac_eph,
                              Hcoh=self.Hcoh, picture=i.picture, expt=i.expt, precision=precision, device=device,
-                             f_ref=self.f_eq if self.f_eq is not None else self.f_dm, linear=bool(i.linear))
+                             f_ref=self.f_eq if self.f_eq is not None else self.f_dm, linear=bool(i.linear),
+                             ee_flag=self.ee is not None)
         try:
             _ck(_lib().dmdh_prepare(self._h, g._h))
         except Exception:

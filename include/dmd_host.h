@@ -62,10 +62,14 @@ int dmdh_get_f(const dmdh_system* s, double* f);
 int dmdh_get_smat(const dmdh_system* s, double* smat);
 /* equilibrium occupations f_eq (double [nk][nb_dm]); DMD_E_ARG unless alg_ddmdteq */
 int dmdh_get_f_eq(const dmdh_system* s, double* f_eq);
-/* Per-handle set-up after dmd_create: with alg_ddmdteq, computes the equilibrium drift on the GPU
+/* Per-handle set-up after dmd_create: attaches the e-e model of param.in (dmd_ee_attach); with
+ * alg_ddmdteq, computes the equilibrium drift on the GPU
  * (electronphonon::compute_ddmdt_eq, evolve_eph.cpp:3-19, via dmd_evolve_driver at t = 0) and
  * installs it with dmd_set_ddmdt_eq; otherwise clears it. */
 int dmdh_prepare(const dmdh_system* s, dmd_handle* h);
+/* The e-e model of param.in (eeMode = Pee_update or Pee_fixed_at_eq with static screening) as the
+ * descriptor dmdh_prepare passes to dmd_ee_attach (pointers into s); *on = 0 without one. */
+int dmdh_ee_desc(const dmdh_system* s, dmd_ee_desc* ee, int32_t* on);
 
 /* value of a param.in key after get()'s unit conversion; returns 0 and *found = 1 if present */
 int dmdh_param(const dmdh_system* s, const char* key, double unit, double* value, int* found);

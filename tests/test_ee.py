@@ -174,3 +174,32 @@ def test_ee_larger_random_case_vs_oracle(oracle, built, tmp_path):
     print("nk120 npair %d: P_ee rel err %.3g %.3g, nfree %.17g vs %.17g" % (s.npair, e1, e2, n, s.ee.nfree))
     assert e1 < P_TOL and e2 < P_TOL
     assert abs(n - s.ee.nfree) <= 1e-14 * abs(s.ee.nfree)
+
+
+@pytest.mark.parametrize("case", EE_CASES)
+def test_ee_host_library_rkf45_vs_golden_gsl(case, oracle, built):
+    """The host library path (dmdh_load of param.in with eeMode = Pee_update, dmdh_prepare attaching
+    the model) through DMD's evolve_gsl loop: S_z per output interval, the final state and the RHS
+    calls per interval equal the reference's evolve_gsl with the rebuild before every evaluation."""
+    from denmat_dynm_development_gb300 import host
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = oracle.load(d)
+    hs_sys = host.System(d)
+    with hs_sys.gpu("f64") as gpu:
+        gpu.set_state(s.t0, oracle.y_of(s.dm0))
+        gpu.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
+        hs, ti, tcur = s.ode["hstart"], s.t0, s.t0
+        sz, nf = [], []
+        while tcur < s.tend:
+            ti += s.tstep
+            hs, n = gpu.rkf45_apply(ti, hs, s.ode["hmin"], s.ode["hmax"], s.ode["epsabs"], 0.0)
+            tcur, _ = gpu.get_state()
+            sz.append(gpu.measure(0, s.nv_dm)[0])
+            nf.append(n)
+        _, y = gpu.get_state()
+    hs_sys.close()
+    e = rel(np.array(sz), g["gsl_sz"][1:, 1])
+    print("%s: RKF45 S_z rel err %.3g, state %.3g, ncalls %s" % (case, e, rel(y, g["gsl_y"]), nf))
+    assert rel(y, g["gsl_y"]) < 1e-10 and e < 1e-10
+    np.testing.assert_array_equal(np.array(nf), g["gsl_ncalls"])

@@ -6,7 +6,7 @@ import shutil
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, FIXED_P_CASES, ROOT
+from conftest import EE_CASES, FIXED_P_CASES, GOLDEN, ROOT
 
 
 @pytest.fixture(scope="module")
@@ -115,3 +115,41 @@ def test_setup_pieces_match_oracle(host, oracle):
     Bp = np.array([0.05, 0.0, 0.1]) * oracle.Tesla2au
     dm = host.dm_bpert(o.smat, o.e_dm, o.f_dm, o.temperature, Bp, 0.0, 0)
     np.testing.assert_array_equal(dm, o.dm0)
+
+
+@pytest.mark.parametrize("case", EE_CASES)
+def test_load_ee_model_matches_reference_setup(case, host, oracle):
+    """e-e cases: the host library's e-e descriptor (what dmdh_prepare attaches) equals the reference's
+    set-up values (screening density, reciprocal metric, windows) and the oracle's inputs; the base
+    operators are P_eph (+ P_eimp) before the e-e term."""
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    meta = dict(zip(g["meta_keys"], g["meta_vals"]))
+    s = host.System(d)
+    o = oracle.load(d)
+    ee = s.ee
+    assert ee is not None
+    assert ee["nfree"] == meta["ee_nfree"]
+    np.testing.assert_array_equal(ee["GGT"], [meta["ee_ggt%d%d" % (i, j)] for i in range(3) for j in range(3)])
+    assert ee["degauss"] == meta["ee_degauss"] and ee["ethr"] == meta["ee_ethr"]
+    assert ee["eps_background"] == meta["ee_eps"] and ee["meff"] == meta["ee_meff"]
+    assert ee["temperature"] == meta["ee_T"] and ee["nv"] == int(meta["ee_nv"])
+    assert ee["antisymmetry"] == int(meta["ee_antisym"]) and ee["scale"] == meta["ee_scale"]
+    assert ee["every_rhs"] == 1 and ee["formula"] == o.ee.formula and ee["update_screening"] == o.ee.update_screening
+    np.testing.assert_array_equal(ee["U"], o.ee.U)
+    np.testing.assert_array_equal(ee["kvec"], o.ee.kvec)
+    np.testing.assert_array_equal(ee["f"], g["f_dm"][:, o.bstart:o.bend])
+    np.testing.assert_array_equal(s.P1, o.ee.P1base.reshape(s.P1.shape))
+    np.testing.assert_array_equal(s.P2, o.ee.P2base.reshape(s.P2.shape))
+    np.testing.assert_array_equal(s.dm0, g["dm0"])
+
+
+def test_ee_options_outside_the_path_are_rejected(host, tmp_path):
+    for extra, msg in [("scrFormula = RPA\n", "scrFormula RPA"), ("dynamic_screening = ppa\n", "static"),
+                       ("alg_ddmdteq = 1\n", "alg_ddmdteq"), ("freq_update_eimp_model = 3\n", "freq_update_eimp_model")]:
+        dst = str(tmp_path / ("c%d" % len(msg)))
+        shutil.copytree(os.path.join(GOLDEN, "ee_nb2_debye"), dst)
+        with open(os.path.join(dst, "param.in"), "a") as f:
+            f.write(extra)
+        with pytest.raises(RuntimeError, match=msg):
+            host.System(dst)
