@@ -83,6 +83,8 @@ struct dmd_handle {
   double* d_ee_f = nullptr;
   double2* d_ee_dm = nullptr;
   double2* d_ee_dm1 = nullptr;
+  float4* d_ee_dmf = nullptr;
+  float4* d_ee_dm1f = nullptr;
   dmd::EeScreen* d_ee_scr = nullptr;
   double2* d_ee_Pee = nullptr;
   float2* d_x0y0 = nullptr;    // tensor-core form: contraction of diag(f_ref), back-transformed, by k
@@ -1124,7 +1126,7 @@ void release(dmd_handle* h) {
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
                   h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0, h->d_Praw, h->d_kkraw,
                   h->d_dst, h->d_ee_kvec, h->d_ee_kidx, h->d_ee_kmap, h->d_ee_U, h->d_ee_erng, h->d_ee_f,
-                  h->d_ee_dm, h->d_ee_dm1, h->d_ee_scr, h->d_ee_Pee};
+                  h->d_ee_dm, h->d_ee_dm1, h->d_ee_dmf, h->d_ee_dm1f, h->d_ee_scr, h->d_ee_Pee};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -1151,17 +1153,23 @@ int ee_rebuild(dmd_handle* h, const double2* y, const TimeArg& ta, bool eq) {
   EeArgs a = h->ee_args;
   if (!eq) {  // the window density matrix of y in the Schrodinger picture
     k_ee_dm<NB><<<blocks_for((long long)h->nk * NB2, 256), 256, 0, h->st>>>(
-        h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->picture == DMD_PICTURE_INTERACTION ? 1 : 0, h->d_ee_dm, h->d_ee_dm1);
+        h->nk, h->nbdm, h->bs, y, h->d_ew, ta, h->picture == DMD_PICTURE_INTERACTION ? 1 : 0, h->d_ee_dm, h->d_ee_dm1,
+        h->d_ee_dmf, h->d_ee_dm1f);
     a.dm = h->d_ee_dm;
     a.dm1 = h->d_ee_dm1;
+    a.dmf = h->d_ee_dmf;
+    a.dm1f = h->d_ee_dm1f;
     a.f = nullptr;
   } else {  // the set-up: occupations instead of rho (calc_A1f, calc_A1fbar)
     a.dm = a.dm1 = nullptr;
+    a.dmf = a.dm1f = nullptr;
     a.f = h->d_ee_f;
   }
   k_ee_screen<<<1, 256, 0, h->st>>>(h->nk, NB, h->ee_nv, h->d_ee_dm, (!eq && h->ee_update) ? 1 : 0, h->ee_nfree0,
                                     h->ee_nkfull, h->ee_cell, h->ee_eps, h->ee_T, h->ee_meff, h->d_ee_scr);
-  k_ee_pairs<NB><<<(unsigned)((h->npair + 3) / 4), 128, 0, h->st>>>(a);
+  // FP64 handles contract in FP64, the others in double-float on the FP32 pipes
+  if (h->prec == DMD_PREC_F64) k_ee_pairs<NB, EeF64><<<(unsigned)((h->npair + 3) / 4), 128, 0, h->st>>>(a);
+  else k_ee_pairs<NB, EeDF><<<(unsigned)((h->npair + 3) / 4), 128, 0, h->st>>>(a);
   const bool dev = deviation_form(h->prec) && !h->lin;
   if (dev && cudaMemsetAsync(h->d_acc0, 0, (size_t)h->nk * 2 * NB2 * sizeof(double2), h->st) != cudaSuccess)
     return fail(h, DMD_E_CUDA, "e-e refill");
@@ -2446,6 +2454,7 @@ int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
       (rc = dalloc(h, &h->d_ee_kmap, nmesh)) || (rc = dalloc(h, &h->d_ee_U, (size_t)nk * ee->nbw * nb)) ||
       (rc = dalloc(h, &h->d_ee_erng, (size_t)nk)) || (rc = dalloc(h, &h->d_ee_f, (size_t)nk * nb)) ||
       (rc = dalloc(h, &h->d_ee_dm, (size_t)nk * h->nb2)) || (rc = dalloc(h, &h->d_ee_dm1, (size_t)nk * h->nb2)) ||
+      (rc = dalloc(h, &h->d_ee_dmf, (size_t)nk * h->nb2)) || (rc = dalloc(h, &h->d_ee_dm1f, (size_t)nk * h->nb2)) ||
       (rc = dalloc(h, &h->d_ee_scr, 1)) || (rc = dalloc(h, &h->d_ee_Pee, (size_t)h->npair * 2 * h->nb4)))
     return rc;
   CK(cudaMemcpy(h->d_ee_kvec, ee->kvec, (size_t)nk * 3 * 8, cudaMemcpyHostToDevice));

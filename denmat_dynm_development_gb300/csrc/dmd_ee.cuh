@@ -18,11 +18,15 @@
 // the candidates to a warp buffer. Phase 2: groups of G = 2 nb^2 lanes take one candidate each
 // (4 groups for nb = 2, one for nb = 4); lane (w, r), r = (i1, i3), builds one row of A into shared
 // memory, then forms its own A1rho (w = 0) or A1rhobar (w = 1) row and accumulates P1ee or P2ee
-// over (i2, i4) in registers. The groups' partial sums are added with shuffles at the end. FP64
-// throughout (FMA in the contractions).
+// over (i2, i4) in registers. The groups' partial sums are added with shuffles at the end. The
+// candidate search, the overlaps, delta and A are FP64; the two contractions (A1rho and the
+// accumulation, 90 % of the multiply-adds) are FP64 for FP64 handles and double-float (FP32 pairs,
+// ~2^-47 per product, renormalised after every work item) otherwise: GB300's FP32 pipes run them at
+// several times the FP64 rate.
 #pragma once
 #include "dmd_common.cuh"
 #include "dmd_kernels.cuh"
+#include "dmd_pairs_cb.cuh"
 
 namespace dmd {
 
@@ -48,6 +52,8 @@ struct EeArgs {
   const double2* erng;               // [nk] (min, max) of the window energies
   const double2* dm;                 // [nk][nb^2] window density matrix (Schrodinger picture), or null
   const double2* dm1;                // [nk][nb^2] 1 - dm
+  const float4* dmf;                 // the same as double-floats (re_h, re_l, im_h, im_l)
+  const float4* dm1f;
   const double* f;                   // [nk][nb] occupations when dm is null
   const EeScreen* scr;
   double2* Pee;                      // [npair][2][nb^4]: P1ee, P2ee (prefactor included)
@@ -91,9 +97,15 @@ __device__ __forceinline__ double2 ee_ovlp(const EeArgs& a, int ki, int kj, int 
 // the window density matrix in the Schrodinger picture and 1 - rho from the state y (one thread per
 // (k, i, j) of the window): electronphonon::reset_scatt's window copy (ElectronPhonon.cpp:19-28)
 // and add_scatt_contrib's conversion (ElectronPhonon.cpp:56-66)
+__device__ __forceinline__ float4 split_dfc(double2 v) {
+  const float2 a = split_df1(v.x), b = split_df1(v.y);
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+
 template <int NB>
 __global__ void k_ee_dm(int nk, int nbdm, int bs, const double2* __restrict__ y, const double* __restrict__ ew,
-                        TimeArg ta, int interaction, double2* __restrict__ dm, double2* __restrict__ dm1) {
+                        TimeArg ta, int interaction, double2* __restrict__ dm, double2* __restrict__ dm1,
+                        float4* __restrict__ dmf, float4* __restrict__ dm1f) {
   constexpr int NB2 = NB * NB;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nk * NB2) return;
@@ -105,15 +117,113 @@ __global__ void k_ee_dm(int nk, int nbdm, int bs, const double2* __restrict__ y,
     const double* ek = ew + (size_t)k * NB;
     v = cmul_rn(v, ccis((ek[hi_j] - ek[lo_i]) * t));
   }
+  double2 d, d1;
   if (i == j) {  // zhemm reads the diagonal as real (BLAS ZHEMM)
-    dm[idx] = mk2(v.x, 0.0);
-    dm1[idx] = mk2(1.0 - v.x, 0.0);
+    d = mk2(v.x, 0.0);
+    d1 = mk2(1.0 - v.x, 0.0);
   } else {
-    const double2 u = i < j ? v : cconj(v);  // lower = conj(upper)
-    dm[idx] = u;
-    dm1[idx] = mk2(-u.x, -u.y);
+    d = i < j ? v : cconj(v);  // lower = conj(upper)
+    d1 = mk2(-d.x, -d.y);
   }
+  dm[idx] = d;
+  dm1[idx] = d1;
+  dmf[idx] = split_dfc(d);
+  dm1f[idx] = split_dfc(d1);
 }
+
+// exp(x) for x <= 0 as a double-float: Cody-Waite reduction x = k ln2 + r in FP64 (ln2 in two
+// parts), |r| <= ln2/2, then exp(r) from its Taylor series to degree 13 in double-float by Horner's
+// rule (truncation below 2e-17 relative) and the scaling by 2^k. Below x = -80 the FP32 exponent
+// range of the low part ends and the FP64 value is split instead.
+__device__ __forceinline__ float2 df_exp_neg(double x) {
+  if (x < -80.0) return split_df1(exp(x));
+  const double k = rint(x * 1.4426950408889634);
+  double r = fma(-k, 6.93147180369123816490e-01, x);  // ln2 high part (trailing bits zero)
+  r = fma(-k, 1.90821492927058770002e-10, r);         // ln2 - high part
+  const float2 rr = split_df1(r);
+  // 1/n! for n = 13 .. 0 as (hi, lo)
+  float ph = (float)(1.0 / 6227020800.0), pl = (float)(1.0 / 6227020800.0 - (double)(float)(1.0 / 6227020800.0));
+  const double inv[13] = {1.0 / 479001600.0, 1.0 / 39916800.0, 1.0 / 3628800.0, 1.0 / 362880.0, 1.0 / 40320.0,
+                          1.0 / 5040.0,      1.0 / 720.0,      1.0 / 120.0,     1.0 / 24.0,     1.0 / 6.0,
+                          0.5,               1.0,              1.0};
+#pragma unroll
+  for (int n = 0; n < 13; ++n) {
+    float h, l;
+    df_mul(h, l, ph, pl, rr.x, rr.y);
+    df_renorm(h, l);
+    const float ch = (float)inv[n], cl = (float)(inv[n] - (double)(float)inv[n]);
+    df_add(h, l, ch, cl);
+    ph = h;
+    pl = l;
+  }
+  df_renorm(ph, pl);
+  const int ki = (int)k;
+  return make_float2(ldexpf(ph, ki), ldexpf(pl, ki));
+}
+
+// complex arithmetic of the two contractions: FP64, or double-float on the FP32 pipes
+struct EeF64 {
+  static constexpr bool kDF = false;
+  typedef double2 c;
+  static __device__ __forceinline__ c zero() { return mk2(0, 0); }
+  static __device__ __forceinline__ c from(double2 v) { return v; }
+  static __device__ __forceinline__ c load(const double2* d, const float4*, size_t i) { return d[i]; }
+  static __device__ __forceinline__ void mac(c& acc, c x, c y) { acc = cfma(x, y, acc); }  // acc += x y
+  static __device__ __forceinline__ void mac_conj(c& acc, c x, c y) {                      // acc += x conj(y)
+    acc = mk2(fma(x.x, y.x, fma(x.y, y.y, acc.x)), fma(x.y, y.x, fma(-x.x, y.y, acc.y)));
+  }
+  static __device__ __forceinline__ c scale(c x, double s) { return mk2(x.x * s, x.y * s); }
+  static __device__ __forceinline__ void renorm(c&) {}
+  static __device__ __forceinline__ double2 value(c v) { return v; }
+};
+
+struct EeDF {
+  static constexpr bool kDF = true;
+  typedef float4 c;  // (re_h, re_l, im_h, im_l)
+  static __device__ __forceinline__ c zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+  static __device__ __forceinline__ c from(double2 v) { return split_dfc(v); }
+  static __device__ __forceinline__ c load(const double2*, const float4* f, size_t i) { return f[i]; }
+  static __device__ __forceinline__ void mac(c& a, c x, c y) {
+    df_mac(a.x, a.y, x.x, x.y, y.x, y.y);
+    df_mac(a.x, a.y, -x.z, -x.w, y.z, y.w);
+    df_mac(a.z, a.w, x.x, x.y, y.z, y.w);
+    df_mac(a.z, a.w, x.z, x.w, y.x, y.y);
+  }
+  static __device__ __forceinline__ void mac_conj(c& a, c x, c y) {
+    df_mac(a.x, a.y, x.x, x.y, y.x, y.y);
+    df_mac(a.x, a.y, x.z, x.w, y.z, y.w);
+    df_mac(a.z, a.w, x.z, x.w, y.x, y.y);
+    df_mac(a.z, a.w, -x.x, -x.y, y.z, y.w);
+  }
+  static __device__ __forceinline__ c scale(c x, double s) {
+    const float2 v = split_df1(s);
+    c r;
+    df_mul(r.x, r.y, x.x, x.y, v.x, v.y);
+    df_mul(r.z, r.w, x.z, x.w, v.x, v.y);
+    return r;
+  }
+  static __device__ __forceinline__ void renorm(c& a) {
+    df_renorm(a.x, a.y);
+    df_renorm(a.z, a.w);
+  }
+  static __device__ __forceinline__ double2 value(c v) { return mk2((double)v.x + (double)v.y, (double)v.z + (double)v.w); }
+  static __device__ __forceinline__ c mul(c x, c y) {  // x y
+    c r;
+    df_mul(r.x, r.y, x.x, x.y, y.x, y.y);
+    df_mac(r.x, r.y, -x.z, -x.w, y.z, y.w);
+    df_mul(r.z, r.w, x.x, x.y, y.z, y.w);
+    df_mac(r.z, r.w, x.z, x.w, y.x, y.y);
+    renorm(r);
+    return r;
+  }
+  static __device__ __forceinline__ c scale_df(c x, float2 s) {
+    c r;
+    df_mul(r.x, r.y, x.x, x.y, s.x, s.y);
+    df_mul(r.z, r.w, x.z, x.w, s.x, s.y);
+    renorm(r);
+    return r;
+  }
+};
 
 // screening density and constants (one block): with update, nfree = sum over k and window bands of
 // the electron (or, below nv, hole) occupations / (nk_full cell_size) (Coulomb_Model.h:533-553)
@@ -153,18 +263,19 @@ __global__ void k_ee_screen(int nk, int nb, int nv, const double2* __restrict__ 
   }
 }
 
-template <int NB>
+template <int NB, typename V>
 struct EeSmem {
   static constexpr int NB2 = NB * NB, NB4 = NB2 * NB2, G = 2 * NB2, NG = 32 / G;
-  double2 o12[NB2];
-  double2 o34[NG][NB2], o14[NG][NB2], o32[NG][NB2];
-  double2 A[NG][NB4];
+  typename V::c o12[NB2];  // the overlaps in the contraction's arithmetic
+  typename V::c o34[NG][NB2], o14[NG][NB2], o32[NG][NB2];
+  typename V::c A[NG][NB4];
   int2 cand[64];
 };
 
-template <int NB>
+template <int NB, typename V = EeF64>
 __global__ void __launch_bounds__(128) k_ee_pairs(EeArgs a) {
-  typedef EeSmem<NB> S;
+  typedef EeSmem<NB, V> S;
+  typedef typename V::c C;
   constexpr int NB2 = S::NB2, NB4 = S::NB4, G = S::G, NG = S::NG;
   __shared__ S smem_all[4];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -183,11 +294,11 @@ __global__ void __launch_bounds__(128) k_ee_pairs(EeArgs a) {
   if (lane < NB2) {  // o12 = vq(k1 - k2) U_k1^dag U_k2
     const double vq = ee_vq(a, scr, k1, k2);
     const double2 o = ee_ovlp<NB>(a, k1, k2, lane / NB, lane % NB);
-    sm.o12[lane] = mk2(vq * o.x, vq * o.y);
+    sm.o12[lane] = V::from(mk2(vq * o.x, vq * o.y));
   }
-  double2 acc[NB2];
+  C acc[NB2];
 #pragma unroll
-  for (int e = 0; e < NB2; ++e) acc[e] = mk2(0, 0);
+  for (int e = 0; e < NB2; ++e) acc[e] = V::zero();
   const int4 i1v = a.kidx[k1], i2v = a.kidx[k2];
   const double2 r1 = a.erng[k1], r2 = a.erng[k2];
   const double* e1 = a.ew + (size_t)k1 * NB;
@@ -230,33 +341,44 @@ __global__ void __launch_bounds__(128) k_ee_pairs(EeArgs a) {
         // overlaps of this candidate: lanes w = 0 build o34 (and o14), lanes w = 1 o32
         const int c = r / NB, d = r % NB;
         if (w == 0) {
-          sm.o34[grp][r] = ee_ovlp<NB>(a, ka, kb, c, d);
+          sm.o34[grp][r] = V::from(ee_ovlp<NB>(a, ka, kb, c, d));
           if (a.antisym) {
             const double vq = ee_vq(a, scr, k1, kb);
             const double2 o = ee_ovlp<NB>(a, k1, kb, c, d);
-            sm.o14[grp][r] = mk2(vq * o.x, vq * o.y);
+            sm.o14[grp][r] = V::from(mk2(vq * o.x, vq * o.y));
           }
         } else if (a.antisym) {
-          sm.o32[grp][r] = ee_ovlp<NB>(a, ka, k2, c, d);
+          sm.o32[grp][r] = V::from(ee_ovlp<NB>(a, ka, k2, c, d));
         }
       }
       __syncwarp();
       if (act && w == 0) {  // row r = (i1, i3) of A (calc_delta, calc_mee[_ex], calc_A)
         const double* e3 = a.ew + (size_t)ka * NB;
         const double* e4 = a.ew + (size_t)kb * NB;
-        const double2 m12 = sm.o12[i1 * NB + i3];
+        const C m12 = sm.o12[i1 * NB + i3];
 #pragma unroll
         for (int cd = 0; cd < NB2; ++cd) {
           const int c = cd / NB, d = cd % NB;
-          const double de = e1[i1] - e2[i3] + e3[c] - e4[d];
-          double2 v = mk2(0, 0);
+          const double de = e1[i1] - e2[i3] + e3[c] - e4[d];  // the window test stays FP64
+          C v = V::zero();
           if (fabs(de) < a.ethr) {
-            double2 mee = cmul_rn(m12, sm.o34[grp][cd]);
-            if (a.antisym) {
-              const double2 mex = cmul_rn(sm.o14[grp][i1 * NB + d], sm.o32[grp][c * NB + i3]);
-              mee = mk2(-0.5 * mex.x + 0.5 * mee.x, -0.5 * mex.y + 0.5 * mee.y);
+            if constexpr (V::kDF) {
+              C mee = V::mul(m12, sm.o34[grp][cd]);
+              if (a.antisym) {
+                const C mex = V::mul(sm.o14[grp][i1 * NB + d], sm.o32[grp][c * NB + i3]);
+                mee = make_float4(0.5f * mee.x, 0.5f * mee.y, 0.5f * mee.z, 0.5f * mee.w);  // exact halves
+                df_add(mee.x, mee.y, -0.5f * mex.x, -0.5f * mex.y);
+                df_add(mee.z, mee.w, -0.5f * mex.z, -0.5f * mex.w);
+              }
+              v = V::scale_df(mee, df_exp_neg(a.prefac_exp * (de * de)));
+            } else {
+              double2 mee = cmul_rn(m12, sm.o34[grp][cd]);
+              if (a.antisym) {
+                const double2 mex = cmul_rn(sm.o14[grp][i1 * NB + d], sm.o32[grp][c * NB + i3]);
+                mee = mk2(-0.5 * mex.x + 0.5 * mee.x, -0.5 * mex.y + 0.5 * mee.y);
+              }
+              v = cscale_rn(exp(a.prefac_exp * (de * de)), mee);
             }
-            v = cscale_rn(exp(a.prefac_exp * (de * de)), mee);
           }
           sm.A[grp][r * NB2 + cd] = v;
         }
@@ -264,28 +386,31 @@ __global__ void __launch_bounds__(128) k_ee_pairs(EeArgs a) {
       __syncwarp();
       if (act) {
         // X = dm1_k3 A[(i1,i3)] dm_k4 (w = 0) or dm_k3 A[(i3,i1)] dm1_k4 (w = 1)
-        const double2* Ar = &sm.A[grp][(w == 0 ? r : i3 * NB + i1) * NB2];
-        double2 X[NB2];
+        const C* Ar = &sm.A[grp][(w == 0 ? r : i3 * NB + i1) * NB2];
+        C X[NB2];
         if (a.dm) {
-          const double2* L = (w == 0 ? a.dm1 : a.dm) + (size_t)ka * NB2;
-          const double2* R = (w == 0 ? a.dm : a.dm1) + (size_t)kb * NB2;
-          double2 T[NB2];
+          const size_t lo = (size_t)ka * NB2, ro = (size_t)kb * NB2;
+          C T[NB2];
 #pragma unroll
           for (int i = 0; i < NB; ++i)
 #pragma unroll
             for (int j = 0; j < NB; ++j) {
-              double2 t = mk2(0, 0);
+              C t = V::zero();
 #pragma unroll
-              for (int m = 0; m < NB; ++m) t = cfma(Ar[i * NB + m], R[m * NB + j], t);
+              for (int m = 0; m < NB; ++m)
+                V::mac(t, Ar[i * NB + m], w == 0 ? V::load(a.dm, a.dmf, ro + m * NB + j)
+                                                 : V::load(a.dm1, a.dm1f, ro + m * NB + j));
               T[i * NB + j] = t;
             }
 #pragma unroll
           for (int i = 0; i < NB; ++i)
 #pragma unroll
             for (int j = 0; j < NB; ++j) {
-              double2 t = mk2(0, 0);
+              C t = V::zero();
 #pragma unroll
-              for (int m = 0; m < NB; ++m) t = cfma(L[i * NB + m], T[m * NB + j], t);
+              for (int m = 0; m < NB; ++m)
+                V::mac(t, w == 0 ? V::load(a.dm1, a.dm1f, lo + i * NB + m) : V::load(a.dm, a.dmf, lo + i * NB + m),
+                       T[m * NB + j]);
               X[i * NB + j] = t;
             }
         } else {
@@ -296,7 +421,7 @@ __global__ void __launch_bounds__(128) k_ee_pairs(EeArgs a) {
 #pragma unroll
             for (int j = 0; j < NB; ++j) {
               const double sl = w == 0 ? 1 - f3[i] : f3[i], sr = w == 0 ? f4[j] : 1 - f4[j];
-              X[i * NB + j] = cscale_rn(sr, cscale_rn(sl, Ar[i * NB + j]));
+              X[i * NB + j] = V::scale(V::scale(Ar[i * NB + j], sl), sr);
             }
         }
         // acc[(i2,i4)] += sum_(i6,i8) X[i6,i8] conj(A[(i2,i4) or (i4,i2)][i6,i8])
@@ -304,13 +429,11 @@ __global__ void __launch_bounds__(128) k_ee_pairs(EeArgs a) {
         for (int i2 = 0; i2 < NB; ++i2)
 #pragma unroll
           for (int i4 = 0; i4 < NB; ++i4) {
-            const double2* B = &sm.A[grp][(w == 0 ? i2 * NB + i4 : i4 * NB + i2) * NB2];
-            double2 t = acc[i2 * NB + i4];
+            const C* B = &sm.A[grp][(w == 0 ? i2 * NB + i4 : i4 * NB + i2) * NB2];
+            C t = acc[i2 * NB + i4];
 #pragma unroll
-            for (int q = 0; q < NB2; ++q) {
-              const double2 b = B[q];
-              t = mk2(fma(X[q].x, b.x, fma(X[q].y, b.y, t.x)), fma(X[q].y, b.x, fma(-X[q].x, b.y, t.y)));
-            }
+            for (int q = 0; q < NB2; ++q) V::mac_conj(t, X[q], B[q]);
+            V::renorm(t);
             acc[i2 * NB + i4] = t;
           }
       }
@@ -325,20 +448,23 @@ __global__ void __launch_bounds__(128) k_ee_pairs(EeArgs a) {
     ncand = rest;
     __syncwarp();
   }
-  // add the groups' partial sums (lanes with the same role)
+  // add the groups' partial sums (lanes with the same role), in FP64
+  double2 accd[NB2];
+#pragma unroll
+  for (int e = 0; e < NB2; ++e) accd[e] = V::value(acc[e]);
 #pragma unroll
   for (int off = G; off < 32; off <<= 1)
 #pragma unroll
     for (int e = 0; e < NB2; ++e) {
-      acc[e].x += __shfl_xor_sync(FULL, acc[e].x, off);
-      acc[e].y += __shfl_xor_sync(FULL, acc[e].y, off);
+      accd[e].x += __shfl_xor_sync(FULL, accd[e].x, off);
+      accd[e].y += __shfl_xor_sync(FULL, accd[e].y, off);
     }
   if (grp == 0) {
 #pragma unroll
     for (int i2 = 0; i2 < NB; ++i2)
 #pragma unroll
       for (int i4 = 0; i4 < NB; ++i4) {
-        const double2 v = acc[i2 * NB + i4];
+        const double2 v = accd[i2 * NB + i4];
         out[w * NB4 + ((i1 * NB + i2) * NB + i3) * NB + i4] = mk2(a.prefac * v.x, a.prefac * v.y);
       }
   }

@@ -18,6 +18,8 @@ from conftest import EE_CASES, GOLDEN
 pytestmark = pytest.mark.gpu
 
 P_TOL = 1e-12
+# handles of the FP32-pair arithmetic build P_ee with double-float contractions (~2^-47 per product)
+P_TOL_DF = 5e-12
 RHS_TOL = {"f64": 1e-12, "f64x": 1e-11, "f32": 2e-6, "bf16x2": 2e-5}
 
 
@@ -56,19 +58,22 @@ def fresh(oracle, case):
     return oracle.load(d), dict(np.load(os.path.join(d, "golden.npz")))
 
 
+@pytest.mark.parametrize("prec", ["f64", "f64x"])
 @pytest.mark.parametrize("case", EE_CASES)
-def test_ee_setup_and_rebuilds_vs_golden(case, oracle, built):
+def test_ee_setup_and_rebuilds_vs_golden(case, prec, oracle, built):
     """P_ee at set-up (equilibrium occupations, set-up screening) and after dmd_ee_update on the three
-    golden states: P_base + scale P_ee and the screening density match the reference's."""
+    golden states: P_base + scale P_ee and the screening density match the reference's (FP64
+    contractions for f64 handles, double-float for f64x)."""
     s, g = fresh(oracle, case)
     nb4 = (s.bend - s.bstart) ** 4
+    tol = P_TOL if prec == "f64" else P_TOL_DF
     B1, B2 = s.ee.P1base.reshape(-1, nb4), s.ee.P2base.reshape(-1, nb4)
-    with make_ee_gpu(s, every_rhs=0) as gpu:
+    with make_ee_gpu(s, prec, every_rhs=0) as gpu:
         P1, P2, n0 = gpu.ee_read()
         e1 = rel(B1 + s.ee.scale * P1, g["ee_P1_eq"])
         e2 = rel(B2 + s.ee.scale * P2, g["ee_P2_eq"])
-        print("%s set-up: P rel err %.3g %.3g" % (case, e1, e2))
-        assert e1 < P_TOL and e2 < P_TOL
+        print("%s %s set-up: P rel err %.3g %.3g" % (case, prec, e1, e2))
+        assert e1 < tol and e2 < tol
         assert n0 == s.ee.c.nfree
         for i, (t, y) in enumerate(zip(g["rhs_t"], g["rhs_y"])):
             gpu.set_state(t, y)
@@ -76,8 +81,9 @@ def test_ee_setup_and_rebuilds_vs_golden(case, oracle, built):
             P1, P2, n = gpu.ee_read()
             e1 = rel(B1 + s.ee.scale * P1, g["pee_P1"][i].reshape(-1, nb4))
             e2 = rel(B2 + s.ee.scale * P2, g["pee_P2"][i].reshape(-1, nb4))
-            print("%s state %d: P rel err %.3g %.3g, nfree %.17g vs %.17g" % (case, i, e1, e2, n, g["pee_nfree"][i]))
-            assert e1 < P_TOL and e2 < P_TOL
+            print("%s %s state %d: P rel err %.3g %.3g, nfree %.17g vs %.17g" % (case, prec, i, e1, e2, n,
+                                                                                 g["pee_nfree"][i]))
+            assert e1 < tol and e2 < tol
             assert abs(n - g["pee_nfree"][i]) <= 1e-14 * abs(g["pee_nfree"][i])
 
 
@@ -150,7 +156,8 @@ def test_ee_reduced_precision_rhs(prec, oracle, built):
             assert e < RHS_TOL[prec]
 
 
-def test_ee_larger_random_case_vs_oracle(oracle, built, tmp_path):
+@pytest.mark.parametrize("prec", ["f64", "f64x"])
+def test_ee_larger_random_case_vs_oracle(prec, oracle, built, tmp_path):
     """a denser ball of k-points (nk = 120, ~6k pairs, many k3 per pair) with the exchange term:
     P_ee from a perturbed state against the oracle"""
     from denmat_dynm_development_gb300.ldbd_synth import SynthConfig, make_ldbd
@@ -165,14 +172,15 @@ def test_ee_larger_random_case_vs_oracle(oracle, built, tmp_path):
     dm = 0.5 * (dm + np.conj(np.swapaxes(dm, 1, 2)))
     y = oracle.y_of(dm.reshape(s.nk, -1))
     t = 13.0 * oracle.fs
-    with make_ee_gpu(s, every_rhs=0) as gpu:
+    with make_ee_gpu(s, prec, every_rhs=0) as gpu:
         gpu.set_state(t, y)
         gpu.ee_update()
         P1, P2, n = gpu.ee_read()
     oracle.ee_rebuild(s, t, y)
     e1, e2 = rel(P1, s.ee.P1ee.reshape(P1.shape)), rel(P2, s.ee.P2ee.reshape(P2.shape))
-    print("nk120 npair %d: P_ee rel err %.3g %.3g, nfree %.17g vs %.17g" % (s.npair, e1, e2, n, s.ee.nfree))
-    assert e1 < P_TOL and e2 < P_TOL
+    print("nk120 %s npair %d: P_ee rel err %.3g %.3g, nfree %.17g vs %.17g" % (prec, s.npair, e1, e2, n, s.ee.nfree))
+    tol = P_TOL if prec == "f64" else P_TOL_DF
+    assert e1 < tol and e2 < tol
     assert abs(n - s.ee.nfree) <= 1e-14 * abs(s.ee.nfree)
 
 
