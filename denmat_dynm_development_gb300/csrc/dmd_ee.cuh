@@ -273,7 +273,7 @@ struct EeSmem {
 };
 
 template <int NB, typename V = EeF64>
-__global__ void __launch_bounds__(128) k_ee_pairs(EeArgs a) {
+__global__ void __launch_bounds__(128, (NB == 2 && V::kDF) ? 7 : 1) k_ee_pairs(EeArgs a) {
   typedef EeSmem<NB, V> S;
   typedef typename V::c C;
   constexpr int NB2 = S::NB2, NB4 = S::NB4, G = S::G, NG = S::NG;
