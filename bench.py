@@ -632,7 +632,8 @@ def run_ee(args):
     rebuild before every RHS evaluation, on a ball of k-points of a GaAs-like mesh."""
     from denmat_dynm_development_gb300 import host as H
     from denmat_dynm_development_gb300.dmd import LindbladGPU
-    nb, nbw = 2, 4
+    nb = args.ee_nb
+    nbw = 2 * nb
     cfg = S.SynthConfig(nk=args.ee_nk, nb=nb, seed=51, de_pair_mev=args.ee_de_mev, nwannier=nbw, kball=True)
     t0 = time.time()
     st, P1, P2, _, _ = S.generate_arrays(cfg, procs=max(1, min(16, os.cpu_count() or 1)))
@@ -692,9 +693,9 @@ def run_ee(args):
     line = {"metric": "e-e operator rebuilds/s (P_ee of every k-pair from rho, Pee_update)", "value": 1e3 / ms,
             "unit": "rebuilds/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "ee_ball_nk%d: nb=2, nk=%d (ball of a %d^3 mesh), %d k-pairs, %d Wannier functions, "
+            "config": {"workload": "ee_ball_nk%d: nb=%d, nk=%d (ball of a %d^3 mesh), %d k-pairs, %d Wannier functions, "
                                    "Debye screening from rho, Lindblad e-e (ElecElec_Model.h:186-262)"
-                                   % (cfg.nk, cfg.nk, n, st.npair, nbw),
+                                   % (cfg.nk, nb, cfg.nk, n, st.npair, nbw),
                        "npair": st.npair, "nk": cfg.nk, "k3_candidates": st.npair * cfg.nk,
                        "work_items_estimated": surv, "work_item_sample_pairs": int(sample.size),
                        "l2": "per rebuild the operators (%.2f GB) are read and written; no flush" %
@@ -762,6 +763,7 @@ def main():
     ap.add_argument("--ee", action="store_true", help="e-e operators rebuilt from rho (Pee_update)")
     ap.add_argument("--ee-nk", type=int, default=2000, help="e-e: k-points of the ball")
     ap.add_argument("--ee-de-mev", type=float, default=20.0, help="e-e: pair energy window (meV)")
+    ap.add_argument("--ee-nb", type=int, default=2, choices=[2, 4], help="e-e: bands of the window")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world = env_int("RANK", 0), env_int("WORLD_SIZE", 1)

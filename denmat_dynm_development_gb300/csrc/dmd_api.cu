@@ -79,7 +79,7 @@ struct dmd_handle {
   int4* d_ee_kidx = nullptr;
   int* d_ee_kmap = nullptr;
   double2* d_ee_U = nullptr;
-  double2* d_ee_erng = nullptr;
+  float* d_ee_ewf = nullptr;
   double* d_ee_f = nullptr;
   double2* d_ee_dm = nullptr;
   double2* d_ee_dm1 = nullptr;
@@ -1125,7 +1125,7 @@ void release(dmd_handle* h) {
   void* ptrs[] = {h->d_err, h->d_pos, h->d_rb, h->d_items, h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
                   h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0, h->d_Praw, h->d_kkraw,
-                  h->d_dst, h->d_ee_kvec, h->d_ee_kidx, h->d_ee_kmap, h->d_ee_U, h->d_ee_erng, h->d_ee_f,
+                  h->d_dst, h->d_ee_kvec, h->d_ee_kidx, h->d_ee_kmap, h->d_ee_U, h->d_ee_ewf, h->d_ee_f,
                   h->d_ee_dm, h->d_ee_dm1, h->d_ee_dmf, h->d_ee_dm1f, h->d_ee_scr, h->d_ee_Pee};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1168,8 +1168,10 @@ int ee_rebuild(dmd_handle* h, const double2* y, const TimeArg& ta, bool eq) {
   k_ee_screen<<<1, 256, 0, h->st>>>(h->nk, NB, h->ee_nv, h->d_ee_dm, (!eq && h->ee_update) ? 1 : 0, h->ee_nfree0,
                                     h->ee_nkfull, h->ee_cell, h->ee_eps, h->ee_T, h->ee_meff, h->d_ee_scr);
   // FP64 handles contract in FP64, the others in double-float on the FP32 pipes
-  if (h->prec == DMD_PREC_F64) k_ee_pairs<NB, EeF64><<<(unsigned)((h->npair + 3) / 4), 128, 0, h->st>>>(a);
-  else k_ee_pairs<NB, EeDF><<<(unsigned)((h->npair + 3) / 4), 128, 0, h->st>>>(a);
+  constexpr int WPC = ee_warps_per_cta(NB);
+  const unsigned grid = (unsigned)((h->npair + WPC - 1) / WPC);
+  if (h->prec == DMD_PREC_F64) k_ee_pairs<NB, EeF64><<<grid, 32 * WPC, 0, h->st>>>(a);
+  else k_ee_pairs<NB, EeDF><<<grid, 32 * WPC, 0, h->st>>>(a);
   const bool dev = deviation_form(h->prec) && !h->lin;
   if (dev && cudaMemsetAsync(h->d_acc0, 0, (size_t)h->nk * 2 * NB2 * sizeof(double2), h->st) != cudaSuccess)
     return fail(h, DMD_E_CUDA, "e-e refill");
@@ -2440,19 +2442,20 @@ int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
   }
   std::vector<double> ew((size_t)nk * nb);
   CK(cudaMemcpy(ew.data(), h->d_ew, ew.size() * 8, cudaMemcpyDeviceToHost));
-  std::vector<double2> erng(nk);
-  for (int k = 0; k < nk; ++k) {
-    double lo = ew[(size_t)k * nb], hi = lo;
-    for (int b = 1; b < nb; ++b) {
-      lo = std::min(lo, ew[(size_t)k * nb + b]);
-      hi = std::max(hi, ew[(size_t)k * nb + b]);
-    }
-    erng[k] = make_double2(lo, hi);
+  // FP32 window energies relative to their minimum for the candidate test; the FP32 sum of four
+  // of them is within 4 x 2^-24 x span of the exact one, so the margin keeps the test a superset
+  double emin = ew[0], emax = ew[0];
+  for (double v : ew) {
+    emin = std::min(emin, v);
+    emax = std::max(emax, v);
   }
+  std::vector<float> ewf(ew.size());
+  for (size_t i = 0; i < ew.size(); ++i) ewf[i] = (float)(ew[i] - emin);
+  const double margin = 1e-6 * (emax - emin) + 1e-12;
   int rc;
   if ((rc = dalloc(h, &h->d_ee_kvec, (size_t)nk * 3)) || (rc = dalloc(h, &h->d_ee_kidx, (size_t)nk)) ||
       (rc = dalloc(h, &h->d_ee_kmap, nmesh)) || (rc = dalloc(h, &h->d_ee_U, (size_t)nk * ee->nbw * nb)) ||
-      (rc = dalloc(h, &h->d_ee_erng, (size_t)nk)) || (rc = dalloc(h, &h->d_ee_f, (size_t)nk * nb)) ||
+      (rc = dalloc(h, &h->d_ee_ewf, (size_t)nk * nb)) || (rc = dalloc(h, &h->d_ee_f, (size_t)nk * nb)) ||
       (rc = dalloc(h, &h->d_ee_dm, (size_t)nk * h->nb2)) || (rc = dalloc(h, &h->d_ee_dm1, (size_t)nk * h->nb2)) ||
       (rc = dalloc(h, &h->d_ee_dmf, (size_t)nk * h->nb2)) || (rc = dalloc(h, &h->d_ee_dm1f, (size_t)nk * h->nb2)) ||
       (rc = dalloc(h, &h->d_ee_scr, 1)) || (rc = dalloc(h, &h->d_ee_Pee, (size_t)h->npair * 2 * h->nb4)))
@@ -2461,7 +2464,7 @@ int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
   CK(cudaMemcpy(h->d_ee_kidx, kidx.data(), (size_t)nk * sizeof(int4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_ee_kmap, kmap.data(), nmesh * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_ee_U, ee->U, (size_t)nk * ee->nbw * nb * 16, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->d_ee_erng, erng.data(), (size_t)nk * sizeof(double2), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_ee_ewf, ewf.data(), ewf.size() * sizeof(float), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_ee_f, ee->f, (size_t)nk * nb * 8, cudaMemcpyHostToDevice));
   CK(cudaMemset(h->d_ee_dm, 0, (size_t)nk * h->nb2 * 16));
   EeArgs& a = h->ee_args;
@@ -2483,7 +2486,8 @@ int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
   a.kmap = h->d_ee_kmap;
   a.U = h->d_ee_U;
   a.ew = h->d_ew;
-  a.erng = h->d_ee_erng;
+  a.ewf = h->d_ee_ewf;
+  a.thr32 = (float)(ee->ethr + margin);
   a.scr = h->d_ee_scr;
   a.Pee = h->d_ee_Pee;
   h->ee_every = ee->every_rhs ? 1 : 0;

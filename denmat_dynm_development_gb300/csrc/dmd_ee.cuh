@@ -49,7 +49,8 @@ struct EeArgs {
   const int* kmap;                   // [n0 n1 n2] mesh index -> k or -1
   const double2* U;                  // [nk][nbw][nb]
   const double* ew;                  // [nk][nb] window energies
-  const double2* erng;               // [nk] (min, max) of the window energies
+  const float* ewf;                  // [nk][nb] window energies minus their minimum, FP32 (candidate test)
+  float thr32;                       // ethr plus a margin above the FP32 rounding of that test
   const double2* dm;                 // [nk][nb^2] window density matrix (Schrodinger picture), or null
   const double2* dm1;                // [nk][nb^2] 1 - dm
   const float4* dmf;                 // the same as double-floats (re_h, re_l, im_h, im_l)
@@ -272,15 +273,20 @@ struct EeSmem {
   int2 cand[64];
 };
 
+// warps (pairs) per CTA: nb = 4 keeps 2 so that the per-lane scratch fits the static shared memory
+__host__ __device__ constexpr int ee_warps_per_cta(int nb) { return nb == 4 ? 2 : 4; }
+
 template <int NB, typename V = EeF64>
-__global__ void __launch_bounds__(128, (NB == 2 && V::kDF) ? 7 : 1) k_ee_pairs(EeArgs a) {
+__global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF) ? 7 : 1) k_ee_pairs(EeArgs a) {
   typedef EeSmem<NB, V> S;
   typedef typename V::c C;
+  constexpr int WPC = ee_warps_per_cta(NB);
   constexpr int NB2 = S::NB2, NB4 = S::NB4, G = S::G, NG = S::NG;
-  __shared__ S smem_all[4];
+  __shared__ S smem_all[WPC];
+  __shared__ typename V::c scratch[NB == 4 ? WPC : 1][NB == 4 ? 32 : 1][NB == 4 ? 2 * NB * NB : 1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   S& sm = smem_all[warp];
-  const int p = blockIdx.x * 4 + warp;
+  const int p = blockIdx.x * WPC + warp;
   if (p >= a.npair) return;
   const int k1 = a.kk[p].x, k2 = a.kk[p].y;
   const unsigned FULL = 0xffffffffu;
@@ -300,7 +306,11 @@ __global__ void __launch_bounds__(128, (NB == 2 && V::kDF) ? 7 : 1) k_ee_pairs(E
 #pragma unroll
   for (int e = 0; e < NB2; ++e) acc[e] = V::zero();
   const int4 i1v = a.kidx[k1], i2v = a.kidx[k2];
-  const double2 r1 = a.erng[k1], r2 = a.erng[k2];
+  float x12[NB2];  // e1a - e2b of this pair for the FP32 candidate test
+#pragma unroll
+  for (int i = 0; i < NB; ++i)
+#pragma unroll
+    for (int j = 0; j < NB; ++j) x12[i * NB + j] = a.ewf[(size_t)k1 * NB + i] - a.ewf[(size_t)k2 * NB + j];
   const double* e1 = a.ew + (size_t)k1 * NB;
   const double* e2 = a.ew + (size_t)k2 * NB;
   int ncand = 0;
@@ -316,11 +326,17 @@ __global__ void __launch_bounds__(128, (NB == 2 && V::kDF) ? 7 : 1) k_ee_pairs(E
       m1 += m1 < 0 ? a.kmesh[1] : 0;
       m2 += m2 < 0 ? a.kmesh[2] : 0;
       k4 = a.kmap[((size_t)m0 * a.kmesh[1] + m1) * a.kmesh[2] + m2];
-      if (k4 >= 0) {  // some band combination may be inside the window (exact test in phase 2)
-        const double2 r3 = a.erng[k3], r4 = a.erng[k4];
-        const double lo = r1.x - r2.y + r3.x - r4.y, hi = r1.y - r2.x + r3.y - r4.x;
-        const double tol = 1e-12 * (fabs(lo) + fabs(hi)) + 1e-300;
-        if (!(lo < a.ethr + tol && hi > -a.ethr - tol)) k4 = -1;
+      if (k4 >= 0) {  // some band combination inside the window, with a margin (exact FP64 test in phase 2)
+        bool hit = false;
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+#pragma unroll
+          for (int d = 0; d < NB; ++d) {
+            const float y = a.ewf[(size_t)k3 * NB + c] - a.ewf[(size_t)k4 * NB + d];
+#pragma unroll
+            for (int q = 0; q < NB2; ++q) hit |= fabsf(x12[q] + y) < a.thr32;
+          }
+        if (!hit) k4 = -1;
       }
     }
     const unsigned ball = __ballot_sync(FULL, k4 >= 0);
@@ -387,55 +403,103 @@ __global__ void __launch_bounds__(128, (NB == 2 && V::kDF) ? 7 : 1) k_ee_pairs(E
       if (act) {
         // X = dm1_k3 A[(i1,i3)] dm_k4 (w = 0) or dm_k3 A[(i3,i1)] dm1_k4 (w = 1)
         const C* Ar = &sm.A[grp][(w == 0 ? r : i3 * NB + i1) * NB2];
-        C X[NB2];
-        if (a.dm) {
-          const size_t lo = (size_t)ka * NB2, ro = (size_t)kb * NB2;
-          C T[NB2];
+        const size_t lo = (size_t)ka * NB2, ro = (size_t)kb * NB2;
+        const double2* Ld = w == 0 ? a.dm1 : a.dm;
+        const float4* Lf = w == 0 ? a.dm1f : a.dmf;
+        const double2* Rd = w == 0 ? a.dm : a.dm1;
+        const float4* Rf = w == 0 ? a.dmf : a.dm1f;
+        if constexpr (NB == 2) {
+          C X[NB2];
+          if (a.dm) {
+            C T[NB2];
 #pragma unroll
-          for (int i = 0; i < NB; ++i)
+            for (int i = 0; i < NB; ++i)
 #pragma unroll
-            for (int j = 0; j < NB; ++j) {
-              C t = V::zero();
+              for (int j = 0; j < NB; ++j) {
+                C t = V::zero();
 #pragma unroll
-              for (int m = 0; m < NB; ++m)
-                V::mac(t, Ar[i * NB + m], w == 0 ? V::load(a.dm, a.dmf, ro + m * NB + j)
-                                                 : V::load(a.dm1, a.dm1f, ro + m * NB + j));
-              T[i * NB + j] = t;
-            }
+                for (int m = 0; m < NB; ++m) V::mac(t, Ar[i * NB + m], V::load(Rd, Rf, ro + m * NB + j));
+                T[i * NB + j] = t;
+              }
 #pragma unroll
-          for (int i = 0; i < NB; ++i)
+            for (int i = 0; i < NB; ++i)
 #pragma unroll
-            for (int j = 0; j < NB; ++j) {
-              C t = V::zero();
+              for (int j = 0; j < NB; ++j) {
+                C t = V::zero();
 #pragma unroll
-              for (int m = 0; m < NB; ++m)
-                V::mac(t, w == 0 ? V::load(a.dm1, a.dm1f, lo + i * NB + m) : V::load(a.dm, a.dmf, lo + i * NB + m),
-                       T[m * NB + j]);
-              X[i * NB + j] = t;
+                for (int m = 0; m < NB; ++m) V::mac(t, V::load(Ld, Lf, lo + i * NB + m), T[m * NB + j]);
+                X[i * NB + j] = t;
+              }
+          } else {
+            const double* f3 = a.f + (size_t)ka * NB;
+            const double* f4 = a.f + (size_t)kb * NB;
+#pragma unroll
+            for (int i = 0; i < NB; ++i)
+#pragma unroll
+              for (int j = 0; j < NB; ++j) {
+                const double sl = w == 0 ? 1 - f3[i] : f3[i], sr = w == 0 ? f4[j] : 1 - f4[j];
+                X[i * NB + j] = V::scale(V::scale(Ar[i * NB + j], sl), sr);
+              }
+          }
+          // acc[(i2,i4)] += sum_(i6,i8) X[i6,i8] conj(A[(i2,i4) or (i4,i2)][i6,i8])
+#pragma unroll
+          for (int i2 = 0; i2 < NB; ++i2)
+#pragma unroll
+            for (int i4 = 0; i4 < NB; ++i4) {
+              const C* B = &sm.A[grp][(w == 0 ? i2 * NB + i4 : i4 * NB + i2) * NB2];
+              C t = acc[i2 * NB + i4];
+#pragma unroll
+              for (int q = 0; q < NB2; ++q) V::mac_conj(t, X[q], B[q]);
+              V::renorm(t);
+              acc[i2 * NB + i4] = t;
             }
         } else {
-          const double* f3 = a.f + (size_t)ka * NB;
-          const double* f4 = a.f + (size_t)kb * NB;
+          // nb = 4: the same with rolled outer loops and T, X in this lane's shared scratch, so the
+          // code stays within the instruction cache
+          C* Ts = scratch[warp][lane];
+          C* Xs = Ts + NB2;
+          if (a.dm) {
+#pragma unroll 1
+            for (int i = 0; i < NB; ++i)
 #pragma unroll
-          for (int i = 0; i < NB; ++i)
+              for (int j = 0; j < NB; ++j) {
+                C t = V::zero();
 #pragma unroll
-            for (int j = 0; j < NB; ++j) {
-              const double sl = w == 0 ? 1 - f3[i] : f3[i], sr = w == 0 ? f4[j] : 1 - f4[j];
-              X[i * NB + j] = V::scale(V::scale(Ar[i * NB + j], sl), sr);
-            }
-        }
-        // acc[(i2,i4)] += sum_(i6,i8) X[i6,i8] conj(A[(i2,i4) or (i4,i2)][i6,i8])
+                for (int m = 0; m < NB; ++m) V::mac(t, Ar[i * NB + m], V::load(Rd, Rf, ro + m * NB + j));
+                Ts[i * NB + j] = t;
+              }
+#pragma unroll 1
+            for (int i = 0; i < NB; ++i)
 #pragma unroll
-        for (int i2 = 0; i2 < NB; ++i2)
+              for (int j = 0; j < NB; ++j) {
+                C t = V::zero();
 #pragma unroll
-          for (int i4 = 0; i4 < NB; ++i4) {
-            const C* B = &sm.A[grp][(w == 0 ? i2 * NB + i4 : i4 * NB + i2) * NB2];
-            C t = acc[i2 * NB + i4];
+                for (int m = 0; m < NB; ++m) V::mac(t, V::load(Ld, Lf, lo + i * NB + m), Ts[m * NB + j]);
+                Xs[i * NB + j] = t;
+              }
+          } else {
+            const double* f3 = a.f + (size_t)ka * NB;
+            const double* f4 = a.f + (size_t)kb * NB;
+#pragma unroll 1
+            for (int i = 0; i < NB; ++i)
 #pragma unroll
-            for (int q = 0; q < NB2; ++q) V::mac_conj(t, X[q], B[q]);
-            V::renorm(t);
-            acc[i2 * NB + i4] = t;
+              for (int j = 0; j < NB; ++j) {
+                const double sl = w == 0 ? 1 - f3[i] : f3[i], sr = w == 0 ? f4[j] : 1 - f4[j];
+                Xs[i * NB + j] = V::scale(V::scale(Ar[i * NB + j], sl), sr);
+              }
           }
+#pragma unroll 1
+          for (int q = 0; q < NB2; ++q) {
+            const C xq = Xs[q];
+#pragma unroll
+            for (int i2 = 0; i2 < NB; ++i2)
+#pragma unroll
+              for (int i4 = 0; i4 < NB; ++i4)
+                V::mac_conj(acc[i2 * NB + i4], xq, sm.A[grp][(w == 0 ? i2 * NB + i4 : i4 * NB + i2) * NB2 + q]);
+          }
+#pragma unroll
+          for (int e = 0; e < NB2; ++e) V::renorm(acc[e]);
+        }
       }
       __syncwarp();
     }
