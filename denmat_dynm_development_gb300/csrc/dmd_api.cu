@@ -86,6 +86,7 @@ struct dmd_handle {
   float4* d_ee_dmf = nullptr;
   float4* d_ee_dm1f = nullptr;
   dmd::EeScreen* d_ee_scr = nullptr;
+  double* d_ee_vqtab = nullptr;  // static RPA vq by q mesh index
   double2* d_ee_Pee = nullptr;
   float2* d_x0y0 = nullptr;    // tensor-core form: contraction of diag(f_ref), back-transformed, by k
   float2* d_v0 = nullptr;      // tensor-core form: (prefac/2)(C0 + C0^dagger) by k
@@ -1126,7 +1127,7 @@ void release(dmd_handle* h) {
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
                   h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0, h->d_Praw, h->d_kkraw,
                   h->d_dst, h->d_ee_kvec, h->d_ee_kidx, h->d_ee_kmap, h->d_ee_U, h->d_ee_ewf, h->d_ee_f,
-                  h->d_ee_dm, h->d_ee_dm1, h->d_ee_dmf, h->d_ee_dm1f, h->d_ee_scr, h->d_ee_Pee};
+                  h->d_ee_dm, h->d_ee_dm1, h->d_ee_dmf, h->d_ee_dm1f, h->d_ee_scr, h->d_ee_Pee, h->d_ee_vqtab};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -2415,7 +2416,7 @@ int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
   if (!h->eek || !h->d_dst || !h->d_Praw) return fail(h, DMD_E_STATE, "the handle was not made with DMD_FLAG_EE");
   if (h->ee_on) return fail(h, DMD_E_STATE, "an e-e model is already attached");
   if (ee->nbw < h->nb || !ee->kvec || !ee->U || !ee->f || ee->kmesh[0] < 1 || ee->kmesh[1] < 1 || ee->kmesh[2] < 1 ||
-      ee->formula < DMD_SCREEN_UNSCREENED || ee->formula > DMD_SCREEN_BECHSTEDT || !(ee->degauss > 0) ||
+      ee->formula < DMD_SCREEN_UNSCREENED || ee->formula > DMD_SCREEN_RPA || !(ee->degauss > 0) ||
       !(ee->ethr >= 0) || !(ee->cell_size > 0) || !(ee->nk_full > 0) || !(ee->temperature > 0) ||
       !(ee->eps_background >= 1) || !(ee->meff > 0))
     return fail(h, DMD_E_ARG, "e-e model description");
@@ -2500,6 +2501,27 @@ int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
   h->ee_eps = ee->eps_background;
   h->ee_T = ee->temperature;
   h->ee_meff = ee->meff;
+  if (ee->formula == DMD_SCREEN_RPA) {  // the static RPA table from the set-up occupations
+    double* qacc = nullptr;
+    unsigned int* qhit = nullptr;
+    if ((rc = dalloc(h, &h->d_ee_vqtab, nmesh)) || (rc = dalloc(h, &qacc, nmesh)) || (rc = dalloc(h, &qhit, nmesh))) {
+      cudaFree(qacc);
+      return rc;
+    }
+    a.vqtab = h->d_ee_vqtab;
+    cudaMemsetAsync(qacc, 0, nmesh * 8, h->st);
+    cudaMemsetAsync(qhit, 0, nmesh * 4, h->st);
+    const long long npp = (long long)nk * nk;
+    if (nb == 2) k_ee_rpa_sum<2><<<blocks_for(npp, 256), 256, 0, h->st>>>(a, ee->temperature, h->d_ee_f, qacc, qhit);
+    else k_ee_rpa_sum<4><<<blocks_for(npp, 256), 256, 0, h->st>>>(a, ee->temperature, h->d_ee_f, qacc, qhit);
+    k_ee_rpa_table<<<blocks_for((long long)nmesh, 256), 256, 0, h->st>>>(a, 4 * M_PI / ee->eps_background / ee->cell_size,
+                                                                        ee->nk_full, qacc, qhit, h->d_ee_vqtab);
+    const cudaError_t e = cudaStreamSynchronize(h->st);
+    cudaFree(qacc);
+    cudaFree(qhit);
+    if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("RPA screening: ") + cudaGetErrorString(e));
+    h->launches += 2;
+  }
   h->ee_on = 1;
   if ((rc = ee_rebuild_nb(h, nullptr, time_value(h->t), true))) return rc;
   CK(cudaStreamSynchronize(h->st));

@@ -30,7 +30,7 @@
 
 namespace dmd {
 
-enum { EE_UNSCREENED = 0, EE_DEBYE = 1, EE_BECHSTEDT = 2 };
+enum { EE_UNSCREENED = 0, EE_DEBYE = 1, EE_BECHSTEDT = 2, EE_RPA = 3 };
 
 // screening constants (Coulomb_Model.h:423-424, 555-569), computed on the device from nfree
 struct EeScreen {
@@ -57,6 +57,7 @@ struct EeArgs {
   const float4* dm1f;
   const double* f;                   // [nk][nb] occupations when dm is null
   const EeScreen* scr;
+  const double* vqtab;               // [n0 n1 n2] static RPA vq by the q mesh index (EE_RPA)
   double2* Pee;                      // [npair][2][nb^4]: P1ee, P2ee (prefactor included)
 };
 
@@ -73,11 +74,20 @@ __device__ __forceinline__ double ee_q2(const EeArgs& a, double q0, double q1, d
          2 * (v[0] * v[1] * m[1] + v[0] * v[2] * m[2] + v[1] * v[2] * m[5]);
 }
 
-// coulomb_model::vq, static branches (Coulomb_Model.h:632-660), q = k_i - k_j
+__device__ __forceinline__ size_t ee_qmesh(const int* kmesh, int4 u, int4 v) {
+  int m0 = (u.x - v.x) % kmesh[0], m1 = (u.y - v.y) % kmesh[1], m2 = (u.z - v.z) % kmesh[2];
+  m0 += m0 < 0 ? kmesh[0] : 0;
+  m1 += m1 < 0 ? kmesh[1] : 0;
+  m2 += m2 < 0 ? kmesh[2] : 0;
+  return ((size_t)m0 * kmesh[1] + m1) * kmesh[2] + m2;
+}
+
+// coulomb_model::vq, static branches (Coulomb_Model.h:632-666), q = k_i - k_j
 __device__ __forceinline__ double ee_vq(const EeArgs& a, const EeScreen& s, int ki, int kj) {
   const double* x = a.kvec + 3 * ki;
   const double* y = a.kvec + 3 * kj;
   const double q2 = ee_q2(a, x[0] - y[0], x[1] - y[1], x[2] - y[2]);
+  if (a.formula == EE_RPA) return q2 < 1e-20 ? 0.0 : a.vqtab[ee_qmesh(a.kmesh, a.kidx[ki], a.kidx[kj])];
   if (a.formula == EE_UNSCREENED) return q2 < 1e-20 ? 0.0 : s.prefac_vq / q2;
   if (a.formula == EE_DEBYE) return s.prefac_vq / (s.qscr2_debye + q2);
   if (q2 < 1e-20) return 0.0;
@@ -93,6 +103,56 @@ __device__ __forceinline__ double2 ee_ovlp(const EeArgs& a, int ki, int kj, int 
   double2 s = mk2(0, 0);
   for (int w = 0; w < a.nbw; ++w) s = cfma_conja(ui[w * NB + c], uj[w * NB + d], s);
   return s;
+}
+
+// static RPA screening (Coulomb_Model.h:690-736): one thread per ordered pair (i, j) of k-points adds
+// sum_(b1,b2) dfde |<i b1|j b2>|^2 to the accumulator of the mesh index of q = k_i - k_j (FP64
+// atomics), with dfde = (f_j - f_i) / (e_i - e_j), or (1 - f) f / T at degenerate energies
+template <int NB>
+__global__ void k_ee_rpa_sum(EeArgs a, double T, const double* __restrict__ f, double* __restrict__ qacc,
+                             unsigned int* __restrict__ qhit) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)a.nk * a.nk) return;
+  const int i = (int)(idx / a.nk), j = (int)(idx % a.nk);
+  const int4 vi = a.kidx[i], vj = a.kidx[j];
+  // the k-point of this mesh index as the table keeps it (a duplicate index is served by its first k)
+  if (a.kmap[((size_t)vj.x * a.kmesh[1] + vj.y) * a.kmesh[2] + vj.z] != j) return;
+  double g = 0;
+#pragma unroll
+  for (int b1 = 0; b1 < NB; ++b1)
+#pragma unroll
+    for (int b2 = 0; b2 < NB; ++b2) {
+      const double de = a.ew[(size_t)i * NB + b1] - a.ew[(size_t)j * NB + b2];
+      double dfde;
+      if (fabs(de) < 1e-8) {
+        const double favg = 0.5 * (f[(size_t)i * NB + b1] + f[(size_t)j * NB + b2]);
+        dfde = (1 - favg) * favg / T;
+      } else {
+        dfde = (f[(size_t)j * NB + b2] - f[(size_t)i * NB + b1]) / de;
+      }
+      const double2 o = ee_ovlp<NB>(a, i, j, b1, b2);
+      g += dfde * (o.x * o.x + o.y * o.y);
+    }
+  const size_t m = ee_qmesh(a.kmesh, vi, vj);
+  atomicAdd(&qacc[m], g);
+  qhit[m] = 1u;
+}
+
+// vq = prefac_vq / (|q|^2 + qscr2) for every q mesh index that occurs (Coulomb_Model.h:819-826);
+// |q|^2 from the mesh index wrapped to [-0.5, 0.5)
+__global__ void k_ee_rpa_table(EeArgs a, double prefac_vq, double nk_full, const double* __restrict__ qacc,
+                               const unsigned int* __restrict__ qhit, double* __restrict__ vqtab) {
+  const size_t n = (size_t)a.kmesh[0] * a.kmesh[1] * a.kmesh[2];
+  const size_t m = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  if (!qhit[m]) {
+    vqtab[m] = 0.0;
+    return;
+  }
+  const int m2 = (int)(m % a.kmesh[2]), m1 = (int)((m / a.kmesh[2]) % a.kmesh[1]), m0 = (int)(m / ((size_t)a.kmesh[1] * a.kmesh[2]));
+  const double q2 = ee_q2(a, (double)m0 / a.kmesh[0], (double)m1 / a.kmesh[1], (double)m2 / a.kmesh[2]);
+  const double qs = prefac_vq / nk_full * qacc[m];
+  vqtab[m] = q2 < 1e-20 ? 0.0 : prefac_vq / (q2 + qs);
 }
 
 // the window density matrix in the Schrodinger picture and 1 - rho from the state y (one thread per

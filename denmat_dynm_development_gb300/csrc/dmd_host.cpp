@@ -367,8 +367,10 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
       return err(DMD_E_ARG, "eeMode must be none, Pee_fixed_at_eq or Pee_update");
     if (scr_mode != "medium") return err(DMD_E_ARG, "the e-e model needs scrMode = medium");
     const std::string f = sget(pm, "scrFormula", "RPA");
-    if (f != "unscreened" && f != "debye" && f != "Bechstedt")
-      return err(DMD_E_ARG, "scrFormula " + f + " is not supported (unscreened, debye, Bechstedt are)");
+    if (f == "lindhard")  // the reference builds no vq table for it (init_RPA runs for RPA only)
+      return err(DMD_E_ARG, "scrFormula lindhard has no static vq table in the reference (Coulomb_Model.h:537-545)");
+    if (f != "unscreened" && f != "debye" && f != "Bechstedt" && f != "RPA")
+      return err(DMD_E_ARG, "scrFormula " + f + " is not supported (unscreened, debye, Bechstedt, RPA are)");
     if (sget(pm, "dynamic_screening", "static") != "static") return err(DMD_E_ARG, "only static screening is supported");
     if (linear) return err(DMD_E_ARG, "the e-e model is not supported with alg_linearize");
     if (pget(pm, "alg_ddmdteq", 0) != 0) return err(DMD_E_ARG, "the e-e model is not supported with alg_ddmdteq");
@@ -725,7 +727,10 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
     ee.temperature = T;
     ee.eps_background = pget(pm, "epsilon_background", 1);
     ee.meff = pget(pm, "meff_screening", 1);
-    ee.formula = f == "unscreened" ? DMD_SCREEN_UNSCREENED : f == "debye" ? DMD_SCREEN_DEBYE : DMD_SCREEN_BECHSTEDT;
+    ee.formula = f == "unscreened" ? DMD_SCREEN_UNSCREENED
+                 : f == "debye"    ? DMD_SCREEN_DEBYE
+                 : f == "RPA"      ? DMD_SCREEN_RPA
+                                   : DMD_SCREEN_BECHSTEDT;
     ee.nfree = s->nfree;
     ee.update_screening = pget(pm, "update_screening", 1) != 0;
     ee.nv = in.nv_dm - bs;  // coul_model->nv (Coulomb_Model.h:418)

@@ -48,7 +48,7 @@ class _EEDesc(C.Structure):
                 ("every_rhs", C.c_int32)]
 
 
-SCREEN = {"unscreened": 0, "debye": 1, "Bechstedt": 2}
+SCREEN = {"unscreened": 0, "debye": 1, "Bechstedt": 2, "RPA": 3}
 
 _L = None
 

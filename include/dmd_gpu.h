@@ -209,13 +209,16 @@ int dmd_selftest_wait_timeout(int device, uint32_t polls, int* status);
 #define DMD_SCREEN_UNSCREENED 0 /* clp.scrFormula = "unscreened" */
 #define DMD_SCREEN_DEBYE 1      /* "debye" */
 #define DMD_SCREEN_BECHSTEDT 2  /* "Bechstedt" */
+#define DMD_SCREEN_RPA 3        /* "RPA" with static screening: the q table of calc_qscr2_static_RPA
+                                   (Coulomb_Model.h:690-736, 819-826) from f and U, built at attach */
 
 typedef struct dmd_ee_desc {
   int32_t nbw;              /* Wannier functions (elec->nb_wannier) */
   const double* kvec;       /* [nk][3] fractional k-points (ldbd_kvec.bin) */
   int32_t kmesh[3];         /* elec->kmesh */
   const double* U;          /* complex128 [nk][nbw][nb]: the window's columns of U (ldbd_Umat.bin) */
-  const double* f;          /* [nk][nb] window occupations of the set-up (coul_model->f) */
+  const double* f;          /* [nk][nb] window occupations of the set-up (coul_model->f; also the
+                               occupations of the static RPA screening, which later updates keep) */
   double GGT[9];            /* reciprocal metric, row-major (lattice.h:41-42) */
   double cell_size;         /* latt->cell_size */
   double nk_full;           /* elec->nk_full */

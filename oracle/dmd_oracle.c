@@ -63,7 +63,7 @@ typedef struct orc_ee {
   const zc* U;             /* [nk][nbw][nb] (electron.cpp:388-410) */
   double GGT[9];           /* lattice.h:41-42 */
   double cell_size, nk_full, T, eps, meff;
-  int formula;             /* 0 unscreened, 1 debye, 2 Bechstedt (clp.scrFormula) */
+  int formula;             /* 0 unscreened, 1 debye, 2 Bechstedt, 3 RPA, 4 lindhard (clp.scrFormula) */
   double nfree;            /* clp.nfreetot: the screening density */
   int update_screening;    /* clp.update: nfree from rho at each rebuild (Coulomb_Model.h:533-553) */
   int nv;                  /* coul_model->nv: window bands below it count holes */
@@ -77,6 +77,8 @@ typedef struct orc_ee {
   zc* P2eff;
   zc* P1ee;                /* the last P_ee (prefactor included, scale not) */
   zc* P2ee;
+  const double* f_setup;   /* [nk][nb] window occupations of the set-up (coul_model->f): static RPA */
+  double* vq_rpa;          /* [n0 n1 n2] static RPA / Lindhard vq by the q mesh index (orc_ee_rpa_table) */
 } orc_ee;
 
 void orc_ee_rebuild(struct orc_ee* ee, const orc_sys* s, double t, const double* y);
@@ -414,9 +416,17 @@ static ee_scr ee_screen(const orc_ee* ee, double n) {
   return c;
 }
 
+static void ee_ikvec3(const orc_ee* ee, const double* k, int* v);
+
 /* coulomb_model::vq, static branches (Coulomb_Model.h:632-660) */
 static double ee_vq(const orc_ee* ee, const ee_scr* c, const double* q) {
   const double q2 = ee_q2(ee, q);
+  if (ee->formula >= 3) { /* vq_RPA[q2iq(q)][0].real() (Coulomb_Model.h:662-666) */
+    if (q2 < 1e-20) return 0.0;
+    int v[3];
+    ee_ikvec3(ee, q, v);
+    return ee->vq_rpa[((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2]];
+  }
   if (ee->formula == 0) return q2 < 1e-20 ? 0.0 : c->prefac_vq / q2;
   if (ee->formula == 1) return c->prefac_vq / (c->qscr2_debye + q2);
   if (q2 < 1e-20) return 0.0;
@@ -454,6 +464,86 @@ static void ee_ovlp(const orc_ee* ee, const ee_scr* c, zc* ovlp, zc* Uih, int ik
   for (int d = 0; d < 3; d++) q[d] = ee->kvec[3 * ik + d] - ee->kvec[3 * jk + d];
   const zc vq = zmk(ee_vq(ee, c, q), 0);
   for (int i = 0; i < nb * nb; i++) ovlp[i] = zmul(vq, ovlp[i]); /* axbyc(ovlp, nullptr, n, c0, vq) */
+}
+
+/* coulomb_model's static RPA / Lindhard screening (Coulomb_Model.h:690-736 calc_qscr2_static_RPA,
+ * 819-826 calc_vq_RPA, static): the q set of qIndexMap::build (comm/kmap.h:43-56: every k_i - k_j, first
+ * occurrence of a mesh index), then for each q in that order and each k in order with k - q on the
+ * set, dfde |<k|k-q>|^2 summed (Lindhard: b1 = b2, no overlap), times prefac_vq / nk_full, and
+ * vq = prefac_vq / (|q|^2 + qscr2) with scalar.h's complex division. Stored by q mesh index. */
+void orc_ee_rpa_table(orc_ee* ee, int nk, const double* e /* [nk][nb] */) {
+  const int nb = ee->nb;
+  const size_t nmesh = (size_t)ee->kmesh[0] * ee->kmesh[1] * ee->kmesh[2];
+  int* table = (int*)xmalloc(sizeof(int) * nmesh);
+  for (size_t i = 0; i < nmesh; i++) table[i] = -1;
+  for (int ik = 0; ik < nk; ik++) {
+    int v[3];
+    ee_ikvec3(ee, ee->kvec + 3 * ik, v);
+    int* slot = &table[((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2]];
+    if (*slot < 0) *slot = ik;
+  }
+  /* qvec in qIndexMap::build order: wrap(k_ik - k_jk), the first of each mesh index */
+  int* qseen = (int*)xmalloc(sizeof(int) * nmesh);
+  for (size_t i = 0; i < nmesh; i++) qseen[i] = -1;
+  double* qvec = (double*)xmalloc(sizeof(double) * 3 * (size_t)nk * nk);
+  size_t nq = 0;
+  for (int ik = 0; ik < nk; ik++)
+    for (int jk = 0; jk < nk; jk++) {
+      double d[3], q[3];
+      for (int x = 0; x < 3; x++) d[x] = ee->kvec[3 * ik + x] - ee->kvec[3 * jk + x];
+      ee_wrap(d, q);
+      int v[3];
+      ee_ikvec3(ee, q, v);
+      const size_t m = ((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2];
+      if (qseen[m] < 0) {
+        qseen[m] = (int)nq;
+        memcpy(qvec + 3 * nq, q, sizeof(q));
+        nq++;
+      }
+    }
+  ee_scr c = ee_screen(ee, ee->nfree);
+  zc* Uih = (zc*)xmalloc(sizeof(zc) * nb * ee->nbw);
+  zc* ovlp = (zc*)xmalloc(sizeof(zc) * nb * nb);
+  for (size_t iq = 0; iq < nq; iq++) {
+    const double* q = qvec + 3 * iq;
+    zc sum = zmk(0, 0);
+    for (int ik = 0; ik < nk; ik++) {
+      double kj[3];
+      for (int x = 0; x < 3; x++) kj[x] = ee->kvec[3 * ik + x] - q[x];
+      const int jk = ee_findk(ee, table, kj);
+      if (jk < 0) continue;
+      ee_ovlp(ee, &c, ovlp, Uih, ik, jk, 0);
+      for (int b1 = 0; b1 < nb; b1++)
+        for (int b2 = 0; b2 < nb; b2++) {
+          if (ee->formula == 4 && b1 != b2) continue;
+          const double de = e[ik * nb + b1] - e[jk * nb + b2];
+          zc dfde;
+          if (sqrt(de * de + 0.0 * 0.0) < 1e-8) { /* abs(complex) (scalar.h:103) */
+            const double favg = 0.5 * (ee->f_setup[ik * nb + b1] + ee->f_setup[jk * nb + b2]);
+            dfde = zmk((1 - favg) * favg / ee->T, 0);
+          } else { /* complex(f_j - f_i, 0) / complex(de, 0) (scalar.h:99) */
+            const double fd = ee->f_setup[jk * nb + b2] - ee->f_setup[ik * nb + b1];
+            const double nrm = de * de + 0.0 * 0.0, r = 1.0 / nrm;
+            dfde = zmk((fd * de + 0.0 * 0.0) * r, (0.0 * de - fd * 0.0) * r);
+          }
+          if (ee->formula == 3) {
+            const double n2 = ovlp[b1 * nb + b2].x * ovlp[b1 * nb + b2].x + ovlp[b1 * nb + b2].y * ovlp[b1 * nb + b2].y;
+            sum = zadd(sum, zmk(dfde.x * n2, dfde.y * n2));
+          } else {
+            sum = zadd(sum, dfde);
+          }
+        }
+    }
+    sum = zmul(zmk(c.prefac_vq / ee->nk_full, 0), sum);
+    const double q2 = ee_q2(ee, q);
+    /* complex(prefac_vq, 0) / (q2 + qscr2) */
+    const double dx = q2 + sum.x, dy = sum.y;
+    const double r = 1.0 / (dx * dx + dy * dy);
+    int v[3];
+    ee_ikvec3(ee, q, v);
+    ee->vq_rpa[((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2]] = (c.prefac_vq * dx + 0.0 * dy) * r;
+  }
+  free(table); free(qseen); free(qvec); free(Uih); free(ovlp);
 }
 
 /* elecelec_model::calc_P for every stored pair (ElecElec_Model.h:186-262, static screening,

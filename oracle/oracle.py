@@ -71,6 +71,8 @@ def lib():
         _lib.orc_ee_P.restype = None
         _lib.orc_ee_rebuild.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
         _lib.orc_ee_rebuild.restype = None
+        _lib.orc_ee_rpa_table.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_ee_rpa_table.restype = None
         _lib.orc_rhs_parts.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_rk4.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_long, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p]
         _lib.orc_rkf45.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -120,10 +122,10 @@ class _EE(C.Structure):
                 ("update_screening", C.c_int), ("nv", C.c_int), ("degauss", C.c_double), ("ethr", C.c_double),
                 ("antisym", C.c_int), ("scale", C.c_double), ("inside", C.c_int), ("P1base", C.c_void_p),
                 ("P2base", C.c_void_p), ("P1eff", C.c_void_p), ("P2eff", C.c_void_p), ("P1ee", C.c_void_p),
-                ("P2ee", C.c_void_p)]
+                ("P2ee", C.c_void_p), ("f_setup", C.c_void_p), ("vq_rpa", C.c_void_p)]
 
 
-EE_FORMULAS = {"unscreened": 0, "debye": 1, "Bechstedt": 2}
+EE_FORMULAS = {"unscreened": 0, "debye": 1, "Bechstedt": 2, "RPA": 3, "lindhard": 4}
 
 
 def ggt_of(R):
@@ -158,7 +160,7 @@ class EEModel:
     P1eff, P2eff are the system's P1, P2: P_base + scale P_ee, rebuilt in place from rho."""
 
     def __init__(self, *, nb, kvec, kmesh, U, GGT, cell_size, nk_full, T, eps, meff, formula, nfree, update_screening,
-                 nv, degauss, ethr, antisym, scale, inside, P1base, P2base):
+                 nv, degauss, ethr, antisym, scale, inside, P1base, P2base, f_setup=None, e_window=None):
         self.kvec = np.ascontiguousarray(kvec, np.float64)
         self.U = np.ascontiguousarray(U, np.complex128)
         self.P1base = np.ascontiguousarray(P1base, np.complex128)
@@ -175,12 +177,21 @@ class EEModel:
         self.update_screening, self.nv = int(update_screening), int(nv)
         self.degauss, self.ethr, self.antisym, self.scale = degauss, ethr, int(antisym), scale
         self.inside = int(inside)
+        self.f_setup = None if f_setup is None else np.ascontiguousarray(f_setup, np.float64)
+        self.vq_rpa = np.zeros(int(np.prod(self.kmesh)), np.float64) if self.formula >= 3 else None
         self.c = _EE(nb=self.nb, nbw=self.nbw, kvec=self.kvec.ctypes.data, kmesh=(C.c_int * 3)(*self.kmesh),
                      U=self.U.ctypes.data, GGT=(C.c_double * 9)(*self.GGT), cell_size=cell_size, nk_full=nk_full, T=T,
                      eps=eps, meff=meff, formula=self.formula, nfree=nfree, update_screening=self.update_screening,
                      nv=self.nv, degauss=degauss, ethr=ethr, antisym=self.antisym, scale=scale, inside=self.inside,
                      P1base=self.P1base.ctypes.data, P2base=self.P2base.ctypes.data, P1eff=self.P1eff.ctypes.data,
-                     P2eff=self.P2eff.ctypes.data, P1ee=self.P1ee.ctypes.data, P2ee=self.P2ee.ctypes.data)
+                     P2eff=self.P2eff.ctypes.data, P1ee=self.P1ee.ctypes.data, P2ee=self.P2ee.ctypes.data,
+                     f_setup=None if self.f_setup is None else self.f_setup.ctypes.data,
+                     vq_rpa=None if self.vq_rpa is None else self.vq_rpa.ctypes.data)
+        if self.formula >= 3:  # the static RPA / Lindhard screening of the set-up (Coulomb_Model.h:690-826)
+            if self.f_setup is None or e_window is None:
+                raise ValueError("RPA / lindhard screening needs the set-up occupations and energies")
+            ew = np.ascontiguousarray(e_window, np.float64)
+            lib().orc_ee_rpa_table(C.addressof(self.c), C.c_int(self.kvec.shape[0]), ew.ctypes.data)
 
     @property
     def nfree(self):
@@ -477,7 +488,8 @@ def load(d: str) -> OracleSystem:
                      update_screening=int(pget(pm, "update_screening", 1)), nv=nv_dm - bstart,
                      degauss=pget(pm, "degauss_ee", degauss / eV, eV), ethr=degauss * ndegauss,
                      antisym=int(pget(pm, "ee_antisymmetry", 0)), scale=pget(pm, "scale_ee", scale_scatt),
-                     inside=pget(pm, "freq_update_ee_model", 0) < 0, P1base=P1, P2base=P2)
+                     inside=pget(pm, "freq_update_ee_model", 0) < 0, P1base=P1, P2base=P2,
+                     f_setup=f_dm[:, bstart:bend], e_window=e_dm[:, bstart:bend])
         # set-up (ElectronPhonon.cpp:3-14): P_ee at the equilibrium occupations with the set-up density
         tmp = OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
                            k1st=k1, k2nd=k2, P1=ee.P1eff, P2=ee.P2eff, prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=None,

@@ -87,6 +87,15 @@ CASES = {
     "ee_nb4_unscreened": dict(cfg=SynthConfig(nk=16, nb=4, seed=33, de_pair_mev=60.0, nwannier=6, kball=True),
                               param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0.5, 0.3, 0),
                                          extra=dict(EE_COMMON, scrFormula="unscreened", update_screening=0))),
+    # static RPA screening (the reference's default scrFormula) with the screening density updated
+    "ee_nb2_rpa": dict(cfg=SynthConfig(nk=36, nb=2, seed=34, de_pair_mev=60.0, nwannier=4, kball=True),
+                       param=dict(Bpert_T=(0, 0.05, 0.1), B_T=(0, 0, 0.7),
+                                  extra=dict(EE_COMMON, scrFormula="RPA", update_screening=1))),
+    # static RPA, nb = 4, exchange term
+    "ee_nb4_rpa_anti": dict(cfg=SynthConfig(nk=14, nb=4, seed=35, de_pair_mev=60.0, nwannier=6, kball=True),
+                            param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0.3, 0, 0.2),
+                                       extra=dict(EE_COMMON, scrFormula="RPA", update_screening=1,
+                                                  ee_antisymmetry=1))),
     # two valence bands below the e-ph window (holes: nv_dm = 2), equilibrium drift subtracted
     "nb2_holes_eq": dict(cfg=SynthConfig(nk=24, nb=2, seed=17, de_pair_mev=60.0, extra_bands=2, nv=2),
                          param=dict(Bpert_T=(0.1, 0, 0.05), B_T=(0, 0, 1.0), extra={"alg_ddmdteq": 1})),

@@ -145,7 +145,8 @@ def test_load_ee_model_matches_reference_setup(case, host, oracle):
 
 
 def test_ee_options_outside_the_path_are_rejected(host, tmp_path):
-    for extra, msg in [("scrFormula = RPA\n", "scrFormula RPA"), ("dynamic_screening = ppa\n", "static"),
+    for extra, msg in [("scrFormula = heg\n", "scrFormula heg"), ("scrFormula = lindhard\n", "lindhard"),
+                       ("dynamic_screening = ppa\n", "static"),
                        ("alg_ddmdteq = 1\n", "alg_ddmdteq"), ("freq_update_eimp_model = 3\n", "freq_update_eimp_model")]:
         dst = str(tmp_path / ("c%d" % len(msg)))
         shutil.copytree(os.path.join(GOLDEN, "ee_nb2_debye"), dst)

@@ -144,4 +144,4 @@ def test_ee_cases_cover_the_model():
         seen.add(pm["scrFormula"])
         seen.add("anti" if pm.get("ee_antisymmetry", "0") == "1" else "direct")
         seen.add(pm.get("alg_picture", "interaction"))
-    assert {"debye", "Bechstedt", "unscreened", "anti", "direct", "schrodinger", "interaction"} <= seen
+    assert {"debye", "Bechstedt", "unscreened", "RPA", "anti", "direct", "schrodinger", "interaction"} <= seen
