@@ -1429,9 +1429,9 @@ static int create_impl(const dmd_desc* d, dmd_handle** out, PairSource* src) {
   if (!h->use_tc)
     h->pair_bytes = h->use_cb ? (int64_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) : (int64_t)h->npair * 2 * h->nb4 * 16;
   if (src && (!h->use_cb || h->use_tc || h->adj)) return bail(fail(h, DMD_E_ARG, "streamed operators need the column-block form"));
-  if (h->eek && (!h->use_cb || h->use_tc || h->nrhs != 1 || h->lin || src))
-    return bail(fail(h, DMD_E_ARG, "DMD_FLAG_EE needs nb = 2 or 4, a single state, no linearization and the "
-                                   "operators as arrays"));
+  if (h->eek && (!h->use_cb || h->use_tc || h->nrhs != 1 || h->lin || src || h->adj))
+    return bail(fail(h, DMD_E_ARG, "DMD_FLAG_EE needs nb = 2 or 4, a single state, no linearization, no adjoint "
+                                   "(P_ee depends on rho) and the operators as arrays"));
   h->src = src;
   rc = h->use_tc ? upload_pairs_tc(h, d) : h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d);
   h->src = nullptr;

@@ -61,7 +61,7 @@ extern "C" {
                                (one extra copy of P on the device; single state only) */
 #define DMD_FLAG_EE 4u      /* keep the operators P_eph (+ P_eimp) in their stored order and the
                                column-block map, for the e-e model (dmd_ee_attach); single state,
-                               not linearized, operators given as arrays */
+                               not linearized, not with DMD_FLAG_ADJOINT, operators given as arrays */
 
 /* pictures (alg.picture) */
 #define DMD_PICTURE_INTERACTION 0

@@ -211,3 +211,40 @@ def test_ee_host_library_rkf45_vs_golden_gsl(case, oracle, built):
     print("%s: RKF45 S_z rel err %.3g, state %.3g, ncalls %s" % (case, e, rel(y, g["gsl_y"]), nf))
     assert rel(y, g["gsl_y"]) < 1e-10 and e < 1e-10
     np.testing.assert_array_equal(np.array(nf), g["gsl_ncalls"])
+
+
+def test_ee_argument_and_order_checks(oracle, built):
+    """dmd_ee_attach needs DMD_FLAG_EE (DMD_E_STATE without it), a second attach is refused, update and
+    read need an attached model, the flag is refused with the adjoint and for batches, and a bad
+    description is DMD_E_ARG; the handle stays usable after each refusal."""
+    from denmat_dynm_development_gb300.dmd import DMDError, LindbladGPU
+    s, g = fresh(oracle, "ee_nb2_debye")
+    common = dict(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
+                  P1=s.ee.P1base, P2=s.ee.P2base, prefac_eph=s.prefac_eph, Hcoh=s.Hcoh, picture=s.picture_schrodinger,
+                  expt=s.expt)
+    with LindbladGPU(precision="f64", **common) as plain:
+        with pytest.raises(DMDError) as ex:
+            plain.ee_attach(**ee_desc(s))
+        assert ex.value.status == 7  # DMD_E_STATE
+        with pytest.raises(DMDError):
+            plain.ee_update()
+        out = plain.func(g["rhs_t"][0], g["rhs_y"][0])
+        assert np.isfinite(out).all()
+    for kw in (dict(adjoint=True), dict(nrhs=2, precision="bf16x2", f_ref=s.f_dm)):
+        args = dict(common, precision="f64")
+        args.update(kw)
+        with pytest.raises(DMDError) as ex:
+            LindbladGPU(ee_flag=True, **args)
+        assert ex.value.status == 1  # DMD_E_ARG
+    with LindbladGPU(precision="f64", ee_flag=True, **common) as gpu:
+        bad = ee_desc(s)
+        bad["degauss"] = 0.0
+        with pytest.raises(DMDError) as ex:
+            gpu.ee_attach(**bad)
+        assert ex.value.status == 1
+        gpu.ee_attach(**ee_desc(s))
+        with pytest.raises(DMDError) as ex:
+            gpu.ee_attach(**ee_desc(s))
+        assert ex.value.status == 7
+        e = rel(gpu.func(g["rhs_t"][1], g["rhs_y"][1]), g["rhs_dydt"][1])
+        assert e < RHS_TOL["f64"]
