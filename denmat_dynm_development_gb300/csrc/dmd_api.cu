@@ -235,6 +235,10 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
       k_prep_herm<ArithDF, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_inv, ta, h->expt,
                                                       (float2*)h->d_rs, h->d_acc, h->d_hflag, fref, h->d_acc0, h->lin,
                                                       h->nrhs, qc, h->d_ph, 1);
+    else if (h->use_tc)  // one thread per (rank, state chunk) for the tensor-core form
+      k_prep_tc<NB><<<dim3(blocks_for(h->nk, 128), (h->nrhs + qc - 1) / qc), 128, 0, h->st>>>(
+          h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_inv, ta, h->expt, (float*)h->d_rs, h->d_hflag, fref, h->nrhs, qc,
+          (float2*)h->d_ph);
     else if (deviation_form(h->prec))
       k_prep_herm<ArithF32, NB><<<g, 256, 0, h->st>>>(h->nk, h->nbdm, h->bs, y, h->d_ew, h->d_inv, ta, h->expt,
                                                        (float*)h->d_rs, h->use_tc ? nullptr : h->d_acc, h->d_hflag,

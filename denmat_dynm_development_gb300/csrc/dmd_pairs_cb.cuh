@@ -355,6 +355,98 @@ __global__ void k_prep_herm(int nk, int nbdm, int bs, const double2* __restrict_
   }
 }
 
+// Prep of the tensor-core batched form: the same r coordinates and FP32 phases as k_prep_herm's
+// FP32 tensor-core path, but one thread per (energy rank p, chunk of qc states) covering all nb^2
+// elements, so that every lane of a warp runs the same code (the per-element form leaves the lanes of
+// i > j idle and splits diagonal from off-diagonal work) and each state's window block is read and
+// its coordinates written as whole vectors.
+template <int NB>
+__global__ void k_prep_tc(int nk, int nbdm, int bs, const double2* __restrict__ y, const double* __restrict__ ew,
+                          const int* __restrict__ inv, TimeArg ta, int phase, float* __restrict__ rs,
+                          unsigned int* __restrict__ hflag, const double* __restrict__ fref, int nrhs, int qc,
+                          float2* __restrict__ ph) {
+  constexpr int NB2 = NB * NB;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nk) return;
+  const int q0 = blockIdx.y * qc, q1 = min(nrhs, q0 + qc);
+  const size_t cstride = (size_t)nk * 2 * NB2;
+  const size_t sstride = (size_t)nk * nbdm * nbdm;
+  const int k = inv[p];
+  float2 dc[NB2];  // conj(D) for i < j
+#pragma unroll
+  for (int e = 0; e < NB2; ++e) dc[e] = make_float2(1.f, 0.f);
+  if (phase) {
+    const double t = eval_time(ta);
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int j = i + 1; j < NB; ++j) {
+        const double x = (ew[k * NB + i] - ew[k * NB + j]) * t;
+        const double xr = fma(-6.283185307179586, rint(x * 0.15915494309189535), x);
+        float sn, cs;
+        sincosf((float)xr, &sn, &cs);
+        dc[i * NB + j] = make_float2(cs, -sn);
+      }
+  }
+  if (ph && blockIdx.y == 0) {
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        const float2 d = i < j ? dc[i * NB + j] : (i > j ? dc[j * NB + i] : make_float2(1.f, 0.f));
+        ph[(size_t)k * NB2 + i * NB + j] = i < j ? make_float2(d.x, -d.y) : d;  // D = conj(conj(D)), D_ji = conj(D_ij)
+      }
+  }
+  double fi[NB];
+#pragma unroll
+  for (int i = 0; i < NB; ++i) fi[i] = fref ? fref[(size_t)k * NB + i] : 0.0;
+  for (int q = q0; q < q1; ++q) {
+    const double2* yk = y + (size_t)q * sstride + (size_t)k * nbdm * nbdm;
+    double2 v[NB2];
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int j = 0; j < NB; ++j) v[i * NB + j] = yk[(bs + i) * nbdm + bs + j];
+    float r[NB2], a[NB2];
+    bool nonherm = false;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      const double2 vii = v[i * NB + i];
+      r[i * NB + i] = __double2float_rn(fref ? __dsub_rn(vii.x, fi[i]) : vii.x);
+      a[i * NB + i] = __double2float_rn(vii.y);
+      nonherm |= vii.y != 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int j = i + 1; j < NB; ++j) {
+        const double2 vij = v[i * NB + j], vji = v[j * NB + i];
+        float2 hf = make_float2(0.5f * ((float)vij.x + (float)vji.x), 0.5f * ((float)vij.y - (float)vji.y));
+        float2 af = make_float2(0.f, 0.f);
+        if (vij.x != vji.x || vij.y != -vji.y) {  // not exactly Hermitian: the anti-Hermitian pass runs
+          nonherm = true;
+          const double2 hij = mk2(__dmul_rn(__dadd_rn(vij.x, vji.x), 0.5), __dmul_rn(__dsub_rn(vij.y, vji.y), 0.5));
+          const double2 dif = mk2(__dsub_rn(vij.x, vji.x), __dadd_rn(vij.y, vji.y));
+          hf = make_float2((float)hij.x, (float)hij.y);
+          af = make_float2((float)__dmul_rn(dif.y, 0.5), (float)__dmul_rn(-dif.x, 0.5));
+        }
+        const float2 d = dc[i * NB + j];
+        r[i * NB + j] = __fmaf_rn(d.x, hf.x, -d.y * hf.y);
+        r[j * NB + i] = __fmaf_rn(d.x, hf.y, d.y * hf.x);
+        a[i * NB + j] = __fmaf_rn(d.x, af.x, -d.y * af.y);
+        a[j * NB + i] = __fmaf_rn(d.x, af.y, d.y * af.x);
+      }
+    if (nonherm) atomicOr(hflag, 1u);
+    float4* rh = (float4*)(rs + (size_t)q * cstride + (size_t)p * 2 * NB2);
+    float4* ra = (float4*)(rs + (size_t)(nrhs + q) * cstride + (size_t)p * 2 * NB2);
+#pragma unroll
+    for (int e = 0; e < NB2 / 4; ++e) {
+      rh[e] = make_float4(r[4 * e], r[4 * e + 1], r[4 * e + 2], r[4 * e + 3]);
+      ra[e] = make_float4(a[4 * e], a[4 * e + 1], a[4 * e + 2], a[4 * e + 3]);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // The contraction. P2 is stored column-major, so both halves of a pair are consumed "line by
 // line": a Q1 row a gives X'_k[a] and a Q2 column j gives Y'_k[j], while the reverse sums Y'_c
