@@ -185,12 +185,33 @@ __global__ void k_finish(FinishArgs a) {
 
   // scattering finish on the window (evolve_eph.cpp:140-162, evolve_driver :21-32)
   if (DEV && a.want_eph) {
-    const float2* Xs = (const float2*)a.acc + (size_t)q * a.astride + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2;
-    float2 X[NB2], Y[NB2];
+    // the sums (and for nb = 2 the per-k constants) as 16-byte loads (every block starts on a
+    // 16-byte boundary); for nb = 4 the constants stay element loads, which keeps it free of spills
+    constexpr bool PRE = NB == 2;
+    const float4* Xs4 =
+        (const float4*)((const float2*)a.acc + (size_t)q * a.astride + (size_t)(a.pos ? a.pos[k] : k) * 2 * NB2);
+    float2 X[NB2], Y[NB2], X0[PRE ? NB2 : 1], Y0[PRE ? NB2 : 1], Dk[PRE ? NB2 : 1], V0[PRE ? NB2 : 1];
 #pragma unroll
-    for (int i = 0; i < NB2; ++i) {
-      X[i] = Xs[i];
-      Y[i] = Xs[NB2 + i];
+    for (int i = 0; i < NB2 / 2; ++i) {
+      const float4 x = Xs4[i], yv = Xs4[NB2 / 2 + i];
+      X[2 * i] = make_float2(x.x, x.y);
+      X[2 * i + 1] = make_float2(x.z, x.w);
+      Y[2 * i] = make_float2(yv.x, yv.y);
+      Y[2 * i + 1] = make_float2(yv.z, yv.w);
+      if constexpr (!PRE) continue;
+      const float4 x0 = a.x0y0 ? ((const float4*)(a.x0y0 + (size_t)k * 2 * NB2))[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 y0 =
+          a.x0y0 ? ((const float4*)(a.x0y0 + (size_t)k * 2 * NB2))[NB2 / 2 + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      X0[2 * i] = make_float2(x0.x, x0.y);
+      X0[2 * i + 1] = make_float2(x0.z, x0.w);
+      Y0[2 * i] = make_float2(y0.x, y0.y);
+      Y0[2 * i + 1] = make_float2(y0.z, y0.w);
+      const float4 d = a.phase ? ((const float4*)(a.ph32 + (size_t)k * NB2))[i] : make_float4(1.f, 0.f, 1.f, 0.f);
+      Dk[2 * i] = make_float2(d.x, d.y);
+      Dk[2 * i + 1] = make_float2(d.z, d.w);
+      const float4 v = a.v0 ? ((const float4*)(a.v0 + (size_t)k * NB2))[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      V0[2 * i] = make_float2(v.x, v.y);
+      V0[2 * i + 1] = make_float2(v.z, v.w);
     }
     if (a.herm) {  // X = (M^H)^-1 X'
 #pragma unroll
@@ -218,9 +239,16 @@ __global__ void k_finish(FinishArgs a) {
         if (i == j) dh[e] = make_float2((float)__dsub_rn(yk[(bs + i) * nd + bs + i].x, fk[i]), 0.f);
         else if (i < j) dh[e] = f2(yk[(bs + i) * nd + bs + j]);
         else dh[e] = make_float2(dh[j * NB + i].x, -dh[j * NB + i].y);
-        D[e] = (a.phase && i != j) ? a.ph32[(size_t)k * NB2 + e] : make_float2(1.f, 0.f);
-        const float2 x0 = a.x0y0 ? a.x0y0[(size_t)k * 2 * NB2 + e] : make_float2(0.f, 0.f);
-        const float2 y0 = a.x0y0 ? a.x0y0[(size_t)k * 2 * NB2 + NB2 + e] : make_float2(0.f, 0.f);
+        float2 x0, y0;
+        if constexpr (PRE) {
+          D[e] = (a.phase && i != j) ? Dk[e] : make_float2(1.f, 0.f);
+          x0 = X0[e];
+          y0 = Y0[e];
+        } else {
+          D[e] = (a.phase && i != j) ? a.ph32[(size_t)k * NB2 + e] : make_float2(1.f, 0.f);
+          x0 = a.x0y0 ? a.x0y0[(size_t)k * 2 * NB2 + e] : make_float2(0.f, 0.f);
+          y0 = a.x0y0 ? a.x0y0[(size_t)k * 2 * NB2 + NB2 + e] : make_float2(0.f, 0.f);
+        }
         PXd[e] = fmul(D[e], X[e]);
         PYd[e] = fmul(D[e], Y[e]);
         PXt[e] = ffma(D[e], x0, PXd[e]);
@@ -252,7 +280,10 @@ __global__ void k_finish(FinishArgs a) {
       for (int j = i; j < NB; ++j) {
         const float2 c1 = c[i * NB + j], c2 = c[j * NB + i];
         float2 vf = make_float2(pf * (c1.x + c2.x), pf * (c1.y - c2.y));
-        if (a.v0) vf = ffma(D[i * NB + j], a.v0[(size_t)k * NB2 + i * NB + j], vf);  // + D o V0
+        if (a.v0) {  // + D o V0
+          if constexpr (PRE) vf = ffma(D[i * NB + j], V0[i * NB + j], vf);
+          else vf = ffma(D[i * NB + j], a.v0[(size_t)k * NB2 + i * NB + j], vf);
+        }
         const double2 v = mk2((double)vf.x, (double)vf.y);
 #pragma unroll
         for (int w = 0; w < (i == j ? 1 : 2); ++w) {
@@ -262,7 +293,11 @@ __global__ void k_finish(FinishArgs a) {
             const double2 qv = a.eq[(size_t)k * NB2 + ii * NB + jj];
             if (ii == jj || a.picture == 1) u = csub_rn(u, qv);
             else {
-              const float2 d = a.phase ? a.ph32[(size_t)k * NB2 + ii * NB + jj] : make_float2(1.f, 0.f);
+              float2 d = make_float2(1.f, 0.f);
+              if (a.phase) {
+                if constexpr (PRE) d = Dk[ii * NB + jj];
+                else d = a.ph32[(size_t)k * NB2 + ii * NB + jj];
+              }
               u = csub_rn(u, cmul_rn(qv, mk2((double)d.x, (double)d.y)));
             }
           }
