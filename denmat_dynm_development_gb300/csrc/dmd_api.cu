@@ -358,7 +358,9 @@ int launch_finish(dmd_handle* h, FinishArgs a) {
   const dim3 g(blocks_for(h->nk, 128), h->nrhs);
   if constexpr (NB == 2 || NB == 4) {
     if (h->use_tc) {  // split FP64 / FP32 finish of the tensor-core form
-      if (h->nbdm == NB) k_finish<NB, NB, true><<<g, 128, 0, h->st>>>(a);
+      if (NB == 4 && h->nbdm == NB)  // one thread per row: a quarter of the registers
+        k_finish_rows<NB><<<dim3(blocks_for(h->nk, 128 / NB), h->nrhs), 128, 0, h->st>>>(a);
+      else if (h->nbdm == NB) k_finish<NB, NB, true><<<g, 128, 0, h->st>>>(a);
       else k_finish<NB, 0, true><<<g, 128, 0, h->st>>>(a);
       h->launches++;
       CKL();

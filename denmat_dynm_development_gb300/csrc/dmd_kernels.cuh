@@ -428,6 +428,182 @@ __global__ void k_finish(FinishArgs a) {
   }
 }
 
+// The split finish of k_finish<NB, NB, true> with NB threads per (k, state): thread i computes row i
+// of the result and the operands the rows share (the column terms D o (X + X0) and rho - F) go
+// through shared memory. Each thread then holds a row instead of the whole NB x NB block, which for
+// nb = 4 takes k_finish from 251 registers per thread (8 warps per SM) to a third of that. Same
+// arithmetic element by element, so the result equals k_finish's; the (j, i) element of the
+// Hermitian sum is formed from the (j, i) operands, which gives the exact conjugate of (i, j).
+// Blocks of 128 threads: 32 (k, state) groups of NB = 4 threads, blockIdx.y the state.
+template <int NB>
+__global__ void __launch_bounds__(128) k_finish_rows(FinishArgs a) {
+  constexpr int NB2 = NB * NB, GPB = 128 / NB;  // groups per block
+  __shared__ float2 sPX[GPB][NB2], sdh[GPB][NB2], sc[GPB][NB2];
+  __shared__ double2 sf[GPB][NB2];  // H(t), then the result's transpose (Euler)
+  const int g = threadIdx.x / NB, i = threadIdx.x % NB;
+  const int k = blockIdx.x * GPB + g;
+  const int q = blockIdx.y;
+  if (a.hflag && k == 0 && q == 0 && i == 0) *a.hflag = 0u;
+  const bool live = k < a.nk;  // dead groups still reach the warp barriers
+  const int kk = live ? k : 0;
+  const double t = eval_time(a.ta);
+  const size_t qs = (size_t)q * a.sstride;
+  const double2* yk = a.y + qs + (size_t)kk * NB2;
+  const unsigned gm = ((1u << NB) - 1u) << ((threadIdx.x & 31) / NB * NB);  // this group's lanes
+  double2 f[NB];
+#pragma unroll
+  for (int j = 0; j < NB; ++j) f[j] = mk2(0.0, 0.0);
+
+  // coherent term, row i (as k_finish)
+  if (a.want_coh) {
+    const double* ek = a.edm + (size_t)kk * NB;
+    if (a.H) {
+      const double2* Hk = a.H + (size_t)kk * NB2;
+#pragma unroll
+      for (int j = 0; j < NB; ++j)  // row i of H(t) into shared memory
+        sf[g][i * NB + j] =
+            (a.picture == 0 && i != j) ? cmul_rn(Hk[i * NB + j], ccis((ek[i] - ek[j]) * t)) : Hk[i * NB + j];
+      __syncwarp(gm);
+      auto hup = [&](int r, int c) {  // read with zhemm's upper-triangle semantics
+        if (r == c) return mk2(sf[g][r * NB + r].x, 0.0);
+        return r < c ? sf[g][r * NB + c] : cconj(sf[g][c * NB + r]);
+      };
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        double2 s1 = mk2(0.0, 0.0), s2 = mk2(0.0, 0.0);
+#pragma unroll
+        for (int l = 0; l < NB; ++l) s1 = cadd_rn(s1, cmul_rn(yk[i * NB + l], hup(l, j)));
+        const double2 c1 = cmul_rn(mk2(1.0, 0.0), s1);
+#pragma unroll
+        for (int l = 0; l < NB; ++l) s2 = cadd_rn(s2, cmul_rn(hup(i, l), yk[l * NB + j]));
+        const double2 o = cadd_rn(cmul_rn(mk2(1.0, 0.0), s2), cmul_rn(mk2(-1.0, 0.0), c1));
+        f[j] = cadd_rn(mk2(0.0, 0.0), cmul_rn(o, mk2(0.0, -1.0)));
+      }
+      __syncwarp(gm);  // sf is reused below
+    } else if (a.picture == 1) {
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        const double2 d = yk[i * NB + j];
+        const double2 c = mk2(-__dmul_rn(d.x, ek[j]), -__dmul_rn(d.y, ek[j]));
+        f[j] = cadd_rn(mk2(0.0, 0.0), cmul_rn(cadd_rn(c, cmul_rn(mk2(ek[i], 0.0), d)), mk2(0.0, -1.0)));
+      }
+    }
+  }
+
+  if (a.want_eph) {
+    const float2* Xs = (const float2*)a.acc + (size_t)q * a.astride + (size_t)(a.pos ? a.pos[kk] : kk) * 2 * NB2;
+    const double* fk = a.fref + (size_t)kk * NB;
+    float2 PXd[NB], PYd[NB], PYt[NB], D[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const int e = i * NB + j;
+      // X = (M^H)^-1 X' element (i, j) from X'(i, j) and X'(j, i)
+      float2 x = Xs[e], yv = Xs[NB2 + e];
+      if (a.herm && i != j) {
+        const int lo = i < j ? i : j, hi = i < j ? j : i;
+        const float2 xu = Xs[lo * NB + hi], xl = Xs[hi * NB + lo], yu = Xs[NB2 + lo * NB + hi],
+                     yl = Xs[NB2 + hi * NB + lo];
+        if (i < j) {
+          x = make_float2(0.5f * (xu.x - xl.y), 0.5f * (xu.y + xl.x));
+          yv = make_float2(0.5f * (yu.x - yl.y), 0.5f * (yu.y + yl.x));
+        } else {
+          x = make_float2(0.5f * (xu.x + xl.y), 0.5f * (xu.y - xl.x));
+          yv = make_float2(0.5f * (yu.x + yl.y), 0.5f * (yu.y - yl.x));
+        }
+      }
+      D[j] = (a.phase && i != j) ? a.ph32[(size_t)kk * NB2 + e] : make_float2(1.f, 0.f);
+      const float2 x0 = a.x0y0 ? a.x0y0[(size_t)kk * 2 * NB2 + e] : make_float2(0.f, 0.f);
+      const float2 y0 = a.x0y0 ? a.x0y0[(size_t)kk * 2 * NB2 + NB2 + e] : make_float2(0.f, 0.f);
+      PXd[j] = fmul(D[j], x);
+      PYd[j] = fmul(D[j], yv);
+      sPX[g][e] = ffma(D[j], x0, PXd[j]);
+      PYt[j] = ffma(D[j], y0, PYd[j]);
+      // herm_up(rho - F) (the diagonal difference in FP64)
+      float2 dh;
+      if (i == j) dh = make_float2((float)__dsub_rn(yk[i * NB + i].x, fk[i]), 0.f);
+      else if (i < j) dh = f2(yk[i * NB + j]);
+      else {
+        const float2 u = f2(yk[j * NB + i]);
+        dh = make_float2(u.x, -u.y);
+      }
+      sdh[g][e] = dh;
+    }
+    __syncwarp(gm);
+    const float fi = (float)fk[i];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      float2 c;
+      if (a.lin) {
+        c = PXd[j];
+      } else {
+        const float fj = (float)fk[j];
+        c = make_float2((1.f - fi) * PXd[j].x - fj * PYd[j].x, (1.f - fi) * PXd[j].y - fj * PYd[j].y);
+#pragma unroll
+        for (int l = 0; l < NB; ++l) {
+          const float2 d1 = sdh[g][i * NB + l], d2 = sdh[g][l * NB + j];
+          c = ffma(make_float2(-d1.x, -d1.y), sPX[g][l * NB + j], c);
+          c = ffma(make_float2(-PYt[l].x, -PYt[l].y), d2, c);
+        }
+      }
+      sc[g][i * NB + j] = c;
+    }
+    __syncwarp(gm);
+    const float pf = (float)(a.prefac * 0.5);
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const float2 c1 = sc[g][i * NB + j], c2 = sc[g][j * NB + i];
+      float2 vf = make_float2(pf * (c1.x + c2.x), pf * (c1.y - c2.y));
+      if (a.v0) vf = ffma(D[j], a.v0[(size_t)kk * NB2 + i * NB + j], vf);  // + D o V0
+      double2 u = mk2((double)vf.x, (double)vf.y);
+      if (a.eq) {
+        const double2 qv = a.eq[(size_t)kk * NB2 + i * NB + j];
+        if (i == j || a.picture == 1) u = csub_rn(u, qv);
+        else u = csub_rn(u, cmul_rn(qv, mk2((double)D[j].x, (double)D[j].y)));
+      }
+      f[j] = a.want_coh ? cadd_rn(f[j], u) : u;
+    }
+  }
+
+  if (!live) return;
+  const size_t base = qs + (size_t)k * NB2 + (size_t)i * NB;
+  if (a.mode == 0) {
+#pragma unroll
+    for (int j = 0; j < NB; ++j) a.out[base + j] = f[j];
+    return;
+  }
+  const size_t n = a.sstride * a.nrhs;
+  if (a.mode == 1) {
+    const double h = a.tref[1], hh = 0.5 * h, h6 = h / 6.0;
+    double2* Ks = a.K + (size_t)a.stage * n;
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const double2 yb = a.ybase[base + j];
+      Ks[base + j] = f[j];
+      if (a.stage == 0) a.ytmp[base + j] = cadd_rn(yb, cscale_rn(hh, f[j]));
+      else if (a.stage == 1) a.ytmp[base + j] = cadd_rn(yb, cscale_rn(hh, f[j]));
+      else if (a.stage == 2) a.ytmp[base + j] = cadd_rn(yb, cscale_rn(h, f[j]));
+      else {
+        const double2 k1 = a.K[base + j], k2 = a.K[n + base + j], k3 = a.K[2 * n + base + j];
+        const double sx = __dadd_rn(__dadd_rn(__dadd_rn(k1.x, __dmul_rn(2.0, k2.x)), __dmul_rn(2.0, k3.x)), f[j].x);
+        const double sy = __dadd_rn(__dadd_rn(__dadd_rn(k1.y, __dmul_rn(2.0, k2.y)), __dmul_rn(2.0, k3.y)), f[j].y);
+        a.ybase[base + j] = mk2(__dadd_rn(yb.x, __dmul_rn(h6, sx)), __dadd_rn(yb.y, __dmul_rn(h6, sy)));
+      }
+    }
+    return;
+  }
+  if (a.mode == 2) {  // update_dm_euler: dm += 0.5 dt (ddmdt + ddmdt^dagger); f^T through shared memory
+#pragma unroll
+    for (int j = 0; j < NB; ++j) sf[g][i * NB + j] = f[j];
+    __syncwarp(gm);
+    const double hf = 0.5 * a.tref[1];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const double2 v = cscale_rn(hf, cadd_rn(f[j], cconj(sf[g][j * NB + i])));
+      a.ybase[base + j] = cadd_rn(a.ybase[base + j], v);
+    }
+  }
+}
+
 // advance the device step counter after the last kernel of a step
 __global__ void k_step_inc(long long* step) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1;
