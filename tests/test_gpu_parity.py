@@ -708,3 +708,51 @@ def test_bounded_wait_gives_up_and_reports_a_timeout(oracle, built):
         gpu.rk4(1.0 * oracle.fs, 3)
         _, y = gpu.get_state()
         assert np.all(np.isfinite(y))
+
+
+def _random_system(oracle, nk, nb_dm, bstart, bend, npair, seed, with_H=True, picture=0):
+    """a random system with an arbitrary band window: random Hermitian states, energies, operators
+    (the RHS needs no structure of P) and pairs drawn with repeats and either orientation"""
+    rng = np.random.default_rng(seed)
+    nb = bend - bstart
+    e = np.sort(rng.uniform(0.05, 0.06, (nk, nb_dm)), axis=1)
+    f = 1.0 / (np.exp((e - 0.052) / 9.5e-4) + 1.0)
+    k1 = rng.integers(0, nk, npair).astype(np.uint64)
+    k2 = rng.integers(0, nk, npair).astype(np.uint64)
+    P1 = (rng.standard_normal((npair, nb ** 4)) + 1j * rng.standard_normal((npair, nb ** 4))) * 1e-3
+    P2 = (rng.standard_normal((npair, nb ** 4)) + 1j * rng.standard_normal((npair, nb ** 4))) * 1e-3
+    dm = rng.standard_normal((nk, nb_dm, nb_dm)) + 1j * rng.standard_normal((nk, nb_dm, nb_dm))
+    dm = 1e-3 * 0.5 * (dm + np.conj(np.swapaxes(dm, 1, 2)))
+    dm[:, range(nb_dm), range(nb_dm)] = f + 1e-3 * rng.standard_normal((nk, nb_dm))
+    H = None
+    if with_H:
+        H = rng.standard_normal((nk, nb_dm, nb_dm)) + 1j * rng.standard_normal((nk, nb_dm, nb_dm))
+        H = 1e-6 * 0.5 * (H + np.conj(np.swapaxes(H, 1, 2)))
+        if picture == 1:  # the Schrodinger picture's H carries the band energies
+            H[:, range(nb_dm), range(nb_dm)] += e
+        H = H.reshape(nk, -1)
+    return oracle.from_arrays(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, e_dm=e, f_dm=f, k1st=k1, k2nd=k2,
+                              P1=P1.reshape(-1), P2=P2.reshape(-1), prefac_eph=2 * np.pi / 1e5,
+                              dm0=dm.reshape(nk, -1), Hcoh=H, picture_schrodinger=picture, expt=1 - picture,
+                              smat=np.zeros((nk, 3, nb_dm * nb_dm), np.complex128))
+
+
+@pytest.mark.parametrize("nb_dm,bstart,bend,npair,picture", [(3, 0, 3, 150, 0), (1, 0, 1, 80, 1), (4, 1, 4, 60, 0),
+                                                             (2, 0, 2, 0, 0), (3, 1, 2, 50, 1)])
+def test_band_windows_and_empty_pairs_vs_oracle(nb_dm, bstart, bend, npair, picture, oracle, built):
+    """Windows outside the column-block form (nb = 1, 3 on the per-thread FP64 kernel, including a
+    window inside the density matrix), a system without k-pairs (the coherent term alone), both
+    pictures: the FP64 RHS and 5 RK4 steps against the oracle."""
+    s = _random_system(oracle, 23, nb_dm, bstart, bend, npair, seed=nb_dm * 10 + npair, picture=picture)
+    y = oracle.y_of(s.dm0)
+    t = 5.0 * oracle.fs
+    with make_gpu(s, "f64") as gpu:
+        e = rel(gpu.func(t, y), oracle.rhs(s, t, y))
+        gpu.set_state(0.0, y)
+        gpu.rk4(1.0 * oracle.fs, 5)
+        _, yg = gpu.get_state()
+    yo, _ = oracle.rk4(s, 0.0, 1.0 * oracle.fs, 5, y)
+    e2 = rel(yg - y, yo - y)
+    print("nb_dm %d window [%d,%d) npair %d picture %d: RHS rel err %.3g, 5-step change %.3g"
+          % (nb_dm, bstart, bend, npair, picture, e, e2))
+    assert e < RHS_TOL["f64"] and e2 < 1e-11
