@@ -428,13 +428,14 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
         }
       }
       __syncwarp();
-      if (act && w == 0) {  // row r = (i1, i3) of A (calc_delta, calc_mee[_ex], calc_A)
+      if (act) {  // row r = (i1, i3) of A, columns cd of half w (calc_delta, calc_mee[_ex], calc_A)
         const double* e3 = a.ew + (size_t)ka * NB;
         const double* e4 = a.ew + (size_t)kb * NB;
         const C m12 = sm.o12[i1 * NB + i3];
+        constexpr int HALF = NB2 / 2;  // both halves of the group share the row's elements
 #pragma unroll
-        for (int cd = 0; cd < NB2; ++cd) {
-          const int c = cd / NB, d = cd % NB;
+        for (int h = 0; h < HALF; ++h) {
+          const int cd = w * HALF + h, c = cd / NB, d = cd % NB;
           const double de = e1[i1] - e2[i3] + e3[c] - e4[d];  // the window test stays FP64
           C v = V::zero();
           if (fabs(de) < a.ethr) {
