@@ -16,9 +16,10 @@
 // GPU layout of the work: one warp per pair. Phase 1: the 32 lanes test 32 k3 at a time (k4 by
 // integer mesh arithmetic and a dense mesh table, energy window by per-k band ranges) and append
 // the candidates to a warp buffer. Phase 2: groups of G = 2 nb^2 lanes take one candidate each
-// (4 groups for nb = 2, one for nb = 4); lane (w, r), r = (i1, i3), builds one row of A into shared
-// memory, then forms its own A1rho (w = 0) or A1rhobar (w = 1) row and accumulates P1ee or P2ee
-// over (i2, i4) in registers. The groups' partial sums are added with shuffles at the end. The
+// (4 groups for nb = 2, one for nb = 4); lane (w, r), r = (i1, i3), forms the real (w = 0) or
+// imaginary (w = 1) part of the overlaps' entry r and half w of the columns of row r of A in shared
+// memory, then its own A1rho (w = 0) or A1rhobar (w = 1) row, and accumulates P1ee or P2ee over
+// (i2, i4) in registers. The groups' partial sums are added with shuffles at the end. The
 // candidate search, the overlaps, delta and A are FP64; the two contractions (A1rho and the
 // accumulation, 90 % of the multiply-adds) are FP64 for FP64 handles and double-float (FP32 pairs,
 // ~2^-47 per product, renormalised after every work item) otherwise: GB300's FP32 pipes run them at
@@ -74,8 +75,9 @@ __device__ __forceinline__ double ee_q2(const EeArgs& a, double q0, double q1, d
          2 * (v[0] * v[1] * m[1] + v[0] * v[2] * m[2] + v[1] * v[2] * m[5]);
 }
 
+// mesh index of u - v; both lie in [0, n), so the difference lies in (-n, n)
 __device__ __forceinline__ size_t ee_qmesh(const int* kmesh, int4 u, int4 v) {
-  int m0 = (u.x - v.x) % kmesh[0], m1 = (u.y - v.y) % kmesh[1], m2 = (u.z - v.z) % kmesh[2];
+  int m0 = u.x - v.x, m1 = u.y - v.y, m2 = u.z - v.z;
   m0 += m0 < 0 ? kmesh[0] : 0;
   m1 += m1 < 0 ? kmesh[1] : 0;
   m2 += m2 < 0 ? kmesh[2] : 0;
@@ -102,6 +104,22 @@ __device__ __forceinline__ double2 ee_ovlp(const EeArgs& a, int ki, int kj, int 
   const double2* uj = a.U + (size_t)kj * a.nbw * NB;
   double2 s = mk2(0, 0);
   for (int w = 0; w < a.nbw; ++w) s = cfma_conja(ui[w * NB + c], uj[w * NB + d], s);
+  return s;
+}
+
+// one part of ee_ovlp: the real (part 0) or imaginary (part 1) FMA chain of cfma_conja, with the
+// same operations in the same order, chosen by operand selection so that lanes with different
+// parts do not diverge
+template <int NB>
+__device__ __forceinline__ double ee_ovlp_part(const EeArgs& a, int ki, int kj, int c, int d, int part) {
+  const double2* ui = a.U + (size_t)ki * a.nbw * NB;
+  const double2* uj = a.U + (size_t)kj * a.nbw * NB;
+  double s = 0;
+  for (int w = 0; w < a.nbw; ++w) {
+    const double2 x = ui[w * NB + c], y = uj[w * NB + d];
+    // real: x.x y.x + (x.y y.y + s); imaginary: x.x y.y + (-x.y y.x + s)
+    s = fma(x.x, part ? y.y : y.x, fma(part ? -x.y : x.y, part ? y.x : y.y, s));
+  }
   return s;
 }
 
@@ -228,6 +246,9 @@ struct EeF64 {
   typedef double2 c;
   static __device__ __forceinline__ c zero() { return mk2(0, 0); }
   static __device__ __forceinline__ c from(double2 v) { return v; }
+  static __device__ __forceinline__ void set_part(c& dst, int part, double v) {  // from(), one part
+    reinterpret_cast<double*>(&dst)[part] = v;
+  }
   static __device__ __forceinline__ c load(const double2* d, const float4*, size_t i) { return d[i]; }
   static __device__ __forceinline__ void mac(c& acc, c x, c y) { acc = cfma(x, y, acc); }  // acc += x y
   static __device__ __forceinline__ void mac_conj(c& acc, c x, c y) {                      // acc += x conj(y)
@@ -243,6 +264,9 @@ struct EeDF {
   typedef float4 c;  // (re_h, re_l, im_h, im_l)
   static __device__ __forceinline__ c zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
   static __device__ __forceinline__ c from(double2 v) { return split_dfc(v); }
+  static __device__ __forceinline__ void set_part(c& dst, int part, double v) {  // from(), one part
+    reinterpret_cast<float2*>(&dst)[part] = split_df1(v);
+  }
   static __device__ __forceinline__ c load(const double2*, const float4* f, size_t i) { return f[i]; }
   static __device__ __forceinline__ void mac(c& a, c x, c y) {
     df_mac(a.x, a.y, x.x, x.y, y.x, y.y);
@@ -380,11 +404,11 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
     int k4 = -1;
     if (k3 < a.nk && !(a.antisym && k1 == k2 && k2 == k3)) {
       const int4 i3v = a.kidx[k3];
-      int m0 = (i1v.x + i3v.x - i2v.x) % a.kmesh[0], m1 = (i1v.y + i3v.y - i2v.y) % a.kmesh[1],
-          m2 = (i1v.z + i3v.z - i2v.z) % a.kmesh[2];
-      m0 += m0 < 0 ? a.kmesh[0] : 0;
-      m1 += m1 < 0 ? a.kmesh[1] : 0;
-      m2 += m2 < 0 ? a.kmesh[2] : 0;
+      // the mesh indices lie in [0, n), so i1 + i3 - i2 lies in (-n, 2n): one fold per axis
+      int m0 = i1v.x + i3v.x - i2v.x, m1 = i1v.y + i3v.y - i2v.y, m2 = i1v.z + i3v.z - i2v.z;
+      m0 += m0 < 0 ? a.kmesh[0] : (m0 >= a.kmesh[0] ? -a.kmesh[0] : 0);
+      m1 += m1 < 0 ? a.kmesh[1] : (m1 >= a.kmesh[1] ? -a.kmesh[1] : 0);
+      m2 += m2 < 0 ? a.kmesh[2] : (m2 >= a.kmesh[2] ? -a.kmesh[2] : 0);
       k4 = a.kmap[((size_t)m0 * a.kmesh[1] + m1) * a.kmesh[2] + m2];
       if (k4 >= 0) {  // some band combination inside the window, with a margin (exact FP64 test in phase 2)
         bool hit = false;
@@ -414,17 +438,14 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
       if (act) {
         ka = sm.cand[s].x;
         kb = sm.cand[s].y;
-        // overlaps of this candidate: lanes w = 0 build o34 (and o14), lanes w = 1 o32
+        // overlaps of this candidate: lane (w, r) forms the real (w = 0) or imaginary (w = 1) part of
+        // entry r of o34 (and of o14, o32 with the exchange term)
         const int c = r / NB, d = r % NB;
-        if (w == 0) {
-          sm.o34[grp][r] = V::from(ee_ovlp<NB>(a, ka, kb, c, d));
-          if (a.antisym) {
-            const double vq = ee_vq(a, scr, k1, kb);
-            const double2 o = ee_ovlp<NB>(a, k1, kb, c, d);
-            sm.o14[grp][r] = V::from(mk2(vq * o.x, vq * o.y));
-          }
-        } else if (a.antisym) {
-          sm.o32[grp][r] = V::from(ee_ovlp<NB>(a, ka, k2, c, d));
+        V::set_part(sm.o34[grp][r], w, ee_ovlp_part<NB>(a, ka, kb, c, d, w));
+        if (a.antisym) {
+          const double vq = ee_vq(a, scr, k1, kb);
+          V::set_part(sm.o14[grp][r], w, vq * ee_ovlp_part<NB>(a, k1, kb, c, d, w));
+          V::set_part(sm.o32[grp][r], w, ee_ovlp_part<NB>(a, ka, k2, c, d, w));
         }
       }
       __syncwarp();
