@@ -211,8 +211,9 @@ __global__ void k_ee_dm(int nk, int nbdm, int bs, const double2* __restrict__ y,
 }
 
 // exp(x) for x <= 0 as a double-float: Cody-Waite reduction x = k ln2 + r in FP64 (ln2 in two
-// parts), |r| <= ln2/2, then exp(r) from its Taylor series to degree 13 in double-float by Horner's
-// rule (truncation below 2e-17 relative) and the scaling by 2^k. Below x = -80 the FP32 exponent
+// parts), |r| <= ln2/2, then exp(r) from its Taylor series to degree 12 by Horner's rule, the terms
+// of degree 12 .. 9 in FP32 and the rest in double-float (truncation and FP32 rounding together
+// below 2.5e-16 relative), and the scaling by 2^k. Below x = -80 the FP32 exponent
 // range of the low part ends and the FP64 value is split instead.
 __device__ __forceinline__ float2 df_exp_neg(double x) {
   if (x < -80.0) return split_df1(exp(x));
@@ -220,13 +221,17 @@ __device__ __forceinline__ float2 df_exp_neg(double x) {
   double r = fma(-k, 6.93147180369123816490e-01, x);  // ln2 high part (trailing bits zero)
   r = fma(-k, 1.90821492927058770002e-10, r);         // ln2 - high part
   const float2 rr = split_df1(r);
-  // 1/n! for n = 13 .. 0 as (hi, lo)
-  float ph = (float)(1.0 / 6227020800.0), pl = (float)(1.0 / 6227020800.0 - (double)(float)(1.0 / 6227020800.0));
-  const double inv[13] = {1.0 / 479001600.0, 1.0 / 39916800.0, 1.0 / 3628800.0, 1.0 / 362880.0, 1.0 / 40320.0,
-                          1.0 / 5040.0,      1.0 / 720.0,      1.0 / 120.0,     1.0 / 24.0,     1.0 / 6.0,
-                          0.5,               1.0,              1.0};
+  // the terms of degree 12 .. 9 in FP32: their sum is below 2.8e-6 r^9 and r^9 below 7.3e-5, so its
+  // FP32 rounding stays under 1e-16 of the result
+  float ph = 1.0f / 479001600.0f, pl = 0.f;
+  ph = fmaf(ph, rr.x, 1.0f / 39916800.0f);
+  ph = fmaf(ph, rr.x, 1.0f / 3628800.0f);
+  ph = fmaf(ph, rr.x, 1.0f / 362880.0f);
+  // 1/n! for n = 8 .. 0 as (hi, lo), by Horner's rule in double-float
+  const double inv[9] = {1.0 / 40320.0, 1.0 / 5040.0, 1.0 / 720.0, 1.0 / 120.0, 1.0 / 24.0,
+                         1.0 / 6.0,     0.5,          1.0,          1.0};
 #pragma unroll
-  for (int n = 0; n < 13; ++n) {
+  for (int n = 0; n < 9; ++n) {
     float h, l;
     df_mul(h, l, ph, pl, rr.x, rr.y);
     df_renorm(h, l);
