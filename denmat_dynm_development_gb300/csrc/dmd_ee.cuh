@@ -210,6 +210,14 @@ __global__ void k_ee_dm(int nk, int nbdm, int bs, const double2* __restrict__ y,
   dm1f[idx] = split_dfc(d1);
 }
 
+// 1/n! for n = 8 .. 0 as double-floats (hi, lo)
+#define EE_DF_CONST(v) {(float)(v), (float)((v) - (double)(float)(v))}
+__constant__ float2 c_ee_inv_fact[9] = {
+    EE_DF_CONST(1.0 / 40320.0), EE_DF_CONST(1.0 / 5040.0), EE_DF_CONST(1.0 / 720.0),
+    EE_DF_CONST(1.0 / 120.0),   EE_DF_CONST(1.0 / 24.0),   EE_DF_CONST(1.0 / 6.0),
+    EE_DF_CONST(0.5),           EE_DF_CONST(1.0),          EE_DF_CONST(1.0)};
+#undef EE_DF_CONST
+
 // exp(x) for x <= 0 as a double-float: Cody-Waite reduction x = k ln2 + r in FP64 (ln2 in two
 // parts), |r| <= ln2/2, then exp(r) from its Taylor series to degree 12 by Horner's rule, the terms
 // of degree 12 .. 9 in FP32 and the rest in double-float (truncation and FP32 rounding together
@@ -227,16 +235,15 @@ __device__ __forceinline__ float2 df_exp_neg(double x) {
   ph = fmaf(ph, rr.x, 1.0f / 39916800.0f);
   ph = fmaf(ph, rr.x, 1.0f / 3628800.0f);
   ph = fmaf(ph, rr.x, 1.0f / 362880.0f);
-  // 1/n! for n = 8 .. 0 as (hi, lo), by Horner's rule in double-float
-  const double inv[9] = {1.0 / 40320.0, 1.0 / 5040.0, 1.0 / 720.0, 1.0 / 120.0, 1.0 / 24.0,
-                         1.0 / 6.0,     0.5,          1.0,          1.0};
-#pragma unroll
+  // the terms of degree 8 .. 0 by Horner's rule in double-float; the loop stays rolled (with the
+  // coefficients in constant memory) to keep the kernel's code within the instruction cache
+#pragma unroll 1
   for (int n = 0; n < 9; ++n) {
     float h, l;
     df_mul(h, l, ph, pl, rr.x, rr.y);
     df_renorm(h, l);
-    const float ch = (float)inv[n], cl = (float)(inv[n] - (double)(float)inv[n]);
-    df_add(h, l, ch, cl);
+    const float2 cn = c_ee_inv_fact[n];
+    df_add(h, l, cn.x, cn.y);
     ph = h;
     pl = l;
   }
@@ -459,8 +466,8 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
         const double* e4 = a.ew + (size_t)kb * NB;
         const C m12 = sm.o12[i1 * NB + i3];
         constexpr int HALF = NB2 / 2;  // both halves of the group share the row's elements
-#pragma unroll
-        for (int h = 0; h < HALF; ++h) {
+#pragma unroll 1
+        for (int h = 0; h < HALF; ++h) {  // rolled: one copy of the exp in the code
           const int cd = w * HALF + h, c = cd / NB, d = cd % NB;
           const double de = e1[i1] - e2[i3] + e3[c] - e4[d];  // the window test stays FP64
           C v = V::zero();
