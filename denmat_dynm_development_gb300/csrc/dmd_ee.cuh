@@ -14,8 +14,8 @@
 // occupations (calc_A1f / calc_A1fbar).
 //
 // GPU layout of the work: one warp per pair. Phase 1: the 32 lanes test 32 k3 at a time (k4 by
-// integer mesh arithmetic and a dense mesh table, energy window by per-k band ranges) and append
-// the candidates to a warp buffer. Phase 2: groups of G = 2 nb^2 lanes take one candidate each
+// integer mesh arithmetic and a dense mesh table, the energy window by every band combination in
+// FP32 with a margin above its rounding) and append the candidates to a warp buffer. Phase 2: groups of G = 2 nb^2 lanes take one candidate each
 // (4 groups for nb = 2, one for nb = 4); lane (w, r), r = (i1, i3), forms the real (w = 0) or
 // imaginary (w = 1) part of the overlaps' entry r and half w of the columns of row r of A in shared
 // memory, then its own A1rho (w = 0) or A1rhobar (w = 1) row, and accumulates P1ee or P2ee over
