@@ -2269,6 +2269,58 @@ __global__ void k_wait_never(unsigned int* errflag, uint32_t polls) {
   if (threadIdx.x == 0) mbar_wait_bounded(&bar, 0u, errflag, polls);
 }
 __global__ void k_set_one(unsigned int* p) { *p = 1u; }
+
+// fused multiply-add throughput: 8 independent chains per thread, `iters` rounds; the sums are
+// stored only when `sink` is set (never by the probe), which keeps the chains live
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_rate(int iters, T a, T b, T* sink) {
+  T c[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) c[i] = (T)(threadIdx.x + i);
+#pragma unroll 1
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int r = 0; r < 16; ++r)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) c[i] = fma(c[i], a, b);
+  }
+  if (sink) {
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += c[i];
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
+  }
+}
+
+template <typename T>
+int fma_rate(int device, double* tflops) {
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return DMD_E_CUDA;
+  const int blocks = nsm * 8, threads = 256;
+  const int iters = sizeof(T) == 8 ? 256 : 8192;  // ~20 ms (FP64) / ~10 ms (FP32) per launch on GB300
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return DMD_E_CUDA;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return DMD_E_CUDA;
+  }
+  int rc = DMD_OK;
+  float best = 0.f;
+  for (int rep = 0; rep < 4 && rc == DMD_OK; ++rep) {  // the first launch warms up
+    cudaEventRecord(e0);
+    k_fma_rate<T><<<blocks, threads>>>(iters, (T)0.999999, (T)1e-7, (T*)nullptr);
+    cudaEventRecord(e1);
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = DMD_E_CUDA;
+    else if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != DMD_OK || best <= 0.f) return rc ? rc : DMD_E_CUDA;
+  const double flops = 2.0 * blocks * threads * (double)iters * 16 * 8;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return DMD_OK;
+}
 }  // namespace
 
 extern "C" {
@@ -2295,6 +2347,13 @@ int dmd_selftest_wait_timeout(int device, uint32_t polls, int* status) {
   if (hv[1] != 1u) return DMD_E_CUDA;
   *status = (hv[0] & DMD_DEVERR_TIMEOUT) ? DMD_E_TIMEOUT : DMD_OK;
   return DMD_OK;
+}
+
+int dmd_peak_fma(int device, int fp64, double* tflops) {
+  if (!tflops) return DMD_E_ARG;
+  *tflops = 0.0;
+  if (cudaSetDevice(device) != cudaSuccess) return DMD_E_NODEV;
+  return fp64 ? fma_rate<double>(device, tflops) : fma_rate<float>(device, tflops);
 }
 
 int dmd_autotune(dmd_handle* h, int evals, int* chosen) {

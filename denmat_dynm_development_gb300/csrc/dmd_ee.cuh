@@ -221,10 +221,14 @@ __constant__ float2 c_ee_inv_fact[9] = {
 // exp(x) for x <= 0 as a double-float: Cody-Waite reduction x = k ln2 + r in FP64 (ln2 in two
 // parts), |r| <= ln2/2, then exp(r) from its Taylor series to degree 12 by Horner's rule, the terms
 // of degree 12 .. 9 in FP32 and the rest in double-float (truncation and FP32 rounding together
-// below 2.5e-16 relative), and the scaling by 2^k. Below x = -80 the FP32 exponent
-// range of the low part ends and the FP64 value is split instead.
+// below 2.5e-16 relative), and the scaling by 2^k. The bound holds for x >= -55: the low part lies
+// up to ~2^-50 below the high part, and once 2^k scales it under FP32's smallest normal (k below
+// about -80) it rounds to the subnormal grid, whose spacing 2^-149 is then no longer negligible
+// against the result. Below x = -55 the FP64 value is split instead.
+// The two parts of ln2 are the published split of fdlibm's e_exp.c (ln2HI[0], ln2LO[0], Sun
+// Microsystems, 1993): a 32-bit high part whose products with integers k are exact, and the rest.
 __device__ __forceinline__ float2 df_exp_neg(double x) {
-  if (x < -80.0) return split_df1(exp(x));
+  if (x < -55.0) return split_df1(exp(x));
   const double k = rint(x * 1.4426950408889634);
   double r = fma(-k, 6.93147180369123816490e-01, x);  // ln2 high part (trailing bits zero)
   r = fma(-k, 1.90821492927058770002e-10, r);         // ln2 - high part

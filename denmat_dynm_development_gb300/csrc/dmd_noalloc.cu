@@ -10,7 +10,10 @@
 // call should come before any stream capture). Every call shares the array and it keeps the last
 // call's contents; the kernels clear what must start at zero. Calls whose work overlaps on the GPU
 // (different streams, or another host thread) race on the array and must be serialised by the
-// caller.
+// caller. The address is cached per device for the life of the process: resetting a device
+// (cudaDeviceReset) after its first call is not supported, since the array then moves.
+// This path is a plain FP64 reference-speed implementation (one thread per pair product with FP64
+// atomics, one thread per k in the finish); the fast contraction is the handle-based one.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -166,6 +169,8 @@ int run_noalloc(int nk, int nbdm, int bs, long long npair, const unsigned long l
   double2* rs = scratch;
   double2* acc = scratch + (size_t)2 * nk * NB2;
   const int nprep = nk * NB2;
+  // an error left pending by the caller's earlier work is theirs: report it without consuming it
+  if (cudaPeekAtLastError() != cudaSuccess) return DMD_E_CUDA;
   k_na_prep<NB><<<(nprep + 255) / 256, 256, 0, st>>>(nk, nbdm, bs, dm, edm, t, expt, rs, acc);
   if (npair > 0) {
     const long long nthr = npair * 4LL * NB2;

@@ -58,7 +58,7 @@ EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_s
            "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
            "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes", "dmd_adjoint_rk4", "dmd_autotune",
            "dmd_group_create", "dmd_group_rk4", "dmd_group_destroy",
-           "dmd_create_from_files", "dmd_create_from_sparse_files", "dmd_selftest_wait_timeout",
+           "dmd_create_from_files", "dmd_create_from_sparse_files", "dmd_selftest_wait_timeout", "dmd_peak_fma",
            "dmd_ee_attach", "dmd_ee_update", "dmd_ee_read"]
 
 
@@ -95,6 +95,7 @@ def _lib():
         L.dmd_group_rk4.argtypes = [vp, d, i64]
         L.dmd_group_destroy.argtypes = [vp]
         L.dmd_selftest_wait_timeout.argtypes = [C.c_int, C.c_uint32, C.POINTER(C.c_int)]
+        L.dmd_peak_fma.argtypes = [C.c_int, C.c_int, C.POINTER(d)]
         L.dmd_create_from_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                             C.POINTER(vp)]
         L.dmd_create_from_sparse_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p,
@@ -113,6 +114,15 @@ def _lib():
                                                 C.c_int32, d, vp, vp, vp]
         _L = L
     return _L
+
+
+def peak_fma(device: int = 0, fp64: bool = True) -> float:
+    """Measured fused multiply-add throughput of the device in TFLOP/s (dmd_peak_fma)."""
+    v = C.c_double(0.0)
+    st = _lib().dmd_peak_fma(int(device), 1 if fp64 else 0, C.byref(v))
+    if st != 0:
+        raise DMDError(st, "dmd_peak_fma failed")
+    return float(v.value)
 
 
 def _c(a, dtype):

@@ -196,6 +196,12 @@ int dmd_group_destroy(dmd_group* g);
  * (DMD_E_TIMEOUT) and the call checks that the context still runs a kernel afterwards. */
 int dmd_selftest_wait_timeout(int device, uint32_t polls, int* status);
 
+/* No counterpart in the reference. Measured fused multiply-add throughput of the device (fp64 = 1:
+ * FP64, 0: FP32) in TFLOP/s (2 flops per FMA), from CUDA-event-timed launches of a kernel whose
+ * threads run 8 independent FMA chains (best of three after a warm-up launch, ~20 ms each). The
+ * FP64 figure is the ceiling of the plain FP64 contraction, whose work is FP64 multiply-adds. */
+int dmd_peak_fma(int device, int fp64, double* tflops);
+
 /* ---- e-e scattering rebuilt from the density matrix (eeMode = Pee_update) ------------------------
  * The e-e operators P_ee(rho) of elecelec_model::calc_P (ElecElec_Model.h:186-262) for every stored
  * k-pair, with the static screened Coulomb interaction of coulomb_model::vq (Coulomb_Model.h:632-660),
@@ -260,9 +266,11 @@ int dmd_profile_get(const dmd_handle* h, int kernel_class, double* total_ms, int
  * stream is a cudaStream_t (NULL for the default stream). Nothing is allocated: the scratch lives in
  * a static device array of 16 MiB that every GPU loading this library keeps until exit, which
  * limits nk * (bend - bstart)^2 to 262144 (DMD_E_ARG above that). The first call on a device looks
- * up the array's device address and should come before any stream capture. All calls share the
- * array: calls that overlap on the GPU race and must be serialised by the caller. Pairs whose
- * indices fall outside [0, nk) are skipped. The call is asynchronous on `stream`. */
+ * up the array's device address and should come before any stream capture; a device reset after it
+ * is not supported. All calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. Pairs whose indices fall outside [0, nk) are skipped. The call is
+ * asynchronous on `stream`; a CUDA error already pending when it is made gives DMD_E_CUDA and is
+ * left pending for the caller. */
 int dmd_evolve_driver_noalloc(int32_t nk, int32_t nb_dm, int32_t bstart, int32_t bend, int64_t nkpair,
                               const uint64_t* k1st, const uint64_t* k2nd, const double* P1, const double* P2,
                               const double* e_dm, double prefac_eph, int32_t expt, double t, const double* dm,

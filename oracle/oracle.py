@@ -306,6 +306,26 @@ def fermi(T, mu, e):
     return out
 
 
+def dm_bpert(smat, e, f, T, Bpert, t0=0.0, picture=0):
+    """Initial state: electron::compute_dm_Bpert_1st (electron.cpp:62-98) followed by
+    singdenmat_k::init_dm (DenMat.cpp:65-81), as load() builds it. smat [nk][3][nb^2] complex,
+    e, f [nk][nb]; returns complex [nk][nb^2]."""
+    _setup_prototypes()
+    smat = np.ascontiguousarray(smat, dtype=np.complex128)
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    B = np.ascontiguousarray(Bpert, dtype=np.float64)
+    nk, nb = e.shape
+    L = lib()
+    dmB = np.zeros((nk, nb * nb), np.complex128)
+    L.orc_dm_bpert(C.c_int(nk), C.c_int(nb), C.c_void_p(smat.ctypes.data), C.c_void_p(e.ctypes.data),
+                   C.c_void_p(f.ctypes.data), C.c_double(T), C.c_void_p(B.ctypes.data), C.c_double(t0),
+                   C.c_int(picture), C.c_void_p(dmB.ctypes.data))
+    dm0 = np.zeros_like(dmB)
+    L.orc_init_dm(C.c_int(nk), C.c_int(nb), C.c_void_p(dmB.ctypes.data), C.c_void_p(dm0.ctypes.data))
+    return dm0
+
+
 @dataclass
 class OracleSystem:
     nk: int

@@ -3,7 +3,9 @@
 Run in a container that has the reference sources (it builds oracle/_ref/dmd_ref with
 oracle/Makefile.ref first):
 
-    python tests/golden/make_golden.py [--ref /root/reference/src_v4.5.7]
+    python tests/golden/make_golden.py [--ref <reference checkout>/src_v4.5.7]
+
+(the default is $DMD_REFERENCE_ROOT/src_v4.5.7, DMD_REFERENCE_ROOT defaulting to /root/reference)
 
 For every case it writes a small synthetic DMD input (param.in + ldbd_data/ from the package's
 seeded generator) and runs the shim-built reference program on it:
@@ -212,7 +214,8 @@ def make_case(name, spec, ref_bin, outroot):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference/src_v4.5.7")
+    ap.add_argument("--ref", default=os.path.join(os.environ.get("DMD_REFERENCE_ROOT", "/root/reference"),
+                                                  "src_v4.5.7"))
     ap.add_argument("--cases", nargs="*", default=list(CASES))
     a = ap.parse_args()
     subprocess.run(["make", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), "-j8", "REF=" + a.ref], check=True,

@@ -6,6 +6,8 @@ first 3.2 ps; tau_t.dat: two-point log-fit lifetimes). This script copies the nu
 t1_gaas_example.npz; it reads the reference tree and runs only where that tree exists.
 
     python tests/golden/make_t1_golden.py [REFERENCE_ROOT]
+
+(REFERENCE_ROOT defaults to $DMD_REFERENCE_ROOT, itself defaulting to /root/reference)
 """
 import os
 import sys
@@ -16,7 +18,7 @@ EXAMPLE = "Examples/RealTime_Example_GaAs_20230105/ld-dmd/t300/mult8_gauss0.005/
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DMD_REFERENCE_ROOT", "/root/reference")
     d = os.path.join(ref, EXAMPLE)
     sz = np.loadtxt(os.path.join(d, "sz_elec_tot.out"))
     sfit = np.loadtxt(os.path.join(d, "sfit.out"))

@@ -218,15 +218,19 @@ def test_equilibrium_drift_on_gpu(case, built):
         assert i.ddmdteq == 1
 
 
-def test_t1_from_gpu_trajectory(oracle, built):
+@pytest.mark.parametrize("prec", ["f64", "f64x"])
+def test_t1_from_gpu_trajectory(prec, oracle, built):
     """T1 (the fit.py restatement) from the GPU RK4 trajectory against the oracle's: S(t) within the
-    trajectory bound 1e-10, fitted lifetimes within 1e-8 (leastsq's convergence tolerance on beta)."""
+    trajectory bound 1e-10, and the least-squares lifetime converged to machine precision (tau_conv)
+    within 1e-10 -- the bound the FP64 path is held to for rho(t), S(t) and the fitted T1/T2. The
+    fit.py-faithful tau_lsq / tau_cf stop at leastsq's xtol (~1.5e-8 on beta) and are compared at
+    that tolerance."""
     from denmat_dynm_development_gb300.t1fit import fit_t1
     s = oracle.load(os.path.join(GOLDEN, "nb2_carrier_eq"))
     h, nsteps, every = 2.0 * oracle.fs, 1500, 50
     y0 = oracle.y_of(s.dm0)
     _, rec_o = oracle.rk4(s, s.t0, h, nsteps, y0, every=every)
-    with make_gpu(s, "f64") as gpu:
+    with make_gpu(s, prec) as gpu:
         gpu.set_state(s.t0, y0)
         gpu.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
         rec = []
@@ -238,12 +242,15 @@ def test_t1_from_gpu_trajectory(oracle, built):
     assert rel(rec[:, 1], rec_o[:, 1]) < 1e-10
     fo = fit_t1(rec_o[:, 0], rec_o[:, 1])
     fg = fit_t1(rec[:, 0], rec[:, 1])
-    print("T1 oracle %.12g ps gpu %.12g ps" % (fo.tau_lsq, fg.tau_lsq))
+    err = abs(fg.tau_conv - fo.tau_conv) / abs(fo.tau_conv)
+    print("%s: T1 oracle %.15g ps gpu %.15g ps (converged fit), rel err %.3g; S(t) rel err %.3g"
+          % (prec, fo.tau_conv, fg.tau_conv, err, rel(rec[:, 1], rec_o[:, 1])))
     # the synthetic P follows the initializer's smeared-delta construction without detailed balance,
     # so |S| need not decay; the fit is still a well-defined function of the trajectory
-    assert np.isfinite(fo.tau_lsq) and np.isfinite(fg.tau_lsq)
-    assert abs(fg.tau_lsq - fo.tau_lsq) / fo.tau_lsq < 1e-8
-    assert abs(fg.tau_cf - fo.tau_cf) / fo.tau_cf < 1e-8
+    assert np.isfinite(fo.tau_conv) and np.isfinite(fg.tau_conv)
+    assert err < 1e-10
+    assert abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq) < 1e-7
+    assert abs(fg.tau_cf - fo.tau_cf) / abs(fo.tau_cf) < 1e-7
 
 
 @pytest.mark.parametrize("prec", ["f64", "f64x"])
@@ -327,8 +334,9 @@ def test_lowp_t1_vs_oracle(prec, oracle, built):
     rec = np.array(rec)
     es = rel(rec[:, 1], rec_o[:, 1])
     fo, fg = fit_t1(rec_o[:, 0], rec_o[:, 1]), fit_t1(rec[:, 0], rec[:, 1])
-    et = abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq)
-    print("%s: S(t) rel err %.3g, T1 %.10g vs %.10g ps, rel err %.3g" % (prec, es, fg.tau_lsq, fo.tau_lsq, et))
+    et = abs(fg.tau_conv - fo.tau_conv) / abs(fo.tau_conv)
+    print("%s: S(t) rel err %.3g, T1 %.10g vs %.10g ps (converged fit), rel err %.3g"
+          % (prec, es, fg.tau_conv, fo.tau_conv, et))
     assert et < 1e-4
 
 
@@ -508,9 +516,9 @@ def test_batched_tensor_core_t1_vs_oracle(oracle, built):
             rec.append((t, tot[0]))
     rec = np.array(rec)
     fo, fg = fit_t1(rec_o[:, 0], rec_o[:, 1]), fit_t1(rec[:, 0], rec[:, 1])
-    et = abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq)
-    print("tensor-core batch: S(t) rel err %.3g, T1 %.10g vs %.10g ps, rel err %.3g"
-          % (rel(rec[:, 1], rec_o[:, 1]), fg.tau_lsq, fo.tau_lsq, et))
+    et = abs(fg.tau_conv - fo.tau_conv) / abs(fo.tau_conv)
+    print("tensor-core batch: S(t) rel err %.3g, T1 %.10g vs %.10g ps (converged fit), rel err %.3g"
+          % (rel(rec[:, 1], rec_o[:, 1]), fg.tau_conv, fo.tau_conv, et))
     assert et < 1e-4
 
 
@@ -665,17 +673,18 @@ def test_create_from_sparse_files_matches_dense(prec, oracle, built, tmp_path, m
     assert rel(rs, rd) <= (1e-15 if prec == "f64x" else 1e-12)
 
 
-def test_t2_in_transverse_field_from_gpu_trajectory(oracle, built):
+@pytest.mark.parametrize("prec", ["f64", "f64x"])
+def test_t2_in_transverse_field_from_gpu_trajectory(prec, oracle, built):
     """T2: S_z precessing about the 2 T in-plane field of nb2_eimp_B (initial spin along z), fitted
     with the decaying-cosine model of fit.py (the field sets omega); S(t) within 1e-10 of the oracle's,
-    the fitted lifetime within 1e-7 (the nonlinear fit's convergence tolerance is 1e-8 and it moves
-    by about that with the last-bit differences of the FP64 atomic sums between runs)."""
+    and the lifetime and precession period of the least-squares optimum converged to machine
+    precision within 1e-10 (the fit.py-faithful leastsq values stop at its xtol, ~1e-8)."""
     from denmat_dynm_development_gb300.t1fit import fit_t1
     s = oracle.load(os.path.join(GOLDEN, "nb2_eimp_B"))
     h, nsteps, every = 10.0 * oracle.fs, 3000, 50
     y0 = oracle.y_of(s.dm0)
     _, rec_o = oracle.rk4(s, s.t0, h, nsteps, y0, every=every)
-    with make_gpu(s, "f64") as gpu:
+    with make_gpu(s, prec) as gpu:
         gpu.set_state(s.t0, y0)
         gpu.set_observable(0, s.smat[:, 2, :], s.f_dm, s.ob_prefac)
         rec = []
@@ -687,8 +696,12 @@ def test_t2_in_transverse_field_from_gpu_trajectory(oracle, built):
     assert rel(rec[:, 1], rec_o[:, 1]) < 1e-10
     fo = fit_t1(rec_o[:, 0], rec_o[:, 1], bfield_tesla=2.0)
     fg = fit_t1(rec[:, 0], rec[:, 1], bfield_tesla=2.0)
-    print("T2 oracle %.12g ps gpu %.12g ps" % (fo.tau_lsq, fg.tau_lsq))
-    assert np.isfinite(fo.tau_lsq) and np.isfinite(fg.tau_lsq)
+    err = abs(fg.tau_conv - fo.tau_conv) / abs(fo.tau_conv)
+    errp = abs(fg.period_conv - fo.period_conv) / abs(fo.period_conv)
+    print("%s: T2 oracle %.15g ps gpu %.15g ps (converged fit), rel err %.3g, period rel err %.3g"
+          % (prec, fo.tau_conv, fg.tau_conv, err, errp))
+    assert np.isfinite(fo.tau_conv) and np.isfinite(fg.tau_conv)
+    assert err < 1e-10 and errp < 1e-10
     assert abs(fg.tau_lsq - fo.tau_lsq) / abs(fo.tau_lsq) < 1e-7
 
 

@@ -115,6 +115,10 @@ def test_setup_pieces_match_oracle(host, oracle):
     Bp = np.array([0.05, 0.0, 0.1]) * oracle.Tesla2au
     dm = host.dm_bpert(o.smat, o.e_dm, o.f_dm, o.temperature, Bp, 0.0, 0)
     np.testing.assert_array_equal(dm, o.dm0)
+    # the oracle's own set-up (used where the product library must not be loaded: the benchmark's
+    # reference arm) gives the same bits
+    np.testing.assert_array_equal(oracle.fermi(o.temperature, o.mu, o.e_dm), f)
+    np.testing.assert_array_equal(oracle.dm_bpert(o.smat, o.e_dm, o.f_dm, o.temperature, Bp, 0.0, 0), dm)
 
 
 @pytest.mark.parametrize("case", EE_CASES)

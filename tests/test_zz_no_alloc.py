@@ -4,9 +4,10 @@ dmd_evolve_driver_noalloc serves callers that cannot allocate device memory (gra
 frameworks whose pools own the device, plug-ins given device pointers only); its scratch is a static
 device array. Here the test plays such a caller: it owns the device buffers (made with torch), calls
 the entry point twice in a row through the C ABI on different states and times, and compares each
-result with dmd_evolve_driver (host-buffer entry point) at the FP64 RHS tolerance, 1e-12 normwise.
-This file is collected last so that a failure here leaves every other test already run; it must
-also pass on its own in a fresh process.
+result with dmd_evolve_driver (host-buffer entry point) at the FP64 RHS tolerance, 1e-12 normwise,
+and, on the golden states, with the reference's own scattering term (the fixture's rhs_eph). This
+file is collected last so that a failure here leaves every other test already run; it must also pass
+on its own in a fresh process. The size check runs without a GPU.
 """
 import ctypes as C
 import os
@@ -16,13 +17,12 @@ import pytest
 
 from conftest import GOLDEN
 
-pytestmark = pytest.mark.gpu
-
 
 def rel(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("case", ["nb2_eimp_B", "nb4_eimp_B", "nb2_window"])
 def test_noalloc_matches_allocating_entry_point(case, oracle):
     torch = pytest.importorskip("torch")
@@ -63,11 +63,24 @@ def test_noalloc_matches_allocating_entry_point(case, oracle):
             got = out.cpu().numpy()
             want = ref.evolve_driver(t, y)
             assert rel(got, want) < 1e-12
+        # the golden states against the reference's own evolve_driver output
+        g = dict(np.load(os.path.join(GOLDEN, case, "golden.npz")))
+        for i, t in enumerate(g["rhs_t"]):
+            dm.copy_(torch.from_numpy(np.ascontiguousarray(g["rhs_y"][i])))
+            out.fill_(np.nan)
+            stream = torch.cuda.current_stream(dev).cuda_stream
+            st = L.dmd_evolve_driver_noalloc(s.nk, s.nb_dm, s.bstart, s.bend, s.npair, k1.data_ptr(), k2.data_ptr(),
+                                             P1.data_ptr(), P2.data_ptr(), e.data_ptr(), s.prefac_eph, s.expt,
+                                             float(t), dm.data_ptr(), out.data_ptr(), C.c_void_p(stream))
+            assert st == 0
+            torch.cuda.synchronize(dev)
+            assert rel(out.cpu().numpy(), g["rhs_eph"][i]) < 1e-12
     finally:
         ref.close()
 
 
-def test_noalloc_rejects_sizes_beyond_its_scratch(oracle):
+def test_noalloc_rejects_sizes_beyond_its_scratch():
+    """Runs in the CPU suite too: the size check comes before any CUDA call."""
     import __graft_entry__ as G
     G.build()
     from denmat_dynm_development_gb300.dmd import _lib
