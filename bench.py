@@ -463,7 +463,7 @@ def run_gpu(args, w, rank, world, dist):
     t_create = time.perf_counter() - t_create  # layout, device conversion and upload of P
     y0 = np.ascontiguousarray(w["dm0"]).view(np.float64).reshape(-1).copy()
     g.set_state(0.0, y0)
-    shape = g.autotune(3)                      # compiled contraction shapes timed, fastest kept
+    shape = g.autotune(3) if args.autotune else None  # compiled contraction shapes timed, fastest kept
     g.rk4(h, args.warmup)                      # warm-up (also captures the step graph)
 
     def barrier():
@@ -900,6 +900,8 @@ def main():
     ap.add_argument("--workload", default="gaas_nk20k")
     ap.add_argument("--precision", default="f64", choices=["f64", "f64x", "f32", "bf16x2"])
     ap.add_argument("--windows", type=int, default=5, help="timed K-step windows (median reported)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default contraction shape (profiling runs)")
     ap.add_argument("--no-forms", dest="forms", action="store_false",
                     help="skip the other arithmetics of the contraction")
     ap.add_argument("--no-e2e", action="store_true")

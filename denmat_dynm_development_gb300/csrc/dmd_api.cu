@@ -46,7 +46,8 @@ struct dmd_handle {
   // column-block layout (nb = 2)
   int use_cb = 0;
   int lin = 0;                 // linearized master equation (DMD_FLAG_LINEAR)
-  int pcfg = 0;                // pair-kernel shape variant (DMD_PAIR_CFG)
+  int pcfg = 0;                // pair-kernel shape variant of the f64x form (DMD_PAIR_CFG)
+  int pcfg64 = 1;              // pair-kernel shape variant of the f64 form (DMD_PAIR_CFG64)
   int* d_pos = nullptr;        // k -> energy rank
   int* d_inv = nullptr;        // energy rank -> k
   dmd::RowBlock* d_rb = nullptr;
@@ -254,28 +255,28 @@ int launch_prep(dmd_handle* h, const double2* y, const TimeArg& ta) {
 }
 
 // the Hermitian pass and the gated anti-Hermitian pass of the nb = 2 contraction
-template <typename A, int NB, int L, int NST, int MB, int RW = 1>
+template <typename A, int NB, int L, int NST, int MB, int RW = 1, bool FA = false>
 void herm_pair_launches(dmd_handle* h, const typename A::relem* rs, size_t half) {
-  typedef CbTmaSmem<A, NB, L, NST, RW> S;
+  typedef CbTmaSmem<A, NB, L, NST, RW, FA> S;
   const size_t cstride = (size_t)h->nk * 2 * h->nb2;  // coordinates and sums per state
   const long long warps = (long long)h->nitems * ((h->nrhs + RW - 1) / RW);
   const unsigned g = blocks_for(warps, 4);
-  k_pairs_herm<A, NB, L, NST, MB, false, RW><<<g, 128, S::cta_bytes, h->st>>>(
+  k_pairs_herm<A, NB, L, NST, MB, false, RW, FA><<<g, 128, S::cta_bytes, h->st>>>(
       h->d_items, h->nitems, h->d_rb, (const typename A::elem*)h->d_P, rs, (double*)h->d_acc, h->nk, nullptr, h->d_err,
       h->nrhs, cstride, 2 * cstride);
-  k_pairs_herm<A, NB, L, NST, MB, true, RW><<<g, 128, S::cta_bytes, h->st>>>(
+  k_pairs_herm<A, NB, L, NST, MB, true, RW, FA><<<g, 128, S::cta_bytes, h->st>>>(
       h->d_items, h->nitems, h->d_rb, (const typename A::elem*)h->d_P, rs + half, (double*)h->d_acc, h->nk,
       h->d_hflag, h->d_err, h->nrhs, cstride, 2 * cstride);
 }
 
-template <typename A, int NB, int L, int NST, int MB, int RW = 1>
+template <typename A, int NB, int L, int NST, int MB, int RW = 1, bool FA = false>
 cudaError_t herm_pair_attrs() {
-  const int bytes = (int)CbTmaSmem<A, NB, L, NST, RW>::cta_bytes;
-  cudaError_t e = cudaFuncSetAttribute(k_pairs_herm<A, NB, L, NST, MB, false, RW>,
+  const int bytes = (int)CbTmaSmem<A, NB, L, NST, RW, FA>::cta_bytes;
+  cudaError_t e = cudaFuncSetAttribute(k_pairs_herm<A, NB, L, NST, MB, false, RW, FA>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_pairs_herm<A, NB, L, NST, MB, true, RW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             bytes);
+    e = cudaFuncSetAttribute(k_pairs_herm<A, NB, L, NST, MB, true, RW, FA>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   return e;
 }
 
@@ -342,7 +343,20 @@ int launch_pairs(dmd_handle* h) {
       } else if (h->prec == DMD_PREC_BF16X2) {
         herm_pair_launches<ArithBF2, NB, 4, 2, 5>(h, (const float*)h->d_rs, half);
       } else {
-        herm_pair_launches<ArithF64, NB, 2, 2, 4>(h, (const double*)h->d_rs, half);
+        const double* rs = (const double*)h->d_rs;
+        if constexpr (NB == 2) {
+          // shapes of the FP64 contraction (autotuned; 1 by default): 0 reduces the forward partials
+          // over the warp; 1-3 add them with FP64 reductions in L2 (off the FP64 pipe: 2.65 -> 2.47 ms
+          // per launch on the 9.7M-pair workload), with 4 or 5 CTAs per SM
+          switch (h->pcfg64) {
+            case 1: herm_pair_launches<ArithF64, NB, 2, 2, 4, 1, true>(h, rs, half); break;
+            case 2: herm_pair_launches<ArithF64, NB, 2, 2, 5, 1, true>(h, rs, half); break;
+            case 3: herm_pair_launches<ArithF64, NB, 1, 4, 5, 1, true>(h, rs, half); break;
+            default: herm_pair_launches<ArithF64, NB, 2, 2, 4>(h, rs, half); break;
+          }
+        } else {
+          herm_pair_launches<ArithF64, NB, 2, 2, 4>(h, rs, half);
+        }
       }
       h->launches++;
     }
@@ -738,10 +752,13 @@ int upload_pairs_cb(dmd_handle* h, const dmd_desc* d) {
   h->nrb = (long long)L.rb.size();
   // pair-kernel shape (stage lines, resident CTAs per SM); 0 is the default, the others serve tuning
   if (const char* v = getenv("DMD_PAIR_CFG")) h->pcfg = atoi(v);
+  if (const char* v = getenv("DMD_PAIR_CFG64")) h->pcfg64 = atoi(v);
   if (nb == 2) {
     cudaError_t (*const attrs[])() = {
         herm_pair_attrs<ArithDF, 2, 2, 2, 4>, herm_pair_attrs<ArithDF, 2, 2, 3, 3>, herm_pair_attrs<ArithDF, 2, 1, 4, 4>,
         herm_pair_attrs<ArithDF, 2, 1, 3, 4>, herm_pair_attrs<ArithDF, 2, 1, 6, 3>, herm_pair_attrs<ArithF64, 2, 2, 2, 4>,
+        herm_pair_attrs<ArithF64, 2, 2, 2, 4, 1, true>, herm_pair_attrs<ArithF64, 2, 2, 2, 5, 1, true>,
+        herm_pair_attrs<ArithF64, 2, 1, 4, 5, 1, true>,
         herm_pair_attrs<ArithF32, 2, 4, 2, 5>, herm_pair_attrs<ArithBF2, 2, 4, 2, 5>,
         herm_pair_attrs<ArithF32, 2, 4, 2, 2, 4>, herm_pair_attrs<ArithF32, 2, 4, 2, 2, 8>,
         herm_pair_attrs<ArithBF2, 2, 4, 2, 2, 4>};
@@ -2365,6 +2382,9 @@ int dmd_autotune(dmd_handle* h, int evals, int* chosen) {
   if (h->use_cb && !h->use_tc && h->nrhs == 1 && h->prec == DMD_PREC_F64X && h->nb == 2) {
     cand = {0, 1, 2, 3, 4};
     knob = &h->pcfg;
+  } else if (h->use_cb && !h->use_tc && h->nrhs == 1 && h->prec == DMD_PREC_F64 && h->nb == 2) {
+    cand = {0, 1, 2, 3};
+    knob = &h->pcfg64;
   } else if (h->use_cb && !h->use_tc && h->nrhs > 1 && h->prec == DMD_PREC_F32) {
     cand = {4, 8};
     knob = &h->brw;

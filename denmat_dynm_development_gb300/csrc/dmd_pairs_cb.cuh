@@ -461,7 +461,11 @@ __global__ void k_prep_tc(int nk, int nbdm, int bs, const double2* __restrict__ 
 // reduced over the warp through a shared buffer and added with 16 FP64 atomics. Waits are bounded
 // (dmd_tma.cuh); a timeout sets *errflag.
 // ---------------------------------------------------------------------------------------------
-template <typename A, int NB, int LINES, int NST, int RW = 1>
+// FA (forward atomics): each active lane adds its forward partials straight to the row's sums with
+// FP64 reductions in L2 instead of reducing them over the warp through shared memory first; the
+// per-warp reduction buffer is then not allocated. For the FP64 form, whose bound is the FP64 pipe,
+// this moves the cross-lane additions (about one FP64 add per element per pair) off that pipe.
+template <typename A, int NB, int LINES, int NST, int RW = 1, bool FA = false>
 struct CbTmaSmem {
   static constexpr int NB2 = NB * NB, NB4 = NB2 * NB2;
   static constexpr int G = NB2 / 4, W = 32 / G;  // lanes per pair, slots (columns) per row block
@@ -469,11 +473,12 @@ struct CbTmaSmem {
   static constexpr int CPM = NB2 / LINES;        // chunks per matrix
   static constexpr int CPR = 2 * CPM;            // chunks per row block
   static constexpr size_t stage_bytes = (size_t)LINES * NB2 * W * sizeof(typename A::elem);
-  static constexpr size_t red_bytes = (size_t)NV * 32 * sizeof(typename A::red_t);
+  static constexpr size_t red_bytes = FA ? 0 : (size_t)NV * 32 * sizeof(typename A::red_t);
   static constexpr size_t row_bytes = (size_t)4 * NB2 * RW * sizeof(typename A::relem);  // r_k, s_k, zeros
   static constexpr size_t warp_bytes = ((NST * stage_bytes + red_bytes + row_bytes + 8 * NST) + 127) / 128 * 128;
   static constexpr size_t cta_bytes = 4 * warp_bytes;
   static_assert(NB2 % 4 == 0 && (2 * NB2) % FL == 0 && FL % LINES == 0, "shape");
+  static_assert(!FA || G == 1, "forward atomics: one lane per pair (nb = 2)");
 };
 
 // slot of (value v, lane j) in the per-warp reduction buffer: rows rotated by v so that the
@@ -485,7 +490,7 @@ __device__ __forceinline__ int rsw(int v, int j) { return v * 32 + ((j + v) & 31
 // staged element feeds RW products. Warp w of the grid takes RHS group w % ngroups of work item
 // w / ngroups (the warps of a block share an item, so its P chunks come from HBM once and from L2
 // for the others). Coordinates of state q start at rs + q * rstride, its sums at acc + q * astride.
-template <typename A, int NB, int LINES, int NST, int MINB, bool IMAG, int RW = 1>
+template <typename A, int NB, int LINES, int NST, int MINB, bool IMAG, int RW = 1, bool FA = false>
 __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __restrict__ items, int nitems,
                                                           const RowBlock* __restrict__ rbs,
                                                           const typename A::elem* __restrict__ P,
@@ -494,7 +499,7 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
                                                           const unsigned int* __restrict__ gate,
                                                           unsigned int* __restrict__ errflag, int nrhs = 1,
                                                           size_t rstride = 0, size_t astride = 0) {
-  typedef CbTmaSmem<A, NB, LINES, NST, RW> S;
+  typedef CbTmaSmem<A, NB, LINES, NST, RW, FA> S;
   constexpr int NB2 = S::NB2, NB4 = S::NB4, G = S::G, W = S::W, FL = S::FL, NV = S::NV;
   constexpr int CPM = S::CPM, CPR = S::CPR;
   constexpr size_t SE = S::stage_bytes / sizeof(typename A::elem);  // elements per stage
@@ -647,11 +652,22 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
                 A::mac_cx(rY[i][u], p1, rv[u * 2 * NB2 + NB2 + a]);
               }
             }
-            const int v = 2 * ((q * LINES + r) % FL);
+            if constexpr (FA) {
+              double* dst = acc + (size_t)brow * 4 * NB2 + 2 * (q * LINES + r);
 #pragma unroll
-            for (int u = 0; u < RW; ++u) {
-              red[rsw(v * RW + 2 * u, lane)] = IMAG ? A::red_neg(A::red_im(f[u])) : A::red_re(f[u]);
-              red[rsw(v * RW + 2 * u + 1, lane)] = IMAG ? A::red_re(f[u]) : A::red_im(f[u]);
+              for (int u = 0; u < RW; ++u) {
+                if (u < nq) {
+                  atomicAdd(dst + (size_t)(q0 + u) * astride, IMAG ? -A::im_d(f[u]) : A::re_d(f[u]));
+                  atomicAdd(dst + (size_t)(q0 + u) * astride + 1, IMAG ? A::re_d(f[u]) : A::im_d(f[u]));
+                }
+              }
+            } else {
+              const int v = 2 * ((q * LINES + r) % FL);
+#pragma unroll
+              for (int u = 0; u < RW; ++u) {
+                red[rsw(v * RW + 2 * u, lane)] = IMAG ? A::red_neg(A::red_im(f[u])) : A::red_re(f[u]);
+                red[rsw(v * RW + 2 * u + 1, lane)] = IMAG ? A::red_re(f[u]) : A::red_im(f[u]);
+              }
             }
           }
         } else {
@@ -670,11 +686,22 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
                 A::mac_cx(rX[i][u], p2, rv[u * 2 * NB2 + j]);
               }
             }
-            const int v = 2 * ((q * LINES + r) % FL);
+            if constexpr (FA) {
+              double* dst = acc + (size_t)brow * 4 * NB2 + 2 * (q * LINES + r);
 #pragma unroll
-            for (int u = 0; u < RW; ++u) {
-              red[rsw(v * RW + 2 * u, lane)] = IMAG ? A::red_neg(A::red_im(f[u])) : A::red_re(f[u]);
-              red[rsw(v * RW + 2 * u + 1, lane)] = IMAG ? A::red_re(f[u]) : A::red_im(f[u]);
+              for (int u = 0; u < RW; ++u) {
+                if (u < nq) {
+                  atomicAdd(dst + (size_t)(q0 + u) * astride, IMAG ? -A::im_d(f[u]) : A::re_d(f[u]));
+                  atomicAdd(dst + (size_t)(q0 + u) * astride + 1, IMAG ? A::re_d(f[u]) : A::im_d(f[u]));
+                }
+              }
+            } else {
+              const int v = 2 * ((q * LINES + r) % FL);
+#pragma unroll
+              for (int u = 0; u < RW; ++u) {
+                red[rsw(v * RW + 2 * u, lane)] = IMAG ? A::red_neg(A::red_im(f[u])) : A::red_re(f[u]);
+                red[rsw(v * RW + 2 * u + 1, lane)] = IMAG ? A::red_re(f[u]) : A::red_im(f[u]);
+              }
             }
           }
         }
@@ -684,7 +711,7 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
       fence_proxy_async();
       __syncwarp();
       if (c + NST < nch) issue(c + NST);
-      if (((q + 1) * LINES) % FL == 0) {
+      if (!FA && ((q + 1) * LINES) % FL == 0) {
         // lines [L0, L0 + FL) of this row block are complete: reduce over the active lanes and add
         // to the row's sums (line L is real pair 2L, 2L + 1 of [X'(NB2) | Y'(NB2)]); buffer value
         // v * RW + 2u + ri holds line v / 2 (of the flush), part ri, state u

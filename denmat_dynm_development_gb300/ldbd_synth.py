@@ -535,6 +535,8 @@ WORKLOADS = {
     "si_nk500": SynthConfig(nk=500, nb=2, de_pair_mev=60.0),
     # GaAs-like at scale: nb=2, nk=20k, ~10M pairs, e-ph + e-imp.
     "gaas_nk20k": SynthConfig(nk=20000, nb=2, de_pair_mev=4.45, eimp_sigma_mev=5.0),
+    # the same generator at nk=16k (~6.2M pairs, P 3.2 GB): profiling case with several waves of work
+    "gaas_nk16k": SynthConfig(nk=16000, nb=2, de_pair_mev=4.45, eimp_sigma_mev=5.0),
     # the same generator at nk=8k (~1.6M pairs, P 0.8 GB): profiling-sized GaAs-like case
     "gaas_nk8k": SynthConfig(nk=8000, nb=2, de_pair_mev=4.45, eimp_sigma_mev=5.0),
     # MoS2-like precision case: nb=4 (two spin-split pairs), nk=30k, 4.19M pairs (P 34 GB complex128).

@@ -250,7 +250,8 @@ int dmd_ee_update(dmd_handle* h);
 int dmd_ee_read(dmd_handle* h, double* P1ee, double* P2ee, double* nfree);
 
 /* No counterpart in the reference. Shape autotuner: times every compiled shape variant of the
- * handle's contraction (f64x, nb = 2: lines per stage, ring depth, CTAs per SM; CUDA-core batches:
+ * handle's contraction (f64x, nb = 2: lines per stage, ring depth, CTAs per SM; f64, nb = 2: forward
+ * sums reduced over the warp or added in L2, CTAs per SM (1 by default); CUDA-core batches:
  * states per warp; tensor-core batches: pipeline stages, 2 of which leave room for 2 CTAs per SM) on
  * `evals` right-hand-side evaluations of the current device state (CUDA events,
  * after one warm-up evaluation each), keeps the fastest and returns its index in *chosen (0 when
