@@ -891,6 +891,59 @@ def ee_cpu_baseline(st, P1, P2, e, f, ee, nb):
                       "rebuild" % (m2, st.npair, dt2)}
 
 
+def run_sparse(args):
+    """Sparse contraction (alg_sparseP) against the dense FP64 contraction on an nb = 4 MoS2-like P
+    with a fraction of each pair's elements kept at random (the rest set to zero): per fill, the
+    event-timed contraction launch of both forms on the same operators, RK4 steps/s, and the sparse
+    form's RHS against the dense form's."""
+    import dataclasses
+    nk = args.sparse_nk
+    cfg = dataclasses.replace(S.WORKLOADS["mos2_nk30k"], nk=nk)
+    w = build_workload("mos2_nk30k", max(1, min(16, os.cpu_count() or 1)), cfg)
+    st = w["st"]
+    nb = st.cfg.nb
+    h = 1.0 * U.fs
+    y0 = np.ascontiguousarray(w["dm0"]).view(np.float64).reshape(-1).copy()
+    P1d, P2d = w["P1"], w["P2"]
+    rng = np.random.default_rng(77)
+    u = rng.random(P1d.shape)  # one draw per element: fills are nested
+    dense_bytes = 2 * st.npair * nb ** 4 * 16
+    rows = []
+    from denmat_dynm_development_gb300.dmd import LindbladGPU
+    for fill in [float(x) for x in args.sparse_fills.split(",")]:
+        keep = u < fill
+        P1 = np.where(keep, P1d, 0)
+        P2 = np.where(keep, P2d, 0)
+        r = {"fill": fill, "stored_fraction": float(np.mean((P1 != 0) | (P2 != 0)))}
+        out = {}
+        for form in ("dense", "sparse"):
+            g = LindbladGPU(nk=st.cfg.nk, nb_dm=nb, bstart=0, bend=nb, e_dm=w["e"], k1st=st.k1, k2nd=st.k2, P1=P1,
+                            P2=P2, prefac_eph=w["prefac"], picture=0, expt=1, precision="f64",
+                            sparse=(form == "sparse"))
+            try:
+                g.set_state(0.0, y0)
+                out[form] = g.func(3.0 * U.fs, y0)
+                g.rk4(h, args.warmup)
+                tm = Timed(g, h, args.steps, 3)
+                kms, _ = kernel_profile(g, h, max(2, min(args.steps, 10)))
+                r[form] = {"rk4_steps_per_s": 1e3 * args.steps / tm.median, "contraction_ms": kms["pairs"],
+                           "stored_bytes": g.pair_bytes}
+            finally:
+                g.close()
+        r["speedup"] = r["dense"]["contraction_ms"] / r["sparse"]["contraction_ms"]
+        r["sparse_vs_dense_rhs_rel_err"] = rel_err(out["sparse"], out["dense"])
+        r["faster"] = "sparse" if r["speedup"] > 1.0 else "dense"
+        rows.append(r)
+    mid = rows[len(rows) // 2]
+    line = {"metric": "sparse vs dense FP64 k-pair contraction (alg_sparseP), nb = 4", "value": mid["speedup"],
+            "unit": "x (dense / sparse contraction time at fill %.2f)" % mid["fill"], "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "mos2-like nb=4, nk=%d, %d k-pairs (dense P1+P2 %.2f GB complex128); each element "
+                                   "kept with probability = fill, the rest zero" % (nk, st.npair, dense_bytes / 1e9)},
+            "fills": rows}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -913,6 +966,9 @@ def main():
     ap.add_argument("--temperatures", action="store_true", help="batched form over 8 temperature P sets")
     ap.add_argument("--adj-tf-ps", type=float, default=50.0, help="adjoint: t_f in ps")
     ap.add_argument("--ee", action="store_true", help="e-e operators rebuilt from rho (Pee_update)")
+    ap.add_argument("--sparse", action="store_true", help="sparse vs dense FP64 contraction at several fills")
+    ap.add_argument("--sparse-nk", type=int, default=12000, help="sparse: k-points of the nb = 4 system")
+    ap.add_argument("--sparse-fills", default="0.1,0.2,0.35,0.5", help="sparse: kept fractions of the elements")
     ap.add_argument("--ee-nk", type=int, default=2000, help="e-e: k-points of the ball")
     ap.add_argument("--ee-de-mev", type=float, default=20.0, help="e-e: pair energy window (meV)")
     ap.add_argument("--ee-nb", type=int, default=2, choices=[2, 4], help="e-e: bands of the window")
@@ -936,6 +992,10 @@ def main():
     if args.ee:
         if rank == 0:
             run_ee(args)
+        return
+    if args.sparse:
+        if rank == 0:
+            run_sparse(args)
         return
     # the generator's worker processes start before any CUDA call
     w = build_workload(args.workload, max(1, min(16, (os.cpu_count() or 1) // max(world, 1))))

@@ -18,6 +18,7 @@
 #include "dmd_layout.h"
 #include "dmd_pairs.cuh"
 #include "dmd_pairs_cb.cuh"
+#include "dmd_sparse.cuh"
 
 using namespace dmd;
 
@@ -71,6 +72,13 @@ struct dmd_handle {
   double2* d_Praw = nullptr;   // [npair][2][nb4] folded P1, P2
   int2* d_kkraw = nullptr;
   int eek = 0;                 // DMD_FLAG_EE: d_Praw, d_kkraw and d_dst kept for the e-e model
+  // sparse form (DMD_FLAG_SPARSE): per k-point the products of its output threads, lane-interleaved
+  int use_sp = 0;
+  long long sp_nel = 0, sp_nslot = 0;  // stored elements (both directions), ELL slots with padding
+  long long* d_sp_base = nullptr;    // [nk] first slot of each k-point
+  int* d_sp_len = nullptr;           // [nk] products per thread (padded)
+  double2* d_sp_val = nullptr;       // [nslot] element values
+  int* d_sp_gidx = nullptr;          // [nslot] index into the coordinate array
   void* d_dst = nullptr;       // column-block destination of every stored pair (CbDst)
   // e-e model (dmd_ee_attach): P = P_base (d_Praw) + ee_scale P_ee, rebuilt from rho
   int ee_on = 0, ee_every = 0, ee_update = 0, ee_nv = 0;
@@ -310,7 +318,10 @@ template <int NB>
 int launch_pairs(dmd_handle* h) {
   if (h->npair == 0) return DMD_OK;
   ProfScope ps(h, 1);
-  if (!h->use_cb) {
+  if (h->use_sp) {  // stored elements only, one thread per output element of every k-point
+    k_pairs_sparse<NB><<<blocks_for((long long)h->nk * 2 * NB * NB, 256), 256, 0, h->st>>>(
+        h->nk, h->d_sp_base, h->d_sp_len, h->d_sp_val, h->d_sp_gidx, h->d_rs, h->d_acc);
+  } else if (!h->use_cb) {
     const long long nthr = h->npair * 4LL * NB * NB;
     k_pairs_f64_atomic<NB><<<blocks_for(nthr, 256), 256, 0, h->st>>>(h->npair, h->d_kk, h->d_P, h->d_rs, h->d_acc);
   } else {
@@ -932,6 +943,145 @@ cudaError_t tc_attrs() {
   return e;
 }
 
+// Sparse form: the stored elements (|P| > kSparseThr) regrouped by the k-point and output element
+// they update (dmd_sparse.cuh). The operators are read in chunks from the handle's source (arrays or
+// files) and folded with the additive operators in FP64 as the dense forms fold them; every pair
+// (k1, k2) gives its forward products to k1 (P1 rows, P2 columns, sources in k2's coordinates) and,
+// for k1 < k2, the reverse ones to k2 (conj(P2) rows, conj(P1) columns, sources in k1's).
+constexpr double kSparseThr = 1e-40;  // the reference's default alg_thr_sparseP (parameters.cpp:120)
+
+int upload_pairs_sparse(dmd_handle* h, const dmd_desc* d) {
+  const int nb2 = h->nb2, TPR = 2 * nb2;
+  const size_t nb4 = (size_t)h->nb4;
+  const long long np = h->npair;
+  const int nk = h->nk;
+  // pass 1 over the pair list: the pairs that feed each k-point (forward and reverse), as
+  // (pair, direction) in pair order
+  std::vector<long long> rowptr((size_t)nk + 1, 0);
+  for (long long p = 0; p < np; ++p) {
+    const uint64_t k1 = d->k1st[p], k2 = d->k2nd[p];
+    if (k1 >= (uint64_t)nk || k2 >= (uint64_t)nk) return fail(h, DMD_E_ARG, "k-pair index out of range");
+    rowptr[k1 + 1]++;
+    if (k1 < k2) rowptr[k2 + 1]++;
+  }
+  for (int k = 0; k < nk; ++k) rowptr[k + 1] += rowptr[k];
+  // pass 2 over the operators: per pair, the count of stored elements in every row and column of
+  // P1 and P2, and the elements themselves (compact, in pair order)
+  std::vector<uint8_t> cnt((size_t)np * 4 * nb2);  // [pair][P1 rows | P1 cols | P2 rows | P2 cols]
+  std::vector<long long> pe((size_t)np + 1, 0);    // first stored element of each pair
+  std::vector<double2> ev;                         // P1's stored elements (row-major), then P2's
+  std::vector<uint8_t> ei;                         // their (row, column) as row * nb^2 + column
+  ArraySource asrc(d, h->nb4);
+  PairSource* src = h->src ? h->src : &asrc;
+  const bool add = src->has_add();
+  const long long chunk = std::max<long long>(1, (256LL << 20) / (long long)(4 * nb4 * 16));
+  std::vector<double2> buf((size_t)std::min(chunk, std::max<long long>(np, 1)) * 4 * nb4);
+  for (long long p0 = 0; p0 < np; p0 += chunk) {
+    const long long nc = std::min(chunk, np - p0);
+    int rc = src->read(p0, nc, buf.data());
+    if (rc) return fail(h, rc, src->err.empty() ? std::string("reading the pair operators") : src->err);
+    const size_t n = (size_t)nc * nb4;
+    double2* P1 = buf.data();
+    double2* P2 = P1 + n;
+    if (add) {  // P += add_scale P_add (ElectronImpurity.cpp:38-39)
+      const double2* A1 = P2 + n;
+      const double2* A2 = A1 + n;
+      for (size_t i = 0; i < n; ++i) {
+        P1[i] = mk2(P1[i].x + h->add_scale * A1[i].x, P1[i].y + h->add_scale * A1[i].y);
+        P2[i] = mk2(P2[i].x + h->add_scale * A2[i].x, P2[i].y + h->add_scale * A2[i].y);
+      }
+    }
+    for (long long q = 0; q < nc; ++q) {
+      const long long p = p0 + q;
+      uint8_t* c = &cnt[(size_t)p * 4 * nb2];
+      for (int m = 0; m < 2; ++m) {
+        const double2* M = (m ? P2 : P1) + (size_t)q * nb4;
+        for (int a = 0; a < nb2; ++a)
+          for (int b = 0; b < nb2; ++b) {
+            const double2 v = M[(size_t)a * nb2 + b];
+            if (std::sqrt(v.x * v.x + v.y * v.y) > kSparseThr) {
+              ev.push_back(v);
+              ei.push_back((uint8_t)(a * nb2 + b));
+              c[2 * m * nb2 + a]++;
+              c[(2 * m + 1) * nb2 + b]++;
+            }
+          }
+      }
+      pe[(size_t)p + 1] = (long long)ev.size();
+    }
+  }
+  // the products per output thread of every k-point: L_k = the longest list among its threads
+  std::vector<int> len((size_t)nk, 0);
+  std::vector<long long> base((size_t)nk + 1, 0);
+  {
+    std::vector<int> cl((size_t)nk * TPR, 0);
+    for (long long p = 0; p < np; ++p) {
+      const int k1 = (int)d->k1st[p], k2 = (int)d->k2nd[p];
+      const uint8_t* c = &cnt[(size_t)p * 4 * nb2];
+      for (int a = 0; a < nb2; ++a) {
+        cl[(size_t)k1 * TPR + a] += c[a];                    // X_k1[a]: row a of P1
+        cl[(size_t)k1 * TPR + nb2 + a] += c[3 * nb2 + a];    // Y_k1[a]: column a of P2
+        if (k1 < k2) {
+          cl[(size_t)k2 * TPR + a] += c[2 * nb2 + a];        // X_k2[a]: row a of conj(P2)
+          cl[(size_t)k2 * TPR + nb2 + a] += c[nb2 + a];      // Y_k2[a]: column a of conj(P1)
+        }
+      }
+    }
+    for (int k = 0; k < nk; ++k) {
+      int m = 0;
+      for (int l = 0; l < TPR; ++l) m = std::max(m, cl[(size_t)k * TPR + l]);
+      len[k] = m;
+      base[(size_t)k + 1] = base[k] + (long long)m * TPR;
+    }
+  }
+  const long long nslot = base[nk];
+  std::vector<double2> val((size_t)std::max<long long>(1, nslot), mk2(0.0, 0.0));
+  std::vector<int> gidx((size_t)std::max<long long>(1, nslot), 0);
+  std::vector<int> fillc((size_t)nk * TPR, 0);
+  auto put = [&](int k, int l, double2 v, int gi) {
+    const long long s = base[k] + (long long)fillc[(size_t)k * TPR + l]++ * TPR + l;
+    val[(size_t)s] = v;
+    gidx[(size_t)s] = gi;
+  };
+  for (long long p = 0; p < np; ++p) {
+    const int k1 = (int)d->k1st[p], k2 = (int)d->k2nd[p];
+    const bool rev = k1 < k2;
+    long long e = pe[(size_t)p];
+    for (int m = 0; m < 2; ++m) {
+      const uint8_t* c = &cnt[(size_t)p * 4 * nb2 + 2 * m * nb2];
+      long long ne = 0;
+      for (int a = 0; a < nb2; ++a) ne += c[a];
+      for (long long q = 0; q < ne; ++q, ++e) {
+        const int a = ei[(size_t)e] / nb2, b = ei[(size_t)e] % nb2;
+        const double2 v = ev[(size_t)e], vc = mk2(v.x, -v.y);
+        if (m == 0) {  // P1[a][b]: X_k1[a] += P1 rt_k2[b]; reverse Y_k2[b] += st_k1[a] conj(P1)
+          put(k1, a, v, k2 * TPR + b);
+          if (rev) put(k2, nb2 + b, vc, k1 * TPR + nb2 + a);
+        } else {       // P2[a][b]: Y_k1[b] += st_k2[a] P2; reverse X_k2[a] += conj(P2) rt_k1[b]
+          put(k1, nb2 + b, v, k2 * TPR + nb2 + a);
+          if (rev) put(k2, a, vc, k1 * TPR + b);
+        }
+      }
+    }
+  }
+  h->sp_nel = 0;
+  for (long long p = 0; p < np; ++p) {
+    const long long ne = pe[(size_t)p + 1] - pe[(size_t)p];
+    h->sp_nel += ne * (d->k1st[p] < d->k2nd[p] ? 2 : 1);
+  }
+  h->sp_nslot = nslot;
+  int rc;
+  if ((rc = dalloc(h, &h->d_sp_base, (size_t)nk)) || (rc = dalloc(h, &h->d_sp_len, (size_t)nk)) ||
+      (rc = dalloc(h, &h->d_sp_val, val.size())) || (rc = dalloc(h, &h->d_sp_gidx, gidx.size())))
+    return rc;
+  CK(cudaMemcpy(h->d_sp_base, base.data(), (size_t)nk * sizeof(long long), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_sp_len, len.data(), (size_t)nk * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_sp_val, val.data(), val.size() * 16, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_sp_gidx, gidx.data(), gidx.size() * 4, cudaMemcpyHostToDevice));
+  h->pair_bytes = (int64_t)(nslot * 20 + (long long)nk * 12);
+  return DMD_OK;
+}
+
 int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
   const int nb = h->nb, nk = h->nk;
   std::vector<double> ew((size_t)nk * nb);
@@ -1150,7 +1300,8 @@ void release(dmd_handle* h) {
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
                   h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0, h->d_Praw, h->d_kkraw,
                   h->d_dst, h->d_ee_kvec, h->d_ee_kidx, h->d_ee_kmap, h->d_ee_U, h->d_ee_ewf, h->d_ee_f,
-                  h->d_ee_dm, h->d_ee_dm1, h->d_ee_dmf, h->d_ee_dm1f, h->d_ee_scr, h->d_ee_Pee, h->d_ee_vqtab};
+                  h->d_ee_dm, h->d_ee_dm1, h->d_ee_dmf, h->d_ee_dm1f, h->d_ee_scr, h->d_ee_Pee, h->d_ee_vqtab,
+                  h->d_sp_base, h->d_sp_len, h->d_sp_val, h->d_sp_gidx};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -1370,7 +1521,10 @@ static int create_impl(const dmd_desc* d, dmd_handle** out, PairSource* src) {
     return DMD_E_ARG;
   if (d->nkpair > 0 && (!d->k1st || !d->k2nd || (!src && (!d->P1 || !d->P2)))) return DMD_E_ARG;
   if (!src && (d->P1_add == nullptr) != (d->P2_add == nullptr)) return DMD_E_ARG;
-  if (d->flags & ~(DMD_FLAG_LINEAR | DMD_FLAG_ADJOINT | DMD_FLAG_EE)) return DMD_E_ARG;
+  if (d->flags & ~(DMD_FLAG_LINEAR | DMD_FLAG_ADJOINT | DMD_FLAG_EE | DMD_FLAG_SPARSE)) return DMD_E_ARG;
+  if ((d->flags & DMD_FLAG_SPARSE) && (d->precision != DMD_PREC_F64 || d->nrhs > 1 ||
+                                       (d->flags & (DMD_FLAG_LINEAR | DMD_FLAG_ADJOINT | DMD_FLAG_EE))))
+    return DMD_E_ARG;
   if ((d->flags & DMD_FLAG_ADJOINT) && d->nrhs > 1) return DMD_E_ARG;
   const int nrhs = d->nrhs > 1 ? d->nrhs : 1;
   // batched form: FP32 or bf16 hi+lo storage on the column-block contraction
@@ -1404,6 +1558,7 @@ static int create_impl(const dmd_desc* d, dmd_handle** out, PairSource* src) {
   h->lin = (d->flags & DMD_FLAG_LINEAR) ? 1 : 0;
   h->adj = (d->flags & DMD_FLAG_ADJOINT) ? 1 : 0;
   h->eek = (d->flags & DMD_FLAG_EE) ? 1 : 0;
+  h->use_sp = (d->flags & DMD_FLAG_SPARSE) ? 1 : 0;
   h->nrhs = nrhs;
   h->nstate1 = (size_t)h->nk * h->nbdm * h->nbdm;
   h->nstate = h->nstate1 * nrhs;
@@ -1426,8 +1581,8 @@ static int create_impl(const dmd_desc* d, dmd_handle** out, PairSource* src) {
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return bail(DMD_E_CUDA);
   const size_t nk = h->nk, nbdm = h->nbdm;
   if ((rc = dalloc(h, &h->d_ew, nk * h->nb)) || (rc = dalloc(h, &h->d_edm, nk * nbdm)) ||
-      (rc = dalloc(h, &h->d_kk, (h->nb == 2 || h->nb == 4) ? 1 : (size_t)h->npair)) ||
-      (rc = dalloc(h, &h->d_P, h->use_tc ? 1 : ((size_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) + 15) / 16)) ||
+      (rc = dalloc(h, &h->d_kk, (h->nb == 2 || h->nb == 4 || h->use_sp) ? 1 : (size_t)h->npair)) ||
+      (rc = dalloc(h, &h->d_P, (h->use_tc || h->use_sp) ? 1 : ((size_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) + 15) / 16)) ||
       (rc = dalloc(h, &h->d_rs, nk * 2 * h->nb2 * nrhs)) || (rc = dalloc(h, &h->d_acc, nk * 2 * h->nb2 * nrhs)) ||
       (rc = dalloc(h, &h->d_y, h->nstate)) || (rc = dalloc(h, &h->d_ytmp, h->nstate)) ||
       (rc = dalloc(h, &h->d_y0, h->nstate)) || (rc = dalloc(h, &h->d_in, h->nstate)) ||
@@ -1448,15 +1603,17 @@ static int create_impl(const dmd_desc* d, dmd_handle** out, PairSource* src) {
     if (cudaMemcpy(h->d_H, d->Hcoh, h->nstate1 * 16, cudaMemcpyHostToDevice) != cudaSuccess)
       return bail(fail(h, DMD_E_CUDA, "upload H"));
   }
-  h->use_cb = ((h->nb == 2 || h->nb == 4) && h->npair > 0) ? 1 : 0;
+  h->use_cb = ((h->nb == 2 || h->nb == 4) && h->npair > 0 && !h->use_sp) ? 1 : 0;
   if (!h->use_tc)
     h->pair_bytes = h->use_cb ? (int64_t)h->npair * 2 * h->nb4 * elem_bytes(h->prec) : (int64_t)h->npair * 2 * h->nb4 * 16;
-  if (src && (!h->use_cb || h->use_tc || h->adj)) return bail(fail(h, DMD_E_ARG, "streamed operators need the column-block form"));
+  if (src && !h->use_sp && (!h->use_cb || h->use_tc || h->adj))
+    return bail(fail(h, DMD_E_ARG, "streamed operators need the column-block or the sparse form"));
   if (h->eek && (!h->use_cb || h->use_tc || h->nrhs != 1 || h->lin || src || h->adj))
     return bail(fail(h, DMD_E_ARG, "DMD_FLAG_EE needs nb = 2 or 4, a single state, no linearization, no adjoint "
                                    "(P_ee depends on rho) and the operators as arrays"));
   h->src = src;
-  rc = h->use_tc ? upload_pairs_tc(h, d) : h->use_cb ? upload_pairs_cb(h, d) : upload_pairs(h, d);
+  rc = h->use_tc ? upload_pairs_tc(h, d) : h->use_sp ? upload_pairs_sparse(h, d) : h->use_cb ? upload_pairs_cb(h, d)
+                                                                                  : upload_pairs(h, d);
   h->src = nullptr;
   if (rc) return bail(rc);
   if ((h->adj || h->eek) && h->use_cb && h->npair > 0) {  // stored-order P: the adjoint, the e-e refill
@@ -1630,7 +1787,8 @@ int dmd_create_from_sparse_files(const dmd_desc* d, const char* sp1_prefix, cons
   dc.P1 = dc.P2 = dc.P1_add = dc.P2_add = nullptr;
   const char* tc = getenv("DMD_BATCH_TC");
   const bool tc_form = d->nrhs > 1 && nb == 2 && d->precision == DMD_PREC_BF16X2 && !(tc && atoi(tc) == 0);
-  if (!((nb == 2 || nb == 4) && d->nkpair > 0 && !tc_form && !(d->flags & DMD_FLAG_ADJOINT)))
+  if (!(d->flags & DMD_FLAG_SPARSE) &&
+      !((nb == 2 || nb == 4) && d->nkpair > 0 && !tc_form && !(d->flags & DMD_FLAG_ADJOINT)))
     return DMD_E_ARG;  // the other forms take dense operators (dmd_create, dmd_create_from_files)
   return create_impl(&dc, out, &ss);
 }
@@ -1653,7 +1811,8 @@ int dmd_create_from_files(const dmd_desc* d, const char* p1_path, const char* p2
   dc.P1 = dc.P2 = dc.P1_add = dc.P2_add = nullptr;
   const char* tc = getenv("DMD_BATCH_TC");
   const bool tc_form = d->nrhs > 1 && nb == 2 && d->precision == DMD_PREC_BF16X2 && !(tc && atoi(tc) == 0);
-  if ((nb == 2 || nb == 4) && d->nkpair > 0 && !tc_form && !(d->flags & DMD_FLAG_ADJOINT))
+  if (((nb == 2 || nb == 4) && d->nkpair > 0 && !tc_form && !(d->flags & DMD_FLAG_ADJOINT)) ||
+      (d->flags & DMD_FLAG_SPARSE))
     return create_impl(&dc, out, &fs);  // streamed: two chunks of the files in host memory at a time
   // the other forms take the operators from host memory
   std::vector<double> buf[4];

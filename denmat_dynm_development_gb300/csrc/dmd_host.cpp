@@ -220,6 +220,7 @@ struct dmdh_system {
   double carrier_gs[3] = {0, 0, 0};  // eip.carrier_bvk_gs, ne_bvk_gs, nh_bvk_gs (electron.h:155-157)
   std::vector<std::pair<std::vector<double>, std::vector<double>>> imp;  // impurity P x |n_i V| (linear mode)
   int nimp = 0;                      // number of impurity densities (eip.ni.size())
+  int sparse = 0;                    // alg_sparseP: the handle contracts the stored elements only
   double nfree = 0;                  // clp.nfreetot = |ne| + |nh| of set_mu_and_n (electron.h:157)
   // e-e model (eeMode): the descriptor for dmd_ee_attach and the arrays it points into
   int ee = 0;                        // 1: Pee_update, 2: Pee_fixed_at_eq
@@ -350,11 +351,16 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
   auto& pm = s->pm;
   // features outside this path are rejected explicitly
   const char* unsupported[] = {"alg_linearize_dPee", "alg_phenom_relax", "alg_semiclassical",
-                               "alg_sparseP", "alg_Pin_is_sparse", "alg_only_eimp", "alg_only_ee", "needL",
+                               "alg_Pin_is_sparse", "alg_only_eimp", "alg_only_ee", "needL",
                                "alg_read_Bso", "gfac_normal_dist", "partial_ionized"};
   for (const char* k : unsupported)
     if (pget(pm, k, 0) != 0) return err(DMD_E_ARG, std::string(k) + " is not supported by the GB300 path");
   const bool linear = pget(pm, "alg_linearize", 0) != 0;
+  s->sparse = pget(pm, "alg_sparseP", 0) != 0;  // the sparse contraction (DMD_FLAG_SPARSE, FP64)
+  if (s->sparse && linear)  // parameters.cpp:434-435
+    return err(DMD_E_ARG, "linearization does not support sparse matrices");
+  if (s->sparse && sget(pm, "eeMode", "none") != "none")
+    return err(DMD_E_ARG, "alg_sparseP with the e-e model is not supported by the GB300 path");
   if (linear && pget(pm, "alg_ddmdteq", 0) != 0)  // parameters.cpp:428-429
     return err(DMD_E_ARG, "if master equation is linearized, ddmdt_eq is not needed");
   if (sget(pm, "code", "jdftx") != "jdftx" || sget(pm, "material_model", "none") != "none")
@@ -542,6 +548,8 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
     if (ni == 0) break;
     if (sget(pm, "impMode" + nm, "model_ionized") != "ab_neutral")
       return err(DMD_E_ARG, "only impMode = ab_neutral is supported");
+    if (s->sparse)  // parameters.cpp:472-473
+      return err(DMD_E_ARG, "ab initio neutral e-imp does not support sparse matrices");
     s->nimp = iD + 1;
     const double fraction = fabs(ni * cell);  // electronimpurity ctor (ElectronImpurity.h:18)
     if (iD == 0) in.eimp_fraction = fraction;
@@ -778,7 +786,7 @@ int dmdh_desc(const dmdh_system* s, int32_t precision, int32_t device, dmd_desc*
   d->expt = s->info.expt;
   d->precision = precision;
   d->device = device;
-  d->flags = (s->info.linear ? DMD_FLAG_LINEAR : 0u) | (s->ee ? DMD_FLAG_EE : 0u);
+  d->flags = (s->info.linear ? DMD_FLAG_LINEAR : 0u) | (s->ee ? DMD_FLAG_EE : 0u) | (s->sparse ? DMD_FLAG_SPARSE : 0u);
   d->f_ref = s->f_eq.empty() ? s->f_dm.data() : s->f_eq.data();
   return DMD_OK;
 }

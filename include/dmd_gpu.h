@@ -62,6 +62,12 @@ extern "C" {
 #define DMD_FLAG_EE 4u      /* keep the operators P_eph (+ P_eimp) in their stored order and the
                                column-block map, for the e-e model (dmd_ee_attach); single state,
                                not linearized, not with DMD_FLAG_ADJOINT, operators given as arrays */
+#define DMD_FLAG_SPARSE 8u  /* alg_sparseP / alg_Pin_is_sparse (evolve_eph.cpp:67-82, sparse_zgemm in
+                               comm/sparse_matrix.cpp:6-40): keep only the elements with |P| > 1e-40
+                               (the reference's default thr_sparseP; explicit zeros of sparse files are
+                               dropped as well) and contract those; DMD_PREC_F64, a single state, not
+                               with DMD_FLAG_LINEAR, DMD_FLAG_ADJOINT or DMD_FLAG_EE. It pays below
+                               about a third of the elements stored (bench --sparse) */
 
 /* pictures (alg.picture) */
 #define DMD_PICTURE_INTERACTION 0

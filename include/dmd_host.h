@@ -53,7 +53,8 @@ int dmdh_load(const char* dir, dmdh_system** out);
 void dmdh_free(dmdh_system* s);
 const char* dmdh_error(void);
 int dmdh_info_get(const dmdh_system* s, dmdh_info* info);
-/* descriptor for dmd_create pointing into the loaded arrays (valid while s lives) */
+/* descriptor for dmd_create pointing into the loaded arrays (valid while s lives); with alg_sparseP
+ * the descriptor asks for the sparse contraction (DMD_FLAG_SPARSE), which needs DMD_PREC_F64 */
 int dmdh_desc(const dmdh_system* s, int32_t precision, int32_t device, dmd_desc* d);
 /* copies of set-up arrays: dm0 (complex [nk][nb_dm^2]), f (double [nk][nb_dm]),
  * spin matrices (complex [nk][3][nb_dm^2]) */

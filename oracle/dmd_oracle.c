@@ -52,6 +52,8 @@ typedef struct {
   int linear;          /* alg.linearize: P1, P2 hold Lscij, Lscji (ElectronPhonon_linear.cpp) */
   const double* f_lin; /* [nk][nb] window f_eq of the linearization */
   struct orc_ee* ee;   /* e-e model rebuilt from rho on every RHS (eeMode Pee_update, freq < 0), or NULL */
+  int sparse;          /* alg.sparseP: P kept as sparse_mat per pair and contracted by sparse_zgemm */
+  double thr_sparse;   /* alg.thr_sparseP */
 } orc_sys;
 
 /* e-e scattering model (ElecElec_Model.h) with static screening (Coulomb_Model.h:394-688):
@@ -143,12 +145,89 @@ static void compute_Pt(int nb, double t, const double* ek, const double* ekp, co
   }
 }
 
+/* sparse_mat::sparse (comm/sparse_matrix.h:57-69): the elements with abs(A) = sqrt(norm) > thr, row-major */
+static int sparse_of(const zc* A, int n2, double thr, zc* sv, int* si, int* sj) {
+  int ns = 0;
+  for (int i = 0; i < n2; i++)
+    for (int j = 0; j < n2; j++) {
+      const zc a = A[i * n2 + j];
+      if (sqrt(a.x * a.x + a.y * a.y) > thr) {
+        sv[ns] = a;
+        si[ns] = i;
+        sj[ns] = j;
+        ns++;
+      }
+    }
+  return ns;
+}
+
+/* compute_sPt (evolve_eph.cpp:194-203): the phase of every stored element; ij2i / ij2j split the
+ * operator's row (i1 i2) and column (i3 i4) indices */
+static void compute_sPt(int nb, double t, const double* ek, const double* ekp, const zc* sv, const int* si,
+                        const int* sj, int ns, zc* st, int minus) {
+  for (int is = 0; is < ns; is++) {
+    const int i = si[is] / nb, j = si[is] % nb, k = sj[is] / nb, l = sj[is] % nb;
+    if (!minus) st[is] = zmul(sv[is], zcis((ek[i] - ekp[k] - ek[j] + ekp[l]) * t));
+    else st[is] = zmul(sv[is], zcis((ek[k] - ekp[i] - ek[l] + ekp[j]) * t));
+  }
+}
+
+/* sparse_zgemm (comm/sparse_matrix.cpp:6-40) with alpha = beta = 1 for the two shapes the evolve
+ * loop uses: left (m = nb^2, n = 1): c[i] += s b[j]; right (m = 1, n = nb^2): c[j] += b[i] s. The
+ * c *= beta pass over the whole output is kept. */
+static void sparse_zgemm_v(zc* c, int left, const zc* sv, const int* si, const int* sj, int ns, const zc* b, int n2) {
+  const zc one = zmk(1, 0);
+  for (int i = 0; i < n2; i++) c[i] = zmul(c[i], one);
+  if (left)
+    for (int is = 0; is < ns; is++) c[si[is]] = zadd(c[si[is]], zmul(sv[is], b[sj[is]]));
+  else
+    for (int is = 0; is < ns; is++) c[sj[is]] = zadd(c[sj[is]], zmul(b[si[is]], sv[is]));
+}
+
+/* The sparse branch of the pair loop (alg.sparseP, evolve_eph.cpp:67-82): P1 and P2 of every pair as
+ * sparse_mat (built from the dense operators with thr_sparseP, ElectronPhonon.cpp:115-130), phases per
+ * element, sparse GEMVs, and for k < k' the conjugated elements of P2 / P1 on the k' side. */
+static void orc_pairs_sparse(const orc_sys* s, const double* e, double t, const zc* dm, const zc* dm1, int64_t p0,
+                             int64_t p1, zc* Pdm, zc* dm1P) {
+  const int nb = s->bend - s->bstart, nb2 = nb * nb, nb4 = nb2 * nb2;
+  zc *s1 = (zc*)xmalloc(sizeof(zc) * nb4), *s2 = (zc*)xmalloc(sizeof(zc) * nb4);
+  zc *t1 = (zc*)xmalloc(sizeof(zc) * nb4), *t2 = (zc*)xmalloc(sizeof(zc) * nb4);
+  zc *n1 = (zc*)xmalloc(sizeof(zc) * nb4), *n2 = (zc*)xmalloc(sizeof(zc) * nb4);
+  int *i1 = (int*)xmalloc(sizeof(int) * nb4), *j1 = (int*)xmalloc(sizeof(int) * nb4);
+  int *i2 = (int*)xmalloc(sizeof(int) * nb4), *j2 = (int*)xmalloc(sizeof(int) * nb4);
+  for (int64_t ip = p0; ip < p1; ip++) {
+    const int ik = (int)s->k1st[ip], ikp = (int)s->k2nd[ip];
+    const int ns1 = sparse_of(s->P1 + (size_t)ip * nb4, nb2, s->thr_sparse, s1, i1, j1);
+    const int ns2 = sparse_of(s->P2 + (size_t)ip * nb4, nb2, s->thr_sparse, s2, i2, j2);
+    if (!s->expt) {
+      memcpy(t1, s1, sizeof(zc) * ns1);
+      memcpy(t2, s2, sizeof(zc) * ns2);
+    } else {
+      compute_sPt(nb, t, e + (size_t)ik * nb, e + (size_t)ikp * nb, s1, i1, j1, ns1, t1, 0);
+      compute_sPt(nb, t, e + (size_t)ik * nb, e + (size_t)ikp * nb, s2, i2, j2, ns2, t2, 1);
+    }
+    sparse_zgemm_v(Pdm + (size_t)ik * nb2, 1, t1, i1, j1, ns1, dm + (size_t)ikp * nb2, nb2);
+    sparse_zgemm_v(dm1P + (size_t)ik * nb2, 0, t2, i2, j2, ns2, dm1 + (size_t)ikp * nb2, nb2);
+    if (ik < ikp) {
+      for (int q = 0; q < ns2; q++) n1[q] = zconj(t2[q]); /* sm1_next = conj(smat2_time) */
+      for (int q = 0; q < ns1; q++) n2[q] = zconj(t1[q]); /* sm2_next = conj(smat1_time) */
+      sparse_zgemm_v(Pdm + (size_t)ikp * nb2, 1, n1, i2, j2, ns2, dm + (size_t)ik * nb2, nb2);
+      sparse_zgemm_v(dm1P + (size_t)ikp * nb2, 0, n2, i1, j1, ns1, dm1 + (size_t)ik * nb2, nb2);
+    }
+  }
+  free(s1); free(s2); free(t1); free(t2); free(n1); free(n2); free(i1); free(j1); free(i2); free(j2);
+}
+
 /* The rank-local pair loop of electronphonon::evolve (evolve_eph.cpp:49-135) over pairs [p0, p1)
  * (one MPI rank's contiguous slice, mymp::distribute_var mymp.cpp:8-36), accumulating into Pdm and
  * dm1P (summode, dense P, expt or not; no valley filtering: the default alg.only_intra/intervalley =
  * false and fewer than two valleys keep every pair, evolve_eph.cpp:52-58). e is [nk][nb]. */
 void orc_pairs_partial(const orc_sys* s, const double* e, double t, const zc* dm, const zc* dm1, int64_t p0, int64_t p1,
                        zc* Pdm, zc* dm1P) {
+  if (s->sparse) {
+    orc_pairs_sparse(s, e, t, dm, dm1, p0, p1, Pdm, dm1P);
+    return;
+  }
   const int nb = s->bend - s->bstart, nb2 = nb * nb, nb4 = nb2 * nb2;
   const zc c1 = zmk(1, 0);
   zc *P1t = (zc*)xmalloc(sizeof(zc) * nb4), *P2t = (zc*)xmalloc(sizeof(zc) * nb4);

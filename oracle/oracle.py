@@ -111,7 +111,8 @@ class _Sys(C.Structure):
                 ("k1st", C.c_void_p), ("k2nd", C.c_void_p), ("P1", C.c_void_p), ("P2", C.c_void_p),
                 ("e_dm", C.c_void_p), ("prefac_eph", C.c_double), ("Hcoh", C.c_void_p),
                 ("picture_schrodinger", C.c_int), ("expt", C.c_int), ("ddmdt_eq", C.c_void_p), ("scatt_enable", C.c_int),
-                ("linear", C.c_int), ("f_lin", C.c_void_p), ("ee", C.c_void_p)]
+                ("linear", C.c_int), ("f_lin", C.c_void_p), ("ee", C.c_void_p), ("sparse", C.c_int),
+                ("thr_sparse", C.c_double)]
 
 
 class _EE(C.Structure):
@@ -362,13 +363,16 @@ class OracleSystem:
     linear: bool = False                     # alg_linearize: P1, P2 hold Lscij, Lscji
     f_lin: Optional[np.ndarray] = None       # [nk][nb] window f_eq of the linearization
     ee: Optional[EEModel] = None             # eeMode = Pee_update: P1, P2 are ee.P1eff, ee.P2eff
+    sparse: bool = False                     # alg.sparseP: P contracted as sparse_mat (sparse_zgemm)
+    thr_sparse: float = 1e-40                # alg.thr_sparseP
 
     def cstruct(self):
         s = _Sys(nk=self.nk, nb_dm=self.nb_dm, bstart=self.bstart, bend=self.bend, npair=self.npair,
                  k1st=_ptr(self.k1st), k2nd=_ptr(self.k2nd), P1=_ptr(self.P1), P2=_ptr(self.P2), e_dm=_ptr(self.e_dm),
                  prefac_eph=self.prefac_eph, Hcoh=_ptr(self.Hcoh), picture_schrodinger=self.picture_schrodinger,
                  expt=self.expt, ddmdt_eq=_ptr(self.ddmdt_eq), scatt_enable=1, linear=1 if self.linear else 0,
-                 f_lin=_ptr(self.f_lin), ee=C.addressof(self.ee.c) if self.ee is not None else None)
+                 f_lin=_ptr(self.f_lin), ee=C.addressof(self.ee.c) if self.ee is not None else None,
+                 sparse=1 if self.sparse else 0, thr_sparse=self.thr_sparse)
         return s
 
     @property
@@ -524,7 +528,8 @@ def load(d: str) -> OracleSystem:
                         picture_schrodinger=schrod, expt=expt, t0=t0, tstep=tstep, tend=pget(pm, "tend", 0.0, fs),
                         temperature=T, mu=mu, nk_full=sz["nk_full"], ob_prefac=(1.0 / sz["nk_full"]) / cell_size_cmd,
                         ode=ode, params=pm, nv_dm=nv_dm, mue=mue, muh=muh, f_eq=f_eq, ddmdt_eq=ddmdt_eq, linear=linear,
-                        f_lin=f_lin, ee=ee)
+                        f_lin=f_lin, ee=ee, sparse=int(pget(pm, "alg_sparseP", 0.0)) != 0,
+                        thr_sparse=pget(pm, "alg_thr_sparseP", 1e-40))
 
 
 def ee_operators(s: OracleSystem, ee: EEModel, dm_window, f_window, nfree):

@@ -98,6 +98,17 @@ CASES = {
                             param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0.3, 0, 0.2),
                                        extra=dict(EE_COMMON, scrFormula="RPA", update_screening=1,
                                                   ee_antisymmetry=1))),
+    # sparse operators (alg_sparseP): 70 % of every pair's P1 / P2 elements zeroed, nb = 4, B field;
+    # the reference contracts the stored elements with sparse_zgemm (e-ph only: the reference refuses
+    # ab-initio e-imp with sparse P)
+    "nb4_sparse": dict(cfg=SynthConfig(nk=16, nb=4, seed=41, de_pair_mev=60.0),
+                       param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0.4, 0, 0.3), extra={"alg_sparseP": 1}),
+                       zero_fraction=0.7),
+    # the same for nb = 2 with half the elements zeroed, Schrodinger picture without phases
+    "nb2_sparse": dict(cfg=SynthConfig(nk=40, nb=2, seed=42, de_pair_mev=60.0),
+                       param=dict(Bpert_T=(0, 0, 0.1), B_T=(0, 0.8, 0),
+                                  extra={"alg_sparseP": 1, "alg_picture": "schrodinger", "alg_expt": 0}),
+                       zero_fraction=0.5),
     # two valence bands below the e-ph window (holes: nv_dm = 2), equilibrium drift subtracted
     "nb2_holes_eq": dict(cfg=SynthConfig(nk=24, nb=2, seed=17, de_pair_mev=60.0, extra_bands=2, nv=2),
                          param=dict(Bpert_T=(0.1, 0, 0.05), B_T=(0, 0, 1.0), extra={"alg_ddmdteq": 1})),
@@ -133,6 +144,15 @@ def make_case(name, spec, ref_bin, outroot):
     os.makedirs(d)
     cfg = spec["cfg"]
     info = make_ldbd(d, cfg, tstep_fs=1.0, tend_fs=20.0, **spec["param"])
+    if spec.get("zero_fraction"):  # structural zeros, the same positions in P1 and P2 of a pair
+        rng = np.random.default_rng([cfg.seed, 7])
+        nb4 = cfg.nb ** 4
+        paths = [os.path.join(d, "ldbd_data", "ldbd_P%d_lindblad.bin" % m) for m in (1, 2)]
+        P = [np.fromfile(q, dtype=np.complex128).reshape(-1, nb4) for q in paths]
+        mask = rng.random(P[0].shape) < spec["zero_fraction"]
+        for q, a in zip(paths, P):
+            a[mask] = 0.0
+            a.tofile(q)
     if spec.get("carrier_scale"):
         # an electron density carrier_scale times the one at the generator's mu, in cm^-3
         e = np.fromfile(os.path.join(d, "ldbd_data", "ldbd_ek.bin")).reshape(cfg.nk, -1)[:, cfg.nv:]

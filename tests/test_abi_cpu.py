@@ -77,3 +77,20 @@ def test_create_from_sparse_files_checks_the_counts_file(tmp_path):
     st = L.dmd_create_from_sparse_files(C.byref(d), str(tmp_path / "sP1").encode(), str(tmp_path / "sP2").encode(),
                                         None, None, C.byref(h))
     assert st == 3  # DMD_E_FILE
+
+
+def test_sparse_flag_is_validated_before_any_device_call():
+    """DMD_FLAG_SPARSE is the FP64 form of one state without the linearized, adjoint or e-e options:
+    other combinations give DMD_E_ARG before the device is queried"""
+    import ctypes as C
+    from denmat_dynm_development_gb300 import dmd
+    L = dmd._lib()
+    e = np.zeros((4, 2))
+    k = np.zeros(1, np.uint64)
+    P = np.zeros(16, np.complex128)
+    h = C.c_void_p()
+    for prec, flags, nrhs in ((dmd.PREC["f64x"], dmd.FLAG_SPARSE, 1), (dmd.PREC["f64"], dmd.FLAG_SPARSE | dmd.FLAG_ADJOINT, 1),
+                              (dmd.PREC["f64"], dmd.FLAG_SPARSE | dmd.FLAG_EE, 1), (dmd.PREC["f32"], dmd.FLAG_SPARSE, 4)):
+        d = dmd._Desc(nk=4, nb_dm=2, bstart=0, bend=2, nkpair=1, e_dm=e.ctypes.data, k1st=k.ctypes.data,
+                      k2nd=k.ctypes.data, P1=P.ctypes.data, P2=P.ctypes.data, precision=prec, flags=flags, nrhs=nrhs)
+        assert L.dmd_create(C.byref(d), C.byref(h)) == 1
