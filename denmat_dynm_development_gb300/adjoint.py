@@ -87,6 +87,92 @@ class ModeScaledRK4:
         return s, grad
 
 
+class StreamedModeScaledRK4:
+    """ModeScaledRK4 for systems whose operator sets do not fit in memory together (the 4.19M-pair
+    nb = 4 MoS2-like system: 34 GB per set in complex128). The sets come from a source with
+    scaled(theta), mode(m) and contract(G) -- ldbd_synth.ModeSets regenerates them chunk by chunk --
+    and one device handle (DMD_FLAG_ADJOINT) at theta serves both the gradient and the central
+    differences: dmd_add_operators shifts one set's scale in place (P += delta P^(m)), so at most one
+    set besides P is on the host at a time and P itself lives only on the device after set-up.
+
+    The gradient is dJ/dtheta_m = Re sum conj(dJ/dP) P^(m): dJ/dP (one more set's worth of memory)
+    is written by the library's adjoint into shared memory and contracted by the source's workers."""
+
+    def __init__(self, *, modes, nk, nb_dm, bstart, bend, e_dm, k1st, k2nd, prefac_eph, y0, dt, nsteps, obs_steps,
+                 obs, f_obs, ob_prefac, theta, obs_bstart=0, t0=0.0, Hcoh=None, picture="interaction", expt=1,
+                 precision="f64x", checkpoint=200, device=0):
+        self.modes = modes
+        self.nparams = modes.nparams
+        self.theta = np.asarray(theta, np.float64)
+        if self.theta.shape != (self.nparams,):
+            raise ValueError("theta must have %d entries" % self.nparams)
+        self.y0 = np.ascontiguousarray(y0, np.float64)
+        self.t0, self.dt, self.nsteps = float(t0), float(dt), int(nsteps)
+        self.obs_steps = np.asarray(obs_steps, np.int64)
+        self.obs_bstart = int(obs_bstart)
+        self.checkpoint = int(checkpoint)
+        P = modes.scaled(self.theta)
+        try:
+            self.g = LindbladGPU(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, e_dm=e_dm, k1st=k1st, k2nd=k2nd,
+                                 P1=P.a[0], P2=P.a[1], prefac_eph=prefac_eph, Hcoh=Hcoh, picture=picture, expt=expt,
+                                 precision=precision, device=device, adjoint=True)
+        finally:
+            P.close()
+        self.g.set_observable(0, obs, f_obs, ob_prefac)
+
+    def close(self):
+        if self.g is not None:
+            self.g.close()
+            self.g = None
+
+    def forward(self):
+        """S at the observed steps with the handle's current operators"""
+        g = self.g
+        g.set_state(self.t0, self.y0)
+        out, cur = [], 0
+        for s in self.obs_steps:
+            if s > cur:
+                g.rk4(self.dt, int(s - cur))
+                cur = int(s)
+            out.append(g.measure(0, self.obs_bstart)[0])
+        return np.array(out)
+
+    def gradient(self, weights):
+        """(S at the observed steps, dJ/dtheta) at self.theta for J = sum_i weights[i] S(t_i)"""
+        import time
+        from .ldbd_synth import SharedPair
+        w = np.asarray(weights, np.float64)
+        G = SharedPair(self.g.npair, self.g.nb4)
+        try:
+            t0 = time.perf_counter()
+            s, _, _ = self.g.adjoint_rk4(self.t0, self.y0, self.dt, self.nsteps, self.obs_steps, w, slot=0,
+                                         bstart=self.obs_bstart, checkpoint=self.checkpoint, dP_out=G.a)
+            t1 = time.perf_counter()
+            grad = self.modes.contract(G)
+            self.last_timing = {"adjoint_rk4_s": t1 - t0, "mode_contraction_s": time.perf_counter() - t1}
+        finally:
+            G.close()
+        return s, grad
+
+    def central_differences(self, weights, rel_step=1e-4):
+        """dJ/dtheta_m by central differences, h = rel_step * theta_m, each set shifted in place"""
+        w = np.asarray(weights, np.float64)
+        out = np.zeros(self.nparams)
+        for m in range(self.nparams):
+            h = rel_step * self.theta[m]
+            Pm = self.modes.mode(m)
+            try:
+                self.g.add_operators(Pm.a[0], Pm.a[1], h)
+                jp = float(w @ self.forward())
+                self.g.add_operators(Pm.a[0], Pm.a[1], -2.0 * h)
+                jm = float(w @ self.forward())
+                self.g.add_operators(Pm.a[0], Pm.a[1], h)
+            finally:
+                Pm.close()
+            out[m] = (jp - jm) / (2.0 * h)
+        return out
+
+
 def sz_trajectory(theta, model: ModeScaledRK4):
     """torch: S(t_i) as a differentiable function of theta (a float64 tensor of nmodes entries)."""
     return _SzFn.apply(theta, model)

@@ -893,7 +893,7 @@ int fill_pairs_cb(dmd_handle* h, PairSource& src, const std::vector<CbDst>& dst,
     if (e != cudaSuccess) break;
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-  if (e == cudaSuccess && h->eek) {  // kept for the e-e model's refills
+  if (e == cudaSuccess && (h->eek || h->adj)) {  // kept for the e-e model's refills, dmd_add_operators
     h->d_dst = d_dst;
     d_dst = nullptr;
   }
@@ -2468,6 +2468,20 @@ __global__ void __launch_bounds__(256) k_fma_rate(int iters, T a, T b, T* sink) 
   }
 }
 
+// raw operators of a chunk of pairs ([pair][P1 | P2][nb^4]) += scale * (P1_add | P2_add), the additive
+// operators of the chunk given as [P1: cnt][nb^4] then [P2: cnt][nb^4]
+__global__ void k_praw_axpy(long long cnt, size_t nb4, const double2* __restrict__ add, double scale,
+                            double2* __restrict__ raw) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long n = cnt * (long long)nb4;
+  if (i >= 2 * n) return;
+  const int m = (int)(i / n);
+  const long long r = i - m * n, j = r / (long long)nb4, e = r - j * (long long)nb4;
+  double2& o = raw[(size_t)j * 2 * nb4 + (size_t)m * nb4 + e];
+  const double2 a = add[i];
+  o = mk2(__dadd_rn(o.x, __dmul_rn(a.x, scale)), __dadd_rn(o.y, __dmul_rn(a.y, scale)));
+}
+
 template <typename T>
 int fma_rate(int device, double* tflops) {
   int nsm = 0;
@@ -2522,6 +2536,50 @@ int dmd_selftest_wait_timeout(int device, uint32_t polls, int* status) {
   if (rc != DMD_OK) return rc;
   if (hv[1] != 1u) return DMD_E_CUDA;
   *status = (hv[0] & DMD_DEVERR_TIMEOUT) ? DMD_E_TIMEOUT : DMD_OK;
+  return DMD_OK;
+}
+
+int dmd_add_operators(dmd_handle* h, const double* P1_add, const double* P2_add, double scale) {
+  if (!h || !P1_add || !P2_add) return DMD_E_ARG;
+  if (!h->use_cb || h->use_tc || h->lin || h->nrhs != 1 || !h->d_Praw || !h->d_dst || h->ee_on)
+    return fail(h, DMD_E_ARG, "dmd_add_operators needs a handle made with DMD_FLAG_ADJOINT (or DMD_FLAG_EE without "
+                              "an attached e-e model), nb = 2 or 4, a single state, not linearized");
+  CK(cudaSetDevice(h->dev));
+  CK(cudaStreamSynchronize(h->st));
+  const size_t nb4 = (size_t)h->nb4;
+  const long long chunk = std::max<long long>(1, std::min<long long>(h->npair, (128LL << 20) / (long long)(2 * nb4 * 16)));
+  double2* tmp = nullptr;
+  int rc;
+  if ((rc = dalloc(h, &tmp, (size_t)chunk * 2 * nb4))) return rc;
+  cudaError_t e = cudaSuccess;
+  for (long long p0 = 0; p0 < h->npair && e == cudaSuccess; p0 += chunk) {
+    const long long cnt = std::min<long long>(chunk, h->npair - p0);
+    const size_t n = (size_t)cnt * nb4;
+    e = cudaMemcpy(tmp, P1_add + 2 * (size_t)p0 * nb4, n * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(tmp + n, P2_add + 2 * (size_t)p0 * nb4, n * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      k_praw_axpy<<<blocks_for((long long)(2 * n), 256), 256, 0, h->st>>>((long long)cnt, nb4, tmp, scale,
+                                                                           h->d_Praw + 2 * (size_t)p0 * nb4);
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    }
+  }
+  cudaFree(tmp);
+  if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("dmd_add_operators: ") + cudaGetErrorString(e));
+  // the stored form again from the updated operators (and, in the deviation forms, the constant term)
+  const bool dev = deviation_form(h->prec);
+  if (dev) CK(cudaMemsetAsync(h->d_acc0, 0, (size_t)h->nk * 2 * h->nb2 * sizeof(double2), h->st));
+  const FillSrc fs = {h->d_Praw, nb4, 2 * nb4, nullptr, 0, 0};
+  const unsigned g = blocks_for(h->npair, 128);
+  if (h->nb == 2)
+    k_cb_fill<2><<<g, 128, 0, h->st>>>(0, h->npair, fs, 0.0, (const CbDst*)h->d_dst, 0, h->prec, elem_bytes(h->prec),
+                                       (unsigned char*)h->d_P, h->d_fref, dev ? (double*)h->d_acc0 : nullptr);
+  else
+    k_cb_fill<4><<<g, 128, 0, h->st>>>(0, h->npair, fs, 0.0, (const CbDst*)h->d_dst, 0, h->prec, elem_bytes(h->prec),
+                                       (unsigned char*)h->d_P, h->d_fref, dev ? (double*)h->d_acc0 : nullptr);
+  h->launches += 1 + (h->npair + chunk - 1) / chunk;
+  CKL();
+  CK(cudaStreamSynchronize(h->st));
   return DMD_OK;
 }
 

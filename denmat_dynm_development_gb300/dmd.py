@@ -71,7 +71,7 @@ EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_s
            "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
            "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes", "dmd_adjoint_rk4", "dmd_autotune",
            "dmd_group_create", "dmd_group_rk4", "dmd_group_destroy",
-           "dmd_create_from_files", "dmd_create_from_sparse_files", "dmd_selftest_wait_timeout", "dmd_peak_fma",
+           "dmd_create_from_files", "dmd_create_from_sparse_files", "dmd_selftest_wait_timeout", "dmd_peak_fma", "dmd_add_operators",
            "dmd_ee_attach", "dmd_ee_update", "dmd_ee_read"]
 
 
@@ -109,6 +109,7 @@ def _lib():
         L.dmd_group_destroy.argtypes = [vp]
         L.dmd_selftest_wait_timeout.argtypes = [C.c_int, C.c_uint32, C.POINTER(C.c_int)]
         L.dmd_peak_fma.argtypes = [C.c_int, C.c_int, C.POINTER(d)]
+        L.dmd_add_operators.argtypes = [vp, vp, vp, d]
         L.dmd_create_from_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                             C.POINTER(vp)]
         L.dmd_create_from_sparse_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p,
@@ -321,16 +322,22 @@ class LindbladGPU:
         return n.value
 
     def adjoint_rk4(self, t0, y0, dt, nsteps, obs_step, obs_weight, slot=0, bstart=0, bend=None, checkpoint=200,
-                    want_dP=True, want_dy0=False):
+                    want_dP=True, want_dy0=False, dP_out=None):
         """Reverse mode of `nsteps` RK4 steps from (t0, y0) for J = sum_i w_i S(t0 + obs_step[i] dt) (S: the
         total of observable `slot`). Returns (S at the observed steps, dJ/dP as complex [2][nkpair][nb^4]
-        with dJ = Re sum(conj(dJ/dP) dP) or None, dJ/dy0 as y0's layout or None)."""
+        with dJ = Re sum(conj(dJ/dP) dP) or None, dJ/dy0 as y0's layout or None). dP_out: a C-contiguous
+        complex128 [2][nkpair][nb^4] array to receive dJ/dP (e.g. in shared memory) instead of a new one."""
         bend = self.nb_dm if bend is None else bend
         y0 = np.ascontiguousarray(y0, dtype=np.float64)
         st = np.ascontiguousarray(obs_step, dtype=np.int64)
         w = np.ascontiguousarray(obs_weight, dtype=np.float64)
         s = np.zeros(st.size)
-        dP = np.zeros(2 * self.npair * self.nb4 * 2) if want_dP else None
+        if dP_out is not None:
+            if dP_out.dtype != np.complex128 or dP_out.size != 2 * self.npair * self.nb4 or not dP_out.flags.c_contiguous:
+                raise ValueError("dP_out must be a C-contiguous complex128 [2][nkpair][nb^4] array")
+            dP = dP_out.reshape(-1).view(np.float64)
+        else:
+            dP = np.zeros(2 * self.npair * self.nb4 * 2) if want_dP else None
         dy = np.zeros(self.ny) if want_dy0 else None
         ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
         self._ck(_lib().dmd_adjoint_rk4(self._h, float(t0), y0.ctypes.data, float(dt), int(nsteps), int(checkpoint),
@@ -339,6 +346,14 @@ class LindbladGPU:
         if dP is not None:
             dP = dP.view(np.complex128).reshape(2, self.npair, self.nb4)
         return s, dP, dy
+
+    def add_operators(self, P1_add, P2_add, scale):
+        """P += scale * P_add on the device (DMD_FLAG_ADJOINT handles), stored form rebuilt"""
+        A1 = np.ascontiguousarray(P1_add, np.complex128)
+        A2 = np.ascontiguousarray(P2_add, np.complex128)
+        if A1.size != self.npair * self.nb4 or A2.size != self.npair * self.nb4:
+            raise ValueError("P1_add, P2_add must hold nkpair * nb^4 elements")
+        self._ck(_lib().dmd_add_operators(self._h, A1.ctypes.data, A2.ctypes.data, float(scale)))
 
     def autotune(self, evals=3):
         """time the compiled contraction shapes on the current state, keep the fastest; returns its index"""

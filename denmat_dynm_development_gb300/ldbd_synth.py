@@ -414,6 +414,100 @@ def generate_arrays(cfg: SynthConfig, fold_fraction: Optional[float] = None, pro
     return (st, outs[0], outs[1], outs[2] if want_q else None, outs[3] if want_q else None)
 
 
+def _modes_worker(args):
+    """Worker (spawned process, numpy only): one chunk of the per-parameter operator sets (the phonon
+    modes, then the unscaled e-imp operators when the configuration has them) put to one use:
+      ("scaled", theta): P = sum_m theta_m P^(m) written to the two output buffers;
+      ("mode", m):       P^(m) written to the two output buffers;
+      ("contract", _):   Re sum conj(G) P^(m) for every m, with G read from the two buffers."""
+    from multiprocessing import shared_memory
+    cfg_d, ew, k1, k2, omegas, ic, p0, names, nb4, npair, job = args
+    cfg = SynthConfig(**cfg_d)
+    ek = ew[k1.astype(np.int64)]
+    ekp = ew[k2.astype(np.int64)]
+    a1, a2 = eph_chunk_modes(cfg, ek, ekp, omegas, ic)
+    if cfg.eimp_sigma_mev is not None:
+        q1, q2 = eimp_chunk(cfg, ek, ekp, ic)
+        a1 = np.concatenate([a1, q1[None]])
+        a2 = np.concatenate([a2, q2[None]])
+    p1 = p0 + a1.shape[1]
+    bufs = [shared_memory.SharedMemory(name=n) for n in names]
+    try:
+        views = np.ndarray((2, npair, nb4), np.complex128, buffer=bufs[0].buf)
+        kind, arg = job
+        out = None
+        if kind == "scaled":
+            th = np.asarray(arg, np.float64)
+            views[0][p0:p1] = np.tensordot(th, a1, 1)
+            views[1][p0:p1] = np.tensordot(th, a2, 1)
+        elif kind == "mode":
+            views[0][p0:p1] = a1[arg]
+            views[1][p0:p1] = a2[arg]
+        else:
+            g1, g2 = views[0][p0:p1], views[1][p0:p1]
+            out = np.array([np.vdot(g1, a1[m]).real + np.vdot(g2, a2[m]).real for m in range(a1.shape[0])])
+        del views
+    finally:
+        for b in bufs:
+            b.close()
+    return ic, out
+
+
+class SharedPair:
+    """complex128 [2][npair][nb^4] in shared memory -- the operators P1, P2 or a gradient with respect
+    to them, one block after the other as the library's dJdP -- readable by the generator's worker
+    processes; a[0], a[1] are the two blocks; close() releases them."""
+
+    def __init__(self, npair, nb4):
+        from multiprocessing import shared_memory
+        self.shm = [shared_memory.SharedMemory(create=True, size=max(16, 2 * npair * nb4 * 16))]
+        self.a = np.ndarray((2, npair, nb4), np.complex128, buffer=self.shm[0].buf)
+
+    def close(self):
+        self.a = None
+        for m in self.shm:
+            m.close()
+            m.unlink()
+        self.shm = []
+
+
+class ModeSets:
+    """The per-parameter operator sets of a synthetic system (the phonon modes' |g|^2 scales, then the
+    impurity operator when cfg.eimp_sigma_mev is set), produced chunk by chunk by `procs` spawned
+    worker processes and never held together: P(theta) = sum_m theta_m P^(m), one set P^(m), or the
+    contractions Re sum conj(G) P^(m) with a gradient G. The chunks are the generator's, so every
+    set equals mode_operators' arrays."""
+
+    def __init__(self, cfg: SynthConfig, procs: Optional[int] = None):
+        self.cfg = cfg
+        self.st = setup(cfg)
+        self.procs = procs or min(16, os.cpu_count() or 1)
+        self.nb4 = cfg.nb ** 4
+        self.nparams = cfg.nmodes + (1 if cfg.eimp_sigma_mev is not None else 0)
+
+    def _run(self, pair: SharedPair, job):
+        import multiprocessing as mp
+        st, C = self.st, self.st.chunk_size()
+        jobs = [(self.cfg.to_dict(), st.ew, st.k1[p0:min(st.npair, p0 + C)], st.k2[p0:min(st.npair, p0 + C)],
+                 st.omegas, ic, p0, [m.name for m in pair.shm], self.nb4, st.npair, job)
+                for ic, p0 in enumerate(range(0, st.npair, C))]
+        with mp.get_context("spawn").Pool(processes=self.procs) as pool:
+            return [r for _, r in sorted(pool.imap_unordered(_modes_worker, jobs), key=lambda x: x[0])]
+
+    def scaled(self, theta) -> SharedPair:
+        out = SharedPair(self.st.npair, self.nb4)
+        self._run(out, ("scaled", [float(x) for x in theta]))
+        return out
+
+    def mode(self, m: int) -> SharedPair:
+        out = SharedPair(self.st.npair, self.nb4)
+        self._run(out, ("mode", int(m)))
+        return out
+
+    def contract(self, G: SharedPair) -> np.ndarray:
+        return np.sum(self._run(G, ("contract", None)), axis=0)
+
+
 def mode_operators(cfg: SynthConfig):
     """Per-mode e-ph operators and the unscaled e-imp operators of a (small) synthetic system:
     (setup, P1m [nmodes][npair][nb^4], P2m, Q1 or None, Q2 or None), chunk by chunk in one process."""

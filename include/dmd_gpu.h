@@ -170,6 +170,13 @@ int dmd_pair_bytes(const dmd_handle* h, int64_t* bytes);
 int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64_t nsteps, int64_t checkpoint,
                     int slot, int bstart, int bend, int64_t nobs, const int64_t* obs_step,
                     const double* obs_weight, double* s_obs, double* dJdP, double* dJdy0);
+/* No counterpart in the reference (its operators are fixed after set-up, apart from the e-e model).
+ * P += scale * P_add on the device for both operators (complex128 [nkpair][nb^4] each, in the stored
+ * pair order), then the handle's stored form is rebuilt from them: how central differences of a
+ * trajectory with respect to an operator set's scale are taken without a second copy of P. Needs a
+ * handle made with DMD_FLAG_ADJOINT (or DMD_FLAG_EE before an e-e model is attached), nb = 2 or 4, a
+ * single state, not linearized. Synchronous; the state and time are unchanged. */
+int dmd_add_operators(dmd_handle* h, const double* P1_add, const double* P2_add, double scale);
 /* wait for the handle's stream */
 int dmd_sync(dmd_handle* h);
 

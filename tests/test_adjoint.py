@@ -177,3 +177,53 @@ def test_t1_loglinear_recovers_an_exponential():
     t = np.linspace(0, 10, 21)
     s = torch.tensor(3e-4 * np.exp(-t / 4.5), dtype=torch.float64)
     assert abs(float(t1_loglinear(t, s)) - 4.5) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["f64", "f64x"])
+def test_add_operators_equals_a_new_handle(precision, oracle, built):
+    """dmd_add_operators (P += scale P_add on the device, stored form rebuilt) gives the RHS of a
+    handle created with the shifted operators, and adding the opposite shift restores it."""
+    s = oracle.load(os.path.join(GOLDEN, "nb4_eimp_B"))
+    rng = np.random.default_rng(2)
+    A1 = 1e-2 * (rng.standard_normal(s.P1.shape) + 1j * rng.standard_normal(s.P1.shape)) * np.abs(s.P1).max()
+    A2 = 1e-2 * (rng.standard_normal(s.P2.shape) + 1j * rng.standard_normal(s.P2.shape)) * np.abs(s.P2).max()
+    y = oracle.y_of(s.dm0)
+    t = 17.0 * oracle.fs
+    tol = 1e-15 if precision == "f64" else 1e-13
+    with _gpu(s, adjoint=True, precision=precision) as g, \
+            _gpu(s, P1=s.P1 + 0.3 * A1, P2=s.P2 + 0.3 * A2, precision=precision) as h:
+        r0 = g.func(t, y)
+        g.add_operators(A1, A2, 0.3)
+        assert rel(g.func(t, y), h.func(t, y)) < 10 * tol
+        g.add_operators(A1, A2, -0.3)
+        assert rel(g.func(t, y), r0) < 10 * tol
+
+
+@pytest.mark.gpu
+def test_streamed_mode_model_matches_the_in_memory_one(oracle, built, tmp_path):
+    """StreamedModeScaledRK4 (operator sets regenerated chunk by chunk, one device handle, central
+    differences by in-place shifts) gives the in-memory model's gradient, and its own central
+    differences agree with it at the adjoint's tolerance."""
+    from denmat_dynm_development_gb300 import ldbd_synth as S
+    from denmat_dynm_development_gb300.adjoint import StreamedModeScaledRK4
+    s, model, theta, steps = _mode_model(oracle, tmp_path)
+    cfg = S.SynthConfig(nk=60, nb=2, seed=11, eimp_sigma_mev=5.0)  # _mode_model's system
+    w = np.zeros(steps.size)
+    w[-1] = 1.0
+    _, g_mem = model.gradient(theta, w)
+    ms = S.ModeSets(cfg, procs=2)
+    assert ms.nparams == theta.size and ms.st.npair == s.npair
+    sm = StreamedModeScaledRK4(modes=ms, nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm,
+                               k1st=s.k1st, k2nd=s.k2nd, prefac_eph=s.prefac_eph, y0=oracle.y_of(s.dm0),
+                               dt=model.dt, nsteps=model.nsteps, obs_steps=steps, obs=s.smat[:, 2, :], f_obs=s.f_dm,
+                               ob_prefac=s.ob_prefac, theta=theta, obs_bstart=s.nv_dm, t0=s.t0, Hcoh=s.Hcoh,
+                               picture=s.picture_schrodinger, expt=s.expt, precision="f64", checkpoint=16)
+    try:
+        _, g_st = sm.gradient(w)
+        fd = sm.central_differences(w, FD_H)
+    finally:
+        sm.close()
+    print("streamed adjoint", g_st, "\n in-memory", g_mem, "\n fd", fd)
+    assert rel(g_st, g_mem) < 1e-10
+    assert rel(g_st, fd) < TOL

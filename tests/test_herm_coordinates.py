@@ -90,3 +90,4 @@ def test_non_hermitian_state_as_two_passes():
     np.testing.assert_allclose(H + 1j * A, V, atol=1e-15)
     xp = Q1 @ coords(H.reshape(-1), nb) + 1j * (Q1 @ coords(A.reshape(-1), nb))
     np.testing.assert_allclose(back(xp, nb), P1 @ V.reshape(-1), atol=1e-12)
+
