@@ -2844,6 +2844,75 @@ int dmd_ee_update(dmd_handle* h) {
   return DMD_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// P_ee at the occupations d_f and P3..P6 of every pair (k_ee_p36), into d_p [4][npair][nb^4]
+template <int NB>
+int ee_linear_nb(dmd_handle* h, const double* d_f, double2* d_p) {
+  constexpr int NB4 = NB * NB * NB * NB;
+  EeArgs a = h->ee_args;
+  a.dm = a.dm1 = nullptr;
+  a.dmf = a.dm1f = nullptr;
+  a.f = d_f;
+  constexpr int WPC = ee_warps_per_cta(NB);
+  const unsigned grid = (unsigned)((h->npair + WPC - 1) / WPC);
+  if (h->prec == DMD_PREC_F64) k_ee_pairs<NB, EeF64><<<grid, 32 * WPC, 0, h->st>>>(a);
+  else k_ee_pairs<NB, EeDF><<<grid, 32 * WPC, 0, h->st>>>(a);
+  const size_t n = (size_t)h->npair * NB4;
+  k_ee_p36<NB><<<(unsigned)h->npair, NB == 4 ? 256 : 32, 0, h->st>>>(a, d_f, d_p, d_p + n, d_p + 2 * n, d_p + 3 * n);
+  h->launches += 2;
+  CKL();
+  return DMD_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int dmd_ee_linear_terms(dmd_handle* h, const double* f_eq, double nfree, double* P1ee, double* P2ee, double* P3,
+                        double* P4, double* P5, double* P6) {
+  if (!h || !f_eq) return DMD_E_ARG;
+  if (!h->ee_on) return fail(h, DMD_E_STATE, "no e-e model attached");
+  if (h->npair == 0) return DMD_OK;
+  CK(cudaSetDevice(h->dev));
+  const size_t nb4 = (size_t)h->nb4, np = (size_t)h->npair;
+  double* d_f = nullptr;
+  double2* d_p = nullptr;
+  int rc;
+  if ((rc = dalloc(h, &d_f, (size_t)h->nk * h->nb)) || (rc = dalloc(h, &d_p, 4 * np * nb4))) {
+    cudaFree(d_f);
+    return rc;
+  }
+  auto done = [&](int r) {
+    cudaFree(d_f);
+    cudaFree(d_p);
+    return r;
+  };
+  if (cudaMemcpy(d_f, f_eq, (size_t)h->nk * h->nb * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+    return done(fail(h, DMD_E_CUDA, "dmd_ee_linear_terms: upload f"));
+  // the screening constants of density nfree (coulomb_model::init(f_eq) when the model updates it)
+  k_ee_screen<<<1, 256, 0, h->st>>>(h->nk, h->nb, h->ee_nv, nullptr, 0, nfree, h->ee_nkfull, h->ee_cell, h->ee_eps,
+                                    h->ee_T, h->ee_meff, h->d_ee_scr);
+  rc = h->nb == 2 ? ee_linear_nb<2>(h, d_f, d_p) : ee_linear_nb<4>(h, d_f, d_p);
+  // the attach-time screening again
+  k_ee_screen<<<1, 256, 0, h->st>>>(h->nk, h->nb, h->ee_nv, nullptr, 0, h->ee_nfree0, h->ee_nkfull, h->ee_cell,
+                                    h->ee_eps, h->ee_T, h->ee_meff, h->d_ee_scr);
+  if (rc) return done(rc);
+  if (cudaStreamSynchronize(h->st) != cudaSuccess) return done(fail(h, DMD_E_CUDA, "dmd_ee_linear_terms"));
+  std::vector<double2> buf(np * 2 * nb4);
+  if (cudaMemcpy(buf.data(), h->d_ee_Pee, buf.size() * 16, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return done(fail(h, DMD_E_CUDA, "dmd_ee_linear_terms: read P_ee"));
+  for (size_t p = 0; p < np; ++p) {
+    if (P1ee) memcpy(P1ee + 2 * p * nb4, &buf[p * 2 * nb4], nb4 * 16);
+    if (P2ee) memcpy(P2ee + 2 * p * nb4, &buf[(p * 2 + 1) * nb4], nb4 * 16);
+  }
+  double* outs[4] = {P3, P4, P5, P6};
+  for (int m = 0; m < 4; ++m)
+    if (outs[m] && cudaMemcpy(outs[m], d_p + m * np * nb4, np * nb4 * 16, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return done(fail(h, DMD_E_CUDA, "dmd_ee_linear_terms: read P3..P6"));
+  return done(DMD_OK);
+}
+
 int dmd_ee_read(dmd_handle* h, double* P1ee, double* P2ee, double* nfree) {
   if (!h) return DMD_E_ARG;
   if (!h->ee_on) return fail(h, DMD_E_STATE, "no e-e model attached");

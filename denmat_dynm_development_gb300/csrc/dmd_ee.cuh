@@ -632,4 +632,144 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
   }
 }
 
+// The e-e source of the linearized operators besides P_ee (elecelec_model::calc_P3P4 and calc_P5P6,
+// ElecElec_Model_linear.cpp:3-112), at the occupations f (the f_eq of the linearization), for every
+// stored pair (k1, ka), FP64:
+//   P3 / P4[(i1,i2),(ia,ib)] = sum_(k3, i3, i4) A[(i1,i4),(i3,ia)] w conj(A[(i2,i4),(i3,ib)]), A of
+//     (k1, k4, k3, ka) with k4 = k1 + k3 - ka, w = (1 - f3) f4 (P3) or f3 (1 - f4) (P4);
+//   P5 / P6[(i1,i2),(ia,ib)] = sum_(k3, i3, i4) A[(i1,i3),(ib,i4)] w conj(A[(i2,i3),(ia,i4)]), A of
+//     (k1, k3, ka, k4) with k4 = k1 + ka - k3, w = f3 f4 (P5) or (1 - f3)(1 - f4) (P6);
+// A(q1, q2, q3, q4)[(a,b),(c,d)] = delta(e_q1 a - e_q2 b + e_q3 c - e_q4 d) vq(q1 - q2) o(q1,q2)[a][b]
+// o(q3,q4)[c][d] (the exchange form with the exchange term), as calc_A (ElecElec_Model.h:144-162).
+// With the exchange term P3, P4 stay zero (the reference skips them). A set-up computation: one block
+// per pair; its first warp tests 32 k3 at a time for a k4 on the set and a band combination in the
+// window (the exact FP64 test), keeping the candidates in k3 order; then all threads build A of
+// each candidate in shared memory and thread (i1,i2,ia,ib) accumulates its four outputs in k3 order.
+__device__ __forceinline__ double2 ee_cmul(double2 a, double2 b) {
+  return mk2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 ee_cfma_conjb(double2 a, double2 b, double2 c) {  // c + a conj(b)
+  return mk2(fma(a.x, b.x, fma(a.y, b.y, c.x)), fma(a.y, b.x, fma(-a.x, b.y, c.y)));
+}
+
+template <int NB>
+__global__ void __launch_bounds__(NB == 4 ? 256 : 32) k_ee_p36(EeArgs a, const double* __restrict__ f,
+                                                              double2* __restrict__ P3, double2* __restrict__ P4,
+                                                              double2* __restrict__ P5, double2* __restrict__ P6) {
+  constexpr int NB2 = NB * NB, NB4 = NB2 * NB2;
+  __shared__ double2 sA[NB4];
+  __shared__ double2 so12[NB2], so34[NB2], so14[NB2], so32[NB2];
+  __shared__ int cand3[32], cand4[32];
+  __shared__ int ncand;
+  const int p = blockIdx.x;
+  if (p >= a.npair) return;
+  const int t = threadIdx.x;
+  const int k1 = a.kk[p].x, ka = a.kk[p].y;
+  const EeScreen scr = *a.scr;
+  const unsigned FULL = 0xffffffffu;
+  const int i1 = t / (NB * NB2), i2 = (t / NB2) % NB, ia = (t / NB) % NB, ib = t % NB;  // output (i1,i2),(ia,ib)
+  for (int phase = 0; phase < 2; ++phase) {
+    double2 x = mk2(0, 0), y = mk2(0, 0);
+    if (!(phase == 0 && a.antisym)) {
+      for (int c0 = 0; c0 < a.nk; c0 += 32) {
+        if (t < 32) {
+          const int k3 = c0 + t;
+          int k4 = -1;
+          bool ok = k3 < a.nk;
+          if (ok && phase == 0) ok = !(ka == k3 && !a.antisym) && !(a.antisym && ka == k3 && k1 == ka);
+          if (ok && phase == 1) ok = !(k1 == k3 && !a.antisym) && !(a.antisym && k1 == k3 && ka == k3);
+          if (ok) {  // k4 = k1 + k3 - ka (phase 0) or k1 + ka - k3 (phase 1) by mesh index arithmetic
+            const int4 u = a.kidx[k1], v = a.kidx[phase ? ka : k3], w = a.kidx[phase ? k3 : ka];
+            int m[3] = {u.x + v.x - w.x, u.y + v.y - w.y, u.z + v.z - w.z};
+            for (int d = 0; d < 3; ++d) m[d] += m[d] < 0 ? a.kmesh[d] : (m[d] >= a.kmesh[d] ? -a.kmesh[d] : 0);
+            k4 = a.kmap[((size_t)m[0] * a.kmesh[1] + m[1]) * a.kmesh[2] + m[2]];
+            ok = k4 >= 0;
+          }
+          if (ok) {  // calc_delta's window test over every band combination
+            const int q1 = k1, q2 = phase ? k3 : k4, q3 = phase ? ka : k3, q4 = phase ? k4 : ka;
+            bool hit = false;
+            for (int c = 0; c < NB4; ++c) {
+              const double de = a.ew[(size_t)q1 * NB + c / (NB * NB2)] - a.ew[(size_t)q2 * NB + (c / NB2) % NB] +
+                                a.ew[(size_t)q3 * NB + (c / NB) % NB] - a.ew[(size_t)q4 * NB + c % NB];
+              hit |= fabs(de) < a.ethr;
+            }
+            ok = hit;
+          }
+          const unsigned ball = __ballot_sync(FULL, ok);
+          if (ok) {
+            const int pos = __popc(ball & ((1u << t) - 1));
+            cand3[pos] = k3;
+            cand4[pos] = k4;
+          }
+          if (t == 0) ncand = __popc(ball);
+        }
+        __syncthreads();
+        const int nc = ncand;
+        for (int ci = 0; ci < nc; ++ci) {
+          const int k3 = cand3[ci], k4 = cand4[ci];
+          const int q1 = k1, q2 = phase ? k3 : k4, q3 = phase ? ka : k3, q4 = phase ? k4 : ka;
+          if (t < NB2) {  // calc_ovlps with the first overlap times vq
+            const double vq = ee_vq(a, scr, q1, q2);
+            const double2 o = ee_ovlp<NB>(a, q1, q2, t / NB, t % NB);
+            so12[t] = mk2(vq * o.x, vq * o.y);
+            so34[t] = ee_ovlp<NB>(a, q3, q4, t / NB, t % NB);
+            if (a.antisym) {
+              const double vx = ee_vq(a, scr, q1, q4);
+              const double2 ox = ee_ovlp<NB>(a, q1, q4, t / NB, t % NB);
+              so14[t] = mk2(vx * ox.x, vx * ox.y);
+              so32[t] = ee_ovlp<NB>(a, q3, q2, t / NB, t % NB);
+            }
+          }
+          __syncthreads();
+          if (t < NB4) {  // A[(c1,c2),(c3,c4)] = delta mee (calc_delta, calc_mee[_ex], calc_A)
+            const int c1 = t / (NB * NB2), c2 = (t / NB2) % NB, c3 = (t / NB) % NB, c4 = t % NB;
+            const double de = a.ew[(size_t)q1 * NB + c1] - a.ew[(size_t)q2 * NB + c2] + a.ew[(size_t)q3 * NB + c3] -
+                              a.ew[(size_t)q4 * NB + c4];
+            double2 mee = ee_cmul(so12[c1 * NB + c2], so34[c3 * NB + c4]);
+            if (a.antisym) {
+              const double2 mex = ee_cmul(so14[c1 * NB + c4], so32[c3 * NB + c2]);
+              mee = mk2(0.5 * mee.x - 0.5 * mex.x, 0.5 * mee.y - 0.5 * mex.y);
+            }
+            const double dl = fabs(de) < a.ethr ? exp(a.prefac_exp * de * de) : 0.0;
+            sA[t] = mk2(dl * mee.x, dl * mee.y);
+          }
+          __syncthreads();
+          if (t < NB4) {
+            const double* f3 = f + (size_t)k3 * NB;
+            const double* f4 = f + (size_t)k4 * NB;
+            if (phase == 0) {
+              for (int i4 = 0; i4 < NB; ++i4)
+                for (int i3 = 0; i3 < NB; ++i3) {
+                  const double2 A1 = sA[((i1 * NB + i4) * NB + i3) * NB + ia];
+                  const double2 A2 = sA[((i2 * NB + i4) * NB + i3) * NB + ib];
+                  const double w3 = (1 - f3[i3]) * f4[i4], w4 = f3[i3] * (1 - f4[i4]);
+                  x = ee_cfma_conjb(mk2(w3 * A1.x, w3 * A1.y), A2, x);
+                  y = ee_cfma_conjb(mk2(w4 * A1.x, w4 * A1.y), A2, y);
+                }
+            } else {
+              for (int i3 = 0; i3 < NB; ++i3)
+                for (int i4 = 0; i4 < NB; ++i4) {
+                  const double2 A1 = sA[((i1 * NB + i3) * NB + ib) * NB + i4];
+                  const double2 A2 = sA[((i2 * NB + i3) * NB + ia) * NB + i4];
+                  const double w5 = f3[i3] * f4[i4], w6 = (1 - f3[i3]) * (1 - f4[i4]);
+                  x = ee_cfma_conjb(mk2(w5 * A1.x, w5 * A1.y), A2, x);
+                  y = ee_cfma_conjb(mk2(w6 * A1.x, w6 * A1.y), A2, y);
+                }
+            }
+          }
+          __syncthreads();
+        }
+        __syncthreads();  // every thread has read ncand before the next chunk's test overwrites it
+      }
+    }
+    if (t < NB4) {
+      double2* ox = (phase ? P5 : P3) + (size_t)p * NB4 + t;
+      double2* oy = (phase ? P6 : P4) + (size_t)p * NB4 + t;
+      *ox = mk2(a.prefac * x.x, a.prefac * x.y);
+      *oy = mk2(a.prefac * y.x, a.prefac * y.y);
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace dmd

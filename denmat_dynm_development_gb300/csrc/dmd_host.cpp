@@ -290,7 +290,7 @@ int dmdh_H_BS(int32_t nk, int32_t nb, const double* smat, const double B[3], con
 // add_Lscij_from_P1_P2 with fac2 = false, ElectronPhonon_linear.cpp:147-225), every pair in order.
 // f is the window f_eq [nk][nb].
 void lsc_add(int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, const zc* P1, const zc* P2, const double* f,
-             zc* Lscii, zc* Lij, zc* Lji) {
+             zc* Lscii, zc* Lij, zc* Lji, bool fac2 = false) {
   const int nb2 = nb * nb, nb4 = nb2 * nb2;
   auto sub = [](zc a, zc b) { return zc{a.x - b.x, a.y - b.y}; };
   auto add = [](zc a, zc b) { return zc{a.x + b.x, a.y + b.y}; };
@@ -329,11 +329,88 @@ void lsc_add(int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, cons
         const int i12 = i1 * nb + i2, n12 = i12 * nb2;
         for (int iab = 0; iab < nb2; iab++) {
           const int i12ab = n12 + iab, iab12 = iab * nb2 + i12;
-          a[i12ab] = add(a[i12ab], add(scl(1 - f[(size_t)ik * nb + i1], P1p[i12ab]), scl(f[(size_t)ik * nb + i2], P2p[iab12])));
-          b[i12ab] = add(b[i12ab], add(scl(1 - f[(size_t)jk * nb + i1], cj(P2p[i12ab])), scl(f[(size_t)jk * nb + i2], cj(P1p[iab12]))));
+          const zc ca = add(scl(1 - f[(size_t)ik * nb + i1], P1p[i12ab]), scl(f[(size_t)ik * nb + i2], P2p[iab12]));
+          const zc cb = add(scl(1 - f[(size_t)jk * nb + i1], cj(P2p[i12ab])), scl(f[(size_t)jk * nb + i2], cj(P1p[iab12])));
+          a[i12ab] = add(a[i12ab], fac2 ? scl(2, ca) : ca);  // the exchange term doubles it (ElectronPhonon_linear.cpp:84)
+          b[i12ab] = add(b[i12ab], fac2 ? scl(2, cb) : cb);
         }
       }
   }
+}
+
+// The e-e terms of the linear operators beyond P_ee: add_Lscij_from_P3_P4 and add_Lscij_from_P5_P6
+// (ElectronPhonon_linear.cpp:199-245), every pair in order.
+void lsc_add_p36(int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, const zc* P3, const zc* P4,
+                 const zc* P5, const zc* P6, const double* f, zc* Lij, zc* Lji) {
+  const int nb2 = nb * nb, nb4 = nb2 * nb2;
+  auto sub = [](zc a, zc b) { return zc{a.x - b.x, a.y - b.y}; };
+  auto add = [](zc a, zc b) { return zc{a.x + b.x, a.y + b.y}; };
+  auto scl = [](double r, zc a) { return zc{a.x * r, a.y * r}; };
+  auto cj = [](zc a) { return zc{a.x, -a.y}; };
+  for (int64_t p = 0; p < npair; p++) {
+    const int ik = (int)k1[p], jk = (int)k2[p];
+    const double *fi = f + (size_t)ik * nb, *fj = f + (size_t)jk * nb;
+    zc* a = Lij + (size_t)p * nb4;
+    zc* b = Lji + (size_t)p * nb4;
+    if (P3) {
+      const zc *a3 = P3 + (size_t)p * nb4, *a4 = P4 + (size_t)p * nb4;
+      for (int i1 = 0; i1 < nb; i1++)
+        for (int i2 = 0; i2 < nb; i2++) {
+          const int i12 = i1 * nb + i2, n12 = i12 * nb2;
+          for (int iab = 0; iab < nb2; iab++) {
+            const int i12ab = n12 + iab, iab12 = iab * nb2 + i12;
+            a[i12ab] = sub(a[i12ab], add(scl(1 - fi[i1], a3[i12ab]), scl(fi[i2], a4[i12ab])));
+            b[i12ab] = sub(b[i12ab], add(scl(1 - fj[i1], cj(a4[iab12])), scl(fj[i2], cj(a3[iab12]))));
+          }
+        }
+    }
+    const zc *a5 = P5 + (size_t)p * nb4, *a6 = P6 + (size_t)p * nb4;
+    for (int i1 = 0; i1 < nb; i1++)
+      for (int i2 = 0; i2 < nb; i2++) {
+        const int n12 = (i1 * nb + i2) * nb2, i21 = i2 * nb + i1;
+        for (int ia = 0; ia < nb; ia++)
+          for (int ib = 0; ib < nb; ib++) {
+            const int i12ab = n12 + ia * nb + ib, iba21 = (ib * nb + ia) * nb2 + i21;
+            a[i12ab] = sub(a[i12ab], add(scl(1 - fi[i1], a5[i12ab]), scl(fi[i2], a6[i12ab])));
+            b[i12ab] = sub(b[i12ab], add(scl(1 - fj[i1], a5[iba21]), scl(fj[i2], a6[iba21])));
+          }
+      }
+  }
+}
+
+// The e-e source of the linear operators, computed on the GPU: a temporary FP64 handle on the e-ph
+// operators with the e-e model attached (the set-up screening and static RPA table), then P_ee and
+// P3..P6 at the f_eq window (dmd_ee_linear_terms) with the screening density that
+// coulomb_model::init(f_eq) gives when the model updates it (Coulomb_Model.h:532-544), the set-up one
+// otherwise. T6: six complex [nkpair][nb^4] sets (P1ee, P2ee, P3, P4, P5, P6), scale_ee not applied.
+static int ee_linear_terms(dmdh_system* s, const std::vector<double>& fw, std::vector<double>& T6) {
+  dmd_desc d;
+  dmdh_desc(s, DMD_PREC_F64, 0, &d);
+  d.flags = DMD_FLAG_EE;
+  d.Hcoh = nullptr;
+  const dmdh_info& in = s->info;
+  const int nb = in.bend - in.bstart;
+  double nfree = s->eed.nfree;
+  if (s->eed.update_screening) {
+    double n = 0;
+    for (int ik = 0; ik < in.nk; ik++)
+      for (int b = 0; b < nb; b++) n += b < s->eed.nv ? (1 - fw[(size_t)ik * nb + b]) : fw[(size_t)ik * nb + b];
+    nfree = n / (s->eed.nk_full * s->eed.cell_size);
+  }
+  dmd_handle* h = nullptr;
+  int rc = dmd_create(&d, &h);
+  if (rc) return err(rc, "the e-e source of the linear operators needs a GPU handle: dmd_create failed");
+  const size_t n = (size_t)in.nkpair * nb * nb * nb * nb * 2;  // doubles per set
+  if (!(rc = dmd_ee_attach(h, &s->eed)))
+    rc = dmd_ee_linear_terms(h, fw.data(), nfree, T6.data(), T6.data() + n, T6.data() + 2 * n, T6.data() + 3 * n,
+                             T6.data() + 4 * n, T6.data() + 5 * n);
+  if (rc) {
+    const std::string m = dmd_last_error(h);
+    dmd_destroy(h);
+    return err(rc, "the e-e source of the linear operators: " + m);
+  }
+  dmd_destroy(h);
+  return DMD_OK;
 }
 
 int dmdh_load(const char* dir_c, dmdh_system** out) {
@@ -378,7 +455,6 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
     if (f != "unscreened" && f != "debye" && f != "Bechstedt" && f != "RPA")
       return err(DMD_E_ARG, "scrFormula " + f + " is not supported (unscreened, debye, Bechstedt, RPA are)");
     if (sget(pm, "dynamic_screening", "static") != "static") return err(DMD_E_ARG, "only static screening is supported");
-    if (linear) return err(DMD_E_ARG, "the e-e model is not supported with alg_linearize");
     if (pget(pm, "alg_ddmdteq", 0) != 0) return err(DMD_E_ARG, "the e-e model is not supported with alg_ddmdteq");
     if (pget(pm, "alg_summode", 1) == 0) return err(DMD_E_ARG, "the e-e model needs alg_summode");
     const double fe = pget(pm, "freq_update_ee_model", 0), fi = pget(pm, "freq_update_eimp_model", 0);
@@ -650,34 +726,6 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
       for (int i = 0; i < nb_dm; i++)
         s->f_eq[(size_t)ik * nb_dm + i] = fermi(T, i < nvd ? in.muh : in.mue, s->e_dm[(size_t)ik * nb_dm + i]);
   }
-  if (linear) {
-    // electronphonon::set_Lsc (ElectronPhonon_linear.cpp:3-31): the e-ph operators, each impurity's,
-    // then Lscii onto the diagonal pairs; the linear operators replace P1, P2
-    std::vector<double> fw((size_t)nk * nbw);
-    for (int ik = 0; ik < nk; ik++)
-      for (int b = 0; b < nbw; b++) fw[(size_t)ik * nbw + b] = s->f_eq[(size_t)ik * nb_dm + bs + b];
-    const size_t nb4 = (size_t)nbw * nbw * nbw * nbw;
-    std::vector<double> Lii(2 * (size_t)nk * nb4, 0.0), Lij(2 * np4, 0.0), Lji(2 * np4, 0.0);
-    lsc_add(nbw, nkpair, s->k1.data(), s->k2.data(), (const zc*)s->P1.data(), (const zc*)s->P2.data(), fw.data(),
-            (zc*)Lii.data(), (zc*)Lij.data(), (zc*)Lji.data());
-    for (auto& a : s->imp)
-      lsc_add(nbw, nkpair, s->k1.data(), s->k2.data(), (const zc*)a.first.data(), (const zc*)a.second.data(), fw.data(),
-              (zc*)Lii.data(), (zc*)Lij.data(), (zc*)Lji.data());
-    for (int p = 0; p < nkpair; p++) {
-      if (s->k1[p] != s->k2[p]) continue;
-      const zc* x = (const zc*)Lii.data() + s->k1[p] * nb4;
-      zc* a = (zc*)Lij.data() + (size_t)p * nb4;
-      zc* b = (zc*)Lji.data() + (size_t)p * nb4;
-      for (size_t e = 0; e < nb4; e++) {  // axbyc(L, Lscii, n, c1, c1): L += Lscii + 0
-        const zc t = {x[e].x + 0.0, x[e].y + 0.0};
-        a[e] = {a[e].x + t.x, a[e].y + t.y};
-        b[e] = {b[e].x + t.x, b[e].y + t.y};
-      }
-    }
-    s->P1.swap(Lij);
-    s->P2.swap(Lji);
-    s->imp.clear();
-  }
   if (s->ee) {
     // elecelec_model / coulomb_model inputs (ElecElec_Model.h:22-37, Coulomb_Model.h:415-424): the
     // k-points and U (electron.cpp:134-146, 388-410; U's partial layout [nk][nb_wannier][nb_eph] is
@@ -748,6 +796,54 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
     ee.scale = pget(pm, "scale_ee", scale_scatt);
     ee.every_rhs = s->ee == 1 && pget(pm, "freq_update_ee_model", 0) < 0;
   }
+  if (linear) {
+    // electronphonon::set_Lsc (ElectronPhonon_linear.cpp:3-31): the e-ph operators, each impurity's,
+    // then Lscii onto the diagonal pairs; the linear operators replace P1, P2
+    std::vector<double> fw((size_t)nk * nbw);
+    for (int ik = 0; ik < nk; ik++)
+      for (int b = 0; b < nbw; b++) fw[(size_t)ik * nbw + b] = s->f_eq[(size_t)ik * nb_dm + bs + b];
+    const size_t nb4 = (size_t)nbw * nbw * nbw * nbw;
+    std::vector<double> Lii(2 * (size_t)nk * nb4, 0.0), Lij(2 * np4, 0.0), Lji(2 * np4, 0.0);
+    lsc_add(nbw, nkpair, s->k1.data(), s->k2.data(), (const zc*)s->P1.data(), (const zc*)s->P2.data(), fw.data(),
+            (zc*)Lii.data(), (zc*)Lij.data(), (zc*)Lji.data());
+    for (auto& a : s->imp)
+      lsc_add(nbw, nkpair, s->k1.data(), s->k2.data(), (const zc*)a.first.data(), (const zc*)a.second.data(), fw.data(),
+              (zc*)Lii.data(), (zc*)Lij.data(), (zc*)Lji.data());
+    if (s->ee) {  // add_Lsc_contrib("ee") (ElectronPhonon_linear.cpp:17-22, 44-100), computed on the GPU
+      std::vector<double> T6((size_t)6 * np4 * 2, 0.0);
+      int rc = ee_linear_terms(s.get(), fw, T6);
+      if (rc) return rc;
+      const double sc = s->eed.scale;
+      if (sc != 1.)
+        for (size_t i = 0; i < T6.size(); i += 2) {  // complex(scale_ee, 0) * P
+          const double x = T6[i], y = T6[i + 1];
+          T6[i] = sc * x - 0 * y;
+          T6[i + 1] = sc * y + 0 * x;
+        }
+      const zc* T = (const zc*)T6.data();
+      const size_t n4 = np4;  // complex elements per operator set
+      const bool anti = s->eed.antisymmetry != 0, fixed = s->ee == 2;
+      lsc_add(nbw, nkpair, s->k1.data(), s->k2.data(), T, T + n4, fw.data(), (zc*)Lii.data(), (zc*)Lij.data(),
+              (zc*)Lji.data(), anti);
+      if (!fixed)
+        lsc_add_p36(nbw, nkpair, s->k1.data(), s->k2.data(), anti ? nullptr : T + 2 * n4, T + 3 * n4, T + 4 * n4,
+                    T + 5 * n4, fw.data(), (zc*)Lij.data(), (zc*)Lji.data());
+    }
+    for (int p = 0; p < nkpair; p++) {
+      if (s->k1[p] != s->k2[p]) continue;
+      const zc* x = (const zc*)Lii.data() + s->k1[p] * nb4;
+      zc* a = (zc*)Lij.data() + (size_t)p * nb4;
+      zc* b = (zc*)Lji.data() + (size_t)p * nb4;
+      for (size_t e = 0; e < nb4; e++) {  // axbyc(L, Lscii, n, c1, c1): L += Lscii + 0
+        const zc t = {x[e].x + 0.0, x[e].y + 0.0};
+        a[e] = {a[e].x + t.x, a[e].y + t.y};
+        b[e] = {b[e].x + t.x, b[e].y + t.y};
+      }
+    }
+    s->P1.swap(Lij);
+    s->P2.swap(Lji);
+    s->imp.clear();
+  }
   // coherent Hamiltonian (main.cpp:51)
   const double Blen = sqrt(in.B[0] * in.B[0] + in.B[1] * in.B[1] + in.B[2] * in.B[2]);
   if (Blen > 1e-10) {
@@ -786,7 +882,9 @@ int dmdh_desc(const dmdh_system* s, int32_t precision, int32_t device, dmd_desc*
   d->expt = s->info.expt;
   d->precision = precision;
   d->device = device;
-  d->flags = (s->info.linear ? DMD_FLAG_LINEAR : 0u) | (s->ee ? DMD_FLAG_EE : 0u) | (s->sparse ? DMD_FLAG_SPARSE : 0u);
+  // (linearized: the e-e term is part of the linear operators, no model on the handle)
+  d->flags = (s->info.linear ? DMD_FLAG_LINEAR : 0u) | (s->ee && !s->info.linear ? DMD_FLAG_EE : 0u) |
+             (s->sparse ? DMD_FLAG_SPARSE : 0u);
   d->f_ref = s->f_eq.empty() ? s->f_dm.data() : s->f_eq.data();
   return DMD_OK;
 }
@@ -817,7 +915,7 @@ int dmdh_ee_desc(const dmdh_system* s, dmd_ee_desc* ee, int32_t* on) {
 
 int dmdh_prepare(const dmdh_system* s, dmd_handle* h) {
   if (!s || !h) return DMD_E_ARG;
-  if (s->ee) {  // electronphonon::set_eph's e-e term (ElectronPhonon.cpp:12)
+  if (s->ee && !s->info.linear) {  // electronphonon::set_eph's e-e term (ElectronPhonon.cpp:12)
     const int rc = dmd_ee_attach(h, &s->eed);
     if (rc) return err(rc, dmd_last_error(h));
   }

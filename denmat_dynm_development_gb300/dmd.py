@@ -71,7 +71,7 @@ EXPORTS = ["dmd_create", "dmd_destroy", "dmd_last_error", "dmd_strerror", "dmd_s
            "dmd_pinned_alloc", "dmd_pinned_free", "dmd_timer", "dmd_set_profiling", "dmd_profile_get",
            "dmd_evolve_driver_noalloc", "dmd_measure_batch", "dmd_pair_bytes", "dmd_adjoint_rk4", "dmd_autotune",
            "dmd_group_create", "dmd_group_rk4", "dmd_group_destroy",
-           "dmd_create_from_files", "dmd_create_from_sparse_files", "dmd_selftest_wait_timeout", "dmd_peak_fma", "dmd_add_operators",
+           "dmd_create_from_files", "dmd_create_from_sparse_files", "dmd_selftest_wait_timeout", "dmd_peak_fma", "dmd_add_operators", "dmd_ee_linear_terms",
            "dmd_ee_attach", "dmd_ee_update", "dmd_ee_read"]
 
 
@@ -110,6 +110,7 @@ def _lib():
         L.dmd_selftest_wait_timeout.argtypes = [C.c_int, C.c_uint32, C.POINTER(C.c_int)]
         L.dmd_peak_fma.argtypes = [C.c_int, C.c_int, C.POINTER(d)]
         L.dmd_add_operators.argtypes = [vp, vp, vp, d]
+        L.dmd_ee_linear_terms.argtypes = [vp, vp, d, vp, vp, vp, vp, vp, vp]
         L.dmd_create_from_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
                                             C.POINTER(vp)]
         L.dmd_create_from_sparse_files.argtypes = [C.POINTER(_Desc), C.c_char_p, C.c_char_p, C.c_char_p,
@@ -211,6 +212,15 @@ class LindbladGPU:
     def ee_update(self):
         """Rebuild P_ee from the handle's state at its time (dmd_ee_update)."""
         self._ck(_lib().dmd_ee_update(self._h))
+
+    def ee_linear_terms(self, f_eq, nfree):
+        """P_ee at f_eq and P3..P6 of every pair (the e-e source of the linearized operators):
+        complex [6][npair][nb^4], prefactor included, scale_ee not"""
+        f = np.ascontiguousarray(f_eq, np.float64)
+        out = np.zeros((6, self.npair, self.nb4), np.complex128)
+        p = [out[i].ctypes.data for i in range(6)]
+        self._ck(_lib().dmd_ee_linear_terms(self._h, f.ctypes.data, float(nfree), *p))
+        return out
 
     def ee_read(self):
         """(P1ee, P2ee complex [npair][nb^4], screening density) of the last rebuild."""

@@ -128,13 +128,16 @@ class System:
 
     def gpu(self, precision="f64", device=0):
         """A LindbladGPU built from this system (dmd_create on the loaded arrays), with the e-e model
-        attached and the equilibrium drift installed when param.in asks for them (dmdh_prepare)."""
+        attached and the equilibrium drift installed when param.in asks for them (dmdh_prepare); with
+        alg_linearize the e-e term is already inside the linear operators, with alg_sparseP the handle
+        contracts the stored elements only."""
         i = self.info
         g = _dmd.LindbladGPU(nk=i.nk, nb_dm=i.nb_dm, bstart=i.bstart, bend=i.bend, e_dm=self.e_dm,
                              k1st=self.k1st, k2nd=self.k2nd, P1=self.P1, P2=self.P2, prefac_eph=i.prefac_eph,
                              Hcoh=self.Hcoh, picture=i.picture, expt=i.expt, precision=precision, device=device,
                              f_ref=self.f_eq if self.f_eq is not None else self.f_dm, linear=bool(i.linear),
-                             ee_flag=self.ee is not None)
+                             ee_flag=self.ee is not None and not i.linear,
+                             sparse=bool(self.param("alg_sparseP") or 0))
         try:
             _ck(_lib().dmdh_prepare(self._h, g._h))
         except Exception:

@@ -258,6 +258,16 @@ typedef struct dmd_ee_desc {
 int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee);
 /* Update from the handle's state at its time (set_state / after stepping). */
 int dmd_ee_update(dmd_handle* h);
+/* The e-e source of the linearized operators (electronphonon::set_Lsc's add_Lsc_contrib("ee"),
+ * ElectronPhonon_linear.cpp:17-22, 44-100): for every stored pair, P_ee at the occupations f_eq
+ * ([nk][nb] window; elecelec_model::calc_P with f = f_eq, ElecElec_Model.h:186-262) and the terms of
+ * calc_P3P4 and calc_P5P6 (ElecElec_Model_linear.cpp:3-112; P3, P4 zero with the exchange term), with
+ * the screening of density nfree (the set-up density, or coulomb_model::init(f_eq)'s when the model
+ * updates it) and the attached model's static RPA table. Outputs complex128 [npair][nb^4] each
+ * (prefactor included, scale_ee not; any may be NULL). Needs an attached e-e model; the handle's
+ * own operators and screening are left as they were. */
+int dmd_ee_linear_terms(dmd_handle* h, const double* f_eq, double nfree, double* P1ee, double* P2ee, double* P3,
+                        double* P4, double* P5, double* P6);
 /* The last P_ee (complex128 [npair][nb^4] each, prefactor included, scale not; either may be NULL)
  * and the screening density it used (may be NULL). */
 int dmd_ee_read(dmd_handle* h, double* P1ee, double* P2ee, double* nfree);

@@ -340,9 +340,16 @@ static void orc_evolve_linear(const orc_sys* s, const double* e, double t, zc* d
 }
 
 /* Linear operators from one source of P (ElectronPhonon_linear.cpp:147-225): for every pair,
- * add_Lscii_from_P1_P2 then add_Lscij_from_P1_P2 (fac2 = false). f is the window f_eq [nk][nb]. */
+ * add_Lscii_from_P1_P2 then add_Lscij_from_P1_P2 (fac2 = false; the e-e source with the exchange
+ * term passes fac2 = true, ElectronPhonon_linear.cpp:84). f is the window f_eq [nk][nb]. */
+void orc_lsc_add2(int nk, int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, const zc* P1, const zc* P2,
+                  const double* f, zc* Lscii, zc* Lij, zc* Lji, int fac2);
 void orc_lsc_add(int nk, int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, const zc* P1, const zc* P2,
                  const double* f, zc* Lscii, zc* Lij, zc* Lji) {
+  orc_lsc_add2(nk, nb, npair, k1, k2, P1, P2, f, Lscii, Lij, Lji, 0);
+}
+void orc_lsc_add2(int nk, int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, const zc* P1, const zc* P2,
+                  const double* f, zc* Lscii, zc* Lij, zc* Lji, int fac2) {
   const int nb2 = nb * nb, nb4 = nb2 * nb2;
   (void)nk;
   for (int64_t p = 0; p < npair; p++) {
@@ -380,9 +387,9 @@ void orc_lsc_add(int nk, int nb, int64_t npair, const uint64_t* k1, const uint64
           for (int ib = 0; ib < nb; ib++) {
             const int iab = ia * nb + ib, i12ab = n12 + iab, iab12 = iab * nb2 + i12;
             zc c = zadd(zscale(1 - f[(size_t)ik * nb + i1], P1p[i12ab]), zscale(f[(size_t)ik * nb + i2], P2p[iab12]));
-            Lijp[i12ab] = zadd(Lijp[i12ab], c);
+            Lijp[i12ab] = zadd(Lijp[i12ab], fac2 ? zscale(2, c) : c);
             c = zadd(zscale(1 - f[(size_t)jk * nb + i1], zconj(P2p[i12ab])), zscale(f[(size_t)jk * nb + i2], zconj(P1p[iab12])));
-            Ljip[i12ab] = zadd(Ljip[i12ab], c);
+            Ljip[i12ab] = zadd(Ljip[i12ab], fac2 ? zscale(2, c) : c);
           }
       }
   }
@@ -744,6 +751,215 @@ void orc_ee_P(const orc_ee* ee, const orc_sys* s, const zc* dm, const zc* dm1, c
   }
   free(e); free(table); free(Uih); free(o12); free(o34); free(o14); free(o32); free(mee); free(mex); free(A);
   free(A1rho); free(A1rhobar); free(mtmp); free(P1); free(P2); free(delta);
+}
+
+/* elecelec_model::calc_A (ElecElec_Model.h:144-162) on k-points (q1, q2, q3, q4) with calc_ovlp12:
+ * calc_delta over e[q1][i1] - e[q2][i2] + e[q3][i3] - e[q4][i4] (:164-184), calc_ovlps (:64-71),
+ * calc_mee and, with the exchange term, calc_mee_ex and mee = (mee - mee_ex)/2 (:81-138). Lindblad:
+ * A1 = A2 = delta mee. Returns 0 when no band combination conserves energy. */
+static int ee_calc_A(const orc_ee* ee, const ee_scr* c, const double* e, int q1, int q2, int q3, int q4, zc* Uih,
+                     zc* o12, zc* o34, zc* o14, zc* o32, double* delta, zc* mee, zc* mex, zc* A) {
+  const int nb = ee->nb, nb4 = nb * nb * nb * nb;
+  const double prefac_exp = -0.25 / pow(ee->degauss, 2);
+  int conserved = 0;
+  for (int i1 = 0; i1 < nb; i1++)
+    for (int i2 = 0; i2 < nb; i2++)
+      for (int i3 = 0; i3 < nb; i3++)
+        for (int i4 = 0; i4 < nb; i4++) {
+          const int i1234 = ((i1 * nb + i2) * nb + i3) * nb + i4;
+          const double de = e[q1 * nb + i1] - e[q2 * nb + i2] + e[q3 * nb + i3] - e[q4 * nb + i4];
+          if (fabs(de) < ee->ethr) {
+            delta[i1234] = exp(prefac_exp * pow(de, 2));
+            conserved = 1;
+          } else {
+            delta[i1234] = 0;
+          }
+        }
+  if (!conserved) return 0;
+  ee_ovlp(ee, c, o12, Uih, q1, q2, 1);
+  ee_ovlp(ee, c, o34, Uih, q3, q4, 0);
+  if (ee->antisym) {
+    ee_ovlp(ee, c, o14, Uih, q1, q4, 1);
+    ee_ovlp(ee, c, o32, Uih, q3, q2, 0);
+  }
+  for (int i1 = 0; i1 < nb; i1++)
+    for (int i2 = 0; i2 < nb; i2++)
+      for (int i3 = 0; i3 < nb; i3++)
+        for (int i4 = 0; i4 < nb; i4++) {
+          const int i1234 = ((i1 * nb + i2) * nb + i3) * nb + i4;
+          mee[i1234] = zmul(o12[i1 * nb + i2], o34[i3 * nb + i4]);
+          if (ee->antisym) mex[i1234] = zmul(o14[i1 * nb + i4], o32[i3 * nb + i2]);
+        }
+  if (ee->antisym)
+    for (int i = 0; i < nb4; i++) mee[i] = zadd(zmul(zmk(-0.5, 0), mex[i]), zmul(zmk(0.5, 0), mee[i]));
+  for (int i = 0; i < nb4; i++) A[i] = zscale(delta[i], mee[i]);
+  return 1;
+}
+
+/* elecelec_model::calc_P3P4 and calc_P5P6 (ElecElec_Model_linear.cpp:3-112) for every stored pair
+ * (k1, ka) at the occupations f (window [nk][nb]: the f_eq of the linearization) with screening
+ * density nfree. P3, P4 are left zero with the exchange term (the reference skips them then). */
+void orc_ee_P3P6(const orc_ee* ee, const orc_sys* s, const double* f, double nfree, zc* P3out, zc* P4out, zc* P5out,
+                 zc* P6out) {
+  const int nk = s->nk, nb = ee->nb, nb2 = nb * nb, nb4 = nb2 * nb2, nd = s->nb_dm, bs = s->bstart;
+  const ee_scr c = ee_screen(ee, nfree);
+  double* e = (double*)xmalloc(sizeof(double) * nk * nb);
+  for (int ik = 0; ik < nk; ik++)
+    for (int b = 0; b < nb; b++) e[ik * nb + b] = s->e_dm[(size_t)ik * nd + bs + b];
+  const size_t nmesh = (size_t)ee->kmesh[0] * ee->kmesh[1] * ee->kmesh[2];
+  int* table = (int*)xmalloc(sizeof(int) * nmesh);
+  for (size_t i = 0; i < nmesh; i++) table[i] = -1;
+  for (int ik = 0; ik < nk; ik++) {
+    int v[3];
+    ee_ikvec3(ee, ee->kvec + 3 * ik, v);
+    int* slot = &table[((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2]];
+    if (*slot < 0) *slot = ik;
+  }
+  zc *Uih = (zc*)xmalloc(sizeof(zc) * nb * ee->nbw), *o12 = (zc*)xmalloc(sizeof(zc) * nb2),
+     *o34 = (zc*)xmalloc(sizeof(zc) * nb2), *o14 = (zc*)xmalloc(sizeof(zc) * nb2), *o32 = (zc*)xmalloc(sizeof(zc) * nb2),
+     *mee = (zc*)xmalloc(sizeof(zc) * nb4), *mex = (zc*)xmalloc(sizeof(zc) * nb4), *A = (zc*)xmalloc(sizeof(zc) * nb4),
+     *A1rho = (zc*)xmalloc(sizeof(zc) * nb2), *A1rhobar = (zc*)xmalloc(sizeof(zc) * nb2);
+  double* delta = (double*)xmalloc(sizeof(double) * nb4);
+  const double prefac_gauss = 1. / (ee->degauss * sqrt(2. * M_PI));
+  zc prefac = zmk(prefac_gauss / ee->nk_full, 0);
+  if (ee->antisym) prefac = zmk(prefac.x * 2, prefac.y * 2);
+  for (int64_t ip = 0; ip < s->npair; ip++) {
+    const int ik1 = (int)s->k1st[ip], ika = (int)s->k2nd[ip];
+    zc* P3 = P3out + (size_t)ip * nb4;
+    zc* P4 = P4out + (size_t)ip * nb4;
+    zc* P5 = P5out + (size_t)ip * nb4;
+    zc* P6 = P6out + (size_t)ip * nb4;
+    memset(P3, 0, sizeof(zc) * nb4);
+    memset(P4, 0, sizeof(zc) * nb4);
+    memset(P5, 0, sizeof(zc) * nb4);
+    memset(P6, 0, sizeof(zc) * nb4);
+    if (!ee->antisym) {
+      /* calc_P3P4: k4 = k1 + k3 - ka, A(k1, k4, k3, ka) */
+      for (int ik3 = 0; ik3 < nk; ik3++) {
+        if (ika == ik3 && !ee->antisym) continue;
+        if (ee->antisym && ika == ik3 && ik1 == ika) continue;
+        double k4v[3];
+        for (int d = 0; d < 3; d++) k4v[d] = ee->kvec[3 * ik1 + d] + ee->kvec[3 * ik3 + d] - ee->kvec[3 * ika + d];
+        const int ik4 = ee_findk(ee, table, k4v);
+        if (ik4 < 0) continue;
+        if (!ee_calc_A(ee, &c, e, ik1, ik4, ik3, ika, Uih, o12, o34, o14, o32, delta, mee, mex, A)) continue;
+        const double *f3 = f + (size_t)ik3 * nb, *f4 = f + (size_t)ik4 * nb;
+        for (int i1 = 0; i1 < nb; i1++)
+          for (int ia = 0; ia < nb; ia++) {
+            for (int i4 = 0; i4 < nb; i4++) {
+              const int n14 = (i1 * nb + i4) * nb2;
+              for (int i3 = 0; i3 < nb; i3++) {
+                const int i43 = i4 * nb + i3, i143a = n14 + i3 * nb + ia;
+                A1rho[i43] = zscale(f4[i4], zscale(1 - f3[i3], A[i143a]));
+                A1rhobar[i43] = zscale(1 - f4[i4], zscale(f3[i3], A[i143a]));
+              }
+            }
+            for (int i2 = 0; i2 < nb; i2++) {
+              const int n12 = (i1 * nb + i2) * nb2;
+              for (int ib = 0; ib < nb; ib++) {
+                const int i12ab = n12 + ia * nb + ib;
+                for (int i4 = 0; i4 < nb; i4++) {
+                  const int n24 = (i2 * nb + i4) * nb2;
+                  for (int i3 = 0; i3 < nb; i3++) {
+                    const int i43 = i4 * nb + i3, i243b = n24 + i3 * nb + ib;
+                    P3[i12ab] = zadd(P3[i12ab], zmul(A1rho[i43], zconj(A[i243b])));
+                    P4[i12ab] = zadd(P4[i12ab], zmul(A1rhobar[i43], zconj(A[i243b])));
+                  }
+                }
+              }
+            }
+          }
+      }
+      for (int i = 0; i < nb4; i++) {
+        P3[i] = zmul(prefac, P3[i]);
+        P4[i] = zmul(prefac, P4[i]);
+      }
+    }
+    /* calc_P5P6: k4 = k1 + ka - k3, A(k1, k3, ka, k4) */
+    for (int ik3 = 0; ik3 < nk; ik3++) {
+      if (ik1 == ik3 && !ee->antisym) continue;
+      if (ee->antisym && ik1 == ik3 && ika == ik3) continue;
+      double k4v[3];
+      for (int d = 0; d < 3; d++) k4v[d] = ee->kvec[3 * ik1 + d] + ee->kvec[3 * ika + d] - ee->kvec[3 * ik3 + d];
+      const int ik4 = ee_findk(ee, table, k4v);
+      if (ik4 < 0) continue;
+      if (!ee_calc_A(ee, &c, e, ik1, ik3, ika, ik4, Uih, o12, o34, o14, o32, delta, mee, mex, A)) continue;
+      const double *f3 = f + (size_t)ik3 * nb, *f4 = f + (size_t)ik4 * nb;
+      for (int i1 = 0; i1 < nb; i1++)
+        for (int ib = 0; ib < nb; ib++) {
+          for (int i3 = 0; i3 < nb; i3++) {
+            const int n13 = (i1 * nb + i3) * nb2;
+            for (int i4 = 0; i4 < nb; i4++) {
+              const int i34 = i3 * nb + i4, i13b4 = n13 + ib * nb + i4;
+              A1rho[i34] = zscale(f4[i4], zscale(f3[i3], A[i13b4]));
+              A1rhobar[i34] = zscale(1 - f4[i4], zscale(1 - f3[i3], A[i13b4]));
+            }
+          }
+          for (int i2 = 0; i2 < nb; i2++) {
+            const int n12 = (i1 * nb + i2) * nb2;
+            for (int ia = 0; ia < nb; ia++) {
+              const int i12ab = n12 + ia * nb + ib;
+              for (int i3 = 0; i3 < nb; i3++) {
+                const int n23 = (i2 * nb + i3) * nb2;
+                for (int i4 = 0; i4 < nb; i4++) {
+                  const int i34 = i3 * nb + i4, i23a4 = n23 + ia * nb + i4;
+                  P5[i12ab] = zadd(P5[i12ab], zmul(A1rho[i34], zconj(A[i23a4])));
+                  P6[i12ab] = zadd(P6[i12ab], zmul(A1rhobar[i34], zconj(A[i23a4])));
+                }
+              }
+            }
+          }
+        }
+    }
+    for (int i = 0; i < nb4; i++) {
+      P5[i] = zmul(prefac, P5[i]);
+      P6[i] = zmul(prefac, P6[i]);
+    }
+  }
+  free(e); free(table); free(Uih); free(o12); free(o34); free(o14); free(o32); free(mee); free(mex); free(A);
+  free(A1rho); free(A1rhobar); free(delta);
+}
+
+/* electronphonon::add_Lscij_from_P3_P4 (ElectronPhonon_linear.cpp:199-221) for every pair */
+void orc_lsc_add_p3p4(int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, const zc* P3, const zc* P4,
+                      const double* f, zc* Lij, zc* Lji) {
+  const int nb2 = nb * nb, nb4 = nb2 * nb2;
+  for (int64_t p = 0; p < npair; p++) {
+    const int ik = (int)k1[p], jk = (int)k2[p];
+    const zc *a3 = P3 + (size_t)p * nb4, *a4 = P4 + (size_t)p * nb4;
+    zc *x = Lij + (size_t)p * nb4, *y = Lji + (size_t)p * nb4;
+    for (int i1 = 0; i1 < nb; i1++)
+      for (int i2 = 0; i2 < nb; i2++) {
+        const int i12 = i1 * nb + i2, n12 = i12 * nb2;
+        for (int iab = 0; iab < nb2; iab++) {
+          const int i12ab = n12 + iab, iab12 = iab * nb2 + i12;
+          x[i12ab] = zsub(x[i12ab], zadd(zscale(1 - f[(size_t)ik * nb + i1], a3[i12ab]), zscale(f[(size_t)ik * nb + i2], a4[i12ab])));
+          y[i12ab] = zsub(y[i12ab], zadd(zscale(1 - f[(size_t)jk * nb + i1], zconj(a4[iab12])),
+                                         zscale(f[(size_t)jk * nb + i2], zconj(a3[iab12]))));
+        }
+      }
+  }
+}
+
+/* electronphonon::add_Lscij_from_P5_P6 (ElectronPhonon_linear.cpp:223-245) for every pair */
+void orc_lsc_add_p5p6(int nb, int64_t npair, const uint64_t* k1, const uint64_t* k2, const zc* P5, const zc* P6,
+                      const double* f, zc* Lij, zc* Lji) {
+  const int nb2 = nb * nb, nb4 = nb2 * nb2;
+  for (int64_t p = 0; p < npair; p++) {
+    const int ik = (int)k1[p], jk = (int)k2[p];
+    const zc *a5 = P5 + (size_t)p * nb4, *a6 = P6 + (size_t)p * nb4;
+    zc *x = Lij + (size_t)p * nb4, *y = Lji + (size_t)p * nb4;
+    for (int i1 = 0; i1 < nb; i1++)
+      for (int i2 = 0; i2 < nb; i2++) {
+        const int n12 = (i1 * nb + i2) * nb2, i21 = i2 * nb + i1;
+        for (int ia = 0; ia < nb; ia++)
+          for (int ib = 0; ib < nb; ib++) {
+            const int i12ab = n12 + ia * nb + ib, iba21 = (ib * nb + ia) * nb2 + i21;
+            x[i12ab] = zsub(x[i12ab], zadd(zscale(1 - f[(size_t)ik * nb + i1], a5[i12ab]), zscale(f[(size_t)ik * nb + i2], a6[i12ab])));
+            y[i12ab] = zsub(y[i12ab], zadd(zscale(1 - f[(size_t)jk * nb + i1], a5[iba21]), zscale(f[(size_t)jk * nb + i2], a6[iba21])));
+          }
+      }
+  }
 }
 
 /* electronphonon::reset_scatt (ElectronPhonon.cpp:15-42) for the e-e update on state y (the

@@ -101,6 +101,16 @@ def lib():
         _lib.orc_lsc_add.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_lsc_add.restype = None
+        _lib.orc_lsc_add2.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        _lib.orc_lsc_add2.restype = None
+        _lib.orc_ee_P3P6.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p]
+        _lib.orc_ee_P3P6.restype = None
+        for n in ("orc_lsc_add_p3p4", "orc_lsc_add_p5p6"):
+            getattr(_lib, n).argtypes = [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]
+            getattr(_lib, n).restype = None
         _lib.orc_lsc_diag.argtypes = [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.orc_lsc_diag.restype = None
     return _lib
@@ -364,6 +374,7 @@ class OracleSystem:
     f_lin: Optional[np.ndarray] = None       # [nk][nb] window f_eq of the linearization
     ee: Optional[EEModel] = None             # eeMode = Pee_update: P1, P2 are ee.P1eff, ee.P2eff
     sparse: bool = False                     # alg.sparseP: P contracted as sparse_mat (sparse_zgemm)
+    lin_ee: Optional[tuple] = None           # linearized e-e source: P1ee, P2ee, P3..P6 (times scale_ee)
     thr_sparse: float = 1e-40                # alg.thr_sparseP
 
     def cstruct(self):
@@ -378,6 +389,62 @@ class OracleSystem:
     @property
     def ny(self):
         return 2 * self.nk * self.nb_dm * self.nb_dm
+
+
+def _ee_model_of(pm, sz, dd, R, nk, nb, nb_dm, bstart, bend, e_dm, f_dm, nv_dm, T, cell_size, nfree, P1, P2):
+    """The e-e model's inputs as elecelec_model / coulomb_model read them (ElecElec_Model.h:22-37,
+    Coulomb_Model.h:394-450): U, k-points, reciprocal metric, screening parameters."""
+    if pm.get("dynamic_screening", "static") != "static":
+        raise ValueError("the oracle restates static screening only")
+    nbw = sz["nb_wannier"]
+    nb_eph = sz["bEnd_eph"] - sz["bStart_eph"]
+    U = np.fromfile(os.path.join(dd, "ldbd_Umat.bin"), dtype=np.complex128).reshape(nk, nbw, nb_eph)
+    kvec = np.fromfile(os.path.join(dd, "ldbd_kvec.bin"), dtype=np.float64).reshape(nk, 3)
+    degauss, ndegauss = sz["degauss"], sz["ndegauss"]
+    degauss = pget(pm, "degauss", degauss / eV, eV)
+    ndegauss = pget(pm, "ndegauss", ndegauss)
+    scale_scatt = pget(pm, "scale_scatt", 1.0)
+    return EEModel(nb=nb, kvec=kvec, kmesh=sz["kmesh"], U=U, GGT=ggt_of(R), cell_size=cell_size,
+                   nk_full=sz["nk_full"], T=T, eps=pget(pm, "epsilon_background", 1.0),
+                   meff=pget(pm, "meff_screening", 1.0), formula=pm.get("scrFormula", "RPA"), nfree=nfree,
+                   update_screening=int(pget(pm, "update_screening", 1)), nv=nv_dm - bstart,
+                   degauss=pget(pm, "degauss_ee", degauss / eV, eV), ethr=degauss * ndegauss,
+                   antisym=int(pget(pm, "ee_antisymmetry", 0)), scale=pget(pm, "scale_ee", scale_scatt),
+                   inside=pget(pm, "freq_update_ee_model", 0) < 0, P1base=P1, P2base=P2,
+                   f_setup=f_dm[:, bstart:bend], e_window=e_dm[:, bstart:bend])
+
+
+def _ee_linear_terms(pm, sz, dd, R, nk, nb, nb_dm, bstart, bend, npair, k1, k2, e_dm, f_dm, f_lin, nv_dm, T,
+                     cell_size, nfree, smat, dm0, schrod, expt, t0, mu):
+    """The e-e source of the linear operators (electronphonon::set_Lsc, ElectronPhonon_linear.cpp:
+    17-22, 44-100): the screening density from f_eq when the model updates it (coulomb_model::init,
+    Coulomb_Model.h:532-544), P_ee at f_eq (calc_P with ee_model->f = f_eq) and, unless eeMode =
+    Pee_fixed_at_eq, P3..P6 (ElecElec_Model_linear.cpp), each times scale_ee."""
+    nb4 = nb ** 4
+    zero = np.zeros(npair * nb4, np.complex128)
+    ee = _ee_model_of(pm, sz, dd, R, nk, nb, nb_dm, bstart, bend, e_dm, f_dm, nv_dm, T, cell_size, nfree, zero, zero)
+    n = nfree
+    if ee.update_screening:
+        fw = f_lin
+        n = float(sum((1 - fw[ik, b]) if b < ee.nv else fw[ik, b] for ik in range(nk) for b in range(nb)))
+        n /= (sz["nk_full"] * cell_size)
+    tmp = OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm, k1st=k1,
+                       k2nd=k2, P1=zero, P2=zero, prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=None, smat=smat,
+                       dm0=dm0, picture_schrodinger=schrod, expt=expt, t0=t0, tstep=0.0, tend=0.0, temperature=T,
+                       mu=mu, nk_full=sz["nk_full"], ob_prefac=1.0, ode={}, params={})
+    cs = tmp.cstruct()
+    L = lib()
+    fl = np.ascontiguousarray(f_lin)
+    L.orc_ee_P(C.addressof(ee.c), C.addressof(cs), None, None, fl.ctypes.data, C.c_double(n), ee.P1ee.ctypes.data,
+               ee.P2ee.ctypes.data)
+    P = [np.zeros(npair * nb4, np.complex128) for _ in range(4)]
+    fixed = pm.get("eeMode", "none") == "Pee_fixed_at_eq"
+    if not fixed:
+        L.orc_ee_P3P6(C.addressof(ee.c), C.addressof(cs), fl.ctypes.data, C.c_double(n), *[x.ctypes.data for x in P])
+    out = [ee.P1ee.copy(), ee.P2ee.copy()] + P
+    if ee.scale != 1.0:
+        out = [x * complex(ee.scale, 0) for x in out]
+    return tuple(out) + (bool(ee.antisym), fixed)
 
 
 def load(d: str) -> OracleSystem:
@@ -480,6 +547,20 @@ def load(d: str) -> OracleSystem:
         for a, b in srcs:
             L.orc_lsc_add(nk, nb, npair, k1.ctypes.data, k2.ctypes.data, a.ctypes.data, b.ctypes.data, f_lin.ctypes.data,
                           Lii.ctypes.data, Lij.ctypes.data, Lji.ctypes.data)
+        lin_ee = None
+        if pm.get("eeMode", "none") != "none":  # add_Lsc_contrib("ee"), ElectronPhonon_linear.cpp:17-22, 44-100
+            lin_ee = _ee_linear_terms(pm, sz, dd, R, nk, nb, nb_dm, bstart, bend, npair, k1, k2, e_dm, f_dm, f_lin,
+                                      nv_dm, T, cell_size, nfree, smat, dm0, schrod, expt, t0, mu)
+            P1ee, P2ee, P3, P4, P5, P6, antisym, fixed = lin_ee
+            lin_ee = lin_ee[:6]
+            L.orc_lsc_add2(nk, nb, npair, k1.ctypes.data, k2.ctypes.data, P1ee.ctypes.data, P2ee.ctypes.data,
+                           f_lin.ctypes.data, Lii.ctypes.data, Lij.ctypes.data, Lji.ctypes.data, int(antisym))
+            if not fixed:
+                if not antisym:
+                    L.orc_lsc_add_p3p4(nb, npair, k1.ctypes.data, k2.ctypes.data, P3.ctypes.data, P4.ctypes.data,
+                                       f_lin.ctypes.data, Lij.ctypes.data, Lji.ctypes.data)
+                L.orc_lsc_add_p5p6(nb, npair, k1.ctypes.data, k2.ctypes.data, P5.ctypes.data, P6.ctypes.data,
+                                   f_lin.ctypes.data, Lij.ctypes.data, Lji.ctypes.data)
         L.orc_lsc_diag(nb, npair, k1.ctypes.data, k2.ctypes.data, Lii.ctypes.data, Lij.ctypes.data, Lji.ctypes.data)
         P1, P2 = Lij, Lji
     if int(pget(pm, "alg_ddmdteq", 0)):
@@ -493,27 +574,10 @@ def load(d: str) -> OracleSystem:
         L.orc_compute_ddmdt_eq(C.addressof(cs), f_eq.ctypes.data, ddmdt_eq.ctypes.data)
     ee = None
     ee_mode = pm.get("eeMode", "none")
-    if ee_mode != "none":
-        if ee_mode != "Pee_update" or linear or int(pget(pm, "alg_linearize_dPee", 0)):
+    if ee_mode != "none" and not linear:  # (with alg_linearize the e-e term is part of the operators)
+        if ee_mode != "Pee_update" or int(pget(pm, "alg_linearize_dPee", 0)):
             raise ValueError("the oracle restates eeMode = Pee_update without linearization")
-        if pm.get("dynamic_screening", "static") != "static":
-            raise ValueError("the oracle restates static screening only")
-        nbw = sz["nb_wannier"]
-        nb_eph = sz["bEnd_eph"] - sz["bStart_eph"]
-        U = np.fromfile(os.path.join(dd, "ldbd_Umat.bin"), dtype=np.complex128).reshape(nk, nbw, nb_eph)
-        kvec = np.fromfile(os.path.join(dd, "ldbd_kvec.bin"), dtype=np.float64).reshape(nk, 3)
-        degauss, ndegauss = sz["degauss"], sz["ndegauss"]
-        degauss = pget(pm, "degauss", degauss / eV, eV)
-        ndegauss = pget(pm, "ndegauss", ndegauss)
-        scale_scatt = pget(pm, "scale_scatt", 1.0)
-        ee = EEModel(nb=nb, kvec=kvec, kmesh=sz["kmesh"], U=U, GGT=ggt_of(R), cell_size=cell_size,
-                     nk_full=sz["nk_full"], T=T, eps=pget(pm, "epsilon_background", 1.0),
-                     meff=pget(pm, "meff_screening", 1.0), formula=pm.get("scrFormula", "RPA"), nfree=nfree,
-                     update_screening=int(pget(pm, "update_screening", 1)), nv=nv_dm - bstart,
-                     degauss=pget(pm, "degauss_ee", degauss / eV, eV), ethr=degauss * ndegauss,
-                     antisym=int(pget(pm, "ee_antisymmetry", 0)), scale=pget(pm, "scale_ee", scale_scatt),
-                     inside=pget(pm, "freq_update_ee_model", 0) < 0, P1base=P1, P2base=P2,
-                     f_setup=f_dm[:, bstart:bend], e_window=e_dm[:, bstart:bend])
+        ee = _ee_model_of(pm, sz, dd, R, nk, nb, nb_dm, bstart, bend, e_dm, f_dm, nv_dm, T, cell_size, nfree, P1, P2)
         # set-up (ElectronPhonon.cpp:3-14): P_ee at the equilibrium occupations with the set-up density
         tmp = OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
                            k1st=k1, k2nd=k2, P1=ee.P1eff, P2=ee.P2eff, prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=None,
@@ -529,6 +593,7 @@ def load(d: str) -> OracleSystem:
                         temperature=T, mu=mu, nk_full=sz["nk_full"], ob_prefac=(1.0 / sz["nk_full"]) / cell_size_cmd,
                         ode=ode, params=pm, nv_dm=nv_dm, mue=mue, muh=muh, f_eq=f_eq, ddmdt_eq=ddmdt_eq, linear=linear,
                         f_lin=f_lin, ee=ee, sparse=int(pget(pm, "alg_sparseP", 0.0)) != 0,
+                        lin_ee=lin_ee if linear else None,
                         thr_sparse=pget(pm, "alg_thr_sparseP", 1e-40))
 
 

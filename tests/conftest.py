@@ -10,8 +10,9 @@ if ROOT not in sys.path:
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 GOLDEN_CASES = sorted(d for d in os.listdir(GOLDEN) if os.path.isfile(os.path.join(GOLDEN, d, "golden.npz")))
 # cases whose operators are rebuilt from rho by the e-e model (eeMode = Pee_update), and the others
-EE_CASES = [c for c in GOLDEN_CASES if c.startswith("ee_")]
-FIXED_P_CASES = [c for c in GOLDEN_CASES if not c.startswith("ee_")]
+# (the linearized e-e cases hold the e-e term inside their fixed linear operators)
+EE_CASES = [c for c in GOLDEN_CASES if c.startswith("ee_") and "linear" not in c]
+FIXED_P_CASES = [c for c in GOLDEN_CASES if c not in EE_CASES]
 
 
 def pytest_configure(config):

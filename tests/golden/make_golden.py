@@ -98,6 +98,23 @@ CASES = {
                             param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0.3, 0, 0.2),
                                        extra=dict(EE_COMMON, scrFormula="RPA", update_screening=1,
                                                   ee_antisymmetry=1))),
+    # linearized master equation with the e-e source (add_Lsc_contrib("ee"): P_ee at f_eq and the P3-P6
+    # terms), Debye screening from f_eq, e-imp, B field
+    "ee_nb2_linear": dict(cfg=SynthConfig(nk=40, nb=2, seed=36, de_pair_mev=60.0, eimp_sigma_mev=5.0, nwannier=4,
+                                          kball=True),
+                          param=dict(Bpert_T=(0, 0, 0.1), B_T=(0.6, 0, 0), eimp_fraction=0.05,
+                                     extra=dict(EE_COMMON, scrFormula="debye", update_screening=1, alg_linearize=1)),
+                          carrier_scale=1.3),
+    # linearized, nb = 4, static RPA, exchange term (P3/P4 skipped, P_ee doubled in Lscij)
+    "ee_nb4_linear_rpa_anti": dict(cfg=SynthConfig(nk=14, nb=4, seed=37, de_pair_mev=60.0, nwannier=6, kball=True),
+                                   param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0.3, 0, 0.2),
+                                              extra=dict(EE_COMMON, scrFormula="RPA", update_screening=1,
+                                                         ee_antisymmetry=1, alg_linearize=1))),
+    # linearized, P_ee fixed at equilibrium (no P3-P6), Bechstedt, screening density of the set-up
+    "ee_nb2_linear_fixed": dict(cfg=SynthConfig(nk=32, nb=2, seed=38, de_pair_mev=60.0, nwannier=3, kball=True),
+                                param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0, 0.6, 0),
+                                           extra=dict(EE_COMMON, eeMode="Pee_fixed_at_eq", scrFormula="Bechstedt",
+                                                      update_screening=0, meff_screening=0.3, alg_linearize=1))),
     # sparse operators (alg_sparseP): 70 % of every pair's P1 / P2 elements zeroed, nb = 4, B field;
     # the reference contracts the stored elements with sparse_zgemm (e-ph only: the reference refuses
     # ab-initio e-imp with sparse P)
@@ -189,7 +206,7 @@ def make_case(name, spec, ref_bin, outroot):
         out["Lscji"] = np.fromfile(os.path.join(tmp, "o", "Lscji.bin"), dtype=np.complex128).reshape(-1, nbw ** 4)
     if meta["has_H"]:
         out["Hcoh"] = np.fromfile(os.path.join(tmp, "o", "Hcoh.bin"), dtype=np.complex128).reshape(nk, nbdm * nbdm)
-    ee = bool(meta.get("ee", 0))
+    ee = bool(meta.get("ee", 0)) and not meta["linearize"]  # (linearized: the e-e term is inside Lscij / Lscji)
     if ee:  # P after set-up: P_eph (+ P_eimp) + scale_ee P_ee at the equilibrium occupations
         out["ee_P1_eq"] = np.fromfile(os.path.join(tmp, "o", "P1.bin"), dtype=np.complex128).reshape(-1, nbw ** 4)
         out["ee_P2_eq"] = np.fromfile(os.path.join(tmp, "o", "P2.bin"), dtype=np.complex128).reshape(-1, nbw ** 4)

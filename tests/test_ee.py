@@ -13,7 +13,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import EE_CASES, GOLDEN
+from conftest import EE_CASES, FIXED_P_CASES, GOLDEN
 
 pytestmark = pytest.mark.gpu
 
@@ -248,3 +248,65 @@ def test_ee_argument_and_order_checks(oracle, built):
         assert ex.value.status == 7
         e = rel(gpu.func(g["rhs_t"][1], g["rhs_y"][1]), g["rhs_dydt"][1])
         assert e < RHS_TOL["f64"]
+
+
+LINEAR_EE_CASES = [c for c in FIXED_P_CASES if c.startswith("ee_") and "linear" in c]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", LINEAR_EE_CASES)
+def test_linearized_ee_source_vs_reference(case, oracle, built):
+    """The e-e source of the linearized operators (add_Lsc_contrib("ee"): P_ee at f_eq and, unless
+    eeMode = Pee_fixed_at_eq, the P3..P6 terms), built by the host library with the GPU
+    (dmd_ee_linear_terms): the operators within 1e-12 of the reference's Lscij / Lscji, and the RHS
+    and 40 RK4 steps of the resulting linearized system against the reference's."""
+    from denmat_dynm_development_gb300.host import System
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = System(d)
+    e1 = rel(s.P1.reshape(g["Lscij"].shape), g["Lscij"])
+    e2 = rel(s.P2.reshape(g["Lscji"].shape), g["Lscji"])
+    print("%s: Lscij rel err %.3g, Lscji %.3g" % (case, e1, e2))
+    assert e1 < 1e-12 and e2 < 1e-12
+    with s.gpu("f64") as gpu:
+        for i, t in enumerate(g["rhs_t"]):
+            assert rel(gpu.func(t, g["rhs_y"][i]), g["rhs_dydt"][i]) < 1e-12
+        gpu.set_state(s.info.t0, np.ascontiguousarray(s.dm0).view(np.float64).reshape(-1))
+        gpu.rk4(1.0 * oracle.fs, 40)
+        _, y = gpu.get_state()
+    assert rel(y, g["rk4_y"]) < 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["ee_nb2_linear", "ee_nb4_linear_rpa_anti"])
+def test_p3_to_p6_on_gpu_vs_oracle(case, oracle, built):
+    """dmd_ee_linear_terms' P_ee at f_eq and P3..P6 (k_ee_p36) against the oracle's restatement of
+    calc_P / calc_P3P4 / calc_P5P6 on the same inputs, 1e-12 normwise each."""
+    from denmat_dynm_development_gb300.dmd import LindbladGPU
+    from denmat_dynm_development_gb300.host import System
+    d = os.path.join(GOLDEN, case)
+    s = System(d)
+    o = oracle.load(d)
+    ee = s.ee
+    assert ee is not None and o.lin_ee is not None
+    i = s.info
+    nb = i.bend - i.bstart
+    f_lin = np.ascontiguousarray(s.f_eq[:, i.bstart:i.bend])
+    n = ee["nfree"]
+    if ee["update_screening"]:  # coulomb_model::init(f_eq)
+        n = float(sum((1 - f_lin[k, b]) if b < ee["nv"] else f_lin[k, b] for k in range(i.nk) for b in range(nb)))
+        n /= ee["nk_full"] * ee["cell_size"]
+    base = np.zeros(o.npair * nb ** 4, np.complex128)
+    with LindbladGPU(nk=o.nk, nb_dm=o.nb_dm, bstart=o.bstart, bend=o.bend, e_dm=o.e_dm, k1st=o.k1st, k2nd=o.k2nd,
+                     P1=base, P2=base, prefac_eph=o.prefac_eph, precision="f64", ee=dict(ee, every_rhs=0)) as g:
+        got = g.ee_linear_terms(f_lin, n)
+    sc = ee["scale"]
+    for j, nm in enumerate(["P1ee", "P2ee", "P3", "P4", "P5", "P6"]):
+        want = o.lin_ee[j].reshape(o.npair, -1)
+        want = want / sc if sc != 1.0 else want
+        if np.abs(want).max() == 0:
+            assert np.abs(got[j]).max() == 0, nm
+            continue
+        err = rel(got[j], want)
+        print("%s %s rel err %.3g" % (case, nm, err))
+        assert err < 1e-12, nm
