@@ -198,7 +198,7 @@ def measured_peak():
 def profile_traffic(precision):
     """DRAM bytes per pair-kernel launch from the committed ncu summary of this arithmetic, as
     (bytes, npair of the captured workload); scaled by the caller to the benchmarked workload."""
-    p = os.path.join(ROOT, "profiles", "pairs_herm_%s_gaas_nk8k.md" % precision)
+    p = os.path.join(ROOT, "profiles", "pairs_herm_%s_gaas_nk16k.md" % precision)
     try:
         vals = {}
         with open(p) as f:
