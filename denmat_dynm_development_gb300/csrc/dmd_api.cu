@@ -602,7 +602,7 @@ __host__ __device__ uint32_t pack_bf2(double x) {
 __host__ __device__ void pack_elem(int prec, cd v, unsigned char* out) {
   if (prec == DMD_PREC_F64X) {
     const float xh = (float)v.re, yh = (float)v.im;
-    const float f[4] = {xh, (float)(v.re - (double)xh), yh, (float)(v.im - (double)yh)};
+    const float f[4] = {xh, yh, (float)(v.re - (double)xh), (float)(v.im - (double)yh)};  // high parts, low parts
     memcpy(out, f, 16);
   } else if (prec == DMD_PREC_F32) {
     const float f[2] = {(float)v.re, (float)v.im};

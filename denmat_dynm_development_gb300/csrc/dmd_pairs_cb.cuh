@@ -28,7 +28,8 @@
 //   ArithDF  -- (hi, lo) FP32 pairs for P and the coordinates; products are error-free transformed
 //               (p = xh*yh, e = fma(xh,yh,-p) + xh*yl + xl*yh) and sums use TwoSum on the high
 //               parts, so each product carries ~2^-47 relative error and the FP32 pipes (64x the
-//               FP64 rate on this part) do the work.
+//               FP64 rate on this part) do the work; the real and the imaginary half of each step
+//               are one FP32x2 instruction.
 #pragma once
 #include "dmd_common.cuh"
 #include "dmd_layout.h"
@@ -85,36 +86,68 @@ __device__ __forceinline__ float2 split_df1(double v) {
   return make_float2(h, __double2float_rn(v - (double)h));
 }
 
+// Packed (re, im) double-float arithmetic on the FP32x2 instructions (fma/add/mul .f32x2): both
+// halves of every instruction are the same round-to-nearest operation that the scalar helpers above
+// perform, so the results are bit-identical to applying those helpers to the real and the imaginary
+// part, at half the issued instructions. a - b is fma(b, -1, a), one rounding of the exact difference.
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+// packed TwoSum: s + e = a + b exactly, per half
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  const float2 bb = f2sub(s, a);
+  e = __fadd2_rn(f2sub(a, f2sub(s, bb)), f2sub(b, bb));
+}
+
 struct ArithDF {
-  typedef float4 elem;  // P element: (re_h, re_l, im_h, im_l)
+  // P element: (re_h, im_h, re_l, im_l) -- the high parts and the low parts as FP32x2 pairs
+  typedef float4 elem;
   typedef float2 relem;  // real coordinate: (h, l)
+  // a coordinate prepared for the products: (h, h, l, l), or (h, -h, l, -l) for conj(x) * v
+  typedef float4 pcoord;
+  typedef float4 pcoord_cx;
   struct acc {
-    float rh, rl, ih, il;
+    float2 h, l;  // (re, im) high parts, (re, im) low parts
   };
-  static __device__ __forceinline__ void zero(acc& a) { a.rh = a.rl = a.ih = a.il = 0.f; }
-  // a += x * v (complex x real)
-  static __device__ __forceinline__ void mac(acc& a, const elem& x, const relem& v) {
-    df_mac(a.rh, a.rl, x.x, x.y, v.x, v.y);
-    df_mac(a.ih, a.il, x.z, x.w, v.x, v.y);
+  static __device__ __forceinline__ pcoord prep(relem v) { return make_float4(v.x, v.x, v.y, v.y); }
+  static __device__ __forceinline__ pcoord_cx prep_cx(relem v) { return make_float4(v.x, -v.x, v.y, -v.y); }
+  static __device__ __forceinline__ float2 hi(const float4& x) { return make_float2(x.x, x.y); }
+  static __device__ __forceinline__ float2 lo(const float4& x) { return make_float2(x.z, x.w); }
+  static __device__ __forceinline__ void zero(acc& a) { a.h = a.l = make_float2(0.f, 0.f); }
+  // a += x * v, v prepared: the error-free product (p = xh*vh, e = fma(xh,vh,-p) + xh*vl + xl*vh)
+  // added with TwoSum on the high parts
+  static __device__ __forceinline__ void pmac(acc& a, const elem& x, const float4& v) {
+    const float2 xh = hi(x), xl = lo(x), vh = hi(v), vl = lo(v);
+    const float2 p = __fmul2_rn(xh, vh);
+    float2 e = __ffma2_rn(xh, vh, make_float2(-p.x, -p.y));
+    e = __ffma2_rn(xh, vl, e);
+    e = __ffma2_rn(xl, vh, e);
+    float2 s, t;
+    two_sum2(a.h, p, s, t);
+    a.h = s;
+    a.l = __fadd2_rn(a.l, __fadd2_rn(t, e));
   }
+  static __device__ __forceinline__ void mac(acc& a, const elem& x, const pcoord& v) { pmac(a, x, v); }
+  // a += conj(x) * v (v prepared by prep_cx: the imaginary half multiplies by -v)
+  static __device__ __forceinline__ void mac_cx(acc& a, const elem& x, const pcoord_cx& v) { pmac(a, x, v); }
   // a = x * v
-  static __device__ __forceinline__ void mul(acc& a, const elem& x, const relem& v) {
-    df_mul(a.rh, a.rl, x.x, x.y, v.x, v.y);
-    df_mul(a.ih, a.il, x.z, x.w, v.x, v.y);
-  }
-  // a += conj(x) * v
-  static __device__ __forceinline__ void mac_cx(acc& a, const elem& x, const relem& v) {
-    df_mac(a.rh, a.rl, x.x, x.y, v.x, v.y);
-    df_mac(a.ih, a.il, -x.z, -x.w, v.x, v.y);
+  static __device__ __forceinline__ void mul(acc& a, const elem& x, const pcoord& v) {
+    const float2 xh = hi(x), xl = lo(x), vh = hi(v), vl = lo(v);
+    const float2 p = __fmul2_rn(xh, vh);
+    float2 e = __ffma2_rn(xh, vh, make_float2(-p.x, -p.y));
+    e = __ffma2_rn(xh, vl, e);
+    a.l = __ffma2_rn(xl, vh, e);
+    a.h = p;
   }
   static __device__ __forceinline__ void renorm(acc& a) {
-    df_renorm(a.rh, a.rl);
-    df_renorm(a.ih, a.il);
+    const float2 s = __fadd2_rn(a.h, a.l);
+    a.l = f2sub(a.l, f2sub(s, a.h));
+    a.h = s;
   }
   // reduction scratch entry: one real (hi, lo)
   typedef float2 red_t;
-  static __device__ __forceinline__ float2 red_re(const acc& a) { return make_float2(a.rh, a.rl); }
-  static __device__ __forceinline__ float2 red_im(const acc& a) { return make_float2(a.ih, a.il); }
+  static __device__ __forceinline__ float2 red_re(const acc& a) { return make_float2(a.h.x, a.l.x); }
+  static __device__ __forceinline__ float2 red_im(const acc& a) { return make_float2(a.h.y, a.l.y); }
   static __device__ __forceinline__ float2 red_neg(float2 v) { return make_float2(-v.x, -v.y); }
   static __device__ __forceinline__ float2 red_zero() { return make_float2(0.f, 0.f); }
   static __device__ __forceinline__ void red_add(float2& s, float2 b) { df_add(s.x, s.y, b.x, b.y); }
@@ -122,14 +155,18 @@ struct ArithDF {
     return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
   }
   static __device__ __forceinline__ double red_to_double(float2 v) { return (double)v.x + (double)v.y; }
-  static __device__ __forceinline__ double re_d(const acc& a) { return (double)a.rh + (double)a.rl; }
-  static __device__ __forceinline__ double im_d(const acc& a) { return (double)a.ih + (double)a.il; }
+  static __device__ __forceinline__ double re_d(const acc& a) { return (double)a.h.x + (double)a.l.x; }
+  static __device__ __forceinline__ double im_d(const acc& a) { return (double)a.h.y + (double)a.l.y; }
   static __device__ __forceinline__ relem from_double(double v) { return split_df1(v); }
 };
 
 struct ArithF64 {
   typedef double2 elem;
   typedef double relem;
+  typedef double pcoord;
+  typedef double pcoord_cx;
+  static __device__ __forceinline__ double prep(double v) { return v; }
+  static __device__ __forceinline__ double prep_cx(double v) { return v; }
   struct acc {
     double x, y;
   };
@@ -166,6 +203,10 @@ struct ArithF64 {
 struct ArithF32 {
   typedef float2 elem;
   typedef float relem;
+  typedef float pcoord;
+  typedef float pcoord_cx;
+  static __device__ __forceinline__ float prep(float v) { return v; }
+  static __device__ __forceinline__ float prep_cx(float v) { return v; }
   typedef float2 acc;
   static __device__ __forceinline__ float2 val(const elem& x) { return x; }
   static __device__ __forceinline__ void zero(acc& a) { a.x = a.y = 0.f; }
@@ -563,15 +604,15 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
   for (int i = lane; i < RV; i += 32) rowv[RV + i] = V();
   const int col = w.J * W + sl;
   const bool colok = col < nk;
-  V rc[4][RW], sc[4][RW];  // r_col, s_col on this lane's quarter, per state
+  typename A::pcoord rc[4][RW], sc[4][RW];  // r_col, s_col on this lane's quarter, per state
 #pragma unroll
   for (int u = 0; u < RW; ++u)
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const bool ok = colok && u < nq;
       const V* rq = rs + (size_t)(q0 + u) * rstride + (size_t)col * 2 * NB2;
-      rc[i][u] = ok ? rq[q4 + i] : V();
-      sc[i][u] = ok ? rq[NB2 + q4 + i] : V();
+      rc[i][u] = A::prep(ok ? rq[q4 + i] : V());
+      sc[i][u] = A::prep(ok ? rq[NB2 + q4 + i] : V());
     }
   Acc rX[4][RW], rY[4][RW];
 #pragma unroll
@@ -642,6 +683,9 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
           for (int r = 0; r < LINES; ++r) {
             const int a = l0 + r;
             Acc f[RW];
+            typename A::pcoord_cx sa[RW];
+#pragma unroll
+            for (int u = 0; u < RW; ++u) sa[u] = A::prep_cx(rv[u * 2 * NB2 + NB2 + a]);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
               const E p1 = st[(r * NB2 + q4 + i) * n];
@@ -649,7 +693,7 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
               for (int u = 0; u < RW; ++u) {
                 if (i == 0) A::mul(f[u], p1, rc[i][u]);
                 else A::mac(f[u], p1, rc[i][u]);
-                A::mac_cx(rY[i][u], p1, rv[u * 2 * NB2 + NB2 + a]);
+                A::mac_cx(rY[i][u], p1, sa[u]);
               }
             }
             if constexpr (FA) {
@@ -676,6 +720,9 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
           for (int r = 0; r < LINES; ++r) {
             const int j = l0 + r;
             Acc f[RW];
+            typename A::pcoord_cx rj[RW];
+#pragma unroll
+            for (int u = 0; u < RW; ++u) rj[u] = A::prep_cx(rv[u * 2 * NB2 + j]);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
               const E p2 = st[(r * NB2 + q4 + i) * n];
@@ -683,7 +730,7 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
               for (int u = 0; u < RW; ++u) {
                 if (i == 0) A::mul(f[u], p2, sc[i][u]);
                 else A::mac(f[u], p2, sc[i][u]);
-                A::mac_cx(rX[i][u], p2, rv[u * 2 * NB2 + j]);
+                A::mac_cx(rX[i][u], p2, rj[u]);
               }
             }
             if constexpr (FA) {
