@@ -144,6 +144,18 @@ struct ArithDF {
     a.l = f2sub(a.l, f2sub(s, a.h));
     a.h = s;
   }
+  // forward flush on packed complex entries (re_h, im_h, re_l, im_l), multiplied by i when imag
+  static constexpr bool kPackedRed = true;
+  static __device__ __forceinline__ float4 red_pack(const acc& a, bool imag) {
+    return imag ? make_float4(-a.h.y, a.h.x, -a.l.y, a.l.x) : make_float4(a.h.x, a.h.y, a.l.x, a.l.y);
+  }
+  // s += b (double-float, per half)
+  static __device__ __forceinline__ void red_add4(float4& s, const float4& b) {
+    float2 h, t;
+    two_sum2(hi(s), hi(b), h, t);
+    const float2 l = __fadd2_rn(lo(s), __fadd2_rn(t, lo(b)));
+    s = make_float4(h.x, h.y, l.x, l.y);
+  }
   // reduction scratch entry: one real (hi, lo)
   typedef float2 red_t;
   static __device__ __forceinline__ float2 red_re(const acc& a) { return make_float2(a.h.x, a.l.x); }
@@ -184,6 +196,7 @@ struct ArithF64 {
     a.y = x.y * v;
   }
   static __device__ __forceinline__ void renorm(acc&) {}
+  static constexpr bool kPackedRed = false;
   typedef double red_t;
   static __device__ __forceinline__ double red_re(const acc& a) { return a.x; }
   static __device__ __forceinline__ double red_im(const acc& a) { return a.y; }
@@ -223,6 +236,7 @@ struct ArithF32 {
     a.y = __fmul_rn(x.y, v);
   }
   static __device__ __forceinline__ void renorm(acc&) {}
+  static constexpr bool kPackedRed = false;
   typedef float red_t;
   static __device__ __forceinline__ float red_re(const acc& a) { return a.x; }
   static __device__ __forceinline__ float red_im(const acc& a) { return a.y; }
@@ -513,8 +527,10 @@ struct CbTmaSmem {
   static constexpr int FL = 8, NV = 2 * FL * RW; // lines per forward flush, reals per flush (all RHS)
   static constexpr int CPM = NB2 / LINES;        // chunks per matrix
   static constexpr int CPR = 2 * CPM;            // chunks per row block
+  // packed complex flush entries (one state, one lane per pair)
+  static constexpr bool PR = A::kPackedRed && !FA && RW == 1 && G == 1;
   static constexpr size_t stage_bytes = (size_t)LINES * NB2 * W * sizeof(typename A::elem);
-  static constexpr size_t red_bytes = FA ? 0 : (size_t)NV * 32 * sizeof(typename A::red_t);
+  static constexpr size_t red_bytes = FA ? 0 : PR ? (size_t)FL * 32 * 16 : (size_t)NV * 32 * sizeof(typename A::red_t);
   static constexpr size_t row_bytes = (size_t)4 * NB2 * RW * sizeof(typename A::relem);  // r_k, s_k, zeros
   static constexpr size_t warp_bytes = ((NST * stage_bytes + red_bytes + row_bytes + 8 * NST) + 127) / 128 * 128;
   static constexpr size_t cta_bytes = 4 * warp_bytes;
@@ -705,6 +721,8 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
                   atomicAdd(dst + (size_t)(q0 + u) * astride + 1, IMAG ? A::re_d(f[u]) : A::im_d(f[u]));
                 }
               }
+            } else if constexpr (S::PR) {
+              reinterpret_cast<float4*>(red)[rsw((q * LINES + r) % FL, lane)] = A::red_pack(f[0], IMAG);
             } else {
               const int v = 2 * ((q * LINES + r) % FL);
 #pragma unroll
@@ -742,6 +760,8 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
                   atomicAdd(dst + (size_t)(q0 + u) * astride + 1, IMAG ? A::re_d(f[u]) : A::im_d(f[u]));
                 }
               }
+            } else if constexpr (S::PR) {
+              reinterpret_cast<float4*>(red)[rsw((q * LINES + r) % FL, lane)] = A::red_pack(f[0], IMAG);
             } else {
               const int v = 2 * ((q * LINES + r) % FL);
 #pragma unroll
@@ -758,7 +778,34 @@ __global__ void __launch_bounds__(128, MINB) k_pairs_herm(const WorkItem* __rest
       fence_proxy_async();
       __syncwarp();
       if (c + NST < nch) issue(c + NST);
-      if (!FA && ((q + 1) * LINES) % FL == 0) {
+      if constexpr (S::PR) {
+        if (((q + 1) * LINES) % FL == 0) {
+          // packed entries: lane (part, v) sums line v over the active lanes [8 part, 8 part + 8) (the
+          // 8 lanes of a quarter warp read 8 lines of one source lane: distinct banks), the four parts
+          // are added with two shuffles, and lanes 0-15 add line (lane & 7)'s real (part 0) or
+          // imaginary (part 1) sum to the row
+          const int L0 = (q + 1) * LINES - FL;
+          const int v = lane & 7, part = lane >> 3;
+          const float4* red4 = reinterpret_cast<const float4*>(red);
+          float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+          unsigned m = (lm >> (part * 8)) & 0xffu;
+          while (m) {
+            const int jj = __ffs(m) - 1;
+            m &= m - 1;
+            A::red_add4(sum, red4[rsw(v, part * 8 + jj)]);
+        }
+#pragma unroll
+        for (int mm = 8; mm < 32; mm <<= 1) {
+          const float4 o = make_float4(__shfl_xor_sync(FULL, sum.x, mm), __shfl_xor_sync(FULL, sum.y, mm),
+                                       __shfl_xor_sync(FULL, sum.z, mm), __shfl_xor_sync(FULL, sum.w, mm));
+          A::red_add4(sum, o);
+        }
+        if (lane < 16)
+          atomicAdd(acc + (size_t)q0 * astride + (size_t)brow * 4 * NB2 + 2 * L0 + 2 * v + part,
+                    part == 0 ? (double)sum.x + (double)sum.z : (double)sum.y + (double)sum.w);
+        __syncwarp();
+        }
+      } else if (!FA && ((q + 1) * LINES) % FL == 0) {
         // lines [L0, L0 + FL) of this row block are complete: reduce over the active lanes and add
         // to the row's sums (line L is real pair 2L, 2L + 1 of [X'(NB2) | Y'(NB2)]); buffer value
         // v * RW + 2u + ri holds line v / 2 (of the flush), part ri, state u
