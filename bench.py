@@ -15,7 +15,8 @@ The headline arithmetic is the reference's: plain FP64 (P complex128, FP64 multi
               K-step window is timed `--windows` times (CUDA events) and the median is reported,
               with the spread
   e2e         the same metric through the reference-facing GSL callback dmd_func: the host runs
-              the RK4 combination and every RHS call copies y in and dydt out (pinned buffers)
+              the RK4 combination in C loops (dmdh_rk4_func) and every RHS call copies y in and
+              dydt out (page-locked buffers)
   roofline    k-pair contraction kernel: algorithmic work per launch / its mean event-timed
               duration, against the ceiling that binds it -- the FP64 multiply-add rate measured in
               this process for the FP64 form (its work is FP64 multiply-adds; the HBM fraction is
@@ -487,41 +488,23 @@ def run_gpu(args, w, rank, world, dist):
     e2e = None
     if not args.no_e2e:
         n = y0.size
-        bufs = [PinnedArray(n) for _ in range(7)]  # y, stage input, k1..k4, sum
+        from denmat_dynm_development_gb300 import host as HL
+        bufs = [PinnedArray(n), PinnedArray(5 * n)]  # y; stage input and k1..k4
         try:
-            yv, ys, k1, k2, k3, k4, acc = (b.array for b in bufs)
-
-            def step(t):  # one host RK4 step, 4 GSL-callback RHS calls (H2D of the input, D2H of dydt)
-                g.func(t, yv, k1)
-                np.multiply(k1, 0.5 * h, out=ys)
-                np.add(ys, yv, out=ys)
-                g.func(t + 0.5 * h, ys, k2)
-                np.multiply(k2, 0.5 * h, out=ys)
-                np.add(ys, yv, out=ys)
-                g.func(t + 0.5 * h, ys, k3)
-                np.multiply(k3, h, out=ys)
-                np.add(ys, yv, out=ys)
-                g.func(t + h, ys, k4)
-                np.add(k2, k3, out=acc)
-                np.multiply(acc, 2.0, out=acc)
-                np.add(acc, k1, out=acc)
-                np.add(acc, k4, out=acc)
-                np.multiply(acc, h / 6.0, out=acc)
-                np.add(yv, acc, out=yv)
+            yv, work = bufs[0].array, bufs[1].array
             _, ycur = g.get_state()
             yv[:] = ycur
             t = 0.0
-            step(t)       # warm-up
+            HL.rk4_func(g, t, h, 1, yv, work)  # warm-up
             barrier()
             t0 = time.perf_counter()
-            for _ in range(args.steps):
-                step(t)
-                t += h
+            HL.rk4_func(g, t, h, args.steps, yv, work)
             el = time.perf_counter() - t0
+            t += args.steps * h
             e2e = {"value": world * args.steps / el, "unit": UNIT, "h2d_bytes_per_step": 4 * n * 8,
                    "d2h_bytes_per_step": 4 * n * 8,
-                   "path": "host RK4 loop calling dmd_func (GSL callback semantics) 4x per step from pinned "
-                           "buffers, stage sums in place on the host; %d steps" % args.steps}
+                   "path": "host RK4 loop (dmdh_rk4_func) calling the GSL-callback entry dmd_func 4x per step "
+                           "from page-locked buffers, stage combinations in host loops; %d steps" % args.steps}
         finally:
             for b in bufs:
                 b.free()

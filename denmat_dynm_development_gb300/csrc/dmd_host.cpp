@@ -239,6 +239,32 @@ int dmdh_fermi(double T, double mu, const double* e, double* f, size_t n) {
   return DMD_OK;
 }
 
+// Fixed-step RK4 on the host around the GSL-callback entry, as a GSL-driven host runs it: every
+// stage is one dmd_func call (its input copied to the device, dydt copied back) and the stage
+// combinations are host loops: y_s = y + c h k, then y += h/6 (k1 + 2 k2 + 2 k3 + k4).
+int dmdh_rk4_func(dmd_handle* h, double t, double dt, int64_t nsteps, double* y, size_t n, double* work) {
+  if (!h || !y || !work || n == 0 || nsteps < 0) return DMD_E_ARG;
+  double* ys = work;
+  double* k1 = work + n;
+  double* k2 = work + 2 * n;
+  double* k3 = work + 3 * n;
+  double* k4 = work + 4 * n;
+  int rc = DMD_OK;
+  for (int64_t s = 0; s < nsteps; ++s) {
+    const double ts = t + (double)s * dt, hh = 0.5 * dt;
+    if ((rc = dmd_func(h, ts, y, k1))) return rc;
+    for (size_t i = 0; i < n; ++i) ys[i] = y[i] + hh * k1[i];
+    if ((rc = dmd_func(h, ts + hh, ys, k2))) return rc;
+    for (size_t i = 0; i < n; ++i) ys[i] = y[i] + hh * k2[i];
+    if ((rc = dmd_func(h, ts + hh, ys, k3))) return rc;
+    for (size_t i = 0; i < n; ++i) ys[i] = y[i] + dt * k3[i];
+    if ((rc = dmd_func(h, ts + dt, ys, k4))) return rc;
+    const double c = dt / 6.0;
+    for (size_t i = 0; i < n; ++i) y[i] += c * (k1[i] + 2.0 * k2[i] + 2.0 * k3[i] + k4[i]);
+  }
+  return DMD_OK;
+}
+
 int dmdh_dm_bpert(int32_t nk, int32_t nb, const double* smat, const double* e, const double* f, double T,
                   const double Bpert[3], double t0, int32_t picture, double* dm) {
   if (nk <= 0 || nb <= 0 || !smat || !e || !f || !Bpert || !dm) return DMD_E_ARG;

@@ -14,7 +14,7 @@ _L = None
 
 EXPORTS = ["dmdh_load", "dmdh_free", "dmdh_error", "dmdh_info_get", "dmdh_desc", "dmdh_get_dm0", "dmdh_get_f",
            "dmdh_get_smat", "dmdh_get_f_eq", "dmdh_prepare", "dmdh_param", "dmdh_fermi", "dmdh_dm_bpert",
-           "dmdh_H_BS", "dmdh_run", "dmdh_ee_desc"]
+           "dmdh_H_BS", "dmdh_run", "dmdh_ee_desc", "dmdh_rk4_func"]
 
 
 class Info(C.Structure):
@@ -52,6 +52,7 @@ def _lib():
         L.dmdh_dm_bpert.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, d, vp, d, C.c_int32, vp]
         L.dmdh_H_BS.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, C.c_int32, vp]
         L.dmdh_run.argtypes = [C.c_char_p, C.c_int32, C.c_int64]
+        L.dmdh_rk4_func.argtypes = [vp, d, d, C.c_int64, vp, C.c_size_t, vp]
         _L = L
     return _L
 
@@ -184,6 +185,14 @@ def H_BS(smat, B, e, picture=0):
     H = np.zeros((nk, nb * nb), np.complex128)
     _ck(_lib().dmdh_H_BS(nk, nb, smat.ctypes.data, Bv.ctypes.data, e.ctypes.data, picture, H.ctypes.data))
     return H
+
+
+def rk4_func(handle, t, dt, nsteps, y, work):
+    """Fixed-step RK4 driven from the host over the GSL-callback entry dmd_func (4 calls per step,
+    host copies in and out of each call): y (float64, 2 nk nb_dm^2) is advanced in place; work holds
+    5 y.size doubles (page-locked arrays make the copies direct)."""
+    assert y.dtype == np.float64 and y.flags.c_contiguous and work.dtype == np.float64 and work.size >= 5 * y.size
+    _ck(_lib().dmdh_rk4_func(handle._h, float(t), float(dt), int(nsteps), y.ctypes.data, y.size, work.ctypes.data))
 
 
 def run(directory: str, precision="f64", nsteps_max=-1):

@@ -82,6 +82,13 @@ int dmdh_dm_bpert(int32_t nk, int32_t nb, const double* smat, const double* e, c
 int dmdh_H_BS(int32_t nk, int32_t nb, const double* smat, const double B[3], const double* e, int32_t picture,
               double* H);
 
+/* Fixed-step RK4 over the GSL-callback entry dmd_func, driven from the host the way GSL's stepper
+ * drives func (DensityMatrix_Dynamics.h:358-369): nsteps steps of dt from t on the host state y (n
+ * doubles, updated in place), 4 dmd_func calls per step (each copies its input to the device and
+ * dydt back), stage combinations in host loops. work: 5 n doubles, caller-owned (page-locked memory
+ * makes the copies direct). */
+int dmdh_rk4_func(dmd_handle* h, double t, double dt, int64_t nsteps, double* y, size_t n, double* work);
+
 /* DMD's time loop on the GPU: evolve_gsl (rkf45), evolve_euler, or fixed-step RK4, writing
  * sx/sy/sz_elec_tot.out into dir after every output step. nsteps_max < 0 runs to tend. */
 int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max);

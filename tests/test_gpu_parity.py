@@ -92,6 +92,25 @@ def test_rk4_vs_golden(case, prec, oracle, built):
         assert rel(rec[:, 2], ref[:, 2]) < 1e-10
 
 
+@pytest.mark.parametrize("case", FIXED_P_CASES)
+def test_host_rk4_over_callback_vs_golden(case, oracle, built):
+    """dmdh_rk4_func (the host drives RK4 through the GSL-callback entry, 4 dmd_func calls per step)
+    reaches the reference's RK4 state after 40 steps, like the device-resident loop"""
+    from denmat_dynm_development_gb300 import host as HL
+    d = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(d, "golden.npz")))
+    s = oracle.load(d)
+    with make_gpu(s, "f64") as gpu:
+        y = np.ascontiguousarray(oracle.y_of(s.dm0), dtype=np.float64).copy()
+        work = np.zeros(5 * y.size)
+        HL.rk4_func(gpu, s.t0, 1.0 * oracle.fs, 40, y, work)
+        assert rel(y, g["rk4_y"]) < 1e-10
+        gpu.set_state(s.t0, oracle.y_of(s.dm0))
+        gpu.rk4(1.0 * oracle.fs, 40)
+        _, yd = gpu.get_state()
+        assert rel(y, yd) < 1e-13
+
+
 @pytest.mark.parametrize("case,prec", ALL)
 def test_rkf45_vs_golden(case, prec, oracle, built):
     """DMD's evolve_gsl loop: one driver_apply per output interval (DensityMatrix_Dynamics.h:210-223)."""
