@@ -22,6 +22,7 @@
 #pragma once
 #include "dmd_common.cuh"
 #include "dmd_kernels.cuh"
+#include "dmd_pairs_cb.cuh"
 
 namespace dmd {
 
@@ -41,6 +42,10 @@ struct AdjLocalArgs {
   double2* rt;          // forward coordinates conj(D) o rho, conj(D) o (1 - rho) [k][NB2]
   double2* st;
   double2* ubar;        // [k][nbdm^2]: coherent adjoint + local e-ph adjoint
+  double2* rtb;         // transposed-contraction sums [k][NB2], zeroed here for the pair pass (or null)
+  double2* stb;
+  float4* dfv;          // double-float forms (x, S(x)) of Xb, Yb, rt, st for k_adj_pairs_df (or null)
+  size_t nk2;           // nk NB2
 };
 
 __device__ __forceinline__ double2 cmulc(double2 a, double2 b) {  // conj(a) * b
@@ -52,6 +57,12 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return mk2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
 
+// a complex as a double-float (re_h, im_h, re_l, im_l)
+__device__ __forceinline__ float4 dfc_split(double re, double im) {
+  const float rh = __double2float_rn(re), ih = __double2float_rn(im);
+  return make_float4(rh, ih, __double2float_rn(__dsub_rn(re, (double)rh)), __double2float_rn(__dsub_rn(im, (double)ih)));
+}
+
 template <int NB>
 __global__ void k_adj_local(AdjLocalArgs a) {
   constexpr int NB2 = NB * NB;
@@ -61,6 +72,11 @@ __global__ void k_adj_local(AdjLocalArgs a) {
   const double2* yk = a.u + (size_t)k * nd2;
   const double2* vk = a.vbar + (size_t)k * nd2;
   double2* ub = a.ubar + (size_t)k * nd2;
+  if (a.rtb)
+    for (int e = 0; e < NB2; ++e) {
+      a.rtb[(size_t)k * NB2 + e] = mk2(0.0, 0.0);
+      a.stb[(size_t)k * NB2 + e] = mk2(0.0, 0.0);
+    }
   for (int e = 0; e < nd2; ++e) ub[e] = mk2(0.0, 0.0);
   // coherent term -i[H(t), rho]: adjoint i(H v - v H) (H Hermitian, read from its upper triangle)
   if (a.want_coh) {
@@ -150,6 +166,14 @@ __global__ void k_adj_local(AdjLocalArgs a) {
       Ybk[e] = cmulc(D[e], db);
       a.rt[(size_t)k * NB2 + e] = cmulc(D[e], r[e]);
       a.st[(size_t)k * NB2 + e] = cmulc(D[e], om[e]);
+      if (a.dfv) {  // (x, S(x)), S(x) = (Im x, -Re x), of the four vectors
+        const double2 v4[4] = {Xbk[e], Ybk[e], a.rt[(size_t)k * NB2 + e], a.st[(size_t)k * NB2 + e]};
+        for (int v = 0; v < 4; ++v) {
+          float4* o = a.dfv + 2 * ((size_t)v * a.nk2 + (size_t)k * NB2 + e);
+          o[0] = dfc_split(v4[v].x, v4[v].y);
+          o[1] = dfc_split(v4[v].y, -v4[v].x);
+        }
+      }
       double2& o = ub[(a.bs + i) * nd + a.bs + j];
       o = cadd(o, rb);
     }
@@ -210,6 +234,149 @@ __global__ void k_adj_pairs(long long npair, const int2* __restrict__ kk, const 
     atomicAdd(&rtb[((size_t)k * NB2 + b) * 2 + 1], a3.y);
     atomicAdd(&stb[((size_t)k * NB2 + b) * 2], a4.x);
     atomicAdd(&stb[((size_t)k * NB2 + b) * 2 + 1], a4.y);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Double-float form of the transposed pair contraction and of the operator gradient (handles whose
+// forward sums are double-float): the same sums as k_adj_pairs with every product error-free
+// transformed on the FP32 pipes (ArithDF's packed (re, im) steps, ~2^-44 relative) instead of on the
+// FP64 pipe; the gradient G is kept as double-float (re_h, im_h, re_l, im_l) per element,
+// renormalised after every update, and converted to FP64 once at the end (k_df_to_f64).
+// A complex product is two packed multiply-adds: with S(x) = (Im x, -Re x),
+//   conj(p) x = x o (Re p, Re p) + S(x) o (Im p, Im p),   p x = x o (Re p, Re p) - S(x) o (Im p, Im p),
+//   conj(x) y = y o (Re x, Re x) + S(y) o (Im x, Im x).
+// ---------------------------------------------------------------------------------------------
+// broadcast of the real / imaginary part of a double-float complex (re_h, im_h, re_l, im_l)
+__device__ __forceinline__ float4 df_bre(const float4& x) { return make_float4(x.x, x.x, x.z, x.z); }
+__device__ __forceinline__ float4 df_bim(const float4& x) { return make_float4(x.y, x.y, x.w, x.w); }
+__device__ __forceinline__ float4 df_bimn(const float4& x) { return make_float4(-x.y, -x.y, -x.w, -x.w); }
+
+// pair operators [pair][P1 | P2][nb^4] (complex128) -> double-float copy, one thread per element
+__global__ void k_p_to_df(size_t n, const double2* __restrict__ P, float4* __restrict__ out) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = dfc_split(P[i].x, P[i].y);
+}
+
+// double-float complex (re_h, im_h, re_l, im_l) -> complex128 in place (its conjugate when conj)
+__global__ void k_df_to_f64(size_t n, float4* __restrict__ g, int conj) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 v = g[i];
+  const double im = (double)v.y + (double)v.w;
+  reinterpret_cast<double2*>(g)[i] = mk2((double)v.x + (double)v.z, conj ? -im : im);
+}
+
+// out[j][e] = G[j][m][e] for the n = cnt nb4 elements of a chunk of pairs (G: [pair][2][nb4])
+__global__ void k_gather_half(size_t n, size_t nb4, const double2* __restrict__ G, int m, double2* __restrict__ out) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const size_t j = i / nb4, e = i - j * nb4;
+  out[i] = G[(j * 2 + m) * nb4 + e];
+}
+
+// g = conj(g) in place
+__global__ void k_conj(size_t n, double2* __restrict__ g) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) g[i].y = -g[i].y;
+}
+
+// One thread per (pair, index b), as k_adj_pairs. dfv: k_adj_local's double-float forms; P: double-float pair
+// operators; G: double-float gradient [pair][G1 | G2][nb^4].
+template <int NB>
+__global__ void __launch_bounds__(128) k_adj_pairs_df(long long npair, const int2* __restrict__ kk,
+                                                      const float4* __restrict__ P, const float4* __restrict__ dfv,
+                                                      size_t nk2, double* __restrict__ rtb, double* __restrict__ stb,
+                                                      float4* __restrict__ G) {
+  constexpr int NB2 = NB * NB, NB4 = NB2 * NB2;
+  typedef ArithDF D;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= npair * NB2) return;
+  const long long p = idx / NB2;
+  const int b = (int)(idx - p * NB2);
+  const int2 kp2 = kk[p];
+  const int k = kp2.x, kq = kp2.y;
+  const float4* P1 = P + (size_t)p * 2 * NB4;
+  const float4* P2 = P1 + NB4;
+  float4* G1 = G + (size_t)p * 2 * NB4;
+  float4* G2 = G1 + NB4;
+  // element e of vector v at k: (x, S(x)) at dfv[2 ((v nk + k) NB2 + e)]
+  auto vx = [&](int v, int kk_, int e) -> const float4* { return dfv + 2 * ((size_t)v * nk2 + (size_t)kk_ * NB2 + e); };
+  D::acc a1, a2;
+  D::zero(a1);
+  D::zero(a2);
+#pragma unroll
+  for (int a = 0; a < NB2; ++a) {
+    const float4 x = P1[a * NB2 + b];  // conj(P1[a][b]) Xbar[k][a]
+    const float4* X = vx(0, k, a);
+    D::pmac(a1, X[0], df_bre(x));
+    D::pmac(a1, X[1], df_bim(x));
+    const float4 y = P2[b * NB2 + a];  // conj(P2[b][a]) Ybar[k][a]
+    const float4* Y = vx(1, k, a);
+    D::pmac(a2, Y[0], df_bre(y));
+    D::pmac(a2, Y[1], df_bim(y));
+  }
+  double* ro = rtb + ((size_t)kq * NB2 + b) * 2;
+  double* so = stb + ((size_t)kq * NB2 + b) * 2;
+  atomicAdd(ro, D::re_d(a1));
+  atomicAdd(ro + 1, D::im_d(a1));
+  atomicAdd(so, D::re_d(a2));
+  atomicAdd(so + 1, D::im_d(a2));
+  const bool rev = k < kq;
+  // G1[a][b] += conj(Xbar[k][a]) rt[k'][b] (+ conj(st[k][a]) Ybar[k'][b]);
+  // G2[a][b] += conj(Ybar[k][b]) st[k'][a] (+ conj(rt[k][b]) Xbar[k'][a])
+  const float4* rq = vx(2, kq, b);
+  const float4* Yq = vx(1, kq, b);
+  const float4 Ykb = vx(1, k, b)[0];
+  const float4 rkb = vx(2, k, b)[0];
+#pragma unroll
+  for (int a = 0; a < NB2; ++a) {
+    float4 g = G1[a * NB2 + b];
+    D::acc c = {make_float2(g.x, g.y), make_float2(g.z, g.w)};
+    const float4 Xka = vx(0, k, a)[0];
+    D::pmac(c, rq[0], df_bre(Xka));
+    D::pmac(c, rq[1], df_bim(Xka));
+    if (rev) {
+      const float4 ska = vx(3, k, a)[0];
+      D::pmac(c, Yq[0], df_bre(ska));
+      D::pmac(c, Yq[1], df_bim(ska));
+    }
+    D::renorm(c);
+    G1[a * NB2 + b] = make_float4(c.h.x, c.h.y, c.l.x, c.l.y);
+    g = G2[a * NB2 + b];
+    c = {make_float2(g.x, g.y), make_float2(g.z, g.w)};
+    const float4* sq = vx(3, kq, a);
+    D::pmac(c, sq[0], df_bre(Ykb));
+    D::pmac(c, sq[1], df_bim(Ykb));
+    if (rev) {
+      const float4* Xq = vx(0, kq, a);
+      D::pmac(c, Xq[0], df_bre(rkb));
+      D::pmac(c, Xq[1], df_bim(rkb));
+    }
+    D::renorm(c);
+    G2[a * NB2 + b] = make_float4(c.h.x, c.h.y, c.l.x, c.l.y);
+  }
+  if (rev) {
+    D::acc a3, a4;
+    D::zero(a3);
+    D::zero(a4);
+#pragma unroll
+    for (int a = 0; a < NB2; ++a) {
+      const float4 x = P2[a * NB2 + b];  // P2[a][b] Xbar[k'][a]
+      const float4* X = vx(0, kq, a);
+      D::pmac(a3, X[0], df_bre(x));
+      D::pmac(a3, X[1], df_bimn(x));
+      const float4 y = P1[b * NB2 + a];  // P1[b][a] Ybar[k'][a]
+      const float4* Y = vx(1, kq, a);
+      D::pmac(a4, Y[0], df_bre(y));
+      D::pmac(a4, Y[1], df_bimn(y));
+    }
+    double* r2 = rtb + ((size_t)k * NB2 + b) * 2;
+    double* s2 = stb + ((size_t)k * NB2 + b) * 2;
+    atomicAdd(r2, D::re_d(a3));
+    atomicAdd(r2 + 1, D::im_d(a3));
+    atomicAdd(s2, D::re_d(a4));
+    atomicAdd(s2 + 1, D::im_d(a4));
   }
 }
 

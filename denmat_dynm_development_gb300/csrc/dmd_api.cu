@@ -71,6 +71,8 @@ struct dmd_handle {
   int adj = 0;                 // DMD_FLAG_ADJOINT: pair operators also in stored order (d_Praw, d_kkraw)
   double2* d_Praw = nullptr;   // [npair][2][nb4] folded P1, P2
   int2* d_kkraw = nullptr;
+  float4* d_Padf = nullptr;    // adjoint of a double-float handle: the stored-order operators as double-floats
+  int padf_ok = 0;             // d_Padf matches the current operators
   int eek = 0;                 // DMD_FLAG_EE: d_Praw, d_kkraw and d_dst kept for the e-e model
   // sparse form (DMD_FLAG_SPARSE): per k-point the products of its output threads, lane-interleaved
   int use_sp = 0;
@@ -1301,7 +1303,7 @@ void release(dmd_handle* h) {
                   h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0, h->d_Praw, h->d_kkraw,
                   h->d_dst, h->d_ee_kvec, h->d_ee_kidx, h->d_ee_kmap, h->d_ee_U, h->d_ee_ewf, h->d_ee_f,
                   h->d_ee_dm, h->d_ee_dm1, h->d_ee_dmf, h->d_ee_dm1f, h->d_ee_scr, h->d_ee_Pee, h->d_ee_vqtab,
-                  h->d_sp_base, h->d_sp_len, h->d_sp_val, h->d_sp_gidx};
+                  h->d_sp_base, h->d_sp_len, h->d_sp_val, h->d_sp_gidx, h->d_Padf};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -1367,11 +1369,40 @@ int ee_rebuild_nb(dmd_handle* h, const double2* y, const TimeArg& ta, bool eq) {
 // ---------------------------------------------------------------------------------------------
 // adjoint (dmd_adjoint_rk4): work buffers, forward RK4 with stored stage inputs, one VJP
 // ---------------------------------------------------------------------------------------------
+// page-locked host buffer (freed on scope exit)
+struct PinnedStage {
+  void* p = nullptr;
+  bool alloc(size_t bytes) { return cudaHostAlloc(&p, bytes, cudaHostAllocDefault) == cudaSuccess; }
+  ~PinnedStage() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
+// memcpy split over host threads (first-touch page faults of a fresh destination run in parallel)
+void parallel_copy(void* dst, const void* src, size_t bytes) {
+  const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  if (bytes < (8u << 20) || nt == 1) {
+    memcpy(dst, src, bytes);
+    return;
+  }
+  std::vector<std::thread> th;
+  const size_t part = (bytes / nt + 4095) / 4096 * 4096;
+  for (unsigned i = 0; i < nt; ++i) {
+    const size_t b0 = (size_t)i * part;
+    if (b0 >= bytes) break;
+    const size_t nb = std::min(part, bytes - b0);
+    th.emplace_back([=] { memcpy((char*)dst + b0, (const char*)src + b0, nb); });
+  }
+  for (auto& t : th) t.join();
+}
+
 struct AdjWork {
   dmd_handle* h = nullptr;
   std::vector<void*> owned;
   double2 *ck = nullptr, *U = nullptr, *yb = nullptr, *ub = nullptr, *kb = nullptr, *tmp = nullptr;
   double2 *Xb = nullptr, *Yb = nullptr, *rt = nullptr, *st = nullptr, *rtb = nullptr, *stb = nullptr, *G = nullptr;
+  float4* dfv = nullptr;  // double-float form: (x, S(x)) of Xbar, Ybar, rt, st
+  double2* A = nullptr;    // forward sums (d_acc) at every stage input of the stretch being reversed
   ~AdjWork() {
     for (void* p : owned) cudaFree(p);
   }
@@ -1383,39 +1414,48 @@ struct AdjWork {
   }
 };
 
-// y_out = one RK4 step of y; the stage inputs u1..u4 go to U[0..3] (stride n) when U is set
-int adj_rk4_step(dmd_handle* h, const double2* y, double t, double dt, double2* U, double2* y_out, double2* tmp) {
-  const size_t n = h->nstate;
+// y_out = one RK4 step of y; the stage inputs u1..u4 go to U[0..3] (stride n) when U is set, and the
+// forward sums of the four evaluations (d_acc) to A[0..3] (stride nk 2 nb^2) when A is set
+int adj_rk4_step(dmd_handle* h, const double2* y, double t, double dt, double2* U, double2* y_out, double2* tmp,
+                 double2* A = nullptr) {
+  const size_t n = h->nstate, na = (size_t)h->nk * 2 * h->nb2;
   const unsigned g = blocks_for((long long)n, 256);
   double2* K = h->d_K;
   int rc;
+  auto keep = [&](int q) -> int {
+    if (A) CK(cudaMemcpyAsync(A + (size_t)q * na, h->d_acc, na * 16, cudaMemcpyDeviceToDevice, h->st));
+    return DMD_OK;
+  };
   if (U) CK(cudaMemcpyAsync(U, y, n * 16, cudaMemcpyDeviceToDevice, h->st));
-  if ((rc = rhs_plain(h, t, y, K))) return rc;
+  if ((rc = rhs_plain(h, t, y, K)) || (rc = keep(0))) return rc;
   double2* u = U ? U + n : tmp;
   k_axpy<<<g, 256, 0, h->st>>>(n, u, y, 0.5 * dt, K);
-  if ((rc = rhs_plain(h, t + 0.5 * dt, u, K + n))) return rc;
+  if ((rc = rhs_plain(h, t + 0.5 * dt, u, K + n)) || (rc = keep(1))) return rc;
   u = U ? U + 2 * n : tmp;
   k_axpy<<<g, 256, 0, h->st>>>(n, u, y, 0.5 * dt, K + n);
-  if ((rc = rhs_plain(h, t + 0.5 * dt, u, K + 2 * n))) return rc;
+  if ((rc = rhs_plain(h, t + 0.5 * dt, u, K + 2 * n)) || (rc = keep(2))) return rc;
   u = U ? U + 3 * n : tmp;
   k_axpy<<<g, 256, 0, h->st>>>(n, u, y, dt, K + 2 * n);
-  if ((rc = rhs_plain(h, t + dt, u, K + 3 * n))) return rc;
+  if ((rc = rhs_plain(h, t + dt, u, K + 3 * n)) || (rc = keep(3))) return rc;
   k_rk4_final<<<g, 256, 0, h->st>>>(n, y_out, y, K, n, dt);
   h->launches += 5;
   CKL();
   return DMD_OK;
 }
 
-// ybar += VJP_f(u, t)(vbar); kprev += c * VJP_f(u, t)(vbar) when kprev is set
+// ybar += VJP_f(u, t)(vbar); kprev += c * VJP_f(u, t)(vbar) when kprev is set. accs: the forward sums
+// at u kept when u was evaluated (the phases are then recomputed from t), or null to evaluate them
 template <int NB>
-int adj_vjp_nb(dmd_handle* h, AdjWork& w, const double2* u, double t, const double2* vbar, double2* kprev, double c) {
+int adj_vjp_nb(dmd_handle* h, AdjWork& w, const double2* u, double t, const double2* vbar, double2* kprev, double c,
+               const double2* accs) {
   int rc;
-  const TimeArg ta = time_value(t);
-  if ((rc = launch_prep<NB>(h, u, ta)) || (rc = launch_pairs<NB>(h))) return rc;  // forward sums at u
-  CK(cudaMemsetAsync(h->d_hflag, 0, sizeof(unsigned int), h->st));
+  if (!accs) {
+    const TimeArg ta = time_value(t);
+    if ((rc = launch_prep<NB>(h, u, ta)) || (rc = launch_pairs<NB>(h))) return rc;  // forward sums at u
+    CK(cudaMemsetAsync(h->d_hflag, 0, sizeof(unsigned int), h->st));
+  }
   const size_t nk2 = (size_t)h->nk * NB * NB;
-  CK(cudaMemsetAsync(w.rtb, 0, nk2 * 16, h->st));
-  CK(cudaMemsetAsync(w.stb, 0, nk2 * 16, h->st));
+  const double2* ph = (h->expt && !accs) ? h->d_ph : nullptr;
   AdjLocalArgs a;
   a.nk = h->nk;
   a.nbdm = h->nbdm;
@@ -1429,9 +1469,9 @@ int adj_vjp_nb(dmd_handle* h, AdjWork& w, const double2* u, double t, const doub
   a.t = t;
   a.u = u;
   a.vbar = vbar;
-  a.acc = h->d_acc;
+  a.acc = accs ? accs : h->d_acc;
   a.pos = h->use_cb ? h->d_pos : nullptr;
-  a.ph = h->expt ? h->d_ph : nullptr;
+  a.ph = ph;
   a.ew = h->d_ew;
   a.edm = h->d_edm;
   a.H = h->d_H;
@@ -1440,26 +1480,36 @@ int adj_vjp_nb(dmd_handle* h, AdjWork& w, const double2* u, double t, const doub
   a.rt = w.rt;
   a.st = w.st;
   a.ubar = w.ub;
+  a.rtb = w.rtb;  // zeroed by k_adj_local before the pair pass adds into them
+  a.stb = w.stb;
+  a.dfv = w.dfv;
+  a.nk2 = nk2;
   k_adj_local<NB><<<blocks_for(h->nk, 128), 128, 0, h->st>>>(a);
   if (h->npair > 0) {
-    const double2* P = h->use_cb ? h->d_Praw : h->d_P;
     const int2* kk = h->use_cb ? h->d_kkraw : h->d_kk;
-    k_adj_pairs<NB><<<blocks_for(h->npair * NB * NB, 128), 128, 0, h->st>>>(h->npair, kk, P, w.Xb, w.Yb, w.rt, w.st,
-                                                                           (double*)w.rtb, (double*)w.stb, w.G);
+    if (w.dfv) {  // double-float products on the FP32 pipes
+      k_adj_pairs_df<NB><<<blocks_for(h->npair * NB * NB, 128), 128, 0, h->st>>>(
+          h->npair, kk, h->d_Padf, w.dfv, nk2, (double*)w.rtb, (double*)w.stb, (float4*)w.G);
+    } else {
+      const double2* P = h->use_cb ? h->d_Praw : h->d_P;
+      k_adj_pairs<NB><<<blocks_for(h->npair * NB * NB, 128), 128, 0, h->st>>>(h->npair, kk, P, w.Xb, w.Yb, w.rt, w.st,
+                                                                             (double*)w.rtb, (double*)w.stb, w.G);
+    }
   }
   k_adj_combine<NB><<<blocks_for((long long)h->nstate, 256), 256, 0, h->st>>>(
-      h->nk, h->nbdm, h->bs, h->expt, t, h->d_ew, h->expt ? h->d_ph : nullptr, w.rtb, w.stb, w.ub, w.yb, kprev, c);
+      h->nk, h->nbdm, h->bs, h->expt, t, h->d_ew, ph, w.rtb, w.stb, w.ub, w.yb, kprev, c);
   h->launches += 3;
   CKL();
   return DMD_OK;
 }
 
-int adj_vjp(dmd_handle* h, AdjWork& w, const double2* u, double t, const double2* vbar, double2* kprev, double c) {
+int adj_vjp(dmd_handle* h, AdjWork& w, const double2* u, double t, const double2* vbar, double2* kprev, double c,
+            const double2* accs) {
   switch (h->nb) {
-    case 1: return adj_vjp_nb<1>(h, w, u, t, vbar, kprev, c);
-    case 2: return adj_vjp_nb<2>(h, w, u, t, vbar, kprev, c);
-    case 3: return adj_vjp_nb<3>(h, w, u, t, vbar, kprev, c);
-    case 4: return adj_vjp_nb<4>(h, w, u, t, vbar, kprev, c);
+    case 1: return adj_vjp_nb<1>(h, w, u, t, vbar, kprev, c, accs);
+    case 2: return adj_vjp_nb<2>(h, w, u, t, vbar, kprev, c, accs);
+    case 3: return adj_vjp_nb<3>(h, w, u, t, vbar, kprev, c, accs);
+    case 4: return adj_vjp_nb<4>(h, w, u, t, vbar, kprev, c, accs);
   }
   return fail(h, DMD_E_ARG, "nb out of range");
 }
@@ -2227,8 +2277,9 @@ int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64
     return DMD_E_ARG;
   if (slot < 0 || slot >= 8 || !h->d_obs[slot] || bstart < 0 || bend > h->nbdm || bstart > bend) return DMD_E_ARG;
   if (!h->adj) return fail(h, DMD_E_ARG, "dmd_adjoint_rk4 needs a handle created with DMD_FLAG_ADJOINT");
-  if (h->lin || h->d_eq || h->nrhs != 1)
-    return fail(h, DMD_E_ARG, "dmd_adjoint_rk4: linearized form, equilibrium drift and batches are not supported");
+  if (h->lin || h->d_eq || h->nrhs != 1 || h->ee_on)
+    return fail(h, DMD_E_ARG, "dmd_adjoint_rk4: linearized form, equilibrium drift, batches and an attached e-e "
+                              "model are not supported");
   for (int64_t i = 0; i < nobs; ++i)
     if (obs_step[i] < 0 || obs_step[i] > nsteps || (i > 0 && obs_step[i] < obs_step[i - 1]))
       return fail(h, DMD_E_ARG, "obs_step must be ascending in [0, nsteps]");
@@ -2243,8 +2294,22 @@ int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64
   if ((rc = w.get(&w.ck, (size_t)nseg * n)) || (rc = w.get(&w.U, (size_t)seglen * 4 * n)) || (rc = w.get(&w.yb, n)) ||
       (rc = w.get(&w.ub, n)) || (rc = w.get(&w.kb, 4 * n)) || (rc = w.get(&w.tmp, 3 * n)) || (rc = w.get(&w.Xb, nk2)) ||
       (rc = w.get(&w.Yb, nk2)) || (rc = w.get(&w.rt, nk2)) || (rc = w.get(&w.st, nk2)) || (rc = w.get(&w.rtb, nk2)) ||
-      (rc = w.get(&w.stb, nk2)) || (rc = w.get(&w.G, np)))
+      (rc = w.get(&w.stb, nk2)) || (rc = w.get(&w.G, np)) ||
+      (rc = w.get(&w.A, (size_t)seglen * 4 * (size_t)h->nk * 2 * h->nb2)))
     return rc;
+  const size_t na = (size_t)h->nk * 2 * h->nb2;
+  // double-float handles run the backward pair pass in double-float arithmetic (k_adj_pairs_df)
+  const bool dfb = h->prec == DMD_PREC_F64X;
+  if (dfb) {
+    if ((rc = w.get(&w.dfv, 8 * nk2))) return rc;
+    if (!h->d_Padf && (rc = dalloc(h, &h->d_Padf, np))) return rc;
+    if (!h->padf_ok && np) {
+      k_p_to_df<<<blocks_for((long long)np, 256), 256, 0, h->st>>>(np, h->use_cb ? h->d_Praw : h->d_P, h->d_Padf);
+      h->launches++;
+      CKL();
+      h->padf_ok = 1;
+    }
+  }
   CK(cudaMemsetAsync(w.G, 0, (np ? np : 1) * 16, h->st));
   CK(cudaMemsetAsync(w.yb, 0, n * 16, h->st));
   CK(cudaMemcpyAsync(w.ck, y0, n * 16, cudaMemcpyHostToDevice, h->st));
@@ -2278,7 +2343,9 @@ int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64
     const double2* y = w.ck + (size_t)sg * n;
     for (int64_t s = n0; s < n1; ++s) {  // stage inputs of the stretch
       double2* out = spare[sp];
-      if ((rc = adj_rk4_step(h, y, t0 + (double)s * dt, dt, w.U + (size_t)(s - n0) * 4 * n, out, w.tmp))) return rc;
+      if ((rc = adj_rk4_step(h, y, t0 + (double)s * dt, dt, w.U + (size_t)(s - n0) * 4 * n, out, w.tmp,
+                             w.A + (size_t)(s - n0) * 4 * na)))
+        return rc;
       y = out;
       sp ^= 1;
     }
@@ -2294,10 +2361,11 @@ int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64
       h->launches += 4;
       CKL();
       const double2* U = w.U + (size_t)(s - n0) * 4 * n;
-      if ((rc = adj_vjp(h, w, U + 3 * n, t + dt, w.kb + 3 * n, w.kb + 2 * n, dt)) ||
-          (rc = adj_vjp(h, w, U + 2 * n, t + 0.5 * dt, w.kb + 2 * n, w.kb + n, 0.5 * dt)) ||
-          (rc = adj_vjp(h, w, U + n, t + 0.5 * dt, w.kb + n, w.kb, 0.5 * dt)) ||
-          (rc = adj_vjp(h, w, U, t, w.kb, nullptr, 0.0)))
+      const double2* As = w.A + (size_t)(s - n0) * 4 * na;  // forward sums of the four stages
+      if ((rc = adj_vjp(h, w, U + 3 * n, t + dt, w.kb + 3 * n, w.kb + 2 * n, dt, As + 3 * na)) ||
+          (rc = adj_vjp(h, w, U + 2 * n, t + 0.5 * dt, w.kb + 2 * n, w.kb + n, 0.5 * dt, As + 2 * na)) ||
+          (rc = adj_vjp(h, w, U + n, t + 0.5 * dt, w.kb + n, w.kb, 0.5 * dt, As + na)) ||
+          (rc = adj_vjp(h, w, U, t, w.kb, nullptr, 0.0, As)))
         return rc;
     }
   }
@@ -2306,21 +2374,32 @@ int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64
                                      obs_weight[j] * h->obs_prefac[slot], w.yb);
     h->launches++;
   }
+  if (dJdP && np) {  // device G is [pair][P1 | P2][nb4] with dJ = Re sum(dP o G): conj(G) in FP64 in place
+    if (dfb) k_df_to_f64<<<blocks_for((long long)np, 256), 256, 0, h->st>>>(np, (float4*)w.G, 1);
+    else k_conj<<<blocks_for((long long)np, 256), 256, 0, h->st>>>(np, w.G);
+    h->launches++;
+  }
   CKL();
   if (dJdy0) CK(cudaMemcpyAsync(dJdy0, w.yb, n * 16, cudaMemcpyDeviceToHost, h->st));
-  std::vector<double> g(dJdP ? 2 * np : 0);
-  if (dJdP && np) CK(cudaMemcpyAsync(g.data(), w.G, np * 16, cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  if (dJdP) {  // device G is [pair][P1 | P2][nb4] with dJ = Re sum(dP o G); out: dJ/dRe P = Re G, dJ/dIm P = -Im G
-    const size_t nb4 = h->nb4, npair = (size_t)h->npair;
-    for (size_t p = 0; p < npair; ++p)
-      for (size_t m = 0; m < 2; ++m)
-        for (size_t e = 0; e < nb4; ++e) {
-          const size_t src = (p * 2 + m) * nb4 + e, dst = (m * npair + p) * nb4 + e;
-          dJdP[2 * dst] = g[2 * src];
-          dJdP[2 * dst + 1] = -g[2 * src + 1];
-        }
+  if (dJdP && np) {  // out: [P1 | P2][pair][nb4], dJ/dRe P = Re G, dJ/dIm P = -Im G: each half gathered on
+                     // the device in chunks and copied contiguously
+    const size_t nb4 = (size_t)h->nb4, npair = (size_t)h->npair;
+    const size_t chunk = std::max<size_t>(1, std::min<size_t>(npair, (256u << 20) / (nb4 * 16)));
+    double2* tmp = nullptr;
+    if ((rc = w.get(&tmp, chunk * nb4))) return rc;
+    PinnedStage stage;  // page-locked staging, then a threaded copy into the caller's (pageable) array
+    if (!stage.alloc(chunk * nb4 * 16)) return fail(h, DMD_E_NOMEM, "dmd_adjoint_rk4: page-locked staging buffer");
+    for (int m = 0; m < 2; ++m)
+      for (size_t p0 = 0; p0 < npair; p0 += chunk) {
+        const size_t cnt = std::min(chunk, npair - p0);
+        k_gather_half<<<blocks_for((long long)(cnt * nb4), 256), 256, 0, h->st>>>(cnt * nb4, nb4, w.G + p0 * 2 * nb4, m, tmp);
+        h->launches++;
+        CK(cudaMemcpyAsync(stage.p, tmp, cnt * nb4 * 16, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        parallel_copy(dJdP + 2 * ((size_t)m * npair + p0) * nb4, stage.p, cnt * nb4 * 16);
+      }
   }
+  CK(cudaStreamSynchronize(h->st));
   unsigned int derr = 0;
   CK(cudaMemcpy(&derr, h->d_err, sizeof(derr), cudaMemcpyDeviceToHost));
   if (derr) {
@@ -2565,6 +2644,7 @@ int dmd_add_operators(dmd_handle* h, const double* P1_add, const double* P2_add,
     }
   }
   cudaFree(tmp);
+  h->padf_ok = 0;
   if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("dmd_add_operators: ") + cudaGetErrorString(e));
   // the stored form again from the updated operators (and, in the deviation forms, the constant term)
   const bool dev = deviation_form(h->prec);

@@ -89,6 +89,29 @@ def test_adjoint_directional_derivatives_vs_fd(case, oracle, built):
     assert abs(ad - fd) <= TOL * abs(fd)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_schrod", "nb4_eimp_B"])
+def test_double_float_backward_matches_fp64(case, oracle, built):
+    """a double-float ("f64x") handle runs the backward pair pass in double-float arithmetic
+    (k_adj_pairs_df, gradient kept as double-floats): its dJ/dP and dJ/dy0 equal the FP64 handle's
+    (k_adj_pairs) to the forms' accuracy, far inside the adjoint's 1e-5"""
+    s = oracle.load(os.path.join(GOLDEN, case))
+    rng = np.random.default_rng(5)
+    dt = 2.0 * oracle.fs
+    steps = np.array([0, 9, 20, 33])
+    w = rng.standard_normal(steps.size)
+    y0 = oracle.y_of(s.dm0)
+    out = {}
+    for prec in ("f64", "f64x"):
+        with _gpu(s, adjoint=True, precision=prec) as g:
+            out[prec] = g.adjoint_rk4(s.t0, y0, dt, int(steps[-1]), steps, w, slot=0, bstart=s.nv_dm, checkpoint=7,
+                                      want_dy0=True)
+    (s64, dP64, dy64), (sdf, dPdf, dydf) = out["f64"], out["f64x"]
+    e_s, e_p, e_y = rel(sdf, s64), rel(dPdf, dP64), rel(dydf, dy64)
+    print("%s f64x vs f64 adjoint: S %.3g dJ/dP %.3g dJ/dy0 %.3g" % (case, e_s, e_p, e_y))
+    assert e_s < 1e-11 and e_p < 1e-9 and e_y < 1e-9
+
+
 def _mode_model(oracle, tmp_path, nb=2, nk=60, nsteps=60):
     """a synthetic system whose operators are sum_m theta_m P^(m): 6 phonon modes + impurities"""
     from denmat_dynm_development_gb300.adjoint import ModeScaledRK4
