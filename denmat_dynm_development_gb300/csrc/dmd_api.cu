@@ -85,6 +85,8 @@ struct dmd_handle {
   // e-e model (dmd_ee_attach): P = P_base (d_Praw) + ee_scale P_ee, rebuilt from rho
   int ee_on = 0, ee_every = 0, ee_update = 0, ee_nv = 0;
   double ee_scale = 1, ee_nfree0 = 0, ee_nkfull = 1, ee_cell = 1, ee_eps = 1, ee_T = 1, ee_meff = 1;
+  double ee_eppa = 0, ee_smear = 0;  // plasmon pole: energy and smearing in use
+  int ee_gn = 1;
   dmd::EeArgs ee_args;
   double* d_ee_kvec = nullptr;
   int4* d_ee_kidx = nullptr;
@@ -98,6 +100,8 @@ struct dmd_handle {
   float4* d_ee_dm1f = nullptr;
   dmd::EeScreen* d_ee_scr = nullptr;
   double* d_ee_vqtab = nullptr;  // static RPA vq by q mesh index
+  double2* d_ee_Aq = nullptr;     // plasmon-pole A(q), E^2(q) by q mesh index
+  double2* d_ee_Eq2 = nullptr;
   double2* d_ee_Pee = nullptr;
   float2* d_x0y0 = nullptr;    // tensor-core form: contraction of diag(f_ref), back-transformed, by k
   float2* d_v0 = nullptr;      // tensor-core form: (prefac/2)(C0 + C0^dagger) by k
@@ -1303,7 +1307,7 @@ void release(dmd_handle* h) {
                   h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0, h->d_Praw, h->d_kkraw,
                   h->d_dst, h->d_ee_kvec, h->d_ee_kidx, h->d_ee_kmap, h->d_ee_U, h->d_ee_ewf, h->d_ee_f,
                   h->d_ee_dm, h->d_ee_dm1, h->d_ee_dmf, h->d_ee_dm1f, h->d_ee_scr, h->d_ee_Pee, h->d_ee_vqtab,
-                  h->d_sp_base, h->d_sp_len, h->d_sp_val, h->d_sp_gidx, h->d_Padf};
+                  h->d_sp_base, h->d_sp_len, h->d_sp_val, h->d_sp_gidx, h->d_Padf, h->d_ee_Aq, h->d_ee_Eq2};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -1347,8 +1351,13 @@ int ee_rebuild(dmd_handle* h, const double2* y, const TimeArg& ta, bool eq) {
   // FP64 handles contract in FP64, the others in double-float on the FP32 pipes
   constexpr int WPC = ee_warps_per_cta(NB);
   const unsigned grid = (unsigned)((h->npair + WPC - 1) / WPC);
-  if (h->prec == DMD_PREC_F64) k_ee_pairs<NB, EeF64><<<grid, 32 * WPC, 0, h->st>>>(a);
-  else k_ee_pairs<NB, EeDF><<<grid, 32 * WPC, 0, h->st>>>(a);
+  if (h->prec == DMD_PREC_F64) {
+    if (a.dynamic) k_ee_pairs<NB, EeF64, true><<<grid, 32 * WPC, 0, h->st>>>(a);
+    else k_ee_pairs<NB, EeF64><<<grid, 32 * WPC, 0, h->st>>>(a);
+  } else {
+    if (a.dynamic) k_ee_pairs<NB, EeDF, true><<<grid, 32 * WPC, 0, h->st>>>(a);
+    else k_ee_pairs<NB, EeDF><<<grid, 32 * WPC, 0, h->st>>>(a);
+  }
   const bool dev = deviation_form(h->prec) && !h->lin;
   if (dev && cudaMemsetAsync(h->d_acc0, 0, (size_t)h->nk * 2 * NB2 * sizeof(double2), h->st) != cudaSuccess)
     return fail(h, DMD_E_CUDA, "e-e refill");
@@ -2800,8 +2809,13 @@ int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
   if (ee->nbw < h->nb || !ee->kvec || !ee->U || !ee->f || ee->kmesh[0] < 1 || ee->kmesh[1] < 1 || ee->kmesh[2] < 1 ||
       ee->formula < DMD_SCREEN_UNSCREENED || ee->formula > DMD_SCREEN_RPA || !(ee->degauss > 0) ||
       !(ee->ethr >= 0) || !(ee->cell_size > 0) || !(ee->nk_full > 0) || !(ee->temperature > 0) ||
-      !(ee->eps_background >= 1) || !(ee->meff > 0))
+      !(ee->eps_background >= 1) || !(ee->meff > 0) || ee->dynamic < 0 || ee->dynamic > 1 || !(ee->eppa >= 0) ||
+      !(ee->smearing >= 0))
     return fail(h, DMD_E_ARG, "e-e model description");
+  if (ee->dynamic && ee->formula != DMD_SCREEN_RPA)  // Scatt_Param.h:28-29
+    return fail(h, DMD_E_ARG, "plasmon-pole screening needs the RPA formula (debye and Bechstedt are static)");
+  if (!ee->dynamic && ee->two_freqs)
+    return fail(h, DMD_E_ARG, "only for dynamic screening, dynamic_screening_ee_two_freqs can be true");
   CK(cudaSetDevice(h->dev));
   const int nk = h->nk, nb = h->nb;
   const size_t nmesh = (size_t)ee->kmesh[0] * ee->kmesh[1] * ee->kmesh[2];
@@ -2873,6 +2887,15 @@ int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
   a.thr32 = (float)(ee->ethr + margin);
   a.scr = h->d_ee_scr;
   a.Pee = h->d_ee_Pee;
+  // plasmon pole: eppa defaults to the plasma frequency of the set-up density (init_RPA,
+  // Coulomb_Model.h:572-573), the smearing to 0.5 T except for Godby-Needs (:523)
+  const double eppa = ee->eppa == 0 ? std::sqrt(4 * M_PI * ee->nfree / ee->meff / ee->eps_background) : ee->eppa;
+  a.dynamic = ee->dynamic ? 1 : 0;
+  a.two_freqs = ee->two_freqs ? 1 : 0;
+  a.smearing = (ee->dynamic && ee->ppa_gn) ? ee->smearing : (ee->smearing <= 0 ? 0.5 * ee->temperature : ee->smearing);
+  h->ee_eppa = eppa;
+  h->ee_smear = a.smearing;
+  h->ee_gn = ee->ppa_gn ? 1 : 0;
   h->ee_every = ee->every_rhs ? 1 : 0;
   h->ee_update = ee->update_screening ? 1 : 0;
   h->ee_nv = ee->nv;
@@ -2883,23 +2906,36 @@ int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
   h->ee_eps = ee->eps_background;
   h->ee_T = ee->temperature;
   h->ee_meff = ee->meff;
-  if (ee->formula == DMD_SCREEN_RPA) {  // the static RPA table from the set-up occupations
+  if (ee->formula == DMD_SCREEN_RPA) {  // the RPA table from the set-up occupations (+ plasmon-pole terms)
     double* qacc = nullptr;
+    double* qacc1 = nullptr;  // Godby-Needs: the sums at i eppa
     unsigned int* qhit = nullptr;
-    if ((rc = dalloc(h, &h->d_ee_vqtab, nmesh)) || (rc = dalloc(h, &qacc, nmesh)) || (rc = dalloc(h, &qhit, nmesh))) {
+    const bool gn = ee->dynamic && ee->ppa_gn;
+    if ((rc = dalloc(h, &h->d_ee_vqtab, nmesh)) || (rc = dalloc(h, &qacc, nmesh)) || (rc = dalloc(h, &qhit, nmesh)) ||
+        (gn && (rc = dalloc(h, &qacc1, 2 * nmesh))) ||
+        (ee->dynamic && ((rc = dalloc(h, &h->d_ee_Aq, nmesh)) || (rc = dalloc(h, &h->d_ee_Eq2, nmesh))))) {
       cudaFree(qacc);
+      cudaFree(qacc1);
+      cudaFree(qhit);
       return rc;
     }
     a.vqtab = h->d_ee_vqtab;
+    a.Aq = h->d_ee_Aq;
+    a.Eq2 = h->d_ee_Eq2;
     cudaMemsetAsync(qacc, 0, nmesh * 8, h->st);
     cudaMemsetAsync(qhit, 0, nmesh * 4, h->st);
+    if (qacc1) cudaMemsetAsync(qacc1, 0, 2 * nmesh * 8, h->st);
     const long long npp = (long long)nk * nk;
-    if (nb == 2) k_ee_rpa_sum<2><<<blocks_for(npp, 256), 256, 0, h->st>>>(a, ee->temperature, h->d_ee_f, qacc, qhit);
-    else k_ee_rpa_sum<4><<<blocks_for(npp, 256), 256, 0, h->st>>>(a, ee->temperature, h->d_ee_f, qacc, qhit);
-    k_ee_rpa_table<<<blocks_for((long long)nmesh, 256), 256, 0, h->st>>>(a, 4 * M_PI / ee->eps_background / ee->cell_size,
-                                                                        ee->nk_full, qacc, qhit, h->d_ee_vqtab);
+    if (nb == 2)
+      k_ee_rpa_sum<2><<<blocks_for(npp, 256), 256, 0, h->st>>>(a, ee->temperature, h->d_ee_f, qacc, qhit, eppa, qacc1);
+    else
+      k_ee_rpa_sum<4><<<blocks_for(npp, 256), 256, 0, h->st>>>(a, ee->temperature, h->d_ee_f, qacc, qhit, eppa, qacc1);
+    k_ee_rpa_table<<<blocks_for((long long)nmesh, 256), 256, 0, h->st>>>(
+        a, 4 * M_PI / ee->eps_background / ee->cell_size, ee->nk_full, qacc, qhit, h->d_ee_vqtab, eppa, qacc1,
+        h->d_ee_Aq, h->d_ee_Eq2);
     const cudaError_t e = cudaStreamSynchronize(h->st);
     cudaFree(qacc);
+    cudaFree(qacc1);
     cudaFree(qhit);
     if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("RPA screening: ") + cudaGetErrorString(e));
     h->launches += 2;
@@ -2937,8 +2973,13 @@ int ee_linear_nb(dmd_handle* h, const double* d_f, double2* d_p) {
   a.f = d_f;
   constexpr int WPC = ee_warps_per_cta(NB);
   const unsigned grid = (unsigned)((h->npair + WPC - 1) / WPC);
-  if (h->prec == DMD_PREC_F64) k_ee_pairs<NB, EeF64><<<grid, 32 * WPC, 0, h->st>>>(a);
-  else k_ee_pairs<NB, EeDF><<<grid, 32 * WPC, 0, h->st>>>(a);
+  if (h->prec == DMD_PREC_F64) {
+    if (a.dynamic) k_ee_pairs<NB, EeF64, true><<<grid, 32 * WPC, 0, h->st>>>(a);
+    else k_ee_pairs<NB, EeF64><<<grid, 32 * WPC, 0, h->st>>>(a);
+  } else {
+    if (a.dynamic) k_ee_pairs<NB, EeDF, true><<<grid, 32 * WPC, 0, h->st>>>(a);
+    else k_ee_pairs<NB, EeDF><<<grid, 32 * WPC, 0, h->st>>>(a);
+  }
   const size_t n = (size_t)h->npair * NB4;
   k_ee_p36<NB><<<(unsigned)h->npair, NB == 4 ? 256 : 32, 0, h->st>>>(a, d_f, d_p, d_p + n, d_p + 2 * n, d_p + 3 * n);
   h->launches += 2;
@@ -2953,6 +2994,8 @@ int dmd_ee_linear_terms(dmd_handle* h, const double* f_eq, double nfree, double*
                         double* P4, double* P5, double* P6) {
   if (!h || !f_eq) return DMD_E_ARG;
   if (!h->ee_on) return fail(h, DMD_E_STATE, "no e-e model attached");
+  if (h->ee_args.dynamic)
+    return fail(h, DMD_E_ARG, "the linearized e-e terms are restated with static screening only");
   if (h->npair == 0) return DMD_OK;
   CK(cudaSetDevice(h->dev));
   const size_t nb4 = (size_t)h->nb4, np = (size_t)h->npair;

@@ -60,6 +60,11 @@ struct EeArgs {
   const EeScreen* scr;
   const double* vqtab;               // [n0 n1 n2] static RPA vq by the q mesh index (EE_RPA)
   double2* Pee;                      // [npair][2][nb^4]: P1ee, P2ee (prefactor included)
+  // plasmon-pole screening (dynamic): vq(q, w) per matrix element from A(q), E^2(q) by q mesh index
+  int dynamic, two_freqs;
+  double smearing;
+  const double2* Aq;
+  const double2* Eq2;
 };
 
 // wrap to [-0.5, 0.5) (comm/kmap.h:6-15) and |q|^2 in the reciprocal metric (comm/matrix3.h:119-121)
@@ -97,6 +102,37 @@ __device__ __forceinline__ double ee_vq(const EeArgs& a, const EeScreen& s, int 
   return s.prefac_vq_bare / epsq / q2;
 }
 
+// a / b as scalar.h computes it: complex(a.x b.x + a.y b.y, a.y b.x - a.x b.y) times 1 / b.norm()
+__device__ __forceinline__ double2 ee_cdiv(double2 a, double2 b) {
+  const double r = 1.0 / (b.x * b.x + b.y * b.y);
+  return mk2((a.x * b.x + a.y * b.y) * r, (a.y * b.x - a.x * b.y) * r);
+}
+
+// coulomb_model::vq(q, w) with plasmon-pole screening (Coulomb_Model.h:659-687), q by its |q|^2 and
+// mesh index: the static value at w = 0, else (prefac_vq + A / (cw^2 - E^2)) / |q|^2 with
+// cw = |w| + i smearing, conjugated for w < 0
+__device__ __forceinline__ double2 ee_vq_dyn(const EeArgs& a, const EeScreen& s, double q2, size_t m, double w) {
+  if (q2 < 1e-20) return mk2(0, 0);
+  if (w == 0) return mk2(a.vqtab[m], 0);
+  const double cx = fabs(w), cy = a.smearing;
+  const double2 E = a.Eq2[m];
+  const double2 t = ee_cdiv(a.Aq[m], mk2(cx * cx - cy * cy - E.x, cy * cx + cx * cy - E.y));
+  const double rq = 1.0 / q2;
+  return mk2((t.x + s.prefac_vq) * rq, (w < 0 ? -t.y : t.y) * rq);
+}
+
+// the interaction factor of one matrix element (ElecElec_Model.h:96-110, 124-135): vq at the mean
+// energy transfer, or with the two-frequency option sqrt(|vq(wa)| |vq(wb)|) cis(mean phase)
+__device__ __forceinline__ double2 ee_vq_elem(const EeArgs& a, const EeScreen& s, double q2, size_t m, double wa,
+                                              double wb, double wmean) {
+  if (!a.two_freqs) return ee_vq_dyn(a, s, q2, m, wmean);
+  const double2 va = ee_vq_dyn(a, s, q2, m, wa), vb = ee_vq_dyn(a, s, q2, m, wb);
+  const double vabs = sqrt(sqrt(va.x * va.x + va.y * va.y) * sqrt(vb.x * vb.x + vb.y * vb.y));
+  double sn, cs;
+  sincos(0.5 * (atan2(va.y, va.x) + atan2(vb.y, vb.x)), &sn, &cs);
+  return mk2(cs * vabs, sn * vabs);
+}
+
 // element (c, d) of U_ki^dag U_kj (elecelec_model::calc_ovlp, ElecElec_Model.h:72-80)
 template <int NB>
 __device__ __forceinline__ double2 ee_ovlp(const EeArgs& a, int ki, int kj, int c, int d) {
@@ -126,9 +162,11 @@ __device__ __forceinline__ double ee_ovlp_part(const EeArgs& a, int ki, int kj, 
 // static RPA screening (Coulomb_Model.h:690-736): one thread per ordered pair (i, j) of k-points adds
 // sum_(b1,b2) dfde |<i b1|j b2>|^2 to the accumulator of the mesh index of q = k_i - k_j (FP64
 // atomics), with dfde = (f_j - f_i) / (e_i - e_j), or (1 - f) f / T at degenerate energies
+// With eppa > 0 (Godby-Needs plasmon pole, Coulomb_Model.h:794-819) the sums at w = i eppa as well:
+// dfde = (f_j - f_i) / (e_i - e_j - i eppa) into qacc1 (complex).
 template <int NB>
 __global__ void k_ee_rpa_sum(EeArgs a, double T, const double* __restrict__ f, double* __restrict__ qacc,
-                             unsigned int* __restrict__ qhit) {
+                             unsigned int* __restrict__ qhit, double eppa = 0.0, double* __restrict__ qacc1 = nullptr) {
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (idx >= (long long)a.nk * a.nk) return;
   const int i = (int)(idx / a.nk), j = (int)(idx % a.nk);
@@ -136,6 +174,7 @@ __global__ void k_ee_rpa_sum(EeArgs a, double T, const double* __restrict__ f, d
   // the k-point of this mesh index as the table keeps it (a duplicate index is served by its first k)
   if (a.kmap[((size_t)vj.x * a.kmesh[1] + vj.y) * a.kmesh[2] + vj.z] != j) return;
   double g = 0;
+  double2 g1 = mk2(0, 0);
 #pragma unroll
   for (int b1 = 0; b1 < NB; ++b1)
 #pragma unroll
@@ -149,20 +188,40 @@ __global__ void k_ee_rpa_sum(EeArgs a, double T, const double* __restrict__ f, d
         dfde = (f[(size_t)j * NB + b2] - f[(size_t)i * NB + b1]) / de;
       }
       const double2 o = ee_ovlp<NB>(a, i, j, b1, b2);
-      g += dfde * (o.x * o.x + o.y * o.y);
+      const double n2 = o.x * o.x + o.y * o.y;
+      g += dfde * n2;
+      if (qacc1) {
+        const double2 d1 = ee_cdiv(mk2(f[(size_t)j * NB + b2] - f[(size_t)i * NB + b1], 0), mk2(de, -eppa));
+        g1.x += d1.x * n2;
+        g1.y += d1.y * n2;
+      }
     }
   const size_t m = ee_qmesh(a.kmesh, vi, vj);
   atomicAdd(&qacc[m], g);
+  if (qacc1) {
+    atomicAdd(&qacc1[2 * m], g1.x);
+    atomicAdd(&qacc1[2 * m + 1], g1.y);
+  }
   qhit[m] = 1u;
 }
 
 // vq = prefac_vq / (|q|^2 + qscr2) for every q mesh index that occurs (Coulomb_Model.h:819-826);
 // |q|^2 from the mesh index wrapped to [-0.5, 0.5)
+// With ppa (Aq set): the plasmon-pole terms of calc_vq_RPA (Coulomb_Model.h:855-874), eps^-1(w) =
+// 1 + A / (w^2 - E^2): Hybertsen-Louie (qacc1 null) A = prefac_vq wp2, E^2 = wp2 (1 + |q|^2 / qscr2);
+// Godby-Needs from eps^-1 at 0 and at i eppa: E^2 = wp2 (1 - epspinv) / (epspinv - eps0inv),
+// A = prefac_vq (1 - eps0inv) E^2; wp2 = eppa^2, zero at Gamma.
 __global__ void k_ee_rpa_table(EeArgs a, double prefac_vq, double nk_full, const double* __restrict__ qacc,
-                               const unsigned int* __restrict__ qhit, double* __restrict__ vqtab) {
+                               const unsigned int* __restrict__ qhit, double* __restrict__ vqtab,
+                               double eppa = 0.0, const double* __restrict__ qacc1 = nullptr,
+                               double2* __restrict__ Aq = nullptr, double2* __restrict__ Eq2 = nullptr) {
   const size_t n = (size_t)a.kmesh[0] * a.kmesh[1] * a.kmesh[2];
   const size_t m = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (m >= n) return;
+  if (Aq) {
+    Aq[m] = mk2(0, 0);
+    Eq2[m] = mk2(0, 0);
+  }
   if (!qhit[m]) {
     vqtab[m] = 0.0;
     return;
@@ -171,6 +230,22 @@ __global__ void k_ee_rpa_table(EeArgs a, double prefac_vq, double nk_full, const
   const double q2 = ee_q2(a, (double)m0 / a.kmesh[0], (double)m1 / a.kmesh[1], (double)m2 / a.kmesh[2]);
   const double qs = prefac_vq / nk_full * qacc[m];
   vqtab[m] = q2 < 1e-20 ? 0.0 : prefac_vq / (q2 + qs);
+  if (!Aq || q2 < 1e-20) return;
+  const double wp2 = eppa * eppa;
+  if (!qacc1) {  // Hybertsen-Louie
+    const double2 t = ee_cdiv(mk2(q2, 0), mk2(qs, 0));
+    Aq[m] = mk2(prefac_vq * wp2, 0);
+    Eq2[m] = mk2((t.x + 1) * wp2, t.y * wp2);
+  } else {  // Godby-Needs
+    const double sc = prefac_vq / nk_full, rq = 1.0 / q2;
+    const double2 qs1 = mk2(sc * qacc1[2 * m], sc * qacc1[2 * m + 1]);
+    const double2 e0 = ee_cdiv(mk2(1, 0), mk2(qs * rq + 1, 0));
+    const double2 ep = ee_cdiv(mk2(1, 0), mk2(qs1.x * rq + 1, qs1.y * rq));
+    const double2 E = ee_cdiv(mk2((-ep.x + 1) * wp2, -ep.y * wp2), mk2(ep.x - e0.x, ep.y - e0.y));
+    const double2 c = mk2((-e0.x + 1) * prefac_vq, -e0.y * prefac_vq);
+    Eq2[m] = E;
+    Aq[m] = mk2(c.x * E.x - c.y * E.y, c.x * E.y + c.y * E.x);
+  }
 }
 
 // the window density matrix in the Schrodinger picture and 1 - rho from the state y (one thread per
@@ -376,7 +451,9 @@ struct EeSmem {
 // warps (pairs) per CTA: nb = 4 keeps 2 so that the per-lane scratch fits the static shared memory
 __host__ __device__ constexpr int ee_warps_per_cta(int nb) { return nb == 4 ? 2 : 4; }
 
-template <int NB, typename V = EeF64>
+// DYN: plasmon-pole screening (a.dynamic); a separate instantiation so that the static kernel keeps
+// its registers and occupancy
+template <int NB, typename V = EeF64, bool DYN = false>
 __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF) ? 7 : 1) k_ee_pairs(EeArgs a) {
   typedef EeSmem<NB, V> S;
   typedef typename V::c C;
@@ -397,8 +474,14 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
     return;
   }
   const EeScreen scr = *a.scr;
+  // plasmon-pole screening: the overlaps stay unscaled and each matrix element takes vq(q, w) (its
+  // |q|^2 and mesh index for q = k1 - k2 here, k1 - k4 per candidate)
+  const double q2_12 = DYN ? ee_q2(a, a.kvec[3 * k1] - a.kvec[3 * k2], a.kvec[3 * k1 + 1] - a.kvec[3 * k2 + 1],
+                                         a.kvec[3 * k1 + 2] - a.kvec[3 * k2 + 2])
+                                 : 0.0;
+  const size_t m_12 = DYN ? ee_qmesh(a.kmesh, a.kidx[k1], a.kidx[k2]) : 0;
   if (lane < NB2) {  // o12 = vq(k1 - k2) U_k1^dag U_k2
-    const double vq = ee_vq(a, scr, k1, k2);
+    const double vq = DYN ? 1.0 : ee_vq(a, scr, k1, k2);
     const double2 o = ee_ovlp<NB>(a, k1, k2, lane / NB, lane % NB);
     sm.o12[lane] = V::from(mk2(vq * o.x, vq * o.y));
   }
@@ -459,7 +542,7 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
         const int c = r / NB, d = r % NB;
         V::set_part(sm.o34[grp][r], w, ee_ovlp_part<NB>(a, ka, kb, c, d, w));
         if (a.antisym) {
-          const double vq = ee_vq(a, scr, k1, kb);
+          const double vq = DYN ? 1.0 : ee_vq(a, scr, k1, kb);
           V::set_part(sm.o14[grp][r], w, vq * ee_ovlp_part<NB>(a, k1, kb, c, d, w));
           V::set_part(sm.o32[grp][r], w, ee_ovlp_part<NB>(a, ka, k2, c, d, w));
         }
@@ -469,6 +552,13 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
         const double* e3 = a.ew + (size_t)ka * NB;
         const double* e4 = a.ew + (size_t)kb * NB;
         const C m12 = sm.o12[i1 * NB + i3];
+        double q2_14 = 0.0;
+        size_t m_14 = 0;
+        if (DYN && a.antisym) {
+          q2_14 = ee_q2(a, a.kvec[3 * k1] - a.kvec[3 * kb], a.kvec[3 * k1 + 1] - a.kvec[3 * kb + 1],
+                        a.kvec[3 * k1 + 2] - a.kvec[3 * kb + 2]);
+          m_14 = ee_qmesh(a.kmesh, a.kidx[k1], a.kidx[kb]);
+        }
         constexpr int HALF = NB2 / 2;  // both halves of the group share the row's elements
 #pragma unroll 1
         for (int h = 0; h < HALF; ++h) {  // rolled: one copy of the exp in the code
@@ -476,8 +566,20 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
           const double de = e1[i1] - e2[i3] + e3[c] - e4[d];  // the window test stays FP64
           C v = V::zero();
           if (fabs(de) < a.ethr) {
+            // plasmon pole: mee *= vq(k1 - k2, w) (calc_mee) and, with the exchange term, mee *=
+            // vq(k1 - k4, w_ex) (calc_mee_ex scales the direct term), the exchange term unscreened
+            double2 f12 = mk2(1, 0), f14 = mk2(1, 0);
+            if constexpr (DYN) {
+              f12 = ee_vq_elem(a, scr, q2_12, m_12, e1[i1] - e2[i3], e4[d] - e3[c], 0.5 * (e1[i1] - e2[i3] + e4[d] - e3[c]));
+              if (a.antisym)
+                f14 = ee_vq_elem(a, scr, q2_14, m_14, e1[i1] - e4[d], e2[i3] - e3[c], 0.5 * (e1[i1] - e4[d] + e2[i3] - e3[c]));
+            }
             if constexpr (V::kDF) {
               C mee = V::mul(m12, sm.o34[grp][cd]);
+              if constexpr (DYN) {
+                mee = V::mul(mee, V::from(f12));
+                if (a.antisym) mee = V::mul(mee, V::from(f14));
+              }
               if (a.antisym) {
                 const C mex = V::mul(sm.o14[grp][i1 * NB + d], sm.o32[grp][c * NB + i3]);
                 mee = make_float4(0.5f * mee.x, 0.5f * mee.y, 0.5f * mee.z, 0.5f * mee.w);  // exact halves
@@ -487,6 +589,10 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
               v = V::scale_df(mee, df_exp_neg(a.prefac_exp * (de * de)));
             } else {
               double2 mee = cmul_rn(m12, sm.o34[grp][cd]);
+              if constexpr (DYN) {
+                mee = cmul_rn(mee, f12);
+                if (a.antisym) mee = cmul_rn(mee, f14);
+              }
               if (a.antisym) {
                 const double2 mex = cmul_rn(sm.o14[grp][i1 * NB + d], sm.o32[grp][c * NB + i3]);
                 mee = mk2(-0.5 * mex.x + 0.5 * mee.x, -0.5 * mex.y + 0.5 * mee.y);

@@ -480,7 +480,19 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
       return err(DMD_E_ARG, "scrFormula lindhard has no static vq table in the reference (Coulomb_Model.h:537-545)");
     if (f != "unscreened" && f != "debye" && f != "Bechstedt" && f != "RPA")
       return err(DMD_E_ARG, "scrFormula " + f + " is not supported (unscreened, debye, Bechstedt, RPA are)");
-    if (sget(pm, "dynamic_screening", "static") != "static") return err(DMD_E_ARG, "only static screening is supported");
+    // dynamic screening (Scatt_Param.h:20-49): static, or the plasmon-pole approximation with RPA
+    const std::string dyn = sget(pm, "dynamic_screening", "static");
+    if (dyn != "static" && dyn != "ppa")
+      return err(DMD_E_ARG, "dynamic_screening " + dyn + " is not supported (static, ppa are)");
+    if (dyn == "static" && pget(pm, "dynamic_screening_ee_two_freqs", 0) != 0)
+      return err(DMD_E_ARG, "only for dynamic screening, dynamic_screening_ee_two_freqs can be true");
+    if (dyn != "static" && f != "RPA") return err(DMD_E_ARG, "debye and Bechstedt models are in static limit");
+    if (dyn != "static" && pget(pm, "alg_linearize", 0) != 0)
+      return err(DMD_E_ARG, "the linearized e-e source is supported with static screening only");
+    const std::string ppam = sget(pm, "ppamodel", "gn");
+    if (ppam != "gn" && ppam != "hl") return err(DMD_E_ARG, "ppamodel is invalid");
+    if (pget(pm, "eppa_screening", 0) < 0) return err(DMD_E_ARG, "eppa must >= 0");
+    if (pget(pm, "smearing_screening", 0) < 0) return err(DMD_E_ARG, "smearing must >= 0");
     if (pget(pm, "alg_ddmdteq", 0) != 0) return err(DMD_E_ARG, "the e-e model is not supported with alg_ddmdteq");
     if (pget(pm, "alg_summode", 1) == 0) return err(DMD_E_ARG, "the e-e model needs alg_summode");
     const double fe = pget(pm, "freq_update_ee_model", 0), fi = pget(pm, "freq_update_eimp_model", 0);
@@ -821,6 +833,11 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
     ee.antisymmetry = pget(pm, "ee_antisymmetry", 0) != 0;
     ee.scale = pget(pm, "scale_ee", scale_scatt);
     ee.every_rhs = s->ee == 1 && pget(pm, "freq_update_ee_model", 0) < 0;
+    ee.dynamic = sget(pm, "dynamic_screening", "static") == "ppa";  // parameters.cpp:196-204
+    ee.ppa_gn = sget(pm, "ppamodel", "gn") == "gn";
+    ee.eppa = pget(pm, "eppa_screening", 0);
+    ee.smearing = pget(pm, "smearing_screening", 0, kEV);
+    ee.two_freqs = pget(pm, "dynamic_screening_ee_two_freqs", 0) != 0;
   }
   if (linear) {
     // electronphonon::set_Lsc (ElectronPhonon_linear.cpp:3-31): the e-ph operators, each impurity's,

@@ -58,7 +58,8 @@ class _EEDesc(C.Structure):
                 ("temperature", C.c_double), ("eps_background", C.c_double), ("meff", C.c_double),
                 ("formula", C.c_int32), ("nfree", C.c_double), ("update_screening", C.c_int32), ("nv", C.c_int32),
                 ("degauss", C.c_double), ("ethr", C.c_double), ("antisymmetry", C.c_int32), ("scale", C.c_double),
-                ("every_rhs", C.c_int32)]
+                ("every_rhs", C.c_int32), ("dynamic", C.c_int32), ("ppa_gn", C.c_int32), ("eppa", C.c_double),
+                ("smearing", C.c_double), ("two_freqs", C.c_int32)]
 
 
 SCREEN = {"unscreened": 0, "debye": 1, "Bechstedt": 2, "RPA": 3}
@@ -195,9 +196,12 @@ class LindbladGPU:
 
     # ------------------------------------------------------------------ e-e model (eeMode = Pee_update)
     def ee_attach(self, *, kvec, kmesh, U, f, GGT, cell_size, nk_full, temperature, eps_background, meff, formula,
-                  nfree, update_screening, nv, degauss, ethr, antisymmetry, scale, every_rhs):
+                  nfree, update_screening, nv, degauss, ethr, antisymmetry, scale, every_rhs, dynamic=0, ppa_gn=1,
+                  eppa=0.0, smearing=0.0, two_freqs=0):
         """Attach the e-e model (dmd_ee_attach): U complex [nk][nbw][nb], kvec [nk][3] fractional,
-        f [nk][nb] window occupations of the set-up, formula "unscreened" / "debye" / "Bechstedt"."""
+        f [nk][nb] window occupations of the set-up, formula "unscreened" / "debye" / "Bechstedt" /
+        "RPA"; dynamic = 1 (or "ppa"): plasmon-pole screening (RPA), ppa_gn 1 Godby-Needs / 0
+        Hybertsen-Louie, eppa / smearing in Hartree (0: the reference's defaults)."""
         U = np.ascontiguousarray(U, np.complex128)
         keep = dict(kvec=np.ascontiguousarray(kvec, np.float64), U=U, f=np.ascontiguousarray(f, np.float64))
         d = _EEDesc(nbw=int(U.shape[1]), kvec=keep["kvec"].ctypes.data, kmesh=(C.c_int32 * 3)(*[int(x) for x in kmesh]),
@@ -206,7 +210,10 @@ class LindbladGPU:
                     nk_full=nk_full, temperature=temperature, eps_background=eps_background, meff=meff,
                     formula=SCREEN[formula] if isinstance(formula, str) else int(formula), nfree=nfree,
                     update_screening=int(update_screening), nv=int(nv), degauss=degauss, ethr=ethr,
-                    antisymmetry=int(antisymmetry), scale=scale, every_rhs=int(every_rhs))
+                    antisymmetry=int(antisymmetry), scale=scale, every_rhs=int(every_rhs),
+                    dynamic=(1 if dynamic == "ppa" else 0) if isinstance(dynamic, str) else int(dynamic),
+                    ppa_gn=(1 if ppa_gn == "gn" else 0) if isinstance(ppa_gn, str) else int(ppa_gn),
+                    eppa=float(eppa), smearing=float(smearing), two_freqs=int(two_freqs))
         self._ck(_lib().dmd_ee_attach(self._h, C.byref(d)))
 
     def ee_update(self):

@@ -111,7 +111,9 @@ class System:
                            cell_size=ed.cell_size, nk_full=ed.nk_full, temperature=ed.temperature,
                            eps_background=ed.eps_background, meff=ed.meff, formula=ed.formula, nfree=ed.nfree,
                            update_screening=ed.update_screening, nv=ed.nv, degauss=ed.degauss, ethr=ed.ethr,
-                           antisymmetry=ed.antisymmetry, scale=ed.scale, every_rhs=ed.every_rhs)
+                           antisymmetry=ed.antisymmetry, scale=ed.scale, every_rhs=ed.every_rhs,
+                           dynamic=ed.dynamic, ppa_gn=ed.ppa_gn, eppa=ed.eppa, smearing=ed.smearing,
+                           two_freqs=ed.two_freqs)
 
     def desc(self, precision="f64", device=0):
         d = _dmd._Desc()

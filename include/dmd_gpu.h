@@ -228,8 +228,9 @@ int dmd_peak_fma(int device, int fp64, double* tflops);
 #define DMD_SCREEN_UNSCREENED 0 /* clp.scrFormula = "unscreened" */
 #define DMD_SCREEN_DEBYE 1      /* "debye" */
 #define DMD_SCREEN_BECHSTEDT 2  /* "Bechstedt" */
-#define DMD_SCREEN_RPA 3        /* "RPA" with static screening: the q table of calc_qscr2_static_RPA
-                                   (Coulomb_Model.h:690-736, 819-826) from f and U, built at attach */
+#define DMD_SCREEN_RPA 3        /* "RPA": the q table of calc_qscr2_static_RPA (Coulomb_Model.h:690-736,
+                                   819-826) from f and U, built at attach (with the plasmon-pole
+                                   terms of calc_vq_RPA, :780-874, when dynamic) */
 
 typedef struct dmd_ee_desc {
   int32_t nbw;              /* Wannier functions (elec->nb_wannier) */
@@ -253,6 +254,15 @@ typedef struct dmd_ee_desc {
   int32_t antisymmetry;     /* eep.antisymmetry: the exchange term */
   double scale;             /* scale_ee */
   int32_t every_rhs;        /* freq_update_ee_model < 0: update before every RHS evaluation */
+  /* dynamic screening (clp.dynamic, Coulomb_Model.h:572-575, 780-874, 659-687; ElecElec_Model.h:
+   * 81-138): 0 static, 1 the plasmon-pole approximation ("ppa", DMD_SCREEN_RPA only). The
+   * interaction of each matrix element is vq(q, w) at its energy transfer, the exchange factor
+   * vq(k1 - k4, w_ex) applied as the reference applies it (to the direct term) */
+  int32_t dynamic;
+  int32_t ppa_gn;           /* clp.ppamodel: 1 "gn" (Godby-Needs), 0 "hl" (Hybertsen-Louie) */
+  double eppa;              /* clp.eppa (eppa_screening, Hartree); 0: the plasma frequency of nfree */
+  double smearing;          /* clp.smearing (smearing_screening, Hartree); <= 0: 0.5 T, except for gn */
+  int32_t two_freqs;        /* clp.dynamic_screening_ee_two_freqs */
 } dmd_ee_desc;
 
 int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee);

@@ -12,6 +12,7 @@
  * to the reference tree. complex128 arrays are interleaved (re, im) doubles, k-major, then
  * row-major nb x nb.
  */
+#define _GNU_SOURCE /* sincos (glibc), as scalar.h's cis calls it */
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -29,6 +30,12 @@ static inline zc zsub(zc a, zc b) { return zmk(a.x - b.x, a.y - b.y); }
 static inline zc zconj(zc a) { return zmk(a.x, -a.y); }
 static inline zc zscale(double s, zc a) { return zmk(a.x * s, a.y * s); } /* complex*double (scalar.h:96) */
 static inline zc zcis(double x) { return zmk(cos(x), sin(x)); }          /* cis (scalar.h:122-125) */
+/* a / b: complex(a.x b.x + a.y b.y, a.y b.x - a.x b.y) / b.norm(), the division by a double a
+ * multiplication by its reciprocal (scalar.h:98-101) */
+static inline zc zdiv(zc a, zc b) {
+  const double r = 1.0 / (b.x * b.x + b.y * b.y);
+  return zmk((a.x * b.x + a.y * b.y) * r, (a.y * b.x - a.x * b.y) * r);
+}
 
 /* ---------------------------------------------------------------------------------------------
  * System description (what DMD holds in electronphonon / singdenmat_k after setup).
@@ -81,6 +88,13 @@ typedef struct orc_ee {
   zc* P2ee;
   const double* f_setup;   /* [nk][nb] window occupations of the set-up (coul_model->f): static RPA */
   double* vq_rpa;          /* [n0 n1 n2] static RPA / Lindhard vq by the q mesh index (orc_ee_rpa_table) */
+  int dynamic;             /* clp.dynamic: 0 "static", 1 "ppa" (plasmon-pole approximation) */
+  int ppa_gn;              /* clp.ppamodel: 1 "gn" (Godby-Needs), 0 "hl" (Hybertsen-Louie) */
+  double eppa;             /* clp.eppa after init_RPA (the plasma frequency when given as 0) */
+  double smearing;         /* clp.smearing after Coulomb_Model.h:523 (0.5 T when <= 0, except gn) */
+  int two_freqs;           /* clp.dynamic_screening_ee_two_freqs */
+  zc* Aq_ppa;              /* [n0 n1 n2] by q mesh index: eps^-1(w) = 1 + A / (w^2 - E^2) (:855-874) */
+  zc* Eq2_ppa;
 } orc_ee;
 
 void orc_ee_rebuild(struct orc_ee* ee, const orc_sys* s, double t, const double* y);
@@ -520,6 +534,37 @@ static double ee_vq(const orc_ee* ee, const ee_scr* c, const double* q) {
   return c->prefac_vq_bare / epsq / q2;
 }
 
+/* coulomb_model::vq(q, w) with dynamic = ppa (Coulomb_Model.h:659-687): RPA / Lindhard only (the
+ * reference refuses the other formulas with dynamic screening); w = 0 gives the static value
+ * vq_RPA[iq][0].real(); otherwise (prefac_vq + A / (cw^2 - E^2)) / |q|^2 with cw = |w| + i smearing,
+ * conjugated for w < 0 (eps(q, -w) = eps(q, w)^*) */
+static zc ee_vq_dyn(const orc_ee* ee, const ee_scr* c, const double* q, double w) {
+  const double q2 = ee_q2(ee, q);
+  int v[3];
+  ee_ikvec3(ee, q, v);
+  const size_t m = ((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2];
+  if (q2 < 1e-20) return zmk(0, 0);
+  if (w == 0) return zmk(ee->vq_rpa[m], 0);
+  const zc cw = zmk(fabs(w), ee->smearing);
+  const zc t = zdiv(ee->Aq_ppa[m], zsub(zmk(cw.x * cw.x - cw.y * cw.y, cw.y * cw.x + cw.x * cw.y), ee->Eq2_ppa[m]));
+  const double rq = 1.0 / q2;
+  const zc r = zmk((t.x + c->prefac_vq) * rq, t.y * rq);
+  return w < 0 ? zconj(r) : r;
+}
+
+/* the interaction factor of one mee element (ElecElec_Model.h:96-110, 124-135): vq(q, w) at the mean
+ * energy transfer w = 0.5 (wa + wb), or with the two-frequency option sqrt(|vq(q, wa)| |vq(q, wb)|)
+ * cis of the mean phase */
+static zc ee_vq_elem(const orc_ee* ee, const ee_scr* c, const double* q, double wa, double wb, double wmean) {
+  if (!ee->two_freqs) return ee_vq_dyn(ee, c, q, wmean);
+  const zc va = ee_vq_dyn(ee, c, q, wa), vb = ee_vq_dyn(ee, c, q, wb);
+  const double vabs = sqrt(sqrt(va.x * va.x + va.y * va.y) * sqrt(vb.x * vb.x + vb.y * vb.y));
+  const double varg = 0.5 * (atan2(va.y, va.x) + atan2(vb.y, vb.x));
+  double sn, cs;
+  sincos(varg, &sn, &cs);
+  return zmk(cs * vabs, sn * vabs);
+}
+
 /* kIndexMap::ikvec3 -- comm/kmap.cpp:15-23 */
 static void ee_ikvec3(const orc_ee* ee, const double* k, int* v) {
   for (int d = 0; d < 3; d++) {
@@ -627,7 +672,48 @@ void orc_ee_rpa_table(orc_ee* ee, int nk, const double* e /* [nk][nb] */) {
     const double r = 1.0 / (dx * dx + dy * dy);
     int v[3];
     ee_ikvec3(ee, q, v);
-    ee->vq_rpa[((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2]] = (c.prefac_vq * dx + 0.0 * dy) * r;
+    const size_t m = ((size_t)v[0] * ee->kmesh[1] + v[1]) * ee->kmesh[2] + v[2];
+    ee->vq_rpa[m] = (c.prefac_vq * dx + 0.0 * dy) * r;
+    if (!ee->dynamic) continue;
+    /* plasmon pole (Coulomb_Model.h:780-874): Godby-Needs needs the sums at w = i eppa as well */
+    zc sum1 = zmk(0, 0);
+    if (ee->ppa_gn) {
+      for (int ik = 0; ik < nk; ik++) {
+        double kj[3];
+        for (int x = 0; x < 3; x++) kj[x] = ee->kvec[3 * ik + x] - q[x];
+        const int jk = ee_findk(ee, table, kj);
+        if (jk < 0) continue;
+        ee_ovlp(ee, &c, ovlp, Uih, ik, jk, 0);
+        for (int b1 = 0; b1 < nb; b1++)
+          for (int b2 = 0; b2 < nb; b2++) {
+            if (ee->formula == 4 && b1 != b2) continue;
+            /* de = e_i - e_j - i eppa; dfde = complex(f_j - f_i, 0) / de */
+            const zc de = zmk(e[ik * nb + b1] - e[jk * nb + b2], -ee->eppa);
+            const zc dfde = zdiv(zmk(ee->f_setup[jk * nb + b2] - ee->f_setup[ik * nb + b1], 0), de);
+            if (ee->formula == 3) {
+              const double n2 = ovlp[b1 * nb + b2].x * ovlp[b1 * nb + b2].x + ovlp[b1 * nb + b2].y * ovlp[b1 * nb + b2].y;
+              sum1 = zadd(sum1, zmk(dfde.x * n2, dfde.y * n2));
+            } else {
+              sum1 = zadd(sum1, dfde);
+            }
+          }
+      }
+      sum1 = zmul(zmk(c.prefac_vq / ee->nk_full, 0), sum1);
+    }
+    if (q2 < 1e-20) continue; /* Gamma skipped: A = E^2 = 0 */
+    const double wp2 = ee->eppa * ee->eppa;
+    if (!ee->ppa_gn) { /* Hybertsen-Louie */
+      ee->Aq_ppa[m] = zmk(c.prefac_vq * wp2, 0);
+      const zc t = zdiv(zmk(q2, 0), sum);
+      ee->Eq2_ppa[m] = zmk((t.x + 1) * wp2, t.y * wp2);
+    } else { /* Godby-Needs */
+      const double rq = 1.0 / q2;
+      const zc eps0inv = zdiv(zmk(1, 0), zmk(sum.x * rq + 1, sum.y * rq));
+      const zc epspinv = zdiv(zmk(1, 0), zmk(sum1.x * rq + 1, sum1.y * rq));
+      /* wp2 (1 - epspinv) / (epspinv - eps0inv); 1 - z is -z + 1 */
+      ee->Eq2_ppa[m] = zdiv(zmk((-epspinv.x + 1) * wp2, -epspinv.y * wp2), zsub(epspinv, eps0inv));
+      ee->Aq_ppa[m] = zmul(zmk((-eps0inv.x + 1) * c.prefac_vq, -eps0inv.y * c.prefac_vq), ee->Eq2_ppa[m]);
+    }
   }
   free(table); free(qseen); free(qvec); free(Uih); free(ovlp);
 }
@@ -670,7 +756,9 @@ void orc_ee_P(const orc_ee* ee, const orc_sys* s, const zc* dm, const zc* dm1, c
     }
     memset(P1, 0, sizeof(zc) * nb4);
     memset(P2, 0, sizeof(zc) * nb4);
-    ee_ovlp(ee, &c, o12, Uih, ik1, ik2, 1);
+    ee_ovlp(ee, &c, o12, Uih, ik1, ik2, !ee->dynamic);
+    double q12[3];
+    for (int d = 0; d < 3; d++) q12[d] = ee->kvec[3 * ik1 + d] - ee->kvec[3 * ik2 + d];
     for (int ik3 = 0; ik3 < nk; ik3++) {
       if (ee->antisym && ik1 == ik2 && ik2 == ik3) continue;
       double k4v[3];
@@ -697,16 +785,26 @@ void orc_ee_P(const orc_ee* ee, const orc_sys* s, const zc* dm, const zc* dm1, c
       /* calc_ovlps (ElecElec_Model.h:64-71; ovlp12 kept from above) and calc_mee / calc_mee_ex */
       ee_ovlp(ee, &c, o34, Uih, ik3, ik4, 0);
       if (ee->antisym) {
-        ee_ovlp(ee, &c, o14, Uih, ik1, ik4, 1);
+        ee_ovlp(ee, &c, o14, Uih, ik1, ik4, !ee->dynamic);
         ee_ovlp(ee, &c, o32, Uih, ik3, ik2, 0);
       }
+      double q14[3];
+      for (int d = 0; d < 3; d++) q14[d] = ee->kvec[3 * ik1 + d] - ee->kvec[3 * ik4 + d];
       for (int i1 = 0; i1 < nb; i1++)
         for (int i2 = 0; i2 < nb; i2++)
           for (int i3 = 0; i3 < nb; i3++)
             for (int i4 = 0; i4 < nb; i4++) {
               const int i1234 = ((i1 * nb + i2) * nb + i3) * nb + i4;
               mee[i1234] = zmul(o12[i1 * nb + i2], o34[i3 * nb + i4]);
-              if (ee->antisym) mex[i1234] = zmul(o14[i1 * nb + i4], o32[i3 * nb + i2]);
+              if (ee->dynamic) /* calc_mee: mee *= vq(k1 - k2, w) */
+                mee[i1234] = zmul(mee[i1234], ee_vq_elem(ee, &c, q12, e1[i1] - e2[i2], e4[i4] - e3[i3],
+                                                        0.5 * (e1[i1] - e2[i2] + e4[i4] - e3[i3])));
+              if (ee->antisym) {
+                mex[i1234] = zmul(o14[i1 * nb + i4], o32[i3 * nb + i2]);
+                if (ee->dynamic) /* calc_mee_ex multiplies mee (not mee_ex) by vq(k1 - k4, w_ex) */
+                  mee[i1234] = zmul(mee[i1234], ee_vq_elem(ee, &c, q14, e1[i1] - e4[i4], e2[i2] - e3[i3],
+                                                          0.5 * (e1[i1] - e4[i4] + e2[i2] - e3[i3])));
+              }
             }
       if (ee->antisym) /* axbyc(mee, mee_ex, n, -0.5, 0.5): mee = -0.5 mee_ex + 0.5 mee */
         for (int i = 0; i < nb4; i++) mee[i] = zadd(zmul(zmk(-0.5, 0), mex[i]), zmul(zmk(0.5, 0), mee[i]));

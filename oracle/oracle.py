@@ -133,7 +133,9 @@ class _EE(C.Structure):
                 ("update_screening", C.c_int), ("nv", C.c_int), ("degauss", C.c_double), ("ethr", C.c_double),
                 ("antisym", C.c_int), ("scale", C.c_double), ("inside", C.c_int), ("P1base", C.c_void_p),
                 ("P2base", C.c_void_p), ("P1eff", C.c_void_p), ("P2eff", C.c_void_p), ("P1ee", C.c_void_p),
-                ("P2ee", C.c_void_p), ("f_setup", C.c_void_p), ("vq_rpa", C.c_void_p)]
+                ("P2ee", C.c_void_p), ("f_setup", C.c_void_p), ("vq_rpa", C.c_void_p), ("dynamic", C.c_int),
+                ("ppa_gn", C.c_int), ("eppa", C.c_double), ("smearing", C.c_double), ("two_freqs", C.c_int),
+                ("Aq_ppa", C.c_void_p), ("Eq2_ppa", C.c_void_p)]
 
 
 EE_FORMULAS = {"unscreened": 0, "debye": 1, "Bechstedt": 2, "RPA": 3, "lindhard": 4}
@@ -171,7 +173,8 @@ class EEModel:
     P1eff, P2eff are the system's P1, P2: P_base + scale P_ee, rebuilt in place from rho."""
 
     def __init__(self, *, nb, kvec, kmesh, U, GGT, cell_size, nk_full, T, eps, meff, formula, nfree, update_screening,
-                 nv, degauss, ethr, antisym, scale, inside, P1base, P2base, f_setup=None, e_window=None):
+                 nv, degauss, ethr, antisym, scale, inside, P1base, P2base, f_setup=None, e_window=None,
+                 dynamic="static", ppamodel="gn", eppa=0.0, smearing=0.0, two_freqs=0):
         self.kvec = np.ascontiguousarray(kvec, np.float64)
         self.U = np.ascontiguousarray(U, np.complex128)
         self.P1base = np.ascontiguousarray(P1base, np.complex128)
@@ -190,6 +193,23 @@ class EEModel:
         self.inside = int(inside)
         self.f_setup = None if f_setup is None else np.ascontiguousarray(f_setup, np.float64)
         self.vq_rpa = np.zeros(int(np.prod(self.kmesh)), np.float64) if self.formula >= 3 else None
+        # dynamic screening (Scatt_Param.h:20-49, Coulomb_Model.h:520-530, 572-575): the plasmon-pole
+        # approximation with RPA / Lindhard screening only; eppa defaults to the plasma frequency of
+        # the set-up density, the smearing to 0.5 T except for Godby-Needs
+        if dynamic not in ("static", "ppa"):
+            raise ValueError("the oracle restates static and ppa screening only")
+        self.dynamic = 1 if dynamic == "ppa" else 0
+        if self.dynamic and self.formula < 3:
+            raise ValueError("dynamic screening needs RPA or lindhard (the reference refuses the other formulas)")
+        self.ppa_gn = 1 if ppamodel == "gn" else 0
+        if self.dynamic and eppa == 0:
+            eppa = math.sqrt(4 * math.pi * nfree / meff / eps)
+        if not (self.dynamic and self.ppa_gn):
+            smearing = 0.5 * T if smearing <= 0 else smearing
+        self.eppa, self.smearing, self.two_freqs = float(eppa), float(smearing), int(two_freqs)
+        nm = int(np.prod(self.kmesh)) if self.dynamic else 1
+        self.Aq_ppa = np.zeros(nm, np.complex128)
+        self.Eq2_ppa = np.zeros(nm, np.complex128)
         self.c = _EE(nb=self.nb, nbw=self.nbw, kvec=self.kvec.ctypes.data, kmesh=(C.c_int * 3)(*self.kmesh),
                      U=self.U.ctypes.data, GGT=(C.c_double * 9)(*self.GGT), cell_size=cell_size, nk_full=nk_full, T=T,
                      eps=eps, meff=meff, formula=self.formula, nfree=nfree, update_screening=self.update_screening,
@@ -197,7 +217,9 @@ class EEModel:
                      P1base=self.P1base.ctypes.data, P2base=self.P2base.ctypes.data, P1eff=self.P1eff.ctypes.data,
                      P2eff=self.P2eff.ctypes.data, P1ee=self.P1ee.ctypes.data, P2ee=self.P2ee.ctypes.data,
                      f_setup=None if self.f_setup is None else self.f_setup.ctypes.data,
-                     vq_rpa=None if self.vq_rpa is None else self.vq_rpa.ctypes.data)
+                     vq_rpa=None if self.vq_rpa is None else self.vq_rpa.ctypes.data, dynamic=self.dynamic,
+                     ppa_gn=self.ppa_gn, eppa=self.eppa, smearing=self.smearing, two_freqs=self.two_freqs,
+                     Aq_ppa=self.Aq_ppa.ctypes.data, Eq2_ppa=self.Eq2_ppa.ctypes.data)
         if self.formula >= 3:  # the static RPA / Lindhard screening of the set-up (Coulomb_Model.h:690-826)
             if self.f_setup is None or e_window is None:
                 raise ValueError("RPA / lindhard screening needs the set-up occupations and energies")
@@ -394,8 +416,6 @@ class OracleSystem:
 def _ee_model_of(pm, sz, dd, R, nk, nb, nb_dm, bstart, bend, e_dm, f_dm, nv_dm, T, cell_size, nfree, P1, P2):
     """The e-e model's inputs as elecelec_model / coulomb_model read them (ElecElec_Model.h:22-37,
     Coulomb_Model.h:394-450): U, k-points, reciprocal metric, screening parameters."""
-    if pm.get("dynamic_screening", "static") != "static":
-        raise ValueError("the oracle restates static screening only")
     nbw = sz["nb_wannier"]
     nb_eph = sz["bEnd_eph"] - sz["bStart_eph"]
     U = np.fromfile(os.path.join(dd, "ldbd_Umat.bin"), dtype=np.complex128).reshape(nk, nbw, nb_eph)
@@ -411,7 +431,10 @@ def _ee_model_of(pm, sz, dd, R, nk, nb, nb_dm, bstart, bend, e_dm, f_dm, nv_dm, 
                    degauss=pget(pm, "degauss_ee", degauss / eV, eV), ethr=degauss * ndegauss,
                    antisym=int(pget(pm, "ee_antisymmetry", 0)), scale=pget(pm, "scale_ee", scale_scatt),
                    inside=pget(pm, "freq_update_ee_model", 0) < 0, P1base=P1, P2base=P2,
-                   f_setup=f_dm[:, bstart:bend], e_window=e_dm[:, bstart:bend])
+                   f_setup=f_dm[:, bstart:bend], e_window=e_dm[:, bstart:bend],
+                   dynamic=pm.get("dynamic_screening", "static"), ppamodel=pm.get("ppamodel", "gn"),
+                   eppa=pget(pm, "eppa_screening", 0.0), smearing=pget(pm, "smearing_screening", 0.0, eV),
+                   two_freqs=int(pget(pm, "dynamic_screening_ee_two_freqs", 0)))
 
 
 def _ee_linear_terms(pm, sz, dd, R, nk, nb, nb_dm, bstart, bend, npair, k1, k2, e_dm, f_dm, f_lin, nv_dm, T,
@@ -421,6 +444,8 @@ def _ee_linear_terms(pm, sz, dd, R, nk, nb, nb_dm, bstart, bend, npair, k1, k2, 
     Coulomb_Model.h:532-544), P_ee at f_eq (calc_P with ee_model->f = f_eq) and, unless eeMode =
     Pee_fixed_at_eq, P3..P6 (ElecElec_Model_linear.cpp), each times scale_ee."""
     nb4 = nb ** 4
+    if pm.get("dynamic_screening", "static") != "static":
+        raise ValueError("the linearized e-e source is restated with static screening only")
     zero = np.zeros(npair * nb4, np.complex128)
     ee = _ee_model_of(pm, sz, dd, R, nk, nb, nb_dm, bstart, bend, e_dm, f_dm, nv_dm, T, cell_size, nfree, zero, zero)
     n = nfree

@@ -115,6 +115,29 @@ CASES = {
                                 param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0, 0.6, 0),
                                            extra=dict(EE_COMMON, eeMode="Pee_fixed_at_eq", scrFormula="Bechstedt",
                                                       update_screening=0, meff_screening=0.3, alg_linearize=1))),
+    # dynamic screening in the plasmon-pole approximation (dynamic_screening = ppa, Godby-Needs: the RPA
+    # sums at zero and at i * eppa, eppa the plasma frequency of the set-up density), vq(q, w) per
+    # matrix element at the mean energy transfer
+    "ee_nb2_rpa_ppa": dict(cfg=SynthConfig(nk=36, nb=2, seed=41, de_pair_mev=60.0, nwannier=4, kball=True),
+                           param=dict(Bpert_T=(0, 0.05, 0.1), B_T=(0, 0, 0.7),
+                                      extra=dict(EE_COMMON, scrFormula="RPA", update_screening=1,
+                                                 dynamic_screening="ppa"))),
+    # Hybertsen-Louie plasmon pole, nb = 4, exchange term (the exchange factor vq(k1 - k4, w_ex) as
+    # the reference applies it), smearing of the real frequency 0.5 T (the default)
+    "ee_nb4_rpa_ppa_hl_anti": dict(cfg=SynthConfig(nk=14, nb=4, seed=42, de_pair_mev=60.0, nwannier=6, kball=True),
+                                   param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0.3, 0, 0.2),
+                                              extra=dict(EE_COMMON, scrFormula="RPA", update_screening=1,
+                                                         dynamic_screening="ppa", ppamodel="hl",
+                                                         ee_antisymmetry=1))),
+    # Godby-Needs with a given plasmon energy and smearing, the two-frequency interaction
+    # (dynamic_screening_ee_two_freqs: |vq| geometric mean, mean phase), exchange term
+    "ee_nb2_ppa_twofreq_anti": dict(cfg=SynthConfig(nk=32, nb=2, seed=43, de_pair_mev=60.0, nwannier=3, kball=True),
+                                    param=dict(Bpert_T=(0.05, 0, 0.1), B_T=(0, 0.6, 0),
+                                               extra=dict(EE_COMMON, scrFormula="RPA", update_screening=0,
+                                                          dynamic_screening="ppa", eppa_screening=0.002,
+                                                          smearing_screening=0.004,
+                                                          dynamic_screening_ee_two_freqs=1,
+                                                          ee_antisymmetry=1))),
     # sparse operators (alg_sparseP): 70 % of every pair's P1 / P2 elements zeroed, nb = 4, B field;
     # the reference contracts the stored elements with sparse_zgemm (e-ph only: the reference refuses
     # ab-initio e-imp with sparse P)

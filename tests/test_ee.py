@@ -40,7 +40,8 @@ def ee_desc(s, every_rhs=None):
                 cell_size=e.cell_size, nk_full=e.nk_full, temperature=e.T, eps_background=e.eps, meff=e.meff,
                 formula=e.formula, nfree=e.c.nfree, update_screening=e.update_screening, nv=e.nv,
                 degauss=e.degauss, ethr=e.ethr, antisymmetry=e.antisym, scale=e.scale,
-                every_rhs=e.inside if every_rhs is None else every_rhs)
+                every_rhs=e.inside if every_rhs is None else every_rhs, dynamic=e.dynamic, ppa_gn=e.ppa_gn,
+                eppa=e.eppa, smearing=e.smearing, two_freqs=e.two_freqs)
 
 
 def make_ee_gpu(s, prec="f64", every_rhs=None):
@@ -242,6 +243,12 @@ def test_ee_argument_and_order_checks(oracle, built):
         with pytest.raises(DMDError) as ex:
             gpu.ee_attach(**bad)
         assert ex.value.status == 1
+        for key, val in (("dynamic", 1), ("two_freqs", 1)):  # ppa needs RPA; two frequencies need ppa
+            bad = ee_desc(s)
+            bad[key] = val
+            with pytest.raises(DMDError) as ex:
+                gpu.ee_attach(**bad)
+            assert ex.value.status == 1
         gpu.ee_attach(**ee_desc(s))
         with pytest.raises(DMDError) as ex:
             gpu.ee_attach(**ee_desc(s))

@@ -144,6 +144,14 @@ def test_load_ee_model_matches_reference_setup(case, host, oracle):
     assert ee["temperature"] == meta["ee_T"] and ee["nv"] == int(meta["ee_nv"])
     assert ee["antisymmetry"] == int(meta["ee_antisym"]) and ee["scale"] == meta["ee_scale"]
     assert ee["every_rhs"] == 1 and ee["formula"] == o.ee.formula and ee["update_screening"] == o.ee.update_screening
+    # dynamic screening: the raw parameters (the library applies init_RPA's and :523's defaults)
+    assert ee["dynamic"] == o.ee.dynamic and ee["two_freqs"] == o.ee.two_freqs
+    if o.ee.dynamic:
+        assert ee["ppa_gn"] == o.ee.ppa_gn
+        eppa = ee["eppa"] if ee["eppa"] != 0 else np.sqrt(4 * np.pi * ee["nfree"] / ee["meff"] / ee["eps_background"])
+        assert eppa == o.ee.eppa
+        sm = ee["smearing"] if o.ee.ppa_gn or ee["smearing"] > 0 else 0.5 * ee["temperature"]
+        assert sm == o.ee.smearing
     np.testing.assert_array_equal(ee["U"], o.ee.U)
     np.testing.assert_array_equal(ee["kvec"], o.ee.kvec)
     np.testing.assert_array_equal(ee["f"], g["f_dm"][:, o.bstart:o.bend])
@@ -154,7 +162,9 @@ def test_load_ee_model_matches_reference_setup(case, host, oracle):
 
 def test_ee_options_outside_the_path_are_rejected(host, tmp_path):
     for extra, msg in [("scrFormula = heg\n", "scrFormula heg"), ("scrFormula = lindhard\n", "lindhard"),
-                       ("dynamic_screening = ppa\n", "static"),
+                       ("dynamic_screening = ppa\n", "static limit"),
+                       ("dynamic_screening = real-axis\n", "real-axis"),
+                       ("dynamic_screening_ee_two_freqs = 1\n", "only for dynamic screening"),
                        ("alg_ddmdteq = 1\n", "alg_ddmdteq"), ("freq_update_eimp_model = 3\n", "freq_update_eimp_model")]:
         dst = str(tmp_path / ("c%d" % len(msg)))
         shutil.copytree(os.path.join(GOLDEN, "ee_nb2_debye"), dst)
