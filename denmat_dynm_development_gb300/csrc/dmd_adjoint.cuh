@@ -23,6 +23,7 @@
 #include "dmd_common.cuh"
 #include "dmd_kernels.cuh"
 #include "dmd_pairs_cb.cuh"
+#include "dmd_tma.cuh"
 
 namespace dmd {
 
@@ -377,6 +378,184 @@ __global__ void __launch_bounds__(128) k_adj_pairs_df(long long npair, const int
     atomicAdd(r2 + 1, D::im_d(a3));
     atomicAdd(s2, D::re_d(a4));
     atomicAdd(s2 + 1, D::im_d(a4));
+  }
+}
+
+// nb = 4: one warp per pair, a pair's double-float operators (8 KB) and gradient (8 KB) staged in
+// shared memory by bulk copies (TMA unit) in a 2-stage ring per warp, the per-k vectors of both
+// k-points in shared memory. The same sums as k_adj_pairs_df: lanes 0-15 form conj(P1)^T Xbar[k] and
+// conj(P2) Ybar[k] for b = lane, lanes 16-31 P2^T Xbar[k'] and P1 Ybar[k'] for b = lane - 16 (k < k'),
+// reading rows with a per-lane rotation so that the 16 lanes hit distinct banks; then every lane
+// updates 8 elements of G1 and 8 of G2 and stores them to global memory (coalesced). A warp takes a
+// contiguous run of pairs. Waits are bounded; a timeout sets *errflag and the warp drains its copies.
+template <int NST_, int W_ = 4>
+struct AdjBulkSmem {
+  static constexpr int NB = 4, NB2 = 16, NB4 = 256;
+  static constexpr int NST = NST_;  // ring stages per warp
+  static constexpr size_t half_bytes = (size_t)2 * NB4 * 16;           // P1 | P2 (or G1 | G2)
+  static constexpr size_t stage_bytes = 2 * half_bytes;                 // operators, then gradient
+  static constexpr size_t vec_bytes = (size_t)8 * NB2 * 2 * 16;         // 8 vectors x 16 x (x, S(x))
+  static constexpr size_t warp_bytes = (NST * stage_bytes + vec_bytes + 8 * NST + 127) / 128 * 128;
+  static constexpr int warps = W_;  // warps (pairs in flight) per CTA
+  static constexpr size_t cta_bytes = warps * warp_bytes;
+};
+
+template <int NST_, int W_>
+__global__ void __launch_bounds__(32 * W_, 2) k_adj_pairs_bulk4(long long npair, const int2* __restrict__ kk,
+                                                                  const float4* __restrict__ P,
+                                                                  const float4* __restrict__ dfv, size_t nk2,
+                                                                  double* __restrict__ rtb, double* __restrict__ stb,
+                                                                  float4* __restrict__ G,
+                                                                  unsigned int* __restrict__ errflag) {
+  typedef AdjBulkSmem<NST_, W_> S;
+  typedef ArithDF D;
+  constexpr int NB2 = S::NB2, NB4 = S::NB4, NST = S::NST;
+  constexpr unsigned FULL = 0xffffffffu;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char* wbase = smem_raw + (size_t)wib * S::warp_bytes;
+  float4* const stage0 = (float4*)wbase;                                   // [NST][P1 P2 G1 G2][NB4]
+  float4* const vec = (float4*)(wbase + NST * S::stage_bytes);            // [8][NB2][2]
+  uint64_t* const bar = (uint64_t*)(wbase + NST * S::stage_bytes + S::vec_bytes);
+  const long long nwarps = (long long)gridDim.x * S::warps;
+  const long long gw = (long long)blockIdx.x * S::warps + wib;
+  const long long per = (npair + nwarps - 1) / nwarps;
+  const long long p0 = gw * per, p1 = p0 + per < npair ? p0 + per : npair;
+  if (p0 >= p1) return;
+  const long long n = p1 - p0;
+  if (lane == 0) {
+#pragma unroll
+    for (int st = 0; st < NST; ++st) mbar_init(&bar[st], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  const uint64_t pol = policy_evict_first();
+  auto issue = [&](long long i) {  // pair p0 + i into stage i % NST (lane 0)
+    if (lane == 0) {
+      const int st = (int)(i % NST);
+      float4* dst = stage0 + (size_t)st * 4 * NB4;
+      const size_t p = (size_t)(p0 + i);
+      mbar_arrive_expect_tx(&bar[st], (uint32_t)S::stage_bytes);
+      bulk_g2s(dst, P + p * 2 * NB4, (uint32_t)S::half_bytes, &bar[st], pol);
+      bulk_g2s(dst + 2 * NB4, G + p * 2 * NB4, (uint32_t)S::half_bytes, &bar[st], pol);
+    }
+  };
+#pragma unroll
+  for (int i = 0; i < NST; ++i)
+    if (i < n) issue(i);
+  long long fail = -1;
+  const int half = lane >> 4, b = lane & 15;
+#pragma unroll 1
+  for (long long i = 0; i < n; ++i) {
+    const size_t p = (size_t)(p0 + i);
+    const int2 kp2 = kk[p];
+    const int k = kp2.x, kq = kp2.y;
+    const bool rev = k < kq;
+    // per-k vectors: v = 0..3 (Xbar, Ybar, rt, st) at k, 4..7 at k'; 32 float4 (x, S(x)) each
+#pragma unroll
+    for (int v = 0; v < 8; ++v)
+      vec[v * 32 + lane] = dfv[2 * ((size_t)(v & 3) * nk2 + (size_t)(v < 4 ? k : kq) * NB2) + lane];
+    const int st = (int)(i % NST);
+    if (!__all_sync(FULL, mbar_wait_bounded(&bar[st], (uint32_t)((i / NST) & 1), errflag))) {
+      fail = i;
+      break;
+    }
+    __syncwarp();  // the vectors are visible to the warp
+    const float4* P1 = stage0 + (size_t)st * 4 * NB4;
+    const float4* P2 = P1 + NB4;
+    const float4* G1 = P1 + 2 * NB4;
+    const float4* G2 = P1 + 3 * NB4;
+    auto V = [&](int v, int e) -> const float4* { return vec + v * 32 + 2 * e; };  // (x, S(x)) of element e
+    // transposed contraction
+    // half 0: conj(P1[a][b]) Xbar[k][a], conj(P2[b][a]) Ybar[k][a]; half 1: P2[a][b] Xbar[k'][a],
+    // P1[b][a] Ybar[k'][a] -- one instruction stream, operands selected per half
+    // (two partial sums per output -- the real-part and the imaginary-part products of p -- so that
+    // four accumulation chains run side by side)
+    D::acc s1, s2, t1, t2;
+    D::zero(s1);
+    D::zero(s2);
+    D::zero(t1);
+    D::zero(t2);
+    {
+      const float4* Pc = half ? P2 : P1;  // read by columns
+      const float4* Pr = half ? P1 : P2;  // read by rows
+      const int vx = half ? 4 : 0, vy = half ? 5 : 1;
+      const float sg = half ? -1.f : 1.f;  // conj(p) x takes +Im p, p x takes -Im p (exact sign flips)
+#pragma unroll 4
+      for (int j = 0; j < NB2; ++j) {
+        const int a = (j + b) & 15;
+        const float4 x = Pc[a * NB2 + b], y = Pr[b * NB2 + a];
+        const float4* X = V(vx, a);
+        const float4* Y = V(vy, a);
+        D::pmac(s1, X[0], df_bre(x));
+        D::pmac(t1, X[1], make_float4(sg * x.y, sg * x.y, sg * x.w, sg * x.w));
+        D::pmac(s2, Y[0], df_bre(y));
+        D::pmac(t2, Y[1], make_float4(sg * y.y, sg * y.y, sg * y.w, sg * y.w));
+      }
+    }
+    {  // s += t (double-float, per half)
+      float4 u1 = make_float4(s1.h.x, s1.h.y, s1.l.x, s1.l.y), u2 = make_float4(s2.h.x, s2.h.y, s2.l.x, s2.l.y);
+      D::red_add4(u1, make_float4(t1.h.x, t1.h.y, t1.l.x, t1.l.y));
+      D::red_add4(u2, make_float4(t2.h.x, t2.h.y, t2.l.x, t2.l.y));
+      s1 = D::acc{make_float2(u1.x, u1.y), make_float2(u1.z, u1.w)};
+      s2 = D::acc{make_float2(u2.x, u2.y), make_float2(u2.z, u2.w)};
+    }
+    // gradient: element e = lane + 32 j of G1 and of G2, a = e / 16, c = e % 16 (the column)
+    float4* g1o = G + p * 2 * NB4;
+    float4* g2o = g1o + NB4;
+#pragma unroll 2
+    for (int j = 0; j < NB4 / 32; ++j) {
+      const int e = lane + 32 * j, a = e >> 4, c = e & 15;
+      // G1[a][c] += conj(Xbar[k][a]) rt[k'][c] (+ conj(st[k][a]) Ybar[k'][c])
+      D::acc g = {make_float2(G1[e].x, G1[e].y), make_float2(G1[e].z, G1[e].w)};
+      const float4 Xka = V(0, a)[0];
+      const float4* rq = V(6, c);
+      D::pmac(g, rq[0], df_bre(Xka));
+      D::pmac(g, rq[1], df_bim(Xka));
+      if (rev) {
+        const float4 ska = V(3, a)[0];
+        const float4* Yq = V(5, c);
+        D::pmac(g, Yq[0], df_bre(ska));
+        D::pmac(g, Yq[1], df_bim(ska));
+      }
+      D::renorm(g);
+      g1o[e] = make_float4(g.h.x, g.h.y, g.l.x, g.l.y);
+      // G2[a][c] += conj(Ybar[k][c]) st[k'][a] (+ conj(rt[k][c]) Xbar[k'][a])
+      D::acc h2 = {make_float2(G2[e].x, G2[e].y), make_float2(G2[e].z, G2[e].w)};
+      const float4 Ykc = V(1, c)[0];
+      const float4* sq = V(7, a);
+      D::pmac(h2, sq[0], df_bre(Ykc));
+      D::pmac(h2, sq[1], df_bim(Ykc));
+      if (rev) {
+        const float4 rkc = V(2, c)[0];
+        const float4* Xq = V(4, a);
+        D::pmac(h2, Xq[0], df_bre(rkc));
+        D::pmac(h2, Xq[1], df_bim(rkc));
+      }
+      D::renorm(h2);
+      g2o[e] = make_float4(h2.h.x, h2.h.y, h2.l.x, h2.l.y);
+    }
+    // the stage and the vectors are free once every lane has read them: order those reads before the
+    // next bulk copy into the stage (generic -> async proxy), then refill it
+    fence_proxy_async();
+    __syncwarp();
+    if (i + NST < n) issue(i + NST);
+    if (half == 0 || rev) {
+      const int kt = half == 0 ? kq : k;
+      double* ro = rtb + ((size_t)kt * NB2 + b) * 2;
+      double* so = stb + ((size_t)kt * NB2 + b) * 2;
+      atomicAdd(ro, D::re_d(s1));
+      atomicAdd(ro + 1, D::im_d(s1));
+      atomicAdd(so, D::re_d(s2));
+      atomicAdd(so + 1, D::im_d(s2));
+    }
+  }
+  if (fail >= 0) {  // drain the copies still in flight (bounded), then leave
+    if (lane == 0) {
+      const long long last = (fail + NST < n ? fail + NST : n) - 1;
+      for (long long c = fail; c <= last; ++c) mbar_wait_bounded(&bar[c % NST], (uint32_t)((c / NST) & 1), nullptr, 1u << 16);
+    }
+    __syncwarp();
   }
 }
 

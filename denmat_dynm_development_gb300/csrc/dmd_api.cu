@@ -1452,6 +1452,37 @@ int adj_rk4_step(dmd_handle* h, const double2* y, double t, double dt, double2* 
   return DMD_OK;
 }
 
+// the nb = 4 double-float adjoint pair pass (k_adj_pairs_bulk4): a persistent grid of two CTAs per
+// SM; shape from DMD_ADJ_BULK_SHAPE (0: 1 stage x 5 warps, the default; 1: 1 stage x 4 warps;
+// 2: 2 stages x 2 warps)
+template <int NST, int W>
+int adj_bulk4_launch_shape(dmd_handle* h, const int2* kk, const float4* dfv, size_t nk2, double* rtb, double* stb,
+                           float4* G) {
+  typedef AdjBulkSmem<NST, W> S;
+  static bool attr_set = false;
+  if (!attr_set) {
+    CK(cudaFuncSetAttribute(k_adj_pairs_bulk4<NST, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::cta_bytes));
+    attr_set = true;
+  }
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev) != cudaSuccess || nsm <= 0) nsm = 1;
+  const long long ctas = std::min<long long>((long long)nsm * 2, (h->npair + S::warps - 1) / S::warps);
+  k_adj_pairs_bulk4<NST, W><<<(unsigned)ctas, 32 * S::warps, S::cta_bytes, h->st>>>(h->npair, kk, h->d_Padf, dfv,
+                                                                                     nk2, rtb, stb, G, h->d_err);
+  return DMD_OK;
+}
+
+int adj_bulk4_launch(dmd_handle* h, const int2* kk, const float4* dfv, size_t nk2, double* rtb, double* stb, float4* G) {
+  static int shape = -1;
+  if (shape < 0) {
+    const char* e = getenv("DMD_ADJ_BULK_SHAPE");
+    shape = e ? atoi(e) : 0;
+  }
+  if (shape == 1) return adj_bulk4_launch_shape<1, 4>(h, kk, dfv, nk2, rtb, stb, G);
+  if (shape == 2) return adj_bulk4_launch_shape<2, 2>(h, kk, dfv, nk2, rtb, stb, G);
+  return adj_bulk4_launch_shape<1, 5>(h, kk, dfv, nk2, rtb, stb, G);
+}
+
 // ybar += VJP_f(u, t)(vbar); kprev += c * VJP_f(u, t)(vbar) when kprev is set. accs: the forward sums
 // at u kept when u was evaluated (the phases are then recomputed from t), or null to evaluate them
 template <int NB>
@@ -1496,7 +1527,9 @@ int adj_vjp_nb(dmd_handle* h, AdjWork& w, const double2* u, double t, const doub
   k_adj_local<NB><<<blocks_for(h->nk, 128), 128, 0, h->st>>>(a);
   if (h->npair > 0) {
     const int2* kk = h->use_cb ? h->d_kkraw : h->d_kk;
-    if (w.dfv) {  // double-float products on the FP32 pipes
+    if (w.dfv && NB == 4) {  // double-float, one warp per pair, operators and gradient staged by bulk copies
+      if ((rc = adj_bulk4_launch(h, kk, w.dfv, nk2, (double*)w.rtb, (double*)w.stb, (float4*)w.G))) return rc;
+    } else if (w.dfv) {  // double-float products on the FP32 pipes
       k_adj_pairs_df<NB><<<blocks_for(h->npair * NB * NB, 128), 128, 0, h->st>>>(
           h->npair, kk, h->d_Padf, w.dfv, nk2, (double*)w.rtb, (double*)w.stb, (float4*)w.G);
     } else {
