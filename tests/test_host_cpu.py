@@ -172,3 +172,16 @@ def test_ee_options_outside_the_path_are_rejected(host, tmp_path):
             f.write(extra)
         with pytest.raises(RuntimeError, match=msg):
             host.System(dst)
+
+
+def test_rk4_func_validates_its_arguments(host):
+    """dmdh_rk4_func refuses a null handle, state or work array before any device call"""
+    import ctypes as C
+    L = C.CDLL(host.HOST_LIB)
+    L.dmdh_rk4_func.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_void_p, C.c_size_t, C.c_void_p]
+    y = np.zeros(8)
+    w = np.zeros(40)
+    assert L.dmdh_rk4_func(None, 0.0, 1.0, 1, y.ctypes.data, y.size, w.ctypes.data) == 1  # DMD_E_ARG
+    assert L.dmdh_rk4_func(C.c_void_p(1), 0.0, 1.0, 1, None, y.size, w.ctypes.data) == 1
+    assert L.dmdh_rk4_func(C.c_void_p(1), 0.0, 1.0, 1, y.ctypes.data, y.size, None) == 1
+    assert L.dmdh_rk4_func(C.c_void_p(1), 0.0, 1.0, -1, y.ctypes.data, y.size, w.ctypes.data) == 1
