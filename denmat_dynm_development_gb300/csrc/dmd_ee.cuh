@@ -54,7 +54,7 @@ struct EeArgs {
   float thr32;                       // ethr plus a margin above the FP32 rounding of that test
   const double2* dm;                 // [nk][nb^2] window density matrix (Schrodinger picture), or null
   const double2* dm1;                // [nk][nb^2] 1 - dm
-  const float4* dmf;                 // the same as double-floats (re_h, re_l, im_h, im_l)
+  const float4* dmf;                 // the same as double-floats (re_h, im_h, re_l, im_l)
   const float4* dm1f;
   const double* f;                   // [nk][nb] occupations when dm is null
   const EeScreen* scr;
@@ -251,9 +251,9 @@ __global__ void k_ee_rpa_table(EeArgs a, double prefac_vq, double nk_full, const
 // the window density matrix in the Schrodinger picture and 1 - rho from the state y (one thread per
 // (k, i, j) of the window): electronphonon::reset_scatt's window copy (ElectronPhonon.cpp:19-28)
 // and add_scatt_contrib's conversion (ElectronPhonon.cpp:56-66)
-__device__ __forceinline__ float4 split_dfc(double2 v) {
+__device__ __forceinline__ float4 split_dfc(double2 v) {  // (re_h, im_h, re_l, im_l)
   const float2 a = split_df1(v.x), b = split_df1(v.y);
-  return make_float4(a.x, a.y, b.x, b.y);
+  return make_float4(a.x, b.x, a.y, b.y);
 }
 
 template <int NB>
@@ -350,55 +350,65 @@ struct EeF64 {
   static __device__ __forceinline__ double2 value(c v) { return v; }
 };
 
+// Double-float complex arithmetic with the real and imaginary halves as FP32x2 pairs
+// (re_h, im_h, re_l, im_l), each step one packed instruction (ArithDF): a complex product is two
+// packed error-free multiply-adds, x y = y o (Re x, Re x) + (-Im y, Re y) o (Im x, Im x) and
+// x conj(y) = x o (Re y, Re y) + (Im x, -Re x) o (Im y, Im y).
 struct EeDF {
   static constexpr bool kDF = true;
-  typedef float4 c;  // (re_h, re_l, im_h, im_l)
+  typedef float4 c;  // (re_h, im_h, re_l, im_l)
+  typedef ArithDF::acc A;
+  static __device__ __forceinline__ A un(const c& v) { return A{make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
+  static __device__ __forceinline__ c pk(const A& a) { return make_float4(a.h.x, a.h.y, a.l.x, a.l.y); }
+  static __device__ __forceinline__ float4 bre(const c& v) { return make_float4(v.x, v.x, v.z, v.z); }
+  static __device__ __forceinline__ float4 bim(const c& v) { return make_float4(v.y, v.y, v.w, v.w); }
   static __device__ __forceinline__ c zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
   static __device__ __forceinline__ c from(double2 v) { return split_dfc(v); }
   static __device__ __forceinline__ void set_part(c& dst, int part, double v) {  // from(), one part
-    reinterpret_cast<float2*>(&dst)[part] = split_df1(v);
+    const float2 f = split_df1(v);
+    reinterpret_cast<float*>(&dst)[part] = f.x;
+    reinterpret_cast<float*>(&dst)[2 + part] = f.y;
   }
   static __device__ __forceinline__ c load(const double2*, const float4* f, size_t i) { return f[i]; }
-  static __device__ __forceinline__ void mac(c& a, c x, c y) {
-    df_mac(a.x, a.y, x.x, x.y, y.x, y.y);
-    df_mac(a.x, a.y, -x.z, -x.w, y.z, y.w);
-    df_mac(a.z, a.w, x.x, x.y, y.z, y.w);
-    df_mac(a.z, a.w, x.z, x.w, y.x, y.y);
+  static __device__ __forceinline__ void mac(c& a, c x, c y) {  // a += x y
+    A t = un(a);
+    ArithDF::pmac(t, y, bre(x));
+    ArithDF::pmac(t, make_float4(-y.y, y.x, -y.w, y.z), bim(x));
+    a = pk(t);
   }
-  static __device__ __forceinline__ void mac_conj(c& a, c x, c y) {
-    df_mac(a.x, a.y, x.x, x.y, y.x, y.y);
-    df_mac(a.x, a.y, x.z, x.w, y.z, y.w);
-    df_mac(a.z, a.w, x.z, x.w, y.x, y.y);
-    df_mac(a.z, a.w, -x.x, -x.y, y.z, y.w);
+  static __device__ __forceinline__ void mac_conj(c& a, c x, c y) {  // a += x conj(y)
+    A t = un(a);
+    ArithDF::pmac(t, x, bre(y));
+    ArithDF::pmac(t, make_float4(x.y, -x.x, x.w, -x.z), bim(y));
+    a = pk(t);
   }
   static __device__ __forceinline__ c scale(c x, double s) {
     const float2 v = split_df1(s);
-    c r;
-    df_mul(r.x, r.y, x.x, x.y, v.x, v.y);
-    df_mul(r.z, r.w, x.z, x.w, v.x, v.y);
-    return r;
+    A r;
+    ArithDF::mul(r, x, make_float4(v.x, v.x, v.y, v.y));
+    return pk(r);
   }
   static __device__ __forceinline__ void renorm(c& a) {
-    df_renorm(a.x, a.y);
-    df_renorm(a.z, a.w);
+    A t = un(a);
+    ArithDF::renorm(t);
+    a = pk(t);
   }
-  static __device__ __forceinline__ double2 value(c v) { return mk2((double)v.x + (double)v.y, (double)v.z + (double)v.w); }
+  static __device__ __forceinline__ double2 value(c v) { return mk2((double)v.x + (double)v.z, (double)v.y + (double)v.w); }
   static __device__ __forceinline__ c mul(c x, c y) {  // x y
-    c r;
-    df_mul(r.x, r.y, x.x, x.y, y.x, y.y);
-    df_mac(r.x, r.y, -x.z, -x.w, y.z, y.w);
-    df_mul(r.z, r.w, x.x, x.y, y.z, y.w);
-    df_mac(r.z, r.w, x.z, x.w, y.x, y.y);
-    renorm(r);
-    return r;
+    A r;
+    ArithDF::mul(r, y, bre(x));
+    ArithDF::pmac(r, make_float4(-y.y, y.x, -y.w, y.z), bim(x));
+    ArithDF::renorm(r);
+    return pk(r);
   }
   static __device__ __forceinline__ c scale_df(c x, float2 s) {
-    c r;
-    df_mul(r.x, r.y, x.x, x.y, s.x, s.y);
-    df_mul(r.z, r.w, x.z, x.w, s.x, s.y);
-    renorm(r);
-    return r;
+    A r;
+    ArithDF::mul(r, x, make_float4(s.x, s.x, s.y, s.y));
+    ArithDF::renorm(r);
+    return pk(r);
   }
+  // a += b (double-float, per half)
+  static __device__ __forceinline__ void add(c& a, const c& b) { ArithDF::red_add4(a, b); }
 };
 
 // screening density and constants (one block): with update, nfree = sum over k and window bands of
@@ -583,8 +593,7 @@ __global__ void __launch_bounds__(32 * ee_warps_per_cta(NB), (NB == 2 && V::kDF)
               if (a.antisym) {
                 const C mex = V::mul(sm.o14[grp][i1 * NB + d], sm.o32[grp][c * NB + i3]);
                 mee = make_float4(0.5f * mee.x, 0.5f * mee.y, 0.5f * mee.z, 0.5f * mee.w);  // exact halves
-                df_add(mee.x, mee.y, -0.5f * mex.x, -0.5f * mex.y);
-                df_add(mee.z, mee.w, -0.5f * mex.z, -0.5f * mex.w);
+                V::add(mee, make_float4(-0.5f * mex.x, -0.5f * mex.y, -0.5f * mex.z, -0.5f * mex.w));
               }
               v = V::scale_df(mee, df_exp_neg(a.prefac_exp * (de * de)));
             } else {
