@@ -72,7 +72,7 @@ def build_host(force=False):
     tmp = HOST_LIB + ".tmp"
     build_gpu()
     _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", INC, "-o", tmp] + HOST_SRCS +
-         ["-L", PKG, "-l:libdmdgpu.so", "-Wl,-rpath,$ORIGIN", "-lm"])
+         ["-L", PKG, "-l:libdmdgpu.so", "-Wl,-rpath,$ORIGIN", "-lm", "-lpthread"])
     os.replace(tmp, HOST_LIB)
     return HOST_LIB
 

@@ -5,8 +5,13 @@
 
 #include <sys/stat.h>
 
+#include <atomic>
 #include <cfloat>
 #include <cmath>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -239,9 +244,80 @@ int dmdh_fermi(double T, double mu, const double* e, double* f, size_t n) {
   return DMD_OK;
 }
 
+// Worker threads that run one loop body over contiguous slices of [0, n), phase after phase (the
+// caller's thread takes slice 0 and waits for the others); they sleep between phases.
+class SlicePool {
+ public:
+  explicit SlicePool(unsigned nt) : nt_(nt < 1 ? 1 : nt) {
+    for (unsigned w = 1; w < nt_; ++w) th_.emplace_back([this, w] { loop(w); });
+  }
+  ~SlicePool() {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  void run(size_t n, const std::function<void(size_t, size_t)>& body) {
+    if (nt_ == 1) {
+      body(0, n);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> g(m_);
+      body_ = &body;
+      n_ = n;
+      left_ = nt_ - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    slice(0, n, body);
+    std::unique_lock<std::mutex> l(m_);
+    done_.wait(l, [this] { return left_ == 0; });
+  }
+
+ private:
+  void slice(unsigned w, size_t n, const std::function<void(size_t, size_t)>& body) const {
+    const size_t per = (n + nt_ - 1) / nt_, i0 = std::min(n, (size_t)w * per), i1 = std::min(n, i0 + per);
+    if (i0 < i1) body(i0, i1);
+  }
+  void loop(unsigned w) {
+    uint64_t seen = 0;
+    for (;;) {
+      const std::function<void(size_t, size_t)>* body;
+      size_t n;
+      {
+        std::unique_lock<std::mutex> l(m_);
+        cv_.wait(l, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (stop_) return;
+        body = body_;
+        n = n_;
+      }
+      slice(w, n, *body);
+      {
+        std::lock_guard<std::mutex> g(m_);
+        if (--left_ == 0) done_.notify_one();
+      }
+    }
+  }
+  unsigned nt_;
+  std::vector<std::thread> th_;
+  std::mutex m_;
+  std::condition_variable cv_, done_;
+  const std::function<void(size_t, size_t)>* body_ = nullptr;
+  size_t n_ = 0;
+  unsigned left_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
 // Fixed-step RK4 on the host around the GSL-callback entry, as a GSL-driven host runs it: every
 // stage is one dmd_func call (its input copied to the device, dydt copied back) and the stage
-// combinations are host loops: y_s = y + c h k, then y += h/6 (k1 + 2 k2 + 2 k3 + k4).
+// combinations are host loops: y_s = y + c h k, then y += h/6 (k1 + 2 k2 + 2 k3 + k4), split over
+// up to 8 host threads (elementwise, so the result does not depend on the split).
 int dmdh_rk4_func(dmd_handle* h, double t, double dt, int64_t nsteps, double* y, size_t n, double* work) {
   if (!h || !y || !work || n == 0 || nsteps < 0) return DMD_E_ARG;
   double* ys = work;
@@ -249,18 +325,27 @@ int dmdh_rk4_func(dmd_handle* h, double t, double dt, int64_t nsteps, double* y,
   double* k2 = work + 2 * n;
   double* k3 = work + 3 * n;
   double* k4 = work + 4 * n;
+  const unsigned hw = std::thread::hardware_concurrency();
+  SlicePool pool(n < (1u << 16) ? 1u : std::max(1u, std::min(8u, hw)));
   int rc = DMD_OK;
   for (int64_t s = 0; s < nsteps; ++s) {
     const double ts = t + (double)s * dt, hh = 0.5 * dt;
+    auto stage = [&](const double* k, double c) {
+      pool.run(n, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; ++i) ys[i] = y[i] + c * k[i];
+      });
+    };
     if ((rc = dmd_func(h, ts, y, k1))) return rc;
-    for (size_t i = 0; i < n; ++i) ys[i] = y[i] + hh * k1[i];
+    stage(k1, hh);
     if ((rc = dmd_func(h, ts + hh, ys, k2))) return rc;
-    for (size_t i = 0; i < n; ++i) ys[i] = y[i] + hh * k2[i];
+    stage(k2, hh);
     if ((rc = dmd_func(h, ts + hh, ys, k3))) return rc;
-    for (size_t i = 0; i < n; ++i) ys[i] = y[i] + dt * k3[i];
+    stage(k3, dt);
     if ((rc = dmd_func(h, ts + dt, ys, k4))) return rc;
     const double c = dt / 6.0;
-    for (size_t i = 0; i < n; ++i) y[i] += c * (k1[i] + 2.0 * k2[i] + 2.0 * k3[i] + k4[i]);
+    pool.run(n, [&](size_t i0, size_t i1) {
+      for (size_t i = i0; i < i1; ++i) y[i] += c * (k1[i] + 2.0 * k2[i] + 2.0 * k3[i] + k4[i]);
+    });
   }
   return DMD_OK;
 }

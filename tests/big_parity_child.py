@@ -73,7 +73,7 @@ def main():
         par.close()
     st_c0, s_c0 = workload("si_nk500")
     y_c0 = O.y_of(s_c0.dm0)
-    h, nsteps = 1.0 * U.fs, 200
+    h, nsteps = 1.0 * U.fs, 200  # (h is also the step of the host-driver check below)
     par = O.ParallelRHS(s_c0, ncpu)
     try:
         yo, tt = y_c0.copy(), 0.0
@@ -87,6 +87,14 @@ def main():
     for prec in ("f64", "f64x"):
         with gpu(st_big, s_big, prec) as g:
             out["rhs_gaas_nk20k_" + prec] = rel(g.func(t, y_big), ref_big)
+            if prec == "f64":  # the host RK4 driver over the callback (threaded stage loops at this size)
+                from denmat_dynm_development_gb300 import host as HL
+                yh = np.ascontiguousarray(y_big, dtype=np.float64).copy()
+                HL.rk4_func(g, t, h, 2, yh, np.zeros(5 * yh.size))
+                g.set_state(t, y_big)
+                g.rk4(h, 2)
+                _, yd = g.get_state()
+                out["host_rk4_vs_device_gaas_nk20k"] = rel(yh, yd)
         with gpu(st_c0, s_c0, prec) as g:
             g.set_state(0.0, y_c0)
             g.rk4(h, nsteps)

@@ -43,3 +43,8 @@ def test_rhs_at_benchmark_size(big, prec, tol):
 def test_rk4_200_steps_si_nk500(big, prec):
     assert big["rk4_si_nk500_200_" + prec] < 1e-10
     assert big["sz_si_nk500_200_" + prec] < 1e-10
+
+
+def test_host_rk4_driver_at_benchmark_size(big):
+    """dmdh_rk4_func (host stage loops split over threads at this size) equals the device RK4 loop"""
+    assert big["host_rk4_vs_device_gaas_nk20k"] < 1e-13
