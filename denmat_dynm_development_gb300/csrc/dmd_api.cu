@@ -2327,9 +2327,18 @@ int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64
       return fail(h, DMD_E_ARG, "obs_step must be ascending in [0, nsteps]");
   CK(cudaSetDevice(h->dev));
   const size_t n = h->nstate;
-  const int64_t nseg = (nsteps + checkpoint - 1) / checkpoint, seglen = checkpoint < nsteps ? checkpoint : nsteps;
   const size_t nk2 = (size_t)h->nk * h->nb2;
   const size_t np = (size_t)h->npair * 2 * h->nb4;
+  // When the stage inputs and forward sums of every step fit in 40 % of the free device memory, the
+  // forward pass keeps them and the backward pass recomputes nothing (one stretch); otherwise the
+  // trajectory is reversed stretch by stretch from checkpoints every `checkpoint` steps.
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
+  const double all_bytes = (double)nsteps * 4.0 * (double)(n + (size_t)h->nk * 2 * h->nb2) * 16.0;
+  const char* kv = getenv("DMD_ADJ_KEEP_ALL");  // 0: always reverse by stretches (tests of that path)
+  const bool keep_all = !(kv && atoi(kv) == 0) && all_bytes <= 0.4 * (double)free_b;
+  if (keep_all) checkpoint = nsteps;
+  const int64_t nseg = (nsteps + checkpoint - 1) / checkpoint, seglen = checkpoint < nsteps ? checkpoint : nsteps;
   AdjWork w;
   w.h = h;
   int rc;
@@ -2368,7 +2377,9 @@ int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64
   for (int64_t s = 0; s < nsteps; ++s) {
     double2* next = ((s + 1) % checkpoint == 0 && (s + 1) < nsteps) ? w.ck + (size_t)((s + 1) / checkpoint) * n
                                                                       : spare[sp];
-    if ((rc = adj_rk4_step(h, cur, t0 + (double)s * dt, dt, nullptr, next, w.tmp))) return rc;
+    if ((rc = adj_rk4_step(h, cur, t0 + (double)s * dt, dt, keep_all ? w.U + (size_t)s * 4 * n : nullptr, next,
+                           w.tmp, keep_all ? w.A + (size_t)s * 4 * na : nullptr)))
+      return rc;
     for (; j < nobs && obs_step[j] == s + 1; ++j) {
       double v;
       if ((rc = measure_on(h, slot, bstart, bend, next, t0 + (double)(s + 1) * dt, &v))) return rc;
@@ -2383,7 +2394,7 @@ int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64
   for (int64_t sg = nseg - 1; sg >= 0; --sg) {
     const int64_t n0 = sg * checkpoint, n1 = std::min<int64_t>(n0 + checkpoint, nsteps);
     const double2* y = w.ck + (size_t)sg * n;
-    for (int64_t s = n0; s < n1; ++s) {  // stage inputs of the stretch
+    for (int64_t s = n0; s < n1 && !keep_all; ++s) {  // stage inputs of the stretch
       double2* out = spare[sp];
       if ((rc = adj_rk4_step(h, y, t0 + (double)s * dt, dt, w.U + (size_t)(s - n0) * 4 * n, out, w.tmp,
                              w.A + (size_t)(s - n0) * 4 * na)))

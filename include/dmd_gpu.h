@@ -159,9 +159,11 @@ int dmd_pair_bytes(const dmd_handle* h, int64_t* bytes);
 /* No counterpart in the reference (DMD computes no gradients). Reverse mode of nsteps fixed-step RK4
  * steps of size dt from (t0, y0) (y0: 2 nk nb_dm^2 doubles, as dmd_func's y), for the objective
  * J = sum_i obs_weight[i] * S(t0 + obs_step[i] dt), S = the total of observable `slot` over bands
- * [bstart, bend) as dmd_measure returns it. The forward pass keeps the state every `checkpoint`
- * steps; the backward pass recomputes each stretch of steps from its checkpoint and integrates the
- * adjoint through the exact discrete RK4 map with the transposed k-pair contraction. Outputs (any
+ * [bstart, bend) as dmd_measure returns it. When the stage inputs and forward sums of all steps fit
+ * in 40 % of the free device memory the forward pass keeps them all; otherwise it keeps the state
+ * every `checkpoint` steps and the backward pass recomputes each stretch from its checkpoint (also
+ * when the environment sets DMD_ADJ_KEEP_ALL=0). The
+ * adjoint runs through the exact discrete RK4 map with the transposed k-pair contraction. Outputs (any
  * may be null): s_obs [nobs] the observed totals, dJdP [2][nkpair][nb^4] complex (dJ/dRe P, dJ/dIm P
  * interleaved, P1 then P2, of the folded operators P = P + add_scale P_add), dJdy0 [2 nk nb_dm^2]
  * (the gradient with respect to y0's real and imaginary parts). Requires DMD_FLAG_ADJOINT, a single

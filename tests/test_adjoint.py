@@ -53,8 +53,12 @@ def _objective(s, y0, dt, steps, w, P1=None, P2=None):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("keep", ["1", "0"])
 @pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_schrod", "nb4_eimp_B"])
-def test_adjoint_directional_derivatives_vs_fd(case, oracle, built):
+def test_adjoint_directional_derivatives_vs_fd(case, keep, oracle, built, monkeypatch):
+    """keep = 1: the forward pass keeps every stage (these sizes fit); keep = 0: the backward pass
+    recomputes stretches of 7 steps from checkpoints"""
+    monkeypatch.setenv("DMD_ADJ_KEEP_ALL", keep)
     s = oracle.load(os.path.join(GOLDEN, case))
     rng = np.random.default_rng(3)
     dt = 2.0 * oracle.fs
@@ -110,6 +114,26 @@ def test_double_float_backward_matches_fp64(case, oracle, built):
     e_s, e_p, e_y = rel(sdf, s64), rel(dPdf, dP64), rel(dydf, dy64)
     print("%s f64x vs f64 adjoint: S %.3g dJ/dP %.3g dJ/dy0 %.3g" % (case, e_s, e_p, e_y))
     assert e_s < 1e-11 and e_p < 1e-9 and e_y < 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["f64", "f64x"])
+def test_kept_stages_equal_recomputed_stretches(prec, oracle, built, monkeypatch):
+    """the backward pass over stages kept by the forward pass and over stretches recomputed from
+    checkpoints (DMD_ADJ_KEEP_ALL=0, 7 steps per stretch) give the same gradients"""
+    s = oracle.load(os.path.join(GOLDEN, "nb4_eimp_B"))
+    rng = np.random.default_rng(9)
+    steps = np.array([0, 9, 20, 33])
+    w = rng.standard_normal(steps.size)
+    out = {}
+    for keep in ("1", "0"):
+        monkeypatch.setenv("DMD_ADJ_KEEP_ALL", keep)
+        with _gpu(s, adjoint=True, precision=prec) as g:
+            out[keep] = g.adjoint_rk4(s.t0, oracle.y_of(s.dm0), 2.0 * oracle.fs, int(steps[-1]), steps, w, slot=0,
+                                      bstart=s.nv_dm, checkpoint=7, want_dy0=True)
+    assert rel(out["1"][0], out["0"][0]) < 1e-13
+    assert rel(out["1"][1], out["0"][1]) < 1e-12
+    assert rel(out["1"][2], out["0"][2]) < 1e-12
 
 
 def _mode_model(oracle, tmp_path, nb=2, nk=60, nsteps=60):
