@@ -6,7 +6,7 @@ Tolerances (normwise relative, max|gpu - ref| / max|ref|):
     run in a different order;
   * RHS in the FP32-pair ("f64x") arithmetic: 1e-11 -- products carry ~2^-47 relative error and
     the scattering-in and scattering-out terms of the finish partly cancel;
-  * trajectories (40 RK4 steps, RKF45 to 20 fs): 1e-10 (the benchmark spec's bound for rho(t), S(t)).
+  * trajectories (40 RK4 steps, RKF45 to 20 fs): 1e-10 (the bound rho(t) and S(t) are held to).
 """
 import os
 
