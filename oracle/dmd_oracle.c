@@ -1,7 +1,8 @@
 /* ORACLE -- CPU restatement of DMD's Lindblad density-matrix right-hand side and steppers.
  *
  * TEST INFRASTRUCTURE ONLY. Imported solely by tests/, __graft_entry__.smoke() and bench.py's
- * CPU-baseline leg, always as the checker; never part of the product path.
+ * CPU-baseline leg, always as the side the GPU results are compared with (or timed beside); never
+ * part of the product path.
  *
  * Pinned against the reference: tests/golden/ holds vectors produced by the reference's own
  * sources (src_v4.5.7, compiled unmodified against oracle/ref_shim by oracle/Makefile.ref) and the

@@ -1,7 +1,7 @@
 """ORACLE (test infrastructure only): Python side of the CPU restatement in dmd_oracle.c.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module, always as
-the checker. It reads a DMD input directory (param.in + ldbd_data/) the way the reference's
+the side the GPU results are compared with (or timed beside). It reads a DMD input directory (param.in + ldbd_data/) the way the reference's
 constructors do and calls the C restatement through ctypes.
 
 Setup statements restated here (reference file:line):
