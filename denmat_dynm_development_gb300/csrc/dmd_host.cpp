@@ -578,7 +578,6 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
     if (ppam != "gn" && ppam != "hl") return err(DMD_E_ARG, "ppamodel is invalid");
     if (pget(pm, "eppa_screening", 0) < 0) return err(DMD_E_ARG, "eppa must >= 0");
     if (pget(pm, "smearing_screening", 0) < 0) return err(DMD_E_ARG, "smearing must >= 0");
-    if (pget(pm, "alg_ddmdteq", 0) != 0) return err(DMD_E_ARG, "the e-e model is not supported with alg_ddmdteq");
     if (pget(pm, "alg_summode", 1) == 0) return err(DMD_E_ARG, "the e-e model needs alg_summode");
     const double fe = pget(pm, "freq_update_ee_model", 0), fi = pget(pm, "freq_update_eimp_model", 0);
     if (ee_mode == "Pee_update" && fe == 0)  // parameters.cpp:483-484
@@ -1062,6 +1061,9 @@ int dmdh_prepare(const dmdh_system* s, dmd_handle* h) {
       y[((size_t)ik * nd2 + (size_t)i * nd + i) * 2] = s->f_eq[(size_t)ik * nd + i];
       y1[((size_t)ik * nd2 + (size_t)i * nd + i) * 2] = 1 - s->f_eq[(size_t)ik * nd + i];
     }
+  if (s->ee && !in.linear) {  // reset_scatt at rho_eq (DensityMatrix_Dynamics.h:58-63): P_ee(rho_eq)
+    if ((rc = dmd_set_state(h, 0.0, y.data())) || (rc = dmd_ee_update(h))) return err(rc, dmd_last_error(h));
+  }
   if ((rc = dmd_evolve_driver(h, 0.0, y.data(), y1.data(), out.data()))) return err(rc, dmd_last_error(h));
   for (int ik = 0; ik < in.nk; ik++)
     for (int i = 0; i < nb; i++)

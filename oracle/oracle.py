@@ -588,7 +588,9 @@ def load(d: str) -> OracleSystem:
                                    f_lin.ctypes.data, Lij.ctypes.data, Lji.ctypes.data)
         L.orc_lsc_diag(nb, npair, k1.ctypes.data, k2.ctypes.data, Lii.ctypes.data, Lij.ctypes.data, Lji.ctypes.data)
         P1, P2 = Lij, Lji
-    if int(pget(pm, "alg_ddmdteq", 0)):
+    ee_mode = pm.get("eeMode", "none")
+    with_ee = ee_mode != "none" and not linear
+    if int(pget(pm, "alg_ddmdteq", 0)) and not with_ee:
         tmp = OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
                            k1st=k1, k2nd=k2, P1=np.ascontiguousarray(P1), P2=np.ascontiguousarray(P2),
                            prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=None, smat=smat, dm0=dm0,
@@ -598,7 +600,6 @@ def load(d: str) -> OracleSystem:
         cs = tmp.cstruct()
         L.orc_compute_ddmdt_eq(C.addressof(cs), f_eq.ctypes.data, ddmdt_eq.ctypes.data)
     ee = None
-    ee_mode = pm.get("eeMode", "none")
     if ee_mode != "none" and not linear:  # (with alg_linearize the e-e term is part of the operators)
         if ee_mode != "Pee_update" or int(pget(pm, "alg_linearize_dPee", 0)):
             raise ValueError("the oracle restates eeMode = Pee_update without linearization")
@@ -610,6 +611,23 @@ def load(d: str) -> OracleSystem:
                            temperature=T, mu=mu, nk_full=sz["nk_full"], ob_prefac=1.0, ode={}, params={})
         ee_operators(tmp, ee, None, np.ascontiguousarray(f_dm[:, bstart:bend]), nfree)
         P1, P2 = ee.P1eff, ee.P2eff
+        if int(pget(pm, "alg_ddmdteq", 0)):
+            # DensityMatrix_Dynamics.h:58-63: reset_scatt at rho_eq = diag(f_eq) (the screening density
+            # from rho_eq when the model updates it, P_ee(rho_eq)), then compute_ddmdt_eq with those
+            # operators; the rebuilds before every RHS start from there
+            dm_eq = np.zeros((nk, nb_dm, nb_dm), np.complex128)
+            dm_eq[:, range(nb_dm), range(nb_dm)] = f_eq
+            y_eq = y_of(dm_eq.reshape(nk, -1))
+            cs = tmp.cstruct()
+            L.orc_ee_rebuild(C.addressof(ee.c), C.addressof(cs), C.c_double(t0), y_eq.ctypes.data)
+            tmp2 = OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
+                                k1st=k1, k2nd=k2, P1=ee.P1eff.copy(), P2=ee.P2eff.copy(),
+                                prefac_eph=2 * math.pi / sz["nk_full"], Hcoh=None, smat=smat, dm0=dm0,
+                                picture_schrodinger=schrod, expt=expt, t0=t0, tstep=0.0, tend=0.0, temperature=T,
+                                mu=mu, nk_full=sz["nk_full"], ob_prefac=1.0, ode={}, params={})
+            ddmdt_eq = np.zeros((nk, nb * nb), np.complex128)
+            cs2 = tmp2.cstruct()
+            L.orc_compute_ddmdt_eq(C.addressof(cs2), f_eq.ctypes.data, ddmdt_eq.ctypes.data)
     return OracleSystem(nk=nk, nb_dm=nb_dm, bstart=bstart, bend=bend, npair=npair, e_dm=e_dm, f_dm=f_dm,
                         k1st=k1, k2nd=k2, P1=P1 if ee is not None else np.ascontiguousarray(P1),
                         P2=P2 if ee is not None else np.ascontiguousarray(P2),

@@ -138,6 +138,15 @@ CASES = {
                                                           smearing_screening=0.004,
                                                           dynamic_screening_ee_two_freqs=1,
                                                           ee_antisymmetry=1))),
+    # e-e with the equilibrium drift subtracted (alg_ddmdteq): the set-up rebuilds P_ee at rho_eq (its
+    # screening density from rho_eq) and the drift is the RHS there; the rebuilds before every RHS then
+    # use rho, the drift stays fixed; carrier density given, e-imp folded in
+    "ee_nb2_rpa_ddmdteq": dict(cfg=SynthConfig(nk=36, nb=2, seed=45, de_pair_mev=60.0, eimp_sigma_mev=5.0, nwannier=4,
+                                               kball=True),
+                               param=dict(Bpert_T=(0, 0, 0.1), B_T=(0.5, 0, 0), eimp_fraction=0.05,
+                                          extra=dict(EE_COMMON, scrFormula="RPA", update_screening=1,
+                                                     alg_ddmdteq=1)),
+                               carrier_scale=1.4),
     # sparse operators (alg_sparseP): 70 % of every pair's P1 / P2 elements zeroed, nb = 4, B field;
     # the reference contracts the stored elements with sparse_zgemm (e-ph only: the reference refuses
     # ab-initio e-imp with sparse P)

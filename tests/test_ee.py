@@ -45,13 +45,22 @@ def ee_desc(s, every_rhs=None):
 
 
 def make_ee_gpu(s, prec="f64", every_rhs=None):
-    """a handle over P_base = P_eph (+ P_eimp) with the e-e model attached (set-up: P_ee at f)"""
+    """a handle over P_base = P_eph (+ P_eimp) with the e-e model attached (set-up: P_ee at f); with
+    the equilibrium drift (alg_ddmdteq) P_ee rebuilt at rho_eq = diag(f_eq) as the reference's set-up
+    does (DensityMatrix_Dynamics.h:58-63) and the drift installed"""
     from denmat_dynm_development_gb300.dmd import LindbladGPU
     dev = prec in ("f32", "bf16x2")
-    return LindbladGPU(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
-                       P1=s.ee.P1base, P2=s.ee.P2base, prefac_eph=s.prefac_eph, Hcoh=s.Hcoh,
-                       picture=s.picture_schrodinger, expt=s.expt, precision=prec,
-                       f_ref=s.f_dm if dev else None, ee=ee_desc(s, every_rhs))
+    g = LindbladGPU(nk=s.nk, nb_dm=s.nb_dm, bstart=s.bstart, bend=s.bend, e_dm=s.e_dm, k1st=s.k1st, k2nd=s.k2nd,
+                    P1=s.ee.P1base, P2=s.ee.P2base, prefac_eph=s.prefac_eph, Hcoh=s.Hcoh,
+                    picture=s.picture_schrodinger, expt=s.expt, precision=prec,
+                    f_ref=s.f_dm if dev else None, ee=ee_desc(s, every_rhs))
+    if s.ddmdt_eq is not None:
+        dm_eq = np.zeros((s.nk, s.nb_dm, s.nb_dm), np.complex128)
+        dm_eq[:, range(s.nb_dm), range(s.nb_dm)] = s.f_eq
+        g.set_state(0.0, np.ascontiguousarray(dm_eq.reshape(s.nk, -1)).view(np.float64).reshape(-1).copy())
+        g.ee_update()
+        g.set_ddmdt_eq(s.ddmdt_eq)
+    return g
 
 
 def fresh(oracle, case):
@@ -75,7 +84,10 @@ def test_ee_setup_and_rebuilds_vs_golden(case, prec, oracle, built):
         e2 = rel(B2 + s.ee.scale * P2, g["ee_P2_eq"])
         print("%s %s set-up: P rel err %.3g %.3g" % (case, prec, e1, e2))
         assert e1 < tol and e2 < tol
-        assert n0 == s.ee.c.nfree
+        if s.ddmdt_eq is None:  # the set-up density itself
+            assert n0 == s.ee.c.nfree
+        else:  # the density of rho_eq, summed on the device
+            assert abs(n0 - s.ee.c.nfree) <= 1e-14 * abs(s.ee.c.nfree)
         for i, (t, y) in enumerate(zip(g["rhs_t"], g["rhs_y"])):
             gpu.set_state(t, y)
             gpu.ee_update()
