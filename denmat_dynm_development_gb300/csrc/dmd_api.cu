@@ -128,6 +128,8 @@ struct dmd_handle {
   double t = 0;                // time of the device state
   long long launches = 0;
   cudaGraphExec_t g_rk4 = nullptr;
+  cudaGraphExec_t g_rk4_rec = nullptr;  // the RK4 step that also copies its stage inputs and sums to d_rec
+  double2* d_rec = nullptr;             // [4][nstate] stage inputs, then [4][nk 2 nb^2] forward sums
   std::string err;
   // timing / profiling
   cudaEvent_t tev[2] = {nullptr, nullptr};
@@ -1298,16 +1300,24 @@ int upload_pairs_tc(dmd_handle* h, const dmd_desc* d) {
   return out;
 }
 
+// the captured RK4 steps hold kernel arguments: capture again at the next use
+void drop_graphs(dmd_handle* h) {
+  if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
+  if (h->g_rk4_rec) cudaGraphExecDestroy(h->g_rk4_rec);
+  h->g_rk4 = h->g_rk4_rec = nullptr;
+}
+
 void release(dmd_handle* h) {
   if (!h) return;
   cudaSetDevice(h->dev);
   if (h->g_rk4) cudaGraphExecDestroy(h->g_rk4);
+  if (h->g_rk4_rec) cudaGraphExecDestroy(h->g_rk4_rec);
   void* ptrs[] = {h->d_err, h->d_pos, h->d_rb, h->d_items, h->d_ew, h->d_edm, h->d_kk, h->d_P, h->d_H, h->d_eq, h->d_rs, h->d_acc, h->d_y, h->d_ytmp,
                   h->d_y0, h->d_in, h->d_in1, h->d_out, h->d_K, h->d_tref, h->d_step, h->d_red, h->d_coef_i,
                   h->d_coef, h->d_flag, h->d_hflag, h->d_acc0, h->d_fref, h->d_tcB, h->d_tcA, h->d_tiles, h->d_ph, h->d_inv, h->d_x0y0, h->d_v0, h->d_Praw, h->d_kkraw,
                   h->d_dst, h->d_ee_kvec, h->d_ee_kidx, h->d_ee_kmap, h->d_ee_U, h->d_ee_ewf, h->d_ee_f,
                   h->d_ee_dm, h->d_ee_dm1, h->d_ee_dmf, h->d_ee_dm1f, h->d_ee_scr, h->d_ee_Pee, h->d_ee_vqtab,
-                  h->d_sp_base, h->d_sp_len, h->d_sp_val, h->d_sp_gidx, h->d_Padf, h->d_ee_Aq, h->d_ee_Eq2};
+                  h->d_sp_base, h->d_sp_len, h->d_sp_val, h->d_sp_gidx, h->d_Padf, h->d_ee_Aq, h->d_ee_Eq2, h->d_rec};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; ++i) {
@@ -1935,10 +1945,7 @@ int dmd_set_ddmdt_eq(dmd_handle* h, const double* eq) {
   if (!h) return DMD_E_ARG;
   CK(cudaSetDevice(h->dev));
   CK(cudaStreamSynchronize(h->st));
-  if (h->g_rk4) {  // the captured step holds the drift pointer: capture again at the next dmd_rk4
-    cudaGraphExecDestroy(h->g_rk4);
-    h->g_rk4 = nullptr;
-  }
+  drop_graphs(h);  // the captured step holds the drift pointer: capture again at the next dmd_rk4
   if (!eq) {
     if (h->d_eq) cudaFree(h->d_eq);
     h->d_eq = nullptr;
@@ -2013,7 +2020,11 @@ int dmd_get_state(dmd_handle* h, double* t, double* y) {
   return DMD_OK;
 }
 
-static int rk4_step_launches(dmd_handle* h) {
+// RK4 step launches (captured into a graph by dmd_rk4). With recU / recA, the step also copies each
+// stage's input (before its evaluation, which may overwrite it with the next stage's) to recU[s] and
+// its forward sums (after the contraction) to recA[s].
+static int rk4_step_launches(dmd_handle* h, double2* recU = nullptr, double2* recA = nullptr) {
+  const size_t na = (size_t)h->nk * 2 * h->nb2;
   for (int s = 0; s < 4; ++s) {
     TimeArg ta;
     ta.t = 0;
@@ -2029,8 +2040,10 @@ static int rk4_step_launches(dmd_handle* h) {
     fa.K = h->d_K;
     fa.ybase = h->d_y;
     fa.ytmp = h->d_ytmp;
+    if (recU) CK(cudaMemcpyAsync(recU + (size_t)s * h->nstate, in, h->nstate * 16, cudaMemcpyDeviceToDevice, h->st));
     int rc = rhs(h, in, ta, fa);
     if (rc) return rc;
+    if (recA) CK(cudaMemcpyAsync(recA + (size_t)s * na, h->d_acc, na * 16, cudaMemcpyDeviceToDevice, h->st));
   }
   {
     ProfScope ps(h, 3);
@@ -2374,7 +2387,50 @@ int dmd_adjoint_rk4(dmd_handle* h, double t0, const double* y0, double dt, int64
     if ((rc = measure_on(h, slot, bstart, bend, cur, t0, &v))) return rc;
     if (s_obs) s_obs[j] = v;
   }
-  for (int64_t s = 0; s < nsteps; ++s) {
+  if (keep_all && !h->prof_on) {
+    // the forward pass as captured RK4 steps (the handle's graph of dmd_rk4 plus copies of every
+    // stage input and forward sums into d_rec), each step's stage data then moved to its slot; the
+    // handle's own state and time are restored afterwards
+    double2* ysave = nullptr;
+    if ((rc = w.get(&ysave, n))) return rc;
+    if (!h->d_rec && (rc = dalloc(h, &h->d_rec, 4 * (n + na)))) return rc;
+    const double tsave = h->t;
+    const double tref[2] = {t0, dt};
+    const long long zero = 0;
+    CK(cudaMemcpyAsync(ysave, h->d_y, n * 16, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_y, w.ck, n * 16, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_tref, tref, 16, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->d_step, &zero, 8, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));  // pageable sources
+    if (!h->g_rk4_rec) {
+      cudaGraph_t g;
+      const long long l0 = h->launches;
+      CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+      rc = rk4_step_launches(h, h->d_rec, h->d_rec + 4 * n);
+      cudaError_t e = cudaStreamEndCapture(h->st, &g);
+      if (rc) return rc;
+      if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&h->g_rk4_rec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return fail(h, DMD_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+      h->launches = l0;
+    }
+    const long long per_step = h->npair ? (h->use_tc ? 21 : h->use_cb ? 17 : 13) : 9;
+    for (int64_t s = 0; s < nsteps; ++s) {
+      CK(cudaGraphLaunch(h->g_rk4_rec, h->st));
+      h->launches += per_step;
+      CK(cudaMemcpyAsync(w.U + (size_t)s * 4 * n, h->d_rec, 4 * n * 16, cudaMemcpyDeviceToDevice, h->st));
+      CK(cudaMemcpyAsync(w.A + (size_t)s * 4 * na, h->d_rec + 4 * n, 4 * na * 16, cudaMemcpyDeviceToDevice, h->st));
+      for (; j < nobs && obs_step[j] == s + 1; ++j) {
+        double v;
+        if ((rc = measure_on(h, slot, bstart, bend, h->d_y, t0 + (double)(s + 1) * dt, &v))) return rc;
+        if (s_obs) s_obs[j] = v;
+      }
+    }
+    CK(cudaMemcpyAsync(h->d_y, ysave, n * 16, cudaMemcpyDeviceToDevice, h->st));
+    h->t = tsave;
+  }
+  for (int64_t s = 0; s < nsteps && !(keep_all && !h->prof_on); ++s) {
     double2* next = ((s + 1) % checkpoint == 0 && (s + 1) < nsteps) ? w.ck + (size_t)((s + 1) / checkpoint) * n
                                                                       : spare[sp];
     if ((rc = adj_rk4_step(h, cur, t0 + (double)s * dt, dt, keep_all ? w.U + (size_t)s * 4 * n : nullptr, next,
@@ -2773,10 +2829,7 @@ int dmd_autotune(dmd_handle* h, int evals, int* chosen) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   *knob = rc ? keep : best;
-  if (h->g_rk4) {  // the captured step holds the old kernels
-    cudaGraphExecDestroy(h->g_rk4);
-    h->g_rk4 = nullptr;
-  }
+  drop_graphs(h);  // the captured step holds the old kernels
   if (rc) return rc;
   if (chosen) *chosen = best;
   return check_state(h);
@@ -2987,10 +3040,7 @@ int dmd_ee_attach(dmd_handle* h, const dmd_ee_desc* ee) {
   h->ee_on = 1;
   if ((rc = ee_rebuild_nb(h, nullptr, time_value(h->t), true))) return rc;
   CK(cudaStreamSynchronize(h->st));
-  if (h->g_rk4) {  // the captured step must include the update
-    cudaGraphExecDestroy(h->g_rk4);
-    h->g_rk4 = nullptr;
-  }
+  drop_graphs(h);  // the captured step must include the update
   return DMD_OK;
 }
 
