@@ -94,3 +94,28 @@ def test_sparse_flag_is_validated_before_any_device_call():
         d = dmd._Desc(nk=4, nb_dm=2, bstart=0, bend=2, nkpair=1, e_dm=e.ctypes.data, k1st=k.ctypes.data,
                       k2nd=k.ctypes.data, P1=P.ctypes.data, P2=P.ctypes.data, precision=prec, flags=flags, nrhs=nrhs)
         assert L.dmd_create(C.byref(d), C.byref(h)) == 1
+
+
+def test_binding_refuses_to_run_without_its_library(monkeypatch):
+    """the Python binding has no host fallback: a missing libdmdgpu.so is an error at first use"""
+    from denmat_dynm_development_gb300 import dmd
+    monkeypatch.setattr(dmd, "_L", None)
+    monkeypatch.setattr(dmd, "GPU_LIB", os.path.join(ROOT, "no_such_dir", "libdmdgpu.so"))
+    with pytest.raises(RuntimeError, match="not built"):
+        dmd.LindbladGPU(nk=1, nb_dm=1, bstart=0, bend=1, e_dm=np.zeros(1), k1st=np.zeros(1, np.uint64),
+                        k2nd=np.zeros(1, np.uint64), P1=np.zeros(1, np.complex128), P2=np.zeros(1, np.complex128),
+                        prefac_eph=1.0)
+
+
+@pytest.mark.skipif(os.path.exists("/dev/nvidia0"), reason="a GPU is present: the handle is created there")
+def test_create_without_a_device_is_an_error_not_a_host_path():
+    """with no CUDA device a valid descriptor gives DMD_E_NODEV (or DMD_E_CUDA): nothing is computed
+    on the host instead"""
+    from denmat_dynm_development_gb300 import dmd
+    nk, nb = 2, 2
+    e = np.array([[0.0, 0.01], [0.002, 0.012]])
+    with pytest.raises(dmd.DMDError) as ei:
+        dmd.LindbladGPU(nk=nk, nb_dm=nb, bstart=0, bend=nb, e_dm=e, k1st=np.array([0], np.uint64),
+                        k2nd=np.array([1], np.uint64), P1=np.zeros(nb ** 4, np.complex128),
+                        P2=np.zeros(nb ** 4, np.complex128), prefac_eph=1.0)
+    assert ei.value.status in (4, 8)
