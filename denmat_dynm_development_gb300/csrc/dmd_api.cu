@@ -1469,11 +1469,9 @@ template <int NST, int W>
 int adj_bulk4_launch_shape(dmd_handle* h, const int2* kk, const float4* dfv, size_t nk2, double* rtb, double* stb,
                            float4* G) {
   typedef AdjBulkSmem<NST, W> S;
-  static bool attr_set = false;
-  if (!attr_set) {
-    CK(cudaFuncSetAttribute(k_adj_pairs_bulk4<NST, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::cta_bytes));
-    attr_set = true;
-  }
+  // set on every launch: the attribute belongs to the current device's context, and handles may
+  // live on different devices
+  CK(cudaFuncSetAttribute(k_adj_pairs_bulk4<NST, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::cta_bytes));
   int nsm = 0;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev) != cudaSuccess || nsm <= 0) nsm = 1;
   const long long ctas = std::min<long long>((long long)nsm * 2, (h->npair + S::warps - 1) / S::warps);
