@@ -54,7 +54,7 @@ def _objective(s, y0, dt, steps, w, P1=None, P2=None):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("keep", ["1", "0"])
-@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_schrod", "nb4_eimp_B"])
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_schrod", "nb4_eimp_B", "nb2_window"])
 def test_adjoint_directional_derivatives_vs_fd(case, keep, oracle, built, monkeypatch):
     """keep = 1: the forward pass keeps every stage (these sizes fit); keep = 0: the backward pass
     recomputes stretches of 7 steps from checkpoints"""
@@ -94,7 +94,51 @@ def test_adjoint_directional_derivatives_vs_fd(case, keep, oracle, built, monkey
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_schrod", "nb4_eimp_B"])
+@pytest.mark.parametrize("nb_dm,bstart,bend,npair,picture", [(3, 0, 3, 90, 0), (1, 0, 1, 60, 1), (3, 1, 2, 50, 1)])
+def test_adjoint_generic_windows_vs_fd(nb_dm, bstart, bend, npair, picture, oracle, built):
+    """nb = 1 and 3 windows (FP64 handles on the per-thread pair kernels, one window inside the density
+    matrix), both pictures, random operators and a random Hermitian observable: dJ/dP and dJ/dy0 of
+    the adjoint against central differences of the GPU forward"""
+    from test_gpu_parity import _random_system
+    s = _random_system(oracle, 17, nb_dm, bstart, bend, npair, seed=100 + nb_dm * 10 + npair, picture=picture)
+    rng = np.random.default_rng(11)
+    ob = rng.standard_normal((s.nk, nb_dm, nb_dm)) + 1j * rng.standard_normal((s.nk, nb_dm, nb_dm))
+    ob = 0.5 * (ob + np.conj(np.swapaxes(ob, 1, 2)))
+    smat = np.zeros((s.nk, 3, nb_dm * nb_dm), np.complex128)
+    smat[:, 2, :] = ob.reshape(s.nk, -1)
+    s = dataclasses.replace(s, smat=smat)
+    dt = 2.0 * oracle.fs
+    steps = np.array([0, 6, 13, 21])
+    w = rng.standard_normal(steps.size)
+    y0 = oracle.y_of(s.dm0)
+    with _gpu(s, adjoint=True) as g:
+        sv, dP, dy0 = g.adjoint_rk4(s.t0, y0, dt, int(steps[-1]), steps, w, slot=0, bstart=s.nv_dm, checkpoint=5,
+                                    want_dy0=True)
+    J0, s_fwd = _objective(s, y0, dt, steps, w)
+    assert rel(sv, s_fwd) < 1e-12
+    n = s.P1.size
+    d1 = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * np.abs(s.P1).max()
+    d2 = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) * np.abs(s.P2).max()
+    jp, _ = _objective(s, y0, dt, steps, w, s.P1 + FD_H * d1, s.P2 + FD_H * d2)
+    jm, _ = _objective(s, y0, dt, steps, w, s.P1 - FD_H * d1, s.P2 - FD_H * d2)
+    fd = (jp - jm) / (2 * FD_H)
+    ad = np.vdot(dP[0].reshape(-1), d1).real + np.vdot(dP[1].reshape(-1), d2).real
+    dm = rng.standard_normal(s.dm0.shape) + 1j * rng.standard_normal(s.dm0.shape)
+    dm = dm.reshape(s.nk, nb_dm, nb_dm)
+    dm = 0.5 * (dm + np.conj(np.swapaxes(dm, 1, 2)))
+    dy = oracle.y_of(dm.reshape(s.nk, -1)) * 1e-3
+    jp, _ = _objective(s, y0 + FD_H * dy, dt, steps, w)
+    jm, _ = _objective(s, y0 - FD_H * dy, dt, steps, w)
+    fdy = (jp - jm) / (2 * FD_H)
+    ady = float(np.dot(dy0, dy))
+    print("nb_dm %d window [%d,%d) picture %d: dJ/dP rel %.3g, dJ/dy0 rel %.3g"
+          % (nb_dm, bstart, bend, picture, abs(ad - fd) / abs(fd), abs(ady - fdy) / abs(fdy)))
+    assert abs(ad - fd) <= TOL * abs(fd)
+    assert abs(ady - fdy) <= TOL * abs(fdy)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_schrod", "nb4_eimp_B", "nb2_window"])
 def test_double_float_backward_matches_fp64(case, oracle, built):
     """a double-float ("f64x") handle runs the backward pair pass in double-float arithmetic
     (k_adj_pairs_df, gradient kept as double-floats): its dJ/dP and dJ/dy0 equal the FP64 handle's
