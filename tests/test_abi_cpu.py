@@ -119,3 +119,48 @@ def test_create_without_a_device_is_an_error_not_a_host_path():
                         k2nd=np.array([1], np.uint64), P1=np.zeros(nb ** 4, np.complex128),
                         P2=np.zeros(nb ** 4, np.complex128), prefac_eph=1.0)
     assert ei.value.status in (4, 8)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "dmd_gpu.h"
+#include "dmd_host.h"
+
+int main(void) {
+  dmd_handle* h = 0;
+  dmdh_system* s = 0;
+  double e[3] = {-0.01, 0.0, 0.01}, f[3];
+  if (strcmp(dmd_strerror(DMD_OK), "ok") != 0) return 1;
+  if (dmd_create(0, &h) != DMD_E_ARG) return 2;              /* null descriptor */
+  if (dmdh_load("/nonexistent/ldbd/dir", &s) == 0) return 3; /* missing inputs */
+  if (dmdh_error() == 0 || dmdh_error()[0] == 0) return 4;
+  if (dmdh_fermi(1e-3, 0.0, e, f, 3) != 0) return 5;         /* host arithmetic, no device */
+  printf("%.17g %.17g %.17g\n", f[0], f[1], f[2]);
+  return 0;
+}
+"""
+
+
+def test_plain_c_caller_links_and_calls_the_abi(tmp_path):
+    """The public headers are plain C (C99, no C++ types): a C program includes both, links
+    libdmdgpu.so and libdmdhost.so, and calls entry points that need no device"""
+    import shutil
+    import subprocess
+    from denmat_dynm_development_gb300 import build as B
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    B.build_gpu()
+    B.build_host()
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(B.GPU_LIB)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-o", str(exe), "-L", libdir, "-ldmdhost", "-ldmdgpu", "-Wl,-rpath," + libdir],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stderr)
+    f = np.array([float(x) for x in out.stdout.split()])
+    from denmat_dynm_development_gb300 import host as H
+    np.testing.assert_array_equal(f, H.fermi(1e-3, 0.0, np.array([-0.01, 0.0, 0.01])))
