@@ -13,10 +13,11 @@ seeded generator) and runs the shim-built reference program on it:
   * rhs   -- func / evolve_driver / evolve_coh on three states;
   * rk4   -- 40 classic RK4 steps through DMD's func, S_z every 5 steps;
   * gsl   -- DMD's own evolve_gsl (RKF45) for 20 output intervals (S_z file + restart state);
+  * euler -- DMD's own evolve_euler for 20 steps of tstep (S_z file + restart state);
   * pee   -- (e-e cases) the operators rebuilt on the three states by reset_scatt: screening density
              from the state, P = P_eph (+ P_eimp) + scale_ee P_ee(rho).
 The e-e cases rebuild P_ee on every RHS evaluation (eeMode = Pee_update, freq_update_ee_model < 0),
-so their rhs / rk4 / gsl records include the rebuild.
+so their rhs / rk4 / gsl / euler records include the rebuild.
 The outputs are stored in golden.npz next to the inputs. Nothing here runs at test time.
 """
 from __future__ import annotations
@@ -276,6 +277,10 @@ def make_case(name, spec, ref_bin, outroot):
     out["gsl_sz"] = read_s_file(os.path.join(tmp, "sz_elec_tot.out"))
     out["gsl_ncalls"] = np.array([int(m) for m in re.findall(r"ncalls= (\d+) at ti=", log)])
     out["gsl_y"] = np.fromfile(os.path.join(tmp, "restart", "denmat_restart.bin"))
+    # euler: DMD's evolve_euler to tend = 20 fs in steps of tstep = 1 fs
+    run(ref_bin, tmp, "euler")
+    out["euler_sz"] = read_s_file(os.path.join(tmp, "sz_elec_tot.out"))
+    out["euler_y"] = np.fromfile(os.path.join(tmp, "restart", "denmat_restart.bin"))
     np.savez_compressed(os.path.join(d, "golden.npz"), **out)
     shutil.rmtree(tmp)
     return info

@@ -91,6 +91,29 @@ def test_rkf45_gsl_driver(case, oracle):
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_euler_driver(case, oracle):
+    """DMD's own evolve_euler (DensityMatrix_Dynamics.h:176-186, 229-233): steps of tstep while
+    t < tend, t advanced by repeated addition (the loop takes a 21st step when 20 sums of 1 fs fall
+    short of tend), dm += dt/2 (ddmdt + ddmdt^dagger) (update_dm_euler, DenMat.cpp:236-248); the
+    final state bitwise and S_z at every step to the S file's printed digits"""
+    d, g, s = _load(case, oracle)
+    y = oracle.y_of(s.dm0)
+    t = s.t0
+    rec = []
+    while t < s.tend:
+        y = oracle.euler(s, t, s.tstep, 1, y)
+        t += s.tstep
+        rec.append((t,) + oracle.measure(s, y, t))
+    np.testing.assert_array_equal(y, g["euler_y"])
+    rec = np.array(rec)
+    ref = g["euler_sz"][1:]  # first row is report(0) at t0
+    assert rec.shape[0] == ref.shape[0]
+    np.testing.assert_allclose(rec[:, 0], ref[:, 0], rtol=2e-14)
+    np.testing.assert_allclose(rec[:, 1], ref[:, 1], rtol=2e-14, atol=1e-300)
+    np.testing.assert_allclose(rec[:, 2], ref[:, 2], rtol=2e-14, atol=1e-300)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_hermiticity_of_rhs(case, oracle):
     """dρ/dt is exactly Hermitian: (c + c†)/2 in the finish (evolve_eph.cpp:149-151)."""
     d, g, s = _load(case, oracle)
