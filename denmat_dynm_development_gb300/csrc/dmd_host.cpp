@@ -5,6 +5,7 @@
 
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cfloat>
 #include <cmath>
@@ -230,6 +231,8 @@ struct dmdh_system {
   // e-e model (eeMode): the descriptor for dmd_ee_attach and the arrays it points into
   int ee = 0;                        // 1: Pee_update, 2: Pee_fixed_at_eq
   int ee_freq = 0;                   // freq_update_ee_model (> 0: update between output steps)
+  int64_t freq_measure = 1;          // S files every freq_measure-th step (report, DensityMatrix_Dynamics.h:323)
+  int64_t freq_compute_tau = 10;     // tau files every freq_compute_tau-th step (:211, 230)
   std::vector<double> kvec, U, f_win;
   dmd_ee_desc eed;
 };
@@ -792,6 +795,10 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
   in.ode_hmin = pget(pm, "ode_hmin", 0, kFs);
   in.ode_hmax = pget(pm, "ode_hmax", in.tstep / kFs, kFs);
   in.ode_epsabs = pget(pm, "ode_epsabs", 1e-8);
+  // measurement frequencies (parameters.cpp:324-326); DMD takes them modulo, so they must be >= 1
+  s->freq_measure = (int64_t)pget(pm, "freq_measure", 1);
+  s->freq_compute_tau = (int64_t)pget(pm, "freq_compute_tau", (double)(int64_t)pget(pm, "freq_measure_ene", 10));
+  if (s->freq_measure < 1 || s->freq_compute_tau < 1) return err(DMD_E_ARG, "freq_measure and freq_compute_tau must be >= 1");
   const std::string om = sget(pm, "alg_ode_method", "rkf45");
   in.ode_method = om == "rkf45" ? 0 : om == "euler" ? 1 : om == "rk4" ? 2 : -1;
   if (in.ode_method < 0) return err(DMD_E_ARG, "alg_ode_method must be rkf45, euler or rk4");
@@ -1102,6 +1109,7 @@ struct Reporter {
   std::string dir;
   int nv_dm, nb_dm;
   dmd_handle* h;
+  int64_t freq_measure;
   // observable.h:169-183 (header) and 368-383 (one line per output step)
   int write_line(const std::string& what, const std::string& scarr, double t, double tot, double amp) {
     const std::string fname = dir + "/" + what + scarr + "_tot.out";
@@ -1117,6 +1125,7 @@ struct Reporter {
   }
   int report(int it, double t, std::vector<double>& ybuf) {
     int rc;
+    if (it % freq_measure != 0) return DMD_OK;  // DensityMatrix_Dynamics.h:323
     if (it > 0) {  // singdenmat_k::write_dm_tofile (DenMat.cpp:318-334), written to a temp name then renamed
       double tt;
       if ((rc = dmd_get_state(h, &tt, ybuf.data()))) return err(rc, dmd_last_error(h));
@@ -1151,7 +1160,109 @@ struct Reporter {
   }
 };
 
+const double kPs = 1000 * kFs;  // comm/Units.h
+
+// one line of tau_<what><scarr>_tot.out (observable.h:185-191 header, 392-401 line)
+int write_tau_line(const std::string& dir, const std::string& what, const std::string& scarr, double t,
+                   const double tau[3], int32_t picture) {
+  const std::string fname = dir + "/tau_" + what + scarr + "_tot.out";
+  const bool fresh = !exists(fname);
+  FILE* f = fopen(fname.c_str(), "a");
+  if (!f) return err(DMD_E_FILE, "cannot write " + fname);
+  if (fresh) fprintf(f, "#time(au), tau by FD, tau without precession, tau\n");
+  if (picture == DMD_PICTURE_INTERACTION) {
+    if (fabs(t) < 1e-30)
+      fprintf(f, " 0.0000000000e+01 fs: %14.7le %14.7le %14.7le ps\n", tau[0] / kPs, tau[1] / kPs, tau[2] / kPs);
+    else
+      fprintf(f, "%17.10le fs: %14.7le %14.7le %14.7le ps\n", t / kFs, tau[0] / kPs, tau[1] / kPs, tau[2] / kPs);
+  } else {
+    if (fabs(t) < 1e-30) fprintf(f, " 0.0000000000e+01 fs: %14.7le ps\n", tau[1] / kPs);
+    else fprintf(f, "%17.10le fs: %14.7le ps\n", t / kFs, tau[1] / kPs);
+  }
+  fclose(f);
+  return DMD_OK;
+}
+
 }  // namespace
+
+extern "C" int dmdh_tau(int32_t nk, int32_t nb, const double* obs, const double* e, const double* f,
+                        const double* dm, const double* ddmdt, double t, double dt, int32_t picture, int32_t bstart,
+                        int32_t bend, double prefac, double out[3]) {
+  if (nk <= 0 || nb <= 0 || !obs || !e || !f || !dm || !ddmdt || !out || bstart < 0 || bend > nb || bstart >= bend)
+    return DMD_E_ARG;
+  const bool inter = picture == DMD_PICTURE_INTERACTION;
+  const size_t nb2 = (size_t)nb * nb;
+  double tot = 0, tot_tplusdt = 0, dottot = 0, dottot_term2 = 0;
+  for (int ik = 0; ik < nk; ik++) {
+    const zc* ok = (const zc*)obs + (size_t)ik * nb2;
+    const zc* dk = (const zc*)dm + (size_t)ik * nb2;
+    const zc* gk = (const zc*)ddmdt + (size_t)ik * nb2;
+    const double* ek = e + (size_t)ik * nb;
+    const double* fk = f + (size_t)ik * nb;
+    for (int i = bstart; i < bend; i++) {
+      double ob = 0, dot = 0, ob_tplusdt = 0, dot_term2 = 0;
+      for (int b = 0; b < nb; b++) {
+        const zc o = ok[i * nb + b];
+        const zc ot = (i == b || !inter) ? o : zmul(o, zcis((ek[i] - ek[b]) * t));
+        zc dkbi = dk[b * nb + i];
+        if (i == b) dkbi.x = dkbi.x - fk[i];
+        ob += zmul(ot, dkbi).x;
+        dot += zmul(ot, gk[b * nb + i]).x;
+        const zc ctmp = zmul(ot, dkbi);
+        if (inter) dot_term2 -= 2 * (ctmp.y * ek[i]);
+        if (dt > 0) {
+          const zc otp = (i == b || !inter) ? o : zmul(o, zcis((ek[i] - ek[b]) * (t + dt)));
+          zc dp = zadd(dk[b * nb + i], zscale(dt, gk[b * nb + i]));
+          if (i == b) dp.x = dp.x - fk[i];
+          ob_tplusdt += zmul(otp, dp).x;
+        }
+      }
+      tot += ob;
+      tot_tplusdt += ob_tplusdt;
+      dottot += dot;
+      dottot_term2 += dot_term2;
+    }
+  }
+  tot *= prefac;
+  tot_tplusdt *= prefac;
+  dottot *= prefac;
+  dottot_term2 *= prefac;
+  out[0] = (dt == 0) ? 0 : -tot * dt / (tot_tplusdt - tot);
+  out[1] = -tot / dottot;
+  out[2] = -tot / (dottot + dottot_term2);
+  return DMD_OK;
+}
+
+extern "C" int dmdh_report_tau(const dmdh_system* s, const char* dir, double t, const double* y, const double* dydt) {
+  if (!s || !dir || !y || !dydt) return DMD_E_ARG;
+  const dmdh_info& in = s->info;
+  const int nk = in.nk, nb = in.nb_dm, nv = in.nv_dm;
+  const size_t nd2 = (size_t)nb * nb;
+  const double dt = std::min(in.ode_hstart, std::min(in.tstep / 10, in.tstep / 10));  // dt_tiny, tstep_laser = tstep
+  const double bl = sqrt(in.Bpert[0] * in.Bpert[0] + in.Bpert[1] * in.Bpert[1] + in.Bpert[2] * in.Bpert[2]);
+  const char* names[3] = {"sx", "sy", "sz"};
+  std::vector<double> obs(nd2 * 2 * nk);
+  for (int d = 0; d < 3; ++d) {
+    if (bl > 1e-10 && in.Bpert[d] == 0) continue;  // DensityMatrix_Dynamics.h:350-352
+    for (int ik = 0; ik < nk; ++ik)
+      memcpy(&obs[(size_t)ik * nd2 * 2], &s->smat[((size_t)ik * 3 + d) * nd2 * 2], nd2 * 16);
+    double tau[3];
+    int rc;
+    if (nb > nv) {
+      if ((rc = dmdh_tau(nk, nb, obs.data(), s->e_dm.data(), s->f_dm.data(), y, dydt, t, dt, in.picture, nv, nb,
+                         in.ob_prefac, tau)) ||
+          (rc = write_tau_line(dir, names[d], "_elec", t, tau, in.picture)))
+        return rc;
+    }
+    if (nv > 0) {
+      if ((rc = dmdh_tau(nk, nb, obs.data(), s->e_dm.data(), s->f_dm.data(), y, dydt, t, dt, in.picture, 0, nv,
+                         in.ob_prefac, tau)) ||
+          (rc = write_tau_line(dir, names[d], "_hole", t, tau, in.picture)))
+        return rc;
+    }
+  }
+  return DMD_OK;
+}
 
 extern "C" int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max) {
   dmdh_system* s = nullptr;
@@ -1179,7 +1290,17 @@ extern "C" int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max) 
     if ((rc = dmd_set_observable(h, dirn, obs.data(), s->f_dm.data(), in.ob_prefac))) return err(rc, dmd_last_error(h));
   }
   mkdir((std::string(dir) + "/restart").c_str(), 0755);
-  Reporter rep{dir, in.nv_dm, in.nb_dm, h};
+  Reporter rep{dir, in.nv_dm, in.nb_dm, h, s->freq_measure};
+  std::vector<double> dbuf(ny);
+  // compute + report_tau from the state before the step (DensityMatrix_Dynamics.h:211, 229-230):
+  // the right-hand side through the GSL-callback entry, which leaves the handle's state alone
+  auto tau_report = [&]() -> int {
+    double tt;
+    int r;
+    if ((r = dmd_get_state(h, &tt, ybuf.data())) || (r = dmd_func(h, tt, ybuf.data(), dbuf.data())))
+      return err(r, dmd_last_error(h));
+    return dmdh_report_tau(s, dir, tt, ybuf.data(), dbuf.data());
+  };
   if ((rc = rep.report(0, in.t0, ybuf))) return rc;
   double t = in.t0, ti = in.t0, hs = in.ode_hstart;
   const std::string stopfile = std::string(dir) + "/EXIT_DMD";
@@ -1188,10 +1309,13 @@ extern "C" int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max) 
       remove(stopfile.c_str());
       break;
     }
+    const bool tau_now = (it - 1) % s->freq_compute_tau == 0;
+    if (tau_now && in.ode_method != 1 && (rc = tau_report())) return rc;  // evolve_gsl: before the update
     ti += in.tstep;
     // update_scatt_outside (DensityMatrix_Dynamics.h:216-217, 290-299): the e-e operators from the
     // state before every freq_update_ee_model-th step
     if (s->ee_freq > 0 && (it - 1) % s->ee_freq == 0 && (rc = dmd_ee_update(h))) return err(rc, dmd_last_error(h));
+    if (tau_now && in.ode_method == 1 && (rc = tau_report())) return rc;  // evolve_euler: after it
     int64_t nfev = 0;
     if (in.ode_method == 0) rc = dmd_rkf45_apply(h, ti, &hs, in.ode_hmin, in.ode_hmax, in.ode_epsabs, 0.0, &nfev);
     else if (in.ode_method == 1) rc = dmd_euler(h, in.tstep, 1), nfev = 1;

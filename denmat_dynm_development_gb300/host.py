@@ -14,7 +14,7 @@ _L = None
 
 EXPORTS = ["dmdh_load", "dmdh_free", "dmdh_error", "dmdh_info_get", "dmdh_desc", "dmdh_get_dm0", "dmdh_get_f",
            "dmdh_get_smat", "dmdh_get_f_eq", "dmdh_prepare", "dmdh_param", "dmdh_fermi", "dmdh_dm_bpert",
-           "dmdh_H_BS", "dmdh_run", "dmdh_ee_desc", "dmdh_rk4_func"]
+           "dmdh_H_BS", "dmdh_run", "dmdh_ee_desc", "dmdh_rk4_func", "dmdh_tau", "dmdh_report_tau"]
 
 
 class Info(C.Structure):
@@ -53,6 +53,8 @@ def _lib():
         L.dmdh_H_BS.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, C.c_int32, vp]
         L.dmdh_run.argtypes = [C.c_char_p, C.c_int32, C.c_int64]
         L.dmdh_rk4_func.argtypes = [vp, d, d, C.c_int64, vp, C.c_size_t, vp]
+        L.dmdh_tau.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, vp, d, d, C.c_int32, C.c_int32, C.c_int32, d, vp]
+        L.dmdh_report_tau.argtypes = [vp, C.c_char_p, d, vp, vp]
         _L = L
     return _L
 
@@ -148,6 +150,14 @@ class System:
             raise
         return g
 
+    def report_tau(self, directory: str, t: float, y, dydt):
+        """DMD's report_tau at (t, y) with dydt the right-hand side there: appends the lines of
+        tau_s{x,y,z}_{elec,hole}_tot.out in directory"""
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        dydt = np.ascontiguousarray(dydt, dtype=np.float64)
+        assert y.size == dydt.size == 2 * self.nk * self.nb_dm ** 2
+        _ck(_lib().dmdh_report_tau(self._h, directory.encode(), float(t), y.ctypes.data, dydt.ctypes.data))
+
     def close(self):
         if getattr(self, "_h", None):
             _lib().dmdh_free(self._h)
@@ -187,6 +197,22 @@ def H_BS(smat, B, e, picture=0):
     H = np.zeros((nk, nb * nb), np.complex128)
     _ck(_lib().dmdh_H_BS(nk, nb, smat.ctypes.data, Bv.ctypes.data, e.ctypes.data, picture, H.ctypes.data))
     return H
+
+
+def tau(obs, e, f, dm, ddmdt, t, dt, picture=0, bstart=0, bend=None, prefac=1.0):
+    """Instantaneous lifetimes (tau by finite difference over dt, without precession, with it; atomic
+    units) of one observable (complex [nk][nb^2]) over bands [bstart, bend) from the state dm and
+    its time derivative ddmdt (complex [nk][nb^2])"""
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    nk, nb = e.shape
+    obs, dm, ddmdt = (np.ascontiguousarray(a, dtype=np.complex128) for a in (obs, dm, ddmdt))
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    assert obs.size == dm.size == ddmdt.size == nk * nb * nb and f.size == nk * nb
+    out = np.zeros(3)
+    _ck(_lib().dmdh_tau(nk, nb, obs.ctypes.data, e.ctypes.data, f.ctypes.data, dm.ctypes.data, ddmdt.ctypes.data,
+                        float(t), float(dt), int(picture), int(bstart), int(nb if bend is None else bend),
+                        float(prefac), out.ctypes.data))
+    return out
 
 
 def rk4_func(handle, t, dt, nsteps, y, work):

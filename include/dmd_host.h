@@ -16,6 +16,8 @@
  *   dmdh_run             dm_dynamics_jdftx + dm_dynamics::evolve_gsl / evolve_euler
  *                        (main.cpp:38-84, DensityMatrix_Dynamics.h:177-225), S files as
  *                        ob_1dmk::measure writes them (observable.h:145-193, 368-404)
+ *   dmdh_tau             ob_1dmk::measure_brange with ddmdt (observable.h:185-191, 297-336, 356-365, 392-401)
+ *   dmdh_report_tau      dm_dynamics::report_tau (DensityMatrix_Dynamics.h:347-354, dt_tiny :236-238)
  */
 #ifndef DMD_HOST_H
 #define DMD_HOST_H
@@ -89,8 +91,24 @@ int dmdh_H_BS(int32_t nk, int32_t nb, const double* smat, const double B[3], con
  * makes the copies direct). */
 int dmdh_rk4_func(dmd_handle* h, double t, double dt, int64_t nsteps, double* y, size_t n, double* work);
 
+/* Instantaneous lifetimes of one observable over bands [bstart, bend) of nb from the state dm and
+ * its time derivative ddmdt at time t (complex [nk][nb^2] each; obs: complex [nk][nb^2], the
+ * observable's matrices; e, f: double [nk][nb]; prefac: the observable's density prefactor):
+ * out[0] = -S dt / (S(t + dt) - S) with S(t + dt) from dm + dt ddmdt (0 when dt = 0),
+ * out[1] = -S / dS (without the precession term), out[2] = -S / (dS + precession term); atomic
+ * units; the precession term is that of the interaction picture (0 in the Schrodinger picture). */
+int dmdh_tau(int32_t nk, int32_t nb, const double* obs, const double* e, const double* f, const double* dm,
+             const double* ddmdt, double t, double dt, int32_t picture, int32_t bstart, int32_t bend,
+             double prefac, double out[3]);
+/* DMD's report_tau for a loaded system at (t, y) with dydt = the right-hand side there (dmd_func):
+ * appends one line per spin direction that param.in's Bpert selects (all three without Bpert) to
+ * tau_s{x,y,z}_elec_tot.out (and _hole with valence bands) in dir, with dt = min(ode_hstart,
+ * tstep / 10). */
+int dmdh_report_tau(const dmdh_system* s, const char* dir, double t, const double* y, const double* dydt);
+
 /* DMD's time loop on the GPU: evolve_gsl (rkf45), evolve_euler, or fixed-step RK4, writing
- * sx/sy/sz_elec_tot.out into dir after every output step. nsteps_max < 0 runs to tend. */
+ * sx/sy/sz_elec_tot.out into dir every freq_measure-th step and the tau files (dmdh_report_tau)
+ * every freq_compute_tau-th step. nsteps_max < 0 runs to tend. */
 int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max);
 
 #ifdef __cplusplus

@@ -12,7 +12,8 @@ seeded generator) and runs the shim-built reference program on it:
   * dump  -- setup arrays (initial density matrix, H_BS, occupations);
   * rhs   -- func / evolve_driver / evolve_coh on three states;
   * rk4   -- 40 classic RK4 steps through DMD's func, S_z every 5 steps;
-  * gsl   -- DMD's own evolve_gsl (RKF45) for 20 output intervals (S_z file + restart state);
+  * gsl   -- DMD's own evolve_gsl (RKF45) for 20 output intervals (S_z file + restart state, and the
+             tau files of its report_tau at t0);
   * euler -- DMD's own evolve_euler for 20 steps of tstep (S_z file + restart state);
   * pee   -- (e-e cases) the operators rebuilt on the three states by reset_scatt: screening density
              from the state, P = P_eph (+ P_eimp) + scale_ee P_ee(rho).
@@ -277,6 +278,10 @@ def make_case(name, spec, ref_bin, outroot):
     out["gsl_sz"] = read_s_file(os.path.join(tmp, "sz_elec_tot.out"))
     out["gsl_ncalls"] = np.array([int(m) for m in re.findall(r"ncalls= (\d+) at ti=", log)])
     out["gsl_y"] = np.fromfile(os.path.join(tmp, "restart", "denmat_restart.bin"))
+    # the tau files evolve_gsl wrote at its first step (compute + report_tau at t0), as text
+    tau_files = sorted(f for f in os.listdir(tmp) if f.startswith("tau_") and f.endswith("_tot.out"))
+    out["gsl_tau_names"] = np.array(tau_files)
+    out["gsl_tau_text"] = np.array([open(os.path.join(tmp, f)).read() for f in tau_files])
     # euler: DMD's evolve_euler to tend = 20 fs in steps of tstep = 1 fs
     run(ref_bin, tmp, "euler")
     out["euler_sz"] = read_s_file(os.path.join(tmp, "sz_elec_tot.out"))

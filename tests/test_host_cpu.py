@@ -6,7 +6,7 @@ import shutil
 import numpy as np
 import pytest
 
-from conftest import EE_CASES, FIXED_P_CASES, GOLDEN, ROOT
+from conftest import EE_CASES, FIXED_P_CASES, GOLDEN, GOLDEN_CASES, ROOT
 
 
 @pytest.fixture(scope="module")
@@ -198,3 +198,48 @@ def test_rk4_func_validates_its_arguments(host):
     assert L.dmdh_rk4_func(C.c_void_p(1), 0.0, 1.0, 1, None, y.size, w.ctypes.data) == 1
     assert L.dmdh_rk4_func(C.c_void_p(1), 0.0, 1.0, 1, y.ctypes.data, y.size, None) == 1
     assert L.dmdh_rk4_func(C.c_void_p(1), 0.0, 1.0, -1, y.ctypes.data, y.size, w.ctypes.data) == 1
+
+
+# the linearized e-e cases load through a GPU handle (their e-e source is built there)
+TAU_CPU_CASES = [c for c in GOLDEN_CASES if not (c.startswith("ee_") and "linear" in c)]
+
+
+@pytest.mark.parametrize("case", TAU_CPU_CASES)
+def test_report_tau_writes_the_reference_files(case, host, oracle, tmp_path):
+    """dmdh_report_tau at t0 on the set-up state, with dydt the oracle's right-hand side there (the
+    oracle equals DMD's func bit for bit), writes the tau files that DMD's evolve_gsl writes at its
+    first step (compute + report_tau), byte for byte: the spin directions Bpert selects, electron and
+    hole ranges, both pictures' line formats"""
+    d = os.path.join(GOLDEN, case)
+    g = np.load(os.path.join(d, "golden.npz"))
+    s = host.System(d)
+    try:
+        so = oracle.load(d)
+        y0 = s.y0()
+        s.report_tau(str(tmp_path), so.t0, y0, oracle.rhs(so, so.t0, y0))
+    finally:
+        s.close()
+    names = sorted(f for f in os.listdir(str(tmp_path)) if f.startswith("tau_"))
+    assert names == [str(n) for n in g["gsl_tau_names"]]
+    for n, text in zip(names, g["gsl_tau_text"]):
+        with open(os.path.join(str(tmp_path), n)) as f:
+            assert f.read() == str(text), n
+
+
+def test_tau_of_a_pure_decay():
+    """tau of an observable whose deviation decays as dS/dt = -S/T1 is T1 (without precession)"""
+    from denmat_dynm_development_gb300 import host as H
+    rng = np.random.default_rng(4)
+    nk, nb = 5, 2
+    e = np.sort(rng.uniform(0, 0.01, (nk, nb)), axis=1)
+    f = rng.uniform(0.1, 0.9, (nk, nb))
+    obs = rng.standard_normal((nk, nb, nb)) + 1j * rng.standard_normal((nk, nb, nb))
+    obs = 0.5 * (obs + np.conj(np.swapaxes(obs, 1, 2)))
+    dev = 1e-3 * (rng.standard_normal((nk, nb, nb)) + 1j * rng.standard_normal((nk, nb, nb)))
+    dev = 0.5 * (dev + np.conj(np.swapaxes(dev, 1, 2)))
+    dm = dev.copy()
+    dm[:, range(nb), range(nb)] += f
+    T1 = 1234.5
+    tau = H.tau(obs.reshape(nk, -1), e, f, dm.reshape(nk, -1), (-dev / T1).reshape(nk, -1), 0.0, 0.0, picture=1)
+    assert tau[0] == 0.0
+    assert abs(tau[1] - T1) <= 1e-12 * T1 and abs(tau[2] - T1) <= 1e-12 * T1

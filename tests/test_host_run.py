@@ -1,0 +1,81 @@
+"""DMD's whole time loop through the host library (dmdh_run) against the reference's own run.
+
+dmdh_run reads param.in and ldbd_data/ from a directory, sets the system up, and runs DMD's
+evolve_gsl loop on the GPU, writing DMD's output files there. The golden fixtures hold what the
+reference program wrote for the same directory: the S_z file of evolve_gsl (20 output intervals),
+its final state (restart/denmat_restart.bin), the tau files of its report_tau at t0, and the RHS
+calls per interval. Tolerances: S(t) and the state 1e-10 (the FP64 bound), the tau files to the
+printed digits (%14.7le), the RHS-call counts exactly.
+"""
+import os
+import re
+import shutil
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+RUN_CASES = ["nb2_eimp_B", "nb2_holes_eq", "nb2_schrod", "nb4_eimp_B", "ee_nb2_debye"]
+
+
+def read_s_file(path):
+    rows = []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("#") or not line.strip():
+                continue
+            rows.append([float(x) for x in line.split()])
+    return np.array(rows)
+
+
+def tau_numbers(text):
+    """the numbers of a tau file's lines ('<t> fs: <tau> ... ps')"""
+    out = []
+    for line in text.splitlines():
+        if line.startswith("#") or not line.strip():
+            continue
+        out.append([float(x) for x in line.replace("fs:", " ").replace("ps", " ").split()])
+    return np.array(out)
+
+
+def check_run_dir(rundir, g, stdout):
+    """compare a run directory (and the run's standard output) with a case's golden records"""
+    def rel(a, b):
+        return float(np.abs(a - b).max() / np.abs(b).max())
+    sz = read_s_file(os.path.join(rundir, "sz_elec_tot.out"))
+    ref = g["gsl_sz"]
+    assert sz.shape == ref.shape, (sz.shape, ref.shape)
+    np.testing.assert_allclose(sz[:, 0], ref[:, 0], rtol=1e-13)
+    assert rel(sz[:, 1], ref[:, 1]) < 1e-10 and rel(sz[:, 2], ref[:, 2]) < 1e-10
+    y = np.fromfile(os.path.join(rundir, "restart", "denmat_restart.bin"))
+    assert rel(y, g["gsl_y"]) < 1e-10
+    names = sorted(f for f in os.listdir(rundir) if f.startswith("tau_") and f.endswith("_tot.out"))
+    assert names == [str(n) for n in g["gsl_tau_names"]]
+    for n, text in zip(names, g["gsl_tau_text"]):
+        with open(os.path.join(rundir, n)) as f:
+            got = tau_numbers(f.read())
+        np.testing.assert_allclose(got, tau_numbers(str(text)), rtol=2e-7, atol=0)
+    ncalls = np.array([int(m) for m in re.findall(r"ncalls= (\d+) at ti=", stdout)])
+    np.testing.assert_array_equal(ncalls, g["gsl_ncalls"])
+
+
+@pytest.fixture(scope="module")
+def built():
+    import __graft_entry__ as G
+    G.build()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", RUN_CASES)
+def test_dmdh_run_reproduces_the_reference_run(case, built, tmp_path, capfd):
+    from denmat_dynm_development_gb300 import host
+    src = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(src, "golden.npz")))
+    rundir = str(tmp_path / case)
+    os.makedirs(rundir)
+    shutil.copy(os.path.join(src, "param.in"), rundir)
+    shutil.copytree(os.path.join(src, "ldbd_data"), os.path.join(rundir, "ldbd_data"))
+    capfd.readouterr()
+    host.run(rundir, "f64")
+    check_run_dir(rundir, g, capfd.readouterr().out)
