@@ -47,6 +47,10 @@ bool exists(const std::string& name) {
   struct stat b;
   return stat(name.c_str(), &b) == 0;
 }
+bool is_dir(const std::string& name) {
+  struct stat b;
+  return stat(name.c_str(), &b) == 0 && S_ISDIR(b.st_mode);
+}
 
 std::string trim(std::string s) {
   s.erase(0, s.find_first_not_of(" "));
@@ -233,6 +237,7 @@ struct dmdh_system {
   int ee_freq = 0;                   // freq_update_ee_model (> 0: update between output steps)
   int64_t freq_measure = 1;          // S files every freq_measure-th step (report, DensityMatrix_Dynamics.h:323)
   int64_t freq_compute_tau = 10;     // tau files every freq_compute_tau-th step (:211, 230)
+  int restart = 0;                   // restart = 1: state and time read from restart/
   std::vector<double> kvec, U, f_win;
   dmd_ee_desc eed;
 };
@@ -782,6 +787,7 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
   in.expt = (int)pget(pm, "alg_expt", 1);
   if (in.picture == DMD_PICTURE_SCHRODINGER && in.expt) return err(DMD_E_ARG, "in schrodinger picture, alg_expt must be false");
   const bool restart = pget(pm, "restart", 0) != 0;
+  s->restart = restart ? 1 : 0;
   in.t0 = pget(pm, "t0", 0., kFs);
   if (restart) {
     FILE* ft = fopen((dir + "/restart/time_restart.dat").c_str(), "r");
@@ -1270,6 +1276,9 @@ extern "C" int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max) 
   if (rc) return rc;
   std::unique_ptr<dmdh_system> guard(s);
   const dmdh_info& in = s->info;
+  // a new run does not overwrite the restart files of an earlier one (parameters.cpp:67-68)
+  if (!s->restart && is_dir(std::string(dir) + "/restart"))
+    return err(DMD_E_ARG, "directory restart presents, you should run a restart calculation");
   dmd_desc d;
   dmdh_desc(s, precision, 0, &d);
   dmd_handle* h = nullptr;

@@ -15,6 +15,9 @@ seeded generator) and runs the shim-built reference program on it:
   * gsl   -- DMD's own evolve_gsl (RKF45) for 20 output intervals (S_z file + restart state, and the
              tau files of its report_tau at t0);
   * euler -- DMD's own evolve_euler for 20 steps of tstep (S_z file + restart state);
+  * restart (three cases) -- the set-up dump again with restart = 1 on the state and time that
+             evolve_gsl wrote: initial state, t0, chemical potentials and, with alg_ddmdteq, f_eq
+             and the equilibrium drift recomputed from the restart state;
   * pee   -- (e-e cases) the operators rebuilt on the three states by reset_scatt: screening density
              from the state, P = P_eph (+ P_eimp) + scale_ee P_ee(rho).
 The e-e cases rebuild P_ee on every RHS evaluation (eeMode = Pee_update, freq_update_ee_model < 0),
@@ -165,6 +168,9 @@ CASES = {
                          param=dict(Bpert_T=(0.1, 0, 0.05), B_T=(0, 0, 1.0), extra={"alg_ddmdteq": 1})),
 }
 
+# cases whose set-up is also recorded in restart mode (restart = 1 on the files evolve_gsl wrote)
+RESTART_CASES = ("nb2_eimp_B", "nb2_carrier_eq", "nb2_holes_eq")
+
 
 def run(ref_bin, d, *args):
     shutil.rmtree(os.path.join(d, "restart"), ignore_errors=True)
@@ -282,6 +288,38 @@ def make_case(name, spec, ref_bin, outroot):
     tau_files = sorted(f for f in os.listdir(tmp) if f.startswith("tau_") and f.endswith("_tot.out"))
     out["gsl_tau_names"] = np.array(tau_files)
     out["gsl_tau_text"] = np.array([open(os.path.join(tmp, f)).read() for f in tau_files])
+    if name in RESTART_CASES:
+        # the reference's set-up with restart = 1 (parameters.cpp:298-309, read_dm_restart
+        # DenMat.cpp:301-316) from the state and time its evolve_gsl wrote (write_dm_tofile)
+        rdir = os.path.join(d, "_restart")
+        os.makedirs(rdir)
+        shutil.copytree(os.path.join(d, "ldbd_data"), os.path.join(rdir, "ldbd_data"))
+        shutil.copytree(os.path.join(tmp, "restart"), os.path.join(rdir, "restart"))
+        with open(os.path.join(d, "param.in")) as f:
+            text = f.read()
+        assert "restart = 0\n" in text
+        with open(os.path.join(rdir, "param.in"), "w") as f:
+            f.write(text.replace("restart = 0\n", "restart = 1\n"))
+        os.makedirs(os.path.join(rdir, "o"))
+        p = subprocess.run([ref_bin, "dump", "o"], cwd=rdir, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("reference restart dump failed:\n" + p.stdout[-3000:] + p.stderr[-3000:])
+        rmeta = {}
+        with open(os.path.join(rdir, "o", "meta.txt")) as f:
+            for line in f:
+                k, v = line.split()
+                rmeta[k] = float(v)
+        out["restart_in_y"] = np.fromfile(os.path.join(rdir, "restart", "denmat_restart.bin"))
+        with open(os.path.join(rdir, "restart", "time_restart.dat")) as f:
+            out["restart_in_time"] = np.array(f.read())
+        out["restart_t0"] = np.float64(rmeta["t0"])
+        out["restart_mu"] = np.array([rmeta["mue"], rmeta["muh"]])
+        out["restart_dm0"] = np.fromfile(os.path.join(rdir, "o", "dm0.bin"), dtype=np.complex128).reshape(nk, nbdm * nbdm)
+        if rmeta["ddmdteq"]:
+            out["restart_f_eq"] = np.fromfile(os.path.join(rdir, "o", "f_eq.bin")).reshape(nk, nbdm)
+            out["restart_ddmdt_eq"] = np.fromfile(os.path.join(rdir, "o", "ddmdt_eq.bin"),
+                                                  dtype=np.complex128).reshape(nk, nbw * nbw)
+        shutil.rmtree(rdir)
     # euler: DMD's evolve_euler to tend = 20 fs in steps of tstep = 1 fs
     run(ref_bin, tmp, "euler")
     out["euler_sz"] = read_s_file(os.path.join(tmp, "sz_elec_tot.out"))

@@ -243,3 +243,52 @@ def test_tau_of_a_pure_decay():
     tau = H.tau(obs.reshape(nk, -1), e, f, dm.reshape(nk, -1), (-dev / T1).reshape(nk, -1), 0.0, 0.0, picture=1)
     assert tau[0] == 0.0
     assert abs(tau[1] - T1) <= 1e-12 * T1 and abs(tau[2] - T1) <= 1e-12 * T1
+
+
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb2_carrier_eq", "nb2_holes_eq"])
+def test_restart_setup_bitwise(case, host, oracle, tmp_path):
+    """restart = 1 (parameters.cpp:298-309, read_dm_restart DenMat.cpp:301-316): the state and the
+    time read from the restart files the reference's evolve_gsl wrote, and with alg_ddmdteq
+    set_dm_eq on that state (chemical potentials, f_eq), equal the reference's restart set-up bit
+    for bit; the equilibrium drift from that f_eq (compute_ddmdt_eq at t = 0, evolve_eph.cpp:3-19)
+    too"""
+    import ctypes as C
+    import dataclasses
+    src = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(src, "golden.npz")))
+    d = tmp_path / case
+    shutil.copytree(os.path.join(src, "ldbd_data"), str(d / "ldbd_data"))
+    with open(os.path.join(src, "param.in")) as f:
+        text = f.read()
+    assert "restart = 0\n" in text
+    (d / "param.in").write_text(text.replace("restart = 0\n", "restart = 1\n"))
+    os.makedirs(str(d / "restart"))
+    g["restart_in_y"].tofile(str(d / "restart" / "denmat_restart.bin"))
+    (d / "restart" / "time_restart.dat").write_text(str(g["restart_in_time"]))
+    s = host.System(str(d))
+    try:
+        np.testing.assert_array_equal(s.dm0, g["restart_dm0"])
+        assert s.info.t0 == g["restart_t0"]
+        assert s.info.mue == g["restart_mu"][0] and s.info.muh == g["restart_mu"][1]
+        if "restart_f_eq" in g:
+            np.testing.assert_array_equal(s.f_eq, g["restart_f_eq"])
+            so = oracle.load(src)
+            drift = np.zeros_like(g["restart_ddmdt_eq"])
+            cs = dataclasses.replace(so, Hcoh=None, ddmdt_eq=None).cstruct()
+            f_eq = np.ascontiguousarray(s.f_eq)
+            oracle.lib().orc_compute_ddmdt_eq(C.addressof(cs), f_eq.ctypes.data, drift.ctypes.data)
+            np.testing.assert_array_equal(drift, g["restart_ddmdt_eq"])
+    finally:
+        s.close()
+
+
+def test_run_refuses_to_overwrite_an_earlier_run(host, tmp_path):
+    """restart = 0 with a restart/ directory present is an error before any device work, as in the
+    reference (parameters.cpp:67-68)"""
+    src = os.path.join(GOLDEN, "nb2_eimp_B")
+    d = tmp_path / "run"
+    shutil.copytree(os.path.join(src, "ldbd_data"), str(d / "ldbd_data"))
+    shutil.copy(os.path.join(src, "param.in"), str(d))
+    os.makedirs(str(d / "restart"))
+    with pytest.raises(RuntimeError, match="you should run a restart calculation"):
+        host.run(str(d))
