@@ -238,6 +238,7 @@ struct dmdh_system {
   int64_t freq_measure = 1;          // S files every freq_measure-th step (report, DensityMatrix_Dynamics.h:323)
   int64_t freq_compute_tau = 10;     // tau files every freq_compute_tau-th step (:211, 230)
   int restart = 0;                   // restart = 1: state and time read from restart/
+  int compute_tau_only = 0;          // report the tau files at t0 and stop (main.cpp:79)
   std::vector<double> kvec, U, f_win;
   dmd_ee_desc eed;
 };
@@ -788,6 +789,7 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
   if (in.picture == DMD_PICTURE_SCHRODINGER && in.expt) return err(DMD_E_ARG, "in schrodinger picture, alg_expt must be false");
   const bool restart = pget(pm, "restart", 0) != 0;
   s->restart = restart ? 1 : 0;
+  s->compute_tau_only = pget(pm, "compute_tau_only", 0) != 0 ? 1 : 0;
   in.t0 = pget(pm, "t0", 0., kFs);
   if (restart) {
     FILE* ft = fopen((dir + "/restart/time_restart.dat").c_str(), "r");
@@ -1310,7 +1312,10 @@ extern "C" int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max) 
       return err(r, dmd_last_error(h));
     return dmdh_report_tau(s, dir, tt, ybuf.data(), dbuf.data());
   };
-  if ((rc = rep.report(0, in.t0, ybuf))) return rc;
+  // the initial excess quantities (a restart continues the files of the earlier run), then with
+  // compute_tau_only the lifetimes at t0 and no evolution (DensityMatrix_Dynamics.h:72-75, main.cpp:79)
+  if (!s->restart && (rc = rep.report(0, in.t0, ybuf))) return rc;
+  if (s->compute_tau_only) return tau_report();
   double t = in.t0, ti = in.t0, hs = in.ode_hstart;
   const std::string stopfile = std::string(dir) + "/EXIT_DMD";
   for (int64_t it = 1; t < in.tend && (nsteps_max < 0 || it <= nsteps_max); ++it) {

@@ -107,8 +107,10 @@ int dmdh_tau(int32_t nk, int32_t nb, const double* obs, const double* e, const d
 int dmdh_report_tau(const dmdh_system* s, const char* dir, double t, const double* y, const double* dydt);
 
 /* DMD's time loop on the GPU: evolve_gsl (rkf45), evolve_euler, or fixed-step RK4, writing
- * sx/sy/sz_elec_tot.out into dir every freq_measure-th step and the tau files (dmdh_report_tau)
- * every freq_compute_tau-th step. nsteps_max < 0 runs to tend. */
+ * sx/sy/sz_elec_tot.out into dir every freq_measure-th step (the t0 line unless restart = 1) and the
+ * tau files (dmdh_report_tau) every freq_compute_tau-th step; with compute_tau_only = 1 only the t0
+ * line and the tau files at t0. restart = 0 with a restart/ folder in dir is refused (DMD_E_ARG).
+ * nsteps_max < 0 runs to tend. */
 int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max);
 
 #ifdef __cplusplus

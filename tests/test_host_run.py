@@ -102,3 +102,36 @@ def test_dmdh_run_euler_reproduces_the_reference_run(case, built, tmp_path, capf
     capfd.readouterr()
     host.run(rundir, "f64")
     check_run_dir(rundir, g, capfd.readouterr().out, loop="euler")
+
+
+def check_tau_only_dir(rundir, g):
+    """compute_tau_only: the S files hold the t0 line only, the tau files equal the reference's at t0,
+    and no step was taken (no restart state)"""
+    sz = read_s_file(os.path.join(rundir, "sz_elec_tot.out"))
+    assert sz.shape == (1, 3)
+    np.testing.assert_allclose(sz[0], g["gsl_sz"][0], rtol=1e-12, atol=0)
+    names = sorted(f for f in os.listdir(rundir) if f.startswith("tau_") and f.endswith("_tot.out"))
+    assert names == [str(n) for n in g["gsl_tau_names"]]
+    for n, text in zip(names, g["gsl_tau_text"]):
+        with open(os.path.join(rundir, n)) as f:
+            np.testing.assert_allclose(tau_numbers(f.read()), tau_numbers(str(text)), rtol=2e-7, atol=0)
+    assert not os.path.exists(os.path.join(rundir, "restart", "denmat_restart.bin"))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["nb2_holes_eq", "nb4_eimp_B"])
+def test_dmdh_run_compute_tau_only(case, built, tmp_path):
+    """compute_tau_only = 1: the initial S line and the lifetimes at t0, then no evolution
+    (DensityMatrix_Dynamics.h:72-75, main.cpp:79)"""
+    from denmat_dynm_development_gb300 import host
+    src = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(src, "golden.npz")))
+    rundir = str(tmp_path / case)
+    os.makedirs(rundir)
+    with open(os.path.join(src, "param.in")) as f:
+        text = f.read()
+    with open(os.path.join(rundir, "param.in"), "w") as f:
+        f.write(text + "compute_tau_only = 1\n")
+    shutil.copytree(os.path.join(src, "ldbd_data"), os.path.join(rundir, "ldbd_data"))
+    host.run(rundir, "f64")
+    check_tau_only_dir(rundir, g)
