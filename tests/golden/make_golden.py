@@ -17,7 +17,8 @@ seeded generator) and runs the shim-built reference program on it:
   * euler -- DMD's own evolve_euler for 20 steps of tstep (S_z file + restart state);
   * restart (three cases) -- the set-up dump again with restart = 1 on the state and time that
              evolve_gsl wrote: initial state, t0, chemical potentials and, with alg_ddmdteq, f_eq
-             and the equilibrium drift recomputed from the restart state;
+             and the equilibrium drift recomputed from the restart state; then compute + report_tau
+             there (the tau files at t0 != 0);
   * pee   -- (e-e cases) the operators rebuilt on the three states by reset_scatt: screening density
              from the state, P = P_eph (+ P_eimp) + scale_ee P_ee(rho).
 The e-e cases rebuild P_ee on every RHS evaluation (eeMode = Pee_update, freq_update_ee_model < 0),
@@ -319,6 +320,13 @@ def make_case(name, spec, ref_bin, outroot):
             out["restart_f_eq"] = np.fromfile(os.path.join(rdir, "o", "f_eq.bin")).reshape(nk, nbdm)
             out["restart_ddmdt_eq"] = np.fromfile(os.path.join(rdir, "o", "ddmdt_eq.bin"),
                                                   dtype=np.complex128).reshape(nk, nbw * nbw)
+        # compute + report_tau at the restart time (t0 != 0: the phases and the other line format)
+        p = subprocess.run([ref_bin, "tau"], cwd=rdir, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("reference restart tau failed:\n" + p.stdout[-3000:] + p.stderr[-3000:])
+        tau_files = sorted(f for f in os.listdir(rdir) if f.startswith("tau_") and f.endswith("_tot.out"))
+        out["restart_tau_names"] = np.array(tau_files)
+        out["restart_tau_text"] = np.array([open(os.path.join(rdir, f)).read() for f in tau_files])
         shutil.rmtree(rdir)
     # euler: DMD's evolve_euler to tend = 20 fs in steps of tstep = 1 fs
     run(ref_bin, tmp, "euler")

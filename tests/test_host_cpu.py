@@ -251,7 +251,7 @@ def test_restart_setup_bitwise(case, host, oracle, tmp_path):
     time read from the restart files the reference's evolve_gsl wrote, and with alg_ddmdteq
     set_dm_eq on that state (chemical potentials, f_eq), equal the reference's restart set-up bit
     for bit; the equilibrium drift from that f_eq (compute_ddmdt_eq at t = 0, evolve_eph.cpp:3-19)
-    too"""
+    too, and the tau files of compute + report_tau at the restart time (t0 != 0) byte for byte"""
     import ctypes as C
     import dataclasses
     src = os.path.join(GOLDEN, case)
@@ -278,6 +278,20 @@ def test_restart_setup_bitwise(case, host, oracle, tmp_path):
             f_eq = np.ascontiguousarray(s.f_eq)
             oracle.lib().orc_compute_ddmdt_eq(C.addressof(cs), f_eq.ctypes.data, drift.ctypes.data)
             np.testing.assert_array_equal(drift, g["restart_ddmdt_eq"])
+        # report_tau at the restart time (t0 != 0) on the restart state, the right-hand side from the
+        # oracle with the restart drift: the reference's tau files byte for byte
+        so = oracle.load(src)
+        if "restart_ddmdt_eq" in g:
+            so = dataclasses.replace(so, ddmdt_eq=np.ascontiguousarray(g["restart_ddmdt_eq"]))
+        y0 = s.y0()
+        out = tmp_path / "tau"
+        os.makedirs(str(out))
+        s.report_tau(str(out), s.info.t0, y0, oracle.rhs(so, s.info.t0, y0))
+        names = sorted(f for f in os.listdir(str(out)) if f.startswith("tau_"))
+        assert names == [str(n) for n in g["restart_tau_names"]]
+        for n, text in zip(names, g["restart_tau_text"]):
+            with open(os.path.join(str(out), n)) as f:
+                assert f.read() == str(text), n
     finally:
         s.close()
 
