@@ -239,6 +239,7 @@ struct dmdh_system {
   int64_t freq_compute_tau = 10;     // tau files every freq_compute_tau-th step (:211, 230)
   int restart = 0;                   // restart = 1: state and time read from restart/
   int compute_tau_only = 0;          // report the tau files at t0 and stop (main.cpp:79)
+  int print_tot_band = 0;            // the S files' per-band columns (observable.h:376-378)
   std::vector<double> kvec, U, f_win;
   dmd_ee_desc eed;
 };
@@ -790,6 +791,7 @@ int dmdh_load(const char* dir_c, dmdh_system** out) {
   const bool restart = pget(pm, "restart", 0) != 0;
   s->restart = restart ? 1 : 0;
   s->compute_tau_only = pget(pm, "compute_tau_only", 0) != 0 ? 1 : 0;
+  s->print_tot_band = pget(pm, "print_tot_band", 0) != 0 ? 1 : 0;
   in.t0 = pget(pm, "t0", 0., kFs);
   if (restart) {
     FILE* ft = fopen((dir + "/restart/time_restart.dat").c_str(), "r");
@@ -1118,8 +1120,10 @@ struct Reporter {
   int nv_dm, nb_dm;
   dmd_handle* h;
   int64_t freq_measure;
-  // observable.h:169-183 (header) and 368-383 (one line per output step)
-  int write_line(const std::string& what, const std::string& scarr, double t, double tot, double amp) {
+  bool print_tot_band;  // one more column per band of the range (the band's share of the total)
+  // observable.h:169-183 (header) and 368-385 (one line per output step)
+  int write_line(const std::string& what, const std::string& scarr, double t, double tot,
+                 const std::vector<double>& bands, double amp) {
     const std::string fname = dir + "/" + what + scarr + "_tot.out";
     const bool fresh = !exists(fname);
     FILE* f = fopen(fname.c_str(), "a");
@@ -1127,9 +1131,24 @@ struct Reporter {
     if (fresh) fprintf(f, "#time(au), s(t), s(t) without exp(iwt)\n");
     if (fabs(t) < 1e-30) fprintf(f, " 0.00000000000000e+01 %21.14le", tot);
     else fprintf(f, "%21.14le %21.14le", t, tot);
+    for (double b : bands) fprintf(f, " %21.14le", b);
     fprintf(f, " %21.14le\n", amp);
     fclose(f);
     return DMD_OK;
+  }
+  // the total of direction d over bands [b0, b1) and, with print_tot_band, of each band alone
+  int measure_line(int d, int b0, int b1, const char* scarr, double t) {
+    static const char* names[3] = {"sx", "sy", "sz"};
+    double tot, amp;
+    int rc;
+    if ((rc = dmd_measure(h, d, b0, b1, &tot, &amp))) return err(rc, dmd_last_error(h));
+    std::vector<double> bands;
+    for (int i = b0; print_tot_band && i < b1; ++i) {
+      double tb, ab;
+      if ((rc = dmd_measure(h, d, i, i + 1, &tb, &ab))) return err(rc, dmd_last_error(h));
+      bands.push_back(tb);
+    }
+    return write_line(names[d], scarr, t, tot, bands, amp);
   }
   int report(int it, double t, std::vector<double>& ybuf) {
     int rc;
@@ -1152,17 +1171,9 @@ struct Reporter {
       rename((rb + ".tmp").c_str(), rb.c_str());
       rename((rt + ".tmp").c_str(), rt.c_str());
     }
-    const char* names[3] = {"sx", "sy", "sz"};
     for (int d = 0; d < 3; ++d) {
-      double tot, amp;
-      if (nb_dm > nv_dm) {
-        if ((rc = dmd_measure(h, d, nv_dm, nb_dm, &tot, &amp))) return err(rc, dmd_last_error(h));
-        if ((rc = write_line(names[d], "_elec", t, tot, amp))) return rc;
-      }
-      if (nv_dm > 0) {
-        if ((rc = dmd_measure(h, d, 0, nv_dm, &tot, &amp))) return err(rc, dmd_last_error(h));
-        if ((rc = write_line(names[d], "_hole", t, tot, amp))) return rc;
-      }
+      if (nb_dm > nv_dm && (rc = measure_line(d, nv_dm, nb_dm, "_elec", t))) return rc;
+      if (nv_dm > 0 && (rc = measure_line(d, 0, nv_dm, "_hole", t))) return rc;
     }
     return DMD_OK;
   }
@@ -1301,7 +1312,7 @@ extern "C" int dmdh_run(const char* dir, int32_t precision, int64_t nsteps_max) 
     if ((rc = dmd_set_observable(h, dirn, obs.data(), s->f_dm.data(), in.ob_prefac))) return err(rc, dmd_last_error(h));
   }
   mkdir((std::string(dir) + "/restart").c_str(), 0755);
-  Reporter rep{dir, in.nv_dm, in.nb_dm, h, s->freq_measure};
+  Reporter rep{dir, in.nv_dm, in.nb_dm, h, s->freq_measure, s->print_tot_band != 0};
   std::vector<double> dbuf(ny);
   // compute + report_tau from the state before the step (DensityMatrix_Dynamics.h:211, 229-230):
   // the right-hand side through the GSL-callback entry, which leaves the handle's state alone

@@ -107,7 +107,8 @@ int dmdh_tau(int32_t nk, int32_t nb, const double* obs, const double* e, const d
 int dmdh_report_tau(const dmdh_system* s, const char* dir, double t, const double* y, const double* dydt);
 
 /* DMD's time loop on the GPU: evolve_gsl (rkf45), evolve_euler, or fixed-step RK4, writing
- * sx/sy/sz_elec_tot.out into dir every freq_measure-th step (the t0 line unless restart = 1) and the
+ * sx/sy/sz_elec_tot.out into dir every freq_measure-th step (the t0 line unless restart = 1; with
+ * print_tot_band = 1 a column per band before the amplitude) and the
  * tau files (dmdh_report_tau) every freq_compute_tau-th step; with compute_tau_only = 1 only the t0
  * line and the tau files at t0. restart = 0 with a restart/ folder in dir is refused (DMD_E_ARG).
  * nsteps_max < 0 runs to tend. */

@@ -15,6 +15,7 @@ seeded generator) and runs the shim-built reference program on it:
   * gsl   -- DMD's own evolve_gsl (RKF45) for 20 output intervals (S_z file + restart state, and the
              tau files of its report_tau at t0);
   * euler -- DMD's own evolve_euler for 20 steps of tstep (S_z file + restart state);
+  * bands (two cases) -- evolve_gsl again with print_tot_band = 1 (S_z file with per-band columns);
   * restart (three cases) -- the set-up dump again with restart = 1 on the state and time that
              evolve_gsl wrote: initial state, t0, chemical potentials and, with alg_ddmdteq, f_eq
              and the equilibrium drift recomputed from the restart state; then compute + report_tau
@@ -171,6 +172,10 @@ CASES = {
 
 # cases whose set-up is also recorded in restart mode (restart = 1 on the files evolve_gsl wrote)
 RESTART_CASES = ("nb2_eimp_B", "nb2_carrier_eq", "nb2_holes_eq")
+# cases run once more with print_tot_band = 1 (per-band columns in the S files); without valence
+# bands only: with bStart > 0 the reference scales its band columns at tot_band[i - bStart] for
+# i from 0 (observable.h:357-358), outside the array
+BAND_CASES = ("nb2_eimp_B", "nb4_eimp_B")
 
 
 def run(ref_bin, d, *args):
@@ -289,6 +294,19 @@ def make_case(name, spec, ref_bin, outroot):
     tau_files = sorted(f for f in os.listdir(tmp) if f.startswith("tau_") and f.endswith("_tot.out"))
     out["gsl_tau_names"] = np.array(tau_files)
     out["gsl_tau_text"] = np.array([open(os.path.join(tmp, f)).read() for f in tau_files])
+    if name in BAND_CASES:
+        bdir = os.path.join(d, "_bands")
+        os.makedirs(bdir)
+        shutil.copytree(os.path.join(d, "ldbd_data"), os.path.join(bdir, "ldbd_data"))
+        with open(os.path.join(d, "param.in")) as f:
+            text = f.read()
+        with open(os.path.join(bdir, "param.in"), "w") as f:
+            f.write(text + "print_tot_band = 1\n")
+        run(ref_bin, bdir, "gsl")
+        with open(os.path.join(bdir, "sz_elec_tot.out")) as f:  # every column: t, total, bands, amplitude
+            out["bands_gsl_sz"] = np.array([[float(x) for x in line.split()] for line in f
+                                            if line.strip() and not line.startswith("#")])
+        shutil.rmtree(bdir)
     if name in RESTART_CASES:
         # the reference's set-up with restart = 1 (parameters.cpp:298-309, read_dm_restart
         # DenMat.cpp:301-316) from the state and time its evolve_gsl wrote (write_dm_tofile)

@@ -135,3 +135,33 @@ def test_dmdh_run_compute_tau_only(case, built, tmp_path):
     shutil.copytree(os.path.join(src, "ldbd_data"), os.path.join(rundir, "ldbd_data"))
     host.run(rundir, "f64")
     check_tau_only_dir(rundir, g)
+
+
+def check_band_columns(rundir, g):
+    """print_tot_band = 1: every column of the S_z file (time, total, one per band, amplitude)
+    against the reference's run with the same flag"""
+    with open(os.path.join(rundir, "sz_elec_tot.out")) as f:
+        got = np.array([[float(x) for x in line.split()] for line in f if line.strip() and not line.startswith("#")])
+    ref = g["bands_gsl_sz"]
+    assert got.shape == ref.shape, (got.shape, ref.shape)
+    np.testing.assert_allclose(got[:, 0], ref[:, 0], rtol=1e-13)
+    for c in range(1, ref.shape[1]):
+        assert np.abs(got[:, c] - ref[:, c]).max() < 1e-10 * np.abs(ref[:, c]).max(), c
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["nb2_eimp_B", "nb4_eimp_B"])
+def test_dmdh_run_band_columns(case, built, tmp_path):
+    """print_tot_band = 1 (observable.h:376-378): the S files carry each band's share of the total"""
+    from denmat_dynm_development_gb300 import host
+    src = os.path.join(GOLDEN, case)
+    g = dict(np.load(os.path.join(src, "golden.npz")))
+    rundir = str(tmp_path / case)
+    os.makedirs(rundir)
+    with open(os.path.join(src, "param.in")) as f:
+        text = f.read()
+    with open(os.path.join(rundir, "param.in"), "w") as f:
+        f.write(text + "print_tot_band = 1\n")
+    shutil.copytree(os.path.join(src, "ldbd_data"), os.path.join(rundir, "ldbd_data"))
+    host.run(rundir, "f64")
+    check_band_columns(rundir, g)
