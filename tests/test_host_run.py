@@ -165,3 +165,39 @@ def test_dmdh_run_band_columns(case, built, tmp_path):
     shutil.copytree(os.path.join(src, "ldbd_data"), os.path.join(rundir, "ldbd_data"))
     host.run(rundir, "f64")
     check_band_columns(rundir, g)
+
+
+REF_BIN = os.path.join(os.path.dirname(GOLDEN), os.pardir, "oracle", "_ref", "dmd_ref")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BIN), reason="the reference program is built only where its sources are")
+def test_checkers_accept_the_reference_runs(tmp_path):
+    """The checkers above, applied to the reference program's own run directories for the same
+    inputs (evolve_gsl, evolve_euler, compute_tau_only, print_tot_band), accept them: what the GPU
+    tests hold dmdh_run to is exactly what the reference writes."""
+    import subprocess
+
+    def ref_run(case, mode, edit=lambda t: t):
+        d = tmp_path / ("%s_%s_%d" % (case, mode, len(os.listdir(str(tmp_path)))))
+        shutil.copytree(os.path.join(GOLDEN, case, "ldbd_data"), str(d / "ldbd_data"))
+        with open(os.path.join(GOLDEN, case, "param.in")) as f:
+            (d / "param.in").write_text(edit(f.read()))
+        args = [REF_BIN, mode] + (["o"] if mode == "dump" else [])
+        if mode == "dump":
+            os.makedirs(str(d / "o"))
+        p = subprocess.run(args, cwd=str(d), capture_output=True, text=True)
+        assert p.returncode == 0, p.stderr[-2000:]
+        return str(d), p.stdout, dict(np.load(os.path.join(GOLDEN, case, "golden.npz")))
+
+    for case in RUN_CASES:
+        d, out, g = ref_run(case, "gsl")
+        check_run_dir(d, g, out)
+    for case in ["nb2_eimp_B", "nb2_holes_eq"]:
+        d, out, g = ref_run(case, "euler", lambda t: t.replace("alg_ode_method = rkf45\n", "alg_ode_method = euler\n"))
+        check_run_dir(d, g, out, loop="euler")
+    for case in ["nb2_holes_eq", "nb4_eimp_B"]:
+        d, out, g = ref_run(case, "dump", lambda t: t + "compute_tau_only = 1\n")
+        check_tau_only_dir(d, g)
+    for case in ["nb2_eimp_B", "nb4_eimp_B"]:
+        d, out, g = ref_run(case, "gsl", lambda t: t + "print_tot_band = 1\n")
+        check_band_columns(d, g)
