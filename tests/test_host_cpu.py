@@ -306,3 +306,42 @@ def test_run_refuses_to_overwrite_an_earlier_run(host, tmp_path):
     os.makedirs(str(d / "restart"))
     with pytest.raises(RuntimeError, match="you should run a restart calculation"):
         host.run(str(d))
+
+
+@pytest.mark.parametrize("what,match", [
+    ("size_short", "ldbd_size.dat is too short"),
+    ("size_bands", "inconsistent band ranges"),
+    ("size_nk", "ldbd_size.dat line 3"),
+    ("no_R", "ldbd_R.dat does not exist"),
+    ("ek_truncated", "ldbd_ek.bin"),
+    ("no_kpair", "ldbd_kpair_k1st.bin"),
+])
+def test_broken_inputs_are_file_errors(what, match, host, tmp_path):
+    """Host-side fault injection on DMD's inputs (the reference aborts in check_file_size or reads
+    garbage): each broken file is a DMD_E_FILE / DMD_E_ARG status with a message, never a crash"""
+    dst = str(tmp_path / "case")
+    shutil.copytree(os.path.join(GOLDEN, "nb2_eph"), dst)
+    ld = os.path.join(dst, "ldbd_data")
+    size = os.path.join(ld, "ldbd_size.dat")
+    with open(size) as f:
+        lines = f.readlines()
+    if what == "size_short":
+        lines = lines[:5]
+    elif what == "size_bands":  # bTop_dm beyond nb
+        v = lines[1].split("#")[0].split()
+        v[3] = "7"
+        lines[1] = " ".join(v) + " # nb nv ...\n"
+    elif what == "size_nk":
+        lines[2] = "nonsense # nk_full nk kmesh\n"
+    elif what == "no_R":
+        os.remove(os.path.join(ld, "ldbd_R.dat"))
+    elif what == "ek_truncated":
+        p = os.path.join(ld, "ldbd_ek.bin")
+        with open(p, "r+b") as f:
+            f.truncate(os.path.getsize(p) // 2)
+    elif what == "no_kpair":
+        os.remove(os.path.join(ld, "ldbd_kpair_k1st.bin"))
+    with open(size, "w") as f:
+        f.writelines(lines)
+    with pytest.raises(RuntimeError, match=match):
+        host.System(dst)
