@@ -25,3 +25,9 @@ def oracle():
     O.build()
     O._setup_prototypes()
     return O
+
+
+def pytest_collection_modifyitems(config, items):
+    """The whole-run tests (DMD's time loop through the host library, which writes its output files)
+    go after every other test; the order is otherwise unchanged."""
+    items[:] = sorted(items, key=lambda it: "test_host_run.py::" in it.nodeid)
