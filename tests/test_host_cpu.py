@@ -345,3 +345,16 @@ def test_broken_inputs_are_file_errors(what, match, host, tmp_path):
         f.writelines(lines)
     with pytest.raises(RuntimeError, match=match):
         host.System(dst)
+
+
+def test_tau_argument_checks(host):
+    """dmdh_tau refuses empty or out-of-range band ranges before reading any array"""
+    import ctypes as C
+    L = C.CDLL(host.HOST_LIB)
+    L.dmdh_tau.argtypes = [C.c_int32, C.c_int32] + [C.c_void_p] * 5 + [C.c_double, C.c_double] + [C.c_int32] * 3 + \
+        [C.c_double, C.c_void_p]
+    buf = (C.c_double * 64)()
+    out = (C.c_double * 3)()
+    for nk, nb, b0, b1 in ((1, 2, 1, 1), (1, 2, 0, 3), (1, 2, -1, 1), (0, 2, 0, 2), (1, 0, 0, 0)):
+        assert L.dmdh_tau(nk, nb, buf, buf, buf, buf, buf, 0.0, 0.0, 0, b0, b1, 1.0, out) == 1
+    assert L.dmdh_tau(1, 2, None, buf, buf, buf, buf, 0.0, 0.0, 0, 0, 2, 1.0, out) == 1
